@@ -1,0 +1,141 @@
+"""ctypes binding of the C ABI declared in include/crashcat_gpu.h.
+
+The shared library is built in-tree (``crashcat_gb300/libcrashcat_gpu.so``).
+Loading fails loudly when it is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcrashcat_gpu.so")
+
+CC_OK = 0
+CC_ERR_INVALID = 1
+CC_ERR_CAPACITY = 2
+CC_ERR_TIMEOUT = 3
+CC_ERR_NAN = 4
+CC_ERR_CUDA = 5
+CC_ERR_UNSUPPORTED = 6
+
+SHAPE_SPHERE = 0
+SHAPE_BOX = 1
+STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
+COMBINE_AVERAGE, COMBINE_MULTIPLY, COMBINE_MIN, COMBINE_MAX, COMBINE_GEOMETRIC_MEAN = 0, 1, 2, 3, 4
+MAX_LAYERS = 32
+STATE_FLOATS = 16  # position[3] quaternion[4] linear_velocity[3] angular_velocity[3] center_of_mass[3]
+
+
+class Settings(C.Structure):
+    _fields_ = [
+        ("gravity", C.c_double * 3),
+        ("gravity_enabled", C.c_int32),
+        ("speculative_contact_distance", C.c_double),
+        ("manifold_tolerance", C.c_double),
+        ("collision_tolerance", C.c_double),
+        ("penetration_tolerance", C.c_double),
+        ("normal_cos_max_delta_rotation", C.c_double),
+        ("contact_point_preserve_lambda_max_dist_sq", C.c_double),
+        ("velocity_iterations", C.c_int32),
+        ("position_iterations", C.c_int32),
+        ("warm_starting", C.c_int32),
+        ("penetration_slop", C.c_double),
+        ("baumgarte_factor", C.c_double),
+        ("max_penetration_distance", C.c_double),
+        ("min_velocity_for_restitution", C.c_double),
+        ("allow_sleeping", C.c_int32),
+        ("time_before_sleep", C.c_double),
+        ("point_velocity_sleep_threshold", C.c_double),
+        ("num_object_layers", C.c_int32),
+        ("num_broadphase_layers", C.c_int32),
+        ("object_to_broadphase", C.c_int32 * MAX_LAYERS),
+        ("object_pairs", C.c_uint32 * MAX_LAYERS),
+        ("object_vs_broadphase", C.c_uint32 * MAX_LAYERS),
+        ("broadphase_pairs", C.c_uint32 * MAX_LAYERS),
+        ("max_bodies", C.c_int32),
+        ("max_pairs", C.c_int32),
+        ("max_manifolds", C.c_int32),
+        ("num_worlds", C.c_int32),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in (
+        "num_bodies", "num_awake", "num_pairs", "num_manifolds", "num_contact_points", "num_epa",
+        "num_islands", "max_island_constraints", "overflow_flags", "gpu_launches_per_step")]
+
+
+# numpy mirror of cc_body_desc (natural C alignment, 4-byte fields only)
+BODY_DTYPE = np.dtype([
+    ("shape_type", np.int32), ("shape_params", np.float32, 4), ("density", np.float32),
+    ("motion_type", np.int32), ("object_layer", np.int32), ("world", np.int32), ("allow_sleeping", np.int32),
+    ("position", np.float32, 3), ("quaternion", np.float32, 4), ("linear_velocity", np.float32, 3),
+    ("angular_velocity", np.float32, 3), ("friction", np.float32), ("restitution", np.float32),
+    ("gravity_factor", np.float32), ("linear_damping", np.float32), ("angular_damping", np.float32),
+    ("max_linear_velocity", np.float32), ("max_angular_velocity", np.float32),
+    ("friction_combine", np.int32), ("restitution_combine", np.int32),
+    ("collision_groups", np.uint32), ("collision_mask", np.uint32), ("allowed_dofs", np.int32),
+])
+
+EXPORTS = {
+    "cc_world_settings_default": ([C.POINTER(Settings)], C.c_int),
+    "cc_world_create": ([C.POINTER(Settings), C.POINTER(C.c_void_p)], C.c_int),
+    "cc_world_destroy": ([C.c_void_p], C.c_int),
+    "cc_world_add_bodies": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
+    "cc_world_num_bodies": ([C.c_void_p, C.POINTER(C.c_int32)], C.c_int),
+    "cc_world_step": ([C.c_void_p, C.c_float, C.c_int32], C.c_int),
+    "cc_world_step_host": ([C.c_void_p, C.c_float, C.c_void_p, C.c_void_p], C.c_int),
+    "cc_world_get_state": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "cc_world_set_state": ([C.c_void_p, C.c_void_p], C.c_int),
+    "cc_world_get_pairs": ([C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
+    "cc_world_get_manifolds": ([C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
+    "cc_world_get_stats": ([C.c_void_p, C.POINTER(Stats)], C.c_int),
+    "cc_status_string": ([C.c_int], C.c_char_p),
+}
+
+_lib = None
+
+
+class CCError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        super().__init__(f"{what}: {status_string(status)} (status {status})")
+        self.status = status
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Load the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+            "(the CUDA path has no CPU fallback)")
+    lib = C.CDLL(path)
+    for name, (args, res) in EXPORTS.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def status_string(status: int) -> str:
+    try:
+        return load().cc_status_string(status).decode()
+    except Exception:  # library not loadable: describe the code locally
+        return {0: "ok", 1: "invalid argument", 2: "capacity", 3: "timeout", 4: "nan", 5: "cuda",
+                6: "unsupported"}.get(status, "unknown")
+
+
+def check(status: int, what: str) -> None:
+    if status != CC_OK:
+        raise CCError(status, what)
+
+
+def ptr(a: np.ndarray) -> C.c_void_p:
+    assert a.flags["C_CONTIGUOUS"]
+    return C.c_void_p(a.ctypes.data)

@@ -1,0 +1,314 @@
+// Internal device data layout and helpers of the GB300 world step.
+//
+// Body state lives in device memory as structure-of-arrays of float4 rows so
+// that every per-body kernel issues 16-byte coalesced loads.  One handle can
+// hold many independent worlds (the batched form); every body carries its
+// world index and pairs never cross worlds.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/crashcat_gpu.h"
+
+namespace cc {
+
+// ---------------------------------------------------------------------------
+// body flag word
+// ---------------------------------------------------------------------------
+enum : uint32_t {
+    F_MOTION_MASK = 0x3u,        // bits 0-1: STATIC / KINEMATIC / DYNAMIC
+    F_SLEEPING = 1u << 2,
+    F_ALLOW_SLEEP = 1u << 3,
+    F_SENSOR = 1u << 4,
+    F_KIN_VS_NONDYN = 1u << 5,
+    F_SHAPE_SHIFT = 6,           // bits 6-8 shape type
+    F_DOF_SHIFT = 9,             // bits 9-14 allowed DOFs
+    F_FCOMB_SHIFT = 15,          // bits 15-17 friction combine mode
+    F_RCOMB_SHIFT = 18,          // bits 18-20 restitution combine mode
+    F_LAYER_SHIFT = 21,          // bits 21-25 object layer
+};
+__host__ __device__ inline int motion_of(uint32_t f) { return (int)(f & F_MOTION_MASK); }
+__host__ __device__ inline int shape_of(uint32_t f) { return (int)((f >> F_SHAPE_SHIFT) & 7u); }
+__host__ __device__ inline int dof_of(uint32_t f) { return (int)((f >> F_DOF_SHIFT) & 63u); }
+__host__ __device__ inline int layer_of(uint32_t f) { return (int)((f >> F_LAYER_SHIFT) & 31u); }
+__host__ __device__ inline bool sleeping_of(uint32_t f) { return (f & F_SLEEPING) != 0; }
+
+constexpr int STATIC = 0, KINEMATIC = 1, DYNAMIC = 2;
+constexpr int SHAPE_SPHERE = 0, SHAPE_BOX = 1;
+
+// Per-step overflow flags (status bits in DevCounters::overflow)
+enum : int { OVF_PAIRS = 1, OVF_MANIFOLDS = 2, OVF_EPA = 4, OVF_ISLAND = 8, OVF_CACHE = 16, OVF_SLOTS = 32 };
+
+// Device-resident counters of one step (one 128-byte line).
+struct DevCounters {
+    int num_pairs;
+    int num_manifolds;
+    int num_epa;
+    int num_islands;
+    int num_large_islands;
+    int num_small_islands;
+    int overflow;
+    int num_points;
+    int num_awake;
+    int max_island_constraints;
+    int island_cursor;
+    int large_cursor;
+    int pad[20];
+};
+
+// Settings copied into constant memory once per world.
+struct DevSettings {
+    float gravity[3];
+    int gravity_enabled;
+    float spec_dist;
+    float manifold_tol;
+    float collision_tol;
+    float penetration_tol;
+    float normal_cos;
+    float preserve_lambda_dsq;
+    int vel_iters;
+    int pos_iters;
+    int warm_starting;
+    float slop;
+    float baumgarte;
+    float max_pen;
+    float min_vel_restitution;
+    int allow_sleeping;
+    float time_before_sleep;
+    float sleep_threshold;
+    uint32_t allowed_pairs[CC_MAX_LAYERS];  // combined layer predicate, bit j of [i]
+};
+
+// Manifold produced by the narrowphase for one body pair (<= 4 points),
+// points stored relative to the position of body `base`.
+struct Manifold {
+    int a, b;          // narrowphase order (A has the lower motion type)
+    int n;
+    float3 base;       // position of A when the pair was collided
+    float3 normal;     // A -> B, normalised
+    float depth;
+    float3 ra[4];      // point on A relative to base (= position of A)
+    float3 rb[4];
+};
+
+// Contact constraint in solver form (one per manifold that creates a constraint).
+struct ContactPoint {
+    float3 rA, rB;          // moment arms from the centres of mass (midpoint - com)
+    float3 localA, localB;  // contact points in body space (for the position solve)
+    float eff_n, eff_t1, eff_t2;
+    float lam_n, lam_t1, lam_t2;
+    float bias_n;
+    float pad;
+};
+struct ContactConstraint {
+    int a, b;              // body indices ordered by id
+    int n;
+    int island;
+    float3 normal;
+    float friction;
+    float3 t1;
+    float invMassA;
+    float3 t2;
+    float invMassB;
+    uint32_t sort_key;
+    int cache_slot;
+    int pad0, pad1;
+    ContactPoint p[4];
+};
+
+// Contact cache record (contacts.ts:9-81): persistent across steps.
+struct CacheRecord {
+    unsigned long long key;  // (idxA << 32) | idxB, both ordered by id
+    int n;
+    int pad;
+    float3 p1[4];
+    float3 p2[4];
+    float ln[4], lt1[4], lt2[4];
+};
+
+struct DevWorld {
+    int n;          // bodies in use
+    int cap;        // body capacity
+    int max_pairs, max_manifolds, max_epa, cache_cap;
+    int num_worlds;
+    // body SoA
+    float4 *pos, *quat, *com, *linvel, *angvel, *force, *torque;
+    float4 *inv_inertia;  // xyz inverse inertia diagonal, w inverse mass
+    float4 *inertia_rot;
+    float4 *shape;        // box: hx hy hz convexRadius ; sphere: r
+    float4 *material;     // friction, restitution, gravity factor, 0
+    float4 *damping;      // linear damping, angular damping, max linear v, max angular v
+    uint32_t *flags;
+    uint2 *groups;        // collision groups, mask
+    int *world;
+    float4 *sleep_sph;    // 3 per body: centre xyz, radius w
+    float *sleep_timer;
+    double *aabb64;       // 6 per body, exact FP64 bounds
+    float4 *aabb_lo, *aabb_hi;  // FP32 bounds rounded outward
+    int *wake;            // wake requests raised by the contact setup
+    // broadphase
+    unsigned long long *morton, *morton_alt;
+    int *order, *order_alt;
+    int *node_parent;     // 2n-1 nodes: internal [0, n-1), leaves [n-1, 2n-1)
+    int2 *node_child;
+    float4 *node_lo, *node_hi;  // node bounds (w of lo = min world, w of hi = max world, as float bits)
+    int *node_flag;
+    int *pair_count;      // per body count of pairs it reports
+    int *pair_offset;
+    int2 *pair_slots;     // per body fixed slots
+    int2 *pairs;
+    // narrowphase
+    Manifold *manifolds;
+    int *manifold_valid;
+    int *epa_list;
+    // constraints
+    ContactConstraint *cons;
+    int *cons_of_manifold;
+    CacheRecord *cache_prev, *cache_cur;
+    // islands
+    int *uf_parent;
+    int *island_of_body;
+    int *island_id_of_root;
+    int *island_body_count, *island_cons_count;
+    int *island_body_off, *island_cons_off;
+    int *island_bodies, *island_cons;
+    int *island_fill_b, *island_fill_c;
+    int *island_order;
+    float4 *inv_inertia_world;   // 2 per body: xx xy xz yy | yz zz 0 0
+    // scan scratch
+    int *scan_tmp;
+    DevCounters *ctr;
+    // broadphase scratch
+    unsigned int *scene;   // ordered-int scene bounds of AABB centres
+    int2 *node_world;      // world range of each LBVH node
+    // narrowphase scratch
+    void *epa_items;
+    void *epa_scratch;     // one EPA polytope per EPA thread
+    // persistent contact cache (double buffered by parity)
+    unsigned long long *cache_keys[2];
+    CacheRecord *cache_recs[2];
+    int *cache_parity;
+    // island solve scratch
+    int *root_flag;
+    int *small_list, *large_list;
+    int *scratch_order, *scratch_colour, *scratch_claim;
+};
+
+// ---------------------------------------------------------------------------
+// float3 / quaternion helpers (FP32 device path)
+// ---------------------------------------------------------------------------
+__host__ __device__ inline float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__host__ __device__ inline float3 xyz(float4 a) { return make_float3(a.x, a.y, a.z); }
+__host__ __device__ inline float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ inline float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ inline float3 operator-(float3 a) { return f3(-a.x, -a.y, -a.z); }
+__host__ __device__ inline float3 operator*(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__host__ __device__ inline float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__host__ __device__ inline float lensq3(float3 a) { return dot3(a, a); }
+__host__ __device__ inline float3 cross3(float3 a, float3 b) {
+    return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ inline float3 normalize3(float3 a) {
+    float l = lensq3(a);
+    if (l > 0.f) l = rsqrtf(l);
+    return a * l;
+}
+// rotate vector by quaternion (x,y,z,w)
+__host__ __device__ inline float3 qrot(float4 q, float3 v) {
+    float3 u = f3(q.x, q.y, q.z);
+    float3 t = cross3(u, v) * 2.f;
+    return v + t * q.w + cross3(u, t);
+}
+__host__ __device__ inline float3 qrot_inv(float4 q, float3 v) { return qrot(make_float4(-q.x, -q.y, -q.z, q.w), v); }
+__host__ __device__ inline float4 qmul(float4 a, float4 b) {
+    return make_float4(a.x * b.w + a.w * b.x + a.y * b.z - a.z * b.y, a.y * b.w + a.w * b.y + a.z * b.x - a.x * b.z,
+                       a.z * b.w + a.w * b.z + a.x * b.y - a.y * b.x, a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z);
+}
+__device__ inline float4 qnormalize(float4 q) {
+    float l = q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w;
+    if (l > 0.f) l = rsqrtf(l);
+    return make_float4(q.x * l, q.y * l, q.z * l, q.w * l);
+}
+// rotation matrix rows from a quaternion: r0, r1, r2 are the ROWS of R
+struct Mat3 {
+    float3 r0, r1, r2;
+};
+__host__ __device__ inline Mat3 quat_to_mat(float4 q) {
+    float x2 = q.x + q.x, y2 = q.y + q.y, z2 = q.z + q.z;
+    float xx = q.x * x2, yx = q.y * x2, yy = q.y * y2, zx = q.z * x2, zy = q.z * y2, zz = q.z * z2;
+    float wx = q.w * x2, wy = q.w * y2, wz = q.w * z2;
+    Mat3 m;
+    m.r0 = f3(1.f - yy - zz, yx - wz, zx + wy);
+    m.r1 = f3(yx + wz, 1.f - xx - zz, zy - wx);
+    m.r2 = f3(zx - wy, zy + wx, 1.f - xx - yy);
+    return m;
+}
+__host__ __device__ inline float3 mmul(const Mat3 &m, float3 v) { return f3(dot3(m.r0, v), dot3(m.r1, v), dot3(m.r2, v)); }
+__host__ __device__ inline float3 mtmul(const Mat3 &m, float3 v) {
+    return m.r0 * v.x + m.r1 * v.y + m.r2 * v.z;
+}
+
+// Symmetric 3x3 (world inverse inertia): xx xy xz yy yz zz
+struct Sym3 {
+    float xx, xy, xz, yy, yz, zz;
+};
+__host__ __device__ inline float3 symmul(const Sym3 &s, float3 v) {
+    return f3(s.xx * v.x + s.xy * v.y + s.xz * v.z, s.xy * v.x + s.yy * v.y + s.yz * v.z,
+              s.xz * v.x + s.yz * v.y + s.zz * v.z);
+}
+// I^-1_world = R Ri diag(d) (R Ri)^T, masked by the rotation DOFs
+// (getInverseInertiaForRotation, motion-properties.ts:494-621)
+__device__ inline Sym3 world_inv_inertia(float4 q, float4 inertia_rot, float3 d, int dof) {
+    Mat3 m = quat_to_mat(qmul(q, inertia_rot));
+    // columns of R*Ri are c0 = (r0.x, r1.x, r2.x) ...
+    float3 c0 = f3(m.r0.x, m.r1.x, m.r2.x), c1 = f3(m.r0.y, m.r1.y, m.r2.y), c2 = f3(m.r0.z, m.r1.z, m.r2.z);
+    Sym3 s;
+    s.xx = d.x * c0.x * c0.x + d.y * c1.x * c1.x + d.z * c2.x * c2.x;
+    s.xy = d.x * c0.x * c0.y + d.y * c1.x * c1.y + d.z * c2.x * c2.y;
+    s.xz = d.x * c0.x * c0.z + d.y * c1.x * c1.z + d.z * c2.x * c2.z;
+    s.yy = d.x * c0.y * c0.y + d.y * c1.y * c1.y + d.z * c2.y * c2.y;
+    s.yz = d.x * c0.y * c0.z + d.y * c1.y * c1.z + d.z * c2.y * c2.z;
+    s.zz = d.x * c0.z * c0.z + d.y * c1.z * c1.z + d.z * c2.z * c2.z;
+    int ar = (dof >> 3) & 7;
+    if (ar != 7) {
+        float mx = (ar & 1) ? 1.f : 0.f, my = (ar & 2) ? 1.f : 0.f, mz = (ar & 4) ? 1.f : 0.f;
+        s.xx *= mx * mx;
+        s.xy *= mx * my;
+        s.xz *= mx * mz;
+        s.yy *= my * my;
+        s.yz *= my * mz;
+        s.zz *= mz * mz;
+    }
+    return s;
+}
+
+// grid sizing: 152 SMs on GB300
+constexpr int NUM_SMS = 152;
+inline int grid_for(int n, int block, int max_blocks_per_sm = 8) {
+    int g = (n + block - 1) / block;
+    int cap = NUM_SMS * max_blocks_per_sm;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return g;
+}
+
+// host launchers implemented in the .cu files
+void launch_integrate_forces(DevWorld &w, float dt, cudaStream_t s);
+void launch_broadphase(DevWorld &w, cudaStream_t s);
+void launch_narrowphase(DevWorld &w, float dt, cudaStream_t s);
+void launch_contacts_and_islands(DevWorld &w, float dt, float warm_ratio, cudaStream_t s);
+void launch_solver(DevWorld &w, float dt, float warm_ratio, cudaStream_t s);
+void launch_update_bounds(DevWorld &w, cudaStream_t s);
+void upload_settings(const DevSettings &s, double spec64, cudaStream_t st);
+void launch_cache_begin(DevWorld &w, cudaStream_t s);
+size_t epa_scratch_bytes();
+size_t epa_item_bytes();
+constexpr int EPA_THREADS = 1024;
+
+// scan / sort utilities (cc_scan.cu)
+void exclusive_scan_int(const int *in, int *out, int n, int *total, int *tmp, cudaStream_t s);
+void radix_sort_pairs_u64(unsigned long long *keys, unsigned long long *keys_alt, int *vals, int *vals_alt, int n,
+                          int bits, int *tmp, cudaStream_t s, const int *n_dev = nullptr);
+size_t scan_tmp_ints(int n);
+
+}  // namespace cc

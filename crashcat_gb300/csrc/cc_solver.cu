@@ -1,0 +1,1018 @@
+// Contact constraints, contact cache, islands and the island-partitioned
+// sequential-impulse solver with integration and sleeping fused in.
+//
+// Reference: addContactConstraint (src/constraints/contact-constraints.ts:437-857),
+// the contact cache (src/contacts.ts), islands (src/islands.ts), the solver
+// loops of updateWorld (src/update.ts:101-233), warm start / velocity /
+// position solve (contact-constraints.ts:906-1216, constraint-part/
+// axis-constraint-part.ts:500-847), velocityIntegrationUpdate
+// (update.ts:896-976) and island sleeping (islands.ts:392-423, body/sleep.ts).
+//
+// Islands are independent, so each is solved to completion by one owner:
+//  * islands with few contacts: one thread runs the reference's sequential
+//    Gauss-Seidel order exactly (contacts sorted by (sortKey, A, B));
+//  * larger islands: one CTA sorts the contacts the same way, colours them
+//    greedily in that order (min rank claims a body first) and sweeps the
+//    colours in parallel.
+// After the velocity iterations the owner stores impulses into the cache,
+// integrates its bodies, runs the position iterations, derives positions and
+// decides sleeping for the island - the integration and sleep test are fused
+// into the last solver pass.
+#include "cc_internal.cuh"
+
+namespace cc {
+
+static __constant__ DevSettings c_settings;
+
+void upload_settings_solver(const DevSettings &s, cudaStream_t st) {
+    cudaMemcpyToSymbolAsync(c_settings, &s, sizeof(DevSettings), 0, cudaMemcpyHostToDevice, st);
+}
+
+constexpr unsigned long long EMPTY_KEY = 0xffffffffffffffffull;
+constexpr int SMALL_ISLAND_MAX_CONS = 8;
+constexpr int SMALL_ISLAND_MAX_BODIES = 24;
+
+struct CacheTables {
+    unsigned long long *keys[2];
+    CacheRecord *recs[2];
+    int *parity;
+};
+
+__device__ __forceinline__ unsigned int hash64(unsigned long long k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return (unsigned int)k;
+}
+
+__device__ int cache_find(const unsigned long long *keys, int cap, unsigned long long key) {
+    unsigned int mask = (unsigned)cap - 1u;
+    unsigned int h = hash64(key) & mask;
+    for (int probe = 0; probe < cap; probe++) {
+        unsigned long long k = keys[h];
+        if (k == key) return (int)h;
+        if (k == EMPTY_KEY) return -1;
+        h = (h + 1u) & mask;
+    }
+    return -1;
+}
+__device__ int cache_insert(unsigned long long *keys, int cap, unsigned long long key) {
+    unsigned int mask = (unsigned)cap - 1u;
+    unsigned int h = hash64(key) & mask;
+    for (int probe = 0; probe < cap; probe++) {
+        unsigned long long prev = atomicCAS(&keys[h], EMPTY_KEY, key);
+        if (prev == EMPTY_KEY || prev == key) return (int)h;
+        h = (h + 1u) & mask;
+    }
+    return -1;
+}
+
+// combineMaterial combine-material.ts:40-57
+__device__ float combine(float a, float b, int ma, int mb) {
+    const int prio[5] = {0, 1, 3, 4, 2};
+    int mode = prio[ma] >= prio[mb] ? ma : mb;
+    switch (mode) {
+        case 1:
+            return a * b;
+        case 2:
+            return fminf(a, b);
+        case 3:
+            return fmaxf(a, b);
+        case 4:
+            return sqrtf(a * b);
+        default:
+            return (a + b) * 0.5f;
+    }
+}
+
+// computeContactSortKey contact-constraints.ts:1222-1231
+__device__ uint32_t contact_sort_key(int a, int b, uint32_t sa, uint32_t sb) {
+    uint32_t h = 0;
+    h = h * 31u + (uint32_t)a;
+    h = h * 31u + (uint32_t)b;
+    h = h * 31u + sa;
+    h = h * 31u + sb;
+    return h;
+}
+
+__device__ __forceinline__ Sym3 load_sym(const float4 *iw, int i) {
+    float4 a = iw[2 * i], b = iw[2 * i + 1];
+    return Sym3{a.x, a.y, a.z, a.w, b.x, b.y};
+}
+
+// inverse effective mass of one axis (calculateInverseEffectiveMass, axis-constraint-part.ts:86-148)
+__device__ __forceinline__ float inv_eff_mass(bool dynA, bool dynB, float imA, float imB, const Sym3 &IA,
+                                              const Sym3 &IB, float3 rA, float3 rB, float3 ax) {
+    float iem = 0.f;
+    if (dynA) {
+        float3 c = cross3(rA, ax);
+        iem += imA + dot3(symmul(IA, c), c);
+    }
+    if (dynB) {
+        float3 c = cross3(rB, ax);
+        iem += imB + dot3(symmul(IB, c), c);
+    }
+    return iem;
+}
+
+// ---------------------------------------------------------------------------
+// contact setup: one manifold per thread
+// ---------------------------------------------------------------------------
+__global__ void k_contact_setup(DevWorld w, CacheTables ct, float dt) {
+    int par = *ct.parity;
+    const unsigned long long *pkeys = ct.keys[par ^ 1];
+    const CacheRecord *precs = ct.recs[par ^ 1];
+    unsigned long long *ckeys = ct.keys[par];
+    CacheRecord *crecs = ct.recs[par];
+    int nm = min(w.ctr->num_manifolds, w.max_manifolds);
+    for (int mi = blockIdx.x * blockDim.x + threadIdx.x; mi < nm; mi += gridDim.x * blockDim.x) {
+        Manifold m = w.manifolds[mi];
+        float3 base = m.base;
+        int A = m.a, B = m.b;
+        float3 nrm = m.normal;
+        float3 ra[4], rb[4];
+        for (int k = 0; k < 4; k++) {
+            ra[k] = m.ra[k];
+            rb[k] = m.rb[k];
+        }
+        if (A > B) {  // ids grow with the body index: order by id (contact-constraints.ts:448-453)
+            int t = A;
+            A = B;
+            B = t;
+            nrm = -nrm;
+            for (int k = 0; k < 4; k++) {
+                float3 tt = ra[k];
+                ra[k] = rb[k];
+                rb[k] = tt;
+            }
+        }
+        unsigned long long key = ((unsigned long long)(unsigned)A << 32) | (unsigned)B;
+        int prev = cache_find(pkeys, w.cache_cap, key);
+        int slot = cache_insert(ckeys, w.cache_cap, key);
+        if (slot < 0) {
+            atomicOr(&w.ctr->overflow, OVF_CACHE);
+            continue;
+        }
+        uint32_t fa = w.flags[A], fb = w.flags[B];
+        int ma = motion_of(fa), mb = motion_of(fb);
+        float4 qa = w.quat[A], qb = w.quat[B];
+        float3 comA = xyz(w.com[A]) - base, comB = xyz(w.com[B]) - base;
+        Mat3 RA = quat_to_mat(qa), RB = quat_to_mat(qb);
+        float4 ia = w.inv_inertia[A], ib = w.inv_inertia[B];
+        float4 mta = w.material[A], mtb = w.material[B];
+        float friction = combine(mta.x, mtb.x, (fa >> F_FCOMB_SHIFT) & 7, (fb >> F_FCOMB_SHIFT) & 7);
+        float restitution = combine(mta.y, mtb.y, (fa >> F_RCOMB_SHIFT) & 7, (fb >> F_RCOMB_SHIFT) & 7);
+        bool sensor = ((fa | fb) & F_SENSOR) != 0;
+        CacheRecord rec;
+        rec.key = key;
+        rec.n = m.n;
+        rec.pad = 0;
+        bool creates = !sensor && ((ma == DYNAMIC && ia.w != 0.f) || (mb == DYNAMIC && ib.w != 0.f));
+        if (!creates) {
+            for (int k = 0; k < m.n; k++) {
+                rec.p1[k] = mtmul(RA, ra[k] - comA);
+                rec.p2[k] = mtmul(RB, rb[k] - comB);
+                rec.ln[k] = rec.lt1[k] = rec.lt2[k] = 0.f;
+            }
+            crecs[slot] = rec;
+            continue;
+        }
+        int ci = mi;  // one constraint slot per manifold
+        ContactConstraint c;
+        c.a = A;
+        c.b = B;
+        c.n = m.n;
+        c.island = -1;
+        c.normal = nrm;
+        c.friction = friction;
+        if (fabsf(nrm.x) > fabsf(nrm.y)) {
+            float tl = sqrtf(nrm.x * nrm.x + nrm.z * nrm.z);
+            c.t1 = f3(nrm.z / tl, 0.f, -nrm.x / tl);
+        } else {
+            float tl = sqrtf(nrm.y * nrm.y + nrm.z * nrm.z);
+            c.t1 = f3(0.f, nrm.z / tl, -nrm.y / tl);
+        }
+        c.t2 = cross3(nrm, c.t1);
+        c.invMassA = ia.w;
+        c.invMassB = ib.w;
+        c.sort_key = contact_sort_key(A, B, 0xffffffffu, 0xffffffffu);
+        c.cache_slot = slot;
+        c.pad0 = c.pad1 = 0;
+        bool dynA = ma == DYNAMIC, dynB = mb == DYNAMIC;
+        Sym3 IA{0, 0, 0, 0, 0, 0}, IB{0, 0, 0, 0, 0, 0};
+        if (dynA) IA = world_inv_inertia(qa, w.inertia_rot[A], xyz(ia), dof_of(fa));
+        if (dynB) IB = world_inv_inertia(qb, w.inertia_rot[B], xyz(ib), dof_of(fb));
+        float4 va = w.linvel[A], wa = w.angvel[A], vb = w.linvel[B], wb = w.angvel[B];
+        float3 g = f3(c_settings.gravity[0], c_settings.gravity[1], c_settings.gravity[2]);
+        const CacheRecord *pr = prev >= 0 ? &precs[prev] : nullptr;
+        int pn = pr ? pr->n : 0;
+        for (int k = 0; k < m.n; k++) {
+            ContactPoint &p = c.p[k];
+            float3 pa = ra[k], pb = rb[k];
+            p.localA = mtmul(RA, pa - comA);
+            p.localB = mtmul(RB, pb - comB);
+            p.lam_n = p.lam_t1 = p.lam_t2 = 0.f;
+            for (int j = 0; j < pn; j++) {
+                float3 d1 = p.localA - pr->p1[j], d2 = p.localB - pr->p2[j];
+                float th = c_settings.preserve_lambda_dsq;
+                if (lensq3(d1) < th && lensq3(d2) < th) {
+                    p.lam_n = pr->ln[j];
+                    p.lam_t1 = pr->lt1[j];
+                    p.lam_t2 = pr->lt2[j];
+                    break;
+                }
+            }
+            float3 mid = (pa + pb) * 0.5f;
+            p.rA = mid - comA;
+            p.rB = mid - comB;
+            // calculateNormalVelocityBias contact-constraints.ts:288-423
+            bool aM = ma != STATIC, bM = mb != STATIC;
+            float3 v1 = xyz(va) + cross3(xyz(wa), p.rA);
+            float3 v2 = xyz(vb) + cross3(xyz(wb), p.rB);
+            float3 rv = aM && bM ? v2 - v1 : (aM ? -v1 : (bM ? v2 : f3(0.f, 0.f, 0.f)));
+            float nv = dot3(rv, nrm);
+            float pen = dot3(pa - pb, nrm);
+            float spec = fmaxf(0.f, -pen / dt);
+            float bias = spec;
+            if (restitution > 0.f && nv < -c_settings.min_vel_restitution && nv < -spec) {
+                float3 rel = f3(0.f, 0.f, 0.f);
+                if (aM && bM)
+                    rel = g * (mtb.z - mta.z);
+                else if (aM)
+                    rel = g * (-mta.z);
+                else if (bM)
+                    rel = g * mtb.z;
+                if (dynA) rel = rel + xyz(w.force[A]) * (-ia.w);
+                if (dynB) rel = rel + xyz(w.force[B]) * ib.w;
+                float fdv = fminf(0.f, dot3(rel, nrm) * dt);
+                bias = restitution * (nv - fdv);
+            }
+            p.bias_n = bias;
+            float iem = inv_eff_mass(dynA, dynB, c.invMassA, c.invMassB, IA, IB, p.rA, p.rB, nrm);
+            if (iem == 0.f) {
+                p.eff_n = 0.f;
+                p.lam_n = 0.f;
+            } else {
+                p.eff_n = 1.f / iem;
+            }
+            if (friction > 0.f) {
+                float i1 = inv_eff_mass(dynA, dynB, c.invMassA, c.invMassB, IA, IB, p.rA, p.rB, c.t1);
+                float i2 = inv_eff_mass(dynA, dynB, c.invMassA, c.invMassB, IA, IB, p.rA, p.rB, c.t2);
+                if (i1 == 0.f) {
+                    p.eff_t1 = 0.f;
+                    p.lam_t1 = 0.f;
+                } else {
+                    p.eff_t1 = 1.f / i1;
+                }
+                if (i2 == 0.f) {
+                    p.eff_t2 = 0.f;
+                    p.lam_t2 = 0.f;
+                } else {
+                    p.eff_t2 = 1.f / i2;
+                }
+            } else {
+                p.eff_t1 = p.eff_t2 = 0.f;
+                p.lam_t1 = p.lam_t2 = 0.f;
+            }
+            p.pad = 0.f;
+            rec.p1[k] = p.localA;
+            rec.p2[k] = p.localB;
+            rec.ln[k] = p.lam_n;
+            rec.lt1[k] = p.lam_t1;
+            rec.lt2[k] = p.lam_t2;
+        }
+        crecs[slot] = rec;
+        w.cons[ci] = c;
+        w.cons_of_manifold[mi] = ci;
+        atomicAdd(&w.ctr->num_points, m.n);
+        if (ma == DYNAMIC && sleeping_of(fa)) w.wake[A] = 1;
+        if (mb == DYNAMIC && sleeping_of(fb)) w.wake[B] = 1;
+    }
+}
+
+// sleep test points (getSleepTestPoints sleep.ts:22-74)
+__device__ void sleep_points(uint32_t f, float4 sp, float4 q, float3 com, float3 out[3]) {
+    float3 e = shape_of(f) == SHAPE_BOX ? f3(sp.x, sp.y, sp.z) : f3(sp.x, sp.x, sp.x);
+    out[0] = com;
+    int lowest = (e.x <= e.y && e.x <= e.z) ? 0 : (e.y <= e.z ? 1 : 2);
+    float3 X = f3(1.f, 0.f, 0.f), Y = f3(0.f, 1.f, 0.f), Z = f3(0.f, 0.f, 1.f);
+    if (lowest == 0) {
+        out[1] = com + qrot(q, Y) * e.y;
+        out[2] = com + qrot(q, Z) * e.z;
+    } else if (lowest == 1) {
+        out[1] = com + qrot(q, X) * e.x;
+        out[2] = com + qrot(q, Z) * e.z;
+    } else {
+        out[1] = com + qrot(q, X) * e.x;
+        out[2] = com + qrot(q, Y) * e.y;
+    }
+}
+__device__ void reset_sleep(DevWorld &w, int i) {
+    float3 p[3];
+    sleep_points(w.flags[i], w.shape[i], w.quat[i], xyz(w.com[i]), p);
+    for (int k = 0; k < 3; k++) w.sleep_sph[3 * i + k] = make_float4(p[k].x, p[k].y, p[k].z, 0.f);
+    w.sleep_timer[i] = 0.f;
+}
+
+// wake bodies touched by a new contact constraint (update.ts:84-91, sleep.ts:186-203)
+__global__ void k_apply_wake(DevWorld w) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
+        if (!w.wake[i]) continue;
+        w.wake[i] = 0;
+        w.flags[i] &= ~F_SLEEPING;
+        reset_sleep(w, i);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// islands: union-find over contact constraints between active bodies
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool active_body(uint32_t f) { return motion_of(f) != STATIC && !sleeping_of(f); }
+
+__device__ int uf_find(int *parent, int i) {
+    while (true) {
+        int p = parent[i];
+        if (p == i) return i;
+        int gp = parent[p];
+        if (gp != p) parent[i] = gp;  // path halving
+        i = p;
+    }
+}
+
+__global__ void k_uf_init(DevWorld w) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
+        w.uf_parent[i] = i;
+        w.island_body_count[i] = 0;
+        w.island_cons_count[i] = 0;
+        w.island_fill_b[i] = 0;
+        w.island_fill_c[i] = 0;
+    }
+}
+
+__global__ void k_uf_link(DevWorld w) {
+    int nm = min(w.ctr->num_manifolds, w.max_manifolds);
+    for (int ci = blockIdx.x * blockDim.x + threadIdx.x; ci < nm; ci += gridDim.x * blockDim.x) {
+        if (w.cons_of_manifold[ci] < 0) continue;
+        int a = w.cons[ci].a, b = w.cons[ci].b;
+        if (!active_body(w.flags[a]) || !active_body(w.flags[b])) continue;
+        for (int guard = 0; guard < 1000000; guard++) {
+            int ra = uf_find(w.uf_parent, a), rb = uf_find(w.uf_parent, b);
+            if (ra == rb) break;
+            int hi = max(ra, rb), lo = min(ra, rb);
+            if (atomicCAS(&w.uf_parent[hi], hi, lo) == hi) break;
+        }
+    }
+}
+
+__global__ void k_uf_roots(DevWorld w, int *root_flag) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
+        bool act = active_body(w.flags[i]);
+        int r = act ? uf_find(w.uf_parent, i) : -1;
+        w.uf_parent[i] = r;
+        root_flag[i] = (act && r == i) ? 1 : 0;
+    }
+}
+
+__global__ void k_island_count(DevWorld w, const int *island_id_of_root) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
+        int r = w.uf_parent[i];
+        int isl = r >= 0 ? island_id_of_root[r] : -1;
+        w.island_of_body[i] = isl;
+        if (isl >= 0) atomicAdd(&w.island_body_count[isl], 1);
+    }
+    int nm = min(w.ctr->num_manifolds, w.max_manifolds);
+    for (int ci = blockIdx.x * blockDim.x + threadIdx.x; ci < nm; ci += gridDim.x * blockDim.x) {
+        if (w.cons_of_manifold[ci] < 0) continue;
+        int a = w.cons[ci].a, b = w.cons[ci].b;
+        int owner = active_body(w.flags[a]) ? a : b;
+        int r = w.uf_parent[owner];
+        int isl = r >= 0 ? island_id_of_root[r] : -1;
+        w.cons[ci].island = isl;
+        if (isl >= 0) atomicAdd(&w.island_cons_count[isl], 1);
+    }
+}
+
+__global__ void k_island_scatter(DevWorld w) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
+        int isl = w.island_of_body[i];
+        if (isl < 0) continue;
+        int k = atomicAdd(&w.island_fill_b[isl], 1);
+        w.island_bodies[w.island_body_off[isl] + k] = i;
+    }
+    int nm = min(w.ctr->num_manifolds, w.max_manifolds);
+    for (int ci = blockIdx.x * blockDim.x + threadIdx.x; ci < nm; ci += gridDim.x * blockDim.x) {
+        if (w.cons_of_manifold[ci] < 0) continue;
+        int isl = w.cons[ci].island;
+        if (isl < 0) continue;
+        int k = atomicAdd(&w.island_fill_c[isl], 1);
+        w.island_cons[w.island_cons_off[isl] + k] = ci;
+    }
+}
+
+// split islands into the per-thread and per-CTA classes
+__global__ void k_island_classify(DevWorld w, int *small_list, int *large_list) {
+    int ni = w.ctr->num_islands;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x) {
+        int nc = w.island_cons_count[i], nb = w.island_body_count[i];
+        atomicMax(&w.ctr->max_island_constraints, nc);
+        if (nc <= SMALL_ISLAND_MAX_CONS && nb <= SMALL_ISLAND_MAX_BODIES) {
+            int k = atomicAdd(&w.ctr->num_small_islands, 1);
+            small_list[k] = i;
+        } else {
+            int k = atomicAdd(&w.ctr->num_large_islands, 1);
+            large_list[k] = i;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// solver primitives (FP32), body velocities in global memory
+// ---------------------------------------------------------------------------
+struct BodyRef {
+    float3 v, w;
+    float im;
+    Sym3 I;
+    int motion;
+    int dof;
+};
+__device__ __forceinline__ BodyRef load_body(const DevWorld &w, int i) {
+    BodyRef b;
+    float4 v = w.linvel[i], av = w.angvel[i];
+    uint32_t f = w.flags[i];
+    b.v = xyz(v);
+    b.w = xyz(av);
+    b.im = w.inv_inertia[i].w;
+    b.motion = motion_of(f);
+    b.dof = dof_of(f);
+    if (b.motion == DYNAMIC)
+        b.I = load_sym(w.inv_inertia_world, i);
+    else
+        b.I = Sym3{0, 0, 0, 0, 0, 0};
+    return b;
+}
+__device__ __forceinline__ void store_body_vel(DevWorld &w, int i, const BodyRef &b) {
+    if (b.motion != DYNAMIC) return;
+    w.linvel[i] = make_float4(b.v.x, b.v.y, b.v.z, 0.f);
+    w.angvel[i] = make_float4(b.w.x, b.w.y, b.w.z, 0.f);
+}
+__device__ __forceinline__ void mask_lin(BodyRef &b) {
+    if (!(b.dof & 1)) b.v.x = 0.f;
+    if (!(b.dof & 2)) b.v.y = 0.f;
+    if (!(b.dof & 4)) b.v.z = 0.f;
+}
+// getTotalLambda axis-constraint-part.ts:578-625 (softness 0, bias b)
+__device__ __forceinline__ float total_lambda(const BodyRef &A, const BodyRef &B, float3 ax, float3 rA, float3 rB,
+                                              float eff, float lam, float bias) {
+    bool mA = A.motion != STATIC, mB = B.motion != STATIC;
+    float jv = 0.f;
+    if (mA && mB)
+        jv = dot3(ax, A.v - B.v);
+    else if (mA)
+        jv = dot3(ax, A.v);
+    else if (mB)
+        jv = -dot3(ax, B.v);
+    if (mA) jv += dot3(cross3(rA, ax), A.w);
+    if (mB) jv -= dot3(cross3(rB, ax), B.w);
+    return lam + eff * (jv - bias);
+}
+// applyLambda axis-constraint-part.ts:640-707
+__device__ __forceinline__ void apply_impulse(BodyRef &A, BodyRef &B, float imA, float imB, float3 ax, float3 rA,
+                                              float3 rB, float dl) {
+    if (dl == 0.f) return;
+    if (A.motion == DYNAMIC) {
+        A.v = A.v - ax * (dl * imA);
+        mask_lin(A);
+        A.w = A.w - symmul(A.I, cross3(rA, ax)) * dl;
+    }
+    if (B.motion == DYNAMIC) {
+        B.v = B.v + ax * (dl * imB);
+        mask_lin(B);
+        B.w = B.w + symmul(B.I, cross3(rB, ax)) * dl;
+    }
+}
+
+// warm start of one constraint (contact-constraints.ts:906-955)
+__device__ void warm_start_con(ContactConstraint &c, BodyRef &A, BodyRef &B, float ratio) {
+    for (int k = 0; k < c.n; k++) {
+        ContactPoint &p = c.p[k];
+        if (p.eff_t1 != 0.f || p.eff_t2 != 0.f) {
+            p.lam_t1 *= ratio;
+            apply_impulse(A, B, c.invMassA, c.invMassB, c.t1, p.rA, p.rB, p.lam_t1);
+            p.lam_t2 *= ratio;
+            apply_impulse(A, B, c.invMassA, c.invMassB, c.t2, p.rA, p.rB, p.lam_t2);
+        }
+        p.lam_n *= ratio;
+        apply_impulse(A, B, c.invMassA, c.invMassB, c.normal, p.rA, p.rB, p.lam_n);
+    }
+}
+
+// one PGS pass over one contact (contact-constraints.ts:963-1053)
+__device__ void solve_velocity_con(ContactConstraint &c, BodyRef &A, BodyRef &B) {
+    if (A.motion != DYNAMIC && B.motion != DYNAMIC) return;
+    for (int k = 0; k < c.n; k++) {
+        ContactPoint &p = c.p[k];
+        if (p.eff_t1 != 0.f || p.eff_t2 != 0.f) {
+            float l1 = total_lambda(A, B, c.t1, p.rA, p.rB, p.eff_t1, p.lam_t1, 0.f);
+            float l2 = total_lambda(A, B, c.t2, p.rA, p.rB, p.eff_t2, p.lam_t2, 0.f);
+            float mf = c.friction * p.lam_n;
+            float fm = l1 * l1 + l2 * l2;
+            if (fm > mf * mf) {
+                float s = mf / sqrtf(fm);
+                l1 *= s;
+                l2 *= s;
+            }
+            float d1 = l1 - p.lam_t1;
+            p.lam_t1 = l1;
+            apply_impulse(A, B, c.invMassA, c.invMassB, c.t1, p.rA, p.rB, d1);
+            float d2 = l2 - p.lam_t2;
+            p.lam_t2 = l2;
+            apply_impulse(A, B, c.invMassA, c.invMassB, c.t2, p.rA, p.rB, d2);
+        }
+    }
+    for (int k = 0; k < c.n; k++) {
+        ContactPoint &p = c.p[k];
+        float tl = total_lambda(A, B, c.normal, p.rA, p.rB, p.eff_n, p.lam_n, p.bias_n);
+        tl = fmaxf(0.f, tl);
+        float dl = tl - p.lam_n;
+        p.lam_n = tl;
+        apply_impulse(A, B, c.invMassA, c.invMassB, c.normal, p.rA, p.rB, dl);
+    }
+}
+
+// rotation step (rigid-body-step.ts:55-97)
+__device__ __forceinline__ float4 rotation_step(float4 q, float3 a) {
+    float l = sqrtf(lensq3(a));
+    if (l > 1.0e-6f) {
+        float3 axis = a * (1.f / l);
+        float s, co;
+        sincosf(l * 0.5f, &s, &co);
+        float4 r = make_float4(axis.x * s, axis.y * s, axis.z * s, co);
+        q = qnormalize(qmul(r, q));
+    }
+    return q;
+}
+
+struct PoseRef {
+    float3 com;
+    float4 q;
+};
+
+// position solve of one contact (contact-constraints.ts:1098-1216); returns true if an impulse was applied
+__device__ bool solve_position_con(DevWorld &w, const ContactConstraint &c, PoseRef &PA, PoseRef &PB, int ma, int mb,
+                                   uint32_t fa, uint32_t fb) {
+    if (ma != DYNAMIC && mb != DYNAMIC) return false;
+    bool any = false;
+    Mat3 RA = quat_to_mat(PA.q), RB = quat_to_mat(PB.q);
+    Sym3 IA{0, 0, 0, 0, 0, 0}, IB{0, 0, 0, 0, 0, 0};
+    if (ma == DYNAMIC) IA = world_inv_inertia(PA.q, w.inertia_rot[c.a], xyz(w.inv_inertia[c.a]), dof_of(fa));
+    if (mb == DYNAMIC) IB = world_inv_inertia(PB.q, w.inertia_rot[c.b], xyz(w.inv_inertia[c.b]), dof_of(fb));
+    for (int k = 0; k < c.n; k++) {
+        const ContactPoint &p = c.p[k];
+        float3 pa = PA.com + mmul(RA, p.localA);
+        float3 pb = PB.com + mmul(RB, p.localB);
+        float sep = dot3(pb - pa, c.normal) + c_settings.slop;
+        sep = fmaxf(sep, -c_settings.max_pen);
+        if (sep >= 0.f) continue;
+        float3 mid = (pa + pb) * 0.5f;
+        float3 rA = mid - PA.com, rB = mid - PB.com;
+        float iem = inv_eff_mass(ma == DYNAMIC, mb == DYNAMIC, c.invMassA, c.invMassB, IA, IB, rA, rB, c.normal);
+        if (iem == 0.f) continue;
+        float eff = 1.f / iem;
+        float lambda = -eff * c_settings.baumgarte * sep;
+        if (ma == DYNAMIC) {
+            PA.com = PA.com - c.normal * (lambda * c.invMassA);
+            int d = dof_of(fa);
+            if (!(d & 1)) PA.com.x = 0.f;
+            if (!(d & 2)) PA.com.y = 0.f;
+            if (!(d & 4)) PA.com.z = 0.f;
+            PA.q = rotation_step(PA.q, -(symmul(IA, cross3(rA, c.normal)) * lambda));
+            RA = quat_to_mat(PA.q);
+        }
+        if (mb == DYNAMIC) {
+            PB.com = PB.com + c.normal * (lambda * c.invMassB);
+            int d = dof_of(fb);
+            if (!(d & 1)) PB.com.x = 0.f;
+            if (!(d & 2)) PB.com.y = 0.f;
+            if (!(d & 4)) PB.com.z = 0.f;
+            PB.q = rotation_step(PB.q, symmul(IB, cross3(rB, c.normal)) * lambda);
+            RB = quat_to_mat(PB.q);
+        }
+        any = true;
+    }
+    return any;
+}
+
+// velocity integration of one body (update.ts:896-976, discrete)
+__device__ void integrate_body(DevWorld &w, int i, float dt) {
+    uint32_t f = w.flags[i];
+    int m = motion_of(f);
+    if (m == STATIC || sleeping_of(f)) return;
+    float3 v = xyz(w.linvel[i]), av = xyz(w.angvel[i]);
+    if (m == DYNAMIC) {
+        float4 d = w.damping[i];
+        float ls = lensq3(v);
+        if (ls > d.z * d.z) v = normalize3(v) * d.z;
+        float as = lensq3(av);
+        if (as > d.w * d.w) av = normalize3(av) * d.w;
+        w.linvel[i] = make_float4(v.x, v.y, v.z, 0.f);
+        w.angvel[i] = make_float4(av.x, av.y, av.z, 0.f);
+    }
+    float4 q = rotation_step(w.quat[i], av * dt);
+    w.quat[i] = q;
+    float3 com = xyz(w.com[i]) + v * dt;
+    w.com[i] = make_float4(com.x, com.y, com.z, 0.f);
+}
+
+// positions from the centre of mass, force clear (update.ts:322-330, 235-238)
+__device__ void finish_body(DevWorld &w, int i) {
+    uint32_t f = w.flags[i];
+    if (motion_of(f) == STATIC || sleeping_of(f)) return;
+    float3 com = xyz(w.com[i]);  // shape centre of mass is the origin for boxes and spheres
+    w.pos[i] = make_float4(com.x, com.y, com.z, 0.f);
+    w.force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    w.torque[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// updateSleepState sleep.ts:88-117
+__device__ bool sleep_update(DevWorld &w, int i, float dt) {
+    uint32_t f = w.flags[i];
+    if (!(f & F_ALLOW_SLEEP) || (f & F_SENSOR)) return false;
+    float3 p[3];
+    sleep_points(f, w.shape[i], w.quat[i], xyz(w.com[i]), p);
+    float maxMove = c_settings.sleep_threshold * c_settings.time_before_sleep;
+    for (int k = 0; k < 3; k++) {
+        float4 s = w.sleep_sph[3 * i + k];
+        float d = sqrtf(lensq3(xyz(s) - p[k]));
+        s.w = fmaxf(s.w, d);
+        w.sleep_sph[3 * i + k] = s;
+        if (s.w > maxMove) {
+            reset_sleep(w, i);
+            return false;
+        }
+    }
+    float t = w.sleep_timer[i] + dt;
+    w.sleep_timer[i] = t;
+    return t >= c_settings.time_before_sleep;
+}
+__device__ void sleep_body(DevWorld &w, int i) {
+    w.flags[i] |= F_SLEEPING;
+    w.linvel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    w.angvel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// world inverse inertia of the island's dynamic bodies at the start of the solve
+__device__ void prepare_body(DevWorld &w, int i) {
+    uint32_t f = w.flags[i];
+    if (motion_of(f) != DYNAMIC) return;
+    float4 ii = w.inv_inertia[i];
+    Sym3 s = world_inv_inertia(w.quat[i], w.inertia_rot[i], xyz(ii), dof_of(f));
+    w.inv_inertia_world[2 * i] = make_float4(s.xx, s.xy, s.xz, s.yy);
+    w.inv_inertia_world[2 * i + 1] = make_float4(s.yz, s.zz, 0.f, 0.f);
+}
+
+__device__ __forceinline__ bool con_less(const ContactConstraint &x, const ContactConstraint &y) {
+    if (x.sort_key != y.sort_key) return x.sort_key < y.sort_key;
+    if (x.a != y.a) return x.a < y.a;
+    return x.b < y.b;
+}
+
+__device__ void store_impulses(DevWorld &w, CacheRecord *crecs, const ContactConstraint &c) {
+    CacheRecord *r = crecs + c.cache_slot;
+    for (int k = 0; k < c.n; k++) {
+        r->ln[k] = c.p[k].lam_n;
+        r->lt1[k] = c.p[k].lam_t1;
+        r->lt2[k] = c.p[k].lam_t2;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// small islands: one thread runs the island in the reference's exact order
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_solve_small(DevWorld w, CacheTables ct, const int *small_list, float dt,
+                                                      float ratio) {
+    int ns = w.ctr->num_small_islands;
+    CacheRecord *crecs = ct.recs[*ct.parity];
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+        int isl = small_list[s];
+        int nb = w.island_body_count[isl], nc = w.island_cons_count[isl];
+        const int *bl = w.island_bodies + w.island_body_off[isl];
+        const int *cl = w.island_cons + w.island_cons_off[isl];
+        int order[SMALL_ISLAND_MAX_CONS];
+        for (int k = 0; k < nc; k++) order[k] = cl[k];
+        // sortContactIndices: insertion sort by (sortKey, idA, idB)
+        for (int k = 1; k < nc; k++) {
+            int x = order[k];
+            int j = k - 1;
+            while (j >= 0 && con_less(w.cons[x], w.cons[order[j]])) {
+                order[j + 1] = order[j];
+                j--;
+            }
+            order[j + 1] = x;
+        }
+        for (int k = 0; k < nb; k++) prepare_body(w, bl[k]);
+        if (nc > 0) {
+            if (c_settings.warm_starting) {
+                for (int k = 0; k < nc; k++) {
+                    ContactConstraint &c = w.cons[order[k]];
+                    BodyRef A = load_body(w, c.a), B = load_body(w, c.b);
+                    warm_start_con(c, A, B, ratio);
+                    store_body_vel(w, c.a, A);
+                    store_body_vel(w, c.b, B);
+                }
+            }
+            for (int it = 0; it < c_settings.vel_iters; it++) {
+                for (int k = 0; k < nc; k++) {
+                    ContactConstraint &c = w.cons[order[k]];
+                    BodyRef A = load_body(w, c.a), B = load_body(w, c.b);
+                    solve_velocity_con(c, A, B);
+                    store_body_vel(w, c.a, A);
+                    store_body_vel(w, c.b, B);
+                }
+            }
+            for (int k = 0; k < nc; k++) store_impulses(w, crecs, w.cons[order[k]]);
+        }
+        for (int k = 0; k < nb; k++) integrate_body(w, bl[k], dt);
+        if (nc > 0) {
+            for (int it = 0; it < c_settings.pos_iters; it++) {
+                bool any = false;
+                for (int k = 0; k < nc; k++) {
+                    const ContactConstraint &c = w.cons[order[k]];
+                    uint32_t fa = w.flags[c.a], fb = w.flags[c.b];
+                    PoseRef PA{xyz(w.com[c.a]), w.quat[c.a]}, PB{xyz(w.com[c.b]), w.quat[c.b]};
+                    bool applied = solve_position_con(w, c, PA, PB, motion_of(fa), motion_of(fb), fa, fb);
+                    if (applied) {
+                        if (motion_of(fa) == DYNAMIC) {
+                            w.com[c.a] = make_float4(PA.com.x, PA.com.y, PA.com.z, 0.f);
+                            w.quat[c.a] = PA.q;
+                        }
+                        if (motion_of(fb) == DYNAMIC) {
+                            w.com[c.b] = make_float4(PB.com.x, PB.com.y, PB.com.z, 0.f);
+                            w.quat[c.b] = PB.q;
+                        }
+                        any = true;
+                    }
+                }
+                if (!any) break;
+            }
+        }
+        for (int k = 0; k < nb; k++) finish_body(w, bl[k]);
+        if (c_settings.allow_sleeping) {
+            bool all = true;
+            for (int k = 0; k < nb; k++) {
+                int i = bl[k];
+                if (motion_of(w.flags[i]) != DYNAMIC) continue;
+                bool cs = sleep_update(w, i, dt);
+                all = all && cs;
+            }
+            if (all)
+                for (int k = 0; k < nb; k++)
+                    if (motion_of(w.flags[bl[k]]) == DYNAMIC) sleep_body(w, bl[k]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// large islands: one CTA per island, contacts sorted by the reference key,
+// greedily coloured in that order and swept colour by colour
+// ---------------------------------------------------------------------------
+constexpr int LARGE_BLOCK = 256;
+
+__global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTables ct, const int *large_list,
+                                                              int *scratch_order, int *scratch_colour,
+                                                              int *scratch_claim, float dt, float ratio) {
+    __shared__ int s_any;
+    __shared__ int s_ncol;
+    __shared__ int s_colour_start[257];
+    int nl = w.ctr->num_large_islands;
+    CacheRecord *crecs = ct.recs[*ct.parity];
+    for (int li = blockIdx.x; li < nl; li += gridDim.x) {
+        int isl = large_list[li];
+        int nb = w.island_body_count[isl], nc = w.island_cons_count[isl];
+        const int *bl = w.island_bodies + w.island_body_off[isl];
+        const int *cl = w.island_cons + w.island_cons_off[isl];
+        int *order = scratch_order + w.island_cons_off[isl];
+        int *colour = scratch_colour + w.island_cons_off[isl];
+        // rank of each contact in (sortKey, A, B) order (ties cannot occur: keys include both bodies)
+        for (int k = threadIdx.x; k < nc; k += blockDim.x) {
+            const ContactConstraint &c = w.cons[cl[k]];
+            int rank = 0;
+            for (int j = 0; j < nc; j++) {
+                const ContactConstraint &o = w.cons[cl[j]];
+                if (con_less(o, c) || (!con_less(c, o) && j < k)) rank++;
+            }
+            order[rank] = cl[k];
+        }
+        for (int k = threadIdx.x; k < nb; k += blockDim.x) prepare_body(w, bl[k]);
+        __syncthreads();
+        // greedy colouring in rank order: per round, the lowest rank claims each dynamic body
+        for (int k = threadIdx.x; k < nc; k += blockDim.x) colour[k] = -1;
+        if (threadIdx.x == 0) s_ncol = 0;
+        __syncthreads();
+        int round = 0;
+        while (true) {
+            for (int k = threadIdx.x; k < nb; k += blockDim.x) scratch_claim[bl[k]] = 0x7fffffff;
+            __syncthreads();
+            int left = 0;
+            for (int k = threadIdx.x; k < nc; k += blockDim.x) {
+                if (colour[k] >= 0) continue;
+                left = 1;
+                const ContactConstraint &c = w.cons[order[k]];
+                if (motion_of(w.flags[c.a]) == DYNAMIC) atomicMin(&scratch_claim[c.a], k);
+                if (motion_of(w.flags[c.b]) == DYNAMIC) atomicMin(&scratch_claim[c.b], k);
+            }
+            if (!__syncthreads_or(left)) break;
+            for (int k = threadIdx.x; k < nc; k += blockDim.x) {
+                if (colour[k] >= 0) continue;
+                const ContactConstraint &c = w.cons[order[k]];
+                bool oka = motion_of(w.flags[c.a]) != DYNAMIC || scratch_claim[c.a] == k;
+                bool okb = motion_of(w.flags[c.b]) != DYNAMIC || scratch_claim[c.b] == k;
+                if (oka && okb) colour[k] = round;
+            }
+            __syncthreads();
+            round++;
+            if (round >= 256) {
+                // put the rest in the last colour, solved serially by one thread
+                for (int k = threadIdx.x; k < nc; k += blockDim.x)
+                    if (colour[k] < 0) colour[k] = 256;
+                __syncthreads();
+                break;
+            }
+        }
+        int ncol = round;
+        // counting sort of ranks by colour (stable: keeps rank order inside a colour)
+        if (threadIdx.x == 0) {
+            for (int c = 0; c <= 256; c++) s_colour_start[c] = 0;
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < nc; k += blockDim.x) atomicAdd(&s_colour_start[min(colour[k], 256)], 1);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int acc = 0;
+            for (int c = 0; c <= 256; c++) {
+                int t = s_colour_start[c];
+                s_colour_start[c] = acc;
+                acc += t;
+            }
+            s_ncol = ncol;
+        }
+        __syncthreads();
+        // place contacts: sequential per colour by one thread keeps rank order
+        int *sorted = scratch_claim + w.cap;  // second half of the claim scratch
+        int *sorted_i = sorted + w.island_cons_off[isl];
+        if (threadIdx.x == 0) {
+            int fill[257];
+            for (int c = 0; c <= 256; c++) fill[c] = s_colour_start[c];
+            for (int k = 0; k < nc; k++) {
+                int c = min(colour[k], 256);
+                sorted_i[fill[c]++] = order[k];
+            }
+        }
+        __syncthreads();
+        int colour_end_last = nc;
+        // warm start (per colour)
+        auto sweep = [&](int mode) {
+            for (int c = 0; c <= 256; c++) {
+                int s0 = s_colour_start[c];
+                int s1 = (c < 256) ? s_colour_start[c + 1] : colour_end_last;
+                if (s1 <= s0) {
+                    if (c >= s_ncol) break;
+                    continue;
+                }
+                if (c < 256) {
+                    for (int k = s0 + threadIdx.x; k < s1; k += blockDim.x) {
+                        ContactConstraint &con = w.cons[sorted_i[k]];
+                        BodyRef A = load_body(w, con.a), B = load_body(w, con.b);
+                        if (mode == 0)
+                            warm_start_con(con, A, B, ratio);
+                        else
+                            solve_velocity_con(con, A, B);
+                        store_body_vel(w, con.a, A);
+                        store_body_vel(w, con.b, B);
+                    }
+                } else if (threadIdx.x == 0) {
+                    for (int k = s0; k < s1; k++) {
+                        ContactConstraint &con = w.cons[sorted_i[k]];
+                        BodyRef A = load_body(w, con.a), B = load_body(w, con.b);
+                        if (mode == 0)
+                            warm_start_con(con, A, B, ratio);
+                        else
+                            solve_velocity_con(con, A, B);
+                        store_body_vel(w, con.a, A);
+                        store_body_vel(w, con.b, B);
+                    }
+                }
+                __syncthreads();
+            }
+        };
+        if (c_settings.warm_starting) sweep(0);
+        for (int it = 0; it < c_settings.vel_iters; it++) sweep(1);
+        for (int k = threadIdx.x; k < nc; k += blockDim.x) store_impulses(w, crecs, w.cons[cl[k]]);
+        for (int k = threadIdx.x; k < nb; k += blockDim.x) integrate_body(w, bl[k], dt);
+        __syncthreads();
+        for (int it = 0; it < c_settings.pos_iters; it++) {
+            if (threadIdx.x == 0) s_any = 0;
+            __syncthreads();
+            for (int c = 0; c <= 256; c++) {
+                int s0 = s_colour_start[c];
+                int s1 = (c < 256) ? s_colour_start[c + 1] : colour_end_last;
+                if (s1 <= s0) {
+                    if (c >= s_ncol) break;
+                    continue;
+                }
+                int kbeg = (c < 256) ? s0 + (int)threadIdx.x : (threadIdx.x == 0 ? s0 : s1);
+                int kstep = (c < 256) ? (int)blockDim.x : 1;
+                for (int k = kbeg; k < s1; k += kstep) {
+                    const ContactConstraint &con = w.cons[sorted_i[k]];
+                    uint32_t fa = w.flags[con.a], fb = w.flags[con.b];
+                    PoseRef PA{xyz(w.com[con.a]), w.quat[con.a]}, PB{xyz(w.com[con.b]), w.quat[con.b]};
+                    if (solve_position_con(w, con, PA, PB, motion_of(fa), motion_of(fb), fa, fb)) {
+                        if (motion_of(fa) == DYNAMIC) {
+                            w.com[con.a] = make_float4(PA.com.x, PA.com.y, PA.com.z, 0.f);
+                            w.quat[con.a] = PA.q;
+                        }
+                        if (motion_of(fb) == DYNAMIC) {
+                            w.com[con.b] = make_float4(PB.com.x, PB.com.y, PB.com.z, 0.f);
+                            w.quat[con.b] = PB.q;
+                        }
+                        s_any = 1;
+                    }
+                }
+                __syncthreads();
+            }
+            if (!s_any) break;
+            __syncthreads();
+        }
+        for (int k = threadIdx.x; k < nb; k += blockDim.x) finish_body(w, bl[k]);
+        __syncthreads();
+        if (c_settings.allow_sleeping) {
+            int mine = 1;
+            for (int k = threadIdx.x; k < nb; k += blockDim.x) {
+                int i = bl[k];
+                if (motion_of(w.flags[i]) != DYNAMIC) continue;
+                if (!sleep_update(w, i, dt)) mine = 0;
+            }
+            int all = __syncthreads_and(mine);
+            if (all)
+                for (int k = threadIdx.x; k < nb; k += blockDim.x)
+                    if (motion_of(w.flags[bl[k]]) == DYNAMIC) sleep_body(w, bl[k]);
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static CacheTables tables_of(DevWorld &w) {
+    CacheTables ct;
+    ct.keys[0] = w.cache_keys[0];
+    ct.keys[1] = w.cache_keys[1];
+    ct.recs[0] = w.cache_recs[0];
+    ct.recs[1] = w.cache_recs[1];
+    ct.parity = w.cache_parity;
+    return ct;
+}
+
+__global__ void k_flip_parity(int *parity) { *parity ^= 1; }
+__global__ void k_mark_no_constraint(DevWorld w) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.max_manifolds; i += gridDim.x * blockDim.x)
+        w.cons_of_manifold[i] = -1;
+}
+__global__ void k_clear_cache_keys(CacheTables ct, int cap) {
+    unsigned long long *k = ct.keys[*ct.parity];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x) k[i] = EMPTY_KEY;
+}
+
+void launch_cache_begin(DevWorld &w, cudaStream_t s) {
+    // flip first so that keys[parity] is the table of two steps ago, then clear it
+    k_flip_parity<<<1, 1, 0, s>>>(w.cache_parity);
+    k_clear_cache_keys<<<grid_for(w.cache_cap, 256), 256, 0, s>>>(tables_of(w), w.cache_cap);
+}
+
+void launch_contacts_and_islands(DevWorld &w, float dt, float, cudaStream_t s) {
+    CacheTables ct = tables_of(w);
+    int nmax = w.n > w.max_manifolds ? w.n : w.max_manifolds;
+    k_mark_no_constraint<<<grid_for(w.max_manifolds, 256), 256, 0, s>>>(w);
+    k_contact_setup<<<grid_for(w.max_manifolds, 128, 16), 128, 0, s>>>(w, ct, dt);
+    k_apply_wake<<<grid_for(w.n, 256), 256, 0, s>>>(w);
+    k_uf_init<<<grid_for(w.n, 256), 256, 0, s>>>(w);
+    k_uf_link<<<grid_for(w.max_manifolds, 256), 256, 0, s>>>(w);
+    k_uf_roots<<<grid_for(w.n, 256), 256, 0, s>>>(w, w.root_flag);
+    exclusive_scan_int(w.root_flag, w.island_id_of_root, w.n, &w.ctr->num_islands, w.scan_tmp, s);
+    k_island_count<<<grid_for(nmax, 256), 256, 0, s>>>(w, w.island_id_of_root);
+    exclusive_scan_int(w.island_body_count, w.island_body_off, w.n, nullptr, w.scan_tmp, s);
+    exclusive_scan_int(w.island_cons_count, w.island_cons_off, w.n, nullptr, w.scan_tmp, s);
+    k_island_scatter<<<grid_for(nmax, 256), 256, 0, s>>>(w);
+    k_island_classify<<<grid_for(w.n, 256), 256, 0, s>>>(w, w.small_list, w.large_list);
+}
+
+void launch_solver(DevWorld &w, float dt, float ratio, cudaStream_t s) {
+    CacheTables ct = tables_of(w);
+    k_solve_small<<<grid_for(w.n, 128, 16), 128, 0, s>>>(w, ct, w.small_list, dt, ratio);
+    k_solve_large<<<NUM_SMS * 2, LARGE_BLOCK, 0, s>>>(w, ct, w.large_list, w.scratch_order, w.scratch_colour,
+                                                      w.scratch_claim, dt, ratio);
+}
+
+}  // namespace cc

@@ -1,0 +1,660 @@
+// C ABI of the GB300 world step: world creation, body upload (mass
+// properties, sleep spheres), state exchange, and the per-step launch
+// sequence captured once into a CUDA graph and replayed every step.
+//
+// Reference: createWorldSettings (src/world-settings.ts:224-264),
+// createWorld (src/world.ts:46-58), rigidBody.create (src/body/rigid-body.ts:
+// 390-434), updateWorld (src/update.ts:45-239).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "cc_internal.cuh"
+
+using namespace cc;
+
+struct cc_world {
+    cc_world_settings settings;
+    DevSettings dev_settings;
+    DevWorld w;
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    float graph_dt = -1.f, graph_ratio = -1.f;
+    double prev_dt = 0.0;
+    int steps_done = 0;
+    int last_status = CC_OK;
+    DevCounters last_ctr{};
+    std::vector<uint64_t> ids;
+    float *d_state_rows = nullptr;  // 16 floats per body staging for get/set state
+    float *h_pinned_rows = nullptr;
+    DevCounters *h_ctr = nullptr;   // pinned mirror of the device counters
+};
+
+static int cuda_ok(cudaError_t e) {
+    if (e != cudaSuccess) {
+        fprintf(stderr, "crashcat_gpu: CUDA error %s\n", cudaGetErrorString(e));
+        return CC_ERR_CUDA;
+    }
+    return CC_OK;
+}
+#define CC_TRY(x)                                    \
+    do {                                             \
+        int _r = cuda_ok(x);                         \
+        if (_r != CC_OK) return _r;                  \
+    } while (0)
+
+template <typename T>
+static int dalloc(T **p, size_t count) {
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)p, sizeof(T) * count);
+    if (e != cudaSuccess) return cuda_ok(e);
+    return cuda_ok(cudaMemset(*p, 0, sizeof(T) * count));
+}
+
+static int next_pow2(int v) {
+    int p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+extern "C" {
+
+const char *cc_status_string(int status) {
+    switch (status) {
+        case CC_OK:
+            return "ok";
+        case CC_ERR_INVALID:
+            return "invalid argument";
+        case CC_ERR_CAPACITY:
+            return "a per-step buffer overflowed (pairs, manifolds, EPA queue or contact cache)";
+        case CC_ERR_TIMEOUT:
+            return "a bounded device-side wait gave up";
+        case CC_ERR_NAN:
+            return "non-finite body state";
+        case CC_ERR_CUDA:
+            return "CUDA runtime error";
+        case CC_ERR_UNSUPPORTED:
+            return "unsupported feature";
+    }
+    return "unknown status";
+}
+
+// createWorldSettings world-settings.ts:224-264, with the two-layer setup of
+// the reference's tests (tst/helpers.ts:5-26): MOVING (0) collides with MOVING
+// and NOT_MOVING (1).
+int cc_world_settings_default(cc_world_settings *o) {
+    if (!o) return CC_ERR_INVALID;
+    memset(o, 0, sizeof(*o));
+    o->gravity[0] = 0;
+    o->gravity[1] = -9.81;
+    o->gravity[2] = 0;
+    o->gravity_enabled = 1;
+    o->speculative_contact_distance = 0.02;
+    o->manifold_tolerance = 1e-3;
+    o->collision_tolerance = 1e-4;
+    o->penetration_tolerance = 1e-4;
+    o->normal_cos_max_delta_rotation = cos((5 * M_PI) / 180);
+    o->contact_point_preserve_lambda_max_dist_sq = 0.01 * 0.01;
+    o->velocity_iterations = 10;
+    o->position_iterations = 2;
+    o->warm_starting = 1;
+    o->penetration_slop = 0.02;
+    o->baumgarte_factor = 0.2;
+    o->max_penetration_distance = 0.2;
+    o->min_velocity_for_restitution = 1;
+    o->allow_sleeping = 1;
+    o->time_before_sleep = 0.5;
+    o->point_velocity_sleep_threshold = 0.03;
+    o->num_object_layers = 2;
+    o->num_broadphase_layers = 2;
+    o->object_to_broadphase[0] = 0;
+    o->object_to_broadphase[1] = 1;
+    o->object_pairs[0] = 0b11;
+    o->object_pairs[1] = 0b01;
+    o->object_vs_broadphase[0] = 0b11;
+    o->object_vs_broadphase[1] = 0b11;
+    o->broadphase_pairs[0] = 0b11;
+    o->broadphase_pairs[1] = 0b01;
+    o->max_bodies = 1 << 16;
+    o->num_worlds = 1;
+    return CC_OK;
+}
+
+int cc_world_create(const cc_world_settings *s, cc_world **out) {
+    if (!s || !out) return CC_ERR_INVALID;
+    if (s->num_object_layers < 1 || s->num_object_layers > CC_MAX_LAYERS || s->num_broadphase_layers < 1 ||
+        s->num_broadphase_layers > CC_MAX_LAYERS || s->max_bodies < 1 || s->num_worlds < 1)
+        return CC_ERR_INVALID;
+    cc_world *W = new (std::nothrow) cc_world();
+    if (!W) return CC_ERR_INVALID;
+    W->settings = *s;
+    DevSettings &d = W->dev_settings;
+    memset(&d, 0, sizeof(d));
+    for (int k = 0; k < 3; k++) d.gravity[k] = (float)s->gravity[k];
+    d.gravity_enabled = s->gravity_enabled;
+    d.spec_dist = (float)s->speculative_contact_distance;
+    d.manifold_tol = (float)s->manifold_tolerance;
+    d.collision_tol = (float)s->collision_tolerance;
+    d.penetration_tol = (float)s->penetration_tolerance;
+    d.normal_cos = (float)s->normal_cos_max_delta_rotation;
+    d.preserve_lambda_dsq = (float)s->contact_point_preserve_lambda_max_dist_sq;
+    d.vel_iters = s->velocity_iterations;
+    d.pos_iters = s->position_iterations;
+    d.warm_starting = s->warm_starting;
+    d.slop = (float)s->penetration_slop;
+    d.baumgarte = (float)s->baumgarte_factor;
+    d.max_pen = (float)s->max_penetration_distance;
+    d.min_vel_restitution = (float)s->min_velocity_for_restitution;
+    d.allow_sleeping = s->allow_sleeping;
+    d.time_before_sleep = (float)s->time_before_sleep;
+    d.sleep_threshold = (float)s->point_velocity_sleep_threshold;
+    // combined layer predicate: object layer pair enabled AND the querying
+    // layer may query the other's broadphase layer AND the broadphase layers
+    // collide (broadphase.ts:252-272, dbvt.ts:657-660)
+    for (int a = 0; a < s->num_object_layers; a++) {
+        uint32_t m = 0;
+        int bpa = s->object_to_broadphase[a];
+        for (int b = 0; b < s->num_object_layers; b++) {
+            int bpb = s->object_to_broadphase[b];
+            bool ok = (s->object_pairs[a] >> b) & 1;
+            ok = ok && ((s->object_vs_broadphase[a] >> bpb) & 1);
+            ok = ok && ((s->broadphase_pairs[bpa] >> bpb) & 1);
+            if (ok) m |= 1u << b;
+        }
+        d.allowed_pairs[a] = m;
+    }
+    DevWorld &w = W->w;
+    memset(&w, 0, sizeof(w));
+    int cap = s->max_bodies;
+    w.cap = cap;
+    w.n = 0;
+    w.num_worlds = s->num_worlds;
+    w.max_pairs = s->max_pairs > 0 ? s->max_pairs : 16 * cap + 1024;
+    w.max_manifolds = s->max_manifolds > 0 ? s->max_manifolds : 8 * cap + 1024;
+    w.max_epa = w.max_manifolds;
+    w.cache_cap = next_pow2(2 * w.max_manifolds);
+    int r = CC_OK;
+#define ALLOC(field, count)                       \
+    if ((r = dalloc(&w.field, (count))) != CC_OK) { \
+        cc_world_destroy(W);                      \
+        return r;                                 \
+    }
+    ALLOC(pos, cap);
+    ALLOC(quat, cap);
+    ALLOC(com, cap);
+    ALLOC(linvel, cap);
+    ALLOC(angvel, cap);
+    ALLOC(force, cap);
+    ALLOC(torque, cap);
+    ALLOC(inv_inertia, cap);
+    ALLOC(inertia_rot, cap);
+    ALLOC(shape, cap);
+    ALLOC(material, cap);
+    ALLOC(damping, cap);
+    ALLOC(flags, cap);
+    ALLOC(groups, cap);
+    ALLOC(world, cap);
+    ALLOC(sleep_sph, 3 * (size_t)cap);
+    ALLOC(sleep_timer, cap);
+    ALLOC(aabb64, 6 * (size_t)cap);
+    ALLOC(aabb_lo, cap);
+    ALLOC(aabb_hi, cap);
+    ALLOC(wake, cap);
+    ALLOC(morton, cap);
+    ALLOC(morton_alt, cap);
+    ALLOC(order, cap);
+    ALLOC(order_alt, cap);
+    ALLOC(node_parent, 2 * (size_t)cap);
+    ALLOC(node_child, cap);
+    ALLOC(node_lo, 2 * (size_t)cap);
+    ALLOC(node_hi, 2 * (size_t)cap);
+    ALLOC(node_flag, cap);
+    ALLOC(pairs, w.max_pairs);
+    ALLOC(manifolds, w.max_manifolds);
+    ALLOC(cons, w.max_manifolds);
+    ALLOC(cons_of_manifold, w.max_manifolds);
+    ALLOC(uf_parent, cap);
+    ALLOC(island_of_body, cap);
+    ALLOC(island_id_of_root, cap);
+    ALLOC(island_body_count, cap);
+    ALLOC(island_cons_count, cap);
+    ALLOC(island_body_off, cap);
+    ALLOC(island_cons_off, cap);
+    ALLOC(island_bodies, cap);
+    ALLOC(island_cons, w.max_manifolds);
+    ALLOC(island_fill_b, cap);
+    ALLOC(island_fill_c, cap);
+    ALLOC(inv_inertia_world, 2 * (size_t)cap);
+    {
+        size_t tmp = scan_tmp_ints(cap > w.max_manifolds ? cap : w.max_manifolds);
+        ALLOC(scan_tmp, tmp);
+    }
+    ALLOC(ctr, 1);
+    ALLOC(scene, 16);
+    ALLOC(node_world, 2 * (size_t)cap);
+    {
+        char *p = nullptr;
+        if ((r = dalloc(&p, epa_item_bytes() * (size_t)w.max_epa)) != CC_OK) {
+            cc_world_destroy(W);
+            return r;
+        }
+        w.epa_items = p;
+        char *q = nullptr;
+        if ((r = dalloc(&q, epa_scratch_bytes() * (size_t)EPA_THREADS)) != CC_OK) {
+            cc_world_destroy(W);
+            return r;
+        }
+        w.epa_scratch = q;
+    }
+    for (int k = 0; k < 2; k++) {
+        ALLOC(cache_keys[k], w.cache_cap);
+        ALLOC(cache_recs[k], w.cache_cap);
+        cudaMemset(w.cache_keys[k], 0xff, sizeof(unsigned long long) * w.cache_cap);
+    }
+    ALLOC(cache_parity, 1);
+    ALLOC(root_flag, cap);
+    ALLOC(small_list, cap);
+    ALLOC(large_list, cap);
+    ALLOC(scratch_order, w.max_manifolds);
+    ALLOC(scratch_colour, w.max_manifolds);
+    ALLOC(scratch_claim, (size_t)cap + (size_t)w.max_manifolds + 16);
+#undef ALLOC
+    if ((r = cuda_ok(cudaStreamCreateWithFlags(&W->stream, cudaStreamNonBlocking))) != CC_OK) {
+        cc_world_destroy(W);
+        return r;
+    }
+    if ((r = dalloc(&W->d_state_rows, 16 * (size_t)cap)) != CC_OK) {
+        cc_world_destroy(W);
+        return r;
+    }
+    if ((r = cuda_ok(cudaMallocHost((void **)&W->h_ctr, sizeof(DevCounters)))) != CC_OK) {
+        cc_world_destroy(W);
+        return r;
+    }
+    memset(W->h_ctr, 0, sizeof(DevCounters));
+    *out = W;
+    return CC_OK;
+}
+
+int cc_world_destroy(cc_world *W) {
+    if (!W) return CC_ERR_INVALID;
+    DevWorld &w = W->w;
+    if (W->stream) cudaStreamSynchronize(W->stream);
+    if (W->graph_exec) cudaGraphExecDestroy(W->graph_exec);
+    if (W->graph) cudaGraphDestroy(W->graph);
+    void *ptrs[] = {w.pos, w.quat, w.com, w.linvel, w.angvel, w.force, w.torque, w.inv_inertia, w.inertia_rot,
+                    w.shape, w.material, w.damping, w.flags, w.groups, w.world, w.sleep_sph, w.sleep_timer,
+                    w.aabb64, w.aabb_lo, w.aabb_hi, w.wake, w.morton, w.morton_alt, w.order, w.order_alt,
+                    w.node_parent, w.node_child, w.node_lo, w.node_hi, w.node_flag, w.pairs, w.manifolds, w.cons,
+                    w.cons_of_manifold, w.uf_parent, w.island_of_body, w.island_id_of_root, w.island_body_count,
+                    w.island_cons_count, w.island_body_off, w.island_cons_off, w.island_bodies, w.island_cons,
+                    w.island_fill_b, w.island_fill_c, w.inv_inertia_world, w.scan_tmp, w.ctr, w.scene,
+                    w.node_world, w.epa_items, w.epa_scratch, w.cache_keys[0], w.cache_keys[1], w.cache_recs[0],
+                    w.cache_recs[1], w.cache_parity, w.root_flag, w.small_list, w.large_list, w.scratch_order,
+                    w.scratch_colour, w.scratch_claim, W->d_state_rows};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (W->h_ctr) cudaFreeHost(W->h_ctr);
+    if (W->stream) cudaStreamDestroy(W->stream);
+    delete W;
+    return CC_OK;
+}
+
+int cc_world_num_bodies(const cc_world *W, int32_t *out) {
+    if (!W || !out) return CC_ERR_INVALID;
+    *out = W->w.n;
+    return CC_OK;
+}
+
+// rigidBody.create rigid-body.ts:390-434: mass properties (box: setMassAndInertiaOfSolidBox
+// mass-properties.ts:36-52; sphere: sphere.ts:97-123), setMassProperties
+// (motion-properties.ts:419-491; the inertia of boxes and spheres is diagonal so
+// the principal rotation is the identity), centre of mass, sleep spheres.
+int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *out_index) {
+    if (!W || (!b && n > 0) || n < 0) return CC_ERR_INVALID;
+    DevWorld &w = W->w;
+    if (w.n + n > w.cap) return CC_ERR_CAPACITY;
+    std::vector<float4> pos(n), quat(n), com(n), lin(n), ang(n), zero(n), ii(n), ir(n), sh(n), mat(n), damp(n),
+        sph(3 * (size_t)n);
+    std::vector<uint32_t> flags(n);
+    std::vector<uint2> groups(n);
+    std::vector<int> world(n);
+    std::vector<float> timer(n, 0.f);
+    for (int i = 0; i < n; i++) {
+        const cc_body_desc &d = b[i];
+        if (d.shape_type != CC_SHAPE_BOX && d.shape_type != CC_SHAPE_SPHERE) return CC_ERR_UNSUPPORTED;
+        if (d.motion_type < 0 || d.motion_type > 2) return CC_ERR_INVALID;
+        if (d.object_layer < 0 || d.object_layer >= W->settings.num_object_layers) return CC_ERR_INVALID;
+        if (d.world < 0 || d.world >= w.num_worlds) return CC_ERR_INVALID;
+        double mass;
+        double idiag[3];
+        if (d.shape_type == CC_SHAPE_BOX) {
+            double fx = 2.0 * d.shape_params[0], fy = 2.0 * d.shape_params[1], fz = 2.0 * d.shape_params[2];
+            mass = fx * fy * fz * d.density;
+            idiag[0] = (fy * fy + fz * fz) * (mass / 12.0);
+            idiag[1] = (fx * fx + fz * fz) * (mass / 12.0);
+            idiag[2] = (fx * fx + fy * fy) * (mass / 12.0);
+        } else {
+            double r = d.shape_params[0];
+            mass = (4.0 / 3.0) * M_PI * r * r * r * d.density;
+            double in = 0.4 * mass * r * r;
+            idiag[0] = idiag[1] = idiag[2] = in;
+        }
+        int dof = d.allowed_dofs & 63;
+        float inv_mass = 0.f;
+        float3 inv_i = f3(0.f, 0.f, 0.f);
+        if (d.motion_type != CC_STATIC) {
+            if ((dof & 7) != 0) {
+                if (!(mass > 0)) return CC_ERR_INVALID;
+                inv_mass = (float)(1.0 / mass);
+            }
+            if (((dof >> 3) & 7) != 0) {
+                double l = idiag[0] * idiag[0] + idiag[1] * idiag[1] + idiag[2] * idiag[2];
+                if (l > 1e-20)
+                    inv_i = f3(idiag[0] != 0 ? (float)(1.0 / idiag[0]) : 0.f, idiag[1] != 0 ? (float)(1.0 / idiag[1]) : 0.f,
+                               idiag[2] != 0 ? (float)(1.0 / idiag[2]) : 0.f);
+                else
+                    inv_i = f3(2.5f * inv_mass, 2.5f * inv_mass, 2.5f * inv_mass);
+            }
+        }
+        pos[i] = make_float4(d.position[0], d.position[1], d.position[2], 0.f);
+        quat[i] = make_float4(d.quaternion[0], d.quaternion[1], d.quaternion[2], d.quaternion[3]);
+        com[i] = pos[i];  // shape centre of mass is the origin for boxes and spheres
+        lin[i] = make_float4(d.linear_velocity[0], d.linear_velocity[1], d.linear_velocity[2], 0.f);
+        ang[i] = make_float4(d.angular_velocity[0], d.angular_velocity[1], d.angular_velocity[2], 0.f);
+        zero[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        ii[i] = make_float4(inv_i.x, inv_i.y, inv_i.z, inv_mass);
+        ir[i] = make_float4(0.f, 0.f, 0.f, 1.f);
+        sh[i] = make_float4(d.shape_params[0], d.shape_params[1], d.shape_params[2], d.shape_params[3]);
+        mat[i] = make_float4(d.friction, d.restitution, d.gravity_factor, 0.f);
+        damp[i] = make_float4(d.linear_damping, d.angular_damping, d.max_linear_velocity, d.max_angular_velocity);
+        uint32_t f = (uint32_t)d.motion_type;
+        if (d.allow_sleeping) f |= F_ALLOW_SLEEP;
+        f |= (uint32_t)d.shape_type << F_SHAPE_SHIFT;
+        f |= (uint32_t)dof << F_DOF_SHIFT;
+        f |= (uint32_t)(d.friction_combine & 7) << F_FCOMB_SHIFT;
+        f |= (uint32_t)(d.restitution_combine & 7) << F_RCOMB_SHIFT;
+        f |= (uint32_t)(d.object_layer & 31) << F_LAYER_SHIFT;
+        flags[i] = f;
+        groups[i] = make_uint2(d.collision_groups, d.collision_mask);
+        world[i] = d.world;
+        // resetSleepTimer sleep.ts:123-130
+        float3 e = d.shape_type == CC_SHAPE_BOX ? f3(d.shape_params[0], d.shape_params[1], d.shape_params[2])
+                                                 : f3(d.shape_params[0], d.shape_params[0], d.shape_params[0]);
+        float3 c = xyz(com[i]);
+        float3 p[3];
+        p[0] = c;
+        int lowest = (e.x <= e.y && e.x <= e.z) ? 0 : (e.y <= e.z ? 1 : 2);
+        float3 X = f3(1, 0, 0), Y = f3(0, 1, 0), Z = f3(0, 0, 1);
+        float4 q = quat[i];
+        if (lowest == 0) {
+            p[1] = c + qrot(q, Y) * e.y;
+            p[2] = c + qrot(q, Z) * e.z;
+        } else if (lowest == 1) {
+            p[1] = c + qrot(q, X) * e.x;
+            p[2] = c + qrot(q, Z) * e.z;
+        } else {
+            p[1] = c + qrot(q, X) * e.x;
+            p[2] = c + qrot(q, Y) * e.y;
+        }
+        for (int k = 0; k < 3; k++) sph[3 * i + k] = make_float4(p[k].x, p[k].y, p[k].z, 0.f);
+        if (out_index) out_index[i] = w.n + i;
+    }
+    size_t o = w.n;
+    cudaStream_t s = W->stream;
+    CC_TRY(cudaMemcpyAsync(w.pos + o, pos.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaMemcpyAsync(w.quat + o, quat.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaMemcpyAsync(w.com + o, com.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaMemcpyAsync(w.linvel + o, lin.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaMemcpyAsync(w.angvel + o, ang.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaMemcpyAsync(w.force + o, zero.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaMemcpyAsync(w.torque + o, zero.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaMemcpyAsync(w.inv_inertia + o, ii.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaMemcpyAsync(w.inertia_rot + o, ir.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaMemcpyAsync(w.shape + o, sh.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaMemcpyAsync(w.material + o, mat.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaMemcpyAsync(w.damping + o, damp.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaMemcpyAsync(w.flags + o, flags.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaMemcpyAsync(w.groups + o, groups.data(), sizeof(uint2) * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaMemcpyAsync(w.world + o, world.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaMemcpyAsync(w.sleep_sph + 3 * o, sph.data(), sizeof(float4) * 3 * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaMemcpyAsync(w.sleep_timer + o, timer.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaStreamSynchronize(s));
+    w.n += n;
+    // body count changed: the captured step graph no longer matches
+    if (W->graph_exec) {
+        cudaGraphExecDestroy(W->graph_exec);
+        W->graph_exec = nullptr;
+    }
+    if (W->graph) {
+        cudaGraphDestroy(W->graph);
+        W->graph = nullptr;
+    }
+    return CC_OK;
+}
+
+}  // extern "C"
+
+// one step's launch sequence (update.ts:45-239)
+static void enqueue_step(cc_world *W, float dt, float ratio) {
+    DevWorld &w = W->w;
+    cudaStream_t s = W->stream;
+    cudaMemsetAsync(w.ctr, 0, sizeof(DevCounters), s);
+    launch_cache_begin(w, s);
+    launch_integrate_forces(w, dt, s);
+    launch_broadphase(w, s);
+    launch_narrowphase(w, dt, s);
+    launch_contacts_and_islands(w, dt, ratio, s);
+    if (dt > 0.f) launch_solver(w, dt, ratio, s);
+    cudaMemcpyAsync(W->h_ctr, w.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s);
+}
+
+static int run_steps(cc_world *W, float dt, int n_steps) {
+    if (W->w.n == 0) return CC_OK;
+    upload_settings(W->dev_settings, W->settings.speculative_contact_distance, W->stream);
+    int status = CC_OK;
+    for (int i = 0; i < n_steps; i++) {
+        // warm start ratio dt / previous dt, 0 on the first step (update.ts:118-124)
+        float ratio = (W->settings.warm_starting && W->prev_dt > 0) ? (float)(dt / W->prev_dt) : 0.f;
+        if (dt <= 0.f) ratio = 0.f;
+        bool use_graph = ratio != 0.f;  // the first step after creation runs eagerly
+        if (use_graph) {
+            if (!W->graph_exec || W->graph_dt != dt || W->graph_ratio != ratio) {
+                if (W->graph_exec) cudaGraphExecDestroy(W->graph_exec);
+                if (W->graph) cudaGraphDestroy(W->graph);
+                W->graph_exec = nullptr;
+                W->graph = nullptr;
+                CC_TRY(cudaStreamBeginCapture(W->stream, cudaStreamCaptureModeThreadLocal));
+                enqueue_step(W, dt, ratio);
+                CC_TRY(cudaStreamEndCapture(W->stream, &W->graph));
+                CC_TRY(cudaGraphInstantiate(&W->graph_exec, W->graph, 0));
+                W->graph_dt = dt;
+                W->graph_ratio = ratio;
+            }
+            CC_TRY(cudaGraphLaunch(W->graph_exec, W->stream));
+        } else {
+            enqueue_step(W, dt, ratio);
+        }
+        if (dt > 0.f) W->prev_dt = dt;
+        W->steps_done++;
+    }
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    CC_TRY(cudaGetLastError());
+    W->last_ctr = *W->h_ctr;
+    if (W->last_ctr.overflow) status = CC_ERR_CAPACITY;
+    W->last_status = status;
+    return status;
+}
+
+__global__ void k_pack_state(DevWorld w, float *rows, unsigned char *sleeping) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
+        float *o = rows + (size_t)i * 16;
+        float4 p = w.pos[i], q = w.quat[i], v = w.linvel[i], a = w.angvel[i], c = w.com[i];
+        o[0] = p.x;
+        o[1] = p.y;
+        o[2] = p.z;
+        o[3] = q.x;
+        o[4] = q.y;
+        o[5] = q.z;
+        o[6] = q.w;
+        o[7] = v.x;
+        o[8] = v.y;
+        o[9] = v.z;
+        o[10] = a.x;
+        o[11] = a.y;
+        o[12] = a.z;
+        o[13] = c.x;
+        o[14] = c.y;
+        o[15] = c.z;
+        if (sleeping) sleeping[i] = sleeping_of(w.flags[i]) ? 1 : 0;
+    }
+}
+
+// setTransform / setLinearVelocity / setAngularVelocity: pose, velocity and the
+// derived centre of mass (rigid-body.ts:527-536, 758-774)
+__global__ void k_unpack_state(DevWorld w, const float *rows) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
+        const float *o = rows + (size_t)i * 16;
+        w.pos[i] = make_float4(o[0], o[1], o[2], 0.f);
+        w.quat[i] = make_float4(o[3], o[4], o[5], o[6]);
+        w.linvel[i] = make_float4(o[7], o[8], o[9], 0.f);
+        w.angvel[i] = make_float4(o[10], o[11], o[12], 0.f);
+        w.com[i] = make_float4(o[0], o[1], o[2], 0.f);
+    }
+}
+
+extern "C" {
+
+int cc_world_step(cc_world *W, float dt, int32_t n_steps) {
+    if (!W || n_steps < 0 || !std::isfinite(dt)) return CC_ERR_INVALID;
+    return run_steps(W, dt, n_steps);
+}
+
+int cc_world_get_state(cc_world *W, float *rows, uint8_t *sleeping) {
+    if (!W || !rows) return CC_ERR_INVALID;
+    DevWorld &w = W->w;
+    if (w.n == 0) return CC_OK;
+    k_pack_state<<<grid_for(w.n, 256), 256, 0, W->stream>>>(w, W->d_state_rows, nullptr);
+    CC_TRY(cudaMemcpyAsync(rows, W->d_state_rows, sizeof(float) * 16 * w.n, cudaMemcpyDeviceToHost, W->stream));
+    if (sleeping) {
+        std::vector<uint32_t> f(w.n);
+        CC_TRY(cudaMemcpyAsync(f.data(), w.flags, sizeof(uint32_t) * w.n, cudaMemcpyDeviceToHost, W->stream));
+        CC_TRY(cudaStreamSynchronize(W->stream));
+        for (int i = 0; i < w.n; i++) sleeping[i] = sleeping_of(f[i]) ? 1 : 0;
+    }
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    return CC_OK;
+}
+
+int cc_world_set_state(cc_world *W, const float *rows) {
+    if (!W || !rows) return CC_ERR_INVALID;
+    DevWorld &w = W->w;
+    if (w.n == 0) return CC_OK;
+    CC_TRY(cudaMemcpyAsync(W->d_state_rows, rows, sizeof(float) * 16 * w.n, cudaMemcpyHostToDevice, W->stream));
+    k_unpack_state<<<grid_for(w.n, 256), 256, 0, W->stream>>>(w, W->d_state_rows);
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    return CC_OK;
+}
+
+int cc_world_step_host(cc_world *W, float dt, const float *state_in, float *state_out) {
+    if (!W || !state_in || !state_out) return CC_ERR_INVALID;
+    DevWorld &w = W->w;
+    if (w.n == 0) return CC_OK;
+    CC_TRY(cudaMemcpyAsync(W->d_state_rows, state_in, sizeof(float) * 16 * w.n, cudaMemcpyHostToDevice, W->stream));
+    k_unpack_state<<<grid_for(w.n, 256), 256, 0, W->stream>>>(w, W->d_state_rows);
+    int st = run_steps(W, dt, 1);
+    k_pack_state<<<grid_for(w.n, 256), 256, 0, W->stream>>>(w, W->d_state_rows, nullptr);
+    CC_TRY(cudaMemcpyAsync(state_out, W->d_state_rows, sizeof(float) * 16 * w.n, cudaMemcpyDeviceToHost, W->stream));
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    return st;
+}
+
+int cc_world_get_pairs(cc_world *W, int32_t *out, int32_t capacity, int32_t *count) {
+    if (!W || !count) return CC_ERR_INVALID;
+    int np = W->last_ctr.num_pairs;
+    if (np > W->w.max_pairs) np = W->w.max_pairs;
+    *count = np;
+    if (!out) return CC_OK;
+    if (capacity < np) return CC_ERR_CAPACITY;
+    if (np > 0) CC_TRY(cudaMemcpy(out, W->w.pairs, sizeof(int2) * np, cudaMemcpyDeviceToHost));
+    return CC_OK;
+}
+
+int cc_world_get_manifolds(cc_world *W, float *out, int32_t capacity, int32_t *count) {
+    if (!W || !count) return CC_ERR_INVALID;
+    DevWorld &w = W->w;
+    int nm = W->last_ctr.num_manifolds;
+    if (nm > w.max_manifolds) nm = w.max_manifolds;
+    std::vector<Manifold> ms(nm);
+    std::vector<int> cm(nm);
+    if (nm > 0) {
+        CC_TRY(cudaMemcpy(ms.data(), w.manifolds, sizeof(Manifold) * nm, cudaMemcpyDeviceToHost));
+        CC_TRY(cudaMemcpy(cm.data(), w.cons_of_manifold, sizeof(int) * nm, cudaMemcpyDeviceToHost));
+    }
+    int k = 0;
+    for (int i = 0; i < nm; i++) {
+        if (cm[i] < 0) continue;
+        if (out && k >= capacity) return CC_ERR_CAPACITY;
+        if (out) {
+            const Manifold &m = ms[i];
+            float *o = out + 32 * (size_t)k;
+            int A = m.a, B = m.b;
+            float3 n = m.normal;
+            bool swap = A > B;
+            float3 base = m.base;
+            o[0] = (float)(swap ? B : A);
+            o[1] = (float)(swap ? A : B);
+            o[2] = (float)m.n;
+            float3 nn = swap ? -n : n;
+            o[3] = nn.x;
+            o[4] = nn.y;
+            o[5] = nn.z;
+            o[6] = m.depth;
+            o[7] = 0.f;
+            for (int j = 0; j < 4; j++) {
+                float *p = o + 8 + 6 * j;
+                if (j < m.n) {
+                    float3 pa = (swap ? m.rb[j] : m.ra[j]) + base;
+                    float3 pb = (swap ? m.ra[j] : m.rb[j]) + base;
+                    p[0] = pa.x;
+                    p[1] = pa.y;
+                    p[2] = pa.z;
+                    p[3] = pb.x;
+                    p[4] = pb.y;
+                    p[5] = pb.z;
+                } else {
+                    for (int t = 0; t < 6; t++) p[t] = 0.f;
+                }
+            }
+        }
+        k++;
+    }
+    *count = k;
+    return CC_OK;
+}
+
+int cc_world_get_stats(cc_world *W, cc_stats *o) {
+    if (!W || !o) return CC_ERR_INVALID;
+    memset(o, 0, sizeof(*o));
+    const DevCounters &c = W->last_ctr;
+    o->num_bodies = W->w.n;
+    o->num_pairs = c.num_pairs;
+    o->num_manifolds = c.num_manifolds;
+    o->num_contact_points = c.num_points;
+    o->num_epa = c.num_epa;
+    o->num_islands = c.num_islands;
+    o->max_island_constraints = c.max_island_constraints;
+    o->overflow_flags = c.overflow;
+    o->gpu_launches_per_step = 0;
+    if (W->graph) {
+        size_t nn = 0;
+        cudaGraphGetNodes(W->graph, nullptr, &nn);
+        o->gpu_launches_per_step = (int)nn;
+    }
+    return CC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,217 @@
+"""Seeded synthetic scenes for the benchmark workloads and the parity tests.
+
+A scene is a ``BODY_DTYPE`` array (the C ``cc_body_desc`` layout) plus the
+world settings it runs with.  No public dataset is involved: every workload is
+generated from a numpy PCG64 generator with a recorded seed, following the
+shapes, sizes and value ranges of the workload descriptions.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+from ._lib import BODY_DTYPE, COMBINE_GEOMETRIC_MEAN, COMBINE_MAX, DYNAMIC, SHAPE_BOX, SHAPE_SPHERE, STATIC
+
+# object layers of the reference's test helper (tst/helpers.ts:5-26)
+LAYER_MOVING = 0
+LAYER_NOT_MOVING = 1
+
+# DEFAULT_RIGID_BODY_SETTINGS (src/body/rigid-body.ts:120-139)
+DEFAULT_FRICTION = 0.2
+DEFAULT_RESTITUTION = 0.0
+DEFAULT_DAMPING = 0.05
+DEFAULT_MAX_LINEAR_VELOCITY = 500.0
+DEFAULT_MAX_ANGULAR_VELOCITY = 0.25 * math.pi * 60.0
+DEFAULT_CONVEX_RADIUS = 0.05  # src/collision/support.ts:5
+DEFAULT_DENSITY = 1000.0  # src/shapes/shapes.ts:121
+
+
+@dataclasses.dataclass
+class Scene:
+    name: str
+    bodies: np.ndarray
+    dt: float
+    steps: int
+    velocity_iterations: int = 10
+    position_iterations: int = 2
+    num_worlds: int = 1
+    seed: int = 0
+
+    @property
+    def n(self) -> int:
+        return len(self.bodies)
+
+
+def blank_bodies(n: int) -> np.ndarray:
+    b = np.zeros(n, dtype=BODY_DTYPE)
+    b["density"] = DEFAULT_DENSITY
+    b["motion_type"] = DYNAMIC
+    b["object_layer"] = LAYER_MOVING
+    b["allow_sleeping"] = 1
+    b["quaternion"] = (0.0, 0.0, 0.0, 1.0)
+    b["friction"] = DEFAULT_FRICTION
+    b["restitution"] = DEFAULT_RESTITUTION
+    b["gravity_factor"] = 1.0
+    b["linear_damping"] = DEFAULT_DAMPING
+    b["angular_damping"] = DEFAULT_DAMPING
+    b["max_linear_velocity"] = DEFAULT_MAX_LINEAR_VELOCITY
+    b["max_angular_velocity"] = DEFAULT_MAX_ANGULAR_VELOCITY
+    b["friction_combine"] = COMBINE_GEOMETRIC_MEAN
+    b["restitution_combine"] = COMBINE_MAX
+    b["collision_groups"] = 0xFFFFFFFF
+    b["collision_mask"] = 0xFFFFFFFF
+    b["allowed_dofs"] = 0b111111
+    return b
+
+
+def set_box(b: np.ndarray, idx, half_extents, convex_radius: float = DEFAULT_CONVEX_RADIUS) -> None:
+    b["shape_type"][idx] = SHAPE_BOX
+    he = np.asarray(half_extents, dtype=np.float32)
+    b["shape_params"][idx, 0:3] = he
+    b["shape_params"][idx, 3] = convex_radius
+
+
+def set_sphere(b: np.ndarray, idx, radius) -> None:
+    b["shape_type"][idx] = SHAPE_SPHERE
+    b["shape_params"][idx, 0] = radius
+    b["shape_params"][idx, 1:] = 0.0
+
+
+def static_floor(b: np.ndarray, idx: int, half=(50.0, 0.5, 50.0), y=-0.5, friction=0.5, world=0) -> None:
+    set_box(b, idx, half)
+    b["motion_type"][idx] = STATIC
+    b["object_layer"][idx] = LAYER_NOT_MOVING
+    b["position"][idx] = (0.0, y, 0.0)
+    b["friction"][idx] = friction
+    b["world"][idx] = world
+
+
+def random_quaternions(rng: np.random.Generator, n: int) -> np.ndarray:
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    return q.astype(np.float32)
+
+
+def cube_heap(n_side: int = 10, seed: int = 1) -> Scene:
+    """1,000 dynamic boxes (half extents 0.5 m, density 1000, friction 0.5,
+    restitution 0) on an n_side^3 grid with 1.1 m spacing and uniform +-0.05 m
+    jitter, dropped onto a static 100 x 1 x 100 m box floor; dt 1/60, 10/2
+    iterations, 600 steps."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = n_side ** 3
+    b = blank_bodies(n + 1)
+    static_floor(b, 0, friction=0.5)
+    idx = np.arange(1, n + 1)
+    set_box(b, idx, (0.5, 0.5, 0.5))
+    b["friction"][idx] = 0.5
+    b["restitution"][idx] = 0.0
+    g = np.stack(np.meshgrid(np.arange(n_side), np.arange(n_side), np.arange(n_side), indexing="ij"), -1).reshape(-1, 3)
+    pos = np.empty((n, 3))
+    pos[:, 0] = (g[:, 0] - (n_side - 1) / 2) * 1.1
+    pos[:, 1] = 1.0 + g[:, 1] * 1.1
+    pos[:, 2] = (g[:, 2] - (n_side - 1) / 2) * 1.1
+    pos += rng.uniform(-0.05, 0.05, size=(n, 3))
+    b["position"][idx] = pos.astype(np.float32)
+    return Scene("cube_heap", b, dt=1.0 / 60.0, steps=600, velocity_iterations=10, position_iterations=2, seed=seed)
+
+
+def batched_worlds(num_worlds: int = 4096, seed: int = 4, n_min: int = 8, n_max: int = 512) -> Scene:
+    """num_worlds independent worlds with body counts drawn log-uniformly from
+    [n_min, n_max]; boxes (half extents 0.2-0.8 m) and spheres (r 0.2-0.6 m),
+    each world with its own static floor and seeded drop positions on a jittered
+    2 m grid; dt 1/120, 8/2 iterations, 1,000 steps."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    counts = np.rint(np.exp(rng.uniform(math.log(n_min), math.log(n_max), size=num_worlds))).astype(np.int64)
+    counts = np.clip(counts, n_min, n_max)
+    total = int(counts.sum()) + num_worlds
+    b = blank_bodies(total)
+    o = 0
+    for wi in range(num_worlds):
+        static_floor(b, o, half=(40.0, 0.5, 40.0), friction=0.5, world=wi)
+        o += 1
+        c = int(counts[wi])
+        sl = slice(o, o + c)
+        b["world"][sl] = wi
+        is_box = rng.random(c) < 0.5
+        he = rng.uniform(0.2, 0.8, size=(c, 3)).astype(np.float32)
+        r = rng.uniform(0.2, 0.6, size=c).astype(np.float32)
+        for k in range(c):
+            if is_box[k]:
+                set_box(b, o + k, he[k])
+            else:
+                set_sphere(b, o + k, r[k])
+        side = 8
+        layer = np.arange(c) // (side * side)
+        cell = np.arange(c) % (side * side)
+        pos = np.stack([(cell % side - (side - 1) / 2) * 2.0, 1.5 + layer * 2.0, (cell // side - (side - 1) / 2) * 2.0], 1)
+        pos += rng.uniform(-0.1, 0.1, size=(c, 3))
+        b["position"][sl] = pos.astype(np.float32)
+        b["quaternion"][sl] = random_quaternions(rng, c)
+        b["friction"][sl] = 0.5
+        o += c
+    return Scene("batched_worlds", b, dt=1.0 / 120.0, steps=1000, velocity_iterations=8, position_iterations=2,
+                 num_worlds=num_worlds, seed=seed)
+
+
+def random_pairs_scene(n: int = 200, seed: int = 7, extent: float = 6.0, box_fraction: float = 0.6) -> Scene:
+    """Boxes and spheres at random poses inside a small region above a floor:
+    a contact-rich state for stage-level parity (broadphase pairs, contacts)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = blank_bodies(n + 1)
+    static_floor(b, 0, half=(20.0, 0.5, 20.0), friction=0.5)
+    idx = np.arange(1, n + 1)
+    is_box = rng.random(n) < box_fraction
+    for k, i in enumerate(idx):
+        if is_box[k]:
+            set_box(b, i, rng.uniform(0.2, 0.7, size=3))
+        else:
+            set_sphere(b, i, rng.uniform(0.2, 0.6))
+    pos = rng.uniform((-extent, 0.1, -extent), (extent, 2.5, extent), size=(n, 3))
+    b["position"][idx] = pos.astype(np.float32)
+    b["quaternion"][idx] = random_quaternions(rng, n)
+    b["linear_velocity"][idx] = rng.normal(scale=1.0, size=(n, 3)).astype(np.float32)
+    b["angular_velocity"][idx] = rng.normal(scale=1.0, size=(n, 3)).astype(np.float32)
+    b["friction"][idx] = rng.uniform(0.1, 1.0, size=n).astype(np.float32)
+    return Scene("random_pairs", b, dt=1.0 / 60.0, steps=1, seed=seed)
+
+
+def resting_boxes(n: int = 64, seed: int = 3, spacing: float = 3.0) -> Scene:
+    """Separated boxes resting (slightly penetrating) on a floor: every island
+    holds one contact, so the solve order cannot differ from the reference."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = blank_bodies(n + 1)
+    static_floor(b, 0, half=(60.0, 0.5, 60.0), friction=0.5)
+    idx = np.arange(1, n + 1)
+    side = int(math.ceil(math.sqrt(n)))
+    he = rng.uniform(0.3, 0.6, size=(n, 3)).astype(np.float32)
+    for k, i in enumerate(idx):
+        set_box(b, i, he[k])
+    gx = (np.arange(n) % side - side / 2) * spacing
+    gz = (np.arange(n) // side - side / 2) * spacing
+    y = he[:, 1] - rng.uniform(0.0, 0.01, size=n)
+    b["position"][idx] = np.stack([gx, y, gz], 1).astype(np.float32)
+    b["linear_velocity"][idx] = rng.normal(scale=0.3, size=(n, 3)).astype(np.float32)
+    b["angular_velocity"][idx] = rng.normal(scale=0.3, size=(n, 3)).astype(np.float32)
+    b["friction"][idx] = 0.5
+    return Scene("resting_boxes", b, dt=1.0 / 60.0, steps=1, seed=seed)
+
+
+def free_fall(n: int = 256, seed: int = 11) -> Scene:
+    """Bodies far apart in free fall with spin: no contacts, pure integration."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = blank_bodies(n)
+    for i in range(n):
+        if i % 2:
+            set_box(b, i, rng.uniform(0.2, 0.8, size=3))
+        else:
+            set_sphere(b, i, rng.uniform(0.2, 0.6))
+    side = int(math.ceil(n ** (1 / 3)))
+    g = np.stack(np.meshgrid(np.arange(side), np.arange(side), np.arange(side), indexing="ij"), -1).reshape(-1, 3)[:n]
+    b["position"] = (g * 10.0 + np.array([0.0, 100.0, 0.0])).astype(np.float32)
+    b["quaternion"] = random_quaternions(rng, n)
+    b["linear_velocity"] = rng.normal(scale=2.0, size=(n, 3)).astype(np.float32)
+    b["angular_velocity"] = rng.normal(scale=2.0, size=(n, 3)).astype(np.float32)
+    b["allow_sleeping"] = 0
+    return Scene("free_fall", b, dt=1.0 / 60.0, steps=30, seed=seed)

@@ -1,0 +1,386 @@
+"""Host-side mirror of crashcat's world / body / update API over the C ABI.
+
+The reference's user-facing calls (src/index.ts) map as follows:
+
+    createWorldSettings()            -> create_world_settings()           world-settings.ts:224
+    addBroadphaseLayer / addObjectLayer / enableCollision                 world-settings.ts:267-284
+    createWorld(settings)            -> create_world(settings)            world.ts:46
+    rigidBody.create(world, {...})   -> create_body(world, RigidBodySettings(...))   rigid-body.ts:390
+    updateWorld(world, listener, dt) -> update_world(world, None, dt)     update.ts:45
+
+The device world is created lazily on the first ``update_world`` with every
+body added so far; later bodies are appended to it.  Body state lives on the
+device; ``RigidBody`` views read it back on demand.  Listener callbacks
+cannot run inside kernels: ``update_world`` accepts ``listener=None`` only and
+raises otherwise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import math
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import BODY_DTYPE, STATE_FLOATS, check, ptr
+from . import scenes as _sc
+
+
+# ---------------------------------------------------------------------------
+# settings and layers (src/world-settings.ts, src/layers.ts)
+# ---------------------------------------------------------------------------
+@dataclasses.dataclass
+class Layers:
+    broadphase_layers: int = 0
+    object_to_broadphase: list = dataclasses.field(default_factory=list)
+    object_pairs: list = dataclasses.field(default_factory=list)        # per object layer: bitmask of object layers
+    object_vs_broadphase: list = dataclasses.field(default_factory=list)  # per object layer: bitmask of bp layers
+    broadphase_pairs: list = dataclasses.field(default_factory=list)     # per bp layer: bitmask of bp layers
+
+
+@dataclasses.dataclass
+class WorldSettings:
+    gravity: tuple = (0.0, -9.81, 0.0)
+    gravity_enabled: bool = True
+    speculative_contact_distance: float = 0.02
+    manifold_tolerance: float = 1e-3
+    collision_tolerance: float = 1e-4
+    penetration_tolerance: float = 1e-4
+    normal_cos_max_delta_rotation: float = math.cos(5 * math.pi / 180)
+    contact_point_preserve_lambda_max_dist_sq: float = 0.01 * 0.01
+    velocity_iterations: int = 10
+    position_iterations: int = 2
+    warm_starting: bool = True
+    penetration_slop: float = 0.02
+    baumgarte_factor: float = 0.2
+    max_penetration_distance: float = 0.2
+    min_velocity_for_restitution: float = 1.0
+    allow_sleeping: bool = True
+    time_before_sleep: float = 0.5
+    point_velocity_sleep_threshold: float = 0.03
+    layers: Layers = dataclasses.field(default_factory=Layers)
+    num_worlds: int = 1
+    max_bodies: int = 0
+
+    def to_c(self, max_bodies: int) -> _lib.Settings:
+        s = _lib.Settings()
+        for k in range(3):
+            s.gravity[k] = self.gravity[k]
+        s.gravity_enabled = int(self.gravity_enabled)
+        for f in ("speculative_contact_distance", "manifold_tolerance", "collision_tolerance",
+                  "penetration_tolerance", "normal_cos_max_delta_rotation",
+                  "contact_point_preserve_lambda_max_dist_sq", "penetration_slop", "baumgarte_factor",
+                  "max_penetration_distance", "min_velocity_for_restitution", "time_before_sleep",
+                  "point_velocity_sleep_threshold"):
+            setattr(s, f, float(getattr(self, f)))
+        s.velocity_iterations = self.velocity_iterations
+        s.position_iterations = self.position_iterations
+        s.warm_starting = int(self.warm_starting)
+        s.allow_sleeping = int(self.allow_sleeping)
+        L = self.layers
+        if not L.object_to_broadphase:
+            raise ValueError("world settings need at least one object layer (add_object_layer)")
+        s.num_object_layers = len(L.object_to_broadphase)
+        s.num_broadphase_layers = L.broadphase_layers
+        for i, bp in enumerate(L.object_to_broadphase):
+            s.object_to_broadphase[i] = bp
+            s.object_pairs[i] = L.object_pairs[i]
+            s.object_vs_broadphase[i] = L.object_vs_broadphase[i]
+        for i in range(L.broadphase_layers):
+            s.broadphase_pairs[i] = L.broadphase_pairs[i]
+        s.max_bodies = max(1, max_bodies)
+        s.num_worlds = self.num_worlds
+        return s
+
+
+def create_world_settings() -> WorldSettings:
+    """createWorldSettings (world-settings.ts:224-264)."""
+    return WorldSettings()
+
+
+def add_broadphase_layer(settings: WorldSettings) -> int:
+    """layers.addBroadphaseLayer (layers.ts:26-45)."""
+    L = settings.layers
+    if L.broadphase_layers >= _lib.MAX_LAYERS:
+        raise ValueError("at most 32 broadphase layers")
+    L.broadphase_layers += 1
+    L.broadphase_pairs.append(0)
+    return L.broadphase_layers - 1
+
+
+def add_object_layer(settings: WorldSettings, broadphase_layer: int) -> int:
+    """layers.addObjectLayer (layers.ts:47-71): the layer may query its own broadphase layer."""
+    L = settings.layers
+    if len(L.object_to_broadphase) >= _lib.MAX_LAYERS:
+        raise ValueError("at most 32 object layers")
+    L.object_to_broadphase.append(broadphase_layer)
+    L.object_pairs.append(0)
+    L.object_vs_broadphase.append(1 << broadphase_layer)
+    return len(L.object_to_broadphase) - 1
+
+
+def enable_collision(settings: WorldSettings, a: int, b: int) -> None:
+    """layers.enableCollision (layers.ts:73-100)."""
+    L = settings.layers
+    L.object_pairs[a] |= 1 << b
+    L.object_pairs[b] |= 1 << a
+    bpa, bpb = L.object_to_broadphase[a], L.object_to_broadphase[b]
+    L.broadphase_pairs[bpa] |= 1 << bpb
+    L.broadphase_pairs[bpb] |= 1 << bpa
+    L.object_vs_broadphase[a] |= 1 << bpb
+    L.object_vs_broadphase[b] |= 1 << bpa
+
+
+def disable_collision(settings: WorldSettings, a: int, b: int) -> None:
+    """layers.disableCollision (layers.ts:102-110): only the object pair table changes."""
+    L = settings.layers
+    L.object_pairs[a] &= ~(1 << b)
+    L.object_pairs[b] &= ~(1 << a)
+
+
+def standard_settings(**overrides) -> WorldSettings:
+    """The two-layer setup of the reference's tests (tst/helpers.ts:5-26)."""
+    s = create_world_settings()
+    bp_moving = add_broadphase_layer(s)
+    bp_static = add_broadphase_layer(s)
+    moving = add_object_layer(s, bp_moving)
+    static = add_object_layer(s, bp_static)
+    enable_collision(s, moving, moving)
+    enable_collision(s, moving, static)
+    for k, v in overrides.items():
+        setattr(s, k, v)
+    return s
+
+
+# ---------------------------------------------------------------------------
+# shapes and bodies
+# ---------------------------------------------------------------------------
+@dataclasses.dataclass
+class Box:
+    half_extents: tuple
+    convex_radius: float = _sc.DEFAULT_CONVEX_RADIUS
+    density: float = _sc.DEFAULT_DENSITY
+
+
+@dataclasses.dataclass
+class Sphere:
+    radius: float
+    density: float = _sc.DEFAULT_DENSITY
+
+
+@dataclasses.dataclass
+class RigidBodySettings:
+    """RigidBodySettings (rigid-body.ts:37-118) for the supported shapes."""
+    shape: object
+    object_layer: int
+    motion_type: int = _lib.DYNAMIC
+    position: tuple = (0.0, 0.0, 0.0)
+    quaternion: tuple = (0.0, 0.0, 0.0, 1.0)
+    linear_velocity: tuple = (0.0, 0.0, 0.0)
+    angular_velocity: tuple = (0.0, 0.0, 0.0)
+    friction: float = _sc.DEFAULT_FRICTION
+    restitution: float = _sc.DEFAULT_RESTITUTION
+    gravity_factor: float = 1.0
+    linear_damping: float = _sc.DEFAULT_DAMPING
+    angular_damping: float = _sc.DEFAULT_DAMPING
+    max_linear_velocity: float = _sc.DEFAULT_MAX_LINEAR_VELOCITY
+    max_angular_velocity: float = _sc.DEFAULT_MAX_ANGULAR_VELOCITY
+    allow_sleeping: bool = True
+    friction_combine: int = _lib.COMBINE_GEOMETRIC_MEAN
+    restitution_combine: int = _lib.COMBINE_MAX
+    collision_groups: int = 0xFFFFFFFF
+    collision_mask: int = 0xFFFFFFFF
+    allowed_degrees_of_freedom: int = 0b111111
+    world: int = 0
+
+
+def body_desc(s: RigidBodySettings) -> np.ndarray:
+    d = np.zeros(1, dtype=BODY_DTYPE)
+    if isinstance(s.shape, Box):
+        d["shape_type"] = _lib.SHAPE_BOX
+        d["shape_params"][0, :3] = s.shape.half_extents
+        d["shape_params"][0, 3] = s.shape.convex_radius
+        d["density"] = s.shape.density
+    elif isinstance(s.shape, Sphere):
+        d["shape_type"] = _lib.SHAPE_SPHERE
+        d["shape_params"][0, 0] = s.shape.radius
+        d["density"] = s.shape.density
+    else:
+        raise TypeError(f"unsupported shape {type(s.shape).__name__}: box and sphere are supported")
+    d["motion_type"] = s.motion_type
+    d["object_layer"] = s.object_layer
+    d["world"] = s.world
+    d["allow_sleeping"] = int(s.allow_sleeping)
+    d["position"] = s.position
+    d["quaternion"] = s.quaternion
+    d["linear_velocity"] = s.linear_velocity
+    d["angular_velocity"] = s.angular_velocity
+    for f in ("friction", "restitution", "gravity_factor", "linear_damping", "angular_damping",
+              "max_linear_velocity", "max_angular_velocity", "friction_combine", "restitution_combine",
+              "collision_groups", "collision_mask"):
+        d[f] = getattr(s, f)
+    d["allowed_dofs"] = s.allowed_degrees_of_freedom
+    return d
+
+
+class GpuWorld:
+    """Owns one cc_world handle (one or many independent worlds)."""
+
+    def __init__(self, settings: WorldSettings, max_bodies: int):
+        lib = _lib.load()
+        self._lib = lib
+        self.settings = settings
+        cs = settings.to_c(max_bodies)
+        h = C.c_void_p()
+        check(lib.cc_world_create(C.byref(cs), C.byref(h)), "cc_world_create")
+        self.handle = h
+        self.n = 0
+
+    def close(self) -> None:
+        if self.handle:
+            self._lib.cc_world_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_bodies(self, bodies: np.ndarray) -> np.ndarray:
+        bodies = np.ascontiguousarray(bodies, dtype=BODY_DTYPE)
+        out = np.zeros(len(bodies), dtype=np.int32)
+        check(self._lib.cc_world_add_bodies(self.handle, ptr(bodies), len(bodies), ptr(out)), "cc_world_add_bodies")
+        self.n += len(bodies)
+        return out
+
+    def step(self, dt: float, n_steps: int = 1) -> int:
+        st = self._lib.cc_world_step(self.handle, C.c_float(dt), n_steps)
+        if st not in (_lib.CC_OK, _lib.CC_ERR_CAPACITY):
+            check(st, "cc_world_step")
+        return st
+
+    def step_host(self, dt: float, state_in: np.ndarray, state_out: np.ndarray) -> int:
+        st = self._lib.cc_world_step_host(self.handle, C.c_float(dt), ptr(state_in), ptr(state_out))
+        if st not in (_lib.CC_OK, _lib.CC_ERR_CAPACITY):
+            check(st, "cc_world_step_host")
+        return st
+
+    def get_state(self):
+        rows = np.zeros((self.n, STATE_FLOATS), dtype=np.float32)
+        sl = np.zeros(self.n, dtype=np.uint8)
+        check(self._lib.cc_world_get_state(self.handle, ptr(rows), ptr(sl)), "cc_world_get_state")
+        return rows, sl
+
+    def set_state(self, rows: np.ndarray) -> None:
+        rows = np.ascontiguousarray(rows, dtype=np.float32)
+        assert rows.shape == (self.n, STATE_FLOATS)
+        check(self._lib.cc_world_set_state(self.handle, ptr(rows)), "cc_world_set_state")
+
+    def get_pairs(self) -> np.ndarray:
+        cnt = C.c_int32()
+        check(self._lib.cc_world_get_pairs(self.handle, None, 0, C.byref(cnt)), "cc_world_get_pairs")
+        out = np.zeros((max(cnt.value, 1), 2), dtype=np.int32)
+        check(self._lib.cc_world_get_pairs(self.handle, ptr(out), cnt.value, C.byref(cnt)), "cc_world_get_pairs")
+        return out[: cnt.value]
+
+    def get_manifolds(self) -> np.ndarray:
+        cnt = C.c_int32()
+        check(self._lib.cc_world_get_manifolds(self.handle, None, 0, C.byref(cnt)), "cc_world_get_manifolds")
+        out = np.zeros((max(cnt.value, 1), 32), dtype=np.float32)
+        check(self._lib.cc_world_get_manifolds(self.handle, ptr(out), cnt.value, C.byref(cnt)),
+              "cc_world_get_manifolds")
+        return out[: cnt.value]
+
+    def stats(self) -> dict:
+        s = _lib.Stats()
+        check(self._lib.cc_world_get_stats(self.handle, C.byref(s)), "cc_world_get_stats")
+        return {f: getattr(s, f) for f, _ in _lib.Stats._fields_}
+
+
+# ---------------------------------------------------------------------------
+# reference-shaped facade
+# ---------------------------------------------------------------------------
+class RigidBody:
+    """View of one body; pose and velocities are read from the device world."""
+
+    def __init__(self, world: "World", index: int):
+        self._world = world
+        self.index = index
+        self.id = index  # bodies are never recycled: id order equals index order
+
+    def _row(self):
+        return self._world._state()[0][self.index]
+
+    @property
+    def position(self):
+        return self._row()[0:3].copy()
+
+    @property
+    def quaternion(self):
+        return self._row()[3:7].copy()
+
+    @property
+    def linear_velocity(self):
+        return self._row()[7:10].copy()
+
+    @property
+    def angular_velocity(self):
+        return self._row()[10:13].copy()
+
+    @property
+    def sleeping(self) -> bool:
+        return bool(self._world._state()[1][self.index])
+
+
+class World:
+    """createWorld (world.ts:46-58)."""
+
+    def __init__(self, settings: WorldSettings, max_bodies: int = 0):
+        self.settings = settings
+        self._pending: list = []
+        self._gpu: Optional[GpuWorld] = None
+        self._max_bodies = max_bodies
+        self._cache = None
+        self.bodies: list = []
+
+    def _flush(self) -> None:
+        if self._gpu is None:
+            cap = self._max_bodies or max(1024, 2 * len(self._pending))
+            self._gpu = GpuWorld(self.settings, cap)
+        if self._pending:
+            self._gpu.add_bodies(np.concatenate(self._pending))
+            self._pending = []
+        self._cache = None
+
+    def _state(self):
+        self._flush()
+        if self._cache is None:
+            self._cache = self._gpu.get_state()
+        return self._cache
+
+
+def create_world(settings: WorldSettings, max_bodies: int = 0) -> World:
+    return World(settings, max_bodies)
+
+
+def create_body(world: World, settings: RigidBodySettings) -> RigidBody:
+    """rigidBody.create (rigid-body.ts:390-434)."""
+    world._pending.append(body_desc(settings))
+    b = RigidBody(world, len(world.bodies))
+    world.bodies.append(b)
+    world._cache = None
+    return b
+
+
+def update_world(world: World, listener, time_step: float) -> None:
+    """updateWorld (update.ts:45): one step of every body in the world on the GPU."""
+    if listener is not None:
+        raise NotImplementedError("listener callbacks cannot run inside kernels; pass None")
+    world._flush()
+    st = world._gpu.step(time_step, 1)
+    world._cache = None
+    if st != _lib.CC_OK:
+        check(st, "updateWorld")

@@ -1,0 +1,175 @@
+/*
+ * crashcat_gpu.h - C ABI of the GB300 (sm_103a) implementation of crashcat's
+ * per-step world update.
+ *
+ * Every entry point returns an int status (CC_OK = 0).  No C++ exception and
+ * no torch type crosses this boundary; all arrays are plain host pointers
+ * owned by the caller, except where a function says "device pointer".
+ *
+ * Reference interface replaced by each entry point (paths inside
+ * isaac-mason/crashcat):
+ *   cc_world_settings_default  <- createWorldSettings        src/world-settings.ts:224-264
+ *   cc_world_create            <- createWorld                src/world.ts:46-58
+ *   cc_world_destroy           <- (world dropped by the GC)  src/world.ts:12-39
+ *   cc_world_add_bodies        <- rigidBody.create           src/body/rigid-body.ts:390-434
+ *   cc_world_step              <- updateWorld                src/update.ts:45-239
+ *   cc_world_step_host         <- updateWorld, with the body state read from
+ *                                 and written back to host arrays (the form a
+ *                                 Node-API addon binds)      src/update.ts:45
+ *   cc_world_get_state         <- reading body.position / quaternion /
+ *                                 motionProperties.linearVelocity / angularVelocity /
+ *                                 sleeping                   src/body/rigid-body.ts:142-252
+ *   cc_world_set_state         <- rigidBody.setTransform / setLinearVelocity /
+ *                                 setAngularVelocity         src/body/rigid-body.ts:758-774,
+ *                                                            src/body/motion-properties.ts:647-672
+ *   cc_world_get_pairs         <- world.broadphase.pairs     src/broadphase/broadphase.ts:30-35
+ *   cc_world_get_manifolds     <- contact manifolds handed to
+ *                                 addContactConstraint        src/constraints/contact-constraints.ts:437
+ *   cc_world_get_stats         <- (no counterpart: per-step counters)
+ *   cc_status_string           <- assert() messages          src/utils/assert.ts:1-9
+ */
+#ifndef CRASHCAT_GPU_H
+#define CRASHCAT_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum cc_status {
+    CC_OK = 0,
+    CC_ERR_INVALID = 1,   /* bad argument */
+    CC_ERR_CAPACITY = 2,  /* a per-step buffer overflowed; results of that step are incomplete */
+    CC_ERR_TIMEOUT = 3,   /* a bounded device-side wait gave up */
+    CC_ERR_NAN = 4,       /* non-finite body state detected */
+    CC_ERR_CUDA = 5,      /* a CUDA runtime call failed */
+    CC_ERR_UNSUPPORTED = 6
+};
+
+enum cc_shape_type { CC_SHAPE_SPHERE = 0, CC_SHAPE_BOX = 1 };
+enum cc_motion_type { CC_STATIC = 0, CC_KINEMATIC = 1, CC_DYNAMIC = 2 };
+enum cc_combine_mode { CC_COMBINE_AVERAGE = 0, CC_COMBINE_MULTIPLY = 1, CC_COMBINE_MIN = 2, CC_COMBINE_MAX = 3,
+                       CC_COMBINE_GEOMETRIC_MEAN = 4 };
+
+#define CC_MAX_LAYERS 32
+
+/* WorldSettings (src/world-settings.ts:4-222).  Layer tables follow
+ * src/layers.ts: bit j of object_pairs[i] = objectLayerPairs[i][j], bit b of
+ * object_vs_broadphase[i] = objectVsBroadphase[i][b], bit b of
+ * broadphase_pairs[a] = broadphasePairs[a][b]. */
+typedef struct cc_world_settings {
+    double gravity[3];
+    int32_t gravity_enabled;
+    double speculative_contact_distance;
+    double manifold_tolerance;
+    double collision_tolerance;
+    double penetration_tolerance;
+    double normal_cos_max_delta_rotation;
+    double contact_point_preserve_lambda_max_dist_sq;
+    int32_t velocity_iterations;
+    int32_t position_iterations;
+    int32_t warm_starting;
+    double penetration_slop;
+    double baumgarte_factor;
+    double max_penetration_distance;
+    double min_velocity_for_restitution;
+    int32_t allow_sleeping;
+    double time_before_sleep;
+    double point_velocity_sleep_threshold;
+    int32_t num_object_layers;
+    int32_t num_broadphase_layers;
+    int32_t object_to_broadphase[CC_MAX_LAYERS];
+    uint32_t object_pairs[CC_MAX_LAYERS];
+    uint32_t object_vs_broadphase[CC_MAX_LAYERS];
+    uint32_t broadphase_pairs[CC_MAX_LAYERS];
+    /* capacities of the device world (0 = derive from max_bodies) */
+    int32_t max_bodies;
+    int32_t max_pairs;
+    int32_t max_manifolds;
+    /* number of independent worlds held by this handle (batched form); bodies
+     * name their world in cc_body_desc.world */
+    int32_t num_worlds;
+} cc_world_settings;
+
+/* RigidBodySettings (src/body/rigid-body.ts:37-139) for the supported shapes.
+ * shape_params: box = half extents xyz + convex radius; sphere = radius. */
+typedef struct cc_body_desc {
+    int32_t shape_type;
+    float shape_params[4];
+    float density;
+    int32_t motion_type;
+    int32_t object_layer;
+    int32_t world;
+    int32_t allow_sleeping;
+    float position[3];
+    float quaternion[4];
+    float linear_velocity[3];
+    float angular_velocity[3];
+    float friction;
+    float restitution;
+    float gravity_factor;
+    float linear_damping;
+    float angular_damping;
+    float max_linear_velocity;
+    float max_angular_velocity;
+    int32_t friction_combine;
+    int32_t restitution_combine;
+    uint32_t collision_groups;
+    uint32_t collision_mask;
+    int32_t allowed_dofs;
+} cc_body_desc;
+
+/* Per-step counters of the last completed step. */
+typedef struct cc_stats {
+    int32_t num_bodies;
+    int32_t num_awake;
+    int32_t num_pairs;
+    int32_t num_manifolds;
+    int32_t num_contact_points;
+    int32_t num_epa;
+    int32_t num_islands;
+    int32_t max_island_constraints;
+    int32_t overflow_flags;
+    int32_t gpu_launches_per_step;
+} cc_stats;
+
+typedef struct cc_world cc_world;
+
+int cc_world_settings_default(cc_world_settings *out);
+int cc_world_create(const cc_world_settings *settings, cc_world **out);
+int cc_world_destroy(cc_world *world);
+int cc_world_add_bodies(cc_world *world, const cc_body_desc *bodies, int32_t n, int32_t *out_index);
+int cc_world_num_bodies(const cc_world *world, int32_t *out);
+
+/* Advance every world held by the handle by n_steps steps of dt seconds; the
+ * body state stays resident in device memory.  Blocks until the steps end. */
+int cc_world_step(cc_world *world, float dt, int32_t n_steps);
+
+/* One step with the body state exchanged through host arrays: the
+ * per-body state rows (cc_world_set_state layout) are uploaded, the world is
+ * stepped once, and the new state is written to state_out. */
+int cc_world_step_host(cc_world *world, float dt, const float *state_in, float *state_out);
+
+/* State rows of 16 floats per body: position[3] quaternion[4]
+ * linear_velocity[3] angular_velocity[3] center_of_mass[3]; plus one byte
+ * per body for the sleeping flag (may be NULL). */
+int cc_world_get_state(cc_world *world, float *rows, uint8_t *sleeping);
+int cc_world_set_state(cc_world *world, const float *rows);
+
+/* Broadphase pairs of the last step as (query body index, other body index). */
+int cc_world_get_pairs(cc_world *world, int32_t *out, int32_t capacity, int32_t *count);
+
+/* Contact manifolds of the last step, 32 floats each: bodyA, bodyB (ordered by
+ * id), point count, normal[3] (A to B), penetration depth, 0, then 4 x
+ * (world point on A[3], world point on B[3]). */
+int cc_world_get_manifolds(cc_world *world, float *out, int32_t capacity, int32_t *count);
+
+int cc_world_get_stats(cc_world *world, cc_stats *out);
+
+const char *cc_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CRASHCAT_GPU_H */

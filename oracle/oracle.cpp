@@ -1,0 +1,1557 @@
+// FP64 CPU restatement of crashcat's per-step world update (`updateWorld`,
+// src/update.ts:45-239) used as the parity oracle and the timed CPU baseline.
+//
+// TEST INFRASTRUCTURE ONLY.  Nothing in the GPU library links, loads or calls
+// this code; only tests/, __graft_entry__.smoke() and bench.py's CPU baseline
+// use it.  The restatement covers the bodies, shapes and settings the GPU path
+// supports (box and sphere bodies, static / kinematic / dynamic motion,
+// discrete motion quality, no user joints, no listener).
+//
+// Parity notes:
+//  * JS numbers are IEEE doubles, so FP64 C++ with -ffp-contract=off
+//    reproduces the reference's arithmetic except for sin/cos and the
+//    mathcat choices documented in oracle_math.h.
+//  * The reference finds pairs with a DBVT; the pair SET it reports depends
+//    only on the tight-AABB predicate at the leaves (dbvt.ts:669), so the
+//    oracle uses a median-split BVH over the same predicate.  Pair ORDER has no
+//    effect on the step's results because the solver sorts each island's
+//    contacts by (sortKey, idA, idB) (contact-constraints.ts:1240-1264).
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <tuple>
+#include <vector>
+
+#include "oracle_collide.h"
+
+namespace orc {
+
+enum MotionType : int { STATIC = 0, KINEMATIC = 1, DYNAMIC = 2 };
+enum Combine : int { C_AVERAGE = 0, C_MULTIPLY = 1, C_MIN = 2, C_MAX = 3, C_GEOMETRIC_MEAN = 4 };
+constexpr int64_t INACTIVE = 9007199254740991LL;  // Number.MAX_SAFE_INTEGER, sleep.ts:8
+
+// WorldSettings defaults, world-settings.ts:224-264
+struct Settings {
+    V3 gravity{0, -9.81, 0};
+    bool gravityEnabled = true;
+    double preserveLambdaMaxDistSq = 0.01 * 0.01;
+    double collisionTolerance = 1e-4, penetrationTolerance = 1e-4;
+    double speculativeContactDistance = 0.02, manifoldTolerance = 1e-3;
+    bool useManifoldReduction = true;
+    double normalCosMaxDeltaRotation = std::cos((5 * M_PI) / 180);
+    double minVelocityForRestitution = 1;
+    int velocityIterations = 10, positionIterations = 2;
+    bool warmStarting = true;
+    double penetrationSlop = 0.02, baumgarteFactor = 0.2, maxPenetrationDistance = 0.2;
+    bool allowSleeping = true;
+    double timeBeforeSleep = 0.5, pointVelocitySleepThreshold = 0.03;
+};
+
+struct SleepSphere {
+    V3 c;
+    double r = 0;
+};
+
+// RigidBody + MotionProperties (rigid-body.ts:142-252, motion-properties.ts:25-69)
+struct Body {
+    int index = 0;
+    int64_t id = 0;
+    Shape shape;
+    V3 position, com;
+    Q4 quat;
+    int motion = DYNAMIC;
+    V3 linvel, angvel, force, torque;
+    V3 invInertiaDiag;
+    Q4 inertiaRot;
+    double invMass = 0, linDamp = 0.05, angDamp = 0.05, maxLin = 500, maxAng = 0.25 * M_PI * 60, gravityFactor = 1;
+    int dof = 0b111111;
+    int velOverride = 0, posOverride = 0;
+    SleepSphere spheres[3];
+    bool allowSleeping = true;
+    double sleepTimer = 0;
+    double friction = 0.2, restitution = 0;
+    int frictionCombine = C_GEOMETRIC_MEAN, restitutionCombine = C_MAX;
+    uint32_t groups = 0xffffffffu, mask = 0xffffffffu;
+    bool sensor = false, collideKinematicVsNonDynamic = false, useManifoldReduction = true;
+    bool sleeping = false;
+    Box3 aabb;
+    int objectLayer = 0;
+    int64_t activeIndex = INACTIVE;
+    int islandIndex = -1;
+};
+
+struct CachedPoint {
+    V3 p1, p2;
+    double ln = 0, lt1 = 0, lt2 = 0;
+};
+// Contact (contacts.ts:9-81): persistent record keyed by ids + sub-shape ids
+struct Contact {
+    int64_t idA, idB;
+    uint32_t subA, subB;
+    bool processed = false;
+    V3 normalB;
+    int n = 0;
+    CachedPoint pts[4];
+};
+using ContactKey = std::tuple<int64_t, int64_t, uint32_t, uint32_t>;
+
+// AxisConstraintPart (axis-constraint-part.ts:23-60)
+struct AxisPart {
+    V3 r1xa, r2xa, invI1, invI2;
+    double effMass = 0, totalLambda = 0, softness = 0, bias = 0;
+};
+struct WorldContactPoint {
+    V3 posA, posB, localA, localB;
+    AxisPart n, t1, t2;
+};
+struct ContactConstraint {
+    int bodyA, bodyB;
+    uint32_t subA, subB;
+    V3 normal, t1, t2;
+    double friction, restitution;
+    int n = 0;
+    WorldContactPoint pts[4];
+    double invMassA, invMassB;
+    M4 invIA, invIB;
+    double invIScaleA = 1, invIScaleB = 1;
+    ContactKey contactKey;
+    uint32_t sortKey;
+};
+
+struct Island {
+    std::vector<int64_t> bodyIndices;  // active indices
+    std::vector<int> contactIndices;
+    int velSteps = 0, posSteps = 0;
+};
+
+struct Layers {
+    int nObj = 0, nBp = 0;
+    std::vector<int> objToBp;
+    std::vector<uint8_t> objPairs, objVsBp, bpPairs;
+};
+
+struct World {
+    Settings s;
+    Layers layers;
+    std::vector<Body> bodies;
+    std::vector<int> activeBodyIndices;
+    int64_t activeCount = 0;
+    int nextSequence = 0;
+    std::map<ContactKey, Contact> contacts;
+    std::vector<ContactConstraint> constraints;
+    std::vector<Island> islands;
+    double prevDt = 0;
+    // per-step diagnostics
+    std::vector<std::pair<int, int>> pairs;
+    std::vector<Manifold> manifolds;  // manifolds that produced constraints, after id ordering
+    std::vector<std::pair<int, int>> manifoldBodies;
+    double bodySteps = 0;
+};
+
+// ---------------------------------------------------------------------------
+// Mass and motion properties
+// ---------------------------------------------------------------------------
+// setMassAndInertiaOfSolidBox mass-properties.ts:36-52 / sphere.ts:97-123
+static void shape_mass(const Shape &s, double &mass, V3 &inertiaDiag) {
+    if (s.type == SHAPE_BOX) {
+        V3 full = scale(s.half_extents, 2);
+        mass = full.x * full.y * full.z * s.density;
+        V3 sq{full.x * full.x, full.y * full.y, full.z * full.z};
+        inertiaDiag = {(sq.y + sq.z) * (mass / 12.0), (sq.x + sq.z) * (mass / 12.0), (sq.x + sq.y) * (mass / 12.0)};
+    } else if (s.type == SHAPE_SPHERE) {
+        double r2 = s.radius * s.radius;
+        mass = (4.0 / 3.0) * M_PI * s.radius * r2 * s.density;
+        double in = (2.0 / 5.0) * mass * r2;
+        inertiaDiag = {in, in, in};
+    } else {
+        mass = 0;
+        inertiaDiag = {0, 0, 0};
+    }
+}
+
+// setMassProperties motion-properties.ts:419-491 for a diagonal inertia tensor
+// (the Jacobi decomposition exits immediately with an identity rotation when
+// all off-diagonal terms are zero, motion-properties.ts:232-245).
+static void set_mass_properties(Body &b, double mass, V3 d) {
+    int tr = b.dof & 0b111, rot = (b.dof >> 3) & 0b111;
+    b.invMass = tr == 0 ? 0.0 : 1.0 / mass;
+    if (rot == 0) {
+        b.invInertiaDiag = {0, 0, 0};
+        b.inertiaRot = {0, 0, 0, 1};
+    } else {
+        double l = d.x * d.x + d.y * d.y + d.z * d.z;
+        const double EPS = 1e-10;  // EPSILON, motion-properties.ts:178
+        if (l > EPS * EPS) {
+            b.invInertiaDiag = {d.x != 0 ? 1.0 / d.x : 0, d.y != 0 ? 1.0 / d.y : 0, d.z != 0 ? 1.0 / d.z : 0};
+            b.inertiaRot = {0, 0, 0, 1};
+        } else {
+            double si = 2.5 * b.invMass;
+            b.invInertiaDiag = {si, si, si};
+            b.inertiaRot = {0, 0, 0, 1};
+        }
+    }
+}
+
+// getInverseInertiaForRotation motion-properties.ts:494-621
+static M4 inv_inertia_for_rotation(const Body &b, const M4 &R) {
+    Q4 q = b.inertiaRot;
+    double qx2 = q.x + q.x, qy2 = q.y + q.y, qz2 = q.z + q.z;
+    double qxx = q.x * qx2, qyx = q.y * qx2, qyy = q.y * qy2, qzx = q.z * qx2, qzy = q.z * qy2, qzz = q.z * qz2,
+           qwx = q.w * qx2, qwy = q.w * qy2, qwz = q.w * qz2;
+    double i00 = 1 - qyy - qzz, i01 = qyx + qwz, i02 = qzx - qwy;
+    double i10 = qyx - qwz, i11 = 1 - qxx - qzz, i12 = qzy + qwx;
+    double i20 = qzx + qwy, i21 = qzy - qwx, i22 = 1 - qxx - qyy;
+    const double *m = R.m;
+    double b00 = m[0], b01 = m[1], b02 = m[2], b10 = m[4], b11 = m[5], b12 = m[6], b20 = m[8], b21 = m[9],
+           b22 = m[10];
+    double r00 = b00 * i00 + b10 * i01 + b20 * i02, r01 = b01 * i00 + b11 * i01 + b21 * i02,
+           r02 = b02 * i00 + b12 * i01 + b22 * i02;
+    double r10 = b00 * i10 + b10 * i11 + b20 * i12, r11 = b01 * i10 + b11 * i11 + b21 * i12,
+           r12 = b02 * i10 + b12 * i11 + b22 * i12;
+    double r20 = b00 * i20 + b10 * i21 + b20 * i22, r21 = b01 * i20 + b11 * i21 + b21 * i22,
+           r22 = b02 * i20 + b12 * i21 + b22 * i22;
+    double d0 = b.invInertiaDiag.x, d1 = b.invInertiaDiag.y, d2 = b.invInertiaDiag.z;
+    double s00 = d0 * r00, s01 = d0 * r01, s02 = d0 * r02, s10 = d1 * r10, s11 = d1 * r11, s12 = d1 * r12,
+           s20 = d2 * r20, s21 = d2 * r21, s22 = d2 * r22;
+    M4 o{};
+    o.m[0] = s00 * r00 + s10 * r10 + s20 * r20;
+    o.m[1] = s00 * r01 + s10 * r11 + s20 * r21;
+    o.m[2] = s00 * r02 + s10 * r12 + s20 * r22;
+    o.m[4] = s01 * r00 + s11 * r10 + s21 * r20;
+    o.m[5] = s01 * r01 + s11 * r11 + s21 * r21;
+    o.m[6] = s01 * r02 + s11 * r12 + s21 * r22;
+    o.m[8] = s02 * r00 + s12 * r10 + s22 * r20;
+    o.m[9] = s02 * r01 + s12 * r11 + s22 * r21;
+    o.m[10] = s02 * r02 + s12 * r12 + s22 * r22;
+    o.m[15] = 1;
+    int ar = (b.dof >> 3) & 0b111;
+    if (ar != 0b111) {
+        double mx = ar & 1 ? 1.0 : 0.0, my = ar & 2 ? 1.0 : 0.0, mz = ar & 4 ? 1.0 : 0.0;
+        o.m[0] *= mx * mx;
+        o.m[1] *= my * mx;
+        o.m[2] *= mz * mx;
+        o.m[4] *= mx * my;
+        o.m[5] *= my * my;
+        o.m[6] *= mz * my;
+        o.m[8] *= mx * mz;
+        o.m[9] *= my * mz;
+        o.m[10] *= mz * mz;
+    }
+    return o;
+}
+
+// ---------------------------------------------------------------------------
+// Transform / AABB / sleep helpers
+// ---------------------------------------------------------------------------
+// updateCenterOfMassPosition rigid-body.ts:527-536
+static void update_com(Body &b) { b.com = add(rotate(b.quat, b.shape.com), b.position); }
+// updatePositionFromCenterOfMass rigid-body.ts:545-553
+static void update_pos_from_com(Body &b) { b.position = sub(b.com, rotate(b.quat, b.shape.com)); }
+// updateAABB rigid-body.ts:561-674
+static void update_aabb(Body &b) {
+    const Box3 &s = b.shape.aabb;
+    M4 R = mat4_from_quat(b.quat);
+    const double *m = R.m;
+    double xs[2] = {s.mn.x, s.mx.x}, ys[2] = {s.mn.y, s.mx.y}, zs[2] = {s.mn.z, s.mx.z};
+    // corner order: (min,min,min) (max,min,min) (min,max,min) (max,max,min) ...
+    double mnx = 0, mny = 0, mnz = 0, mxx = 0, mxy = 0, mxz = 0;
+    for (int c = 0; c < 8; c++) {
+        double x = xs[c & 1], y = ys[(c >> 1) & 1], z = zs[(c >> 2) & 1];
+        double wx = m[0] * x + m[4] * y + m[8] * z + b.position.x;
+        double wy = m[1] * x + m[5] * y + m[9] * z + b.position.y;
+        double wz = m[2] * x + m[6] * y + m[10] * z + b.position.z;
+        if (c == 0) {
+            mnx = mxx = wx;
+            mny = mxy = wy;
+            mnz = mxz = wz;
+        } else {
+            mnx = std::min(mnx, wx);
+            mny = std::min(mny, wy);
+            mnz = std::min(mnz, wz);
+            mxx = std::max(mxx, wx);
+            mxy = std::max(mxy, wy);
+            mxz = std::max(mxz, wz);
+        }
+    }
+    b.aabb = {{mnx, mny, mnz}, {mxx, mxy, mxz}};
+}
+static void set_transform(Body &b) {
+    update_com(b);
+    update_aabb(b);
+}
+
+// getSleepTestPoints sleep.ts:22-74
+static void sleep_points(const Body &b, V3 out[3]) {
+    out[0] = b.com;
+    const Box3 &a = b.shape.aabb;
+    V3 e{(a.mx.x - a.mn.x) * 0.5, (a.mx.y - a.mn.y) * 0.5, (a.mx.z - a.mn.z) * 0.5};
+    int lowest;
+    if (e.x <= e.y && e.x <= e.z)
+        lowest = 0;
+    else if (e.y <= e.z)
+        lowest = 1;
+    else
+        lowest = 2;
+    V3 X{1, 0, 0}, Y{0, 1, 0}, Z{0, 0, 1};
+    if (lowest == 0) {
+        out[1] = scale_add(b.com, rotate(b.quat, Y), e.y);
+        out[2] = scale_add(b.com, rotate(b.quat, Z), e.z);
+    } else if (lowest == 1) {
+        out[1] = scale_add(b.com, rotate(b.quat, X), e.x);
+        out[2] = scale_add(b.com, rotate(b.quat, Z), e.z);
+    } else {
+        out[1] = scale_add(b.com, rotate(b.quat, X), e.x);
+        out[2] = scale_add(b.com, rotate(b.quat, Y), e.y);
+    }
+}
+static void reset_sleep_spheres(Body &b, V3 p[3]) {
+    for (int i = 0; i < 3; i++) {
+        b.spheres[i].c = p[i];
+        b.spheres[i].r = 0;
+    }
+    b.sleepTimer = 0;
+}
+// resetSleepTimer sleep.ts:123-130
+static void reset_sleep_timer(Body &b) {
+    if (b.motion != DYNAMIC) return;
+    V3 p[3];
+    sleep_points(b, p);
+    reset_sleep_spheres(b, p);
+}
+// updateSleepState sleep.ts:88-117
+static bool update_sleep_state(Body &b, double dt, double maxMove, double tbs) {
+    if (!b.allowSleeping || b.sensor) return false;
+    V3 p[3];
+    sleep_points(b, p);
+    for (int i = 0; i < 3; i++) {
+        SleepSphere &s = b.spheres[i];
+        double d = distance(s.c, p[i]);
+        s.r = std::max(s.r, d);
+        if (s.r > maxMove) {
+            reset_sleep_spheres(b, p);
+            return false;
+        }
+    }
+    b.sleepTimer += dt;
+    return b.sleepTimer >= tbs;
+}
+// addBodyToActiveBodies / removeBodyFromActiveBodies sleep.ts:132-166
+static void add_active(World &w, Body &b) {
+    if (b.activeIndex != INACTIVE) return;
+    b.activeIndex = w.activeCount;
+    if ((int64_t)w.activeBodyIndices.size() <= w.activeCount) w.activeBodyIndices.resize(w.activeCount + 1);
+    w.activeBodyIndices[w.activeCount] = b.index;
+    w.activeCount++;
+}
+static void remove_active(World &w, Body &b) {
+    if (b.activeIndex == INACTIVE) return;
+    int64_t last = w.activeCount - 1;
+    if (b.activeIndex != last) {
+        int lastBody = w.activeBodyIndices[last];
+        w.activeBodyIndices[b.activeIndex] = lastBody;
+        w.bodies[lastBody].activeIndex = b.activeIndex;
+    }
+    b.activeIndex = INACTIVE;
+    w.activeCount--;
+}
+// sleep / wake sleep.ts:169-203
+static void sleep_body(World &w, Body &b) {
+    if (b.motion == STATIC || b.sleeping) return;
+    remove_active(w, b);
+    b.sleeping = true;
+    b.linvel = {0, 0, 0};
+    b.angvel = {0, 0, 0};
+}
+static void wake_body(World &w, Body &b) {
+    if (b.motion == STATIC) return;
+    reset_sleep_timer(b);
+    if (!b.sleeping) return;
+    b.sleeping = false;
+    add_active(w, b);
+}
+
+// ---------------------------------------------------------------------------
+// Broadphase (broadphase.ts:44-277)
+// ---------------------------------------------------------------------------
+static bool should_query(const Body &b) { return b.motion != STATIC && !b.sleeping; }
+static int64_t dedup_index(const Body &b) { return should_query(b) ? (int64_t)b.index : INACTIVE; }
+
+struct BvhNode {
+    Box3 box;
+    int left = -1, right = -1, first = 0, count = 0;
+};
+static void bvh_build(const std::vector<Body> &bodies, std::vector<int> &idx, std::vector<BvhNode> &nodes, int first,
+                      int count) {
+    int ni = (int)nodes.size();
+    nodes.emplace_back();
+    Box3 bx = bodies[idx[first]].aabb;
+    for (int i = first + 1; i < first + count; i++) {
+        const Box3 &a = bodies[idx[i]].aabb;
+        bx.mn = {std::min(bx.mn.x, a.mn.x), std::min(bx.mn.y, a.mn.y), std::min(bx.mn.z, a.mn.z)};
+        bx.mx = {std::max(bx.mx.x, a.mx.x), std::max(bx.mx.y, a.mx.y), std::max(bx.mx.z, a.mx.z)};
+    }
+    nodes[ni].box = bx;
+    if (count <= 4) {
+        nodes[ni].first = first;
+        nodes[ni].count = count;
+        return;
+    }
+    V3 ext = sub(bx.mx, bx.mn);
+    int axis = (ext.x >= ext.y && ext.x >= ext.z) ? 0 : (ext.y >= ext.z ? 1 : 2);
+    auto key = [&](int i) {
+        const Box3 &a = bodies[i].aabb;
+        return axis == 0 ? a.mn.x + a.mx.x : (axis == 1 ? a.mn.y + a.mx.y : a.mn.z + a.mx.z);
+    };
+    int mid = first + count / 2;
+    std::nth_element(idx.begin() + first, idx.begin() + mid, idx.begin() + first + count,
+                     [&](int a, int b) { return key(a) < key(b) || (key(a) == key(b) && a < b); });
+    int l = (int)nodes.size();
+    bvh_build(bodies, idx, nodes, first, mid - first);
+    int r = (int)nodes.size();
+    bvh_build(bodies, idx, nodes, mid, first + count - mid);
+    nodes[ni].left = l;
+    nodes[ni].right = r;
+}
+
+static void find_colliding_pairs(World &w) {
+    w.pairs.clear();
+    std::vector<int> idx(w.bodies.size());
+    std::iota(idx.begin(), idx.end(), 0);
+    std::vector<BvhNode> nodes;
+    if (!idx.empty()) bvh_build(w.bodies, idx, nodes, 0, (int)idx.size());
+    // bodies sorted (stably) by broadphase layer, broadphase.ts:235-239
+    std::vector<int> order(w.bodies.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return w.layers.objToBp[w.bodies[a].objectLayer] < w.layers.objToBp[w.bodies[b].objectLayer];
+    });
+    std::vector<int> cand;
+    std::vector<int> stack;
+    for (int qi : order) {
+        Body &A = w.bodies[qi];
+        if (!should_query(A)) continue;
+        Box3 E = box_expand(A.aabb, w.s.speculativeContactDistance);
+        int la = A.objectLayer, bpa = w.layers.objToBp[la];
+        cand.clear();
+        stack.clear();
+        stack.push_back(0);
+        while (!stack.empty()) {
+            int n = stack.back();
+            stack.pop_back();
+            if (!box_overlap(nodes[n].box, E)) continue;
+            if (nodes[n].left >= 0) {
+                stack.push_back(nodes[n].left);
+                stack.push_back(nodes[n].right);
+                continue;
+            }
+            for (int k = 0; k < nodes[n].count; k++) cand.push_back(idx[nodes[n].first + k]);
+        }
+        std::sort(cand.begin(), cand.end());
+        for (int bi : cand) {
+            Body &B = w.bodies[bi];
+            int lb = B.objectLayer, bpb = w.layers.objToBp[lb];
+            // layer gating of the per-layer tree query (broadphase.ts:252-272)
+            if (!w.layers.objVsBp[la * w.layers.nBp + bpb]) continue;
+            if (!w.layers.bpPairs[bpa * w.layers.nBp + bpb]) continue;
+            // dbvt.intersectAABB leaf filters (dbvt.ts:645-670)
+            if (!((A.groups & B.mask) != 0 && (B.groups & A.mask) != 0)) continue;
+            if (!w.layers.objPairs[la * w.layers.nObj + lb]) continue;
+            if (!box_overlap(B.aabb, E)) continue;
+            // CollisionBodyPairVisitor.visit broadphase.ts:83-138
+            if (A.id == B.id) continue;
+            if (dedup_index(A) >= dedup_index(B)) continue;
+            if (A.motion == STATIC && B.motion == STATIC) continue;
+            if (!A.collideKinematicVsNonDynamic && !B.collideKinematicVsNonDynamic && A.motion != DYNAMIC &&
+                B.motion != DYNAMIC && !(A.motion == KINEMATIC && B.sensor) && !(B.motion == KINEMATIC && A.sensor))
+                continue;
+            w.pairs.push_back({A.index, B.index});
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Contact constraints (contact-constraints.ts)
+// ---------------------------------------------------------------------------
+static double combine(double a, double b, int ma, int mb) {  // combine-material.ts:40-57
+    static const int prio[5] = {0, 1, 3, 4, 2};                // AVERAGE, MULTIPLY, MIN, MAX, GEOMETRIC_MEAN
+    int mode = prio[ma] >= prio[mb] ? ma : mb;
+    switch (mode) {
+        case C_MULTIPLY:
+            return a * b;
+        case C_MIN:
+            return std::min(a, b);
+        case C_MAX:
+            return std::max(a, b);
+        case C_GEOMETRIC_MEAN:
+            return std::sqrt(a * b);
+        default:
+            return (a + b) / 2;
+    }
+}
+
+// calculateInverseEffectiveMass axis-constraint-part.ts:86-148.  For a
+// non-dynamic body the cross terms are zeroed (the reference leaves stale
+// values there, which only kinematic bodies ever read).
+static double inv_eff_mass(AxisPart &p, const Body &A, const Body &B, double imA, double imB, const M4 &IA,
+                           const M4 &IB, V3 r1, V3 r2, V3 ax) {
+    double iem = 0;
+    p.r1xa = p.r2xa = p.invI1 = p.invI2 = {0, 0, 0};
+    if (A.motion == DYNAMIC) {
+        p.r1xa = {r1.y * ax.z - r1.z * ax.y, r1.z * ax.x - r1.x * ax.z, r1.x * ax.y - r1.y * ax.x};
+        V3 c = p.r1xa;
+        p.invI1 = {IA.m[0] * c.x + IA.m[4] * c.y + IA.m[8] * c.z, IA.m[1] * c.x + IA.m[5] * c.y + IA.m[9] * c.z,
+                   IA.m[2] * c.x + IA.m[6] * c.y + IA.m[10] * c.z};
+        iem += imA + (p.invI1.x * c.x + p.invI1.y * c.y + p.invI1.z * c.z);
+    }
+    if (B.motion == DYNAMIC) {
+        p.r2xa = {r2.y * ax.z - r2.z * ax.y, r2.z * ax.x - r2.x * ax.z, r2.x * ax.y - r2.y * ax.x};
+        V3 c = p.r2xa;
+        p.invI2 = {IB.m[0] * c.x + IB.m[4] * c.y + IB.m[8] * c.z, IB.m[1] * c.x + IB.m[5] * c.y + IB.m[9] * c.z,
+                   IB.m[2] * c.x + IB.m[6] * c.y + IB.m[10] * c.z};
+        iem += imB + (p.invI2.x * c.x + p.invI2.y * c.y + p.invI2.z * c.z);
+    }
+    return iem;
+}
+// calculateConstraintProperties axis-constraint-part.ts:165-200
+static void calc_props(AxisPart &p, const Body &A, const Body &B, double imA, double imB, const M4 &IA, const M4 &IB,
+                       V3 r1, V3 r2, V3 ax, double bias) {
+    double iem = inv_eff_mass(p, A, B, imA, imB, IA, IB, r1, r2, ax);
+    if (iem == 0) {
+        p.effMass = 0;
+        p.totalLambda = 0;
+    } else {
+        p.effMass = 1 / iem;
+        p.softness = 0;
+        p.bias = bias;
+    }
+}
+static bool part_active(const AxisPart &p) { return p.effMass != 0; }
+
+// calculateNormalVelocityBias contact-constraints.ts:288-423
+static double normal_velocity_bias(const Body &A, const Body &B, V3 pA, V3 pB, V3 n, V3 rA, V3 rB, double e,
+                                   double dt, V3 g, double minVel) {
+    bool aM = A.motion != STATIC, bM = B.motion != STATIC, aD = A.motion == DYNAMIC, bD = B.motion == DYNAMIC;
+    auto vel_at = [](const Body &b, V3 r) {
+        return V3{b.linvel.x + (b.angvel.y * r.z - b.angvel.z * r.y), b.linvel.y + (b.angvel.z * r.x - b.angvel.x * r.z),
+                  b.linvel.z + (b.angvel.x * r.y - b.angvel.y * r.x)};
+    };
+    V3 rv;
+    if (aM && bM) {
+        V3 v1 = vel_at(A, rA), v2 = vel_at(B, rB);
+        rv = sub(v2, v1);
+    } else if (aM) {
+        rv = neg(vel_at(A, rA));
+    } else if (bM) {
+        rv = vel_at(B, rB);
+    } else {
+        return 0;
+    }
+    double nv = rv.x * n.x + rv.y * n.y + rv.z * n.z;
+    V3 d = sub(pA, pB);
+    double pen = d.x * n.x + d.y * n.y + d.z * n.z;
+    double spec = std::max(0.0, -pen / dt);
+    if (e > 0 && nv < -minVel) {
+        if (nv < -spec) {
+            double rx = 0, ry = 0, rz = 0;
+            if (aM && bM) {
+                double gs = B.gravityFactor - A.gravityFactor;
+                rx += g.x * gs;
+                ry += g.y * gs;
+                rz += g.z * gs;
+            } else if (aM) {
+                rx += g.x * -A.gravityFactor;
+                ry += g.y * -A.gravityFactor;
+                rz += g.z * -A.gravityFactor;
+            } else if (bM) {
+                rx += g.x * B.gravityFactor;
+                ry += g.y * B.gravityFactor;
+                rz += g.z * B.gravityFactor;
+            }
+            if (aD) {
+                double fs = -A.invMass;
+                rx += A.force.x * fs;
+                ry += A.force.y * fs;
+                rz += A.force.z * fs;
+            }
+            if (bD) {
+                double fs = B.invMass;
+                rx += B.force.x * fs;
+                ry += B.force.y * fs;
+                rz += B.force.z * fs;
+            }
+            double adn = rx * n.x + ry * n.y + rz * n.z;
+            double fdv = std::min(0.0, adn * dt);
+            return e * (nv - fdv);
+        }
+        return spec;
+    }
+    return spec;
+}
+
+// computeContactSortKey contact-constraints.ts:1222-1231
+static uint32_t sort_key(int a, int b, uint32_t sa, uint32_t sb) {
+    int32_t h = 0;
+    auto step = [](int32_t h, int64_t v) { return (int32_t)(uint32_t)((int64_t)h * 31 + v); };
+    h = step(h, a);
+    h = step(h, b);
+    h = step(h, (int32_t)sa);
+    h = step(h, (int32_t)sb);
+    return (uint32_t)h;
+}
+
+// addContactConstraint contact-constraints.ts:437-857 (no listener)
+static bool add_contact_constraint(World &w, Body *A, Body *B, Manifold m, double dt) {
+    if (A->id > B->id) {
+        std::swap(A, B);
+        // swapShapes manifold.ts:86-105
+        m.normal = neg(m.normal);
+        std::swap(m.subA, m.subB);
+        for (int i = 0; i < m.n; i++) std::swap(m.relA[i], m.relB[i]);
+    }
+    ContactKey key{A->id, B->id, m.subA, m.subB};
+    auto it = w.contacts.find(key);
+    bool existing = it != w.contacts.end();
+    Contact prev;
+    if (existing) prev = it->second;
+    Contact &c = w.contacts[key];
+    if (!existing) {
+        c.idA = A->id;
+        c.idB = B->id;
+        c.subA = m.subA;
+        c.subB = m.subB;
+    }
+    c.processed = true;
+    M4 rotA = mat4_from_quat(A->quat), rotB = mat4_from_quat(B->quat);
+    V3 nw = m.normal;
+    c.normalB = normalize(V3{rotB.m[0] * nw.x + rotB.m[1] * nw.y + rotB.m[2] * nw.z,
+                             rotB.m[4] * nw.x + rotB.m[5] * nw.y + rotB.m[6] * nw.z,
+                             rotB.m[8] * nw.x + rotB.m[9] * nw.y + rotB.m[10] * nw.z});
+    c.n = m.n;
+    double friction = combine(A->friction, B->friction, A->frictionCombine, B->frictionCombine);
+    double restitution = combine(A->restitution, B->restitution, A->restitutionCombine, B->restitutionCombine);
+    bool isSensor = A->sensor || B->sensor;
+    if (!isSensor && ((A->motion == DYNAMIC && A->invMass != 0) || (B->motion == DYNAMIC && B->invMass != 0))) {
+        w.constraints.emplace_back();
+        ContactConstraint &cc = w.constraints.back();
+        cc.bodyA = A->index;
+        cc.bodyB = B->index;
+        cc.subA = m.subA;
+        cc.subB = m.subB;
+        cc.contactKey = key;
+        cc.sortKey = sort_key(A->index, B->index, m.subA, m.subB);
+        cc.normal = m.normal;
+        double nx = cc.normal.x, ny = cc.normal.y, nz = cc.normal.z;
+        if (std::fabs(nx) > std::fabs(ny)) {
+            double tl = std::sqrt(nx * nx + nz * nz);
+            cc.t1 = {nz / tl, 0, -nx / tl};
+        } else {
+            double tl = std::sqrt(ny * ny + nz * nz);
+            cc.t1 = {0, nz / tl, -ny / tl};
+        }
+        cc.t2 = {ny * cc.t1.z - nz * cc.t1.y, nz * cc.t1.x - nx * cc.t1.z, nx * cc.t1.y - ny * cc.t1.x};
+        cc.friction = friction;
+        cc.restitution = restitution;
+        cc.invMassA = A->invMass * 1.0;
+        cc.invMassB = B->invMass * 1.0;
+        cc.invIScaleA = 1;
+        cc.invIScaleB = 1;
+        std::memset(&cc.invIA, 0, sizeof(M4));
+        std::memset(&cc.invIB, 0, sizeof(M4));
+        if (A->motion == DYNAMIC) cc.invIA = inv_inertia_for_rotation(*A, rotA);
+        if (B->motion == DYNAMIC) cc.invIB = inv_inertia_for_rotation(*B, rotB);
+        cc.n = 0;
+        for (int i = 0; i < m.n; i++) {
+            WorldContactPoint &cp = cc.pts[cc.n];
+            cc.n++;
+            cp.posA = add(m.base, m.relA[i]);
+            cp.posB = add(m.base, m.relB[i]);
+            V3 la = sub(cp.posA, A->com), lb = sub(cp.posB, B->com);
+            cp.localA = m3tmul(rotA, la);
+            cp.localB = m3tmul(rotB, lb);
+            bool set = false;
+            if (existing) {
+                for (int j = 0; j < prev.n; j++) {
+                    const CachedPoint &p = prev.pts[j];
+                    V3 d1 = sub(cp.localA, p.p1), d2 = sub(cp.localB, p.p2);
+                    double s1 = d1.x * d1.x + d1.y * d1.y + d1.z * d1.z;
+                    double s2 = d2.x * d2.x + d2.y * d2.y + d2.z * d2.z;
+                    double th = w.s.preserveLambdaMaxDistSq;
+                    if (s1 < th && s2 < th) {
+                        cp.n.totalLambda = p.ln;
+                        cp.t1.totalLambda = p.lt1;
+                        cp.t2.totalLambda = p.lt2;
+                        set = true;
+                        break;
+                    }
+                }
+            }
+            if (!set) {
+                cp.n.totalLambda = 0;
+                cp.t1.totalLambda = 0;
+                cp.t2.totalLambda = 0;
+            }
+            V3 mid{(cp.posA.x + cp.posB.x) * 0.5, (cp.posA.y + cp.posB.y) * 0.5, (cp.posA.z + cp.posB.z) * 0.5};
+            V3 rA = sub(mid, A->com), rB = sub(mid, B->com);
+            double nb = normal_velocity_bias(*A, *B, cp.posA, cp.posB, cc.normal, rA, rB, restitution, dt, w.s.gravity,
+                                             w.s.minVelocityForRestitution);
+            calc_props(cp.n, *A, *B, cc.invMassA, cc.invMassB, cc.invIA, cc.invIB, rA, rB, cc.normal, nb);
+            if (friction > 0) {
+                // zero surface velocity: calculateFrictionBias contact-constraints.ts:252-266 returns 0
+                calc_props(cp.t1, *A, *B, cc.invMassA, cc.invMassB, cc.invIA, cc.invIB, rA, rB, cc.t1, 0.0);
+                calc_props(cp.t2, *A, *B, cc.invMassA, cc.invMassB, cc.invIA, cc.invIB, rA, rB, cc.t2, 0.0);
+            } else {
+                cp.t1.effMass = 0;
+                cp.t1.totalLambda = 0;
+                cp.t2.effMass = 0;
+                cp.t2.totalLambda = 0;
+            }
+            CachedPoint &cpt = c.pts[i];
+            cpt.p1 = cp.localA;
+            cpt.p2 = cp.localB;
+            cpt.ln = cp.n.totalLambda;
+            cpt.lt1 = cp.t1.totalLambda;
+            cpt.lt2 = cp.t2.totalLambda;
+        }
+        w.manifolds.push_back(m);
+        w.manifoldBodies.push_back({A->index, B->index});
+        return true;
+    }
+    for (int i = 0; i < m.n; i++) {
+        V3 pa = add(m.base, m.relA[i]), pb = add(m.base, m.relB[i]);
+        V3 la = sub(pa, A->com), lb = sub(pb, B->com);
+        c.pts[i].p1 = m3tmul(rotA, la);
+        c.pts[i].p2 = m3tmul(rotB, lb);
+        c.pts[i].ln = c.pts[i].lt1 = c.pts[i].lt2 = 0;
+    }
+    return false;
+}
+
+// narrowphase update.ts:714-850 with the reduction collector update.ts:333-563
+static bool narrowphase(World &w, Body *A, Body *B, double dt) {
+    CollideSettings cs;
+    cs.collectFaces = true;
+    cs.collisionTolerance = w.s.collisionTolerance;
+    cs.penetrationTolerance = w.s.penetrationTolerance;
+    cs.maxSeparation = (A->sensor || B->sensor) ? 0 : w.s.speculativeContactDistance;
+    Hit hit;
+    if (!collide_shapes(hit, cs, A->shape, A->position, A->quat, B->shape, B->position, B->quat)) return false;
+    // addHit update.ts:385-519 (one hit per convex pair: one manifold)
+    double maxContactDistance = w.s.speculativeContactDistance + w.s.manifoldTolerance;
+    Manifold m;
+    m.base = A->position;
+    m.normal = normalize(hit.axis);
+    m.depth = hit.penetration;
+    m.subA = hit.subA;
+    m.subB = hit.subB;
+    Manifold tmp;
+    tmp.base = A->position;
+    if (hit.faceA.n >= 2 && hit.faceB.n >= 3) {
+        manifold_between_faces(tmp, hit.pa, hit.pb, hit.axis, maxContactDistance, hit.faceA, hit.faceB);
+    } else {
+        set_contact_point(tmp, 0, hit.pa, hit.pb);
+        tmp.n = 1;
+    }
+    for (int i = 0; i < tmp.n; i++) {
+        if (m.n >= 64) break;
+        m.relA[m.n] = tmp.relA[i];
+        m.relB[m.n] = tmp.relB[i];
+        m.n++;
+    }
+    if (hit.penetration > m.depth) m.depth = hit.penetration;
+    if (m.n > 32) prune_contact_points(m, m.normal);
+    // finalizeAndCreateConstraints update.ts:525-558
+    m.normal = normalize(m.normal);
+    if (m.n > 4) prune_contact_points(m, m.normal);
+    if (m.n > 0) return add_contact_constraint(w, A, B, m, dt);
+    return false;
+}
+
+// ---------------------------------------------------------------------------
+// Solver (contact-constraints.ts:906-1216, axis-constraint-part.ts:500-847)
+// ---------------------------------------------------------------------------
+static void apply_dof_lin(Body &b) {
+    int t = b.dof & 0b111;
+    if (!(t & 1)) b.linvel.x = 0;
+    if (!(t & 2)) b.linvel.y = 0;
+    if (!(t & 4)) b.linvel.z = 0;
+}
+static void warm_start(AxisPart &p, Body &A, Body &B, double imA, double imB, V3 ax, double ratio) {
+    p.totalLambda *= ratio;
+    if (p.totalLambda == 0) return;
+    if (A.motion == DYNAMIC) {
+        V3 imp = scale(ax, p.totalLambda * imA);
+        A.linvel = sub(A.linvel, imp);
+        apply_dof_lin(A);
+        V3 ai = scale(p.invI1, p.totalLambda);
+        A.angvel = sub(A.angvel, ai);
+    }
+    if (B.motion == DYNAMIC) {
+        V3 imp = scale(ax, p.totalLambda * imB);
+        B.linvel = add(B.linvel, imp);
+        apply_dof_lin(B);
+        V3 ai = scale(p.invI2, p.totalLambda);
+        B.angvel = add(B.angvel, ai);
+    }
+}
+// getTotalLambda axis-constraint-part.ts:578-625
+static double total_lambda(const AxisPart &p, const Body &A, const Body &B, V3 ax) {
+    bool mA = A.motion != STATIC, mB = B.motion != STATIC;
+    double jv;
+    if (mA && mB) {
+        double dx = A.linvel.x - B.linvel.x, dy = A.linvel.y - B.linvel.y, dz = A.linvel.z - B.linvel.z;
+        jv = ax.x * dx + ax.y * dy + ax.z * dz;
+    } else if (mA) {
+        jv = ax.x * A.linvel.x + ax.y * A.linvel.y + ax.z * A.linvel.z;
+    } else if (mB) {
+        jv = -(ax.x * B.linvel.x + ax.y * B.linvel.y + ax.z * B.linvel.z);
+    } else {
+        jv = 0;
+    }
+    if (mA) jv += p.r1xa.x * A.angvel.x + p.r1xa.y * A.angvel.y + p.r1xa.z * A.angvel.z;
+    if (mB) jv -= p.r2xa.x * B.angvel.x + p.r2xa.y * B.angvel.y + p.r2xa.z * B.angvel.z;
+    double lambda = p.effMass * (jv - (p.softness * p.totalLambda + p.bias));
+    return p.totalLambda + lambda;
+}
+// applyLambda axis-constraint-part.ts:640-707
+static bool apply_lambda(AxisPart &p, Body &A, Body &B, double imA, double imB, V3 ax, double tl) {
+    double dl = tl - p.totalLambda;
+    p.totalLambda = tl;
+    if (dl == 0) return false;
+    if (A.motion == DYNAMIC) {
+        double ls = dl * imA;
+        A.linvel.x -= ax.x * ls;
+        A.linvel.y -= ax.y * ls;
+        A.linvel.z -= ax.z * ls;
+        apply_dof_lin(A);
+        A.angvel.x -= p.invI1.x * dl;
+        A.angvel.y -= p.invI1.y * dl;
+        A.angvel.z -= p.invI1.z * dl;
+    }
+    if (B.motion == DYNAMIC) {
+        double ls = dl * imB;
+        B.linvel.x += ax.x * ls;
+        B.linvel.y += ax.y * ls;
+        B.linvel.z += ax.z * ls;
+        apply_dof_lin(B);
+        B.angvel.x += p.invI2.x * dl;
+        B.angvel.y += p.invI2.y * dl;
+        B.angvel.z += p.invI2.z * dl;
+    }
+    return true;
+}
+
+static void warm_start_all(World &w, double ratio) {
+    for (ContactConstraint &c : w.constraints) {
+        Body &A = w.bodies[c.bodyA], &B = w.bodies[c.bodyB];
+        for (int i = 0; i < c.n; i++) {
+            WorldContactPoint &cp = c.pts[i];
+            if (part_active(cp.t1) || part_active(cp.t2)) {
+                warm_start(cp.t1, A, B, c.invMassA, c.invMassB, c.t1, ratio);
+                warm_start(cp.t2, A, B, c.invMassA, c.invMassB, c.t2, ratio);
+            }
+            warm_start(cp.n, A, B, c.invMassA, c.invMassB, c.normal, ratio);
+        }
+    }
+}
+
+// solveVelocityConstraintsForIsland contact-constraints.ts:963-1053
+static void solve_velocity(World &w, const std::vector<int> &ids) {
+    for (int ci : ids) {
+        ContactConstraint &c = w.constraints[ci];
+        Body &A = w.bodies[c.bodyA], &B = w.bodies[c.bodyB];
+        if (A.motion != DYNAMIC && B.motion != DYNAMIC) continue;
+        for (int i = 0; i < c.n; i++) {
+            WorldContactPoint &cp = c.pts[i];
+            if (part_active(cp.t1) || part_active(cp.t2)) {
+                double l1 = total_lambda(cp.t1, A, B, c.t1);
+                double l2 = total_lambda(cp.t2, A, B, c.t2);
+                double mf = c.friction * cp.n.totalLambda;
+                double fm = l1 * l1 + l2 * l2;
+                double mfs = mf * mf;
+                if (fm > mfs) {
+                    double s = mf / std::sqrt(fm);
+                    l1 *= s;
+                    l2 *= s;
+                }
+                apply_lambda(cp.t1, A, B, c.invMassA, c.invMassB, c.t1, l1);
+                apply_lambda(cp.t2, A, B, c.invMassA, c.invMassB, c.t2, l2);
+            }
+        }
+        for (int i = 0; i < c.n; i++) {
+            WorldContactPoint &cp = c.pts[i];
+            double tl = total_lambda(cp.n, A, B, c.normal);
+            apply_lambda(cp.n, A, B, c.invMassA, c.invMassB, c.normal, std::max(0.0, tl));
+        }
+    }
+}
+
+// rigid-body-step.ts:16-97
+static void add_rotation_step(Body &b, V3 a) {
+    double l = len(a);
+    if (l > 1.0e-6) {
+        V3 axis = scale(a, 1 / l);
+        Q4 r = qaxis_angle(axis, l);
+        b.quat = qnormalize(qmul(r, b.quat));
+    }
+}
+static void sub_rotation_step(Body &b, V3 a) {
+    double l = len(a);
+    if (l > 1.0e-6) {
+        V3 axis = scale(a, 1 / l);
+        Q4 r = qaxis_angle(axis, -l);
+        b.quat = qnormalize(qmul(r, b.quat));
+    }
+}
+static void apply_dof_pos(Body &b) {
+    int t = b.dof & 0b111;
+    if (!(t & 1)) b.com.x = 0;
+    if (!(t & 2)) b.com.y = 0;
+    if (!(t & 4)) b.com.z = 0;
+}
+
+// solvePositionConstraintsForIsland contact-constraints.ts:1098-1216
+static bool solve_position(World &w, const std::vector<int> &ids) {
+    bool any = false;
+    for (int ci : ids) {
+        ContactConstraint &c = w.constraints[ci];
+        Body &A = w.bodies[c.bodyA], &B = w.bodies[c.bodyB];
+        if (A.motion != DYNAMIC && B.motion != DYNAMIC) continue;
+        M4 rotA = mat4_from_quat(A.quat), rotB = mat4_from_quat(B.quat);
+        M4 IA{}, IB{};
+        if (A.motion == DYNAMIC) IA = inv_inertia_for_rotation(A, rotA);
+        if (B.motion == DYNAMIC) IB = inv_inertia_for_rotation(B, rotB);
+        for (int i = 0; i < c.n; i++) {
+            WorldContactPoint &cp = c.pts[i];
+            V3 wra = m3mul(rotA, cp.localA);
+            V3 pa = add(A.com, wra);
+            V3 wrb = m3mul(rotB, cp.localB);
+            V3 pb = add(B.com, wrb);
+            V3 pv = sub(pb, pa);
+            double sep = (pv.x * c.normal.x + pv.y * c.normal.y + pv.z * c.normal.z) + w.s.penetrationSlop;
+            sep = std::max(sep, -w.s.maxPenetrationDistance);
+            if (sep >= 0) continue;
+            V3 mid{(pa.x + pb.x) * 0.5, (pa.y + pb.y) * 0.5, (pa.z + pb.z) * 0.5};
+            V3 rA = sub(mid, A.com), rB = sub(mid, B.com);
+            // calculateConstraintPropertiesWithMassOverride axis-constraint-part.ts:225-264
+            M4 sIA = IA, sIB = IB;
+            for (int k = 0; k < 16; k++) {
+                sIA.m[k] *= c.invIScaleA;
+                sIB.m[k] *= c.invIScaleB;
+            }
+            calc_props(cp.n, A, B, c.invMassA, c.invMassB, sIA, sIB, rA, rB, c.normal, 0);
+            // solvePositionConstraintWithMassOverride axis-constraint-part.ts:790-847
+            AxisPart &p = cp.n;
+            if (sep == 0 || !part_active(p) || p.softness != 0) continue;
+            double lambda = -p.effMass * w.s.baumgarteFactor * sep;
+            if (A.motion == DYNAMIC) {
+                V3 imp = scale(c.normal, lambda * c.invMassA);
+                A.com = sub(A.com, imp);
+                apply_dof_pos(A);
+                sub_rotation_step(A, scale(p.invI1, lambda));
+            }
+            if (B.motion == DYNAMIC) {
+                V3 imp = scale(c.normal, lambda * c.invMassB);
+                B.com = add(B.com, imp);
+                apply_dof_pos(B);
+                add_rotation_step(B, scale(p.invI2, lambda));
+            }
+            any = true;
+        }
+    }
+    return any;
+}
+
+// ---------------------------------------------------------------------------
+// Islands (islands.ts)
+// ---------------------------------------------------------------------------
+static void build_islands(World &w) {
+    int64_t na = w.activeCount;
+    std::vector<int64_t> links(na), bodyIslands(na, 0);
+    for (int64_t i = 0; i < na; i++) links[i] = i;
+    for (Body &b : w.bodies) b.islandIndex = -1;
+    auto lowest = [&](int64_t i) {
+        while (links[i] != i) i = links[i];
+        return i;
+    };
+    std::vector<int64_t> contactLinks(w.constraints.size(), INACTIVE);
+    for (size_t ci = 0; ci < w.constraints.size(); ci++) {
+        const ContactConstraint &c = w.constraints[ci];
+        Body &A = w.bodies[c.bodyA], &B = w.bodies[c.bodyB];
+        if (A.activeIndex != INACTIVE && B.activeIndex != INACTIVE) {
+            // linkBodies islands.ts:103-140
+            int64_t a = A.activeIndex, b = B.activeIndex;
+            if (a < na && b < na) {
+                int64_t f = lowest(a), s = lowest(b);
+                if (f != s) {
+                    if (f < s)
+                        links[s] = f;
+                    else
+                        links[f] = s;
+                    int64_t lo = std::min(f, s);
+                    if (links[a] > lo) links[a] = lo;
+                    if (links[b] > lo) links[b] = lo;
+                }
+            }
+        }
+        contactLinks[ci] = std::min(A.activeIndex, B.activeIndex);
+    }
+    // finalize islands.ts:240-389
+    int ni = 0;
+    for (int64_t i = 0; i < na; i++) {
+        int64_t l = links[i];
+        if (l != i) {
+            bodyIslands[i] = bodyIslands[l];
+        } else {
+            bodyIslands[i] = ni++;
+        }
+    }
+    std::vector<Island> isl(ni);
+    for (int64_t ai = 0; ai < na; ai++) {
+        int bi = w.activeBodyIndices[ai];
+        isl[bodyIslands[ai]].bodyIndices.push_back(ai);
+        w.bodies[bi].islandIndex = (int)bodyIslands[ai];
+    }
+    for (size_t ci = 0; ci < contactLinks.size(); ci++) {
+        int64_t ab = contactLinks[ci];
+        if (ab >= INACTIVE) continue;
+        isl[bodyIslands[ab]].contactIndices.push_back((int)ci);
+    }
+    std::stable_sort(isl.begin(), isl.end(),
+                     [](const Island &a, const Island &b) { return a.contactIndices.size() > b.contactIndices.size(); });
+    for (Island &is : isl) {
+        int vs = 0, ps = 0;
+        bool dv = false, dp = false;
+        for (int64_t ai : is.bodyIndices) {
+            Body &b = w.bodies[w.activeBodyIndices[ai]];
+            if (b.motion != DYNAMIC) continue;
+            vs = std::max(vs, b.velOverride);
+            dv = dv || b.velOverride == 0;
+            ps = std::max(ps, b.posOverride);
+            dp = dp || b.posOverride == 0;
+        }
+        if (dv) vs = std::max(vs, w.s.velocityIterations);
+        if (dp) ps = std::max(ps, w.s.positionIterations);
+        is.velSteps = vs;
+        is.posSteps = ps;
+    }
+    w.islands = std::move(isl);
+}
+
+// checkIslandSleep islands.ts:392-423
+static void check_island_sleep(World &w, Island &is, double dt) {
+    if (!w.s.allowSleeping) return;
+    double tbs = w.s.timeBeforeSleep;
+    double maxMove = w.s.pointVelocitySleepThreshold * tbs;
+    bool all = true;
+    for (int64_t ai : is.bodyIndices) {
+        Body &b = w.bodies[w.activeBodyIndices[ai]];
+        if (b.motion != DYNAMIC) continue;
+        bool cs = update_sleep_state(b, dt, maxMove, tbs);
+        all = all && cs;
+    }
+    if (all) {
+        for (int64_t ai : is.bodyIndices) {
+            Body &b = w.bodies[w.activeBodyIndices[ai]];
+            if (b.motion == DYNAMIC) sleep_body(w, b);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The step: updateWorld update.ts:45-239 (no listener, no joints, no CCD bodies)
+// ---------------------------------------------------------------------------
+static void step(World &w, double dt) {
+    w.constraints.clear();
+    w.manifolds.clear();
+    w.manifoldBodies.clear();
+    for (auto &kv : w.contacts) kv.second.processed = false;
+    // accelerationIntegrationUpdate update.ts:245-319
+    for (Body &b : w.bodies) {
+        if (b.motion != DYNAMIC || b.sleeping) continue;
+        double gs = w.s.gravityEnabled ? b.gravityFactor : 0;
+        V3 g = w.s.gravity;
+        double ax = (b.force.x * b.invMass + g.x * gs) * dt;
+        double ay = (b.force.y * b.invMass + g.y * gs) * dt;
+        double az = (b.force.z * b.invMass + g.z * gs) * dt;
+        b.linvel.x += ax;
+        b.linvel.y += ay;
+        b.linvel.z += az;
+        double ldf = std::max(0.0, 1 - b.linDamp * dt);
+        b.linvel = scale(b.linvel, ldf);
+        double ls = b.linvel.x * b.linvel.x + b.linvel.y * b.linvel.y + b.linvel.z * b.linvel.z;
+        if (ls > b.maxLin * b.maxLin) b.linvel = scale(b.linvel, b.maxLin / std::sqrt(ls));
+        apply_dof_lin(b);
+        M4 R = mat4_from_quat(b.quat);
+        M4 I = inv_inertia_for_rotation(b, R);
+        V3 t = b.torque;
+        b.angvel.x += (I.m[0] * t.x + I.m[4] * t.y + I.m[8] * t.z) * dt;
+        b.angvel.y += (I.m[1] * t.x + I.m[5] * t.y + I.m[9] * t.z) * dt;
+        b.angvel.z += (I.m[2] * t.x + I.m[6] * t.y + I.m[10] * t.z) * dt;
+        double adf = std::max(0.0, 1 - b.angDamp * dt);
+        b.angvel = scale(b.angvel, adf);
+        double as = b.angvel.x * b.angvel.x + b.angvel.y * b.angvel.y + b.angvel.z * b.angvel.z;
+        if (as > b.maxAng * b.maxAng) b.angvel = scale(b.angvel, b.maxAng / std::sqrt(as));
+        int r = (b.dof >> 3) & 0b111;
+        if (!(r & 1)) b.angvel.x = 0;
+        if (!(r & 2)) b.angvel.y = 0;
+        if (!(r & 4)) b.angvel.z = 0;
+    }
+    find_colliding_pairs(w);
+    for (auto &pr : w.pairs) {
+        Body *A = &w.bodies[pr.first], *B = &w.bodies[pr.second];
+        if (A->motion > B->motion || (A->motion == B->motion && B->id < A->id)) std::swap(A, B);
+        bool created = narrowphase(w, A, B, dt);
+        if (created) {
+            if (A->motion == DYNAMIC && A->sleeping) wake_body(w, *A);
+            if (B->motion == DYNAMIC && B->sleeping) wake_body(w, *B);
+        }
+        // destroyStaleContactsBetweenBodies: a convex pair has a single contact key, so any
+        // unprocessed record between A and B is removed with the unprocessed sweep below.
+    }
+    // destroyUnprocessedContacts contacts.ts:534-553
+    for (auto it = w.contacts.begin(); it != w.contacts.end();) {
+        if (!it->second.processed)
+            it = w.contacts.erase(it);
+        else
+            ++it;
+    }
+    if (dt > 0) {
+        build_islands(w);
+        if (w.s.warmStarting) {
+            double ratio = (w.s.warmStarting && w.prevDt > 0) ? dt / w.prevDt : 0.0;
+            warm_start_all(w, ratio);
+        }
+        w.prevDt = dt;
+        for (Island &is : w.islands) {
+            if (is.contactIndices.empty()) continue;
+            // sortContactIndices contact-constraints.ts:1240-1264 (JS sort is stable)
+            std::stable_sort(is.contactIndices.begin(), is.contactIndices.end(), [&](int a, int b) {
+                const ContactConstraint &ca = w.constraints[a], &cb = w.constraints[b];
+                if (ca.sortKey != cb.sortKey) return ca.sortKey < cb.sortKey;
+                int64_t ia = w.bodies[ca.bodyA].id, ib = w.bodies[cb.bodyA].id;
+                if (ia != ib) return ia < ib;
+                return w.bodies[ca.bodyB].id < w.bodies[cb.bodyB].id;
+            });
+            for (int i = 0; i < is.velSteps; i++) solve_velocity(w, is.contactIndices);
+        }
+        // storeAppliedImpulses contact-constraints.ts:1061-1076
+        for (ContactConstraint &c : w.constraints) {
+            Contact &ct = w.contacts[c.contactKey];
+            for (int i = 0; i < c.n; i++) {
+                ct.pts[i].ln = c.pts[i].n.totalLambda;
+                ct.pts[i].lt1 = c.pts[i].t1.totalLambda;
+                ct.pts[i].lt2 = c.pts[i].t2.totalLambda;
+            }
+        }
+        // velocityIntegrationUpdate update.ts:896-976 (discrete motion quality)
+        for (Body &b : w.bodies) {
+            if (b.motion == STATIC || b.sleeping) continue;
+            if (b.motion == DYNAMIC) {
+                // clampLinearVelocity / clampAngularVelocity motion-properties.ts:624-639
+                if (lensq(b.linvel) > b.maxLin * b.maxLin) b.linvel = scale(normalize(b.linvel), b.maxLin);
+                if (lensq(b.angvel) > b.maxAng * b.maxAng) b.angvel = scale(normalize(b.angvel), b.maxAng);
+            }
+            V3 rv = scale(b.angvel, dt);
+            double angle = len(rv);
+            if (angle > 1e-6) {
+                V3 axis = scale(rv, 1 / angle);
+                Q4 rq = qaxis_angle(axis, angle);
+                b.quat = qnormalize(qmul(rq, b.quat));
+            }
+            V3 disp = scale(b.linvel, dt);
+            b.com = add(b.com, disp);
+            update_pos_from_com(b);
+            set_transform(b);
+        }
+        for (Island &is : w.islands) {
+            if (is.contactIndices.empty()) continue;
+            for (int i = 0; i < is.posSteps; i++) {
+                if (!solve_position(w, is.contactIndices)) break;
+            }
+        }
+        // updateBodyPositions update.ts:322-330
+        for (Body &b : w.bodies) {
+            if (b.motion == STATIC || b.sleeping) continue;
+            update_pos_from_com(b);
+            set_transform(b);
+        }
+        for (Island &is : w.islands) check_island_sleep(w, is, dt);
+    }
+    for (Body &b : w.bodies) {
+        if (b.motion == STATIC || b.sleeping) continue;
+        b.force = {0, 0, 0};
+        b.torque = {0, 0, 0};
+    }
+}
+
+}  // namespace orc
+
+// ===========================================================================
+// C ABI used by the Python test harness (ctypes).
+// ===========================================================================
+using namespace orc;
+
+extern "C" {
+
+// Body description: one row of doubles per body, layout shared with the
+// Python scene builder (crashcat_gb300/scenes.py BODY_FIELDS).
+enum {
+    F_SHAPE = 0,       // 0 sphere, 1 box
+    F_P0 = 1,          // shape params (box hx,hy,hz,convexRadius ; sphere r)
+    F_DENSITY = 5,
+    F_MOTION = 6,
+    F_POS = 7,
+    F_QUAT = 10,
+    F_LINVEL = 14,
+    F_ANGVEL = 17,
+    F_FRICTION = 20,
+    F_RESTITUTION = 21,
+    F_LAYER = 22,
+    F_GRAVITY_FACTOR = 23,
+    F_LIN_DAMP = 24,
+    F_ANG_DAMP = 25,
+    F_ALLOW_SLEEP = 26,
+    F_WORLD = 27,
+    F_COUNT = 28
+};
+
+void *orc_world_create(const double *settings, int n_obj, const int *obj_to_bp, int n_bp, const uint8_t *obj_pairs,
+                       const uint8_t *obj_vs_bp, const uint8_t *bp_pairs) {
+    World *w = new World();
+    Settings &s = w->s;
+    s.gravity = {settings[0], settings[1], settings[2]};
+    s.speculativeContactDistance = settings[3];
+    s.manifoldTolerance = settings[4];
+    s.collisionTolerance = settings[5];
+    s.penetrationTolerance = settings[6];
+    s.normalCosMaxDeltaRotation = settings[7];
+    s.preserveLambdaMaxDistSq = settings[8];
+    s.velocityIterations = (int)settings[9];
+    s.positionIterations = (int)settings[10];
+    s.warmStarting = settings[11] != 0;
+    s.penetrationSlop = settings[12];
+    s.baumgarteFactor = settings[13];
+    s.maxPenetrationDistance = settings[14];
+    s.minVelocityForRestitution = settings[15];
+    s.allowSleeping = settings[16] != 0;
+    s.timeBeforeSleep = settings[17];
+    s.pointVelocitySleepThreshold = settings[18];
+    s.gravityEnabled = settings[19] != 0;
+    w->layers.nObj = n_obj;
+    w->layers.nBp = n_bp;
+    w->layers.objToBp.assign(obj_to_bp, obj_to_bp + n_obj);
+    w->layers.objPairs.assign(obj_pairs, obj_pairs + n_obj * n_obj);
+    w->layers.objVsBp.assign(obj_vs_bp, obj_vs_bp + n_obj * n_bp);
+    w->layers.bpPairs.assign(bp_pairs, bp_pairs + n_bp * n_bp);
+    return w;
+}
+
+void orc_world_destroy(void *wp) { delete (World *)wp; }
+
+// rigidBody.create rigid-body.ts:390-434 for each row
+int orc_add_bodies(void *wp, const double *rows, int n) {
+    World &w = *(World *)wp;
+    for (int i = 0; i < n; i++) {
+        const double *r = rows + (size_t)i * F_COUNT;
+        Body b;
+        b.index = (int)w.bodies.size();
+        int seq = w.nextSequence;
+        w.nextSequence = (w.nextSequence + 1) & ((1 << 20) - 1);
+        b.id = (int64_t)b.index + (int64_t)seq * 4294967296LL;
+        Shape &s = b.shape;
+        s.type = (int)r[F_SHAPE];
+        s.density = r[F_DENSITY];
+        if (s.type == SHAPE_BOX) {
+            s.half_extents = {r[F_P0], r[F_P0 + 1], r[F_P0 + 2]};
+            s.convex_radius = r[F_P0 + 3];
+            s.aabb = {neg(s.half_extents), s.half_extents};
+        } else if (s.type == SHAPE_SPHERE) {
+            s.radius = r[F_P0];
+            s.aabb = {{-s.radius, -s.radius, -s.radius}, {s.radius, s.radius, s.radius}};
+        } else {
+            return -1;
+        }
+        s.com = {0, 0, 0};
+        b.position = {r[F_POS], r[F_POS + 1], r[F_POS + 2]};
+        b.quat = {r[F_QUAT], r[F_QUAT + 1], r[F_QUAT + 2], r[F_QUAT + 3]};
+        b.motion = (int)r[F_MOTION];
+        b.linvel = {r[F_LINVEL], r[F_LINVEL + 1], r[F_LINVEL + 2]};
+        b.angvel = {r[F_ANGVEL], r[F_ANGVEL + 1], r[F_ANGVEL + 2]};
+        b.friction = r[F_FRICTION];
+        b.restitution = r[F_RESTITUTION];
+        b.objectLayer = (int)r[F_LAYER];
+        b.gravityFactor = r[F_GRAVITY_FACTOR];
+        b.linDamp = r[F_LIN_DAMP];
+        b.angDamp = r[F_ANG_DAMP];
+        b.allowSleeping = r[F_ALLOW_SLEEP] != 0;
+        double mass;
+        V3 idiag;
+        shape_mass(s, mass, idiag);
+        if (b.motion != STATIC) set_mass_properties(b, mass, idiag);
+        update_com(b);
+        update_aabb(b);
+        w.bodies.push_back(b);
+        Body &bb = w.bodies.back();
+        if (bb.motion == DYNAMIC) reset_sleep_timer(bb);
+        if (bb.motion != STATIC && !bb.sleeping) add_active(w, bb);
+    }
+    return 0;
+}
+
+int orc_body_count(void *wp) { return (int)((World *)wp)->bodies.size(); }
+
+// state rows: pos3 quat4 linvel3 angvel3 com3 sleeping1 = 17 doubles
+int orc_get_state(void *wp, double *out) {
+    World &w = *(World *)wp;
+    for (size_t i = 0; i < w.bodies.size(); i++) {
+        const Body &b = w.bodies[i];
+        double *o = out + i * 17;
+        o[0] = b.position.x;
+        o[1] = b.position.y;
+        o[2] = b.position.z;
+        o[3] = b.quat.x;
+        o[4] = b.quat.y;
+        o[5] = b.quat.z;
+        o[6] = b.quat.w;
+        o[7] = b.linvel.x;
+        o[8] = b.linvel.y;
+        o[9] = b.linvel.z;
+        o[10] = b.angvel.x;
+        o[11] = b.angvel.y;
+        o[12] = b.angvel.z;
+        o[13] = b.com.x;
+        o[14] = b.com.y;
+        o[15] = b.com.z;
+        o[16] = b.sleeping ? 1.0 : 0.0;
+    }
+    return 0;
+}
+
+// Overwrite pose and velocity (rigidBody.setTransform + setLinearVelocity /
+// setAngularVelocity without waking semantics beyond the reference's own).
+int orc_set_state(void *wp, const double *in) {
+    World &w = *(World *)wp;
+    for (size_t i = 0; i < w.bodies.size(); i++) {
+        Body &b = w.bodies[i];
+        const double *o = in + i * 17;
+        b.position = {o[0], o[1], o[2]};
+        b.quat = {o[3], o[4], o[5], o[6]};
+        b.linvel = {o[7], o[8], o[9]};
+        b.angvel = {o[10], o[11], o[12]};
+        set_transform(b);
+    }
+    return 0;
+}
+
+int orc_step(void *wp, double dt, int n_steps) {
+    World &w = *(World *)wp;
+    for (int i = 0; i < n_steps; i++) step(w, dt);
+    return 0;
+}
+
+int orc_pair_count(void *wp) { return (int)((World *)wp)->pairs.size(); }
+int orc_get_pairs(void *wp, int *out) {
+    World &w = *(World *)wp;
+    for (size_t i = 0; i < w.pairs.size(); i++) {
+        out[2 * i] = w.pairs[i].first;
+        out[2 * i + 1] = w.pairs[i].second;
+    }
+    return 0;
+}
+
+// AABBs (min3 max3) per body
+int orc_get_aabbs(void *wp, double *out) {
+    World &w = *(World *)wp;
+    for (size_t i = 0; i < w.bodies.size(); i++) {
+        const Box3 &a = w.bodies[i].aabb;
+        double *o = out + 6 * i;
+        o[0] = a.mn.x;
+        o[1] = a.mn.y;
+        o[2] = a.mn.z;
+        o[3] = a.mx.x;
+        o[4] = a.mx.y;
+        o[5] = a.mx.z;
+    }
+    return 0;
+}
+
+// Manifolds created during the last step (after id ordering).  Row layout:
+// bodyA, bodyB, n, normal3, depth, then 4 x (pointA3 pointB3) world space = 32 doubles.
+int orc_manifold_count(void *wp) { return (int)((World *)wp)->manifolds.size(); }
+int orc_get_manifolds(void *wp, double *out) {
+    World &w = *(World *)wp;
+    for (size_t i = 0; i < w.manifolds.size(); i++) {
+        const Manifold &m = w.manifolds[i];
+        double *o = out + 32 * i;
+        o[0] = w.manifoldBodies[i].first;
+        o[1] = w.manifoldBodies[i].second;
+        o[2] = m.n;
+        o[3] = m.normal.x;
+        o[4] = m.normal.y;
+        o[5] = m.normal.z;
+        o[6] = m.depth;
+        o[7] = 0;
+        for (int k = 0; k < 4; k++) {
+            double *p = o + 8 + 6 * k;
+            if (k < m.n) {
+                V3 a = add(m.base, m.relA[k]), b = add(m.base, m.relB[k]);
+                p[0] = a.x;
+                p[1] = a.y;
+                p[2] = a.z;
+                p[3] = b.x;
+                p[4] = b.y;
+                p[5] = b.z;
+            } else {
+                for (int j = 0; j < 6; j++) p[j] = 0;
+            }
+        }
+    }
+    return 0;
+}
+
+// Island statistics of the last step: number of islands with contacts.
+int orc_island_count(void *wp) { return (int)((World *)wp)->islands.size(); }
+
+// ---- unit-level entry points for the known-answer tests -------------------
+// Faces are passed as n vertices (xyz doubles).  Returns the output vertex count.
+int orc_clip_poly_vs_plane(const double *poly, int n, const double *origin, const double *normal, double *out) {
+    Face in, o;
+    in.n = n;
+    for (int i = 0; i < n; i++) in.v[i] = {poly[3 * i], poly[3 * i + 1], poly[3 * i + 2]};
+    clip_poly_vs_plane(o, in, {origin[0], origin[1], origin[2]}, {normal[0], normal[1], normal[2]});
+    for (int i = 0; i < o.n; i++) {
+        out[3 * i] = o.v[i].x;
+        out[3 * i + 1] = o.v[i].y;
+        out[3 * i + 2] = o.v[i].z;
+    }
+    return o.n;
+}
+int orc_clip_poly_vs_poly(const double *poly, int n, const double *clip, int m, const double *normal, double *out) {
+    Face a, c, o;
+    a.n = n;
+    for (int i = 0; i < n; i++) a.v[i] = {poly[3 * i], poly[3 * i + 1], poly[3 * i + 2]};
+    c.n = m;
+    for (int i = 0; i < m; i++) c.v[i] = {clip[3 * i], clip[3 * i + 1], clip[3 * i + 2]};
+    clip_poly_vs_poly(o, a, c, {normal[0], normal[1], normal[2]});
+    for (int i = 0; i < o.n; i++) {
+        out[3 * i] = o.v[i].x;
+        out[3 * i + 1] = o.v[i].y;
+        out[3 * i + 2] = o.v[i].z;
+    }
+    return o.n;
+}
+// manifoldBetweenTwoFaces with baseOffset 0; writes pointsA then pointsB (n x 3 each).
+int orc_manifold_between_faces(const double *cp1, const double *cp2, const double *axis, double maxDist,
+                               const double *f1, int n1, const double *f2, int n2, double *outA, double *outB) {
+    Face a, b;
+    a.n = n1;
+    b.n = n2;
+    for (int i = 0; i < n1; i++) a.v[i] = {f1[3 * i], f1[3 * i + 1], f1[3 * i + 2]};
+    for (int i = 0; i < n2; i++) b.v[i] = {f2[3 * i], f2[3 * i + 1], f2[3 * i + 2]};
+    Manifold m;
+    m.base = {0, 0, 0};
+    manifold_between_faces(m, {cp1[0], cp1[1], cp1[2]}, {cp2[0], cp2[1], cp2[2]}, {axis[0], axis[1], axis[2]},
+                           maxDist, a, b);
+    for (int i = 0; i < m.n; i++) {
+        outA[3 * i] = m.relA[i].x;
+        outA[3 * i + 1] = m.relA[i].y;
+        outA[3 * i + 2] = m.relA[i].z;
+        outB[3 * i] = m.relB[i].x;
+        outB[3 * i + 1] = m.relB[i].y;
+        outB[3 * i + 2] = m.relB[i].z;
+    }
+    return m.n;
+}
+// pruneContactPoints on n points (relative to base 0); returns the kept count, rewrites in place.
+int orc_prune_contact_points(double *ptsA, double *ptsB, int n, const double *axis) {
+    Manifold m;
+    m.n = n;
+    for (int i = 0; i < n; i++) {
+        m.relA[i] = {ptsA[3 * i], ptsA[3 * i + 1], ptsA[3 * i + 2]};
+        m.relB[i] = {ptsB[3 * i], ptsB[3 * i + 1], ptsB[3 * i + 2]};
+    }
+    prune_contact_points(m, {axis[0], axis[1], axis[2]});
+    for (int i = 0; i < m.n; i++) {
+        ptsA[3 * i] = m.relA[i].x;
+        ptsA[3 * i + 1] = m.relA[i].y;
+        ptsA[3 * i + 2] = m.relA[i].z;
+        ptsB[3 * i] = m.relB[i].x;
+        ptsB[3 * i + 1] = m.relB[i].y;
+        ptsB[3 * i + 2] = m.relB[i].z;
+    }
+    return m.n;
+}
+// Barycentric coordinates (u, v, w, valid) of the closest point to the origin.
+void orc_barycentric(const double *a, const double *b, const double *c, int n, double *out) {
+    Bary r;
+    if (n == 2)
+        r = bary2({a[0], a[1], a[2]}, {b[0], b[1], b[2]}, 1e-10);
+    else
+        r = bary3({a[0], a[1], a[2]}, {b[0], b[1], b[2]}, {c[0], c[1], c[2]}, 1e-10);
+    out[0] = r.u;
+    out[1] = r.v;
+    out[2] = r.w;
+    out[3] = r.valid ? 1 : 0;
+}
+// Single shape pair collision (world space).  shape rows as in orc_add_bodies (F_SHAPE..F_P0+3).
+// out: found, pointA3, pointB3, axis3, penetration, faceA n, faceB n  (13 doubles)
+int orc_collide_pair(const double *rowA, const double *rowB, double maxSep, double *out) {
+    Shape s[2];
+    V3 p[2];
+    Q4 q[2];
+    const double *rows[2] = {rowA, rowB};
+    for (int k = 0; k < 2; k++) {
+        const double *r = rows[k];
+        s[k].type = (int)r[F_SHAPE];
+        if (s[k].type == SHAPE_BOX) {
+            s[k].half_extents = {r[F_P0], r[F_P0 + 1], r[F_P0 + 2]};
+            s[k].convex_radius = r[F_P0 + 3];
+        } else {
+            s[k].radius = r[F_P0];
+        }
+        p[k] = {r[F_POS], r[F_POS + 1], r[F_POS + 2]};
+        q[k] = {r[F_QUAT], r[F_QUAT + 1], r[F_QUAT + 2], r[F_QUAT + 3]};
+    }
+    CollideSettings cs;
+    cs.maxSeparation = maxSep;
+    Hit h;
+    bool f = collide_shapes(h, cs, s[0], p[0], q[0], s[1], p[1], q[1]);
+    out[0] = f ? 1 : 0;
+    out[1] = h.pa.x;
+    out[2] = h.pa.y;
+    out[3] = h.pa.z;
+    out[4] = h.pb.x;
+    out[5] = h.pb.y;
+    out[6] = h.pb.z;
+    out[7] = h.axis.x;
+    out[8] = h.axis.y;
+    out[9] = h.axis.z;
+    out[10] = h.penetration;
+    out[11] = h.faceA.n;
+    out[12] = h.faceB.n;
+    return f ? 1 : 0;
+}
+// World-space inverse inertia (3x3 column-major) for a body row at its orientation.
+void orc_inverse_inertia(const double *row, double *out9) {
+    Body b;
+    Shape &s = b.shape;
+    s.type = (int)row[F_SHAPE];
+    s.density = row[F_DENSITY];
+    if (s.type == SHAPE_BOX)
+        s.half_extents = {row[F_P0], row[F_P0 + 1], row[F_P0 + 2]};
+    else
+        s.radius = row[F_P0];
+    double mass;
+    V3 d;
+    shape_mass(s, mass, d);
+    set_mass_properties(b, mass, d);
+    b.quat = {row[F_QUAT], row[F_QUAT + 1], row[F_QUAT + 2], row[F_QUAT + 3]};
+    M4 I = inv_inertia_for_rotation(b, mat4_from_quat(b.quat));
+    int k = 0;
+    for (int c = 0; c < 3; c++)
+        for (int r = 0; r < 3; r++) out9[k++] = I.m[c * 4 + r];
+}
+
+}  // extern "C"

@@ -1,0 +1,1473 @@
+// FP64 restatement of crashcat's convex collision pipeline for the CPU oracle.
+//
+// TEST INFRASTRUCTURE ONLY (parity oracle, never part of the GPU library).
+//
+// Each function cites the reference function it follows; the arithmetic is
+// kept in the reference's operation order so that the oracle reproduces the
+// reference's IEEE-754 double results (compiled with -ffp-contract=off).
+#pragma once
+#include <algorithm>
+#include <cstring>
+#include <limits>
+#include <vector>
+
+#include "oracle_math.h"
+
+namespace orc {
+
+constexpr double DEFAULT_CONVEX_RADIUS = 0.05;  // src/collision/support.ts:5
+constexpr uint32_t EMPTY_SUB_SHAPE_ID = 0xffffffffu;  // src/body/sub-shape.ts:4
+
+enum ShapeType : int { SHAPE_SPHERE = 0, SHAPE_BOX = 1, SHAPE_CAPSULE = 2 };
+
+// Shape data (src/shapes/box.ts:38-70, src/shapes/sphere.ts, src/shapes/capsule.ts)
+struct Shape {
+    int type = SHAPE_BOX;
+    V3 half_extents;          // box
+    double convex_radius = 0;  // box
+    double radius = 0;         // sphere / capsule
+    double half_height = 0;    // capsule (segment along Y)
+    double density = 1000;
+    V3 com;                    // shape-local centre of mass
+    Box3 aabb;                 // shape-local bounds
+};
+
+// ----------------------------------------------------------------------------
+// Support functions (src/collision/support.ts, src/shapes/sphere.ts:173-266)
+// ----------------------------------------------------------------------------
+enum SupportMode { INCLUDE_CONVEX_RADIUS = 0, EXCLUDE_CONVEX_RADIUS = 1 };
+enum SupportKind { SUP_BOX, SUP_SPHERE_POINT, SUP_SPHERE_SURFACE, SUP_CAPSULE_SEGMENT, SUP_CAPSULE_SURFACE };
+
+struct Support {
+    int kind = SUP_BOX;
+    V3 he;                    // box half extents (already shrunk if EXCLUDE)
+    double radius = 0;        // sphere/capsule radius used by the surface form
+    double half_height = 0;   // capsule
+    double convex_radius = 0;  // reported convex radius
+    bool transformed = false;  // TransformedSupport (support.ts:228-278)
+    M4 m;
+    bool add_radius = false;  // AddConvexRadiusSupport (support.ts:282-315)
+    double add_r = 0;
+
+    V3 inner(V3 d) const {
+        switch (kind) {
+            case SUP_BOX:  // boxGetSupport support.ts:323-327
+                return {d.x >= 0 ? he.x : -he.x, d.y >= 0 ? he.y : -he.y, d.z >= 0 ? he.z : -he.z};
+            case SUP_SPHERE_POINT:  // sphere.ts:184-187
+                return {0, 0, 0};
+            case SUP_SPHERE_SURFACE: {  // sphere.ts:213-229
+                double l = d.x * d.x + d.y * d.y + d.z * d.z;
+                if (l > 0) {
+                    double s = radius / std::sqrt(l);
+                    return {d.x * s, d.y * s, d.z * s};
+                }
+                return {0, 0, 0};
+            }
+            case SUP_CAPSULE_SEGMENT:  // capsule.ts: segment +-h on Y
+                return {0, d.y > 0 ? half_height : -half_height, 0};
+            case SUP_CAPSULE_SURFACE: {
+                double l = d.x * d.x + d.y * d.y + d.z * d.z;
+                V3 o{0, d.y > 0 ? half_height : -half_height, 0};
+                if (l > 0) {
+                    double s = radius / std::sqrt(l);
+                    o.x += d.x * s;
+                    o.y += d.y * s;
+                    o.z += d.z * s;
+                }
+                return o;
+            }
+        }
+        return {0, 0, 0};
+    }
+    V3 get(V3 d) const {
+        V3 o;
+        if (transformed) {
+            // transformedGetSupport support.ts:237-258
+            V3 ld{m.m[0] * d.x + m.m[1] * d.y + m.m[2] * d.z, m.m[4] * d.x + m.m[5] * d.y + m.m[6] * d.z,
+                  m.m[8] * d.x + m.m[9] * d.y + m.m[10] * d.z};
+            V3 s = inner(ld);
+            o = {m.m[0] * s.x + m.m[4] * s.y + m.m[8] * s.z + m.m[12],
+                 m.m[1] * s.x + m.m[5] * s.y + m.m[9] * s.z + m.m[13],
+                 m.m[2] * s.x + m.m[6] * s.y + m.m[10] * s.z + m.m[14]};
+        } else {
+            o = inner(d);
+        }
+        if (add_radius) {
+            // addConvexRadiusGetSupport support.ts:288-301
+            double l = d.x * d.x + d.y * d.y + d.z * d.z;
+            if (l > 0) {
+                double s = add_r / std::sqrt(l);
+                o.x += d.x * s;
+                o.y += d.y * s;
+                o.z += d.z * s;
+            }
+        }
+        return o;
+    }
+};
+
+// getShapeSupportFunction for unit scale (support.ts:57-69, setBoxSupport support.ts:339-370,
+// getSphereSupportFunction sphere.ts:256-266)
+inline Support make_support(const Shape &s, SupportMode mode) {
+    Support o;
+    if (s.type == SHAPE_BOX) {
+        o.kind = SUP_BOX;
+        if (mode == EXCLUDE_CONVEX_RADIUS) {
+            double cr = std::min(s.convex_radius * 1.0, DEFAULT_CONVEX_RADIUS);
+            o.he = {std::max(0.0, s.half_extents.x - cr), std::max(0.0, s.half_extents.y - cr),
+                    std::max(0.0, s.half_extents.z - cr)};
+            o.convex_radius = cr;
+        } else {
+            o.he = s.half_extents;
+            o.convex_radius = 0;
+        }
+    } else if (s.type == SHAPE_SPHERE) {
+        if (mode == INCLUDE_CONVEX_RADIUS) {
+            o.kind = SUP_SPHERE_SURFACE;
+            o.radius = s.radius;
+            o.convex_radius = 0;
+        } else {
+            o.kind = SUP_SPHERE_POINT;
+            o.convex_radius = s.radius;
+        }
+    } else {
+        o.half_height = s.half_height;
+        if (mode == INCLUDE_CONVEX_RADIUS) {
+            o.kind = SUP_CAPSULE_SURFACE;
+            o.radius = s.radius;
+            o.convex_radius = 0;
+        } else {
+            o.kind = SUP_CAPSULE_SEGMENT;
+            o.convex_radius = s.radius;
+        }
+    }
+    return o;
+}
+
+// ----------------------------------------------------------------------------
+// Simplex + closest points (src/collision/simplex.ts, closest-points.ts, gjk.ts)
+// ----------------------------------------------------------------------------
+struct SimplexPoint {
+    V3 y, p, q;
+};
+struct Simplex {
+    SimplexPoint pts[4];
+    int size = 0;
+};
+
+struct Bary {
+    double u = 0, v = 0, w = 0;
+    bool valid = false;
+};
+
+// computeBarycentricCoordinates2d closest-points.ts:19-47
+inline Bary bary2(V3 a, V3 b, double sqtol) {
+    Bary o;
+    V3 ab = sub(b, a);
+    double den = ab.x * ab.x + ab.y * ab.y + ab.z * ab.z;
+    if (den < sqtol) {
+        if (a.x * a.x + a.y * a.y + a.z * a.z < b.x * b.x + b.y * b.y + b.z * b.z) {
+            o.u = 1.0;
+            o.v = 0.0;
+        } else {
+            o.u = 0.0;
+            o.v = 1.0;
+        }
+        o.valid = false;
+        return o;
+    }
+    o.v = -(a.x * ab.x + a.y * ab.y + a.z * ab.z) / den;
+    o.u = 1.0 - o.v;
+    o.valid = true;
+    return o;
+}
+
+// computeBarycentricCoordinates3d closest-points.ts:51-152
+inline Bary bary3(V3 a, V3 b, V3 c, double sqtol) {
+    Bary o;
+    V3 ab = sub(b, a), ac = sub(c, a), bc = sub(c, b);
+    double d00 = ab.x * ab.x + ab.y * ab.y + ab.z * ab.z;
+    double d11 = ac.x * ac.x + ac.y * ac.y + ac.z * ac.z;
+    double d22 = bc.x * bc.x + bc.y * bc.y + bc.z * bc.z;
+    if (d00 <= d22) {
+        double d01 = ab.x * ac.x + ab.y * ac.y + ab.z * ac.z;
+        double den = d00 * d11 - d01 * d01;
+        if (std::fabs(den) < 1.0e-12) {
+            if (d00 > d11) {
+                Bary t = bary2(a, b, sqtol);
+                o.u = t.u;
+                o.v = t.v;
+                o.w = 0.0;
+            } else {
+                Bary t = bary2(a, c, sqtol);
+                o.u = t.u;
+                o.w = t.v;
+                o.v = 0.0;
+            }
+            o.valid = false;
+            return o;
+        }
+        double a0 = a.x * ab.x + a.y * ab.y + a.z * ab.z;
+        double a1 = a.x * ac.x + a.y * ac.y + a.z * ac.z;
+        o.v = (d01 * a1 - d11 * a0) / den;
+        o.w = (d01 * a0 - d00 * a1) / den;
+        o.u = 1.0 - o.v - o.w;
+    } else {
+        double d12 = ac.x * bc.x + ac.y * bc.y + ac.z * bc.z;
+        double den = d11 * d22 - d12 * d12;
+        if (std::fabs(den) < 1.0e-12) {
+            if (d11 > d22) {
+                Bary t = bary2(a, c, sqtol);
+                o.u = t.u;
+                o.w = t.v;
+                o.v = 0.0;
+            } else {
+                Bary t = bary2(b, c, sqtol);
+                o.v = t.u;
+                o.w = t.v;
+                o.u = 0.0;
+            }
+            o.valid = false;
+            return o;
+        }
+        double c1 = c.x * ac.x + c.y * ac.y + c.z * ac.z;
+        double c2 = c.x * bc.x + c.y * bc.y + c.z * bc.z;
+        o.u = (d22 * c1 - d12 * c2) / den;
+        o.v = (d11 * c2 - d12 * c1) / den;
+        o.w = 1.0 - o.u - o.v;
+    }
+    o.valid = true;
+    return o;
+}
+
+struct ClosestPoint {
+    V3 point;
+    int set = 0;
+};
+
+inline double clamp01(double v) { return v < 0.0 ? 0.0 : (v > 1.0 ? 1.0 : v); }
+
+// computeClosestPointOnLine gjk.ts:33-55
+inline ClosestPoint closest_on_line(V3 a, V3 b, double sqtol) {
+    Bary br = bary2(a, b, sqtol);
+    ClosestPoint o;
+    if (br.v <= 0.0) {
+        o.point = a;
+        o.set = 0b0001;
+    } else if (br.u <= 0.0) {
+        o.point = b;
+        o.set = 0b0010;
+    } else {
+        o.point = {a.x * br.u + b.x * br.v, a.y * br.u + b.y * br.v, a.z * br.u + b.z * br.v};
+        o.set = 0b0011;
+    }
+    return o;
+}
+
+// computeClosestPointOnTriangle gjk.ts:57-350
+inline ClosestPoint closest_on_triangle(V3 inA, V3 inB, V3 inC, bool mustIncludeC, double sqtol) {
+    ClosestPoint out;
+    V3 ac0 = sub(inC, inA), bc0 = sub(inC, inB);
+    bool swapAC = bc0.x * bc0.x + bc0.y * bc0.y + bc0.z * bc0.z < ac0.x * ac0.x + ac0.y * ac0.y + ac0.z * ac0.z;
+    V3 a = swapAC ? inC : inA;
+    V3 c = swapAC ? inA : inC;
+    V3 ab = sub(inB, a);
+    V3 ac = sub(c, a);
+    V3 n{ab.y * ac.z - ab.z * ac.y, ab.z * ac.x - ab.x * ac.z, ab.x * ac.y - ab.y * ac.x};
+    double nls = n.x * n.x + n.y * n.y + n.z * n.z;
+    if (nls < 1.0e-10) {
+        int cs = 0b0100;
+        V3 cp = inC;
+        double best = inC.x * inC.x + inC.y * inC.y + inC.z * inC.z;
+        if (!mustIncludeC) {
+            double al = inA.x * inA.x + inA.y * inA.y + inA.z * inA.z;
+            if (al < best) {
+                cs = 0b0001;
+                cp = inA;
+                best = al;
+            }
+            double bl = inB.x * inB.x + inB.y * inB.y + inB.z * inB.z;
+            if (bl < best) {
+                cs = 0b0010;
+                cp = inB;
+                best = bl;
+            }
+        }
+        {
+            V3 ac2 = sub(c, a);
+            double acl = ac2.x * ac2.x + ac2.y * ac2.y + ac2.z * ac2.z;
+            if (acl > sqtol) {
+                double v = clamp01(-(a.x * ac2.x + a.y * ac2.y + a.z * ac2.z) / acl);
+                V3 q{a.x + ac2.x * v, a.y + ac2.y * v, a.z + ac2.z * v};
+                double d = q.x * q.x + q.y * q.y + q.z * q.z;
+                if (d < best) {
+                    cs = 0b0101;
+                    cp = q;
+                    best = d;
+                }
+            }
+        }
+        {
+            V3 bc2 = sub(inC, inB);
+            double bcl = bc2.x * bc2.x + bc2.y * bc2.y + bc2.z * bc2.z;
+            if (bcl > sqtol) {
+                double v = clamp01(-(inB.x * bc2.x + inB.y * bc2.y + inB.z * bc2.z) / bcl);
+                V3 q{inB.x + bc2.x * v, inB.y + bc2.y * v, inB.z + bc2.z * v};
+                double d = q.x * q.x + q.y * q.y + q.z * q.z;
+                if (d < best) {
+                    cs = 0b0110;
+                    cp = q;
+                    best = d;
+                }
+            }
+        }
+        if (!mustIncludeC) {
+            V3 ab2 = sub(inB, inA);
+            double abl = ab2.x * ab2.x + ab2.y * ab2.y + ab2.z * ab2.z;
+            if (abl > sqtol) {
+                double v = clamp01(-(inA.x * ab2.x + inA.y * ab2.y + inA.z * ab2.z) / abl);
+                V3 q{inA.x + ab2.x * v, inA.y + ab2.y * v, inA.z + ab2.z * v};
+                double d = q.x * q.x + q.y * q.y + q.z * q.z;
+                if (d < best) {
+                    cs = 0b0011;
+                    cp = q;
+                }
+            }
+        }
+        out.set = cs;
+        out.point = cp;
+        return out;
+    }
+    V3 ap{-a.x, -a.y, -a.z};
+    double d1 = ab.x * ap.x + ab.y * ap.y + ab.z * ap.z;
+    double d2 = ac.x * ap.x + ac.y * ap.y + ac.z * ap.z;
+    if (d1 <= 0.0 && d2 <= 0.0) {
+        out.set = swapAC ? 0b0100 : 0b0001;
+        out.point = a;
+        return out;
+    }
+    V3 bp{-inB.x, -inB.y, -inB.z};
+    double d3 = ab.x * bp.x + ab.y * bp.y + ab.z * bp.z;
+    double d4 = ac.x * bp.x + ac.y * bp.y + ac.z * bp.z;
+    if (d3 >= 0.0 && d4 <= d3) {
+        out.set = 0b0010;
+        out.point = inB;
+        return out;
+    }
+    if (d1 * d4 <= d3 * d2 && d1 >= 0.0 && d3 <= 0.0) {
+        double v = d1 / (d1 - d3);
+        out.set = swapAC ? 0b0110 : 0b0011;
+        out.point = {a.x + ab.x * v, a.y + ab.y * v, a.z + ab.z * v};
+        return out;
+    }
+    V3 cpp{-c.x, -c.y, -c.z};
+    double d5 = ab.x * cpp.x + ab.y * cpp.y + ab.z * cpp.z;
+    double d6 = ac.x * cpp.x + ac.y * cpp.y + ac.z * cpp.z;
+    if (d6 >= 0.0 && d5 <= d6) {
+        out.set = swapAC ? 0b0001 : 0b0100;
+        out.point = c;
+        return out;
+    }
+    if (d5 * d2 <= d1 * d6 && d2 >= 0.0 && d6 <= 0.0) {
+        double w = d2 / (d2 - d6);
+        out.set = 0b0101;
+        out.point = {a.x + ac.x * w, a.y + ac.y * w, a.z + ac.z * w};
+        return out;
+    }
+    double d43 = d4 - d3;
+    double d56 = d5 - d6;
+    if (d3 * d6 <= d5 * d4 && d43 >= 0.0 && d56 >= 0.0) {
+        double w = d43 / (d43 + d56);
+        out.set = swapAC ? 0b0011 : 0b0110;
+        V3 t = sub(c, inB);
+        out.point = {inB.x + t.x * w, inB.y + t.y * w, inB.z + t.z * w};
+        return out;
+    }
+    out.set = 0b0111;
+    V3 t{a.x + inB.x + c.x, a.y + inB.y + c.y, a.z + inB.z + c.z};
+    double s = (t.x * n.x + t.y * n.y + t.z * n.z) / (3 * nls);
+    out.point = {n.x * s, n.y * s, n.z * s};
+    return out;
+}
+
+// isOriginOutsideOfTrianglePlanes gjk.ts:305-395
+inline void origin_outside_planes(int out[4], V3 a, V3 b, V3 c, V3 d, double tol) {
+    V3 ab = sub(b, a), ac = sub(c, a), ad = sub(d, a), bd = sub(d, b), bc = sub(c, b);
+    V3 abac{ab.y * ac.z - ab.z * ac.y, ab.z * ac.x - ab.x * ac.z, ab.x * ac.y - ab.y * ac.x};
+    V3 acad{ac.y * ad.z - ac.z * ad.y, ac.z * ad.x - ac.x * ad.z, ac.x * ad.y - ac.y * ad.x};
+    V3 adab{ad.y * ab.z - ad.z * ab.y, ad.z * ab.x - ad.x * ab.z, ad.x * ab.y - ad.y * ab.x};
+    V3 bdbc{bd.y * bc.z - bd.z * bc.y, bd.z * bc.x - bd.x * bc.z, bd.x * bc.y - bd.y * bc.x};
+    double spx = a.x * abac.x + a.y * abac.y + a.z * abac.z;
+    double spy = a.x * acad.x + a.y * acad.y + a.z * acad.z;
+    double spz = a.x * adab.x + a.y * adab.y + a.z * adab.z;
+    double spw = b.x * bdbc.x + b.y * bdbc.y + b.z * bdbc.z;
+    double sdx = ad.x * abac.x + ad.y * abac.y + ad.z * abac.z;
+    double sdy = ab.x * acad.x + ab.y * acad.y + ab.z * acad.z;
+    double sdz = ac.x * adab.x + ac.y * adab.y + ac.z * adab.z;
+    double sdw = -(ab.x * bdbc.x + ab.y * bdbc.y + ab.z * bdbc.z);
+    if (sdx > 0 && sdy > 0 && sdz > 0 && sdw > 0) {
+        out[0] = spx >= -tol;
+        out[1] = spy >= -tol;
+        out[2] = spz >= -tol;
+        out[3] = spw >= -tol;
+        return;
+    }
+    if (sdx < 0 && sdy < 0 && sdz < 0 && sdw < 0) {
+        out[0] = spx <= tol;
+        out[1] = spy <= tol;
+        out[2] = spz <= tol;
+        out[3] = spw <= tol;
+        return;
+    }
+    out[0] = out[1] = out[2] = out[3] = 1;
+}
+
+// computeClosestPointOnTetrahedron gjk.ts:399-488
+inline ClosestPoint closest_on_tetra(V3 a, V3 b, V3 c, V3 d, bool mustIncludeD, double tol) {
+    double sqtol = tol * tol;
+    ClosestPoint out;
+    out.set = 0b1111;
+    out.point = {0, 0, 0};
+    double best = std::numeric_limits<double>::infinity();
+    int o[4];
+    origin_outside_planes(o, a, b, c, d, tol);
+    if (o[0]) {
+        if (mustIncludeD) {
+            out.set = 0b0001;
+            out.point = a;
+        } else {
+            out = closest_on_triangle(a, b, c, false, sqtol);
+        }
+        best = lensq(out.point);
+    }
+    if (o[1]) {
+        ClosestPoint t = closest_on_triangle(a, c, d, mustIncludeD, sqtol);
+        double ds = lensq(t.point);
+        if (ds < best) {
+            best = ds;
+            out.point = t.point;
+            out.set = (t.set & 0b0001) + ((t.set & 0b0110) << 1);
+        }
+    }
+    if (o[2]) {
+        ClosestPoint t = closest_on_triangle(a, b, d, mustIncludeD, sqtol);
+        double ds = lensq(t.point);
+        if (ds < best) {
+            best = ds;
+            out.point = t.point;
+            out.set = (t.set & 0b0011) + ((t.set & 0b0100) << 1);
+        }
+    }
+    if (o[3]) {
+        ClosestPoint t = closest_on_triangle(b, c, d, mustIncludeD, sqtol);
+        double ds = lensq(t.point);
+        if (ds < best) {
+            out.point = t.point;
+            out.set = t.set << 1;
+        }
+    }
+    return out;
+}
+
+constexpr double GJK_TOLERANCE = 1e-5;  // gjk.ts:489
+constexpr int GJK_MAX_ITERATIONS = 100;  // gjk.ts:490
+
+struct ClosestToSimplex {
+    V3 point;
+    double sqdist = 0;
+    int set = 0;
+    bool found = false;
+};
+
+// computeClosestPointToSimplex gjk.ts:524-596
+inline bool closest_to_simplex(ClosestToSimplex &r, double prev, bool lastPart, const Simplex &s) {
+    ClosestPoint cp;
+    switch (s.size) {
+        case 1:
+            cp.set = 0b0001;
+            cp.point = s.pts[0].y;
+            break;
+        case 2:
+            cp = closest_on_line(s.pts[0].y, s.pts[1].y, 1e-10);
+            break;
+        case 3:
+            cp = closest_on_triangle(s.pts[0].y, s.pts[1].y, s.pts[2].y, lastPart, 1e-10);
+            break;
+        default:
+            cp = closest_on_tetra(s.pts[0].y, s.pts[1].y, s.pts[2].y, s.pts[3].y, lastPart, 1e-5);
+            break;
+    }
+    double sd = lensq(cp.point);
+    if (sd < prev) {
+        r.point = cp.point;
+        r.sqdist = sd;
+        r.set = cp.set;
+        r.found = true;
+        return true;
+    }
+    r.found = false;
+    return false;
+}
+
+struct GjkResult {
+    double sqdist = 0;
+    V3 axis, pa, pb;
+    Simplex simplex;
+};
+
+// gjkClosestPoints gjk.ts:1294-1546
+inline GjkResult gjk_closest_points(const Support &A, const Support &B, double tolerance, V3 direction,
+                                    double maxDistSq) {
+    GjkResult out;
+    double sqtol = tolerance * tolerance;
+    Simplex sx;
+    ClosestToSimplex c;
+    c.point = direction;
+    c.sqdist = direction.x * direction.x + direction.y * direction.y + direction.z * direction.z;
+    c.set = 0;
+    c.found = true;
+    double prev = std::numeric_limits<double>::max();
+    int it = 0;
+    while (it++ < GJK_MAX_ITERATIONS) {
+        V3 p = A.get(c.point);
+        V3 q = B.get(neg(c.point));
+        V3 w = sub(p, q);
+        double d = c.point.x * w.x + c.point.y * w.y + c.point.z * w.z;
+        if (d < 0.0 && d * d > c.sqdist * maxDistSq) {
+            out.sqdist = std::numeric_limits<double>::max();
+            out.axis = c.point;
+            return out;
+        }
+        sx.pts[sx.size] = {w, p, q};
+        sx.size++;
+        closest_to_simplex(c, prev, true, sx);
+        if (!c.found) {
+            sx.size--;
+            break;
+        }
+        if (c.set == 0xf) {
+            c.point = {0, 0, 0};
+            c.sqdist = 0.0;
+            break;
+        }
+        int ns = 0;
+        for (int i = 0; i < sx.size; i++) {
+            if (c.set & (1 << i)) {
+                if (ns != i) sx.pts[ns] = sx.pts[i];
+                ns++;
+            }
+        }
+        sx.size = ns;
+        if (c.sqdist <= sqtol) {
+            c.point = {0, 0, 0};
+            c.sqdist = 0.0;
+            break;
+        }
+        double ymax = 0;
+        for (int i = 0; i < sx.size; i++) ymax = std::max(ymax, lensq(sx.pts[i].y));
+        if (c.sqdist <= GJK_TOLERANCE * ymax) {
+            c.point = {0, 0, 0};
+            c.sqdist = 0.0;
+            break;
+        }
+        c.point = neg(c.point);
+        if (prev - c.sqdist <= GJK_TOLERANCE * prev) break;
+        prev = c.sqdist;
+    }
+    out.pa = {0, 0, 0};
+    out.pb = {0, 0, 0};
+    out.simplex = sx;
+    if (sx.size == 0) {
+        out.sqdist = std::numeric_limits<double>::max();
+        out.axis = {0, 0, 0};
+        return out;
+    }
+    if (sx.size == 1) {
+        out.pa = sx.pts[0].p;
+        out.pb = sx.pts[0].q;
+    } else if (sx.size == 2) {
+        Bary b = bary2(sx.pts[0].y, sx.pts[1].y, 1e-10);
+        V3 p0 = sx.pts[0].p, p1 = sx.pts[1].p, q0 = sx.pts[0].q, q1 = sx.pts[1].q;
+        out.pa = {p0.x * b.u + p1.x * b.v, p0.y * b.u + p1.y * b.v, p0.z * b.u + p1.z * b.v};
+        out.pb = {q0.x * b.u + q1.x * b.v, q0.y * b.u + q1.y * b.v, q0.z * b.u + q1.z * b.v};
+    } else if (sx.size == 3) {
+        Bary b = bary3(sx.pts[0].y, sx.pts[1].y, sx.pts[2].y, 1e-10);
+        V3 p0 = sx.pts[0].p, p1 = sx.pts[1].p, p2 = sx.pts[2].p;
+        V3 q0 = sx.pts[0].q, q1 = sx.pts[1].q, q2 = sx.pts[2].q;
+        out.pa = {p0.x * b.u + p1.x * b.v + p2.x * b.w, p0.y * b.u + p1.y * b.v + p2.y * b.w,
+                  p0.z * b.u + p1.z * b.v + p2.z * b.w};
+        out.pb = {q0.x * b.u + q1.x * b.v + q2.x * b.w, q0.y * b.u + q1.y * b.v + q2.y * b.w,
+                  q0.z * b.u + q1.z * b.v + q2.z * b.w};
+    }
+    out.axis = c.point;
+    out.sqdist = c.sqdist;
+    return out;
+}
+
+// ----------------------------------------------------------------------------
+// Penetration depth (src/collision/penetration.ts)
+// ----------------------------------------------------------------------------
+enum PenStatus { NOT_COLLIDING = 0, COLLIDING = 1, INDETERMINATE = 2 };
+struct PenDepth {
+    int status = NOT_COLLIDING;
+    V3 axis, pa, pb;
+};
+
+// penetrationDepthStepGJK penetration.ts:35-110
+inline PenDepth pen_step_gjk(Simplex &outSimplex, const Support &A, const Support &B, double rA, double rB,
+                             V3 dir, double tol) {
+    PenDepth o;
+    double cr = rA + rB;
+    double crs = cr * cr;
+    GjkResult g = gjk_closest_points(A, B, tol, dir, crs);
+    if (g.sqdist > crs) {
+        o.status = NOT_COLLIDING;
+        return o;
+    }
+    o.pa = g.pa;
+    o.pb = g.pb;
+    o.axis = g.axis;
+    outSimplex = g.simplex;
+    if (g.sqdist > 0.0) {
+        double vl = std::sqrt(g.sqdist);
+        o.pa = scale_add(o.pa, o.axis, rA / vl);
+        o.pb = scale_add(o.pb, o.axis, -(rB / vl));
+        o.status = COLLIDING;
+        return o;
+    }
+    o.status = INDETERMINATE;
+    return o;
+}
+
+// ---- EPA convex hull builder (src/collision/epa-convex-hull-builder.ts) ----
+constexpr int EPA_MAX_TRIANGLES = 256;
+constexpr int EPA_MAX_EDGE_LENGTH = 128;
+constexpr double EPA_MIN_TRIANGLE_AREA = 1e-10;
+constexpr double EPA_BARYCENTRIC_EPSILON = 1e-3;
+constexpr int EPA_MAX_POINTS_TO_INCLUDE_ORIGIN_IN_HULL = 32;
+constexpr int EPA_MAX_POINTS = 128;
+
+struct EpaTri;
+struct EpaEdge {
+    int nt = -1;  // neighbour triangle index
+    int ne = 0;   // neighbour edge
+    int start = 0;
+};
+struct EpaTri {
+    EpaEdge e[3];
+    V3 normal, centroid;
+    double cls = std::numeric_limits<double>::infinity();
+    double lambda[2] = {0, 0};
+    bool rel0 = false, interior = false, removed = false, inq = false;
+    int index = -1;
+};
+
+struct EpaHull {
+    std::vector<EpaTri> tris;  // pool, grows to EPA_MAX_TRIANGLES
+    std::vector<int> free_list;
+    std::vector<int> queue;
+    const std::vector<V3> *pos = nullptr;
+
+    bool facing(const EpaTri &t, V3 p) const {
+        V3 ab = sub(p, t.centroid);
+        return t.normal.x * ab.x + t.normal.y * ab.y + t.normal.z * ab.z > 0.0;
+    }
+    void push(int ti) {  // pushTriangleToQueue :95-116
+        queue.push_back(ti);
+        tris[ti].inq = true;
+        int cur = (int)queue.size() - 1;
+        while (cur > 0) {
+            int par = (cur - 1) >> 1;
+            if (tris[queue[par]].cls > tris[queue[cur]].cls) {
+                std::swap(queue[par], queue[cur]);
+                cur = par;
+            } else {
+                break;
+            }
+        }
+    }
+    int pop() {  // popClosestTriangleFromQueue :388-425
+        if (queue.empty()) return -1;
+        std::swap(queue[queue.size() - 1], queue[0]);
+        int count = (int)queue.size() - 1;
+        int largest = 0;
+        while (true) {
+            int child = (largest << 1) + 1;
+            if (child >= count) break;
+            int prevL = largest;
+            if (tris[queue[largest]].cls > tris[queue[child]].cls) largest = child;
+            ++child;
+            if (child < count && tris[queue[largest]].cls > tris[queue[child]].cls) largest = child;
+            if (prevL == largest) break;
+            std::swap(queue[prevL], queue[largest]);
+        }
+        int r = queue.back();
+        queue.pop_back();
+        return r;
+    }
+    void link(int t1, int e1, int t2, int e2) {
+        tris[t1].e[e1].nt = t2;
+        tris[t1].e[e1].ne = e2;
+        tris[t2].e[e2].nt = t1;
+        tris[t2].e[e2].ne = e1;
+    }
+    // createTriangle :179-341
+    int create(int i1, int i2, int i3) {
+        int idx;
+        if (!free_list.empty()) {
+            idx = free_list.back();
+            free_list.pop_back();
+        } else {
+            idx = (int)tris.size();
+            if (idx >= EPA_MAX_TRIANGLES) return -1;
+            tris.emplace_back();
+            tris.back().index = idx;
+        }
+        EpaTri &t = tris[idx];
+        t.cls = std::numeric_limits<double>::infinity();
+        t.lambda[0] = t.lambda[1] = 0.0;
+        t.rel0 = t.interior = t.removed = t.inq = false;
+        t.e[0].start = i1;
+        t.e[1].start = i2;
+        t.e[2].start = i3;
+        t.e[0].nt = t.e[1].nt = t.e[2].nt = -1;
+        V3 y0 = (*pos)[i1], y1 = (*pos)[i2], y2 = (*pos)[i3];
+        double cx = (y0.x + y1.x + y2.x) / 3.0, cy = (y0.y + y1.y + y2.y) / 3.0, cz = (y0.z + y1.z + y2.z) / 3.0;
+        t.centroid = {cx, cy, cz};
+        V3 y10 = sub(y1, y0), y20 = sub(y2, y0), y21 = sub(y2, y1);
+        double y20d = y20.x * y20.x + y20.y * y20.y + y20.z * y20.z;
+        double y21d = y21.x * y21.x + y21.y * y21.y + y21.z * y21.z;
+        if (y20d < y21d) {
+            double nx = y10.y * y20.z - y10.z * y20.y, ny = y10.z * y20.x - y10.x * y20.z,
+                   nz = y10.x * y20.y - y10.y * y20.x;
+            t.normal = {nx, ny, nz};
+            double nl = nx * nx + ny * ny + nz * nz;
+            if (nl > EPA_MIN_TRIANGLE_AREA) {
+                double cdn = cx * nx + cy * ny + cz * nz;
+                t.cls = (std::fabs(cdn) * cdn) / nl;
+                double y10d = y10.x * y10.x + y10.y * y10.y + y10.z * y10.z;
+                double y10y20 = y10.x * y20.x + y10.y * y20.y + y10.z * y20.z;
+                double det = y10d * y20d - y10y20 * y10y20;
+                if (det > 0.0) {
+                    double y0y10 = y0.x * y10.x + y0.y * y10.y + y0.z * y10.z;
+                    double y0y20 = y0.x * y20.x + y0.y * y20.y + y0.z * y20.z;
+                    double l0 = (y10y20 * y0y20 - y20d * y0y10) / det;
+                    double l1 = (y10y20 * y0y10 - y10d * y0y20) / det;
+                    t.lambda[0] = l0;
+                    t.lambda[1] = l1;
+                    t.rel0 = true;
+                    if (l0 > -EPA_BARYCENTRIC_EPSILON && l1 > -EPA_BARYCENTRIC_EPSILON &&
+                        l0 + l1 < 1.0 + EPA_BARYCENTRIC_EPSILON)
+                        t.interior = true;
+                }
+            }
+        } else {
+            double nx = y10.y * y21.z - y10.z * y21.y, ny = y10.z * y21.x - y10.x * y21.z,
+                   nz = y10.x * y21.y - y10.y * y21.x;
+            t.normal = {nx, ny, nz};
+            double nl = nx * nx + ny * ny + nz * nz;
+            if (nl > EPA_MIN_TRIANGLE_AREA) {
+                double cdn = cx * nx + cy * ny + cz * nz;
+                t.cls = (std::fabs(cdn) * cdn) / nl;
+                double y10d = y10.x * y10.x + y10.y * y10.y + y10.z * y10.z;
+                double y10y21 = y10.x * y21.x + y10.y * y21.y + y10.z * y21.z;
+                double det = y10d * y21d - y10y21 * y10y21;
+                if (det > 0.0) {
+                    double y1y10 = y1.x * y10.x + y1.y * y10.y + y1.z * y10.z;
+                    double y1y21 = y1.x * y21.x + y1.y * y21.y + y1.z * y21.z;
+                    double l0 = (y21d * y1y10 - y10y21 * y1y21) / det;
+                    double l1 = (y10y21 * y1y10 - y10d * y1y21) / det;
+                    t.lambda[0] = l0;
+                    t.lambda[1] = l1;
+                    t.rel0 = false;
+                    if (l0 > -EPA_BARYCENTRIC_EPSILON && l1 > -EPA_BARYCENTRIC_EPSILON &&
+                        l0 + l1 < 1.0 + EPA_BARYCENTRIC_EPSILON)
+                        t.interior = true;
+                }
+            }
+        }
+        return idx;
+    }
+    // initialize :347-371
+    bool initialize(int i1, int i2, int i3) {
+        free_list.resize(tris.size());
+        for (size_t i = 0; i < tris.size(); i++) free_list[i] = (int)(tris.size() - 1 - i);
+        queue.clear();
+        int t1 = create(i1, i2, i3);
+        int t2 = create(i1, i3, i2);
+        if (t1 < 0 || t2 < 0) return false;
+        link(t1, 0, t2, 2);
+        link(t1, 1, t2, 1);
+        link(t1, 2, t2, 0);
+        push(t1);
+        push(t2);
+        return true;
+    }
+    // findFacingTriangle :427-452
+    int find_facing(V3 p) {
+        int best = -1;
+        double bestd = 0.0;
+        for (size_t i = 0; i < queue.size(); i++) {
+            EpaTri &t = tris[queue[i]];
+            if (t.removed) continue;
+            V3 ab = sub(p, t.centroid);
+            double d = dot(t.normal, ab);
+            if (d > 0.0) {
+                double ds = (d * d) / lensq(t.normal);
+                if (ds > bestd) {
+                    best = queue[i];
+                    bestd = ds;
+                }
+            }
+        }
+        return best;
+    }
+    void free_tri(int ti) { free_list.push_back(ti); }
+    void unlink(int ti) {  // unlinkTriangle :458-474
+        for (int i = 0; i < 3; i++) {
+            EpaEdge &e = tris[ti].e[i];
+            if (e.nt >= 0) {
+                tris[e.nt].e[e.ne].nt = -1;
+                e.nt = -1;
+            }
+        }
+        if (!tris[ti].inq) free_tri(ti);
+    }
+    // findEdge :476-540
+    bool find_edge(int facing_t, V3 vertex, std::vector<EpaEdge> &out) {
+        out.clear();
+        tris[facing_t].removed = true;
+        struct SE {
+            int t, edge, iter;
+        };
+        SE stack[EPA_MAX_EDGE_LENGTH];
+        int sp = 0;
+        stack[0] = {facing_t, 0, -1};
+        int next_expected = -1;
+        while (true) {
+            SE &cur = stack[sp];
+            if (++cur.iter >= 3) {
+                unlink(cur.t);
+                if (--sp < 0) break;
+            } else {
+                EpaEdge e = tris[cur.t].e[(cur.edge + cur.iter) % 3];
+                int n = e.nt;
+                if (n >= 0 && !tris[n].removed) {
+                    if (facing(tris[n], vertex)) {
+                        tris[n].removed = true;
+                        sp++;
+                        if (sp >= EPA_MAX_EDGE_LENGTH) return false;  // the reference stack is 128 deep
+                        stack[sp] = {n, e.ne, 0};
+                    } else {
+                        if (e.start != next_expected && next_expected != -1) return false;
+                        next_expected = tris[n].e[e.ne].start;
+                        out.push_back(e);
+                    }
+                }
+            }
+        }
+        if (!out.empty() && out[0].start != next_expected) return false;
+        return out.size() >= 3;
+    }
+    // addPoint :542-593
+    bool add_point(int facing_t, int idx, double closest, std::vector<int> &outT) {
+        V3 p = (*pos)[idx];
+        std::vector<EpaEdge> edges;
+        if (!find_edge(facing_t, p, edges)) return false;
+        int ne = (int)edges.size();
+        for (int i = 0; i < ne; i++) {
+            int in = (i + 1) % ne;
+            int nt = create(edges[i].start, edges[in].start, idx);
+            if (nt < 0) return false;
+            outT.push_back(nt);
+            if ((tris[nt].interior && tris[nt].cls < closest) || tris[nt].cls < 0.0) push(nt);
+        }
+        for (int i = 0; i < ne; i++) {
+            int in = (i + 1) % ne;
+            link(outT[i], 0, edges[i].nt, edges[i].ne);
+            link(outT[i], 1, outT[in], 2);
+        }
+        return true;
+    }
+};
+
+// penetrationDepthStepEPA penetration.ts:214-614
+inline bool pen_step_epa(PenDepth &out, const Support &A, const Support &B, double tol, const Simplex &sx) {
+    std::vector<V3> Y, P, Q;
+    Y.reserve(256);
+    P.reserve(256);
+    Q.reserve(256);
+    for (int i = 0; i < sx.size; i++) {
+        Y.push_back(sx.pts[i].y);
+        P.push_back(sx.pts[i].p);
+        Q.push_back(sx.pts[i].q);
+    }
+    auto add_sup = [&](V3 d) {
+        V3 p = A.get(d);
+        V3 q = B.get(neg(d));
+        Y.push_back(sub(p, q));
+        P.push_back(p);
+        Q.push_back(q);
+        return (int)Y.size() - 1;
+    };
+    if (Y.size() == 1) {
+        Y.pop_back();
+        P.pop_back();
+        Q.pop_back();
+        add_sup({0, 1, 0});
+        add_sup({-1, -1, -1});
+        add_sup({1, -1, -1});
+        add_sup({0, -1, 1});
+    } else if (Y.size() == 2) {
+        const double COS120 = std::cos(120.0 * M_PI / 180.0);
+        const double SIN120 = std::sin(120.0 * M_PI / 180.0);
+        const double OMC = 1 - COS120;
+        V3 y0 = Y[0], y1 = Y[1];
+        double ax = y1.x - y0.x, ay = y1.y - y0.y, az = y1.z - y0.z;
+        double al = std::sqrt(ax * ax + ay * ay + az * az);
+        double nx = ax / al, ny = ay / al, nz = az / al;
+        double d1x, d1y, d1z;
+        if (std::fabs(nx) > std::fabs(ny)) {
+            double pl = std::sqrt(nx * nx + nz * nz);
+            d1x = nz / pl;
+            d1y = 0.0;
+            d1z = -nx / pl;
+        } else {
+            double pl = std::sqrt(ny * ny + nz * nz);
+            d1x = 0.0;
+            d1y = nz / pl;
+            d1z = -ny / pl;
+        }
+        double r00 = COS120 + nx * nx * OMC, r01 = nx * ny * OMC - nz * SIN120, r02 = nx * nz * OMC + ny * SIN120;
+        double r10 = ny * nx * OMC + nz * SIN120, r11 = COS120 + ny * ny * OMC, r12 = ny * nz * OMC - nx * SIN120;
+        double r20 = nz * nx * OMC - ny * SIN120, r21 = nz * ny * OMC + nx * SIN120, r22 = COS120 + nz * nz * OMC;
+        double d2x = r00 * d1x + r01 * d1y + r02 * d1z, d2y = r10 * d1x + r11 * d1y + r12 * d1z,
+               d2z = r20 * d1x + r21 * d1y + r22 * d1z;
+        double d3x = r00 * d2x + r01 * d2y + r02 * d2z, d3y = r10 * d2x + r11 * d2y + r12 * d2z,
+               d3z = r20 * d2x + r21 * d2y + r22 * d2z;
+        add_sup({d1x, d1y, d1z});
+        add_sup({d2x, d2y, d2z});
+        add_sup({d3x, d3y, d3z});
+    }
+    EpaHull h;
+    h.tris.reserve(EPA_MAX_TRIANGLES);
+    h.pos = &Y;
+    if (!h.initialize(0, 1, 2)) {
+        out.status = NOT_COLLIDING;
+        return false;
+    }
+    std::vector<int> nts;
+    for (int i = 3; i < (int)Y.size(); i++) {
+        int t = h.find_facing(Y[i]);
+        if (t >= 0) {
+            nts.clear();
+            if (!h.add_point(t, i, std::numeric_limits<double>::max(), nts)) {
+                out.status = NOT_COLLIDING;
+                return false;
+            }
+        }
+    }
+    while (true) {
+        if (h.queue.empty()) {
+            out.status = NOT_COLLIDING;
+            return false;
+        }
+        int t = h.queue[0];
+        if (h.tris[t].removed) {
+            h.pop();
+            if (h.queue.empty()) {
+                out.status = NOT_COLLIDING;
+                return false;
+            }
+            h.free_tri(t);
+            continue;
+        }
+        if (h.tris[t].cls >= 0.0) break;
+        h.pop();
+        int ni = add_sup(h.tris[t].normal);
+        V3 w = Y[ni];
+        nts.clear();
+        if (!h.facing(h.tris[t], w) || !h.add_point(t, ni, std::numeric_limits<double>::max(), nts)) {
+            out.status = NOT_COLLIDING;
+            return false;
+        }
+        h.free_tri(t);
+        if (h.queue.empty() || (int)Y.size() >= EPA_MAX_POINTS_TO_INCLUDE_ORIGIN_IN_HULL) {
+            out.status = NOT_COLLIDING;
+            return false;
+        }
+    }
+    double closest = std::numeric_limits<double>::max();
+    int last = -1;
+    bool flip = false;
+    do {
+        int t = h.pop();
+        if (t < 0) {
+            out.status = NOT_COLLIDING;
+            return false;
+        }
+        if (h.tris[t].removed) {
+            h.free_tri(t);
+            continue;
+        }
+        if (h.tris[t].cls >= closest) break;
+        if (last >= 0) h.free_tri(last);
+        last = t;
+        V3 tn = h.tris[t].normal;
+        int ni = add_sup(tn);
+        V3 w = Y[ni];
+        double d = tn.x * w.x + tn.y * w.y + tn.z * w.z;
+        if (d < 0.0) {
+            out.status = NOT_COLLIDING;
+            return false;
+        }
+        double nls = tn.x * tn.x + tn.y * tn.y + tn.z * tn.z;
+        double ds = (d * d) / nls;
+        if (ds - h.tris[t].cls < h.tris[t].cls * tol) break;
+        closest = std::min(closest, ds);
+        if (!h.facing(h.tris[t], w)) break;
+        nts.clear();
+        if (!h.add_point(t, ni, closest, nts)) break;
+        bool defect = false;
+        for (int k : nts) {
+            const EpaTri &q = h.tris[k];
+            if (q.normal.x * q.centroid.x + q.normal.y * q.centroid.y + q.normal.z * q.centroid.z < 0.0) {
+                defect = true;
+                break;
+            }
+        }
+        if (defect) {
+            V3 nn = neg(tn);
+            V3 p2 = A.get(nn);
+            V3 q2 = B.get(tn);
+            V3 w2 = sub(p2, q2);
+            double d2 = nn.x * w2.x + nn.y * w2.y + nn.z * w2.z;
+            if (d2 < d) flip = true;
+            break;
+        }
+    } while (!h.queue.empty() && (int)Y.size() < EPA_MAX_POINTS);
+    if (last < 0) {
+        out.status = NOT_COLLIDING;
+        return false;
+    }
+    const EpaTri &L = h.tris[last];
+    double nls = L.normal.x * L.normal.x + L.normal.y * L.normal.y + L.normal.z * L.normal.z;
+    double cdn = L.centroid.x * L.normal.x + L.centroid.y * L.normal.y + L.centroid.z * L.normal.z;
+    V3 pn = scale(L.normal, cdn / nls);
+    if (pn.x * pn.x + pn.y * pn.y + pn.z * pn.z < 1e-10) {
+        out.status = NOT_COLLIDING;
+        return false;
+    }
+    if (flip) pn = neg(pn);
+    V3 xp0 = P[L.e[0].start], xp1 = P[L.e[1].start], xp2 = P[L.e[2].start];
+    V3 xq0 = Q[L.e[0].start], xq1 = Q[L.e[1].start], xq2 = Q[L.e[2].start];
+    double l0 = L.lambda[0], l1 = L.lambda[1];
+    V3 ca, cb;
+    if (L.rel0) {
+        ca = {xp0.x + (xp1.x - xp0.x) * l0 + (xp2.x - xp0.x) * l1, xp0.y + (xp1.y - xp0.y) * l0 + (xp2.y - xp0.y) * l1,
+              xp0.z + (xp1.z - xp0.z) * l0 + (xp2.z - xp0.z) * l1};
+        cb = {xq0.x + (xq1.x - xq0.x) * l0 + (xq2.x - xq0.x) * l1, xq0.y + (xq1.y - xq0.y) * l0 + (xq2.y - xq0.y) * l1,
+              xq0.z + (xq1.z - xq0.z) * l0 + (xq2.z - xq0.z) * l1};
+    } else {
+        ca = {xp1.x + (xp0.x - xp1.x) * l0 + (xp2.x - xp1.x) * l1, xp1.y + (xp0.y - xp1.y) * l0 + (xp2.y - xp1.y) * l1,
+              xp1.z + (xp0.z - xp1.z) * l0 + (xp2.z - xp1.z) * l1};
+        cb = {xq1.x + (xq0.x - xq1.x) * l0 + (xq2.x - xq1.x) * l1, xq1.y + (xq0.y - xq1.y) * l0 + (xq2.y - xq1.y) * l1,
+              xq1.z + (xq0.z - xq1.z) * l0 + (xq2.z - xq1.z) * l1};
+    }
+    out.axis = pn;
+    out.pa = ca;
+    out.pb = cb;
+    out.status = COLLIDING;
+    return true;
+}
+
+// ----------------------------------------------------------------------------
+// Faces, clipping, manifolds (src/utils/face.ts, src/manifold/clip.ts, manifold.ts)
+// ----------------------------------------------------------------------------
+constexpr int FACE_MAX_VERTICES = 64;
+struct Face {
+    int n = 0;
+    V3 v[FACE_MAX_VERTICES];
+};
+
+// transformFace face.ts:30-80 (unit scale)
+inline void transform_face(Face &f, V3 p, Q4 q) {
+    double qx2 = q.x + q.x, qy2 = q.y + q.y, qz2 = q.z + q.z;
+    double qxx = q.x * qx2, qyx = q.y * qx2, qyy = q.y * qy2, qzx = q.z * qx2, qzy = q.z * qy2, qzz = q.z * qz2,
+           qwx = q.w * qx2, qwy = q.w * qy2, qwz = q.w * qz2;
+    double m00 = (1 - qyy - qzz) * 1.0, m01 = (qyx + qwz) * 1.0, m02 = (qzx - qwy) * 1.0;
+    double m10 = (qyx - qwz) * 1.0, m11 = (1 - qxx - qzz) * 1.0, m12 = (qzy + qwx) * 1.0;
+    double m20 = (qzx + qwy) * 1.0, m21 = (qzy - qwx) * 1.0, m22 = (1 - qxx - qyy) * 1.0;
+    for (int i = 0; i < f.n; i++) {
+        V3 a = f.v[i];
+        f.v[i] = {m00 * a.x + m10 * a.y + m20 * a.z + p.x, m01 * a.x + m11 * a.y + m21 * a.z + p.y,
+                  m02 * a.x + m12 * a.y + m22 * a.z + p.z};
+    }
+}
+
+// box getSupportingFace box.ts:129-332 (scale not inside out)
+inline void box_supporting_face(Face &f, V3 dir, V3 he) {
+    double hx = he.x, hy = he.y, hz = he.z;
+    double ax = std::fabs(dir.x), ay = std::fabs(dir.y), az = std::fabs(dir.z);
+    f.n = 4;
+    if (ax >= ay && ax >= az) {
+        if (dir.x < 0) {
+            f.v[0] = {hx, -hy, -hz};
+            f.v[1] = {hx, hy, -hz};
+            f.v[2] = {hx, hy, hz};
+            f.v[3] = {hx, -hy, hz};
+        } else {
+            f.v[0] = {-hx, -hy, -hz};
+            f.v[1] = {-hx, -hy, hz};
+            f.v[2] = {-hx, hy, hz};
+            f.v[3] = {-hx, hy, -hz};
+        }
+    } else if (ay >= ax && ay >= az) {
+        if (dir.y < 0) {
+            f.v[0] = {-hx, hy, -hz};
+            f.v[1] = {-hx, hy, hz};
+            f.v[2] = {hx, hy, hz};
+            f.v[3] = {hx, hy, -hz};
+        } else {
+            f.v[0] = {-hx, -hy, -hz};
+            f.v[1] = {hx, -hy, -hz};
+            f.v[2] = {hx, -hy, hz};
+            f.v[3] = {-hx, -hy, hz};
+        }
+    } else {
+        if (dir.z < 0) {
+            f.v[0] = {-hx, -hy, hz};
+            f.v[1] = {hx, -hy, hz};
+            f.v[2] = {hx, hy, hz};
+            f.v[3] = {-hx, hy, hz};
+        } else {
+            f.v[0] = {-hx, -hy, -hz};
+            f.v[1] = {-hx, hy, -hz};
+            f.v[2] = {hx, hy, -hz};
+            f.v[3] = {hx, -hy, -hz};
+        }
+    }
+}
+
+// getShapeSupportingFace shapes.ts:489-508 (box and sphere; sphere has no face)
+inline void shape_supporting_face(Face &f, const Shape &s, V3 dir, V3 p, Q4 q) {
+    if (s.type == SHAPE_BOX) {
+        box_supporting_face(f, dir, s.half_extents);
+        transform_face(f, p, q);
+    } else {
+        f.n = 0;
+    }
+}
+
+// clipPolyVsPlane clip.ts:13-92
+inline void clip_poly_vs_plane(Face &out, const Face &in, V3 o, V3 n) {
+    out.n = 0;
+    if (in.n < 2) return;
+    V3 e1 = in.v[in.n - 1];
+    double prevNum = (o.x - e1.x) * n.x + (o.y - e1.y) * n.y + (o.z - e1.z) * n.z;
+    bool prevIn = prevNum < 0.0;
+    for (int j = 0; j < in.n; j++) {
+        V3 e2 = in.v[j];
+        double num = (o.x - e2.x) * n.x + (o.y - e2.y) * n.y + (o.z - e2.z) * n.z;
+        bool curIn = num < 0.0;
+        if (curIn != prevIn) {
+            V3 e12 = sub(e2, e1);
+            double den = e12.x * n.x + e12.y * n.y + e12.z * n.z;
+            if (den != 0.0) {
+                double t = prevNum / den;
+                if (out.n < FACE_MAX_VERTICES) out.v[out.n] = {e1.x + e12.x * t, e1.y + e12.y * t, e1.z + e12.z * t};
+                out.n++;
+            } else {
+                curIn = prevIn;
+            }
+        }
+        if (curIn) {
+            if (out.n < FACE_MAX_VERTICES) out.v[out.n] = e2;
+            out.n++;
+        }
+        prevNum = num;
+        prevIn = curIn;
+        e1 = e2;
+    }
+    if (out.n > FACE_MAX_VERTICES) out.n = FACE_MAX_VERTICES;
+}
+
+// clipPolyVsPoly clip.ts:108-175
+inline void clip_poly_vs_poly(Face &out, const Face &toClip, const Face &clipping, V3 clipNormal) {
+    out.n = 0;
+    if (toClip.n < 2) return;
+    if (clipping.n < 3) return;
+    static thread_local Face tmp[2];
+    int tmpIdx = 0;
+    for (int i = 0; i < clipping.n; i++) {
+        V3 c1 = clipping.v[i];
+        V3 c2 = clipping.v[(i + 1) % clipping.n];
+        V3 e = sub(c2, c1);
+        V3 cn{clipNormal.y * e.z - clipNormal.z * e.y, clipNormal.z * e.x - clipNormal.x * e.z,
+              clipNormal.x * e.y - clipNormal.y * e.x};
+        const Face *src = (i == 0) ? &toClip : (tmpIdx == 0 ? &tmp[0] : &tmp[1]);
+        tmpIdx ^= 1;
+        Face *dst = (i == clipping.n - 1) ? &out : (tmpIdx == 0 ? &tmp[0] : &tmp[1]);
+        clip_poly_vs_plane(*dst, *src, c1, cn);
+        if (dst->n < 3) {
+            out.n = 0;
+            break;
+        }
+    }
+}
+
+struct Manifold {
+    int n = 0;
+    V3 base;
+    V3 relA[FACE_MAX_VERTICES], relB[FACE_MAX_VERTICES];
+    V3 normal;
+    double depth = 0;
+    uint32_t subA = EMPTY_SUB_SHAPE_ID, subB = EMPTY_SUB_SHAPE_ID;
+};
+
+// setContactPoint manifold.ts:134-145
+inline void set_contact_point(Manifold &m, int i, V3 a, V3 b) {
+    m.relA[i] = sub(a, m.base);
+    m.relB[i] = sub(b, m.base);
+}
+
+// pruneContactPoints manifold.ts:192-311
+inline void prune_contact_points(Manifold &m, V3 axis) {
+    constexpr double MIN_DISTANCE_SQ = 1.0e-6;
+    if (m.n <= 4) return;
+    std::vector<V3> proj(m.n);
+    std::vector<double> dsq(m.n);
+    for (int i = 0; i < m.n; i++) {
+        V3 v1 = m.relA[i], v2 = m.relB[i];
+        double d = dot(v1, axis);
+        proj[i] = scale_add(v1, axis, -d);
+        dsq[i] = std::max(MIN_DISTANCE_SQ, lensq(sub(v2, v1)));
+    }
+    int p1 = 0;
+    double mm = std::max(MIN_DISTANCE_SQ, lensq(proj[0])) * dsq[0];
+    for (int i = 1; i < m.n; i++) {
+        double met = std::max(MIN_DISTANCE_SQ, lensq(proj[i])) * dsq[i];
+        if (met > mm) {
+            mm = met;
+            p1 = i;
+        }
+    }
+    int p2 = -1;
+    mm = -std::numeric_limits<double>::infinity();
+    for (int i = 0; i < m.n; i++) {
+        if (i != p1) {
+            double met = std::max(MIN_DISTANCE_SQ, lensq(sub(proj[i], proj[p1]))) * dsq[i];
+            if (met > mm) {
+                mm = met;
+                p2 = i;
+            }
+        }
+    }
+    int p3 = -1, p4 = -1;
+    double minD = 0.0, maxD = 0.0;
+    V3 edge = sub(proj[p2], proj[p1]);
+    V3 perp = cross(edge, axis);
+    for (int i = 0; i < m.n; i++) {
+        if (i != p1 && i != p2) {
+            double d = dot(sub(proj[i], proj[p1]), perp);
+            if (d < minD) {
+                minD = d;
+                p3 = i;
+            } else if (d > maxD) {
+                maxD = d;
+                p4 = i;
+            }
+        }
+    }
+    int order[4] = {p1, p3, p2, p4};
+    int o = 0;
+    for (int k = 0; k < 4; k++) {
+        int s = order[k];
+        if (s != -1) {
+            if (o != s) {
+                m.relA[o] = m.relA[s];
+                m.relB[o] = m.relB[s];
+            }
+            o++;
+        }
+    }
+    m.n = o;
+}
+
+// manifoldBetweenTwoFaces manifold.ts:345-444
+inline void manifold_between_faces(Manifold &out, V3 cp1, V3 cp2, V3 axis, double maxDist, const Face &f1,
+                                   const Face &f2) {
+    out.n = 0;
+    if (f1.n < 2 || f2.n < 3) {
+        set_contact_point(out, 0, cp1, cp2);
+        out.n = 1;
+        return;
+    }
+    static thread_local Face clipped;
+    clipped.n = 0;
+    if (f1.n >= 3) {
+        clip_poly_vs_poly(clipped, f2, f1, axis);
+    }
+    // (edge faces of capsules: clipPolyVsEdge, not needed for box/sphere)
+    V3 po = f1.v[0];
+    V3 e1 = f1.v[1];
+    V3 first = sub(e1, po);
+    V3 pn;
+    if (f1.n >= 3) {
+        V3 second = sub(f1.v[2], po);
+        pn = cross(first, second);
+    } else {
+        V3 perp = cross(first, axis);
+        pn = cross(perp, first);
+    }
+    double adn = dot(axis, pn);
+    if (adn != 0.0) {
+        double al = len(axis);
+        for (int i = 0; i < clipped.n; i++) {
+            V3 p2 = clipped.v[i];
+            double dist = dot(sub(p2, po), pn) / adn;
+            if (dist * al < maxDist) {
+                V3 p1 = scale_add(p2, axis, -dist);
+                set_contact_point(out, out.n, p1, p2);
+                out.n++;
+                if (out.n >= FACE_MAX_VERTICES) break;
+            }
+        }
+    }
+    if (out.n == 0) {
+        set_contact_point(out, 0, cp1, cp2);
+        out.n = 1;
+    }
+}
+
+// Hit produced by a shape-vs-shape collision (collide-shape-vs-shape.ts:8-31)
+struct Hit {
+    V3 pa, pb, axis;
+    double penetration = 0;
+    uint32_t subA = EMPTY_SUB_SHAPE_ID, subB = EMPTY_SUB_SHAPE_ID;
+    Face faceA, faceB;
+};
+
+struct CollideSettings {
+    double maxSeparation = 0.02;
+    double collisionTolerance = 1e-4;
+    double penetrationTolerance = 1e-4;
+    bool collectFaces = true;
+};
+
+// collideConvexVsConvex convex.ts:257-346 + collideConvexVsConvexLocal convex.ts:359-641
+// Returns true and fills `hit` when the shapes touch within the separation distance.
+inline bool collide_convex_vs_convex(Hit &hit, const CollideSettings &cs, const Shape &sa, V3 pA, Q4 qA,
+                                     const Shape &sb, V3 pB, Q4 qB) {
+    double iax = -qA.x, iay = -qA.y, iaz = -qA.z, iaw = qA.w;
+    Q4 rel{iaw * qB.x + iax * qB.w + iay * qB.z - iaz * qB.y, iaw * qB.y - iax * qB.z + iay * qB.w + iaz * qB.x,
+           iaw * qB.z + iax * qB.y - iay * qB.x + iaz * qB.w, iaw * qB.w - iax * qB.x - iay * qB.y - iaz * qB.z};
+    double abx = pB.x - pA.x, aby = pB.y - pA.y, abz = pB.z - pA.z;
+    double qx = iax, qy = iay, qz = iaz, qw = iaw;
+    double uvx = qy * abz - qz * aby + qw * abx, uvy = qz * abx - qx * abz + qw * aby,
+           uvz = qx * aby - qy * abx + qw * abz;
+    double uuvx = qy * uvz - qz * uvy, uuvy = qz * uvx - qx * uvz, uuvz = qx * uvy - qy * uvx;
+    V3 posBInA{abx + 2 * uuvx, aby + 2 * uuvy, abz + 2 * uuvz};
+
+    Support supA = make_support(sa, EXCLUDE_CONVEX_RADIUS);
+    Support supB = make_support(sb, EXCLUDE_CONVEX_RADIUS);
+    supB.transformed = true;
+    supB.m = mat4_from_rt(rel, posBInA);
+    V3 axis = posBInA;
+    if (axis.x * axis.x + axis.y * axis.y + axis.z * axis.z <= 1e-12) axis = {1, 0, 0};
+    Simplex sx;
+    double maxSep = cs.maxSeparation;
+    PenDepth pd = pen_step_gjk(sx, supA, supB, supA.convex_radius + maxSep, supB.convex_radius, axis,
+                               cs.collisionTolerance);
+    if (pd.status == NOT_COLLIDING) return false;
+    if (pd.status == INDETERMINATE) {
+        maxSep = std::min(maxSep, 1.0);
+        Support a2 = make_support(sa, INCLUDE_CONVEX_RADIUS);
+        Support b2 = make_support(sb, INCLUDE_CONVEX_RADIUS);
+        a2.add_radius = true;
+        a2.add_r = maxSep;
+        b2.transformed = true;
+        b2.m = mat4_from_rt(rel, posBInA);
+        if (!pen_step_epa(pd, a2, b2, cs.penetrationTolerance, sx)) return false;
+    }
+    double dx = pd.pa.x - pd.pb.x, dy = pd.pa.y - pd.pb.y, dz = pd.pa.z - pd.pb.z;
+    double penetration = std::sqrt(dx * dx + dy * dy + dz * dz) - maxSep;
+    // collector.earlyOutFraction is Number.MAX_VALUE for the narrowphase collectors (update.ts:349)
+    V3 pax = pd.axis;
+    double pal = std::sqrt(pax.x * pax.x + pax.y * pax.y + pax.z * pax.z);
+    if (pal > 0.0) {
+        double corr = maxSep / pal;
+        pd.pa.x += pax.x * -corr;
+        pd.pa.y += pax.y * -corr;
+        pd.pa.z += pax.z * -corr;
+    }
+    auto to_world = [&](V3 v) {
+        double qax = qA.x, qay = qA.y, qaz = qA.z, qaw = qA.w;
+        double ux = qay * v.z - qaz * v.y + qaw * v.x, uy = qaz * v.x - qax * v.z + qaw * v.y,
+               uz = qax * v.y - qay * v.x + qaw * v.z;
+        double wx = qay * uz - qaz * uy, wy = qaz * ux - qax * uz, wz = qax * uy - qay * ux;
+        return V3{v.x + 2 * wx, v.y + 2 * wy, v.z + 2 * wz};
+    };
+    V3 ca = to_world(pd.pa);
+    hit.pa = {ca.x + pA.x, ca.y + pA.y, ca.z + pA.z};
+    V3 cb = to_world(pd.pb);
+    hit.pb = {cb.x + pA.x, cb.y + pA.y, cb.z + pA.z};
+    hit.axis = to_world(pd.axis);
+    hit.penetration = penetration;
+    hit.subA = EMPTY_SUB_SHAPE_ID;
+    hit.subB = EMPTY_SUB_SHAPE_ID;
+    hit.faceA.n = 0;
+    hit.faceB.n = 0;
+    if (cs.collectFaces) {
+        shape_supporting_face(hit.faceA, sa, neg(pd.axis), pA, qA);
+        double cx = -rel.x, cy = -rel.y, cz = -rel.z, cw = rel.w;
+        V3 fa = pd.axis;
+        double px = cy * fa.z - cz * fa.y + cw * fa.x, py = cz * fa.x - cx * fa.z + cw * fa.y,
+               pz = cx * fa.y - cy * fa.x + cw * fa.z;
+        double ddx = cy * pz - cz * py, ddy = cz * px - cx * pz, ddz = cx * py - cy * px;
+        V3 dirB{fa.x + 2 * ddx, fa.y + 2 * ddy, fa.z + 2 * ddz};
+        V3 pbw = to_world(posBInA);
+        V3 posB{pbw.x + pA.x, pbw.y + pA.y, pbw.z + pA.z};
+        Q4 quatB{qA.w * rel.x + qA.x * rel.w + qA.y * rel.z - qA.z * rel.y,
+                 qA.w * rel.y - qA.x * rel.z + qA.y * rel.w + qA.z * rel.x,
+                 qA.w * rel.z + qA.x * rel.y - qA.y * rel.x + qA.z * rel.w,
+                 qA.w * rel.w - qA.x * rel.x - qA.y * rel.y - qA.z * rel.z};
+        shape_supporting_face(hit.faceB, sb, dirB, posB, quatB);
+    }
+    return true;
+}
+
+// collideSphereVsSphere sphere.ts:319-410
+inline bool collide_sphere_vs_sphere(Hit &hit, const Shape &sa, V3 pA, const Shape &sb, V3 pB) {
+    double rA = sa.radius * 1.0, rB = sb.radius * 1.0;
+    double dx = pB.x - pA.x, dy = pB.y - pA.y, dz = pB.z - pA.z;
+    double ds = dx * dx + dy * dy + dz * dz;
+    double rs = rA + rB;
+    if (ds >= rs * rs) return false;
+    double d = std::sqrt(ds);
+    double pen = rs - d;
+    V3 n;
+    if (d > 0) {
+        double inv = 1 / d;
+        n = {dx * inv, dy * inv, dz * inv};
+    } else {
+        n = {0, 1, 0};
+    }
+    hit.pa = {pA.x + n.x * rA, pA.y + n.y * rA, pA.z + n.z * rA};
+    hit.pb = {pB.x - n.x * rB, pB.y - n.y * rB, pB.z - n.z * rB};
+    hit.axis = n;
+    hit.penetration = pen;
+    hit.subA = hit.subB = EMPTY_SUB_SHAPE_ID;
+    hit.faceA.n = 0;
+    hit.faceB.n = 0;
+    return true;
+}
+
+// collideShapeVsShape narrowphase.ts:172-238 (dispatch for the supported convex shapes)
+inline bool collide_shapes(Hit &hit, const CollideSettings &cs, const Shape &sa, V3 pA, Q4 qA, const Shape &sb,
+                           V3 pB, Q4 qB) {
+    if (sa.type == SHAPE_SPHERE && sb.type == SHAPE_SPHERE) return collide_sphere_vs_sphere(hit, sa, pA, sb, pB);
+    return collide_convex_vs_convex(hit, cs, sa, pA, qA, sb, pB, qB);
+}
+
+}  // namespace orc

@@ -1,0 +1,198 @@
+"""ctypes wrapper of the FP64 CPU oracle (oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg; never by the library.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+
+F_COUNT = 28  # doubles per body row, see oracle.cpp (enum F_*)
+STATE = 17    # pos3 quat4 linvel3 angvel3 com3 sleeping
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB):
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("oracle_build", os.path.join(HERE, "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    lib = C.CDLL(LIB)
+    vp, dp, ip, i32 = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_int
+    sig = {
+        "orc_world_create": ([dp, i32, ip, i32, vp, vp, vp], vp),
+        "orc_world_destroy": ([vp], None),
+        "orc_add_bodies": ([vp, dp, i32], i32),
+        "orc_body_count": ([vp], i32),
+        "orc_get_state": ([vp, dp], i32),
+        "orc_set_state": ([vp, dp], i32),
+        "orc_step": ([vp, C.c_double, i32], i32),
+        "orc_pair_count": ([vp], i32),
+        "orc_get_pairs": ([vp, ip], i32),
+        "orc_get_aabbs": ([vp, dp], i32),
+        "orc_manifold_count": ([vp], i32),
+        "orc_get_manifolds": ([vp, dp], i32),
+        "orc_island_count": ([vp], i32),
+        "orc_clip_poly_vs_plane": ([dp, i32, dp, dp, dp], i32),
+        "orc_clip_poly_vs_poly": ([dp, i32, dp, i32, dp, dp], i32),
+        "orc_manifold_between_faces": ([dp, dp, dp, C.c_double, dp, i32, dp, i32, dp, dp], i32),
+        "orc_prune_contact_points": ([dp, dp, i32, dp], i32),
+        "orc_barycentric": ([dp, dp, dp, i32, dp], None),
+        "orc_collide_pair": ([dp, dp, C.c_double, dp], i32),
+        "orc_inverse_inertia": ([dp, dp], None),
+    }
+    for k, (a, r) in sig.items():
+        f = getattr(lib, k)
+        f.argtypes = a
+        f.restype = r
+    _lib = lib
+    return lib
+
+
+def dptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def iptr(a: np.ndarray):
+    assert a.dtype == np.int32 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def rows_from_bodies(b: np.ndarray) -> np.ndarray:
+    """BODY_DTYPE array -> oracle rows (the FP32 inputs promoted exactly to FP64)."""
+    n = len(b)
+    r = np.zeros((n, F_COUNT), dtype=np.float64)
+    r[:, 0] = b["shape_type"]
+    r[:, 1:5] = b["shape_params"].astype(np.float64)
+    r[:, 5] = b["density"]
+    r[:, 6] = b["motion_type"]
+    r[:, 7:10] = b["position"]
+    r[:, 10:14] = b["quaternion"]
+    r[:, 14:17] = b["linear_velocity"]
+    r[:, 17:20] = b["angular_velocity"]
+    r[:, 20] = b["friction"]
+    r[:, 21] = b["restitution"]
+    r[:, 22] = b["object_layer"]
+    r[:, 23] = b["gravity_factor"]
+    r[:, 24] = b["linear_damping"]
+    r[:, 25] = b["angular_damping"]
+    r[:, 26] = b["allow_sleeping"]
+    r[:, 27] = b["world"]
+    return np.ascontiguousarray(r)
+
+
+def settings_array(ws) -> np.ndarray:
+    """WorldSettings (crashcat_gb300.world) -> the oracle's settings vector."""
+    s = np.zeros(20, dtype=np.float64)
+    s[0:3] = ws.gravity
+    s[3] = ws.speculative_contact_distance
+    s[4] = ws.manifold_tolerance
+    s[5] = ws.collision_tolerance
+    s[6] = ws.penetration_tolerance
+    s[7] = ws.normal_cos_max_delta_rotation
+    s[8] = ws.contact_point_preserve_lambda_max_dist_sq
+    s[9] = ws.velocity_iterations
+    s[10] = ws.position_iterations
+    s[11] = 1.0 if ws.warm_starting else 0.0
+    s[12] = ws.penetration_slop
+    s[13] = ws.baumgarte_factor
+    s[14] = ws.max_penetration_distance
+    s[15] = ws.min_velocity_for_restitution
+    s[16] = 1.0 if ws.allow_sleeping else 0.0
+    s[17] = ws.time_before_sleep
+    s[18] = ws.point_velocity_sleep_threshold
+    s[19] = 1.0 if ws.gravity_enabled else 0.0
+    return s
+
+
+class OracleWorld:
+    """One oracle world built from the same bodies and settings as a GPU world."""
+
+    def __init__(self, ws, bodies: np.ndarray):
+        lib = load()
+        self.lib = lib
+        L = ws.layers
+        n_obj, n_bp = len(L.object_to_broadphase), L.broadphase_layers
+        obj_to_bp = np.array(L.object_to_broadphase, dtype=np.int32)
+        op = np.zeros((n_obj, n_obj), dtype=np.uint8)
+        ovb = np.zeros((n_obj, n_bp), dtype=np.uint8)
+        bpp = np.zeros((n_bp, n_bp), dtype=np.uint8)
+        for a in range(n_obj):
+            for b in range(n_obj):
+                op[a, b] = (L.object_pairs[a] >> b) & 1
+            for b in range(n_bp):
+                ovb[a, b] = (L.object_vs_broadphase[a] >> b) & 1
+        for a in range(n_bp):
+            for b in range(n_bp):
+                bpp[a, b] = (L.broadphase_pairs[a] >> b) & 1
+        self._keep = (op, ovb, bpp, obj_to_bp)
+        s = settings_array(ws)
+        self.h = lib.orc_world_create(dptr(s), n_obj, iptr(obj_to_bp), n_bp, op.ctypes.data, ovb.ctypes.data,
+                                      bpp.ctypes.data)
+        rows = rows_from_bodies(bodies)
+        assert lib.orc_add_bodies(self.h, dptr(rows), len(rows)) == 0
+        self.n = len(rows)
+
+    def close(self):
+        if self.h:
+            self.lib.orc_world_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, dt: float, n: int = 1):
+        self.lib.orc_step(self.h, dt, n)
+
+    def state(self) -> np.ndarray:
+        o = np.zeros((self.n, STATE), dtype=np.float64)
+        self.lib.orc_get_state(self.h, dptr(o))
+        return o
+
+    def set_state(self, st: np.ndarray):
+        st = np.ascontiguousarray(st, dtype=np.float64)
+        self.lib.orc_set_state(self.h, dptr(st))
+
+    def pairs(self) -> np.ndarray:
+        n = self.lib.orc_pair_count(self.h)
+        o = np.zeros((max(n, 1), 2), dtype=np.int32)
+        self.lib.orc_get_pairs(self.h, iptr(o))
+        return o[:n]
+
+    def aabbs(self) -> np.ndarray:
+        o = np.zeros((self.n, 6), dtype=np.float64)
+        self.lib.orc_get_aabbs(self.h, dptr(o))
+        return o
+
+    def manifolds(self) -> np.ndarray:
+        n = self.lib.orc_manifold_count(self.h)
+        o = np.zeros((max(n, 1), 32), dtype=np.float64)
+        self.lib.orc_get_manifolds(self.h, dptr(o))
+        return o[:n]
+
+
+def state_to_gpu_rows(st: np.ndarray) -> np.ndarray:
+    """oracle state rows (17 doubles) -> GPU state rows (16 floats)."""
+    return np.ascontiguousarray(st[:, :16], dtype=np.float32)
+
+
+def gpu_rows_to_state(rows: np.ndarray) -> np.ndarray:
+    o = np.zeros((len(rows), STATE), dtype=np.float64)
+    o[:, :16] = rows
+    return o
