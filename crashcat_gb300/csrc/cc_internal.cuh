@@ -77,6 +77,7 @@ struct DevSettings {
     float time_before_sleep;
     float sleep_threshold;
     uint32_t allowed_pairs[CC_MAX_LAYERS];  // combined layer predicate, bit j of [i]
+    int small_island_max_cons;  // islands up to this many contacts run on one thread
 };
 
 // Manifold produced by the narrowphase for one body pair (<= 4 points),

@@ -29,8 +29,8 @@ void upload_settings_solver(const DevSettings &s, cudaStream_t st) {
 }
 
 constexpr unsigned long long EMPTY_KEY = 0xffffffffffffffffull;
-constexpr int SMALL_ISLAND_MAX_CONS = 8;
-constexpr int SMALL_ISLAND_MAX_BODIES = 24;
+constexpr int SMALL_ISLAND_MAX_CONS = 64;  // upper bound of the per-thread class (register arrays)
+constexpr int SMALL_ISLAND_MAX_BODIES = 64;
 
 struct CacheTables {
     unsigned long long *keys[2];
@@ -331,12 +331,16 @@ __global__ void k_apply_wake(DevWorld w) {
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ bool active_body(uint32_t f) { return motion_of(f) != STATIC && !sleeping_of(f); }
 
+// Union-find root with path splitting.  Parent links written by other CTAs
+// must be seen while linking, so loads bypass L1 (__ldcg) and stores go to L2
+// (__stcg); a plain load could keep returning a stale L1 line, making a CAS
+// retry loop spin on a root that was already hooked elsewhere.
 __device__ int uf_find(int *parent, int i) {
     while (true) {
-        int p = parent[i];
+        int p = __ldcg(&parent[i]);
         if (p == i) return i;
-        int gp = parent[p];
-        if (gp != p) parent[i] = gp;  // path halving
+        int gp = __ldcg(&parent[p]);
+        if (gp != p) __stcg(&parent[i], gp);  // path splitting
         i = p;
     }
 }
@@ -357,12 +361,20 @@ __global__ void k_uf_link(DevWorld w) {
         if (w.cons_of_manifold[ci] < 0) continue;
         int a = w.cons[ci].a, b = w.cons[ci].b;
         if (!active_body(w.flags[a]) || !active_body(w.flags[b])) continue;
-        for (int guard = 0; guard < 1000000; guard++) {
+        bool linked = false;
+        for (int guard = 0; guard < 1 << 20; guard++) {
             int ra = uf_find(w.uf_parent, a), rb = uf_find(w.uf_parent, b);
-            if (ra == rb) break;
+            if (ra == rb) {
+                linked = true;
+                break;
+            }
             int hi = max(ra, rb), lo = min(ra, rb);
-            if (atomicCAS(&w.uf_parent[hi], hi, lo) == hi) break;
+            if (atomicCAS(&w.uf_parent[hi], hi, lo) == hi) {
+                linked = true;
+                break;
+            }
         }
+        if (!linked) atomicOr(&w.ctr->overflow, OVF_ISLAND);  // bounded retry gave up: report it
     }
 }
 
@@ -417,7 +429,7 @@ __global__ void k_island_classify(DevWorld w, int *small_list, int *large_list) 
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x) {
         int nc = w.island_cons_count[i], nb = w.island_body_count[i];
         atomicMax(&w.ctr->max_island_constraints, nc);
-        if (nc <= SMALL_ISLAND_MAX_CONS && nb <= SMALL_ISLAND_MAX_BODIES) {
+        if (nc <= c_settings.small_island_max_cons && nb <= SMALL_ISLAND_MAX_BODIES) {
             int k = atomicAdd(&w.ctr->num_small_islands, 1);
             small_list[k] = i;
         } else {
@@ -564,7 +576,8 @@ __device__ bool solve_position_con(DevWorld &w, const ContactConstraint &c, Pose
                                    uint32_t fa, uint32_t fb) {
     if (ma != DYNAMIC && mb != DYNAMIC) return false;
     bool any = false;
-    Mat3 RA = quat_to_mat(PA.q), RB = quat_to_mat(PB.q);
+    // rotations and inverse inertias are taken once per contact, as the reference does
+    const Mat3 RA = quat_to_mat(PA.q), RB = quat_to_mat(PB.q);
     Sym3 IA{0, 0, 0, 0, 0, 0}, IB{0, 0, 0, 0, 0, 0};
     if (ma == DYNAMIC) IA = world_inv_inertia(PA.q, w.inertia_rot[c.a], xyz(w.inv_inertia[c.a]), dof_of(fa));
     if (mb == DYNAMIC) IB = world_inv_inertia(PB.q, w.inertia_rot[c.b], xyz(w.inv_inertia[c.b]), dof_of(fb));
@@ -588,7 +601,6 @@ __device__ bool solve_position_con(DevWorld &w, const ContactConstraint &c, Pose
             if (!(d & 2)) PA.com.y = 0.f;
             if (!(d & 4)) PA.com.z = 0.f;
             PA.q = rotation_step(PA.q, -(symmul(IA, cross3(rA, c.normal)) * lambda));
-            RA = quat_to_mat(PA.q);
         }
         if (mb == DYNAMIC) {
             PB.com = PB.com + c.normal * (lambda * c.invMassB);
@@ -597,7 +609,6 @@ __device__ bool solve_position_con(DevWorld &w, const ContactConstraint &c, Pose
             if (!(d & 2)) PB.com.y = 0.f;
             if (!(d & 4)) PB.com.z = 0.f;
             PB.q = rotation_step(PB.q, symmul(IB, cross3(rB, c.normal)) * lambda);
-            RB = quat_to_mat(PB.q);
         }
         any = true;
     }

@@ -7,6 +7,7 @@
 // 390-434), updateWorld (src/update.ts:45-239).
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -151,6 +152,13 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
     d.allow_sleeping = s->allow_sleeping;
     d.time_before_sleep = (float)s->time_before_sleep;
     d.sleep_threshold = (float)s->point_velocity_sleep_threshold;
+    // launch-shape tunable: islands with at most this many contacts are solved by one
+    // thread in the reference's exact order, larger ones by a CTA with graph colouring
+    d.small_island_max_cons = 8;
+    if (const char *e = getenv("CRASHCAT_SMALL_ISLAND_MAX")) {
+        int v = atoi(e);
+        if (v >= 0 && v <= 64) d.small_island_max_cons = v;
+    }
     // combined layer predicate: object layer pair enabled AND the querying
     // layer may query the other's broadphase layer AND the broadphase layers
     // collide (broadphase.ts:252-272, dbvt.ts:657-660)
@@ -590,9 +598,11 @@ int cc_world_get_manifolds(cc_world *W, float *out, int32_t capacity, int32_t *c
     if (nm > w.max_manifolds) nm = w.max_manifolds;
     std::vector<Manifold> ms(nm);
     std::vector<int> cm(nm);
+    std::vector<ContactConstraint> cs(nm);
     if (nm > 0) {
         CC_TRY(cudaMemcpy(ms.data(), w.manifolds, sizeof(Manifold) * nm, cudaMemcpyDeviceToHost));
         CC_TRY(cudaMemcpy(cm.data(), w.cons_of_manifold, sizeof(int) * nm, cudaMemcpyDeviceToHost));
+        CC_TRY(cudaMemcpy(cs.data(), w.cons, sizeof(ContactConstraint) * nm, cudaMemcpyDeviceToHost));
     }
     int k = 0;
     for (int i = 0; i < nm; i++) {
@@ -613,7 +623,9 @@ int cc_world_get_manifolds(cc_world *W, float *out, int32_t capacity, int32_t *c
             o[4] = nn.y;
             o[5] = nn.z;
             o[6] = m.depth;
-            o[7] = 0.f;
+            float lsum = 0.f;  // accumulated normal impulse of the contact after the solve
+            for (int j = 0; j < cs[i].n; j++) lsum += cs[i].p[j].lam_n;
+            o[7] = lsum;
             for (int j = 0; j < 4; j++) {
                 float *p = o + 8 + 6 * j;
                 if (j < m.n) {
@@ -629,6 +641,37 @@ int cc_world_get_manifolds(cc_world *W, float *out, int32_t capacity, int32_t *c
                     for (int t = 0; t < 6; t++) p[t] = 0.f;
                 }
             }
+        }
+        k++;
+    }
+    *count = k;
+    return CC_OK;
+}
+
+// Diagnostic readout of the last step's islands: island index per body (-1 for
+// static or sleeping bodies) and, per contact constraint, (bodyA, bodyB, island).
+int cc_world_debug_islands(cc_world *W, int32_t *island_of_body, int32_t *cons_rows, int32_t capacity,
+                           int32_t *count) {
+    if (!W || !count) return CC_ERR_INVALID;
+    DevWorld &w = W->w;
+    int nm = W->last_ctr.num_manifolds;
+    if (nm > w.max_manifolds) nm = w.max_manifolds;
+    std::vector<ContactConstraint> cs(nm);
+    std::vector<int> cm(nm);
+    if (nm > 0) {
+        CC_TRY(cudaMemcpy(cs.data(), w.cons, sizeof(ContactConstraint) * nm, cudaMemcpyDeviceToHost));
+        CC_TRY(cudaMemcpy(cm.data(), w.cons_of_manifold, sizeof(int) * nm, cudaMemcpyDeviceToHost));
+    }
+    if (island_of_body && w.n > 0)
+        CC_TRY(cudaMemcpy(island_of_body, w.island_of_body, sizeof(int) * w.n, cudaMemcpyDeviceToHost));
+    int k = 0;
+    for (int i = 0; i < nm; i++) {
+        if (cm[i] < 0) continue;
+        if (cons_rows) {
+            if (k >= capacity) return CC_ERR_CAPACITY;
+            cons_rows[3 * k] = cs[i].a;
+            cons_rows[3 * k + 1] = cs[i].b;
+            cons_rows[3 * k + 2] = cs[i].island;
         }
         k++;
     }

@@ -121,7 +121,8 @@ def batched_worlds(num_worlds: int = 4096, seed: int = 4, n_min: int = 8, n_max:
     """num_worlds independent worlds with body counts drawn log-uniformly from
     [n_min, n_max]; boxes (half extents 0.2-0.8 m) and spheres (r 0.2-0.6 m),
     each world with its own static floor and seeded drop positions on a jittered
-    2 m grid; dt 1/120, 8/2 iterations, 1,000 steps."""
+    3 m grid (wide enough for the largest rotated box); dt 1/120, 8/2
+    iterations, 1,000 steps."""
     rng = np.random.Generator(np.random.PCG64(seed))
     counts = np.rint(np.exp(rng.uniform(math.log(n_min), math.log(n_max), size=num_worlds))).astype(np.int64)
     counts = np.clip(counts, n_min, n_max)
@@ -129,7 +130,7 @@ def batched_worlds(num_worlds: int = 4096, seed: int = 4, n_min: int = 8, n_max:
     b = blank_bodies(total)
     o = 0
     for wi in range(num_worlds):
-        static_floor(b, o, half=(40.0, 0.5, 40.0), friction=0.5, world=wi)
+        static_floor(b, o, half=(30.0, 0.5, 30.0), friction=0.5, world=wi)
         o += 1
         c = int(counts[wi])
         sl = slice(o, o + c)
@@ -145,7 +146,7 @@ def batched_worlds(num_worlds: int = 4096, seed: int = 4, n_min: int = 8, n_max:
         side = 8
         layer = np.arange(c) // (side * side)
         cell = np.arange(c) % (side * side)
-        pos = np.stack([(cell % side - (side - 1) / 2) * 2.0, 1.5 + layer * 2.0, (cell // side - (side - 1) / 2) * 2.0], 1)
+        pos = np.stack([(cell % side - (side - 1) / 2) * 3.0, 1.5 + layer * 3.0, (cell // side - (side - 1) / 2) * 3.0], 1)
         pos += rng.uniform(-0.1, 0.1, size=(c, 3))
         b["position"][sl] = pos.astype(np.float32)
         b["quaternion"][sl] = random_quaternions(rng, c)
@@ -215,3 +216,36 @@ def free_fall(n: int = 256, seed: int = 11) -> Scene:
     b["angular_velocity"] = rng.normal(scale=2.0, size=(n, 3)).astype(np.float32)
     b["allow_sleeping"] = 0
     return Scene("free_fall", b, dt=1.0 / 60.0, steps=30, seed=seed)
+
+
+def box_stack(height: int = 10, seed: int = 21, half: float = 0.5, jitter: float = 0.02) -> Scene:
+    """A single column of boxes with small seeded offsets, 1 cm above each other."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = blank_bodies(height + 1)
+    static_floor(b, 0, half=(20.0, 0.5, 20.0), friction=0.5)
+    idx = np.arange(1, height + 1)
+    set_box(b, idx, (half, half, half))
+    b["friction"][idx] = 0.5
+    pos = np.zeros((height, 3))
+    pos[:, 1] = half + 0.01 + np.arange(height) * (2 * half + 0.01)
+    pos[:, [0, 2]] = rng.uniform(-jitter, jitter, size=(height, 2))
+    b["position"][idx] = pos.astype(np.float32)
+    return Scene("box_stack", b, dt=1.0 / 60.0, steps=120, seed=seed)
+
+
+def box_row(count: int = 6, seed: int = 31, gap: float = -0.005) -> Scene:
+    """A row of equal boxes resting on the floor, each slightly pressed into its
+    neighbour: one island whose contacts split into several colours."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = blank_bodies(count + 1)
+    static_floor(b, 0, half=(20.0, 0.5, 20.0), friction=0.5)
+    idx = np.arange(1, count + 1)
+    set_box(b, idx, (0.5, 0.5, 0.5))
+    b["friction"][idx] = 0.5
+    pos = np.zeros((count, 3))
+    pos[:, 0] = np.arange(count) * (1.0 + gap)
+    pos[:, 1] = 0.5 - 0.003
+    pos[:, 2] = rng.uniform(-0.05, 0.05, size=count)
+    b["position"][idx] = pos.astype(np.float32)
+    b["linear_velocity"][idx] = rng.normal(scale=0.5, size=(count, 3)).astype(np.float32)
+    return Scene("box_row", b, dt=1.0 / 60.0, steps=1, seed=seed)

@@ -294,6 +294,15 @@ class GpuWorld:
               "cc_world_get_manifolds")
         return out[: cnt.value]
 
+    def debug_islands(self):
+        cnt = C.c_int32()
+        check(self._lib.cc_world_debug_islands(self.handle, None, None, 0, C.byref(cnt)), "cc_world_debug_islands")
+        iob = np.zeros(max(self.n, 1), dtype=np.int32)
+        rows = np.zeros((max(cnt.value, 1), 3), dtype=np.int32)
+        check(self._lib.cc_world_debug_islands(self.handle, ptr(iob), ptr(rows), cnt.value, C.byref(cnt)),
+              "cc_world_debug_islands")
+        return iob[: self.n], rows[: cnt.value]
+
     def stats(self) -> dict:
         s = _lib.Stats()
         check(self._lib.cc_world_get_stats(self.handle, C.byref(s)), "cc_world_get_stats")

@@ -161,11 +161,18 @@ int cc_world_set_state(cc_world *world, const float *rows);
 int cc_world_get_pairs(cc_world *world, int32_t *out, int32_t capacity, int32_t *count);
 
 /* Contact manifolds of the last step, 32 floats each: bodyA, bodyB (ordered by
- * id), point count, normal[3] (A to B), penetration depth, 0, then 4 x
- * (world point on A[3], world point on B[3]). */
+ * id), point count, normal[3] (A to B), penetration depth, summed normal
+ * impulse of the contact after the velocity solve, then 4 x (world point on
+ * A[3], world point on B[3]). */
 int cc_world_get_manifolds(cc_world *world, float *out, int32_t capacity, int32_t *count);
 
 int cc_world_get_stats(cc_world *world, cc_stats *out);
+
+/* Diagnostic readout with no reference counterpart: island index per body of
+ * the last step (-1 for static or sleeping bodies) and, per contact
+ * constraint, the rows (bodyA, bodyB, island). */
+int cc_world_debug_islands(cc_world *world, int32_t *island_of_body, int32_t *cons_rows, int32_t capacity,
+                           int32_t *count);
 
 const char *cc_status_string(int status);
 

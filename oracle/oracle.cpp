@@ -143,10 +143,15 @@ struct World {
     std::vector<ContactConstraint> constraints;
     std::vector<Island> islands;
     double prevDt = 0;
+    // diagnostic: solve each island's contacts in greedy-colour order (the order a
+    // colour-parallel sweep realises) instead of the reference's sorted order
+    bool colouredOrder = false;
+    int reorderedIslands = 0;
     // per-step diagnostics
     std::vector<std::pair<int, int>> pairs;
     std::vector<Manifold> manifolds;  // manifolds that produced constraints, after id ordering
     std::vector<std::pair<int, int>> manifoldBodies;
+    std::vector<double> manifoldLambda;  // summed normal impulse per manifold after the solve
     double bodySteps = 0;
 };
 
@@ -1064,6 +1069,7 @@ static void check_island_sleep(World &w, Island &is, double dt) {
 // ---------------------------------------------------------------------------
 static void step(World &w, double dt) {
     w.constraints.clear();
+    w.manifoldLambda.clear();
     w.manifolds.clear();
     w.manifoldBodies.clear();
     for (auto &kv : w.contacts) kv.second.processed = false;
@@ -1134,9 +1140,44 @@ static void step(World &w, double dt) {
                 if (ia != ib) return ia < ib;
                 return w.bodies[ca.bodyB].id < w.bodies[cb.bodyB].id;
             });
+            if (w.colouredOrder) {
+                std::vector<int> &ci = is.contactIndices;
+                std::vector<int> col(ci.size(), -1);
+                std::map<int, size_t> claim;
+                for (int round = 0;; round++) {
+                    claim.clear();
+                    bool left = false;
+                    for (size_t k = 0; k < ci.size(); k++) {
+                        if (col[k] >= 0) continue;
+                        left = true;
+                        const ContactConstraint &c = w.constraints[ci[k]];
+                        for (int bi : {c.bodyA, c.bodyB})
+                            if (w.bodies[bi].motion == DYNAMIC && !claim.count(bi)) claim[bi] = k;
+                    }
+                    if (!left) break;
+                    for (size_t k = 0; k < ci.size(); k++) {
+                        if (col[k] >= 0) continue;
+                        const ContactConstraint &c = w.constraints[ci[k]];
+                        bool ok = true;
+                        for (int bi : {c.bodyA, c.bodyB})
+                            if (w.bodies[bi].motion == DYNAMIC && claim[bi] != k) ok = false;
+                        if (ok) col[k] = round;
+                    }
+                }
+                std::vector<size_t> ord(ci.size());
+                std::iota(ord.begin(), ord.end(), 0);
+                std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return col[a] < col[b]; });
+                std::vector<int> re(ci.size());
+                for (size_t k = 0; k < ord.size(); k++) re[k] = ci[ord[k]];
+                if (re != ci) w.reorderedIslands++;
+                ci = re;
+            }
             for (int i = 0; i < is.velSteps; i++) solve_velocity(w, is.contactIndices);
         }
         // storeAppliedImpulses contact-constraints.ts:1061-1076
+        w.manifoldLambda.assign(w.constraints.size(), 0.0);
+        for (size_t k = 0; k < w.constraints.size(); k++)
+            for (int i = 0; i < w.constraints[k].n; i++) w.manifoldLambda[k] += w.constraints[k].pts[i].n.totalLambda;
         for (ContactConstraint &c : w.constraints) {
             Contact &ct = w.contacts[c.contactKey];
             for (int i = 0; i < c.n; i++) {
@@ -1301,6 +1342,8 @@ int orc_add_bodies(void *wp, const double *rows, int n) {
 }
 
 int orc_body_count(void *wp) { return (int)((World *)wp)->bodies.size(); }
+void orc_set_coloured_order(void *wp, int on) { ((World *)wp)->colouredOrder = on != 0; }
+int orc_reordered_islands(void *wp) { return ((World *)wp)->reorderedIslands; }
 
 // state rows: pos3 quat4 linvel3 angvel3 com3 sleeping1 = 17 doubles
 int orc_get_state(void *wp, double *out) {
@@ -1392,7 +1435,7 @@ int orc_get_manifolds(void *wp, double *out) {
         o[4] = m.normal.y;
         o[5] = m.normal.z;
         o[6] = m.depth;
-        o[7] = 0;
+        o[7] = i < w.manifoldLambda.size() ? w.manifoldLambda[i] : 0;
         for (int k = 0; k < 4; k++) {
             double *p = o + 8 + 6 * k;
             if (k < m.n) {

@@ -36,6 +36,8 @@ def load():
         "orc_world_destroy": ([vp], None),
         "orc_add_bodies": ([vp, dp, i32], i32),
         "orc_body_count": ([vp], i32),
+        "orc_set_coloured_order": ([vp, i32], None),
+        "orc_reordered_islands": ([vp], i32),
         "orc_get_state": ([vp, dp], i32),
         "orc_set_state": ([vp, dp], i32),
         "orc_step": ([vp, C.c_double, i32], i32),
