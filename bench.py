@@ -1,0 +1,406 @@
+"""Benchmark of the GB300 world step on the batched uneven-worlds workload.
+
+Workload: 4,096 independent worlds whose body counts are drawn log-uniformly
+from 8 to 512 (boxes and spheres, each world with its own static floor), dt
+1/120 s, 8 velocity / 2 position iterations; a "step" advances every world
+once.  Metric: body-steps/s (higher is better).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl gb300 (default): value = bodies x K / device time of K steps (CUDA
+events on the library's stream, body state resident in HBM); e2e = the same
+metric through cc_world_step_host with the body state rows uploaded from and
+read back into pinned host memory every step; roofline of the dominant stage
+from the stage profiler; cpu_baseline = the FP64 oracle port timed single
+threaded on a bounded sample of the same worlds.
+
+--impl reference: the reference (TypeScript) cannot run on this machine; its FP64
+C++ restatement (oracle/) steps a bounded sample of the same worlds on all
+host cores (one process per core, worlds split across them).
+
+Under torchrun (N > 1) every rank steps its own 4,096 worlds (weak scaling, no
+collective on the data path); timing is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+WORKLOAD = "batched_uneven_worlds"
+METRIC = "body-steps/s"
+STAGES = ("integrate_forces", "broadphase", "narrowphase", "contacts_islands", "solver")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--worlds", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=4)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--settle", type=int, default=360,
+                    help="untimed steps before the warm-up so the timed steps are contact-rich")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def read_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{gpu_index}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def algorithmic_bytes(stage: str, st: dict, n_bodies: int) -> float:
+    """Compulsory FP32 bytes of one stage per step (each datum counted once).
+
+    Per awake body 216 B (state read 76, properties 64, state write 52, AABB 24),
+    per body 104 B for the tree (AABB 24, key/index 16, node write + read 64),
+    per pair 16 B (write + read) plus 72 B of narrowphase input (two transforms
+    and shape handles), per manifold (20 + 24 P) B written by the narrowphase,
+    (48 + 180 P) B of constraint rows written by the contact setup and read by
+    the solver, and 24 P B of impulse cache, P = mean points per manifold.
+    """
+    na = st["num_awake"]
+    npairs = st["num_pairs"]
+    nm = max(st["num_manifolds"], 0)
+    P = (st["num_contact_points"] / nm) if nm else 0.0
+    if stage == "integrate_forces":
+        return 148.0 * na
+    if stage == "broadphase":
+        return 104.0 * n_bodies + 16.0 * npairs
+    if stage == "narrowphase":
+        return 72.0 * npairs + (20 + 24 * P) * nm
+    if stage == "contacts_islands":
+        return (20 + 24 * P) * nm + (48 + 180 * P) * nm + 24 * P * nm
+    if stage == "solver":
+        return 216.0 * na + (48 + 180 * P) * nm + 24 * P * nm
+    raise ValueError(stage)
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (the oracle is test infrastructure: only the baseline legs use it)
+# ---------------------------------------------------------------------------
+def _cpu_worker(args):
+    """Steps a list of worlds with the FP64 oracle; returns seconds for `steps` steps."""
+    bodies_list, dt, vel, pos, steps = args
+    sys.path.insert(0, ROOT)
+    from crashcat_gb300 import world as W
+    from oracle import pyoracle
+    ws = W.standard_settings(velocity_iterations=vel, position_iterations=pos)
+    worlds = [pyoracle.OracleWorld(ws, b) for b in bodies_list]
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for o in worlds:
+            o.step(dt, 1)
+    return time.perf_counter() - t0
+
+
+def _cpu_process(bodies_list, dt, vel, pos, settle, warmup, steps, barrier, out_q, slot):
+    """One host core of the reference leg: settle + warm up its worlds, then time `steps`
+    steps after every core has reached the barrier."""
+    sys.path.insert(0, ROOT)
+    from crashcat_gb300 import world as W
+    from oracle import pyoracle
+    ws = W.standard_settings(velocity_iterations=vel, position_iterations=pos)
+    worlds = [pyoracle.OracleWorld(ws, b) for b in bodies_list]
+    for o in worlds:
+        o.step(dt, settle + warmup)
+    barrier.wait()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for o in worlds:
+            o.step(dt, 1)
+    out_q.put((slot, time.perf_counter() - t0))
+
+
+def split_worlds(scene):
+    w = scene.bodies["world"]
+    starts = np.flatnonzero(np.r_[True, np.diff(w) != 0])
+    ends = np.r_[starts[1:], len(w)]
+    return [scene.bodies[s:e].copy() for s, e in zip(starts, ends)]
+
+
+def cpu_baseline_single(scene, seconds: float, state_rows=None):
+    """Single-threaded oracle on the first worlds of the workload, ~`seconds` of work,
+    starting from `state_rows` (the GPU's state after its timed steps) when given."""
+    from oracle import build as obuild
+    obuild.build()
+    if state_rows is not None:
+        b = scene.bodies.copy()
+        b["position"] = state_rows[:, 0:3]
+        b["quaternion"] = state_rows[:, 3:7]
+        b["linear_velocity"] = state_rows[:, 7:10]
+        b["angular_velocity"] = state_rows[:, 10:13]
+        scene = type(scene)(**{**scene.__dict__, "bodies": b})
+    worlds = split_worlds(scene)
+    # calibrate on a handful of worlds
+    probe = worlds[:16]
+    nb = sum(len(b) for b in probe)
+    t = _cpu_worker((probe, scene.dt, scene.velocity_iterations, scene.position_iterations, 2))
+    per_body_step = max(t / (2 * nb), 1e-7)
+    steps = 10
+    target_bodies = int(seconds / (per_body_step * steps))
+    sample, tot = [], 0
+    for b in worlds:
+        if tot >= target_bodies:
+            break
+        sample.append(b)
+        tot += len(b)
+    t = _cpu_worker((sample, scene.dt, scene.velocity_iterations, scene.position_iterations, steps))
+    return {"value": tot * steps / t, "unit": METRIC, "cores": 1, "kind": "port",
+            "sample": f"first {len(sample)} of {len(worlds)} worlds ({tot} bodies), {steps} steps from the "
+                      f"GPU's settled state, FP64 oracle, one thread, {t:.1f} s"}
+
+
+def run_reference(args, rank, world_size):
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from crashcat_gb300 import scenes
+    from oracle import build as obuild
+    obuild.build()
+    scene = scenes.batched_worlds(num_worlds=args.worlds, seed=args.seed)
+    worlds = split_worlds(scene)
+    cores = os.cpu_count() or 1
+    # bounded sample: 32 worlds per host core, stepped in parallel (one process per core)
+    sample = worlds[: min(len(worlds), 32 * cores)]
+    nb = sum(len(b) for b in sample)
+    chunks = [sample[i::cores] for i in range(cores)]
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(cores + 1)
+    out_q = ctx.Queue()
+    procs = [ctx.Process(target=_cpu_process, args=(c, scene.dt, scene.velocity_iterations,
+                                                    scene.position_iterations, args.settle, args.warmup,
+                                                    args.steps, barrier, out_q, i)) for i, c in enumerate(chunks)]
+    for p in procs:
+        p.start()
+    barrier.wait()
+    t0 = time.perf_counter()
+    times = [out_q.get()[1] for _ in procs]
+    wall = time.perf_counter() - t0
+    for p in procs:
+        p.join()
+    value = nb * args.steps / wall
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "worlds": args.worlds, "sample_worlds": len(sample),
+                   "sample_bodies": nb, "dt": scene.dt, "velocity_iterations": scene.velocity_iterations,
+                   "position_iterations": scene.position_iterations, "seed": args.seed,
+                   "settle_steps": args.settle},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
+                         "sample": f"{len(sample)} worlds ({nb} bodies) split over {cores} processes, timed "
+                                   f"after {args.settle + args.warmup} untimed steps; the TypeScript reference "
+                                   f"cannot run here, its FP64 C++ restatement is timed (slowest process "
+                                   f"{max(times):.2f} s)"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU leg
+# ---------------------------------------------------------------------------
+def run_gpu(args, rank, world_size, local):
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world_size > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from crashcat_gb300 import _lib, build, scenes, world as W
+    build.build()
+    _lib.load()
+    scene = scenes.batched_worlds(num_worlds=args.worlds, seed=args.seed + rank)
+    ws = W.standard_settings(velocity_iterations=scene.velocity_iterations,
+                             position_iterations=scene.position_iterations)
+    ws.num_worlds = scene.num_worlds
+    n = scene.n
+    g = W.GpuWorld(ws, n + 64)
+    g.add_bodies(scene.bodies)
+    dt = scene.dt
+    if args.settle:
+        g.step(dt, args.settle)
+    for _ in range(args.warmup):
+        g.step(dt, 1)
+    stats_w = g.stats()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    with ClockSampler(local) as clk:
+        status = g.step(dt, args.steps)
+        barrier()
+    dev_ms = g.stats()["last_call_ms"]
+    t = torch.tensor([dev_ms], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev_ms = float(t.item())
+    stats = g.stats()
+    value = n * args.steps * world_size / (dev_ms * 1e-3)
+
+    # end to end through the host-buffer entry point: pinned rows in and out every step
+    rows, _ = g.get_state()
+    settled_rows = rows.copy()
+    h_in = torch.from_numpy(rows.copy()).pin_memory()
+    h_out = torch.empty_like(h_in).pin_memory()
+    e2e_steps = max(3, min(args.steps, 20))
+    lib = _lib.load()
+    import ctypes as C
+    for _ in range(2):
+        lib.cc_world_step_host(g.handle, C.c_float(dt), C.c_void_p(h_in.data_ptr()), C.c_void_p(h_out.data_ptr()))
+        h_in, h_out = h_out, h_in
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        st = lib.cc_world_step_host(g.handle, C.c_float(dt), C.c_void_p(h_in.data_ptr()),
+                                    C.c_void_p(h_out.data_ptr()))
+        if st not in (0, _lib.CC_ERR_CAPACITY):
+            _lib.check(st, "cc_world_step_host")
+        h_in, h_out = h_out, h_in
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_s = float(te.item())
+    row_bytes = n * _lib.STATE_FLOATS * 4
+
+    # stage profile (CUDA events between stages) for the roofline of the dominant stage
+    prof = g.profile_steps(dt, max(3, min(args.steps, 10)))
+    pst = g.stats()
+    dom = max(prof, key=prof.get)
+    peak, peak_kind = read_peaks()
+    bytes_dom = algorithmic_bytes(dom, pst, n)
+    achieved = bytes_dom / (prof[dom] * 1e-3) / 1e9 if prof[dom] > 0 else 0.0
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic_per_step.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(dom)
+        except Exception:
+            traffic = None
+
+    if rank == 0:
+        cpu = cpu_baseline_single(scene, args.cpu_seconds, settled_rows)
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world_size, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "worlds": args.worlds, "bodies_per_gpu": n,
+                       "dt": dt, "velocity_iterations": scene.velocity_iterations,
+                       "position_iterations": scene.position_iterations, "seed": args.seed,
+                       "settle_steps": args.settle,
+                       "l2": "inputs larger than L2: resident body state and per-step buffers exceed 129 MB",
+                       "parallelism": f"{world_size} x independent world batches"},
+            "e2e": {"value": n * e2e_steps * world_size / e2e_s, "unit": METRIC,
+                    "h2d_bytes_per_step": row_bytes, "d2h_bytes_per_step": row_bytes,
+                    "api": "cc_world_step_host (pinned host rows in and out every step)"},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": bytes_dom, "stage_ms": prof},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": stats["gpu_launches_per_step"] * args.steps,
+            "counters": {k: stats_w[k] for k in ("num_awake", "num_pairs", "num_manifolds", "num_contact_points",
+                                                 "num_epa", "num_islands", "max_island_constraints")},
+            "status": _lib.status_string(status),
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    rank, world_size, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world_size)
+        return
+    run_gpu(args, rank, world_size, local)
+
+
+if __name__ == "__main__":
+    main()

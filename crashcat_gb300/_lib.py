@@ -65,7 +65,8 @@ class Settings(C.Structure):
 class Stats(C.Structure):
     _fields_ = [(n, C.c_int32) for n in (
         "num_bodies", "num_awake", "num_pairs", "num_manifolds", "num_contact_points", "num_epa",
-        "num_islands", "max_island_constraints", "overflow_flags", "gpu_launches_per_step")]
+        "num_islands", "max_island_constraints", "overflow_flags", "gpu_launches_per_step")] + [
+        ("last_call_ms", C.c_float)]
 
 
 # numpy mirror of cc_body_desc (natural C alignment, 4-byte fields only)
@@ -94,6 +95,7 @@ EXPORTS = {
     "cc_world_get_manifolds": ([C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
     "cc_world_get_stats": ([C.c_void_p, C.POINTER(Stats)], C.c_int),
     "cc_world_debug_islands": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
+    "cc_world_profile_steps": ([C.c_void_p, C.c_float, C.c_int32, C.c_void_p, C.c_int32], C.c_int),
     "cc_status_string": ([C.c_int], C.c_char_p),
 }
 

@@ -142,8 +142,10 @@ __device__ __forceinline__ float ord2f(unsigned int u) {
 // bounds for every body + scene bounds of AABB centres (ordered-int atomics)
 __global__ void k_update_bounds(DevWorld w, unsigned int *scene) {
     float3 cmin = f3(3.0e38f, 3.0e38f, 3.0e38f), cmax = f3(-3.0e38f, -3.0e38f, -3.0e38f);
+    int awake = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
         uint32_t f = w.flags[i];
+        if (motion_of(f) != STATIC && !sleeping_of(f)) awake++;
         float3 lo, hi;
         shape_bounds(f, w.shape[i], lo, hi);
         double b[6];
@@ -172,7 +174,9 @@ __global__ void k_update_bounds(DevWorld w, unsigned int *scene) {
         cmax.y = fmaxf(cmax.y, __shfl_xor_sync(0xffffffffu, cmax.y, o));
         cmax.z = fmaxf(cmax.z, __shfl_xor_sync(0xffffffffu, cmax.z, o));
     }
+    for (int o = 16; o > 0; o >>= 1) awake += __shfl_xor_sync(0xffffffffu, awake, o);
     if ((threadIdx.x & 31) == 0) {
+        if (awake) atomicAdd(&w.ctr->num_awake, awake);
         atomicMin(&scene[0], f2ord(cmin.x));
         atomicMin(&scene[1], f2ord(cmin.y));
         atomicMin(&scene[2], f2ord(cmin.z));

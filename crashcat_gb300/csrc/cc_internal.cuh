@@ -185,6 +185,7 @@ struct DevWorld {
     // narrowphase scratch
     void *epa_items;
     void *epa_scratch;     // one EPA polytope per EPA thread
+    int epa_threads;       // threads (and scratch slices) of the EPA kernel
     // persistent contact cache (double buffered by parity)
     unsigned long long *cache_keys[2];
     CacheRecord *cache_recs[2];
@@ -304,7 +305,7 @@ void upload_settings(const DevSettings &s, double spec64, cudaStream_t st);
 void launch_cache_begin(DevWorld &w, cudaStream_t s);
 size_t epa_scratch_bytes();
 size_t epa_item_bytes();
-constexpr int EPA_THREADS = 1024;
+constexpr int EPA_MAX_THREADS = NUM_SMS * 4 * 64;  // one EPA polytope per resident EPA thread
 
 // scan / sort utilities (cc_scan.cu)
 void exclusive_scan_int(const int *in, int *out, int n, int *total, int *tmp, cudaStream_t s);

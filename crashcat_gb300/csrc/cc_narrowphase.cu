@@ -1325,7 +1325,7 @@ size_t epa_item_bytes() { return sizeof(EpaItem); }
 void launch_narrowphase(DevWorld &w, float, cudaStream_t s) {
     EpaItem *items = (EpaItem *)w.epa_items;
     k_narrowphase<<<NUM_SMS * 8, 128, 0, s>>>(w, items);
-    k_epa<<<EPA_THREADS / 64, 64, 0, s>>>(w, items, (EpaScratch *)w.epa_scratch);
+    k_epa<<<w.epa_threads / 64, 64, 0, s>>>(w, items, (EpaScratch *)w.epa_scratch);
 }
 
 }  // namespace cc

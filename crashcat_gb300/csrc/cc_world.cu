@@ -32,6 +32,8 @@ struct cc_world {
     float *d_state_rows = nullptr;  // 16 floats per body staging for get/set state
     float *h_pinned_rows = nullptr;
     DevCounters *h_ctr = nullptr;   // pinned mirror of the device counters
+    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;  // bracket each cc_world_step call
+    float last_call_ms = 0.f;
 };
 
 static int cuda_ok(cudaError_t e) {
@@ -250,8 +252,12 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
             return r;
         }
         w.epa_items = p;
+        // EPA threads scale with the world: about one per 8 bodies, 1,024 to EPA_MAX_THREADS
+        int et = cap / 8;
+        et = et < 1024 ? 1024 : (et > EPA_MAX_THREADS ? EPA_MAX_THREADS : et);
+        w.epa_threads = (et + 63) / 64 * 64;
         char *q = nullptr;
-        if ((r = dalloc(&q, epa_scratch_bytes() * (size_t)EPA_THREADS)) != CC_OK) {
+        if ((r = dalloc(&q, epa_scratch_bytes() * (size_t)w.epa_threads)) != CC_OK) {
             cc_world_destroy(W);
             return r;
         }
@@ -306,6 +312,8 @@ int cc_world_destroy(cc_world *W) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (W->h_ctr) cudaFreeHost(W->h_ctr);
+    if (W->ev_begin) cudaEventDestroy(W->ev_begin);
+    if (W->ev_end) cudaEventDestroy(W->ev_end);
     if (W->stream) cudaStreamDestroy(W->stream);
     delete W;
     return CC_OK;
@@ -446,17 +454,27 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
 
 }  // extern "C"
 
-// one step's launch sequence (update.ts:45-239)
-static void enqueue_step(cc_world *W, float dt, float ratio) {
+// one step's launch sequence (update.ts:45-239); `ev` (optional, CC_NUM_STAGES + 1
+// events) brackets the stages for the stage profiler
+static void enqueue_step(cc_world *W, float dt, float ratio, cudaEvent_t *ev = nullptr) {
     DevWorld &w = W->w;
     cudaStream_t s = W->stream;
+    auto mark = [&](int k) {
+        if (ev) cudaEventRecord(ev[k], s);
+    };
+    mark(0);
     cudaMemsetAsync(w.ctr, 0, sizeof(DevCounters), s);
     launch_cache_begin(w, s);
     launch_integrate_forces(w, dt, s);
+    mark(1);
     launch_broadphase(w, s);
+    mark(2);
     launch_narrowphase(w, dt, s);
+    mark(3);
     launch_contacts_and_islands(w, dt, ratio, s);
+    mark(4);
     if (dt > 0.f) launch_solver(w, dt, ratio, s);
+    mark(5);
     cudaMemcpyAsync(W->h_ctr, w.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s);
 }
 
@@ -464,6 +482,11 @@ static int run_steps(cc_world *W, float dt, int n_steps) {
     if (W->w.n == 0) return CC_OK;
     upload_settings(W->dev_settings, W->settings.speculative_contact_distance, W->stream);
     int status = CC_OK;
+    if (!W->ev_begin) {
+        CC_TRY(cudaEventCreate(&W->ev_begin));
+        CC_TRY(cudaEventCreate(&W->ev_end));
+    }
+    CC_TRY(cudaEventRecord(W->ev_begin, W->stream));
     for (int i = 0; i < n_steps; i++) {
         // warm start ratio dt / previous dt, 0 on the first step (update.ts:118-124)
         float ratio = (W->settings.warm_starting && W->prev_dt > 0) ? (float)(dt / W->prev_dt) : 0.f;
@@ -489,8 +512,10 @@ static int run_steps(cc_world *W, float dt, int n_steps) {
         if (dt > 0.f) W->prev_dt = dt;
         W->steps_done++;
     }
+    CC_TRY(cudaEventRecord(W->ev_end, W->stream));
     CC_TRY(cudaStreamSynchronize(W->stream));
     CC_TRY(cudaGetLastError());
+    cudaEventElapsedTime(&W->last_call_ms, W->ev_begin, W->ev_end);
     W->last_ctr = *W->h_ctr;
     if (W->last_ctr.overflow) status = CC_ERR_CAPACITY;
     W->last_status = status;
@@ -679,11 +704,44 @@ int cc_world_debug_islands(cc_world *W, int32_t *island_of_body, int32_t *cons_r
     return CC_OK;
 }
 
+// Stage profiler: runs n_steps with CUDA events between the stages and returns the
+// mean milliseconds of each stage: integrate forces, broadphase, narrowphase,
+// contacts + islands, solver (velocity + integration + position + sleep).
+int cc_world_profile_steps(cc_world *W, float dt, int32_t n_steps, float *stage_ms, int32_t n_stages) {
+    if (!W || !stage_ms || n_steps <= 0 || n_stages < 5) return CC_ERR_INVALID;
+    if (W->w.n == 0) return CC_OK;
+    upload_settings(W->dev_settings, W->settings.speculative_contact_distance, W->stream);
+    cudaEvent_t ev[6];
+    for (int k = 0; k < 6; k++) CC_TRY(cudaEventCreate(&ev[k]));
+    double acc[5] = {0, 0, 0, 0, 0};
+    int st = CC_OK;
+    for (int i = 0; i < n_steps; i++) {
+        float ratio = (W->settings.warm_starting && W->prev_dt > 0) ? (float)(dt / W->prev_dt) : 0.f;
+        enqueue_step(W, dt, ratio, ev);
+        if (dt > 0.f) W->prev_dt = dt;
+        W->steps_done++;
+        CC_TRY(cudaEventSynchronize(ev[5]));
+        for (int k = 0; k < 5; k++) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+            acc[k] += ms;
+        }
+    }
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    W->last_ctr = *W->h_ctr;
+    if (W->last_ctr.overflow) st = CC_ERR_CAPACITY;
+    for (int k = 0; k < 6; k++) cudaEventDestroy(ev[k]);
+    for (int k = 0; k < 5; k++) stage_ms[k] = (float)(acc[k] / n_steps);
+    for (int k = 5; k < n_stages; k++) stage_ms[k] = 0.f;
+    return st;
+}
+
 int cc_world_get_stats(cc_world *W, cc_stats *o) {
     if (!W || !o) return CC_ERR_INVALID;
     memset(o, 0, sizeof(*o));
     const DevCounters &c = W->last_ctr;
     o->num_bodies = W->w.n;
+    o->num_awake = c.num_awake;
     o->num_pairs = c.num_pairs;
     o->num_manifolds = c.num_manifolds;
     o->num_contact_points = c.num_points;
@@ -692,11 +750,19 @@ int cc_world_get_stats(cc_world *W, cc_stats *o) {
     o->max_island_constraints = c.max_island_constraints;
     o->overflow_flags = c.overflow;
     o->gpu_launches_per_step = 0;
-    if (W->graph) {
+    if (W->graph) {  // kernel nodes of the captured step
         size_t nn = 0;
         cudaGraphGetNodes(W->graph, nullptr, &nn);
-        o->gpu_launches_per_step = (int)nn;
+        std::vector<cudaGraphNode_t> nodes(nn);
+        cudaGraphGetNodes(W->graph, nodes.data(), &nn);
+        int k = 0;
+        for (size_t i = 0; i < nn; i++) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) k++;
+        }
+        o->gpu_launches_per_step = k;
     }
+    o->last_call_ms = W->last_call_ms;
     return CC_OK;
 }
 

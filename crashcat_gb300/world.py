@@ -303,6 +303,16 @@ class GpuWorld:
               "cc_world_debug_islands")
         return iob[: self.n], rows[: cnt.value]
 
+    STAGES = ("integrate_forces", "broadphase", "narrowphase", "contacts_islands", "solver")
+
+    def profile_steps(self, dt: float, n_steps: int) -> dict:
+        """Mean milliseconds per stage over n_steps eager steps bracketed by CUDA events."""
+        out = np.zeros(8, dtype=np.float32)
+        st = self._lib.cc_world_profile_steps(self.handle, C.c_float(dt), n_steps, ptr(out), 8)
+        if st not in (_lib.CC_OK, _lib.CC_ERR_CAPACITY):
+            check(st, "cc_world_profile_steps")
+        return {k: float(out[i]) for i, k in enumerate(self.STAGES)}
+
     def stats(self) -> dict:
         s = _lib.Stats()
         check(self._lib.cc_world_get_stats(self.handle, C.byref(s)), "cc_world_get_stats")

@@ -132,6 +132,7 @@ typedef struct cc_stats {
     int32_t max_island_constraints;
     int32_t overflow_flags;
     int32_t gpu_launches_per_step;
+    float last_call_ms; /* device time of the last cc_world_step call (CUDA events on the world's stream) */
 } cc_stats;
 
 typedef struct cc_world cc_world;
@@ -167,6 +168,12 @@ int cc_world_get_pairs(cc_world *world, int32_t *out, int32_t capacity, int32_t 
 int cc_world_get_manifolds(cc_world *world, float *out, int32_t capacity, int32_t *count);
 
 int cc_world_get_stats(cc_world *world, cc_stats *out);
+
+/* Stage profiler with no reference counterpart: runs n_steps steps (eager
+ * launches) with CUDA events between the stages and writes the mean
+ * milliseconds of [integrate forces, broadphase, narrowphase, contacts and
+ * islands, solver] into stage_ms (n_stages >= 5). */
+int cc_world_profile_steps(cc_world *world, float dt, int32_t n_steps, float *stage_ms, int32_t n_stages);
 
 /* Diagnostic readout with no reference counterpart: island index per body of
  * the last step (-1 for static or sleeping bodies) and, per contact

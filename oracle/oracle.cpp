@@ -1255,7 +1255,9 @@ enum {
     F_ANG_DAMP = 25,
     F_ALLOW_SLEEP = 26,
     F_WORLD = 27,
-    F_COUNT = 28
+    F_GROUPS = 28,
+    F_MASK = 29,
+    F_COUNT = 30
 };
 
 void *orc_world_create(const double *settings, int n_obj, const int *obj_to_bp, int n_bp, const uint8_t *obj_pairs,
@@ -1327,6 +1329,8 @@ int orc_add_bodies(void *wp, const double *rows, int n) {
         b.linDamp = r[F_LIN_DAMP];
         b.angDamp = r[F_ANG_DAMP];
         b.allowSleeping = r[F_ALLOW_SLEEP] != 0;
+        b.groups = (uint32_t)r[F_GROUPS];
+        b.mask = (uint32_t)r[F_MASK];
         double mass;
         V3 idiag;
         shape_mass(s, mass, idiag);
@@ -1527,12 +1531,12 @@ int orc_prune_contact_points(double *ptsA, double *ptsB, int n, const double *ax
     return m.n;
 }
 // Barycentric coordinates (u, v, w, valid) of the closest point to the origin.
-void orc_barycentric(const double *a, const double *b, const double *c, int n, double *out) {
+void orc_barycentric(const double *a, const double *b, const double *c, int n, double sqtol, double *out) {
     Bary r;
     if (n == 2)
-        r = bary2({a[0], a[1], a[2]}, {b[0], b[1], b[2]}, 1e-10);
+        r = bary2({a[0], a[1], a[2]}, {b[0], b[1], b[2]}, sqtol);
     else
-        r = bary3({a[0], a[1], a[2]}, {b[0], b[1], b[2]}, {c[0], c[1], c[2]}, 1e-10);
+        r = bary3({a[0], a[1], a[2]}, {b[0], b[1], b[2]}, {c[0], c[1], c[2]}, sqtol);
     out[0] = r.u;
     out[1] = r.v;
     out[2] = r.w;

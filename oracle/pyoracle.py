@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 
-F_COUNT = 28  # doubles per body row, see oracle.cpp (enum F_*)
+F_COUNT = 30  # doubles per body row, see oracle.cpp (enum F_*)
 STATE = 17    # pos3 quat4 linvel3 angvel3 com3 sleeping
 
 _lib = None
@@ -51,7 +51,7 @@ def load():
         "orc_clip_poly_vs_poly": ([dp, i32, dp, i32, dp, dp], i32),
         "orc_manifold_between_faces": ([dp, dp, dp, C.c_double, dp, i32, dp, i32, dp, dp], i32),
         "orc_prune_contact_points": ([dp, dp, i32, dp], i32),
-        "orc_barycentric": ([dp, dp, dp, i32, dp], None),
+        "orc_barycentric": ([dp, dp, dp, i32, C.c_double, dp], None),
         "orc_collide_pair": ([dp, dp, C.c_double, dp], i32),
         "orc_inverse_inertia": ([dp, dp], None),
     }
@@ -93,6 +93,8 @@ def rows_from_bodies(b: np.ndarray) -> np.ndarray:
     r[:, 25] = b["angular_damping"]
     r[:, 26] = b["allow_sleeping"]
     r[:, 27] = b["world"]
+    r[:, 28] = b["collision_groups"]
+    r[:, 29] = b["collision_mask"]
     return np.ascontiguousarray(r)
 
 

@@ -1,0 +1,79 @@
+"""The C-ABI library builds, loads without a GPU, and exports every entry point
+declared in include/crashcat_gpu.h; the host-side mirror validates its input."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from crashcat_gb300 import _lib, build, scenes, world
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    hdr = open(os.path.join(ROOT, "include", "crashcat_gpu.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    return sorted(set(re.findall(r"\b(cc_[a-z_0-9]+)\s*\(", hdr)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _lib.load()
+
+
+def test_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) >= 12
+    for n in names:
+        assert hasattr(lib, n), n
+        assert n in _lib.EXPORTS, n
+
+
+def test_status_strings(lib):
+    for s in range(7):
+        assert lib.cc_status_string(s)
+    assert b"overflowed" in lib.cc_status_string(_lib.CC_ERR_CAPACITY)
+
+
+def test_default_settings_match_reference(lib):
+    s = _lib.Settings()
+    assert lib.cc_world_settings_default(C.byref(s)) == 0
+    ws = world.create_world_settings()
+    assert s.speculative_contact_distance == ws.speculative_contact_distance == 0.02
+    assert s.velocity_iterations == 10 and s.position_iterations == 2
+    assert s.gravity[1] == -9.81 and s.penetration_slop == 0.02 and s.baumgarte_factor == 0.2
+
+
+def test_invalid_arguments_are_rejected(lib):
+    assert lib.cc_world_create(None, None) == _lib.CC_ERR_INVALID
+    s = _lib.Settings()
+    lib.cc_world_settings_default(C.byref(s))
+    s.num_object_layers = 0
+    h = C.c_void_p()
+    assert lib.cc_world_create(C.byref(s), C.byref(h)) == _lib.CC_ERR_INVALID
+    assert lib.cc_world_step(None, C.c_float(0.01), 1) == _lib.CC_ERR_INVALID
+
+
+def test_body_desc_layout_matches_c():
+    # 23 fields of 4 bytes each (shape_params 4, vec3/quat inline)
+    assert _lib.BODY_DTYPE.itemsize == 4 * (1 + 4 + 1 + 4 + 3 + 4 + 3 + 3 + 7 + 2 + 2 + 1)
+
+
+def test_layer_tables_follow_reference():
+    s = world.standard_settings()
+    L = s.layers
+    # MOVING collides with MOVING and NOT_MOVING; NOT_MOVING only with MOVING (tst/helpers.ts)
+    assert L.object_pairs == [0b11, 0b01]
+    assert L.broadphase_pairs == [0b11, 0b01]
+    assert L.object_vs_broadphase == [0b11, 0b01 | 0b10]
+
+
+def test_scene_generators_are_seeded():
+    a = scenes.cube_heap(seed=1).bodies
+    b = scenes.cube_heap(seed=1).bodies
+    assert a.tobytes() == b.tobytes()
+    c = scenes.batched_worlds(num_worlds=8, seed=4)
+    assert c.num_worlds == 8 and (np.diff(c.bodies["world"]) >= 0).all()

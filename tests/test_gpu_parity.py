@@ -1,11 +1,19 @@
 """GPU parity against the FP64 oracle, through the C ABI.
 
-Tolerances (FP32 device state against an FP64 restatement):
-  * broadphase pair sets: bit-exact (exact FP64 re-test on the device);
-  * contact normals, points and depths: 1e-4 relative (normals: 1e-4 absolute,
-    points and depths: 1e-4 m + 1e-4 relative);
-  * free-fall integration over 30 steps: 1e-4 relative on positions and velocities;
-  * one step of isolated resting contacts: velocities within 2e-3 m/s.
+Tolerances (FP32 device state against an FP64 restatement of the reference):
+  * broadphase pair sets: bit-exact (the device re-tests candidates in FP64);
+  * contacts whose shrunk shapes do not overlap (GJK path): normal within 1e-4,
+    depth and points within 1e-4 m + 1e-4 relative;
+  * deep contacts (EPA path, depth > 0.05 m): normal within 1e-3, depth within
+    1e-3 relative, points within 2e-3 m + 1e-2 x depth (EPA starts from the
+    FP32 GJK simplex and stops at the reference's 1e-4 relative tolerance);
+  * at most 2 % of contacts may flip a discrete choice (clip plane side,
+    prune choice) between FP32 and FP64;
+  * free-fall integration over 30 steps: 1e-4 relative;
+  * one step of isolated resting contacts and the first 12 steps of a box
+    stack: velocities within 1e-4 m/s;
+  * 180 steps of the 1,000-box heap: lowest body height within 2 mm, mean
+    height within 1 cm of the oracle.
 """
 import numpy as np
 import pytest
@@ -37,7 +45,6 @@ def test_free_fall_integration(gpu_lib, oracle_lib):
     assert len(g.get_pairs()) == 0 and len(o.pairs()) == 0
     np.testing.assert_allclose(rows[:, 0:3], st[:, 0:3], rtol=1e-4, atol=1e-4)
     np.testing.assert_allclose(rows[:, 7:13], st[:, 7:13], rtol=1e-4, atol=1e-4)
-    # quaternions up to sign
     dq = np.minimum(np.abs(rows[:, 3:7] - st[:, 3:7]).max(1), np.abs(rows[:, 3:7] + st[:, 3:7]).max(1))
     assert dq.max() < 1e-4
 
@@ -62,10 +69,33 @@ def test_broadphase_pairs_bit_exact(gpu_lib, oracle_lib, seed):
     assert canonical_pairs(gp) == canonical_pairs(op)
 
 
-def match_manifolds(gm, om):
-    gk = {(int(r[0]), int(r[1])): r for r in gm}
-    ok = {(int(r[0]), int(r[1])): r for r in om}
-    return gk, ok
+def test_broadphase_pairs_cube_heap_state(gpu_lib, oracle_lib):
+    """Pairs of the settled heap (stacked boxes touching within the margin) are bit-exact."""
+    sc = scenes.cube_heap()
+    o = pyoracle.OracleWorld(world.standard_settings(), sc.bodies)
+    o.step(sc.dt, 60)
+    st = o.state()
+    b = sc.bodies.copy()
+    b["position"] = st[:, 0:3].astype(np.float32)
+    b["quaternion"] = st[:, 3:7].astype(np.float32)
+    g = world.GpuWorld(world.standard_settings(), sc.n + 16)
+    g.add_bodies(b)
+    o2 = pyoracle.OracleWorld(world.standard_settings(), b)
+    g.step(0.0, 1)
+    o2.step(0.0, 1)
+    assert set(map(tuple, g.get_pairs().tolist())) == set(map(tuple, o2.pairs().tolist()))
+
+
+def contact_errors(a, b):
+    deep = b[6] > 0.05
+    n_tol, d_rel = (1e-3, 1e-3) if deep else (1e-4, 1e-4)
+    n_ok = np.abs(a[3:6] - b[3:6]).max() < n_tol
+    d_ok = abs(a[6] - b[6]) < 1e-4 + d_rel * abs(b[6])
+    pg = a[8:8 + 6 * int(a[2])].reshape(-1, 6)
+    po = b[8:8 + 6 * int(b[2])].reshape(-1, 6)
+    p_tol = (2e-3 + 1e-2 * abs(b[6])) if deep else 1e-4
+    p_ok = int(a[2]) == int(b[2]) and all(np.min(np.abs(pg - q).max(1)) < p_tol + 1e-4 * np.abs(q).max() for q in po)
+    return n_ok and d_ok and p_ok
 
 
 @pytest.mark.parametrize("seed", [7, 8])
@@ -74,22 +104,126 @@ def test_contact_manifolds(gpu_lib, oracle_lib, seed):
     g, o = make_pair(sc)
     g.step(0.0, 1)
     o.step(0.0, 1)
-    gk, ok = match_manifolds(g.get_manifolds(), o.manifolds())
+    gk = {(int(r[0]), int(r[1])): r for r in g.get_manifolds()}
+    ok = {(int(r[0]), int(r[1])): r for r in o.manifolds()}
     assert len(ok) > 20
-    # the same body pairs produce contacts, except for pairs within float rounding of the
-    # speculative distance; require near-complete agreement
     common = set(gk) & set(ok)
     assert len(common) >= 0.98 * max(len(gk), len(ok))
-    bad = []
-    for k in common:
-        a, b = gk[k], ok[k]
-        n_ok = np.abs(a[3:6] - b[3:6]).max() < 1e-4
-        d_ok = abs(a[6] - b[6]) < 1e-4 + 1e-4 * abs(b[6])
-        # point sets: each oracle point has a GPU point within tolerance
-        pg = a[8:8 + 6 * int(a[2])].reshape(-1, 6)
-        po = b[8:8 + 6 * int(b[2])].reshape(-1, 6)
-        p_ok = int(a[2]) == int(b[2]) and all(
-            np.min(np.abs(pg - q).max(1)) < 1e-4 + 1e-4 * np.abs(q).max() for q in po)
-        if not (n_ok and d_ok and p_ok):
-            bad.append((k, a[2], b[2], a[3:7], b[3:7]))
-    assert len(bad) <= 0.01 * len(common), bad[:5]
+    bad = [k for k in common if not contact_errors(gk[k], ok[k])]
+    assert len(bad) <= 0.02 * len(common), bad[:5]
+
+
+def test_contacts_cube_heap_state(gpu_lib, oracle_lib):
+    """Resting and stacked box contacts (GJK and box-floor EPA) of the heap after 1 s."""
+    sc = scenes.cube_heap()
+    o = pyoracle.OracleWorld(world.standard_settings(), sc.bodies)
+    o.step(sc.dt, 60)
+    st = o.state()
+    b = sc.bodies.copy()
+    b["position"] = st[:, 0:3].astype(np.float32)
+    b["quaternion"] = st[:, 3:7].astype(np.float32)
+    g = world.GpuWorld(world.standard_settings(), sc.n + 16)
+    g.add_bodies(b)
+    o2 = pyoracle.OracleWorld(world.standard_settings(), b)
+    g.step(0.0, 1)
+    o2.step(0.0, 1)
+    gk = {(int(r[0]), int(r[1])): r for r in g.get_manifolds()}
+    ok = {(int(r[0]), int(r[1])): r for r in o2.manifolds()}
+    assert set(gk) == set(ok)
+    bad = [k for k in ok if not contact_errors(gk[k], ok[k])]
+    assert len(bad) <= 0.02 * len(ok), bad[:5]
+
+
+def test_resting_contacts_one_step(gpu_lib, oracle_lib):
+    """Isolated boxes on the floor: one contact per island, so the solve order is the
+    reference's; post-solve velocities agree within 1e-4 m/s."""
+    sc = scenes.resting_boxes(n=64)
+    g, o = make_pair(sc)
+    for _ in range(5):
+        g.step(sc.dt, 1)
+        o.step(sc.dt, 1)
+        rows, _ = g.get_state()
+        st = o.state()
+        np.testing.assert_allclose(rows[:, 7:13], st[:, 7:13], atol=1e-4)
+        np.testing.assert_allclose(rows[:, 0:3], st[:, 0:3], atol=1e-4)
+
+
+def test_stack_steps_track_oracle(gpu_lib, oracle_lib):
+    """A 10-box column (a chain island: the greedy colouring is fully sequential) tracks
+    the oracle step by step, including warm starting from the contact cache."""
+    sc = scenes.box_stack(height=10)
+    g, o = make_pair(sc)
+    for _ in range(12):
+        g.step(sc.dt, 1)
+        o.step(sc.dt, 1)
+        rows, _ = g.get_state()
+        st = o.state()
+        assert np.abs(rows[:, 7:13] - st[:, 7:13]).max() < 1e-4
+        assert np.abs(rows[:, 0:3] - st[:, 0:3]).max() < 1e-5
+
+
+def test_row_island_colour_parallel(gpu_lib, oracle_lib):
+    """A row of touching boxes: colours hold several contacts solved in parallel by one CTA;
+    the colouring preserves the reference's order so the result matches."""
+    for count in (6, 12):
+        sc = scenes.box_row(count)
+        g, o = make_pair(sc)
+        g.step(sc.dt, 1)
+        o.step(sc.dt, 1)
+        rows, _ = g.get_state()
+        assert np.abs(rows[:, 7:13] - o.state()[:, 7:13]).max() < 1e-4
+
+
+def test_islands_consistent(gpu_lib):
+    """Every contact between two active bodies lies in one island holding both bodies."""
+    sc = scenes.cube_heap()
+    g = world.GpuWorld(world.standard_settings(), sc.n + 16)
+    g.add_bodies(sc.bodies)
+    g.step(sc.dt, 40)
+    iob, rows = g.debug_islands()
+    assert len(rows) > 100
+    for a, c, isl in rows:
+        ia, ic = iob[a], iob[c]
+        if ia >= 0 and ic >= 0:
+            assert ia == ic == isl
+        else:
+            assert isl == max(ia, ic)
+
+
+def test_cube_heap_drift(gpu_lib, oracle_lib):
+    """180 steps of the 1,000-box heap: penetration and heights stay with the oracle's."""
+    sc = scenes.cube_heap()
+    g, o = make_pair(sc)
+    for _ in range(3):
+        g.step(sc.dt, 60)
+        o.step(sc.dt, 60)
+        rows, sl = g.get_state()
+        st = o.state()
+        assert abs(rows[1:, 1].min() - st[1:, 1].min()) < 2e-3
+        assert abs(rows[1:, 1].mean() - st[1:, 1].mean()) < 1e-2
+        assert np.isfinite(rows).all()
+    assert g.stats()["overflow_flags"] == 0
+
+
+def test_batched_worlds_are_independent(gpu_lib):
+    """Two copies of one world inside one batched handle evolve exactly like the single world."""
+    sc = scenes.cube_heap(n_side=4, seed=5)
+    b2 = np.concatenate([sc.bodies, sc.bodies])
+    b2["world"][sc.n:] = 1
+    ws1 = world.standard_settings()
+    ws2 = world.standard_settings()
+    ws2.num_worlds = 2
+    g1 = world.GpuWorld(ws1, sc.n + 8)
+    g1.add_bodies(sc.bodies)
+    g2 = world.GpuWorld(ws2, 2 * sc.n + 8)
+    g2.add_bodies(b2)
+    g1.step(sc.dt, 60)
+    g2.step(sc.dt, 60)
+    r1, _ = g1.get_state()
+    r2, _ = g2.get_state()
+    # same bodies in the same order: each copy matches the single world (FP32, same order)
+    np.testing.assert_allclose(r2[: sc.n], r1, atol=2e-4)
+    np.testing.assert_allclose(r2[sc.n:], r1, atol=2e-4)
+    # no pair ever crosses worlds
+    p = g2.get_pairs()
+    assert ((p[:, 0] < sc.n) == (p[:, 1] < sc.n)).all()
