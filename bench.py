@@ -39,7 +39,8 @@ import numpy as np  # noqa: E402
 
 WORKLOAD = "batched_uneven_worlds"
 METRIC = "body-steps/s"
-STAGES = ("integrate_forces", "broadphase", "narrowphase", "contacts_islands", "solver")
+STAGES = ("integrate_forces", "broadphase", "narrowphase", "epa", "contacts_islands", "solve_small_islands",
+          "solve_large_islands")
 
 
 def parse():
@@ -146,9 +147,13 @@ def algorithmic_bytes(stage: str, st: dict, n_bodies: int) -> float:
         return 104.0 * n_bodies + 16.0 * npairs
     if stage == "narrowphase":
         return 72.0 * npairs + (20 + 24 * P) * nm
+    if stage == "epa":
+        ne = st["num_epa"]
+        return (72.0 + 20 + 24 * P) * ne
     if stage == "contacts_islands":
         return (20 + 24 * P) * nm + (48 + 180 * P) * nm + 24 * P * nm
-    if stage == "solver":
+    if stage in ("solver", "solve_small_islands", "solve_large_islands"):
+        # both solver kernels together move these bytes; each is charged its share of them
         return 216.0 * na + (48 + 180 * P) * nm + 24 * P * nm
     raise ValueError(stage)
 

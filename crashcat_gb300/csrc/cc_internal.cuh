@@ -297,9 +297,9 @@ inline int grid_for(int n, int block, int max_blocks_per_sm = 8) {
 // host launchers implemented in the .cu files
 void launch_integrate_forces(DevWorld &w, float dt, cudaStream_t s);
 void launch_broadphase(DevWorld &w, cudaStream_t s);
-void launch_narrowphase(DevWorld &w, float dt, cudaStream_t s);
+void launch_narrowphase(DevWorld &w, float dt, cudaStream_t s, cudaEvent_t mid = nullptr);
 void launch_contacts_and_islands(DevWorld &w, float dt, float warm_ratio, cudaStream_t s);
-void launch_solver(DevWorld &w, float dt, float warm_ratio, cudaStream_t s);
+void launch_solver(DevWorld &w, float dt, float warm_ratio, cudaStream_t s, cudaEvent_t mid = nullptr);
 void launch_update_bounds(DevWorld &w, cudaStream_t s);
 void upload_settings(const DevSettings &s, double spec64, cudaStream_t st);
 void launch_cache_begin(DevWorld &w, cudaStream_t s);

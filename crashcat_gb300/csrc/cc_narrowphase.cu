@@ -1322,9 +1322,10 @@ __global__ void __launch_bounds__(64) k_epa(DevWorld w, const EpaItem *items, Ep
 
 size_t epa_item_bytes() { return sizeof(EpaItem); }
 
-void launch_narrowphase(DevWorld &w, float, cudaStream_t s) {
+void launch_narrowphase(DevWorld &w, float, cudaStream_t s, cudaEvent_t mid) {
     EpaItem *items = (EpaItem *)w.epa_items;
     k_narrowphase<<<NUM_SMS * 8, 128, 0, s>>>(w, items);
+    if (mid) cudaEventRecord(mid, s);
     k_epa<<<w.epa_threads / 64, 64, 0, s>>>(w, items, (EpaScratch *)w.epa_scratch);
 }
 

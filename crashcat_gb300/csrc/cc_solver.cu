@@ -1019,9 +1019,10 @@ void launch_contacts_and_islands(DevWorld &w, float dt, float, cudaStream_t s) {
     k_island_classify<<<grid_for(w.n, 256), 256, 0, s>>>(w, w.small_list, w.large_list);
 }
 
-void launch_solver(DevWorld &w, float dt, float ratio, cudaStream_t s) {
+void launch_solver(DevWorld &w, float dt, float ratio, cudaStream_t s, cudaEvent_t mid) {
     CacheTables ct = tables_of(w);
     k_solve_small<<<grid_for(w.n, 128, 16), 128, 0, s>>>(w, ct, w.small_list, dt, ratio);
+    if (mid) cudaEventRecord(mid, s);
     k_solve_large<<<NUM_SMS * 2, LARGE_BLOCK, 0, s>>>(w, ct, w.large_list, w.scratch_order, w.scratch_colour,
                                                       w.scratch_claim, dt, ratio);
 }

@@ -454,8 +454,9 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
 
 }  // extern "C"
 
-// one step's launch sequence (update.ts:45-239); `ev` (optional, CC_NUM_STAGES + 1
+// one step's launch sequence (update.ts:45-239); `ev` (optional, CC_PROFILE_STAGES + 1
 // events) brackets the stages for the stage profiler
+constexpr int CC_PROFILE_STAGES = 7;
 static void enqueue_step(cc_world *W, float dt, float ratio, cudaEvent_t *ev = nullptr) {
     DevWorld &w = W->w;
     cudaStream_t s = W->stream;
@@ -469,12 +470,13 @@ static void enqueue_step(cc_world *W, float dt, float ratio, cudaEvent_t *ev = n
     mark(1);
     launch_broadphase(w, s);
     mark(2);
-    launch_narrowphase(w, dt, s);
-    mark(3);
-    launch_contacts_and_islands(w, dt, ratio, s);
+    launch_narrowphase(w, dt, s, ev ? ev[3] : nullptr);
     mark(4);
-    if (dt > 0.f) launch_solver(w, dt, ratio, s);
+    launch_contacts_and_islands(w, dt, ratio, s);
     mark(5);
+    if (dt > 0.f) launch_solver(w, dt, ratio, s, ev ? ev[6] : nullptr);
+    if (ev && !(dt > 0.f)) mark(6);
+    mark(7);
     cudaMemcpyAsync(W->h_ctr, w.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s);
 }
 
@@ -705,23 +707,24 @@ int cc_world_debug_islands(cc_world *W, int32_t *island_of_body, int32_t *cons_r
 }
 
 // Stage profiler: runs n_steps with CUDA events between the stages and returns the
-// mean milliseconds of each stage: integrate forces, broadphase, narrowphase,
-// contacts + islands, solver (velocity + integration + position + sleep).
+// mean milliseconds of each stage: integrate forces, broadphase, narrowphase (GJK,
+// faces, clipping), EPA, contacts + islands, per-thread island solve, per-CTA island
+// solve.
 int cc_world_profile_steps(cc_world *W, float dt, int32_t n_steps, float *stage_ms, int32_t n_stages) {
-    if (!W || !stage_ms || n_steps <= 0 || n_stages < 5) return CC_ERR_INVALID;
+    if (!W || !stage_ms || n_steps <= 0 || n_stages < CC_PROFILE_STAGES) return CC_ERR_INVALID;
     if (W->w.n == 0) return CC_OK;
     upload_settings(W->dev_settings, W->settings.speculative_contact_distance, W->stream);
-    cudaEvent_t ev[6];
-    for (int k = 0; k < 6; k++) CC_TRY(cudaEventCreate(&ev[k]));
-    double acc[5] = {0, 0, 0, 0, 0};
+    cudaEvent_t ev[CC_PROFILE_STAGES + 1];
+    for (int k = 0; k <= CC_PROFILE_STAGES; k++) CC_TRY(cudaEventCreate(&ev[k]));
+    double acc[CC_PROFILE_STAGES] = {};
     int st = CC_OK;
     for (int i = 0; i < n_steps; i++) {
         float ratio = (W->settings.warm_starting && W->prev_dt > 0) ? (float)(dt / W->prev_dt) : 0.f;
         enqueue_step(W, dt, ratio, ev);
         if (dt > 0.f) W->prev_dt = dt;
         W->steps_done++;
-        CC_TRY(cudaEventSynchronize(ev[5]));
-        for (int k = 0; k < 5; k++) {
+        CC_TRY(cudaEventSynchronize(ev[CC_PROFILE_STAGES]));
+        for (int k = 0; k < CC_PROFILE_STAGES; k++) {
             float ms = 0.f;
             cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
             acc[k] += ms;
@@ -730,9 +733,9 @@ int cc_world_profile_steps(cc_world *W, float dt, int32_t n_steps, float *stage_
     CC_TRY(cudaStreamSynchronize(W->stream));
     W->last_ctr = *W->h_ctr;
     if (W->last_ctr.overflow) st = CC_ERR_CAPACITY;
-    for (int k = 0; k < 6; k++) cudaEventDestroy(ev[k]);
-    for (int k = 0; k < 5; k++) stage_ms[k] = (float)(acc[k] / n_steps);
-    for (int k = 5; k < n_stages; k++) stage_ms[k] = 0.f;
+    for (int k = 0; k <= CC_PROFILE_STAGES; k++) cudaEventDestroy(ev[k]);
+    for (int k = 0; k < CC_PROFILE_STAGES; k++) stage_ms[k] = (float)(acc[k] / n_steps);
+    for (int k = CC_PROFILE_STAGES; k < n_stages; k++) stage_ms[k] = 0.f;
     return st;
 }
 

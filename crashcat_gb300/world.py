@@ -303,7 +303,8 @@ class GpuWorld:
               "cc_world_debug_islands")
         return iob[: self.n], rows[: cnt.value]
 
-    STAGES = ("integrate_forces", "broadphase", "narrowphase", "contacts_islands", "solver")
+    STAGES = ("integrate_forces", "broadphase", "narrowphase", "epa", "contacts_islands", "solve_small_islands",
+              "solve_large_islands")
 
     def profile_steps(self, dt: float, n_steps: int) -> dict:
         """Mean milliseconds per stage over n_steps eager steps bracketed by CUDA events."""

@@ -171,8 +171,9 @@ int cc_world_get_stats(cc_world *world, cc_stats *out);
 
 /* Stage profiler with no reference counterpart: runs n_steps steps (eager
  * launches) with CUDA events between the stages and writes the mean
- * milliseconds of [integrate forces, broadphase, narrowphase, contacts and
- * islands, solver] into stage_ms (n_stages >= 5). */
+ * milliseconds of [integrate forces, broadphase, narrowphase (GJK, faces,
+ * clipping), EPA, contacts and islands, per-thread island solve, per-CTA
+ * island solve] into stage_ms (n_stages >= 7). */
 int cc_world_profile_steps(cc_world *world, float dt, int32_t n_steps, float *stage_ms, int32_t n_stages);
 
 /* Diagnostic readout with no reference counterpart: island index per body of
