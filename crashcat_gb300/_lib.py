@@ -96,8 +96,18 @@ EXPORTS = {
     "cc_world_get_stats": ([C.c_void_p, C.POINTER(Stats)], C.c_int),
     "cc_world_debug_islands": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
     "cc_world_profile_steps": ([C.c_void_p, C.c_float, C.c_int32, C.c_void_p, C.c_int32], C.c_int),
+    "cc_penetration_static": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_float, C.c_float, C.c_void_p], C.c_int),
     "cc_status_string": ([C.c_int], C.c_char_p),
 }
+
+# cc_penetration_static limits and record layouts (numpy mirrors of the C structs)
+STATIC_MAX_QUERIES = 32768
+STATIC_EPA_SLOTS = 304
+SHAPE_POSE_DTYPE = np.dtype([("shape_type", np.int32), ("shape_params", np.float32, 4),
+                             ("position", np.float32, 3), ("quaternion", np.float32, 4)])
+PEN_QUERY_DTYPE = np.dtype([("a", SHAPE_POSE_DTYPE), ("b", SHAPE_POSE_DTYPE), ("max_separation", np.float32)])
+PEN_RESULT_DTYPE = np.dtype([("hit", np.int32), ("normal", np.float32, 3), ("depth", np.float32),
+                             ("point_a", np.float32, 3), ("point_b", np.float32, 3), ("used_epa", np.int32)])
 
 _lib = None
 

@@ -14,6 +14,8 @@
 // body A's position.  Pairs whose shrunk shapes overlap (GJK INDETERMINATE) are
 // queued for a second kernel that runs EPA in FP64 with its polytope in a
 // per-thread slice of global scratch memory.
+#include <mutex>
+
 #include "cc_internal.cuh"
 
 namespace cc {
@@ -1329,4 +1331,221 @@ void launch_narrowphase(DevWorld &w, float, cudaStream_t s, cudaEvent_t mid) {
     k_epa<<<w.epa_threads / 64, 64, 0, s>>>(w, items, (EpaScratch *)w.epa_scratch);
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free penetration query (cc_penetration_static).  The same GJK and
+// EPA device code as the world's narrowphase, run on caller-owned device
+// buffers; the EPA polytopes and the queue of EPA items live in file-scope
+// device arrays, so the call allocates nothing.
+// ---------------------------------------------------------------------------
+struct StaticQueue {
+    int count;  // items queued by the GJK pass; cleared at the start of every call
+    int pad[63];
+};
+static __device__ __align__(256) EpaScratch g_static_slots[CC_STATIC_EPA_SLOTS];
+static __device__ __align__(256) EpaItem g_static_items[CC_STATIC_MAX_QUERIES];
+static __device__ __align__(256) StaticQueue g_static_queue;
+
+__device__ __forceinline__ void pose_of(const cc_shape_pose &s, float4 &pos, float4 &quat, float4 &prm) {
+    pos = make_float4(s.position[0], s.position[1], s.position[2], 0.f);
+    quat = make_float4(s.quaternion[0], s.quaternion[1], s.quaternion[2], s.quaternion[3]);
+    prm = make_float4(s.shape_params[0], s.shape_params[1], s.shape_params[2], s.shape_params[3]);
+}
+
+__device__ __forceinline__ void write_hit(cc_penetration_result &r, float3 posA, float3 pa, float3 pb, float3 axis,
+                                          float depth, int used_epa) {
+    float3 n = normalize3(axis);
+    r.hit = 1;
+    r.normal[0] = n.x;
+    r.normal[1] = n.y;
+    r.normal[2] = n.z;
+    r.depth = depth;
+    r.point_a[0] = posA.x + pa.x;
+    r.point_a[1] = posA.y + pa.y;
+    r.point_a[2] = posA.z + pa.z;
+    r.point_b[0] = posA.x + pb.x;
+    r.point_b[1] = posA.y + pb.y;
+    r.point_b[2] = posA.z + pb.z;
+    r.used_epa = used_epa;
+}
+
+// GJK pass, one query per thread: the dispatch and GJK step of k_narrowphase;
+// INDETERMINATE pairs are queued for the EPA pass.
+__global__ void __launch_bounds__(128) k_static_gjk(const cc_penetration_query *qs, int n, cc_penetration_result *res,
+                                                    EpaItem *items, StaticQueue *queue, float collision_tol) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const cc_penetration_query &qy = qs[i];
+    cc_penetration_result r;
+    r.hit = 0;
+    r.normal[0] = r.normal[1] = r.normal[2] = 0.f;
+    r.depth = 0.f;
+    r.point_a[0] = r.point_a[1] = r.point_a[2] = 0.f;
+    r.point_b[0] = r.point_b[1] = r.point_b[2] = 0.f;
+    r.used_epa = 0;
+    float4 pa4, pb4, qa, qb, sa, sb;
+    pose_of(qy.a, pa4, qa, sa);
+    pose_of(qy.b, pb4, qb, sb);
+    int sha = qy.a.shape_type, shb = qy.b.shape_type;
+    float maxSep = qy.max_separation;
+    if ((sha != SHAPE_SPHERE && sha != SHAPE_BOX) || (shb != SHAPE_SPHERE && shb != SHAPE_BOX)) {
+        res[i] = r;  // unknown shape type: reported as no hit
+        return;
+    }
+    if (sha == SHAPE_SPHERE && shb == SHAPE_SPHERE) {
+        float3 d = xyz(pb4) - xyz(pa4);
+        float dsq = lensq3(d);
+        float rs = sa.x + sb.x;
+        if (dsq < rs * rs) {
+            float dist = sqrtf(dsq);
+            float3 nn = dist > 0.f ? d * (1.f / dist) : f3(0.f, 1.f, 0.f);
+            write_hit(r, xyz(pa4), nn * sa.x, d - nn * sb.x, nn, rs - dist, 0);
+        }
+        res[i] = r;
+        return;
+    }
+    Q<float> qA{qa.x, qa.y, qa.z, qa.w}, qB{qb.x, qb.y, qb.z, qb.w};
+    Q<float> iA{-qa.x, -qa.y, -qa.z, qa.w};
+    Q<float> rel = qmulS(iA, qB);
+    V<float> ab{pb4.x - pa4.x, pb4.y - pa4.y, pb4.z - pa4.z};
+    V<float> posBInA = qrotS(iA, ab);
+    Sup<float> supA = make_sup<float>(sha, sa, true);
+    Sup<float> supB = make_sup<float>(shb, sb, true);
+    set_transform(supB, rel, posBInA);
+    V<float> axis = posBInA;
+    if (lsq(axis) <= 1e-12f) axis = {1.f, 0.f, 0.f};
+    float rA = supA.convex_radius + maxSep, rB = supB.convex_radius;
+    float cr = rA + rB;
+    Simplex<float> sx;
+    GjkOut<float> g = gjk(supA, supB, collision_tol, axis, cr * cr, sx);
+    if (g.sqdist > cr * cr) {
+        res[i] = r;
+        return;
+    }
+    if (!(g.sqdist > 0.f)) {
+        // every query fits the queue (count <= CC_STATIC_MAX_QUERIES is checked on the host)
+        int e = atomicAdd(&queue->count, 1);
+        EpaItem it;
+        it.a = i;
+        it.b = i;
+        it.size = sx.size;
+        it.pad = 0;
+        for (int k = 0; k < 4; k++) {
+            SP<float> s = sx.pts[k < sx.size ? k : 0];
+            it.y[k] = f3(s.y.x, s.y.y, s.y.z);
+            it.p[k] = f3(s.p.x, s.p.y, s.p.z);
+            it.q[k] = f3(s.q.x, s.q.y, s.q.z);
+        }
+        items[e] = it;
+        r.used_epa = 1;
+        res[i] = r;
+        return;
+    }
+    float vl = sqrtf(g.sqdist);
+    V<float> pa = g.pa + g.axis * (rA / vl);
+    V<float> pb = g.pb + g.axis * (-(rB / vl));
+    V<float> dd = pa - pb;
+    float penetration = sqrtf(lsq(dd)) - maxSep;
+    float al = sqrtf(lsq(g.axis));
+    if (al > 0.f) pa = pa + g.axis * (-(maxSep / al));
+    V<float> paw = qrotS(qA, pa), pbw = qrotS(qA, pb), axw = qrotS(qA, g.axis);
+    write_hit(r, xyz(pa4), f3(paw.x, paw.y, paw.z), f3(pbw.x, pbw.y, pbw.z), f3(axw.x, axw.y, axw.z), penetration,
+              0);
+    res[i] = r;
+}
+
+// EPA pass: CC_STATIC_EPA_SLOTS threads, each owning one static polytope,
+// stride over the queued items (the arithmetic of epa_pair).
+__global__ void __launch_bounds__(64) k_static_epa(const cc_penetration_query *qs, cc_penetration_result *res,
+                                                   const EpaItem *items, const StaticQueue *queue,
+                                                   EpaScratch *slots, float penetration_tol) {
+    int ne = queue->count;
+    int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= CC_STATIC_EPA_SLOTS) return;
+    EpaScratch *mine = slots + tid;
+    for (int j = tid; j < ne; j += CC_STATIC_EPA_SLOTS) {
+        const EpaItem &it = items[j];
+        const cc_penetration_query &qy = qs[it.a];
+        float4 pa4, pb4, qa, qb, sa, sb;
+        pose_of(qy.a, pa4, qa, sa);
+        pose_of(qy.b, pb4, qb, sb);
+        double maxSep = (double)qy.max_separation < 1.0 ? (double)qy.max_separation : 1.0;
+        Q<double> iA{-(double)qa.x, -(double)qa.y, -(double)qa.z, (double)qa.w};
+        Q<double> qB{qb.x, qb.y, qb.z, qb.w}, qA{qa.x, qa.y, qa.z, qa.w};
+        Q<double> rel = qmulS(iA, qB);
+        V<double> ab{(double)pb4.x - (double)pa4.x, (double)pb4.y - (double)pa4.y, (double)pb4.z - (double)pa4.z};
+        V<double> posBInA = qrotS(iA, ab);
+        Sup<double> A = make_sup<double>(qy.a.shape_type, sa, false);
+        Sup<double> B = make_sup<double>(qy.b.shape_type, sb, false);
+        A.add_r = maxSep;
+        set_transform(B, rel, posBInA);
+        EpaHull h;
+        h.s = mine;
+        h.npts = it.size;
+        for (int k = 0; k < it.size; k++) {
+            mine->Y[k] = {it.y[k].x, it.y[k].y, it.y[k].z};
+            mine->P[k] = {it.p[k].x, it.p[k].y, it.p[k].z};
+            mine->Qp[k] = {it.q[k].x, it.q[k].y, it.q[k].z};
+        }
+        V<double> axis, pa, pb;
+        if (!epa(h, A, B, (double)penetration_tol, axis, pa, pb)) continue;  // no contact (convex.ts:331)
+        V<double> dd = pa - pb;
+        double penetration = sqrt(lsq(dd)) - maxSep;
+        double al = sqrt(lsq(axis));
+        if (al > 0.0) pa = pa + axis * (-(maxSep / al));
+        V<double> paw = qrotS(qA, pa), pbw = qrotS(qA, pb), axw = qrotS(qA, axis);
+        cc_penetration_result r;
+        write_hit(r, xyz(pa4), f3((float)paw.x, (float)paw.y, (float)paw.z),
+                  f3((float)pbw.x, (float)pbw.y, (float)pbw.z), f3((float)axw.x, (float)axw.y, (float)axw.z),
+                  (float)penetration, 1);
+        res[it.a] = r;
+    }
+}
+
+// Addresses of the static arrays on one device, looked up once.
+struct StaticArrays {
+    EpaScratch *slots;
+    EpaItem *items;
+    StaticQueue *queue;
+};
+constexpr int STATIC_MAX_DEVICES = 64;
+static StaticArrays g_static_addr[STATIC_MAX_DEVICES];
+static bool g_static_ready[STATIC_MAX_DEVICES];
+static std::mutex g_static_mutex;
+
+static int static_arrays(StaticArrays &out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return CC_ERR_CUDA;
+    if (dev < 0 || dev >= STATIC_MAX_DEVICES) return CC_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    if (!g_static_ready[dev]) {
+        StaticArrays a;
+        if (cudaGetSymbolAddress((void **)&a.slots, g_static_slots) != cudaSuccess) return CC_ERR_CUDA;
+        if (cudaGetSymbolAddress((void **)&a.items, g_static_items) != cudaSuccess) return CC_ERR_CUDA;
+        if (cudaGetSymbolAddress((void **)&a.queue, g_static_queue) != cudaSuccess) return CC_ERR_CUDA;
+        g_static_addr[dev] = a;
+        g_static_ready[dev] = true;
+    }
+    out = g_static_addr[dev];
+    return CC_OK;
+}
+
 }  // namespace cc
+
+extern "C" int cc_penetration_static(const cc_penetration_query *queries, int32_t count,
+                                     cc_penetration_result *results, float collision_tolerance,
+                                     float penetration_tolerance, void *stream) {
+    using namespace cc;
+    if (count < 0 || (count > 0 && (queries == nullptr || results == nullptr))) return CC_ERR_INVALID;
+    if (!(collision_tolerance > 0.f) || !(penetration_tolerance > 0.f)) return CC_ERR_INVALID;
+    if (count > CC_STATIC_MAX_QUERIES) return CC_ERR_CAPACITY;
+    if (count == 0) return CC_OK;
+    StaticArrays a;
+    int r = static_arrays(a);
+    if (r != CC_OK) return r;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (cudaMemsetAsync(&a.queue->count, 0, sizeof(int), s) != cudaSuccess) return CC_ERR_CUDA;
+    k_static_gjk<<<(count + 127) / 128, 128, 0, s>>>(queries, count, results, a.items, a.queue, collision_tolerance);
+    k_static_epa<<<CC_STATIC_EPA_SLOTS / 64 + (CC_STATIC_EPA_SLOTS % 64 != 0), 64, 0, s>>>(
+        queries, results, a.items, a.queue, a.slots, penetration_tolerance);
+    return cudaGetLastError() == cudaSuccess ? CC_OK : CC_ERR_CUDA;
+}

@@ -182,6 +182,71 @@ int cc_world_profile_steps(cc_world *world, float dt, int32_t n_steps, float *st
 int cc_world_debug_islands(cc_world *world, int32_t *island_of_body, int32_t *cons_rows, int32_t capacity,
                            int32_t *count);
 
+/* ---------------------------------------------------------------------------
+ * Allocation-free penetration query.  No counterpart in the reference: it is
+ * the narrowphase of one convex pair (collideConvexVsConvex,
+ * src/shapes/convex.ts:257-346, with penetrationDepthStepGJK / EPA of
+ * src/collision/penetration.ts) offered as a batch query on caller-owned
+ * device buffers.
+ *
+ * Why it exists: a world handle reserves its EPA polytopes (about 47 KB per
+ * EPA thread) when it is created.  Some callers cannot allocate device memory
+ * at the point where they want to ask "how deep do these shape pairs overlap":
+ * a frame loop with a fixed device-memory budget, a host thread that must not
+ * stall the device (cudaMalloc and cudaFree synchronise it), or code that only
+ * owns buffers handed to it by another allocator.  This entry point runs on
+ * CC_STATIC_EPA_SLOTS polytopes and a queue of CC_STATIC_MAX_QUERIES items
+ * held in file-scope device arrays of the library (about 20 MB per device),
+ * and calls no cudaMalloc, cudaFree or other allocating routine.
+ *
+ * Use:
+ *   - queries and results are DEVICE pointers to count elements;
+ *     stream is a cudaStream_t (NULL = the legacy default stream).  The call
+ *     returns after queueing its kernels; results are valid once the stream
+ *     has been synchronised.
+ *   - the first call on each device looks up the address of the static
+ *     arrays with cudaGetSymbolAddress (with that device current); make that
+ *     first call before any stream capture begins.
+ *   - count > CC_STATIC_MAX_QUERIES returns CC_ERR_CAPACITY and queues
+ *     nothing; count < 0 or a NULL buffer returns CC_ERR_INVALID; count == 0
+ *     queues nothing and returns CC_OK.
+ *   - the EPA queue counter must start at zero: every call clears it on the
+ *     stream before its first kernel.
+ *   - the arrays are shared by every call on the device: two calls whose
+ *     kernels overlap on the GPU (different streams, or different host
+ *     threads) race on them.  Serialise calls on one stream.
+ *   - A and B are taken in the given order (the world orders a pair by motion
+ *     type and body id first, src/update.ts:74); max_separation is the
+ *     speculative contact distance of the world settings (0 for sensors).
+ * ------------------------------------------------------------------------- */
+#define CC_STATIC_MAX_QUERIES 32768
+#define CC_STATIC_EPA_SLOTS 304
+
+typedef struct cc_shape_pose {
+    int32_t shape_type;     /* cc_shape_type */
+    float shape_params[4];  /* as cc_body_desc.shape_params */
+    float position[3];
+    float quaternion[4];    /* x, y, z, w */
+} cc_shape_pose;
+
+typedef struct cc_penetration_query {
+    cc_shape_pose a;
+    cc_shape_pose b;
+    float max_separation;
+} cc_penetration_query;
+
+typedef struct cc_penetration_result {
+    int32_t hit;        /* 1: the shapes are closer than max_separation */
+    float normal[3];    /* unit contact normal, A to B, world space */
+    float depth;        /* penetration depth (negative: separation) */
+    float point_a[3];   /* deepest point on A, world space */
+    float point_b[3];   /* deepest point on B, world space */
+    int32_t used_epa;   /* 1 when the shrunk shapes overlapped and EPA ran */
+} cc_penetration_result;
+
+int cc_penetration_static(const cc_penetration_query *queries, int32_t count, cc_penetration_result *results,
+                          float collision_tolerance, float penetration_tolerance, void *stream);
+
 const char *cc_status_string(int status);
 
 #ifdef __cplusplus

@@ -77,3 +77,14 @@ def test_scene_generators_are_seeded():
     assert a.tobytes() == b.tobytes()
     c = scenes.batched_worlds(num_worlds=8, seed=4)
     assert c.num_worlds == 8 and (np.diff(c.bodies["world"]) >= 0).all()
+
+
+def test_static_query_checks_arguments_before_any_cuda_call(lib):
+    one = C.c_void_p(256)  # never dereferenced: every check below returns before a launch
+    tol = (C.c_float(1e-4), C.c_float(1e-4))
+    assert lib.cc_penetration_static(one, _lib.STATIC_MAX_QUERIES + 1, one, *tol, None) == _lib.CC_ERR_CAPACITY
+    assert lib.cc_penetration_static(one, -1, one, *tol, None) == _lib.CC_ERR_INVALID
+    assert lib.cc_penetration_static(None, 8, one, *tol, None) == _lib.CC_ERR_INVALID
+    assert lib.cc_penetration_static(one, 8, one, C.c_float(0.0), tol[1], None) == _lib.CC_ERR_INVALID
+    assert lib.cc_penetration_static(None, 0, None, *tol, None) == _lib.CC_OK
+    assert _lib.PEN_QUERY_DTYPE.itemsize == 100 and _lib.PEN_RESULT_DTYPE.itemsize == 48
