@@ -53,7 +53,9 @@ struct DevCounters {
     int max_island_constraints;
     int island_cursor;
     int large_cursor;
-    int pad[20];
+    int num_mid_islands;
+    int mid_cursor;
+    int pad[18];
 };
 
 // Settings copied into constant memory once per world.
@@ -186,6 +188,10 @@ struct DevWorld {
     void *epa_items;
     void *epa_scratch;     // one EPA polytope per EPA thread
     int epa_threads;       // threads (and scratch slices) of the EPA kernel
+    cudaStream_t aux_stream;  // second stream: the per-CTA island solve runs beside the per-warp one
+    cudaEvent_t ev_fork, ev_join;
+    int warp_blocks_per_sm;  // launch shape of the per-warp island solve
+    int warp_carveout;       // shared-memory carveout (percent) of the per-warp island solve
     // persistent contact cache (double buffered by parity)
     unsigned long long *cache_keys[2];
     CacheRecord *cache_recs[2];
@@ -194,6 +200,8 @@ struct DevWorld {
     int *root_flag;
     int *small_list, *large_list;
     int *scratch_order, *scratch_colour, *scratch_claim;
+    int *mid_list;    // islands solved by one warp each
+    int *body_local;  // index of a body inside its island's body list (per-warp solve)
 };
 
 // ---------------------------------------------------------------------------

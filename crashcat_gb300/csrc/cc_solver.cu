@@ -31,6 +31,10 @@ void upload_settings_solver(const DevSettings &s, cudaStream_t st) {
 constexpr unsigned long long EMPTY_KEY = 0xffffffffffffffffull;
 constexpr int SMALL_ISLAND_MAX_CONS = 64;  // upper bound of the per-thread class (register arrays)
 constexpr int SMALL_ISLAND_MAX_BODIES = 64;
+// islands above the per-thread class and within these limits run on one warp
+constexpr int WARP_MAX_CONS = 256;
+constexpr int WARP_MAX_BODIES = 128;
+constexpr int WARP_MAX_COLOURS = 64;  // colours past this one are swept by one lane in order
 
 struct CacheTables {
     unsigned long long *keys[2];
@@ -432,6 +436,9 @@ __global__ void k_island_classify(DevWorld w, int *small_list, int *large_list) 
         if (nc <= c_settings.small_island_max_cons && nb <= SMALL_ISLAND_MAX_BODIES) {
             int k = atomicAdd(&w.ctr->num_small_islands, 1);
             small_list[k] = i;
+        } else if (nc <= WARP_MAX_CONS && nb <= WARP_MAX_BODIES) {
+            int k = atomicAdd(&w.ctr->num_mid_islands, 1);
+            w.mid_list[k] = i;
         } else {
             int k = atomicAdd(&w.ctr->num_large_islands, 1);
             large_list[k] = i;
@@ -973,6 +980,273 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// mid-size islands: one warp per island.  The island's contacts are sorted by
+// the reference key (bitonic sort in shared memory), greedily coloured in that
+// order, and swept colour by colour with the island's body velocities held in
+// shared memory; a __syncwarp separates the colours.
+// ---------------------------------------------------------------------------
+constexpr int WARP_BLOCK = 128;
+constexpr int WARPS_PER_BLOCK = WARP_BLOCK / 32;
+
+struct WarpIsland {
+    uint32_t key[WARP_MAX_CONS];  // sort key, then colour
+    int ia[WARP_MAX_CONS];        // body A id, then local index of A (-1: not in the island)
+    int ib[WARP_MAX_CONS];
+    int idx[WARP_MAX_CONS];       // constraint index in rank order
+    int sorted[WARP_MAX_CONS];    // ranks grouped by colour, rank order inside a colour
+    int cstart[WARP_MAX_COLOURS + 2];
+    float4 v[WARP_MAX_BODIES];    // linear velocity | inverse mass
+    float4 av[WARP_MAX_BODIES];   // angular velocity | flags (bit pattern)
+    float4 I0[WARP_MAX_BODIES];   // world inverse inertia xx xy xz yy
+    float2 I1[WARP_MAX_BODIES];   // yz zz
+    int body[WARP_MAX_BODIES];
+    int claim[WARP_MAX_BODIES];
+};
+
+__device__ __forceinline__ bool rank_less(const WarpIsland &s, int x, int y) {
+    if (s.key[x] != s.key[y]) return s.key[x] < s.key[y];
+    if (s.ia[x] != s.ia[y]) return s.ia[x] < s.ia[y];
+    return s.ib[x] < s.ib[y];
+}
+
+__device__ __forceinline__ BodyRef warp_body(const DevWorld &w, const WarpIsland &s, int local, int global) {
+    if (local < 0) return load_body(w, global);
+    BodyRef b;
+    float4 v = s.v[local], av = s.av[local];
+    uint32_t f = __float_as_uint(av.w);
+    b.v = xyz(v);
+    b.w = xyz(av);
+    b.im = v.w;
+    b.motion = motion_of(f);
+    b.dof = dof_of(f);
+    float4 i0 = s.I0[local];
+    float2 i1 = s.I1[local];
+    b.I = Sym3{i0.x, i0.y, i0.z, i0.w, i1.x, i1.y};
+    return b;
+}
+__device__ __forceinline__ void warp_store(WarpIsland &s, int local, const BodyRef &b) {
+    if (local < 0 || b.motion != DYNAMIC) return;
+    s.v[local] = make_float4(b.v.x, b.v.y, b.v.z, s.v[local].w);
+    s.av[local] = make_float4(b.w.x, b.w.y, b.w.z, s.av[local].w);
+}
+
+__global__ void __launch_bounds__(WARP_BLOCK) k_solve_warp(DevWorld w, CacheTables ct, float dt, float ratio) {
+    extern __shared__ WarpIsland s_isl[];  // WARPS_PER_BLOCK entries
+    const int lane = threadIdx.x & 31;
+    WarpIsland &S = s_isl[threadIdx.x >> 5];
+    const unsigned FULL = 0xffffffffu;
+    const int nmid = w.ctr->num_mid_islands;
+    CacheRecord *crecs = ct.recs[*ct.parity];
+    while (true) {
+        int li = 0;
+        if (lane == 0) li = atomicAdd(&w.ctr->mid_cursor, 1);
+        li = __shfl_sync(FULL, li, 0);
+        if (li >= nmid) break;
+        const int isl = w.mid_list[li];
+        const int nb = w.island_body_count[isl], nc = w.island_cons_count[isl];
+        const int *bl = w.island_bodies + w.island_body_off[isl];
+        const int *cl = w.island_cons + w.island_cons_off[isl];
+        // bodies: velocities, inverse mass, flags and world inverse inertia into shared memory
+        for (int k = lane; k < nb; k += 32) {
+            int i = bl[k];
+            uint32_t f = w.flags[i];
+            float4 ii = w.inv_inertia[i];
+            float4 v = w.linvel[i], av = w.angvel[i];
+            Sym3 I{0, 0, 0, 0, 0, 0};
+            if (motion_of(f) == DYNAMIC) I = world_inv_inertia(w.quat[i], w.inertia_rot[i], xyz(ii), dof_of(f));
+            S.v[k] = make_float4(v.x, v.y, v.z, ii.w);
+            S.av[k] = make_float4(av.x, av.y, av.z, __uint_as_float(f));
+            S.I0[k] = make_float4(I.xx, I.xy, I.xz, I.yy);
+            S.I1[k] = make_float2(I.yz, I.zz);
+            S.body[k] = i;
+            w.body_local[i] = k;
+        }
+        // contacts: keys for the rank sort, padded to a power of two
+        int P = 32;
+        while (P < nc) P <<= 1;
+        for (int k = lane; k < P; k += 32) {
+            if (k < nc) {
+                int ci = cl[k];
+                const ContactConstraint &c = w.cons[ci];
+                S.key[k] = c.sort_key;
+                S.ia[k] = c.a;
+                S.ib[k] = c.b;
+                S.idx[k] = ci;
+            } else {
+                S.key[k] = 0xffffffffu;
+                S.ia[k] = 0x7fffffff;
+                S.ib[k] = 0x7fffffff;
+                S.idx[k] = -1;
+            }
+        }
+        __syncwarp();
+        // sortContactIndices (contact-constraints.ts:1240-1264): bitonic sort by (sortKey, idA, idB)
+        for (int kk = 2; kk <= P; kk <<= 1) {
+            for (int j = kk >> 1; j > 0; j >>= 1) {
+                for (int i = lane; i < P; i += 32) {
+                    int l = i ^ j;
+                    if (l > i) {
+                        bool up = (i & kk) == 0;
+                        if (rank_less(S, l, i) == up) {
+                            uint32_t tk = S.key[i];
+                            S.key[i] = S.key[l];
+                            S.key[l] = tk;
+                            int t = S.ia[i];
+                            S.ia[i] = S.ia[l];
+                            S.ia[l] = t;
+                            t = S.ib[i];
+                            S.ib[i] = S.ib[l];
+                            S.ib[l] = t;
+                            t = S.idx[i];
+                            S.idx[i] = S.idx[l];
+                            S.idx[l] = t;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        // local body indices (-1 when the body is not one of this island's bodies)
+        for (int k = lane; k < nc; k += 32) {
+            int a = S.ia[k], b = S.ib[k];
+            int la = w.body_local[a], lb = w.body_local[b];
+            S.ia[k] = (la >= 0 && la < nb && S.body[la] == a) ? la : -1;
+            S.ib[k] = (lb >= 0 && lb < nb && S.body[lb] == b) ? lb : -1;
+            S.key[k] = 0xffffffffu;  // colour: unassigned
+        }
+        __syncwarp();
+        // greedy colouring in rank order: per round, the lowest unassigned rank on each dynamic body claims it
+        int ncol = 0;
+        bool tail = false;
+        while (true) {
+            for (int k = lane; k < nb; k += 32) S.claim[k] = 0x7fffffff;
+            __syncwarp();
+            bool left = false;
+            for (int k = lane; k < nc; k += 32) {
+                if (S.key[k] != 0xffffffffu) continue;
+                left = true;
+                int la = S.ia[k], lb = S.ib[k];
+                if (la >= 0 && motion_of(__float_as_uint(S.av[la].w)) == DYNAMIC) atomicMin(&S.claim[la], k);
+                if (lb >= 0 && motion_of(__float_as_uint(S.av[lb].w)) == DYNAMIC) atomicMin(&S.claim[lb], k);
+            }
+            __syncwarp();
+            if (!__any_sync(FULL, left)) break;
+            if (ncol == WARP_MAX_COLOURS) {
+                for (int k = lane; k < nc; k += 32)
+                    if (S.key[k] == 0xffffffffu) S.key[k] = WARP_MAX_COLOURS;
+                tail = true;
+                __syncwarp();
+                break;
+            }
+            for (int k = lane; k < nc; k += 32) {
+                if (S.key[k] != 0xffffffffu) continue;
+                int la = S.ia[k], lb = S.ib[k];
+                bool oka = la < 0 || motion_of(__float_as_uint(S.av[la].w)) != DYNAMIC || S.claim[la] == k;
+                bool okb = lb < 0 || motion_of(__float_as_uint(S.av[lb].w)) != DYNAMIC || S.claim[lb] == k;
+                if (oka && okb) S.key[k] = (uint32_t)ncol;
+            }
+            __syncwarp();
+            ncol++;
+        }
+        const int nsweep = ncol + (tail ? 1 : 0);
+        // group ranks by colour, keeping rank order inside each colour
+        {
+            int pos = 0;
+            for (int c = 0; c < nsweep; c++) {
+                uint32_t col = (c < ncol) ? (uint32_t)c : (uint32_t)WARP_MAX_COLOURS;
+                if (lane == 0) S.cstart[c] = pos;
+                for (int base = 0; base < nc; base += 32) {
+                    int k = base + lane;
+                    bool pred = k < nc && S.key[k] == col;
+                    unsigned m = __ballot_sync(FULL, pred);
+                    if (pred) S.sorted[pos + __popc(m & ((1u << lane) - 1u))] = k;
+                    pos += __popc(m);
+                }
+            }
+            if (lane == 0) S.cstart[nsweep] = pos;
+        }
+        __syncwarp();
+        // warm start and velocity iterations, colour by colour
+        for (int pass = (c_settings.warm_starting ? -1 : 0); pass < c_settings.vel_iters; pass++) {
+            for (int c = 0; c < nsweep; c++) {
+                int s0 = S.cstart[c], s1 = S.cstart[c + 1];
+                bool serial = tail && c == ncol;
+                int e0 = serial ? (lane == 0 ? s0 : s1) : s0 + lane;
+                int es = serial ? 1 : 32;
+                for (int e = e0; e < s1; e += es) {
+                    int k = S.sorted[e];
+                    ContactConstraint &con = w.cons[S.idx[k]];
+                    int la = S.ia[k], lb = S.ib[k];
+                    BodyRef A = warp_body(w, S, la, con.a), B = warp_body(w, S, lb, con.b);
+                    if (pass < 0)
+                        warm_start_con(con, A, B, ratio);
+                    else
+                        solve_velocity_con(con, A, B);
+                    warp_store(S, la, A);
+                    warp_store(S, lb, B);
+                }
+                __syncwarp();
+            }
+        }
+        for (int k = lane; k < nc; k += 32) store_impulses(w, crecs, w.cons[S.idx[k]]);
+        // velocities back to global memory, then integration (update.ts:896-976)
+        for (int k = lane; k < nb; k += 32) {
+            int i = S.body[k];
+            if (motion_of(__float_as_uint(S.av[k].w)) == DYNAMIC) {
+                float4 v = S.v[k], av = S.av[k];
+                w.linvel[i] = make_float4(v.x, v.y, v.z, 0.f);
+                w.angvel[i] = make_float4(av.x, av.y, av.z, 0.f);
+            }
+            integrate_body(w, i, dt);
+        }
+        __syncwarp();
+        // position iterations (contact-constraints.ts:1098-1216), early exit as update.ts:218-221
+        for (int it = 0; it < c_settings.pos_iters; it++) {
+            bool any = false;
+            for (int c = 0; c < nsweep; c++) {
+                int s0 = S.cstart[c], s1 = S.cstart[c + 1];
+                bool serial = tail && c == ncol;
+                int e0 = serial ? (lane == 0 ? s0 : s1) : s0 + lane;
+                int es = serial ? 1 : 32;
+                for (int e = e0; e < s1; e += es) {
+                    const ContactConstraint &con = w.cons[S.idx[S.sorted[e]]];
+                    uint32_t fa = w.flags[con.a], fb = w.flags[con.b];
+                    PoseRef PA{xyz(w.com[con.a]), w.quat[con.a]}, PB{xyz(w.com[con.b]), w.quat[con.b]};
+                    if (solve_position_con(w, con, PA, PB, motion_of(fa), motion_of(fb), fa, fb)) {
+                        if (motion_of(fa) == DYNAMIC) {
+                            w.com[con.a] = make_float4(PA.com.x, PA.com.y, PA.com.z, 0.f);
+                            w.quat[con.a] = PA.q;
+                        }
+                        if (motion_of(fb) == DYNAMIC) {
+                            w.com[con.b] = make_float4(PB.com.x, PB.com.y, PB.com.z, 0.f);
+                            w.quat[con.b] = PB.q;
+                        }
+                        any = true;
+                    }
+                }
+                __syncwarp();
+            }
+            if (!__any_sync(FULL, any)) break;
+        }
+        for (int k = lane; k < nb; k += 32) finish_body(w, S.body[k]);
+        __syncwarp();
+        if (c_settings.allow_sleeping) {
+            bool mine = true;
+            for (int k = lane; k < nb; k += 32) {
+                int i = S.body[k];
+                if (motion_of(w.flags[i]) != DYNAMIC) continue;
+                if (!sleep_update(w, i, dt)) mine = false;
+            }
+            if (__all_sync(FULL, mine))
+                for (int k = lane; k < nb; k += 32)
+                    if (motion_of(w.flags[S.body[k]]) == DYNAMIC) sleep_body(w, S.body[k]);
+        }
+        __syncwarp();
+    }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -1023,8 +1297,22 @@ void launch_solver(DevWorld &w, float dt, float ratio, cudaStream_t s, cudaEvent
     CacheTables ct = tables_of(w);
     k_solve_small<<<grid_for(w.n, 128, 16), 128, 0, s>>>(w, ct, w.small_list, dt, ratio);
     if (mid) cudaEventRecord(mid, s);
-    k_solve_large<<<NUM_SMS * 2, LARGE_BLOCK, 0, s>>>(w, ct, w.large_list, w.scratch_order, w.scratch_colour,
-                                                      w.scratch_claim, dt, ratio);
+    static bool warp_smem_set = false;  // set on the first (eager) step, before any graph capture
+    const size_t warp_smem = sizeof(WarpIsland) * WARPS_PER_BLOCK;
+    if (!warp_smem_set) {
+        cudaFuncSetAttribute(k_solve_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)warp_smem);
+        warp_smem_set = true;
+    }
+    if (w.warp_carveout >= 0)
+        cudaFuncSetAttribute(k_solve_warp, cudaFuncAttributePreferredSharedMemoryCarveout, w.warp_carveout);
+    // the per-CTA and per-warp classes hold disjoint islands: run them side by side
+    cudaEventRecord(w.ev_fork, s);
+    cudaStreamWaitEvent(w.aux_stream, w.ev_fork, 0);
+    k_solve_large<<<NUM_SMS * 2, LARGE_BLOCK, 0, w.aux_stream>>>(w, ct, w.large_list, w.scratch_order,
+                                                                 w.scratch_colour, w.scratch_claim, dt, ratio);
+    cudaEventRecord(w.ev_join, w.aux_stream);
+    k_solve_warp<<<NUM_SMS * w.warp_blocks_per_sm, WARP_BLOCK, warp_smem, s>>>(w, ct, dt, ratio);
+    cudaStreamWaitEvent(s, w.ev_join, 0);
 }
 
 }  // namespace cc

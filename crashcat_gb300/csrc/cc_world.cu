@@ -155,7 +155,8 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
     d.time_before_sleep = (float)s->time_before_sleep;
     d.sleep_threshold = (float)s->point_velocity_sleep_threshold;
     // launch-shape tunable: islands with at most this many contacts are solved by one
-    // thread in the reference's exact order, larger ones by a CTA with graph colouring
+    // thread in the reference's exact order, larger ones by a warp (up to 256 contacts
+    // and 128 bodies) or a CTA with order-preserving graph colouring
     d.small_island_max_cons = 8;
     if (const char *e = getenv("CRASHCAT_SMALL_ISLAND_MAX")) {
         int v = atoi(e);
@@ -256,6 +257,16 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
         int et = cap / 8;
         et = et < 1024 ? 1024 : (et > EPA_MAX_THREADS ? EPA_MAX_THREADS : et);
         w.epa_threads = (et + 63) / 64 * 64;
+        w.warp_blocks_per_sm = 4;
+        w.warp_carveout = 50;
+        if (const char *e = getenv("CRASHCAT_WARP_BLOCKS_PER_SM")) {
+            int v = atoi(e);
+            if (v >= 1 && v <= 4) w.warp_blocks_per_sm = v;
+        }
+        if (const char *e = getenv("CRASHCAT_WARP_CARVEOUT")) {
+            int v = atoi(e);
+            if (v >= 0 && v <= 100) w.warp_carveout = v;
+        }
         char *q = nullptr;
         if ((r = dalloc(&q, epa_scratch_bytes() * (size_t)w.epa_threads)) != CC_OK) {
             cc_world_destroy(W);
@@ -275,8 +286,13 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
     ALLOC(scratch_order, w.max_manifolds);
     ALLOC(scratch_colour, w.max_manifolds);
     ALLOC(scratch_claim, (size_t)cap + (size_t)w.max_manifolds + 16);
+    ALLOC(mid_list, cap);
+    ALLOC(body_local, cap);
 #undef ALLOC
-    if ((r = cuda_ok(cudaStreamCreateWithFlags(&W->stream, cudaStreamNonBlocking))) != CC_OK) {
+    if ((r = cuda_ok(cudaStreamCreateWithFlags(&W->stream, cudaStreamNonBlocking))) != CC_OK ||
+        (r = cuda_ok(cudaStreamCreateWithFlags(&w.aux_stream, cudaStreamNonBlocking))) != CC_OK ||
+        (r = cuda_ok(cudaEventCreateWithFlags(&w.ev_fork, cudaEventDisableTiming))) != CC_OK ||
+        (r = cuda_ok(cudaEventCreateWithFlags(&w.ev_join, cudaEventDisableTiming))) != CC_OK) {
         cc_world_destroy(W);
         return r;
     }
@@ -308,13 +324,16 @@ int cc_world_destroy(cc_world *W) {
                     w.island_fill_b, w.island_fill_c, w.inv_inertia_world, w.scan_tmp, w.ctr, w.scene,
                     w.node_world, w.epa_items, w.epa_scratch, w.cache_keys[0], w.cache_keys[1], w.cache_recs[0],
                     w.cache_recs[1], w.cache_parity, w.root_flag, w.small_list, w.large_list, w.scratch_order,
-                    w.scratch_colour, w.scratch_claim, W->d_state_rows};
+                    w.scratch_colour, w.scratch_claim, w.mid_list, w.body_local, W->d_state_rows};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (W->h_ctr) cudaFreeHost(W->h_ctr);
     if (W->ev_begin) cudaEventDestroy(W->ev_begin);
     if (W->ev_end) cudaEventDestroy(W->ev_end);
     if (W->stream) cudaStreamDestroy(W->stream);
+    if (w.aux_stream) cudaStreamDestroy(w.aux_stream);
+    if (w.ev_fork) cudaEventDestroy(w.ev_fork);
+    if (w.ev_join) cudaEventDestroy(w.ev_join);
     delete W;
     return CC_OK;
 }

@@ -249,3 +249,25 @@ def box_row(count: int = 6, seed: int = 31, gap: float = -0.005) -> Scene:
     b["position"][idx] = pos.astype(np.float32)
     b["linear_velocity"][idx] = rng.normal(scale=0.5, size=(count, 3)).astype(np.float32)
     return Scene("box_row", b, dt=1.0 / 60.0, steps=1, seed=seed)
+
+
+def box_pyramid(base: int = 8, seed: int = 41, gap: float = -0.004) -> Scene:
+    """A 2-D pyramid of equal boxes (rows of base, base-1, ..., 1) resting on the
+    floor, each box pressed slightly into its neighbours: one island of about
+    3 x base^2 / 2 contacts, solved by one warp up to 256 contacts."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    count = base * (base + 1) // 2
+    b = blank_bodies(count + 1)
+    static_floor(b, 0, half=(30.0, 0.5, 30.0), friction=0.5)
+    idx = np.arange(1, count + 1)
+    set_box(b, idx, (0.5, 0.5, 0.5))
+    b["friction"][idx] = 0.5
+    pos = []
+    for row in range(base):
+        for k in range(base - row):
+            pos.append(((k + 0.5 * row) * (1.0 + gap), 0.5 - 0.003 + row * (1.0 - 0.006), 0.0))
+    pos = np.asarray(pos)
+    pos[:, 2] = rng.uniform(-0.03, 0.03, size=count)
+    b["position"][idx] = pos.astype(np.float32)
+    b["linear_velocity"][idx] = rng.normal(scale=0.3, size=(count, 3)).astype(np.float32)
+    return Scene("box_pyramid", b, dt=1.0 / 60.0, steps=1, seed=seed)
