@@ -55,7 +55,9 @@ struct DevCounters {
     int large_cursor;
     int num_mid_islands;
     int mid_cursor;
-    int pad[18];
+    int epa_cursor;
+    int epa_fallback;  // EPA items handed to the pass with the reference's polytope limits
+    int pad[16];
 };
 
 // Settings copied into constant memory once per world.
@@ -186,8 +188,12 @@ struct DevWorld {
     int2 *node_world;      // world range of each LBVH node
     // narrowphase scratch
     void *epa_items;
-    void *epa_scratch;     // one EPA polytope per EPA thread
-    int epa_threads;       // threads (and scratch slices) of the EPA kernel
+    void *epa_packed;      // packed EPA polytopes, one per thread of the packed pass
+    void *epa_scratch;     // polytopes with the reference's limits, one per thread of the fallback pass
+    int *epa_fallback;     // items the packed pass handed to the fallback pass
+    int epa_threads;       // threads of the packed EPA pass
+    int epa_packed_points; // support points a packed polytope may hold before its item falls back
+    int epa_fetch_warp;    // EPA items taken 32 at a time per warp (1) or one at a time per thread (0)
     cudaStream_t aux_stream;  // second stream: the per-CTA island solve runs beside the per-warp one
     cudaEvent_t ev_fork, ev_join;
     int warp_blocks_per_sm;  // launch shape of the per-warp island solve
@@ -312,8 +318,11 @@ void launch_update_bounds(DevWorld &w, cudaStream_t s);
 void upload_settings(const DevSettings &s, double spec64, cudaStream_t st);
 void launch_cache_begin(DevWorld &w, cudaStream_t s);
 size_t epa_scratch_bytes();
+size_t epa_packed_block_bytes();
 size_t epa_item_bytes();
-constexpr int EPA_MAX_THREADS = NUM_SMS * 4 * 64;  // one EPA polytope per resident EPA thread
+constexpr int EPA_DEFAULT_MAX_THREADS = NUM_SMS * 4 * 64;  // one EPA polytope per resident EPA thread
+constexpr int EPA_MAX_THREADS = NUM_SMS * 8 * 64;          // upper bound of the launch-shape override
+constexpr int EPA_BIG_THREADS = 1024;  // threads of the fallback pass with the reference's polytope limits
 
 // scan / sort utilities (cc_scan.cu)
 void exclusive_scan_int(const int *in, int *out, int n, int *total, int *tmp, cudaStream_t s);

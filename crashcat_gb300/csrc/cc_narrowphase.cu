@@ -908,52 +908,229 @@ __global__ void __launch_bounds__(128) k_narrowphase(DevWorld w, EpaItem *epa_it
 }
 
 // ---------------------------------------------------------------------------
-// EPA (penetration.ts:214-614 + epa-convex-hull-builder.ts) in FP64 with the
-// polytope in a per-thread slice of global scratch memory
+// EPA (penetration.ts:214-614 + epa-convex-hull-builder.ts) in FP64.
+//
+// The hull algorithm is written once over a storage policy:
+//  * PackedStore: a compact polytope (32 support points, 64 triangles) with every
+//    array interleaved across the 64 threads of a block ([element][thread]), so a
+//    warp touching the same element of its lanes' polytopes reads one or two
+//    cache lines.  The reference's polytopes stay far below these limits (on the
+//    seeded scenes: 15 points and 25 triangles at most).
+//  * BigStore: the reference's limits (128 points, 256 triangles, 128-edge
+//    horizon) in a per-thread slice.  Items whose polytope outgrows the packed
+//    limits are re-run from their GJK simplex with this store, so every item gets
+//    the reference's behaviour at the reference's limits.
 // ---------------------------------------------------------------------------
+// the real type of the polytope arithmetic
+using R = double;
+constexpr R R_EPS_INTERIOR = R(1e-3);           // interior test margin (:287-289)
+constexpr R R_ONE_PLUS_EPS = R(1.0 + 1e-3);
+constexpr R R_MIN_NORMAL_SQ = R(1e-10);         // degenerate-normal threshold (:255, :300)
+constexpr R R_THIRD = R(1.0 / 3.0);
 constexpr int EPA_MAX_TRI = 256;
 constexpr int EPA_PTS_CAP = 160;
 constexpr int EPA_QUEUE_CAP = 512;
+constexpr int EPA_EDGE_CAP = 128;
+constexpr int EPA_BLOCK = 64;
+
+// triangle flags
+enum : int { TF_REL0 = 1, TF_INTERIOR = 2, TF_REMOVED = 4, TF_INQ = 8 };
 
 struct EpaTri {
-    V<double> normal, centroid;
-    double cls;
-    double l0, l1;
+    V<R> normal, centroid;
+    R cls;
     int nt[3];
     int ne[3];
     int st[3];
-    int flags;  // 1 rel0, 2 interior, 4 removed, 8 inq
+    int flags;
 };
 struct EpaScratch {
-    V<double> Y[EPA_PTS_CAP], P[EPA_PTS_CAP], Qp[EPA_PTS_CAP];
+    V<R> Y[EPA_PTS_CAP], P[EPA_PTS_CAP], Qp[EPA_PTS_CAP];
     EpaTri tri[EPA_MAX_TRI];
     int queue[EPA_QUEUE_CAP];
     int freel[EPA_MAX_TRI];
-    int edge_nt[128], edge_ne[128], edge_st[128];
-    int stk_t[128], stk_e[128], stk_i[128];
-    int newt[128];
+    int edge_nt[EPA_EDGE_CAP], edge_ne[EPA_EDGE_CAP], edge_st[EPA_EDGE_CAP];
+    int stk_t[EPA_EDGE_CAP], stk_e[EPA_EDGE_CAP], stk_i[EPA_EDGE_CAP];
+    int newt[EPA_EDGE_CAP];
 };
 size_t epa_scratch_bytes() { return sizeof(EpaScratch); }
-size_t epa_item_bytes();
 
-struct EpaHull {
+struct BigStore {
+    static constexpr int PTS = EPA_PTS_CAP, TRI = EPA_MAX_TRI, QCAP = EPA_QUEUE_CAP, ECAP = EPA_EDGE_CAP;
+    static constexpr bool PACKED = false;
     EpaScratch *s;
-    int ntri, nfree, nq, npts;
-    __device__ bool facing(int t, V<double> p) const {
-        const EpaTri &T = s->tri[t];
-        return dot(T.normal, p - T.centroid) > 0.0;
+    __device__ V<R> Y(int i) const { return s->Y[i]; }
+    __device__ V<R> P(int i) const { return s->P[i]; }
+    __device__ V<R> Q(int i) const { return s->Qp[i]; }
+    __device__ void set_point(int i, V<R> y, V<R> p, V<R> q) {
+        s->Y[i] = y;
+        s->P[i] = p;
+        s->Qp[i] = q;
     }
+    __device__ V<R> normal(int t) const { return s->tri[t].normal; }
+    __device__ V<R> centroid(int t) const { return s->tri[t].centroid; }
+    __device__ R cls(int t) const { return s->tri[t].cls; }
+    __device__ int flags(int t) const { return s->tri[t].flags; }
+    __device__ int st(int t, int k) const { return s->tri[t].st[k]; }
+    __device__ int nt(int t, int k) const { return s->tri[t].nt[k]; }
+    __device__ int ne(int t, int k) const { return s->tri[t].ne[k]; }
+    __device__ void set_geom(int t, V<R> n, V<R> c, R cls) {
+        s->tri[t].normal = n;
+        s->tri[t].centroid = c;
+        s->tri[t].cls = cls;
+    }
+    __device__ void set_flags(int t, int f) { s->tri[t].flags = f; }
+    __device__ void set_st(int t, int a, int b, int c) {
+        s->tri[t].st[0] = a;
+        s->tri[t].st[1] = b;
+        s->tri[t].st[2] = c;
+    }
+    __device__ void set_nb(int t, int k, int n, int e) {
+        s->tri[t].nt[k] = n;
+        s->tri[t].ne[k] = e;
+    }
+    __device__ int q(int i) const { return s->queue[i]; }
+    __device__ void set_q(int i, int t) { s->queue[i] = t; }
+    __device__ int fr(int i) const { return s->freel[i]; }
+    __device__ void set_fr(int i, int t) { s->freel[i] = t; }
+    __device__ void set_edge(int i, int n, int e, int st) {
+        s->edge_nt[i] = n;
+        s->edge_ne[i] = e;
+        s->edge_st[i] = st;
+    }
+    __device__ int edge_nt(int i) const { return s->edge_nt[i]; }
+    __device__ int edge_ne(int i) const { return s->edge_ne[i]; }
+    __device__ int edge_st(int i) const { return s->edge_st[i]; }
+    __device__ void set_stk(int i, int t, int e, int k) {
+        s->stk_t[i] = t;
+        s->stk_e[i] = e;
+        s->stk_i[i] = k;
+    }
+    __device__ int stk_t(int i) const { return s->stk_t[i]; }
+    __device__ int stk_e(int i) const { return s->stk_e[i]; }
+    __device__ int stk_i(int i) const { return s->stk_i[i]; }
+    __device__ void set_stk_i(int i, int k) { s->stk_i[i] = k; }
+    __device__ int newt(int i) const { return s->newt[i]; }
+    __device__ void set_newt(int i, int t) { s->newt[i] = t; }
+};
+
+// one block's packed polytopes: element e of thread j lives at [e][j]
+constexpr int PK_PTS = 32, PK_TRI = 64, PK_Q = 64, PK_E = 32;
+struct PackedBlock {
+    R yx[PK_PTS][EPA_BLOCK], yy[PK_PTS][EPA_BLOCK], yz[PK_PTS][EPA_BLOCK];
+    R px[PK_PTS][EPA_BLOCK], py[PK_PTS][EPA_BLOCK], pz[PK_PTS][EPA_BLOCK];
+    R qx[PK_PTS][EPA_BLOCK], qy[PK_PTS][EPA_BLOCK], qz[PK_PTS][EPA_BLOCK];
+    R nx[PK_TRI][EPA_BLOCK], ny[PK_TRI][EPA_BLOCK], nz[PK_TRI][EPA_BLOCK];
+    R cx[PK_TRI][EPA_BLOCK], cy[PK_TRI][EPA_BLOCK], cz[PK_TRI][EPA_BLOCK];
+    R cl[PK_TRI][EPA_BLOCK];
+    uint32_t vf[PK_TRI][EPA_BLOCK];   // st0 | st1 << 8 | st2 << 16 | flags << 24
+    uint32_t nbt[PK_TRI][EPA_BLOCK];  // neighbour triangles, 8 bits each (0xff: none)
+    uint32_t nbe[PK_TRI][EPA_BLOCK];  // neighbour edges, 8 bits each
+    uint8_t queue[PK_Q][EPA_BLOCK];
+    uint8_t freel[PK_TRI][EPA_BLOCK];
+    uint8_t e_nt[PK_E][EPA_BLOCK], e_ne[PK_E][EPA_BLOCK], e_st[PK_E][EPA_BLOCK];
+    uint8_t s_t[PK_E][EPA_BLOCK], s_e[PK_E][EPA_BLOCK], s_i[PK_E][EPA_BLOCK];
+    uint8_t nw[PK_E][EPA_BLOCK];
+};
+size_t epa_packed_block_bytes() { return sizeof(PackedBlock); }
+
+struct PackedStore {
+    static constexpr int PTS = PK_PTS, TRI = PK_TRI, QCAP = PK_Q, ECAP = PK_E;
+    static constexpr bool PACKED = true;
+    PackedBlock *b;
+    int j;  // thread within the block
+    __device__ V<R> Y(int i) const { return {b->yx[i][j], b->yy[i][j], b->yz[i][j]}; }
+    __device__ V<R> P(int i) const { return {b->px[i][j], b->py[i][j], b->pz[i][j]}; }
+    __device__ V<R> Q(int i) const { return {b->qx[i][j], b->qy[i][j], b->qz[i][j]}; }
+    __device__ void set_point(int i, V<R> y, V<R> p, V<R> q) {
+        b->yx[i][j] = y.x;
+        b->yy[i][j] = y.y;
+        b->yz[i][j] = y.z;
+        b->px[i][j] = p.x;
+        b->py[i][j] = p.y;
+        b->pz[i][j] = p.z;
+        b->qx[i][j] = q.x;
+        b->qy[i][j] = q.y;
+        b->qz[i][j] = q.z;
+    }
+    __device__ V<R> normal(int t) const { return {b->nx[t][j], b->ny[t][j], b->nz[t][j]}; }
+    __device__ V<R> centroid(int t) const { return {b->cx[t][j], b->cy[t][j], b->cz[t][j]}; }
+    __device__ R cls(int t) const { return b->cl[t][j]; }
+    __device__ int flags(int t) const { return (int)(b->vf[t][j] >> 24); }
+    __device__ int st(int t, int k) const { return (int)((b->vf[t][j] >> (8 * k)) & 0xffu); }
+    __device__ int nt(int t, int k) const {
+        uint32_t v = (b->nbt[t][j] >> (8 * k)) & 0xffu;
+        return v == 0xffu ? -1 : (int)v;
+    }
+    __device__ int ne(int t, int k) const { return (int)((b->nbe[t][j] >> (8 * k)) & 0xffu); }
+    __device__ void set_geom(int t, V<R> n, V<R> c, R cls) {
+        b->nx[t][j] = n.x;
+        b->ny[t][j] = n.y;
+        b->nz[t][j] = n.z;
+        b->cx[t][j] = c.x;
+        b->cy[t][j] = c.y;
+        b->cz[t][j] = c.z;
+        b->cl[t][j] = cls;
+    }
+    __device__ void set_flags(int t, int f) { b->vf[t][j] = (b->vf[t][j] & 0x00ffffffu) | ((uint32_t)f << 24); }
+    __device__ void set_st(int t, int a, int c, int d) {
+        b->vf[t][j] = (b->vf[t][j] & 0xff000000u) | (uint32_t)a | ((uint32_t)c << 8) | ((uint32_t)d << 16);
+    }
+    __device__ void set_nb(int t, int k, int n, int e) {
+        uint32_t sh = 8 * k, m = ~(0xffu << sh);
+        b->nbt[t][j] = (b->nbt[t][j] & m) | ((uint32_t)(n < 0 ? 0xff : n) << sh);
+        b->nbe[t][j] = (b->nbe[t][j] & m) | ((uint32_t)e << sh);
+    }
+    __device__ int q(int i) const { return b->queue[i][j]; }
+    __device__ void set_q(int i, int t) { b->queue[i][j] = (uint8_t)t; }
+    __device__ int fr(int i) const { return b->freel[i][j]; }
+    __device__ void set_fr(int i, int t) { b->freel[i][j] = (uint8_t)t; }
+    __device__ void set_edge(int i, int n, int e, int st) {
+        b->e_nt[i][j] = (uint8_t)n;
+        b->e_ne[i][j] = (uint8_t)e;
+        b->e_st[i][j] = (uint8_t)st;
+    }
+    __device__ int edge_nt(int i) const { return b->e_nt[i][j]; }
+    __device__ int edge_ne(int i) const { return b->e_ne[i][j]; }
+    __device__ int edge_st(int i) const { return b->e_st[i][j]; }
+    __device__ void set_stk(int i, int t, int e, int k) {
+        b->s_t[i][j] = (uint8_t)t;
+        b->s_e[i][j] = (uint8_t)e;
+        b->s_i[i][j] = (uint8_t)k;
+    }
+    __device__ int stk_t(int i) const { return b->s_t[i][j]; }
+    __device__ int stk_e(int i) const { return b->s_e[i][j]; }
+    __device__ int stk_i(int i) const { return (int)(int8_t)b->s_i[i][j]; }
+    __device__ void set_stk_i(int i, int k) { b->s_i[i][j] = (uint8_t)(int8_t)k; }
+    __device__ int newt(int i) const { return b->nw[i][j]; }
+    __device__ void set_newt(int i, int t) { b->nw[i][j] = (uint8_t)t; }
+};
+
+template <class S>
+struct Hull {
+    S st;
+    int ntri, nfree, nq, npts;
+    int pts_limit;  // support points this store may hold (at most S::PTS)
+    bool overflow;  // a packed limit was exceeded: the item must be re-run with the reference's limits
+    __device__ bool facing(int t, V<R> p) const { return dot(st.normal(t), p - st.centroid(t)) > 0.0; }
+    __device__ R cls(int t) const { return st.cls(t); }
+    __device__ int flags(int t) const { return st.flags(t); }
+    __device__ void add_flags(int t, int f) { st.set_flags(t, st.flags(t) | f); }
+    // pushTriangleToQueue epa-convex-hull-builder.ts:95-116
     __device__ void push(int t) {
-        if (nq >= EPA_QUEUE_CAP) return;
-        s->queue[nq] = t;
-        s->tri[t].flags |= 8;
+        if (nq >= S::QCAP) {
+            if (S::PACKED) overflow = true;
+            return;
+        }
+        st.set_q(nq, t);
+        add_flags(t, TF_INQ);
         int cur = nq++;
         while (cur > 0) {
             int par = (cur - 1) >> 1;
-            if (s->tri[s->queue[par]].cls > s->tri[s->queue[cur]].cls) {
-                int tmp = s->queue[par];
-                s->queue[par] = s->queue[cur];
-                s->queue[cur] = tmp;
+            int qp = st.q(par), qc = st.q(cur);
+            if (st.cls(qp) > st.cls(qc)) {
+                st.set_q(par, qc);
+                st.set_q(cur, qp);
                 cur = par;
             } else {
                 break;
@@ -962,115 +1139,142 @@ struct EpaHull {
     }
     __device__ int pop() {
         if (nq == 0) return -1;
-        int tmp = s->queue[nq - 1];
-        s->queue[nq - 1] = s->queue[0];
-        s->queue[0] = tmp;
+        int last = st.q(nq - 1);
+        st.set_q(nq - 1, st.q(0));
+        st.set_q(0, last);
         int count = nq - 1;
         int largest = 0;
         while (true) {
             int child = (largest << 1) + 1;
             if (child >= count) break;
             int prevL = largest;
-            if (s->tri[s->queue[largest]].cls > s->tri[s->queue[child]].cls) largest = child;
+            if (st.cls(st.q(largest)) > st.cls(st.q(child))) largest = child;
             ++child;
-            if (child < count && s->tri[s->queue[largest]].cls > s->tri[s->queue[child]].cls) largest = child;
+            if (child < count && st.cls(st.q(largest)) > st.cls(st.q(child))) largest = child;
             if (prevL == largest) break;
-            int t2 = s->queue[prevL];
-            s->queue[prevL] = s->queue[largest];
-            s->queue[largest] = t2;
+            int t2 = st.q(prevL);
+            st.set_q(prevL, st.q(largest));
+            st.set_q(largest, t2);
         }
         nq--;
-        return s->queue[nq];
+        return st.q(nq);
     }
     __device__ void link(int t1, int e1, int t2, int e2) {
-        s->tri[t1].nt[e1] = t2;
-        s->tri[t1].ne[e1] = e2;
-        s->tri[t2].nt[e2] = t1;
-        s->tri[t2].ne[e2] = e1;
+        st.set_nb(t1, e1, t2, e2);
+        st.set_nb(t2, e2, t1, e1);
     }
+    // createTriangle epa-convex-hull-builder.ts:179-345
     __device__ int create(int i1, int i2, int i3) {
         int idx;
         if (nfree > 0) {
-            idx = s->freel[--nfree];
+            idx = st.fr(--nfree);
         } else {
-            if (ntri >= EPA_MAX_TRI) return -1;
+            if (ntri >= S::TRI) {
+                if (S::PACKED) overflow = true;
+                return -1;
+            }
             idx = ntri++;
         }
-        EpaTri &t = s->tri[idx];
-        t.cls = 1.0 / 0.0;
-        t.l0 = t.l1 = 0.0;
-        t.flags = 0;
-        t.st[0] = i1;
-        t.st[1] = i2;
-        t.st[2] = i3;
-        t.nt[0] = t.nt[1] = t.nt[2] = -1;
-        t.ne[0] = t.ne[1] = t.ne[2] = 0;
-        V<double> y0 = s->Y[i1], y1 = s->Y[i2], y2 = s->Y[i3];
-        V<double> c{(y0.x + y1.x + y2.x) / 3.0, (y0.y + y1.y + y2.y) / 3.0, (y0.z + y1.z + y2.z) / 3.0};
-        t.centroid = c;
-        V<double> y10 = y1 - y0, y20 = y2 - y0, y21 = y2 - y1;
-        double y20d = lsq(y20), y21d = lsq(y21);
+        int fl = 0;
+        R cls = 1.0 / 0.0;
+        st.set_st(idx, i1, i2, i3);
+        for (int k = 0; k < 3; k++) st.set_nb(idx, k, -1, 0);
+        V<R> y0 = st.Y(i1), y1 = st.Y(i2), y2 = st.Y(i3);
+        // centroid (:219-225): the division by 3 is a multiplication by 1/3 here
+        V<R> c{(y0.x + y1.x + y2.x) * R_THIRD, (y0.y + y1.y + y2.y) * R_THIRD, (y0.z + y1.z + y2.z) * R_THIRD};
+        V<R> y10 = y1 - y0, y20 = y2 - y0, y21 = y2 - y1;
+        R y20d = lsq(y20), y21d = lsq(y21);
+        // the interior test l0 > -1e-3, l1 > -1e-3, l0 + l1 < 1 + 1e-3 is taken on the numerators
+        // (det > 0); the lambdas of the triangle the result uses are divided out in epa()
+        V<R> n;
         if (y20d < y21d) {
-            V<double> n = crs(y10, y20);
-            t.normal = n;
-            double nl = lsq(n);
-            if (nl > 1e-10) {
-                double cdn = dot(c, n);
-                t.cls = (fabs(cdn) * cdn) / nl;
-                double y10d = lsq(y10), y1020 = dot(y10, y20);
-                double det = y10d * y20d - y1020 * y1020;
+            n = crs(y10, y20);
+            R nl = lsq(n);
+            if (nl > R_MIN_NORMAL_SQ) {
+                R cdn = dot(c, n);
+                cls = (s_abs(cdn) * cdn) / nl;
+                R y10d = lsq(y10), y1020 = dot(y10, y20);
+                R det = y10d * y20d - y1020 * y1020;
                 if (det > 0.0) {
-                    double a = dot(y0, y10), b = dot(y0, y20);
-                    double l0 = (y1020 * b - y20d * a) / det, l1 = (y1020 * a - y10d * b) / det;
-                    t.l0 = l0;
-                    t.l1 = l1;
-                    t.flags |= 1;
-                    if (l0 > -1e-3 && l1 > -1e-3 && l0 + l1 < 1.0 + 1e-3) t.flags |= 2;
+                    R a = dot(y0, y10), b = dot(y0, y20);
+                    R l0n = y1020 * b - y20d * a, l1n = y1020 * a - y10d * b;
+                    fl |= TF_REL0;
+                    if (l0n > -R_EPS_INTERIOR * det && l1n > -R_EPS_INTERIOR * det && l0n + l1n < R_ONE_PLUS_EPS * det)
+                        fl |= TF_INTERIOR;
                 }
             }
         } else {
-            V<double> n = crs(y10, y21);
-            t.normal = n;
-            double nl = lsq(n);
-            if (nl > 1e-10) {
-                double cdn = dot(c, n);
-                t.cls = (fabs(cdn) * cdn) / nl;
-                double y10d = lsq(y10), y1021 = dot(y10, y21);
-                double det = y10d * y21d - y1021 * y1021;
+            n = crs(y10, y21);
+            R nl = lsq(n);
+            if (nl > R_MIN_NORMAL_SQ) {
+                R cdn = dot(c, n);
+                cls = (s_abs(cdn) * cdn) / nl;
+                R y10d = lsq(y10), y1021 = dot(y10, y21);
+                R det = y10d * y21d - y1021 * y1021;
                 if (det > 0.0) {
-                    double a = dot(y1, y10), b = dot(y1, y21);
-                    double l0 = (y21d * a - y1021 * b) / det, l1 = (y1021 * a - y10d * b) / det;
-                    t.l0 = l0;
-                    t.l1 = l1;
-                    if (l0 > -1e-3 && l1 > -1e-3 && l0 + l1 < 1.0 + 1e-3) t.flags |= 2;
+                    R a = dot(y1, y10), b = dot(y1, y21);
+                    R l0n = y21d * a - y1021 * b, l1n = y1021 * a - y10d * b;
+                    if (l0n > -R_EPS_INTERIOR * det && l1n > -R_EPS_INTERIOR * det && l0n + l1n < R_ONE_PLUS_EPS * det)
+                        fl |= TF_INTERIOR;
                 }
             }
         }
+        st.set_geom(idx, n, c, cls);
+        st.set_flags(idx, fl);
         return idx;
     }
+    // barycentric lambdas of triangle t (the second half of createTriangle)
+    __device__ void lambdas(int t, R &l0, R &l1, bool &rel0) const {
+        V<R> y0 = st.Y(st.st(t, 0)), y1 = st.Y(st.st(t, 1)), y2 = st.Y(st.st(t, 2));
+        V<R> y10 = y1 - y0, y20 = y2 - y0, y21 = y2 - y1;
+        R y20d = lsq(y20), y21d = lsq(y21);
+        l0 = l1 = 0.0;
+        rel0 = false;
+        if (y20d < y21d) {
+            if (!(lsq(crs(y10, y20)) > R_MIN_NORMAL_SQ)) return;
+            R y10d = lsq(y10), y1020 = dot(y10, y20);
+            R det = y10d * y20d - y1020 * y1020;
+            if (det > 0.0) {
+                R a = dot(y0, y10), b = dot(y0, y20);
+                l0 = (y1020 * b - y20d * a) / det;
+                l1 = (y1020 * a - y10d * b) / det;
+                rel0 = true;
+            }
+        } else {
+            if (!(lsq(crs(y10, y21)) > R_MIN_NORMAL_SQ)) return;
+            R y10d = lsq(y10), y1021 = dot(y10, y21);
+            R det = y10d * y21d - y1021 * y1021;
+            if (det > 0.0) {
+                R a = dot(y1, y10), b = dot(y1, y21);
+                l0 = (y21d * a - y1021 * b) / det;
+                l1 = (y1021 * a - y10d * b) / det;
+            }
+        }
+    }
     __device__ void free_tri(int t) {
-        if (nfree < EPA_MAX_TRI) s->freel[nfree++] = t;
+        if (nfree < S::TRI) st.set_fr(nfree++, t);
     }
     __device__ void unlink(int t) {
         for (int i = 0; i < 3; i++) {
-            int n = s->tri[t].nt[i];
+            int n = st.nt(t, i);
             if (n >= 0) {
-                s->tri[n].nt[s->tri[t].ne[i]] = -1;
-                s->tri[t].nt[i] = -1;
+                st.set_nb(n, st.ne(t, i), -1, 0);
+                st.set_nb(t, i, -1, 0);
             }
         }
-        if (!(s->tri[t].flags & 8)) free_tri(t);
+        if (!(flags(t) & TF_INQ)) free_tri(t);
     }
-    __device__ int find_facing(V<double> p) {
+    // findFacingTriangle epa-convex-hull-builder.ts:420-474
+    __device__ int find_facing(V<R> p) {
         int best = -1;
-        double bestd = 0.0;
+        R bestd = 0.0;
         for (int i = 0; i < nq; i++) {
-            int t = s->queue[i];
-            const EpaTri &T = s->tri[t];
-            if (T.flags & 4) continue;
-            double d = dot(T.normal, p - T.centroid);
+            int t = st.q(i);
+            if (flags(t) & TF_REMOVED) continue;
+            V<R> n = st.normal(t);
+            R d = dot(n, p - st.centroid(t));
             if (d > 0.0) {
-                double dsq = (d * d) / lsq(T.normal);
+                R dsq = (d * d) / lsq(n);
                 if (dsq > bestd) {
                     best = t;
                     bestd = dsq;
@@ -1079,113 +1283,128 @@ struct EpaHull {
         }
         return best;
     }
-    // findEdge epa-convex-hull-builder.ts:476-540; returns edge count or -1
-    __device__ int find_edge(int ft, V<double> vtx) {
+    // findEdge epa-convex-hull-builder.ts:476-540; returns the edge count or -1
+    __device__ int find_edge(int ft, V<R> vtx) {
         int ne = 0;
-        s->tri[ft].flags |= 4;
+        add_flags(ft, TF_REMOVED);
         int sp = 0;
-        s->stk_t[0] = ft;
-        s->stk_e[0] = 0;
-        s->stk_i[0] = -1;
+        st.set_stk(0, ft, 0, -1);
         int next_expected = -1;
         int guard = 0;
         while (guard++ < 100000) {
-            int ct = s->stk_t[sp];
-            if (++s->stk_i[sp] >= 3) {
+            int ct = st.stk_t(sp);
+            int si = st.stk_i(sp) + 1;
+            st.set_stk_i(sp, si);
+            if (si >= 3) {
                 unlink(ct);
                 if (--sp < 0) break;
             } else {
-                int ei = (s->stk_e[sp] + s->stk_i[sp]) % 3;
-                int n = s->tri[ct].nt[ei];
-                int nen = s->tri[ct].ne[ei];
-                int est = s->tri[ct].st[ei];
-                if (n >= 0 && !(s->tri[n].flags & 4)) {
+                int ei = (st.stk_e(sp) + si) % 3;
+                int n = st.nt(ct, ei);
+                int nen = st.ne(ct, ei);
+                int est = st.st(ct, ei);
+                if (n >= 0 && !(flags(n) & TF_REMOVED)) {
                     if (facing(n, vtx)) {
-                        s->tri[n].flags |= 4;
+                        add_flags(n, TF_REMOVED);
                         sp++;
-                        if (sp >= 128) return -1;
-                        s->stk_t[sp] = n;
-                        s->stk_e[sp] = nen;
-                        s->stk_i[sp] = 0;
+                        if (sp >= S::ECAP) {
+                            if (S::PACKED) overflow = true;
+                            return -1;
+                        }
+                        st.set_stk(sp, n, nen, 0);
                     } else {
                         if (est != next_expected && next_expected != -1) return -1;
-                        next_expected = s->tri[n].st[nen];
-                        if (ne >= 128) return -1;
-                        s->edge_nt[ne] = n;
-                        s->edge_ne[ne] = nen;
-                        s->edge_st[ne] = est;
+                        next_expected = st.st(n, nen);
+                        if (ne >= S::ECAP) {
+                            if (S::PACKED) overflow = true;
+                            return -1;
+                        }
+                        st.set_edge(ne, n, nen, est);
                         ne++;
                     }
                 }
             }
         }
-        if (ne > 0 && s->edge_st[0] != next_expected) return -1;
+        if (ne > 0 && st.edge_st(0) != next_expected) return -1;
         return ne >= 3 ? ne : -1;
     }
-    __device__ int add_point(int ft, int idx, double closest) {
-        int ne = find_edge(ft, s->Y[idx]);
+    // addPoint epa-convex-hull-builder.ts:541-600
+    __device__ int add_point(int ft, int idx, R closest) {
+        int ne = find_edge(ft, st.Y(idx));
         if (ne < 0) return -1;
         for (int i = 0; i < ne; i++) {
             int in = (i + 1) % ne;
-            int nt = create(s->edge_st[i], s->edge_st[in], idx);
+            int nt = create(st.edge_st(i), st.edge_st(in), idx);
             if (nt < 0) return -1;
-            s->newt[i] = nt;
-            const EpaTri &T = s->tri[nt];
-            if (((T.flags & 2) && T.cls < closest) || T.cls < 0.0) push(nt);
+            st.set_newt(i, nt);
+            if (((flags(nt) & TF_INTERIOR) && cls(nt) < closest) || cls(nt) < 0.0) push(nt);
         }
         for (int i = 0; i < ne; i++) {
             int in = (i + 1) % ne;
-            link(s->newt[i], 0, s->edge_nt[i], s->edge_ne[i]);
-            link(s->newt[i], 1, s->newt[in], 2);
+            link(st.newt(i), 0, st.edge_nt(i), st.edge_ne(i));
+            link(st.newt(i), 1, st.newt(in), 2);
         }
         return ne;
     }
+    __device__ int add_sup(const Sup<R> &A, const Sup<R> &B, V<R> d) {
+        if (npts >= pts_limit) {
+            if (S::PACKED) overflow = true;
+            return -1;
+        }
+        V<R> p = A.get(d), q = B.get(-d);
+        int i = npts++;
+        st.set_point(i, p - q, p, q);
+        return i;
+    }
+    // the GJK simplex the polytope starts from
+    __device__ void start(const EpaItem &it, int limit = S::PTS) {
+        pts_limit = limit < S::PTS ? limit : S::PTS;
+        npts = it.size;
+        nq = ntri = nfree = 0;
+        overflow = false;
+        for (int k = 0; k < it.size; k++) {
+            V<R> y{R(it.y[k].x), R(it.y[k].y), R(it.y[k].z)}, p{R(it.p[k].x), R(it.p[k].y), R(it.p[k].z)};
+            V<R> q{R(it.q[k].x), R(it.q[k].y), R(it.q[k].z)};
+            st.set_point(k, y, p, q);
+        }
+    }
 };
 
-__device__ int epa_add_sup(EpaHull &h, const Sup<double> &A, const Sup<double> &B, V<double> d) {
-    if (h.npts >= EPA_PTS_CAP) return -1;
-    V<double> p = A.get(d), q = B.get(-d);
-    int i = h.npts++;
-    h.s->Y[i] = p - q;
-    h.s->P[i] = p;
-    h.s->Qp[i] = q;
-    return i;
-}
-
-// returns true and the penetration result on success
-__device__ bool epa(EpaHull &h, const Sup<double> &A, const Sup<double> &B, double tol, V<double> &outAxis,
-                    V<double> &outPa, V<double> &outPb) {
-    const double MAXD = 1.7976931348623157e308;
+// penetrationDepthStepEPA penetration.ts:214-614; true and the result on success
+template <class S>
+__device__ bool epa(Hull<S> &h, const Sup<R> &A, const Sup<R> &B, R tol, V<R> &outAxis,
+                    V<R> &outPa, V<R> &outPb) {
+    const R MAXD = 1.7976931348623157e308;
     if (h.npts == 1) {
         h.npts = 0;
-        epa_add_sup(h, A, B, {0.0, 1.0, 0.0});
-        epa_add_sup(h, A, B, {-1.0, -1.0, -1.0});
-        epa_add_sup(h, A, B, {1.0, -1.0, -1.0});
-        epa_add_sup(h, A, B, {0.0, -1.0, 1.0});
+        h.add_sup(A, B, {0.0, 1.0, 0.0});
+        h.add_sup(A, B, {-1.0, -1.0, -1.0});
+        h.add_sup(A, B, {1.0, -1.0, -1.0});
+        h.add_sup(A, B, {0.0, -1.0, 1.0});
     } else if (h.npts == 2) {
-        const double C120 = -0.4999999999999998, S120 = 0.8660254037844387, OMC = 1.0 - C120;
-        V<double> y0 = h.s->Y[0], y1 = h.s->Y[1];
-        V<double> ax = y1 - y0;
-        double al = sqrt(lsq(ax));
-        double nx = ax.x / al, ny = ax.y / al, nz = ax.z / al;
-        V<double> d1;
-        if (fabs(nx) > fabs(ny)) {
-            double pl = sqrt(nx * nx + nz * nz);
+        constexpr R C120 = R(-0.4999999999999998), S120 = R(0.8660254037844387), OMC = R(1.4999999999999998);
+        V<R> y0 = h.st.Y(0), y1 = h.st.Y(1);
+        V<R> ax = y1 - y0;
+        R al = sq_root(lsq(ax));
+        R nx = ax.x / al, ny = ax.y / al, nz = ax.z / al;
+        V<R> d1;
+        if (s_abs(nx) > s_abs(ny)) {
+            R pl = sq_root(nx * nx + nz * nz);
             d1 = {nz / pl, 0.0, -nx / pl};
         } else {
-            double pl = sqrt(ny * ny + nz * nz);
+            R pl = sq_root(ny * ny + nz * nz);
             d1 = {0.0, nz / pl, -ny / pl};
         }
-        double r00 = C120 + nx * nx * OMC, r01 = nx * ny * OMC - nz * S120, r02 = nx * nz * OMC + ny * S120;
-        double r10 = ny * nx * OMC + nz * S120, r11 = C120 + ny * ny * OMC, r12 = ny * nz * OMC - nx * S120;
-        double r20 = nz * nx * OMC - ny * S120, r21 = nz * ny * OMC + nx * S120, r22 = C120 + nz * nz * OMC;
-        V<double> d2{r00 * d1.x + r01 * d1.y + r02 * d1.z, r10 * d1.x + r11 * d1.y + r12 * d1.z,
+        R r00 = C120 + nx * nx * OMC, r01 = nx * ny * OMC - nz * S120, r02 = nx * nz * OMC + ny * S120;
+        R r10 = ny * nx * OMC + nz * S120, r11 = C120 + ny * ny * OMC, r12 = ny * nz * OMC - nx * S120;
+        R r20 = nz * nx * OMC - ny * S120, r21 = nz * ny * OMC + nx * S120, r22 = C120 + nz * nz * OMC;
+        V<R> d2{r00 * d1.x + r01 * d1.y + r02 * d1.z, r10 * d1.x + r11 * d1.y + r12 * d1.z,
                      r20 * d1.x + r21 * d1.y + r22 * d1.z};
-        V<double> d3{r00 * d2.x + r01 * d2.y + r02 * d2.z, r10 * d2.x + r11 * d2.y + r12 * d2.z,
+        V<R> d3{r00 * d2.x + r01 * d2.y + r02 * d2.z, r10 * d2.x + r11 * d2.y + r12 * d2.z,
                      r20 * d2.x + r21 * d2.y + r22 * d2.z};
-        epa_add_sup(h, A, B, d1);
-        epa_add_sup(h, A, B, d2);
-        epa_add_sup(h, A, B, d3);
+        h.add_sup(A, B, d1);
+        h.add_sup(A, B, d2);
+        h.add_sup(A, B, d3);
     }
     if (h.npts < 3) return false;
     h.ntri = 0;
@@ -1199,127 +1418,204 @@ __device__ bool epa(EpaHull &h, const Sup<double> &A, const Sup<double> &B, doub
     h.push(t1);
     h.push(t2);
     for (int i = 3; i < h.npts; i++) {
-        int t = h.find_facing(h.s->Y[i]);
+        int t = h.find_facing(h.st.Y(i));
         if (t >= 0 && h.add_point(t, i, MAXD) < 0) return false;
     }
     int guard = 0;
     while (guard++ < 4096) {
         if (h.nq == 0) return false;
-        int t = h.s->queue[0];
-        if (h.s->tri[t].flags & 4) {
+        int t = h.st.q(0);
+        if (h.flags(t) & TF_REMOVED) {
             h.pop();
             if (h.nq == 0) return false;
             h.free_tri(t);
             continue;
         }
-        if (h.s->tri[t].cls >= 0.0) break;
+        if (h.cls(t) >= 0.0) break;
         h.pop();
-        int ni = epa_add_sup(h, A, B, h.s->tri[t].normal);
+        int ni = h.add_sup(A, B, h.st.normal(t));
         if (ni < 0) return false;
-        if (!h.facing(t, h.s->Y[ni]) || h.add_point(t, ni, MAXD) < 0) return false;
+        if (!h.facing(t, h.st.Y(ni)) || h.add_point(t, ni, MAXD) < 0) return false;
         h.free_tri(t);
         if (h.nq == 0 || h.npts >= 32) return false;
     }
-    double closest = MAXD;
+    R closest = MAXD;
     int last = -1;
     bool flip = false;
     guard = 0;
     do {
         int t = h.pop();
         if (t < 0) return false;
-        if (h.s->tri[t].flags & 4) {
+        if (h.flags(t) & TF_REMOVED) {
             h.free_tri(t);
             continue;
         }
-        if (h.s->tri[t].cls >= closest) break;
+        if (h.cls(t) >= closest) break;
         if (last >= 0) h.free_tri(last);
         last = t;
-        V<double> tn = h.s->tri[t].normal;
-        int ni = epa_add_sup(h, A, B, tn);
+        V<R> tn = h.st.normal(t);
+        int ni = h.add_sup(A, B, tn);
         if (ni < 0) break;
-        V<double> wv = h.s->Y[ni];
-        double d = dot(tn, wv);
+        V<R> wv = h.st.Y(ni);
+        R d = dot(tn, wv);
         if (d < 0.0) return false;
-        double dsq = (d * d) / lsq(tn);
-        if (dsq - h.s->tri[t].cls < h.s->tri[t].cls * tol) break;
+        R dsq = (d * d) / lsq(tn);
+        if (dsq - h.cls(t) < h.cls(t) * tol) break;
         closest = closest < dsq ? closest : dsq;
         if (!h.facing(t, wv)) break;
         int ne = h.add_point(t, ni, closest);
         if (ne < 0) break;
         bool defect = false;
         for (int k = 0; k < ne; k++) {
-            const EpaTri &q = h.s->tri[h.s->newt[k]];
-            if (dot(q.normal, q.centroid) < 0.0) {
+            int q = h.st.newt(k);
+            if (dot(h.st.normal(q), h.st.centroid(q)) < 0.0) {
                 defect = true;
                 break;
             }
         }
         if (defect) {
-            V<double> nn = -tn;
-            V<double> w2 = A.get(nn) - B.get(tn);
+            V<R> nn = -tn;
+            V<R> w2 = A.get(nn) - B.get(tn);
             if (dot(nn, w2) < d) flip = true;
             break;
         }
     } while (h.nq > 0 && h.npts < 128 && guard++ < 4096);
+    if (h.overflow) return false;
     if (last < 0) return false;
-    const EpaTri &L = h.s->tri[last];
-    double nls = lsq(L.normal);
-    V<double> pn = L.normal * (dot(L.centroid, L.normal) / nls);
-    if (lsq(pn) < 1e-10) return false;
+    V<R> ln = h.st.normal(last);
+    R nls = lsq(ln);
+    V<R> pn = ln * (dot(h.st.centroid(last), ln) / nls);
+    if (lsq(pn) < R_MIN_NORMAL_SQ) return false;
     if (flip) pn = -pn;
-    V<double> xp0 = h.s->P[L.st[0]], xp1 = h.s->P[L.st[1]], xp2 = h.s->P[L.st[2]];
-    V<double> xq0 = h.s->Qp[L.st[0]], xq1 = h.s->Qp[L.st[1]], xq2 = h.s->Qp[L.st[2]];
-    if (L.flags & 1) {
-        outPa = xp0 + (xp1 - xp0) * L.l0 + (xp2 - xp0) * L.l1;
-        outPb = xq0 + (xq1 - xq0) * L.l0 + (xq2 - xq0) * L.l1;
+    R l0, l1;
+    bool rel0;
+    h.lambdas(last, l0, l1, rel0);
+    int s0 = h.st.st(last, 0), s1 = h.st.st(last, 1), s2 = h.st.st(last, 2);
+    V<R> xp0 = h.st.P(s0), xp1 = h.st.P(s1), xp2 = h.st.P(s2);
+    V<R> xq0 = h.st.Q(s0), xq1 = h.st.Q(s1), xq2 = h.st.Q(s2);
+    if (rel0) {
+        outPa = xp0 + (xp1 - xp0) * l0 + (xp2 - xp0) * l1;
+        outPb = xq0 + (xq1 - xq0) * l0 + (xq2 - xq0) * l1;
     } else {
-        outPa = xp1 + (xp0 - xp1) * L.l0 + (xp2 - xp1) * L.l1;
-        outPb = xq1 + (xq0 - xq1) * L.l0 + (xq2 - xq1) * L.l1;
+        outPa = xp1 + (xp0 - xp1) * l0 + (xp2 - xp1) * l1;
+        outPb = xq1 + (xq0 - xq1) * l0 + (xq2 - xq1) * l1;
     }
     outAxis = pn;
     return true;
 }
 
-// Runs the FP64 EPA stage for one queued pair with the given scratch slice.
-__device__ void epa_pair(DevWorld &w, const EpaItem &it, EpaScratch *scratch) {
+// Supports of one queued pair in A's local frame (convex.ts:440-452): EPA runs on the full
+// shapes with the speculative distance (at most 1) added to A as a radius.
+__device__ void epa_setup(const DevWorld &w, const EpaItem &it, Sup<R> &A, Sup<R> &B, R &maxSep) {
     int a = it.a, b = it.b;
     uint32_t fa = w.flags[a], fb = w.flags[b];
     float maxSepF = ((fa | fb) & F_SENSOR) ? 0.f : c_settings.spec_dist;
-    double maxSep = (double)maxSepF < 1.0 ? (double)maxSepF : 1.0;
+    maxSep = R(maxSepF < 1.f ? maxSepF : 1.f);
     float4 pa4 = w.pos[a], pb4 = w.pos[b], qa = w.quat[a], qb = w.quat[b];
-    Q<double> iA{-(double)qa.x, -(double)qa.y, -(double)qa.z, (double)qa.w};
-    Q<double> qB{qb.x, qb.y, qb.z, qb.w}, qA{qa.x, qa.y, qa.z, qa.w};
-    Q<double> rel = qmulS(iA, qB);
-    V<double> ab{(double)pb4.x - (double)pa4.x, (double)pb4.y - (double)pa4.y, (double)pb4.z - (double)pa4.z};
-    V<double> posBInA = qrotS(iA, ab);
-    Sup<double> A = make_sup<double>(shape_of(fa), w.shape[a], false);
-    Sup<double> B = make_sup<double>(shape_of(fb), w.shape[b], false);
+    Q<R> iA{R(-qa.x), R(-qa.y), R(-qa.z), R(qa.w)};
+    Q<R> qB{R(qb.x), R(qb.y), R(qb.z), R(qb.w)};
+    Q<R> rel = qmulS(iA, qB);
+    V<R> ab{R(pb4.x) - R(pa4.x), R(pb4.y) - R(pa4.y), R(pb4.z) - R(pa4.z)};
+    V<R> posBInA = qrotS(iA, ab);
+    A = make_sup<R>(shape_of(fa), w.shape[a], false);
+    B = make_sup<R>(shape_of(fb), w.shape[b], false);
     A.add_r = maxSep;
     set_transform(B, rel, posBInA);
-    EpaHull h;
-    h.s = scratch;
-    h.npts = it.size;
-    for (int k = 0; k < it.size; k++) {
-        scratch->Y[k] = {it.y[k].x, it.y[k].y, it.y[k].z};
-        scratch->P[k] = {it.p[k].x, it.p[k].y, it.p[k].z};
-        scratch->Qp[k] = {it.q[k].x, it.q[k].y, it.q[k].z};
-    }
-    V<double> axis, pa, pb;
-    if (!epa(h, A, B, (double)c_settings.penetration_tol, axis, pa, pb)) return;
-    V<double> dd = pa - pb;
-    double penetration = sqrt(lsq(dd)) - maxSep;
-    double al = sqrt(lsq(axis));
-    if (al > 0.0) pa = pa + axis * (-(maxSep / al));
-    V<double> paw = qrotS(qA, pa), pbw = qrotS(qA, pb), axw = qrotS(qA, axis);
-    emit_manifold(w, a, b, f3((float)paw.x, (float)paw.y, (float)paw.z), f3((float)pbw.x, (float)pbw.y, (float)pbw.z),
-                  f3((float)axw.x, (float)axw.y, (float)axw.z), (float)penetration, true);
 }
 
-__global__ void __launch_bounds__(64) k_epa(DevWorld w, const EpaItem *items, EpaScratch *scratch) {
+// The hit of one item (penetrationDepthStepEPA :502-548) written back into the item for
+// k_epa_emit: size = 1 with pa in y[0], pb in p[0], axis in q[0] and the depth in pad
+// (all in world orientation, relative to A's position), or size = 0 for no contact.
+__device__ void epa_finish(const DevWorld &w, EpaItem &it, bool ok, R maxSep, V<R> axis, V<R> pa,
+                           V<R> pb) {
+    if (!ok) {
+        it.size = 0;
+        return;
+    }
+    float4 qa = w.quat[it.a];
+    Q<R> qA{R(qa.x), R(qa.y), R(qa.z), R(qa.w)};
+    V<R> dd = pa - pb;
+    R penetration = sq_root(lsq(dd)) - maxSep;
+    R al = sq_root(lsq(axis));
+    if (al > 0.0) pa = pa + axis * (-(maxSep / al));
+    V<R> paw = qrotS(qA, pa), pbw = qrotS(qA, pb), axw = qrotS(qA, axis);
+    it.size = 1;
+    it.y[0] = f3((float)(paw.x), (float)(paw.y), (float)(paw.z));
+    it.p[0] = f3((float)(pbw.x), (float)(pbw.y), (float)(pbw.z));
+    it.q[0] = f3((float)(axw.x), (float)(axw.y), (float)(axw.z));
+    it.pad = __float_as_int((float)(penetration));
+}
+
+// Packed pass.  fetch_warp = 1: a warp takes 32 consecutive items at a time and its lanes
+// start them together, which keeps the lanes in the same phase of the algorithm (on GB300
+// an FP64 warp instruction costs the same whatever the number of active lanes);
+// fetch_warp = 0: each thread takes its next item as soon as it finishes one.  Items that
+// outgrow the packed limits go to the fallback list.
+__device__ __forceinline__ void epa_packed_item(DevWorld &w, EpaItem *items, int i, Hull<PackedStore> &h,
+                                                int *fallback, int pts_limit) {
+    EpaItem &it = items[i];
+    Sup<R> A, B;
+    R maxSep;
+    epa_setup(w, it, A, B, maxSep);
+    h.start(it, pts_limit);
+    V<R> axis, pa, pb;
+    bool ok = epa(h, A, B, R(c_settings.penetration_tol), axis, pa, pb);
+    if (h.overflow) {
+        fallback[atomicAdd(&w.ctr->epa_fallback, 1)] = i;
+        return;
+    }
+    epa_finish(w, it, ok, maxSep, axis, pa, pb);
+}
+
+__global__ void __launch_bounds__(EPA_BLOCK) k_epa(DevWorld w, EpaItem *items, PackedBlock *blocks,
+                                                   int *fallback, int pts_limit, int fetch_warp) {
     int ne = min(w.ctr->num_epa, w.max_epa);
+    Hull<PackedStore> h;
+    h.st.b = blocks + blockIdx.x;
+    h.st.j = threadIdx.x;
+    if (fetch_warp) {
+        const int lane = threadIdx.x & 31;
+        while (true) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&w.ctr->epa_cursor, 32);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= ne) break;
+            if (base + lane < ne) epa_packed_item(w, items, base + lane, h, fallback, pts_limit);
+            __syncwarp();
+        }
+    } else {
+        for (int i = atomicAdd(&w.ctr->epa_cursor, 1); i < ne; i = atomicAdd(&w.ctr->epa_cursor, 1))
+            epa_packed_item(w, items, i, h, fallback, pts_limit);
+    }
+}
+
+// Fallback pass with the reference's limits, for the items the packed pass handed over.
+__global__ void __launch_bounds__(EPA_BLOCK) k_epa_big(DevWorld w, EpaItem *items, EpaScratch *scratch,
+                                                       const int *fallback) {
+    int nf = w.ctr->epa_fallback;
     int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    EpaScratch *mine = scratch + tid;
-    for (int i = tid; i < ne; i += gridDim.x * blockDim.x) epa_pair(w, items[i], mine);
+    Hull<BigStore> h;
+    h.st.s = scratch + tid;
+    for (int k = tid; k < nf; k += gridDim.x * blockDim.x) {
+        EpaItem &it = items[fallback[k]];
+        Sup<R> A, B;
+        R maxSep;
+        epa_setup(w, it, A, B, maxSep);
+        h.start(it);
+        V<R> axis, pa, pb;
+        bool ok = epa(h, A, B, R(c_settings.penetration_tol), axis, pa, pb);
+        epa_finish(w, it, ok, maxSep, axis, pa, pb);
+    }
+}
+
+// Manifolds of the EPA hits (faces, clipping, reduction in FP32), one item per thread.
+__global__ void __launch_bounds__(128) k_epa_emit(DevWorld w, const EpaItem *items) {
+    int ne = min(w.ctr->num_epa, w.max_epa);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ne; i += gridDim.x * blockDim.x) {
+        const EpaItem &it = items[i];
+        if (it.size != 1) continue;
+        emit_manifold(w, it.a, it.b, it.y[0], it.p[0], it.q[0], __int_as_float(it.pad), true);
+    }
 }
 
 size_t epa_item_bytes() { return sizeof(EpaItem); }
@@ -1328,7 +1624,11 @@ void launch_narrowphase(DevWorld &w, float, cudaStream_t s, cudaEvent_t mid) {
     EpaItem *items = (EpaItem *)w.epa_items;
     k_narrowphase<<<NUM_SMS * 8, 128, 0, s>>>(w, items);
     if (mid) cudaEventRecord(mid, s);
-    k_epa<<<w.epa_threads / 64, 64, 0, s>>>(w, items, (EpaScratch *)w.epa_scratch);
+    k_epa<<<w.epa_threads / EPA_BLOCK, EPA_BLOCK, 0, s>>>(w, items, (PackedBlock *)w.epa_packed, w.epa_fallback,
+                                                          w.epa_packed_points, w.epa_fetch_warp);
+    k_epa_big<<<EPA_BIG_THREADS / EPA_BLOCK, EPA_BLOCK, 0, s>>>(w, items, (EpaScratch *)w.epa_scratch,
+                                                                w.epa_fallback);
+    k_epa_emit<<<NUM_SMS * 8, 128, 0, s>>>(w, items);
 }
 
 // ---------------------------------------------------------------------------
@@ -1468,35 +1768,30 @@ __global__ void __launch_bounds__(64) k_static_epa(const cc_penetration_query *q
         float4 pa4, pb4, qa, qb, sa, sb;
         pose_of(qy.a, pa4, qa, sa);
         pose_of(qy.b, pb4, qb, sb);
-        double maxSep = (double)qy.max_separation < 1.0 ? (double)qy.max_separation : 1.0;
-        Q<double> iA{-(double)qa.x, -(double)qa.y, -(double)qa.z, (double)qa.w};
-        Q<double> qB{qb.x, qb.y, qb.z, qb.w}, qA{qa.x, qa.y, qa.z, qa.w};
-        Q<double> rel = qmulS(iA, qB);
-        V<double> ab{(double)pb4.x - (double)pa4.x, (double)pb4.y - (double)pa4.y, (double)pb4.z - (double)pa4.z};
-        V<double> posBInA = qrotS(iA, ab);
-        Sup<double> A = make_sup<double>(qy.a.shape_type, sa, false);
-        Sup<double> B = make_sup<double>(qy.b.shape_type, sb, false);
+        R maxSep = R(qy.max_separation < 1.f ? qy.max_separation : 1.f);
+        Q<R> iA{R(-qa.x), R(-qa.y), R(-qa.z), R(qa.w)};
+        Q<R> qB{R(qb.x), R(qb.y), R(qb.z), R(qb.w)}, qA{R(qa.x), R(qa.y), R(qa.z), R(qa.w)};
+        Q<R> rel = qmulS(iA, qB);
+        V<R> ab{R(pb4.x) - R(pa4.x), R(pb4.y) - R(pa4.y), R(pb4.z) - R(pa4.z)};
+        V<R> posBInA = qrotS(iA, ab);
+        Sup<R> A = make_sup<R>(qy.a.shape_type, sa, false);
+        Sup<R> B = make_sup<R>(qy.b.shape_type, sb, false);
         A.add_r = maxSep;
         set_transform(B, rel, posBInA);
-        EpaHull h;
-        h.s = mine;
-        h.npts = it.size;
-        for (int k = 0; k < it.size; k++) {
-            mine->Y[k] = {it.y[k].x, it.y[k].y, it.y[k].z};
-            mine->P[k] = {it.p[k].x, it.p[k].y, it.p[k].z};
-            mine->Qp[k] = {it.q[k].x, it.q[k].y, it.q[k].z};
-        }
-        V<double> axis, pa, pb;
-        if (!epa(h, A, B, (double)penetration_tol, axis, pa, pb)) continue;  // no contact (convex.ts:331)
-        V<double> dd = pa - pb;
-        double penetration = sqrt(lsq(dd)) - maxSep;
-        double al = sqrt(lsq(axis));
-        if (al > 0.0) pa = pa + axis * (-(maxSep / al));
-        V<double> paw = qrotS(qA, pa), pbw = qrotS(qA, pb), axw = qrotS(qA, axis);
+        Hull<BigStore> h;
+        h.st.s = mine;
+        h.start(it);
+        V<R> axis, pa, pb;
+        if (!epa(h, A, B, R(penetration_tol), axis, pa, pb)) continue;  // no contact (convex.ts:331)
+        V<R> dd = pa - pb;
+        R penetration = sq_root(lsq(dd)) - maxSep;
+        R al = sq_root(lsq(axis));
+        if (al > R(0)) pa = pa + axis * (-(maxSep / al));
+        V<R> paw = qrotS(qA, pa), pbw = qrotS(qA, pb), axw = qrotS(qA, axis);
         cc_penetration_result r;
-        write_hit(r, xyz(pa4), f3((float)paw.x, (float)paw.y, (float)paw.z),
-                  f3((float)pbw.x, (float)pbw.y, (float)pbw.z), f3((float)axw.x, (float)axw.y, (float)axw.z),
-                  (float)penetration, 1);
+        write_hit(r, xyz(pa4), f3((float)(paw.x), (float)(paw.y), (float)(paw.z)),
+                  f3((float)(pbw.x), (float)(pbw.y), (float)(pbw.z)),
+                  f3((float)(axw.x), (float)(axw.y), (float)(axw.z)), (float)(penetration), 1);
         res[it.a] = r;
     }
 }

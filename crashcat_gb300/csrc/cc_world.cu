@@ -253,10 +253,23 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
             return r;
         }
         w.epa_items = p;
-        // EPA threads scale with the world: about one per 8 bodies, 1,024 to EPA_MAX_THREADS
+        // EPA threads scale with the world: about one per 8 bodies, 1,024 to EPA_DEFAULT_MAX_THREADS
         int et = cap / 8;
-        et = et < 1024 ? 1024 : (et > EPA_MAX_THREADS ? EPA_MAX_THREADS : et);
+        et = et < 1024 ? 1024 : (et > EPA_DEFAULT_MAX_THREADS ? EPA_DEFAULT_MAX_THREADS : et);
+        if (const char *e = getenv("CRASHCAT_EPA_THREADS")) {
+            int v = atoi(e);
+            if (v >= 64 && v <= EPA_MAX_THREADS) et = v;
+        }
         w.epa_threads = (et + 63) / 64 * 64;
+        // launch-shape tunable: the packed polytope's point limit (4 to 32); items that need
+        // more support points are re-run by the pass with the reference's limits
+        w.epa_packed_points = 32;
+        w.epa_fetch_warp = 1;
+        if (const char *e = getenv("CRASHCAT_EPA_FETCH_WARP")) w.epa_fetch_warp = atoi(e) != 0;
+        if (const char *e = getenv("CRASHCAT_EPA_PACKED_POINTS")) {
+            int v = atoi(e);
+            if (v >= 4 && v <= 32) w.epa_packed_points = v;
+        }
         w.warp_blocks_per_sm = 4;
         w.warp_carveout = 50;
         if (const char *e = getenv("CRASHCAT_WARP_BLOCKS_PER_SM")) {
@@ -268,12 +281,19 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
             if (v >= 0 && v <= 100) w.warp_carveout = v;
         }
         char *q = nullptr;
-        if ((r = dalloc(&q, epa_scratch_bytes() * (size_t)w.epa_threads)) != CC_OK) {
+        if ((r = dalloc(&q, epa_packed_block_bytes() * (size_t)(w.epa_threads / 64))) != CC_OK) {
             cc_world_destroy(W);
             return r;
         }
-        w.epa_scratch = q;
+        w.epa_packed = q;
+        char *g = nullptr;
+        if ((r = dalloc(&g, epa_scratch_bytes() * (size_t)EPA_BIG_THREADS)) != CC_OK) {
+            cc_world_destroy(W);
+            return r;
+        }
+        w.epa_scratch = g;
     }
+    ALLOC(epa_fallback, w.max_epa);
     for (int k = 0; k < 2; k++) {
         ALLOC(cache_keys[k], w.cache_cap);
         ALLOC(cache_recs[k], w.cache_cap);
@@ -322,7 +342,7 @@ int cc_world_destroy(cc_world *W) {
                     w.cons_of_manifold, w.uf_parent, w.island_of_body, w.island_id_of_root, w.island_body_count,
                     w.island_cons_count, w.island_body_off, w.island_cons_off, w.island_bodies, w.island_cons,
                     w.island_fill_b, w.island_fill_c, w.inv_inertia_world, w.scan_tmp, w.ctr, w.scene,
-                    w.node_world, w.epa_items, w.epa_scratch, w.cache_keys[0], w.cache_keys[1], w.cache_recs[0],
+                    w.node_world, w.epa_items, w.epa_packed, w.epa_scratch, w.epa_fallback, w.cache_keys[0], w.cache_keys[1], w.cache_recs[0],
                     w.cache_recs[1], w.cache_parity, w.root_flag, w.small_list, w.large_list, w.scratch_order,
                     w.scratch_colour, w.scratch_claim, w.mid_list, w.body_local, W->d_state_rows};
     for (void *p : ptrs)

@@ -265,3 +265,26 @@ def test_warp_island_matches_sequential_order(gpu_lib, base, monkeypatch):
     r_warp, _ = g_warp.get_state()
     r_seq, _ = g_seq.get_state()
     np.testing.assert_allclose(r_warp, r_seq, atol=1e-6)
+
+
+def test_epa_fallback_pass_matches_packed_pass(gpu_lib, monkeypatch):
+    """EPA items whose polytope outgrows the packed pass's point limit are re-run with
+    the reference's limits.  Forcing most items over a limit of 5 points gives the same
+    contacts as the packed pass (both run the same FP64 hull code)."""
+    sc = scenes.random_pairs_scene(n=300, seed=7)
+    ws = world.standard_settings()
+
+    def contacts():
+        g = world.GpuWorld(ws, sc.n + 16)
+        g.add_bodies(sc.bodies)
+        g.step(0.0, 1)
+        return g.stats()["num_epa"], {(int(r[0]), int(r[1])): r for r in g.get_manifolds()}
+
+    n_epa, packed = contacts()
+    monkeypatch.setenv("CRASHCAT_EPA_PACKED_POINTS", "5")
+    _, fallback = contacts()
+    assert n_epa > 20
+    assert set(packed) == set(fallback)
+    for k in packed:
+        np.testing.assert_allclose(packed[k][:7], fallback[k][:7], atol=1e-5)
+        np.testing.assert_allclose(packed[k][8:], fallback[k][8:], atol=1e-4)
