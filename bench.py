@@ -14,6 +14,13 @@ read back into pinned host memory every step; roofline of the dominant stage
 from the stage profiler; cpu_baseline = the FP64 oracle port timed single
 threaded on a bounded sample of the same worlds.
 
+vs_single_world: the same settled worlds stepped through the plain single-world
+path (one cc_world handle per world, cc_world_step(handle, dt, 1) world after
+world, as a caller without the batched form would) on a spread sample of the
+4,096 worlds; both paths run the same kernels and settings, so the tolerance is
+the same.  value = sampled bodies x steps / wall time of the sampled worlds'
+steps; batched_over_single = the batched value / that value.
+
 --impl reference: the reference (TypeScript) cannot run on this machine; its FP64
 C++ restatement (oracle/) steps a bounded sample of the same worlds on all
 host cores (one process per core, worlds split across them).
@@ -284,6 +291,42 @@ def run_reference(args, rank, world_size):
 # ---------------------------------------------------------------------------
 # GPU leg
 # ---------------------------------------------------------------------------
+def single_world_comparison(scene, ws_batched, settled_rows, dt, steps: int, sample_worlds: int = 48):
+    """Steps a spread sample of the workload's worlds through the plain single-world path:
+    one handle per world, each stepped once per step with cc_world_step (which blocks until
+    the step ends), world after world.  Starts from the batched run's settled state."""
+    import copy
+    import torch
+    from crashcat_gb300 import world as W
+    worlds = split_worlds(scene)
+    offs = np.cumsum([0] + [len(b) for b in worlds])
+    pick = np.unique(np.linspace(0, len(worlds) - 1, sample_worlds).astype(int))
+    handles, nb = [], 0
+    for k in pick:
+        b = worlds[k].copy()
+        r = settled_rows[offs[k]:offs[k + 1]]
+        b["position"], b["quaternion"] = r[:, 0:3], r[:, 3:7]
+        b["linear_velocity"], b["angular_velocity"] = r[:, 7:10], r[:, 10:13]
+        b["world"] = 0
+        ws = copy.deepcopy(ws_batched)
+        ws.num_worlds = 1
+        g = W.GpuWorld(ws, len(b) + 8)
+        g.add_bodies(b)
+        g.step(dt, 2)  # first step (warm-start ratio 0) and the graph capture
+        handles.append(g)
+        nb += len(b)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for g in handles:
+            g.step(dt, 1)
+    t = time.perf_counter() - t0
+    del handles
+    return {"value": nb * steps / t, "unit": METRIC, "worlds_sampled": int(len(pick)), "bodies_sampled": int(nb),
+            "steps": steps, "ms_per_world_step": t * 1e3 / (steps * len(pick)),
+            "api": "cc_world_step(handle, dt, 1) per world, one handle per world"}
+
+
 def run_gpu(args, rank, world_size, local):
     import torch
     torch.cuda.set_device(local)
@@ -367,6 +410,9 @@ def run_gpu(args, rank, world_size, local):
         except Exception:
             traffic = None
 
+    single = single_world_comparison(scene, ws, settled_rows, dt, steps=max(3, min(args.steps, 10)))
+    single["batched_over_single"] = value / world_size / single["value"]
+
     if rank == 0:
         cpu = cpu_baseline_single(scene, args.cpu_seconds, settled_rows)
         line = {
@@ -386,6 +432,7 @@ def run_gpu(args, rank, world_size, local):
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                          "algorithmic_bytes_per_launch": bytes_dom, "stage_ms": prof},
             "cpu_baseline": cpu,
+            "vs_single_world": single,
             "clocks": clk.summary(),
             "gpu_launches": stats["gpu_launches_per_step"] * args.steps,
             "counters": {k: stats_w[k] for k in ("num_awake", "num_pairs", "num_manifolds", "num_contact_points",
