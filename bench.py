@@ -21,6 +21,13 @@ world, as a caller without the batched form would) on a spread sample of the
 the same.  value = sampled bodies x steps / wall time of the sampled worlds'
 steps; batched_over_single = the batched value / that value.
 
+adjoint: the differentiable-rollout workload (1,024 worlds x 64 boxes, 120 steps at
+dt 1/60, checkpoint every 10 steps).  forward_ms_per_step = the plain rollout (graph-
+replayed steps, CUDA events); ms_per_step = cc_world_rollout_grad (forward with
+checkpoints, recomputation with tapes, reverse sweep, gradients to the host) / 120;
+fd_check = central finite differences (h = 1e-3) of the full step along seeded
+directions against the adjoint, on the first 8 worlds.
+
 --impl reference: the reference (TypeScript) cannot run on this machine; its FP64
 C++ restatement (oracle/) steps a bounded sample of the same worlds on all
 host cores (one process per core, worlds split across them).
@@ -59,6 +66,7 @@ def parse():
     ap.add_argument("--worlds", type=int, default=4096)
     ap.add_argument("--seed", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--adjoint", type=int, default=1, help="measure the rollout adjoint (1) or skip it (0)")
     ap.add_argument("--settle", type=int, default=360,
                     help="untimed steps before the warm-up so the timed steps are contact-rich")
     return ap.parse_args()
@@ -291,6 +299,74 @@ def run_reference(args, rank, world_size):
 # ---------------------------------------------------------------------------
 # GPU leg
 # ---------------------------------------------------------------------------
+def adjoint_measurement(num_worlds: int = 1024, steps: int = 120, checkpoint_every: int = 10):
+    """Adjoint ms/step of the differentiable-rollout workload against its forward ms/step."""
+    import copy
+    from crashcat_gb300 import scenes, world as W
+    sc, targets = scenes.diff_rollout_worlds(num_worlds=num_worlds)
+
+    def make(bodies, nw):
+        ws = W.standard_settings(velocity_iterations=sc.velocity_iterations,
+                                 position_iterations=sc.position_iterations, allow_sleeping=False)
+        ws.num_worlds = nw
+        g = W.GpuWorld(ws, len(bodies) + 8)
+        g.add_bodies(bodies)
+        return g
+
+    gf = make(sc.bodies, num_worlds)
+    gf.step(sc.dt, 1)
+    gf.step(sc.dt, steps - 1)
+    fwd_ms = gf.stats()["last_call_ms"] / (steps - 1)
+    del gf
+    ga = make(sc.bodies, num_worlds)
+    loss, gv, gw, gm = ga.rollout_grad(sc.dt, steps, targets, checkpoint_every=checkpoint_every)
+    adj_ms = ga.stats()["last_call_ms"] / steps
+    del ga
+    # finite differences on the first 8 worlds
+    nw = 8
+    sub = sc.bodies[sc.bodies["world"] < nw].copy()
+    tg = targets[:nw]
+
+    def host_loss(b):
+        g = make(b, nw)
+        g.step(sc.dt, steps)
+        rows, _ = g.get_state()
+        tot = 0.0
+        for k in range(nw):
+            m = (b["world"] == k) & (b["motion_type"] == 2)
+            tot += float(((rows[m, 0:3].astype(np.float64).mean(0) - tg[k]) ** 2).sum())
+        return tot
+
+    g8 = make(sub, nw)
+    _, gv8, gw8, gm8 = g8.rollout_grad(sc.dt, steps, tg, checkpoint_every=checkpoint_every)
+    rng = np.random.default_rng(5)
+    dyn = (sub["motion_type"] == 2)[:, None]
+    checks, h = [], 1e-3
+    for k in range(3):
+        dv = rng.normal(size=(len(sub), 3)) * dyn
+        dw = rng.normal(size=(len(sub), 3)) * dyn * (k >= 1)
+        dm = rng.normal(size=len(sub)) * dyn[:, 0] * 0.2 * (k == 2)
+
+        def pert(sgn):
+            b = copy.deepcopy(sub)
+            b["linear_velocity"] = (b["linear_velocity"] + sgn * h * dv).astype(np.float32)
+            b["angular_velocity"] = (b["angular_velocity"] + sgn * h * dw).astype(np.float32)
+            b["friction"] = (b["friction"] + sgn * h * dm).astype(np.float32)
+            return b
+
+        fd = (host_loss(pert(1)) - host_loss(pert(-1))) / (2 * h)
+        ad = float((gv8 * dv).sum() + (gw8 * dw).sum() + (gm8 * dm).sum())
+        checks.append({"direction": ["v", "v+w", "v+w+friction"][k], "fd": fd, "adjoint": ad,
+                       "rel_err": abs(fd - ad) / max(abs(fd), 1e-12)})
+    return {"workload": "diff_rollout_worlds", "worlds": num_worlds, "bodies": int(sc.n), "steps": steps,
+            "checkpoint_every": checkpoint_every, "ms_per_step": adj_ms, "forward_ms_per_step": fwd_ms,
+            "adjoint_over_forward": adj_ms / fwd_ms, "loss": float(loss.sum()),
+            "grad_norms": {"linvel": float(np.linalg.norm(gv)), "angvel": float(np.linalg.norm(gw)),
+                           "friction": float(np.linalg.norm(gm))},
+            "fd_check": {"worlds": nw, "h": h, "directions": checks,
+                         "model": "adjoint over each step's fixed contact set; FD through the full step"}}
+
+
 def single_world_comparison(scene, ws_batched, settled_rows, dt, steps: int, sample_worlds: int = 48):
     """Steps a spread sample of the workload's worlds through the plain single-world path:
     one handle per world, each stepped once per step with cc_world_step (which blocks until
@@ -411,6 +487,7 @@ def run_gpu(args, rank, world_size, local):
             traffic = None
 
     single = single_world_comparison(scene, ws, settled_rows, dt, steps=max(3, min(args.steps, 10)))
+    adjoint = adjoint_measurement() if args.adjoint else None
     single["batched_over_single"] = value / world_size / single["value"]
 
     if rank == 0:
@@ -433,6 +510,7 @@ def run_gpu(args, rank, world_size, local):
                          "algorithmic_bytes_per_launch": bytes_dom, "stage_ms": prof},
             "cpu_baseline": cpu,
             "vs_single_world": single,
+            "adjoint": adjoint,
             "clocks": clk.summary(),
             "gpu_launches": stats["gpu_launches_per_step"] * args.steps,
             "counters": {k: stats_w[k] for k in ("num_awake", "num_pairs", "num_manifolds", "num_contact_points",

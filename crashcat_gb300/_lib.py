@@ -96,6 +96,8 @@ EXPORTS = {
     "cc_world_get_stats": ([C.c_void_p, C.POINTER(Stats)], C.c_int),
     "cc_world_debug_islands": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
     "cc_world_profile_steps": ([C.c_void_p, C.c_float, C.c_int32, C.c_void_p, C.c_int32], C.c_int),
+    "cc_world_rollout_grad": ([C.c_void_p, C.c_float, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                               C.c_void_p, C.c_void_p], C.c_int),
     "cc_penetration_static": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_float, C.c_float, C.c_void_p], C.c_int),
     "cc_status_string": ([C.c_int], C.c_char_p),
 }

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcrashcat_gpu.so")
-SOURCES = ["cc_scan.cu", "cc_broadphase.cu", "cc_narrowphase.cu", "cc_solver.cu", "cc_world.cu"]
+SOURCES = ["cc_scan.cu", "cc_broadphase.cu", "cc_narrowphase.cu", "cc_solver.cu", "cc_adjoint.cu", "cc_world.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

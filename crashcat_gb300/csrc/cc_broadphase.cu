@@ -28,6 +28,7 @@ void upload_settings(const DevSettings &s, double spec64, cudaStream_t st) {
     cudaMemcpyToSymbolAsync(c_spec_dist64, &spec64, sizeof(double), 0, cudaMemcpyHostToDevice, st);
     upload_settings_narrowphase(s, st);
     upload_settings_solver(s, st);
+    upload_settings_adjoint(s, st);
 }
 
 // ---------------------------------------------------------------------------

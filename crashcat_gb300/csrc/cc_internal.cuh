@@ -121,6 +121,8 @@ struct ContactConstraint {
     ContactPoint p[4];
 };
 
+constexpr unsigned long long EMPTY_KEY = 0xffffffffffffffffull;  // free slot of the contact cache tables
+
 // Contact cache record (contacts.ts:9-81): persistent across steps.
 struct CacheRecord {
     unsigned long long key;  // (idxA << 32) | idxB, both ordered by id
@@ -129,6 +131,44 @@ struct CacheRecord {
     float3 p1[4];
     float3 p2[4];
     float ln[4], lt1[4], lt2[4];
+};
+
+// Adjoint rollout (cc_adjoint.cu): one step's tape, taken between the contact setup and the
+// solver, indexed like the world's per-step arrays.
+struct TapeStep {
+    ContactConstraint *cons;  // constraint rows by manifold index
+    int *valid;               // constraint index of each manifold (-1: no constraint)
+    float4 *v, *w, *q;        // velocities after force integration, orientation before the solve
+    uint32_t *flags;
+    int *isl_off, *isl_cnt;   // per island: first entry in isl_cons, contact count
+    int *isl_cons;
+    int *counts;              // [manifolds, islands]
+};
+// State a rollout resumes from: body state and the contact cache table the next step reads.
+struct Checkpoint {
+    float4 *pos, *quat, *com, *linvel, *angvel, *force, *torque, *sleep_sph;
+    float *sleep_timer;
+    uint32_t *flags;
+    unsigned long long *keys;
+    CacheRecord *recs;
+    int *parity;
+};
+struct AdjBuffers {
+    float4 *vbar, *wbar;    // adjoints of the linear / angular velocity
+    float4 *xbar;           // dL/dx of each body
+    float4 *vwork, *wwork;  // replayed velocities
+    float4 *iw;             // world inverse inertia (2 per body) of the step being reversed
+    float *u_tape;          // pre-projection value of every row update: iterations x manifolds x 12
+    float *lam_bar;         // adjoint of every row's impulse: manifolds x 12
+    float *mu_con;          // dL/d(combined friction) per constraint
+    float *mu_body;         // dL/d(friction) per body
+    float dt;
+};
+
+// impulse adjoints handed from one step's reverse to the previous step's, keyed by body pair
+struct AdjHandoff {
+    unsigned long long *keys;  // cache_cap entries, EMPTY_KEY when free
+    float *vals;               // 12 per entry: 4 points x (t1, t2, n)
 };
 
 struct DevWorld {
@@ -318,6 +358,14 @@ void launch_update_bounds(DevWorld &w, cudaStream_t s);
 void upload_settings(const DevSettings &s, double spec64, cudaStream_t st);
 void launch_cache_begin(DevWorld &w, cudaStream_t s);
 size_t epa_scratch_bytes();
+void upload_settings_adjoint(const DevSettings &s, cudaStream_t st);
+void launch_tape_record(DevWorld &w, TapeStep &t, cudaStream_t s);
+void checkpoint_save(const DevWorld &w, Checkpoint &c, cudaStream_t s);
+void checkpoint_restore(DevWorld &w, const Checkpoint &c, cudaStream_t s);
+void launch_rollout_loss(const DevWorld &w, const float *targets, float4 *sums, float *loss, AdjBuffers &a,
+                         cudaStream_t s);
+void launch_adjoint_step(DevWorld &w, TapeStep &t, AdjBuffers &a, float dt, float ratio, const AdjHandoff &in,
+                         const AdjHandoff &out, cudaStream_t s);
 size_t epa_packed_block_bytes();
 size_t epa_item_bytes();
 constexpr int EPA_DEFAULT_MAX_THREADS = NUM_SMS * 4 * 64;  // one EPA polytope per resident EPA thread

@@ -28,7 +28,6 @@ void upload_settings_solver(const DevSettings &s, cudaStream_t st) {
     cudaMemcpyToSymbolAsync(c_settings, &s, sizeof(DevSettings), 0, cudaMemcpyHostToDevice, st);
 }
 
-constexpr unsigned long long EMPTY_KEY = 0xffffffffffffffffull;
 constexpr int SMALL_ISLAND_MAX_CONS = 64;  // upper bound of the per-thread class (register arrays)
 constexpr int SMALL_ISLAND_MAX_BODIES = 64;
 // islands above the per-thread class and within these limits run on one warp
@@ -203,7 +202,8 @@ __global__ void k_contact_setup(DevWorld w, CacheTables ct, float dt) {
         c.invMassB = ib.w;
         c.sort_key = contact_sort_key(A, B, 0xffffffffu, 0xffffffffu);
         c.cache_slot = slot;
-        c.pad0 = c.pad1 = 0;
+        c.pad0 = prev;  // record of the previous step's table this contact was matched with (-1: none)
+        c.pad1 = 0;
         bool dynA = ma == DYNAMIC, dynB = mb == DYNAMIC;
         Sym3 IA{0, 0, 0, 0, 0, 0}, IB{0, 0, 0, 0, 0, 0};
         if (dynA) IA = world_inv_inertia(qa, w.inertia_rot[A], xyz(ia), dof_of(fa));
@@ -218,6 +218,7 @@ __global__ void k_contact_setup(DevWorld w, CacheTables ct, float dt) {
             p.localA = mtmul(RA, pa - comA);
             p.localB = mtmul(RB, pb - comB);
             p.lam_n = p.lam_t1 = p.lam_t2 = 0.f;
+            int matched = -1;
             for (int j = 0; j < pn; j++) {
                 float3 d1 = p.localA - pr->p1[j], d2 = p.localB - pr->p2[j];
                 float th = c_settings.preserve_lambda_dsq;
@@ -225,6 +226,7 @@ __global__ void k_contact_setup(DevWorld w, CacheTables ct, float dt) {
                     p.lam_n = pr->ln[j];
                     p.lam_t1 = pr->lt1[j];
                     p.lam_t2 = pr->lt2[j];
+                    matched = j;
                     break;
                 }
             }
@@ -280,7 +282,7 @@ __global__ void k_contact_setup(DevWorld w, CacheTables ct, float dt) {
                 p.eff_t1 = p.eff_t2 = 0.f;
                 p.lam_t1 = p.lam_t2 = 0.f;
             }
-            p.pad = 0.f;
+            p.pad = __int_as_float(matched);  // cached point that warm-started this one (-1: none)
             rec.p1[k] = p.localA;
             rec.p2[k] = p.localB;
             rec.ln[k] = p.lam_n;

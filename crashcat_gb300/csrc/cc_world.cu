@@ -34,6 +34,19 @@ struct cc_world {
     DevCounters *h_ctr = nullptr;   // pinned mirror of the device counters
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr;  // bracket each cc_world_step call
     float last_call_ms = 0.f;
+    // rollout gradient (cc_world_rollout_grad): tapes of one segment, checkpoints, adjoint buffers
+    struct Adjoint {
+        int seg_len = 0, n_ckpt = 0;
+        std::vector<TapeStep> tapes;
+        std::vector<float> tape_ratio;
+        std::vector<Checkpoint> ckpts;  // one per segment, then the state after the rollout
+        std::vector<double> ckpt_prev_dt;
+        AdjBuffers buf{};
+        AdjHandoff hand[2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+        float4 *sums = nullptr;
+        float *d_targets = nullptr, *d_loss = nullptr;
+        std::vector<void *> allocs;
+    } adj;
 };
 
 static int cuda_ok(cudaError_t e) {
@@ -347,6 +360,8 @@ int cc_world_destroy(cc_world *W) {
                     w.scratch_colour, w.scratch_claim, w.mid_list, w.body_local, W->d_state_rows};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    for (void *p : W->adj.allocs)
+        if (p) cudaFree(p);
     if (W->h_ctr) cudaFreeHost(W->h_ctr);
     if (W->ev_begin) cudaEventDestroy(W->ev_begin);
     if (W->ev_end) cudaEventDestroy(W->ev_end);
@@ -496,7 +511,7 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
 // one step's launch sequence (update.ts:45-239); `ev` (optional, CC_PROFILE_STAGES + 1
 // events) brackets the stages for the stage profiler
 constexpr int CC_PROFILE_STAGES = 7;
-static void enqueue_step(cc_world *W, float dt, float ratio, cudaEvent_t *ev = nullptr) {
+static void enqueue_step(cc_world *W, float dt, float ratio, cudaEvent_t *ev = nullptr, TapeStep *tape = nullptr) {
     DevWorld &w = W->w;
     cudaStream_t s = W->stream;
     auto mark = [&](int k) {
@@ -512,6 +527,7 @@ static void enqueue_step(cc_world *W, float dt, float ratio, cudaEvent_t *ev = n
     launch_narrowphase(w, dt, s, ev ? ev[3] : nullptr);
     mark(4);
     launch_contacts_and_islands(w, dt, ratio, s);
+    if (tape) launch_tape_record(w, *tape, s);
     mark(5);
     if (dt > 0.f) launch_solver(w, dt, ratio, s, ev ? ev[6] : nullptr);
     if (ev && !(dt > 0.f)) mark(6);
@@ -809,3 +825,161 @@ int cc_world_get_stats(cc_world *W, cc_stats *o) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// rollout gradient
+// ---------------------------------------------------------------------------
+template <typename T>
+static int adj_alloc(cc_world *W, T **p, size_t count) {
+    int r = dalloc(p, count);
+    if (r == CC_OK) W->adj.allocs.push_back((void *)*p);
+    return r;
+}
+
+static int ensure_adjoint(cc_world *W, int seg_len, int n_ckpt) {
+    auto &A = W->adj;
+    if (A.seg_len >= seg_len && A.n_ckpt >= n_ckpt) return CC_OK;
+    for (void *p : A.allocs) cudaFree(p);
+    A = cc_world::Adjoint{};
+    DevWorld &w = W->w;
+    size_t cap = (size_t)w.cap, nm = (size_t)w.max_manifolds, cc = (size_t)w.cache_cap;
+    int r;
+#define AA(ptr, count)                                  \
+    if ((r = adj_alloc(W, &(ptr), (count))) != CC_OK) { \
+        return r;                                       \
+    }
+    A.tapes.resize(seg_len);
+    A.tape_ratio.assign(seg_len, 0.f);
+    for (auto &t : A.tapes) {
+        AA(t.cons, nm);
+        AA(t.valid, nm);
+        AA(t.v, cap);
+        AA(t.w, cap);
+        AA(t.q, cap);
+        AA(t.flags, cap);
+        AA(t.isl_off, cap);
+        AA(t.isl_cnt, cap);
+        AA(t.isl_cons, nm);
+        AA(t.counts, 2);
+    }
+    A.ckpts.resize(n_ckpt);
+    A.ckpt_prev_dt.assign(n_ckpt, 0.0);
+    for (auto &c : A.ckpts) {
+        AA(c.pos, cap);
+        AA(c.quat, cap);
+        AA(c.com, cap);
+        AA(c.linvel, cap);
+        AA(c.angvel, cap);
+        AA(c.force, cap);
+        AA(c.torque, cap);
+        AA(c.sleep_sph, 3 * cap);
+        AA(c.sleep_timer, cap);
+        AA(c.flags, cap);
+        AA(c.keys, cc);
+        AA(c.recs, cc);
+        AA(c.parity, 1);
+    }
+    AdjBuffers &b = A.buf;
+    AA(b.vbar, cap);
+    AA(b.wbar, cap);
+    AA(b.xbar, cap);
+    AA(b.vwork, cap);
+    AA(b.wwork, cap);
+    AA(b.iw, 2 * cap);
+    AA(b.u_tape, (size_t)W->settings.velocity_iterations * nm * 12);
+    AA(b.lam_bar, nm * 12);
+    AA(b.mu_con, nm);
+    AA(b.mu_body, cap);
+    for (int k = 0; k < 2; k++) {
+        AA(A.hand[k].keys, cc);
+        AA(A.hand[k].vals, cc * 12);
+    }
+    AA(A.sums, (size_t)w.num_worlds);
+    AA(A.d_targets, 3 * (size_t)w.num_worlds);
+    AA(A.d_loss, (size_t)w.num_worlds);
+#undef AA
+    A.seg_len = seg_len;
+    A.n_ckpt = n_ckpt;
+    return CC_OK;
+}
+
+static float warm_ratio(const cc_world *W, float dt) {
+    if (!(dt > 0.f)) return 0.f;
+    return (W->settings.warm_starting && W->prev_dt > 0) ? (float)(dt / W->prev_dt) : 0.f;
+}
+
+extern "C" int cc_world_rollout_grad(cc_world *W, float dt, int32_t n_steps, int32_t checkpoint_every,
+                                     const float *targets, float *loss, float *grad_linvel, float *grad_angvel,
+                                     float *grad_friction) {
+    if (!W || !targets || n_steps <= 0 || checkpoint_every <= 0 || !(dt > 0.f)) return CC_ERR_INVALID;
+    DevWorld &w = W->w;
+    if (w.n == 0) return CC_ERR_INVALID;
+    int K = checkpoint_every < n_steps ? checkpoint_every : n_steps;
+    int nseg = (n_steps + K - 1) / K;
+    int r = ensure_adjoint(W, K, nseg + 1);
+    if (r != CC_OK) return r;
+    auto &A = W->adj;
+    cudaStream_t s = W->stream;
+    upload_settings(W->dev_settings, W->settings.speculative_contact_distance, s);
+    if (!W->ev_begin) {
+        CC_TRY(cudaEventCreate(&W->ev_begin));
+        CC_TRY(cudaEventCreate(&W->ev_end));
+    }
+    CC_TRY(cudaEventRecord(W->ev_begin, s));
+    // forward with a checkpoint at the start of every segment
+    for (int t = 0; t < n_steps; t++) {
+        if (t % K == 0) {
+            checkpoint_save(w, A.ckpts[t / K], s);
+            A.ckpt_prev_dt[t / K] = W->prev_dt;
+        }
+        enqueue_step(W, dt, warm_ratio(W, dt));
+        W->prev_dt = dt;
+    }
+    checkpoint_save(w, A.ckpts[nseg], s);
+    A.ckpt_prev_dt[nseg] = W->prev_dt;
+    CC_TRY(cudaMemcpyAsync(A.d_targets, targets, sizeof(float) * 3 * w.num_worlds, cudaMemcpyHostToDevice, s));
+    launch_rollout_loss(w, A.d_targets, A.sums, A.d_loss, A.buf, s);
+    CC_TRY(cudaMemsetAsync(A.hand[0].keys, 0xff, sizeof(unsigned long long) * (size_t)w.cache_cap, s));
+    int in = 0;
+    // backward: recompute each segment with tapes, then reverse its steps
+    for (int seg = nseg - 1; seg >= 0; seg--) {
+        checkpoint_restore(w, A.ckpts[seg], s);
+        W->prev_dt = A.ckpt_prev_dt[seg];
+        int len = n_steps - seg * K < K ? n_steps - seg * K : K;
+        for (int j = 0; j < len; j++) {
+            A.tape_ratio[j] = warm_ratio(W, dt);
+            enqueue_step(W, dt, A.tape_ratio[j], nullptr, &A.tapes[j]);
+            W->prev_dt = dt;
+        }
+        for (int j = len - 1; j >= 0; j--) {
+            launch_adjoint_step(w, A.tapes[j], A.buf, dt, A.tape_ratio[j], A.hand[in], A.hand[in ^ 1], s);
+            in ^= 1;
+        }
+    }
+    // the world ends where the forward rollout ended
+    checkpoint_restore(w, A.ckpts[nseg], s);
+    W->prev_dt = A.ckpt_prev_dt[nseg];
+    W->steps_done += n_steps;
+    CC_TRY(cudaEventRecord(W->ev_end, s));
+    std::vector<float4> tmp((size_t)w.n);
+    if (loss) CC_TRY(cudaMemcpyAsync(loss, A.d_loss, sizeof(float) * w.num_worlds, cudaMemcpyDeviceToHost, s));
+    if (grad_friction)
+        CC_TRY(cudaMemcpyAsync(grad_friction, A.buf.mu_body, sizeof(float) * w.n, cudaMemcpyDeviceToHost, s));
+    for (int k = 0; k < 2; k++) {
+        float *out = k == 0 ? grad_linvel : grad_angvel;
+        if (!out) continue;
+        CC_TRY(cudaMemcpyAsync(tmp.data(), k == 0 ? A.buf.vbar : A.buf.wbar, sizeof(float4) * w.n,
+                               cudaMemcpyDeviceToHost, s));
+        CC_TRY(cudaStreamSynchronize(s));
+        for (int i = 0; i < w.n; i++) {
+            out[3 * i] = tmp[i].x;
+            out[3 * i + 1] = tmp[i].y;
+            out[3 * i + 2] = tmp[i].z;
+        }
+    }
+    CC_TRY(cudaStreamSynchronize(s));
+    CC_TRY(cudaGetLastError());
+    cudaEventElapsedTime(&W->last_call_ms, W->ev_begin, W->ev_end);
+    W->last_ctr = *W->h_ctr;
+    return CC_OK;
+}

@@ -271,3 +271,44 @@ def box_pyramid(base: int = 8, seed: int = 41, gap: float = -0.004) -> Scene:
     b["position"][idx] = pos.astype(np.float32)
     b["linear_velocity"][idx] = rng.normal(scale=0.3, size=(count, 3)).astype(np.float32)
     return Scene("box_pyramid", b, dt=1.0 / 60.0, steps=1, seed=seed)
+
+
+def diff_rollout_worlds(num_worlds: int = 1024, seed: int = 5, boxes: int = 64) -> tuple:
+    """Differentiable-rollout workload: num_worlds worlds of `boxes` boxes (half extents
+    0.25-0.5 m, density 500-2000 kg/m^3, friction 0.1-1.0 per body) resting on their own
+    floor on an 8-wide grid, with seeded initial linear (horizontal, up to 3 m/s per axis)
+    and angular (up to 1 rad/s per axis) velocities so that they slide, spin and collide;
+    120 steps at dt 1/60.  Returns (scene, targets): one seeded target point per world, within 2 m of
+    the world's initial centroid.  Sleeping is off for this workload (the settings the
+    caller builds pass allow_sleeping=False)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = blank_bodies(num_worlds * (boxes + 1))
+    targets = np.zeros((num_worlds, 3), dtype=np.float32)
+    side = 8
+    o = 0
+    for wi in range(num_worlds):
+        static_floor(b, o, half=(20.0, 0.5, 20.0), friction=0.5, world=wi)
+        o += 1
+        sl = slice(o, o + boxes)
+        b["world"][sl] = wi
+        he = rng.uniform(0.25, 0.5, size=(boxes, 3)).astype(np.float32)
+        for k in range(boxes):
+            set_box(b, o + k, he[k])
+        b["density"][sl] = rng.uniform(500.0, 2000.0, size=boxes).astype(np.float32)
+        layer = np.arange(boxes) // (side * side)
+        cell = np.arange(boxes) % (side * side)
+        pos = np.stack([(cell % side - (side - 1) / 2) * 1.6, he[:, 1] + layer * 1.1,
+                        (cell // side - (side - 1) / 2) * 1.6], 1)
+        b["position"][sl] = pos.astype(np.float32)
+        vel = np.zeros((boxes, 3))
+        vel[:, 0] = rng.uniform(-3.0, 3.0, size=boxes)
+        vel[:, 2] = rng.uniform(-3.0, 3.0, size=boxes)
+        b["linear_velocity"][sl] = vel.astype(np.float32)
+        b["angular_velocity"][sl] = rng.uniform(-1.0, 1.0, size=(boxes, 3)).astype(np.float32)
+        b["friction"][sl] = rng.uniform(0.1, 1.0, size=boxes).astype(np.float32)
+        b["allow_sleeping"][sl] = 0
+        targets[wi] = pos.mean(0) + np.array([rng.uniform(-2, 2), 0.0, rng.uniform(-2, 2)])
+        o += boxes
+    sc = Scene("diff_rollout_worlds", b, dt=1.0 / 60.0, steps=120, velocity_iterations=10, position_iterations=2,
+               num_worlds=num_worlds, seed=seed)
+    return sc, targets

@@ -314,6 +314,21 @@ class GpuWorld:
             check(st, "cc_world_profile_steps")
         return {k: float(out[i]) for i, k in enumerate(self.STAGES)}
 
+    def rollout_grad(self, dt: float, n_steps: int, targets: np.ndarray, checkpoint_every: int = 10):
+        """Loss and gradients of an n_steps rollout from the current state (cc_world_rollout_grad):
+        returns (loss per world, dL/d linear velocity [n, 3], dL/d angular velocity [n, 3],
+        dL/d friction [n]).  The world ends in the state after the rollout."""
+        n = self.n
+        targets = np.ascontiguousarray(targets, dtype=np.float32).reshape(-1, 3)
+        loss = np.zeros(len(targets), dtype=np.float32)
+        gv = np.zeros((n, 3), dtype=np.float32)
+        gw = np.zeros((n, 3), dtype=np.float32)
+        gm = np.zeros(n, dtype=np.float32)
+        _lib.check(self._lib.cc_world_rollout_grad(self.handle, C.c_float(dt), n_steps, checkpoint_every,
+                                                  _lib.ptr(targets), _lib.ptr(loss), _lib.ptr(gv), _lib.ptr(gw),
+                                                  _lib.ptr(gm)), "cc_world_rollout_grad")
+        return loss, gv, gw, gm
+
     def stats(self) -> dict:
         s = _lib.Stats()
         check(self._lib.cc_world_get_stats(self.handle, C.byref(s)), "cc_world_get_stats")

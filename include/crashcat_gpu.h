@@ -182,6 +182,26 @@ int cc_world_profile_steps(cc_world *world, float dt, int32_t n_steps, float *st
 int cc_world_debug_islands(cc_world *world, int32_t *island_of_body, int32_t *cons_rows, int32_t capacity,
                            int32_t *count);
 
+/* Gradient of a rollout.  No counterpart in the reference: a vector-Jacobian product of
+ * n_steps world steps from the current state, differentiating the velocity solve (warm start
+ * and PGS, src/constraints/contact-constraints.ts:906-1053) and the integration
+ * (src/update.ts:245-319, 896-976) of every step over that step's fixed contact set; the
+ * contact geometry and the position-solve corrections of each step are constants, and the
+ * warm start carries impulse adjoints from one step to the one before it through the contact
+ * cache match.
+ *   loss = sum over worlds w of |centroid_w - targets[w]|^2, the centroid taken over the
+ *          world's dynamic bodies after the last step (targets: num_worlds x 3 floats);
+ *   loss (num_worlds floats), grad_linvel / grad_angvel (n x 3 floats: dloss / d initial
+ *   linear / angular velocity of each body) and grad_friction (n floats: dloss / d friction
+ *   coefficient of each body) are written when not NULL.
+ * The forward pass keeps a checkpoint every checkpoint_every steps; the backward pass
+ * recomputes each segment from its checkpoint.  The world ends in the state after the
+ * n_steps forward steps.  Device memory for tapes and checkpoints is allocated on the first
+ * call and kept with the world. */
+int cc_world_rollout_grad(cc_world *world, float dt, int32_t n_steps, int32_t checkpoint_every,
+                          const float *targets, float *loss, float *grad_linvel, float *grad_angvel,
+                          float *grad_friction);
+
 /* ---------------------------------------------------------------------------
  * Allocation-free penetration query.  No counterpart in the reference: it is
  * the narrowphase of one convex pair (collideConvexVsConvex,

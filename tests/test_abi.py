@@ -88,3 +88,8 @@ def test_static_query_checks_arguments_before_any_cuda_call(lib):
     assert lib.cc_penetration_static(one, 8, one, C.c_float(0.0), tol[1], None) == _lib.CC_ERR_INVALID
     assert lib.cc_penetration_static(None, 0, None, *tol, None) == _lib.CC_OK
     assert _lib.PEN_QUERY_DTYPE.itemsize == 100 and _lib.PEN_RESULT_DTYPE.itemsize == 48
+
+
+def test_rollout_grad_checks_arguments_before_any_cuda_call(lib):
+    t = (C.c_float * 3)()
+    assert lib.cc_world_rollout_grad(None, C.c_float(0.01), 10, 5, t, None, None, None, None) == _lib.CC_ERR_INVALID
