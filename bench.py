@@ -478,11 +478,15 @@ def run_gpu(args, rank, world_size, local):
     peak, peak_kind = read_peaks()
     bytes_dom = algorithmic_bytes(dom, pst, n)
     achieved = bytes_dom / (prof[dom] * 1e-3) / 1e9 if prof[dom] > 0 else 0.0
+    # DRAM bytes per launch of the dominant stage: the per-unit traffic of the committed ncu
+    # capture (profiles/traffic_per_unit.json) times this step's units
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic_per_step.json")
+    tpath = os.path.join(ROOT, "profiles", "traffic_per_unit.json")
     if os.path.exists(tpath):
         try:
-            traffic = json.load(open(tpath)).get(dom)
+            t = json.load(open(tpath)).get(dom)
+            if t:
+                traffic = t["bytes_per_unit"] * pst[t["unit"]]
         except Exception:
             traffic = None
 
