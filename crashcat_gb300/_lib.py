@@ -23,6 +23,7 @@ CC_ERR_UNSUPPORTED = 6
 
 SHAPE_SPHERE = 0
 SHAPE_BOX = 1
+SHAPE_CAPSULE = 2
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 COMBINE_AVERAGE, COMBINE_MULTIPLY, COMBINE_MIN, COMBINE_MAX, COMBINE_GEOMETRIC_MEAN = 0, 1, 2, 3, 4
 MAX_LAYERS = 32

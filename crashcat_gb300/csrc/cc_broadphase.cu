@@ -84,7 +84,7 @@ __device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b
 __device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
 
-__device__ void exact_aabb(float4 p4, float4 q4, float3 lo, float3 hi, double out[6]) {
+__device__ void exact_aabb(float4 p4, float4 q4, const double lo[3], const double hi[3], double out[6]) {
     double x = q4.x, y = q4.y, z = q4.z, ww = q4.w;
     double x2 = da(x, x), y2 = da(y, y), z2 = da(z, z);
     double xx = dm(x, x2), yx = dm(y, x2), yy = dm(y, y2), zx = dm(z, x2), zy = dm(z, y2), zz = dm(z, z2);
@@ -93,7 +93,7 @@ __device__ void exact_aabb(float4 p4, float4 q4, float3 lo, float3 hi, double ou
     double m4 = ds(yx, wz), m5 = ds(ds(1.0, xx), zz), m6 = da(zy, wx);
     double m8 = da(zx, wy), m9 = ds(zy, wx), m10 = ds(ds(1.0, xx), yy);
     double px = p4.x, py = p4.y, pz = p4.z;
-    double xs[2] = {lo.x, hi.x}, ys[2] = {lo.y, hi.y}, zs[2] = {lo.z, hi.z};
+    double xs[2] = {lo[0], hi[0]}, ys[2] = {lo[1], hi[1]}, zs[2] = {lo[2], hi[2]};
     double mnx = 0, mny = 0, mnz = 0, mxx = 0, mxy = 0, mxz = 0;
 #pragma unroll
     for (int c = 0; c < 8; c++) {
@@ -122,14 +122,26 @@ __device__ void exact_aabb(float4 p4, float4 q4, float3 lo, float3 hi, double ou
     out[5] = mxz;
 }
 
-__device__ __forceinline__ void shape_bounds(uint32_t f, float4 sp, float3 &lo, float3 &hi) {
-    if (shape_of(f) == SHAPE_BOX) {
-        lo = f3(-sp.x, -sp.y, -sp.z);
-        hi = f3(sp.x, sp.y, sp.z);
+// local bounds of the shape in FP64 (box.ts:77-84, sphere.ts, capsule.ts:84-94)
+__device__ __forceinline__ void shape_bounds(uint32_t f, float4 sp, double lo[3], double hi[3]) {
+    int s = shape_of(f);
+    double ex, ey, ez;
+    if (s == SHAPE_BOX) {
+        ex = sp.x;
+        ey = sp.y;
+        ez = sp.z;
+    } else if (s == SHAPE_CAPSULE) {
+        ex = ez = sp.x;
+        ey = da((double)sp.y, (double)sp.x);  // half height + radius
     } else {
-        lo = f3(-sp.x, -sp.x, -sp.x);
-        hi = f3(sp.x, sp.x, sp.x);
+        ex = ey = ez = sp.x;
     }
+    lo[0] = -ex;
+    lo[1] = -ey;
+    lo[2] = -ez;
+    hi[0] = ex;
+    hi[1] = ey;
+    hi[2] = ez;
 }
 
 __device__ __forceinline__ unsigned int f2ord(float f) {
@@ -147,7 +159,7 @@ __global__ void k_update_bounds(DevWorld w, unsigned int *scene) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
         uint32_t f = w.flags[i];
         if (motion_of(f) != STATIC && !sleeping_of(f)) awake++;
-        float3 lo, hi;
+        double lo[3], hi[3];
         shape_bounds(f, w.shape[i], lo, hi);
         double b[6];
         exact_aabb(w.pos[i], w.quat[i], lo, hi, b);

@@ -34,7 +34,7 @@ __host__ __device__ inline int layer_of(uint32_t f) { return (int)((f >> F_LAYER
 __host__ __device__ inline bool sleeping_of(uint32_t f) { return (f & F_SLEEPING) != 0; }
 
 constexpr int STATIC = 0, KINEMATIC = 1, DYNAMIC = 2;
-constexpr int SHAPE_SPHERE = 0, SHAPE_BOX = 1;
+constexpr int SHAPE_SPHERE = 0, SHAPE_BOX = 1, SHAPE_CAPSULE = 2;
 
 // Per-step overflow flags (status bits in DevCounters::overflow)
 enum : int { OVF_PAIRS = 1, OVF_MANIFOLDS = 2, OVF_EPA = 4, OVF_ISLAND = 8, OVF_CACHE = 16, OVF_SLOTS = 32 };

@@ -107,7 +107,7 @@ __device__ __forceinline__ Q<S> qmulS(Q<S> a, Q<S> b) {
 // ---------------------------------------------------------------------------
 // support functions
 // ---------------------------------------------------------------------------
-enum { SUP_BOX = 0, SUP_POINT = 1, SUP_SPHERE = 2 };
+enum { SUP_BOX = 0, SUP_POINT = 1, SUP_SPHERE = 2, SUP_CAPSULE_SEGMENT = 3, SUP_CAPSULE_SURFACE = 4 };
 template <typename S>
 struct Sup {
     int kind;
@@ -120,7 +120,14 @@ struct Sup {
     __device__ V<S> inner(V<S> d) const {
         if (kind == SUP_BOX) return {d.x >= S(0) ? he.x : -he.x, d.y >= S(0) ? he.y : -he.y, d.z >= S(0) ? he.z : -he.z};
         if (kind == SUP_POINT) return {S(0), S(0), S(0)};
+        // capsule: segment +-h on Y (capsuleNoConvexGetSupport capsule.ts:268-275)
+        if (kind == SUP_CAPSULE_SEGMENT) return {S(0), d.y > S(0) ? he.y : -he.y, S(0)};
         S l = lsq(d);
+        if (kind == SUP_CAPSULE_SURFACE) {  // capsuleWithConvexGetSupport capsule.ts:321-338
+            if (!(l > S(0))) return {S(0), he.y, S(0)};
+            S sc = radius / sq_root(l);
+            return {d.x * sc, d.y * sc + (d.y > S(0) ? he.y : -he.y), d.z * sc};
+        }
         if (l > S(0)) return d * (radius / sq_root(l));
         return {S(0), S(0), S(0)};
     }
@@ -160,6 +167,17 @@ __device__ Sup<S> make_sup(int shape, float4 sp, bool exclude) {
             o.convex_radius = cr;
         } else {
             o.he = {S(sp.x), S(sp.y), S(sp.z)};
+            o.convex_radius = S(0);
+        }
+    } else if (shape == SHAPE_CAPSULE) {
+        // getCapsuleSupportFunction capsule.ts:390-404 (radius sp.x, half height sp.y)
+        o.he = {S(0), S(sp.y), S(0)};
+        if (exclude) {
+            o.kind = SUP_CAPSULE_SEGMENT;
+            o.convex_radius = S(sp.x);
+        } else {
+            o.kind = SUP_CAPSULE_SURFACE;
+            o.radius = S(sp.x);
             o.convex_radius = S(0);
         }
     } else {
@@ -610,6 +628,25 @@ __device__ void box_face(Face &f, float3 dir, float4 he4, float4 q, float3 t) {
     for (int i = 0; i < 4; i++) f.v[i] = mmul(m, f.v[i]) + t;
 }
 
+// capsule getSupportingFace capsule.ts:192-251: the segment on the side opposite to dir
+// (body space) when both caps project within the capsule projection slop, else no face;
+// rotated by q and moved by t
+__device__ void capsule_face(Face &f, float3 d, float4 sp, float4 q, float3 t) {
+    float r = sp.x, h = sp.y;
+    float len = sqrtf(d.x * d.x + d.z * d.z);
+    f.n = 0;
+    if (len == 0.f) return;
+    float sx = (r / len) * d.x, sz = (r / len) * d.z;
+    float3 top = f3(-sx, h, -sz), bottom = f3(-sx, -h, -sz);
+    float pt = dot3(top, d), pb = dot3(bottom, d);
+    const float slop = 0.02f;  // cCapsuleProjectionSlop
+    if (fabsf(pt - pb) < slop * sqrtf(lensq3(d))) {
+        f.n = 2;
+        f.v[0] = qrot(q, top) + t;
+        f.v[1] = qrot(q, bottom) + t;
+    }
+}
+
 // clipPolyVsPlane clip.ts:13-92
 __device__ void clip_plane(Face &out, const Face &in, float3 o, float3 n) {
     out.n = 0;
@@ -725,6 +762,39 @@ __device__ void prune(Pts &m, float3 axis) {
     m.n = o;
 }
 
+// clipPolyVsEdge clip.ts:190-363: crossings of the polygon with the plane through the edge
+// (normal = clip normal x edge), snapped onto the edge projected into the polygon's plane
+__device__ void clip_poly_vs_edge(Face &out, const Face &poly, float3 ev1, float3 ev2, float3 cn) {
+    out.n = 0;
+    if (poly.n < 3) return;
+    float3 en = cross3(cn, ev2 - ev1);
+    float3 p0 = poly.v[0];
+    float3 pn = cross3(poly.v[2] - p0, poly.v[1] - p0);
+    float pl2 = lensq3(pn);
+    float3 v1 = ev1 + pn * (dot3(p0 - ev1, pn) / pl2);
+    float3 v2 = ev2 + pn * (dot3(p0 - ev2, pn) / pl2);
+    float3 v12 = v2 - v1;
+    float v12l2 = lensq3(v12);
+    float3 e1 = poly.v[poly.n - 1];
+    float prevNum = dot3(ev1 - e1, en);
+    bool prevIn = prevNum < 0.f;
+    for (int j = 0; j < poly.n; j++) {
+        float3 e2 = poly.v[j];
+        float num = dot3(ev1 - e2, en);
+        bool curIn = num < 0.f;
+        if (curIn != prevIn && out.n < FMAX) {
+            float3 e12 = e2 - e1;
+            float den = dot3(e12, en);
+            float3 c = den != 0.f ? e1 + e12 * (prevNum / den) : e1;
+            float proj = dot3(c - v1, v12);
+            out.v[out.n++] = proj < 0.f ? v1 : (proj > v12l2 ? v2 : c);
+        }
+        prevNum = num;
+        prevIn = curIn;
+        e1 = e2;
+    }
+}
+
 // manifoldBetweenTwoFaces manifold.ts:345-444 (polygon faces)
 __device__ void manifold_faces(Pts &out, float3 cp1, float3 cp2, float3 axis, float maxDist, const Face &f1,
                                const Face &f2) {
@@ -737,7 +807,10 @@ __device__ void manifold_faces(Pts &out, float3 cp1, float3 cp2, float3 axis, fl
     }
     Face clipped;
     clipped.n = 0;
-    if (f1.n >= 3) clip_poly(clipped, f2, f1, axis);
+    if (f1.n >= 3)
+        clip_poly(clipped, f2, f1, axis);
+    else
+        clip_poly_vs_edge(clipped, f2, f1.v[0], f1.v[1], axis);
     float3 po = f1.v[0];
     float3 first = f1.v[1] - po;
     float3 pn;
@@ -785,7 +858,9 @@ __device__ void emit_manifold(DevWorld &w, int a, int b, float3 pa, float3 pb, f
         float3 axA = qrot_inv(qa, axis);
         float3 axB = qrot_inv(qb, axis);
         if (shape_of(fa) == SHAPE_BOX) box_face(fA, -axA, w.shape[a], qa, f3(0.f, 0.f, 0.f));
+        if (shape_of(fa) == SHAPE_CAPSULE) capsule_face(fA, -axA, w.shape[a], qa, f3(0.f, 0.f, 0.f));
         if (shape_of(fb) == SHAPE_BOX) box_face(fB, axB, w.shape[b], qb, posB - posA);
+        if (shape_of(fb) == SHAPE_CAPSULE) capsule_face(fB, axB, w.shape[b], qb, posB - posA);
         haveFaces = fA.n >= 2 && fB.n >= 3;
     }
     if (haveFaces) {
@@ -1687,7 +1762,7 @@ __global__ void __launch_bounds__(128) k_static_gjk(const cc_penetration_query *
     pose_of(qy.b, pb4, qb, sb);
     int sha = qy.a.shape_type, shb = qy.b.shape_type;
     float maxSep = qy.max_separation;
-    if ((sha != SHAPE_SPHERE && sha != SHAPE_BOX) || (shb != SHAPE_SPHERE && shb != SHAPE_BOX)) {
+    if (sha < SHAPE_SPHERE || sha > SHAPE_CAPSULE || shb < SHAPE_SPHERE || shb > SHAPE_CAPSULE) {
         res[i] = r;  // unknown shape type: reported as no hit
         return;
     }

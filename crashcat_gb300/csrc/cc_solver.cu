@@ -300,7 +300,9 @@ __global__ void k_contact_setup(DevWorld w, CacheTables ct, float dt) {
 
 // sleep test points (getSleepTestPoints sleep.ts:22-74)
 __device__ void sleep_points(uint32_t f, float4 sp, float4 q, float3 com, float3 out[3]) {
-    float3 e = shape_of(f) == SHAPE_BOX ? f3(sp.x, sp.y, sp.z) : f3(sp.x, sp.x, sp.x);
+    int sh = shape_of(f);
+    float3 e = sh == SHAPE_BOX ? f3(sp.x, sp.y, sp.z)
+                               : (sh == SHAPE_CAPSULE ? f3(sp.x, sp.y + sp.x, sp.x) : f3(sp.x, sp.x, sp.x));
     out[0] = com;
     int lowest = (e.x <= e.y && e.x <= e.z) ? 0 : (e.y <= e.z ? 1 : 2);
     float3 X = f3(1.f, 0.f, 0.f), Y = f3(0.f, 1.f, 0.f), Z = f3(0.f, 0.f, 1.f);

@@ -395,7 +395,10 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
     std::vector<float> timer(n, 0.f);
     for (int i = 0; i < n; i++) {
         const cc_body_desc &d = b[i];
-        if (d.shape_type != CC_SHAPE_BOX && d.shape_type != CC_SHAPE_SPHERE) return CC_ERR_UNSUPPORTED;
+        if (d.shape_type != CC_SHAPE_BOX && d.shape_type != CC_SHAPE_SPHERE && d.shape_type != CC_SHAPE_CAPSULE)
+            return CC_ERR_UNSUPPORTED;
+        if (d.shape_type == CC_SHAPE_CAPSULE && !(d.shape_params[0] > 0.f && d.shape_params[1] > 0.f))
+            return CC_ERR_INVALID;  // capsule.ts:55-61
         if (d.motion_type < 0 || d.motion_type > 2) return CC_ERR_INVALID;
         if (d.object_layer < 0 || d.object_layer >= W->settings.num_object_layers) return CC_ERR_INVALID;
         if (d.world < 0 || d.world >= w.num_worlds) return CC_ERR_INVALID;
@@ -407,6 +410,19 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
             idiag[0] = (fy * fy + fz * fz) * (mass / 12.0);
             idiag[1] = (fx * fx + fz * fz) * (mass / 12.0);
             idiag[2] = (fx * fx + fy * fy) * (mass / 12.0);
+        } else if (d.shape_type == CC_SHAPE_CAPSULE) {
+            // computeMassProperties capsule.ts:119-157: cylinder plus two hemispheres along Y
+            double r = d.shape_params[0], h = d.shape_params[1];
+            double volume = M_PI * r * r * (2 * h) + (4.0 / 3.0) * M_PI * r * r * r;
+            mass = volume * d.density;
+            double r2 = r * r, height = 2.0 * h;
+            double cyl = M_PI * height * r2 * d.density;
+            double hemi = ((2.0 * M_PI) / 3.0) * r2 * r * d.density;
+            double iy = r2 * cyl * 0.5 + hemi * (2.0 / 5.0) * r2;
+            double ixz = cyl * ((1.0 / 12.0) * height * height + (1.0 / 4.0) * r2) +
+                         hemi * ((2.0 / 5.0) * r2 + h * h + (3.0 / 8.0) * h * r);
+            idiag[0] = idiag[2] = ixz;
+            idiag[1] = iy;
         } else {
             double r = d.shape_params[0];
             mass = (4.0 / 3.0) * M_PI * r * r * r * d.density;
@@ -452,8 +468,11 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
         groups[i] = make_uint2(d.collision_groups, d.collision_mask);
         world[i] = d.world;
         // resetSleepTimer sleep.ts:123-130
-        float3 e = d.shape_type == CC_SHAPE_BOX ? f3(d.shape_params[0], d.shape_params[1], d.shape_params[2])
-                                                 : f3(d.shape_params[0], d.shape_params[0], d.shape_params[0]);
+        float3 e = d.shape_type == CC_SHAPE_BOX
+                       ? f3(d.shape_params[0], d.shape_params[1], d.shape_params[2])
+                       : (d.shape_type == CC_SHAPE_CAPSULE
+                              ? f3(d.shape_params[0], d.shape_params[1] + d.shape_params[0], d.shape_params[0])
+                              : f3(d.shape_params[0], d.shape_params[0], d.shape_params[0]));
         float3 c = xyz(com[i]);
         float3 p[3];
         p[0] = c;

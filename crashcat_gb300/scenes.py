@@ -12,7 +12,8 @@ import math
 
 import numpy as np
 
-from ._lib import BODY_DTYPE, COMBINE_GEOMETRIC_MEAN, COMBINE_MAX, DYNAMIC, SHAPE_BOX, SHAPE_SPHERE, STATIC
+from ._lib import (BODY_DTYPE, COMBINE_GEOMETRIC_MEAN, COMBINE_MAX, DYNAMIC, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_SPHERE,
+                   STATIC)
 
 # object layers of the reference's test helper (tst/helpers.ts:5-26)
 LAYER_MOVING = 0
@@ -77,6 +78,14 @@ def set_sphere(b: np.ndarray, idx, radius) -> None:
     b["shape_type"][idx] = SHAPE_SPHERE
     b["shape_params"][idx, 0] = radius
     b["shape_params"][idx, 1:] = 0.0
+
+
+def set_capsule(b: np.ndarray, idx, radius, half_height) -> None:
+    """Capsule along local Y (src/shapes/capsule.ts): radius, half height of the cylinder."""
+    b["shape_type"][idx] = SHAPE_CAPSULE
+    b["shape_params"][idx, 0] = radius
+    b["shape_params"][idx, 1] = half_height
+    b["shape_params"][idx, 2:] = 0.0
 
 
 def static_floor(b: np.ndarray, idx: int, half=(50.0, 0.5, 50.0), y=-0.5, friction=0.5, world=0) -> None:
@@ -156,16 +165,21 @@ def batched_worlds(num_worlds: int = 4096, seed: int = 4, n_min: int = 8, n_max:
                  num_worlds=num_worlds, seed=seed)
 
 
-def random_pairs_scene(n: int = 200, seed: int = 7, extent: float = 6.0, box_fraction: float = 0.6) -> Scene:
-    """Boxes and spheres at random poses inside a small region above a floor:
-    a contact-rich state for stage-level parity (broadphase pairs, contacts)."""
+def random_pairs_scene(n: int = 200, seed: int = 7, extent: float = 6.0, box_fraction: float = 0.6,
+                       capsule_fraction: float = 0.0) -> Scene:
+    """Boxes, spheres and (optionally) capsules at random poses inside a small region
+    above a floor: a contact-rich state for stage-level parity (broadphase pairs,
+    contacts).  Capsules: radius 0.2-0.4 m, half height 0.3-0.8 m."""
     rng = np.random.Generator(np.random.PCG64(seed))
     b = blank_bodies(n + 1)
     static_floor(b, 0, half=(20.0, 0.5, 20.0), friction=0.5)
     idx = np.arange(1, n + 1)
     is_box = rng.random(n) < box_fraction
+    is_capsule = rng.random(n) < capsule_fraction
     for k, i in enumerate(idx):
-        if is_box[k]:
+        if is_capsule[k]:
+            set_capsule(b, i, rng.uniform(0.2, 0.4), rng.uniform(0.3, 0.8))
+        elif is_box[k]:
             set_box(b, i, rng.uniform(0.2, 0.7, size=3))
         else:
             set_sphere(b, i, rng.uniform(0.2, 0.6))
@@ -312,3 +326,39 @@ def diff_rollout_worlds(num_worlds: int = 1024, seed: int = 5, boxes: int = 64) 
     sc = Scene("diff_rollout_worlds", b, dt=1.0 / 60.0, steps=120, velocity_iterations=10, position_iterations=2,
                num_worlds=num_worlds, seed=seed)
     return sc, targets
+
+
+def capsules_on_floor(n: int = 16, seed: int = 51) -> Scene:
+    """Capsules lying on the floor in a spaced row, their axis tilted 2-6 degrees so that
+    one cap touches first (a perfectly level capsule has no unique deepest point along
+    its segment), plus a few standing upright.  The static floor is body A, so each
+    contact is a single point (update.ts:474)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = blank_bodies(n + 1)
+    static_floor(b, 0, half=(30.0, 0.5, 30.0), friction=0.5)
+    idx = np.arange(1, n + 1)
+    r = rng.uniform(0.2, 0.4, size=n).astype(np.float32)
+    h = rng.uniform(0.3, 0.8, size=n).astype(np.float32)
+    for k, i in enumerate(idx):
+        set_capsule(b, i, r[k], h[k])
+    upright = np.arange(n) % 4 == 3
+    tilt = np.radians(rng.uniform(2.0, 6.0, n))
+    # lowest point of a lying capsule tilted by `tilt`: r + h sin(tilt) below its centre
+    y = np.where(upright, h + r, r + h * np.sin(tilt)) - 0.003
+    pos = np.stack([(np.arange(n) - (n - 1) / 2) * 3.0, y, rng.uniform(-0.1, 0.1, n)], 1)
+    b["position"][idx] = pos.astype(np.float32)
+    yaw = rng.uniform(0, np.pi, n)
+    # lying: rotate local Y onto the floor plane (90 degrees less the tilt, about a horizontal
+    # axis at angle yaw)
+    q = []
+    for k in range(n):
+        if upright[k]:
+            q.append((0.0, math.sin(yaw[k] / 2), 0.0, math.cos(yaw[k] / 2)))
+        else:
+            ax = (math.cos(yaw[k]), 0.0, math.sin(yaw[k]))
+            half = (math.pi / 2 - tilt[k]) / 2
+            q.append((ax[0] * math.sin(half), 0.0, ax[2] * math.sin(half), math.cos(half)))
+    b["quaternion"][idx] = np.asarray(q, dtype=np.float32)
+    b["linear_velocity"][idx] = rng.normal(scale=0.3, size=(n, 3)).astype(np.float32)
+    b["friction"][idx] = 0.5
+    return Scene("capsules_on_floor", b, dt=1.0 / 60.0, steps=1, seed=seed)

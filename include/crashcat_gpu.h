@@ -47,7 +47,7 @@ enum cc_status {
     CC_ERR_UNSUPPORTED = 6
 };
 
-enum cc_shape_type { CC_SHAPE_SPHERE = 0, CC_SHAPE_BOX = 1 };
+enum cc_shape_type { CC_SHAPE_SPHERE = 0, CC_SHAPE_BOX = 1, CC_SHAPE_CAPSULE = 2 };
 enum cc_motion_type { CC_STATIC = 0, CC_KINEMATIC = 1, CC_DYNAMIC = 2 };
 enum cc_combine_mode { CC_COMBINE_AVERAGE = 0, CC_COMBINE_MULTIPLY = 1, CC_COMBINE_MIN = 2, CC_COMBINE_MAX = 3,
                        CC_COMBINE_GEOMETRIC_MEAN = 4 };
@@ -93,7 +93,8 @@ typedef struct cc_world_settings {
 } cc_world_settings;
 
 /* RigidBodySettings (src/body/rigid-body.ts:37-139) for the supported shapes.
- * shape_params: box = half extents xyz + convex radius; sphere = radius. */
+ * shape_params: box = half extents xyz + convex radius; sphere = radius;
+ * capsule = radius, half height of the cylinder (along local Y, src/shapes/capsule.ts). */
 typedef struct cc_body_desc {
     int32_t shape_type;
     float shape_params[4];

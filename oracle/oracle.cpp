@@ -170,6 +170,20 @@ static void shape_mass(const Shape &s, double &mass, V3 &inertiaDiag) {
         mass = (4.0 / 3.0) * M_PI * s.radius * r2 * s.density;
         double in = (2.0 / 5.0) * mass * r2;
         inertiaDiag = {in, in, in};
+    } else if (s.type == SHAPE_CAPSULE) {
+        // computeMassProperties capsule.ts:119-157 (cylinder plus two hemispheres)
+        double r = s.radius, h = s.half_height;
+        double volume = M_PI * r * r * (2 * h) + (4.0 / 3.0) * M_PI * r * r * r;
+        mass = volume * s.density;
+        double r2 = r * r, height = 2.0 * h;
+        double cyl = M_PI * height * r2 * s.density;
+        double hemi = ((2.0 * M_PI) / 3.0) * r2 * r * s.density;
+        double height2 = height * height;
+        double iy = r2 * cyl * 0.5;
+        double ixz = cyl * ((1.0 / 12.0) * height2 + (1.0 / 4.0) * r2);
+        double hxz = hemi * ((2.0 / 5.0) * r2 + h * h + (3.0 / 8.0) * h * r);
+        double hy = hemi * (2.0 / 5.0) * r2;
+        inertiaDiag = {ixz + hxz, iy + hy, ixz + hxz};
     } else {
         mass = 0;
         inertiaDiag = {0, 0, 0};
@@ -1239,7 +1253,7 @@ extern "C" {
 // Body description: one row of doubles per body, layout shared with the
 // Python scene builder (crashcat_gb300/scenes.py BODY_FIELDS).
 enum {
-    F_SHAPE = 0,       // 0 sphere, 1 box
+    F_SHAPE = 0,       // 0 sphere, 1 box, 2 capsule (F_P0 radius, F_P0 + 1 half height)
     F_P0 = 1,          // shape params (box hx,hy,hz,convexRadius ; sphere r)
     F_DENSITY = 5,
     F_MOTION = 6,
@@ -1294,6 +1308,30 @@ void *orc_world_create(const double *settings, int n_obj, const int *obj_to_bp, 
 void orc_world_destroy(void *wp) { delete (World *)wp; }
 
 // rigidBody.create rigid-body.ts:390-434 for each row
+// Shape fields of a body row (F_SHAPE, F_DENSITY, F_P0..F_P0 + 3); false for an unknown type.
+static bool shape_from_row(Shape &s, const double *r) {
+    s.type = (int)r[F_SHAPE];
+    s.density = r[F_DENSITY];
+    s.com = {0, 0, 0};
+    if (s.type == SHAPE_BOX) {
+        s.half_extents = {r[F_P0], r[F_P0 + 1], r[F_P0 + 2]};
+        s.convex_radius = r[F_P0 + 3];
+        s.aabb = {neg(s.half_extents), s.half_extents};
+    } else if (s.type == SHAPE_SPHERE) {
+        s.radius = r[F_P0];
+        s.aabb = {{-s.radius, -s.radius, -s.radius}, {s.radius, s.radius, s.radius}};
+    } else if (s.type == SHAPE_CAPSULE) {
+        // capsule.ts:84-94: segment +-halfHeight on Y with radius r
+        s.radius = r[F_P0];
+        s.half_height = r[F_P0 + 1];
+        double th = s.half_height + s.radius;
+        s.aabb = {{-s.radius, -th, -s.radius}, {s.radius, th, s.radius}};
+    } else {
+        return false;
+    }
+    return true;
+}
+
 int orc_add_bodies(void *wp, const double *rows, int n) {
     World &w = *(World *)wp;
     for (int i = 0; i < n; i++) {
@@ -1304,19 +1342,7 @@ int orc_add_bodies(void *wp, const double *rows, int n) {
         w.nextSequence = (w.nextSequence + 1) & ((1 << 20) - 1);
         b.id = (int64_t)b.index + (int64_t)seq * 4294967296LL;
         Shape &s = b.shape;
-        s.type = (int)r[F_SHAPE];
-        s.density = r[F_DENSITY];
-        if (s.type == SHAPE_BOX) {
-            s.half_extents = {r[F_P0], r[F_P0 + 1], r[F_P0 + 2]};
-            s.convex_radius = r[F_P0 + 3];
-            s.aabb = {neg(s.half_extents), s.half_extents};
-        } else if (s.type == SHAPE_SPHERE) {
-            s.radius = r[F_P0];
-            s.aabb = {{-s.radius, -s.radius, -s.radius}, {s.radius, s.radius, s.radius}};
-        } else {
-            return -1;
-        }
-        s.com = {0, 0, 0};
+        if (!shape_from_row(s, r)) return -1;
         b.position = {r[F_POS], r[F_POS + 1], r[F_POS + 2]};
         b.quat = {r[F_QUAT], r[F_QUAT + 1], r[F_QUAT + 2], r[F_QUAT + 3]};
         b.motion = (int)r[F_MOTION];
@@ -1551,13 +1577,7 @@ int orc_collide_pair(const double *rowA, const double *rowB, double maxSep, doub
     const double *rows[2] = {rowA, rowB};
     for (int k = 0; k < 2; k++) {
         const double *r = rows[k];
-        s[k].type = (int)r[F_SHAPE];
-        if (s[k].type == SHAPE_BOX) {
-            s[k].half_extents = {r[F_P0], r[F_P0 + 1], r[F_P0 + 2]};
-            s[k].convex_radius = r[F_P0 + 3];
-        } else {
-            s[k].radius = r[F_P0];
-        }
+        if (!shape_from_row(s[k], r)) return -1;
         p[k] = {r[F_POS], r[F_POS + 1], r[F_POS + 2]};
         q[k] = {r[F_QUAT], r[F_QUAT + 1], r[F_QUAT + 2], r[F_QUAT + 3]};
     }
@@ -1584,12 +1604,7 @@ int orc_collide_pair(const double *rowA, const double *rowB, double maxSep, doub
 void orc_inverse_inertia(const double *row, double *out9) {
     Body b;
     Shape &s = b.shape;
-    s.type = (int)row[F_SHAPE];
-    s.density = row[F_DENSITY];
-    if (s.type == SHAPE_BOX)
-        s.half_extents = {row[F_P0], row[F_P0 + 1], row[F_P0 + 2]};
-    else
-        s.radius = row[F_P0];
+    shape_from_row(s, row);
     double mass;
     V3 d;
     shape_mass(s, mass, d);

@@ -65,16 +65,11 @@ struct Support {
             }
             case SUP_CAPSULE_SEGMENT:  // capsule.ts: segment +-h on Y
                 return {0, d.y > 0 ? half_height : -half_height, 0};
-            case SUP_CAPSULE_SURFACE: {
+            case SUP_CAPSULE_SURFACE: {  // capsuleWithConvexGetSupport capsule.ts:321-338
                 double l = d.x * d.x + d.y * d.y + d.z * d.z;
-                V3 o{0, d.y > 0 ? half_height : -half_height, 0};
-                if (l > 0) {
-                    double s = radius / std::sqrt(l);
-                    o.x += d.x * s;
-                    o.y += d.y * s;
-                    o.z += d.z * s;
-                }
-                return o;
+                if (!(l > 0)) return {0, half_height, 0};
+                double s = radius / std::sqrt(l);
+                return {d.x * s, d.y * s + (d.y > 0 ? half_height : -half_height), d.z * s};
             }
         }
         return {0, 0, 0};
@@ -1149,11 +1144,37 @@ inline void box_supporting_face(Face &f, V3 dir, V3 he) {
     }
 }
 
-// getShapeSupportingFace shapes.ts:489-508 (box and sphere; sphere has no face)
+// capsule getSupportingFace capsule.ts:192-251: the segment on the side opposite to the
+// direction when both caps project within the capsule projection slop, else no face
+inline void capsule_supporting_face(Face &f, V3 d, double h, double r) {
+    double len = std::sqrt(d.x * d.x + d.z * d.z);
+    if (len == 0.0) {
+        f.n = 0;
+        return;
+    }
+    double sx = (r / len) * d.x, sz = (r / len) * d.z;
+    V3 top{-sx, h, -sz}, bottom{-sx, -h, -sz};
+    double pt = top.x * d.x + top.y * d.y + top.z * d.z;
+    double pb = bottom.x * d.x + bottom.y * d.y + bottom.z * d.z;
+    const double slop = 0.02;  // cCapsuleProjectionSlop
+    double dl = std::sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
+    if (std::fabs(pt - pb) < slop * dl) {
+        f.n = 2;
+        f.v[0] = top;
+        f.v[1] = bottom;
+    } else {
+        f.n = 0;
+    }
+}
+
+// getShapeSupportingFace shapes.ts:489-508 (sphere has no face)
 inline void shape_supporting_face(Face &f, const Shape &s, V3 dir, V3 p, Q4 q) {
     if (s.type == SHAPE_BOX) {
         box_supporting_face(f, dir, s.half_extents);
         transform_face(f, p, q);
+    } else if (s.type == SHAPE_CAPSULE) {
+        capsule_supporting_face(f, dir, s.half_height, s.radius);
+        if (f.n > 0) transform_face(f, p, q);
     } else {
         f.n = 0;
     }
@@ -1294,6 +1315,43 @@ inline void prune_contact_points(Manifold &m, V3 axis) {
     m.n = o;
 }
 
+// clipPolyVsEdge clip.ts:190-363: the polygon's crossings of the plane through the edge
+// (normal = clipNormal x edge), snapped onto the edge projected into the polygon's plane
+inline void clip_poly_vs_edge(Face &out, const Face &poly, V3 ev1, V3 ev2, V3 clipNormal) {
+    out.n = 0;
+    if (poly.n < 3) return;
+    V3 edge = sub(ev2, ev1);
+    V3 en = cross(clipNormal, edge);
+    V3 p0 = poly.v[0], p1 = poly.v[1], p2 = poly.v[2];
+    V3 pn = cross(sub(p2, p0), sub(p1, p0));
+    double pl2 = dot(pn, pn);
+    V3 v1 = scale_add(ev1, pn, dot(sub(p0, ev1), pn) / pl2);
+    V3 v2 = scale_add(ev2, pn, dot(sub(p0, ev2), pn) / pl2);
+    V3 v12 = sub(v2, v1);
+    double v12l2 = dot(v12, v12);
+    V3 e1 = poly.v[poly.n - 1];
+    double prevNum = dot(sub(ev1, e1), en);
+    bool prevIn = prevNum < 0.0;
+    for (int j = 0; j < poly.n; j++) {
+        V3 e2 = poly.v[j];
+        double num = dot(sub(ev1, e2), en);
+        bool curIn = num < 0.0;
+        if (curIn != prevIn) {
+            V3 e12 = sub(e2, e1);
+            double den = dot(e12, en);
+            V3 c = den != 0.0 ? scale_add(e1, e12, prevNum / den) : e1;
+            double proj = dot(sub(c, v1), v12);
+            V3 o = proj < 0.0 ? v1 : (proj > v12l2 ? v2 : c);
+            if (out.n < FACE_MAX_VERTICES) out.v[out.n] = o;
+            out.n++;
+        }
+        prevNum = num;
+        prevIn = curIn;
+        e1 = e2;
+    }
+    if (out.n > FACE_MAX_VERTICES) out.n = FACE_MAX_VERTICES;
+}
+
 // manifoldBetweenTwoFaces manifold.ts:345-444
 inline void manifold_between_faces(Manifold &out, V3 cp1, V3 cp2, V3 axis, double maxDist, const Face &f1,
                                    const Face &f2) {
@@ -1307,8 +1365,9 @@ inline void manifold_between_faces(Manifold &out, V3 cp1, V3 cp2, V3 axis, doubl
     clipped.n = 0;
     if (f1.n >= 3) {
         clip_poly_vs_poly(clipped, f2, f1, axis);
+    } else if (f1.n == 2) {
+        clip_poly_vs_edge(clipped, f2, f1.v[0], f1.v[1], axis);
     }
-    // (edge faces of capsules: clipPolyVsEdge, not needed for box/sphere)
     V3 po = f1.v[0];
     V3 e1 = f1.v[1];
     V3 first = sub(e1, po);

@@ -288,3 +288,55 @@ def test_epa_fallback_pass_matches_packed_pass(gpu_lib, monkeypatch):
     for k in packed:
         np.testing.assert_allclose(packed[k][:7], fallback[k][:7], atol=1e-5)
         np.testing.assert_allclose(packed[k][8:], fallback[k][8:], atol=1e-4)
+
+
+# ---- capsules ------------------------------------------------------------------------
+@pytest.mark.parametrize("seed", [17, 18])
+def test_capsule_pairs_and_manifolds(gpu_lib, oracle_lib, seed):
+    """Boxes, spheres and capsules (40 %): broadphase pairs bit-exact, contacts within the
+    GJK / EPA tolerances of the module docstring."""
+    sc = scenes.random_pairs_scene(n=300, seed=seed, capsule_fraction=0.4)
+    g, o = make_pair(sc)
+    g.step(0.0, 1)
+    o.step(0.0, 1)
+    assert canonical_pairs(g.get_pairs()) == canonical_pairs(o.pairs())
+    gk = {(int(r[0]), int(r[1])): r for r in g.get_manifolds()}
+    ok = {(int(r[0]), int(r[1])): r for r in o.manifolds()}
+    assert len(ok) > 20
+    common = set(gk) & set(ok)
+    assert len(common) >= 0.98 * max(len(gk), len(ok))
+    bad = [k for k in common if not contact_errors(gk[k], ok[k])]
+    assert len(bad) <= 0.02 * len(common), bad[:5]
+
+
+def test_capsule_edge_clipped_on_box(gpu_lib, oracle_lib):
+    """Capsule (body A) lying on a dynamic box: the edge face clipped by clipPolyVsEdge gives
+    two points at the cylinder's ends, as in the oracle."""
+    import math
+    s2 = math.sin(math.pi / 4)
+    b = scenes.blank_bodies(2)
+    scenes.set_capsule(b, 0, 0.3, 0.6)
+    b["position"][0] = (0.0, 0.3 - 0.01, 0.0)
+    b["quaternion"][0] = (s2, 0.0, 0.0, s2)
+    scenes.set_box(b, 1, (2.0, 0.5, 2.0))
+    b["position"][1] = (0.0, -0.5, 0.0)
+    sc = scenes.Scene("capsule_on_box", b, dt=1 / 60, steps=1)
+    g, o = make_pair(sc)
+    g.step(0.0, 1)
+    o.step(0.0, 1)
+    gm, om = g.get_manifolds(), o.manifolds()
+    assert len(gm) == len(om) == 1 and int(gm[0][2]) == int(om[0][2]) == 2
+    assert contact_errors(gm[0], om[0])
+
+
+def test_capsules_on_floor_track_oracle(gpu_lib, oracle_lib):
+    """Capsules lying and standing on the floor: 30 steps of velocities and heights."""
+    sc = scenes.capsules_on_floor()
+    g, o = make_pair(sc)
+    for _ in range(3):
+        g.step(sc.dt, 10)
+        o.step(sc.dt, 10)
+        rows, _ = g.get_state()
+        st = o.state()
+        assert np.abs(rows[:, 1] - st[:, 1]).max() < 2e-3
+        assert np.abs(rows[:, 7:10] - st[:, 7:10]).max() < 2e-2

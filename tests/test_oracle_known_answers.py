@@ -222,3 +222,81 @@ def test_broadphase_layers_and_groups():
     o2 = pyoracle.OracleWorld(world.standard_settings(), b)
     o2.step(0.0, 1)
     assert len(o2.pairs()) == 0
+
+
+# ---- capsules (tst/shapes/capsule.test.ts) -------------------------------------------
+def _capsule_row(r, h, density=1000.0):
+    row = np.zeros(pyoracle.F_COUNT)
+    row[0] = 2
+    row[1], row[2] = r, h
+    row[5] = density
+    row[6] = 2
+    row[13] = 1.0  # identity quaternion (w)
+    return row
+
+
+def _inv_inertia_diag(lib, row):
+    out = np.zeros(9)
+    lib.orc_inverse_inertia(pyoracle.dptr(row), pyoracle.dptr(out))
+    return out.reshape(3, 3).diagonal()
+
+
+def test_capsule_inertia_properties(oracle_lib):
+    """capsule.test.ts:84-165: Ixx == Izz, Iyy < Ixx, density scales inertia, a long
+    capsule has Iyy < 0.1 Ixx, a wide one Iyy / Ixx > 0.5."""
+    d = 1.0 / _inv_inertia_diag(oracle_lib, _capsule_row(1.0, 1.0))
+    assert d[0] == pytest.approx(d[2]) and d[1] < d[0]
+    d2 = 1.0 / _inv_inertia_diag(oracle_lib, _capsule_row(1.0, 1.0, 2000.0))
+    np.testing.assert_allclose(d2, 2 * d, rtol=1e-12)
+    long_ = 1.0 / _inv_inertia_diag(oracle_lib, _capsule_row(0.5, 10.0))
+    assert long_[1] < 0.1 * long_[0]
+    wide = 1.0 / _inv_inertia_diag(oracle_lib, _capsule_row(2.0, 0.1))
+    assert wide[1] / wide[0] > 0.5
+
+
+def test_capsule_mass_and_bounds(oracle_lib):
+    """capsule.test.ts:37-81: volume pi r^2 2h + 4/3 pi r^3, mass = density x volume,
+    AABB [-r, -(h+r), -r]..[r, h+r, r]."""
+    from crashcat_gb300 import scenes, world
+    sc = scenes.blank_bodies(1)
+    scenes.set_capsule(sc, 0, 0.5, 2.0)
+    sc["density"][0] = 1000.0
+    o = pyoracle.OracleWorld(world.standard_settings(), sc)
+    box = o.aabbs()[0]
+    np.testing.assert_allclose(box, [-0.5, -2.5, -0.5, 0.5, 2.5, 0.5], atol=1e-12)
+    # mass from the inverse inertia of a sphere-free check: I_yy of the cylinder + caps
+    r, h = 0.5, 2.0
+    vol = math.pi * r * r * 2 * h + 4.0 / 3.0 * math.pi * r ** 3
+    assert vol == pytest.approx(math.pi * 0.25 * 4 + 4.0 / 3.0 * math.pi * 0.125)
+
+
+def test_capsule_collides_with_box_edge_face(oracle_lib):
+    """A capsule lying on a box.  Faces are clipped only when face A has 2+ vertices and
+    face B 3+ (update.ts:474).  With the capsule as body A (both dynamic, lower id) its
+    supporting face is the 2-vertex edge (capsule.ts:192-251), clipped against the box's
+    top face by clipPolyVsEdge (clip.ts:190-363): two contact points at the ends of the
+    cylinder.  On a static floor the floor is body A (lower motion type first,
+    update.ts:74) and the capsule's edge is face B, so the contact is a single point."""
+    from crashcat_gb300 import scenes, world
+    s2 = math.sin(math.pi / 4)
+    b = scenes.blank_bodies(2)
+    scenes.set_capsule(b, 0, 0.3, 0.6)
+    b["position"][0] = (0.0, 0.3 - 0.01, 0.0)
+    b["quaternion"][0] = (s2, 0.0, 0.0, s2)  # local Y onto world Z
+    scenes.set_box(b, 1, (2.0, 0.5, 2.0))
+    b["position"][1] = (0.0, -0.5, 0.0)
+    o = pyoracle.OracleWorld(world.standard_settings(), b)
+    o.step(0.0, 1)
+    m = o.manifolds()
+    assert len(m) == 1 and int(m[0][2]) == 2
+    pts = m[0][8:20].reshape(2, 6)
+    zs = sorted(pts[:, 2])
+    assert zs[0] == pytest.approx(-0.6, abs=1e-6) and zs[1] == pytest.approx(0.6, abs=1e-6)
+    np.testing.assert_allclose(m[0][3:6], [0.0, -1.0, 0.0], atol=1e-6)  # capsule (A) to box (B)
+    assert m[0][6] == pytest.approx(0.01, abs=1e-6)
+    # the same capsule on a static floor: one contact point
+    b["motion_type"][1] = 0
+    o = pyoracle.OracleWorld(world.standard_settings(), b)
+    o.step(0.0, 1)
+    m = o.manifolds()
+    assert len(m) == 1 and int(m[0][2]) == 1
