@@ -57,7 +57,8 @@ struct DevCounters {
     int mid_cursor;
     int epa_cursor;
     int epa_fallback;  // EPA items handed to the pass with the reference's polytope limits
-    int pad[16];
+    int num_removed;   // contact pairs of the previous step not found in this step
+    int pad[15];
 };
 
 // Settings copied into constant memory once per world.
@@ -246,6 +247,8 @@ struct DevWorld {
     int *root_flag;
     int *small_list, *large_list;
     int *scratch_order, *scratch_colour, *scratch_claim;
+    int *contact_event;               // per manifold: 1 added, 2 persisted (listener.ts:58-79)
+    unsigned long long *removed_keys;  // pairs in contact last step but not this step
     int *mid_list;    // islands solved by one warp each
     int *body_local;  // index of a body inside its island's body list (per-warp solve)
 };

@@ -158,6 +158,8 @@ __global__ void k_contact_setup(DevWorld w, CacheTables ct, float dt) {
             atomicOr(&w.ctr->overflow, OVF_CACHE);
             continue;
         }
+        // onContactPersisted / onContactAdded (contact-constraints.ts:494-499), sensors included
+        w.contact_event[mi] = prev >= 0 ? 2 : 1;
         uint32_t fa = w.flags[A], fb = w.flags[B];
         int ma = motion_of(fa), mb = motion_of(fb);
         float4 qa = w.quat[A], qb = w.quat[B];
@@ -1264,10 +1266,25 @@ static CacheTables tables_of(DevWorld &w) {
     return ct;
 }
 
+// onContactRemoved (contacts.ts:297-324, 534-553): pairs of the previous step's table that
+// this step did not re-insert
+__global__ void k_removed_contacts(DevWorld w, CacheTables ct) {
+    int par = *ct.parity;
+    const unsigned long long *pkeys = ct.keys[par ^ 1], *ckeys = ct.keys[par];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.cache_cap; i += gridDim.x * blockDim.x) {
+        unsigned long long key = pkeys[i];
+        if (key == EMPTY_KEY || cache_find(ckeys, w.cache_cap, key) >= 0) continue;
+        int k = atomicAdd(&w.ctr->num_removed, 1);
+        if (k < w.max_manifolds) w.removed_keys[k] = key;
+    }
+}
+
 __global__ void k_flip_parity(int *parity) { *parity ^= 1; }
 __global__ void k_mark_no_constraint(DevWorld w) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.max_manifolds; i += gridDim.x * blockDim.x)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.max_manifolds; i += gridDim.x * blockDim.x) {
         w.cons_of_manifold[i] = -1;
+        w.contact_event[i] = 0;
+    }
 }
 __global__ void k_clear_cache_keys(CacheTables ct, int cap) {
     unsigned long long *k = ct.keys[*ct.parity];
@@ -1285,6 +1302,7 @@ void launch_contacts_and_islands(DevWorld &w, float dt, float, cudaStream_t s) {
     int nmax = w.n > w.max_manifolds ? w.n : w.max_manifolds;
     k_mark_no_constraint<<<grid_for(w.max_manifolds, 256), 256, 0, s>>>(w);
     k_contact_setup<<<grid_for(w.max_manifolds, 128, 16), 128, 0, s>>>(w, ct, dt);
+    k_removed_contacts<<<grid_for(w.cache_cap, 256), 256, 0, s>>>(w, ct);
     k_apply_wake<<<grid_for(w.n, 256), 256, 0, s>>>(w);
     k_uf_init<<<grid_for(w.n, 256), 256, 0, s>>>(w);
     k_uf_link<<<grid_for(w.max_manifolds, 256), 256, 0, s>>>(w);

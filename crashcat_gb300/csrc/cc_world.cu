@@ -5,6 +5,8 @@
 // Reference: createWorldSettings (src/world-settings.ts:224-264),
 // createWorld (src/world.ts:46-58), rigidBody.create (src/body/rigid-body.ts:
 // 390-434), updateWorld (src/update.ts:45-239).
+#include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -320,6 +322,8 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
     ALLOC(scratch_colour, w.max_manifolds);
     ALLOC(scratch_claim, (size_t)cap + (size_t)w.max_manifolds + 16);
     ALLOC(mid_list, cap);
+    ALLOC(contact_event, w.max_manifolds);
+    ALLOC(removed_keys, w.max_manifolds);
     ALLOC(body_local, cap);
 #undef ALLOC
     if ((r = cuda_ok(cudaStreamCreateWithFlags(&W->stream, cudaStreamNonBlocking))) != CC_OK ||
@@ -357,7 +361,8 @@ int cc_world_destroy(cc_world *W) {
                     w.island_fill_b, w.island_fill_c, w.inv_inertia_world, w.scan_tmp, w.ctr, w.scene,
                     w.node_world, w.epa_items, w.epa_packed, w.epa_scratch, w.epa_fallback, w.cache_keys[0], w.cache_keys[1], w.cache_recs[0],
                     w.cache_recs[1], w.cache_parity, w.root_flag, w.small_list, w.large_list, w.scratch_order,
-                    w.scratch_colour, w.scratch_claim, w.mid_list, w.body_local, W->d_state_rows};
+                    w.scratch_colour, w.scratch_claim, w.mid_list, w.body_local, w.contact_event,
+                    w.removed_keys, W->d_state_rows};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : W->adj.allocs)
@@ -811,6 +816,45 @@ int cc_world_profile_steps(cc_world *W, float dt, int32_t n_steps, float *stage_
     for (int k = 0; k < CC_PROFILE_STAGES; k++) stage_ms[k] = (float)(acc[k] / n_steps);
     for (int k = CC_PROFILE_STAGES; k < n_stages; k++) stage_ms[k] = 0.f;
     return st;
+}
+
+int cc_world_get_contact_events(cc_world *W, int32_t *out, int32_t capacity, int32_t *count) {
+    if (!W || !count || capacity < 0 || (capacity > 0 && !out)) return CC_ERR_INVALID;
+    DevWorld &w = W->w;
+    const DevCounters &c = W->last_ctr;
+    int nm = c.num_manifolds < w.max_manifolds ? c.num_manifolds : w.max_manifolds;
+    int nr = c.num_removed < w.max_manifolds ? c.num_removed : w.max_manifolds;
+    std::vector<int> ev((size_t)nm);
+    std::vector<Manifold> man((size_t)nm);
+    std::vector<unsigned long long> rk((size_t)nr);
+    if (nm > 0) {
+        CC_TRY(cudaMemcpyAsync(ev.data(), w.contact_event, sizeof(int) * nm, cudaMemcpyDeviceToHost, W->stream));
+        CC_TRY(cudaMemcpyAsync(man.data(), w.manifolds, sizeof(Manifold) * nm, cudaMemcpyDeviceToHost, W->stream));
+    }
+    if (nr > 0)
+        CC_TRY(cudaMemcpyAsync(rk.data(), w.removed_keys, sizeof(unsigned long long) * nr, cudaMemcpyDeviceToHost,
+                               W->stream));
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    // (type, body A, body B) with A < B, sorted for a deterministic order
+    std::vector<std::array<int32_t, 3>> rows;
+    rows.reserve((size_t)nm + nr);
+    for (int i = 0; i < nm; i++) {
+        if (ev[i] == 0) continue;
+        int a = man[i].a, b = man[i].b;
+        rows.push_back({ev[i], a < b ? a : b, a < b ? b : a});
+    }
+    for (int i = 0; i < nr; i++) rows.push_back({3, (int32_t)(rk[i] >> 32), (int32_t)(rk[i] & 0xffffffffu)});
+    std::sort(rows.begin(), rows.end());
+    *count = (int32_t)rows.size();
+    int32_t k = 0;
+    for (const auto &r : rows) {
+        if (k >= capacity) break;
+        out[3 * k] = r[0];
+        out[3 * k + 1] = r[1];
+        out[3 * k + 2] = r[2];
+        k++;
+    }
+    return (c.overflow & OVF_CACHE) || c.num_removed > w.max_manifolds ? CC_ERR_CAPACITY : CC_OK;
 }
 
 int cc_world_get_stats(cc_world *W, cc_stats *o) {

@@ -362,3 +362,22 @@ def capsules_on_floor(n: int = 16, seed: int = 51) -> Scene:
     b["linear_velocity"][idx] = rng.normal(scale=0.3, size=(n, 3)).astype(np.float32)
     b["friction"][idx] = 0.5
     return Scene("capsules_on_floor", b, dt=1.0 / 60.0, steps=1, seed=seed)
+
+
+def bouncing_spheres(n: int = 48, seed: int = 61) -> Scene:
+    """Spheres (restitution 0.6-0.9) dropped from 0.5-2 m above the floor, spaced apart:
+    every contact with the floor is added, persists for a few steps, and is removed when the
+    sphere bounces off, so the contact events of the listener cycle through all three kinds."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = blank_bodies(n + 1)
+    static_floor(b, 0, half=(40.0, 0.5, 40.0), friction=0.5)
+    idx = np.arange(1, n + 1)
+    r = rng.uniform(0.2, 0.5, size=n).astype(np.float32)
+    for k, i in enumerate(idx):
+        set_sphere(b, i, r[k])
+    side = int(math.ceil(math.sqrt(n)))
+    pos = np.stack([(np.arange(n) % side) * 3.0 - 10.0, r + rng.uniform(0.5, 2.0, n), (np.arange(n) // side) * 3.0 - 10.0], 1)
+    b["position"][idx] = pos.astype(np.float32)
+    b["restitution"][idx] = rng.uniform(0.6, 0.9, size=n).astype(np.float32)
+    b["allow_sleeping"][idx] = 0
+    return Scene("bouncing_spheres", b, dt=1.0 / 60.0, steps=120, seed=seed)

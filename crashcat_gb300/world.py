@@ -329,6 +329,17 @@ class GpuWorld:
                                                   _lib.ptr(gm)), "cc_world_rollout_grad")
         return loss, gv, gw, gm
 
+    def contact_events(self) -> np.ndarray:
+        """Contact events of the last step as rows (type 1 added / 2 persisted / 3 removed,
+        body A, body B), A < B, sorted (cc_world_get_contact_events)."""
+        cnt = C.c_int32(0)
+        self._lib.cc_world_get_contact_events(self.handle, None, 0, C.byref(cnt))
+        out = np.zeros((max(cnt.value, 1), 3), dtype=np.int32)
+        st = self._lib.cc_world_get_contact_events(self.handle, ptr(out), cnt.value, C.byref(cnt))
+        if st not in (_lib.CC_OK, _lib.CC_ERR_CAPACITY):
+            check(st, "cc_world_get_contact_events")
+        return out[: cnt.value]
+
     def stats(self) -> dict:
         s = _lib.Stats()
         check(self._lib.cc_world_get_stats(self.handle, C.byref(s)), "cc_world_get_stats")
@@ -410,12 +421,30 @@ def create_body(world: World, settings: RigidBodySettings) -> RigidBody:
     return b
 
 
+_EVENT_CALLBACKS = {1: "onContactAdded", 2: "onContactPersisted", 3: "onContactRemoved"}
+_UNSUPPORTED_CALLBACKS = ("onBodyPairValidate", "onContactValidate")
+
+
 def update_world(world: World, listener, time_step: float) -> None:
-    """updateWorld (update.ts:45): one step of every body in the world on the GPU."""
+    """updateWorld (update.ts:45): one step of every body in the world on the GPU.
+
+    A listener (listener.ts:23-99) may observe contacts: after the step its
+    onContactAdded / onContactPersisted / onContactRemoved are called with the two
+    RigidBody handles (ordered by id) for every event of the step, read from the
+    library's event buffer.  Callbacks that decide the step itself (onBodyPairValidate,
+    onContactValidate, edits of ContactSettings) cannot run inside kernels and are
+    rejected."""
     if listener is not None:
-        raise NotImplementedError("listener callbacks cannot run inside kernels; pass None")
+        for name in _UNSUPPORTED_CALLBACKS:
+            if getattr(listener, name, None) is not None:
+                raise NotImplementedError(f"{name} cannot run inside the GPU step")
     world._flush()
     st = world._gpu.step(time_step, 1)
     world._cache = None
     if st != _lib.CC_OK:
         check(st, "updateWorld")
+    if listener is not None and any(getattr(listener, n, None) for n in _EVENT_CALLBACKS.values()):
+        for kind, a, b in world._gpu.contact_events():
+            fn = getattr(listener, _EVENT_CALLBACKS[kind], None)
+            if fn is not None:
+                fn(world.bodies[a], world.bodies[b])

@@ -25,6 +25,8 @@
  *   cc_world_get_pairs         <- world.broadphase.pairs     src/broadphase/broadphase.ts:30-35
  *   cc_world_get_manifolds     <- contact manifolds handed to
  *                                 addContactConstraint        src/constraints/contact-constraints.ts:437
+ *   cc_world_get_contact_events <- Listener.onContactAdded / onContactPersisted /
+ *                                 onContactRemoved, as a post-step buffer  src/listener.ts:58-98
  *   cc_world_get_stats         <- (no counterpart: per-step counters)
  *   cc_status_string           <- assert() messages          src/utils/assert.ts:1-9
  */
@@ -169,6 +171,14 @@ int cc_world_get_pairs(cc_world *world, int32_t *out, int32_t capacity, int32_t 
 int cc_world_get_manifolds(cc_world *world, float *out, int32_t capacity, int32_t *count);
 
 int cc_world_get_stats(cc_world *world, cc_stats *out);
+
+/* Contact events of the last step, the event buffer that stands in for the listener
+ * callbacks onContactAdded / onContactPersisted / onContactRemoved (src/listener.ts:58-98;
+ * fired at src/constraints/contact-constraints.ts:494-499 and src/contacts.ts:305-307), which
+ * kernels cannot call.  3 ints per event: type (1 added, 2 persisted, 3 removed), body A,
+ * body B (body indices, A < B), sorted by (type, A, B).  *count is the number of events
+ * (more than capacity when out is too small). */
+int cc_world_get_contact_events(cc_world *world, int32_t *out, int32_t capacity, int32_t *count);
 
 /* Stage profiler with no reference counterpart: runs n_steps steps (eager
  * launches) with CUDA events between the stages and writes the mean

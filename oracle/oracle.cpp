@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <array>
 #include <map>
 #include <numeric>
 #include <tuple>
@@ -140,6 +141,9 @@ struct World {
     int64_t activeCount = 0;
     int nextSequence = 0;
     std::map<ContactKey, Contact> contacts;
+    // contact events of the last step: (type 1 added / 2 persisted / 3 removed, body index A, body index B)
+    // at the listener call sites (contact-constraints.ts:494-499, contacts.ts:305-307)
+    std::vector<std::array<int64_t, 3>> events;
     std::vector<ContactConstraint> constraints;
     std::vector<Island> islands;
     double prevDt = 0;
@@ -632,6 +636,7 @@ static bool add_contact_constraint(World &w, Body *A, Body *B, Manifold m, doubl
     ContactKey key{A->id, B->id, m.subA, m.subB};
     auto it = w.contacts.find(key);
     bool existing = it != w.contacts.end();
+    w.events.push_back({existing ? 2 : 1, A->id & 0xffffffffLL, B->id & 0xffffffffLL});
     Contact prev;
     if (existing) prev = it->second;
     Contact &c = w.contacts[key];
@@ -1087,6 +1092,7 @@ static void step(World &w, double dt) {
     w.manifolds.clear();
     w.manifoldBodies.clear();
     for (auto &kv : w.contacts) kv.second.processed = false;
+    w.events.clear();
     // accelerationIntegrationUpdate update.ts:245-319
     for (Body &b : w.bodies) {
         if (b.motion != DYNAMIC || b.sleeping) continue;
@@ -1132,10 +1138,12 @@ static void step(World &w, double dt) {
     }
     // destroyUnprocessedContacts contacts.ts:534-553
     for (auto it = w.contacts.begin(); it != w.contacts.end();) {
-        if (!it->second.processed)
+        if (!it->second.processed) {
+            w.events.push_back({3, it->second.idA & 0xffffffffLL, it->second.idB & 0xffffffffLL});
             it = w.contacts.erase(it);
-        else
+        } else {
             ++it;
+        }
     }
     if (dt > 0) {
         build_islands(w);
@@ -1372,6 +1380,14 @@ int orc_add_bodies(void *wp, const double *rows, int n) {
 }
 
 int orc_body_count(void *wp) { return (int)((World *)wp)->bodies.size(); }
+// Contact events of the last step, 3 int64 per event (type, body index A, body index B); returns the count.
+int orc_get_events(void *wp, int64_t *out, int cap) {
+    const World &w = *(World *)wp;
+    int n = (int)w.events.size();
+    for (int i = 0; i < n && i < cap; i++)
+        for (int k = 0; k < 3; k++) out[3 * i + k] = w.events[i][k];
+    return n;
+}
 void orc_set_coloured_order(void *wp, int on) { ((World *)wp)->colouredOrder = on != 0; }
 int orc_reordered_islands(void *wp) { return ((World *)wp)->reorderedIslands; }
 

@@ -54,6 +54,7 @@ def load():
         "orc_barycentric": ([dp, dp, dp, i32, C.c_double, dp], None),
         "orc_collide_pair": ([dp, dp, C.c_double, dp], i32),
         "orc_inverse_inertia": ([dp, dp], None),
+        "orc_get_events": ([vp, C.c_void_p, i32], i32),
     }
     for k, (a, r) in sig.items():
         f = getattr(lib, k)
@@ -183,6 +184,17 @@ class OracleWorld:
         o = np.zeros((self.n, 6), dtype=np.float64)
         self.lib.orc_get_aabbs(self.h, dptr(o))
         return o
+
+    def contact_events(self) -> dict:
+        """Contact events of the last step: {'added' | 'persisted' | 'removed': set of (a, b)}."""
+        n = self.lib.orc_get_events(self.h, None, 0)
+        out = np.zeros((max(n, 1), 3), dtype=np.int64)
+        self.lib.orc_get_events(self.h, C.c_void_p(out.ctypes.data), n)
+        names = {1: "added", 2: "persisted", 3: "removed"}
+        ev = {v: set() for v in names.values()}
+        for t, a, b in out[:n].tolist():
+            ev[names[t]].add((a, b))
+        return ev
 
     def manifolds(self) -> np.ndarray:
         n = self.lib.orc_manifold_count(self.h)

@@ -93,3 +93,8 @@ def test_static_query_checks_arguments_before_any_cuda_call(lib):
 def test_rollout_grad_checks_arguments_before_any_cuda_call(lib):
     t = (C.c_float * 3)()
     assert lib.cc_world_rollout_grad(None, C.c_float(0.01), 10, 5, t, None, None, None, None) == _lib.CC_ERR_INVALID
+
+
+def test_contact_events_check_arguments(lib):
+    cnt = C.c_int32(0)
+    assert lib.cc_world_get_contact_events(None, None, 0, C.byref(cnt)) == _lib.CC_ERR_INVALID
