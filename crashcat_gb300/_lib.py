@@ -101,8 +101,47 @@ EXPORTS = {
     "cc_world_rollout_grad": ([C.c_void_p, C.c_float, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_void_p], C.c_int),
     "cc_penetration_static": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_float, C.c_float, C.c_void_p], C.c_int),
+    "cc_world_add_hinges": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
+    "cc_world_set_hinge_limits": ([C.c_void_p, C.c_int32, C.c_float, C.c_float], C.c_int),
+    "cc_world_set_hinge_motor": ([C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_float], C.c_int),
+    "cc_world_set_hinge_enabled": ([C.c_void_p, C.c_int32, C.c_int32], C.c_int),
+    "cc_world_get_hinge_angles": ([C.c_void_p, C.c_void_p, C.c_int32], C.c_int),
+    "cc_world_set_skip_joint_pairs": ([C.c_void_p, C.c_int32], C.c_int),
     "cc_status_string": ([C.c_int], C.c_char_p),
 }
+
+# cc_hinge_desc (4-byte fields only) and its enums
+SPACE_WORLD, SPACE_LOCAL = 0, 1
+SPRING_FREQUENCY_AND_DAMPING, SPRING_STIFFNESS_AND_DAMPING = 0, 1
+MOTOR_OFF, MOTOR_VELOCITY, MOTOR_POSITION = 0, 1, 2
+SPRING_DTYPE = np.dtype([("mode", np.int32), ("frequency_or_stiffness", np.float32), ("damping", np.float32)])
+HINGE_DTYPE = np.dtype([
+    ("body_a", np.int32), ("body_b", np.int32), ("space", np.int32),
+    ("point_a", np.float32, 3), ("point_b", np.float32, 3),
+    ("hinge_axis_a", np.float32, 3), ("hinge_axis_b", np.float32, 3),
+    ("normal_axis_a", np.float32, 3), ("normal_axis_b", np.float32, 3),
+    ("limits_min", np.float32), ("limits_max", np.float32), ("limits_spring", SPRING_DTYPE),
+    ("max_friction_torque", np.float32), ("motor_state", np.int32),
+    ("target_angular_velocity", np.float32), ("target_angle", np.float32), ("motor_spring", SPRING_DTYPE),
+    ("min_torque_limit", np.float32), ("max_torque_limit", np.float32),
+    ("priority", np.int32), ("enabled", np.int32),
+])
+
+
+def hinge_defaults(n: int) -> np.ndarray:
+    """n hinge records with hingeConstraint.create's defaults (hinge-constraint.ts:240-387):
+    no limits, rigid limit spring, motor off, position-motor spring 2 Hz / damping 1,
+    unbounded motor torque, priority 0, enabled."""
+    h = np.zeros(n, HINGE_DTYPE)
+    h["limits_min"] = -np.pi
+    h["limits_max"] = np.pi
+    h["motor_spring"]["frequency_or_stiffness"] = 2.0
+    h["motor_spring"]["damping"] = 1.0
+    h["min_torque_limit"] = -np.inf
+    h["max_torque_limit"] = np.inf
+    h["enabled"] = 1
+    return h
+
 
 # cc_penetration_static limits and record layouts (numpy mirrors of the C structs)
 STATIC_MAX_QUERIES = 32768

@@ -376,6 +376,14 @@ __global__ void __launch_bounds__(128) k_find_pairs(DevWorld w, const int2 *node
                 if (!(fa & F_KIN_VS_NONDYN) && !(fb & F_KIN_VS_NONDYN) && amotion != DYNAMIC && bmotion != DYNAMIC &&
                     !(amotion == KINEMATIC && (fb & F_SENSOR)) && !(bmotion == KINEMATIC && (fa & F_SENSOR)))
                     continue;
+                // bodies that share an enabled joint: the declarative form of an onBodyPairValidate
+                // that rejects them (broadphase.ts:112-123)
+                if (w.skip_joint_pairs) {
+                    const int *jp = w.joint_partners + (size_t)i * JOINT_PARTNERS;
+                    bool joined = false;
+                    for (int k = 0; k < JOINT_PARTNERS; k++) joined |= jp[k] == b;
+                    if (joined) continue;
+                }
                 if (cnt == PAIR_BUF) {
                     flush_pairs(w, buf, cnt);
                     cnt = 0;

@@ -166,6 +166,38 @@ struct AdjBuffers {
     float dt;
 };
 
+// Hinge joint (src/constraints/hinge-constraint.ts) with the state of its constraint parts:
+// point (point-constraint-part.ts), hinge rotation (hinge-rotation-constraint-part.ts), and
+// the limit and motor angle parts (angle-constraint-part.ts, spring-part.ts).
+enum : int { JF_ENABLED = 1, JF_LIMITS = 2 };
+struct DevHinge {
+    int a, b, priority, index;
+    int flags, motor_state, limits_spring_mode, motor_spring_mode;
+    int island;                 // island of this step (-1: in none)
+    float3 lp1, lp2, lh1, lh2;  // attachment points (from the centre of mass) and hinge axes, body space
+    float4 inv_initial;         // inverse initial relative orientation
+    float limits_min, limits_max, limits_freq, limits_damping;
+    float max_friction_torque, target_angular_velocity, target_angle;
+    float motor_freq, motor_damping, min_torque, max_torque;
+    // per-step state
+    float theta;
+    float3 wh1;  // world hinge axis of body A
+    // point part
+    float3 r1, r2;
+    float invI1_r1X[9], invI2_r2X[9], p_eff[9];  // row-major 3x3
+    float3 p_lambda;
+    int p_active;
+    // hinge rotation part
+    float3 a1, b2, c2, b2xA1, c2xA1;
+    float invI1[6], invI2[6];  // symmetric xx xy xz yy yz zz
+    float r_eff[4], r_lambda[2];
+    // limit and motor angle parts
+    float3 l_i1, l_i2;
+    float l_eff, l_soft, l_bias, l_lambda;
+    float3 m_i1, m_i2;
+    float m_eff, m_soft, m_bias, m_lambda;
+};
+
 // impulse adjoints handed from one step's reverse to the previous step's, keyed by body pair
 struct AdjHandoff {
     unsigned long long *keys;  // cache_cap entries, EMPTY_KEY when free
@@ -250,6 +282,14 @@ struct DevWorld {
     int *contact_event;               // per manifold: 1 added, 2 persisted (listener.ts:58-79)
     unsigned long long *removed_keys;  // pairs in contact last step but not this step
     int *mid_list;    // islands solved by one warp each
+    // hinge joints and their island lists
+    DevHinge *hinges;
+    int num_hinges, max_hinges;
+    int skip_joint_pairs;              // broadphase skips body pairs that share an enabled joint
+    int *joint_partners;               // JOINT_PARTNERS per body: other bodies joined to it (-1: none)
+    int *island_joint_count, *island_joint_off, *island_fill_j;
+    int *island_joints;  // 3 x max_hinges: as scattered | by index | by (priority, index)
+    int *joint_wake;     // flag: some joint has to wake a body this step
     int *body_local;  // index of a body inside its island's body list (per-warp solve)
 };
 
@@ -374,6 +414,7 @@ size_t epa_item_bytes();
 constexpr int EPA_DEFAULT_MAX_THREADS = NUM_SMS * 4 * 64;  // one EPA polytope per resident EPA thread
 constexpr int EPA_MAX_THREADS = NUM_SMS * 8 * 64;          // upper bound of the launch-shape override
 constexpr int EPA_BIG_THREADS = 1024;  // threads of the fallback pass with the reference's polytope limits
+constexpr int JOINT_PARTNERS = 8;      // joined bodies remembered per body for the broadphase pair filter
 
 // scan / sort utilities (cc_scan.cu)
 void exclusive_scan_int(const int *in, int *out, int n, int *total, int *tmp, cudaStream_t s);

@@ -362,29 +362,39 @@ __global__ void k_uf_init(DevWorld w) {
         w.island_cons_count[i] = 0;
         w.island_fill_b[i] = 0;
         w.island_fill_c[i] = 0;
+        if (w.island_joint_count) {
+            w.island_joint_count[i] = 0;
+            w.island_fill_j[i] = 0;
+        }
     }
 }
 
+// union of the sets of two bodies (bounded retry; gives up with an overflow flag)
+__device__ void uf_union(DevWorld &w, int a, int b) {
+    for (int guard = 0; guard < 1 << 20; guard++) {
+        int ra = uf_find(w.uf_parent, a), rb = uf_find(w.uf_parent, b);
+        if (ra == rb) return;
+        int hi = max(ra, rb), lo = min(ra, rb);
+        if (atomicCAS(&w.uf_parent[hi], hi, lo) == hi) return;
+    }
+    atomicOr(&w.ctr->overflow, OVF_ISLAND);  // bounded retry gave up: report it
+}
+
+// contacts between active bodies (islands.ts:103-140) and enabled joints between
+// active bodies (linkUserConstraints islands.ts:209-224) join their bodies' islands
 __global__ void k_uf_link(DevWorld w) {
     int nm = min(w.ctr->num_manifolds, w.max_manifolds);
     for (int ci = blockIdx.x * blockDim.x + threadIdx.x; ci < nm; ci += gridDim.x * blockDim.x) {
         if (w.cons_of_manifold[ci] < 0) continue;
         int a = w.cons[ci].a, b = w.cons[ci].b;
         if (!active_body(w.flags[a]) || !active_body(w.flags[b])) continue;
-        bool linked = false;
-        for (int guard = 0; guard < 1 << 20; guard++) {
-            int ra = uf_find(w.uf_parent, a), rb = uf_find(w.uf_parent, b);
-            if (ra == rb) {
-                linked = true;
-                break;
-            }
-            int hi = max(ra, rb), lo = min(ra, rb);
-            if (atomicCAS(&w.uf_parent[hi], hi, lo) == hi) {
-                linked = true;
-                break;
-            }
-        }
-        if (!linked) atomicOr(&w.ctr->overflow, OVF_ISLAND);  // bounded retry gave up: report it
+        uf_union(w, a, b);
+    }
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < w.num_hinges; j += gridDim.x * blockDim.x) {
+        const DevHinge &h = w.hinges[j];
+        if (!(h.flags & JF_ENABLED)) continue;
+        if (!active_body(w.flags[h.a]) || !active_body(w.flags[h.b])) continue;
+        uf_union(w, h.a, h.b);
     }
 }
 
@@ -414,6 +424,20 @@ __global__ void k_island_count(DevWorld w, const int *island_id_of_root) {
         w.cons[ci].island = isl;
         if (isl >= 0) atomicAdd(&w.island_cons_count[isl], 1);
     }
+    // a joint belongs to the island of its lower active body (islands.ts:163-178, 318-332)
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < w.num_hinges; j += gridDim.x * blockDim.x) {
+        DevHinge &h = w.hinges[j];
+        int isl = -1;
+        if (h.flags & JF_ENABLED) {
+            bool aa = active_body(w.flags[h.a]), ab = active_body(w.flags[h.b]);
+            if (aa || ab) {
+                int r = w.uf_parent[aa ? h.a : h.b];
+                isl = r >= 0 ? island_id_of_root[r] : -1;
+            }
+        }
+        h.island = isl;
+        if (isl >= 0) atomicAdd(&w.island_joint_count[isl], 1);
+    }
 }
 
 __global__ void k_island_scatter(DevWorld w) {
@@ -431,6 +455,12 @@ __global__ void k_island_scatter(DevWorld w) {
         int k = atomicAdd(&w.island_fill_c[isl], 1);
         w.island_cons[w.island_cons_off[isl] + k] = ci;
     }
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < w.num_hinges; j += gridDim.x * blockDim.x) {
+        int isl = w.hinges[j].island;
+        if (isl < 0) continue;
+        int k = atomicAdd(&w.island_fill_j[isl], 1);
+        w.island_joints[w.island_joint_off[isl] + k] = j;
+    }
 }
 
 // split islands into the per-thread and per-CTA classes
@@ -438,8 +468,12 @@ __global__ void k_island_classify(DevWorld w, int *small_list, int *large_list) 
     int ni = w.ctr->num_islands;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x) {
         int nc = w.island_cons_count[i], nb = w.island_body_count[i];
-        atomicMax(&w.ctr->max_island_constraints, nc);
-        if (nc <= c_settings.small_island_max_cons && nb <= SMALL_ISLAND_MAX_BODIES) {
+        int nj = w.num_hinges > 0 ? w.island_joint_count[i] : 0;
+        atomicMax(&w.ctr->max_island_constraints, nc + nj);
+        if (nj > 0) {  // islands with joints: the per-CTA solve, joints by one thread in the reference's order
+            int k = atomicAdd(&w.ctr->num_large_islands, 1);
+            large_list[k] = i;
+        } else if (nc <= c_settings.small_island_max_cons && nb <= SMALL_ISLAND_MAX_BODIES) {
             int k = atomicAdd(&w.ctr->num_small_islands, 1);
             small_list[k] = i;
         } else if (nc <= WARP_MAX_CONS && nb <= WARP_MAX_BODIES) {
@@ -711,6 +745,50 @@ __device__ void store_impulses(DevWorld &w, CacheRecord *crecs, const ContactCon
     }
 }
 
+#include "cc_joints.cuh"
+
+// wakeBodiesInUserConstraints (update.ts:853-888): an enabled joint with an awake body
+// wakes its sleeping dynamic body.  The reference walks the joints in order, so a wake can
+// run down a chain within one step; the scan finds whether any joint has work, and only
+// then one thread walks them in order (joints of different worlds never share a body).
+__device__ __forceinline__ bool joint_wakes(const DevWorld &w, const DevHinge &h) {
+    if (!(h.flags & JF_ENABLED)) return false;
+    uint32_t fa = w.flags[h.a], fb = w.flags[h.b];
+    bool act = !sleeping_of(fa) || !sleeping_of(fb);
+    bool dyn = motion_of(fa) == DYNAMIC || motion_of(fb) == DYNAMIC;
+    return act && dyn && ((sleeping_of(fa) && motion_of(fa) == DYNAMIC) || (sleeping_of(fb) && motion_of(fb) == DYNAMIC));
+}
+__global__ void k_joint_wake_scan(DevWorld w) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < w.num_hinges; j += gridDim.x * blockDim.x)
+        if (joint_wakes(w, w.hinges[j])) *w.joint_wake = 1;
+}
+__global__ void k_joint_wake_serial(DevWorld w) {
+    if (!*w.joint_wake) return;
+    *w.joint_wake = 0;
+    for (int j = 0; j < w.num_hinges; j++) {
+        const DevHinge &h = w.hinges[j];
+        if (!joint_wakes(w, h)) continue;
+        int ids[2] = {h.a, h.b};
+        for (int k = 0; k < 2; k++) {
+            int i = ids[k];
+            uint32_t f = w.flags[i];
+            if (!(sleeping_of(f) && motion_of(f) == DYNAMIC)) continue;
+            w.flags[i] = f & ~F_SLEEPING;
+            reset_sleep(w, i);
+        }
+    }
+}
+// setupVelocityConstraints (constraints.ts:276-287) for every enabled joint with an awake
+// body (updateSleeping constraints.ts:264-274)
+__global__ void k_joint_setup(DevWorld w, float dt) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < w.num_hinges; j += gridDim.x * blockDim.x) {
+        DevHinge h = w.hinges[j];
+        if (!hinge_active(w, h)) continue;
+        hinge_setup(w, h, dt);
+        w.hinges[j] = h;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // small islands: one thread runs the island in the reference's exact order
 // ---------------------------------------------------------------------------
@@ -829,6 +907,25 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
             order[rank] = cl[k];
         }
         for (int k = threadIdx.x; k < nb; k += blockDim.x) prepare_body(w, bl[k]);
+        // the island's joints in index order (warm start) and in (priority, index) order
+        // (sortConstraintIds constraints.ts:248-261)
+        int nj = w.num_hinges > 0 ? w.island_joint_count[isl] : 0;
+        const int *jl = w.island_joints + (nj > 0 ? w.island_joint_off[isl] : 0);
+        int *j_idx = const_cast<int *>(jl) + w.max_hinges;
+        int *j_pri = j_idx + w.max_hinges;
+        for (int k = threadIdx.x; k < nj; k += blockDim.x) {
+            int jk = jl[k];
+            int pk = w.hinges[jk].priority;
+            int r1 = 0, r2 = 0;
+            for (int m = 0; m < nj; m++) {
+                int jm = jl[m];
+                int pm = w.hinges[jm].priority;
+                r1 += jm < jk;
+                r2 += (pm < pk || (pm == pk && jm < jk));
+            }
+            j_idx[r1] = jk;
+            j_pri[r2] = jk;
+        }
         __syncthreads();
         // greedy colouring in rank order: per round, the lowest rank claims each dynamic body
         for (int k = threadIdx.x; k < nc; k += blockDim.x) colour[k] = -1;
@@ -930,8 +1027,25 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
                 __syncthreads();
             }
         };
-        if (c_settings.warm_starting) sweep(0);
-        for (int it = 0; it < c_settings.vel_iters; it++) sweep(1);
+        // contacts, then joints (update.ts:116-165)
+        if (c_settings.warm_starting) {
+            sweep(0);
+            if (nj > 0) {
+                __syncthreads();
+                if (threadIdx.x == 0)
+                    for (int k = 0; k < nj; k++) hinge_warm(w, w.hinges[j_idx[k]], ratio);
+                __syncthreads();
+            }
+        }
+        for (int it = 0; it < c_settings.vel_iters; it++) {
+            sweep(1);
+            if (nj > 0) {
+                __syncthreads();
+                if (threadIdx.x == 0)
+                    for (int k = 0; k < nj; k++) hinge_solve_velocity(w, w.hinges[j_pri[k]], dt);
+                __syncthreads();
+            }
+        }
         for (int k = threadIdx.x; k < nc; k += blockDim.x) store_impulses(w, crecs, w.cons[cl[k]]);
         for (int k = threadIdx.x; k < nb; k += blockDim.x) integrate_body(w, bl[k], dt);
         __syncthreads();
@@ -962,6 +1076,15 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
                         }
                         s_any = 1;
                     }
+                }
+                __syncthreads();
+            }
+            if (nj > 0) {
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    bool applied = false;
+                    for (int k = 0; k < nj; k++) applied = hinge_solve_position(w, w.hinges[j_pri[k]], dt) || applied;
+                    if (applied) s_any = 1;
                 }
                 __syncthreads();
             }
@@ -1304,6 +1427,10 @@ void launch_contacts_and_islands(DevWorld &w, float dt, float, cudaStream_t s) {
     k_contact_setup<<<grid_for(w.max_manifolds, 128, 16), 128, 0, s>>>(w, ct, dt);
     k_removed_contacts<<<grid_for(w.cache_cap, 256), 256, 0, s>>>(w, ct);
     k_apply_wake<<<grid_for(w.n, 256), 256, 0, s>>>(w);
+    if (w.num_hinges > 0 && dt > 0.f) {
+        k_joint_wake_scan<<<grid_for(w.num_hinges, 256), 256, 0, s>>>(w);
+        k_joint_wake_serial<<<1, 1, 0, s>>>(w);
+    }
     k_uf_init<<<grid_for(w.n, 256), 256, 0, s>>>(w);
     k_uf_link<<<grid_for(w.max_manifolds, 256), 256, 0, s>>>(w);
     k_uf_roots<<<grid_for(w.n, 256), 256, 0, s>>>(w, w.root_flag);
@@ -1311,8 +1438,10 @@ void launch_contacts_and_islands(DevWorld &w, float dt, float, cudaStream_t s) {
     k_island_count<<<grid_for(nmax, 256), 256, 0, s>>>(w, w.island_id_of_root);
     exclusive_scan_int(w.island_body_count, w.island_body_off, w.n, nullptr, w.scan_tmp, s);
     exclusive_scan_int(w.island_cons_count, w.island_cons_off, w.n, nullptr, w.scan_tmp, s);
+    if (w.num_hinges > 0) exclusive_scan_int(w.island_joint_count, w.island_joint_off, w.n, nullptr, w.scan_tmp, s);
     k_island_scatter<<<grid_for(nmax, 256), 256, 0, s>>>(w);
     k_island_classify<<<grid_for(w.n, 256), 256, 0, s>>>(w, w.small_list, w.large_list);
+    if (w.num_hinges > 0 && dt > 0.f) k_joint_setup<<<grid_for(w.num_hinges, 128), 128, 0, s>>>(w, dt);
 }
 
 void launch_solver(DevWorld &w, float dt, float ratio, cudaStream_t s, cudaEvent_t mid) {

@@ -31,6 +31,7 @@ struct cc_world {
     int last_status = CC_OK;
     DevCounters last_ctr{};
     std::vector<uint64_t> ids;
+    std::vector<DevHinge> hinges;  // host copy of each joint as created (bodies, flags, limits, motor)
     float *d_state_rows = nullptr;  // 16 floats per body staging for get/set state
     float *h_pinned_rows = nullptr;
     DevCounters *h_ctr = nullptr;   // pinned mirror of the device counters
@@ -70,6 +71,19 @@ static int dalloc(T **p, size_t count) {
     cudaError_t e = cudaMalloc((void **)p, sizeof(T) * count);
     if (e != cudaSuccess) return cuda_ok(e);
     return cuda_ok(cudaMemset(*p, 0, sizeof(T) * count));
+}
+
+// the captured step graph holds the device world by value: drop it when a count or a
+// buffer changes
+static void drop_graph(cc_world *W) {
+    if (W->graph_exec) {
+        cudaGraphExecDestroy(W->graph_exec);
+        W->graph_exec = nullptr;
+    }
+    if (W->graph) {
+        cudaGraphDestroy(W->graph);
+        W->graph = nullptr;
+    }
 }
 
 static int next_pow2(int v) {
@@ -362,7 +376,8 @@ int cc_world_destroy(cc_world *W) {
                     w.node_world, w.epa_items, w.epa_packed, w.epa_scratch, w.epa_fallback, w.cache_keys[0], w.cache_keys[1], w.cache_recs[0],
                     w.cache_recs[1], w.cache_parity, w.root_flag, w.small_list, w.large_list, w.scratch_order,
                     w.scratch_colour, w.scratch_claim, w.mid_list, w.body_local, w.contact_event,
-                    w.removed_keys, W->d_state_rows};
+                    w.removed_keys, W->d_state_rows, w.hinges, w.island_joints, w.island_joint_count,
+                    w.island_joint_off, w.island_fill_j, w.joint_wake, w.joint_partners};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : W->adj.allocs)
@@ -518,15 +533,7 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
     CC_TRY(cudaMemcpyAsync(w.sleep_timer + o, timer.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
     CC_TRY(cudaStreamSynchronize(s));
     w.n += n;
-    // body count changed: the captured step graph no longer matches
-    if (W->graph_exec) {
-        cudaGraphExecDestroy(W->graph_exec);
-        W->graph_exec = nullptr;
-    }
-    if (W->graph) {
-        cudaGraphDestroy(W->graph);
-        W->graph = nullptr;
-    }
+    drop_graph(W);  // body count changed: the captured step graph no longer matches
     return CC_OK;
 }
 
@@ -977,6 +984,7 @@ extern "C" int cc_world_rollout_grad(cc_world *W, float dt, int32_t n_steps, int
     if (!W || !targets || n_steps <= 0 || checkpoint_every <= 0 || !(dt > 0.f)) return CC_ERR_INVALID;
     DevWorld &w = W->w;
     if (w.n == 0) return CC_ERR_INVALID;
+    if (w.num_hinges > 0) return CC_ERR_UNSUPPORTED;  // the adjoint covers contacts only
     int K = checkpoint_every < n_steps ? checkpoint_every : n_steps;
     int nseg = (n_steps + K - 1) / K;
     int r = ensure_adjoint(W, K, nseg + 1);
@@ -1046,3 +1054,308 @@ extern "C" int cc_world_rollout_grad(cc_world *W, float dt, int32_t n_steps, int
     W->last_ctr = *W->h_ctr;
     return CC_OK;
 }
+
+// ---------------------------------------------------------------------------
+// hinge joints: creation in FP64 from the bodies' current poses
+// (hingeConstraint.create hinge-constraint.ts:240-387) and the setters
+// ---------------------------------------------------------------------------
+namespace {
+struct D3 {
+    double x, y, z;
+};
+struct DQ {
+    double x, y, z, w;
+};
+D3 d3(const float *v) { return {v[0], v[1], v[2]}; }
+D3 d3(float4 v) { return {v.x, v.y, v.z}; }
+D3 dsub(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+D3 dcross(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+D3 dnormalize(D3 a) {  // vec3.normalize: a zero vector stays zero
+    double l = a.x * a.x + a.y * a.y + a.z * a.z;
+    if (l > 0) l = 1.0 / std::sqrt(l);
+    return {a.x * l, a.y * l, a.z * l};
+}
+DQ dq(float4 q) { return {q.x, q.y, q.z, q.w}; }
+DQ dconj(DQ q) { return {-q.x, -q.y, -q.z, q.w}; }
+DQ dqmul(DQ a, DQ b) {
+    return {a.x * b.w + a.w * b.x + a.y * b.z - a.z * b.y, a.y * b.w + a.w * b.y + a.z * b.x - a.x * b.z,
+            a.z * b.w + a.w * b.z + a.x * b.y - a.y * b.x, a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z};
+}
+D3 drot(DQ q, D3 v) {  // q v q^-1 for a unit quaternion
+    D3 u{q.x, q.y, q.z};
+    D3 t = dcross(u, v);
+    t = {2 * t.x, 2 * t.y, 2 * t.z};
+    D3 c = dcross(u, t);
+    return {v.x + q.w * t.x + c.x, v.y + q.w * t.y + c.y, v.z + q.w * t.z + c.z};
+}
+// rotation quaternion of the 3x3 matrix with columns c0 c1 c2 (Shoemake's method, as quat.fromMat3)
+DQ quat_from_columns(D3 c0, D3 c1, D3 c2) {
+    double m[3][3] = {{c0.x, c1.x, c2.x}, {c0.y, c1.y, c2.y}, {c0.z, c1.z, c2.z}};  // m[row][col]
+    double tr = m[0][0] + m[1][1] + m[2][2];
+    DQ o;
+    if (tr > 0.0) {
+        double r = std::sqrt(tr + 1.0);
+        o.w = 0.5 * r;
+        r = 0.5 / r;
+        o.x = (m[2][1] - m[1][2]) * r;
+        o.y = (m[0][2] - m[2][0]) * r;
+        o.z = (m[1][0] - m[0][1]) * r;
+        return o;
+    }
+    int i = 0;
+    if (m[1][1] > m[0][0]) i = 1;
+    if (m[2][2] > m[i][i]) i = 2;
+    int j = (i + 1) % 3, k = (i + 2) % 3;
+    double q[3];
+    double r = std::sqrt(m[i][i] - m[j][j] - m[k][k] + 1.0);
+    q[i] = 0.5 * r;
+    r = 0.5 / r;
+    o.w = (m[k][j] - m[j][k]) * r;
+    q[j] = (m[j][i] + m[i][j]) * r;
+    q[k] = (m[k][i] + m[i][k]) * r;
+    o.x = q[0];
+    o.y = q[1];
+    o.z = q[2];
+    return o;
+}
+// getInvInitialOrientationXZ (hinge-constraint.ts:166-205)
+DQ inv_initial_orientation_xz(D3 n1, D3 h1, D3 n2, D3 h2) {
+    const double eps = 1e-6;
+    if (std::fabs(n1.x - n2.x) < eps && std::fabs(n1.y - n2.y) < eps && std::fabs(n1.z - n2.z) < eps &&
+        std::fabs(h1.x - h2.x) < eps && std::fabs(h1.y - h2.y) < eps && std::fabs(h1.z - h2.z) < eps)
+        return {0, 0, 0, 1};
+    DQ q1 = quat_from_columns(n1, dcross(h1, n1), h1), q2 = quat_from_columns(n2, dcross(h2, n2), h2);
+    return dqmul(q2, dconj(q1));
+}
+float3 f3d(D3 v) { return make_float3((float)v.x, (float)v.y, (float)v.z); }
+bool finite3(const float *v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+bool spring_ok(const cc_spring_settings &s) {
+    return (s.mode == 0 || s.mode == 1) && std::isfinite(s.frequency_or_stiffness) && std::isfinite(s.damping);
+}
+}  // namespace
+
+// grow the joint arrays (and create the per-island joint lists on first use)
+static int ensure_hinge_capacity(cc_world *W, int need) {
+    DevWorld &w = W->w;
+    if (!w.island_joint_count) {
+        int r;
+        if ((r = dalloc(&w.island_joint_count, w.cap)) != CC_OK || (r = dalloc(&w.island_joint_off, w.cap)) != CC_OK ||
+            (r = dalloc(&w.island_fill_j, w.cap)) != CC_OK || (r = dalloc(&w.joint_wake, 1)) != CC_OK ||
+            (r = dalloc(&w.joint_partners, (size_t)w.cap * JOINT_PARTNERS)) != CC_OK)
+            return r;
+        CC_TRY(cudaMemset(w.joint_partners, 0xff, sizeof(int) * (size_t)w.cap * JOINT_PARTNERS));
+    }
+    if (need <= w.max_hinges) return CC_OK;
+    int cap = std::max(need, std::max(64, 2 * w.max_hinges));
+    DevHinge *nh = nullptr;
+    int *nl = nullptr;
+    int r;
+    if ((r = dalloc(&nh, cap)) != CC_OK) return r;
+    if ((r = dalloc(&nl, 3 * (size_t)cap)) != CC_OK) {
+        cudaFree(nh);
+        return r;
+    }
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    if (w.num_hinges > 0) CC_TRY(cudaMemcpy(nh, w.hinges, sizeof(DevHinge) * w.num_hinges, cudaMemcpyDeviceToDevice));
+    if (w.hinges) cudaFree(w.hinges);
+    if (w.island_joints) cudaFree(w.island_joints);
+    w.hinges = nh;
+    w.island_joints = nl;
+    w.max_hinges = cap;
+    drop_graph(W);
+    return CC_OK;
+}
+
+// partner lists of the broadphase joint-pair filter, from the enabled joints
+static int upload_partners(cc_world *W) {
+    DevWorld &w = W->w;
+    if (!w.joint_partners) return CC_OK;
+    std::vector<int> part((size_t)w.cap * JOINT_PARTNERS, -1);
+    bool over = false;
+    auto add = [&](int a, int b) {
+        int *p = part.data() + (size_t)a * JOINT_PARTNERS;
+        for (int k = 0; k < JOINT_PARTNERS; k++) {
+            if (p[k] == b) return;
+            if (p[k] < 0) {
+                p[k] = b;
+                return;
+            }
+        }
+        over = true;
+    };
+    for (const DevHinge &h : W->hinges) {
+        if (!(h.flags & JF_ENABLED)) continue;
+        add(h.a, h.b);
+        add(h.b, h.a);
+    }
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    CC_TRY(cudaMemcpy(w.joint_partners, part.data(), sizeof(int) * part.size(), cudaMemcpyHostToDevice));
+    return over && w.skip_joint_pairs ? CC_ERR_CAPACITY : CC_OK;
+}
+
+extern "C" {
+
+int cc_world_add_hinges(cc_world *W, const cc_hinge_desc *d, int32_t n, int32_t *out_index) {
+    if (!W || (!d && n > 0) || n < 0) return CC_ERR_INVALID;
+    if (n == 0) return CC_OK;
+    DevWorld &w = W->w;
+    for (int i = 0; i < n; i++) {
+        const cc_hinge_desc &h = d[i];
+        if (h.body_a < 0 || h.body_b < 0 || h.body_a >= w.n || h.body_b >= w.n) return CC_ERR_INVALID;
+        if (h.space != CC_SPACE_WORLD && h.space != CC_SPACE_LOCAL) return CC_ERR_INVALID;
+        if (h.motor_state < 0 || h.motor_state > 2) return CC_ERR_INVALID;
+        if (!spring_ok(h.limits_spring) || !spring_ok(h.motor_spring)) return CC_ERR_INVALID;
+        if (!finite3(h.point_a) || !finite3(h.point_b) || !finite3(h.hinge_axis_a) || !finite3(h.hinge_axis_b) ||
+            !finite3(h.normal_axis_a) || !finite3(h.normal_axis_b))
+            return CC_ERR_INVALID;
+        if (std::isnan(h.limits_min) || std::isnan(h.limits_max) || std::isnan(h.max_friction_torque) ||
+            std::isnan(h.min_torque_limit) || std::isnan(h.max_torque_limit) ||
+            !std::isfinite(h.target_angular_velocity) || !std::isfinite(h.target_angle))
+            return CC_ERR_INVALID;
+    }
+    // current poses and worlds of the bodies
+    std::vector<float4> quat((size_t)w.n), com((size_t)w.n);
+    std::vector<int> world((size_t)w.n);
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    CC_TRY(cudaMemcpy(quat.data(), w.quat, sizeof(float4) * w.n, cudaMemcpyDeviceToHost));
+    CC_TRY(cudaMemcpy(com.data(), w.com, sizeof(float4) * w.n, cudaMemcpyDeviceToHost));
+    CC_TRY(cudaMemcpy(world.data(), w.world, sizeof(int) * w.n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; i++)
+        if (world[d[i].body_a] != world[d[i].body_b]) return CC_ERR_INVALID;
+    std::vector<DevHinge> made((size_t)n);
+    const double PI = 3.14159265358979323846;
+    for (int i = 0; i < n; i++) {
+        const cc_hinge_desc &h = d[i];
+        DevHinge j;
+        memset(&j, 0, sizeof(j));
+        j.a = h.body_a;
+        j.b = h.body_b;
+        j.index = w.num_hinges + i;
+        j.priority = h.priority;
+        j.island = -1;
+        DQ qa = dq(quat[j.a]), qb = dq(quat[j.b]);
+        D3 h1 = dnormalize(d3(h.hinge_axis_a)), h2 = dnormalize(d3(h.hinge_axis_b));
+        D3 n1 = dnormalize(d3(h.normal_axis_a)), n2 = dnormalize(d3(h.normal_axis_b));
+        DQ inv_initial;
+        if (h.space == CC_SPACE_WORLD) {
+            DQ iqa = dconj(qa), iqb = dconj(qb);
+            j.lp1 = f3d(drot(iqa, dsub(d3(h.point_a), d3(com[j.a]))));
+            j.lp2 = f3d(drot(iqb, dsub(d3(h.point_b), d3(com[j.b]))));
+            j.lh1 = f3d(drot(iqa, h1));
+            j.lh2 = f3d(drot(iqb, h2));
+            DQ r0 = inv_initial_orientation_xz(n1, h1, n2, h2);
+            inv_initial = dqmul(dqmul(iqb, r0), qa);
+        } else {
+            j.lp1 = f3d(d3(h.point_a));
+            j.lp2 = f3d(d3(h.point_b));
+            j.lh1 = f3d(h1);
+            j.lh2 = f3d(h2);
+            inv_initial = inv_initial_orientation_xz(drot(qa, n1), drot(qa, h1), drot(qb, n2), drot(qb, h2));
+        }
+        j.inv_initial = make_float4((float)inv_initial.x, (float)inv_initial.y, (float)inv_initial.z,
+                                    (float)inv_initial.w);
+        double mn = h.limits_min, mx = h.limits_max;
+        bool has_limits = !(mn <= -PI && mx >= PI);
+        j.limits_min = has_limits ? (float)std::max(mn, -PI) : (float)-PI;
+        j.limits_max = has_limits ? (float)std::min(mx, PI) : (float)PI;
+        j.flags = (h.enabled ? JF_ENABLED : 0) | (has_limits ? JF_LIMITS : 0);
+        j.limits_spring_mode = h.limits_spring.mode;
+        j.limits_freq = h.limits_spring.frequency_or_stiffness;
+        j.limits_damping = h.limits_spring.damping;
+        j.max_friction_torque = h.max_friction_torque;
+        j.motor_state = h.motor_state;
+        j.target_angular_velocity = h.target_angular_velocity;
+        double ta = h.target_angle;
+        j.target_angle = has_limits ? (float)std::max((double)j.limits_min, std::min((double)j.limits_max, ta)) : (float)ta;
+        j.motor_spring_mode = h.motor_spring.mode;
+        j.motor_freq = h.motor_spring.frequency_or_stiffness;
+        j.motor_damping = h.motor_spring.damping;
+        j.min_torque = h.min_torque_limit;
+        j.max_torque = h.max_torque_limit;
+        made[i] = j;
+    }
+    int r = ensure_hinge_capacity(W, w.num_hinges + n);
+    if (r != CC_OK) return r;
+    CC_TRY(cudaMemcpy(w.hinges + w.num_hinges, made.data(), sizeof(DevHinge) * n, cudaMemcpyHostToDevice));
+    for (int i = 0; i < n; i++) {
+        W->hinges.push_back(made[i]);
+        if (out_index) out_index[i] = w.num_hinges + i;
+    }
+    w.num_hinges += n;
+    drop_graph(W);
+    return upload_partners(W);
+}
+
+}  // extern "C"
+
+// read-modify-write of one joint's device record (the host copy follows)
+template <typename F>
+static int edit_hinge(cc_world *W, int32_t index, F f) {
+    DevWorld &w = W->w;
+    if (index < 0 || index >= w.num_hinges) return CC_ERR_INVALID;
+    DevHinge j;
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    CC_TRY(cudaMemcpy(&j, w.hinges + index, sizeof(DevHinge), cudaMemcpyDeviceToHost));
+    f(j);
+    f(W->hinges[index]);
+    CC_TRY(cudaMemcpy(w.hinges + index, &j, sizeof(DevHinge), cudaMemcpyHostToDevice));
+    return CC_OK;
+}
+
+extern "C" {
+
+int cc_world_set_hinge_limits(cc_world *W, int32_t index, float limits_min, float limits_max) {
+    if (!W || std::isnan(limits_min) || std::isnan(limits_max)) return CC_ERR_INVALID;
+    const double PI = 3.14159265358979323846;
+    return edit_hinge(W, index, [&](DevHinge &j) {  // setLimits hinge-constraint.ts:429-439
+        double mn = std::max((double)limits_min, -PI), mx = std::min((double)limits_max, PI);
+        j.limits_min = (float)mn;
+        j.limits_max = (float)mx;
+        bool has = mn > -PI || mx < PI;
+        j.flags = has ? (j.flags | JF_LIMITS) : (j.flags & ~JF_LIMITS);
+        if (has) j.target_angle = (float)std::max(mn, std::min(mx, (double)j.target_angle));
+    });
+}
+
+int cc_world_set_hinge_motor(cc_world *W, int32_t index, int32_t motor_state, float target_angular_velocity,
+                             float target_angle) {
+    if (!W || motor_state < 0 || motor_state > 2 || !std::isfinite(target_angular_velocity) ||
+        !std::isfinite(target_angle))
+        return CC_ERR_INVALID;
+    return edit_hinge(W, index, [&](DevHinge &j) {  // hinge-constraint.ts:441-465
+        j.motor_state = motor_state;
+        j.target_angular_velocity = target_angular_velocity;
+        j.target_angle = (j.flags & JF_LIMITS)
+                             ? (float)std::max((double)j.limits_min, std::min((double)j.limits_max, (double)target_angle))
+                             : target_angle;
+    });
+}
+
+int cc_world_set_hinge_enabled(cc_world *W, int32_t index, int32_t enabled) {
+    if (!W) return CC_ERR_INVALID;
+    int r = edit_hinge(W, index, [&](DevHinge &j) { j.flags = enabled ? (j.flags | JF_ENABLED) : (j.flags & ~JF_ENABLED); });
+    if (r != CC_OK) return r;
+    return upload_partners(W);
+}
+
+int cc_world_get_hinge_angles(cc_world *W, float *out, int32_t capacity) {
+    if (!W || capacity < 0 || (capacity > 0 && !out)) return CC_ERR_INVALID;
+    DevWorld &w = W->w;
+    int n = std::min(capacity, w.num_hinges);
+    if (n == 0) return capacity < w.num_hinges ? CC_ERR_CAPACITY : CC_OK;
+    CC_TRY(cudaMemcpy2DAsync(out, sizeof(float), (const char *)w.hinges + offsetof(DevHinge, theta), sizeof(DevHinge),
+                             sizeof(float), n, cudaMemcpyDeviceToHost, W->stream));
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    return capacity < w.num_hinges ? CC_ERR_CAPACITY : CC_OK;
+}
+
+int cc_world_set_skip_joint_pairs(cc_world *W, int32_t on) {
+    if (!W) return CC_ERR_INVALID;
+    W->w.skip_joint_pairs = on ? 1 : 0;
+    int r = ensure_hinge_capacity(W, 0);
+    if (r != CC_OK) return r;
+    drop_graph(W);
+    return upload_partners(W);
+}
+
+}  // extern "C"

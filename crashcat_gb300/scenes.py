@@ -12,8 +12,10 @@ import math
 
 import numpy as np
 
-from ._lib import (BODY_DTYPE, COMBINE_GEOMETRIC_MEAN, COMBINE_MAX, DYNAMIC, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_SPHERE,
-                   STATIC)
+from typing import Optional
+
+from ._lib import (BODY_DTYPE, COMBINE_GEOMETRIC_MEAN, COMBINE_MAX, DYNAMIC, MOTOR_OFF, MOTOR_POSITION,
+                   MOTOR_VELOCITY, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_SPHERE, STATIC, hinge_defaults)
 
 # object layers of the reference's test helper (tst/helpers.ts:5-26)
 LAYER_MOVING = 0
@@ -39,6 +41,8 @@ class Scene:
     position_iterations: int = 2
     num_worlds: int = 1
     seed: int = 0
+    hinges: Optional[np.ndarray] = None  # cc_hinge_desc records (_lib.HINGE_DTYPE)
+    skip_joint_pairs: bool = False
 
     @property
     def n(self) -> int:
@@ -381,3 +385,80 @@ def bouncing_spheres(n: int = 48, seed: int = 61) -> Scene:
     b["restitution"][idx] = rng.uniform(0.6, 0.9, size=n).astype(np.float32)
     b["allow_sleeping"][idx] = 0
     return Scene("bouncing_spheres", b, dt=1.0 / 60.0, steps=120, seed=seed)
+
+
+def hinge_chains(num_chains: int = 4, links: int = 6, seed: int = 71, limits: bool = True) -> Scene:
+    """Chains of boxes (0.8 x 0.2 x 0.2 m) joined end to end by hinges about Z, each hung
+    from a static anchor and released horizontally, so they swing down under gravity.  Every
+    other chain has limits of +-40 degrees on its joints (soft, 20 Hz, on the last chain);
+    joined bodies do not collide (the ragdoll example's pair filter).  Chains are 3 m apart
+    in Z and do not touch one another."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = num_chains * (links + 1)
+    b = blank_bodies(n)
+    h = hinge_defaults(num_chains * links)
+    k = 0
+    for c in range(num_chains):
+        a = c * (links + 1)
+        set_box(b, a, (0.1, 0.1, 0.1))
+        b["motion_type"][a] = STATIC
+        b["object_layer"][a] = LAYER_NOT_MOVING
+        z = 3.0 * c
+        b["position"][a] = (0.0, 5.0, z)
+        prev, pivot_x = a, 0.0
+        for i in range(links):
+            j = a + 1 + i
+            set_box(b, j, (0.4, 0.1, 0.1))
+            b["position"][j] = (pivot_x + 0.5, 5.0, z)
+            b["linear_velocity"][j] = (0.0, 0.0, rng.uniform(-0.05, 0.05))
+            h[k]["body_a"], h[k]["body_b"] = prev, j
+            h[k]["point_a"] = h[k]["point_b"] = (pivot_x, 5.0, z)
+            h[k]["hinge_axis_a"] = h[k]["hinge_axis_b"] = (0.0, 0.0, 1.0)
+            h[k]["normal_axis_a"] = h[k]["normal_axis_b"] = (1.0, 0.0, 0.0)
+            if limits and c % 2 == 1:
+                h[k]["limits_min"], h[k]["limits_max"] = -np.radians(40.0), np.radians(40.0)
+                if c == num_chains - 1:
+                    h[k]["limits_spring"]["frequency_or_stiffness"] = 20.0
+                    h[k]["limits_spring"]["damping"] = 0.5
+            prev, pivot_x = j, pivot_x + 1.0
+            k += 1
+    b["allow_sleeping"][:] = 0
+    return Scene("hinge_chains", b, dt=1.0 / 60.0, steps=60, seed=seed, hinges=h, skip_joint_pairs=True)
+
+
+def hinge_motors(n: int = 6, seed: int = 81) -> Scene:
+    """Wings (3 x 0.2 x 0.2 m boxes) hinged about Z at their centre to static posts, one per
+    motor configuration: velocity motors at -5 and 3 rad/s (one with its torque capped at
+    200 N m), position motors driven to 60 and -30 degrees, a free wing held by 5 N m of
+    hinge friction, and a wing with limits of -20..70 degrees.  Gravity acts on a wing that
+    starts off balance (it is shifted 0.3 m from the pivot along its length)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = blank_bodies(2 * n)
+    h = hinge_defaults(n)
+    for i in range(n):
+        post, wing = 2 * i, 2 * i + 1
+        x = 5.0 * i
+        set_box(b, post, (0.1, 0.1, 0.1))
+        b["motion_type"][post] = STATIC
+        b["object_layer"][post] = LAYER_NOT_MOVING
+        b["position"][post] = (x, 3.0, -1.0)
+        set_box(b, wing, (1.5, 0.1, 0.1))
+        b["position"][wing] = (x + 0.3, 3.0, 0.0)
+        b["quaternion"][wing] = (0.0, 0.0, math.sin(0.05), math.cos(0.05))
+        h[i]["body_a"], h[i]["body_b"] = post, wing
+        h[i]["point_a"] = h[i]["point_b"] = (x, 3.0, 0.0)
+        h[i]["hinge_axis_a"] = h[i]["hinge_axis_b"] = (0.0, 0.0, 1.0)
+        h[i]["normal_axis_a"] = h[i]["normal_axis_b"] = (1.0, 0.0, 0.0)
+        b["angular_velocity"][wing] = (0.0, 0.0, rng.uniform(-0.5, 0.5))
+    h[0]["motor_state"], h[0]["target_angular_velocity"] = MOTOR_VELOCITY, -5.0
+    h[1]["motor_state"], h[1]["target_angular_velocity"] = MOTOR_VELOCITY, 3.0
+    h[1]["min_torque_limit"], h[1]["max_torque_limit"] = -200.0, 200.0
+    h[2]["motor_state"], h[2]["target_angle"] = MOTOR_POSITION, np.radians(60.0)
+    h[3]["motor_state"], h[3]["target_angle"] = MOTOR_POSITION, -np.radians(30.0)
+    h[3]["motor_spring"]["mode"], h[3]["motor_spring"]["frequency_or_stiffness"] = 1, 4000.0
+    h[3]["motor_spring"]["damping"] = 300.0
+    h[4]["motor_state"], h[4]["max_friction_torque"] = MOTOR_OFF, 5.0
+    if n > 5:
+        h[5]["limits_min"], h[5]["limits_max"] = -np.radians(20.0), np.radians(70.0)
+    b["allow_sleeping"][:] = 0
+    return Scene("hinge_motors", b, dt=1.0 / 60.0, steps=90, seed=seed, hinges=h)

@@ -340,6 +340,35 @@ class GpuWorld:
             check(st, "cc_world_get_contact_events")
         return out[: cnt.value]
 
+    # ---- hinge joints (hinge-constraint.ts) ----
+    def add_hinges(self, hinges: np.ndarray) -> np.ndarray:
+        """cc_world_add_hinges: records of _lib.HINGE_DTYPE; returns the joint indices."""
+        hinges = np.ascontiguousarray(hinges, dtype=_lib.HINGE_DTYPE)
+        out = np.zeros(len(hinges), dtype=np.int32)
+        check(self._lib.cc_world_add_hinges(self.handle, ptr(hinges), len(hinges), ptr(out)), "cc_world_add_hinges")
+        return out
+
+    def set_hinge_limits(self, index: int, lo: float, hi: float) -> None:
+        check(self._lib.cc_world_set_hinge_limits(self.handle, index, C.c_float(lo), C.c_float(hi)),
+              "cc_world_set_hinge_limits")
+
+    def set_hinge_motor(self, index: int, state: int, target_angular_velocity: float = 0.0,
+                        target_angle: float = 0.0) -> None:
+        check(self._lib.cc_world_set_hinge_motor(self.handle, index, state, C.c_float(target_angular_velocity),
+                                                 C.c_float(target_angle)), "cc_world_set_hinge_motor")
+
+    def set_hinge_enabled(self, index: int, enabled: bool) -> None:
+        check(self._lib.cc_world_set_hinge_enabled(self.handle, index, int(bool(enabled))),
+              "cc_world_set_hinge_enabled")
+
+    def hinge_angles(self, n: int) -> np.ndarray:
+        out = np.zeros(max(n, 1), dtype=np.float32)
+        check(self._lib.cc_world_get_hinge_angles(self.handle, ptr(out), n), "cc_world_get_hinge_angles")
+        return out[:n]
+
+    def set_skip_joint_pairs(self, on: bool) -> None:
+        check(self._lib.cc_world_set_skip_joint_pairs(self.handle, int(bool(on))), "cc_world_set_skip_joint_pairs")
+
     def stats(self) -> dict:
         s = _lib.Stats()
         check(self._lib.cc_world_get_stats(self.handle, C.byref(s)), "cc_world_get_stats")

@@ -180,6 +180,63 @@ int cc_world_get_stats(cc_world *world, cc_stats *out);
  * (more than capacity when out is too small). */
 int cc_world_get_contact_events(cc_world *world, int32_t *out, int32_t capacity, int32_t *count);
 
+/* ---------------------------------------------------------------------------
+ * Hinge joints (src/constraints/hinge-constraint.ts).  HingeConstraintSettings
+ * (hinge-constraint.ts:125-164) with its SpringSettings (src/constraints/
+ * constraint-part/spring-settings.ts) and MotorSettings (motor-settings.ts)
+ * flattened.  A joint joins two bodies of the same world; it links their
+ * islands, is set up, warm started and solved after the island's contacts in
+ * (priority, creation order), as updateWorld does (src/update.ts:100-165).
+ * ------------------------------------------------------------------------- */
+enum cc_constraint_space { CC_SPACE_WORLD = 0, CC_SPACE_LOCAL = 1 };
+enum cc_spring_mode { CC_SPRING_FREQUENCY_AND_DAMPING = 0, CC_SPRING_STIFFNESS_AND_DAMPING = 1 };
+enum cc_motor_state { CC_MOTOR_OFF = 0, CC_MOTOR_VELOCITY = 1, CC_MOTOR_POSITION = 2 };
+
+typedef struct cc_spring_settings {
+    int32_t mode;                      /* cc_spring_mode */
+    float frequency_or_stiffness;      /* Hz, or N/m (N m/rad); 0 = rigid */
+    float damping;                     /* damping ratio, or N s/m */
+} cc_spring_settings;
+
+typedef struct cc_hinge_desc {
+    int32_t body_a, body_b;            /* body indices (cc_world_add_bodies order) */
+    int32_t space;                     /* cc_constraint_space of the points and axes below */
+    float point_a[3], point_b[3];      /* pivot on each body */
+    float hinge_axis_a[3], hinge_axis_b[3];    /* normalised on creation */
+    float normal_axis_a[3], normal_axis_b[3];  /* angle reference, perpendicular to the hinge axis */
+    float limits_min, limits_max;      /* radians; [-pi, pi] or wider = no limits */
+    cc_spring_settings limits_spring;  /* soft limits (frequency 0 = hard) */
+    float max_friction_torque;         /* N m while the motor is off */
+    int32_t motor_state;               /* cc_motor_state */
+    float target_angular_velocity;     /* rad/s (velocity motor) */
+    float target_angle;                /* rad (position motor); clamped to the limits */
+    cc_spring_settings motor_spring;   /* position motor spring (reference default: frequency 2 Hz, damping 1) */
+    float min_torque_limit, max_torque_limit;  /* N m (reference default: -inf, +inf) */
+    int32_t priority;                  /* constraintPriority: lower is solved first */
+    int32_t enabled;
+} cc_hinge_desc;
+
+/* hingeConstraint.create (hinge-constraint.ts:240-387) for n joints; out_index (may be NULL)
+ * receives each joint's index.  Bodies must exist and belong to one world.  World-space points
+ * and axes are taken against the bodies' current poses. */
+int cc_world_add_hinges(cc_world *world, const cc_hinge_desc *hinges, int32_t n, int32_t *out_index);
+
+/* setLimits / setMotorState / setTargetAngularVelocity / setTargetAngle / enabled
+ * (hinge-constraint.ts:429-465, ConstraintBase.enabled) of one joint. */
+int cc_world_set_hinge_limits(cc_world *world, int32_t index, float limits_min, float limits_max);
+int cc_world_set_hinge_motor(cc_world *world, int32_t index, int32_t motor_state, float target_angular_velocity,
+                             float target_angle);
+int cc_world_set_hinge_enabled(cc_world *world, int32_t index, int32_t enabled);
+
+/* getCurrentAngle (hinge-constraint.ts:467-474) of every joint, n floats. */
+int cc_world_get_hinge_angles(cc_world *world, float *out, int32_t capacity);
+
+/* on != 0: the broadphase skips body pairs that share an enabled joint, the declarative form
+ * of a Listener.onBodyPairValidate that rejects them (src/broadphase/broadphase.ts:112-123; the
+ * ragdoll example's filter).  Each body may then share joints with at most 8 other bodies
+ * (CC_ERR_CAPACITY otherwise). */
+int cc_world_set_skip_joint_pairs(cc_world *world, int32_t on);
+
 /* Stage profiler with no reference counterpart: runs n_steps steps (eager
  * launches) with CUDA events between the stages and writes the mean
  * milliseconds of [integrate forces, broadphase, narrowphase (GJK, faces,

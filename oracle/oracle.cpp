@@ -22,6 +22,7 @@
 #include <array>
 #include <map>
 #include <numeric>
+#include <set>
 #include <tuple>
 #include <vector>
 
@@ -124,8 +125,11 @@ struct ContactConstraint {
 struct Island {
     std::vector<int64_t> bodyIndices;  // active indices
     std::vector<int> contactIndices;
+    std::vector<int> jointIndices;
     int velSteps = 0, posSteps = 0;
 };
+
+#include "oracle_joint_types.h"
 
 struct Layers {
     int nObj = 0, nBp = 0;
@@ -144,6 +148,10 @@ struct World {
     // contact events of the last step: (type 1 added / 2 persisted / 3 removed, body index A, body index B)
     // at the listener call sites (contact-constraints.ts:494-499, contacts.ts:305-307)
     std::vector<std::array<int64_t, 3>> events;
+    std::vector<HingeJoint> joints;
+    // skip broadphase pairs of bodies that share an enabled joint: the declarative form of the
+    // ragdoll example's onBodyPairValidate (examples/src/example-ragdoll.ts:487-489)
+    bool skipJointPairs = false;
     std::vector<ContactConstraint> constraints;
     std::vector<Island> islands;
     double prevDt = 0;
@@ -440,6 +448,10 @@ static void bvh_build(const std::vector<Body> &bodies, std::vector<int> &idx, st
 
 static void find_colliding_pairs(World &w) {
     w.pairs.clear();
+    std::set<std::pair<int, int>> joined;  // body pairs that share an enabled joint
+    if (w.skipJointPairs)
+        for (const HingeJoint &j : w.joints)
+            if (j.enabled) joined.insert({std::min(j.a, j.b), std::max(j.a, j.b)});
     std::vector<int> idx(w.bodies.size());
     std::iota(idx.begin(), idx.end(), 0);
     std::vector<BvhNode> nodes;
@@ -489,6 +501,8 @@ static void find_colliding_pairs(World &w) {
             if (!A.collideKinematicVsNonDynamic && !B.collideKinematicVsNonDynamic && A.motion != DYNAMIC &&
                 B.motion != DYNAMIC && !(A.motion == KINEMATIC && B.sensor) && !(B.motion == KINEMATIC && A.sensor))
                 continue;
+            // onBodyPairValidate (broadphase.ts:112-123) as the declarative joint-pair filter
+            if (w.skipJointPairs && joined.count({std::min(A.index, B.index), std::max(A.index, B.index)})) continue;
             w.pairs.push_back({A.index, B.index});
         }
     }
@@ -935,6 +949,8 @@ static void apply_dof_pos(Body &b) {
     if (!(t & 4)) b.com.z = 0;
 }
 
+#include "oracle_joints.h"
+
 // solvePositionConstraintsForIsland contact-constraints.ts:1098-1216
 static bool solve_position(World &w, const std::vector<int> &ids) {
     bool any = false;
@@ -999,27 +1015,37 @@ static void build_islands(World &w) {
         while (links[i] != i) i = links[i];
         return i;
     };
+    // linkBodies islands.ts:103-140
+    auto link_bodies = [&](int64_t a, int64_t b) {
+        if (a < na && b < na) {
+            int64_t f = lowest(a), s = lowest(b);
+            if (f != s) {
+                if (f < s)
+                    links[s] = f;
+                else
+                    links[f] = s;
+                int64_t lo = std::min(f, s);
+                if (links[a] > lo) links[a] = lo;
+                if (links[b] > lo) links[b] = lo;
+            }
+        }
+    };
     std::vector<int64_t> contactLinks(w.constraints.size(), INACTIVE);
     for (size_t ci = 0; ci < w.constraints.size(); ci++) {
         const ContactConstraint &c = w.constraints[ci];
         Body &A = w.bodies[c.bodyA], &B = w.bodies[c.bodyB];
-        if (A.activeIndex != INACTIVE && B.activeIndex != INACTIVE) {
-            // linkBodies islands.ts:103-140
-            int64_t a = A.activeIndex, b = B.activeIndex;
-            if (a < na && b < na) {
-                int64_t f = lowest(a), s = lowest(b);
-                if (f != s) {
-                    if (f < s)
-                        links[s] = f;
-                    else
-                        links[f] = s;
-                    int64_t lo = std::min(f, s);
-                    if (links[a] > lo) links[a] = lo;
-                    if (links[b] > lo) links[b] = lo;
-                }
-            }
-        }
+        if (A.activeIndex != INACTIVE && B.activeIndex != INACTIVE) link_bodies(A.activeIndex, B.activeIndex);
         contactLinks[ci] = std::min(A.activeIndex, B.activeIndex);
+    }
+    // linkUserConstraints islands.ts:209-224, linkConstraint :163-178
+    std::vector<int64_t> jointLinks(w.joints.size(), INACTIVE);
+    for (size_t ji = 0; ji < w.joints.size(); ji++) {
+        const HingeJoint &j = w.joints[ji];
+        if (!j.enabled) continue;
+        Body &A = w.bodies[j.a], &B = w.bodies[j.b];
+        if (A.activeIndex == INACTIVE && B.activeIndex == INACTIVE) continue;
+        if (A.activeIndex != INACTIVE && B.activeIndex != INACTIVE) link_bodies(A.activeIndex, B.activeIndex);
+        jointLinks[ji] = std::min(A.activeIndex, B.activeIndex);
     }
     // finalize islands.ts:240-389
     int ni = 0;
@@ -1042,8 +1068,14 @@ static void build_islands(World &w) {
         if (ab >= INACTIVE) continue;
         isl[bodyIslands[ab]].contactIndices.push_back((int)ci);
     }
-    std::stable_sort(isl.begin(), isl.end(),
-                     [](const Island &a, const Island &b) { return a.contactIndices.size() > b.contactIndices.size(); });
+    for (size_t ji = 0; ji < jointLinks.size(); ji++) {
+        int64_t ab = jointLinks[ji];
+        if (ab >= INACTIVE) continue;
+        isl[bodyIslands[ab]].jointIndices.push_back((int)ji);
+    }
+    std::stable_sort(isl.begin(), isl.end(), [](const Island &a, const Island &b) {
+        return a.contactIndices.size() + a.jointIndices.size() > b.contactIndices.size() + b.jointIndices.size();
+    });
     for (Island &is : isl) {
         int vs = 0, ps = 0;
         bool dv = false, dp = false;
@@ -1146,14 +1178,38 @@ static void step(World &w, double dt) {
         }
     }
     if (dt > 0) {
+        // wakeBodiesInUserConstraints update.ts:863-888
+        for (HingeJoint &j : w.joints) {
+            if (!j.enabled) continue;
+            Body &A = w.bodies[j.a], &B = w.bodies[j.b];
+            bool act = !A.sleeping || !B.sleeping, dyn = A.motion == DYNAMIC || B.motion == DYNAMIC;
+            if (act && dyn) {
+                if (A.sleeping && A.motion == DYNAMIC) wake_body(w, A);
+                if (B.sleeping && B.motion == DYNAMIC) wake_body(w, B);
+            }
+        }
         build_islands(w);
+        // updateSleeping + setupVelocityConstraints constraints.ts:264-287
+        auto joint_active = [&](const HingeJoint &j) {
+            return j.enabled && !(w.bodies[j.a].sleeping && w.bodies[j.b].sleeping);
+        };
+        for (HingeJoint &j : w.joints)
+            if (joint_active(j)) hinge_setup(j, w.bodies[j.a], w.bodies[j.b], dt);
         if (w.s.warmStarting) {
             double ratio = (w.s.warmStarting && w.prevDt > 0) ? dt / w.prevDt : 0.0;
             warm_start_all(w, ratio);
+            for (HingeJoint &j : w.joints)
+                if (joint_active(j)) hinge_warm(j, w.bodies[j.a], w.bodies[j.b], ratio);
         }
         w.prevDt = dt;
         for (Island &is : w.islands) {
-            if (is.contactIndices.empty()) continue;
+            if (is.contactIndices.empty() && is.jointIndices.empty()) continue;
+            // sortConstraintIds constraints.ts:248-261 (priority, then index)
+            std::stable_sort(is.jointIndices.begin(), is.jointIndices.end(), [&](int a, int b) {
+                const HingeJoint &ja = w.joints[a], &jb = w.joints[b];
+                if (ja.priority != jb.priority) return ja.priority < jb.priority;
+                return ja.index < jb.index;
+            });
             // sortContactIndices contact-constraints.ts:1240-1264 (JS sort is stable)
             std::stable_sort(is.contactIndices.begin(), is.contactIndices.end(), [&](int a, int b) {
                 const ContactConstraint &ca = w.constraints[a], &cb = w.constraints[b];
@@ -1194,7 +1250,13 @@ static void step(World &w, double dt) {
                 if (re != ci) w.reorderedIslands++;
                 ci = re;
             }
-            for (int i = 0; i < is.velSteps; i++) solve_velocity(w, is.contactIndices);
+            for (int i = 0; i < is.velSteps; i++) {
+                if (!is.contactIndices.empty()) solve_velocity(w, is.contactIndices);
+                for (int ji : is.jointIndices) {
+                    HingeJoint &j = w.joints[ji];
+                    hinge_solve_velocity(j, w.bodies[j.a], w.bodies[j.b], dt);
+                }
+            }
         }
         // storeAppliedImpulses contact-constraints.ts:1061-1076
         w.manifoldLambda.assign(w.constraints.size(), 0.0);
@@ -1229,9 +1291,15 @@ static void step(World &w, double dt) {
             set_transform(b);
         }
         for (Island &is : w.islands) {
-            if (is.contactIndices.empty()) continue;
+            if (is.contactIndices.empty() && is.jointIndices.empty()) continue;
             for (int i = 0; i < is.posSteps; i++) {
-                if (!solve_position(w, is.contactIndices)) break;
+                bool applied = false;
+                if (!is.contactIndices.empty()) applied = solve_position(w, is.contactIndices);
+                for (int ji : is.jointIndices) {
+                    HingeJoint &j = w.joints[ji];
+                    applied = hinge_solve_position(j, w.bodies[j.a], w.bodies[j.b], dt, w.s.baumgarteFactor) || applied;
+                }
+                if (!applied) break;
             }
         }
         // updateBodyPositions update.ts:322-330
@@ -1380,6 +1448,70 @@ int orc_add_bodies(void *wp, const double *rows, int n) {
 }
 
 int orc_body_count(void *wp) { return (int)((World *)wp)->bodies.size(); }
+
+// Hinge joint (hinge-constraint.ts create), 36 doubles:
+//  0 bodyA, 1 bodyB, 2-4 pointA, 5-7 pointB, 8-10 hingeAxisA, 11-13 hingeAxisB, 14-16 normalAxisA,
+//  17-19 normalAxisB, 20 space (0 world, 1 local), 21 limitsMin, 22 limitsMax,
+//  23-25 limits spring (mode, frequency or stiffness, damping), 26 maxFrictionTorque,
+//  27 motor state (0 off, 1 velocity, 2 position), 28 target angular velocity, 29 target angle,
+//  30-32 motor spring (mode, frequency or stiffness, damping), 33 min torque, 34 max torque,
+//  35 priority.  Returns the joint index or -1.
+int orc_add_hinge(void *wp, const double *d) {
+    World &w = *(World *)wp;
+    int a = (int)d[0], b = (int)d[1];
+    if (a < 0 || b < 0 || a >= (int)w.bodies.size() || b >= (int)w.bodies.size()) return -1;
+    const Body &A = w.bodies[a], &B = w.bodies[b];
+    HingeJoint j;
+    j.a = a;
+    j.b = b;
+    j.index = (int)w.joints.size();
+    j.priority = (int)d[35];
+    V3 pA{d[2], d[3], d[4]}, pB{d[5], d[6], d[7]};
+    V3 h1 = normalize(V3{d[8], d[9], d[10]}), h2 = normalize(V3{d[11], d[12], d[13]});
+    V3 n1 = normalize(V3{d[14], d[15], d[16]}), n2 = normalize(V3{d[17], d[18], d[19]});
+    if ((int)d[20] == 0) {
+        Q4 iqA = qconj(A.quat), iqB = qconj(B.quat);
+        j.lp1 = rotate(iqA, sub(pA, A.com));
+        j.lp2 = rotate(iqB, sub(pB, B.com));
+        j.lh1 = rotate(iqA, h1);
+        j.lh2 = rotate(iqB, h2);
+        j.ln1 = rotate(iqA, n1);
+        j.ln2 = rotate(iqB, n2);
+        Q4 r0 = inv_initial_orientation_xz(n1, h1, n2, h2);
+        j.invInitial = qmul(qmul(iqB, r0), A.quat);
+    } else {
+        j.lp1 = pA;
+        j.lp2 = pB;
+        j.lh1 = h1;
+        j.lh2 = h2;
+        j.ln1 = n1;
+        j.ln2 = n2;
+        j.invInitial = inv_initial_orientation_xz(rotate(A.quat, n1), rotate(A.quat, h1), rotate(B.quat, n2),
+                                                  rotate(B.quat, h2));
+    }
+    double mn = d[21], mx = d[22];
+    if (mn <= -M_PI && mx >= M_PI) {
+        j.hasLimits = false;
+        j.limitsMin = -M_PI;
+        j.limitsMax = M_PI;
+    } else {
+        j.hasLimits = true;
+        j.limitsMin = std::max(mn, -M_PI);
+        j.limitsMax = std::min(mx, M_PI);
+    }
+    j.limitsSpring = {(int)d[23], d[24], d[25]};
+    j.maxFrictionTorque = d[26];
+    j.motorSpring = {(int)d[30], d[31], d[32]};
+    j.minTorqueLimit = d[33];
+    j.maxTorqueLimit = d[34];
+    // setMotorState / setTargetAngularVelocity / setTargetAngle (hinge-constraint.ts)
+    j.motorState = (int)d[27];
+    j.targetAngularVelocity = d[28];
+    j.targetAngle = j.hasLimits ? std::max(j.limitsMin, std::min(j.limitsMax, d[29])) : d[29];
+    w.joints.push_back(j);
+    return j.index;
+}
+void orc_set_skip_joint_pairs(void *wp, int on) { ((World *)wp)->skipJointPairs = on != 0; }
 // Contact events of the last step, 3 int64 per event (type, body index A, body index B); returns the count.
 int orc_get_events(void *wp, int64_t *out, int cap) {
     const World &w = *(World *)wp;

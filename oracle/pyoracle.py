@@ -55,6 +55,8 @@ def load():
         "orc_collide_pair": ([dp, dp, C.c_double, dp], i32),
         "orc_inverse_inertia": ([dp, dp], None),
         "orc_get_events": ([vp, C.c_void_p, i32], i32),
+        "orc_add_hinge": ([vp, dp], i32),
+        "orc_set_skip_joint_pairs": ([vp, i32], None),
     }
     for k, (a, r) in sig.items():
         f = getattr(lib, k)
@@ -184,6 +186,33 @@ class OracleWorld:
         o = np.zeros((self.n, 6), dtype=np.float64)
         self.lib.orc_get_aabbs(self.h, dptr(o))
         return o
+
+    def add_hinge(self, desc: np.ndarray) -> int:
+        """Hinge joint from a 36-double descriptor (oracle.cpp orc_add_hinge layout)."""
+        d = np.ascontiguousarray(desc, dtype=np.float64)
+        k = self.lib.orc_add_hinge(self.h, dptr(d))
+        assert k >= 0
+        return k
+
+    def add_hinge_record(self, h) -> int:
+        """Hinge joint from a cc_hinge_desc record (fields by name)."""
+        d = np.zeros(36, dtype=np.float64)
+        d[0], d[1] = h["body_a"], h["body_b"]
+        for k, f in enumerate(("point_a", "point_b", "hinge_axis_a", "hinge_axis_b", "normal_axis_a", "normal_axis_b")):
+            d[2 + 3 * k: 5 + 3 * k] = h[f]
+        d[20] = h["space"]
+        d[21], d[22] = h["limits_min"], h["limits_max"]
+        d[23:26] = (h["limits_spring"]["mode"], h["limits_spring"]["frequency_or_stiffness"],
+                    h["limits_spring"]["damping"])
+        d[26], d[27], d[28], d[29] = (h["max_friction_torque"], h["motor_state"], h["target_angular_velocity"],
+                                      h["target_angle"])
+        d[30:33] = (h["motor_spring"]["mode"], h["motor_spring"]["frequency_or_stiffness"],
+                    h["motor_spring"]["damping"])
+        d[33], d[34], d[35] = h["min_torque_limit"], h["max_torque_limit"], h["priority"]
+        return self.add_hinge(d)
+
+    def set_skip_joint_pairs(self, on: bool) -> None:
+        self.lib.orc_set_skip_joint_pairs(self.h, 1 if on else 0)
 
     def contact_events(self) -> dict:
         """Contact events of the last step: {'added' | 'persisted' | 'removed': set of (a, b)}."""
