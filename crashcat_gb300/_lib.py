@@ -107,6 +107,11 @@ EXPORTS = {
     "cc_world_set_hinge_enabled": ([C.c_void_p, C.c_int32, C.c_int32], C.c_int),
     "cc_world_get_hinge_angles": ([C.c_void_p, C.c_void_p, C.c_int32], C.c_int),
     "cc_world_set_skip_joint_pairs": ([C.c_void_p, C.c_int32], C.c_int),
+    "cc_world_add_swing_twists": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
+    "cc_world_set_swing_twist_limits": ([C.c_void_p, C.c_int32, C.c_float, C.c_float, C.c_float, C.c_float], C.c_int),
+    "cc_world_set_swing_twist_motor": ([C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                        C.c_float], C.c_int),
+    "cc_world_set_swing_twist_enabled": ([C.c_void_p, C.c_int32, C.c_int32], C.c_int),
     "cc_status_string": ([C.c_int], C.c_char_p),
 }
 
@@ -139,6 +144,39 @@ def hinge_defaults(n: int) -> np.ndarray:
     h["motor_spring"]["damping"] = 1.0
     h["min_torque_limit"] = -np.inf
     h["max_torque_limit"] = np.inf
+    h["enabled"] = 1
+    return h
+
+
+# cc_swing_twist_desc
+SWING_CONE, SWING_PYRAMID = 0, 1
+SWING_TWIST_DTYPE = np.dtype([
+    ("body_a", np.int32), ("body_b", np.int32), ("space", np.int32),
+    ("position_a", np.float32, 3), ("position_b", np.float32, 3),
+    ("twist_axis_a", np.float32, 3), ("plane_axis_a", np.float32, 3),
+    ("twist_axis_b", np.float32, 3), ("plane_axis_b", np.float32, 3),
+    ("swing_type", np.int32), ("normal_half_cone_angle", np.float32), ("plane_half_cone_angle", np.float32),
+    ("twist_min_angle", np.float32), ("twist_max_angle", np.float32), ("max_friction_torque", np.float32),
+    ("swing_motor_state", np.int32), ("twist_motor_state", np.int32),
+    ("target_angular_velocity", np.float32, 3), ("target_orientation", np.float32, 4),
+    ("swing_motor_spring", SPRING_DTYPE), ("twist_motor_spring", SPRING_DTYPE),
+    ("swing_min_torque_limit", np.float32), ("swing_max_torque_limit", np.float32),
+    ("twist_min_torque_limit", np.float32), ("twist_max_torque_limit", np.float32),
+    ("priority", np.int32), ("enabled", np.int32),
+])
+
+
+def swing_twist_defaults(n: int) -> np.ndarray:
+    """n swing-twist records with swingTwistConstraint.create's defaults
+    (swing-twist-constraint.ts:180-296): cone swing, all limits 0 (locked), motors off with
+    2 Hz / damping 1 springs and unbounded torque, identity target, priority 0, enabled."""
+    h = np.zeros(n, SWING_TWIST_DTYPE)
+    h["target_orientation"] = (0.0, 0.0, 0.0, 1.0)
+    for f in ("swing_motor_spring", "twist_motor_spring"):
+        h[f]["frequency_or_stiffness"] = 2.0
+        h[f]["damping"] = 1.0
+    h["swing_min_torque_limit"] = h["twist_min_torque_limit"] = -np.inf
+    h["swing_max_torque_limit"] = h["twist_max_torque_limit"] = np.inf
     h["enabled"] = 1
     return h
 

@@ -170,10 +170,32 @@ struct AdjBuffers {
 // point (point-constraint-part.ts), hinge rotation (hinge-rotation-constraint-part.ts), and
 // the limit and motor angle parts (angle-constraint-part.ts, spring-part.ts).
 enum : int { JF_ENABLED = 1, JF_LIMITS = 2 };
+// user joints of both types share one id space: hinges 0.., swing-twists JOINT_SWING | index
+constexpr int JOINT_SWING = 1 << 30;
+
+// fields every joint type starts with
+struct DevJointHead {
+    int a, b;             // body indices
+    int priority, index;  // constraintPriority and the per-type creation index (sort key)
+    int flags;            // JF_*
+    int island;           // island of this step (-1: in none)
+};
+// PointConstraintPart (point-constraint-part.ts)
+struct DevPoint {
+    float3 r1, r2;
+    float invI1_r1X[9], invI2_r2X[9], eff[9];  // row-major 3x3
+    float3 lambda;
+    int active;
+};
+// AngleConstraintPart (angle-constraint-part.ts)
+struct DevAngle {
+    float3 i1, i2;  // I1^-1 axis, I2^-1 axis
+    float eff, soft, bias, lambda;
+};
+
 struct DevHinge {
-    int a, b, priority, index;
-    int flags, motor_state, limits_spring_mode, motor_spring_mode;
-    int island;                 // island of this step (-1: in none)
+    DevJointHead h;
+    int motor_state, limits_spring_mode, motor_spring_mode;
     float3 lp1, lp2, lh1, lh2;  // attachment points (from the centre of mass) and hinge axes, body space
     float4 inv_initial;         // inverse initial relative orientation
     float limits_min, limits_max, limits_freq, limits_damping;
@@ -182,20 +204,36 @@ struct DevHinge {
     // per-step state
     float theta;
     float3 wh1;  // world hinge axis of body A
-    // point part
-    float3 r1, r2;
-    float invI1_r1X[9], invI2_r2X[9], p_eff[9];  // row-major 3x3
-    float3 p_lambda;
-    int p_active;
+    DevPoint pt;
     // hinge rotation part
     float3 a1, b2, c2, b2xA1, c2xA1;
     float invI1[6], invI2[6];  // symmetric xx xy xz yy yz zz
     float r_eff[4], r_lambda[2];
-    // limit and motor angle parts
-    float3 l_i1, l_i2;
-    float l_eff, l_soft, l_bias, l_lambda;
-    float3 m_i1, m_i2;
-    float m_eff, m_soft, m_bias, m_lambda;
+    DevAngle limit, motor;
+};
+
+// SwingTwistConstraint (swing-twist-constraint.ts) with its SwingTwistConstraintPart limits
+// (swing-twist-constraint-part.ts): sines and cosines of the half-angle limits
+enum : int { ST_TWIST_LOCKED = 1, ST_SWING_Y_LOCKED = 2, ST_SWING_Z_LOCKED = 4, ST_TWIST_FREE = 8,
+             ST_SWING_Y_FREE = 16, ST_SWING_Z_FREE = 32, ST_SWING_YZ_FREE = 48 };
+struct DevSwing {
+    DevJointHead h;
+    int swing_type, rotation_flags;
+    int swing_motor_state, twist_motor_state, swing_spring_mode, twist_spring_mode;
+    float3 lp1, lp2;
+    float4 c2b1, c2b2;  // constraint space to body space
+    float normal_half_cone, plane_half_cone, twist_min, twist_max, max_friction_torque;
+    float sin_twist_min, sin_twist_max, cos_twist_min, cos_twist_max;
+    float y_half_min, y_half_max, sin_y_min, sin_y_max, cos_y_min, cos_y_max;
+    float z_half_min, z_half_max, sin_z_min, sin_z_max, cos_z_min, cos_z_max;
+    float3 target_w;  // target angular velocity, constraint space of body B
+    float4 target_q;  // target orientation, constraint space
+    float swing_freq, swing_damping, twist_freq, twist_damping;
+    float swing_min_torque, swing_max_torque, twist_min_torque, twist_max_torque;
+    // per-step state
+    float3 ws_y, ws_z, ws_twist, ws_motor[3];
+    DevPoint pt;
+    DevAngle sy, sz, tw, motor[3];  // limits (swing Y, swing Z, twist), motors (twist, swing Y, swing Z)
 };
 
 // impulse adjoints handed from one step's reverse to the previous step's, keyed by body pair
@@ -285,13 +323,38 @@ struct DevWorld {
     // hinge joints and their island lists
     DevHinge *hinges;
     int num_hinges, max_hinges;
+    DevSwing *swings;
+    int num_swings, max_swings;
     int skip_joint_pairs;              // broadphase skips body pairs that share an enabled joint
     int *joint_partners;               // JOINT_PARTNERS per body: other bodies joined to it (-1: none)
     int *island_joint_count, *island_joint_off, *island_fill_j;
-    int *island_joints;  // 3 x max_hinges: as scattered | by index | by (priority, index)
+    int *island_joints;  // 3 x max_joints: as scattered | by (type, index) | by (priority, index, type)
+    int max_joints;      // capacity of the per-island joint lists
     int *joint_wake;     // flag: some joint has to wake a body this step
     int *body_local;  // index of a body inside its island's body list (per-warp solve)
 };
+
+// ---- user joints of every type under one id ---------------------------------------------
+__device__ __forceinline__ int joint_total(const DevWorld &w) { return w.num_hinges + w.num_swings; }
+// the k-th joint in type order (hinges, then swing-twists), each type in creation order
+__device__ __forceinline__ int joint_id_at(const DevWorld &w, int k) {
+    return k < w.num_hinges ? k : (JOINT_SWING | (k - w.num_hinges));
+}
+__device__ __forceinline__ DevJointHead &joint_head(const DevWorld &w, int id) {
+    return id & JOINT_SWING ? w.swings[id & ~JOINT_SWING].h : w.hinges[id].h;
+}
+__device__ __forceinline__ bool joint_active(const DevWorld &w, const DevJointHead &h) {
+    return (h.flags & JF_ENABLED) && !(sleeping_of(w.flags[h.a]) && sleeping_of(w.flags[h.b]));
+}
+// solve order inside an island: (priority, per-type index, type) (constraints.ts:248-261, a
+// stable sort of a list built type by type)
+__device__ __forceinline__ bool joint_before(const DevWorld &w, int x, int y) {
+    const DevJointHead &a = joint_head(w, x), &b = joint_head(w, y);
+    if (a.priority != b.priority) return a.priority < b.priority;
+    if (a.index != b.index) return a.index < b.index;
+    return (x & JOINT_SWING) < (y & JOINT_SWING);
+}
+
 
 // ---------------------------------------------------------------------------
 // float3 / quaternion helpers (FP32 device path)

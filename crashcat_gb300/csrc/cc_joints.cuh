@@ -1,10 +1,12 @@
-// Hinge joints on the device: setup, warm start, velocity and position solve of
-// src/constraints/hinge-constraint.ts and the constraint parts it is built from
-// (point-constraint-part.ts, hinge-rotation-constraint-part.ts, angle-constraint-part.ts,
-// spring-part.ts).  FP32 like the contact solver; the 3x3 and 2x2 effective-mass inversions
-// run in FP64.  Body state is read and written in global memory; a joint is solved by one
-// thread (the per-thread island solve, or thread 0 of the per-CTA solve).
-// Included by cc_solver.cu inside namespace cc (it uses that file's c_settings and rotation_step).
+// User joints on the device: setup, warm start, velocity and position solve of the hinge
+// (src/constraints/hinge-constraint.ts) and swing-twist (swing-twist-constraint.ts) joints and
+// the constraint parts they are built from (constraint-part/point-, hinge-rotation-, angle-,
+// swing-twist-, rotation-euler-constraint-part.ts, spring-part.ts).  FP32 like the contact
+// solver; the 3x3 and 2x2 effective-mass inversions and the swing ellipse projection run in
+// FP64.  Body state is read and written in global memory; the joints of an island are solved
+// in order by one thread of the per-CTA island solve.
+// Included by cc_solver.cu inside namespace cc (it uses that file's c_settings and rotation_step,
+// and the swing-twist clamping of cc_swing.cuh).
 #pragma once
 
 // ---- 3x3 helpers, row-major float[9] ------------------------------------------------
@@ -117,68 +119,104 @@ __device__ float spring_settings(float &soft, float &bias_out, float dt, float i
     return 1.f / (iem + soft);
 }
 
-// ---- point part --------------------------------------------------------------------
-__device__ void point_calc(DevHinge &j, const JBody &A, const JBody &B, float4 qa, float4 qb) {
-    j.r1 = qrot(qa, j.lp1);
-    j.r2 = qrot(qb, j.lp2);
+// ---- point part (point-constraint-part.ts) ---------------------------------------------
+__device__ void point_deactivate(DevPoint &p) {
+    for (int k = 0; k < 9; k++) p.eff[k] = 0.f;
+    p.lambda = f3(0.f, 0.f, 0.f);
+    p.active = 0;
+}
+__device__ void point_calc(DevPoint &p, const JBody &A, const JBody &B, float4 qa, float4 qb, float3 lp1, float3 lp2) {
+    p.r1 = qrot(qa, lp1);
+    p.r2 = qrot(qb, lp2);
     float iem[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     float sm = 0.f;
     float I[9], X[9], T[9], T2[9];
     if (A.motion == DYNAMIC) {
         sm += A.im;
         jm_from_sym(I, A.I);
-        jm_cross(X, j.r1);
-        jm_mm(j.invI1_r1X, I, X);
+        jm_cross(X, p.r1);
+        jm_mm(p.invI1_r1X, I, X);
         jm_mm(T, X, I);
         jm_mm_bt(T2, T, X);
         for (int k = 0; k < 9; k++) iem[k] += T2[k];
     } else {
-        for (int k = 0; k < 9; k++) j.invI1_r1X[k] = 0.f;
+        for (int k = 0; k < 9; k++) p.invI1_r1X[k] = 0.f;
     }
     if (B.motion == DYNAMIC) {
         sm += B.im;
         jm_from_sym(I, B.I);
-        jm_cross(X, j.r2);
-        jm_mm(j.invI2_r2X, I, X);
+        jm_cross(X, p.r2);
+        jm_mm(p.invI2_r2X, I, X);
         jm_mm(T, X, I);
         jm_mm_bt(T2, T, X);
         for (int k = 0; k < 9; k++) iem[k] += T2[k];
     } else {
-        for (int k = 0; k < 9; k++) j.invI2_r2X[k] = 0.f;
+        for (int k = 0; k < 9; k++) p.invI2_r2X[k] = 0.f;
     }
     iem[0] += sm;
     iem[4] += sm;
     iem[8] += sm;
-    if (jm_invert(j.p_eff, iem)) {
-        j.p_active = 1;
-    } else {
-        for (int k = 0; k < 9; k++) j.p_eff[k] = 0.f;
-        j.p_lambda = f3(0.f, 0.f, 0.f);
-        j.p_active = 0;
-    }
+    if (jm_invert(p.eff, iem))
+        p.active = 1;
+    else
+        point_deactivate(p);
 }
-__device__ bool point_apply(DevWorld &w, const DevHinge &j, const JBody &A, const JBody &B, float3 l) {
+__device__ bool point_apply(DevWorld &w, const DevPoint &p, const JBody &A, const JBody &B, float3 l) {
     if (lensq3(l) == 0.f) return false;
     if (A.motion == DYNAMIC) {
         add_lin(w, A.i, l * (-A.im));
-        add_ang(w, A.i, -jm_mv(j.invI1_r1X, l));
+        add_ang(w, A.i, -jm_mv(p.invI1_r1X, l));
     }
     if (B.motion == DYNAMIC) {
         add_lin(w, B.i, l * B.im);
-        add_ang(w, B.i, jm_mv(j.invI2_r2X, l));
+        add_ang(w, B.i, jm_mv(p.invI2_r2X, l));
     }
     return true;
 }
-__device__ bool point_solve_velocity(DevWorld &w, DevHinge &j, const JBody &A, const JBody &B) {
-    if (!j.p_active) return false;
-    float3 jv = xyz(w.linvel[A.i]) - cross3(j.r1, xyz(w.angvel[A.i])) - xyz(w.linvel[B.i]) +
-                cross3(j.r2, xyz(w.angvel[B.i]));
-    float3 l = jm_mv(j.p_eff, jv);
-    j.p_lambda = j.p_lambda + l;
-    return point_apply(w, j, A, B, l);
+__device__ void point_warm(DevWorld &w, DevPoint &p, const JBody &A, const JBody &B, float ratio) {
+    if (!p.active) return;
+    p.lambda = p.lambda * ratio;
+    point_apply(w, p, A, B, p.lambda);
+}
+__device__ bool point_solve_velocity(DevWorld &w, DevPoint &p, const JBody &A, const JBody &B) {
+    if (!p.active) return false;
+    float3 jv = xyz(w.linvel[A.i]) - cross3(p.r1, xyz(w.angvel[A.i])) - xyz(w.linvel[B.i]) +
+                cross3(p.r2, xyz(w.angvel[B.i]));
+    float3 l = jm_mv(p.eff, jv);
+    p.lambda = p.lambda + l;
+    return point_apply(w, p, A, B, l);
 }
 
-// ---- hinge rotation part -------------------------------------------------------------
+// position steps (rigid-body-step.ts:16-97)
+__device__ __forceinline__ void add_position_step(DevWorld &w, int i, float3 d) {
+    float4 c = w.com[i];
+    float3 p = f3(c.x + d.x, c.y + d.y, c.z + d.z);
+    int dof = dof_of(w.flags[i]);
+    if (!(dof & 1)) p.x = 0.f;
+    if (!(dof & 2)) p.y = 0.f;
+    if (!(dof & 4)) p.z = 0.f;
+    w.com[i] = make_float4(p.x, p.y, p.z, 0.f);
+}
+__device__ __forceinline__ void add_rotation(DevWorld &w, int i, float3 a) { w.quat[i] = rotation_step(w.quat[i], a); }
+
+// solvePositionConstraint of the point part, after point_calc on the current poses
+__device__ bool point_solve_position(DevWorld &w, DevPoint &p, const JBody &A, const JBody &B, float beta) {
+    if (!p.active) return false;
+    float3 sep = xyz(w.com[B.i]) + p.r2 - xyz(w.com[A.i]) - p.r1;
+    if (lensq3(sep) < 1e-12f) return false;
+    float3 l = jm_mv(p.eff, sep) * (-beta);
+    if (A.motion == DYNAMIC) {
+        add_position_step(w, A.i, l * (-A.im));
+        add_rotation(w, A.i, -jm_mv(p.invI1_r1X, l));
+    }
+    if (B.motion == DYNAMIC) {
+        add_position_step(w, B.i, l * B.im);
+        add_rotation(w, B.i, jm_mv(p.invI2_r2X, l));
+    }
+    return true;
+}
+
+// ---- hinge rotation part (hinge-rotation-constraint-part.ts) --------------------------
 __device__ __forceinline__ float3 perpendicular3(float3 v) {
     if (fabsf(v.x) > fabsf(v.y)) {
         float l = sqrtf(v.x * v.x + v.z * v.z);
@@ -253,27 +291,17 @@ __device__ bool hrot_solve_velocity(DevWorld &w, DevHinge &j, const JBody &A, co
     return hrot_apply(w, j, A, B, l0, l1);
 }
 
-// ---- angle parts (limit: l_*, motor: m_*) -----------------------------------------------
-struct AngleRef {
-    float3 &i1, &i2;
-    float &eff, &soft, &bias, &lambda;
-};
-__device__ __forceinline__ AngleRef limit_part(DevHinge &j) {
-    return AngleRef{j.l_i1, j.l_i2, j.l_eff, j.l_soft, j.l_bias, j.l_lambda};
-}
-__device__ __forceinline__ AngleRef motor_part(DevHinge &j) {
-    return AngleRef{j.m_i1, j.m_i2, j.m_eff, j.m_soft, j.m_bias, j.m_lambda};
-}
-__device__ __forceinline__ void angle_deactivate(AngleRef p) {
+// ---- angle part (angle-constraint-part.ts) ---------------------------------------------
+__device__ __forceinline__ void angle_deactivate(DevAngle &p) {
     p.eff = 0.f;
     p.lambda = 0.f;
 }
-__device__ float angle_iem(AngleRef p, const JBody &A, const JBody &B, float3 axis) {
+__device__ float angle_iem(DevAngle &p, const JBody &A, const JBody &B, float3 axis) {
     p.i1 = A.motion == DYNAMIC ? symmul(A.I, axis) : f3(0.f, 0.f, 0.f);
     p.i2 = B.motion == DYNAMIC ? symmul(B.I, axis) : f3(0.f, 0.f, 0.f);
     return dot3(axis, p.i1 + p.i2);
 }
-__device__ void angle_calc(AngleRef p, const JBody &A, const JBody &B, float3 axis, float bias) {
+__device__ void angle_calc(DevAngle &p, const JBody &A, const JBody &B, float3 axis, float bias) {
     float iem = angle_iem(p, A, B, axis);
     if (iem == 0.f) {
         angle_deactivate(p);
@@ -283,7 +311,7 @@ __device__ void angle_calc(AngleRef p, const JBody &A, const JBody &B, float3 ax
         p.bias = bias;
     }
 }
-__device__ void angle_calc_settings(AngleRef p, float dt, const JBody &A, const JBody &B, float3 axis, float bias,
+__device__ void angle_calc_settings(DevAngle &p, float dt, const JBody &A, const JBody &B, float3 axis, float bias,
                                     float C, int mode, float fs, float damping) {
     float iem = angle_iem(p, A, B, axis);
     if (iem == 0.f)
@@ -291,13 +319,17 @@ __device__ void angle_calc_settings(AngleRef p, float dt, const JBody &A, const 
     else
         p.eff = spring_settings(p.soft, p.bias, dt, iem, bias, C, mode, fs, damping);
 }
-__device__ bool angle_apply(DevWorld &w, AngleRef p, const JBody &A, const JBody &B, float l) {
+__device__ bool angle_apply(DevWorld &w, const DevAngle &p, const JBody &A, const JBody &B, float l) {
     if (l == 0.f) return false;
     if (A.motion == DYNAMIC) add_ang(w, A.i, -(p.i1 * l));
     if (B.motion == DYNAMIC) add_ang(w, B.i, p.i2 * l);
     return true;
 }
-__device__ bool angle_solve_velocity(DevWorld &w, AngleRef p, const JBody &A, const JBody &B, float3 axis, float mn,
+__device__ void angle_warm(DevWorld &w, DevAngle &p, const JBody &A, const JBody &B, float ratio) {
+    p.lambda *= ratio;
+    angle_apply(w, p, A, B, p.lambda);
+}
+__device__ bool angle_solve_velocity(DevWorld &w, DevAngle &p, const JBody &A, const JBody &B, float3 axis, float mn,
                                      float mx) {
     if (p.eff == 0.f) return false;
     float jv = 0.f;
@@ -310,7 +342,7 @@ __device__ bool angle_solve_velocity(DevWorld &w, AngleRef p, const JBody &A, co
     return angle_apply(w, p, A, B, dl);
 }
 
-// ---- hinge ---------------------------------------------------------------------------
+// ---- hinge (hinge-constraint.ts) -------------------------------------------------------
 __device__ __forceinline__ float center_angle(float a) {
     const float PI = 3.14159265358979f;
     while (a > PI) a -= 2.f * PI;
@@ -319,7 +351,7 @@ __device__ __forceinline__ float center_angle(float a) {
 }
 // calculateA1AndTheta
 __device__ void hinge_theta(DevHinge &j, float4 qa, float4 qb) {
-    if (!(j.flags & JF_LIMITS) && j.motor_state == 0 && !(j.max_friction_torque > 0.f)) return;
+    if (!(j.h.flags & JF_LIMITS) && j.motor_state == 0 && !(j.max_friction_torque > 0.f)) return;
     float3 wh = qrot(qa, j.lh1);
     j.wh1 = wh;
     float4 rel = qmul(qmul(qb, j.inv_initial), make_float4(-qa.x, -qa.y, -qa.z, qa.w));
@@ -334,36 +366,33 @@ __device__ __forceinline__ bool hinge_min_closest(const DevHinge &j) {
     return fabsf(center_angle(j.theta - j.limits_min)) < fabsf(center_angle(j.theta - j.limits_max));
 }
 __device__ void hinge_limit_props(DevHinge &j, const JBody &A, const JBody &B, float dt) {
-    if ((j.flags & JF_LIMITS) && (j.theta <= j.limits_min || j.theta >= j.limits_max))
-        angle_calc_settings(limit_part(j), dt, A, B, j.wh1, 0.f, hinge_to_limit(j), j.limits_spring_mode,
-                            j.limits_freq, j.limits_damping);
+    if ((j.h.flags & JF_LIMITS) && (j.theta <= j.limits_min || j.theta >= j.limits_max))
+        angle_calc_settings(j.limit, dt, A, B, j.wh1, 0.f, hinge_to_limit(j), j.limits_spring_mode, j.limits_freq,
+                            j.limits_damping);
     else
-        angle_deactivate(limit_part(j));
+        angle_deactivate(j.limit);
 }
 __device__ void hinge_motor_props(DevHinge &j, const JBody &A, const JBody &B, float dt) {
     if (j.motor_state == 0) {
         if (j.max_friction_torque > 0.f)
-            angle_calc(motor_part(j), A, B, j.wh1, 0.f);
+            angle_calc(j.motor, A, B, j.wh1, 0.f);
         else
-            angle_deactivate(motor_part(j));
+            angle_deactivate(j.motor);
     } else if (j.motor_state == 1) {
-        angle_calc(motor_part(j), A, B, j.wh1, -j.target_angular_velocity);
+        angle_calc(j.motor, A, B, j.wh1, -j.target_angular_velocity);
     } else {
         if (j.motor_freq > 0.f)
-            angle_calc_settings(motor_part(j), dt, A, B, j.wh1, 0.f, center_angle(j.theta - j.target_angle),
+            angle_calc_settings(j.motor, dt, A, B, j.wh1, 0.f, center_angle(j.theta - j.target_angle),
                                 j.motor_spring_mode, j.motor_freq, j.motor_damping);
         else
-            angle_deactivate(motor_part(j));
+            angle_deactivate(j.motor);
     }
-}
-__device__ __forceinline__ bool hinge_active(const DevWorld &w, const DevHinge &j) {
-    return (j.flags & JF_ENABLED) && !(sleeping_of(w.flags[j.a]) && sleeping_of(w.flags[j.b]));
 }
 // setupVelocity
 __device__ void hinge_setup(DevWorld &w, DevHinge &j, float dt) {
-    JBody A = jbody(w, j.a), B = jbody(w, j.b);
-    float4 qa = w.quat[j.a], qb = w.quat[j.b];
-    point_calc(j, A, B, qa, qb);
+    JBody A = jbody(w, j.h.a), B = jbody(w, j.h.b);
+    float4 qa = w.quat[j.h.a], qb = w.quat[j.h.b];
+    point_calc(j.pt, A, B, qa, qb, j.lp1, j.lp2);
     hrot_calc(j, A, B, qrot(qa, j.lh1), qrot(qb, j.lh2));
     hinge_theta(j, qa, qb);
     hinge_limit_props(j, A, B, dt);
@@ -371,35 +400,30 @@ __device__ void hinge_setup(DevWorld &w, DevHinge &j, float dt) {
 }
 // warmStartVelocity: motor, point, rotation, limits
 __device__ void hinge_warm(DevWorld &w, DevHinge &j, float ratio) {
-    JBody A = jbody(w, j.a, false), B = jbody(w, j.b, false);
-    j.m_lambda *= ratio;
-    angle_apply(w, motor_part(j), A, B, j.m_lambda);
-    if (j.p_active) {
-        j.p_lambda = j.p_lambda * ratio;
-        point_apply(w, j, A, B, j.p_lambda);
-    }
+    JBody A = jbody(w, j.h.a, false), B = jbody(w, j.h.b, false);
+    angle_warm(w, j.motor, A, B, ratio);
+    point_warm(w, j.pt, A, B, ratio);
     j.r_lambda[0] *= ratio;
     j.r_lambda[1] *= ratio;
     hrot_apply(w, j, A, B, j.r_lambda[0], j.r_lambda[1]);
-    j.l_lambda *= ratio;
-    angle_apply(w, limit_part(j), A, B, j.l_lambda);
+    angle_warm(w, j.limit, A, B, ratio);
 }
 // solveVelocity
 __device__ bool hinge_solve_velocity(DevWorld &w, DevHinge &j, float dt) {
-    JBody A = jbody(w, j.a, false), B = jbody(w, j.b, false);
+    JBody A = jbody(w, j.h.a, false), B = jbody(w, j.h.b, false);
     const float INF = __int_as_float(0x7f800000);
     bool motor = false, limit = false;
-    if (j.m_eff != 0.f) {
+    if (j.motor.eff != 0.f) {
         if (j.motor_state == 0) {
             float ml = j.max_friction_torque * dt;
-            motor = angle_solve_velocity(w, motor_part(j), A, B, j.wh1, -ml, ml);
+            motor = angle_solve_velocity(w, j.motor, A, B, j.wh1, -ml, ml);
         } else {
-            motor = angle_solve_velocity(w, motor_part(j), A, B, j.wh1, dt * j.min_torque, dt * j.max_torque);
+            motor = angle_solve_velocity(w, j.motor, A, B, j.wh1, dt * j.min_torque, dt * j.max_torque);
         }
     }
-    bool pos = point_solve_velocity(w, j, A, B);
+    bool pos = point_solve_velocity(w, j.pt, A, B);
     bool rot = hrot_solve_velocity(w, j, A, B);
-    if (j.l_eff != 0.f) {
+    if (j.limit.eff != 0.f) {
         float mn, mx;
         if (j.limits_min == j.limits_max) {
             mn = -INF;
@@ -411,47 +435,19 @@ __device__ bool hinge_solve_velocity(DevWorld &w, DevHinge &j, float dt) {
             mn = -INF;
             mx = 0.f;
         }
-        limit = angle_solve_velocity(w, limit_part(j), A, B, j.wh1, mn, mx);
+        limit = angle_solve_velocity(w, j.limit, A, B, j.wh1, mn, mx);
     }
     return motor || pos || rot || limit;
 }
-
-// position steps (rigid-body-step.ts:16-97)
-__device__ __forceinline__ void add_position_step(DevWorld &w, int i, float3 d) {
-    float4 c = w.com[i];
-    float3 p = f3(c.x + d.x, c.y + d.y, c.z + d.z);
-    int dof = dof_of(w.flags[i]);
-    if (!(dof & 1)) p.x = 0.f;
-    if (!(dof & 2)) p.y = 0.f;
-    if (!(dof & 4)) p.z = 0.f;
-    w.com[i] = make_float4(p.x, p.y, p.z, 0.f);
-}
-__device__ __forceinline__ void add_rotation(DevWorld &w, int i, float3 a) { w.quat[i] = rotation_step(w.quat[i], a); }
-
 // solvePosition
 __device__ bool hinge_solve_position(DevWorld &w, DevHinge &j, float dt) {
     const float beta = c_settings.baumgarte;
-    JBody A = jbody(w, j.a), B = jbody(w, j.b);
-    point_calc(j, A, B, w.quat[j.a], w.quat[j.b]);
-    bool pos = false;
-    if (j.p_active) {
-        float3 sep = xyz(w.com[j.b]) + j.r2 - xyz(w.com[j.a]) - j.r1;
-        if (!(lensq3(sep) < 1e-12f)) {
-            float3 l = jm_mv(j.p_eff, sep) * (-beta);
-            if (A.motion == DYNAMIC) {
-                add_position_step(w, A.i, l * (-A.im));
-                add_rotation(w, A.i, -jm_mv(j.invI1_r1X, l));
-            }
-            if (B.motion == DYNAMIC) {
-                add_position_step(w, B.i, l * B.im);
-                add_rotation(w, B.i, jm_mv(j.invI2_r2X, l));
-            }
-            pos = true;
-        }
-    }
-    A = jbody(w, j.a);
-    B = jbody(w, j.b);
-    float4 qa = w.quat[j.a], qb = w.quat[j.b];
+    JBody A = jbody(w, j.h.a), B = jbody(w, j.h.b);
+    point_calc(j.pt, A, B, w.quat[j.h.a], w.quat[j.h.b], j.lp1, j.lp2);
+    bool pos = point_solve_position(w, j.pt, A, B, beta);
+    A = jbody(w, j.h.a);
+    B = jbody(w, j.h.b);
+    float4 qa = w.quat[j.h.a], qb = w.quat[j.h.b];
     hrot_calc(j, A, B, qrot(qa, j.lh1), qrot(qb, j.lh2));
     bool rot = false;
     if (hrot_active(j)) {
@@ -465,24 +461,245 @@ __device__ bool hinge_solve_position(DevWorld &w, DevHinge &j, float dt) {
         }
     }
     bool limit = false;
-    if ((j.flags & JF_LIMITS) && !(j.limits_freq > 0.f)) {
-        A = jbody(w, j.a);
-        B = jbody(w, j.b);
-        hinge_theta(j, w.quat[j.a], w.quat[j.b]);
+    if ((j.h.flags & JF_LIMITS) && !(j.limits_freq > 0.f)) {
+        A = jbody(w, j.h.a);
+        B = jbody(w, j.h.b);
+        hinge_theta(j, w.quat[j.h.a], w.quat[j.h.b]);
         hinge_limit_props(j, A, B, dt);
         float C = hinge_to_limit(j);
-        if (j.l_eff != 0.f && C != 0.f && j.l_soft == 0.f) {
-            float l = -j.l_eff * beta * C;
-            if (A.motion == DYNAMIC) add_rotation(w, A.i, -(j.l_i1 * l));
-            if (B.motion == DYNAMIC) add_rotation(w, B.i, j.l_i2 * l);
+        if (j.limit.eff != 0.f && C != 0.f && j.limit.soft == 0.f) {
+            float l = -j.limit.eff * beta * C;
+            if (A.motion == DYNAMIC) add_rotation(w, A.i, -(j.limit.i1 * l));
+            if (B.motion == DYNAMIC) add_rotation(w, B.i, j.limit.i2 * l);
             limit = true;
         }
     }
     return pos || rot || limit;
 }
 
-__device__ __forceinline__ bool hinge_before(const DevHinge &x, const DevHinge &y) {
-    if (x.priority != y.priority) return x.priority < y.priority;
-    return x.index < y.index;
+// ---- swing-twist limits (swing-twist-constraint-part.ts) -------------------------------
+// calculateConstraintProperties :481-652 (limit axes and their angle parts)
+__device__ void st_calc(DevSwing &p, const JBody &A, const JBody &B, float4 q, float4 c2w) {
+    float4 sw, tw;
+    get_swing_twist(q, sw, tw);
+    float4 csw = sw, ctw = tw;
+    int cl = clamp_swing_twist(p, csw, ctw);
+    int rf = p.rotation_flags;
+    const float3 X = f3(1.f, 0.f, 0.f), Y = f3(0.f, 1.f, 0.f), Z = f3(0.f, 0.f, 1.f);
+    float4 t2w = qmul(c2w, sw);
+    if (rf & ST_SWING_Y_LOCKED) {
+        p.ws_y = qrot(t2w, Y);
+        p.ws_z = qrot(t2w, Z);
+        angle_calc(p.sy, A, B, p.ws_y, 0.f);
+        if (rf & ST_SWING_Z_LOCKED) {
+            angle_calc(p.sz, A, B, p.ws_z, 0.f);
+        } else if (cl & (CL_Z_MIN | CL_Z_MAX)) {
+            if (cl & CL_Z_MIN) p.ws_z = -p.ws_z;
+            angle_calc(p.sz, A, B, p.ws_z, 0.f);
+        } else {
+            angle_deactivate(p.sz);
+        }
+    } else if (rf & ST_SWING_Z_LOCKED) {
+        p.ws_y = qrot(t2w, Y);
+        p.ws_z = qrot(t2w, Z);
+        if (cl & (CL_Y_MIN | CL_Y_MAX)) {
+            if (cl & CL_Y_MIN) p.ws_y = -p.ws_y;
+            angle_calc(p.sy, A, B, p.ws_y, 0.f);
+        } else {
+            angle_deactivate(p.sy);
+        }
+        angle_calc(p.sz, A, B, p.ws_z, 0.f);
+    } else if ((rf & ST_SWING_YZ_FREE) != ST_SWING_YZ_FREE) {
+        if (cl & (CL_Y_MIN | CL_Y_MAX | CL_Z_MIN | CL_Z_MAX)) {
+            float3 current = qrot(t2w, X), desired = qrot(qmul(c2w, csw), X);
+            float3 c = cross3(desired, current);
+            float l = sqrtf(lensq3(c));
+            if (l > 1e-6f) {
+                p.ws_y = c * (1.f / l);
+                angle_calc(p.sy, A, B, p.ws_y, 0.f);
+            } else {
+                angle_deactivate(p.sy);
+            }
+        } else {
+            angle_deactivate(p.sy);
+        }
+        angle_deactivate(p.sz);
+    } else {
+        angle_deactivate(p.sy);
+        angle_deactivate(p.sz);
+    }
+    if (rf & ST_TWIST_LOCKED) {
+        p.ws_twist = qrot(t2w, X);
+        angle_calc(p.tw, A, B, p.ws_twist, 0.f);
+    } else if (!(rf & ST_TWIST_FREE)) {
+        if (cl & (CL_TWIST_MIN | CL_TWIST_MAX)) {
+            p.ws_twist = qrot(t2w, X);
+            if (cl & CL_TWIST_MIN) p.ws_twist = -p.ws_twist;
+            angle_calc(p.tw, A, B, p.ws_twist, 0.f);
+        } else {
+            angle_deactivate(p.tw);
+        }
+    } else {
+        angle_deactivate(p.tw);
+    }
+}
+// solvePositionConstraint :743-776 through a RotationEulerConstraintPart
+// (rotation-euler-constraint-part.ts calculateConstraintProperties, solvePositionConstraint)
+__device__ bool st_solve_position(DevWorld &w, DevSwing &p, const JBody &A, const JBody &B, float4 q, float beta) {
+    float4 sw, tw;
+    get_swing_twist(q, sw, tw);
+    if (clamp_swing_twist(p, sw, tw) == 0) return false;
+    float4 inv_initial = qmul(p.c2b2, qconj4(qmul(qmul(p.c2b1, sw), tw)));
+    float I1[9], I2[9], S[9], eff[9];
+    jm_from_sym(I1, A.I);
+    jm_from_sym(I2, B.I);
+    for (int k = 0; k < 9; k++) S[k] = I1[k] + I2[k];
+    if (!jm_invert(eff, S))
+        for (int k = 0; k < 9; k++) eff[k] = 0.f;
+    float4 qa = w.quat[A.i], qb = w.quat[B.i];
+    float4 diff = qmul(qmul(qb, inv_initial), qconj4(qa));
+    if (diff.w < 0.f) diff = qscale4(diff, -1.f);
+    float3 err = f3(2.f * diff.x, 2.f * diff.y, 2.f * diff.z);
+    if (lensq3(err) < 1e-12f) return false;
+    float3 l = jm_mv(eff, err) * (-beta);
+    if (A.motion == DYNAMIC) add_rotation(w, A.i, -jm_mv(I1, l));
+    if (B.motion == DYNAMIC) add_rotation(w, B.i, jm_mv(I2, l));
+    return true;
 }
 
+// ---- swing-twist (swing-twist-constraint.ts) ------------------------------------------
+// setupVelocity :484-666
+__device__ void swing_setup(DevWorld &w, DevSwing &j, float dt) {
+    JBody A = jbody(w, j.h.a), B = jbody(w, j.h.b);
+    float4 qa = w.quat[j.h.a], qb = w.quat[j.h.b];
+    point_calc(j.pt, A, B, qa, qb, j.lp1, j.lp2);
+    float4 c1w = qmul(qa, j.c2b1), c2w = qmul(qb, j.c2b2);
+    float4 q = qmul(qconj4(c1w), c2w);
+    st_calc(j, A, B, q, c1w);
+    if (j.swing_motor_state != 0 || j.twist_motor_state != 0 || j.max_friction_torque > 0.f) {
+        j.ws_motor[0] = qrot(c2w, f3(1.f, 0.f, 0.f));
+        j.ws_motor[1] = qrot(c2w, f3(0.f, 1.f, 0.f));
+        j.ws_motor[2] = qrot(c2w, f3(0.f, 0.f, 1.f));
+        float e[3] = {0.f, 0.f, 0.f};
+        if (j.swing_motor_state == 2 || j.twist_motor_state == 2) {
+            float4 t = j.target_q;
+            if (q.x * t.x + q.y * t.y + q.z * t.z + q.w * t.w < 0.f) t = qscale4(t, -1.f);
+            float4 d = qmul(qconj4(q), t);
+            e[0] = -2.f * d.x;
+            e[1] = -2.f * d.y;
+            e[2] = -2.f * d.z;
+        }
+        float tav[3] = {j.target_w.x, j.target_w.y, j.target_w.z};
+        if (j.swing_motor_state == 0) {
+            if (j.max_friction_torque > 0.f) {
+                for (int i = 1; i < 3; i++) angle_calc(j.motor[i], A, B, j.ws_motor[i], 0.f);
+            } else {
+                for (int i = 0; i < 3; i++) angle_deactivate(j.motor[i]);
+            }
+        } else if (j.swing_motor_state == 1) {
+            for (int i = 1; i < 3; i++) angle_calc(j.motor[i], A, B, j.ws_motor[i], -tav[i]);
+        } else if (j.swing_freq > 0.f) {
+            for (int i = 1; i < 3; i++)
+                angle_calc_settings(j.motor[i], dt, A, B, j.ws_motor[i], 0.f, e[i], j.swing_spring_mode, j.swing_freq,
+                                    j.swing_damping);
+        } else {
+            for (int i = 1; i < 3; i++) angle_deactivate(j.motor[i]);
+        }
+        if (j.twist_motor_state == 0) {
+            if (j.max_friction_torque > 0.f)
+                angle_calc(j.motor[0], A, B, j.ws_motor[0], 0.f);
+            else
+                angle_deactivate(j.motor[0]);
+        } else if (j.twist_motor_state == 1) {
+            angle_calc(j.motor[0], A, B, j.ws_motor[0], -tav[0]);
+        } else if (j.twist_freq > 0.f) {
+            angle_calc_settings(j.motor[0], dt, A, B, j.ws_motor[0], 0.f, e[0], j.twist_spring_mode, j.twist_freq,
+                                j.twist_damping);
+        } else {
+            angle_deactivate(j.motor[0]);
+        }
+    } else {
+        for (int i = 0; i < 3; i++) angle_deactivate(j.motor[i]);
+    }
+}
+// warmStartVelocity :668-680: motors, limits, point
+__device__ void swing_warm(DevWorld &w, DevSwing &j, float ratio) {
+    JBody A = jbody(w, j.h.a, false), B = jbody(w, j.h.b, false);
+    for (int i = 0; i < 3; i++) angle_warm(w, j.motor[i], A, B, ratio);
+    angle_warm(w, j.sy, A, B, ratio);
+    angle_warm(w, j.sz, A, B, ratio);
+    angle_warm(w, j.tw, A, B, ratio);
+    point_warm(w, j.pt, A, B, ratio);
+}
+// solveVelocity :682-748
+__device__ bool swing_solve_velocity(DevWorld &w, DevSwing &j, float dt) {
+    JBody A = jbody(w, j.h.a, false), B = jbody(w, j.h.b, false);
+    const float INF = __int_as_float(0x7f800000);
+    bool imp = false;
+    if (j.motor[0].eff != 0.f) {
+        float mn, mx;
+        if (j.twist_motor_state == 0) {
+            mx = dt * j.max_friction_torque;
+            mn = -mx;
+        } else {
+            mn = dt * j.twist_min_torque;
+            mx = dt * j.twist_max_torque;
+        }
+        imp = angle_solve_velocity(w, j.motor[0], A, B, j.ws_motor[0], mn, mx) || imp;
+    }
+    if (j.motor[1].eff != 0.f) {
+        float mn, mx;
+        if (j.swing_motor_state == 0) {
+            mx = dt * j.max_friction_torque;
+            mn = -mx;
+        } else {
+            mn = dt * j.swing_min_torque;
+            mx = dt * j.swing_max_torque;
+        }
+        for (int i = 1; i < 3; i++) imp = angle_solve_velocity(w, j.motor[i], A, B, j.ws_motor[i], mn, mx) || imp;
+    }
+    if (j.sy.eff != 0.f)
+        imp = angle_solve_velocity(w, j.sy, A, B, j.ws_y, -INF, j.sin_y_min == j.sin_y_max ? INF : 0.f) || imp;
+    if (j.sz.eff != 0.f)
+        imp = angle_solve_velocity(w, j.sz, A, B, j.ws_z, -INF, j.sin_z_min == j.sin_z_max ? INF : 0.f) || imp;
+    if (j.tw.eff != 0.f)
+        imp = angle_solve_velocity(w, j.tw, A, B, j.ws_twist, -INF, j.sin_twist_min == j.sin_twist_max ? INF : 0.f) ||
+              imp;
+    imp = point_solve_velocity(w, j.pt, A, B) || imp;
+    return imp;
+}
+// solvePosition :757-800: rotation limits, then the point from the corrected poses
+__device__ bool swing_solve_position(DevWorld &w, DevSwing &j) {
+    const float beta = c_settings.baumgarte;
+    JBody A = jbody(w, j.h.a), B = jbody(w, j.h.b);
+    float4 qa = w.quat[j.h.a], qb = w.quat[j.h.b];
+    float4 q = qmul(qconj4(qmul(qa, j.c2b1)), qmul(qb, j.c2b2));
+    bool imp = st_solve_position(w, j, A, B, q, beta);
+    A = jbody(w, j.h.a);
+    B = jbody(w, j.h.b);
+    point_calc(j.pt, A, B, w.quat[j.h.a], w.quat[j.h.b], j.lp1, j.lp2);
+    imp = point_solve_position(w, j.pt, A, B, beta) || imp;
+    return imp;
+}
+
+// ---- dispatch on the joint id (the id helpers are in cc_internal.cuh) ------------------
+__device__ void joint_setup(DevWorld &w, int id, float dt) {
+    if (id & JOINT_SWING)
+        swing_setup(w, w.swings[id & ~JOINT_SWING], dt);
+    else
+        hinge_setup(w, w.hinges[id], dt);
+}
+__device__ void joint_warm(DevWorld &w, int id, float ratio) {
+    if (id & JOINT_SWING)
+        swing_warm(w, w.swings[id & ~JOINT_SWING], ratio);
+    else
+        hinge_warm(w, w.hinges[id], ratio);
+}
+__device__ bool joint_solve_velocity(DevWorld &w, int id, float dt) {
+    return id & JOINT_SWING ? swing_solve_velocity(w, w.swings[id & ~JOINT_SWING], dt)
+                            : hinge_solve_velocity(w, w.hinges[id], dt);
+}
+__device__ bool joint_solve_position(DevWorld &w, int id, float dt) {
+    return id & JOINT_SWING ? swing_solve_position(w, w.swings[id & ~JOINT_SWING])
+                            : hinge_solve_position(w, w.hinges[id], dt);
+}

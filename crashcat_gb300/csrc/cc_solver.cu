@@ -19,6 +19,7 @@
 // decides sleeping for the island - the integration and sleep test are fused
 // into the last solver pass.
 #include "cc_internal.cuh"
+#include "cc_swing.cuh"
 
 namespace cc {
 
@@ -390,8 +391,8 @@ __global__ void k_uf_link(DevWorld w) {
         if (!active_body(w.flags[a]) || !active_body(w.flags[b])) continue;
         uf_union(w, a, b);
     }
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < w.num_hinges; j += gridDim.x * blockDim.x) {
-        const DevHinge &h = w.hinges[j];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < joint_total(w); k += gridDim.x * blockDim.x) {
+        const DevJointHead &h = joint_head(w, joint_id_at(w, k));
         if (!(h.flags & JF_ENABLED)) continue;
         if (!active_body(w.flags[h.a]) || !active_body(w.flags[h.b])) continue;
         uf_union(w, h.a, h.b);
@@ -425,8 +426,8 @@ __global__ void k_island_count(DevWorld w, const int *island_id_of_root) {
         if (isl >= 0) atomicAdd(&w.island_cons_count[isl], 1);
     }
     // a joint belongs to the island of its lower active body (islands.ts:163-178, 318-332)
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < w.num_hinges; j += gridDim.x * blockDim.x) {
-        DevHinge &h = w.hinges[j];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < joint_total(w); k += gridDim.x * blockDim.x) {
+        DevJointHead &h = joint_head(w, joint_id_at(w, k));
         int isl = -1;
         if (h.flags & JF_ENABLED) {
             bool aa = active_body(w.flags[h.a]), ab = active_body(w.flags[h.b]);
@@ -455,11 +456,12 @@ __global__ void k_island_scatter(DevWorld w) {
         int k = atomicAdd(&w.island_fill_c[isl], 1);
         w.island_cons[w.island_cons_off[isl] + k] = ci;
     }
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < w.num_hinges; j += gridDim.x * blockDim.x) {
-        int isl = w.hinges[j].island;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < joint_total(w); k += gridDim.x * blockDim.x) {
+        int id = joint_id_at(w, k);
+        int isl = joint_head(w, id).island;
         if (isl < 0) continue;
-        int k = atomicAdd(&w.island_fill_j[isl], 1);
-        w.island_joints[w.island_joint_off[isl] + k] = j;
+        int f = atomicAdd(&w.island_fill_j[isl], 1);
+        w.island_joints[w.island_joint_off[isl] + f] = id;
     }
 }
 
@@ -468,7 +470,7 @@ __global__ void k_island_classify(DevWorld w, int *small_list, int *large_list) 
     int ni = w.ctr->num_islands;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x) {
         int nc = w.island_cons_count[i], nb = w.island_body_count[i];
-        int nj = w.num_hinges > 0 ? w.island_joint_count[i] : 0;
+        int nj = joint_total(w) > 0 ? w.island_joint_count[i] : 0;
         atomicMax(&w.ctr->max_island_constraints, nc + nj);
         if (nj > 0) {  // islands with joints: the per-CTA solve, joints by one thread in the reference's order
             int k = atomicAdd(&w.ctr->num_large_islands, 1);
@@ -751,7 +753,7 @@ __device__ void store_impulses(DevWorld &w, CacheRecord *crecs, const ContactCon
 // wakes its sleeping dynamic body.  The reference walks the joints in order, so a wake can
 // run down a chain within one step; the scan finds whether any joint has work, and only
 // then one thread walks them in order (joints of different worlds never share a body).
-__device__ __forceinline__ bool joint_wakes(const DevWorld &w, const DevHinge &h) {
+__device__ __forceinline__ bool joint_wakes(const DevWorld &w, const DevJointHead &h) {
     if (!(h.flags & JF_ENABLED)) return false;
     uint32_t fa = w.flags[h.a], fb = w.flags[h.b];
     bool act = !sleeping_of(fa) || !sleeping_of(fb);
@@ -759,18 +761,18 @@ __device__ __forceinline__ bool joint_wakes(const DevWorld &w, const DevHinge &h
     return act && dyn && ((sleeping_of(fa) && motion_of(fa) == DYNAMIC) || (sleeping_of(fb) && motion_of(fb) == DYNAMIC));
 }
 __global__ void k_joint_wake_scan(DevWorld w) {
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < w.num_hinges; j += gridDim.x * blockDim.x)
-        if (joint_wakes(w, w.hinges[j])) *w.joint_wake = 1;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < joint_total(w); k += gridDim.x * blockDim.x)
+        if (joint_wakes(w, joint_head(w, joint_id_at(w, k)))) *w.joint_wake = 1;
 }
 __global__ void k_joint_wake_serial(DevWorld w) {
     if (!*w.joint_wake) return;
     *w.joint_wake = 0;
-    for (int j = 0; j < w.num_hinges; j++) {
-        const DevHinge &h = w.hinges[j];
+    for (int k = 0; k < joint_total(w); k++) {
+        const DevJointHead &h = joint_head(w, joint_id_at(w, k));
         if (!joint_wakes(w, h)) continue;
         int ids[2] = {h.a, h.b};
-        for (int k = 0; k < 2; k++) {
-            int i = ids[k];
+        for (int e = 0; e < 2; e++) {
+            int i = ids[e];
             uint32_t f = w.flags[i];
             if (!(sleeping_of(f) && motion_of(f) == DYNAMIC)) continue;
             w.flags[i] = f & ~F_SLEEPING;
@@ -781,11 +783,9 @@ __global__ void k_joint_wake_serial(DevWorld w) {
 // setupVelocityConstraints (constraints.ts:276-287) for every enabled joint with an awake
 // body (updateSleeping constraints.ts:264-274)
 __global__ void k_joint_setup(DevWorld w, float dt) {
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < w.num_hinges; j += gridDim.x * blockDim.x) {
-        DevHinge h = w.hinges[j];
-        if (!hinge_active(w, h)) continue;
-        hinge_setup(w, h, dt);
-        w.hinges[j] = h;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < joint_total(w); k += gridDim.x * blockDim.x) {
+        int id = joint_id_at(w, k);
+        if (joint_active(w, joint_head(w, id))) joint_setup(w, id, dt);
     }
 }
 
@@ -909,19 +909,17 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
         for (int k = threadIdx.x; k < nb; k += blockDim.x) prepare_body(w, bl[k]);
         // the island's joints in index order (warm start) and in (priority, index) order
         // (sortConstraintIds constraints.ts:248-261)
-        int nj = w.num_hinges > 0 ? w.island_joint_count[isl] : 0;
+        int nj = joint_total(w) > 0 ? w.island_joint_count[isl] : 0;
         const int *jl = w.island_joints + (nj > 0 ? w.island_joint_off[isl] : 0);
-        int *j_idx = const_cast<int *>(jl) + w.max_hinges;
-        int *j_pri = j_idx + w.max_hinges;
+        int *j_idx = const_cast<int *>(jl) + w.max_joints;
+        int *j_pri = j_idx + w.max_joints;
         for (int k = threadIdx.x; k < nj; k += blockDim.x) {
             int jk = jl[k];
-            int pk = w.hinges[jk].priority;
             int r1 = 0, r2 = 0;
             for (int m = 0; m < nj; m++) {
                 int jm = jl[m];
-                int pm = w.hinges[jm].priority;
-                r1 += jm < jk;
-                r2 += (pm < pk || (pm == pk && jm < jk));
+                r1 += jm < jk;  // ids order by type, then creation index
+                r2 += joint_before(w, jm, jk);
             }
             j_idx[r1] = jk;
             j_pri[r2] = jk;
@@ -1033,7 +1031,7 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
             if (nj > 0) {
                 __syncthreads();
                 if (threadIdx.x == 0)
-                    for (int k = 0; k < nj; k++) hinge_warm(w, w.hinges[j_idx[k]], ratio);
+                    for (int k = 0; k < nj; k++) joint_warm(w, j_idx[k], ratio);
                 __syncthreads();
             }
         }
@@ -1042,7 +1040,7 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
             if (nj > 0) {
                 __syncthreads();
                 if (threadIdx.x == 0)
-                    for (int k = 0; k < nj; k++) hinge_solve_velocity(w, w.hinges[j_pri[k]], dt);
+                    for (int k = 0; k < nj; k++) joint_solve_velocity(w, j_pri[k], dt);
                 __syncthreads();
             }
         }
@@ -1083,7 +1081,7 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
                 __syncthreads();
                 if (threadIdx.x == 0) {
                     bool applied = false;
-                    for (int k = 0; k < nj; k++) applied = hinge_solve_position(w, w.hinges[j_pri[k]], dt) || applied;
+                    for (int k = 0; k < nj; k++) applied = joint_solve_position(w, j_pri[k], dt) || applied;
                     if (applied) s_any = 1;
                 }
                 __syncthreads();
@@ -1427,8 +1425,9 @@ void launch_contacts_and_islands(DevWorld &w, float dt, float, cudaStream_t s) {
     k_contact_setup<<<grid_for(w.max_manifolds, 128, 16), 128, 0, s>>>(w, ct, dt);
     k_removed_contacts<<<grid_for(w.cache_cap, 256), 256, 0, s>>>(w, ct);
     k_apply_wake<<<grid_for(w.n, 256), 256, 0, s>>>(w);
-    if (w.num_hinges > 0 && dt > 0.f) {
-        k_joint_wake_scan<<<grid_for(w.num_hinges, 256), 256, 0, s>>>(w);
+    const int nj = w.num_hinges + w.num_swings;
+    if (nj > 0 && dt > 0.f) {
+        k_joint_wake_scan<<<grid_for(nj, 256), 256, 0, s>>>(w);
         k_joint_wake_serial<<<1, 1, 0, s>>>(w);
     }
     k_uf_init<<<grid_for(w.n, 256), 256, 0, s>>>(w);
@@ -1438,10 +1437,10 @@ void launch_contacts_and_islands(DevWorld &w, float dt, float, cudaStream_t s) {
     k_island_count<<<grid_for(nmax, 256), 256, 0, s>>>(w, w.island_id_of_root);
     exclusive_scan_int(w.island_body_count, w.island_body_off, w.n, nullptr, w.scan_tmp, s);
     exclusive_scan_int(w.island_cons_count, w.island_cons_off, w.n, nullptr, w.scan_tmp, s);
-    if (w.num_hinges > 0) exclusive_scan_int(w.island_joint_count, w.island_joint_off, w.n, nullptr, w.scan_tmp, s);
+    if (nj > 0) exclusive_scan_int(w.island_joint_count, w.island_joint_off, w.n, nullptr, w.scan_tmp, s);
     k_island_scatter<<<grid_for(nmax, 256), 256, 0, s>>>(w);
     k_island_classify<<<grid_for(w.n, 256), 256, 0, s>>>(w, w.small_list, w.large_list);
-    if (w.num_hinges > 0 && dt > 0.f) k_joint_setup<<<grid_for(w.num_hinges, 128), 128, 0, s>>>(w, dt);
+    if (nj > 0 && dt > 0.f) k_joint_setup<<<grid_for(nj, 128), 128, 0, s>>>(w, dt);
 }
 
 void launch_solver(DevWorld &w, float dt, float ratio, cudaStream_t s, cudaEvent_t mid) {

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "cc_internal.cuh"
+#include "cc_swing.cuh"
 
 using namespace cc;
 
@@ -31,7 +32,8 @@ struct cc_world {
     int last_status = CC_OK;
     DevCounters last_ctr{};
     std::vector<uint64_t> ids;
-    std::vector<DevHinge> hinges;  // host copy of each joint as created (bodies, flags, limits, motor)
+    std::vector<DevHinge> hinges;  // host copy of each joint as created (bodies, flags, limits, motors)
+    std::vector<DevSwing> swings;
     float *d_state_rows = nullptr;  // 16 floats per body staging for get/set state
     float *h_pinned_rows = nullptr;
     DevCounters *h_ctr = nullptr;   // pinned mirror of the device counters
@@ -377,7 +379,7 @@ int cc_world_destroy(cc_world *W) {
                     w.cache_recs[1], w.cache_parity, w.root_flag, w.small_list, w.large_list, w.scratch_order,
                     w.scratch_colour, w.scratch_claim, w.mid_list, w.body_local, w.contact_event,
                     w.removed_keys, W->d_state_rows, w.hinges, w.island_joints, w.island_joint_count,
-                    w.island_joint_off, w.island_fill_j, w.joint_wake, w.joint_partners};
+                    w.island_joint_off, w.island_fill_j, w.joint_wake, w.joint_partners, w.swings};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : W->adj.allocs)
@@ -1134,34 +1136,42 @@ bool spring_ok(const cc_spring_settings &s) {
 }
 }  // namespace
 
-// grow the joint arrays (and create the per-island joint lists on first use)
-static int ensure_hinge_capacity(cc_world *W, int need) {
+// grow the joint arrays of one type and the per-island joint lists (created on first use)
+template <typename T>
+static int grow_joints(cc_world *W, T *&arr, int count, int &cap_io, int need) {
+    if (need <= cap_io) return CC_OK;
+    int cap = std::max(need, std::max(64, 2 * cap_io));
+    T *na = nullptr;
+    int r;
+    if ((r = dalloc(&na, cap)) != CC_OK) return r;
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    if (count > 0) CC_TRY(cudaMemcpy(na, arr, sizeof(T) * count, cudaMemcpyDeviceToDevice));
+    if (arr) cudaFree(arr);
+    arr = na;
+    cap_io = cap;
+    return CC_OK;
+}
+static int ensure_joint_capacity(cc_world *W, int need_hinges, int need_swings) {
     DevWorld &w = W->w;
+    int r;
     if (!w.island_joint_count) {
-        int r;
         if ((r = dalloc(&w.island_joint_count, w.cap)) != CC_OK || (r = dalloc(&w.island_joint_off, w.cap)) != CC_OK ||
             (r = dalloc(&w.island_fill_j, w.cap)) != CC_OK || (r = dalloc(&w.joint_wake, 1)) != CC_OK ||
             (r = dalloc(&w.joint_partners, (size_t)w.cap * JOINT_PARTNERS)) != CC_OK)
             return r;
         CC_TRY(cudaMemset(w.joint_partners, 0xff, sizeof(int) * (size_t)w.cap * JOINT_PARTNERS));
     }
-    if (need <= w.max_hinges) return CC_OK;
-    int cap = std::max(need, std::max(64, 2 * w.max_hinges));
-    DevHinge *nh = nullptr;
-    int *nl = nullptr;
-    int r;
-    if ((r = dalloc(&nh, cap)) != CC_OK) return r;
-    if ((r = dalloc(&nl, 3 * (size_t)cap)) != CC_OK) {
-        cudaFree(nh);
-        return r;
+    if ((r = grow_joints(W, w.hinges, w.num_hinges, w.max_hinges, need_hinges)) != CC_OK) return r;
+    if ((r = grow_joints(W, w.swings, w.num_swings, w.max_swings, need_swings)) != CC_OK) return r;
+    int need_lists = w.max_hinges + w.max_swings;
+    if (need_lists > w.max_joints) {
+        int *nl = nullptr;
+        if ((r = dalloc(&nl, 3 * (size_t)need_lists)) != CC_OK) return r;
+        CC_TRY(cudaStreamSynchronize(W->stream));
+        if (w.island_joints) cudaFree(w.island_joints);
+        w.island_joints = nl;
+        w.max_joints = need_lists;
     }
-    CC_TRY(cudaStreamSynchronize(W->stream));
-    if (w.num_hinges > 0) CC_TRY(cudaMemcpy(nh, w.hinges, sizeof(DevHinge) * w.num_hinges, cudaMemcpyDeviceToDevice));
-    if (w.hinges) cudaFree(w.hinges);
-    if (w.island_joints) cudaFree(w.island_joints);
-    w.hinges = nh;
-    w.island_joints = nl;
-    w.max_hinges = cap;
     drop_graph(W);
     return CC_OK;
 }
@@ -1183,11 +1193,13 @@ static int upload_partners(cc_world *W) {
         }
         over = true;
     };
-    for (const DevHinge &h : W->hinges) {
-        if (!(h.flags & JF_ENABLED)) continue;
+    auto add_joint = [&](const DevJointHead &h) {
+        if (!(h.flags & JF_ENABLED)) return;
         add(h.a, h.b);
         add(h.b, h.a);
-    }
+    };
+    for (const DevHinge &j : W->hinges) add_joint(j.h);
+    for (const DevSwing &j : W->swings) add_joint(j.h);
     CC_TRY(cudaStreamSynchronize(W->stream));
     CC_TRY(cudaMemcpy(w.joint_partners, part.data(), sizeof(int) * part.size(), cudaMemcpyHostToDevice));
     return over && w.skip_joint_pairs ? CC_ERR_CAPACITY : CC_OK;
@@ -1228,19 +1240,19 @@ int cc_world_add_hinges(cc_world *W, const cc_hinge_desc *d, int32_t n, int32_t 
         const cc_hinge_desc &h = d[i];
         DevHinge j;
         memset(&j, 0, sizeof(j));
-        j.a = h.body_a;
-        j.b = h.body_b;
-        j.index = w.num_hinges + i;
-        j.priority = h.priority;
-        j.island = -1;
-        DQ qa = dq(quat[j.a]), qb = dq(quat[j.b]);
+        j.h.a = h.body_a;
+        j.h.b = h.body_b;
+        j.h.index = w.num_hinges + i;
+        j.h.priority = h.priority;
+        j.h.island = -1;
+        DQ qa = dq(quat[j.h.a]), qb = dq(quat[j.h.b]);
         D3 h1 = dnormalize(d3(h.hinge_axis_a)), h2 = dnormalize(d3(h.hinge_axis_b));
         D3 n1 = dnormalize(d3(h.normal_axis_a)), n2 = dnormalize(d3(h.normal_axis_b));
         DQ inv_initial;
         if (h.space == CC_SPACE_WORLD) {
             DQ iqa = dconj(qa), iqb = dconj(qb);
-            j.lp1 = f3d(drot(iqa, dsub(d3(h.point_a), d3(com[j.a]))));
-            j.lp2 = f3d(drot(iqb, dsub(d3(h.point_b), d3(com[j.b]))));
+            j.lp1 = f3d(drot(iqa, dsub(d3(h.point_a), d3(com[j.h.a]))));
+            j.lp2 = f3d(drot(iqb, dsub(d3(h.point_b), d3(com[j.h.b]))));
             j.lh1 = f3d(drot(iqa, h1));
             j.lh2 = f3d(drot(iqb, h2));
             DQ r0 = inv_initial_orientation_xz(n1, h1, n2, h2);
@@ -1258,7 +1270,7 @@ int cc_world_add_hinges(cc_world *W, const cc_hinge_desc *d, int32_t n, int32_t 
         bool has_limits = !(mn <= -PI && mx >= PI);
         j.limits_min = has_limits ? (float)std::max(mn, -PI) : (float)-PI;
         j.limits_max = has_limits ? (float)std::min(mx, PI) : (float)PI;
-        j.flags = (h.enabled ? JF_ENABLED : 0) | (has_limits ? JF_LIMITS : 0);
+        j.h.flags = (h.enabled ? JF_ENABLED : 0) | (has_limits ? JF_LIMITS : 0);
         j.limits_spring_mode = h.limits_spring.mode;
         j.limits_freq = h.limits_spring.frequency_or_stiffness;
         j.limits_damping = h.limits_spring.damping;
@@ -1274,7 +1286,7 @@ int cc_world_add_hinges(cc_world *W, const cc_hinge_desc *d, int32_t n, int32_t 
         j.max_torque = h.max_torque_limit;
         made[i] = j;
     }
-    int r = ensure_hinge_capacity(W, w.num_hinges + n);
+    int r = ensure_joint_capacity(W, w.num_hinges + n, w.num_swings);
     if (r != CC_OK) return r;
     CC_TRY(cudaMemcpy(w.hinges + w.num_hinges, made.data(), sizeof(DevHinge) * n, cudaMemcpyHostToDevice));
     for (int i = 0; i < n; i++) {
@@ -1289,17 +1301,65 @@ int cc_world_add_hinges(cc_world *W, const cc_hinge_desc *d, int32_t n, int32_t 
 }  // extern "C"
 
 // read-modify-write of one joint's device record (the host copy follows)
+template <typename T, typename F>
+static int edit_joint(cc_world *W, T *dev, std::vector<T> &host, int count, int32_t index, F f) {
+    if (index < 0 || index >= count) return CC_ERR_INVALID;
+    T j;
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    CC_TRY(cudaMemcpy(&j, dev + index, sizeof(T), cudaMemcpyDeviceToHost));
+    f(j);
+    f(host[index]);
+    CC_TRY(cudaMemcpy(dev + index, &j, sizeof(T), cudaMemcpyHostToDevice));
+    return CC_OK;
+}
 template <typename F>
 static int edit_hinge(cc_world *W, int32_t index, F f) {
-    DevWorld &w = W->w;
-    if (index < 0 || index >= w.num_hinges) return CC_ERR_INVALID;
-    DevHinge j;
-    CC_TRY(cudaStreamSynchronize(W->stream));
-    CC_TRY(cudaMemcpy(&j, w.hinges + index, sizeof(DevHinge), cudaMemcpyDeviceToHost));
-    f(j);
-    f(W->hinges[index]);
-    CC_TRY(cudaMemcpy(w.hinges + index, &j, sizeof(DevHinge), cudaMemcpyHostToDevice));
-    return CC_OK;
+    return edit_joint(W, W->w.hinges, W->hinges, W->w.num_hinges, index, f);
+}
+template <typename F>
+static int edit_swing(cc_world *W, int32_t index, F f) {
+    return edit_joint(W, W->w.swings, W->swings, W->w.num_swings, index, f);
+}
+
+// SwingTwistConstraintPart.setLimits (swing-twist-constraint-part.ts:140-236) in FP64: a limit
+// inside +-0.5 degrees locks its axis, one beyond +-179.5 degrees frees it
+static void swing_set_limits(DevSwing &p) {
+    const double PI = 3.14159265358979323846;
+    const double locked = 0.5 * PI / 180.0, free_a = 179.5 * PI / 180.0;
+    double ymin = -p.plane_half_cone, ymax = p.plane_half_cone, zmin = -p.normal_half_cone, zmax = p.normal_half_cone;
+    p.y_half_min = (float)(0.5 * ymin);
+    p.y_half_max = (float)(0.5 * ymax);
+    p.z_half_min = (float)(0.5 * zmin);
+    p.z_half_max = (float)(0.5 * zmax);
+    p.rotation_flags = 0;
+    auto axis = [&](double mn, double mx, int lock_flag, int free_flag, float &smin, float &smax, float &cmin,
+                    float &cmax) {
+        if (mn > -locked && mx < locked) {
+            p.rotation_flags |= lock_flag;
+            smin = smax = 0.f;
+            cmin = cmax = 1.f;
+        } else if (mn < -free_a && mx > free_a) {
+            p.rotation_flags |= free_flag;
+            smin = -1.f;
+            smax = 1.f;
+            cmin = cmax = 0.f;
+        } else {
+            smin = (float)std::sin(0.5 * mn);
+            smax = (float)std::sin(0.5 * mx);
+            cmin = (float)std::cos(0.5 * mn);
+            cmax = (float)std::cos(0.5 * mx);
+        }
+    };
+    axis(p.twist_min, p.twist_max, ST_TWIST_LOCKED, ST_TWIST_FREE, p.sin_twist_min, p.sin_twist_max, p.cos_twist_min,
+         p.cos_twist_max);
+    axis(ymin, ymax, ST_SWING_Y_LOCKED, ST_SWING_Y_FREE, p.sin_y_min, p.sin_y_max, p.cos_y_min, p.cos_y_max);
+    axis(zmin, zmax, ST_SWING_Z_LOCKED, ST_SWING_Z_FREE, p.sin_z_min, p.sin_z_max, p.cos_z_min, p.cos_z_max);
+}
+// setTargetOrientationCS (swing-twist-constraint.ts:405-416): the target clamped into the limits
+static void swing_set_target(DevSwing &p, const float *q) {
+    float4 o = make_float4(q[0], q[1], q[2], q[3]), sw, tw;
+    get_swing_twist(o, sw, tw);
+    p.target_q = clamp_swing_twist(p, sw, tw) != 0 ? qmul(sw, tw) : o;
 }
 
 extern "C" {
@@ -1312,7 +1372,7 @@ int cc_world_set_hinge_limits(cc_world *W, int32_t index, float limits_min, floa
         j.limits_min = (float)mn;
         j.limits_max = (float)mx;
         bool has = mn > -PI || mx < PI;
-        j.flags = has ? (j.flags | JF_LIMITS) : (j.flags & ~JF_LIMITS);
+        j.h.flags = has ? (j.h.flags | JF_LIMITS) : (j.h.flags & ~JF_LIMITS);
         if (has) j.target_angle = (float)std::max(mn, std::min(mx, (double)j.target_angle));
     });
 }
@@ -1325,7 +1385,7 @@ int cc_world_set_hinge_motor(cc_world *W, int32_t index, int32_t motor_state, fl
     return edit_hinge(W, index, [&](DevHinge &j) {  // hinge-constraint.ts:441-465
         j.motor_state = motor_state;
         j.target_angular_velocity = target_angular_velocity;
-        j.target_angle = (j.flags & JF_LIMITS)
+        j.target_angle = (j.h.flags & JF_LIMITS)
                              ? (float)std::max((double)j.limits_min, std::min((double)j.limits_max, (double)target_angle))
                              : target_angle;
     });
@@ -1333,7 +1393,8 @@ int cc_world_set_hinge_motor(cc_world *W, int32_t index, int32_t motor_state, fl
 
 int cc_world_set_hinge_enabled(cc_world *W, int32_t index, int32_t enabled) {
     if (!W) return CC_ERR_INVALID;
-    int r = edit_hinge(W, index, [&](DevHinge &j) { j.flags = enabled ? (j.flags | JF_ENABLED) : (j.flags & ~JF_ENABLED); });
+    int r = edit_hinge(W, index,
+                       [&](DevHinge &j) { j.h.flags = enabled ? (j.h.flags | JF_ENABLED) : (j.h.flags & ~JF_ENABLED); });
     if (r != CC_OK) return r;
     return upload_partners(W);
 }
@@ -1349,10 +1410,147 @@ int cc_world_get_hinge_angles(cc_world *W, float *out, int32_t capacity) {
     return capacity < w.num_hinges ? CC_ERR_CAPACITY : CC_OK;
 }
 
+int cc_world_add_swing_twists(cc_world *W, const cc_swing_twist_desc *d, int32_t n, int32_t *out_index) {
+    if (!W || (!d && n > 0) || n < 0) return CC_ERR_INVALID;
+    if (n == 0) return CC_OK;
+    DevWorld &w = W->w;
+    for (int i = 0; i < n; i++) {
+        const cc_swing_twist_desc &h = d[i];
+        if (h.body_a < 0 || h.body_b < 0 || h.body_a >= w.n || h.body_b >= w.n) return CC_ERR_INVALID;
+        if (h.space != CC_SPACE_WORLD && h.space != CC_SPACE_LOCAL) return CC_ERR_INVALID;
+        if (h.swing_type != CC_SWING_CONE && h.swing_type != CC_SWING_PYRAMID) return CC_ERR_INVALID;
+        if (h.swing_motor_state < 0 || h.swing_motor_state > 2 || h.twist_motor_state < 0 || h.twist_motor_state > 2)
+            return CC_ERR_INVALID;
+        if (!spring_ok(h.swing_motor_spring) || !spring_ok(h.twist_motor_spring)) return CC_ERR_INVALID;
+        if (!finite3(h.position_a) || !finite3(h.position_b) || !finite3(h.twist_axis_a) || !finite3(h.plane_axis_a) ||
+            !finite3(h.twist_axis_b) || !finite3(h.plane_axis_b) || !finite3(h.target_angular_velocity))
+            return CC_ERR_INVALID;
+        if (!std::isfinite(h.normal_half_cone_angle) || !std::isfinite(h.plane_half_cone_angle) ||
+            !std::isfinite(h.twist_min_angle) || !std::isfinite(h.twist_max_angle) || std::isnan(h.max_friction_torque))
+            return CC_ERR_INVALID;
+        for (int k = 0; k < 4; k++)
+            if (!std::isfinite(h.target_orientation[k])) return CC_ERR_INVALID;
+    }
+    std::vector<float4> quat((size_t)w.n), com((size_t)w.n);
+    std::vector<int> world((size_t)w.n);
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    CC_TRY(cudaMemcpy(quat.data(), w.quat, sizeof(float4) * w.n, cudaMemcpyDeviceToHost));
+    CC_TRY(cudaMemcpy(com.data(), w.com, sizeof(float4) * w.n, cudaMemcpyDeviceToHost));
+    CC_TRY(cudaMemcpy(world.data(), w.world, sizeof(int) * w.n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; i++)
+        if (world[d[i].body_a] != world[d[i].body_b]) return CC_ERR_INVALID;
+    std::vector<DevSwing> made((size_t)n);
+    for (int i = 0; i < n; i++) {
+        const cc_swing_twist_desc &h = d[i];
+        DevSwing j;
+        memset(&j, 0, sizeof(j));
+        j.h.a = h.body_a;
+        j.h.b = h.body_b;
+        j.h.index = w.num_swings + i;
+        j.h.priority = h.priority;
+        j.h.island = -1;
+        j.h.flags = h.enabled ? JF_ENABLED : 0;
+        // constraint space: X twist, Y normal = plane x twist, Z plane (create :218-260)
+        D3 t1 = dnormalize(d3(h.twist_axis_a)), p1 = dnormalize(d3(h.plane_axis_a));
+        D3 t2 = dnormalize(d3(h.twist_axis_b)), p2 = dnormalize(d3(h.plane_axis_b));
+        DQ c1 = quat_from_columns(t1, dcross(p1, t1), p1), c2 = quat_from_columns(t2, dcross(p2, t2), p2);
+        if (h.space == CC_SPACE_WORLD) {
+            DQ iqa = dconj(dq(quat[j.h.a])), iqb = dconj(dq(quat[j.h.b]));
+            j.lp1 = f3d(drot(iqa, dsub(d3(h.position_a), d3(com[j.h.a]))));
+            j.lp2 = f3d(drot(iqb, dsub(d3(h.position_b), d3(com[j.h.b]))));
+            c1 = dqmul(iqa, c1);
+            c2 = dqmul(iqb, c2);
+        } else {
+            j.lp1 = f3d(d3(h.position_a));
+            j.lp2 = f3d(d3(h.position_b));
+        }
+        j.c2b1 = make_float4((float)c1.x, (float)c1.y, (float)c1.z, (float)c1.w);
+        j.c2b2 = make_float4((float)c2.x, (float)c2.y, (float)c2.z, (float)c2.w);
+        j.swing_type = h.swing_type;
+        j.normal_half_cone = h.normal_half_cone_angle;
+        j.plane_half_cone = h.plane_half_cone_angle;
+        j.twist_min = h.twist_min_angle;
+        j.twist_max = h.twist_max_angle;
+        swing_set_limits(j);
+        j.max_friction_torque = h.max_friction_torque;
+        j.swing_motor_state = h.swing_motor_state;
+        j.twist_motor_state = h.twist_motor_state;
+        j.target_w = make_float3(h.target_angular_velocity[0], h.target_angular_velocity[1], h.target_angular_velocity[2]);
+        swing_set_target(j, h.target_orientation);
+        j.swing_spring_mode = h.swing_motor_spring.mode;
+        j.swing_freq = h.swing_motor_spring.frequency_or_stiffness;
+        j.swing_damping = h.swing_motor_spring.damping;
+        j.twist_spring_mode = h.twist_motor_spring.mode;
+        j.twist_freq = h.twist_motor_spring.frequency_or_stiffness;
+        j.twist_damping = h.twist_motor_spring.damping;
+        j.swing_min_torque = h.swing_min_torque_limit;
+        j.swing_max_torque = h.swing_max_torque_limit;
+        j.twist_min_torque = h.twist_min_torque_limit;
+        j.twist_max_torque = h.twist_max_torque_limit;
+        made[i] = j;
+    }
+    int r = ensure_joint_capacity(W, w.num_hinges, w.num_swings + n);
+    if (r != CC_OK) return r;
+    CC_TRY(cudaMemcpy(w.swings + w.num_swings, made.data(), sizeof(DevSwing) * n, cudaMemcpyHostToDevice));
+    for (int i = 0; i < n; i++) {
+        W->swings.push_back(made[i]);
+        if (out_index) out_index[i] = w.num_swings + i;
+    }
+    w.num_swings += n;
+    drop_graph(W);
+    return upload_partners(W);
+}
+
+int cc_world_set_swing_twist_limits(cc_world *W, int32_t index, float normal_half_cone_angle,
+                                    float plane_half_cone_angle, float twist_min_angle, float twist_max_angle) {
+    if (!W || !std::isfinite(normal_half_cone_angle) || !std::isfinite(plane_half_cone_angle) ||
+        !std::isfinite(twist_min_angle) || !std::isfinite(twist_max_angle))
+        return CC_ERR_INVALID;
+    return edit_swing(W, index, [&](DevSwing &j) {  // setNormalHalfConeAngle ... setTwistMaxAngle :319-341
+        j.normal_half_cone = normal_half_cone_angle;
+        j.plane_half_cone = plane_half_cone_angle;
+        j.twist_min = twist_min_angle;
+        j.twist_max = twist_max_angle;
+        swing_set_limits(j);
+    });
+}
+
+int cc_world_set_swing_twist_motor(cc_world *W, int32_t index, int32_t swing_motor_state, int32_t twist_motor_state,
+                                   const float *target_angular_velocity, const float *target_orientation,
+                                   float max_friction_torque) {
+    if (!W || swing_motor_state < 0 || swing_motor_state > 2 || twist_motor_state < 0 || twist_motor_state > 2 ||
+        !target_angular_velocity || !target_orientation || !finite3(target_angular_velocity) ||
+        std::isnan(max_friction_torque))
+        return CC_ERR_INVALID;
+    for (int k = 0; k < 4; k++)
+        if (!std::isfinite(target_orientation[k])) return CC_ERR_INVALID;
+    return edit_swing(W, index, [&](DevSwing &j) {  // :343-416
+        if (j.swing_motor_state != swing_motor_state) {  // setSwingMotorState resets all three motor parts
+            j.swing_motor_state = swing_motor_state;
+            for (int k = 0; k < 3; k++) j.motor[k].eff = j.motor[k].lambda = 0.f;
+        }
+        if (j.twist_motor_state != twist_motor_state) {  // setTwistMotorState resets the twist part
+            j.twist_motor_state = twist_motor_state;
+            j.motor[0].eff = j.motor[0].lambda = 0.f;
+        }
+        j.target_w = make_float3(target_angular_velocity[0], target_angular_velocity[1], target_angular_velocity[2]);
+        swing_set_target(j, target_orientation);
+        j.max_friction_torque = max_friction_torque;
+    });
+}
+
+int cc_world_set_swing_twist_enabled(cc_world *W, int32_t index, int32_t enabled) {
+    if (!W) return CC_ERR_INVALID;
+    int r = edit_swing(W, index,
+                       [&](DevSwing &j) { j.h.flags = enabled ? (j.h.flags | JF_ENABLED) : (j.h.flags & ~JF_ENABLED); });
+    if (r != CC_OK) return r;
+    return upload_partners(W);
+}
+
 int cc_world_set_skip_joint_pairs(cc_world *W, int32_t on) {
     if (!W) return CC_ERR_INVALID;
     W->w.skip_joint_pairs = on ? 1 : 0;
-    int r = ensure_hinge_capacity(W, 0);
+    int r = ensure_joint_capacity(W, 0, 0);
     if (r != CC_OK) return r;
     drop_graph(W);
     return upload_partners(W);

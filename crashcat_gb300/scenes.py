@@ -15,7 +15,8 @@ import numpy as np
 from typing import Optional
 
 from ._lib import (BODY_DTYPE, COMBINE_GEOMETRIC_MEAN, COMBINE_MAX, DYNAMIC, MOTOR_OFF, MOTOR_POSITION,
-                   MOTOR_VELOCITY, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_SPHERE, STATIC, hinge_defaults)
+                   MOTOR_VELOCITY, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_SPHERE, STATIC, SWING_CONE, SWING_PYRAMID,
+                   hinge_defaults, swing_twist_defaults)
 
 # object layers of the reference's test helper (tst/helpers.ts:5-26)
 LAYER_MOVING = 0
@@ -42,7 +43,9 @@ class Scene:
     num_worlds: int = 1
     seed: int = 0
     hinges: Optional[np.ndarray] = None  # cc_hinge_desc records (_lib.HINGE_DTYPE)
+    swings: Optional[np.ndarray] = None  # cc_swing_twist_desc records (_lib.SWING_TWIST_DTYPE)
     skip_joint_pairs: bool = False
+    gravity: tuple = (0.0, -9.81, 0.0)
 
     @property
     def n(self) -> int:
@@ -462,3 +465,199 @@ def hinge_motors(n: int = 6, seed: int = 81) -> Scene:
         h[5]["limits_min"], h[5]["limits_max"] = -np.radians(20.0), np.radians(70.0)
     b["allow_sleeping"][:] = 0
     return Scene("hinge_motors", b, dt=1.0 / 60.0, steps=90, seed=seed, hinges=h)
+
+
+def _qmul(a, b):
+    ax, ay, az, aw = a
+    bx, by, bz, bw = b
+    return np.array([aw * bx + ax * bw + ay * bz - az * by, aw * by - ax * bz + ay * bw + az * bx,
+                     aw * bz + ax * by - ay * bx + az * bw, aw * bw - ax * bx - ay * by - az * bz])
+
+
+def _qrot(q, v):
+    u = np.asarray(q[:3], dtype=np.float64)
+    t = 2.0 * np.cross(u, v)
+    return np.asarray(v, dtype=np.float64) + q[3] * t + np.cross(u, t)
+
+
+def _tangent(axis):
+    """getTangent of the ragdoll example (examples/src/example-ragdoll.ts:431-445)."""
+    ax, ay, az = np.abs(axis)
+    if ax <= ay and ax <= az:
+        t = np.array([0.0, -axis[2], axis[1]])
+    elif ay <= az:
+        t = np.array([axis[2], 0.0, -axis[0]])
+    else:
+        t = np.array([-axis[1], axis[0], 0.0])
+    return t / np.linalg.norm(t)
+
+
+# ragdoll topology of examples/src/example-ragdoll.ts:75-301 at scale 1.8, with capsule parts:
+# part -> (centre in the ragdoll frame, limb axis, length, thickness)
+def _ragdoll_parts(scale: float = 1.8):
+    sd, ual, lal, uas, las = 0.45 * scale, 0.4 * scale, 0.4 * scale, 0.15 * scale, 0.15 * scale
+    nl, hr, ubl, pl, ps = 0.1 * scale, 0.2 * scale, 0.6 * scale, 0.2 * scale, 0.25 * scale
+    ull, uls, lls, lll = 0.5 * scale, 0.15 * scale, 0.15 * scale, 0.5 * scale
+    lower_leg_y = lll / 2
+    upper_leg_y = lower_leg_y + lll / 2 + ull / 2
+    pelvis_y = upper_leg_y + ull / 2 + pl / 2
+    upper_body_y = pelvis_y + pl / 2 + ubl / 2
+    head_y = upper_body_y + ubl / 2 + hr / 2 + nl
+    arm_y = upper_body_y + ubl / 2
+    Y, X = (0.0, 1.0, 0.0), (1.0, 0.0, 0.0)
+    parts = {
+        "upper_body": ((0, upper_body_y, 0), Y, ubl, sd * 0.6),
+        "head": ((0, head_y, 0), Y, hr * 1.4, hr * 1.2),
+        "upper_left_arm": ((-sd / 2 - ual / 2, arm_y, 0), X, ual, uas),
+        "lower_left_arm": ((-sd / 2 - ual - lal / 2, arm_y, 0), X, lal, las),
+        "upper_right_arm": ((sd / 2 + ual / 2, arm_y, 0), X, ual, uas),
+        "lower_right_arm": ((sd / 2 + ual + lal / 2, arm_y, 0), X, lal, las),
+        "pelvis": ((0, pelvis_y, 0), Y, pl, ps),
+        "upper_left_leg": ((-sd / 3, upper_leg_y, 0), Y, ull, uls),
+        "lower_left_leg": ((-sd / 3, lower_leg_y, 0), Y, lll, lls),
+        "upper_right_leg": ((sd / 3, upper_leg_y, 0), Y, ull, uls),
+        "lower_right_leg": ((sd / 3, lower_leg_y, 0), Y, lll, lls),
+    }
+    # joints: (kind, body A, body B, pivot in the ragdoll frame, twist / hinge axis)
+    joints = [
+        ("swing", "head", "upper_body", (0, upper_body_y + ubl / 2, 0), Y),                  # neck
+        ("hinge", "lower_left_leg", "upper_left_leg", (-sd / 3, lll, 0), X),                 # knees
+        ("hinge", "lower_right_leg", "upper_right_leg", (sd / 3, lll, 0), X),
+        ("swing", "upper_left_leg", "pelvis", (-sd / 3, upper_leg_y + ull / 2, 0), Y),       # hips
+        ("swing", "upper_right_leg", "pelvis", (sd / 3, upper_leg_y + ull / 2, 0), Y),
+        ("swing", "pelvis", "upper_body", (0, pelvis_y + pl / 2, 0), Y),                     # spine
+        ("swing", "upper_body", "upper_left_arm", (-sd / 2, arm_y, 0), X),                   # shoulders
+        ("swing", "upper_body", "upper_right_arm", (sd / 2, arm_y, 0), X),
+        ("hinge", "lower_left_arm", "upper_left_arm", (-sd / 2 - ual, arm_y, 0), (0.0, 0.0, 1.0)),  # elbows
+        ("hinge", "lower_right_arm", "upper_right_arm", (sd / 2 + ual, arm_y, 0), (0.0, 0.0, 1.0)),
+    ]
+    return parts, joints
+
+
+def ragdolls(num: int = 2000, seed: int = 3, arena: float = 60.0, spacing: float = 4.4,
+             cone_deg=(30.0, 80.0), twist_deg: float = 45.0) -> Scene:
+    """Jointed ragdolls: per ragdoll 11 capsule bodies (the ragdoll example's parts and
+    sizes at scale 1.8) joined by 4 hinges (knees, elbows) and 6 swing-twist joints (neck,
+    spine, hips, shoulders; cone half-angles drawn from U(30, 80) degrees per joint, twist
+    limits +-45 degrees, motors off), each ragdoll at a seeded random orientation on a grid
+    inside an arena of 6 static walls (a 60 m box).  Joined bodies do not collide (the
+    ragdoll example's pair filter); dt 1/60, 12 velocity / 4 position iterations."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    parts, joints = _ragdoll_parts()
+    names = list(parts)
+    nb_r = len(names)
+    walls = 6
+    b = blank_bodies(walls + num * nb_r)
+    half = arena / 2
+    t = 1.0
+    wall_specs = [((half + t, t, half + t), (0, -t, 0)), ((half + t, t, half + t), (0, arena + t, 0)),
+                  ((t, half, half + t), (-half - t, half, 0)), ((t, half, half + t), (half + t, half, 0)),
+                  ((half + t, half, t), (0, half, -half - t)), ((half + t, half, t), (0, half, half + t))]
+    for k, (he, pos) in enumerate(wall_specs):
+        set_box(b, k, he)
+        b["motion_type"][k] = STATIC
+        b["object_layer"][k] = LAYER_NOT_MOVING
+        b["position"][k] = pos
+        b["friction"][k] = 0.5
+    n_side = int(math.floor((arena - 2.0) / spacing))
+    cells = [(i, j, k) for j in range(n_side) for i in range(n_side) for k in range(n_side)]
+    assert num <= len(cells), "arena too small for that many ragdolls"
+    h_all = hinge_defaults(num * 4)
+    s_all = swing_twist_defaults(num * 6)
+    hk = sk = 0
+    centre = np.array([0.0, 1.6, 0.0])
+    for r in range(num):
+        i, j, k = cells[r]
+        origin = np.array([-half + 1.0 + spacing * (i + 0.5), 1.0 + spacing * (j + 0.5), -half + 1.0 + spacing * (k + 0.5)])
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        base = walls + r * nb_r
+        idx = {}
+        for p, name in enumerate(names):
+            c, axis, length, thick = parts[name]
+            bi = base + p
+            idx[name] = bi
+            radius = thick / 2
+            set_capsule(b, bi, radius, max(length / 2 - radius, 0.05))
+            b["position"][bi] = origin + _qrot(q, np.asarray(c) - centre)
+            # capsules lie along local Y: arms are turned onto X
+            qp = np.array([0.0, 0.0, -math.sin(math.pi / 4), math.cos(math.pi / 4)]) if axis[0] else np.array([0, 0, 0, 1.0])
+            b["quaternion"][bi] = _qmul(q, qp)
+            b["restitution"][bi] = 0.0
+        for kind, na, nbn, piv, axis in joints:
+            pw = origin + _qrot(q, np.asarray(piv, dtype=np.float64) - centre)
+            aw = _qrot(q, np.asarray(axis, dtype=np.float64))
+            if kind == "hinge":
+                h = h_all[hk]
+                hk += 1
+                h["body_a"], h["body_b"] = idx[na], idx[nbn]
+                h["point_a"] = h["point_b"] = pw
+                h["hinge_axis_a"] = h["hinge_axis_b"] = aw
+                limb = _qrot(q, np.array([1.0, 0, 0]) if axis[2] else np.array([0, 1.0, 0]))
+                h["normal_axis_a"] = h["normal_axis_b"] = limb
+                h["limits_min"], h["limits_max"] = (-2.0, 0.05) if axis[0] else (-0.05, 2.2)
+            else:
+                sj = s_all[sk]
+                sk += 1
+                sj["body_a"], sj["body_b"] = idx[na], idx[nbn]
+                sj["position_a"] = sj["position_b"] = pw
+                pl = _qrot(q, _tangent(np.asarray(axis, dtype=np.float64)))
+                sj["twist_axis_a"] = sj["twist_axis_b"] = aw
+                sj["plane_axis_a"] = sj["plane_axis_b"] = pl
+                sj["swing_type"] = SWING_CONE
+                cone = np.radians(rng.uniform(*cone_deg))
+                sj["normal_half_cone_angle"] = sj["plane_half_cone_angle"] = cone
+                sj["twist_min_angle"], sj["twist_max_angle"] = -np.radians(twist_deg), np.radians(twist_deg)
+    return Scene("ragdolls", b, dt=1.0 / 60.0, steps=600, velocity_iterations=12, position_iterations=4,
+                 seed=seed, hinges=h_all, swings=s_all, skip_joint_pairs=True)
+
+
+def swing_twist_chains(seed: int = 91) -> Scene:
+    """Four chains of five boxes (0.2 x 0.8 x 0.2 m) hung from static anchors by swing-twist
+    joints and released tilted 60 degrees, so that the cone limits engage: a cone of 30
+    degrees, an elliptic cone (20 and 50 degrees), a pyramid of +-30 degrees about Z and +-20
+    degrees about Y, and a chain with its twist and its swing about Y
+    locked (limits inside +-0.5 degrees) and its swing about Z limited to 40 degrees; each link
+    starts with a spin about its own axis so that the twist limits (+-15 degrees) engage too."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    links, chains = 5, 4
+    b = blank_bodies(chains * (links + 1))
+    sj = swing_twist_defaults(chains * links)
+    tilt = math.radians(60.0)
+    d = np.array([math.sin(tilt), -math.cos(tilt), 0.0])  # chain direction, down and out
+    qt = np.array([0.0, 0.0, math.sin(tilt / 2), math.cos(tilt / 2)])
+    k = 0
+    for c in range(chains):
+        a = c * (links + 1)
+        set_box(b, a, (0.1, 0.1, 0.1))
+        b["motion_type"][a] = STATIC
+        b["object_layer"][a] = LAYER_NOT_MOVING
+        top = np.array([0.0, 8.0, 3.0 * c])
+        b["position"][a] = top
+        prev = a
+        for i in range(links):
+            j = a + 1 + i
+            set_box(b, j, (0.1, 0.4, 0.1))
+            b["position"][j] = top + d * (0.5 + i * 1.0)
+            b["quaternion"][j] = qt
+            b["angular_velocity"][j] = d * rng.uniform(2.0, 4.0)
+            h = sj[k]
+            h["body_a"], h["body_b"] = prev, j
+            h["position_a"] = h["position_b"] = top + d * (i * 1.0)
+            h["twist_axis_a"] = h["twist_axis_b"] = d
+            h["plane_axis_a"] = h["plane_axis_b"] = (0.0, 0.0, 1.0)
+            h["twist_min_angle"], h["twist_max_angle"] = -math.radians(15.0), math.radians(15.0)
+            if c == 0:
+                h["normal_half_cone_angle"] = h["plane_half_cone_angle"] = math.radians(30.0)
+            elif c == 1:
+                h["normal_half_cone_angle"], h["plane_half_cone_angle"] = math.radians(20.0), math.radians(50.0)
+            elif c == 2:
+                h["swing_type"] = SWING_PYRAMID
+                h["normal_half_cone_angle"], h["plane_half_cone_angle"] = math.radians(30.0), math.radians(20.0)
+            else:
+                h["normal_half_cone_angle"], h["plane_half_cone_angle"] = math.radians(40.0), math.radians(0.2)
+                h["twist_min_angle"], h["twist_max_angle"] = 0.0, 0.0
+            prev = j
+            k += 1
+    b["allow_sleeping"][:] = 0
+    return Scene("swing_twist_chains", b, dt=1.0 / 60.0, steps=90, seed=seed, swings=sj, skip_joint_pairs=True)

@@ -366,6 +366,32 @@ class GpuWorld:
         check(self._lib.cc_world_get_hinge_angles(self.handle, ptr(out), n), "cc_world_get_hinge_angles")
         return out[:n]
 
+    def add_swing_twists(self, joints: np.ndarray) -> np.ndarray:
+        """cc_world_add_swing_twists: records of _lib.SWING_TWIST_DTYPE; returns the joint indices."""
+        joints = np.ascontiguousarray(joints, dtype=_lib.SWING_TWIST_DTYPE)
+        out = np.zeros(len(joints), dtype=np.int32)
+        check(self._lib.cc_world_add_swing_twists(self.handle, ptr(joints), len(joints), ptr(out)),
+              "cc_world_add_swing_twists")
+        return out
+
+    def set_swing_twist_limits(self, index: int, normal_half_cone: float, plane_half_cone: float,
+                               twist_min: float, twist_max: float) -> None:
+        check(self._lib.cc_world_set_swing_twist_limits(self.handle, index, C.c_float(normal_half_cone),
+                                                        C.c_float(plane_half_cone), C.c_float(twist_min),
+                                                        C.c_float(twist_max)), "cc_world_set_swing_twist_limits")
+
+    def set_swing_twist_motor(self, index: int, swing_state: int, twist_state: int, target_angular_velocity=(0, 0, 0),
+                              target_orientation=(0, 0, 0, 1), max_friction_torque: float = 0.0) -> None:
+        tw = np.asarray(target_angular_velocity, dtype=np.float32)
+        tq = np.asarray(target_orientation, dtype=np.float32)
+        check(self._lib.cc_world_set_swing_twist_motor(self.handle, index, swing_state, twist_state, ptr(tw), ptr(tq),
+                                                       C.c_float(max_friction_torque)),
+              "cc_world_set_swing_twist_motor")
+
+    def set_swing_twist_enabled(self, index: int, enabled: bool) -> None:
+        check(self._lib.cc_world_set_swing_twist_enabled(self.handle, index, int(bool(enabled))),
+              "cc_world_set_swing_twist_enabled")
+
     def set_skip_joint_pairs(self, on: bool) -> None:
         check(self._lib.cc_world_set_skip_joint_pairs(self.handle, int(bool(on))), "cc_world_set_skip_joint_pairs")
 

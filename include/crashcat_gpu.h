@@ -27,6 +27,13 @@
  *                                 addContactConstraint        src/constraints/contact-constraints.ts:437
  *   cc_world_get_contact_events <- Listener.onContactAdded / onContactPersisted /
  *                                 onContactRemoved, as a post-step buffer  src/listener.ts:58-98
+ *   cc_world_add_hinges        <- hingeConstraint.create     src/constraints/hinge-constraint.ts:240-387
+ *   cc_world_set_hinge_*       <- hingeConstraint setters    src/constraints/hinge-constraint.ts:429-465
+ *   cc_world_get_hinge_angles  <- hingeConstraint.getCurrentAngle  src/constraints/hinge-constraint.ts:467-474
+ *   cc_world_add_swing_twists  <- swingTwistConstraint.create src/constraints/swing-twist-constraint.ts:180-296
+ *   cc_world_set_swing_twist_* <- swingTwistConstraint setters src/constraints/swing-twist-constraint.ts:319-416
+ *   cc_world_set_skip_joint_pairs <- a Listener.onBodyPairValidate rejecting joined bodies
+ *                                 src/broadphase/broadphase.ts:112-123
  *   cc_world_get_stats         <- (no counterpart: per-step counters)
  *   cc_status_string           <- assert() messages          src/utils/assert.ts:1-9
  */
@@ -230,6 +237,53 @@ int cc_world_set_hinge_enabled(cc_world *world, int32_t index, int32_t enabled);
 
 /* getCurrentAngle (hinge-constraint.ts:467-474) of every joint, n floats. */
 int cc_world_get_hinge_angles(cc_world *world, float *out, int32_t capacity);
+
+/* ---------------------------------------------------------------------------
+ * Swing-twist joints (src/constraints/swing-twist-constraint.ts), the ragdoll
+ * joint: a point constraint plus swing limits (a cone, or a pyramid, about the
+ * constraint's Y and Z axes) and twist limits (about its X axis), with optional
+ * swing and twist motors.  SwingTwistConstraintSettings
+ * (swing-twist-constraint.ts:121-159) flattened; constraint space X = twist
+ * axis, Z = plane axis, Y = plane x twist.  Joints of both types share the
+ * island solve: ordered by (priority, per-type creation index, type).
+ * ------------------------------------------------------------------------- */
+enum cc_swing_type { CC_SWING_CONE = 0, CC_SWING_PYRAMID = 1 };
+
+typedef struct cc_swing_twist_desc {
+    int32_t body_a, body_b;
+    int32_t space;                             /* cc_constraint_space */
+    float position_a[3], position_b[3];        /* pivot on each body */
+    float twist_axis_a[3], plane_axis_a[3];    /* normalised on creation */
+    float twist_axis_b[3], plane_axis_b[3];
+    int32_t swing_type;                        /* cc_swing_type */
+    float normal_half_cone_angle;              /* swing limit about Z, radians */
+    float plane_half_cone_angle;               /* swing limit about Y, radians */
+    float twist_min_angle, twist_max_angle;    /* radians, in [-pi, pi] */
+    float max_friction_torque;                 /* N m while a motor is off */
+    int32_t swing_motor_state, twist_motor_state;  /* cc_motor_state */
+    float target_angular_velocity[3];          /* rad/s, constraint space of body B */
+    float target_orientation[4];               /* constraint space (x y z w); clamped to the limits */
+    cc_spring_settings swing_motor_spring, twist_motor_spring;
+    float swing_min_torque_limit, swing_max_torque_limit;
+    float twist_min_torque_limit, twist_max_torque_limit;
+    int32_t priority;
+    int32_t enabled;
+} cc_swing_twist_desc;
+
+/* swingTwistConstraint.create (swing-twist-constraint.ts:180-296) for n joints. */
+int cc_world_add_swing_twists(cc_world *world, const cc_swing_twist_desc *joints, int32_t n, int32_t *out_index);
+
+/* setNormalHalfConeAngle / setPlaneHalfConeAngle / setTwistMinAngle / setTwistMaxAngle
+ * (swing-twist-constraint.ts:319-341) of one joint. */
+int cc_world_set_swing_twist_limits(cc_world *world, int32_t index, float normal_half_cone_angle,
+                                    float plane_half_cone_angle, float twist_min_angle, float twist_max_angle);
+/* setSwingMotorState / setTwistMotorState (a change resets the motor parts' impulses),
+ * setTargetAngularVelocityCS, setTargetOrientationCS, setMaxFrictionTorque
+ * (swing-twist-constraint.ts:343-416); target_angular_velocity 3 floats, target_orientation 4. */
+int cc_world_set_swing_twist_motor(cc_world *world, int32_t index, int32_t swing_motor_state,
+                                   int32_t twist_motor_state, const float *target_angular_velocity,
+                                   const float *target_orientation, float max_friction_torque);
+int cc_world_set_swing_twist_enabled(cc_world *world, int32_t index, int32_t enabled);
 
 /* on != 0: the broadphase skips body pairs that share an enabled joint, the declarative form
  * of a Listener.onBodyPairValidate that rejects them (src/broadphase/broadphase.ts:112-123; the

@@ -149,6 +149,7 @@ struct World {
     // at the listener call sites (contact-constraints.ts:494-499, contacts.ts:305-307)
     std::vector<std::array<int64_t, 3>> events;
     std::vector<HingeJoint> joints;
+    std::vector<SwingTwistJoint> swings;
     // skip broadphase pairs of bodies that share an enabled joint: the declarative form of the
     // ragdoll example's onBodyPairValidate (examples/src/example-ragdoll.ts:487-489)
     bool skipJointPairs = false;
@@ -446,12 +447,37 @@ static void bvh_build(const std::vector<Body> &bodies, std::vector<int> &idx, st
     nodes[ni].right = r;
 }
 
+// User joints of every type under one id: hinges are 0.., swing-twists JOINT_SWING + index.
+// joint_ids lists them type by type, each in creation order, the order in which the
+// reference walks its constraint pools (constraints.ts:264-318, islands.ts:210-225).
+constexpr int JOINT_SWING = 1 << 24;
+struct JointInfo {
+    int a, b, priority, index, type;
+    bool enabled;
+};
+static std::vector<int> joint_ids(const World &w) {
+    std::vector<int> ids;
+    for (size_t i = 0; i < w.joints.size(); i++) ids.push_back((int)i);
+    for (size_t i = 0; i < w.swings.size(); i++) ids.push_back(JOINT_SWING + (int)i);
+    return ids;
+}
+static JointInfo joint_info(const World &w, int id) {
+    if (id >= JOINT_SWING) {
+        const SwingTwistJoint &j = w.swings[id - JOINT_SWING];
+        return {j.a, j.b, j.priority, j.index, 6, j.enabled};  // ConstraintType.SWING_TWIST
+    }
+    const HingeJoint &j = w.joints[id];
+    return {j.a, j.b, j.priority, j.index, 2, j.enabled};  // ConstraintType.HINGE
+}
+
 static void find_colliding_pairs(World &w) {
     w.pairs.clear();
     std::set<std::pair<int, int>> joined;  // body pairs that share an enabled joint
     if (w.skipJointPairs)
-        for (const HingeJoint &j : w.joints)
-            if (j.enabled) joined.insert({std::min(j.a, j.b), std::max(j.a, j.b)});
+        for (int id : joint_ids(w)) {
+            JointInfo ji = joint_info(w, id);
+            if (ji.enabled) joined.insert({std::min(ji.a, ji.b), std::max(ji.a, ji.b)});
+        }
     std::vector<int> idx(w.bodies.size());
     std::iota(idx.begin(), idx.end(), 0);
     std::vector<BvhNode> nodes;
@@ -1038,14 +1064,15 @@ static void build_islands(World &w) {
         contactLinks[ci] = std::min(A.activeIndex, B.activeIndex);
     }
     // linkUserConstraints islands.ts:209-224, linkConstraint :163-178
-    std::vector<int64_t> jointLinks(w.joints.size(), INACTIVE);
-    for (size_t ji = 0; ji < w.joints.size(); ji++) {
-        const HingeJoint &j = w.joints[ji];
+    std::vector<int> jointIds = joint_ids(w);
+    std::vector<int64_t> jointLinks(jointIds.size(), INACTIVE);
+    for (size_t k = 0; k < jointIds.size(); k++) {
+        JointInfo j = joint_info(w, jointIds[k]);
         if (!j.enabled) continue;
         Body &A = w.bodies[j.a], &B = w.bodies[j.b];
         if (A.activeIndex == INACTIVE && B.activeIndex == INACTIVE) continue;
         if (A.activeIndex != INACTIVE && B.activeIndex != INACTIVE) link_bodies(A.activeIndex, B.activeIndex);
-        jointLinks[ji] = std::min(A.activeIndex, B.activeIndex);
+        jointLinks[k] = std::min(A.activeIndex, B.activeIndex);
     }
     // finalize islands.ts:240-389
     int ni = 0;
@@ -1068,10 +1095,10 @@ static void build_islands(World &w) {
         if (ab >= INACTIVE) continue;
         isl[bodyIslands[ab]].contactIndices.push_back((int)ci);
     }
-    for (size_t ji = 0; ji < jointLinks.size(); ji++) {
-        int64_t ab = jointLinks[ji];
+    for (size_t k = 0; k < jointLinks.size(); k++) {
+        int64_t ab = jointLinks[k];
         if (ab >= INACTIVE) continue;
-        isl[bodyIslands[ab]].jointIndices.push_back((int)ji);
+        isl[bodyIslands[ab]].jointIndices.push_back(jointIds[k]);
     }
     std::stable_sort(isl.begin(), isl.end(), [](const Island &a, const Island &b) {
         return a.contactIndices.size() + a.jointIndices.size() > b.contactIndices.size() + b.jointIndices.size();
@@ -1179,7 +1206,8 @@ static void step(World &w, double dt) {
     }
     if (dt > 0) {
         // wakeBodiesInUserConstraints update.ts:863-888
-        for (HingeJoint &j : w.joints) {
+        for (int id : joint_ids(w)) {
+            JointInfo j = joint_info(w, id);
             if (!j.enabled) continue;
             Body &A = w.bodies[j.a], &B = w.bodies[j.b];
             bool act = !A.sleeping || !B.sleeping, dyn = A.motion == DYNAMIC || B.motion == DYNAMIC;
@@ -1190,23 +1218,41 @@ static void step(World &w, double dt) {
         }
         build_islands(w);
         // updateSleeping + setupVelocityConstraints constraints.ts:264-287
-        auto joint_active = [&](const HingeJoint &j) {
+        auto joint_active = [&](int id) {
+            JointInfo j = joint_info(w, id);
             return j.enabled && !(w.bodies[j.a].sleeping && w.bodies[j.b].sleeping);
         };
-        for (HingeJoint &j : w.joints)
-            if (joint_active(j)) hinge_setup(j, w.bodies[j.a], w.bodies[j.b], dt);
+        for (int id : joint_ids(w)) {
+            if (!joint_active(id)) continue;
+            if (id >= JOINT_SWING) {
+                SwingTwistJoint &j = w.swings[id - JOINT_SWING];
+                swing_setup(j, w.bodies[j.a], w.bodies[j.b], dt);
+            } else {
+                HingeJoint &j = w.joints[id];
+                hinge_setup(j, w.bodies[j.a], w.bodies[j.b], dt);
+            }
+        }
         if (w.s.warmStarting) {
             double ratio = (w.s.warmStarting && w.prevDt > 0) ? dt / w.prevDt : 0.0;
             warm_start_all(w, ratio);
-            for (HingeJoint &j : w.joints)
-                if (joint_active(j)) hinge_warm(j, w.bodies[j.a], w.bodies[j.b], ratio);
+            for (int id : joint_ids(w)) {
+                if (!joint_active(id)) continue;
+                if (id >= JOINT_SWING) {
+                    SwingTwistJoint &j = w.swings[id - JOINT_SWING];
+                    swing_warm(j, w.bodies[j.a], w.bodies[j.b], ratio);
+                } else {
+                    HingeJoint &j = w.joints[id];
+                    hinge_warm(j, w.bodies[j.a], w.bodies[j.b], ratio);
+                }
+            }
         }
         w.prevDt = dt;
         for (Island &is : w.islands) {
             if (is.contactIndices.empty() && is.jointIndices.empty()) continue;
-            // sortConstraintIds constraints.ts:248-261 (priority, then index)
+            // sortConstraintIds constraints.ts:248-261: (priority, then the per-type index); the
+            // stable sort keeps the type order of the island's list for equal keys
             std::stable_sort(is.jointIndices.begin(), is.jointIndices.end(), [&](int a, int b) {
-                const HingeJoint &ja = w.joints[a], &jb = w.joints[b];
+                JointInfo ja = joint_info(w, a), jb = joint_info(w, b);
                 if (ja.priority != jb.priority) return ja.priority < jb.priority;
                 return ja.index < jb.index;
             });
@@ -1253,8 +1299,13 @@ static void step(World &w, double dt) {
             for (int i = 0; i < is.velSteps; i++) {
                 if (!is.contactIndices.empty()) solve_velocity(w, is.contactIndices);
                 for (int ji : is.jointIndices) {
-                    HingeJoint &j = w.joints[ji];
-                    hinge_solve_velocity(j, w.bodies[j.a], w.bodies[j.b], dt);
+                    if (ji >= JOINT_SWING) {
+                        SwingTwistJoint &j = w.swings[ji - JOINT_SWING];
+                        swing_solve_velocity(j, w.bodies[j.a], w.bodies[j.b], dt);
+                    } else {
+                        HingeJoint &j = w.joints[ji];
+                        hinge_solve_velocity(j, w.bodies[j.a], w.bodies[j.b], dt);
+                    }
                 }
             }
         }
@@ -1296,8 +1347,14 @@ static void step(World &w, double dt) {
                 bool applied = false;
                 if (!is.contactIndices.empty()) applied = solve_position(w, is.contactIndices);
                 for (int ji : is.jointIndices) {
-                    HingeJoint &j = w.joints[ji];
-                    applied = hinge_solve_position(j, w.bodies[j.a], w.bodies[j.b], dt, w.s.baumgarteFactor) || applied;
+                    if (ji >= JOINT_SWING) {
+                        SwingTwistJoint &j = w.swings[ji - JOINT_SWING];
+                        applied = swing_solve_position(j, w.bodies[j.a], w.bodies[j.b], w.s.baumgarteFactor) || applied;
+                    } else {
+                        HingeJoint &j = w.joints[ji];
+                        applied =
+                            hinge_solve_position(j, w.bodies[j.a], w.bodies[j.b], dt, w.s.baumgarteFactor) || applied;
+                    }
                 }
                 if (!applied) break;
             }
@@ -1512,6 +1569,75 @@ int orc_add_hinge(void *wp, const double *d) {
     return j.index;
 }
 void orc_set_skip_joint_pairs(void *wp, int on) { ((World *)wp)->skipJointPairs = on != 0; }
+
+// Swing-twist joint (swing-twist-constraint.ts create :180-296), 47 doubles:
+//  0 bodyA, 1 bodyB, 2-4 position1, 5-7 position2, 8-10 twistAxis1, 11-13 planeAxis1,
+//  14-16 twistAxis2, 17-19 planeAxis2, 20 space (0 world, 1 local), 21 swingType (0 cone, 1 pyramid),
+//  22 normalHalfConeAngle, 23 planeHalfConeAngle, 24 twistMinAngle, 25 twistMaxAngle,
+//  26 maxFrictionTorque, 27 swing motor state, 28 twist motor state, 29-31 target angular velocity,
+//  32-35 target orientation (x y z w, constraint space), 36-38 swing motor spring (mode, f, d),
+//  39-41 twist motor spring, 42-43 swing motor torque limits (min, max), 44-45 twist motor torque
+//  limits, 46 priority.  Returns the joint index or -1.
+int orc_add_swing_twist(void *wp, const double *d) {
+    World &w = *(World *)wp;
+    int a = (int)d[0], b = (int)d[1];
+    if (a < 0 || b < 0 || a >= (int)w.bodies.size() || b >= (int)w.bodies.size()) return -1;
+    const Body &A = w.bodies[a], &B = w.bodies[b];
+    SwingTwistJoint j;
+    j.a = a;
+    j.b = b;
+    j.index = (int)w.swings.size();
+    j.priority = (int)d[46];
+    V3 t1 = normalize(V3{d[8], d[9], d[10]}), p1 = normalize(V3{d[11], d[12], d[13]});
+    V3 t2 = normalize(V3{d[14], d[15], d[16]}), p2 = normalize(V3{d[17], d[18], d[19]});
+    V3 n1 = cross(p1, t1), n2 = cross(p2, t2);
+    // constraint space X = twist, Y = normal, Z = plane (columns of the rotation)
+    M3 m1, m2;
+    V3 c1[3] = {t1, n1, p1}, c2[3] = {t2, n2, p2};
+    for (int c = 0; c < 3; c++) {
+        m1.m[c][0] = c1[c].x;
+        m1.m[c][1] = c1[c].y;
+        m1.m[c][2] = c1[c].z;
+        m2.m[c][0] = c2[c].x;
+        m2.m[c][1] = c2[c].y;
+        m2.m[c][2] = c2[c].z;
+    }
+    j.c2b1 = quat_from_m3(m1);
+    j.c2b2 = quat_from_m3(m2);
+    V3 pos1{d[2], d[3], d[4]}, pos2{d[5], d[6], d[7]};
+    if ((int)d[20] == 0) {
+        Q4 iqA = qconj(A.quat), iqB = qconj(B.quat);
+        j.lp1 = rotate(iqA, sub(pos1, A.com));
+        j.lp2 = rotate(iqB, sub(pos2, B.com));
+        j.c2b1 = qmul(iqA, j.c2b1);
+        j.c2b2 = qmul(iqB, j.c2b2);
+    } else {
+        j.lp1 = pos1;
+        j.lp2 = pos2;
+    }
+    j.normalHalfCone = d[22];
+    j.planeHalfCone = d[23];
+    j.twistMin = d[24];
+    j.twistMax = d[25];
+    j.st.swingType = (int)d[21];
+    swing_update_limits(j);
+    j.maxFrictionTorque = d[26];
+    j.swingMotorState = (int)d[27];
+    j.twistMotorState = (int)d[28];
+    j.targetAngularVelocity = {d[29], d[30], d[31]};
+    // setTargetOrientationCS :405-416: clamped into the limits
+    Q4 to{d[32], d[33], d[34], d[35]}, sw, tw;
+    get_swing_twist(to, sw, tw);
+    j.targetOrientation = clamp_swing_twist(j.st, sw, tw) != 0 ? qmul(sw, tw) : to;
+    j.swingMotorSpring = {(int)d[36], d[37], d[38]};
+    j.twistMotorSpring = {(int)d[39], d[40], d[41]};
+    j.swingMinTorque = d[42];
+    j.swingMaxTorque = d[43];
+    j.twistMinTorque = d[44];
+    j.twistMaxTorque = d[45];
+    w.swings.push_back(j);
+    return j.index;
+}
 // Contact events of the last step, 3 int64 per event (type, body index A, body index B); returns the count.
 int orc_get_events(void *wp, int64_t *out, int cap) {
     const World &w = *(World *)wp;

@@ -63,3 +63,47 @@ struct HingeJoint {
     HingeRotPart rot;
     AnglePart limit, motor;
 };
+
+// SwingTwistConstraintPart swing-twist-constraint-part.ts:47-84 (limits as sines and cosines of
+// half angles; rotation flags :26-35)
+enum SwingType { SWING_CONE = 0, SWING_PYRAMID = 1 };
+enum RotationFlags {
+    TWIST_X_LOCKED = 1,
+    SWING_Y_LOCKED = 2,
+    SWING_Z_LOCKED = 4,
+    TWIST_X_FREE = 8,
+    SWING_Y_FREE = 16,
+    SWING_Z_FREE = 32,
+    SWING_YZ_FREE = 48
+};
+enum ClampedAxis { TWIST_MIN = 1, TWIST_MAX = 2, SWING_Y_MIN = 4, SWING_Y_MAX = 8, SWING_Z_MIN = 16, SWING_Z_MAX = 32 };
+struct SwingTwistPart {
+    int swingType = SWING_CONE, rotationFlags = 0;
+    double sinTwistHalfMin = 0, sinTwistHalfMax = 0, cosTwistHalfMin = 1, cosTwistHalfMax = 1;
+    double swingYHalfMin = 0, swingYHalfMax = 0, sinSwingYHalfMin = 0, sinSwingYHalfMax = 0, cosSwingYHalfMin = 1,
+           cosSwingYHalfMax = 1;
+    double swingZHalfMin = 0, swingZHalfMax = 0, sinSwingZHalfMin = 0, sinSwingZHalfMax = 0, cosSwingZHalfMin = 1,
+           cosSwingZHalfMax = 1;
+    V3 wsSwingY{0, 0, 0}, wsSwingZ{0, 0, 0}, wsTwist{0, 0, 0};
+    AnglePart swingY, swingZ, twist;
+};
+
+// SwingTwistConstraint swing-twist-constraint.ts:35-85
+struct SwingTwistJoint {
+    int a = 0, b = 0;
+    int priority = 0, index = 0;
+    bool enabled = true;
+    V3 lp1, lp2;
+    Q4 c2b1{0, 0, 0, 1}, c2b2{0, 0, 0, 1};  // constraint space to body space
+    double normalHalfCone = 0, planeHalfCone = 0, twistMin = 0, twistMax = 0, maxFrictionTorque = 0;
+    int swingMotorState = MOTOR_OFF, twistMotorState = MOTOR_OFF;
+    V3 targetAngularVelocity{0, 0, 0};
+    Q4 targetOrientation{0, 0, 0, 1};
+    SpringSettings swingMotorSpring{FREQUENCY_AND_DAMPING, 2.0, 1.0}, twistMotorSpring{FREQUENCY_AND_DAMPING, 2.0, 1.0};
+    double swingMinTorque = -1.0 / 0.0, swingMaxTorque = 1.0 / 0.0, twistMinTorque = -1.0 / 0.0,
+           twistMaxTorque = 1.0 / 0.0;
+    V3 wsMotorAxis[3];
+    PointPart point;
+    SwingTwistPart st;
+    AnglePart motor[3];  // twist, swing Y, swing Z
+};

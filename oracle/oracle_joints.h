@@ -493,3 +493,390 @@ inline Q4 inv_initial_orientation_xz(V3 n1, V3 h1, V3 n2, V3 h2) {
     Q4 q1 = quat_from_m3(m1), q2 = quat_from_m3(m2);
     return qmul(q2, qconj(q1));
 }
+
+// ---- SwingTwistConstraintPart (swing-twist-constraint-part.ts) ----------------------
+// setLimits :140-236
+inline void st_set_limits(SwingTwistPart &p, double twistMin, double twistMax, double swingYMin, double swingYMax,
+                          double swingZMin, double swingZMax) {
+    const double locked = 0.5 * M_PI / 180.0, freeA = 179.5 * M_PI / 180.0;
+    p.swingYHalfMin = 0.5 * swingYMin;
+    p.swingYHalfMax = 0.5 * swingYMax;
+    p.swingZHalfMin = 0.5 * swingZMin;
+    p.swingZHalfMax = 0.5 * swingZMax;
+    p.rotationFlags = 0;
+    auto axis = [&](double mn, double mx, int lockedFlag, int freeFlag, double &sMin, double &sMax, double &cMin,
+                    double &cMax) {
+        if (mn > -locked && mx < locked) {
+            p.rotationFlags |= lockedFlag;
+            sMin = sMax = 0;
+            cMin = cMax = 1;
+        } else if (mn < -freeA && mx > freeA) {
+            p.rotationFlags |= freeFlag;
+            sMin = -1;
+            sMax = 1;
+            cMin = cMax = 0;
+        } else {
+            sMin = std::sin(0.5 * mn);
+            sMax = std::sin(0.5 * mx);
+            cMin = std::cos(0.5 * mn);
+            cMax = std::cos(0.5 * mx);
+        }
+    };
+    axis(twistMin, twistMax, TWIST_X_LOCKED, TWIST_X_FREE, p.sinTwistHalfMin, p.sinTwistHalfMax, p.cosTwistHalfMin,
+         p.cosTwistHalfMax);
+    axis(swingYMin, swingYMax, SWING_Y_LOCKED, SWING_Y_FREE, p.sinSwingYHalfMin, p.sinSwingYHalfMax, p.cosSwingYHalfMin,
+         p.cosSwingYHalfMax);
+    axis(swingZMin, swingZMax, SWING_Z_LOCKED, SWING_Z_FREE, p.sinSwingZHalfMin, p.sinSwingZHalfMax, p.cosSwingZHalfMin,
+         p.cosSwingZHalfMax);
+}
+// distanceToMinShorter :239-246
+inline bool distance_to_min_shorter(double dMin, double dMax) {
+    double a = std::fabs(dMin);
+    if (a > 1) a = 2 - a;
+    double b = std::fabs(dMax);
+    if (b > 1) b = 2 - b;
+    return a < b;
+}
+// getSwingTwist :252-269: q = swing * twist, swing.x = 0, twist.y = twist.z = 0
+inline void get_swing_twist(Q4 q, Q4 &swing, Q4 &twist) {
+    double s = std::sqrt(q.w * q.w + q.x * q.x);
+    if (s != 0) {
+        twist = {q.x / s, 0, 0, q.w / s};
+        swing = {0, (q.w * q.y - q.x * q.z) / s, (q.w * q.z + q.x * q.y) / s, s};
+    } else {
+        twist = {0, 0, 0, 1};
+        swing = q;
+    }
+}
+inline Q4 qscale(Q4 q, double s) { return {q.x * s, q.y * s, q.z * s, q.w * s}; }
+// getClosestPointOnEllipse :412-462 (Newton iteration on the Lagrange multiplier)
+inline void closest_point_on_ellipse(double px, double py, double a, double b, double &ox, double &oy) {
+    if (a <= 0) {
+        ox = 0;
+        oy = py >= 0 ? b : -b;
+        return;
+    }
+    if (b <= 0) {
+        ox = px >= 0 ? a : -a;
+        oy = 0;
+        return;
+    }
+    double aSq = a * a, bSq = b * b, t = 0;
+    for (int i = 0; i < 100; i++) {
+        double ta = t + aSq, tb = t + bSq;
+        double ga = a * px / ta, gb = b * py / tb;
+        double gt = ga * ga + gb * gb - 1;
+        if (std::fabs(gt) < 1e-6) {
+            ox = aSq * px / ta;
+            oy = bSq * py / tb;
+            return;
+        }
+        double d = -2 * (aSq * px * px / (ta * ta * ta) + bSq * py * py / (tb * tb * tb));
+        t = t - gt / d;
+    }
+    ox = aSq * px / (t + aSq);
+    oy = bSq * py / (t + bSq);
+}
+// clampSwingTwist :278-402
+inline int clamp_swing_twist(const SwingTwistPart &p, Q4 &swing, Q4 &twist) {
+    int clamped = 0;
+    bool negSwing = swing.w < 0, negTwist = twist.w < 0;
+    if (negSwing) swing = qscale(swing, -1);
+    if (negTwist) twist = qscale(twist, -1);
+    if (p.rotationFlags & TWIST_X_LOCKED) {
+        if (twist.x != 0) clamped |= TWIST_MIN | TWIST_MAX;
+        twist = {0, 0, 0, 1};
+    } else if (!(p.rotationFlags & TWIST_X_FREE)) {
+        double dMin = p.sinTwistHalfMin - twist.x, dMax = twist.x - p.sinTwistHalfMax;
+        if (dMin > 0 || dMax > 0) {
+            if (distance_to_min_shorter(dMin, dMax)) {
+                twist = {p.sinTwistHalfMin, 0, 0, p.cosTwistHalfMin};
+                clamped |= TWIST_MIN;
+            } else {
+                twist = {p.sinTwistHalfMax, 0, 0, p.cosTwistHalfMax};
+                clamped |= TWIST_MAX;
+            }
+        }
+    }
+    if (p.rotationFlags & SWING_Y_LOCKED) {
+        if (p.rotationFlags & SWING_Z_LOCKED) {
+            if (swing.y != 0) clamped |= SWING_Y_MIN | SWING_Y_MAX;
+            if (swing.z != 0) clamped |= SWING_Z_MIN | SWING_Z_MAX;
+            swing = {0, 0, 0, 1};
+        } else {
+            if (swing.y != 0) clamped |= SWING_Y_MIN | SWING_Y_MAX;
+            double dMin = p.sinSwingZHalfMin - swing.z, dMax = swing.z - p.sinSwingZHalfMax;
+            if (dMin > 0 || dMax > 0) {
+                if (distance_to_min_shorter(dMin, dMax)) {
+                    swing = {0, 0, p.sinSwingZHalfMin, p.cosSwingZHalfMin};
+                    clamped |= SWING_Z_MIN;
+                } else {
+                    swing = {0, 0, p.sinSwingZHalfMax, p.cosSwingZHalfMax};
+                    clamped |= SWING_Z_MAX;
+                }
+            } else if (clamped & SWING_Y_MIN) {
+                double z = swing.z;
+                swing = {0, 0, z, std::sqrt(1 - z * z)};
+            }
+        }
+    } else if (p.rotationFlags & SWING_Z_LOCKED) {
+        if (swing.z != 0) clamped |= SWING_Z_MIN | SWING_Z_MAX;
+        double dMin = p.sinSwingYHalfMin - swing.y, dMax = swing.y - p.sinSwingYHalfMax;
+        if (dMin > 0 || dMax > 0) {
+            if (distance_to_min_shorter(dMin, dMax)) {
+                swing = {0, p.sinSwingYHalfMin, 0, p.cosSwingYHalfMin};
+                clamped |= SWING_Y_MIN;
+            } else {
+                swing = {0, p.sinSwingYHalfMax, 0, p.cosSwingYHalfMax};
+                clamped |= SWING_Y_MAX;
+            }
+        } else if (clamped & SWING_Z_MIN) {
+            double y = swing.y;
+            swing = {0, y, 0, std::sqrt(1 - y * y)};
+        }
+    } else if (p.swingType == SWING_CONE) {
+        double y = swing.y, z = swing.z, a = p.sinSwingYHalfMax, b = p.sinSwingZHalfMax;
+        if (a > 0 && b > 0) {
+            double e = y * y / (a * a) + z * z / (b * b);
+            if (e > 1) {
+                double cy, cz;
+                closest_point_on_ellipse(y, z, a, b, cy, cz);
+                double nw = std::sqrt(std::max(0.0, 1 - cy * cy - cz * cz));
+                swing = {0, cy, cz, nw};
+                clamped |= SWING_Y_MIN | SWING_Y_MAX | SWING_Z_MIN | SWING_Z_MAX;
+            }
+        }
+    } else {
+        double hy = std::atan2(swing.y, swing.w), hz = std::atan2(swing.z, swing.w);
+        double cy = std::max(p.swingYHalfMin, std::min(p.swingYHalfMax, hy));
+        double cz = std::max(p.swingZHalfMin, std::min(p.swingZHalfMax, hz));
+        if (hy != cy || hz != cz) {
+            double sy = std::sin(cy), coy = std::cos(cy), sz = std::sin(cz), coz = std::cos(cz);
+            double ny = sy * coz, nz = coy * sz, nw = coy * coz;
+            double l = std::sqrt(ny * ny + nz * nz + nw * nw);
+            swing = {0, ny / l, nz / l, nw / l};
+            clamped |= SWING_Y_MIN | SWING_Y_MAX | SWING_Z_MIN | SWING_Z_MAX;
+        }
+    }
+    if (negSwing) swing = qscale(swing, -1);
+    if (negTwist) twist = qscale(twist, -1);
+    return clamped;
+}
+// calculateConstraintProperties :481-652
+inline void st_calc(SwingTwistPart &p, const Body &A, const Body &B, Q4 q, Q4 c2w) {
+    Q4 sw, tw;
+    get_swing_twist(q, sw, tw);
+    Q4 csw = sw, ctw = tw;
+    int clamped = clamp_swing_twist(p, csw, ctw);
+    const V3 X{1, 0, 0}, Y{0, 1, 0}, Z{0, 0, 1};
+    if (p.rotationFlags & SWING_Y_LOCKED) {
+        Q4 t2w = qmul(c2w, sw);
+        p.wsSwingY = rotate(t2w, Y);
+        p.wsSwingZ = rotate(t2w, Z);
+        if (p.rotationFlags & SWING_Z_LOCKED) {
+            angle_calc(p.swingY, A, B, p.wsSwingY, 0);
+            angle_calc(p.swingZ, A, B, p.wsSwingZ, 0);
+        } else {
+            angle_calc(p.swingY, A, B, p.wsSwingY, 0);
+            if (clamped & (SWING_Z_MIN | SWING_Z_MAX)) {
+                if (clamped & SWING_Z_MIN) p.wsSwingZ = neg(p.wsSwingZ);
+                angle_calc(p.swingZ, A, B, p.wsSwingZ, 0);
+            } else {
+                angle_deactivate(p.swingZ);
+            }
+        }
+    } else if (p.rotationFlags & SWING_Z_LOCKED) {
+        Q4 t2w = qmul(c2w, sw);
+        p.wsSwingY = rotate(t2w, Y);
+        p.wsSwingZ = rotate(t2w, Z);
+        if (clamped & (SWING_Y_MIN | SWING_Y_MAX)) {
+            if (clamped & SWING_Y_MIN) p.wsSwingY = neg(p.wsSwingY);
+            angle_calc(p.swingY, A, B, p.wsSwingY, 0);
+        } else {
+            angle_deactivate(p.swingY);
+        }
+        angle_calc(p.swingZ, A, B, p.wsSwingZ, 0);
+    } else if ((p.rotationFlags & SWING_YZ_FREE) != SWING_YZ_FREE) {
+        if (clamped & (SWING_Y_MIN | SWING_Y_MAX | SWING_Z_MIN | SWING_Z_MAX)) {
+            V3 current = rotate(qmul(c2w, sw), X), desired = rotate(qmul(c2w, csw), X);
+            V3 c = cross(desired, current);
+            double l = len(c);
+            if (l > 1e-6) {
+                p.wsSwingY = scale(c, 1 / l);
+                angle_calc(p.swingY, A, B, p.wsSwingY, 0);
+            } else {
+                angle_deactivate(p.swingY);
+            }
+        } else {
+            angle_deactivate(p.swingY);
+        }
+        angle_deactivate(p.swingZ);
+    } else {
+        angle_deactivate(p.swingY);
+        angle_deactivate(p.swingZ);
+    }
+    if (p.rotationFlags & TWIST_X_LOCKED) {
+        p.wsTwist = rotate(qmul(c2w, sw), X);
+        angle_calc(p.twist, A, B, p.wsTwist, 0);
+    } else if (!(p.rotationFlags & TWIST_X_FREE)) {
+        if (clamped & (TWIST_MIN | TWIST_MAX)) {
+            p.wsTwist = rotate(qmul(c2w, sw), X);
+            if (clamped & TWIST_MIN) p.wsTwist = neg(p.wsTwist);
+            angle_calc(p.twist, A, B, p.wsTwist, 0);
+        } else {
+            angle_deactivate(p.twist);
+        }
+    } else {
+        angle_deactivate(p.twist);
+    }
+}
+inline void st_warm(SwingTwistPart &p, Body &A, Body &B, double ratio) {
+    angle_warm(p.swingY, A, B, ratio);
+    angle_warm(p.swingZ, A, B, ratio);
+    angle_warm(p.twist, A, B, ratio);
+}
+// solveVelocityConstraint :670-722
+inline bool st_solve_velocity(SwingTwistPart &p, Body &A, Body &B) {
+    const double INF = 1.0 / 0.0;
+    bool imp = false;
+    if (angle_active(p.swingY)) {
+        double mx = p.sinSwingYHalfMin == p.sinSwingYHalfMax ? INF : 0;
+        imp = angle_solve_velocity(p.swingY, A, B, p.wsSwingY, -INF, mx) || imp;
+    }
+    if (angle_active(p.swingZ)) {
+        double mx = p.sinSwingZHalfMin == p.sinSwingZHalfMax ? INF : 0;
+        imp = angle_solve_velocity(p.swingZ, A, B, p.wsSwingZ, -INF, mx) || imp;
+    }
+    if (angle_active(p.twist)) {
+        double mx = p.sinTwistHalfMin == p.sinTwistHalfMax ? INF : 0;
+        imp = angle_solve_velocity(p.twist, A, B, p.wsTwist, -INF, mx) || imp;
+    }
+    return imp;
+}
+// solvePositionConstraint :743-776 with RotationEulerConstraintPart
+// (rotation-euler-constraint-part.ts calculateConstraintProperties, solvePositionConstraint)
+inline bool st_solve_position(SwingTwistPart &p, Body &A, Body &B, Q4 q, Q4 c2b1, Q4 c2b2, double baumgarte) {
+    Q4 sw, tw;
+    get_swing_twist(q, sw, tw);
+    int clamped = clamp_swing_twist(p, sw, tw);
+    if (clamped == 0) return false;
+    Q4 invInitial = qmul(c2b2, qconj(qmul(qmul(c2b1, sw), tw)));
+    M3 I1 = world_inv_inertia(A), I2 = world_inv_inertia(B), eff;
+    if (!m3_invert(eff, m3_add(I1, I2))) eff = m3_zero();
+    Q4 diff = qmul(qmul(B.quat, invInitial), qconj(A.quat));
+    if (diff.w < 0) diff = qscale(diff, -1);
+    V3 err{2 * diff.x, 2 * diff.y, 2 * diff.z};
+    if (lensq(err) < 1e-12) return false;
+    V3 l = scale(m3_mul(eff, err), -baumgarte);
+    if (A.motion == DYNAMIC) sub_rotation_step(A, m3_mul(I1, l));
+    if (B.motion == DYNAMIC) add_rotation_step(B, m3_mul(I2, l));
+    return true;
+}
+
+// ---- SwingTwistConstraint (swing-twist-constraint.ts) --------------------------------
+inline void swing_update_limits(SwingTwistJoint &j) {  // updateLimits :300-310
+    st_set_limits(j.st, j.twistMin, j.twistMax, -j.planeHalfCone, j.planeHalfCone, -j.normalHalfCone, j.normalHalfCone);
+}
+// setupVelocity :484-666
+inline void swing_setup(SwingTwistJoint &j, const Body &A, const Body &B, double dt) {
+    point_calc(j.point, A, j.lp1, B, j.lp2);
+    Q4 c1w = qmul(A.quat, j.c2b1), c2w = qmul(B.quat, j.c2b2);
+    Q4 q = qmul(qconj(c1w), c2w);
+    st_calc(j.st, A, B, q, c1w);
+    if (j.swingMotorState != MOTOR_OFF || j.twistMotorState != MOTOR_OFF || j.maxFrictionTorque > 0) {
+        const V3 E[3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+        for (int i = 0; i < 3; i++) j.wsMotorAxis[i] = rotate(c2w, E[i]);
+        V3 err{0, 0, 0};
+        if (j.swingMotorState == MOTOR_POSITION || j.twistMotorState == MOTOR_POSITION) {
+            Q4 t = j.targetOrientation;
+            if (q.x * t.x + q.y * t.y + q.z * t.z + q.w * t.w < 0) t = qscale(t, -1);
+            Q4 d = qmul(qconj(q), t);
+            err = {-2 * d.x, -2 * d.y, -2 * d.z};
+        }
+        double e[3] = {err.x, err.y, err.z};
+        double tav[3] = {j.targetAngularVelocity.x, j.targetAngularVelocity.y, j.targetAngularVelocity.z};
+        switch (j.swingMotorState) {
+            case MOTOR_OFF:
+                if (j.maxFrictionTorque > 0) {
+                    for (int i = 1; i < 3; i++) angle_calc(j.motor[i], A, B, j.wsMotorAxis[i], 0);
+                } else {
+                    for (int i = 0; i < 3; i++) angle_deactivate(j.motor[i]);
+                }
+                break;
+            case MOTOR_VELOCITY:
+                for (int i = 1; i < 3; i++) angle_calc(j.motor[i], A, B, j.wsMotorAxis[i], -tav[i]);
+                break;
+            case MOTOR_POSITION:
+                if (j.swingMotorSpring.frequencyOrStiffness > 0) {
+                    for (int i = 1; i < 3; i++)
+                        angle_calc_settings(j.motor[i], dt, A, B, j.wsMotorAxis[i], 0, e[i], j.swingMotorSpring);
+                } else {
+                    for (int i = 1; i < 3; i++) angle_deactivate(j.motor[i]);
+                }
+                break;
+        }
+        switch (j.twistMotorState) {
+            case MOTOR_OFF:
+                if (j.maxFrictionTorque > 0)
+                    angle_calc(j.motor[0], A, B, j.wsMotorAxis[0], 0);
+                else
+                    angle_deactivate(j.motor[0]);
+                break;
+            case MOTOR_VELOCITY:
+                angle_calc(j.motor[0], A, B, j.wsMotorAxis[0], -tav[0]);
+                break;
+            case MOTOR_POSITION:
+                if (j.twistMotorSpring.frequencyOrStiffness > 0)
+                    angle_calc_settings(j.motor[0], dt, A, B, j.wsMotorAxis[0], 0, e[0], j.twistMotorSpring);
+                else
+                    angle_deactivate(j.motor[0]);
+                break;
+        }
+    } else {
+        for (int i = 0; i < 3; i++) angle_deactivate(j.motor[i]);
+    }
+}
+// warmStartVelocity :668-680: motors, limits, point
+inline void swing_warm(SwingTwistJoint &j, Body &A, Body &B, double ratio) {
+    for (int i = 0; i < 3; i++) angle_warm(j.motor[i], A, B, ratio);
+    st_warm(j.st, A, B, ratio);
+    point_warm(j.point, A, B, ratio);
+}
+// solveVelocity :682-748
+inline bool swing_solve_velocity(SwingTwistJoint &j, Body &A, Body &B, double dt) {
+    bool imp = false;
+    if (angle_active(j.motor[0])) {
+        double mn, mx;
+        if (j.twistMotorState == MOTOR_OFF) {
+            mx = dt * j.maxFrictionTorque;
+            mn = -mx;
+        } else {
+            mn = dt * j.twistMinTorque;
+            mx = dt * j.twistMaxTorque;
+        }
+        imp = angle_solve_velocity(j.motor[0], A, B, j.wsMotorAxis[0], mn, mx) || imp;
+    }
+    if (angle_active(j.motor[1])) {
+        double mn, mx;
+        if (j.swingMotorState == MOTOR_OFF) {
+            mx = dt * j.maxFrictionTorque;
+            mn = -mx;
+        } else {
+            mn = dt * j.swingMinTorque;
+            mx = dt * j.swingMaxTorque;
+        }
+        for (int i = 1; i < 3; i++) imp = angle_solve_velocity(j.motor[i], A, B, j.wsMotorAxis[i], mn, mx) || imp;
+    }
+    imp = st_solve_velocity(j.st, A, B) || imp;
+    imp = point_solve_velocity(j.point, A, B) || imp;
+    return imp;
+}
+// solvePosition :757-800: rotation limits, then the point from the corrected poses
+inline bool swing_solve_position(SwingTwistJoint &j, Body &A, Body &B, double baumgarte) {
+    Q4 c1w = qmul(A.quat, j.c2b1), c2w = qmul(B.quat, j.c2b2);
+    Q4 q = qmul(qconj(c1w), c2w);
+    bool imp = st_solve_position(j.st, A, B, q, j.c2b1, j.c2b2, baumgarte);
+    point_calc(j.point, A, j.lp1, B, j.lp2);
+    imp = point_solve_position(j.point, A, B, baumgarte) || imp;
+    return imp;
+}

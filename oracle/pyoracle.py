@@ -57,6 +57,7 @@ def load():
         "orc_get_events": ([vp, C.c_void_p, i32], i32),
         "orc_add_hinge": ([vp, dp], i32),
         "orc_set_skip_joint_pairs": ([vp, i32], None),
+        "orc_add_swing_twist": ([vp, dp], i32),
     }
     for k, (a, r) in sig.items():
         f = getattr(lib, k)
@@ -210,6 +211,28 @@ class OracleWorld:
                     h["motor_spring"]["damping"])
         d[33], d[34], d[35] = h["min_torque_limit"], h["max_torque_limit"], h["priority"]
         return self.add_hinge(d)
+
+    def add_swing_twist_record(self, h) -> int:
+        """Swing-twist joint from a cc_swing_twist_desc record (fields by name)."""
+        d = np.zeros(47, dtype=np.float64)
+        d[0], d[1] = h["body_a"], h["body_b"]
+        for k, f in enumerate(("position_a", "position_b", "twist_axis_a", "plane_axis_a", "twist_axis_b",
+                               "plane_axis_b")):
+            d[2 + 3 * k: 5 + 3 * k] = h[f]
+        d[20], d[21] = h["space"], h["swing_type"]
+        d[22], d[23] = h["normal_half_cone_angle"], h["plane_half_cone_angle"]
+        d[24], d[25], d[26] = h["twist_min_angle"], h["twist_max_angle"], h["max_friction_torque"]
+        d[27], d[28] = h["swing_motor_state"], h["twist_motor_state"]
+        d[29:32] = h["target_angular_velocity"]
+        d[32:36] = h["target_orientation"]
+        for k, f in enumerate(("swing_motor_spring", "twist_motor_spring")):
+            d[36 + 3 * k: 39 + 3 * k] = (h[f]["mode"], h[f]["frequency_or_stiffness"], h[f]["damping"])
+        d[42], d[43] = h["swing_min_torque_limit"], h["swing_max_torque_limit"]
+        d[44], d[45] = h["twist_min_torque_limit"], h["twist_max_torque_limit"]
+        d[46] = h["priority"]
+        k = self.lib.orc_add_swing_twist(self.h, dptr(d))
+        assert k >= 0
+        return k
 
     def set_skip_joint_pairs(self, on: bool) -> None:
         self.lib.orc_set_skip_joint_pairs(self.h, 1 if on else 0)
