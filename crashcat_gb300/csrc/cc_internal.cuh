@@ -37,7 +37,8 @@ constexpr int STATIC = 0, KINEMATIC = 1, DYNAMIC = 2;
 constexpr int SHAPE_SPHERE = 0, SHAPE_BOX = 1, SHAPE_CAPSULE = 2;
 
 // Per-step overflow flags (status bits in DevCounters::overflow)
-enum : int { OVF_PAIRS = 1, OVF_MANIFOLDS = 2, OVF_EPA = 4, OVF_ISLAND = 8, OVF_CACHE = 16, OVF_SLOTS = 32 };
+enum : int { OVF_PAIRS = 1, OVF_MANIFOLDS = 2, OVF_EPA = 4, OVF_ISLAND = 8, OVF_CACHE = 16, OVF_SLOTS = 32,
+             OVF_TIMEOUT = 64 };
 
 // Device-resident counters of one step (one 128-byte line).
 struct DevCounters {
@@ -58,7 +59,11 @@ struct DevCounters {
     int epa_cursor;
     int epa_fallback;  // EPA items handed to the pass with the reference's polytope limits
     int num_removed;   // contact pairs of the previous step not found in this step
-    int pad[15];
+    int num_giant_islands;              // islands solved by the whole grid (cooperative launch)
+    unsigned int bar_count, bar_gen;    // grid barrier of the giant-island solve
+    int bar_error;                      // a bounded grid-barrier wait gave up
+    int giant_left[2], giant_any[2], giant_sleep;
+    int pad[6];
 };
 
 // Settings copied into constant memory once per world.
@@ -83,6 +88,7 @@ struct DevSettings {
     float sleep_threshold;
     uint32_t allowed_pairs[CC_MAX_LAYERS];  // combined layer predicate, bit j of [i]
     int small_island_max_cons;  // islands up to this many contacts run on one thread
+    int small_island_max_joints;  // islands with joints: up to this many joints run on one thread
 };
 
 // Manifold produced by the narrowphase for one body pair (<= 4 points),
@@ -328,10 +334,18 @@ struct DevWorld {
     int skip_joint_pairs;              // broadphase skips body pairs that share an enabled joint
     int *joint_partners;               // JOINT_PARTNERS per body: other bodies joined to it (-1: none)
     int *island_joint_count, *island_joint_off, *island_fill_j;
-    int *island_joints;  // 3 x max_joints: as scattered | by (type, index) | by (priority, index, type)
+    // 5 x max_joints: as scattered | by (type, index) | by (priority, index, type) | colour of
+    // each ranked joint | ranked joints grouped by colour (per-CTA solve)
+    int *island_joints;
     int max_joints;      // capacity of the per-island joint lists
     int *joint_wake;     // flag: some joint has to wake a body this step
     int *body_local;  // index of a body inside its island's body list (per-warp solve)
+    // giant islands (more constraints than giant_min): solved by the whole grid
+    int giant_min;
+    int giant_blocks;                      // blocks of the cooperative launch (co-resident)
+    int *giant_list;
+    unsigned long long *giant_claim;       // 4 x cap: contact claims, two parities | joint claims, two parities
+    int *giant_count;  // 4 x (GIANT_COLOURS + 2): contact colour offsets, contact fill cursors, joint offsets, joint fill
 };
 
 // ---- user joints of every type under one id ---------------------------------------------
@@ -460,6 +474,7 @@ void launch_broadphase(DevWorld &w, cudaStream_t s);
 void launch_narrowphase(DevWorld &w, float dt, cudaStream_t s, cudaEvent_t mid = nullptr);
 void launch_contacts_and_islands(DevWorld &w, float dt, float warm_ratio, cudaStream_t s);
 void launch_solver(DevWorld &w, float dt, float warm_ratio, cudaStream_t s, cudaEvent_t mid = nullptr);
+int giant_blocks_for_device();
 void launch_update_bounds(DevWorld &w, cudaStream_t s);
 void upload_settings(const DevSettings &s, double spec64, cudaStream_t st);
 void launch_cache_begin(DevWorld &w, cudaStream_t s);
@@ -478,6 +493,7 @@ constexpr int EPA_DEFAULT_MAX_THREADS = NUM_SMS * 4 * 64;  // one EPA polytope p
 constexpr int EPA_MAX_THREADS = NUM_SMS * 8 * 64;          // upper bound of the launch-shape override
 constexpr int EPA_BIG_THREADS = 1024;  // threads of the fallback pass with the reference's polytope limits
 constexpr int JOINT_PARTNERS = 8;      // joined bodies remembered per body for the broadphase pair filter
+constexpr int GIANT_COLOURS = 1024;    // colours of the giant-island solve; the rest go to one thread in order
 
 // scan / sort utilities (cc_scan.cu)
 void exclusive_scan_int(const int *in, int *out, int n, int *total, int *tmp, cudaStream_t s);

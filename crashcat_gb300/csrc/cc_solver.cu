@@ -31,6 +31,7 @@ void upload_settings_solver(const DevSettings &s, cudaStream_t st) {
 
 constexpr int SMALL_ISLAND_MAX_CONS = 64;  // upper bound of the per-thread class (register arrays)
 constexpr int SMALL_ISLAND_MAX_BODIES = 64;
+constexpr int SMALL_ISLAND_MAX_JOINTS = 16;  // bound of the per-thread class's joint list (register array)
 // islands above the per-thread class and within these limits run on one warp
 constexpr int WARP_MAX_CONS = 256;
 constexpr int WARP_MAX_BODIES = 128;
@@ -472,9 +473,20 @@ __global__ void k_island_classify(DevWorld w, int *small_list, int *large_list) 
         int nc = w.island_cons_count[i], nb = w.island_body_count[i];
         int nj = joint_total(w) > 0 ? w.island_joint_count[i] : 0;
         atomicMax(&w.ctr->max_island_constraints, nc + nj);
-        if (nj > 0) {  // islands with joints: the per-CTA solve, joints by one thread in the reference's order
-            int k = atomicAdd(&w.ctr->num_large_islands, 1);
-            large_list[k] = i;
+        if (nc + nj > w.giant_min) {  // a pile: the whole grid solves it
+            int k = atomicAdd(&w.ctr->num_giant_islands, 1);
+            w.giant_list[k] = i;
+        } else if (nj > 0) {
+            // islands with joints: one thread in the reference's exact order when small (a lone
+            // ragdoll), else the per-CTA solve
+            if (nj <= c_settings.small_island_max_joints && nc <= SMALL_ISLAND_MAX_CONS &&
+                nb <= SMALL_ISLAND_MAX_BODIES) {
+                int k = atomicAdd(&w.ctr->num_small_islands, 1);
+                small_list[k] = i;
+            } else {
+                int k = atomicAdd(&w.ctr->num_large_islands, 1);
+                large_list[k] = i;
+            }
         } else if (nc <= c_settings.small_island_max_cons && nb <= SMALL_ISLAND_MAX_BODIES) {
             int k = atomicAdd(&w.ctr->num_small_islands, 1);
             small_list[k] = i;
@@ -799,6 +811,7 @@ __global__ void __launch_bounds__(128) k_solve_small(DevWorld w, CacheTables ct,
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
         int isl = small_list[s];
         int nb = w.island_body_count[isl], nc = w.island_cons_count[isl];
+        int nj = joint_total(w) > 0 ? w.island_joint_count[isl] : 0;
         const int *bl = w.island_bodies + w.island_body_off[isl];
         const int *cl = w.island_cons + w.island_cons_off[isl];
         int order[SMALL_ISLAND_MAX_CONS];
@@ -813,8 +826,22 @@ __global__ void __launch_bounds__(128) k_solve_small(DevWorld w, CacheTables ct,
             }
             order[j + 1] = x;
         }
+        // joints: warm started type by type in creation order (constraints.ts:290-303), solved
+        // by (priority, index, type) (sortConstraintIds constraints.ts:248-261)
+        int jord[SMALL_ISLAND_MAX_JOINTS];
+        if (nj > 0) {
+            const int *jl = w.island_joints + w.island_joint_off[isl];
+            for (int k = 0; k < nj; k++) {
+                int x = jl[k], j = k - 1;
+                while (j >= 0 && jord[j] > x) {
+                    jord[j + 1] = jord[j];
+                    j--;
+                }
+                jord[j + 1] = x;
+            }
+        }
         for (int k = 0; k < nb; k++) prepare_body(w, bl[k]);
-        if (nc > 0) {
+        if (nc > 0 || nj > 0) {
             if (c_settings.warm_starting) {
                 for (int k = 0; k < nc; k++) {
                     ContactConstraint &c = w.cons[order[k]];
@@ -823,6 +850,15 @@ __global__ void __launch_bounds__(128) k_solve_small(DevWorld w, CacheTables ct,
                     store_body_vel(w, c.a, A);
                     store_body_vel(w, c.b, B);
                 }
+                for (int k = 0; k < nj; k++) joint_warm(w, jord[k], ratio);
+            }
+            for (int k = 1; k < nj; k++) {  // now into solve order
+                int x = jord[k], j = k - 1;
+                while (j >= 0 && joint_before(w, x, jord[j])) {
+                    jord[j + 1] = jord[j];
+                    j--;
+                }
+                jord[j + 1] = x;
             }
             for (int it = 0; it < c_settings.vel_iters; it++) {
                 for (int k = 0; k < nc; k++) {
@@ -832,11 +868,12 @@ __global__ void __launch_bounds__(128) k_solve_small(DevWorld w, CacheTables ct,
                     store_body_vel(w, c.a, A);
                     store_body_vel(w, c.b, B);
                 }
+                for (int k = 0; k < nj; k++) joint_solve_velocity(w, jord[k], dt);
             }
             for (int k = 0; k < nc; k++) store_impulses(w, crecs, w.cons[order[k]]);
         }
         for (int k = 0; k < nb; k++) integrate_body(w, bl[k], dt);
-        if (nc > 0) {
+        if (nc > 0 || nj > 0) {
             for (int it = 0; it < c_settings.pos_iters; it++) {
                 bool any = false;
                 for (int k = 0; k < nc; k++) {
@@ -856,6 +893,7 @@ __global__ void __launch_bounds__(128) k_solve_small(DevWorld w, CacheTables ct,
                         any = true;
                     }
                 }
+                for (int k = 0; k < nj; k++) any = joint_solve_position(w, jord[k], dt) || any;
                 if (!any) break;
             }
         }
@@ -880,6 +918,7 @@ __global__ void __launch_bounds__(128) k_solve_small(DevWorld w, CacheTables ct,
 // greedily coloured in that order and swept colour by colour
 // ---------------------------------------------------------------------------
 constexpr int LARGE_BLOCK = 256;
+constexpr int JOINT_COLOURS = 64;  // joint colours of the per-CTA solve; the rest go to one thread
 
 __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTables ct, const int *large_list,
                                                               int *scratch_order, int *scratch_colour,
@@ -887,6 +926,7 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
     __shared__ int s_any;
     __shared__ int s_ncol;
     __shared__ int s_colour_start[257];
+    __shared__ int s_jstart[JOINT_COLOURS + 2];
     int nl = w.ctr->num_large_islands;
     CacheRecord *crecs = ct.recs[*ct.parity];
     for (int li = blockIdx.x; li < nl; li += gridDim.x) {
@@ -989,6 +1029,68 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
             }
         }
         __syncthreads();
+        // joints: greedy colouring in solve order like the contacts, JOINT_COLOURS colours at most
+        // (the rest is solved by one thread in order); warm starting stays serial in index order
+        int *j_col = j_pri + w.max_joints;
+        int *j_grp = j_col + w.max_joints;
+        if (nj > 0) {
+            for (int k = threadIdx.x; k < nj; k += blockDim.x) j_col[k] = -1;
+            int jround = 0;
+            while (true) {
+                for (int k = threadIdx.x; k < nb; k += blockDim.x) scratch_claim[bl[k]] = 0x7fffffff;
+                __syncthreads();
+                int left = 0;
+                for (int k = threadIdx.x; k < nj; k += blockDim.x) {
+                    if (j_col[k] >= 0) continue;
+                    left = 1;
+                    const DevJointHead &h = joint_head(w, j_pri[k]);
+                    if (motion_of(w.flags[h.a]) == DYNAMIC) atomicMin(&scratch_claim[h.a], k);
+                    if (motion_of(w.flags[h.b]) == DYNAMIC) atomicMin(&scratch_claim[h.b], k);
+                }
+                if (!__syncthreads_or(left)) break;
+                for (int k = threadIdx.x; k < nj; k += blockDim.x) {
+                    if (j_col[k] >= 0) continue;
+                    const DevJointHead &h = joint_head(w, j_pri[k]);
+                    bool oka = motion_of(w.flags[h.a]) != DYNAMIC || scratch_claim[h.a] == k;
+                    bool okb = motion_of(w.flags[h.b]) != DYNAMIC || scratch_claim[h.b] == k;
+                    if (oka && okb) j_col[k] = jround;
+                }
+                __syncthreads();
+                if (++jround >= JOINT_COLOURS) {
+                    for (int k = threadIdx.x; k < nj; k += blockDim.x)
+                        if (j_col[k] < 0) j_col[k] = JOINT_COLOURS;
+                    __syncthreads();
+                    break;
+                }
+            }
+            if (threadIdx.x == 0) {  // counting sort by colour, rank order inside a colour
+                for (int c = 0; c <= JOINT_COLOURS + 1; c++) s_jstart[c] = 0;
+                for (int k = 0; k < nj; k++) s_jstart[j_col[k] + 1]++;
+                for (int c = 0; c <= JOINT_COLOURS; c++) s_jstart[c + 1] += s_jstart[c];
+                int fill[JOINT_COLOURS + 1];
+                for (int c = 0; c <= JOINT_COLOURS; c++) fill[c] = s_jstart[c];
+                for (int k = 0; k < nj; k++) j_grp[fill[j_col[k]]++] = j_pri[k];
+            }
+            __syncthreads();
+        }
+        // joint colours in turn: parallel inside a colour, the last (overflow) colour by one thread
+        auto joint_sweep = [&](int mode) -> bool {
+            bool any = false;
+            for (int c = 0; c <= JOINT_COLOURS; c++) {
+                int s0 = s_jstart[c], s1 = s_jstart[c + 1];
+                if (s1 <= s0) continue;
+                int kbeg = c < JOINT_COLOURS ? s0 + (int)threadIdx.x : (threadIdx.x == 0 ? s0 : s1);
+                int kstep = c < JOINT_COLOURS ? (int)blockDim.x : 1;
+                for (int k = kbeg; k < s1; k += kstep) {
+                    if (mode == 0)
+                        joint_solve_velocity(w, j_grp[k], dt);
+                    else
+                        any = joint_solve_position(w, j_grp[k], dt) || any;
+                }
+                __syncthreads();
+            }
+            return any;
+        };
         int colour_end_last = nc;
         // warm start (per colour)
         auto sweep = [&](int mode) {
@@ -1039,9 +1141,7 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
             sweep(1);
             if (nj > 0) {
                 __syncthreads();
-                if (threadIdx.x == 0)
-                    for (int k = 0; k < nj; k++) joint_solve_velocity(w, j_pri[k], dt);
-                __syncthreads();
+                joint_sweep(0);
             }
         }
         for (int k = threadIdx.x; k < nc; k += blockDim.x) store_impulses(w, crecs, w.cons[cl[k]]);
@@ -1079,11 +1179,7 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
             }
             if (nj > 0) {
                 __syncthreads();
-                if (threadIdx.x == 0) {
-                    bool applied = false;
-                    for (int k = 0; k < nj; k++) applied = joint_solve_position(w, j_pri[k], dt) || applied;
-                    if (applied) s_any = 1;
-                }
+                if (joint_sweep(1)) s_any = 1;
                 __syncthreads();
             }
             if (!s_any) break;
@@ -1375,6 +1471,290 @@ __global__ void __launch_bounds__(WARP_BLOCK) k_solve_warp(DevWorld w, CacheTabl
 }
 
 // ---------------------------------------------------------------------------
+// giant islands: an island with more than giant_min constraints (a pile of
+// thousands of bodies) is solved by the whole grid.  One cooperative launch,
+// co-resident blocks meeting at a bounded grid barrier, walks the giant
+// islands one after another:
+//   colouring  - greedy, in the reference's solve order, without sorting: per
+//                round every uncoloured constraint claims its dynamic bodies
+//                with a 64-bit atomicMin of its order key, and the ones that
+//                hold all their claims take the round's colour.  Contacts and
+//                joints are coloured side by side with their own claims;
+//   sweeps     - warm start, velocity and position iterations visit the
+//                contact colours, then the joint colours; inside a colour the
+//                constraints share no dynamic body, so their order does not
+//                change the result.
+// ---------------------------------------------------------------------------
+constexpr int GIANT_BLOCK = 256;
+constexpr unsigned GIANT_SPIN_LIMIT = 1u << 21;  // polls (each ~100 ns or more) before a barrier gives up
+
+// Grid barrier over the co-resident blocks of the cooperative launch.  The wait is bounded:
+// a block that gives up raises bar_error and OVF_TIMEOUT, and every block then leaves.
+__device__ bool grid_barrier(DevCounters *ctr, unsigned nblocks) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = &ctr->bar_gen;
+        volatile int *err = &ctr->bar_error;
+        unsigned g = *gen;
+        __threadfence();
+        int ok = 1;
+        if (atomicAdd(&ctr->bar_count, 1u) == nblocks - 1) {
+            atomicExch(&ctr->bar_count, 0u);
+            __threadfence();
+            atomicAdd(&ctr->bar_gen, 1u);
+        } else {
+            unsigned spins = 0;
+            while (*gen == g) {
+                if (*err || ++spins > GIANT_SPIN_LIMIT) {
+                    atomicExch(&ctr->bar_error, 1);
+                    atomicOr(&ctr->overflow, OVF_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        s_ok = ok && !*err;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// order keys: contacts by (sortKey, idA, idB) with A < B; for a claim on body X the other body
+// breaks ties, which orders the contacts sharing X as the full key does
+__device__ __forceinline__ unsigned long long contact_claim_key(const ContactConstraint &c, int x) {
+    return ((unsigned long long)c.sort_key << 32) | (unsigned)(x == c.a ? c.b : c.a);
+}
+__device__ __forceinline__ unsigned long long joint_claim_key(const DevWorld &w, int id) {
+    const DevJointHead &h = joint_head(w, id);
+    return ((unsigned long long)((unsigned)h.priority ^ 0x80000000u) << 32) | ((unsigned long long)h.index << 1) |
+           (unsigned)((id & JOINT_SWING) != 0);
+}
+
+__global__ void __launch_bounds__(GIANT_BLOCK) k_solve_giant(DevWorld w, CacheTables ct, float dt, float ratio) {
+    DevCounters *ctr = w.ctr;
+    const int ng = ctr->num_giant_islands;
+    if (ng == 0) return;
+    const unsigned nblk = gridDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
+    CacheRecord *crecs = ct.recs[*ct.parity];
+    unsigned long long *cclaim[2] = {w.giant_claim, w.giant_claim + w.cap};
+    unsigned long long *jclaim[2] = {w.giant_claim + 2 * (size_t)w.cap, w.giant_claim + 3 * (size_t)w.cap};
+    int *c_off = w.giant_count, *c_fill = c_off + GIANT_COLOURS + 2;
+    int *j_off = c_fill + GIANT_COLOURS + 2, *j_fill = j_off + GIANT_COLOURS + 2;
+    const unsigned long long NONE = ~0ull;
+    for (int g = 0; g < ng; g++) {
+        int isl = w.giant_list[g];
+        int nb = w.island_body_count[isl], nc = w.island_cons_count[isl];
+        int nj = joint_total(w) > 0 ? w.island_joint_count[isl] : 0;
+        const int *bl = w.island_bodies + w.island_body_off[isl];
+        const int *cl = w.island_cons + w.island_cons_off[isl];
+        int *colour = w.scratch_colour + w.island_cons_off[isl];
+        int *c_grp = w.scratch_claim + w.cap + w.island_cons_off[isl];
+        const int *jl = w.island_joints + (nj > 0 ? w.island_joint_off[isl] : 0);
+        int *j_col = const_cast<int *>(jl) + 3 * w.max_joints;
+        int *j_grp = j_col + w.max_joints;
+        for (int k = tid; k < nb; k += nthr) {
+            int b = bl[k];
+            prepare_body(w, b);
+            cclaim[0][b] = cclaim[1][b] = NONE;
+            jclaim[0][b] = jclaim[1][b] = NONE;
+        }
+        for (int k = tid; k < nc; k += nthr) colour[k] = -1;
+        for (int k = tid; k < nj; k += nthr) j_col[k] = -1;
+        for (int k = tid; k < 4 * (GIANT_COLOURS + 2); k += nthr) w.giant_count[k] = 0;
+        if (tid == 0) {
+            ctr->giant_sleep = 1;
+            ctr->giant_left[0] = ctr->giant_left[1] = 0;
+        }
+        if (!grid_barrier(ctr, nblk)) return;
+        // ---- colouring: round r uses the claims and the flag of parity r & 1 and clears the
+        // other parity's for round r + 1 ----
+        int ncol = 0, round = 0;
+        while (true) {
+            int p = round & 1;
+            int left = 0;
+            for (int k = tid; k < nc; k += nthr) {
+                if (colour[k] >= 0) continue;
+                left = 1;
+                const ContactConstraint &c = w.cons[cl[k]];
+                if (motion_of(w.flags[c.a]) == DYNAMIC) atomicMin(&cclaim[p][c.a], contact_claim_key(c, c.a));
+                if (motion_of(w.flags[c.b]) == DYNAMIC) atomicMin(&cclaim[p][c.b], contact_claim_key(c, c.b));
+            }
+            for (int k = tid; k < nj; k += nthr) {
+                if (j_col[k] >= 0) continue;
+                left = 1;
+                int id = jl[k];
+                const DevJointHead &h = joint_head(w, id);
+                unsigned long long key = joint_claim_key(w, id);
+                if (motion_of(w.flags[h.a]) == DYNAMIC) atomicMin(&jclaim[p][h.a], key);
+                if (motion_of(w.flags[h.b]) == DYNAMIC) atomicMin(&jclaim[p][h.b], key);
+            }
+            left = __syncthreads_or(left);
+            if (threadIdx.x == 0 && left) atomicOr(&ctr->giant_left[p], 1);
+            if (!grid_barrier(ctr, nblk)) return;
+            if (!*(volatile int *)&ctr->giant_left[p]) break;
+            if (tid == 0) ctr->giant_left[p ^ 1] = 0;
+            bool last = ncol == GIANT_COLOURS;  // the overflow colour takes everything left
+            for (int k = tid; k < nc; k += nthr) {
+                if (colour[k] >= 0) continue;
+                const ContactConstraint &c = w.cons[cl[k]];
+                bool ok = last || ((motion_of(w.flags[c.a]) != DYNAMIC || cclaim[p][c.a] == contact_claim_key(c, c.a)) &&
+                                   (motion_of(w.flags[c.b]) != DYNAMIC || cclaim[p][c.b] == contact_claim_key(c, c.b)));
+                if (ok) {
+                    colour[k] = ncol;
+                    atomicAdd(&c_off[ncol + 1], 1);
+                }
+            }
+            for (int k = tid; k < nj; k += nthr) {
+                if (j_col[k] >= 0) continue;
+                int id = jl[k];
+                const DevJointHead &h = joint_head(w, id);
+                unsigned long long key = joint_claim_key(w, id);
+                bool ok = last || ((motion_of(w.flags[h.a]) != DYNAMIC || jclaim[p][h.a] == key) &&
+                                   (motion_of(w.flags[h.b]) != DYNAMIC || jclaim[p][h.b] == key));
+                if (ok) {
+                    j_col[k] = ncol;
+                    atomicAdd(&j_off[ncol + 1], 1);
+                }
+            }
+            for (int k = tid; k < nb; k += nthr) {
+                int b = bl[k];
+                cclaim[p ^ 1][b] = NONE;
+                jclaim[p ^ 1][b] = NONE;
+            }
+            ncol++;
+            round++;
+            if (!grid_barrier(ctr, nblk)) return;
+        }
+        // ---- group by colour: offsets, then a scatter (any order inside a colour) ----
+        if (tid == 0) {
+            for (int c = 0; c < ncol; c++) {
+                c_off[c + 1] += c_off[c];
+                j_off[c + 1] += j_off[c];
+            }
+            for (int c = 0; c <= ncol; c++) {
+                c_fill[c] = c_off[c];
+                j_fill[c] = j_off[c];
+            }
+        }
+        if (!grid_barrier(ctr, nblk)) return;
+        for (int k = tid; k < nc; k += nthr) c_grp[atomicAdd(&c_fill[colour[k]], 1)] = cl[k];
+        for (int k = tid; k < nj; k += nthr) j_grp[atomicAdd(&j_fill[j_col[k]], 1)] = jl[k];
+        if (!grid_barrier(ctr, nblk)) return;
+        if (ncol > GIANT_COLOURS && tid == 0) {
+            // the overflow colour is solved in order by one thread: sort it by the order key
+            int s0 = c_off[GIANT_COLOURS], s1 = c_off[GIANT_COLOURS + 1];
+            for (int k = s0 + 1; k < s1; k++) {
+                int x = c_grp[k], j = k - 1;
+                while (j >= s0 && con_less(w.cons[x], w.cons[c_grp[j]])) {
+                    c_grp[j + 1] = c_grp[j];
+                    j--;
+                }
+                c_grp[j + 1] = x;
+            }
+            s0 = j_off[GIANT_COLOURS];
+            s1 = j_off[GIANT_COLOURS + 1];
+            for (int k = s0 + 1; k < s1; k++) {
+                int x = j_grp[k], j = k - 1;
+                while (j >= s0 && joint_before(w, x, j_grp[j])) {
+                    j_grp[j + 1] = j_grp[j];
+                    j--;
+                }
+                j_grp[j + 1] = x;
+            }
+        }
+        if (!grid_barrier(ctr, nblk)) return;
+        // one pass over the colours of one kind: mode 0 warm start, 1 velocity, 2 position
+        auto sweep = [&](bool joints, int mode, int &any) -> bool {
+            const int *off = joints ? j_off : c_off;
+            const int *grp = joints ? j_grp : c_grp;
+            for (int c = 0; c < ncol; c++) {
+                int s0 = off[c], s1 = off[c + 1];
+                if (s1 <= s0) continue;
+                bool serial = c == GIANT_COLOURS;
+                int kbeg = serial ? (tid == 0 ? s0 : s1) : s0 + tid, kstep = serial ? 1 : nthr;
+                for (int k = kbeg; k < s1; k += kstep) {
+                    int e = grp[k];
+                    if (joints) {
+                        if (mode == 0)
+                            joint_warm(w, e, ratio);
+                        else if (mode == 1)
+                            joint_solve_velocity(w, e, dt);
+                        else if (joint_solve_position(w, e, dt))
+                            any = 1;
+                    } else if (mode < 2) {
+                        ContactConstraint &con = w.cons[e];
+                        BodyRef A = load_body(w, con.a), B = load_body(w, con.b);
+                        if (mode == 0)
+                            warm_start_con(con, A, B, ratio);
+                        else
+                            solve_velocity_con(con, A, B);
+                        store_body_vel(w, con.a, A);
+                        store_body_vel(w, con.b, B);
+                    } else {
+                        const ContactConstraint &con = w.cons[e];
+                        uint32_t fa = w.flags[con.a], fb = w.flags[con.b];
+                        PoseRef PA{xyz(w.com[con.a]), w.quat[con.a]}, PB{xyz(w.com[con.b]), w.quat[con.b]};
+                        if (solve_position_con(w, con, PA, PB, motion_of(fa), motion_of(fb), fa, fb)) {
+                            if (motion_of(fa) == DYNAMIC) {
+                                w.com[con.a] = make_float4(PA.com.x, PA.com.y, PA.com.z, 0.f);
+                                w.quat[con.a] = PA.q;
+                            }
+                            if (motion_of(fb) == DYNAMIC) {
+                                w.com[con.b] = make_float4(PB.com.x, PB.com.y, PB.com.z, 0.f);
+                                w.quat[con.b] = PB.q;
+                            }
+                            any = 1;
+                        }
+                    }
+                }
+                if (!grid_barrier(ctr, nblk)) return false;
+            }
+            return true;
+        };
+        int dummy = 0;
+        if (c_settings.warm_starting) {
+            if (!sweep(false, 0, dummy) || !sweep(true, 0, dummy)) return;
+        }
+        for (int it = 0; it < c_settings.vel_iters; it++)
+            if (!sweep(false, 1, dummy) || !sweep(true, 1, dummy)) return;
+        for (int k = tid; k < nc; k += nthr) store_impulses(w, crecs, w.cons[cl[k]]);
+        for (int k = tid; k < nb; k += nthr) integrate_body(w, bl[k], dt);
+        if (tid == 0) ctr->giant_any[0] = ctr->giant_any[1] = 0;
+        if (!grid_barrier(ctr, nblk)) return;
+        for (int it = 0; it < c_settings.pos_iters; it++) {
+            int p = it & 1, any = 0;
+            if (!sweep(false, 2, any) || !sweep(true, 2, any)) return;
+            any = __syncthreads_or(any);
+            if (threadIdx.x == 0 && any) atomicOr(&ctr->giant_any[p], 1);
+            if (!grid_barrier(ctr, nblk)) return;
+            if (!*(volatile int *)&ctr->giant_any[p]) break;
+            if (tid == 0) ctr->giant_any[p ^ 1] = 0;
+        }
+        for (int k = tid; k < nb; k += nthr) finish_body(w, bl[k]);
+        if (!grid_barrier(ctr, nblk)) return;
+        if (c_settings.allow_sleeping) {
+            int mine = 1;
+            for (int k = tid; k < nb; k += nthr) {
+                int i = bl[k];
+                if (motion_of(w.flags[i]) != DYNAMIC) continue;
+                if (!sleep_update(w, i, dt)) mine = 0;
+            }
+            mine = __syncthreads_and(mine);
+            if (threadIdx.x == 0 && !mine) atomicAnd(&ctr->giant_sleep, 0);
+            if (!grid_barrier(ctr, nblk)) return;
+            if (*(volatile int *)&ctr->giant_sleep)
+                for (int k = tid; k < nb; k += nthr)
+                    if (motion_of(w.flags[bl[k]]) == DYNAMIC) sleep_body(w, bl[k]);
+        }
+        if (!grid_barrier(ctr, nblk)) return;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 static CacheTables tables_of(DevWorld &w) {
@@ -1463,6 +1843,29 @@ void launch_solver(DevWorld &w, float dt, float ratio, cudaStream_t s, cudaEvent
     cudaEventRecord(w.ev_join, w.aux_stream);
     k_solve_warp<<<NUM_SMS * w.warp_blocks_per_sm, WARP_BLOCK, warp_smem, s>>>(w, ct, dt, ratio);
     cudaStreamWaitEvent(s, w.ev_join, 0);
+    // giant islands: a cooperative launch (all blocks co-resident), after the other tiers so that
+    // it runs alone; it returns at once when the step has no giant island
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)w.giant_blocks);
+    cfg.blockDim = dim3(GIANT_BLOCK);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (w.giant_blocks > 0) cudaLaunchKernelEx(&cfg, k_solve_giant, w, ct, dt, ratio);
+}
+
+// blocks of the giant-island launch: one per SM, fewer if the kernel cannot be resident at that
+// count (a cooperative launch needs every block resident at once)
+int giant_blocks_for_device() {
+    int dev = 0, sms = NUM_SMS, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_giant, GIANT_BLOCK, 0);
+    if (per_sm < 1) return 0;
+    return sms;
 }
 
 }  // namespace cc

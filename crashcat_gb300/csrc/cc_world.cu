@@ -188,6 +188,11 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
     // launch-shape tunable: islands with at most this many contacts are solved by one
     // thread in the reference's exact order, larger ones by a warp (up to 256 contacts
     // and 128 bodies) or a CTA with order-preserving graph colouring
+    d.small_island_max_joints = 16;
+    if (const char *e = getenv("CRASHCAT_SMALL_JOINTS_MAX")) {
+        int v = atoi(e);
+        if (v >= 0 && v <= 16) d.small_island_max_joints = v;
+    }
     d.small_island_max_cons = 8;
     if (const char *e = getenv("CRASHCAT_SMALL_ISLAND_MAX")) {
         int v = atoi(e);
@@ -341,7 +346,18 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
     ALLOC(contact_event, w.max_manifolds);
     ALLOC(removed_keys, w.max_manifolds);
     ALLOC(body_local, cap);
+    ALLOC(giant_list, cap);
+    ALLOC(giant_claim, 4 * (size_t)cap);
+    ALLOC(giant_count, 4 * (GIANT_COLOURS + 2));
 #undef ALLOC
+    // islands with more constraints than this are solved by the whole grid (launch-shape tunable)
+    w.giant_min = 8192;
+    if (const char *e = getenv("CRASHCAT_GIANT_MIN")) {
+        int v = atoi(e);
+        if (v >= 64) w.giant_min = v;
+    }
+    w.giant_blocks = giant_blocks_for_device();
+    if (w.giant_blocks <= 0) w.giant_min = 0x7fffffff;
     if ((r = cuda_ok(cudaStreamCreateWithFlags(&W->stream, cudaStreamNonBlocking))) != CC_OK ||
         (r = cuda_ok(cudaStreamCreateWithFlags(&w.aux_stream, cudaStreamNonBlocking))) != CC_OK ||
         (r = cuda_ok(cudaEventCreateWithFlags(&w.ev_fork, cudaEventDisableTiming))) != CC_OK ||
@@ -379,7 +395,8 @@ int cc_world_destroy(cc_world *W) {
                     w.cache_recs[1], w.cache_parity, w.root_flag, w.small_list, w.large_list, w.scratch_order,
                     w.scratch_colour, w.scratch_claim, w.mid_list, w.body_local, w.contact_event,
                     w.removed_keys, W->d_state_rows, w.hinges, w.island_joints, w.island_joint_count,
-                    w.island_joint_off, w.island_fill_j, w.joint_wake, w.joint_partners, w.swings};
+                    w.island_joint_off, w.island_fill_j, w.joint_wake, w.joint_partners, w.swings,
+                    w.giant_list, w.giant_claim, w.giant_count};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : W->adj.allocs)
@@ -607,7 +624,7 @@ static int run_steps(cc_world *W, float dt, int n_steps) {
     CC_TRY(cudaGetLastError());
     cudaEventElapsedTime(&W->last_call_ms, W->ev_begin, W->ev_end);
     W->last_ctr = *W->h_ctr;
-    if (W->last_ctr.overflow) status = CC_ERR_CAPACITY;
+    if (W->last_ctr.overflow) status = (W->last_ctr.overflow & OVF_TIMEOUT) ? CC_ERR_TIMEOUT : CC_ERR_CAPACITY;
     W->last_status = status;
     return status;
 }
@@ -1166,7 +1183,7 @@ static int ensure_joint_capacity(cc_world *W, int need_hinges, int need_swings) 
     int need_lists = w.max_hinges + w.max_swings;
     if (need_lists > w.max_joints) {
         int *nl = nullptr;
-        if ((r = dalloc(&nl, 3 * (size_t)need_lists)) != CC_OK) return r;
+        if ((r = dalloc(&nl, 5 * (size_t)need_lists)) != CC_OK) return r;
         CC_TRY(cudaStreamSynchronize(W->stream));
         if (w.island_joints) cudaFree(w.island_joints);
         w.island_joints = nl;
