@@ -28,6 +28,12 @@ checkpoints, recomputation with tapes, reverse sweep, gradients to the host) / 1
 fd_check = central finite differences (h = 1e-3) of the full step along seeded
 directions against the adjoint, on the first 8 worlds.
 
+ragdolls: the jointed-ragdoll workload (2,000 ragdolls x 11 capsules with 4 hinges and 6
+swing-twist joints each, 600 steps at dt 1/60, 12/4 iterations): GPU body-steps/s over the
+whole run with per-phase ms/step (the ragdolls fall, then pile into one giant island solved
+by the whole grid); cpu_baseline = the oracle on the same scene for a bounded number of steps
+from spawn, against the GPU's value over the same falling phase.
+
 --impl reference: the reference (TypeScript) cannot run on this machine; its FP64
 C++ restatement (oracle/) steps a bounded sample of the same worlds on all
 host cores (one process per core, worlds split across them).
@@ -67,6 +73,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--adjoint", type=int, default=1, help="measure the rollout adjoint (1) or skip it (0)")
+    ap.add_argument("--ragdolls", type=int, default=1, help="measure the jointed-ragdoll workload (1) or skip it (0)")
     ap.add_argument("--settle", type=int, default=360,
                     help="untimed steps before the warm-up so the timed steps are contact-rich")
     return ap.parse_args()
@@ -367,6 +374,53 @@ def adjoint_measurement(num_worlds: int = 1024, steps: int = 120, checkpoint_eve
                          "model": "adjoint over each step's fixed contact set; FD through the full step"}}
 
 
+def ragdoll_measurement(cpu_seconds: float = 8.0):
+    """The jointed-ragdoll workload (2,000 ragdolls of 11 capsules, 4 hinges and 6 swing-twist
+    joints each, in a 60 m arena of static walls; dt 1/60, 12/4 iterations): all 600 steps from
+    spawn on the GPU, timed per phase (falling, piling up, resting pile), and the FP64 oracle on
+    the same scene for a bounded number of steps from spawn on one host core."""
+    from crashcat_gb300 import scenes, world as W
+    from oracle import build as obuild, pyoracle
+    sc = scenes.ragdolls()
+    ws = W.standard_settings(velocity_iterations=sc.velocity_iterations, position_iterations=sc.position_iterations)
+    g = W.GpuWorld(ws, sc.n + 16)
+    g.add_bodies(sc.bodies)
+    g.add_hinges(sc.hinges)
+    g.add_swing_twists(sc.swings)
+    g.set_skip_joint_pairs(True)
+    phases, total_ms, status = [], 0.0, 0
+    for first, count in ((0, 100), (100, 400), (500, 100)):
+        status |= g.step(sc.dt, count)
+        st = g.stats()
+        total_ms += st["last_call_ms"]
+        phases.append({"steps": [first, first + count], "ms_per_step": st["last_call_ms"] / count,
+                       "islands": st["num_islands"], "max_island_constraints": st["max_island_constraints"],
+                       "giant_islands": st["num_giant_islands"], "giant_colours": st["giant_colours"],
+                       "manifolds": st["num_manifolds"]})
+    rows, _ = g.get_state()
+    del g
+    obuild.build()
+    o = pyoracle.OracleWorld(ws, sc.bodies)
+    for h in sc.hinges:
+        o.add_hinge_record(h)
+    for h in sc.swings:
+        o.add_swing_twist_record(h)
+    o.set_skip_joint_pairs(True)
+    t0, k = time.perf_counter(), 0
+    while time.perf_counter() - t0 < cpu_seconds and k < 100:
+        o.step(sc.dt, 1)
+        k += 1
+    cpu_s = time.perf_counter() - t0
+    gpu_first = phases[0]["ms_per_step"]
+    return {"workload": "ragdolls", "ragdolls": 2000, "bodies": int(sc.n), "hinges": int(len(sc.hinges)),
+            "swing_twists": int(len(sc.swings)), "steps": 600, "value": sc.n * 600 / (total_ms * 1e-3),
+            "unit": METRIC, "ms_per_step": total_ms / 600, "phases": phases, "status": int(status),
+            "finite": bool(np.isfinite(rows).all()),
+            "cpu_baseline": {"value": sc.n * k / cpu_s, "unit": METRIC, "cores": 1, "kind": "port",
+                             "sample": f"first {k} steps from spawn (falling phase)",
+                             "gpu_same_phase_value": sc.n / (gpu_first * 1e-3)}}
+
+
 def single_world_comparison(scene, ws_batched, settled_rows, dt, steps: int, sample_worlds: int = 48):
     """Steps a spread sample of the workload's worlds through the plain single-world path:
     one handle per world, each stepped once per step with cc_world_step (which blocks until
@@ -492,6 +546,7 @@ def run_gpu(args, rank, world_size, local):
 
     single = single_world_comparison(scene, ws, settled_rows, dt, steps=max(3, min(args.steps, 10)))
     adjoint = adjoint_measurement() if args.adjoint else None
+    ragdolls = ragdoll_measurement() if args.ragdolls and rank == 0 else None
     single["batched_over_single"] = value / world_size / single["value"]
 
     if rank == 0:
@@ -515,6 +570,7 @@ def run_gpu(args, rank, world_size, local):
             "cpu_baseline": cpu,
             "vs_single_world": single,
             "adjoint": adjoint,
+            "ragdolls": ragdolls,
             "clocks": clk.summary(),
             "gpu_launches": stats["gpu_launches_per_step"] * args.steps,
             "counters": {k: stats_w[k] for k in ("num_awake", "num_pairs", "num_manifolds", "num_contact_points",

@@ -67,7 +67,7 @@ class Stats(C.Structure):
     _fields_ = [(n, C.c_int32) for n in (
         "num_bodies", "num_awake", "num_pairs", "num_manifolds", "num_contact_points", "num_epa",
         "num_islands", "max_island_constraints", "overflow_flags", "gpu_launches_per_step")] + [
-        ("last_call_ms", C.c_float)]
+        ("last_call_ms", C.c_float), ("num_giant_islands", C.c_int32), ("giant_colours", C.c_int32)]
 
 
 # numpy mirror of cc_body_desc (natural C alignment, 4-byte fields only)

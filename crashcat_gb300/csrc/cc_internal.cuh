@@ -63,7 +63,8 @@ struct DevCounters {
     unsigned int bar_count, bar_gen;    // grid barrier of the giant-island solve
     int bar_error;                      // a bounded grid-barrier wait gave up
     int giant_left[2], giant_any[2], giant_sleep;
-    int pad[6];
+    int giant_colours;  // most colours of a giant island this step
+    int pad[5];
 };
 
 // Settings copied into constant memory once per world.

@@ -1631,6 +1631,7 @@ __global__ void __launch_bounds__(GIANT_BLOCK) k_solve_giant(DevWorld w, CacheTa
         }
         // ---- group by colour: offsets, then a scatter (any order inside a colour) ----
         if (tid == 0) {
+            atomicMax(&ctr->giant_colours, ncol);
             for (int c = 0; c < ncol; c++) {
                 c_off[c + 1] += c_off[c];
                 j_off[c + 1] += j_off[c];

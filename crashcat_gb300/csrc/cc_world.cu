@@ -357,6 +357,10 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
         if (v >= 64) w.giant_min = v;
     }
     w.giant_blocks = giant_blocks_for_device();
+    if (const char *e = getenv("CRASHCAT_GIANT_BLOCKS")) {  // launch-shape tunable, at most one per SM
+        int v = atoi(e);
+        if (v >= 1 && v < w.giant_blocks) w.giant_blocks = v;
+    }
     if (w.giant_blocks <= 0) w.giant_min = 0x7fffffff;
     if ((r = cuda_ok(cudaStreamCreateWithFlags(&W->stream, cudaStreamNonBlocking))) != CC_OK ||
         (r = cuda_ok(cudaStreamCreateWithFlags(&w.aux_stream, cudaStreamNonBlocking))) != CC_OK ||
@@ -910,6 +914,8 @@ int cc_world_get_stats(cc_world *W, cc_stats *o) {
         o->gpu_launches_per_step = k;
     }
     o->last_call_ms = W->last_call_ms;
+    o->num_giant_islands = c.num_giant_islands;
+    o->giant_colours = c.giant_colours;
     return CC_OK;
 }
 

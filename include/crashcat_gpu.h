@@ -143,6 +143,8 @@ typedef struct cc_stats {
     int32_t overflow_flags;
     int32_t gpu_launches_per_step;
     float last_call_ms; /* device time of the last cc_world_step call (CUDA events on the world's stream) */
+    int32_t num_giant_islands; /* islands solved by the whole grid in the last step */
+    int32_t giant_colours;     /* colours of the largest of them */
 } cc_stats;
 
 typedef struct cc_world cc_world;
