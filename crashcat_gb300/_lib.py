@@ -24,6 +24,7 @@ CC_ERR_UNSUPPORTED = 6
 SHAPE_SPHERE = 0
 SHAPE_BOX = 1
 SHAPE_CAPSULE = 2
+SHAPE_CONVEX_HULL = 3
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 COMBINE_AVERAGE, COMBINE_MULTIPLY, COMBINE_MIN, COMBINE_MAX, COMBINE_GEOMETRIC_MEAN = 0, 1, 2, 3, 4
 MAX_LAYERS = 32
@@ -61,6 +62,13 @@ class Settings(C.Structure):
         ("max_manifolds", C.c_int32),
         ("num_worlds", C.c_int32),
     ]
+
+
+class HullInfo(C.Structure):
+    _fields_ = [("num_points", C.c_int32), ("num_faces", C.c_int32), ("num_face_vertices", C.c_int32),
+                ("convex_radius", C.c_float), ("volume", C.c_float), ("inner_radius", C.c_float),
+                ("com", C.c_float * 3), ("inertia", C.c_float * 9), ("bounds_min", C.c_float * 3),
+                ("bounds_max", C.c_float * 3)]
 
 
 class Stats(C.Structure):
@@ -102,6 +110,11 @@ EXPORTS = {
                                C.c_void_p, C.c_void_p], C.c_int),
     "cc_penetration_static": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_float, C.c_float, C.c_void_p], C.c_int),
     "cc_world_add_hinges": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
+    "cc_world_add_convex_hull": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.POINTER(C.c_int32)], C.c_int),
+    "cc_world_get_convex_hull": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "cc_convex_hull_build": ([C.c_void_p, C.c_int32, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                              C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "cc_world_set_hinge_limits": ([C.c_void_p, C.c_int32, C.c_float, C.c_float], C.c_int),
     "cc_world_set_hinge_motor": ([C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_float], C.c_int),
     "cc_world_set_hinge_enabled": ([C.c_void_p, C.c_int32, C.c_int32], C.c_int),
@@ -233,3 +246,30 @@ def check(status: int, what: str) -> None:
 def ptr(a: np.ndarray) -> C.c_void_p:
     assert a.flags["C_CONTIGUOUS"]
     return C.c_void_p(a.ctypes.data)
+
+
+def _hull_arrays(call) -> dict:
+    """Runs a hull export (cc_convex_hull_build / cc_world_get_convex_hull) twice: sizes, then data."""
+    info = HullInfo()
+    check(call(C.byref(info), None, None, None, None, None, None), "convex hull")
+    npt, nf, nv = info.num_points, info.num_faces, info.num_face_vertices
+    pts = np.zeros((npt, 3), np.float32)
+    shr = np.zeros((npt, 3), np.float32)
+    faces = np.zeros((nf, 2), np.int32)
+    vidx = np.zeros(max(nv, 1), np.int32)
+    planes = np.zeros((nf, 4), np.float32)
+    pf = np.zeros((npt, 4), np.int32)
+    check(call(C.byref(info), ptr(pts), ptr(shr), ptr(faces), ptr(vidx), ptr(planes), ptr(pf)), "convex hull")
+    return {"points": pts, "shrunk": shr, "faces": faces, "face_vertices": vidx[:nv], "planes": planes,
+            "point_faces": pf, "convex_radius": info.convex_radius, "volume": info.volume,
+            "inner_radius": info.inner_radius, "com": np.array(info.com[:], np.float32),
+            "inertia": np.array(info.inertia[:], np.float32).reshape(3, 3),
+            "bounds_min": np.array(info.bounds_min[:], np.float32),
+            "bounds_max": np.array(info.bounds_max[:], np.float32)}
+
+
+def build_convex_hull(points, convex_radius: float = -1.0) -> dict:
+    """cc_convex_hull_build: the hull of the points as convexHull.create makes it (host only)."""
+    lib = load()
+    p = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+    return _hull_arrays(lambda info, *a: lib.cc_convex_hull_build(ptr(p), len(p), C.c_float(convex_radius), info, *a))

@@ -123,8 +123,18 @@ __device__ void exact_aabb(float4 p4, float4 q4, const double lo[3], const doubl
 }
 
 // local bounds of the shape in FP64 (box.ts:77-84, sphere.ts, capsule.ts:84-94)
-__device__ __forceinline__ void shape_bounds(uint32_t f, float4 sp, double lo[3], double hi[3]) {
+__device__ __forceinline__ void shape_bounds(const DevWorld &w, uint32_t f, float4 sp, double lo[3], double hi[3]) {
     int s = shape_of(f);
+    if (s == SHAPE_HULL) {  // the hull's local bounds (convex-hull.ts:214-231)
+        const DevHull &h = w.hulls[hull_of(sp)];
+        lo[0] = h.lo.x;
+        lo[1] = h.lo.y;
+        lo[2] = h.lo.z;
+        hi[0] = h.hi.x;
+        hi[1] = h.hi.y;
+        hi[2] = h.hi.z;
+        return;
+    }
     double ex, ey, ez;
     if (s == SHAPE_BOX) {
         ex = sp.x;
@@ -160,7 +170,7 @@ __global__ void k_update_bounds(DevWorld w, unsigned int *scene) {
         uint32_t f = w.flags[i];
         if (motion_of(f) != STATIC && !sleeping_of(f)) awake++;
         double lo[3], hi[3];
-        shape_bounds(f, w.shape[i], lo, hi);
+        shape_bounds(w, f, w.shape[i], lo, hi);
         double b[6];
         exact_aabb(w.pos[i], w.quat[i], lo, hi, b);
         double *o = w.aabb64 + (size_t)i * 6;

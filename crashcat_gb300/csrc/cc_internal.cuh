@@ -7,6 +7,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "../../include/crashcat_gpu.h"
 
@@ -34,7 +35,7 @@ __host__ __device__ inline int layer_of(uint32_t f) { return (int)((f >> F_LAYER
 __host__ __device__ inline bool sleeping_of(uint32_t f) { return (f & F_SLEEPING) != 0; }
 
 constexpr int STATIC = 0, KINEMATIC = 1, DYNAMIC = 2;
-constexpr int SHAPE_SPHERE = 0, SHAPE_BOX = 1, SHAPE_CAPSULE = 2;
+constexpr int SHAPE_SPHERE = 0, SHAPE_BOX = 1, SHAPE_CAPSULE = 2, SHAPE_HULL = 3;
 
 // Per-step overflow flags (status bits in DevCounters::overflow)
 enum : int { OVF_PAIRS = 1, OVF_MANIFOLDS = 2, OVF_EPA = 4, OVF_ISLAND = 8, OVF_CACHE = 16, OVF_SLOTS = 32,
@@ -177,6 +178,16 @@ struct AdjBuffers {
 // point (point-constraint-part.ts), hinge rotation (hinge-rotation-constraint-part.ts), and
 // the limit and motor angle parts (angle-constraint-part.ts, spring-part.ts).
 enum : int { JF_ENABLED = 1, JF_LIMITS = 2 };
+// Convex hull shape (src/shapes/convex-hull.ts): points relative to the centre of mass, the
+// points shrunk by the convex radius, polygon faces and their planes.  A hull body's shape
+// record holds (hull index as int bits, convex radius, 0, 0).
+struct DevHull {
+    int first_point, num_points, first_face, num_faces;
+    float convex_radius, inner_radius, pad0, pad1;
+    float4 com;     // centre of mass in the input frame (xyz)
+    float4 lo, hi;  // bounds of the points (xyz)
+};
+
 // user joints of both types share one id space: hinges 0.., swing-twists JOINT_SWING | index
 constexpr int JOINT_SWING = 1 << 30;
 
@@ -341,6 +352,12 @@ struct DevWorld {
     int max_joints;      // capacity of the per-island joint lists
     int *joint_wake;     // flag: some joint has to wake a body this step
     int *body_local;  // index of a body inside its island's body list (per-warp solve)
+    // convex hull shapes
+    DevHull *hulls;
+    int num_hulls;
+    float4 *hull_points, *hull_shrunk, *hull_planes;  // planes: normal xyz, constant w
+    int2 *hull_faces;                                  // first vertex index, vertex count
+    int *hull_vidx;
     // giant islands (more constraints than giant_min): solved by the whole grid
     int giant_min;
     int giant_blocks;                      // blocks of the cooperative launch (co-resident)
@@ -348,6 +365,22 @@ struct DevWorld {
     unsigned long long *giant_claim;       // 4 x cap: contact claims, two parities | joint claims, two parities
     int *giant_count;  // 4 x (GIANT_COLOURS + 2): contact colour offsets, contact fill cursors, joint offsets, joint fill
 };
+
+__host__ __device__ inline int hull_of(float4 sp) {
+#ifdef __CUDA_ARCH__
+    return __float_as_int(sp.x);
+#else
+    int v;
+    memcpy(&v, &sp.x, sizeof(int));
+    return v;
+#endif
+}
+// the shape's centre of mass in the body frame (zero for every shape but the hull)
+__device__ inline float3 shape_com(const DevWorld &w, uint32_t f, float4 sp) {
+    if (shape_of(f) != SHAPE_HULL) return make_float3(0.f, 0.f, 0.f);
+    float4 c = w.hulls[hull_of(sp)].com;
+    return make_float3(c.x, c.y, c.z);
+}
 
 // ---- user joints of every type under one id ---------------------------------------------
 __device__ __forceinline__ int joint_total(const DevWorld &w) { return w.num_hinges + w.num_swings; }

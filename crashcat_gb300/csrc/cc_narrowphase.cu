@@ -107,10 +107,18 @@ __device__ __forceinline__ Q<S> qmulS(Q<S> a, Q<S> b) {
 // ---------------------------------------------------------------------------
 // support functions
 // ---------------------------------------------------------------------------
-enum { SUP_BOX = 0, SUP_POINT = 1, SUP_SPHERE = 2, SUP_CAPSULE_SEGMENT = 3, SUP_CAPSULE_SURFACE = 4 };
+enum { SUP_BOX = 0, SUP_POINT = 1, SUP_SPHERE = 2, SUP_CAPSULE_SEGMENT = 3, SUP_CAPSULE_SURFACE = 4, SUP_HULL = 5 };
+// the world's convex hull arrays, as the support functions read them
+struct HullView {
+    const DevHull *hulls;
+    const float4 *points, *shrunk;
+};
+__device__ __forceinline__ HullView hull_view(const DevWorld &w) { return HullView{w.hulls, w.hull_points, w.hull_shrunk}; }
 template <typename S>
 struct Sup {
     int kind;
+    const float4 *hp;  // hull support points (original or shrunk) and their count
+    int hn;
     V<S> he;      // box half extents
     S radius;     // sphere surface radius
     S convex_radius;
@@ -119,6 +127,21 @@ struct Sup {
     S add_r;
     __device__ V<S> inner(V<S> d) const {
         if (kind == SUP_BOX) return {d.x >= S(0) ? he.x : -he.x, d.y >= S(0) ? he.y : -he.y, d.z >= S(0) ? he.z : -he.z};
+        if (kind == SUP_HULL) {  // the point with the highest projection (convex-hull.ts:588-614, 695-715)
+            S best = -s_max_value<S>();
+            V<S> bp{S(0), S(0), S(0)};
+            bool any = false;
+            for (int k = 0; k < hn; k++) {
+                float4 p = hp[k];
+                S dd = S(p.x) * d.x + S(p.y) * d.y + S(p.z) * d.z;
+                if (!any || dd > best) {
+                    best = dd;
+                    bp = {S(p.x), S(p.y), S(p.z)};
+                    any = true;
+                }
+            }
+            return bp;
+        }
         if (kind == SUP_POINT) return {S(0), S(0), S(0)};
         // capsule: segment +-h on Y (capsuleNoConvexGetSupport capsule.ts:268-275)
         if (kind == SUP_CAPSULE_SEGMENT) return {S(0), d.y > S(0) ? he.y : -he.y, S(0)};
@@ -152,13 +175,28 @@ struct Sup {
 
 // setBoxSupport support.ts:339-370 / getSphereSupportFunction sphere.ts:256-266
 template <typename S>
-__device__ Sup<S> make_sup(int shape, float4 sp, bool exclude) {
+__device__ Sup<S> make_sup(int shape, float4 sp, bool exclude, const HullView &hv) {
     Sup<S> o;
     o.transformed = false;
     o.add_r = S(0);
     o.radius = S(0);
     o.he = {S(0), S(0), S(0)};
-    if (shape == SHAPE_BOX) {
+    o.hp = nullptr;
+    o.hn = 0;
+    if (shape == SHAPE_HULL && hv.hulls) {
+        // getConvexHullSupportFunction convex-hull.ts:968-997: the shrunk points with the convex
+        // radius when it is excluded (and not zero), else the points themselves
+        const DevHull &h = hv.hulls[hull_of(sp)];
+        o.kind = SUP_HULL;
+        o.hn = h.num_points;
+        if (exclude && h.convex_radius != 0.f) {
+            o.hp = hv.shrunk + h.first_point;
+            o.convex_radius = S(h.convex_radius);
+        } else {
+            o.hp = hv.points + h.first_point;
+            o.convex_radius = S(0);
+        }
+    } else if (shape == SHAPE_BOX) {
         o.kind = SUP_BOX;
         if (exclude) {
             S cr = S(sp.w) < S(0.05) ? S(sp.w) : S(0.05);
@@ -576,7 +614,8 @@ __device__ GjkOut<S> gjk(const Sup<S> &A, const Sup<S> &B, S tolerance, V<S> dir
 // ---------------------------------------------------------------------------
 // faces, clipping, reduction (FP32, coordinates relative to body A)
 // ---------------------------------------------------------------------------
-constexpr int FMAX = 16;
+constexpr int FMAX = 32;        // vertices of a face or clipped polygon kept here
+constexpr int FMAX_FACE = 32;   // MAX_FACE_VERTICES (convex-hull.ts:88): a hull face gives at most half
 struct Face {
     int n;
     float3 v[FMAX];
@@ -644,6 +683,31 @@ __device__ void capsule_face(Face &f, float3 d, float4 sp, float4 q, float3 t) {
         f.n = 2;
         f.v[0] = qrot(q, top) + t;
         f.v[1] = qrot(q, bottom) + t;
+    }
+}
+
+// convex hull getSupportingFace convex-hull.ts:479-541 (unit scale): the face whose plane
+// normal is most opposed to dir, at most 16 of its vertices, rotated by q and moved by t
+__device__ void hull_face(Face &f, float3 dir, const DevWorld &w, float4 sp, float4 q, float3 t) {
+    const DevHull &h = w.hulls[hull_of(sp)];
+    int best = 0;
+    float bd = 0.f;
+    for (int i = 0; i < h.num_faces; i++) {
+        float4 pl = w.hull_planes[h.first_face + i];
+        float3 n = f3(pl.x, pl.y, pl.z);
+        float d = dot3(n, dir) / sqrtf(lensq3(n));
+        if (i == 0 || d < bd) {
+            bd = d;
+            best = i;
+        }
+    }
+    int2 fc = w.hull_faces[h.first_face + best];
+    const int maxv = FMAX_FACE / 2;
+    int step = (fc.y + maxv - 1) / maxv;
+    f.n = 0;
+    for (int i = 0; i < fc.y && f.n < FMAX; i += step) {
+        float4 p = w.hull_points[w.hull_vidx[fc.x + i]];
+        f.v[f.n++] = qrot(q, f3(p.x, p.y, p.z)) + t;
     }
 }
 
@@ -859,6 +923,8 @@ __device__ void emit_manifold(DevWorld &w, int a, int b, float3 pa, float3 pb, f
         float3 axB = qrot_inv(qb, axis);
         if (shape_of(fa) == SHAPE_BOX) box_face(fA, -axA, w.shape[a], qa, f3(0.f, 0.f, 0.f));
         if (shape_of(fa) == SHAPE_CAPSULE) capsule_face(fA, -axA, w.shape[a], qa, f3(0.f, 0.f, 0.f));
+        if (shape_of(fa) == SHAPE_HULL) hull_face(fA, -axA, w, w.shape[a], qa, f3(0.f, 0.f, 0.f));
+        if (shape_of(fb) == SHAPE_HULL) hull_face(fB, axB, w, w.shape[b], qb, posB - posA);
         if (shape_of(fb) == SHAPE_BOX) box_face(fB, axB, w.shape[b], qb, posB - posA);
         if (shape_of(fb) == SHAPE_CAPSULE) capsule_face(fB, axB, w.shape[b], qb, posB - posA);
         haveFaces = fA.n >= 2 && fB.n >= 3;
@@ -937,8 +1003,9 @@ __global__ void __launch_bounds__(128) k_narrowphase(DevWorld w, EpaItem *epa_it
         Q<float> rel = qmulS(iA, qB);
         V<float> ab{pb4.x - pa4.x, pb4.y - pa4.y, pb4.z - pa4.z};
         V<float> posBInA = qrotS(iA, ab);
-        Sup<float> supA = make_sup<float>(sha, sa, true);
-        Sup<float> supB = make_sup<float>(shb, sb, true);
+        const HullView hv = hull_view(w);
+        Sup<float> supA = make_sup<float>(sha, sa, true, hv);
+        Sup<float> supB = make_sup<float>(shb, sb, true, hv);
         set_transform(supB, rel, posBInA);
         V<float> axis = posBInA;
         if (lsq(axis) <= 1e-12f) axis = {1.f, 0.f, 0.f};
@@ -1592,8 +1659,8 @@ __device__ void epa_setup(const DevWorld &w, const EpaItem &it, Sup<R> &A, Sup<R
     Q<R> rel = qmulS(iA, qB);
     V<R> ab{R(pb4.x) - R(pa4.x), R(pb4.y) - R(pa4.y), R(pb4.z) - R(pa4.z)};
     V<R> posBInA = qrotS(iA, ab);
-    A = make_sup<R>(shape_of(fa), w.shape[a], false);
-    B = make_sup<R>(shape_of(fb), w.shape[b], false);
+    A = make_sup<R>(shape_of(fa), w.shape[a], false, hull_view(w));
+    B = make_sup<R>(shape_of(fb), w.shape[b], false, hull_view(w));
     A.add_r = maxSep;
     set_transform(B, rel, posBInA);
 }
@@ -1783,8 +1850,9 @@ __global__ void __launch_bounds__(128) k_static_gjk(const cc_penetration_query *
     Q<float> rel = qmulS(iA, qB);
     V<float> ab{pb4.x - pa4.x, pb4.y - pa4.y, pb4.z - pa4.z};
     V<float> posBInA = qrotS(iA, ab);
-    Sup<float> supA = make_sup<float>(sha, sa, true);
-    Sup<float> supB = make_sup<float>(shb, sb, true);
+    const HullView none{nullptr, nullptr, nullptr};  // the static query takes no hull shapes
+    Sup<float> supA = make_sup<float>(sha, sa, true, none);
+    Sup<float> supB = make_sup<float>(shb, sb, true, none);
     set_transform(supB, rel, posBInA);
     V<float> axis = posBInA;
     if (lsq(axis) <= 1e-12f) axis = {1.f, 0.f, 0.f};
@@ -1849,8 +1917,9 @@ __global__ void __launch_bounds__(64) k_static_epa(const cc_penetration_query *q
         Q<R> rel = qmulS(iA, qB);
         V<R> ab{R(pb4.x) - R(pa4.x), R(pb4.y) - R(pa4.y), R(pb4.z) - R(pa4.z)};
         V<R> posBInA = qrotS(iA, ab);
-        Sup<R> A = make_sup<R>(qy.a.shape_type, sa, false);
-        Sup<R> B = make_sup<R>(qy.b.shape_type, sb, false);
+        const HullView none{nullptr, nullptr, nullptr};
+        Sup<R> A = make_sup<R>(qy.a.shape_type, sa, false, none);
+        Sup<R> B = make_sup<R>(qy.b.shape_type, sb, false, none);
         A.add_r = maxSep;
         set_transform(B, rel, posBInA);
         Hull<BigStore> h;

@@ -303,10 +303,14 @@ __global__ void k_contact_setup(DevWorld w, CacheTables ct, float dt) {
 }
 
 // sleep test points (getSleepTestPoints sleep.ts:22-74)
-__device__ void sleep_points(uint32_t f, float4 sp, float4 q, float3 com, float3 out[3]) {
+__device__ void sleep_points(const DevWorld &w, uint32_t f, float4 sp, float4 q, float3 com, float3 out[3]) {
     int sh = shape_of(f);
     float3 e = sh == SHAPE_BOX ? f3(sp.x, sp.y, sp.z)
                                : (sh == SHAPE_CAPSULE ? f3(sp.x, sp.y + sp.x, sp.x) : f3(sp.x, sp.x, sp.x));
+    if (sh == SHAPE_HULL) {  // half extents of the hull's bounds
+        const DevHull &h = w.hulls[hull_of(sp)];
+        e = f3(0.5f * (h.hi.x - h.lo.x), 0.5f * (h.hi.y - h.lo.y), 0.5f * (h.hi.z - h.lo.z));
+    }
     out[0] = com;
     int lowest = (e.x <= e.y && e.x <= e.z) ? 0 : (e.y <= e.z ? 1 : 2);
     float3 X = f3(1.f, 0.f, 0.f), Y = f3(0.f, 1.f, 0.f), Z = f3(0.f, 0.f, 1.f);
@@ -323,7 +327,7 @@ __device__ void sleep_points(uint32_t f, float4 sp, float4 q, float3 com, float3
 }
 __device__ void reset_sleep(DevWorld &w, int i) {
     float3 p[3];
-    sleep_points(w.flags[i], w.shape[i], w.quat[i], xyz(w.com[i]), p);
+    sleep_points(w, w.flags[i], w.shape[i], w.quat[i], xyz(w.com[i]), p);
     for (int k = 0; k < 3; k++) w.sleep_sph[3 * i + k] = make_float4(p[k].x, p[k].y, p[k].z, 0.f);
     w.sleep_timer[i] = 0.f;
 }
@@ -701,7 +705,8 @@ __device__ void integrate_body(DevWorld &w, int i, float dt) {
 __device__ void finish_body(DevWorld &w, int i) {
     uint32_t f = w.flags[i];
     if (motion_of(f) == STATIC || sleeping_of(f)) return;
-    float3 com = xyz(w.com[i]);  // shape centre of mass is the origin for boxes and spheres
+    // updatePositionFromCenterOfMass rigid-body.ts:545-553: position = com - rotation x shape com
+    float3 com = xyz(w.com[i]) - qrot(w.quat[i], shape_com(w, f, w.shape[i]));
     w.pos[i] = make_float4(com.x, com.y, com.z, 0.f);
     w.force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     w.torque[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -712,7 +717,7 @@ __device__ bool sleep_update(DevWorld &w, int i, float dt) {
     uint32_t f = w.flags[i];
     if (!(f & F_ALLOW_SLEEP) || (f & F_SENSOR)) return false;
     float3 p[3];
-    sleep_points(f, w.shape[i], w.quat[i], xyz(w.com[i]), p);
+    sleep_points(w, f, w.shape[i], w.quat[i], xyz(w.com[i]), p);
     float maxMove = c_settings.sleep_threshold * c_settings.time_before_sleep;
     for (int k = 0; k < 3; k++) {
         float4 s = w.sleep_sph[3 * i + k];

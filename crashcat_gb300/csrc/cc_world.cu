@@ -16,6 +16,7 @@
 
 #include "cc_internal.cuh"
 #include "cc_swing.cuh"
+#include "cc_hull.h"
 
 using namespace cc;
 
@@ -34,6 +35,7 @@ struct cc_world {
     std::vector<uint64_t> ids;
     std::vector<DevHinge> hinges;  // host copy of each joint as created (bodies, flags, limits, motors)
     std::vector<DevSwing> swings;
+    std::vector<cc_hull::Hull> hulls;  // convex hull shapes as built
     float *d_state_rows = nullptr;  // 16 floats per body staging for get/set state
     float *h_pinned_rows = nullptr;
     DevCounters *h_ctr = nullptr;   // pinned mirror of the device counters
@@ -87,6 +89,82 @@ static void drop_graph(cc_world *W) {
         W->graph = nullptr;
     }
 }
+
+// FP64 vector and quaternion helpers of the host-side shape and joint set-up
+namespace {
+struct D3 {
+    double x, y, z;
+};
+struct DQ {
+    double x, y, z, w;
+};
+D3 d3(const float *v) { return {v[0], v[1], v[2]}; }
+D3 d3(float4 v) { return {v.x, v.y, v.z}; }
+D3 dsub(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+D3 dcross(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+D3 dnormalize(D3 a) {  // vec3.normalize: a zero vector stays zero
+    double l = a.x * a.x + a.y * a.y + a.z * a.z;
+    if (l > 0) l = 1.0 / std::sqrt(l);
+    return {a.x * l, a.y * l, a.z * l};
+}
+DQ dq(float4 q) { return {q.x, q.y, q.z, q.w}; }
+DQ dconj(DQ q) { return {-q.x, -q.y, -q.z, q.w}; }
+DQ dqmul(DQ a, DQ b) {
+    return {a.x * b.w + a.w * b.x + a.y * b.z - a.z * b.y, a.y * b.w + a.w * b.y + a.z * b.x - a.x * b.z,
+            a.z * b.w + a.w * b.z + a.x * b.y - a.y * b.x, a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z};
+}
+D3 drot(DQ q, D3 v) {  // q v q^-1 for a unit quaternion
+    D3 u{q.x, q.y, q.z};
+    D3 t = dcross(u, v);
+    t = {2 * t.x, 2 * t.y, 2 * t.z};
+    D3 c = dcross(u, t);
+    return {v.x + q.w * t.x + c.x, v.y + q.w * t.y + c.y, v.z + q.w * t.z + c.z};
+}
+// rotation quaternion of the 3x3 matrix with columns c0 c1 c2 (Shoemake's method, as quat.fromMat3)
+DQ quat_from_columns(D3 c0, D3 c1, D3 c2) {
+    double m[3][3] = {{c0.x, c1.x, c2.x}, {c0.y, c1.y, c2.y}, {c0.z, c1.z, c2.z}};  // m[row][col]
+    double tr = m[0][0] + m[1][1] + m[2][2];
+    DQ o;
+    if (tr > 0.0) {
+        double r = std::sqrt(tr + 1.0);
+        o.w = 0.5 * r;
+        r = 0.5 / r;
+        o.x = (m[2][1] - m[1][2]) * r;
+        o.y = (m[0][2] - m[2][0]) * r;
+        o.z = (m[1][0] - m[0][1]) * r;
+        return o;
+    }
+    int i = 0;
+    if (m[1][1] > m[0][0]) i = 1;
+    if (m[2][2] > m[i][i]) i = 2;
+    int j = (i + 1) % 3, k = (i + 2) % 3;
+    double q[3];
+    double r = std::sqrt(m[i][i] - m[j][j] - m[k][k] + 1.0);
+    q[i] = 0.5 * r;
+    r = 0.5 / r;
+    o.w = (m[k][j] - m[j][k]) * r;
+    q[j] = (m[j][i] + m[i][j]) * r;
+    q[k] = (m[k][i] + m[i][k]) * r;
+    o.x = q[0];
+    o.y = q[1];
+    o.z = q[2];
+    return o;
+}
+// getInvInitialOrientationXZ (hinge-constraint.ts:166-205)
+DQ inv_initial_orientation_xz(D3 n1, D3 h1, D3 n2, D3 h2) {
+    const double eps = 1e-6;
+    if (std::fabs(n1.x - n2.x) < eps && std::fabs(n1.y - n2.y) < eps && std::fabs(n1.z - n2.z) < eps &&
+        std::fabs(h1.x - h2.x) < eps && std::fabs(h1.y - h2.y) < eps && std::fabs(h1.z - h2.z) < eps)
+        return {0, 0, 0, 1};
+    DQ q1 = quat_from_columns(n1, dcross(h1, n1), h1), q2 = quat_from_columns(n2, dcross(h2, n2), h2);
+    return dqmul(q2, dconj(q1));
+}
+float3 f3d(D3 v) { return make_float3((float)v.x, (float)v.y, (float)v.z); }
+bool finite3(const float *v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+bool spring_ok(const cc_spring_settings &s) {
+    return (s.mode == 0 || s.mode == 1) && std::isfinite(s.frequency_or_stiffness) && std::isfinite(s.damping);
+}
+}  // namespace
 
 static int next_pow2(int v) {
     int p = 1;
@@ -400,7 +478,8 @@ int cc_world_destroy(cc_world *W) {
                     w.scratch_colour, w.scratch_claim, w.mid_list, w.body_local, w.contact_event,
                     w.removed_keys, W->d_state_rows, w.hinges, w.island_joints, w.island_joint_count,
                     w.island_joint_off, w.island_fill_j, w.joint_wake, w.joint_partners, w.swings,
-                    w.giant_list, w.giant_claim, w.giant_count};
+                    w.giant_list, w.giant_claim, w.giant_count, w.hulls, w.hull_points, w.hull_shrunk,
+                    w.hull_planes, w.hull_faces, w.hull_vidx};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : W->adj.allocs)
@@ -438,8 +517,17 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
     std::vector<float> timer(n, 0.f);
     for (int i = 0; i < n; i++) {
         const cc_body_desc &d = b[i];
-        if (d.shape_type != CC_SHAPE_BOX && d.shape_type != CC_SHAPE_SPHERE && d.shape_type != CC_SHAPE_CAPSULE)
+        if (d.shape_type != CC_SHAPE_BOX && d.shape_type != CC_SHAPE_SPHERE && d.shape_type != CC_SHAPE_CAPSULE &&
+            d.shape_type != CC_SHAPE_CONVEX_HULL)
             return CC_ERR_UNSUPPORTED;
+        const cc_hull::Hull *hull = nullptr;
+        int hull_index = -1;
+        if (d.shape_type == CC_SHAPE_CONVEX_HULL) {
+            hull_index = (int)d.shape_params[0];
+            if (!(d.shape_params[0] == (float)hull_index) || hull_index < 0 || hull_index >= (int)W->hulls.size())
+                return CC_ERR_INVALID;
+            hull = &W->hulls[hull_index];
+        }
         if (d.shape_type == CC_SHAPE_CAPSULE && !(d.shape_params[0] > 0.f && d.shape_params[1] > 0.f))
             return CC_ERR_INVALID;  // capsule.ts:55-61
         if (d.motion_type < 0 || d.motion_type > 2) return CC_ERR_INVALID;
@@ -447,7 +535,14 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
         if (d.world < 0 || d.world >= w.num_worlds) return CC_ERR_INVALID;
         double mass;
         double idiag[3];
-        if (d.shape_type == CC_SHAPE_BOX) {
+        double irot[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};  // principal axes (columns)
+        if (hull) {
+            // computeMassProperties convex-hull.ts:453-459, principal axes of the inertia
+            mass = hull->volume * d.density;
+            double I[9];
+            for (int k = 0; k < 9; k++) I[k] = hull->inertia[k] * d.density;
+            cc_hull::principal_axes(I, idiag, irot);
+        } else if (d.shape_type == CC_SHAPE_BOX) {
             double fx = 2.0 * d.shape_params[0], fy = 2.0 * d.shape_params[1], fz = 2.0 * d.shape_params[2];
             mass = fx * fy * fz * d.density;
             idiag[0] = (fy * fy + fz * fz) * (mass / 12.0);
@@ -491,13 +586,27 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
         }
         pos[i] = make_float4(d.position[0], d.position[1], d.position[2], 0.f);
         quat[i] = make_float4(d.quaternion[0], d.quaternion[1], d.quaternion[2], d.quaternion[3]);
-        com[i] = pos[i];  // shape centre of mass is the origin for boxes and spheres
+        com[i] = pos[i];  // the shape's centre of mass is its origin, hulls aside
+        if (hull) {  // updateCenterOfMassPosition rigid-body.ts:527-536: position + rotation x com
+            DQ q = dq(quat[i]);
+            D3 c = drot(q, D3{hull->com.x, hull->com.y, hull->com.z});
+            com[i] = make_float4((float)(d.position[0] + c.x), (float)(d.position[1] + c.y), (float)(d.position[2] + c.z),
+                                 0.f);
+        }
         lin[i] = make_float4(d.linear_velocity[0], d.linear_velocity[1], d.linear_velocity[2], 0.f);
         ang[i] = make_float4(d.angular_velocity[0], d.angular_velocity[1], d.angular_velocity[2], 0.f);
         zero[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         ii[i] = make_float4(inv_i.x, inv_i.y, inv_i.z, inv_mass);
         ir[i] = make_float4(0.f, 0.f, 0.f, 1.f);
         sh[i] = make_float4(d.shape_params[0], d.shape_params[1], d.shape_params[2], d.shape_params[3]);
+        if (hull) {
+            DQ r = quat_from_columns(D3{irot[0], irot[3], irot[6]}, D3{irot[1], irot[4], irot[7]},
+                                     D3{irot[2], irot[5], irot[8]});
+            ir[i] = make_float4((float)r.x, (float)r.y, (float)r.z, (float)r.w);
+            float hi_bits;
+            memcpy(&hi_bits, &hull_index, sizeof(float));
+            sh[i] = make_float4(hi_bits, (float)hull->convex_radius, 0.f, 0.f);
+        }
         mat[i] = make_float4(d.friction, d.restitution, d.gravity_factor, 0.f);
         damp[i] = make_float4(d.linear_damping, d.angular_damping, d.max_linear_velocity, d.max_angular_velocity);
         uint32_t f = (uint32_t)d.motion_type;
@@ -511,7 +620,9 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
         groups[i] = make_uint2(d.collision_groups, d.collision_mask);
         world[i] = d.world;
         // resetSleepTimer sleep.ts:123-130
-        float3 e = d.shape_type == CC_SHAPE_BOX
+        float3 e = hull ? f3((float)(0.5 * (hull->hi.x - hull->lo.x)), (float)(0.5 * (hull->hi.y - hull->lo.y)),
+                             (float)(0.5 * (hull->hi.z - hull->lo.z)))
+                   : d.shape_type == CC_SHAPE_BOX
                        ? f3(d.shape_params[0], d.shape_params[1], d.shape_params[2])
                        : (d.shape_type == CC_SHAPE_CAPSULE
                               ? f3(d.shape_params[0], d.shape_params[1] + d.shape_params[0], d.shape_params[0])
@@ -666,7 +777,8 @@ __global__ void k_unpack_state(DevWorld w, const float *rows) {
         w.quat[i] = make_float4(o[3], o[4], o[5], o[6]);
         w.linvel[i] = make_float4(o[7], o[8], o[9], 0.f);
         w.angvel[i] = make_float4(o[10], o[11], o[12], 0.f);
-        w.com[i] = make_float4(o[0], o[1], o[2], 0.f);
+        float3 c = qrot(w.quat[i], shape_com(w, w.flags[i], w.shape[i]));
+        w.com[i] = make_float4(o[0] + c.x, o[1] + c.y, o[2] + c.z, 0.f);
     }
 }
 
@@ -1084,80 +1196,6 @@ extern "C" int cc_world_rollout_grad(cc_world *W, float dt, int32_t n_steps, int
 // hinge joints: creation in FP64 from the bodies' current poses
 // (hingeConstraint.create hinge-constraint.ts:240-387) and the setters
 // ---------------------------------------------------------------------------
-namespace {
-struct D3 {
-    double x, y, z;
-};
-struct DQ {
-    double x, y, z, w;
-};
-D3 d3(const float *v) { return {v[0], v[1], v[2]}; }
-D3 d3(float4 v) { return {v.x, v.y, v.z}; }
-D3 dsub(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-D3 dcross(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
-D3 dnormalize(D3 a) {  // vec3.normalize: a zero vector stays zero
-    double l = a.x * a.x + a.y * a.y + a.z * a.z;
-    if (l > 0) l = 1.0 / std::sqrt(l);
-    return {a.x * l, a.y * l, a.z * l};
-}
-DQ dq(float4 q) { return {q.x, q.y, q.z, q.w}; }
-DQ dconj(DQ q) { return {-q.x, -q.y, -q.z, q.w}; }
-DQ dqmul(DQ a, DQ b) {
-    return {a.x * b.w + a.w * b.x + a.y * b.z - a.z * b.y, a.y * b.w + a.w * b.y + a.z * b.x - a.x * b.z,
-            a.z * b.w + a.w * b.z + a.x * b.y - a.y * b.x, a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z};
-}
-D3 drot(DQ q, D3 v) {  // q v q^-1 for a unit quaternion
-    D3 u{q.x, q.y, q.z};
-    D3 t = dcross(u, v);
-    t = {2 * t.x, 2 * t.y, 2 * t.z};
-    D3 c = dcross(u, t);
-    return {v.x + q.w * t.x + c.x, v.y + q.w * t.y + c.y, v.z + q.w * t.z + c.z};
-}
-// rotation quaternion of the 3x3 matrix with columns c0 c1 c2 (Shoemake's method, as quat.fromMat3)
-DQ quat_from_columns(D3 c0, D3 c1, D3 c2) {
-    double m[3][3] = {{c0.x, c1.x, c2.x}, {c0.y, c1.y, c2.y}, {c0.z, c1.z, c2.z}};  // m[row][col]
-    double tr = m[0][0] + m[1][1] + m[2][2];
-    DQ o;
-    if (tr > 0.0) {
-        double r = std::sqrt(tr + 1.0);
-        o.w = 0.5 * r;
-        r = 0.5 / r;
-        o.x = (m[2][1] - m[1][2]) * r;
-        o.y = (m[0][2] - m[2][0]) * r;
-        o.z = (m[1][0] - m[0][1]) * r;
-        return o;
-    }
-    int i = 0;
-    if (m[1][1] > m[0][0]) i = 1;
-    if (m[2][2] > m[i][i]) i = 2;
-    int j = (i + 1) % 3, k = (i + 2) % 3;
-    double q[3];
-    double r = std::sqrt(m[i][i] - m[j][j] - m[k][k] + 1.0);
-    q[i] = 0.5 * r;
-    r = 0.5 / r;
-    o.w = (m[k][j] - m[j][k]) * r;
-    q[j] = (m[j][i] + m[i][j]) * r;
-    q[k] = (m[k][i] + m[i][k]) * r;
-    o.x = q[0];
-    o.y = q[1];
-    o.z = q[2];
-    return o;
-}
-// getInvInitialOrientationXZ (hinge-constraint.ts:166-205)
-DQ inv_initial_orientation_xz(D3 n1, D3 h1, D3 n2, D3 h2) {
-    const double eps = 1e-6;
-    if (std::fabs(n1.x - n2.x) < eps && std::fabs(n1.y - n2.y) < eps && std::fabs(n1.z - n2.z) < eps &&
-        std::fabs(h1.x - h2.x) < eps && std::fabs(h1.y - h2.y) < eps && std::fabs(h1.z - h2.z) < eps)
-        return {0, 0, 0, 1};
-    DQ q1 = quat_from_columns(n1, dcross(h1, n1), h1), q2 = quat_from_columns(n2, dcross(h2, n2), h2);
-    return dqmul(q2, dconj(q1));
-}
-float3 f3d(D3 v) { return make_float3((float)v.x, (float)v.y, (float)v.z); }
-bool finite3(const float *v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
-bool spring_ok(const cc_spring_settings &s) {
-    return (s.mode == 0 || s.mode == 1) && std::isfinite(s.frequency_or_stiffness) && std::isfinite(s.damping);
-}
-}  // namespace
 
 // grow the joint arrays of one type and the per-island joint lists (created on first use)
 template <typename T>
@@ -1580,3 +1618,169 @@ int cc_world_set_skip_joint_pairs(cc_world *W, int32_t on) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// convex hull shapes (convexHull.create convex-hull.ts:106-446)
+// ---------------------------------------------------------------------------
+// every hull's arrays, concatenated and uploaded again whenever a hull is added
+static int upload_hulls(cc_world *W) {
+    DevWorld &w = W->w;
+    std::vector<DevHull> hdr;
+    std::vector<float4> pts, shr, pln;
+    std::vector<int2> faces;
+    std::vector<int> vidx;
+    for (const cc_hull::Hull &h : W->hulls) {
+        DevHull d;
+        memset(&d, 0, sizeof(d));
+        d.first_point = (int)pts.size();
+        d.num_points = (int)h.points.size();
+        d.first_face = (int)faces.size();
+        d.num_faces = (int)h.face_first.size();
+        d.convex_radius = (float)h.convex_radius;
+        d.inner_radius = (float)h.inner_radius;
+        d.com = make_float4((float)h.com.x, (float)h.com.y, (float)h.com.z, 0.f);
+        d.lo = make_float4((float)h.lo.x, (float)h.lo.y, (float)h.lo.z, 0.f);
+        d.hi = make_float4((float)h.hi.x, (float)h.hi.y, (float)h.hi.z, 0.f);
+        int vbase = (int)vidx.size();
+        for (size_t k = 0; k < h.points.size(); k++) {
+            pts.push_back(make_float4((float)h.points[k].x, (float)h.points[k].y, (float)h.points[k].z, 0.f));
+            shr.push_back(make_float4((float)h.shrunk[k].x, (float)h.shrunk[k].y, (float)h.shrunk[k].z, 0.f));
+        }
+        for (size_t f = 0; f < h.face_first.size(); f++) {
+            faces.push_back(make_int2(vbase + h.face_first[f], h.face_count[f]));
+            pln.push_back(make_float4((float)h.plane_n[f].x, (float)h.plane_n[f].y, (float)h.plane_n[f].z,
+                                      (float)h.plane_c[f]));
+        }
+        for (int v : h.vidx) vidx.push_back(d.first_point + v);
+        hdr.push_back(d);
+    }
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    void *old[] = {w.hulls, w.hull_points, w.hull_shrunk, w.hull_planes, w.hull_faces, w.hull_vidx};
+    for (void *p : old)
+        if (p) cudaFree(p);
+    w.hulls = nullptr;
+    w.hull_points = w.hull_shrunk = w.hull_planes = nullptr;
+    w.hull_faces = nullptr;
+    w.hull_vidx = nullptr;
+    int r;
+    if ((r = dalloc(&w.hulls, hdr.size())) != CC_OK || (r = dalloc(&w.hull_points, pts.size())) != CC_OK ||
+        (r = dalloc(&w.hull_shrunk, shr.size())) != CC_OK || (r = dalloc(&w.hull_planes, pln.size())) != CC_OK ||
+        (r = dalloc(&w.hull_faces, faces.size())) != CC_OK || (r = dalloc(&w.hull_vidx, vidx.size())) != CC_OK)
+        return r;
+    CC_TRY(cudaMemcpy(w.hulls, hdr.data(), sizeof(DevHull) * hdr.size(), cudaMemcpyHostToDevice));
+    CC_TRY(cudaMemcpy(w.hull_points, pts.data(), sizeof(float4) * pts.size(), cudaMemcpyHostToDevice));
+    CC_TRY(cudaMemcpy(w.hull_shrunk, shr.data(), sizeof(float4) * shr.size(), cudaMemcpyHostToDevice));
+    CC_TRY(cudaMemcpy(w.hull_planes, pln.data(), sizeof(float4) * pln.size(), cudaMemcpyHostToDevice));
+    CC_TRY(cudaMemcpy(w.hull_faces, faces.data(), sizeof(int2) * faces.size(), cudaMemcpyHostToDevice));
+    CC_TRY(cudaMemcpy(w.hull_vidx, vidx.data(), sizeof(int) * vidx.size(), cudaMemcpyHostToDevice));
+    w.num_hulls = (int)hdr.size();
+    drop_graph(W);
+    return CC_OK;
+}
+
+extern "C" {
+
+}  // extern "C"
+static int build_hull_from(const float *points, int32_t n, float convex_radius, cc_hull::Hull &h);
+extern "C" {
+
+int cc_world_add_convex_hull(cc_world *W, const float *points, int32_t n, float convex_radius, int32_t *out_hull) {
+    if (!W) return CC_ERR_INVALID;
+    cc_hull::Hull h;
+    int r = build_hull_from(points, n, convex_radius, h);
+    if (r != CC_OK) return r;
+    W->hulls.push_back(h);
+    if ((r = upload_hulls(W)) != CC_OK) {
+        W->hulls.pop_back();
+        return r;
+    }
+    if (out_hull) *out_hull = (int32_t)W->hulls.size() - 1;
+    return CC_OK;
+}
+
+}  // extern "C"
+
+static int build_hull_from(const float *points, int32_t n, float convex_radius, cc_hull::Hull &h) {
+    if (!points || n < 4 || n > 65536 || std::isnan(convex_radius)) return CC_ERR_INVALID;
+    std::vector<cc_hull::V> in((size_t)n);
+    for (int i = 0; i < n; i++) {
+        if (!finite3(points + 3 * i)) return CC_ERR_INVALID;
+        in[i] = {points[3 * i], points[3 * i + 1], points[3 * i + 2]};
+    }
+    double radius = convex_radius < 0.f ? 0.05 : (double)convex_radius;  // DEFAULT_CONVEX_RADIUS support.ts:5
+    // hullTolerance 1e-3, maxErrorConvexRadius 0.05, MAX_POINTS_IN_HULL 256 (convex-hull.ts:87, 107, 368)
+    return cc_hull::build(in, radius, 1e-3, 0.05, 256, h) == 0 ? CC_OK : CC_ERR_INVALID;
+}
+
+static int export_hull(const cc_hull::Hull &h, cc_hull_info *info, float *points, float *shrunk, int32_t *faces,
+                       int32_t *face_vertices, float *planes, int32_t *point_faces);
+
+extern "C" {
+
+int cc_convex_hull_build(const float *in_points, int32_t n, float convex_radius, cc_hull_info *info, float *points,
+                         float *shrunk, int32_t *faces, int32_t *face_vertices, float *planes,
+                         int32_t *point_faces) {
+    if (!info) return CC_ERR_INVALID;
+    cc_hull::Hull h;
+    int r = build_hull_from(in_points, n, convex_radius, h);
+    if (r != CC_OK) return r;
+    return export_hull(h, info, points, shrunk, faces, face_vertices, planes, point_faces);
+}
+
+int cc_world_get_convex_hull(cc_world *W, int32_t hull, cc_hull_info *info, float *points, float *shrunk,
+                             int32_t *faces, int32_t *face_vertices, float *planes, int32_t *point_faces) {
+    if (!W || !info || hull < 0 || hull >= (int)W->hulls.size()) return CC_ERR_INVALID;
+    return export_hull(W->hulls[hull], info, points, shrunk, faces, face_vertices, planes, point_faces);
+}
+
+}  // extern "C"
+
+static int export_hull(const cc_hull::Hull &h, cc_hull_info *info, float *points, float *shrunk, int32_t *faces,
+                       int32_t *face_vertices, float *planes, int32_t *point_faces) {
+    memset(info, 0, sizeof(*info));
+    info->num_points = (int32_t)h.points.size();
+    info->num_faces = (int32_t)h.face_first.size();
+    info->num_face_vertices = (int32_t)h.vidx.size();
+    info->convex_radius = (float)h.convex_radius;
+    info->volume = (float)h.volume;
+    info->inner_radius = (float)h.inner_radius;
+    info->com[0] = (float)h.com.x;
+    info->com[1] = (float)h.com.y;
+    info->com[2] = (float)h.com.z;
+    for (int k = 0; k < 9; k++) info->inertia[k] = (float)h.inertia[k];
+    info->bounds_min[0] = (float)h.lo.x;
+    info->bounds_min[1] = (float)h.lo.y;
+    info->bounds_min[2] = (float)h.lo.z;
+    info->bounds_max[0] = (float)h.hi.x;
+    info->bounds_max[1] = (float)h.hi.y;
+    info->bounds_max[2] = (float)h.hi.z;
+    for (size_t k = 0; k < h.points.size(); k++) {
+        if (points) {
+            points[3 * k] = (float)h.points[k].x;
+            points[3 * k + 1] = (float)h.points[k].y;
+            points[3 * k + 2] = (float)h.points[k].z;
+        }
+        if (shrunk) {
+            shrunk[3 * k] = (float)h.shrunk[k].x;
+            shrunk[3 * k + 1] = (float)h.shrunk[k].y;
+            shrunk[3 * k + 2] = (float)h.shrunk[k].z;
+        }
+        if (point_faces)
+            for (int m = 0; m < 4; m++) point_faces[4 * k + m] = h.point_faces[k][m];
+    }
+    for (size_t f = 0; f < h.face_first.size(); f++) {
+        if (faces) {
+            faces[2 * f] = h.face_first[f];
+            faces[2 * f + 1] = h.face_count[f];
+        }
+        if (planes) {
+            planes[4 * f] = (float)h.plane_n[f].x;
+            planes[4 * f + 1] = (float)h.plane_n[f].y;
+            planes[4 * f + 2] = (float)h.plane_n[f].z;
+            planes[4 * f + 3] = (float)h.plane_c[f];
+        }
+    }
+    if (face_vertices)
+        for (size_t k = 0; k < h.vidx.size(); k++) face_vertices[k] = h.vidx[k];
+    return CC_OK;
+}

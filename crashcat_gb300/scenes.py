@@ -15,7 +15,7 @@ import numpy as np
 from typing import Optional
 
 from ._lib import (BODY_DTYPE, COMBINE_GEOMETRIC_MEAN, COMBINE_MAX, DYNAMIC, MOTOR_OFF, MOTOR_POSITION,
-                   MOTOR_VELOCITY, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_SPHERE, STATIC, SWING_CONE, SWING_PYRAMID,
+                   MOTOR_VELOCITY, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_CONVEX_HULL, SHAPE_SPHERE, STATIC, SWING_CONE, SWING_PYRAMID,
                    hinge_defaults, swing_twist_defaults)
 
 # object layers of the reference's test helper (tst/helpers.ts:5-26)
@@ -44,6 +44,7 @@ class Scene:
     seed: int = 0
     hinges: Optional[np.ndarray] = None  # cc_hinge_desc records (_lib.HINGE_DTYPE)
     swings: Optional[np.ndarray] = None  # cc_swing_twist_desc records (_lib.SWING_TWIST_DTYPE)
+    hull_points: Optional[list] = None  # point sets of the convex hulls, in hull index order
     skip_joint_pairs: bool = False
     gravity: tuple = (0.0, -9.81, 0.0)
 
@@ -93,6 +94,21 @@ def set_capsule(b: np.ndarray, idx, radius, half_height) -> None:
     b["shape_params"][idx, 0] = radius
     b["shape_params"][idx, 1] = half_height
     b["shape_params"][idx, 2:] = 0.0
+
+
+def set_hull(b: np.ndarray, idx, hull_index: int) -> None:
+    """A convex hull body: the hull index from GpuWorld.add_convex_hull in shape_params[0]."""
+    b["shape_type"][idx] = SHAPE_CONVEX_HULL
+    b["shape_params"][idx, 0] = float(hull_index)
+    b["shape_params"][idx, 1:] = 0.0
+
+
+def ellipsoid_hull_points(rng: np.random.Generator, k: int, axes) -> np.ndarray:
+    """k points drawn uniformly on the surface of an ellipsoid with the given semi-axes (the
+    mixed convex pile's hulls: 16-32 points, axes 0.3-0.8 m)."""
+    d = rng.normal(size=(k, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return (d * np.asarray(axes)).astype(np.float32)
 
 
 def static_floor(b: np.ndarray, idx: int, half=(50.0, 0.5, 50.0), y=-0.5, friction=0.5, world=0) -> None:
@@ -661,3 +677,45 @@ def swing_twist_chains(seed: int = 91) -> Scene:
             k += 1
     b["allow_sleeping"][:] = 0
     return Scene("swing_twist_chains", b, dt=1.0 / 60.0, steps=90, seed=seed, swings=sj, skip_joint_pairs=True)
+
+
+def mixed_convex_pile(n: int = 400, seed: int = 2, extent: float = 12.0, heights=(1.0, 8.0), floor: bool = True,
+                      speeds=(0.0, 0.0), fast_fraction: float = 0.0) -> Scene:
+    """The mixed convex pile's bodies: shape type uniform over spheres (r 0.2-0.6 m), boxes
+    (half extents 0.2-0.8 m), capsules (r 0.2-0.4 m, half height 0.3-0.8 m) and convex hulls of
+    16-32 points on an ellipsoid (semi-axes 0.3-0.8 m), dropped from the given heights over an
+    area of extent x extent m onto a static box floor (the terrain mesh of the full workload is
+    not part of this scene), at seeded random orientations; fast_fraction of the bodies get
+    speeds drawn from `speeds` in a random direction."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nb = n + (1 if floor else 0)
+    b = blank_bodies(nb)
+    k0 = 0
+    if floor:
+        static_floor(b, 0, half=(extent, 0.5, extent), friction=0.5)
+        k0 = 1
+    idx = np.arange(k0, nb)
+    kinds = rng.integers(0, 4, size=n)
+    hulls = []
+    for j, i in enumerate(idx):
+        if kinds[j] == 0:
+            set_sphere(b, i, rng.uniform(0.2, 0.6))
+        elif kinds[j] == 1:
+            set_box(b, i, rng.uniform(0.2, 0.8, size=3))
+        elif kinds[j] == 2:
+            set_capsule(b, i, rng.uniform(0.2, 0.4), rng.uniform(0.3, 0.8))
+        else:
+            k = int(rng.integers(16, 33))
+            hulls.append(ellipsoid_hull_points(rng, k, rng.uniform(0.3, 0.8, size=3)))
+            set_hull(b, i, len(hulls) - 1)
+    b["position"][idx] = np.stack([rng.uniform(-extent * 0.8, extent * 0.8, n), rng.uniform(*heights, n),
+                                   rng.uniform(-extent * 0.8, extent * 0.8, n)], 1).astype(np.float32)
+    b["quaternion"][idx] = random_quaternions(rng, n)
+    fast = rng.random(n) < fast_fraction
+    if fast.any():
+        d = rng.normal(size=(int(fast.sum()), 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        b["linear_velocity"][idx[fast]] = (d * rng.uniform(*speeds, size=(len(d), 1))).astype(np.float32)
+    b["friction"][idx] = 0.5
+    return Scene("mixed_convex_pile", b, dt=1.0 / 60.0, steps=300, velocity_iterations=8, position_iterations=2,
+                 seed=seed, hull_points=hulls)

@@ -340,6 +340,21 @@ class GpuWorld:
             check(st, "cc_world_get_contact_events")
         return out[: cnt.value]
 
+    # ---- convex hull shapes (convex-hull.ts) ----
+    def add_convex_hull(self, points, convex_radius: float = -1.0) -> int:
+        """cc_world_add_convex_hull: the hull index bodies name in shape_params[0]
+        (convex_radius < 0: the default 0.05)."""
+        p = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+        out = C.c_int32(-1)
+        check(self._lib.cc_world_add_convex_hull(self.handle, ptr(p), len(p), C.c_float(convex_radius),
+                                                 C.byref(out)), "cc_world_add_convex_hull")
+        return out.value
+
+    def get_convex_hull(self, index: int) -> dict:
+        """cc_world_get_convex_hull: the built hull's arrays (the oracle takes them as its shape data)."""
+        return _lib._hull_arrays(
+            lambda info, *a: self._lib.cc_world_get_convex_hull(self.handle, index, info, *a))
+
     # ---- hinge joints (hinge-constraint.ts) ----
     def add_hinges(self, hinges: np.ndarray) -> np.ndarray:
         """cc_world_add_hinges: records of _lib.HINGE_DTYPE; returns the joint indices."""

@@ -27,6 +27,9 @@
  *                                 addContactConstraint        src/constraints/contact-constraints.ts:437
  *   cc_world_get_contact_events <- Listener.onContactAdded / onContactPersisted /
  *                                 onContactRemoved, as a post-step buffer  src/listener.ts:58-98
+ *   cc_world_add_convex_hull   <- convexHull.create          src/shapes/convex-hull.ts:106-446
+ *   cc_world_get_convex_hull   <- reading the ConvexHullShape fields  src/shapes/convex-hull.ts:38-62
+ *   cc_convex_hull_build       <- convexHull.create without a world   src/shapes/convex-hull.ts:106-446
  *   cc_world_add_hinges        <- hingeConstraint.create     src/constraints/hinge-constraint.ts:240-387
  *   cc_world_set_hinge_*       <- hingeConstraint setters    src/constraints/hinge-constraint.ts:429-465
  *   cc_world_get_hinge_angles  <- hingeConstraint.getCurrentAngle  src/constraints/hinge-constraint.ts:467-474
@@ -56,7 +59,7 @@ enum cc_status {
     CC_ERR_UNSUPPORTED = 6
 };
 
-enum cc_shape_type { CC_SHAPE_SPHERE = 0, CC_SHAPE_BOX = 1, CC_SHAPE_CAPSULE = 2 };
+enum cc_shape_type { CC_SHAPE_SPHERE = 0, CC_SHAPE_BOX = 1, CC_SHAPE_CAPSULE = 2, CC_SHAPE_CONVEX_HULL = 3 };
 enum cc_motion_type { CC_STATIC = 0, CC_KINEMATIC = 1, CC_DYNAMIC = 2 };
 enum cc_combine_mode { CC_COMBINE_AVERAGE = 0, CC_COMBINE_MULTIPLY = 1, CC_COMBINE_MIN = 2, CC_COMBINE_MAX = 3,
                        CC_COMBINE_GEOMETRIC_MEAN = 4 };
@@ -103,7 +106,8 @@ typedef struct cc_world_settings {
 
 /* RigidBodySettings (src/body/rigid-body.ts:37-139) for the supported shapes.
  * shape_params: box = half extents xyz + convex radius; sphere = radius;
- * capsule = radius, half height of the cylinder (along local Y, src/shapes/capsule.ts). */
+ * capsule = radius, half height of the cylinder (along local Y, src/shapes/capsule.ts);
+ * convex hull = the hull index from cc_world_add_convex_hull (shape_params[0], a whole number). */
 typedef struct cc_body_desc {
     int32_t shape_type;
     float shape_params[4];
@@ -188,6 +192,40 @@ int cc_world_get_stats(cc_world *world, cc_stats *out);
  * body B (body indices, A < B), sorted by (type, A, B).  *count is the number of events
  * (more than capacity when out is too small). */
 int cc_world_get_contact_events(cc_world *world, int32_t *out, int32_t capacity, int32_t *count);
+
+/* ---------------------------------------------------------------------------
+ * Convex hull shapes (src/shapes/convex-hull.ts).  convexHull.create
+ * (convex-hull.ts:106-446): the hull of the points (hull tolerance 1e-3), its
+ * centre of mass, volume and unit-density inertia, the points relative to the
+ * centre of mass, the convex radius (convex_radius < 0 selects the default
+ * 0.05) reduced for thin hulls and sharp vertices.  At most 256 hull vertices;
+ * flat or degenerate input returns CC_ERR_INVALID.  Bodies name the hull in
+ * cc_body_desc.shape_params[0] with shape_type CC_SHAPE_CONVEX_HULL; a body's
+ * position is the frame of the input points, its centre of mass position +
+ * rotation x com.
+ * ------------------------------------------------------------------------- */
+typedef struct cc_hull_info {
+    int32_t num_points, num_faces, num_face_vertices;
+    float convex_radius, volume, inner_radius;
+    float com[3];           /* centre of mass in the input frame */
+    float inertia[9];       /* about the centre of mass at unit density, row-major */
+    float bounds_min[3], bounds_max[3];  /* of the points, relative to the centre of mass */
+} cc_hull_info;
+
+int cc_world_add_convex_hull(cc_world *world, const float *points, int32_t n, float convex_radius,
+                             int32_t *out_hull);
+/* The same construction without a world (host only, no device needed): fills info and, where
+ * not NULL, the arrays of cc_world_get_convex_hull below (call once with NULL arrays to size
+ * them). */
+int cc_convex_hull_build(const float *in_points, int32_t n, float convex_radius, cc_hull_info *info, float *points,
+                         float *shrunk, int32_t *faces, int32_t *face_vertices, float *planes, int32_t *point_faces);
+/* Read back a built hull: info always; then, where not NULL, points and shrunk points
+ * (num_points x 3 floats, relative to the centre of mass; shrunk = moved inwards by the convex
+ * radius, the support points of the GJK pass), faces (num_faces x 2: first face vertex, count),
+ * face_vertices (num_face_vertices point indices), planes (num_faces x 4: normal, constant),
+ * point_faces (num_points x 4: count, then up to 3 face indices). */
+int cc_world_get_convex_hull(cc_world *world, int32_t hull, cc_hull_info *info, float *points, float *shrunk,
+                             int32_t *faces, int32_t *face_vertices, float *planes, int32_t *point_faces);
 
 /* ---------------------------------------------------------------------------
  * Hinge joints (src/constraints/hinge-constraint.ts).  HingeConstraintSettings

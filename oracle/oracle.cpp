@@ -21,6 +21,7 @@
 #include <cstring>
 #include <array>
 #include <map>
+#include <memory>
 #include <numeric>
 #include <set>
 #include <tuple>
@@ -150,6 +151,7 @@ struct World {
     std::vector<std::array<int64_t, 3>> events;
     std::vector<HingeJoint> joints;
     std::vector<SwingTwistJoint> swings;
+    std::vector<std::unique_ptr<HullData>> hulls;  // convex hull shapes the bodies refer to
     // skip broadphase pairs of bodies that share an enabled joint: the declarative form of the
     // ragdoll example's onBodyPairValidate (examples/src/example-ragdoll.ts:487-489)
     bool skipJointPairs = false;
@@ -183,6 +185,11 @@ static void shape_mass(const Shape &s, double &mass, V3 &inertiaDiag) {
         mass = (4.0 / 3.0) * M_PI * s.radius * r2 * s.density;
         double in = (2.0 / 5.0) * mass * r2;
         inertiaDiag = {in, in, in};
+    } else if (s.type == SHAPE_CONVEX_HULL) {
+        // computeMassProperties convex-hull.ts:453-459: the inertia tensor goes through
+        // set_mass_properties_tensor
+        mass = s.hull->volume * s.density;
+        inertiaDiag = {0, 0, 0};
     } else if (s.type == SHAPE_CAPSULE) {
         // computeMassProperties capsule.ts:119-157 (cylinder plus two hemispheres)
         double r = s.radius, h = s.half_height;
@@ -223,6 +230,55 @@ static void set_mass_properties(Body &b, double mass, V3 d) {
             b.invInertiaDiag = {si, si, si};
             b.inertiaRot = {0, 0, 0, 1};
         }
+    }
+}
+
+inline Q4 quat_from_m3(const M3 &m);  // quat.fromMat3, oracle_joints.h
+
+// setMassProperties for a full inertia tensor (motion-properties.ts:419-491): the principal
+// moments and axes by cyclic Jacobi rotations (decomposePrincipalMomentsOfInertia
+// mass-properties.ts:181-300 diagonalises the same symmetric matrix); the world inverse inertia
+// R diag(1/d) R^T does not depend on the order or signs the decomposition picks.
+static void set_mass_properties_tensor(Body &b, double mass, const double *unit_inertia, double density) {
+    double a[3][3], v[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) a[r][c] = unit_inertia[3 * r + c] * density;
+    for (int sweep = 0; sweep < 50; sweep++) {
+        if (std::fabs(a[0][1]) + std::fabs(a[0][2]) + std::fabs(a[1][2]) < 1e-300) break;
+        for (int p = 0; p < 2; p++)
+            for (int q = p + 1; q < 3; q++) {
+                if (a[p][q] == 0) continue;
+                double th = (a[q][q] - a[p][p]) / (2 * a[p][q]);
+                double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1));
+                double c = 1 / std::sqrt(t * t + 1), sn = t * c;
+                for (int k = 0; k < 3; k++) {
+                    double x = a[k][p], y = a[k][q];
+                    a[k][p] = c * x - sn * y;
+                    a[k][q] = sn * x + c * y;
+                }
+                for (int k = 0; k < 3; k++) {
+                    double x = a[p][k], y = a[q][k];
+                    a[p][k] = c * x - sn * y;
+                    a[q][k] = sn * x + c * y;
+                }
+                for (int k = 0; k < 3; k++) {
+                    double x = v[k][p], y = v[k][q];
+                    v[k][p] = c * x - sn * y;
+                    v[k][q] = sn * x + c * y;
+                }
+            }
+    }
+    double det = v[0][0] * (v[1][1] * v[2][2] - v[1][2] * v[2][1]) - v[0][1] * (v[1][0] * v[2][2] - v[1][2] * v[2][0]) +
+                 v[0][2] * (v[1][0] * v[2][1] - v[1][1] * v[2][0]);
+    if (det < 0)
+        for (int k = 0; k < 3; k++) v[k][2] = -v[k][2];
+    set_mass_properties(b, mass, V3{a[0][0], a[1][1], a[2][2]});
+    int rot = (b.dof >> 3) & 0b111;
+    if (rot != 0) {
+        M3 m;  // columns = principal axes
+        for (int c = 0; c < 3; c++)
+            for (int r = 0; r < 3; r++) m.m[c][r] = v[r][c];
+        b.inertiaRot = quat_from_m3(m);
     }
 }
 
@@ -1442,11 +1498,18 @@ void orc_world_destroy(void *wp) { delete (World *)wp; }
 
 // rigidBody.create rigid-body.ts:390-434 for each row
 // Shape fields of a body row (F_SHAPE, F_DENSITY, F_P0..F_P0 + 3); false for an unknown type.
-static bool shape_from_row(Shape &s, const double *r) {
+static bool shape_from_row(Shape &s, const double *r, const World *w = nullptr) {
     s.type = (int)r[F_SHAPE];
     s.density = r[F_DENSITY];
     s.com = {0, 0, 0};
-    if (s.type == SHAPE_BOX) {
+    if (s.type == SHAPE_CONVEX_HULL) {  // F_P0: the hull index
+        int h = (int)r[F_P0];
+        if (!w || h < 0 || h >= (int)w->hulls.size()) return false;
+        s.hull = w->hulls[h].get();
+        s.com = s.hull->com;
+        s.aabb = s.hull->bounds;
+        s.convex_radius = s.hull->convex_radius;
+    } else if (s.type == SHAPE_BOX) {
         s.half_extents = {r[F_P0], r[F_P0 + 1], r[F_P0 + 2]};
         s.convex_radius = r[F_P0 + 3];
         s.aabb = {neg(s.half_extents), s.half_extents};
@@ -1475,7 +1538,7 @@ int orc_add_bodies(void *wp, const double *rows, int n) {
         w.nextSequence = (w.nextSequence + 1) & ((1 << 20) - 1);
         b.id = (int64_t)b.index + (int64_t)seq * 4294967296LL;
         Shape &s = b.shape;
-        if (!shape_from_row(s, r)) return -1;
+        if (!shape_from_row(s, r, &w)) return -1;
         b.position = {r[F_POS], r[F_POS + 1], r[F_POS + 2]};
         b.quat = {r[F_QUAT], r[F_QUAT + 1], r[F_QUAT + 2], r[F_QUAT + 3]};
         b.motion = (int)r[F_MOTION];
@@ -1493,7 +1556,12 @@ int orc_add_bodies(void *wp, const double *rows, int n) {
         double mass;
         V3 idiag;
         shape_mass(s, mass, idiag);
-        if (b.motion != STATIC) set_mass_properties(b, mass, idiag);
+        if (b.motion != STATIC) {
+            if (s.type == SHAPE_CONVEX_HULL)
+                set_mass_properties_tensor(b, mass, s.hull->inertia, s.density);
+            else
+                set_mass_properties(b, mass, idiag);
+        }
         update_com(b);
         update_aabb(b);
         w.bodies.push_back(b);
@@ -1569,6 +1637,35 @@ int orc_add_hinge(void *wp, const double *d) {
     return j.index;
 }
 void orc_set_skip_joint_pairs(void *wp, int on) { ((World *)wp)->skipJointPairs = on != 0; }
+
+// A convex hull shape given by its data (the hull construction itself is not part of the
+// step): np points and shrunk points (3 doubles each, relative to the centre of mass), nf faces
+// (first face vertex, count), nv face vertex indices, planes (nf x 4: normal, constant),
+// scal = convex radius, volume, com xyz, inertia (9, unit density, row-major), bounds min xyz,
+// max xyz (20 doubles).  Returns the hull index.
+int orc_add_hull(void *wp, int np, const double *points, const double *shrunk, int nf, const int *faces, int nv,
+                 const int *vidx, const double *planes, const double *scal) {
+    World &w = *(World *)wp;
+    auto h = std::make_unique<HullData>();
+    for (int i = 0; i < np; i++) {
+        h->points.push_back({points[3 * i], points[3 * i + 1], points[3 * i + 2]});
+        h->shrunk.push_back({shrunk[3 * i], shrunk[3 * i + 1], shrunk[3 * i + 2]});
+    }
+    for (int f = 0; f < nf; f++) {
+        h->face_first.push_back(faces[2 * f]);
+        h->face_count.push_back(faces[2 * f + 1]);
+        h->plane_n.push_back({planes[4 * f], planes[4 * f + 1], planes[4 * f + 2]});
+        h->plane_c.push_back(planes[4 * f + 3]);
+    }
+    for (int k = 0; k < nv; k++) h->vidx.push_back(vidx[k]);
+    h->convex_radius = scal[0];
+    h->volume = scal[1];
+    h->com = {scal[2], scal[3], scal[4]};
+    for (int k = 0; k < 9; k++) h->inertia[k] = scal[5 + k];
+    h->bounds = {{scal[14], scal[15], scal[16]}, {scal[17], scal[18], scal[19]}};
+    w.hulls.push_back(std::move(h));
+    return (int)w.hulls.size() - 1;
+}
 
 // Swing-twist joint (swing-twist-constraint.ts create :180-296), 47 doubles:
 //  0 bodyA, 1 bodyB, 2-4 position1, 5-7 position2, 8-10 twistAxis1, 11-13 planeAxis1,

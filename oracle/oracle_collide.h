@@ -18,10 +18,25 @@ namespace orc {
 constexpr double DEFAULT_CONVEX_RADIUS = 0.05;  // src/collision/support.ts:5
 constexpr uint32_t EMPTY_SUB_SHAPE_ID = 0xffffffffu;  // src/body/sub-shape.ts:4
 
-enum ShapeType : int { SHAPE_SPHERE = 0, SHAPE_BOX = 1, SHAPE_CAPSULE = 2 };
+enum ShapeType : int { SHAPE_SPHERE = 0, SHAPE_BOX = 1, SHAPE_CAPSULE = 2, SHAPE_CONVEX_HULL = 3 };
 
-// Shape data (src/shapes/box.ts:38-70, src/shapes/sphere.ts, src/shapes/capsule.ts)
+// ConvexHullShape fields (src/shapes/convex-hull.ts:38-62): points relative to the centre of
+// mass, the points shrunk by the convex radius (setConvexHullNoConvexSupport :732-788),
+// polygon faces over point indices and their planes (n . x + c = 0)
+struct HullData {
+    std::vector<V3> points, shrunk;
+    std::vector<int> face_first, face_count, vidx;
+    std::vector<V3> plane_n;
+    std::vector<double> plane_c;
+    double convex_radius = 0, volume = 0;
+    V3 com{0, 0, 0};
+    double inertia[9] = {0};  // unit density, row-major
+    Box3 bounds;
+};
+
+// Shape data (src/shapes/box.ts:38-70, src/shapes/sphere.ts, src/shapes/capsule.ts, convex-hull.ts)
 struct Shape {
+    const HullData *hull = nullptr;  // convex hull
     int type = SHAPE_BOX;
     V3 half_extents;          // box
     double convex_radius = 0;  // box
@@ -36,10 +51,11 @@ struct Shape {
 // Support functions (src/collision/support.ts, src/shapes/sphere.ts:173-266)
 // ----------------------------------------------------------------------------
 enum SupportMode { INCLUDE_CONVEX_RADIUS = 0, EXCLUDE_CONVEX_RADIUS = 1 };
-enum SupportKind { SUP_BOX, SUP_SPHERE_POINT, SUP_SPHERE_SURFACE, SUP_CAPSULE_SEGMENT, SUP_CAPSULE_SURFACE };
+enum SupportKind { SUP_BOX, SUP_SPHERE_POINT, SUP_SPHERE_SURFACE, SUP_CAPSULE_SEGMENT, SUP_CAPSULE_SURFACE, SUP_HULL };
 
 struct Support {
     int kind = SUP_BOX;
+    const std::vector<V3> *pts = nullptr;  // convex hull support points
     V3 he;                    // box half extents (already shrunk if EXCLUDE)
     double radius = 0;        // sphere/capsule radius used by the surface form
     double half_height = 0;   // capsule
@@ -62,6 +78,18 @@ struct Support {
                     return {d.x * s, d.y * s, d.z * s};
                 }
                 return {0, 0, 0};
+            }
+            case SUP_HULL: {  // the point with the highest projection (convex-hull.ts:588-614, 695-715)
+                double best = -1.0 / 0.0;
+                V3 bp{0, 0, 0};
+                for (const V3 &p : *pts) {
+                    double dd = p.x * d.x + p.y * d.y + p.z * d.z;
+                    if (dd > best) {
+                        best = dd;
+                        bp = p;
+                    }
+                }
+                return bp;
             }
             case SUP_CAPSULE_SEGMENT:  // capsule.ts: segment +-h on Y
                 return {0, d.y > 0 ? half_height : -half_height, 0};
@@ -105,7 +133,17 @@ struct Support {
 // getSphereSupportFunction sphere.ts:256-266)
 inline Support make_support(const Shape &s, SupportMode mode) {
     Support o;
-    if (s.type == SHAPE_BOX) {
+    if (s.type == SHAPE_CONVEX_HULL) {
+        // getConvexHullSupportFunction convex-hull.ts:968-997
+        o.kind = SUP_HULL;
+        if (mode == INCLUDE_CONVEX_RADIUS || s.hull->convex_radius == 0) {
+            o.pts = &s.hull->points;
+            o.convex_radius = 0;
+        } else {
+            o.pts = &s.hull->shrunk;
+            o.convex_radius = s.hull->convex_radius;
+        }
+    } else if (s.type == SHAPE_BOX) {
         o.kind = SUP_BOX;
         if (mode == EXCLUDE_CONVEX_RADIUS) {
             double cr = std::min(s.convex_radius * 1.0, DEFAULT_CONVEX_RADIUS);
@@ -1167,9 +1205,32 @@ inline void capsule_supporting_face(Face &f, V3 d, double h, double r) {
     }
 }
 
+// convex hull getSupportingFace convex-hull.ts:479-541 (unit scale): the face whose plane normal
+// is most opposed to dir; at most MAX_FACE_VERTICES / 2 = 16 of its vertices
+inline void hull_supporting_face(Face &f, V3 dir, const HullData &h) {
+    int best = 0;
+    double bd = 0;
+    for (size_t i = 0; i < h.plane_n.size(); i++) {
+        V3 n = h.plane_n[i];
+        double d = (n.x * dir.x + n.y * dir.y + n.z * dir.z) / std::sqrt(n.x * n.x + n.y * n.y + n.z * n.z);
+        if (i == 0 || d < bd) {
+            bd = d;
+            best = (int)i;
+        }
+    }
+    int first = h.face_first[best], nv = h.face_count[best];
+    const int maxv = 32 / 2;
+    int step = (nv + maxv - 1) / maxv;
+    f.n = 0;
+    for (int i = 0; i < nv; i += step) f.v[f.n++] = h.points[h.vidx[first + i]];
+}
+
 // getShapeSupportingFace shapes.ts:489-508 (sphere has no face)
 inline void shape_supporting_face(Face &f, const Shape &s, V3 dir, V3 p, Q4 q) {
-    if (s.type == SHAPE_BOX) {
+    if (s.type == SHAPE_CONVEX_HULL) {
+        hull_supporting_face(f, dir, *s.hull);
+        transform_face(f, p, q);
+    } else if (s.type == SHAPE_BOX) {
         box_supporting_face(f, dir, s.half_extents);
         transform_face(f, p, q);
     } else if (s.type == SHAPE_CAPSULE) {

@@ -58,6 +58,7 @@ def load():
         "orc_add_hinge": ([vp, dp], i32),
         "orc_set_skip_joint_pairs": ([vp, i32], None),
         "orc_add_swing_twist": ([vp, dp], i32),
+        "orc_add_hull": ([vp, i32, dp, dp, i32, C.c_void_p, i32, C.c_void_p, dp, dp], i32),
     }
     for k, (a, r) in sig.items():
         f = getattr(lib, k)
@@ -129,7 +130,9 @@ def settings_array(ws) -> np.ndarray:
 class OracleWorld:
     """One oracle world built from the same bodies and settings as a GPU world."""
 
-    def __init__(self, ws, bodies: np.ndarray):
+    def __init__(self, ws, bodies: np.ndarray, hulls=()):
+        """hulls: convex hull records as GpuWorld.get_convex_hull returns them, in index order
+        (the bodies name them by index)."""
         lib = load()
         self.lib = lib
         L = ws.layers
@@ -150,9 +153,24 @@ class OracleWorld:
         s = settings_array(ws)
         self.h = lib.orc_world_create(dptr(s), n_obj, iptr(obj_to_bp), n_bp, op.ctypes.data, ovb.ctypes.data,
                                       bpp.ctypes.data)
+        for h in hulls:
+            self.add_hull(h)
         rows = rows_from_bodies(bodies)
         assert lib.orc_add_bodies(self.h, dptr(rows), len(rows)) == 0
         self.n = len(rows)
+
+    def add_hull(self, h) -> int:
+        pts = np.ascontiguousarray(h["points"], dtype=np.float64)
+        shr = np.ascontiguousarray(h["shrunk"], dtype=np.float64)
+        faces = np.ascontiguousarray(h["faces"], dtype=np.int32)
+        vidx = np.ascontiguousarray(h["face_vertices"], dtype=np.int32)
+        planes = np.ascontiguousarray(h["planes"], dtype=np.float64)
+        scal = np.concatenate([[h["convex_radius"], h["volume"]], h["com"], np.ravel(h["inertia"]),
+                               h["bounds_min"], h["bounds_max"]]).astype(np.float64)
+        k = self.lib.orc_add_hull(self.h, len(pts), dptr(pts), dptr(shr), len(faces), faces.ctypes.data, len(vidx),
+                                  vidx.ctypes.data, dptr(planes), dptr(scal))
+        assert k >= 0
+        return k
 
     def close(self):
         if self.h:
