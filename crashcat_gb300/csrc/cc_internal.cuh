@@ -65,7 +65,8 @@ struct DevCounters {
     int bar_error;                      // a bounded grid-barrier wait gave up
     int giant_left[2], giant_any[2], giant_sleep;
     int giant_colours;  // most colours of a giant island this step
-    int pad[5];
+    int num_small_joint_islands, num_large_joint_islands;  // islands with joints per tier
+    int pad[3];
 };
 
 // Settings copied into constant memory once per world.
@@ -346,6 +347,7 @@ struct DevWorld {
     int skip_joint_pairs;              // broadphase skips body pairs that share an enabled joint
     int *joint_partners;               // JOINT_PARTNERS per body: other bodies joined to it (-1: none)
     int *island_joint_count, *island_joint_off, *island_fill_j;
+    int *small_joint_list, *large_joint_list;  // islands with joints of the per-thread / per-CTA tiers
     // 5 x max_joints: as scattered | by (type, index) | by (priority, index, type) | colour of
     // each ranked joint | ranked joints grouped by colour (per-CTA solve)
     int *island_joints;

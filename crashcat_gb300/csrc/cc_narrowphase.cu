@@ -114,7 +114,8 @@ struct HullView {
     const float4 *points, *shrunk;
 };
 __device__ __forceinline__ HullView hull_view(const DevWorld &w) { return HullView{w.hulls, w.hull_points, w.hull_shrunk}; }
-template <typename S>
+// H: the support may be a convex hull (the contact-only narrowphase instance compiles it out)
+template <typename S, bool H = true>
 struct Sup {
     int kind;
     const float4 *hp;  // hull support points (original or shrunk) and their count
@@ -127,7 +128,7 @@ struct Sup {
     S add_r;
     __device__ V<S> inner(V<S> d) const {
         if (kind == SUP_BOX) return {d.x >= S(0) ? he.x : -he.x, d.y >= S(0) ? he.y : -he.y, d.z >= S(0) ? he.z : -he.z};
-        if (kind == SUP_HULL) {  // the point with the highest projection (convex-hull.ts:588-614, 695-715)
+        if (H && kind == SUP_HULL) {  // the point with the highest projection (convex-hull.ts:588-614, 695-715)
             S best = -s_max_value<S>();
             V<S> bp{S(0), S(0), S(0)};
             bool any = false;
@@ -174,16 +175,16 @@ struct Sup {
 };
 
 // setBoxSupport support.ts:339-370 / getSphereSupportFunction sphere.ts:256-266
-template <typename S>
-__device__ Sup<S> make_sup(int shape, float4 sp, bool exclude, const HullView &hv) {
-    Sup<S> o;
+template <typename S, bool H = true>
+__device__ Sup<S, H> make_sup(int shape, float4 sp, bool exclude, const HullView &hv) {
+    Sup<S, H> o;
     o.transformed = false;
     o.add_r = S(0);
     o.radius = S(0);
     o.he = {S(0), S(0), S(0)};
     o.hp = nullptr;
     o.hn = 0;
-    if (shape == SHAPE_HULL && hv.hulls) {
+    if (H && shape == SHAPE_HULL && hv.hulls) {
         // getConvexHullSupportFunction convex-hull.ts:968-997: the shrunk points with the convex
         // radius when it is excluded (and not zero), else the points themselves
         const DevHull &h = hv.hulls[hull_of(sp)];
@@ -230,8 +231,8 @@ __device__ Sup<S> make_sup(int shape, float4 sp, bool exclude, const HullView &h
     }
     return o;
 }
-template <typename S>
-__device__ void set_transform(Sup<S> &s, Q<S> q, V<S> p) {
+template <typename S, bool H>
+__device__ void set_transform(Sup<S, H> &s, Q<S> q, V<S> p) {
     S x2 = q.x + q.x, y2 = q.y + q.y, z2 = q.z + q.z;
     S xx = q.x * x2, xy = q.x * y2, xz = q.x * z2, yy = q.y * y2, yz = q.y * z2, zz = q.z * z2;
     S wx = q.w * x2, wy = q.w * y2, wz = q.w * z2;
@@ -511,8 +512,8 @@ struct GjkOut {
 };
 
 // gjkClosestPoints gjk.ts:1294-1546
-template <typename S>
-__device__ GjkOut<S> gjk(const Sup<S> &A, const Sup<S> &B, S tolerance, V<S> dir, S maxDistSq, Simplex<S> &sx) {
+template <typename S, bool H>
+__device__ GjkOut<S> gjk(const Sup<S, H> &A, const Sup<S, H> &B, S tolerance, V<S> dir, S maxDistSq, Simplex<S> &sx) {
     GjkOut<S> out;
     const S GJK_TOL = S(1e-5);
     S sqtol = tolerance * tolerance;
@@ -614,15 +615,20 @@ __device__ GjkOut<S> gjk(const Sup<S> &A, const Sup<S> &B, S tolerance, V<S> dir
 // ---------------------------------------------------------------------------
 // faces, clipping, reduction (FP32, coordinates relative to body A)
 // ---------------------------------------------------------------------------
-constexpr int FMAX = 32;        // vertices of a face or clipped polygon kept here
-constexpr int FMAX_FACE = 32;   // MAX_FACE_VERTICES (convex-hull.ts:88): a hull face gives at most half
-struct Face {
+// Faces and clipped polygons hold at most N vertices: 16 for the pairs of boxes, spheres and
+// capsules (4-vertex faces, 8-vertex clips), 32 when a hull takes part (a hull face gives at
+// most MAX_FACE_VERTICES / 2 = 16 vertices, convex-hull.ts:88, 515-517, and a clip of two such
+// faces up to 32).  The small instance keeps the common pairs' local frames small.
+constexpr int FMAX_FACE = 32;  // MAX_FACE_VERTICES (convex-hull.ts:88)
+template <int N>
+struct FaceN {
     int n;
-    float3 v[FMAX];
+    float3 v[N];
 };
 
 // box getSupportingFace box.ts:129-332 (unit scale), then rotate + translate
-__device__ void box_face(Face &f, float3 dir, float4 he4, float4 q, float3 t) {
+template <int N>
+__device__ void box_face(FaceN<N> &f, float3 dir, float4 he4, float4 q, float3 t) {
     float hx = he4.x, hy = he4.y, hz = he4.z;
     float ax = fabsf(dir.x), ay = fabsf(dir.y), az = fabsf(dir.z);
     f.n = 4;
@@ -670,7 +676,8 @@ __device__ void box_face(Face &f, float3 dir, float4 he4, float4 q, float3 t) {
 // capsule getSupportingFace capsule.ts:192-251: the segment on the side opposite to dir
 // (body space) when both caps project within the capsule projection slop, else no face;
 // rotated by q and moved by t
-__device__ void capsule_face(Face &f, float3 d, float4 sp, float4 q, float3 t) {
+template <int N>
+__device__ void capsule_face(FaceN<N> &f, float3 d, float4 sp, float4 q, float3 t) {
     float r = sp.x, h = sp.y;
     float len = sqrtf(d.x * d.x + d.z * d.z);
     f.n = 0;
@@ -688,7 +695,8 @@ __device__ void capsule_face(Face &f, float3 d, float4 sp, float4 q, float3 t) {
 
 // convex hull getSupportingFace convex-hull.ts:479-541 (unit scale): the face whose plane
 // normal is most opposed to dir, at most 16 of its vertices, rotated by q and moved by t
-__device__ void hull_face(Face &f, float3 dir, const DevWorld &w, float4 sp, float4 q, float3 t) {
+template <int N>
+__device__ void hull_face(FaceN<N> &f, float3 dir, const DevWorld &w, float4 sp, float4 q, float3 t) {
     const DevHull &h = w.hulls[hull_of(sp)];
     int best = 0;
     float bd = 0.f;
@@ -705,14 +713,15 @@ __device__ void hull_face(Face &f, float3 dir, const DevWorld &w, float4 sp, flo
     const int maxv = FMAX_FACE / 2;
     int step = (fc.y + maxv - 1) / maxv;
     f.n = 0;
-    for (int i = 0; i < fc.y && f.n < FMAX; i += step) {
+    for (int i = 0; i < fc.y && f.n < N; i += step) {
         float4 p = w.hull_points[w.hull_vidx[fc.x + i]];
         f.v[f.n++] = qrot(q, f3(p.x, p.y, p.z)) + t;
     }
 }
 
 // clipPolyVsPlane clip.ts:13-92
-__device__ void clip_plane(Face &out, const Face &in, float3 o, float3 n) {
+template <int N>
+__device__ void clip_plane(FaceN<N> &out, const FaceN<N> &in, float3 o, float3 n) {
     out.n = 0;
     if (in.n < 2) return;
     float3 e1 = in.v[in.n - 1];
@@ -727,12 +736,12 @@ __device__ void clip_plane(Face &out, const Face &in, float3 o, float3 n) {
             float den = dot3(e12, n);
             if (den != 0.f) {
                 float t = prevNum / den;
-                if (out.n < FMAX) out.v[out.n++] = e1 + e12 * t;
+                if (out.n < N) out.v[out.n++] = e1 + e12 * t;
             } else {
                 curIn = prevIn;
             }
         }
-        if (curIn && out.n < FMAX) out.v[out.n++] = e2;
+        if (curIn && out.n < N) out.v[out.n++] = e2;
         prevNum = num;
         prevIn = curIn;
         e1 = e2;
@@ -740,18 +749,19 @@ __device__ void clip_plane(Face &out, const Face &in, float3 o, float3 n) {
 }
 
 // clipPolyVsPoly clip.ts:108-175
-__device__ void clip_poly(Face &out, const Face &toClip, const Face &clipping, float3 cn) {
+template <int N>
+__device__ void clip_poly(FaceN<N> &out, const FaceN<N> &toClip, const FaceN<N> &clipping, float3 cn) {
     out.n = 0;
     if (toClip.n < 2 || clipping.n < 3) return;
-    Face t0, t1;
+    FaceN<N> t0, t1;
     int tmpIdx = 0;
     for (int i = 0; i < clipping.n; i++) {
         float3 c1 = clipping.v[i];
         float3 c2 = clipping.v[(i + 1) % clipping.n];
         float3 pn = cross3(cn, c2 - c1);
-        const Face *src = (i == 0) ? &toClip : (tmpIdx == 0 ? &t0 : &t1);
+        const FaceN<N> *src = (i == 0) ? &toClip : (tmpIdx == 0 ? &t0 : &t1);
         tmpIdx ^= 1;
-        Face *dst = (i == clipping.n - 1) ? &out : (tmpIdx == 0 ? &t0 : &t1);
+        FaceN<N> *dst = (i == clipping.n - 1) ? &out : (tmpIdx == 0 ? &t0 : &t1);
         clip_plane(*dst, *src, c1, pn);
         if (dst->n < 3) {
             out.n = 0;
@@ -760,17 +770,19 @@ __device__ void clip_poly(Face &out, const Face &toClip, const Face &clipping, f
     }
 }
 
-struct Pts {
+template <int N>
+struct PtsN {
     int n;
-    float3 a[FMAX], b[FMAX];
+    float3 a[N], b[N];
 };
 
 // pruneContactPoints manifold.ts:192-311
-__device__ void prune(Pts &m, float3 axis) {
+template <int N>
+__device__ void prune(PtsN<N> &m, float3 axis) {
     const float MIN_D = 1.0e-6f;
     if (m.n <= 4) return;
-    float3 proj[FMAX];
-    float dsq[FMAX];
+    float3 proj[N];
+    float dsq[N];
     for (int i = 0; i < m.n; i++) {
         float d = dot3(m.a[i], axis);
         proj[i] = m.a[i] - axis * d;
@@ -828,7 +840,8 @@ __device__ void prune(Pts &m, float3 axis) {
 
 // clipPolyVsEdge clip.ts:190-363: crossings of the polygon with the plane through the edge
 // (normal = clip normal x edge), snapped onto the edge projected into the polygon's plane
-__device__ void clip_poly_vs_edge(Face &out, const Face &poly, float3 ev1, float3 ev2, float3 cn) {
+template <int N>
+__device__ void clip_poly_vs_edge(FaceN<N> &out, const FaceN<N> &poly, float3 ev1, float3 ev2, float3 cn) {
     out.n = 0;
     if (poly.n < 3) return;
     float3 en = cross3(cn, ev2 - ev1);
@@ -846,7 +859,7 @@ __device__ void clip_poly_vs_edge(Face &out, const Face &poly, float3 ev1, float
         float3 e2 = poly.v[j];
         float num = dot3(ev1 - e2, en);
         bool curIn = num < 0.f;
-        if (curIn != prevIn && out.n < FMAX) {
+        if (curIn != prevIn && out.n < N) {
             float3 e12 = e2 - e1;
             float den = dot3(e12, en);
             float3 c = den != 0.f ? e1 + e12 * (prevNum / den) : e1;
@@ -860,8 +873,9 @@ __device__ void clip_poly_vs_edge(Face &out, const Face &poly, float3 ev1, float
 }
 
 // manifoldBetweenTwoFaces manifold.ts:345-444 (polygon faces)
-__device__ void manifold_faces(Pts &out, float3 cp1, float3 cp2, float3 axis, float maxDist, const Face &f1,
-                               const Face &f2) {
+template <int N>
+__device__ void manifold_faces(PtsN<N> &out, float3 cp1, float3 cp2, float3 axis, float maxDist, const FaceN<N> &f1,
+                               const FaceN<N> &f2) {
     out.n = 0;
     if (f1.n < 2 || f2.n < 3) {
         out.a[0] = cp1;
@@ -869,7 +883,7 @@ __device__ void manifold_faces(Pts &out, float3 cp1, float3 cp2, float3 axis, fl
         out.n = 1;
         return;
     }
-    Face clipped;
+    FaceN<N> clipped;
     clipped.n = 0;
     if (f1.n >= 3)
         clip_poly(clipped, f2, f1, axis);
@@ -892,7 +906,7 @@ __device__ void manifold_faces(Pts &out, float3 cp1, float3 cp2, float3 axis, fl
                 out.a[out.n] = p2 - axis * dist;
                 out.b[out.n] = p2;
                 out.n++;
-                if (out.n >= FMAX) break;
+                if (out.n >= N) break;
             }
         }
     }
@@ -905,16 +919,17 @@ __device__ void manifold_faces(Pts &out, float3 cp1, float3 cp2, float3 axis, fl
 
 // Turns one hit (relative to A's position) into a manifold: update.ts:385-558
 // for a convex pair (a single hit, so a single manifold).
+template <int N>
 __device__ void emit_manifold(DevWorld &w, int a, int b, float3 pa, float3 pb, float3 axis, float penetration,
                               bool faces) {
     float4 qa = w.quat[a], qb = w.quat[b];
     float3 posA = xyz(w.pos[a]), posB = xyz(w.pos[b]);
     uint32_t fa = w.flags[a], fb = w.flags[b];
-    Pts pts;
+    PtsN<N> pts;
     float maxd = c_settings.spec_dist + c_settings.manifold_tol;
     float3 nrm = normalize3(axis);
     bool haveFaces = false;
-    Face fA, fB;
+    FaceN<N> fA, fB;
     fA.n = 0;
     fB.n = 0;
     if (faces) {
@@ -966,6 +981,9 @@ struct EpaItem {
 };
 
 // narrowphase for one pair: order A/B (update.ts:74), dispatch, GJK
+// HULLS: the pairs with a convex hull (launched only when the world has hulls); the other
+// instance takes every other pair, without the hull code
+template <bool HULLS>
 __global__ void __launch_bounds__(128) k_narrowphase(DevWorld w, EpaItem *epa_items) {
     int np = min(w.ctr->num_pairs, w.max_pairs);
     for (int pi = blockIdx.x * blockDim.x + threadIdx.x; pi < np; pi += gridDim.x * blockDim.x) {
@@ -986,6 +1004,7 @@ __global__ void __launch_bounds__(128) k_narrowphase(DevWorld w, EpaItem *epa_it
         float4 qa = w.quat[a], qb = w.quat[b];
         float4 sa = w.shape[a], sb = w.shape[b];
         int sha = shape_of(fa), shb = shape_of(fb);
+        if ((sha == SHAPE_HULL || shb == SHAPE_HULL) != HULLS) continue;
         if (sha == SHAPE_SPHERE && shb == SHAPE_SPHERE) {
             // collideSphereVsSphere sphere.ts:319-410 (no speculative distance)
             float3 d = xyz(pb4) - xyz(pa4);
@@ -994,7 +1013,7 @@ __global__ void __launch_bounds__(128) k_narrowphase(DevWorld w, EpaItem *epa_it
             if (dsq >= rs * rs) continue;
             float dist = sqrtf(dsq);
             float3 n = dist > 0.f ? d * (1.f / dist) : f3(0.f, 1.f, 0.f);
-            emit_manifold(w, a, b, n * sa.x, d - n * sb.x, n, rs - dist, false);
+            emit_manifold<16>(w, a, b, n * sa.x, d - n * sb.x, n, rs - dist, false);
             continue;
         }
         // collideConvexVsConvex convex.ts:257-346: B in A's local frame
@@ -1004,8 +1023,8 @@ __global__ void __launch_bounds__(128) k_narrowphase(DevWorld w, EpaItem *epa_it
         V<float> ab{pb4.x - pa4.x, pb4.y - pa4.y, pb4.z - pa4.z};
         V<float> posBInA = qrotS(iA, ab);
         const HullView hv = hull_view(w);
-        Sup<float> supA = make_sup<float>(sha, sa, true, hv);
-        Sup<float> supB = make_sup<float>(shb, sb, true, hv);
+        Sup<float, HULLS> supA = make_sup<float, HULLS>(sha, sa, true, hv);
+        Sup<float, HULLS> supB = make_sup<float, HULLS>(shb, sb, true, hv);
         set_transform(supB, rel, posBInA);
         V<float> axis = posBInA;
         if (lsq(axis) <= 1e-12f) axis = {1.f, 0.f, 0.f};
@@ -1044,8 +1063,8 @@ __global__ void __launch_bounds__(128) k_narrowphase(DevWorld w, EpaItem *epa_it
         float al = sqrtf(lsq(g.axis));
         if (al > 0.f) pa = pa + g.axis * (-(maxSep / al));
         V<float> paw = qrotS(qA, pa), pbw = qrotS(qA, pb), axw = qrotS(qA, g.axis);
-        emit_manifold(w, a, b, f3(paw.x, paw.y, paw.z), f3(pbw.x, pbw.y, pbw.z), f3(axw.x, axw.y, axw.z),
-                      penetration, true);
+        emit_manifold<HULLS ? 32 : 16>(w, a, b, f3(paw.x, paw.y, paw.z), f3(pbw.x, pbw.y, pbw.z),
+                                       f3(axw.x, axw.y, axw.z), penetration, true);
     }
 }
 
@@ -1751,12 +1770,15 @@ __global__ void __launch_bounds__(EPA_BLOCK) k_epa_big(DevWorld w, EpaItem *item
 }
 
 // Manifolds of the EPA hits (faces, clipping, reduction in FP32), one item per thread.
+template <bool HULLS>
 __global__ void __launch_bounds__(128) k_epa_emit(DevWorld w, const EpaItem *items) {
     int ne = min(w.ctr->num_epa, w.max_epa);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ne; i += gridDim.x * blockDim.x) {
         const EpaItem &it = items[i];
         if (it.size != 1) continue;
-        emit_manifold(w, it.a, it.b, it.y[0], it.p[0], it.q[0], __int_as_float(it.pad), true);
+        bool hull = shape_of(w.flags[it.a]) == SHAPE_HULL || shape_of(w.flags[it.b]) == SHAPE_HULL;
+        if (hull != HULLS) continue;
+        emit_manifold<HULLS ? 32 : 16>(w, it.a, it.b, it.y[0], it.p[0], it.q[0], __int_as_float(it.pad), true);
     }
 }
 
@@ -1764,13 +1786,15 @@ size_t epa_item_bytes() { return sizeof(EpaItem); }
 
 void launch_narrowphase(DevWorld &w, float, cudaStream_t s, cudaEvent_t mid) {
     EpaItem *items = (EpaItem *)w.epa_items;
-    k_narrowphase<<<NUM_SMS * 8, 128, 0, s>>>(w, items);
+    k_narrowphase<false><<<NUM_SMS * 8, 128, 0, s>>>(w, items);
+    if (w.num_hulls > 0) k_narrowphase<true><<<NUM_SMS * 8, 128, 0, s>>>(w, items);
     if (mid) cudaEventRecord(mid, s);
     k_epa<<<w.epa_threads / EPA_BLOCK, EPA_BLOCK, 0, s>>>(w, items, (PackedBlock *)w.epa_packed, w.epa_fallback,
                                                           w.epa_packed_points, w.epa_fetch_warp);
     k_epa_big<<<EPA_BIG_THREADS / EPA_BLOCK, EPA_BLOCK, 0, s>>>(w, items, (EpaScratch *)w.epa_scratch,
                                                                 w.epa_fallback);
-    k_epa_emit<<<NUM_SMS * 8, 128, 0, s>>>(w, items);
+    k_epa_emit<false><<<NUM_SMS * 8, 128, 0, s>>>(w, items);
+    if (w.num_hulls > 0) k_epa_emit<true><<<NUM_SMS * 8, 128, 0, s>>>(w, items);
 }
 
 // ---------------------------------------------------------------------------

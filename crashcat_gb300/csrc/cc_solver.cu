@@ -485,11 +485,11 @@ __global__ void k_island_classify(DevWorld w, int *small_list, int *large_list) 
             // ragdoll), else the per-CTA solve
             if (nj <= c_settings.small_island_max_joints && nc <= SMALL_ISLAND_MAX_CONS &&
                 nb <= SMALL_ISLAND_MAX_BODIES) {
-                int k = atomicAdd(&w.ctr->num_small_islands, 1);
-                small_list[k] = i;
+                int k = atomicAdd(&w.ctr->num_small_joint_islands, 1);
+                w.small_joint_list[k] = i;
             } else {
-                int k = atomicAdd(&w.ctr->num_large_islands, 1);
-                large_list[k] = i;
+                int k = atomicAdd(&w.ctr->num_large_joint_islands, 1);
+                w.large_joint_list[k] = i;
             }
         } else if (nc <= c_settings.small_island_max_cons && nb <= SMALL_ISLAND_MAX_BODIES) {
             int k = atomicAdd(&w.ctr->num_small_islands, 1);
@@ -809,14 +809,16 @@ __global__ void k_joint_setup(DevWorld w, float dt) {
 // ---------------------------------------------------------------------------
 // small islands: one thread runs the island in the reference's exact order
 // ---------------------------------------------------------------------------
+// JOINTS: the islands with joints (their own list); the contact-only instance carries no joint code
+template <bool JOINTS>
 __global__ void __launch_bounds__(128) k_solve_small(DevWorld w, CacheTables ct, const int *small_list, float dt,
                                                       float ratio) {
-    int ns = w.ctr->num_small_islands;
+    int ns = JOINTS ? w.ctr->num_small_joint_islands : w.ctr->num_small_islands;
     CacheRecord *crecs = ct.recs[*ct.parity];
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
         int isl = small_list[s];
         int nb = w.island_body_count[isl], nc = w.island_cons_count[isl];
-        int nj = joint_total(w) > 0 ? w.island_joint_count[isl] : 0;
+        int nj = JOINTS ? w.island_joint_count[isl] : 0;
         const int *bl = w.island_bodies + w.island_body_off[isl];
         const int *cl = w.island_cons + w.island_cons_off[isl];
         int order[SMALL_ISLAND_MAX_CONS];
@@ -925,6 +927,7 @@ __global__ void __launch_bounds__(128) k_solve_small(DevWorld w, CacheTables ct,
 constexpr int LARGE_BLOCK = 256;
 constexpr int JOINT_COLOURS = 64;  // joint colours of the per-CTA solve; the rest go to one thread
 
+template <bool JOINTS>
 __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTables ct, const int *large_list,
                                                               int *scratch_order, int *scratch_colour,
                                                               int *scratch_claim, float dt, float ratio) {
@@ -932,7 +935,7 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
     __shared__ int s_ncol;
     __shared__ int s_colour_start[257];
     __shared__ int s_jstart[JOINT_COLOURS + 2];
-    int nl = w.ctr->num_large_islands;
+    int nl = JOINTS ? w.ctr->num_large_joint_islands : w.ctr->num_large_islands;
     CacheRecord *crecs = ct.recs[*ct.parity];
     for (int li = blockIdx.x; li < nl; li += gridDim.x) {
         int isl = large_list[li];
@@ -954,7 +957,7 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
         for (int k = threadIdx.x; k < nb; k += blockDim.x) prepare_body(w, bl[k]);
         // the island's joints in index order (warm start) and in (priority, index) order
         // (sortConstraintIds constraints.ts:248-261)
-        int nj = joint_total(w) > 0 ? w.island_joint_count[isl] : 0;
+        int nj = JOINTS ? w.island_joint_count[isl] : 0;
         const int *jl = w.island_joints + (nj > 0 ? w.island_joint_off[isl] : 0);
         int *j_idx = const_cast<int *>(jl) + w.max_joints;
         int *j_pri = j_idx + w.max_joints;
@@ -1831,7 +1834,9 @@ void launch_contacts_and_islands(DevWorld &w, float dt, float, cudaStream_t s) {
 
 void launch_solver(DevWorld &w, float dt, float ratio, cudaStream_t s, cudaEvent_t mid) {
     CacheTables ct = tables_of(w);
-    k_solve_small<<<grid_for(w.n, 128, 16), 128, 0, s>>>(w, ct, w.small_list, dt, ratio);
+    const bool joints = w.num_hinges + w.num_swings > 0;
+    k_solve_small<false><<<grid_for(w.n, 128, 16), 128, 0, s>>>(w, ct, w.small_list, dt, ratio);
+    if (joints) k_solve_small<true><<<grid_for(w.n, 128, 16), 128, 0, s>>>(w, ct, w.small_joint_list, dt, ratio);
     if (mid) cudaEventRecord(mid, s);
     static bool warp_smem_set = false;  // set on the first (eager) step, before any graph capture
     const size_t warp_smem = sizeof(WarpIsland) * WARPS_PER_BLOCK;
@@ -1844,8 +1849,12 @@ void launch_solver(DevWorld &w, float dt, float ratio, cudaStream_t s, cudaEvent
     // the per-CTA and per-warp classes hold disjoint islands: run them side by side
     cudaEventRecord(w.ev_fork, s);
     cudaStreamWaitEvent(w.aux_stream, w.ev_fork, 0);
-    k_solve_large<<<NUM_SMS * 2, LARGE_BLOCK, 0, w.aux_stream>>>(w, ct, w.large_list, w.scratch_order,
-                                                                 w.scratch_colour, w.scratch_claim, dt, ratio);
+    k_solve_large<false><<<NUM_SMS * 2, LARGE_BLOCK, 0, w.aux_stream>>>(w, ct, w.large_list, w.scratch_order,
+                                                                        w.scratch_colour, w.scratch_claim, dt, ratio);
+    if (joints)
+        k_solve_large<true><<<NUM_SMS * 2, LARGE_BLOCK, 0, w.aux_stream>>>(w, ct, w.large_joint_list, w.scratch_order,
+                                                                           w.scratch_colour, w.scratch_claim, dt,
+                                                                           ratio);
     cudaEventRecord(w.ev_join, w.aux_stream);
     k_solve_warp<<<NUM_SMS * w.warp_blocks_per_sm, WARP_BLOCK, warp_smem, s>>>(w, ct, dt, ratio);
     cudaStreamWaitEvent(s, w.ev_join, 0);

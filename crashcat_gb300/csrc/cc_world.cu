@@ -478,7 +478,8 @@ int cc_world_destroy(cc_world *W) {
                     w.scratch_colour, w.scratch_claim, w.mid_list, w.body_local, w.contact_event,
                     w.removed_keys, W->d_state_rows, w.hinges, w.island_joints, w.island_joint_count,
                     w.island_joint_off, w.island_fill_j, w.joint_wake, w.joint_partners, w.swings,
-                    w.giant_list, w.giant_claim, w.giant_count, w.hulls, w.hull_points, w.hull_shrunk,
+                    w.giant_list, w.giant_claim, w.giant_count, w.small_joint_list, w.large_joint_list,
+                    w.hulls, w.hull_points, w.hull_shrunk,
                     w.hull_planes, w.hull_faces, w.hull_vidx};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -1218,6 +1219,7 @@ static int ensure_joint_capacity(cc_world *W, int need_hinges, int need_swings) 
     if (!w.island_joint_count) {
         if ((r = dalloc(&w.island_joint_count, w.cap)) != CC_OK || (r = dalloc(&w.island_joint_off, w.cap)) != CC_OK ||
             (r = dalloc(&w.island_fill_j, w.cap)) != CC_OK || (r = dalloc(&w.joint_wake, 1)) != CC_OK ||
+            (r = dalloc(&w.small_joint_list, w.cap)) != CC_OK || (r = dalloc(&w.large_joint_list, w.cap)) != CC_OK ||
             (r = dalloc(&w.joint_partners, (size_t)w.cap * JOINT_PARTNERS)) != CC_OK)
             return r;
         CC_TRY(cudaMemset(w.joint_partners, 0xff, sizeof(int) * (size_t)w.cap * JOINT_PARTNERS));

@@ -684,15 +684,15 @@ def mixed_convex_pile(n: int = 400, seed: int = 2, extent: float = 12.0, heights
     """The mixed convex pile's bodies: shape type uniform over spheres (r 0.2-0.6 m), boxes
     (half extents 0.2-0.8 m), capsules (r 0.2-0.4 m, half height 0.3-0.8 m) and convex hulls of
     16-32 points on an ellipsoid (semi-axes 0.3-0.8 m), dropped from the given heights over an
-    area of extent x extent m onto a static box floor (the terrain mesh of the full workload is
-    not part of this scene), at seeded random orientations; fast_fraction of the bodies get
+    area of 1.6 extent x 1.6 extent m onto a static box floor (the terrain mesh of the full
+    workload is not part of this scene), at seeded random orientations; fast_fraction of the bodies get
     speeds drawn from `speeds` in a random direction."""
     rng = np.random.Generator(np.random.PCG64(seed))
     nb = n + (1 if floor else 0)
     b = blank_bodies(nb)
     k0 = 0
-    if floor:
-        static_floor(b, 0, half=(extent, 0.5, extent), friction=0.5)
+    if floor:  # three times the drop area, so that nothing rolls off the edge
+        static_floor(b, 0, half=(3 * extent, 0.5, 3 * extent), friction=0.5)
         k0 = 1
     idx = np.arange(k0, nb)
     kinds = rng.integers(0, 4, size=n)
