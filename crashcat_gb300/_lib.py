@@ -61,6 +61,9 @@ class Settings(C.Structure):
         ("max_pairs", C.c_int32),
         ("max_manifolds", C.c_int32),
         ("num_worlds", C.c_int32),
+        ("ccd_linear_cast_threshold", C.c_double),
+        ("ccd_linear_cast_max_penetration", C.c_double),
+        ("ccd_min_velocity_for_restitution", C.c_double),
     ]
 
 
@@ -75,7 +78,8 @@ class Stats(C.Structure):
     _fields_ = [(n, C.c_int32) for n in (
         "num_bodies", "num_awake", "num_pairs", "num_manifolds", "num_contact_points", "num_epa",
         "num_islands", "max_island_constraints", "overflow_flags", "gpu_launches_per_step")] + [
-        ("last_call_ms", C.c_float), ("num_giant_islands", C.c_int32), ("giant_colours", C.c_int32)]
+        ("last_call_ms", C.c_float), ("num_giant_islands", C.c_int32), ("giant_colours", C.c_int32),
+        ("num_ccd", C.c_int32), ("num_ccd_hits", C.c_int32)]
 
 
 # numpy mirror of cc_body_desc (natural C alignment, 4-byte fields only)
@@ -88,7 +92,9 @@ BODY_DTYPE = np.dtype([
     ("max_linear_velocity", np.float32), ("max_angular_velocity", np.float32),
     ("friction_combine", np.int32), ("restitution_combine", np.int32),
     ("collision_groups", np.uint32), ("collision_mask", np.uint32), ("allowed_dofs", np.int32),
+    ("motion_quality", np.int32),
 ])
+MOTION_DISCRETE, MOTION_LINEAR_CAST = 0, 1
 
 EXPORTS = {
     "cc_world_settings_default": ([C.POINTER(Settings)], C.c_int),

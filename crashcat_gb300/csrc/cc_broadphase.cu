@@ -277,7 +277,8 @@ __global__ void k_lbvh_build(DevWorld w, int2 *node_world) {
     if (blockIdx.x == 0 && threadIdx.x == 0) w.node_parent[n == 1 ? 0 : 0] = -1;
 }
 
-__global__ void k_lbvh_refit(DevWorld w, int2 *node_world) {
+__global__ void k_lbvh_refit(DevWorld w, int2 *node_world, const int *gate) {
+    if (gate && *gate == 0) return;
     int n = w.n;
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
         int body = w.order[j];
@@ -438,6 +439,54 @@ void launch_integrate_forces(DevWorld &w, float dt, cudaStream_t s) {
     k_integrate_forces<<<grid_for(w.n, 256), 256, 0, s>>>(w, dt);
 }
 
+// Continuous collision, after the velocity integration: every body's bounds where the step
+// has put it so far (updatePositionFromCenterOfMass + updateAABB rigid-body.ts:545-674 for the
+// bodies that moved, the cast bodies still at their old position with the new rotation), the
+// record of each cast body (update.ts:940-962) and its world's record count.
+__global__ void k_ccd_prepare(DevWorld w, float dt) {
+    if (w.ctr->num_ccd == 0) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
+        uint32_t f = w.flags[i];
+        const bool cast = w.ccd_flag[i] != 0;
+        const float4 sp = w.shape[i];
+        if (motion_of(f) != STATIC && !sleeping_of(f) && !cast) {
+            float3 p = xyz(w.com[i]) - qrot(w.quat[i], shape_com(w, f, sp));
+            w.pos[i] = make_float4(p.x, p.y, p.z, 0.f);
+        }
+        double lo[3], hi[3], b[6];
+        shape_bounds(w, f, sp, lo, hi);
+        exact_aabb(w.pos[i], w.quat[i], lo, hi, b);
+        double *o = w.aabb64 + (size_t)i * 6;
+        for (int k = 0; k < 6; k++) o[k] = b[k];
+        w.aabb_lo[i] = make_float4(__double2float_rd(b[0]), __double2float_rd(b[1]), __double2float_rd(b[2]), 0.f);
+        w.aabb_hi[i] = make_float4(__double2float_ru(b[3]), __double2float_ru(b[4]), __double2float_ru(b[5]), 0.f);
+        w.ccd_index[i] = cast ? w.ccd_slot[i] : -1;
+        if (!cast) continue;
+        const float inner = shape_inner_radius(w, f, sp);
+        const float thr = c_settings.ccd_threshold * inner;
+        const float3 d = xyz(w.linvel[i]) * dt;
+        CcdRec r;
+        r.delta = make_float4(d.x, d.y, d.z, thr * thr);
+        r.normal = make_float4(0.f, 0.f, 0.f, fminf(c_settings.slop, c_settings.ccd_max_penetration * inner));
+        r.point = make_float4(0.f, 0.f, 0.f, 1.f);
+        r.fps = 1.f;
+        r.friction = r.restitution = 0.f;
+        r.body = i;
+        r.hit = -1;
+        r.slot = 0;
+        r.pad[0] = r.pad[1] = 0;
+        w.ccd[w.ccd_slot[i]] = r;
+        atomicAdd(&w.ccd_world_fill[w.world[i]], 1);
+    }
+}
+
+void launch_ccd_bounds(DevWorld &w, float dt, cudaStream_t s) {
+    int n = w.n;
+    k_ccd_prepare<<<grid_for(n, 256), 256, 0, s>>>(w, dt);
+    if (n > 1) cudaMemsetAsync(w.node_flag, 0, sizeof(int) * (size_t)(n - 1), s);
+    k_lbvh_refit<<<grid_for(n, 256), 256, 0, s>>>(w, w.node_world, &w.ctr->num_ccd);
+}
+
 void launch_broadphase(DevWorld &w, cudaStream_t s) {
     int n = w.n;
     k_reset_scene<<<1, 32, 0, s>>>(w.scene);
@@ -447,7 +496,7 @@ void launch_broadphase(DevWorld &w, cudaStream_t s) {
     while ((1 << wbits) < w.num_worlds) wbits++;
     radix_sort_pairs_u64(w.morton, w.morton_alt, w.order, w.order_alt, n, 30 + wbits, w.scan_tmp, s);
     if (n > 1) k_lbvh_build<<<grid_for(n - 1, 256), 256, 0, s>>>(w, w.node_world);
-    k_lbvh_refit<<<grid_for(n, 256), 256, 0, s>>>(w, w.node_world);
+    k_lbvh_refit<<<grid_for(n, 256), 256, 0, s>>>(w, w.node_world, nullptr);
     k_find_pairs<<<grid_for(n, 128, 16), 128, 0, s>>>(w, w.node_world);
 }
 

@@ -27,6 +27,7 @@ enum : uint32_t {
     F_FCOMB_SHIFT = 15,          // bits 15-17 friction combine mode
     F_RCOMB_SHIFT = 18,          // bits 18-20 restitution combine mode
     F_LAYER_SHIFT = 21,          // bits 21-25 object layer
+    F_LINEAR_CAST = 1u << 26,    // MotionQuality.LINEAR_CAST
 };
 __host__ __device__ inline int motion_of(uint32_t f) { return (int)(f & F_MOTION_MASK); }
 __host__ __device__ inline int shape_of(uint32_t f) { return (int)((f >> F_SHAPE_SHIFT) & 7u); }
@@ -66,7 +67,9 @@ struct DevCounters {
     int giant_left[2], giant_any[2], giant_sleep;
     int giant_colours;  // most colours of a giant island this step
     int num_small_joint_islands, num_large_joint_islands;  // islands with joints per tier
-    int pad[3];
+    int num_ccd;       // bodies that took the continuous-collision path this step
+    int num_ccd_hits;  // of them, those whose cast hit a body
+    int pad[1];
 };
 
 // Settings copied into constant memory once per world.
@@ -89,7 +92,11 @@ struct DevSettings {
     int allow_sleeping;
     float time_before_sleep;
     float sleep_threshold;
+    float ccd_threshold, ccd_max_penetration, ccd_min_vel_restitution;  // WorldSettings.ccd
     uint32_t allowed_pairs[CC_MAX_LAYERS];  // combined layer predicate, bit j of [i]
+    // layer predicate of the continuous-collision cast: object layer pair enabled AND the
+    // querying layer may query the other's broadphase layer (broadphase.ts:334-335, dbvt.ts:954)
+    uint32_t cast_pairs[CC_MAX_LAYERS];
     int small_island_max_cons;  // islands up to this many contacts run on one thread
     int small_island_max_joints;  // islands with joints: up to this many joints run on one thread
 };
@@ -261,6 +268,18 @@ struct AdjHandoff {
     float *vals;               // 12 per entry: 4 points x (t1, t2, n)
 };
 
+// One body's continuous-collision record of a step (CCDBody ccd.ts:20-57)
+struct CcdRec {
+    float4 delta;   // displacement of the step | squared cast threshold
+    float4 normal;  // contact normal | maximum penetration
+    float4 point;   // contact point | fraction of the displacement at the hit
+    float fps;      // fraction plus the penetration allowance
+    float friction, restitution;  // combined materials of the hit
+    int body, hit;  // the body, the body it hits (-1: none)
+    int slot;       // creation rank inside its world (bodies in index order)
+    int pad[2];
+};
+
 struct DevWorld {
     int n;          // bodies in use
     int cap;        // body capacity
@@ -366,6 +385,17 @@ struct DevWorld {
     int *giant_list;
     unsigned long long *giant_claim;       // 4 x cap: contact claims, two parities | joint claims, two parities
     int *giant_count;  // 4 x (GIANT_COLOURS + 2): contact colour offsets, contact fill cursors, joint offsets, joint fill
+    // continuous collision (LINEAR_CAST bodies, update.ts:896-1670)
+    int num_linear_cast;  // bodies with LINEAR_CAST motion quality (0: the single-pass solve)
+    int *ccd_flag;        // per body: deferred its translation this step
+    int *ccd_slot;        // per body: exclusive scan of ccd_flag (its record)
+    int *ccd_index;       // per body: its record this step, -1 for none
+    CcdRec *ccd;          // records in body order
+    int *ccd_world_off;   // num_worlds + 1: records per world, then their offsets
+    int *ccd_world_fill;  // num_worlds: scatter cursors
+    int *ccd_seg;         // records grouped by world
+    float2 *ccd_lambda;   // per world: accumulated lambdas of the normal and friction parts
+    int *ccd_scan_tmp;    // scan scratch over the worlds
 };
 
 __host__ __device__ inline int hull_of(float4 sp) {
@@ -382,6 +412,14 @@ __device__ inline float3 shape_com(const DevWorld &w, uint32_t f, float4 sp) {
     if (shape_of(f) != SHAPE_HULL) return make_float3(0.f, 0.f, 0.f);
     float4 c = w.hulls[hull_of(sp)].com;
     return make_float3(c.x, c.y, c.z);
+}
+
+// getInnerRadius box.ts:333-335, sphere.ts:147-149, capsule.ts:254-256, convex-hull.ts:549-558
+__device__ inline float shape_inner_radius(const DevWorld &w, uint32_t f, float4 sp) {
+    int s = shape_of(f);
+    if (s == SHAPE_BOX) return fminf(sp.x, fminf(sp.y, sp.z));
+    if (s == SHAPE_HULL) return w.hulls[hull_of(sp)].inner_radius;
+    return sp.x;  // sphere and capsule radius
 }
 
 // ---- user joints of every type under one id ---------------------------------------------
@@ -509,7 +547,15 @@ void launch_integrate_forces(DevWorld &w, float dt, cudaStream_t s);
 void launch_broadphase(DevWorld &w, cudaStream_t s);
 void launch_narrowphase(DevWorld &w, float dt, cudaStream_t s, cudaEvent_t mid = nullptr);
 void launch_contacts_and_islands(DevWorld &w, float dt, float warm_ratio, cudaStream_t s);
-void launch_solver(DevWorld &w, float dt, float warm_ratio, cudaStream_t s, cudaEvent_t mid = nullptr);
+// phase: SOLVE_ALL runs each island's whole solve in one pass; a world with LINEAR_CAST bodies
+// runs SOLVE_VELOCITY (through the integration), the continuous-collision pass, then
+// SOLVE_POSITION (position iterations, positions, sleeping)
+enum : int { SOLVE_ALL = 0, SOLVE_VELOCITY = 1, SOLVE_POSITION = 2 };
+void launch_solver(DevWorld &w, float dt, float warm_ratio, cudaStream_t s, cudaEvent_t mid = nullptr,
+                   int phase = SOLVE_ALL);
+void launch_ccd(DevWorld &w, float dt, cudaStream_t s);
+void launch_ccd_bounds(DevWorld &w, float dt, cudaStream_t s);
+void launch_ccd_find(DevWorld &w, float dt, cudaStream_t s);
 int giant_blocks_for_device();
 void launch_update_bounds(DevWorld &w, cudaStream_t s);
 void upload_settings(const DevSettings &s, double spec64, cudaStream_t st);

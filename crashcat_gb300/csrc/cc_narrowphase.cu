@@ -16,6 +16,8 @@
 // per-thread slice of global scratch memory.
 #include <mutex>
 
+#include <math_constants.h>
+
 #include "cc_internal.cuh"
 
 namespace cc {
@@ -1783,6 +1785,263 @@ __global__ void __launch_bounds__(128) k_epa_emit(DevWorld w, const EpaItem *ite
 }
 
 size_t epa_item_bytes() { return sizeof(EpaItem); }
+
+// ---------------------------------------------------------------------------
+// continuous collision: the shape cast of each LINEAR_CAST body against the world
+// ---------------------------------------------------------------------------
+// gjkCastShape gjk.ts:853-1259: A, placed in B's frame, moves by disp; B is fixed.  Returns
+// false on a miss, else the time of impact, the closest points then and the unnormalised
+// separating axis (closest points found without the last point being required,
+// computeClosestPointToSimplex gjk.ts:524-596).
+template <typename S>
+__device__ bool gjk_cast(S &lambda_out, V<S> &pa, V<S> &pb, V<S> &axis_out, const Sup<S> &A, const Sup<S> &B,
+                         V<S> disp, S tol, S rA, S rB, S maxLambda) {
+    S sqtol = tol * tol;
+    const S sumR = rA + rB;
+    Simplex<S> sx;
+    sx.size = 0;
+    S lambda = S(0);
+    V<S> x{S(0), S(0), S(0)};
+    const V<S> zero{S(0), S(0), S(0)};
+    V<S> q = -B.get(zero);
+    V<S> p = A.get(zero);
+    V<S> v = q - p;  // the starting direction (gjk.ts:882-897)
+    S vls = s_max_value<S>();
+    bool allow_restart = false;
+    V<S> prev_v{S(0), S(0), S(0)};
+    for (int it = 0; it < 100; it++) {
+        p = A.get(-v);
+        q = B.get(v);
+        V<S> wv = x - (q - p);
+        S vdw = dot(v, wv) - sumR * sq_root(lsq(v));
+        if (vdw > S(0)) {
+            S vdr = dot(v, disp);
+            if (vdr >= S(-1.0e-18)) return false;
+            S old = lambda;
+            lambda -= vdw / vdr;
+            if (old == lambda) break;
+            if (lambda >= maxLambda) return false;
+            x = disp * lambda;
+            vls = s_max_value<S>();
+            sqtol = (tol + sumR) * (tol + sumR);
+            allow_restart = true;
+        }
+        sx.pts[sx.size].p = p;
+        sx.pts[sx.size].q = q;
+        sx.size++;
+        for (int i = 0; i < sx.size; i++) sx.pts[i].y = x - sx.pts[i].q + sx.pts[i].p;
+        CP<S> cp;
+        switch (sx.size) {
+            case 1:
+                cp = {sx.pts[0].y, 1};
+                break;
+            case 2:
+                cp = closest_line(sx.pts[0].y, sx.pts[1].y, S(1e-10));
+                break;
+            case 3:
+                cp = closest_tri(sx.pts[0].y, sx.pts[1].y, sx.pts[2].y, false, S(1e-10));
+                break;
+            default:
+                cp = closest_tetra(sx.pts[0].y, sx.pts[1].y, sx.pts[2].y, sx.pts[3].y, false, S(1e-5));
+                break;
+        }
+        S nd = lsq(cp.p);
+        if (nd < vls) {
+            vls = nd;
+            v = cp.p;
+        } else {
+            if (!allow_restart) break;
+            allow_restart = false;
+            sx.pts[0].p = p;
+            sx.pts[0].q = q;
+            sx.size = 1;
+            v = x - q;
+            vls = s_max_value<S>();
+            continue;
+        }
+        if (cp.set == 0xf) break;
+        int ns = 0;  // updatePointSetPQ gjk.ts:799-813
+        for (int i = 0; i < sx.size; i++)
+            if (cp.set & (1 << i)) {
+                if (ns != i) {
+                    sx.pts[ns].p = sx.pts[i].p;
+                    sx.pts[ns].q = sx.pts[i].q;
+                }
+                ns++;
+            }
+        sx.size = ns;
+        if (vls <= sqtol) break;
+        prev_v = v;
+    }
+    for (int i = 0; i < sx.size; i++) sx.pts[i].y = x - sx.pts[i].q + sx.pts[i].p;
+    S vl = sq_root(lsq(v));
+    V<S> nv = vl > S(0) ? v * (S(1) / vl) : zero;
+    V<S> sa = zero, sb = zero;
+    if (sx.size == 1) {
+        sa = sx.pts[0].p;
+        sb = sx.pts[0].q;
+    } else if (sx.size == 2) {
+        Bary<S> b = bary2(sx.pts[0].y, sx.pts[1].y, S(1e-10));
+        sa = sx.pts[0].p * b.u + sx.pts[1].p * b.v;
+        sb = sx.pts[0].q * b.u + sx.pts[1].q * b.v;
+    } else if (sx.size >= 3) {
+        Bary<S> b = bary3(sx.pts[0].y, sx.pts[1].y, sx.pts[2].y, S(1e-10));
+        sa = sx.pts[0].p * b.u + sx.pts[1].p * b.v + sx.pts[2].p * b.w;
+        sb = sx.pts[0].q * b.u + sx.pts[1].q * b.v + sx.pts[2].q * b.w;
+    }
+    if (sx.size >= 1) {
+        pb = sb + nv * rB;
+        pa = lambda > S(0) ? pb : sa + nv * (-rA);
+    } else {
+        pa = pb = zero;
+    }
+    lambda_out = lambda;
+    axis_out = sumR > S(0) ? -v : -prev_v;
+    return true;
+}
+
+// entry t of the segment o + t d, t in [0, len], into a box, or +inf on a miss
+// (rayDistanceToBox3 cast-utils.ts:14-49, the slab test the casts use)
+__device__ __forceinline__ float ray_box_entry(float3 o, float3 d, float len, float3 lo, float3 hi) {
+    float t0 = 0.f, t1 = len;
+    const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+    const float mn[3] = {lo.x, lo.y, lo.z}, mx[3] = {hi.x, hi.y, hi.z};
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        if (fabsf(dd[i]) < 1e-10f) {
+            if (oo[i] < mn[i] || oo[i] > mx[i]) return CUDART_INF_F;
+        } else {
+            float inv = 1.f / dd[i];
+            float a = (mn[i] - oo[i]) * inv, c = (mx[i] - oo[i]) * inv;
+            t0 = fmaxf(t0, fminf(a, c));
+            t1 = fminf(t1, fmaxf(a, c));
+            if (t1 < t0) return CUDART_INF_F;
+        }
+    }
+    return t0;
+}
+
+// findCCDContacts update.ts:1354-1470: one thread per record.  The swept bounds are cast
+// through the refitted tree (dbvt.castAABB dbvt.ts:869-975: a ray from the swept centre along
+// the displacement against boxes grown by the swept half extents, nodes past the distance cull
+// skipped), every body found goes through the visitor's filters (update.ts:1153-1206) and the
+// shape cast (castConvexVsConvex convex.ts:675-900, back faces culled), and the collector keeps
+// the earliest fraction plus slop (update.ts:1044-1109); of equal ones the lower body index, the
+// first in the reference's candidate order for bodies of one tree leaf level.
+constexpr int CCD_STACK = 64;
+__global__ void __launch_bounds__(128) k_ccd_find(DevWorld w, const int2 *node_world, float dt) {
+    const int nr = w.ctr->num_ccd;
+    const int n = w.n;
+    const HullView hv = hull_view(w);
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nr; r += gridDim.x * blockDim.x) {
+        CcdRec &c = w.ccd[r];
+        const int a = c.body;
+        const uint32_t fa = w.flags[a];
+        const float3 delta = xyz(c.delta);
+        const float thr_sq = c.delta.w, max_pen = c.normal.w;
+        const float3 alo = xyz(w.aabb_lo[a]), ahi = xyz(w.aabb_hi[a]);
+        const float3 slo = f3(fminf(alo.x, alo.x + delta.x), fminf(alo.y, alo.y + delta.y), fminf(alo.z, alo.z + delta.z));
+        const float3 shi = f3(fmaxf(ahi.x, ahi.x + delta.x), fmaxf(ahi.y, ahi.y + delta.y), fmaxf(ahi.z, ahi.z + delta.z));
+        const float3 origin = (slo + shi) * 0.5f, half = (shi - slo) * 0.5f;
+        const float clen = sqrtf(lensq3(delta));
+        const float3 cdir = normalize3(delta);
+        const float3 half_a = (ahi - alo) * 0.5f;
+        const int wa = w.world[a];
+        const uint32_t allowed = c_settings.cast_pairs[layer_of(fa)];
+        const uint2 ga = w.groups[a];
+        const float3 pA = xyz(w.pos[a]);
+        const float4 qA = w.quat[a];
+        const Sup<float> supA0 = make_sup<float>(shape_of(fa), w.shape[a], true, hv);
+        float best_fps = c.fps, best_frac = c.point.w;
+        int best = -1;
+        float3 best_n = f3(0.f, 0.f, 0.f), best_p = f3(0.f, 0.f, 0.f);
+        int stack[CCD_STACK];
+        int sp = 0;
+        stack[sp++] = 0;
+        while (sp > 0) {
+            int node = stack[--sp];
+            int2 nw = node_world[node];
+            if (wa < nw.x || wa > nw.y) continue;
+            float3 nlo = xyz(w.node_lo[node]) - half, nhi = xyz(w.node_hi[node]) + half;
+            float t = ray_box_entry(origin, cdir, clen, nlo, nhi);
+            if (!(t < CUDART_INF_F) || t / clen > clen) continue;
+            if (node < n - 1) {
+                int2 ch = w.node_child[node];
+                if (sp + 2 <= CCD_STACK) {
+                    stack[sp++] = ch.y;
+                    stack[sp++] = ch.x;
+                } else {
+                    atomicOr(&w.ctr->overflow, OVF_SLOTS);
+                }
+                continue;
+            }
+            const int b = w.order[node - (n - 1)];
+            const uint32_t fb = w.flags[b];
+            if (!(allowed & (1u << layer_of(fb)))) continue;
+            const uint2 gb = w.groups[b];
+            if (!((ga.x & gb.y) != 0u && (gb.x & ga.y) != 0u)) continue;
+            // ccdBodyVisitor.visit update.ts:1153-1206
+            if (b == a) continue;
+            const int cb = w.ccd_index[b];
+            if (cb >= 0 && a > b) continue;  // a pair of cast bodies is cast once, by the lower index
+            if (fb & F_SENSOR) continue;
+            float3 rel = delta;
+            if (cb >= 0) rel = rel - xyz(w.ccd[cb].delta);
+            if (lensq3(rel) < thr_sq) continue;
+            const float3 blo = xyz(w.aabb_lo[b]) - half_a, bhi = xyz(w.aabb_hi[b]) + half_a;
+            if (!(ray_box_entry(pA, rel, sqrtf(lensq3(rel)), blo, bhi) < CUDART_INF_F)) continue;
+            // castConvexVsConvex: A in B's frame
+            const float3 pB = xyz(w.pos[b]);
+            const float4 qB = w.quat[b];
+            const Q<float> iqB{-qB.x, -qB.y, -qB.z, qB.w};
+            const V<float> posAInB = qrotS(iqB, V<float>{pA.x - pB.x, pA.y - pB.y, pA.z - pB.z});
+            const Q<float> qAInB = qmulS(iqB, Q<float>{qA.x, qA.y, qA.z, qA.w});
+            const V<float> dInB = qrotS(iqB, V<float>{rel.x, rel.y, rel.z});
+            Sup<float> supA = supA0;
+            set_transform(supA, qAInB, posAInB);
+            const Sup<float> supB = make_sup<float>(shape_of(fb), w.shape[b], true, hv);
+            float lambda;
+            V<float> cpa, cpb, ax;
+            if (!gjk_cast(lambda, cpa, cpb, ax, supA, supB, dInB, 1e-4f, supA.convex_radius, supB.convex_radius,
+                          best_fps))
+                continue;
+            // penetrationCastShape penetration.ts:693-698: a too short axis becomes the cast direction
+            if (lsq(ax) < 1e-4f * 1e-4f) ax = dInB;
+            if (lambda > 1.f || dot(ax, dInB) <= 0.f || lambda >= best_fps) continue;
+            // ccdCastShapeCollector.addHit update.ts:1044-1109
+            const Q<float> qBq{qB.x, qB.y, qB.z, qB.w};
+            const V<float> axw = qrotS(qBq, ax);
+            const float3 nrm = normalize3(f3(axw.x, axw.y, axw.z));
+            const float den = dot3(nrm, delta);
+            if (den <= max_pen) continue;
+            const float fps = lambda + max_pen / den;
+            if (!(fps < best_fps || (fps == best_fps && best >= 0 && b < best))) continue;
+            best = b;
+            best_fps = fps;
+            best_frac = lambda;
+            best_n = nrm;
+            const V<float> paw = qrotS(qBq, cpa);
+            float3 pt = f3(paw.x + pB.x, paw.y + pB.y, paw.z + pB.z);
+            // calculateBodyMotion update.ts:984-994
+            if (motion_of(fb) != STATIC && (fb & F_LINEAR_CAST)) {
+                float3 mb = xyz(w.linvel[b]) * dt;
+                if (lensq3(mb) > 1e-12f) pt = pt + mb * lambda;
+            }
+            best_p = pt;
+        }
+        if (best >= 0) {
+            c.hit = best;
+            c.fps = best_fps;
+            c.normal = make_float4(best_n.x, best_n.y, best_n.z, max_pen);
+            c.point = make_float4(best_p.x, best_p.y, best_p.z, best_frac);
+            atomicAdd(&w.ctr->num_ccd_hits, 1);
+        }
+    }
+}
+
+void launch_ccd_find(DevWorld &w, float dt, cudaStream_t s) {
+    k_ccd_find<<<grid_for(w.n, 128, 16), 128, 0, s>>>(w, w.node_world, dt);
+}
 
 void launch_narrowphase(DevWorld &w, float, cudaStream_t s, cudaEvent_t mid) {
     EpaItem *items = (EpaItem *)w.epa_items;

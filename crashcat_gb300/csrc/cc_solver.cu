@@ -18,6 +18,8 @@
 // integrates its bodies, runs the position iterations, derives positions and
 // decides sleeping for the island - the integration and sleep test are fused
 // into the last solver pass.
+#include <math_constants.h>
+
 #include "cc_internal.cuh"
 #include "cc_swing.cuh"
 
@@ -372,6 +374,7 @@ __global__ void k_uf_init(DevWorld w) {
             w.island_joint_count[i] = 0;
             w.island_fill_j[i] = 0;
         }
+        if (w.ccd_flag) w.ccd_flag[i] = 0;
     }
 }
 
@@ -680,8 +683,10 @@ __device__ bool solve_position_con(DevWorld &w, const ContactConstraint &c, Pose
     return any;
 }
 
-// velocity integration of one body (update.ts:896-976, discrete)
-__device__ void integrate_body(DevWorld &w, int i, float dt) {
+// velocity integration of one body (update.ts:896-976).  With ccd set, a LINEAR_CAST dynamic
+// non-sensor body whose step is longer than the cast threshold rotates about its position and
+// leaves its translation to the continuous-collision pass (update.ts:930-968).
+__device__ void integrate_body(DevWorld &w, int i, float dt, bool ccd) {
     uint32_t f = w.flags[i];
     int m = motion_of(f);
     if (m == STATIC || sleeping_of(f)) return;
@@ -697,6 +702,16 @@ __device__ void integrate_body(DevWorld &w, int i, float dt) {
     }
     float4 q = rotation_step(w.quat[i], av * dt);
     w.quat[i] = q;
+    if (ccd && (f & F_LINEAR_CAST) && m == DYNAMIC && !(f & F_SENSOR)) {
+        float thr = c_settings.ccd_threshold * shape_inner_radius(w, f, w.shape[i]);
+        if (lensq3(v * dt) > thr * thr) {
+            // setQuaternion rigid-body.ts:737-752: the centre of mass follows the rotation
+            float3 c = xyz(w.pos[i]) + qrot(q, shape_com(w, f, w.shape[i]));
+            w.com[i] = make_float4(c.x, c.y, c.z, 0.f);
+            w.ccd_flag[i] = 1;
+            return;
+        }
+    }
     float3 com = xyz(w.com[i]) + v * dt;
     w.com[i] = make_float4(com.x, com.y, com.z, 0.f);
 }
@@ -812,7 +827,7 @@ __global__ void k_joint_setup(DevWorld w, float dt) {
 // JOINTS: the islands with joints (their own list); the contact-only instance carries no joint code
 template <bool JOINTS>
 __global__ void __launch_bounds__(128) k_solve_small(DevWorld w, CacheTables ct, const int *small_list, float dt,
-                                                      float ratio) {
+                                                      float ratio, int phase) {
     int ns = JOINTS ? w.ctr->num_small_joint_islands : w.ctr->num_small_islands;
     CacheRecord *crecs = ct.recs[*ct.parity];
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
@@ -847,9 +862,10 @@ __global__ void __launch_bounds__(128) k_solve_small(DevWorld w, CacheTables ct,
                 jord[j + 1] = x;
             }
         }
-        for (int k = 0; k < nb; k++) prepare_body(w, bl[k]);
-        if (nc > 0 || nj > 0) {
-            if (c_settings.warm_starting) {
+        const bool vel = phase != SOLVE_POSITION;
+        if (vel) {
+            for (int k = 0; k < nb; k++) prepare_body(w, bl[k]);
+            if ((nc > 0 || nj > 0) && c_settings.warm_starting) {
                 for (int k = 0; k < nc; k++) {
                     ContactConstraint &c = w.cons[order[k]];
                     BodyRef A = load_body(w, c.a), B = load_body(w, c.b);
@@ -859,27 +875,32 @@ __global__ void __launch_bounds__(128) k_solve_small(DevWorld w, CacheTables ct,
                 }
                 for (int k = 0; k < nj; k++) joint_warm(w, jord[k], ratio);
             }
-            for (int k = 1; k < nj; k++) {  // now into solve order
-                int x = jord[k], j = k - 1;
-                while (j >= 0 && joint_before(w, x, jord[j])) {
-                    jord[j + 1] = jord[j];
-                    j--;
-                }
-                jord[j + 1] = x;
-            }
-            for (int it = 0; it < c_settings.vel_iters; it++) {
-                for (int k = 0; k < nc; k++) {
-                    ContactConstraint &c = w.cons[order[k]];
-                    BodyRef A = load_body(w, c.a), B = load_body(w, c.b);
-                    solve_velocity_con(c, A, B);
-                    store_body_vel(w, c.a, A);
-                    store_body_vel(w, c.b, B);
-                }
-                for (int k = 0; k < nj; k++) joint_solve_velocity(w, jord[k], dt);
-            }
-            for (int k = 0; k < nc; k++) store_impulses(w, crecs, w.cons[order[k]]);
         }
-        for (int k = 0; k < nb; k++) integrate_body(w, bl[k], dt);
+        for (int k = 1; k < nj; k++) {  // now into solve order
+            int x = jord[k], j = k - 1;
+            while (j >= 0 && joint_before(w, x, jord[j])) {
+                jord[j + 1] = jord[j];
+                j--;
+            }
+            jord[j + 1] = x;
+        }
+        if (vel) {
+            if (nc > 0 || nj > 0) {
+                for (int it = 0; it < c_settings.vel_iters; it++) {
+                    for (int k = 0; k < nc; k++) {
+                        ContactConstraint &c = w.cons[order[k]];
+                        BodyRef A = load_body(w, c.a), B = load_body(w, c.b);
+                        solve_velocity_con(c, A, B);
+                        store_body_vel(w, c.a, A);
+                        store_body_vel(w, c.b, B);
+                    }
+                    for (int k = 0; k < nj; k++) joint_solve_velocity(w, jord[k], dt);
+                }
+                for (int k = 0; k < nc; k++) store_impulses(w, crecs, w.cons[order[k]]);
+            }
+            for (int k = 0; k < nb; k++) integrate_body(w, bl[k], dt, phase == SOLVE_VELOCITY);
+            if (phase == SOLVE_VELOCITY) continue;
+        }
         if (nc > 0 || nj > 0) {
             for (int it = 0; it < c_settings.pos_iters; it++) {
                 bool any = false;
@@ -930,7 +951,8 @@ constexpr int JOINT_COLOURS = 64;  // joint colours of the per-CTA solve; the re
 template <bool JOINTS>
 __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTables ct, const int *large_list,
                                                               int *scratch_order, int *scratch_colour,
-                                                              int *scratch_claim, float dt, float ratio) {
+                                                              int *scratch_claim, float dt, float ratio,
+                                                              int phase) {
     __shared__ int s_any;
     __shared__ int s_ncol;
     __shared__ int s_colour_start[257];
@@ -954,7 +976,9 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
             }
             order[rank] = cl[k];
         }
-        for (int k = threadIdx.x; k < nb; k += blockDim.x) prepare_body(w, bl[k]);
+        const bool vel = phase != SOLVE_POSITION;
+        if (vel)
+            for (int k = threadIdx.x; k < nb; k += blockDim.x) prepare_body(w, bl[k]);
         // the island's joints in index order (warm start) and in (priority, index) order
         // (sortConstraintIds constraints.ts:248-261)
         int nj = JOINTS ? w.island_joint_count[isl] : 0;
@@ -1136,25 +1160,28 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
             }
         };
         // contacts, then joints (update.ts:116-165)
-        if (c_settings.warm_starting) {
-            sweep(0);
-            if (nj > 0) {
-                __syncthreads();
-                if (threadIdx.x == 0)
-                    for (int k = 0; k < nj; k++) joint_warm(w, j_idx[k], ratio);
-                __syncthreads();
+        if (vel) {
+            if (c_settings.warm_starting) {
+                sweep(0);
+                if (nj > 0) {
+                    __syncthreads();
+                    if (threadIdx.x == 0)
+                        for (int k = 0; k < nj; k++) joint_warm(w, j_idx[k], ratio);
+                    __syncthreads();
+                }
             }
-        }
-        for (int it = 0; it < c_settings.vel_iters; it++) {
-            sweep(1);
-            if (nj > 0) {
-                __syncthreads();
-                joint_sweep(0);
+            for (int it = 0; it < c_settings.vel_iters; it++) {
+                sweep(1);
+                if (nj > 0) {
+                    __syncthreads();
+                    joint_sweep(0);
+                }
             }
+            for (int k = threadIdx.x; k < nc; k += blockDim.x) store_impulses(w, crecs, w.cons[cl[k]]);
+            for (int k = threadIdx.x; k < nb; k += blockDim.x) integrate_body(w, bl[k], dt, phase == SOLVE_VELOCITY);
+            __syncthreads();
+            if (phase == SOLVE_VELOCITY) continue;
         }
-        for (int k = threadIdx.x; k < nc; k += blockDim.x) store_impulses(w, crecs, w.cons[cl[k]]);
-        for (int k = threadIdx.x; k < nb; k += blockDim.x) integrate_body(w, bl[k], dt);
-        __syncthreads();
         for (int it = 0; it < c_settings.pos_iters; it++) {
             if (threadIdx.x == 0) s_any = 0;
             __syncthreads();
@@ -1263,7 +1290,8 @@ __device__ __forceinline__ void warp_store(WarpIsland &s, int local, const BodyR
     s.av[local] = make_float4(b.w.x, b.w.y, b.w.z, s.av[local].w);
 }
 
-__global__ void __launch_bounds__(WARP_BLOCK) k_solve_warp(DevWorld w, CacheTables ct, float dt, float ratio) {
+__global__ void __launch_bounds__(WARP_BLOCK) k_solve_warp(DevWorld w, CacheTables ct, float dt, float ratio,
+                                                            int phase) {
     extern __shared__ WarpIsland s_isl[];  // WARPS_PER_BLOCK entries
     const int lane = threadIdx.x & 31;
     WarpIsland &S = s_isl[threadIdx.x >> 5];
@@ -1400,7 +1428,8 @@ __global__ void __launch_bounds__(WARP_BLOCK) k_solve_warp(DevWorld w, CacheTabl
         }
         __syncwarp();
         // warm start and velocity iterations, colour by colour
-        for (int pass = (c_settings.warm_starting ? -1 : 0); pass < c_settings.vel_iters; pass++) {
+        const bool vel = phase != SOLVE_POSITION;
+        for (int pass = (c_settings.warm_starting ? -1 : 0); vel && pass < c_settings.vel_iters; pass++) {
             for (int c = 0; c < nsweep; c++) {
                 int s0 = S.cstart[c], s1 = S.cstart[c + 1];
                 bool serial = tail && c == ncol;
@@ -1421,18 +1450,21 @@ __global__ void __launch_bounds__(WARP_BLOCK) k_solve_warp(DevWorld w, CacheTabl
                 __syncwarp();
             }
         }
-        for (int k = lane; k < nc; k += 32) store_impulses(w, crecs, w.cons[S.idx[k]]);
-        // velocities back to global memory, then integration (update.ts:896-976)
-        for (int k = lane; k < nb; k += 32) {
-            int i = S.body[k];
-            if (motion_of(__float_as_uint(S.av[k].w)) == DYNAMIC) {
-                float4 v = S.v[k], av = S.av[k];
-                w.linvel[i] = make_float4(v.x, v.y, v.z, 0.f);
-                w.angvel[i] = make_float4(av.x, av.y, av.z, 0.f);
+        if (vel) {
+            for (int k = lane; k < nc; k += 32) store_impulses(w, crecs, w.cons[S.idx[k]]);
+            // velocities back to global memory, then integration (update.ts:896-976)
+            for (int k = lane; k < nb; k += 32) {
+                int i = S.body[k];
+                if (motion_of(__float_as_uint(S.av[k].w)) == DYNAMIC) {
+                    float4 v = S.v[k], av = S.av[k];
+                    w.linvel[i] = make_float4(v.x, v.y, v.z, 0.f);
+                    w.angvel[i] = make_float4(av.x, av.y, av.z, 0.f);
+                }
+                integrate_body(w, i, dt, phase == SOLVE_VELOCITY);
             }
-            integrate_body(w, i, dt);
+            __syncwarp();
+            if (phase == SOLVE_VELOCITY) continue;
         }
-        __syncwarp();
         // position iterations (contact-constraints.ts:1098-1216), early exit as update.ts:218-221
         for (int it = 0; it < c_settings.pos_iters; it++) {
             bool any = false;
@@ -1541,7 +1573,8 @@ __device__ __forceinline__ unsigned long long joint_claim_key(const DevWorld &w,
            (unsigned)((id & JOINT_SWING) != 0);
 }
 
-__global__ void __launch_bounds__(GIANT_BLOCK) k_solve_giant(DevWorld w, CacheTables ct, float dt, float ratio) {
+__global__ void __launch_bounds__(GIANT_BLOCK) k_solve_giant(DevWorld w, CacheTables ct, float dt, float ratio,
+                                                              int phase) {
     DevCounters *ctr = w.ctr;
     const int ng = ctr->num_giant_islands;
     if (ng == 0) return;
@@ -1564,118 +1597,146 @@ __global__ void __launch_bounds__(GIANT_BLOCK) k_solve_giant(DevWorld w, CacheTa
         const int *jl = w.island_joints + (nj > 0 ? w.island_joint_off[isl] : 0);
         int *j_col = const_cast<int *>(jl) + 3 * w.max_joints;
         int *j_grp = j_col + w.max_joints;
-        for (int k = tid; k < nb; k += nthr) {
-            int b = bl[k];
-            prepare_body(w, b);
-            cclaim[0][b] = cclaim[1][b] = NONE;
-            jclaim[0][b] = jclaim[1][b] = NONE;
-        }
-        for (int k = tid; k < nc; k += nthr) colour[k] = -1;
-        for (int k = tid; k < nj; k += nthr) j_col[k] = -1;
-        for (int k = tid; k < 4 * (GIANT_COLOURS + 2); k += nthr) w.giant_count[k] = 0;
-        if (tid == 0) {
-            ctr->giant_sleep = 1;
-            ctr->giant_left[0] = ctr->giant_left[1] = 0;
-        }
-        if (!grid_barrier(ctr, nblk)) return;
-        // ---- colouring: round r uses the claims and the flag of parity r & 1 and clears the
-        // other parity's for round r + 1 ----
-        int ncol = 0, round = 0;
-        while (true) {
-            int p = round & 1;
-            int left = 0;
-            for (int k = tid; k < nc; k += nthr) {
-                if (colour[k] >= 0) continue;
-                left = 1;
-                const ContactConstraint &c = w.cons[cl[k]];
-                if (motion_of(w.flags[c.a]) == DYNAMIC) atomicMin(&cclaim[p][c.a], contact_claim_key(c, c.a));
-                if (motion_of(w.flags[c.b]) == DYNAMIC) atomicMin(&cclaim[p][c.b], contact_claim_key(c, c.b));
-            }
-            for (int k = tid; k < nj; k += nthr) {
-                if (j_col[k] >= 0) continue;
-                left = 1;
-                int id = jl[k];
-                const DevJointHead &h = joint_head(w, id);
-                unsigned long long key = joint_claim_key(w, id);
-                if (motion_of(w.flags[h.a]) == DYNAMIC) atomicMin(&jclaim[p][h.a], key);
-                if (motion_of(w.flags[h.b]) == DYNAMIC) atomicMin(&jclaim[p][h.b], key);
-            }
-            left = __syncthreads_or(left);
-            if (threadIdx.x == 0 && left) atomicOr(&ctr->giant_left[p], 1);
+        int ncol = 0;
+        if (phase == SOLVE_POSITION) {
+            // the colours of the velocity pass are kept per constraint and the constraints
+            // grouped by colour: rebuild the colour offsets from them
+            for (int k = tid; k < 4 * (GIANT_COLOURS + 2); k += nthr) w.giant_count[k] = 0;
             if (!grid_barrier(ctr, nblk)) return;
-            if (!*(volatile int *)&ctr->giant_left[p]) break;
-            if (tid == 0) ctr->giant_left[p ^ 1] = 0;
-            bool last = ncol == GIANT_COLOURS;  // the overflow colour takes everything left
             for (int k = tid; k < nc; k += nthr) {
-                if (colour[k] >= 0) continue;
-                const ContactConstraint &c = w.cons[cl[k]];
-                bool ok = last || ((motion_of(w.flags[c.a]) != DYNAMIC || cclaim[p][c.a] == contact_claim_key(c, c.a)) &&
-                                   (motion_of(w.flags[c.b]) != DYNAMIC || cclaim[p][c.b] == contact_claim_key(c, c.b)));
-                if (ok) {
-                    colour[k] = ncol;
-                    atomicAdd(&c_off[ncol + 1], 1);
-                }
+                atomicAdd(&c_off[colour[k] + 1], 1);
+                atomicMax(&c_fill[0], colour[k] + 1);
             }
             for (int k = tid; k < nj; k += nthr) {
-                if (j_col[k] >= 0) continue;
-                int id = jl[k];
-                const DevJointHead &h = joint_head(w, id);
-                unsigned long long key = joint_claim_key(w, id);
-                bool ok = last || ((motion_of(w.flags[h.a]) != DYNAMIC || jclaim[p][h.a] == key) &&
-                                   (motion_of(w.flags[h.b]) != DYNAMIC || jclaim[p][h.b] == key));
-                if (ok) {
-                    j_col[k] = ncol;
-                    atomicAdd(&j_off[ncol + 1], 1);
-                }
+                atomicAdd(&j_off[j_col[k] + 1], 1);
+                atomicMax(&c_fill[0], j_col[k] + 1);
             }
+            if (!grid_barrier(ctr, nblk)) return;
+            ncol = *(volatile int *)&c_fill[0];
+            if (tid == 0)
+                for (int c = 0; c < ncol; c++) {
+                    c_off[c + 1] += c_off[c];
+                    j_off[c + 1] += j_off[c];
+                }
+            if (tid == 0) {
+                ctr->giant_sleep = 1;
+                ctr->giant_any[0] = ctr->giant_any[1] = 0;
+            }
+            if (!grid_barrier(ctr, nblk)) return;
+        } else {
             for (int k = tid; k < nb; k += nthr) {
                 int b = bl[k];
-                cclaim[p ^ 1][b] = NONE;
-                jclaim[p ^ 1][b] = NONE;
+                prepare_body(w, b);
+                cclaim[0][b] = cclaim[1][b] = NONE;
+                jclaim[0][b] = jclaim[1][b] = NONE;
             }
-            ncol++;
-            round++;
+            for (int k = tid; k < nc; k += nthr) colour[k] = -1;
+            for (int k = tid; k < nj; k += nthr) j_col[k] = -1;
+            for (int k = tid; k < 4 * (GIANT_COLOURS + 2); k += nthr) w.giant_count[k] = 0;
+            if (tid == 0) {
+                ctr->giant_sleep = 1;
+                ctr->giant_left[0] = ctr->giant_left[1] = 0;
+            }
             if (!grid_barrier(ctr, nblk)) return;
-        }
-        // ---- group by colour: offsets, then a scatter (any order inside a colour) ----
-        if (tid == 0) {
-            atomicMax(&ctr->giant_colours, ncol);
-            for (int c = 0; c < ncol; c++) {
-                c_off[c + 1] += c_off[c];
-                j_off[c + 1] += j_off[c];
-            }
-            for (int c = 0; c <= ncol; c++) {
-                c_fill[c] = c_off[c];
-                j_fill[c] = j_off[c];
-            }
-        }
-        if (!grid_barrier(ctr, nblk)) return;
-        for (int k = tid; k < nc; k += nthr) c_grp[atomicAdd(&c_fill[colour[k]], 1)] = cl[k];
-        for (int k = tid; k < nj; k += nthr) j_grp[atomicAdd(&j_fill[j_col[k]], 1)] = jl[k];
-        if (!grid_barrier(ctr, nblk)) return;
-        if (ncol > GIANT_COLOURS && tid == 0) {
-            // the overflow colour is solved in order by one thread: sort it by the order key
-            int s0 = c_off[GIANT_COLOURS], s1 = c_off[GIANT_COLOURS + 1];
-            for (int k = s0 + 1; k < s1; k++) {
-                int x = c_grp[k], j = k - 1;
-                while (j >= s0 && con_less(w.cons[x], w.cons[c_grp[j]])) {
-                    c_grp[j + 1] = c_grp[j];
-                    j--;
+            // ---- colouring: round r uses the claims and the flag of parity r & 1 and clears the
+            // other parity's for round r + 1 ----
+            int round = 0;
+            while (true) {
+                int p = round & 1;
+                int left = 0;
+                for (int k = tid; k < nc; k += nthr) {
+                    if (colour[k] >= 0) continue;
+                    left = 1;
+                    const ContactConstraint &c = w.cons[cl[k]];
+                    if (motion_of(w.flags[c.a]) == DYNAMIC) atomicMin(&cclaim[p][c.a], contact_claim_key(c, c.a));
+                    if (motion_of(w.flags[c.b]) == DYNAMIC) atomicMin(&cclaim[p][c.b], contact_claim_key(c, c.b));
                 }
-                c_grp[j + 1] = x;
-            }
-            s0 = j_off[GIANT_COLOURS];
-            s1 = j_off[GIANT_COLOURS + 1];
-            for (int k = s0 + 1; k < s1; k++) {
-                int x = j_grp[k], j = k - 1;
-                while (j >= s0 && joint_before(w, x, j_grp[j])) {
-                    j_grp[j + 1] = j_grp[j];
-                    j--;
+                for (int k = tid; k < nj; k += nthr) {
+                    if (j_col[k] >= 0) continue;
+                    left = 1;
+                    int id = jl[k];
+                    const DevJointHead &h = joint_head(w, id);
+                    unsigned long long key = joint_claim_key(w, id);
+                    if (motion_of(w.flags[h.a]) == DYNAMIC) atomicMin(&jclaim[p][h.a], key);
+                    if (motion_of(w.flags[h.b]) == DYNAMIC) atomicMin(&jclaim[p][h.b], key);
                 }
-                j_grp[j + 1] = x;
+                left = __syncthreads_or(left);
+                if (threadIdx.x == 0 && left) atomicOr(&ctr->giant_left[p], 1);
+                if (!grid_barrier(ctr, nblk)) return;
+                if (!*(volatile int *)&ctr->giant_left[p]) break;
+                if (tid == 0) ctr->giant_left[p ^ 1] = 0;
+                bool last = ncol == GIANT_COLOURS;  // the overflow colour takes everything left
+                for (int k = tid; k < nc; k += nthr) {
+                    if (colour[k] >= 0) continue;
+                    const ContactConstraint &c = w.cons[cl[k]];
+                    bool ok = last || ((motion_of(w.flags[c.a]) != DYNAMIC || cclaim[p][c.a] == contact_claim_key(c, c.a)) &&
+                                       (motion_of(w.flags[c.b]) != DYNAMIC || cclaim[p][c.b] == contact_claim_key(c, c.b)));
+                    if (ok) {
+                        colour[k] = ncol;
+                        atomicAdd(&c_off[ncol + 1], 1);
+                    }
+                }
+                for (int k = tid; k < nj; k += nthr) {
+                    if (j_col[k] >= 0) continue;
+                    int id = jl[k];
+                    const DevJointHead &h = joint_head(w, id);
+                    unsigned long long key = joint_claim_key(w, id);
+                    bool ok = last || ((motion_of(w.flags[h.a]) != DYNAMIC || jclaim[p][h.a] == key) &&
+                                       (motion_of(w.flags[h.b]) != DYNAMIC || jclaim[p][h.b] == key));
+                    if (ok) {
+                        j_col[k] = ncol;
+                        atomicAdd(&j_off[ncol + 1], 1);
+                    }
+                }
+                for (int k = tid; k < nb; k += nthr) {
+                    int b = bl[k];
+                    cclaim[p ^ 1][b] = NONE;
+                    jclaim[p ^ 1][b] = NONE;
+                }
+                ncol++;
+                round++;
+                if (!grid_barrier(ctr, nblk)) return;
             }
-        }
-        if (!grid_barrier(ctr, nblk)) return;
+            // ---- group by colour: offsets, then a scatter (any order inside a colour) ----
+            if (tid == 0) {
+                atomicMax(&ctr->giant_colours, ncol);
+                for (int c = 0; c < ncol; c++) {
+                    c_off[c + 1] += c_off[c];
+                    j_off[c + 1] += j_off[c];
+                }
+                for (int c = 0; c <= ncol; c++) {
+                    c_fill[c] = c_off[c];
+                    j_fill[c] = j_off[c];
+                }
+            }
+            if (!grid_barrier(ctr, nblk)) return;
+            for (int k = tid; k < nc; k += nthr) c_grp[atomicAdd(&c_fill[colour[k]], 1)] = cl[k];
+            for (int k = tid; k < nj; k += nthr) j_grp[atomicAdd(&j_fill[j_col[k]], 1)] = jl[k];
+            if (!grid_barrier(ctr, nblk)) return;
+            if (ncol > GIANT_COLOURS && tid == 0) {
+                // the overflow colour is solved in order by one thread: sort it by the order key
+                int s0 = c_off[GIANT_COLOURS], s1 = c_off[GIANT_COLOURS + 1];
+                for (int k = s0 + 1; k < s1; k++) {
+                    int x = c_grp[k], j = k - 1;
+                    while (j >= s0 && con_less(w.cons[x], w.cons[c_grp[j]])) {
+                        c_grp[j + 1] = c_grp[j];
+                        j--;
+                    }
+                    c_grp[j + 1] = x;
+                }
+                s0 = j_off[GIANT_COLOURS];
+                s1 = j_off[GIANT_COLOURS + 1];
+                for (int k = s0 + 1; k < s1; k++) {
+                    int x = j_grp[k], j = k - 1;
+                    while (j >= s0 && joint_before(w, x, j_grp[j])) {
+                        j_grp[j + 1] = j_grp[j];
+                        j--;
+                    }
+                    j_grp[j + 1] = x;
+                }
+            }
+            if (!grid_barrier(ctr, nblk)) return;
+        }  // velocity pass: colouring
         // one pass over the colours of one kind: mode 0 warm start, 1 velocity, 2 position
         auto sweep = [&](bool joints, int mode, int &any) -> bool {
             const int *off = joints ? j_off : c_off;
@@ -1724,16 +1785,19 @@ __global__ void __launch_bounds__(GIANT_BLOCK) k_solve_giant(DevWorld w, CacheTa
             }
             return true;
         };
-        int dummy = 0;
-        if (c_settings.warm_starting) {
-            if (!sweep(false, 0, dummy) || !sweep(true, 0, dummy)) return;
+        if (phase != SOLVE_POSITION) {
+            int dummy = 0;
+            if (c_settings.warm_starting) {
+                if (!sweep(false, 0, dummy) || !sweep(true, 0, dummy)) return;
+            }
+            for (int it = 0; it < c_settings.vel_iters; it++)
+                if (!sweep(false, 1, dummy) || !sweep(true, 1, dummy)) return;
+            for (int k = tid; k < nc; k += nthr) store_impulses(w, crecs, w.cons[cl[k]]);
+            for (int k = tid; k < nb; k += nthr) integrate_body(w, bl[k], dt, phase == SOLVE_VELOCITY);
+            if (tid == 0) ctr->giant_any[0] = ctr->giant_any[1] = 0;
+            if (!grid_barrier(ctr, nblk)) return;
+            if (phase == SOLVE_VELOCITY) continue;
         }
-        for (int it = 0; it < c_settings.vel_iters; it++)
-            if (!sweep(false, 1, dummy) || !sweep(true, 1, dummy)) return;
-        for (int k = tid; k < nc; k += nthr) store_impulses(w, crecs, w.cons[cl[k]]);
-        for (int k = tid; k < nb; k += nthr) integrate_body(w, bl[k], dt);
-        if (tid == 0) ctr->giant_any[0] = ctr->giant_any[1] = 0;
-        if (!grid_barrier(ctr, nblk)) return;
         for (int it = 0; it < c_settings.pos_iters; it++) {
             int p = it & 1, any = 0;
             if (!sweep(false, 2, any) || !sweep(true, 2, any)) return;
@@ -1832,11 +1896,14 @@ void launch_contacts_and_islands(DevWorld &w, float dt, float, cudaStream_t s) {
     if (nj > 0 && dt > 0.f) k_joint_setup<<<grid_for(nj, 128), 128, 0, s>>>(w, dt);
 }
 
-void launch_solver(DevWorld &w, float dt, float ratio, cudaStream_t s, cudaEvent_t mid) {
+void launch_solver(DevWorld &w, float dt, float ratio, cudaStream_t s, cudaEvent_t mid, int phase) {
     CacheTables ct = tables_of(w);
     const bool joints = w.num_hinges + w.num_swings > 0;
-    k_solve_small<false><<<grid_for(w.n, 128, 16), 128, 0, s>>>(w, ct, w.small_list, dt, ratio);
-    if (joints) k_solve_small<true><<<grid_for(w.n, 128, 16), 128, 0, s>>>(w, ct, w.small_joint_list, dt, ratio);
+    // the per-warp tier takes its islands from a cursor: rewind it for the second pass
+    if (phase == SOLVE_POSITION) cudaMemsetAsync(&w.ctr->mid_cursor, 0, sizeof(int), s);
+    k_solve_small<false><<<grid_for(w.n, 128, 16), 128, 0, s>>>(w, ct, w.small_list, dt, ratio, phase);
+    if (joints)
+        k_solve_small<true><<<grid_for(w.n, 128, 16), 128, 0, s>>>(w, ct, w.small_joint_list, dt, ratio, phase);
     if (mid) cudaEventRecord(mid, s);
     static bool warp_smem_set = false;  // set on the first (eager) step, before any graph capture
     const size_t warp_smem = sizeof(WarpIsland) * WARPS_PER_BLOCK;
@@ -1849,14 +1916,13 @@ void launch_solver(DevWorld &w, float dt, float ratio, cudaStream_t s, cudaEvent
     // the per-CTA and per-warp classes hold disjoint islands: run them side by side
     cudaEventRecord(w.ev_fork, s);
     cudaStreamWaitEvent(w.aux_stream, w.ev_fork, 0);
-    k_solve_large<false><<<NUM_SMS * 2, LARGE_BLOCK, 0, w.aux_stream>>>(w, ct, w.large_list, w.scratch_order,
-                                                                        w.scratch_colour, w.scratch_claim, dt, ratio);
+    k_solve_large<false><<<NUM_SMS * 2, LARGE_BLOCK, 0, w.aux_stream>>>(
+        w, ct, w.large_list, w.scratch_order, w.scratch_colour, w.scratch_claim, dt, ratio, phase);
     if (joints)
-        k_solve_large<true><<<NUM_SMS * 2, LARGE_BLOCK, 0, w.aux_stream>>>(w, ct, w.large_joint_list, w.scratch_order,
-                                                                           w.scratch_colour, w.scratch_claim, dt,
-                                                                           ratio);
+        k_solve_large<true><<<NUM_SMS * 2, LARGE_BLOCK, 0, w.aux_stream>>>(
+            w, ct, w.large_joint_list, w.scratch_order, w.scratch_colour, w.scratch_claim, dt, ratio, phase);
     cudaEventRecord(w.ev_join, w.aux_stream);
-    k_solve_warp<<<NUM_SMS * w.warp_blocks_per_sm, WARP_BLOCK, warp_smem, s>>>(w, ct, dt, ratio);
+    k_solve_warp<<<NUM_SMS * w.warp_blocks_per_sm, WARP_BLOCK, warp_smem, s>>>(w, ct, dt, ratio, phase);
     cudaStreamWaitEvent(s, w.ev_join, 0);
     // giant islands: a cooperative launch (all blocks co-resident), after the other tiers so that
     // it runs alone; it returns at once when the step has no giant island
@@ -1869,7 +1935,182 @@ void launch_solver(DevWorld &w, float dt, float ratio, cudaStream_t s, cudaEvent
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (w.giant_blocks > 0) cudaLaunchKernelEx(&cfg, k_solve_giant, w, ct, dt, ratio);
+    if (w.giant_blocks > 0) cudaLaunchKernelEx(&cfg, k_solve_giant, w, ct, dt, ratio, phase);
+}
+
+// ---------------------------------------------------------------------------
+// continuous collision: the records of each world resolved in time-of-impact order
+// ---------------------------------------------------------------------------
+template <class Less>
+__device__ void heap_sort(int *a, int m, Less less) {
+    auto sift = [&](int root, int end) {
+        while (true) {
+            int ch = 2 * root + 1;
+            if (ch >= end) return;
+            if (ch + 1 < end && less(a[ch], a[ch + 1])) ch++;
+            if (!less(a[root], a[ch])) return;
+            int t = a[root];
+            a[root] = a[ch];
+            a[ch] = t;
+            root = ch;
+        }
+    };
+    for (int i = m / 2 - 1; i >= 0; i--) sift(i, m);
+    for (int end = m - 1; end > 0; end--) {
+        int t = a[0];
+        a[0] = a[end];
+        a[end] = t;
+        sift(0, end);
+    }
+}
+
+__device__ __forceinline__ float3 masked_lin(float3 v, int dof) {
+    if (!(dof & 1)) v.x = 0.f;
+    if (!(dof & 2)) v.y = 0.f;
+    if (!(dof & 4)) v.z = 0.f;
+    return v;
+}
+
+// applyCCD update.ts:1420-1580: at the time of impact, one unbounded normal iteration (with
+// restitution above the velocity threshold) and one friction iteration along the tangential
+// relative velocity, bounded by the friction times the normal part's accumulated lambda.  The
+// two parts keep their accumulated lambdas from one call to the next (module scope in the
+// reference); lam carries them for the world.  For a body B that is not dynamic the part's
+// B-side arm is zero, which the reference leaves at its previous value.
+__device__ void ccd_apply(DevWorld &w, const CcdRec &c, int a, int b, float2 &lam) {
+    const uint32_t fa = w.flags[a], fb = w.flags[b];
+    if (motion_of(fa) != DYNAMIC) return;
+    const int mb = motion_of(fb);
+    const bool bmov = mb != STATIC, bdyn = mb == DYNAMIC;
+    const float3 n = xyz(c.normal), pt = xyz(c.point);
+    const float3 r1 = pt - (xyz(w.com[a]) + xyz(c.delta) * c.point.w);
+    const float3 r2 = pt - xyz(w.com[b]);
+    float3 va = xyz(w.linvel[a]), wa = xyz(w.angvel[a]);
+    float3 vb = bmov ? xyz(w.linvel[b]) : f3(0.f, 0.f, 0.f), wb = bmov ? xyz(w.angvel[b]) : f3(0.f, 0.f, 0.f);
+    const float3 rel = (vb + cross3(wb, r2)) - (va + cross3(wa, r1));
+    const float nv = dot3(rel, n);
+    if (nv >= 0.f) return;
+    const float4 mta = w.material[a], mtb = w.material[b];
+    const float friction = combine(mta.x, mtb.x, (fa >> F_FCOMB_SHIFT) & 7, (fb >> F_FCOMB_SHIFT) & 7);
+    const float restitution = combine(mta.y, mtb.y, (fa >> F_RCOMB_SHIFT) & 7, (fb >> F_RCOMB_SHIFT) & 7);
+    const float bias = (restitution > 0.f && nv < -c_settings.ccd_min_vel_restitution) ? restitution * nv : 0.f;
+    const float imA = w.inv_inertia[a].w, imB = bdyn ? w.inv_inertia[b].w : 0.f;
+    const int da = dof_of(fa), db = dof_of(fb);
+    const Sym3 IA = world_inv_inertia(w.quat[a], w.inertia_rot[a], xyz(w.inv_inertia[a]), da);
+    const Sym3 IB = bdyn ? world_inv_inertia(w.quat[b], w.inertia_rot[b], xyz(w.inv_inertia[b]), db)
+                         : Sym3{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    // one AxisConstraintPart: properties (calculateConstraintPropertiesWithMassOverride
+    // axis-constraint-part.ts:222-270), total lambda, clamp and apply (:725-740); returns the
+    // new accumulated lambda
+    auto part = [&](float3 ax, float bias_v, float total, float lo, float hi) -> float {
+        const float3 c1 = cross3(r1, ax), c2 = bdyn ? cross3(r2, ax) : f3(0.f, 0.f, 0.f);
+        const float3 i1 = symmul(IA, c1), i2 = symmul(IB, c2);
+        const float iem = imA + dot3(i1, c1) + (bdyn ? imB + dot3(i2, c2) : 0.f);
+        if (iem == 0.f) return 0.f;  // deactivated part: no impulse, lambda reset
+        const float eff = 1.f / iem;
+        float jv = dot3(ax, va - vb) + dot3(c1, wa);
+        if (bmov) jv -= dot3(c2, wb);
+        float tl = fmaxf(lo, fminf(hi, total + eff * (jv - bias_v)));
+        const float dl = tl - total;
+        if (dl != 0.f) {
+            va = masked_lin(va - ax * (dl * imA), da);
+            wa = wa - i1 * dl;
+            if (bdyn) {
+                vb = masked_lin(vb + ax * (dl * imB), db);
+                wb = wb + i2 * dl;
+            }
+        }
+        return tl;
+    };
+    lam.x = part(n, bias, lam.x, -CUDART_INF_F, CUDART_INF_F);
+    if (friction > 0.f) {
+        const float3 tv = rel - n * nv;
+        const float tl2 = lensq3(tv);
+        if (tl2 > 1e-12f) {
+            const float mf = friction * lam.x;
+            lam.y = part(tv * (1.f / sqrtf(tl2)), 0.f, lam.y, -mf, mf);
+        }
+    }
+    // clampLinearVelocity / clampAngularVelocity motion-properties.ts:624-639
+    auto clamp_store = [&](int i, float3 v, float3 av) {
+        const float4 d = w.damping[i];
+        if (lensq3(v) > d.z * d.z) v = normalize3(v) * d.z;
+        if (lensq3(av) > d.w * d.w) av = normalize3(av) * d.w;
+        w.linvel[i] = make_float4(v.x, v.y, v.z, 0.f);
+        w.angvel[i] = make_float4(av.x, av.y, av.z, 0.f);
+    };
+    clamp_store(a, va, wa);
+    if (bdyn) clamp_store(b, vb, wb);
+}
+
+// records into their world's segment
+__global__ void k_ccd_scatter(DevWorld w) {
+    const int nr = w.ctr->num_ccd;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nr; r += gridDim.x * blockDim.x) {
+        int wd = w.world[w.ccd[r].body];
+        w.ccd_seg[w.ccd_world_off[wd] + atomicAdd(&w.ccd_world_fill[wd], 1)] = r;
+    }
+}
+
+// sortCCDBodies update.ts:1583-1611 and resolveCCDContacts update.ts:1616-1670, one thread per
+// world.  A body's record index names its slot in creation (body index) order; after the sort
+// the cascade reads the record that now sits in that slot, as the reference does.
+__global__ void k_ccd_resolve(DevWorld w) {
+    if (w.ctr->num_ccd == 0) return;
+    CcdRec *rec = w.ccd;
+    for (int wd = blockIdx.x * blockDim.x + threadIdx.x; wd < w.num_worlds; wd += gridDim.x * blockDim.x) {
+        const int o0 = w.ccd_world_off[wd], m = w.ccd_world_off[wd + 1] - o0;
+        if (m <= 0) continue;
+        int *seg = w.ccd_seg + o0;
+        heap_sort(seg, m, [&](int x, int y) { return rec[x].body < rec[y].body; });
+        for (int k = 0; k < m; k++) rec[seg[k]].slot = k;
+        heap_sort(seg, m, [&](int x, int y) {
+            if (rec[x].fps != rec[y].fps) return rec[x].fps < rec[y].fps;
+            return rec[x].body < rec[y].body;
+        });
+        float2 lam = w.ccd_lambda[wd];
+        for (int k = 0; k < m; k++) {
+            CcdRec &c = rec[seg[k]];
+            const int a = c.body;
+            float move = 1.f;  // no hit: the whole displacement
+            if (c.hit >= 0) {
+                const int b = c.hit;
+                const int bi = w.ccd_index[b];
+                if (bi >= 0) {
+                    CcdRec &cb = rec[seg[rec[bi].slot]];
+                    if (cb.hit >= 0 && cb.point.w > c.point.w) {
+                        cb.hit = -1;
+                        cb.fps = c.point.w;
+                    }
+                }
+                ccd_apply(w, c, a, b, lam);
+                move = c.fps;
+                if (sleeping_of(w.flags[b])) {
+                    w.flags[b] &= ~F_SLEEPING;
+                    reset_sleep(w, b);
+                }
+            }
+            const uint32_t fa = w.flags[a];
+            const float3 p = xyz(w.pos[a]) + xyz(c.delta) * move;
+            const float3 cm = p + qrot(w.quat[a], shape_com(w, fa, w.shape[a]));
+            w.pos[a] = make_float4(p.x, p.y, p.z, 0.f);
+            w.com[a] = make_float4(cm.x, cm.y, cm.z, 0.f);
+        }
+        w.ccd_lambda[wd] = lam;
+    }
+}
+
+// the continuous-collision pass between the velocity and position solves (update.ts:174-184)
+void launch_ccd(DevWorld &w, float dt, cudaStream_t s) {
+    exclusive_scan_int(w.ccd_flag, w.ccd_slot, w.n, &w.ctr->num_ccd, w.scan_tmp, s);
+    cudaMemsetAsync(w.ccd_world_fill, 0, sizeof(int) * (size_t)w.num_worlds, s);
+    launch_ccd_bounds(w, dt, s);
+    launch_ccd_find(w, dt, s);
+    exclusive_scan_int(w.ccd_world_fill, w.ccd_world_off, w.num_worlds, w.ccd_world_off + w.num_worlds,
+                       w.ccd_scan_tmp, s);
+    cudaMemsetAsync(w.ccd_world_fill, 0, sizeof(int) * (size_t)w.num_worlds, s);
+    k_ccd_scatter<<<grid_for(w.n, 256), 256, 0, s>>>(w);
+    k_ccd_resolve<<<grid_for(w.num_worlds, 64), 64, 0, s>>>(w);
 }
 
 // blocks of the giant-island launch: one per SM, fewer if the kernel cannot be resident at that

@@ -90,6 +90,22 @@ static void drop_graph(cc_world *W) {
     }
 }
 
+// continuous-collision buffers, made when the first LINEAR_CAST body arrives
+static int ensure_ccd_buffers(cc_world *W) {
+    DevWorld &w = W->w;
+    if (w.ccd) return CC_OK;
+    const size_t cap = (size_t)w.cap, nw = (size_t)w.num_worlds;
+    int r;
+    if ((r = dalloc(&w.ccd_flag, cap)) != CC_OK || (r = dalloc(&w.ccd_slot, cap)) != CC_OK ||
+        (r = dalloc(&w.ccd_index, cap)) != CC_OK || (r = dalloc(&w.ccd_seg, cap)) != CC_OK ||
+        (r = dalloc(&w.ccd_world_off, nw + 1)) != CC_OK || (r = dalloc(&w.ccd_world_fill, nw)) != CC_OK ||
+        (r = dalloc(&w.ccd_lambda, nw)) != CC_OK || (r = dalloc(&w.ccd, cap)) != CC_OK ||
+        (r = dalloc(&w.ccd_scan_tmp, scan_tmp_ints((int)nw + 1))) != CC_OK)
+        return r;
+    drop_graph(W);
+    return CC_OK;
+}
+
 // FP64 vector and quaternion helpers of the host-side shape and joint set-up
 namespace {
 struct D3 {
@@ -232,6 +248,9 @@ int cc_world_settings_default(cc_world_settings *o) {
     o->broadphase_pairs[1] = 0b01;
     o->max_bodies = 1 << 16;
     o->num_worlds = 1;
+    o->ccd_linear_cast_threshold = 0.05;  // world-settings.ts:258-262
+    o->ccd_linear_cast_max_penetration = 0.25;
+    o->ccd_min_velocity_for_restitution = 1.0;
     return CC_OK;
 }
 
@@ -263,6 +282,9 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
     d.allow_sleeping = s->allow_sleeping;
     d.time_before_sleep = (float)s->time_before_sleep;
     d.sleep_threshold = (float)s->point_velocity_sleep_threshold;
+    d.ccd_threshold = (float)s->ccd_linear_cast_threshold;
+    d.ccd_max_penetration = (float)s->ccd_linear_cast_max_penetration;
+    d.ccd_min_vel_restitution = (float)s->ccd_min_velocity_for_restitution;
     // launch-shape tunable: islands with at most this many contacts are solved by one
     // thread in the reference's exact order, larger ones by a warp (up to 256 contacts
     // and 128 bodies) or a CTA with order-preserving graph colouring
@@ -290,6 +312,11 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
             if (ok) m |= 1u << b;
         }
         d.allowed_pairs[a] = m;
+        uint32_t mc = 0;
+        for (int b = 0; b < s->num_object_layers; b++)
+            if (((s->object_pairs[a] >> b) & 1) && ((s->object_vs_broadphase[a] >> s->object_to_broadphase[b]) & 1))
+                mc |= 1u << b;
+        d.cast_pairs[a] = mc;
     }
     DevWorld &w = W->w;
     memset(&w, 0, sizeof(w));
@@ -480,7 +507,8 @@ int cc_world_destroy(cc_world *W) {
                     w.island_joint_off, w.island_fill_j, w.joint_wake, w.joint_partners, w.swings,
                     w.giant_list, w.giant_claim, w.giant_count, w.small_joint_list, w.large_joint_list,
                     w.hulls, w.hull_points, w.hull_shrunk,
-                    w.hull_planes, w.hull_faces, w.hull_vidx};
+                    w.hull_planes, w.hull_faces, w.hull_vidx, w.ccd_flag, w.ccd_slot, w.ccd_index, w.ccd,
+                    w.ccd_world_off, w.ccd_world_fill, w.ccd_seg, w.ccd_lambda, w.ccd_scan_tmp};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : W->adj.allocs)
@@ -532,6 +560,7 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
         if (d.shape_type == CC_SHAPE_CAPSULE && !(d.shape_params[0] > 0.f && d.shape_params[1] > 0.f))
             return CC_ERR_INVALID;  // capsule.ts:55-61
         if (d.motion_type < 0 || d.motion_type > 2) return CC_ERR_INVALID;
+        if (d.motion_quality != CC_MOTION_DISCRETE && d.motion_quality != CC_MOTION_LINEAR_CAST) return CC_ERR_INVALID;
         if (d.object_layer < 0 || d.object_layer >= W->settings.num_object_layers) return CC_ERR_INVALID;
         if (d.world < 0 || d.world >= w.num_worlds) return CC_ERR_INVALID;
         double mass;
@@ -617,6 +646,7 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
         f |= (uint32_t)(d.friction_combine & 7) << F_FCOMB_SHIFT;
         f |= (uint32_t)(d.restitution_combine & 7) << F_RCOMB_SHIFT;
         f |= (uint32_t)(d.object_layer & 31) << F_LAYER_SHIFT;
+        if (d.motion_quality == CC_MOTION_LINEAR_CAST) f |= F_LINEAR_CAST;
         flags[i] = f;
         groups[i] = make_uint2(d.collision_groups, d.collision_mask);
         world[i] = d.world;
@@ -667,6 +697,13 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
     CC_TRY(cudaMemcpyAsync(w.sleep_sph + 3 * o, sph.data(), sizeof(float4) * 3 * n, cudaMemcpyHostToDevice, s));
     CC_TRY(cudaMemcpyAsync(w.sleep_timer + o, timer.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
     CC_TRY(cudaStreamSynchronize(s));
+    int lc = 0;
+    for (int i = 0; i < n; i++) lc += (flags[i] & F_LINEAR_CAST) != 0;
+    if (lc > 0) {
+        int r = ensure_ccd_buffers(W);
+        if (r != CC_OK) return r;
+    }
+    w.num_linear_cast += lc;
     w.n += n;
     drop_graph(W);  // body count changed: the captured step graph no longer matches
     return CC_OK;
@@ -695,7 +732,17 @@ static void enqueue_step(cc_world *W, float dt, float ratio, cudaEvent_t *ev = n
     launch_contacts_and_islands(w, dt, ratio, s);
     if (tape) launch_tape_record(w, *tape, s);
     mark(5);
-    if (dt > 0.f) launch_solver(w, dt, ratio, s, ev ? ev[6] : nullptr);
+    if (dt > 0.f) {
+        if (w.num_linear_cast > 0) {
+            // LINEAR_CAST bodies: velocities and integration, the continuous-collision pass, then
+            // the position solve (update.ts:168-227)
+            launch_solver(w, dt, ratio, s, ev ? ev[6] : nullptr, SOLVE_VELOCITY);
+            launch_ccd(w, dt, s);
+            launch_solver(w, dt, ratio, s, nullptr, SOLVE_POSITION);
+        } else {
+            launch_solver(w, dt, ratio, s, ev ? ev[6] : nullptr);
+        }
+    }
     if (ev && !(dt > 0.f)) mark(6);
     mark(7);
     cudaMemcpyAsync(W->h_ctr, w.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s);
@@ -1029,6 +1076,8 @@ int cc_world_get_stats(cc_world *W, cc_stats *o) {
     o->last_call_ms = W->last_call_ms;
     o->num_giant_islands = c.num_giant_islands;
     o->giant_colours = c.giant_colours;
+    o->num_ccd = c.num_ccd;
+    o->num_ccd_hits = c.num_ccd_hits;
     return CC_OK;
 }
 
@@ -1122,7 +1171,8 @@ extern "C" int cc_world_rollout_grad(cc_world *W, float dt, int32_t n_steps, int
     if (!W || !targets || n_steps <= 0 || checkpoint_every <= 0 || !(dt > 0.f)) return CC_ERR_INVALID;
     DevWorld &w = W->w;
     if (w.n == 0) return CC_ERR_INVALID;
-    if (w.num_hinges > 0) return CC_ERR_UNSUPPORTED;  // the adjoint covers contacts only
+    // the adjoint covers contacts and the discrete integration only
+    if (w.num_hinges + w.num_swings > 0 || w.num_linear_cast > 0) return CC_ERR_UNSUPPORTED;
     int K = checkpoint_every < n_steps ? checkpoint_every : n_steps;
     int nseg = (n_steps + K - 1) / K;
     int r = ensure_adjoint(W, K, nseg + 1);

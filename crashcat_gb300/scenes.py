@@ -719,3 +719,84 @@ def mixed_convex_pile(n: int = 400, seed: int = 2, extent: float = 12.0, heights
     b["friction"][idx] = 0.5
     return Scene("mixed_convex_pile", b, dt=1.0 / 60.0, steps=300, velocity_iterations=8, position_iterations=2,
                  seed=seed, hull_points=hulls)
+
+
+def ccd_gallery(num_worlds: int = 1, seed: int = 101, arrival_steps: int = 3) -> Scene:
+    """Fast LINEAR_CAST bodies (MotionQuality.LINEAR_CAST, update.ts:930-968) against thin walls,
+    per world:
+
+    * a static floor and a static wall 10 cm thick (half extents 0.05 x 3 x 6) at x = 8;
+    * five bullets of every shape (spheres of radius 0.12-0.2, a spinning box, a capsule, a
+      convex hull) at 150-260 m/s, aimed at the wall at small angles;
+    * a bullet with restitution 0.6 (it bounces off the wall);
+    * a dynamic box in front of the wall hit by one bullet (impulse into a dynamic body);
+    * two bullets flying head-on into each other (a pair of cast bodies, z = 10).
+
+    The dynamic box is LINEAR_CAST too: at rest it stays below the cast threshold and moves
+    discretely, once hit it is cast.
+
+    The bullets start far enough back to arrive after about ``arrival_steps`` steps at 60 Hz.
+    Hull points: one ellipsoid per world (hull index = world).
+    """
+    rng = np.random.default_rng(seed)
+    per = 12
+    n = per * num_worlds
+    b = blank_bodies(n)
+    hulls = []
+    for wd in range(num_worlds):
+        o = wd * per
+        b["world"][o:o + per] = wd
+        static_floor(b, o, half=(40.0, 0.5, 40.0), world=wd)
+        set_box(b, o + 1, (0.05, 3.0, 6.0))
+        b["motion_type"][o + 1] = STATIC
+        b["object_layer"][o + 1] = LAYER_NOT_MOVING
+        b["position"][o + 1] = (8.0, 3.0, 0.0)
+        hulls.append(ellipsoid_hull_points(rng, 20, (0.15, 0.12, 0.1)))
+        bullets = range(o + 2, o + 7)
+        for k, i in enumerate(bullets):
+            speed = rng.uniform(150.0, 260.0)
+            y = 1.0 + 0.8 * k
+            z = rng.uniform(-3.0, 3.0)
+            ang = rng.uniform(-0.25, 0.25)
+            d = np.array([math.cos(ang), rng.uniform(-0.05, 0.05), math.sin(ang)])
+            d /= np.linalg.norm(d)
+            start = np.array([8.0, y, z]) - d * speed / 60.0 * (arrival_steps - 0.5)
+            b["position"][i] = start
+            b["linear_velocity"][i] = d * speed
+            b["motion_quality"][i] = 1
+            b["gravity_factor"][i] = 0.0
+            b["allow_sleeping"][i] = 0
+        set_sphere(b, o + 2, 0.2)
+        set_sphere(b, o + 3, 0.12)
+        set_box(b, o + 4, (0.1, 0.08, 0.25))
+        b["angular_velocity"][o + 4] = (3.0, 7.0, -2.0)
+        set_capsule(b, o + 5, 0.08, 0.15)
+        b["quaternion"][o + 5] = (0.0, 0.0, math.sin(math.pi / 4), math.cos(math.pi / 4))
+        set_hull(b, o + 6, wd)
+        # a bouncing bullet
+        i = o + 7
+        set_sphere(b, i, 0.15)
+        b["restitution"][i] = 0.6
+        b["position"][i] = (8.0 - 200.0 / 60.0 * (arrival_steps - 0.5), 5.0, -4.0)
+        b["linear_velocity"][i] = (200.0, 0.0, 0.0)
+        b["motion_quality"][i] = 1
+        b["gravity_factor"][i] = 0.0
+        # a dynamic box in front of the wall, hit by a bullet
+        set_box(b, o + 8, (0.4, 0.4, 0.4))
+        b["position"][o + 8] = (6.0, 0.4, 5.0)
+        b["motion_quality"][o + 8] = 1  # below the cast threshold until the bullet hits it
+        i = o + 9
+        set_sphere(b, i, 0.1)
+        b["position"][i] = (6.0 - 180.0 / 60.0 * (arrival_steps - 0.5), 0.45, 5.0)
+        b["linear_velocity"][i] = (180.0, 0.0, 0.0)
+        b["motion_quality"][i] = 1
+        b["gravity_factor"][i] = 0.0
+        # two bullets head-on
+        for i, x, v in ((o + 10, -4.0, 160.0), (o + 11, 4.0, -160.0)):
+            set_sphere(b, i, 0.15)
+            b["position"][i] = (x, 2.0, 10.0)
+            b["linear_velocity"][i] = (v, 0.0, 0.0)
+            b["motion_quality"][i] = 1
+            b["gravity_factor"][i] = 0.0
+    sc = Scene("ccd_gallery", b, dt=1.0 / 60.0, steps=8, num_worlds=num_worlds, seed=seed, hull_points=hulls)
+    return sc

@@ -57,6 +57,9 @@ class WorldSettings:
     baumgarte_factor: float = 0.2
     max_penetration_distance: float = 0.2
     min_velocity_for_restitution: float = 1.0
+    ccd_linear_cast_threshold: float = 0.05
+    ccd_linear_cast_max_penetration: float = 0.25
+    ccd_min_velocity_for_restitution: float = 1.0
     allow_sleeping: bool = True
     time_before_sleep: float = 0.5
     point_velocity_sleep_threshold: float = 0.03
@@ -73,7 +76,8 @@ class WorldSettings:
                   "penetration_tolerance", "normal_cos_max_delta_rotation",
                   "contact_point_preserve_lambda_max_dist_sq", "penetration_slop", "baumgarte_factor",
                   "max_penetration_distance", "min_velocity_for_restitution", "time_before_sleep",
-                  "point_velocity_sleep_threshold"):
+                  "point_velocity_sleep_threshold", "ccd_linear_cast_threshold",
+                  "ccd_linear_cast_max_penetration", "ccd_min_velocity_for_restitution"):
             setattr(s, f, float(getattr(self, f)))
         s.velocity_iterations = self.velocity_iterations
         s.position_iterations = self.position_iterations

@@ -61,6 +61,7 @@ enum cc_status {
 
 enum cc_shape_type { CC_SHAPE_SPHERE = 0, CC_SHAPE_BOX = 1, CC_SHAPE_CAPSULE = 2, CC_SHAPE_CONVEX_HULL = 3 };
 enum cc_motion_type { CC_STATIC = 0, CC_KINEMATIC = 1, CC_DYNAMIC = 2 };
+enum cc_motion_quality { CC_MOTION_DISCRETE = 0, CC_MOTION_LINEAR_CAST = 1 };  /* MotionQuality motion-properties.ts:8-26 */
 enum cc_combine_mode { CC_COMBINE_AVERAGE = 0, CC_COMBINE_MULTIPLY = 1, CC_COMBINE_MIN = 2, CC_COMBINE_MAX = 3,
                        CC_COMBINE_GEOMETRIC_MEAN = 4 };
 
@@ -102,6 +103,11 @@ typedef struct cc_world_settings {
     /* number of independent worlds held by this handle (batched form); bodies
      * name their world in cc_body_desc.world */
     int32_t num_worlds;
+    /* WorldSettings.ccd (world-settings.ts:198-221): a LINEAR_CAST body whose step moves it
+     * more than linearCastThreshold x its inner radius is cast along its motion */
+    double ccd_linear_cast_threshold;
+    double ccd_linear_cast_max_penetration;
+    double ccd_min_velocity_for_restitution;
 } cc_world_settings;
 
 /* RigidBodySettings (src/body/rigid-body.ts:37-139) for the supported shapes.
@@ -132,6 +138,7 @@ typedef struct cc_body_desc {
     uint32_t collision_groups;
     uint32_t collision_mask;
     int32_t allowed_dofs;
+    int32_t motion_quality;  /* cc_motion_quality */
 } cc_body_desc;
 
 /* Per-step counters of the last completed step. */
@@ -149,6 +156,8 @@ typedef struct cc_stats {
     float last_call_ms; /* device time of the last cc_world_step call (CUDA events on the world's stream) */
     int32_t num_giant_islands; /* islands solved by the whole grid in the last step */
     int32_t giant_colours;     /* colours of the largest of them */
+    int32_t num_ccd;           /* LINEAR_CAST bodies cast along their motion in the last step */
+    int32_t num_ccd_hits;      /* of them, those whose cast hit a body (findCCDContacts update.ts:1354) */
 } cc_stats;
 
 typedef struct cc_world cc_world;

@@ -50,6 +50,8 @@ struct Settings {
     double penetrationSlop = 0.02, baumgarteFactor = 0.2, maxPenetrationDistance = 0.2;
     bool allowSleeping = true;
     double timeBeforeSleep = 0.5, pointVelocitySleepThreshold = 0.03;
+    // ccd (world-settings.ts:258-262)
+    double linearCastThreshold = 0.05, linearCastMaxPenetration = 0.25, ccdMinVelocityForRestitution = 1.0;
 };
 
 struct SleepSphere {
@@ -78,6 +80,8 @@ struct Body {
     int frictionCombine = C_GEOMETRIC_MEAN, restitutionCombine = C_MAX;
     uint32_t groups = 0xffffffffu, mask = 0xffffffffu;
     bool sensor = false, collideKinematicVsNonDynamic = false, useManifoldReduction = true;
+    bool linearCast = false;  // MotionQuality.LINEAR_CAST
+    int ccdIndex = -1;        // this step's CCD record, or -1
     bool sleeping = false;
     Box3 aabb;
     int objectLayer = 0;
@@ -168,6 +172,18 @@ struct World {
     std::vector<std::pair<int, int>> manifoldBodies;
     std::vector<double> manifoldLambda;  // summed normal impulse per manifold after the solve
     double bodySteps = 0;
+    // continuous collision: this step's records (ccd.ts:20-57) and the two constraint parts
+    // that applyCCD keeps across calls (update.ts:1413-1414): their accumulated lambdas carry
+    // from one CCD impulse to the next, within a step and across steps
+    struct CCDRecord {
+        int body = -1, hit = -1;
+        V3 delta, normal, point;
+        double fraction = 1, fps = 1, thresholdSq = 0, maxPenetration = 0;
+        double friction = 0, restitution = 0;
+    };
+    std::vector<CCDRecord> ccd;
+    double ccdNormalLambda = 0, ccdFrictionLambda = 0;
+    int ccdHits = 0;  // records whose cast hit a body, last step
 };
 
 // ---------------------------------------------------------------------------
@@ -1201,7 +1217,193 @@ static void check_island_sleep(World &w, Island &is, double dt) {
 // ---------------------------------------------------------------------------
 // The step: updateWorld update.ts:45-239 (no listener, no joints, no CCD bodies)
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// Continuous collision detection for LINEAR_CAST bodies (update.ts:896-976, 979-1700, ccd.ts)
+// ---------------------------------------------------------------------------
+// getInnerRadius box.ts:333-335, sphere.ts:147-149, capsule.ts:254-256, convex-hull.ts:549-558
+static double inner_radius(const Shape &s) {
+    switch (s.type) {
+        case SHAPE_BOX:
+            return std::min(s.half_extents.x, std::min(s.half_extents.y, s.half_extents.z));
+        case SHAPE_CONVEX_HULL: {
+            double r = std::numeric_limits<double>::max();
+            for (double c : s.hull->plane_c) r = std::min(r, -c);
+            return std::max(0.0, r);
+        }
+        default:
+            return s.radius;
+    }
+}
+
+// Slab test of the segment origin + t * dir, t in [0, length], against a box: the entry t, or
+// +inf on a miss.  rayDistanceToBox3 cast-utils.ts:14-49 (which returns t / length); the same
+// slab test stands for mathcat 0.0.10's raycast3.intersectsBox3, which the reference calls with
+// the ray's direction as given (normalised in dbvt.ts:888, the raw displacement in
+// update.ts:1201-1204).
+static double ray_box_entry(V3 o, V3 d, double length, const Box3 &b) {
+    double t0 = 0, t1 = length;
+    const double oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+    const double mn[3] = {b.mn.x, b.mn.y, b.mn.z}, mx[3] = {b.mx.x, b.mx.y, b.mx.z};
+    for (int i = 0; i < 3; i++) {
+        if (std::fabs(dd[i]) < 1e-10) {
+            if (oo[i] < mn[i] || oo[i] > mx[i]) return std::numeric_limits<double>::infinity();
+        } else {
+            double inv = 1.0 / dd[i];
+            double a = (mn[i] - oo[i]) * inv, c = (mx[i] - oo[i]) * inv;
+            t0 = std::max(t0, std::min(a, c));
+            t1 = std::min(t1, std::max(a, c));
+            if (t1 < t0) return std::numeric_limits<double>::infinity();
+        }
+    }
+    return t0;
+}
+
+static Box3 box_grow(const Box3 &b, V3 e) { return {sub(b.mn, e), add(b.mx, e)}; }
+
+// findCCDContacts update.ts:1354-1470 with the broadphase cast (broadphase.ts:327-343,
+// dbvt.ts:869-975), the body visitor (update.ts:1118-1250) and the collector
+// (update.ts:1003-1115).  The candidates are every body in index order; the first of equal
+// fractions wins, as the collector keeps only strictly earlier hits.  The dynamic tree's
+// distance cull (dbvt.ts:905) compares against fattened leaf boxes that depend on the tree's
+// history; the exact box stands in for them here.  The contact-manifold block that follows the
+// cast in the reference (update.ts:1395-1466) is never entered, because the collector's
+// reset() (update.ts:1036-1042) clears hasHit after every visit.
+static void find_ccd_contacts(World &w, double dt) {
+    for (World::CCDRecord &c : w.ccd) {
+        Body &A = w.bodies[c.body];
+        Box3 end{add(A.aabb.mn, c.delta), add(A.aabb.mx, c.delta)};
+        Box3 swept{{std::min(A.aabb.mn.x, end.mn.x), std::min(A.aabb.mn.y, end.mn.y), std::min(A.aabb.mn.z, end.mn.z)},
+                   {std::max(A.aabb.mx.x, end.mx.x), std::max(A.aabb.mx.y, end.mx.y), std::max(A.aabb.mx.z, end.mx.z)}};
+        V3 origin = scale(add(swept.mn, swept.mx), 0.5);
+        V3 half = scale(sub(swept.mx, swept.mn), 0.5);
+        double castLen = len(c.delta);
+        V3 castDir = normalize(c.delta);
+        V3 halfA = scale(sub(A.aabb.mx, A.aabb.mn), 0.5);
+        int la = A.objectLayer;
+        for (Body &B : w.bodies) {
+            int lb = B.objectLayer;
+            // broadphase layer and leaf filters of the tree cast (broadphase.ts:334-335,
+            // dbvt.ts:905-966)
+            if (!w.layers.objVsBp[la * w.layers.nBp + w.layers.objToBp[lb]]) continue;
+            if (!((A.groups & B.mask) != 0 && (B.groups & A.mask) != 0)) continue;
+            if (!w.layers.objPairs[la * w.layers.nObj + lb]) continue;
+            double t = ray_box_entry(origin, castDir, castLen, box_grow(B.aabb, half));
+            if (!(t < std::numeric_limits<double>::infinity()) || t / castLen > castLen) continue;
+            // ccdBodyVisitor.visit update.ts:1153-1250
+            if (B.index == A.index) continue;
+            const World::CCDRecord *cb = B.ccdIndex >= 0 ? &w.ccd[B.ccdIndex] : nullptr;
+            if (cb && c.body > cb->body) continue;
+            if (B.sensor) continue;
+            V3 rel = cb ? sub(c.delta, cb->delta) : c.delta;
+            if (lensq(rel) < c.thresholdSq) continue;
+            double relLen = len(rel);
+            if (!(ray_box_entry(A.position, rel, relLen, box_grow(B.aabb, halfA)) <
+                  std::numeric_limits<double>::infinity()))
+                continue;
+            CastHit h;
+            if (!cast_convex_vs_convex(h, A.shape, A.position, A.quat, rel, B.shape, B.position, B.quat, c.fps, false))
+                continue;
+            // ccdCastShapeCollector.addHit update.ts:1044-1109
+            V3 n = normalize(h.axis);
+            double den = dot(n, c.delta);
+            if (den <= c.maxPenetration) continue;
+            double fps = h.fraction + c.maxPenetration / den;
+            if (fps >= c.fps) continue;
+            c.hit = B.index;
+            c.fraction = h.fraction;
+            c.fps = fps;
+            c.normal = n;
+            // calculateBodyMotion update.ts:984-994: a moving LINEAR_CAST body B counts its
+            // velocity step, whether or not it took the continuous path this step
+            V3 mB{0, 0, 0};
+            if (B.motion != STATIC && B.linearCast) mB = scale(B.linvel, dt);
+            c.point = lensq(mB) > 1e-12 ? add(h.pa, scale(mB, h.fraction)) : h.pa;
+            c.friction = combine(A.friction, B.friction, A.frictionCombine, B.frictionCombine);
+            c.restitution = combine(A.restitution, B.restitution, A.restitutionCombine, B.restitutionCombine);
+        }
+    }
+}
+
+static void clamp_velocities(Body &b) {  // clampLinearVelocity / clampAngularVelocity motion-properties.ts:624-639
+    if (lensq(b.linvel) > b.maxLin * b.maxLin) b.linvel = scale(normalize(b.linvel), b.maxLin);
+    if (lensq(b.angvel) > b.maxAng * b.maxAng) b.angvel = scale(normalize(b.angvel), b.maxAng);
+}
+
+// applyCCD update.ts:1420-1580: one normal and one friction iteration at the time of impact.
+// The two parts keep their accumulated lambdas from earlier calls (module-scope scratch in the
+// reference); the normal impulse itself does not depend on them, the friction bound does.
+static void apply_ccd(World &w, const World::CCDRecord &c, Body &A, Body &B) {
+    if (A.motion != DYNAMIC) return;
+    V3 r1 = sub(c.point, scale_add(A.com, c.delta, c.fraction));
+    V3 r2 = sub(c.point, B.com);
+    V3 v1 = add(A.linvel, cross(A.angvel, r1));
+    V3 v2 = B.motion != STATIC ? add(B.linvel, cross(B.angvel, r2)) : V3{0, 0, 0};
+    V3 rel = sub(v2, v1);
+    double nv = dot(rel, c.normal);
+    if (nv >= 0) return;
+    double bias = (c.restitution > 0 && nv < -w.s.ccdMinVelocityForRestitution) ? c.restitution * nv : 0;
+    double imA = A.invMass, imB = B.motion == DYNAMIC ? B.invMass : 0;
+    M4 IA = inv_inertia_for_rotation(A, mat4_from_quat(A.quat));
+    M4 IB{};
+    if (B.motion == DYNAMIC) IB = inv_inertia_for_rotation(B, mat4_from_quat(B.quat));
+    AxisPart np;
+    np.totalLambda = w.ccdNormalLambda;
+    calc_props(np, A, B, imA, imB, IA, IB, r1, r2, c.normal, bias);
+    apply_lambda(np, A, B, imA, imB, c.normal, total_lambda(np, A, B, c.normal));
+    w.ccdNormalLambda = np.totalLambda;
+    if (c.friction > 0) {
+        V3 tv = sub(rel, scale(c.normal, nv));
+        double tl2 = lensq(tv);
+        if (tl2 > 1e-12) {
+            V3 dir = scale(tv, 1.0 / std::sqrt(tl2));
+            double maxF = c.friction * np.totalLambda;
+            AxisPart fp;
+            fp.totalLambda = w.ccdFrictionLambda;
+            calc_props(fp, A, B, imA, imB, IA, IB, r1, r2, dir, 0);
+            double tl = total_lambda(fp, A, B, dir);
+            apply_lambda(fp, A, B, imA, imB, dir, std::max(-maxF, std::min(maxF, tl)));
+            w.ccdFrictionLambda = fp.totalLambda;
+        }
+    }
+    clamp_velocities(A);
+    if (B.motion == DYNAMIC) clamp_velocities(B);
+}
+
+// sortCCDBodies update.ts:1583-1611 and resolveCCDContacts update.ts:1616-1670.  After the sort
+// a body's record index still names the slot it was created in, so the cascade below reads
+// the record that the sort put in that slot, as the reference does.
+static void resolve_ccd_contacts(World &w) {
+    std::sort(w.ccd.begin(), w.ccd.end(), [](const World::CCDRecord &a, const World::CCDRecord &b) {
+        if (a.fps != b.fps) return a.fps < b.fps;
+        return a.body < b.body;
+    });
+    for (size_t i = 0; i < w.ccd.size(); i++) {
+        World::CCDRecord &c = w.ccd[i];
+        Body &A = w.bodies[c.body];
+        if (c.hit == -1) {
+            A.position = add(A.position, c.delta);
+            set_transform(A);
+            continue;
+        }
+        Body &B = w.bodies[c.hit];
+        if (B.ccdIndex >= 0) {
+            World::CCDRecord &cb = w.ccd[B.ccdIndex];
+            if (cb.hit != -1 && cb.fraction > c.fraction) {
+                cb.hit = -1;
+                cb.fps = c.fraction;
+            }
+        }
+        apply_ccd(w, c, A, B);
+        A.position = add(A.position, scale(c.delta, c.fps));
+        set_transform(A);
+        if (B.sleeping) wake_body(w, B);
+    }
+}
+
 static void step(World &w, double dt) {
+    // ccd.clear ccd.ts:108-124
+    w.ccd.clear();
+    for (Body &b : w.bodies) b.ccdIndex = -1;
     w.constraints.clear();
     w.manifoldLambda.clear();
     w.manifolds.clear();
@@ -1377,7 +1579,7 @@ static void step(World &w, double dt) {
                 ct.pts[i].lt2 = c.pts[i].t2.totalLambda;
             }
         }
-        // velocityIntegrationUpdate update.ts:896-976 (discrete motion quality)
+        // velocityIntegrationUpdate update.ts:896-976
         for (Body &b : w.bodies) {
             if (b.motion == STATIC || b.sleeping) continue;
             if (b.motion == DYNAMIC) {
@@ -1393,10 +1595,31 @@ static void step(World &w, double dt) {
                 b.quat = qnormalize(qmul(rq, b.quat));
             }
             V3 disp = scale(b.linvel, dt);
+            // LINEAR_CAST dynamic non-sensor bodies moving more than the threshold defer their
+            // translation to the continuous-collision pass (update.ts:930-968)
+            if (b.linearCast && b.motion == DYNAMIC && !b.sensor) {
+                double inner = inner_radius(b.shape);
+                double thr = w.s.linearCastThreshold * inner;
+                if (lensq(disp) > thr * thr) {
+                    World::CCDRecord c;
+                    c.body = b.index;
+                    c.delta = disp;
+                    c.thresholdSq = thr * thr;
+                    c.maxPenetration = std::min(w.s.penetrationSlop, w.s.linearCastMaxPenetration * inner);
+                    b.ccdIndex = (int)w.ccd.size();
+                    w.ccd.push_back(c);
+                    set_transform(b);  // setQuaternion: the rotation about the body position
+                    continue;
+                }
+            }
             b.com = add(b.com, disp);
             update_pos_from_com(b);
             set_transform(b);
         }
+        find_ccd_contacts(w, dt);
+        w.ccdHits = 0;
+        for (const World::CCDRecord &c : w.ccd) w.ccdHits += c.hit >= 0;
+        resolve_ccd_contacts(w);
         for (Island &is : w.islands) {
             if (is.contactIndices.empty() && is.jointIndices.empty()) continue;
             for (int i = 0; i < is.posSteps; i++) {
@@ -1460,7 +1683,8 @@ enum {
     F_WORLD = 27,
     F_GROUPS = 28,
     F_MASK = 29,
-    F_COUNT = 30
+    F_MOTION_QUALITY = 30,  // 0 discrete, 1 linear cast (MotionQuality motion-properties.ts:8-26)
+    F_COUNT = 31
 };
 
 void *orc_world_create(const double *settings, int n_obj, const int *obj_to_bp, int n_bp, const uint8_t *obj_pairs,
@@ -1485,6 +1709,9 @@ void *orc_world_create(const double *settings, int n_obj, const int *obj_to_bp, 
     s.timeBeforeSleep = settings[17];
     s.pointVelocitySleepThreshold = settings[18];
     s.gravityEnabled = settings[19] != 0;
+    s.linearCastThreshold = settings[20];
+    s.linearCastMaxPenetration = settings[21];
+    s.ccdMinVelocityForRestitution = settings[22];
     w->layers.nObj = n_obj;
     w->layers.nBp = n_bp;
     w->layers.objToBp.assign(obj_to_bp, obj_to_bp + n_obj);
@@ -1551,6 +1778,7 @@ int orc_add_bodies(void *wp, const double *rows, int n) {
         b.linDamp = r[F_LIN_DAMP];
         b.angDamp = r[F_ANG_DAMP];
         b.allowSleeping = r[F_ALLOW_SLEEP] != 0;
+        b.linearCast = r[F_MOTION_QUALITY] == 1;
         b.groups = (uint32_t)r[F_GROUPS];
         b.mask = (uint32_t)r[F_MASK];
         double mass;
@@ -1857,6 +2085,11 @@ int orc_get_manifolds(void *wp, double *out) {
 
 // Island statistics of the last step: number of islands with contacts.
 int orc_island_count(void *wp) { return (int)((World *)wp)->islands.size(); }
+// continuous collision of the last step: records, and records whose cast hit a body
+void orc_ccd_counts(void *wp, int *out) {
+    out[0] = (int)((World *)wp)->ccd.size();
+    out[1] = ((World *)wp)->ccdHits;
+}
 
 // ---- unit-level entry points for the known-answer tests -------------------
 // Faces are passed as n vertices (xyz doubles).  Returns the output vertex count.

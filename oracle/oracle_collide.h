@@ -1583,6 +1583,139 @@ inline bool collide_sphere_vs_sphere(Hit &hit, const Shape &sa, V3 pA, const Sha
     return true;
 }
 
+// ----------------------------------------------------------------------------
+// Shape cast (gjk.ts:853-1259, penetration.ts:621-699, convex.ts:675-900)
+// ----------------------------------------------------------------------------
+struct CastHit {
+    double fraction = 0;
+    V3 pa, pb, axis;  // world-space points and the unnormalised penetration axis
+};
+
+// gjkCastShape gjk.ts:853-1259.  A (already placed in B's space) moves by disp, B is fixed;
+// returns false on a miss, else the time of impact and the closest points at that time.
+inline bool gjk_cast_shape(double &lambdaOut, V3 &pa, V3 &pb, V3 &axisOut, const Support &A, const Support &B,
+                           V3 disp, double tol, double rA, double rB, double maxLambda) {
+    double sqtol = tol * tol;
+    const double sumR = rA + rB;
+    Simplex sx;
+    double lambda = 0.0;
+    V3 x{0, 0, 0};
+    // the starting direction: the negated support of B plus the negated support of A at the
+    // zero direction (gjk.ts:882-897)
+    V3 q = neg(B.get({0, 0, 0}));
+    V3 p = A.get({0, 0, 0});
+    V3 v = sub(q, p);
+    double vLenSq = std::numeric_limits<double>::max();
+    bool allowRestart = false;
+    V3 prevV{0, 0, 0};
+    for (int it = 0; it < GJK_MAX_ITERATIONS; it++) {
+        p = A.get(neg(v));
+        q = B.get(v);
+        V3 w = sub(x, sub(q, p));
+        double vdw = dot(v, w) - sumR * std::sqrt(lensq(v));
+        if (vdw > 0.0) {
+            double vdr = dot(v, disp);
+            if (vdr >= -1.0e-18) return false;
+            double old = lambda;
+            lambda -= vdw / vdr;
+            if (old == lambda) break;
+            if (lambda >= maxLambda) return false;
+            x = scale(disp, lambda);
+            vLenSq = std::numeric_limits<double>::max();
+            sqtol = (tol + sumR) * (tol + sumR);
+            allowRestart = true;
+        }
+        sx.pts[sx.size].p = p;
+        sx.pts[sx.size].q = q;
+        sx.size++;
+        for (int i = 0; i < sx.size; i++) sx.pts[i].y = add(sub(x, sx.pts[i].q), sx.pts[i].p);
+        ClosestToSimplex c;
+        if (closest_to_simplex(c, vLenSq, false, sx)) {
+            vLenSq = c.sqdist;
+            v = c.point;
+        } else {
+            if (!allowRestart) break;
+            allowRestart = false;
+            sx.pts[0].p = p;
+            sx.pts[0].q = q;
+            sx.size = 1;
+            v = sub(x, q);
+            vLenSq = std::numeric_limits<double>::max();
+            continue;
+        }
+        if (c.set == 0xf) break;
+        // updatePointSetPQ gjk.ts:799-813
+        int ns = 0;
+        for (int i = 0; i < sx.size; i++)
+            if (c.set & (1 << i)) {
+                if (ns != i) {
+                    sx.pts[ns].p = sx.pts[i].p;
+                    sx.pts[ns].q = sx.pts[i].q;
+                }
+                ns++;
+            }
+        sx.size = ns;
+        if (vLenSq <= sqtol) break;
+        prevV = v;
+    }
+    for (int i = 0; i < sx.size; i++) sx.pts[i].y = add(sub(x, sx.pts[i].q), sx.pts[i].p);
+    double vl = std::sqrt(lensq(v));
+    V3 nv = vl > 0 ? scale(v, 1 / vl) : V3{0, 0, 0};
+    V3 sa{0, 0, 0}, sb{0, 0, 0};
+    if (sx.size == 1) {
+        sb = sx.pts[0].q;
+        sa = sx.pts[0].p;
+    } else if (sx.size == 2) {
+        Bary b = bary2(sx.pts[0].y, sx.pts[1].y, 1e-10);
+        sb = add(scale(sx.pts[0].q, b.u), scale(sx.pts[1].q, b.v));
+        sa = add(scale(sx.pts[0].p, b.u), scale(sx.pts[1].p, b.v));
+    } else if (sx.size >= 3) {
+        Bary b = bary3(sx.pts[0].y, sx.pts[1].y, sx.pts[2].y, 1e-10);
+        sb = add(add(scale(sx.pts[0].q, b.u), scale(sx.pts[1].q, b.v)), scale(sx.pts[2].q, b.w));
+        sa = add(add(scale(sx.pts[0].p, b.u), scale(sx.pts[1].p, b.v)), scale(sx.pts[2].p, b.w));
+    }
+    if (sx.size >= 1) {
+        pb = scale_add(sb, nv, rB);
+        pa = lambda > 0.0 ? pb : scale_add(sa, nv, -rA);
+    } else {
+        pa = pb = {0, 0, 0};
+    }
+    lambdaOut = lambda;
+    axisOut = sumR > 0.0 ? neg(v) : neg(prevV);
+    return true;
+}
+
+// castConvexVsConvex convex.ts:675-742 and castConvexVsConvexLocal convex.ts:744-900 with
+// penetrationCastShape penetration.ts:621-699, for the continuous-collision query
+// (update.ts:1210-1240): no deepest point, no faces, back faces culled.  maxLambda is the
+// collector's early-out fraction.
+inline bool cast_convex_vs_convex(CastHit &hit, const Shape &sa, V3 pA, Q4 qA, V3 disp, const Shape &sb, V3 pB,
+                                  Q4 qB, double maxLambda, bool collideWithBackfaces) {
+    Q4 iqB = qconj(qB);
+    V3 posAInB = rotate(iqB, sub(pA, pB));
+    Q4 qAInB = qmul(iqB, qA);
+    V3 dInB = rotate(iqB, disp);
+    Support A = make_support(sa, EXCLUDE_CONVEX_RADIUS);
+    Support B = make_support(sb, EXCLUDE_CONVEX_RADIUS);
+    A.transformed = true;
+    A.m = mat4_from_rt(qAInB, posAInB);
+    const double tol = 1e-4;
+    double lambda;
+    V3 pa, pb, axis;
+    if (!gjk_cast_shape(lambda, pa, pb, axis, A, B, dInB, tol, A.convex_radius, B.convex_radius, maxLambda))
+        return false;
+    // an axis shorter than the tolerance is replaced by the cast direction (penetration.ts:693-698)
+    if (lensq(axis) < tol * tol) axis = dInB;
+    if (lambda > 1.0) return false;
+    if (!collideWithBackfaces && dot(axis, dInB) <= 0) return false;
+    if (lambda >= maxLambda) return false;
+    hit.pa = add(rotate(qB, pa), pB);
+    hit.pb = add(rotate(qB, pb), pB);
+    hit.axis = rotate(qB, axis);
+    hit.fraction = lambda;
+    return true;
+}
+
 // collideShapeVsShape narrowphase.ts:172-238 (dispatch for the supported convex shapes)
 inline bool collide_shapes(Hit &hit, const CollideSettings &cs, const Shape &sa, V3 pA, Q4 qA, const Shape &sb,
                            V3 pB, Q4 qB) {

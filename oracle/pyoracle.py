@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 
-F_COUNT = 30  # doubles per body row, see oracle.cpp (enum F_*)
+F_COUNT = 31  # doubles per body row, see oracle.cpp (enum F_*)
 STATE = 17    # pos3 quat4 linvel3 angvel3 com3 sleeping
 
 _lib = None
@@ -47,6 +47,7 @@ def load():
         "orc_manifold_count": ([vp], i32),
         "orc_get_manifolds": ([vp, dp], i32),
         "orc_island_count": ([vp], i32),
+        "orc_ccd_counts": ([vp, ip], None),
         "orc_clip_poly_vs_plane": ([dp, i32, dp, dp, dp], i32),
         "orc_clip_poly_vs_poly": ([dp, i32, dp, i32, dp, dp], i32),
         "orc_manifold_between_faces": ([dp, dp, dp, C.c_double, dp, i32, dp, i32, dp, dp], i32),
@@ -100,12 +101,13 @@ def rows_from_bodies(b: np.ndarray) -> np.ndarray:
     r[:, 27] = b["world"]
     r[:, 28] = b["collision_groups"]
     r[:, 29] = b["collision_mask"]
+    r[:, 30] = b["motion_quality"]
     return np.ascontiguousarray(r)
 
 
 def settings_array(ws) -> np.ndarray:
     """WorldSettings (crashcat_gb300.world) -> the oracle's settings vector."""
-    s = np.zeros(20, dtype=np.float64)
+    s = np.zeros(23, dtype=np.float64)
     s[0:3] = ws.gravity
     s[3] = ws.speculative_contact_distance
     s[4] = ws.manifold_tolerance
@@ -124,6 +126,9 @@ def settings_array(ws) -> np.ndarray:
     s[17] = ws.time_before_sleep
     s[18] = ws.point_velocity_sleep_threshold
     s[19] = 1.0 if ws.gravity_enabled else 0.0
+    s[20] = ws.ccd_linear_cast_threshold
+    s[21] = ws.ccd_linear_cast_max_penetration
+    s[22] = ws.ccd_min_velocity_for_restitution
     return s
 
 
@@ -200,6 +205,12 @@ class OracleWorld:
         o = np.zeros((max(n, 1), 2), dtype=np.int32)
         self.lib.orc_get_pairs(self.h, iptr(o))
         return o[:n]
+
+    def ccd_counts(self) -> tuple[int, int]:
+        """Continuous collision of the last step: (bodies cast, casts that hit a body)."""
+        o = np.zeros(2, dtype=np.int32)
+        self.lib.orc_ccd_counts(self.h, iptr(o))
+        return int(o[0]), int(o[1])
 
     def aabbs(self) -> np.ndarray:
         o = np.zeros((self.n, 6), dtype=np.float64)

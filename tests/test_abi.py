@@ -58,8 +58,9 @@ def test_invalid_arguments_are_rejected(lib):
 
 
 def test_body_desc_layout_matches_c():
-    # 23 fields of 4 bytes each (shape_params 4, vec3/quat inline)
-    assert _lib.BODY_DTYPE.itemsize == 4 * (1 + 4 + 1 + 4 + 3 + 4 + 3 + 3 + 7 + 2 + 2 + 1)
+    # 24 fields of 4 bytes each (shape_params 4, vec3/quat inline), motion_quality last
+    assert _lib.BODY_DTYPE.itemsize == 4 * (1 + 4 + 1 + 4 + 3 + 4 + 3 + 3 + 7 + 2 + 2 + 1 + 1)
+    assert _lib.BODY_DTYPE.names[-1] == "motion_quality"
 
 
 def test_layer_tables_follow_reference():
