@@ -25,6 +25,7 @@ SHAPE_SPHERE = 0
 SHAPE_BOX = 1
 SHAPE_CAPSULE = 2
 SHAPE_CONVEX_HULL = 3
+SHAPE_TRIANGLE_MESH = 4
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 COMBINE_AVERAGE, COMBINE_MULTIPLY, COMBINE_MIN, COMBINE_MAX, COMBINE_GEOMETRIC_MEAN = 0, 1, 2, 3, 4
 MAX_LAYERS = 32
@@ -74,6 +75,11 @@ class HullInfo(C.Structure):
                 ("bounds_max", C.c_float * 3)]
 
 
+class MeshInfo(C.Structure):
+    _fields_ = [("num_vertices", C.c_int32), ("num_triangles", C.c_int32), ("num_nodes", C.c_int32),
+                ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3)]
+
+
 class Stats(C.Structure):
     _fields_ = [(n, C.c_int32) for n in (
         "num_bodies", "num_awake", "num_pairs", "num_manifolds", "num_contact_points", "num_epa",
@@ -116,6 +122,13 @@ EXPORTS = {
                                C.c_void_p, C.c_void_p], C.c_int),
     "cc_penetration_static": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_float, C.c_float, C.c_void_p], C.c_int),
     "cc_world_add_hinges": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
+    "cc_world_add_triangle_mesh": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_double, C.c_double,
+                                    C.POINTER(C.c_int32)], C.c_int),
+    "cc_triangle_mesh_build": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_void_p,
+                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "cc_world_get_triangle_mesh": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p], C.c_int),
+    "cc_world_get_manifold_sub_shapes": ([C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
     "cc_world_add_convex_hull": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.POINTER(C.c_int32)], C.c_int),
     "cc_world_get_convex_hull": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
@@ -272,6 +285,32 @@ def _hull_arrays(call) -> dict:
             "inertia": np.array(info.inertia[:], np.float32).reshape(3, 3),
             "bounds_min": np.array(info.bounds_min[:], np.float32),
             "bounds_max": np.array(info.bounds_max[:], np.float32)}
+
+
+def _mesh_arrays(call) -> dict:
+    """Runs a mesh export (cc_triangle_mesh_build / cc_world_get_triangle_mesh) twice: sizes, then data."""
+    info = MeshInfo()
+    check(call(C.byref(info), None, None, None, None), "triangle mesh")
+    nv, nt, nn = info.num_vertices, info.num_triangles, info.num_nodes
+    verts = np.zeros((max(nv, 1), 3), np.float32)
+    tris = np.zeros((max(nt, 1), 4), np.int32)
+    normals = np.zeros((max(nt, 1), 3), np.float32)
+    nodes = np.zeros((max(nn, 1), 8), np.float32)
+    check(call(C.byref(info), ptr(verts), ptr(tris), ptr(normals), ptr(nodes)), "triangle mesh")
+    return {"vertices": verts[:nv], "triangles": tris[:nt], "normals": normals[:nt], "nodes": nodes[:nn],
+            "bounds_min": np.array(info.bounds_min[:], np.float32),
+            "bounds_max": np.array(info.bounds_max[:], np.float32)}
+
+
+def build_triangle_mesh(positions, indices, degenerate_tolerance: float = -1.0,
+                        active_edge_cos: float = -2.0) -> dict:
+    """cc_triangle_mesh_build: the mesh as triangleMesh.create builds it (host only):
+    vertices, triangles (a b c active-edge bits), normals, BVH nodes."""
+    lib = load()
+    p = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+    ix = np.ascontiguousarray(indices, dtype=np.int32).reshape(-1, 3)
+    return _mesh_arrays(lambda info, *a: lib.cc_triangle_mesh_build(
+        ptr(p), len(p), ptr(ix), len(ix), C.c_double(degenerate_tolerance), C.c_double(active_edge_cos), info, *a))
 
 
 def build_convex_hull(points, convex_radius: float = -1.0) -> dict:

@@ -125,6 +125,16 @@ __device__ void exact_aabb(float4 p4, float4 q4, const double lo[3], const doubl
 // local bounds of the shape in FP64 (box.ts:77-84, sphere.ts, capsule.ts:84-94)
 __device__ __forceinline__ void shape_bounds(const DevWorld &w, uint32_t f, float4 sp, double lo[3], double hi[3]) {
     int s = shape_of(f);
+    if (s == SHAPE_MESH) {  // the mesh's root node bounds (triangle-mesh.ts:124-130)
+        const DevMesh &m = w.meshes[mesh_of(sp)];
+        lo[0] = m.lo.x;
+        lo[1] = m.lo.y;
+        lo[2] = m.lo.z;
+        hi[0] = m.hi.x;
+        hi[1] = m.hi.y;
+        hi[2] = m.hi.z;
+        return;
+    }
     if (s == SHAPE_HULL) {  // the hull's local bounds (convex-hull.ts:214-231)
         const DevHull &h = w.hulls[hull_of(sp)];
         lo[0] = h.lo.x;

@@ -36,7 +36,7 @@ __host__ __device__ inline int layer_of(uint32_t f) { return (int)((f >> F_LAYER
 __host__ __device__ inline bool sleeping_of(uint32_t f) { return (f & F_SLEEPING) != 0; }
 
 constexpr int STATIC = 0, KINEMATIC = 1, DYNAMIC = 2;
-constexpr int SHAPE_SPHERE = 0, SHAPE_BOX = 1, SHAPE_CAPSULE = 2, SHAPE_HULL = 3;
+constexpr int SHAPE_SPHERE = 0, SHAPE_BOX = 1, SHAPE_CAPSULE = 2, SHAPE_HULL = 3, SHAPE_MESH = 4;
 
 // Per-step overflow flags (status bits in DevCounters::overflow)
 enum : int { OVF_PAIRS = 1, OVF_MANIFOLDS = 2, OVF_EPA = 4, OVF_ISLAND = 8, OVF_CACHE = 16, OVF_SLOTS = 32,
@@ -69,6 +69,9 @@ struct DevCounters {
     int num_small_joint_islands, num_large_joint_islands;  // islands with joints per tier
     int num_ccd;       // bodies that took the continuous-collision path this step
     int num_ccd_hits;  // of them, those whose cast hit a body
+    int num_mesh_pairs;   // broadphase pairs with a triangle mesh body
+    int num_mesh_hits;    // triangle hits reported to the mesh pairs' reduction
+    int mesh_reduced;     // mesh pairs whose hits needed more manifolds than a pair keeps
     int pad[1];
 };
 
@@ -111,6 +114,7 @@ struct Manifold {
     float depth;
     float3 ra[4];      // point on A relative to base (= position of A)
     float3 rb[4];
+    uint32_t sub_a, sub_b;  // sub-shape ids (0xffffffff for a convex shape; a mesh triangle's id)
 };
 
 // Contact constraint in solver form (one per manifold that creates a constraint).
@@ -195,6 +199,19 @@ struct DevHull {
     float4 com;     // centre of mass in the input frame (xyz)
     float4 lo, hi;  // bounds of the points (xyz)
 };
+
+// Triangle mesh shape (src/shapes/triangle-mesh.ts, utils/triangle-mesh-data.ts and
+// triangle-mesh-bvh.ts): welded vertices, triangles (vertex indices, active-edge bits) and
+// the BVH in pre-order, two float4 per node: (min xyz, right child node or first triangle as
+// int bits) and (max xyz, split axis or -(triangle count + 1) as int bits).  A mesh body's
+// shape record holds (mesh index as int bits, 0, 0, 0).
+struct DevMesh {
+    int first_vertex, first_tri, first_node, num_tris;
+    int sub_bits;  // bits of the triangle index in the sub-shape id (subShape.pushIndex sub-shape.ts:60-64)
+    int pad0, pad1, pad2;
+    float4 lo, hi;  // bounds of the root node
+};
+constexpr int MESH_KEY_BITS = 21;  // body indices and triangle indices in a mesh contact's cache key
 
 // user joints of both types share one id space: hinges 0.., swing-twists JOINT_SWING | index
 constexpr int JOINT_SWING = 1 << 30;
@@ -385,6 +402,16 @@ struct DevWorld {
     int *giant_list;
     unsigned long long *giant_claim;       // 4 x cap: contact claims, two parities | joint claims, two parities
     int *giant_count;  // 4 x (GIANT_COLOURS + 2): contact colour offsets, contact fill cursors, joint offsets, joint fill
+    // triangle meshes
+    DevMesh *meshes;
+    int num_meshes;
+    int num_mesh_bodies;  // bodies with a mesh shape (0: the mesh passes are not launched)
+    float4 *mesh_verts;
+    int4 *mesh_tris;      // a b c (vertex indices into mesh_verts), active-edge bits
+    float4 *mesh_nodes;   // 2 per node
+    int *mesh_pairs;      // pairs with a mesh body this step (index into pairs)
+    int *mesh_epa_base;   // per mesh pair: its first EPA item, -1 when it needs none
+    int *mesh_epa_count;  // per mesh pair: its EPA items
     // continuous collision (LINEAR_CAST bodies, update.ts:896-1670)
     int num_linear_cast;  // bodies with LINEAR_CAST motion quality (0: the single-pass solve)
     int *ccd_flag;        // per body: deferred its translation this step
@@ -398,6 +425,16 @@ struct DevWorld {
     int *ccd_scan_tmp;    // scan scratch over the worlds
 };
 
+// the mesh index of a mesh body's shape record (same int-bits encoding as hull_of)
+__host__ __device__ inline int mesh_of(float4 sp) {
+#ifdef __CUDA_ARCH__
+    return __float_as_int(sp.x);
+#else
+    int v;
+    memcpy(&v, &sp.x, sizeof(int));
+    return v;
+#endif
+}
 __host__ __device__ inline int hull_of(float4 sp) {
 #ifdef __CUDA_ARCH__
     return __float_as_int(sp.x);

@@ -109,15 +109,17 @@ __device__ __forceinline__ Q<S> qmulS(Q<S> a, Q<S> b) {
 // ---------------------------------------------------------------------------
 // support functions
 // ---------------------------------------------------------------------------
-enum { SUP_BOX = 0, SUP_POINT = 1, SUP_SPHERE = 2, SUP_CAPSULE_SEGMENT = 3, SUP_CAPSULE_SURFACE = 4, SUP_HULL = 5 };
+enum { SUP_BOX = 0, SUP_POINT = 1, SUP_SPHERE = 2, SUP_CAPSULE_SEGMENT = 3, SUP_CAPSULE_SURFACE = 4, SUP_HULL = 5,
+       SUP_TRIANGLE = 6 };
 // the world's convex hull arrays, as the support functions read them
 struct HullView {
     const DevHull *hulls;
     const float4 *points, *shrunk;
 };
 __device__ __forceinline__ HullView hull_view(const DevWorld &w) { return HullView{w.hulls, w.hull_points, w.hull_shrunk}; }
-// H: the support may be a convex hull (the contact-only narrowphase instance compiles it out)
-template <typename S, bool H = true>
+// H: the support may be a convex hull (the contact-only narrowphase instance compiles it out);
+// T: it may be a mesh triangle (only the mesh passes compile it in)
+template <typename S, bool H = true, bool T = false>
 struct Sup {
     int kind;
     const float4 *hp;  // hull support points (original or shrunk) and their count
@@ -144,6 +146,13 @@ struct Sup {
                 }
             }
             return bp;
+        }
+        if (T && kind == SUP_TRIANGLE) {
+            // triangleGetSupport support.ts:83-118: the vertex with the largest projection (an
+            // untransformed triangle keeps its vertices in r0, r1, r2)
+            S d1 = dot(r0, d), d2 = dot(r1, d), d3 = dot(r2, d);
+            if (d1 > d2) return d1 > d3 ? r0 : r2;
+            return d2 > d3 ? r1 : r2;
         }
         if (kind == SUP_POINT) return {S(0), S(0), S(0)};
         // capsule: segment +-h on Y (capsuleNoConvexGetSupport capsule.ts:268-275)
@@ -177,9 +186,9 @@ struct Sup {
 };
 
 // setBoxSupport support.ts:339-370 / getSphereSupportFunction sphere.ts:256-266
-template <typename S, bool H = true>
-__device__ Sup<S, H> make_sup(int shape, float4 sp, bool exclude, const HullView &hv) {
-    Sup<S, H> o;
+template <typename S, bool H = true, bool T = false>
+__device__ Sup<S, H, T> make_sup(int shape, float4 sp, bool exclude, const HullView &hv) {
+    Sup<S, H, T> o;
     o.transformed = false;
     o.add_r = S(0);
     o.radius = S(0);
@@ -233,8 +242,8 @@ __device__ Sup<S, H> make_sup(int shape, float4 sp, bool exclude, const HullView
     }
     return o;
 }
-template <typename S, bool H>
-__device__ void set_transform(Sup<S, H> &s, Q<S> q, V<S> p) {
+template <typename S, bool H, bool T>
+__device__ void set_transform(Sup<S, H, T> &s, Q<S> q, V<S> p) {
     S x2 = q.x + q.x, y2 = q.y + q.y, z2 = q.z + q.z;
     S xx = q.x * x2, xy = q.x * y2, xz = q.x * z2, yy = q.y * y2, yz = q.y * z2, zz = q.z * z2;
     S wx = q.w * x2, wy = q.w * y2, wz = q.w * z2;
@@ -514,8 +523,8 @@ struct GjkOut {
 };
 
 // gjkClosestPoints gjk.ts:1294-1546
-template <typename S, bool H>
-__device__ GjkOut<S> gjk(const Sup<S, H> &A, const Sup<S, H> &B, S tolerance, V<S> dir, S maxDistSq, Simplex<S> &sx) {
+template <typename S, class SA, class SB>
+__device__ GjkOut<S> gjk(const SA &A, const SB &B, S tolerance, V<S> dir, S maxDistSq, Simplex<S> &sx) {
     GjkOut<S> out;
     const S GJK_TOL = S(1e-5);
     S sqtol = tolerance * tolerance;
@@ -972,6 +981,7 @@ __device__ void emit_manifold(DevWorld &w, int a, int b, float3 pa, float3 pb, f
         m.ra[k] = k < pts.n ? pts.a[k] : f3(0.f, 0.f, 0.f);
         m.rb[k] = k < pts.n ? pts.b[k] : f3(0.f, 0.f, 0.f);
     }
+    m.sub_a = m.sub_b = 0xffffffffu;
     w.manifolds[slot] = m;
 }
 
@@ -980,6 +990,7 @@ struct EpaItem {
     int size;
     int pad;
     float3 y[4], p[4], q[4];
+    int tri;  // -1: a convex pair; else a = the convex body, b = the mesh body, this triangle
 };
 
 // narrowphase for one pair: order A/B (update.ts:74), dispatch, GJK
@@ -1006,6 +1017,13 @@ __global__ void __launch_bounds__(128) k_narrowphase(DevWorld w, EpaItem *epa_it
         float4 qa = w.quat[a], qb = w.quat[b];
         float4 sa = w.shape[a], sb = w.shape[b];
         int sha = shape_of(fa), shb = shape_of(fb);
+        if (sha == SHAPE_MESH || shb == SHAPE_MESH) {  // the mesh passes take these pairs
+            if (!HULLS) {
+                int k = atomicAdd(&w.ctr->num_mesh_pairs, 1);
+                if (k < w.max_pairs) w.mesh_pairs[k] = pi;
+            }
+            continue;
+        }
         if ((sha == SHAPE_HULL || shb == SHAPE_HULL) != HULLS) continue;
         if (sha == SHAPE_SPHERE && shb == SHAPE_SPHERE) {
             // collideSphereVsSphere sphere.ts:319-410 (no speculative distance)
@@ -1047,6 +1065,7 @@ __global__ void __launch_bounds__(128) k_narrowphase(DevWorld w, EpaItem *epa_it
             it.b = b;
             it.size = sx.size;
             it.pad = 0;
+            it.tri = -1;
             for (int k = 0; k < 4; k++) {
                 SP<float> s = sx.pts[k < sx.size ? k : 0];
                 it.y[k] = f3(s.y.x, s.y.y, s.y.z);
@@ -1509,7 +1528,8 @@ struct Hull {
         }
         return ne;
     }
-    __device__ int add_sup(const Sup<R> &A, const Sup<R> &B, V<R> d) {
+    template <class SA, class SB>
+    __device__ int add_sup(const SA &A, const SB &B, V<R> d) {
         if (npts >= pts_limit) {
             if (S::PACKED) overflow = true;
             return -1;
@@ -1534,8 +1554,8 @@ struct Hull {
 };
 
 // penetrationDepthStepEPA penetration.ts:214-614; true and the result on success
-template <class S>
-__device__ bool epa(Hull<S> &h, const Sup<R> &A, const Sup<R> &B, R tol, V<R> &outAxis,
+template <class S, class SA, class SB>
+__device__ bool epa(Hull<S> &h, const SA &A, const SB &B, R tol, V<R> &outAxis,
                     V<R> &outPa, V<R> &outPb) {
     const R MAXD = 1.7976931348623157e308;
     if (h.npts == 1) {
@@ -1669,7 +1689,8 @@ __device__ bool epa(Hull<S> &h, const Sup<R> &A, const Sup<R> &B, R tol, V<R> &o
 
 // Supports of one queued pair in A's local frame (convex.ts:440-452): EPA runs on the full
 // shapes with the speculative distance (at most 1) added to A as a radius.
-__device__ void epa_setup(const DevWorld &w, const EpaItem &it, Sup<R> &A, Sup<R> &B, R &maxSep) {
+template <bool H>
+__device__ void epa_setup(const DevWorld &w, const EpaItem &it, Sup<R, H> &A, Sup<R, H> &B, R &maxSep) {
     int a = it.a, b = it.b;
     uint32_t fa = w.flags[a], fb = w.flags[b];
     float maxSepF = ((fa | fb) & F_SENSOR) ? 0.f : c_settings.spec_dist;
@@ -1680,10 +1701,38 @@ __device__ void epa_setup(const DevWorld &w, const EpaItem &it, Sup<R> &A, Sup<R
     Q<R> rel = qmulS(iA, qB);
     V<R> ab{R(pb4.x) - R(pa4.x), R(pb4.y) - R(pa4.y), R(pb4.z) - R(pa4.z)};
     V<R> posBInA = qrotS(iA, ab);
-    A = make_sup<R>(shape_of(fa), w.shape[a], false, hull_view(w));
-    B = make_sup<R>(shape_of(fb), w.shape[b], false, hull_view(w));
+    A = make_sup<R, H>(shape_of(fa), w.shape[a], false, hull_view(w));
     A.add_r = maxSep;
+    B = make_sup<R, H>(shape_of(fb), w.shape[b], false, hull_view(w));
     set_transform(B, rel, posBInA);
+}
+
+// a mesh triangle's EPA (collideConvexVsTriangleMesh triangle-mesh.ts:1226-1247): A the convex
+// body with its radius and the separation, B the triangle's vertices in A's frame
+__device__ void epa_setup_mesh(const DevWorld &w, const EpaItem &it, Sup<R> &A, Sup<R, true, true> &B, R &maxSep) {
+    int a = it.a, b = it.b;
+    uint32_t fa = w.flags[a], fb = w.flags[b];
+    float maxSepF = ((fa | fb) & F_SENSOR) ? 0.f : c_settings.spec_dist;
+    maxSep = R(maxSepF < 1.f ? maxSepF : 1.f);
+    float4 pa4 = w.pos[a], pb4 = w.pos[b], qa = w.quat[a], qb = w.quat[b];
+    Q<R> iA{R(-qa.x), R(-qa.y), R(-qa.z), R(qa.w)};
+    Q<R> rel = qmulS(iA, Q<R>{R(qb.x), R(qb.y), R(qb.z), R(qb.w)});
+    V<R> posBInA = qrotS(iA, V<R>{R(pb4.x) - R(pa4.x), R(pb4.y) - R(pa4.y), R(pb4.z) - R(pa4.z)});
+    A = make_sup<R>(shape_of(fa), w.shape[a], false, hull_view(w));
+    A.add_r = maxSep;
+    const int4 t = w.mesh_tris[w.meshes[mesh_of(w.shape[b])].first_tri + it.tri];
+    const int vi[3] = {t.x, t.y, t.z};
+    V<R> v[3];
+    for (int k = 0; k < 3; k++) {
+        float4 m = w.mesh_verts[vi[k]];
+        v[k] = posBInA + qrotS(rel, V<R>{R(m.x), R(m.y), R(m.z)});
+    }
+    B = make_sup<R, true, true>(SHAPE_SPHERE, make_float4(0.f, 0.f, 0.f, 0.f), false, hull_view(w));
+    B.kind = SUP_TRIANGLE;
+    B.r0 = v[0];
+    B.r1 = v[1];
+    B.r2 = v[2];
+    B.convex_radius = R(0);
 }
 
 // The hit of one item (penetrationDepthStepEPA :502-548) written back into the item for
@@ -1696,7 +1745,8 @@ __device__ void epa_finish(const DevWorld &w, EpaItem &it, bool ok, R maxSep, V<
         return;
     }
     float4 qa = w.quat[it.a];
-    Q<R> qA{R(qa.x), R(qa.y), R(qa.z), R(qa.w)};
+    // mesh items keep the convex body's frame: the mesh pass fixes the normal there
+    Q<R> qA = it.tri >= 0 ? Q<R>{R(0), R(0), R(0), R(1)} : Q<R>{R(qa.x), R(qa.y), R(qa.z), R(qa.w)};
     V<R> dd = pa - pb;
     R penetration = sq_root(lsq(dd)) - maxSep;
     R al = sq_root(lsq(axis));
@@ -1714,10 +1764,12 @@ __device__ void epa_finish(const DevWorld &w, EpaItem &it, bool ok, R maxSep, V<
 // an FP64 warp instruction costs the same whatever the number of active lanes);
 // fetch_warp = 0: each thread takes its next item as soon as it finishes one.  Items that
 // outgrow the packed limits go to the fallback list.
+template <bool H>
 __device__ __forceinline__ void epa_packed_item(DevWorld &w, EpaItem *items, int i, Hull<PackedStore> &h,
                                                 int *fallback, int pts_limit) {
     EpaItem &it = items[i];
-    Sup<R> A, B;
+    if (it.tri >= 0) return;  // mesh triangles: k_epa_mesh
+    Sup<R, H> A, B;
     R maxSep;
     epa_setup(w, it, A, B, maxSep);
     h.start(it, pts_limit);
@@ -1730,6 +1782,8 @@ __device__ __forceinline__ void epa_packed_item(DevWorld &w, EpaItem *items, int
     epa_finish(w, it, ok, maxSep, axis, pa, pb);
 }
 
+// H: the world has convex hulls (without them the support code leaves the hull loop out)
+template <bool H>
 __global__ void __launch_bounds__(EPA_BLOCK) k_epa(DevWorld w, EpaItem *items, PackedBlock *blocks,
                                                    int *fallback, int pts_limit, int fetch_warp) {
     int ne = min(w.ctr->num_epa, w.max_epa);
@@ -1743,16 +1797,17 @@ __global__ void __launch_bounds__(EPA_BLOCK) k_epa(DevWorld w, EpaItem *items, P
             if (lane == 0) base = atomicAdd(&w.ctr->epa_cursor, 32);
             base = __shfl_sync(0xffffffffu, base, 0);
             if (base >= ne) break;
-            if (base + lane < ne) epa_packed_item(w, items, base + lane, h, fallback, pts_limit);
+            if (base + lane < ne) epa_packed_item<H>(w, items, base + lane, h, fallback, pts_limit);
             __syncwarp();
         }
     } else {
         for (int i = atomicAdd(&w.ctr->epa_cursor, 1); i < ne; i = atomicAdd(&w.ctr->epa_cursor, 1))
-            epa_packed_item(w, items, i, h, fallback, pts_limit);
+            epa_packed_item<H>(w, items, i, h, fallback, pts_limit);
     }
 }
 
 // Fallback pass with the reference's limits, for the items the packed pass handed over.
+template <bool H>
 __global__ void __launch_bounds__(EPA_BLOCK) k_epa_big(DevWorld w, EpaItem *items, EpaScratch *scratch,
                                                        const int *fallback) {
     int nf = w.ctr->epa_fallback;
@@ -1761,9 +1816,30 @@ __global__ void __launch_bounds__(EPA_BLOCK) k_epa_big(DevWorld w, EpaItem *item
     h.st.s = scratch + tid;
     for (int k = tid; k < nf; k += gridDim.x * blockDim.x) {
         EpaItem &it = items[fallback[k]];
-        Sup<R> A, B;
+        Sup<R, H> A, B;
         R maxSep;
         epa_setup(w, it, A, B, maxSep);
+        h.start(it);
+        V<R> axis, pa, pb;
+        bool ok = epa(h, A, B, R(c_settings.penetration_tol), axis, pa, pb);
+        epa_finish(w, it, ok, maxSep, axis, pa, pb);
+    }
+}
+
+// The mesh triangles' EPA items, with the reference's polytope limits (after the fallback pass,
+// whose scratch it reuses)
+__global__ void __launch_bounds__(EPA_BLOCK) k_epa_mesh(DevWorld w, EpaItem *items, EpaScratch *scratch) {
+    int ne = min(w.ctr->num_epa, w.max_epa);
+    int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    Hull<BigStore> h;
+    h.st.s = scratch + tid;
+    for (int k = tid; k < ne; k += gridDim.x * blockDim.x) {
+        EpaItem &it = items[k];
+        if (it.tri < 0) continue;
+        Sup<R> A;
+        Sup<R, true, true> B;
+        R maxSep;
+        epa_setup_mesh(w, it, A, B, maxSep);
         h.start(it);
         V<R> axis, pa, pb;
         bool ok = epa(h, A, B, R(c_settings.penetration_tol), axis, pa, pb);
@@ -1777,7 +1853,7 @@ __global__ void __launch_bounds__(128) k_epa_emit(DevWorld w, const EpaItem *ite
     int ne = min(w.ctr->num_epa, w.max_epa);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ne; i += gridDim.x * blockDim.x) {
         const EpaItem &it = items[i];
-        if (it.size != 1) continue;
+        if (it.size != 1 || it.tri >= 0) continue;
         bool hull = shape_of(w.flags[it.a]) == SHAPE_HULL || shape_of(w.flags[it.b]) == SHAPE_HULL;
         if (hull != HULLS) continue;
         emit_manifold<HULLS ? 32 : 16>(w, it.a, it.b, it.y[0], it.p[0], it.q[0], __int_as_float(it.pad), true);
@@ -1785,6 +1861,530 @@ __global__ void __launch_bounds__(128) k_epa_emit(DevWorld w, const EpaItem *ite
 }
 
 size_t epa_item_bytes() { return sizeof(EpaItem); }
+
+// ---------------------------------------------------------------------------
+// triangle meshes: collideConvexVsTriangleMesh triangle-mesh.ts:1026-1386 and
+// collideSphereVsTriangleMesh :1418-1712 into narrowphaseWithReductionCollector
+// (update.ts:385-558), one mesh pair per thread
+// ---------------------------------------------------------------------------
+constexpr int MESH_MAXM = 4;   // manifolds a mesh pair keeps (the reference's pool holds 32)
+constexpr int MESH_MAXP = 56;  // points of one manifold before its prune (at most 32 + one hit's)
+constexpr int MESH_STACK = 64;
+
+struct MeshReduce {
+    int nm;
+    float3 normal[MESH_MAXM];  // accumulated (unnormalised) normals
+    float depth[MESH_MAXM];
+    uint32_t sub_a[MESH_MAXM], sub_b[MESH_MAXM];
+    PtsN<MESH_MAXP> pts[MESH_MAXM];
+    bool dropped;  // a new normal group arrived with every slot taken
+};
+
+// addHit update.ts:385-519 (points relative to the base, the narrowphase's body A)
+template <int N>
+__device__ void mesh_add_hit(MeshReduce &r, float3 pa, float3 pb, float3 axis, float penetration, uint32_t sa,
+                             uint32_t sb, const FaceN<N> &fA, const FaceN<N> &fB) {
+    const float3 n = normalize3(axis);
+    int m = -1;
+    for (int i = 0; i < r.nm; i++)
+        if (dot3(n, r.normal[i]) >= c_settings.normal_cos) {
+            m = i;
+            break;
+        }
+    if (m < 0) {
+        if (r.nm >= MESH_MAXM) {
+            // pool full: the shallowest manifold makes way for a deeper hit
+            int sh = 0;
+            for (int i = 1; i < r.nm; i++)
+                if (r.depth[i] < r.depth[sh]) sh = i;
+            r.dropped = true;
+            if (penetration < r.depth[sh]) return;
+            m = sh;
+        } else {
+            m = r.nm++;
+        }
+        r.pts[m].n = 0;
+        r.normal[m] = n;
+        r.depth[m] = penetration;
+        r.sub_a[m] = sa;
+        r.sub_b[m] = sb;
+    } else {
+        r.normal[m] = r.normal[m] + n;
+    }
+    PtsN<N> tmp;
+    const float maxd = c_settings.spec_dist + c_settings.manifold_tol;
+    if (fA.n >= 2 && fB.n >= 3) {
+        manifold_faces(tmp, pa, pb, axis, maxd, fA, fB);
+    } else {
+        tmp.n = 1;
+        tmp.a[0] = pa;
+        tmp.b[0] = pb;
+    }
+    PtsN<MESH_MAXP> &P = r.pts[m];
+    for (int i = 0; i < tmp.n && P.n < 64 && P.n < MESH_MAXP; i++) {
+        P.a[P.n] = tmp.a[i];
+        P.b[P.n] = tmp.b[i];
+        P.n++;
+    }
+    if (penetration > r.depth[m]) r.depth[m] = penetration;
+    if (P.n > 32) prune(P, r.normal[m]);
+}
+
+// finalizeAndCreateConstraints update.ts:525-558: the manifolds into the contact pipeline
+__device__ void mesh_emit(DevWorld &w, MeshReduce &r, int a, int b, float3 base) {
+    for (int i = 0; i < r.nm; i++) {
+        PtsN<MESH_MAXP> &P = r.pts[i];
+        float3 nrm = normalize3(r.normal[i]);
+        if (P.n > 4) prune(P, nrm);
+        if (P.n <= 0) continue;
+        int slot = atomicAdd(&w.ctr->num_manifolds, 1);
+        if (slot >= w.max_manifolds) {
+            atomicOr(&w.ctr->overflow, OVF_MANIFOLDS);
+            return;
+        }
+        Manifold m;
+        m.a = a;
+        m.b = b;
+        m.n = P.n;
+        m.base = base;
+        m.normal = nrm;
+        m.depth = r.depth[i];
+        for (int k = 0; k < 4; k++) {
+            m.ra[k] = k < P.n ? P.a[k] : f3(0.f, 0.f, 0.f);
+            m.rb[k] = k < P.n ? P.b[k] : f3(0.f, 0.f, 0.f);
+        }
+        m.sub_a = r.sub_a[i];
+        m.sub_b = r.sub_b[i];
+        w.manifolds[slot] = m;
+    }
+    if (r.dropped) atomicAdd(&w.ctr->mesh_reduced, 1);
+}
+
+// fixNormal active-edges.ts:74-153 (shape A's frame, the point relative to A)
+__device__ float3 fix_normal(float3 v0, float3 v1, float3 v2, float3 tn, int active, float3 point, float3 normal,
+                             float3 move) {
+    if (active == 0b111) return normal;
+    const float nl = sqrtf(lensq3(normal)), tl = sqrtf(lensq3(tn));
+    if (dot3(move, normal) * tl < dot3(move, tn) * nl) return normal;
+    if (active == 0) return tn;
+    if (dot3(tn, normal) > 0.999848f * nl * tl) return normal;  // within 1 degree
+    Bary<float> bc = bary3(V<float>{v0.x - point.x, v0.y - point.y, v0.z - point.z},
+                           V<float>{v1.x - point.x, v1.y - point.y, v1.z - point.z},
+                           V<float>{v2.x - point.x, v2.y - point.y, v2.z - point.z}, 1e-10f);
+    const float E = 1.0e-4f, OME = 1.0f - 1.0e-4f;
+    int edge;
+    if (bc.u > OME)
+        edge = 0b101;
+    else if (bc.v > OME)
+        edge = 0b011;
+    else if (bc.w > OME)
+        edge = 0b110;
+    else if (bc.u < E)
+        edge = 0b010;
+    else if (bc.v < E)
+        edge = 0b100;
+    else if (bc.w < E)
+        edge = 0b001;
+    else
+        return tn;
+    return (active & edge) ? normal : tn;
+}
+
+// getClosestPointOnTriangle triangle.ts:62-197 (the query point at the origin); feature bits
+// A 1, B 2, C 4, edges their vertex pairs, the face 7
+__device__ float3 closest_on_triangle(float3 a, float3 b, float3 c, float &dsq, int &feature) {
+    float3 ab = b - a, ac = c - a;
+    float3 n = cross3(ab, ac);
+    float nl2 = lensq3(n);
+    if (nl2 < 1e-10f) {
+        // degenerate: the nearest of the vertices and edges (handleDegenerateTriangle :199-287)
+        float3 best = c;
+        feature = 0b100;
+        float bd = lensq3(c);
+        if (lensq3(a) < bd) {
+            best = a, bd = lensq3(a), feature = 0b001;
+        }
+        if (lensq3(b) < bd) {
+            best = b, bd = lensq3(b), feature = 0b010;
+        }
+        const float EPS2 = 1.1920929e-7f * 1.1920929e-7f;
+        auto edge = [&](float3 p, float3 e, int f) {
+            float el = lensq3(e);
+            if (el > EPS2) {
+                float v = fmaxf(0.f, fminf(1.f, -dot3(p, e) / el));
+                float3 q = p + e * v;
+                float d = lensq3(q);
+                if (d < bd) best = q, bd = d, feature = f;
+            }
+        };
+        edge(a, ac, 0b101);
+        edge(b, c - b, 0b110);
+        edge(a, ab, 0b011);
+        dsq = bd;
+        return best;
+    }
+    float d1 = -dot3(ab, a), d2 = -dot3(ac, a);
+    if (d1 <= 0.f && d2 <= 0.f) {
+        dsq = lensq3(a), feature = 0b001;
+        return a;
+    }
+    float d3 = -dot3(ab, b), d4 = -dot3(ac, b);
+    if (d3 >= 0.f && d4 <= d3) {
+        dsq = lensq3(b), feature = 0b010;
+        return b;
+    }
+    if (d1 * d4 <= d3 * d2 && d1 >= 0.f && d3 <= 0.f) {
+        float v = d1 / (d1 - d3);
+        float3 p = a + ab * v;
+        dsq = lensq3(p), feature = 0b011;
+        return p;
+    }
+    float d5 = -dot3(ab, c), d6 = -dot3(ac, c);
+    if (d6 >= 0.f && d5 <= d6) {
+        dsq = lensq3(c), feature = 0b100;
+        return c;
+    }
+    if (d5 * d2 <= d1 * d6 && d2 >= 0.f && d6 <= 0.f) {
+        float v = d2 / (d2 - d6);
+        float3 p = a + ac * v;
+        dsq = lensq3(p), feature = 0b101;
+        return p;
+    }
+    float d43 = d4 - d3, d56 = d5 - d6;
+    if (d3 * d6 <= d5 * d4 && d43 >= 0.f && d56 >= 0.f) {
+        float v = d43 / (d43 + d56);
+        float3 p = b + (c - b) * v;
+        dsq = lensq3(p), feature = 0b110;
+        return p;
+    }
+    float sc = dot3(a + b + c, n) / (3.f * nl2);
+    float3 p = n * sc;
+    dsq = lensq3(p), feature = 0b111;
+    return p;
+}
+
+__device__ __forceinline__ bool node_hits_box(const float4 &lo, const float4 &hi, float3 qlo, float3 qhi) {
+    return lo.x <= qhi.x && hi.x >= qlo.x && lo.y <= qhi.y && hi.y >= qlo.y && lo.z <= qhi.z && hi.z >= qlo.z;
+}
+
+// the convex shape's local bounds (box.ts:77-84, sphere, capsule.ts:84-94, convex-hull.ts:214-231)
+__device__ void convex_local_bounds(const DevWorld &w, uint32_t f, float4 sp, float3 &lo, float3 &hi) {
+    int s = shape_of(f);
+    if (s == SHAPE_HULL) {
+        const DevHull &h = w.hulls[hull_of(sp)];
+        lo = xyz(h.lo);
+        hi = xyz(h.hi);
+    } else if (s == SHAPE_BOX) {
+        lo = f3(-sp.x, -sp.y, -sp.z);
+        hi = f3(sp.x, sp.y, sp.z);
+    } else if (s == SHAPE_CAPSULE) {
+        lo = f3(-sp.x, -(sp.y + sp.x), -sp.x);
+        hi = f3(sp.x, sp.y + sp.x, sp.x);
+    } else {
+        lo = f3(-sp.x, -sp.x, -sp.x);
+        hi = f3(sp.x, sp.x, sp.x);
+    }
+}
+
+// One mesh pair.  PASS 0: pairs with no triangle in need of EPA are reduced and emitted; a
+// pair with some reserves one EPA item per such triangle, in traversal order, and waits.
+// PASS 1 (after the EPA passes): those pairs again, each such triangle taking its item.
+template <int PASS>
+__global__ void __launch_bounds__(64) k_mesh_narrowphase(DevWorld w, EpaItem *epa_items) {
+    const int npairs = min(w.ctr->num_mesh_pairs, w.max_pairs);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < npairs; k += gridDim.x * blockDim.x) {
+        if (PASS == 1 && w.mesh_epa_base[k] < 0) continue;
+        int2 pr = w.pairs[w.mesh_pairs[k]];
+        int a = pr.x, b = pr.y;
+        uint32_t fa = w.flags[a], fb = w.flags[b];
+        int ma = motion_of(fa), mb = motion_of(fb);
+        if (ma > mb || (ma == mb && b < a)) {  // narrowphase order (update.ts:74)
+            int t = a;
+            a = b;
+            b = t;
+            uint32_t tf = fa;
+            fa = fb;
+            fb = tf;
+        }
+        if (PASS == 0) w.mesh_epa_base[k] = -1;
+        const bool meshA = shape_of(fa) == SHAPE_MESH, meshB = shape_of(fb) == SHAPE_MESH;
+        if (meshA == meshB) continue;  // mesh against mesh: no collide function (triangle-mesh.ts:223-237)
+        // collideTriangleMeshVsConvex = the convex-vs-mesh function with the hit reversed
+        // (reversedCollideShapeVsShape collide-shape-vs-shape.ts:227-354)
+        const bool inverted = meshA;
+        const int cv = inverted ? b : a, mh = inverted ? a : b;
+        const uint32_t fc = inverted ? fb : fa;
+        const float3 base = xyz(w.pos[a]);
+        const float maxSepIn = ((fa | fb) & F_SENSOR) ? 0.f : c_settings.spec_dist;
+        const float4 qc4 = w.quat[cv], qm4 = w.quat[mh];
+        const float3 pc = xyz(w.pos[cv]), pm = xyz(w.pos[mh]);
+        const float3 cvRel = pc - base;  // the convex body's position relative to the base
+        const Q<float> qC{qc4.x, qc4.y, qc4.z, qc4.w}, iqC{-qc4.x, -qc4.y, -qc4.z, qc4.w};
+        const Q<float> qM{qm4.x, qm4.y, qm4.z, qm4.w}, iqM{-qm4.x, -qm4.y, -qm4.z, qm4.w};
+        // mesh into the convex body's frame, and the convex body into the mesh's frame
+        const Q<float> m2c = qmulS(iqC, qM);
+        const V<float> m2cPos = qrotS(iqC, V<float>{pm.x - pc.x, pm.y - pc.y, pm.z - pc.z});
+        const Q<float> cInM = qmulS(iqM, qC);
+        const V<float> cInMPos = qrotS(iqM, V<float>{pc.x - pm.x, pc.y - pm.y, pc.z - pm.z});
+        const DevMesh &M = w.meshes[mesh_of(w.shape[mh])];
+        const float4 sc = w.shape[cv];
+        const bool sphere = shape_of(fc) == SHAPE_SPHERE;
+        // activeEdgeMovementDirection: A's velocity minus B's in the narrowphase order (update.ts:729-733)
+        const float3 moveW = xyz(w.linvel[a]) - xyz(w.linvel[b]);
+        // query bounds in the mesh frame and the traversal's reference point
+        float3 qlo, qhi, qcenter, blo1, bhi1;
+        V<float> sphereC{0.f, 0.f, 0.f};
+        if (sphere) {
+            sphereC = cInMPos;
+            const float er = sc.x + maxSepIn;
+            qlo = f3(sphereC.x - er, sphereC.y - er, sphereC.z - er);
+            qhi = f3(sphereC.x + er, sphereC.y + er, sphereC.z + er);
+            qcenter = f3(sphereC.x, sphereC.y, sphereC.z);
+        } else {
+            float3 llo, lhi;
+            convex_local_bounds(w, fc, sc, llo, lhi);
+            blo1 = llo - f3(maxSepIn, maxSepIn, maxSepIn);
+            bhi1 = lhi + f3(maxSepIn, maxSepIn, maxSepIn);
+            // box3.transformMat4 of the local bounds (8 corners), grown by the separation
+            qlo = f3(3.0e38f, 3.0e38f, 3.0e38f);
+            qhi = f3(-3.0e38f, -3.0e38f, -3.0e38f);
+            for (int c = 0; c < 8; c++) {
+                V<float> p{(c & 1) ? lhi.x : llo.x, (c & 2) ? lhi.y : llo.y, (c & 4) ? lhi.z : llo.z};
+                V<float> q = qrotS(cInM, p) + cInMPos;
+                qlo = f3(fminf(qlo.x, q.x), fminf(qlo.y, q.y), fminf(qlo.z, q.z));
+                qhi = f3(fmaxf(qhi.x, q.x), fmaxf(qhi.y, q.y), fmaxf(qhi.z, q.z));
+            }
+            qlo = qlo - f3(maxSepIn, maxSepIn, maxSepIn);
+            qhi = qhi + f3(maxSepIn, maxSepIn, maxSepIn);
+            qcenter = (qlo + qhi) * 0.5f;
+        }
+        const HullView hv = hull_view(w);
+        Sup<float> supA;
+        if (!sphere) supA = make_sup<float>(shape_of(fc), sc, true, hv);
+        MeshReduce red;
+        red.nm = 0;
+        red.dropped = false;
+        int epa_needed = 0, epa_next = 0;
+        const int epa_base = PASS == 1 ? w.mesh_epa_base[k] : -1;
+        const int epa_count = PASS == 1 ? w.mesh_epa_count[k] : 0;
+        for (int round = 0; round < 2; round++) {  // PASS 0 runs a second round to fill the EPA items
+            if (round == 1 && (PASS == 1 || epa_needed == 0)) break;
+            int reserve = -1;
+            if (round == 1) {
+                // the whole block or nothing: the EPA passes read every item below min(num_epa, max_epa)
+                int cur = *(volatile int *)&w.ctr->num_epa;
+                for (int guard = 0; guard < (1 << 20); guard++) {
+                    if (cur + epa_needed > w.max_epa) break;
+                    int prev = atomicCAS(&w.ctr->num_epa, cur, cur + epa_needed);
+                    if (prev == cur) {
+                        reserve = cur;
+                        break;
+                    }
+                    cur = prev;
+                }
+                if (reserve < 0) {
+                    atomicOr(&w.ctr->overflow, OVF_EPA);
+                    break;
+                }
+                w.mesh_epa_base[k] = reserve;
+                w.mesh_epa_count[k] = epa_needed;
+                epa_next = 0;
+            }
+            int stack[MESH_STACK];
+            int sp = 0;
+            stack[sp++] = 0;
+            while (sp > 0) {
+                const int node = stack[--sp];
+                const float4 nlo = w.mesh_nodes[2 * (M.first_node + node)], nhi = w.mesh_nodes[2 * (M.first_node + node) + 1];
+                if (!node_hits_box(nlo, nhi, qlo, qhi)) continue;
+                const int aux = __float_as_int(nlo.w), tag = __float_as_int(nhi.w);
+                if (tag >= 0) {
+                    // internal: the nearer child (centre to centre) is visited first
+                    const int left = node + 1, right = aux;
+                    float4 l0 = w.mesh_nodes[2 * (M.first_node + left)], l1 = w.mesh_nodes[2 * (M.first_node + left) + 1];
+                    float4 r0 = w.mesh_nodes[2 * (M.first_node + right)], r1 = w.mesh_nodes[2 * (M.first_node + right) + 1];
+                    float ld = lensq3(qcenter - (xyz(l0) + xyz(l1)) * 0.5f);
+                    float rd = lensq3(qcenter - (xyz(r0) + xyz(r1)) * 0.5f);
+                    if (sp + 2 > MESH_STACK) {
+                        atomicOr(&w.ctr->overflow, OVF_SLOTS);
+                        continue;
+                    }
+                    if (ld <= rd) {
+                        stack[sp++] = right;
+                        stack[sp++] = left;
+                    } else {
+                        stack[sp++] = left;
+                        stack[sp++] = right;
+                    }
+                    continue;
+                }
+                const int tcount = -tag - 1;
+                for (int ti = aux; ti < aux + tcount; ti++) {
+                    const int4 tr = w.mesh_tris[M.first_tri + ti];
+                    const float3 m0 = xyz(w.mesh_verts[tr.x]), m1 = xyz(w.mesh_verts[tr.y]), m2 = xyz(w.mesh_verts[tr.z]);
+                    const uint32_t tsub = M.sub_bits >= 32 ? (uint32_t)ti
+                                                           : ((0xffffffffu & ~((1u << M.sub_bits) - 1u)) | (uint32_t)ti);
+                    float3 hpa, hpb, hax;  // hit in the convex-first order, relative to the base
+                    float hpen;
+                    FaceN<32> fConvex, fTri;
+                    fConvex.n = 0;
+                    fTri.n = 0;
+                    if (sphere) {
+                        // collideSphereVsTriangleMesh triangle-mesh.ts:1510-1646, in the mesh frame
+                        const float r = sc.x;
+                        const float3 c = f3(sphereC.x, sphereC.y, sphereC.z);
+                        const float3 v0 = m0 - c, v1 = m1 - c, v2 = m2 - c;
+                        const float3 tn = cross3(v1 - v0, v2 - v0);
+                        const bool back = dot3(tn, v0) > 0.f;
+                        if (back) continue;
+                        float dsq;
+                        int feature;
+                        float3 p2 = closest_on_triangle(v0, v1, v2, dsq, feature);
+                        if (dsq > (r + maxSepIn) * (r + maxSepIn)) continue;
+                        hpen = r - sqrtf(dsq);
+                        float3 ax = dsq > 0.f ? normalize3(p2) : f3(0.f, 1.f, 0.f);
+                        const float3 p1 = ax * r;
+                        const int feat_edges[8] = {0b000, 0b101, 0b011, 0b001, 0b110, 0b100, 0b010, 0b000};
+                        if (feature != 0b111 && tr.w != 0b111 && (tr.w & feat_edges[feature]) == 0) {
+                            const V<float> mv = qrotS(iqM, V<float>{moveW.x, moveW.y, moveW.z});
+                            const float3 mvm = f3(mv.x, mv.y, mv.z);
+                            const float3 nax = back ? tn : -tn;
+                            if (dot3(mvm, ax) * sqrtf(lensq3(nax)) >= dot3(mvm, nax)) ax = nax;
+                        }
+                        auto to_base = [&](float3 v) {
+                            V<float> q = qrotS(qM, V<float>{v.x, v.y, v.z});
+                            return f3(q.x, q.y, q.z) + (pm - base);
+                        };
+                        hpa = to_base(c + p1);
+                        hpb = to_base(c + p2);
+                        V<float> aw = qrotS(qM, V<float>{ax.x, ax.y, ax.z});
+                        hax = f3(aw.x, aw.y, aw.z);
+                        fTri.n = 3;
+                        fTri.v[0] = to_base(m0);
+                        fTri.v[1] = to_base(m1);
+                        fTri.v[2] = to_base(m2);
+                    } else {
+                        // collideConvexVsTriangleMesh triangle-mesh.ts:1140-1386, in the convex body's frame
+                        auto to_c = [&](float3 v) {
+                            V<float> q = qrotS(m2c, V<float>{v.x, v.y, v.z}) + m2cPos;
+                            return f3(q.x, q.y, q.z);
+                        };
+                        const float3 t0 = to_c(m0), t1 = to_c(m1), t2 = to_c(m2);
+                        const float3 tlo = f3(fminf(t0.x, fminf(t1.x, t2.x)), fminf(t0.y, fminf(t1.y, t2.y)),
+                                              fminf(t0.z, fminf(t1.z, t2.z)));
+                        const float3 thi = f3(fmaxf(t0.x, fmaxf(t1.x, t2.x)), fmaxf(t0.y, fmaxf(t1.y, t2.y)),
+                                              fmaxf(t0.z, fmaxf(t1.z, t2.z)));
+                        if (!(tlo.x <= bhi1.x && thi.x >= blo1.x && tlo.y <= bhi1.y && thi.y >= blo1.y &&
+                              tlo.z <= bhi1.z && thi.z >= blo1.z))
+                            continue;
+                        const float3 tn = cross3(t1 - t0, t2 - t0);
+                        if (dot3(tn, t0) > 0.f) continue;  // back facing
+                        Sup<float, true, true> supT =
+                            make_sup<float, true, true>(SHAPE_SPHERE, make_float4(0.f, 0.f, 0.f, 0.f), false, hv);
+                        supT.kind = SUP_TRIANGLE;
+                        supT.r0 = V<float>{t0.x, t0.y, t0.z};
+                        supT.r1 = V<float>{t1.x, t1.y, t1.z};
+                        supT.r2 = V<float>{t2.x, t2.y, t2.z};
+                        supT.convex_radius = 0.f;
+                        V<float> axis{-tn.x, -tn.y, -tn.z};
+                        if (lsq(axis) < 1e-10f)
+                            axis = {1.f, 0.f, 0.f};
+                        else
+                            axis = axis * (1.f / sq_root(lsq(axis)));
+                        float maxSep = maxSepIn;
+                        const float rA = supA.convex_radius + maxSep;
+                        Simplex<float> sx;
+                        GjkOut<float> g = gjk(supA, supT, c_settings.collision_tol, axis, rA * rA, sx);
+                        if (g.sqdist > rA * rA) continue;  // NOT_COLLIDING
+                        V<float> pa, pb, pax;
+                        if (!(g.sqdist > 0.f)) {
+                            // INDETERMINATE: EPA in FP64 (penetrationDepthStepEPA) through the EPA passes
+                            maxSep = fminf(maxSep, 1.f);
+                            if (PASS == 0) {
+                                if (round == 0) {
+                                    epa_needed++;
+                                    continue;
+                                }
+                                EpaItem it;
+                                it.a = cv;
+                                it.b = mh;
+                                it.tri = ti;
+                                it.size = sx.size;
+                                it.pad = 0;
+                                for (int q = 0; q < 4; q++) {
+                                    SP<float> s = sx.pts[q < sx.size ? q : 0];
+                                    it.y[q] = f3(s.y.x, s.y.y, s.y.z);
+                                    it.p[q] = f3(s.p.x, s.p.y, s.p.z);
+                                    it.q[q] = f3(s.q.x, s.q.y, s.q.z);
+                                }
+                                if (epa_next < epa_needed) epa_items[reserve + epa_next++] = it;
+                                continue;
+                            }
+                            if (epa_next >= epa_count) continue;
+                            const EpaItem &it = epa_items[epa_base + epa_next++];
+                            if (it.size != 1) continue;  // EPA found no contact
+                            pa = V<float>{it.y[0].x, it.y[0].y, it.y[0].z};
+                            pb = V<float>{it.p[0].x, it.p[0].y, it.p[0].z};
+                            pax = V<float>{it.q[0].x, it.q[0].y, it.q[0].z};
+                            hpen = __int_as_float(it.pad);
+                        } else {
+                            if (PASS == 0 && round == 1) continue;  // only the EPA items are filled
+                            // COLLIDING: penetrationDepthStepGJK penetration.ts:84-106
+                            const float vl = sqrtf(g.sqdist);
+                            pa = g.pa + g.axis * (rA / vl);
+                            pb = g.pb;
+                            pax = g.axis;
+                            V<float> dd = pa - pb;
+                            hpen = sqrtf(lsq(dd)) - maxSep;
+                            const float al = sqrtf(lsq(pax));
+                            if (al > 0.f) pa = pa + pax * (-(maxSep / al));
+                        }
+                        if (PASS == 0 && round == 1) continue;
+                        if (tr.w != 0b111) {  // active edges: fixNormal
+                            const V<float> mv = qrotS(iqC, V<float>{moveW.x, moveW.y, moveW.z});
+                            float3 fixed = fix_normal(t0, t1, t2, -tn, tr.w, f3(pb.x, pb.y, pb.z),
+                                                      f3(pax.x, pax.y, pax.z), f3(mv.x, mv.y, mv.z));
+                            pax = V<float>{fixed.x, fixed.y, fixed.z};
+                        }
+                        auto to_base = [&](V<float> v) {
+                            V<float> q = qrotS(qC, v);
+                            return f3(q.x, q.y, q.z) + cvRel;
+                        };
+                        hpa = to_base(pa);
+                        hpb = to_base(pb);
+                        V<float> aw = qrotS(qC, pax);
+                        hax = f3(aw.x, aw.y, aw.z);
+                        // supporting faces: the convex shape's along -axis, the triangle
+                        const float3 axl = f3(pax.x, pax.y, pax.z);
+                        const int s = shape_of(fc);
+                        if (s == SHAPE_BOX) box_face(fConvex, -axl, sc, qc4, cvRel);
+                        if (s == SHAPE_CAPSULE) capsule_face(fConvex, -axl, sc, qc4, cvRel);
+                        if (s == SHAPE_HULL) hull_face(fConvex, -axl, w, sc, qc4, cvRel);
+                        fTri.n = 3;
+                        fTri.v[0] = to_base(V<float>{t0.x, t0.y, t0.z});
+                        fTri.v[1] = to_base(V<float>{t1.x, t1.y, t1.z});
+                        fTri.v[2] = to_base(V<float>{t2.x, t2.y, t2.z});
+                    }
+                    atomicAdd(&w.ctr->num_mesh_hits, 1);
+                    if (inverted)  // the inverted collector: points, axis, sub-shape ids and faces swapped
+                        mesh_add_hit(red, hpb, hpa, -hax, hpen, tsub, 0xffffffffu, fTri, fConvex);
+                    else
+                        mesh_add_hit(red, hpa, hpb, hax, hpen, 0xffffffffu, tsub, fConvex, fTri);
+                }
+            }
+        }
+        if (PASS == 0 && epa_needed > 0) continue;  // finished by the second pass
+        mesh_emit(w, red, a, b, base);
+    }
+}
+
+void launch_mesh_narrowphase(DevWorld &w, int pass, cudaStream_t s) {
+    EpaItem *items = (EpaItem *)w.epa_items;
+    if (pass == 0)
+        k_mesh_narrowphase<0><<<NUM_SMS * 4, 64, 0, s>>>(w, items);
+    else
+        k_mesh_narrowphase<1><<<NUM_SMS * 4, 64, 0, s>>>(w, items);
+}
 
 // ---------------------------------------------------------------------------
 // continuous collision: the shape cast of each LINEAR_CAST body against the world
@@ -1982,6 +2582,9 @@ __global__ void __launch_bounds__(128) k_ccd_find(DevWorld w, const int2 *node_w
             if (!((ga.x & gb.y) != 0u && (gb.x & ga.y) != 0u)) continue;
             // ccdBodyVisitor.visit update.ts:1153-1206
             if (b == a) continue;
+            // casts against triangle meshes (castConvexVsTriangleMesh triangle-mesh.ts:1784-2100)
+            // are not built: a mesh body is not a cast candidate
+            if (shape_of(fb) == SHAPE_MESH) continue;
             const int cb = w.ccd_index[b];
             if (cb >= 0 && a > b) continue;  // a pair of cast bodies is cast once, by the lower index
             if (fb & F_SENSOR) continue;
@@ -2043,17 +2646,31 @@ void launch_ccd_find(DevWorld &w, float dt, cudaStream_t s) {
     k_ccd_find<<<grid_for(w.n, 128, 16), 128, 0, s>>>(w, w.node_world, dt);
 }
 
+void launch_mesh_narrowphase(DevWorld &w, int pass, cudaStream_t s);
+
 void launch_narrowphase(DevWorld &w, float, cudaStream_t s, cudaEvent_t mid) {
     EpaItem *items = (EpaItem *)w.epa_items;
     k_narrowphase<false><<<NUM_SMS * 8, 128, 0, s>>>(w, items);
     if (w.num_hulls > 0) k_narrowphase<true><<<NUM_SMS * 8, 128, 0, s>>>(w, items);
+    if (w.num_mesh_bodies > 0) launch_mesh_narrowphase(w, 0, s);
     if (mid) cudaEventRecord(mid, s);
-    k_epa<<<w.epa_threads / EPA_BLOCK, EPA_BLOCK, 0, s>>>(w, items, (PackedBlock *)w.epa_packed, w.epa_fallback,
-                                                          w.epa_packed_points, w.epa_fetch_warp);
-    k_epa_big<<<EPA_BIG_THREADS / EPA_BLOCK, EPA_BLOCK, 0, s>>>(w, items, (EpaScratch *)w.epa_scratch,
-                                                                w.epa_fallback);
+    if (w.num_hulls > 0) {
+        k_epa<true><<<w.epa_threads / EPA_BLOCK, EPA_BLOCK, 0, s>>>(
+            w, items, (PackedBlock *)w.epa_packed, w.epa_fallback, w.epa_packed_points, w.epa_fetch_warp);
+        k_epa_big<true><<<EPA_BIG_THREADS / EPA_BLOCK, EPA_BLOCK, 0, s>>>(w, items, (EpaScratch *)w.epa_scratch,
+                                                                          w.epa_fallback);
+    } else {
+        k_epa<false><<<w.epa_threads / EPA_BLOCK, EPA_BLOCK, 0, s>>>(
+            w, items, (PackedBlock *)w.epa_packed, w.epa_fallback, w.epa_packed_points, w.epa_fetch_warp);
+        k_epa_big<false><<<EPA_BIG_THREADS / EPA_BLOCK, EPA_BLOCK, 0, s>>>(w, items, (EpaScratch *)w.epa_scratch,
+                                                                           w.epa_fallback);
+    }
     k_epa_emit<false><<<NUM_SMS * 8, 128, 0, s>>>(w, items);
     if (w.num_hulls > 0) k_epa_emit<true><<<NUM_SMS * 8, 128, 0, s>>>(w, items);
+    if (w.num_mesh_bodies > 0) {
+        k_epa_mesh<<<EPA_BIG_THREADS / EPA_BLOCK, EPA_BLOCK, 0, s>>>(w, items, (EpaScratch *)w.epa_scratch);
+        launch_mesh_narrowphase(w, 1, s);
+    }
 }
 
 // ---------------------------------------------------------------------------

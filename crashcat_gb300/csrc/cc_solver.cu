@@ -125,6 +125,22 @@ __device__ __forceinline__ float inv_eff_mass(bool dynA, bool dynB, float imA, f
 }
 
 // ---------------------------------------------------------------------------
+// Contact cache key (the contact's (idA, idB, subShapeIdA, subShapeIdB), contacts.ts:481-513):
+// (A << 32) | B for convex pairs; with a mesh triangle, bit 63 set and A, B and the triangle
+// index in 21 bits each (the triangle index is the low bits of the mesh's sub-shape id)
+__device__ __forceinline__ unsigned long long contact_key(const DevWorld &w, int A, int B, uint32_t subA,
+                                                          uint32_t subB) {
+    if (subA == 0xffffffffu && subB == 0xffffffffu)
+        return ((unsigned long long)(unsigned)A << 32) | (unsigned)B;
+    const uint32_t sub = subA != 0xffffffffu ? subA : subB;
+    const int mb = subA != 0xffffffffu ? A : B;
+    const int bits = w.meshes[mesh_of(w.shape[mb])].sub_bits;
+    const uint32_t tri = bits >= 32 ? sub : (sub & ((1u << bits) - 1u));
+    const unsigned long long M = (1ull << MESH_KEY_BITS) - 1ull;
+    return (1ull << 63) | (((unsigned long long)A & M) << 42) | (((unsigned long long)B & M) << 21) |
+           ((unsigned long long)tri & M);
+}
+
 // contact setup: one manifold per thread
 // ---------------------------------------------------------------------------
 __global__ void k_contact_setup(DevWorld w, CacheTables ct, float dt) {
@@ -138,6 +154,7 @@ __global__ void k_contact_setup(DevWorld w, CacheTables ct, float dt) {
         Manifold m = w.manifolds[mi];
         float3 base = m.base;
         int A = m.a, B = m.b;
+        uint32_t subA = m.sub_a, subB = m.sub_b;
         float3 nrm = m.normal;
         float3 ra[4], rb[4];
         for (int k = 0; k < 4; k++) {
@@ -148,6 +165,9 @@ __global__ void k_contact_setup(DevWorld w, CacheTables ct, float dt) {
             int t = A;
             A = B;
             B = t;
+            uint32_t ts = subA;
+            subA = subB;
+            subB = ts;
             nrm = -nrm;
             for (int k = 0; k < 4; k++) {
                 float3 tt = ra[k];
@@ -155,7 +175,7 @@ __global__ void k_contact_setup(DevWorld w, CacheTables ct, float dt) {
                 rb[k] = tt;
             }
         }
-        unsigned long long key = ((unsigned long long)(unsigned)A << 32) | (unsigned)B;
+        unsigned long long key = contact_key(w, A, B, subA, subB);
         int prev = cache_find(pkeys, w.cache_cap, key);
         int slot = cache_insert(ckeys, w.cache_cap, key);
         if (slot < 0) {
@@ -206,7 +226,7 @@ __global__ void k_contact_setup(DevWorld w, CacheTables ct, float dt) {
         c.t2 = cross3(nrm, c.t1);
         c.invMassA = ia.w;
         c.invMassB = ib.w;
-        c.sort_key = contact_sort_key(A, B, 0xffffffffu, 0xffffffffu);
+        c.sort_key = contact_sort_key(A, B, subA, subB);
         c.cache_slot = slot;
         c.pad0 = prev;  // record of the previous step's table this contact was matched with (-1: none)
         c.pad1 = 0;

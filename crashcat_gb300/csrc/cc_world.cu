@@ -17,6 +17,7 @@
 #include "cc_internal.cuh"
 #include "cc_swing.cuh"
 #include "cc_hull.h"
+#include "cc_mesh.h"
 
 using namespace cc;
 
@@ -36,6 +37,7 @@ struct cc_world {
     std::vector<DevHinge> hinges;  // host copy of each joint as created (bodies, flags, limits, motors)
     std::vector<DevSwing> swings;
     std::vector<cc_hull::Hull> hulls;  // convex hull shapes as built
+    std::vector<cc_mesh::Mesh> meshes;  // triangle meshes as built
     float *d_state_rows = nullptr;  // 16 floats per body staging for get/set state
     float *h_pinned_rows = nullptr;
     DevCounters *h_ctr = nullptr;   // pinned mirror of the device counters
@@ -508,7 +510,9 @@ int cc_world_destroy(cc_world *W) {
                     w.giant_list, w.giant_claim, w.giant_count, w.small_joint_list, w.large_joint_list,
                     w.hulls, w.hull_points, w.hull_shrunk,
                     w.hull_planes, w.hull_faces, w.hull_vidx, w.ccd_flag, w.ccd_slot, w.ccd_index, w.ccd,
-                    w.ccd_world_off, w.ccd_world_fill, w.ccd_seg, w.ccd_lambda, w.ccd_scan_tmp};
+                    w.ccd_world_off, w.ccd_world_fill, w.ccd_seg, w.ccd_lambda, w.ccd_scan_tmp,
+                    w.meshes, w.mesh_verts, w.mesh_tris, w.mesh_nodes, w.mesh_pairs, w.mesh_epa_base,
+                    w.mesh_epa_count};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : W->adj.allocs)
@@ -547,8 +551,20 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
     for (int i = 0; i < n; i++) {
         const cc_body_desc &d = b[i];
         if (d.shape_type != CC_SHAPE_BOX && d.shape_type != CC_SHAPE_SPHERE && d.shape_type != CC_SHAPE_CAPSULE &&
-            d.shape_type != CC_SHAPE_CONVEX_HULL)
+            d.shape_type != CC_SHAPE_CONVEX_HULL && d.shape_type != CC_SHAPE_TRIANGLE_MESH)
             return CC_ERR_UNSUPPORTED;
+        const cc_mesh::Mesh *mesh = nullptr;
+        int mesh_index = -1;
+        if (d.shape_type == CC_SHAPE_TRIANGLE_MESH) {
+            mesh_index = (int)d.shape_params[0];
+            if (!(d.shape_params[0] == (float)mesh_index) || mesh_index < 0 || mesh_index >= (int)W->meshes.size())
+                return CC_ERR_INVALID;
+            // a mesh has no mass (triangle-mesh.ts:153-158): static or kinematic bodies only
+            if (d.motion_type == CC_DYNAMIC) return CC_ERR_INVALID;
+            // the contact key packs body indices in 21 bits
+            if (w.cap >= (1 << MESH_KEY_BITS)) return CC_ERR_UNSUPPORTED;
+            mesh = &W->meshes[mesh_index];
+        }
         const cc_hull::Hull *hull = nullptr;
         int hull_index = -1;
         if (d.shape_type == CC_SHAPE_CONVEX_HULL) {
@@ -566,7 +582,10 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
         double mass;
         double idiag[3];
         double irot[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};  // principal axes (columns)
-        if (hull) {
+        if (mesh) {
+            mass = 0.0;  // computeMassProperties triangle-mesh.ts:153-158
+            idiag[0] = idiag[1] = idiag[2] = 0.0;
+        } else if (hull) {
             // computeMassProperties convex-hull.ts:453-459, principal axes of the inertia
             mass = hull->volume * d.density;
             double I[9];
@@ -600,7 +619,7 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
         int dof = d.allowed_dofs & 63;
         float inv_mass = 0.f;
         float3 inv_i = f3(0.f, 0.f, 0.f);
-        if (d.motion_type != CC_STATIC) {
+        if (d.motion_type != CC_STATIC && !mesh) {
             if ((dof & 7) != 0) {
                 if (!(mass > 0)) return CC_ERR_INVALID;
                 inv_mass = (float)(1.0 / mass);
@@ -637,6 +656,11 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
             memcpy(&hi_bits, &hull_index, sizeof(float));
             sh[i] = make_float4(hi_bits, (float)hull->convex_radius, 0.f, 0.f);
         }
+        if (mesh) {
+            float mi_bits;
+            memcpy(&mi_bits, &mesh_index, sizeof(float));
+            sh[i] = make_float4(mi_bits, 0.f, 0.f, 0.f);
+        }
         mat[i] = make_float4(d.friction, d.restitution, d.gravity_factor, 0.f);
         damp[i] = make_float4(d.linear_damping, d.angular_damping, d.max_linear_velocity, d.max_angular_velocity);
         uint32_t f = (uint32_t)d.motion_type;
@@ -651,7 +675,9 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
         groups[i] = make_uint2(d.collision_groups, d.collision_mask);
         world[i] = d.world;
         // resetSleepTimer sleep.ts:123-130
-        float3 e = hull ? f3((float)(0.5 * (hull->hi.x - hull->lo.x)), (float)(0.5 * (hull->hi.y - hull->lo.y)),
+        float3 e = mesh   ? f3((float)(0.5 * (mesh->hi[0] - mesh->lo[0])), (float)(0.5 * (mesh->hi[1] - mesh->lo[1])),
+                               (float)(0.5 * (mesh->hi[2] - mesh->lo[2])))
+                   : hull ? f3((float)(0.5 * (hull->hi.x - hull->lo.x)), (float)(0.5 * (hull->hi.y - hull->lo.y)),
                              (float)(0.5 * (hull->hi.z - hull->lo.z)))
                    : d.shape_type == CC_SHAPE_BOX
                        ? f3(d.shape_params[0], d.shape_params[1], d.shape_params[2])
@@ -697,8 +723,19 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
     CC_TRY(cudaMemcpyAsync(w.sleep_sph + 3 * o, sph.data(), sizeof(float4) * 3 * n, cudaMemcpyHostToDevice, s));
     CC_TRY(cudaMemcpyAsync(w.sleep_timer + o, timer.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
     CC_TRY(cudaStreamSynchronize(s));
-    int lc = 0;
-    for (int i = 0; i < n; i++) lc += (flags[i] & F_LINEAR_CAST) != 0;
+    int lc = 0, mc = 0;
+    for (int i = 0; i < n; i++) {
+        lc += (flags[i] & F_LINEAR_CAST) != 0;
+        mc += shape_of(flags[i]) == SHAPE_MESH;
+    }
+    if (mc > 0 && !w.mesh_pairs) {
+        int r;
+        if ((r = dalloc(&w.mesh_pairs, (size_t)w.max_pairs)) != CC_OK ||
+            (r = dalloc(&w.mesh_epa_base, (size_t)w.max_pairs)) != CC_OK ||
+            (r = dalloc(&w.mesh_epa_count, (size_t)w.max_pairs)) != CC_OK)
+            return r;
+    }
+    w.num_mesh_bodies += mc;
     if (lc > 0) {
         int r = ensure_ccd_buffers(W);
         if (r != CC_OK) return r;
@@ -887,6 +924,32 @@ int cc_world_get_pairs(cc_world *W, int32_t *out, int32_t capacity, int32_t *cou
     return CC_OK;
 }
 
+int cc_world_get_manifold_sub_shapes(cc_world *W, uint32_t *out, int32_t capacity, int32_t *count) {
+    if (!W || !count) return CC_ERR_INVALID;
+    DevWorld &w = W->w;
+    int nm = W->last_ctr.num_manifolds;
+    if (nm > w.max_manifolds) nm = w.max_manifolds;
+    std::vector<Manifold> ms(nm);
+    std::vector<int> cm(nm);
+    if (nm > 0) {
+        CC_TRY(cudaMemcpy(ms.data(), w.manifolds, sizeof(Manifold) * nm, cudaMemcpyDeviceToHost));
+        CC_TRY(cudaMemcpy(cm.data(), w.cons_of_manifold, sizeof(int) * nm, cudaMemcpyDeviceToHost));
+    }
+    int k = 0;
+    for (int i = 0; i < nm; i++) {
+        if (cm[i] < 0) continue;
+        if (out && k >= capacity) return CC_ERR_CAPACITY;
+        if (out) {
+            bool swap = ms[i].a > ms[i].b;
+            out[2 * k] = swap ? ms[i].sub_b : ms[i].sub_a;
+            out[2 * k + 1] = swap ? ms[i].sub_a : ms[i].sub_b;
+        }
+        k++;
+    }
+    *count = k;
+    return CC_OK;
+}
+
 int cc_world_get_manifolds(cc_world *W, float *out, int32_t capacity, int32_t *count) {
     if (!W || !count) return CC_ERR_INVALID;
     DevWorld &w = W->w;
@@ -1033,7 +1096,15 @@ int cc_world_get_contact_events(cc_world *W, int32_t *out, int32_t capacity, int
         int a = man[i].a, b = man[i].b;
         rows.push_back({ev[i], a < b ? a : b, a < b ? b : a});
     }
-    for (int i = 0; i < nr; i++) rows.push_back({3, (int32_t)(rk[i] >> 32), (int32_t)(rk[i] & 0xffffffffu)});
+    for (int i = 0; i < nr; i++) {
+        const unsigned long long k = rk[i];
+        if (k >> 63) {  // a mesh triangle's contact: A, B and the triangle in 21 bits each
+            const unsigned long long M = (1ull << MESH_KEY_BITS) - 1ull;
+            rows.push_back({3, (int32_t)((k >> 42) & M), (int32_t)((k >> 21) & M)});
+        } else {
+            rows.push_back({3, (int32_t)(k >> 32), (int32_t)(k & 0xffffffffu)});
+        }
+    }
     std::sort(rows.begin(), rows.end());
     *count = (int32_t)rows.size();
     int32_t k = 0;
@@ -1733,6 +1804,147 @@ static int upload_hulls(cc_world *W) {
 extern "C" {
 
 }  // extern "C"
+// ---------------------------------------------------------------------------
+// triangle meshes (triangleMesh.create triangle-mesh.ts:114-140)
+// ---------------------------------------------------------------------------
+static int build_mesh_from(const double *positions, int32_t nv, const int32_t *indices, int32_t nt, double degenerate,
+                           double active_cos, cc_mesh::Mesh &m) {
+    if (!positions || !indices || nv < 0 || nt < 0) return CC_ERR_INVALID;
+    for (int i = 0; i < 3 * nt; i++)
+        if (indices[i] < 0 || indices[i] >= nv) return CC_ERR_INVALID;
+    std::vector<double> p((size_t)3 * nv);
+    for (size_t i = 0; i < p.size(); i++) {
+        p[i] = positions[i];
+        if (!std::isfinite(p[i])) return CC_ERR_INVALID;
+    }
+    cc_mesh::BuildSettings bs;
+    if (degenerate >= 0.0) bs.degenerate_tolerance = degenerate;
+    if (active_cos >= -1.0) bs.active_edge_cos = active_cos;
+    m = cc_mesh::build(p.data(), nv, indices, nt, nullptr, bs);
+    if ((int)m.active.size() >= (1 << MESH_KEY_BITS)) return CC_ERR_UNSUPPORTED;
+    return CC_OK;
+}
+
+// every mesh's arrays, concatenated and uploaded again whenever a mesh is added
+static int upload_meshes(cc_world *W) {
+    DevWorld &w = W->w;
+    std::vector<DevMesh> hdr;
+    std::vector<float4> verts, nodes;
+    std::vector<int4> tris;
+    for (const cc_mesh::Mesh &m : W->meshes) {
+        DevMesh d;
+        memset(&d, 0, sizeof(d));
+        d.first_vertex = (int)verts.size();
+        d.first_tri = (int)tris.size();
+        d.first_node = (int)(nodes.size() / 2);
+        d.num_tris = (int)m.active.size();
+        unsigned maxi = d.num_tris > 0 ? (unsigned)(d.num_tris - 1) : 0u;
+        d.sub_bits = maxi == 0 ? 0 : 32 - __builtin_clz(maxi);
+        d.lo = make_float4((float)m.lo[0], (float)m.lo[1], (float)m.lo[2], 0.f);
+        d.hi = make_float4((float)m.hi[0], (float)m.hi[1], (float)m.hi[2], 0.f);
+        for (size_t k = 0; k < m.positions.size() / 3; k++)
+            verts.push_back(make_float4((float)m.positions[3 * k], (float)m.positions[3 * k + 1],
+                                        (float)m.positions[3 * k + 2], 0.f));
+        for (int t = 0; t < d.num_tris; t++)
+            tris.push_back(make_int4(d.first_vertex + m.tris[3 * t], d.first_vertex + m.tris[3 * t + 1],
+                                     d.first_vertex + m.tris[3 * t + 2], m.active[t]));
+        for (size_t k = 0; k < m.nodes.size() / 8; k++) {
+            const double *nd = &m.nodes[8 * k];
+            int a = (int)nd[6], b = (int)nd[7];
+            if (b >= 0) a /= 8;  // internal node: the right child's offset in doubles, as a node index
+            float fa, fb;
+            memcpy(&fa, &a, sizeof(float));
+            memcpy(&fb, &b, sizeof(float));
+            nodes.push_back(make_float4((float)nd[0], (float)nd[1], (float)nd[2], fa));
+            nodes.push_back(make_float4((float)nd[3], (float)nd[4], (float)nd[5], fb));
+        }
+        hdr.push_back(d);
+    }
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    void *old[] = {w.meshes, w.mesh_verts, w.mesh_tris, w.mesh_nodes};
+    for (void *p : old)
+        if (p) cudaFree(p);
+    w.meshes = nullptr;
+    w.mesh_verts = w.mesh_nodes = nullptr;
+    w.mesh_tris = nullptr;
+    int r;
+    if ((r = dalloc(&w.meshes, hdr.size())) != CC_OK || (r = dalloc(&w.mesh_verts, verts.size())) != CC_OK ||
+        (r = dalloc(&w.mesh_tris, tris.size())) != CC_OK || (r = dalloc(&w.mesh_nodes, nodes.size())) != CC_OK)
+        return r;
+    CC_TRY(cudaMemcpy(w.meshes, hdr.data(), sizeof(DevMesh) * hdr.size(), cudaMemcpyHostToDevice));
+    if (!verts.empty()) CC_TRY(cudaMemcpy(w.mesh_verts, verts.data(), sizeof(float4) * verts.size(), cudaMemcpyHostToDevice));
+    if (!tris.empty()) CC_TRY(cudaMemcpy(w.mesh_tris, tris.data(), sizeof(int4) * tris.size(), cudaMemcpyHostToDevice));
+    if (!nodes.empty()) CC_TRY(cudaMemcpy(w.mesh_nodes, nodes.data(), sizeof(float4) * nodes.size(), cudaMemcpyHostToDevice));
+    w.num_meshes = (int)hdr.size();
+    drop_graph(W);
+    return CC_OK;
+}
+
+static int export_mesh(const cc_mesh::Mesh &m, cc_mesh_info *info, float *vertices, int32_t *triangles,
+                       float *normals, float *nodes) {
+    if (!info) return CC_ERR_INVALID;
+    memset(info, 0, sizeof(*info));
+    info->num_vertices = (int32_t)(m.positions.size() / 3);
+    info->num_triangles = (int32_t)m.active.size();
+    info->num_nodes = (int32_t)(m.nodes.size() / 8);
+    for (int k = 0; k < 3; k++) {
+        info->bounds_min[k] = (float)m.lo[k];
+        info->bounds_max[k] = (float)m.hi[k];
+    }
+    if (vertices)
+        for (size_t k = 0; k < m.positions.size(); k++) vertices[k] = (float)m.positions[k];
+    for (int t = 0; t < info->num_triangles; t++) {
+        if (triangles) {
+            for (int k = 0; k < 3; k++) triangles[4 * t + k] = m.tris[3 * t + k];
+            triangles[4 * t + 3] = m.active[t];
+        }
+        if (normals)
+            for (int k = 0; k < 3; k++) normals[3 * t + k] = (float)m.normals[3 * t + k];
+    }
+    if (nodes)
+        for (int k = 0; k < info->num_nodes; k++) {
+            const double *nd = &m.nodes[8 * k];
+            for (int j = 0; j < 6; j++) nodes[8 * k + j] = (float)nd[j];
+            nodes[8 * k + 6] = (float)(nd[7] >= 0 ? nd[6] / 8 : nd[6]);
+            nodes[8 * k + 7] = (float)nd[7];
+        }
+    return CC_OK;
+}
+
+extern "C" {
+
+int cc_world_add_triangle_mesh(cc_world *W, const double *positions, int32_t nv, const int32_t *indices, int32_t nt,
+                               double degenerate_tolerance, double active_edge_cos, int32_t *out_mesh) {
+    if (!W) return CC_ERR_INVALID;
+    cc_mesh::Mesh m;
+    int r = build_mesh_from(positions, nv, indices, nt, degenerate_tolerance, active_edge_cos, m);
+    if (r != CC_OK) return r;
+    W->meshes.push_back(std::move(m));
+    if ((r = upload_meshes(W)) != CC_OK) {
+        W->meshes.pop_back();
+        return r;
+    }
+    if (out_mesh) *out_mesh = (int32_t)W->meshes.size() - 1;
+    return CC_OK;
+}
+
+int cc_triangle_mesh_build(const double *positions, int32_t nv, const int32_t *indices, int32_t nt,
+                           double degenerate_tolerance, double active_edge_cos, cc_mesh_info *info, float *vertices,
+                           int32_t *triangles, float *normals, float *nodes) {
+    cc_mesh::Mesh m;
+    int r = build_mesh_from(positions, nv, indices, nt, degenerate_tolerance, active_edge_cos, m);
+    if (r != CC_OK) return r;
+    return export_mesh(m, info, vertices, triangles, normals, nodes);
+}
+
+int cc_world_get_triangle_mesh(cc_world *W, int32_t mesh, cc_mesh_info *info, float *vertices, int32_t *triangles,
+                               float *normals, float *nodes) {
+    if (!W || mesh < 0 || mesh >= (int)W->meshes.size()) return CC_ERR_INVALID;
+    return export_mesh(W->meshes[mesh], info, vertices, triangles, normals, nodes);
+}
+
+}  // extern "C"
+
 static int build_hull_from(const float *points, int32_t n, float convex_radius, cc_hull::Hull &h);
 extern "C" {
 

@@ -15,7 +15,8 @@ import numpy as np
 from typing import Optional
 
 from ._lib import (BODY_DTYPE, COMBINE_GEOMETRIC_MEAN, COMBINE_MAX, DYNAMIC, MOTOR_OFF, MOTOR_POSITION,
-                   MOTOR_VELOCITY, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_CONVEX_HULL, SHAPE_SPHERE, STATIC, SWING_CONE, SWING_PYRAMID,
+                   MOTOR_VELOCITY, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_CONVEX_HULL, SHAPE_SPHERE, SHAPE_TRIANGLE_MESH, STATIC,
+                   SWING_CONE, SWING_PYRAMID,
                    hinge_defaults, swing_twist_defaults)
 
 # object layers of the reference's test helper (tst/helpers.ts:5-26)
@@ -47,6 +48,7 @@ class Scene:
     hull_points: Optional[list] = None  # point sets of the convex hulls, in hull index order
     skip_joint_pairs: bool = False
     gravity: tuple = (0.0, -9.81, 0.0)
+    mesh: Optional[tuple] = None  # (positions, indices) of the triangle mesh body shapes name as index 0
 
     @property
     def n(self) -> int:
@@ -799,4 +801,85 @@ def ccd_gallery(num_worlds: int = 1, seed: int = 101, arrival_steps: int = 3) ->
             b["motion_quality"][i] = 1
             b["gravity_factor"][i] = 0.0
     sc = Scene("ccd_gallery", b, dt=1.0 / 60.0, steps=8, num_worlds=num_worlds, seed=seed, hull_points=hulls)
+    return sc
+
+
+def heightfield(n_cells: int = 256, cell: float = 1.0, amplitude: float = 4.0, seed: int = 2,
+                octaves: int = 3) -> tuple:
+    """A terrain of n_cells x n_cells square cells of the given size centred on the origin, two
+    triangles per cell wound upwards, the height value noise (bilinear interpolation of random
+    lattice values over octaves of halving period) scaled to +-amplitude/2.  The rolling
+    terrain of the 20,000-body mixed workload (256 x 256 cells of 1 m, amplitude 4 m, 131,072
+    triangles).  Returns (positions (float32, (n+1)^2 x 3), indices (int32, 2 n^2 x 3))."""
+    rng = np.random.default_rng(seed)
+    n = n_cells + 1
+    h = np.zeros((n, n))
+    for o in range(octaves):
+        period = max(2, n_cells // (4 << o))
+        g = n_cells // period + 2
+        lattice = rng.uniform(-1.0, 1.0, (g, g))
+        u = np.arange(n) / period
+        i0 = np.floor(u).astype(int)
+        f = u - i0
+        a = lattice[i0][:, i0]
+        b = lattice[i0 + 1][:, i0]
+        c = lattice[i0][:, i0 + 1]
+        d = lattice[i0 + 1][:, i0 + 1]
+        fx = f[:, None]
+        fz = f[None, :]
+        h += (a * (1 - fx) * (1 - fz) + b * fx * (1 - fz) + c * (1 - fx) * fz + d * fx * fz) / (2 ** o)
+    h *= 0.5 * amplitude / max(1e-9, np.abs(h).max())
+    xs = (np.arange(n) - n_cells / 2.0) * cell
+    X, Z = np.meshgrid(xs, xs, indexing="ij")
+    pos = np.stack([X, h, Z], axis=-1).reshape(-1, 3).astype(np.float32)
+    idx = []
+    for i in range(n_cells):
+        for j in range(n_cells):
+            v00, v10, v01, v11 = i * n + j, (i + 1) * n + j, i * n + j + 1, (i + 1) * n + j + 1
+            # counter-clockwise seen from above (+Y): normals point up
+            idx.append((v00, v01, v10))
+            idx.append((v10, v01, v11))
+    return pos, np.array(idx, dtype=np.int32)
+
+
+def mesh_drop(n: int = 64, n_cells: int = 24, seed: int = 5, amplitude: float = 2.0,
+              heights=(1.0, 4.0), fast_fraction: float = 0.0) -> Scene:
+    """Bodies of every shape (spheres, boxes, capsules, convex hulls; the mixed pile's size
+    ranges) dropped on a heightfield terrain of n_cells x n_cells 1 m cells (one static mesh
+    body, index 0; hull points per hull body, mesh data in scene.mesh).  fast_fraction of the
+    bodies start at 20-60 m/s in a random downward direction."""
+    rng = np.random.default_rng(seed)
+    pos, idx = heightfield(n_cells, 1.0, amplitude, seed)
+    b = blank_bodies(n + 1)
+    b["shape_type"][0] = SHAPE_TRIANGLE_MESH
+    b["shape_params"][0] = 0.0
+    b["motion_type"][0] = STATIC
+    b["object_layer"][0] = LAYER_NOT_MOVING
+    b["friction"][0] = 0.5
+    hulls = []
+    half = 0.4 * n_cells
+    for i in range(1, n + 1):
+        k = rng.integers(0, 4)
+        if k == 0:
+            set_sphere(b, i, rng.uniform(0.2, 0.6))
+        elif k == 1:
+            set_box(b, i, rng.uniform(0.2, 0.8, 3))
+        elif k == 2:
+            set_capsule(b, i, rng.uniform(0.2, 0.4), rng.uniform(0.3, 0.8))
+        else:
+            hulls.append(ellipsoid_hull_points(rng, int(rng.integers(16, 33)), rng.uniform(0.3, 0.8, 3)))
+            set_hull(b, i, len(hulls) - 1)
+        b["position"][i] = (rng.uniform(-half, half), rng.uniform(*heights) + amplitude / 2 + 1.0,
+                            rng.uniform(-half, half))
+        b["friction"][i] = 0.5
+    b["quaternion"][1:] = random_quaternions(rng, n)
+    fast = rng.random(n) < fast_fraction
+    for i in np.nonzero(fast)[0] + 1:
+        d = rng.normal(size=3)
+        d[1] = -abs(d[1]) - 0.5
+        d /= np.linalg.norm(d)
+        b["linear_velocity"][i] = d * rng.uniform(20.0, 60.0)
+        b["motion_quality"][i] = 1
+    sc = Scene("mesh_drop", b, dt=1.0 / 60.0, steps=120, seed=seed, hull_points=hulls)
+    sc.mesh = (pos, idx)
     return sc

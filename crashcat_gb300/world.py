@@ -359,6 +359,35 @@ class GpuWorld:
         return _lib._hull_arrays(
             lambda info, *a: self._lib.cc_world_get_convex_hull(self.handle, index, info, *a))
 
+    # ---- triangle meshes (triangle-mesh.ts) ----
+    def add_triangle_mesh(self, positions, indices, degenerate_tolerance: float = -1.0,
+                          active_edge_cos: float = -2.0) -> int:
+        """cc_world_add_triangle_mesh: the mesh index bodies name in shape_params[0]
+        (mesh bodies are static or kinematic)."""
+        p = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        ix = np.ascontiguousarray(indices, dtype=np.int32).reshape(-1, 3)
+        out = C.c_int32(-1)
+        check(self._lib.cc_world_add_triangle_mesh(self.handle, ptr(p), len(p), ptr(ix), len(ix),
+                                                   C.c_double(degenerate_tolerance), C.c_double(active_edge_cos),
+                                                   C.byref(out)), "cc_world_add_triangle_mesh")
+        return out.value
+
+    def get_triangle_mesh(self, index: int) -> dict:
+        """cc_world_get_triangle_mesh: the built mesh's arrays (the oracle takes them as its shape data)."""
+        return _lib._mesh_arrays(
+            lambda info, *a: self._lib.cc_world_get_triangle_mesh(self.handle, index, info, *a))
+
+    def get_manifold_sub_shapes(self) -> np.ndarray:
+        """cc_world_get_manifold_sub_shapes: (sub-shape id A, sub-shape id B) per manifold, in
+        get_manifolds order."""
+        n = C.c_int32(0)
+        check(self._lib.cc_world_get_manifold_sub_shapes(self.handle, None, 0, C.byref(n)),
+              "cc_world_get_manifold_sub_shapes")
+        out = np.zeros((max(n.value, 1), 2), dtype=np.uint32)
+        check(self._lib.cc_world_get_manifold_sub_shapes(self.handle, ptr(out), n.value, C.byref(n)),
+              "cc_world_get_manifold_sub_shapes")
+        return out[:n.value]
+
     # ---- hinge joints (hinge-constraint.ts) ----
     def add_hinges(self, hinges: np.ndarray) -> np.ndarray:
         """cc_world_add_hinges: records of _lib.HINGE_DTYPE; returns the joint indices."""

@@ -30,6 +30,11 @@
  *   cc_world_add_convex_hull   <- convexHull.create          src/shapes/convex-hull.ts:106-446
  *   cc_world_get_convex_hull   <- reading the ConvexHullShape fields  src/shapes/convex-hull.ts:38-62
  *   cc_convex_hull_build       <- convexHull.create without a world   src/shapes/convex-hull.ts:106-446
+ *   cc_world_add_triangle_mesh <- triangleMesh.create        src/shapes/triangle-mesh.ts:114-140
+ *   cc_triangle_mesh_build     <- buildTriangleMesh without a world
+ *                                                            src/shapes/utils/triangle-mesh-builder.ts:62-231
+ *   cc_world_get_triangle_mesh <- reading the TriangleMeshShape data and BVH
+ *                                                            src/shapes/utils/triangle-mesh-data.ts:17-25
  *   cc_world_add_hinges        <- hingeConstraint.create     src/constraints/hinge-constraint.ts:240-387
  *   cc_world_set_hinge_*       <- hingeConstraint setters    src/constraints/hinge-constraint.ts:429-465
  *   cc_world_get_hinge_angles  <- hingeConstraint.getCurrentAngle  src/constraints/hinge-constraint.ts:467-474
@@ -59,7 +64,8 @@ enum cc_status {
     CC_ERR_UNSUPPORTED = 6
 };
 
-enum cc_shape_type { CC_SHAPE_SPHERE = 0, CC_SHAPE_BOX = 1, CC_SHAPE_CAPSULE = 2, CC_SHAPE_CONVEX_HULL = 3 };
+enum cc_shape_type { CC_SHAPE_SPHERE = 0, CC_SHAPE_BOX = 1, CC_SHAPE_CAPSULE = 2, CC_SHAPE_CONVEX_HULL = 3,
+                     CC_SHAPE_TRIANGLE_MESH = 4 };
 enum cc_motion_type { CC_STATIC = 0, CC_KINEMATIC = 1, CC_DYNAMIC = 2 };
 enum cc_motion_quality { CC_MOTION_DISCRETE = 0, CC_MOTION_LINEAR_CAST = 1 };  /* MotionQuality motion-properties.ts:8-26 */
 enum cc_combine_mode { CC_COMBINE_AVERAGE = 0, CC_COMBINE_MULTIPLY = 1, CC_COMBINE_MIN = 2, CC_COMBINE_MAX = 3,
@@ -191,6 +197,9 @@ int cc_world_get_pairs(cc_world *world, int32_t *out, int32_t capacity, int32_t 
  * impulse of the contact after the velocity solve, then 4 x (world point on
  * A[3], world point on B[3]). */
 int cc_world_get_manifolds(cc_world *world, float *out, int32_t capacity, int32_t *count);
+/* The sub-shape ids (A, B) of the same manifolds, in the same order: 0xffffffff for a convex
+ * shape, a mesh triangle's id (subShape.pushIndex sub-shape.ts:60-64) for a mesh. */
+int cc_world_get_manifold_sub_shapes(cc_world *world, uint32_t *out, int32_t capacity, int32_t *count);
 
 int cc_world_get_stats(cc_world *world, cc_stats *out);
 
@@ -235,6 +244,41 @@ int cc_convex_hull_build(const float *in_points, int32_t n, float convex_radius,
  * point_faces (num_points x 4: count, then up to 3 face indices). */
 int cc_world_get_convex_hull(cc_world *world, int32_t hull, cc_hull_info *info, float *points, float *shrunk,
                              int32_t *faces, int32_t *face_vertices, float *planes, int32_t *point_faces);
+
+/* ---------------------------------------------------------------------------
+ * Triangle meshes (src/shapes/triangle-mesh.ts).  triangleMesh.create builds the mesh
+ * (buildTriangleMesh triangle-mesh-builder.ts:62-231): vertices welded on a 1e-8 grid,
+ * degenerate triangles (|edge cross| < degenerate_tolerance) and duplicates dropped, active
+ * edges from the dihedral cosine threshold, a BVH of at most 8 triangles per leaf split at
+ * the middle of the longest centre extent.  The triangle order the BVH leaves defines the
+ * triangle indices (sub-shape ids).  A mesh has no mass (triangle-mesh.ts:153-158): mesh
+ * bodies are static or kinematic, named by the mesh index in shape_params[0] with shape_type
+ * CC_SHAPE_TRIANGLE_MESH.  Positions and tolerances are FP64, as the reference builds; the
+ * device keeps the welded vertices in FP32.  Limits of this library: at most 2^21 - 1 triangles per mesh, and a
+ * world holding a mesh body has at most 2^21 - 1 bodies (the contact key packs both).
+ * degenerate_tolerance < 0 selects the default 1e-6, active_edge_cos < -1 the default
+ * cos 5 degrees (0.996195); a negative cosine keeps every edge active.
+ * ------------------------------------------------------------------------- */
+typedef struct cc_mesh_info {
+    int32_t num_vertices, num_triangles, num_nodes;
+    float bounds_min[3], bounds_max[3];
+} cc_mesh_info;
+
+int cc_world_add_triangle_mesh(cc_world *world, const double *positions, int32_t num_vertices,
+                               const int32_t *indices, int32_t num_triangles, double degenerate_tolerance,
+                               double active_edge_cos, int32_t *out_mesh);
+/* The same construction without a world: info and, where not NULL, the arrays of
+ * cc_world_get_triangle_mesh. */
+int cc_triangle_mesh_build(const double *positions, int32_t num_vertices, const int32_t *indices,
+                           int32_t num_triangles, double degenerate_tolerance, double active_edge_cos,
+                           cc_mesh_info *info, float *vertices, int32_t *triangles, float *normals, float *nodes);
+/* Read back a built mesh: vertices (num_vertices x 3), triangles (num_triangles x 4: vertex
+ * indices a b c, active-edge bits AB 1 / BC 2 / CA 4), normals (num_triangles x 3), nodes
+ * (num_nodes x 8: min xyz, max xyz, then the right child's node index or the first triangle,
+ * then the split axis or -(triangle count + 1) for a leaf; nodes in pre-order, a left child
+ * right after its parent). */
+int cc_world_get_triangle_mesh(cc_world *world, int32_t mesh, cc_mesh_info *info, float *vertices,
+                               int32_t *triangles, float *normals, float *nodes);
 
 /* ---------------------------------------------------------------------------
  * Hinge joints (src/constraints/hinge-constraint.ts).  HingeConstraintSettings

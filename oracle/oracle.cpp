@@ -156,6 +156,7 @@ struct World {
     std::vector<HingeJoint> joints;
     std::vector<SwingTwistJoint> swings;
     std::vector<std::unique_ptr<HullData>> hulls;  // convex hull shapes the bodies refer to
+    std::vector<std::unique_ptr<MeshData>> meshes;  // triangle meshes the bodies refer to
     // skip broadphase pairs of bodies that share an enabled joint: the declarative form of the
     // ragdoll example's onBodyPairValidate (examples/src/example-ragdoll.ts:487-489)
     bool skipJointPairs = false;
@@ -871,37 +872,69 @@ static bool narrowphase(World &w, Body *A, Body *B, double dt) {
     cs.collisionTolerance = w.s.collisionTolerance;
     cs.penetrationTolerance = w.s.penetrationTolerance;
     cs.maxSeparation = (A->sensor || B->sensor) ? 0 : w.s.speculativeContactDistance;
-    Hit hit;
-    if (!collide_shapes(hit, cs, A->shape, A->position, A->quat, B->shape, B->position, B->quat)) return false;
-    // addHit update.ts:385-519 (one hit per convex pair: one manifold)
-    double maxContactDistance = w.s.speculativeContactDistance + w.s.manifoldTolerance;
-    Manifold m;
-    m.base = A->position;
-    m.normal = normalize(hit.axis);
-    m.depth = hit.penetration;
-    m.subA = hit.subA;
-    m.subB = hit.subB;
-    Manifold tmp;
-    tmp.base = A->position;
-    if (hit.faceA.n >= 2 && hit.faceB.n >= 3) {
-        manifold_between_faces(tmp, hit.pa, hit.pb, hit.axis, maxContactDistance, hit.faceA, hit.faceB);
-    } else {
-        set_contact_point(tmp, 0, hit.pa, hit.pb);
-        tmp.n = 1;
+    // activeEdgeMovementDirection update.ts:729-733
+    V3 movement = sub(A->linvel, B->linvel);
+    std::vector<Hit> hits;
+    collide_hits(hits, cs, A->shape, A->position, A->quat, B->shape, B->position, B->quat, movement);
+    // narrowphaseWithReductionCollector.addHit update.ts:385-519: hits whose normal is within
+    // normalCosMaxDeltaRotation of a manifold's accumulated normal join it, at most 32 manifolds
+    const double maxContactDistance = w.s.speculativeContactDistance + w.s.manifoldTolerance;
+    std::vector<Manifold> ms;
+    for (const Hit &hit : hits) {
+        V3 n = normalize(hit.axis);
+        int found = -1;
+        for (size_t i = 0; i < ms.size(); i++)
+            if (dot(n, ms[i].normal) >= w.s.normalCosMaxDeltaRotation) {
+                found = (int)i;
+                break;
+            }
+        if (found < 0) {
+            if (ms.size() >= 32) {
+                int sh = 0;
+                for (int i = 1; i < (int)ms.size(); i++)
+                    if (ms[i].depth < ms[sh].depth) sh = i;
+                if (hit.penetration < ms[sh].depth) continue;
+                found = sh;
+            } else {
+                ms.emplace_back();
+                found = (int)ms.size() - 1;
+            }
+            Manifold &m = ms[found];
+            m = Manifold();
+            m.base = A->position;
+            m.normal = n;
+            m.depth = hit.penetration;
+            m.subA = hit.subA;
+            m.subB = hit.subB;
+        } else {
+            ms[found].normal = add(ms[found].normal, n);
+        }
+        Manifold &m = ms[found];
+        Manifold tmp;
+        tmp.base = A->position;
+        if (hit.faceA.n >= 2 && hit.faceB.n >= 3) {
+            manifold_between_faces(tmp, hit.pa, hit.pb, hit.axis, maxContactDistance, hit.faceA, hit.faceB);
+        } else {
+            set_contact_point(tmp, 0, hit.pa, hit.pb);
+            tmp.n = 1;
+        }
+        for (int i = 0; i < tmp.n; i++) {
+            if (m.n >= 64) break;
+            m.relA[m.n] = tmp.relA[i];
+            m.relB[m.n] = tmp.relB[i];
+            m.n++;
+        }
+        if (hit.penetration > m.depth) m.depth = hit.penetration;
+        if (m.n > 32) prune_contact_points(m, m.normal);
     }
-    for (int i = 0; i < tmp.n; i++) {
-        if (m.n >= 64) break;
-        m.relA[m.n] = tmp.relA[i];
-        m.relB[m.n] = tmp.relB[i];
-        m.n++;
-    }
-    if (hit.penetration > m.depth) m.depth = hit.penetration;
-    if (m.n > 32) prune_contact_points(m, m.normal);
     // finalizeAndCreateConstraints update.ts:525-558
-    m.normal = normalize(m.normal);
-    if (m.n > 4) prune_contact_points(m, m.normal);
-    if (m.n > 0) return add_contact_constraint(w, A, B, m, dt);
-    return false;
+    bool created = false;
+    for (Manifold &m : ms) {
+        m.normal = normalize(m.normal);
+        if (m.n > 4) prune_contact_points(m, m.normal);
+        if (m.n > 0) created = add_contact_constraint(w, A, B, m, dt) || created;
+    }
+    return created;
 }
 
 // ---------------------------------------------------------------------------
@@ -1291,6 +1324,8 @@ static void find_ccd_contacts(World &w, double dt) {
             if (!(t < std::numeric_limits<double>::infinity()) || t / castLen > castLen) continue;
             // ccdBodyVisitor.visit update.ts:1153-1250
             if (B.index == A.index) continue;
+            // castConvexVsTriangleMesh (triangle-mesh.ts) is not restated: meshes are not cast against
+            if (B.shape.type == SHAPE_TRIANGLE_MESH) continue;
             const World::CCDRecord *cb = B.ccdIndex >= 0 ? &w.ccd[B.ccdIndex] : nullptr;
             if (cb && c.body > cb->body) continue;
             if (B.sensor) continue;
@@ -1736,6 +1771,11 @@ static bool shape_from_row(Shape &s, const double *r, const World *w = nullptr) 
         s.com = s.hull->com;
         s.aabb = s.hull->bounds;
         s.convex_radius = s.hull->convex_radius;
+    } else if (s.type == SHAPE_TRIANGLE_MESH) {  // F_P0: the mesh index
+        int m = (int)r[F_P0];
+        if (!w || m < 0 || m >= (int)w->meshes.size()) return false;
+        s.mesh = w->meshes[m].get();
+        s.aabb = s.mesh->bounds;
     } else if (s.type == SHAPE_BOX) {
         s.half_extents = {r[F_P0], r[F_P0 + 1], r[F_P0 + 2]};
         s.convex_radius = r[F_P0 + 3];
@@ -1784,7 +1824,8 @@ int orc_add_bodies(void *wp, const double *rows, int n) {
         double mass;
         V3 idiag;
         shape_mass(s, mass, idiag);
-        if (b.motion != STATIC) {
+        if (s.type == SHAPE_TRIANGLE_MESH && b.motion == DYNAMIC) return -1;  // meshes have no mass
+        if (b.motion != STATIC && s.type != SHAPE_TRIANGLE_MESH) {
             if (s.type == SHAPE_CONVEX_HULL)
                 set_mass_properties_tensor(b, mass, s.hull->inertia, s.density);
             else
@@ -1903,6 +1944,25 @@ int orc_add_hull(void *wp, int np, const double *points, const double *shrunk, i
 //  32-35 target orientation (x y z w, constraint space), 36-38 swing motor spring (mode, f, d),
 //  39-41 twist motor spring, 42-43 swing motor torque limits (min, max), 44-45 twist motor torque
 //  limits, 46 priority.  Returns the joint index or -1.
+// a triangle mesh as built: nv vertices (x y z), nt triangles (a b c active-edge bits), nn
+// nodes (8 each: min, max, right child node or first triangle, axis or -(count + 1))
+int orc_add_mesh(void *wp, int nv, const double *verts, int nt, const int *tris, int nn, const double *nodes) {
+    World &w = *(World *)wp;
+    auto m = std::make_unique<MeshData>();
+    for (int i = 0; i < nv; i++) m->verts.push_back({verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]});
+    for (int t = 0; t < nt; t++) m->tris.push_back({tris[4 * t], tris[4 * t + 1], tris[4 * t + 2], tris[4 * t + 3]});
+    for (int k = 0; k < nn; k++) {
+        std::array<double, 8> nd;
+        for (int j = 0; j < 8; j++) nd[j] = nodes[8 * k + j];
+        m->nodes.push_back(nd);
+    }
+    unsigned maxi = nt > 0 ? (unsigned)(nt - 1) : 0u;
+    m->subBits = maxi == 0 ? 0 : 32 - __builtin_clz(maxi);
+    if (nn > 0) m->bounds = {{nodes[0], nodes[1], nodes[2]}, {nodes[3], nodes[4], nodes[5]}};
+    w.meshes.push_back(std::move(m));
+    return (int)w.meshes.size() - 1;
+}
+
 int orc_add_swing_twist(void *wp, const double *d) {
     World &w = *(World *)wp;
     int a = (int)d[0], b = (int)d[1];
@@ -2085,6 +2145,25 @@ int orc_get_manifolds(void *wp, double *out) {
 
 // Island statistics of the last step: number of islands with contacts.
 int orc_island_count(void *wp) { return (int)((World *)wp)->islands.size(); }
+// sub-shape ids of the manifolds, in orc_get_manifolds order (2 per manifold, id order)
+int orc_get_manifold_subs(void *wp, uint32_t *out) {
+    World &w = *(World *)wp;
+    for (size_t i = 0; i < w.manifolds.size(); i++) {
+        out[2 * i] = w.manifolds[i].subA;
+        out[2 * i + 1] = w.manifolds[i].subB;
+    }
+    return (int)w.manifolds.size();
+}
+// fixNormal active-edges.ts:74-153 on 8 vec3 inputs (v0 v1 v2 triangle normal point normal movement,
+// and active bits in in[24]): 1 when it keeps the normal, 0 when it returns the triangle normal
+int orc_fix_normal(const double *in) {
+    auto v = [&](int k) { return V3{in[3 * k], in[3 * k + 1], in[3 * k + 2]}; };
+    V3 tn = v(3), n = v(5);
+    V3 r = fix_normal(v(0), v(1), v(2), tn, (int)in[24], v(4), n, v(6));
+    if (r.x == n.x && r.y == n.y && r.z == n.z) return 1;
+    if (r.x == tn.x && r.y == tn.y && r.z == tn.z) return 0;
+    return -1;
+}
 // continuous collision of the last step: records, and records whose cast hit a body
 void orc_ccd_counts(void *wp, int *out) {
     out[0] = (int)((World *)wp)->ccd.size();

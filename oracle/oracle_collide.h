@@ -7,6 +7,7 @@
 // reference's IEEE-754 double results (compiled with -ffp-contract=off).
 #pragma once
 #include <algorithm>
+#include <array>
 #include <cstring>
 #include <limits>
 #include <vector>
@@ -18,7 +19,19 @@ namespace orc {
 constexpr double DEFAULT_CONVEX_RADIUS = 0.05;  // src/collision/support.ts:5
 constexpr uint32_t EMPTY_SUB_SHAPE_ID = 0xffffffffu;  // src/body/sub-shape.ts:4
 
-enum ShapeType : int { SHAPE_SPHERE = 0, SHAPE_BOX = 1, SHAPE_CAPSULE = 2, SHAPE_CONVEX_HULL = 3 };
+enum ShapeType : int { SHAPE_SPHERE = 0, SHAPE_BOX = 1, SHAPE_CAPSULE = 2, SHAPE_CONVEX_HULL = 3, SHAPE_TRIANGLE_MESH = 4 };
+
+// Triangle mesh as built (src/shapes/utils/triangle-mesh-data.ts, triangle-mesh-bvh.ts): welded
+// vertices, triangles (vertex indices, active-edge bits AB 1 / BC 2 / CA 4) in the order the BVH
+// build left them, nodes in pre-order (min, max, then the right child's node index or the first
+// triangle, then the split axis or -(count + 1) for a leaf)
+struct MeshData {
+    std::vector<V3> verts;
+    std::vector<std::array<int, 4>> tris;
+    std::vector<std::array<double, 8>> nodes;
+    int subBits = 0;
+    Box3 bounds;
+};
 
 // ConvexHullShape fields (src/shapes/convex-hull.ts:38-62): points relative to the centre of
 // mass, the points shrunk by the convex radius (setConvexHullNoConvexSupport :732-788),
@@ -37,6 +50,7 @@ struct HullData {
 // Shape data (src/shapes/box.ts:38-70, src/shapes/sphere.ts, src/shapes/capsule.ts, convex-hull.ts)
 struct Shape {
     const HullData *hull = nullptr;  // convex hull
+    const MeshData *mesh = nullptr;  // triangle mesh
     int type = SHAPE_BOX;
     V3 half_extents;          // box
     double convex_radius = 0;  // box
@@ -51,7 +65,8 @@ struct Shape {
 // Support functions (src/collision/support.ts, src/shapes/sphere.ts:173-266)
 // ----------------------------------------------------------------------------
 enum SupportMode { INCLUDE_CONVEX_RADIUS = 0, EXCLUDE_CONVEX_RADIUS = 1 };
-enum SupportKind { SUP_BOX, SUP_SPHERE_POINT, SUP_SPHERE_SURFACE, SUP_CAPSULE_SEGMENT, SUP_CAPSULE_SURFACE, SUP_HULL };
+enum SupportKind { SUP_BOX, SUP_SPHERE_POINT, SUP_SPHERE_SURFACE, SUP_CAPSULE_SEGMENT, SUP_CAPSULE_SURFACE, SUP_HULL,
+                   SUP_TRIANGLE };
 
 struct Support {
     int kind = SUP_BOX;
@@ -64,6 +79,7 @@ struct Support {
     M4 m;
     bool add_radius = false;  // AddConvexRadiusSupport (support.ts:282-315)
     double add_r = 0;
+    V3 ta, tb, tc;  // TriangleSupport (support.ts:75-142)
 
     V3 inner(V3 d) const {
         switch (kind) {
@@ -90,6 +106,11 @@ struct Support {
                     }
                 }
                 return bp;
+            }
+            case SUP_TRIANGLE: {  // triangleGetSupport support.ts:83-118
+                double d1 = dot(ta, d), d2 = dot(tb, d), d3 = dot(tc, d);
+                if (d1 > d2) return d1 > d3 ? ta : tc;
+                return d2 > d3 ? tb : tc;
             }
             case SUP_CAPSULE_SEGMENT:  // capsule.ts: segment +-h on Y
                 return {0, d.y > 0 ? half_height : -half_height, 0};
@@ -1716,11 +1737,297 @@ inline bool cast_convex_vs_convex(CastHit &hit, const Shape &sa, V3 pA, Q4 qA, V
     return true;
 }
 
+// ----------------------------------------------------------------------------
+// Triangle meshes (src/shapes/triangle-mesh.ts, src/collision/active-edges.ts, triangle.ts)
+// ----------------------------------------------------------------------------
+// fixNormal active-edges.ts:74-153
+inline V3 fix_normal(V3 v0, V3 v1, V3 v2, V3 tn, int active, V3 point, V3 normal, V3 move) {
+    if (active == 0b111) return normal;
+    double nl = len(normal), tl = len(tn);
+    if (dot(move, normal) * tl < dot(move, tn) * nl) return normal;
+    if (active == 0) return tn;
+    if (dot(tn, normal) > 0.999848 * nl * tl) return normal;
+    Bary b = bary3(sub(v0, point), sub(v1, point), sub(v2, point), 1e-10);
+    const double E = 1.0e-4, OME = 1.0 - 1.0e-4;
+    int edge;
+    if (b.u > OME)
+        edge = 0b101;
+    else if (b.v > OME)
+        edge = 0b011;
+    else if (b.w > OME)
+        edge = 0b110;
+    else if (b.u < E)
+        edge = 0b010;
+    else if (b.v < E)
+        edge = 0b100;
+    else if (b.w < E)
+        edge = 0b001;
+    else
+        return tn;
+    return (active & edge) ? normal : tn;
+}
+
+// getClosestPointOnTriangle triangle.ts:62-197 (query point at the origin); feature bits:
+// vertices A 1, B 2, C 4, an edge its two vertices, the face 7
+inline V3 closest_point_on_triangle(V3 a, V3 b, V3 c, double &dsq, int &feature) {
+    V3 ab = sub(b, a), ac = sub(c, a);
+    V3 n = cross(ab, ac);
+    double nl2 = lensq(n);
+    if (nl2 < 1e-10) {  // handleDegenerateTriangle triangle.ts:199-287
+        V3 best = c;
+        feature = 0b100;
+        double bd = lensq(c);
+        if (lensq(a) < bd) best = a, bd = lensq(a), feature = 0b001;
+        if (lensq(b) < bd) best = b, bd = lensq(b), feature = 0b010;
+        const double EPS2 = 1.1920929e-7 * 1.1920929e-7;
+        auto edge = [&](V3 p, V3 e, int f) {
+            double el = lensq(e);
+            if (el > EPS2) {
+                double v = std::max(0.0, std::min(1.0, -dot(p, e) / el));
+                V3 q = scale_add(p, e, v);
+                double d = lensq(q);
+                if (d < bd) best = q, bd = d, feature = f;
+            }
+        };
+        edge(a, ac, 0b101);
+        edge(b, sub(c, b), 0b110);
+        edge(a, ab, 0b011);
+        dsq = bd;
+        return best;
+    }
+    double d1 = -dot(ab, a), d2 = -dot(ac, a);
+    if (d1 <= 0 && d2 <= 0) return dsq = lensq(a), feature = 0b001, a;
+    double d3 = -dot(ab, b), d4 = -dot(ac, b);
+    if (d3 >= 0 && d4 <= d3) return dsq = lensq(b), feature = 0b010, b;
+    if (d1 * d4 <= d3 * d2 && d1 >= 0 && d3 <= 0) {
+        V3 p = scale_add(a, ab, d1 / (d1 - d3));
+        return dsq = lensq(p), feature = 0b011, p;
+    }
+    double d5 = -dot(ab, c), d6 = -dot(ac, c);
+    if (d6 >= 0 && d5 <= d6) return dsq = lensq(c), feature = 0b100, c;
+    if (d5 * d2 <= d1 * d6 && d2 >= 0 && d6 <= 0) {
+        V3 p = scale_add(a, ac, d2 / (d2 - d6));
+        return dsq = lensq(p), feature = 0b101, p;
+    }
+    double d43 = d4 - d3, d56 = d5 - d6;
+    if (d3 * d6 <= d5 * d4 && d43 >= 0 && d56 >= 0) {
+        V3 p = scale_add(b, sub(c, b), d43 / (d43 + d56));
+        return dsq = lensq(p), feature = 0b110, p;
+    }
+    double sc = dot(add(add(a, b), c), n) / (3 * nl2);
+    V3 p = scale(n, sc);
+    return dsq = lensq(p), feature = 0b111, p;
+}
+
+inline uint32_t mesh_sub_shape_id(const MeshData &m, int tri) {  // subShape.pushIndex sub-shape.ts:60-64
+    uint32_t mask = m.subBits >= 32 ? 0xffffffffu : ((1u << m.subBits) - 1u);
+    return (0xffffffffu & ~mask) | (uint32_t)tri;
+}
+
+inline bool node_hits_box(const std::array<double, 8> &nd, const Box3 &q) {  // nodeIntersectsBox bvh.ts:178-196
+    return nd[0] <= q.mx.x && nd[3] >= q.mn.x && nd[1] <= q.mx.y && nd[4] >= q.mn.y && nd[2] <= q.mx.z && nd[5] >= q.mn.z;
+}
+
+// the mesh BVH walk of the collide functions (triangle-mesh.ts:1122-1134, 1359-1385): a node
+// that meets the query box is opened, the child whose centre is nearer the query point first
+template <class F>
+inline void mesh_walk(const MeshData &M, const Box3 &q, V3 qc, F &&leaf) {
+    if (M.nodes.empty()) return;
+    std::vector<int> stack{0};
+    while (!stack.empty()) {
+        int node = stack.back();
+        stack.pop_back();
+        const auto &nd = M.nodes[node];
+        if (!node_hits_box(nd, q)) continue;
+        if (nd[7] < 0) {
+            int start = (int)nd[6], count = (int)(-nd[7]) - 1;
+            for (int t = start; t < start + count; t++) leaf(t);
+            continue;
+        }
+        int left = node + 1, right = (int)nd[6];
+        auto centre = [&](int k) {
+            const auto &c = M.nodes[k];
+            return V3{(c[0] + c[3]) * 0.5, (c[1] + c[4]) * 0.5, (c[2] + c[5]) * 0.5};
+        };
+        double ld = lensq(sub(qc, centre(left))), rd = lensq(sub(qc, centre(right)));
+        if (ld <= rd) {
+            stack.push_back(right);
+            stack.push_back(left);
+        } else {
+            stack.push_back(left);
+            stack.push_back(right);
+        }
+    }
+}
+
+inline bool box_overlap_incl(const Box3 &a, const Box3 &b) {
+    return a.mn.x <= b.mx.x && a.mx.x >= b.mn.x && a.mn.y <= b.mx.y && a.mx.y >= b.mn.y && a.mn.z <= b.mx.z &&
+           a.mx.z >= b.mn.z;
+}
+
+// collideConvexVsTriangleMesh triangle-mesh.ts:1026-1386 (unit scale): hits in world space,
+// A the convex shape, B the mesh
+inline void collide_convex_vs_mesh(std::vector<Hit> &out, const CollideSettings &cs, const Shape &sa, V3 pA, Q4 qA,
+                                   const Shape &sb, V3 pB, Q4 qB, V3 movement) {
+    const MeshData &M = *sb.mesh;
+    Q4 iqA = qconj(qA), iqB = qconj(qB);
+    Q4 m2cQ = qmul(iqA, qB);
+    V3 m2cP = rotate(iqA, sub(pB, pA));
+    Q4 cInMQ = qmul(iqB, qA);
+    V3 cInMP = rotate(iqB, sub(pA, pB));
+    const double ms = cs.maxSeparation;
+    Box3 b1{sub(sa.aabb.mn, V3{ms, ms, ms}), add(sa.aabb.mx, V3{ms, ms, ms})};
+    Box3 b12{{1e300, 1e300, 1e300}, {-1e300, -1e300, -1e300}};
+    for (int c = 0; c < 8; c++) {
+        V3 p{(c & 1) ? sa.aabb.mx.x : sa.aabb.mn.x, (c & 2) ? sa.aabb.mx.y : sa.aabb.mn.y,
+             (c & 4) ? sa.aabb.mx.z : sa.aabb.mn.z};
+        V3 q = add(rotate(cInMQ, p), cInMP);
+        b12.mn = {std::min(b12.mn.x, q.x), std::min(b12.mn.y, q.y), std::min(b12.mn.z, q.z)};
+        b12.mx = {std::max(b12.mx.x, q.x), std::max(b12.mx.y, q.y), std::max(b12.mx.z, q.z)};
+    }
+    b12 = {sub(b12.mn, V3{ms, ms, ms}), add(b12.mx, V3{ms, ms, ms})};
+    Support supA = make_support(sa, EXCLUDE_CONVEX_RADIUS);
+    V3 qc = scale(add(b12.mn, b12.mx), 0.5);
+    mesh_walk(M, b12, qc, [&](int t) {
+        const auto &tr = M.tris[t];
+        V3 a = add(rotate(m2cQ, M.verts[tr[0]]), m2cP), b = add(rotate(m2cQ, M.verts[tr[1]]), m2cP),
+           c = add(rotate(m2cQ, M.verts[tr[2]]), m2cP);
+        Box3 tb{{std::min(a.x, std::min(b.x, c.x)), std::min(a.y, std::min(b.y, c.y)), std::min(a.z, std::min(b.z, c.z))},
+                {std::max(a.x, std::max(b.x, c.x)), std::max(a.y, std::max(b.y, c.y)), std::max(a.z, std::max(b.z, c.z))}};
+        if (!box_overlap_incl(tb, b1)) return;
+        V3 n = cross(sub(b, a), sub(c, a));
+        bool backFacing = dot(n, a) > 0.0;
+        if (backFacing) return;  // collideWithBackfaces false
+        Support tri;
+        tri.kind = SUP_TRIANGLE;
+        tri.ta = a;
+        tri.tb = b;
+        tri.tc = c;
+        tri.convex_radius = 0;
+        V3 axis = neg(n);
+        axis = lensq(axis) < 1e-10 ? V3{1, 0, 0} : normalize(axis);
+        double maxSep = ms;
+        Simplex sx;
+        PenDepth pd = pen_step_gjk(sx, supA, tri, supA.convex_radius + maxSep, 0, axis, cs.collisionTolerance);
+        if (pd.status == NOT_COLLIDING) return;
+        if (pd.status == INDETERMINATE) {
+            maxSep = std::min(maxSep, 1.0);
+            Support a2 = make_support(sa, INCLUDE_CONVEX_RADIUS);
+            a2.add_radius = true;
+            a2.add_r = maxSep;
+            if (!pen_step_epa(pd, a2, tri, cs.penetrationTolerance, sx)) return;
+        }
+        double penetration = distance(pd.pa, pd.pb) - maxSep;
+        double al = len(pd.axis);
+        if (al > 0.0) pd.pa = scale_add(pd.pa, pd.axis, -(maxSep / al));
+        if (tr[3] != 0b111) {
+            V3 mv = rotate(iqA, movement);
+            V3 tn = backFacing ? n : neg(n);
+            pd.axis = fix_normal(a, b, c, tn, tr[3], pd.pb, pd.axis, mv);
+        }
+        Hit h;
+        h.pa = add(rotate(qA, pd.pa), pA);
+        h.pb = add(rotate(qA, pd.pb), pA);
+        h.axis = rotate(qA, pd.axis);
+        h.penetration = penetration;
+        h.subA = EMPTY_SUB_SHAPE_ID;
+        h.subB = mesh_sub_shape_id(M, t);
+        shape_supporting_face(h.faceA, sa, neg(pd.axis), pA, qA);
+        h.faceB.n = 3;
+        h.faceB.v[0] = add(rotate(qA, a), pA);
+        h.faceB.v[1] = add(rotate(qA, b), pA);
+        h.faceB.v[2] = add(rotate(qA, c), pA);
+        out.push_back(h);
+    });
+}
+
+// collideSphereVsTriangleMesh triangle-mesh.ts:1418-1712 (unit scale)
+inline void collide_sphere_vs_mesh(std::vector<Hit> &out, const CollideSettings &cs, const Shape &sa, V3 pA,
+                                   const Shape &sb, V3 pB, Q4 qB, V3 movement) {
+    static const int FEATURE_TO_ACTIVE_EDGES[8] = {0b000, 0b101, 0b011, 0b001, 0b110, 0b100, 0b010, 0b000};
+    const MeshData &M = *sb.mesh;
+    const double r = sa.radius, ms = cs.maxSeparation;
+    const double maxSq = (r + ms) * (r + ms);
+    Q4 iqB = qconj(qB);
+    V3 c = rotate(iqB, sub(pA, pB));
+    double er = r + ms;
+    Box3 q{{c.x - er, c.y - er, c.z - er}, {c.x + er, c.y + er, c.z + er}};
+    mesh_walk(M, q, c, [&](int t) {
+        const auto &tr = M.tris[t];
+        V3 sv0 = M.verts[tr[0]], sv1 = M.verts[tr[1]], sv2 = M.verts[tr[2]];
+        V3 v0 = sub(sv0, c), v1 = sub(sv1, c), v2 = sub(sv2, c);
+        V3 tn = cross(sub(v1, v0), sub(v2, v0));
+        bool back = dot(tn, v0) > 0;
+        if (back) return;
+        double dsq;
+        int feature;
+        V3 p2 = closest_point_on_triangle(v0, v1, v2, dsq, feature);
+        if (dsq > maxSq) return;
+        double pen = r - std::sqrt(dsq);
+        V3 axis = dsq > 0 ? normalize(p2) : V3{0, 1, 0};
+        V3 p1 = scale(axis, r);
+        if (feature != 0b111 && tr[3] != 0b111 && (tr[3] & FEATURE_TO_ACTIVE_EDGES[feature]) == 0) {
+            V3 mv = rotate(iqB, movement);
+            V3 nax = back ? tn : neg(tn);
+            if (dot(mv, axis) * len(nax) >= dot(mv, nax)) axis = nax;
+        }
+        Hit h;
+        h.pa = add(rotate(qB, add(c, p1)), pB);
+        h.pb = add(rotate(qB, add(c, p2)), pB);
+        h.axis = rotate(qB, axis);
+        h.penetration = pen;
+        h.subA = EMPTY_SUB_SHAPE_ID;
+        h.subB = mesh_sub_shape_id(M, t);
+        h.faceA.n = 0;
+        h.faceB.n = 3;
+        h.faceB.v[0] = add(rotate(qB, sv0), pB);
+        h.faceB.v[1] = add(rotate(qB, sv1), pB);
+        h.faceB.v[2] = add(rotate(qB, sv2), pB);
+        out.push_back(h);
+    });
+}
+
+// the hits of a body pair in narrowphase order (collideShapeVsShape narrowphase.ts:172-238 with
+// the mesh registrations triangle-mesh.ts:223-237: a mesh as shape A runs the convex-vs-mesh
+// function reversed, collide-shape-vs-shape.ts:227-354)
+inline void collide_hits(std::vector<Hit> &out, const CollideSettings &cs, const Shape &sa, V3 pA, Q4 qA,
+                         const Shape &sb, V3 pB, Q4 qB, V3 movement);
+
 // collideShapeVsShape narrowphase.ts:172-238 (dispatch for the supported convex shapes)
 inline bool collide_shapes(Hit &hit, const CollideSettings &cs, const Shape &sa, V3 pA, Q4 qA, const Shape &sb,
                            V3 pB, Q4 qB) {
     if (sa.type == SHAPE_SPHERE && sb.type == SHAPE_SPHERE) return collide_sphere_vs_sphere(hit, sa, pA, sb, pB);
     return collide_convex_vs_convex(hit, cs, sa, pA, qA, sb, pB, qB);
+}
+
+inline void collide_hits(std::vector<Hit> &out, const CollideSettings &cs, const Shape &sa, V3 pA, Q4 qA,
+                         const Shape &sb, V3 pB, Q4 qB, V3 movement) {
+    const bool ma = sa.type == SHAPE_TRIANGLE_MESH, mb = sb.type == SHAPE_TRIANGLE_MESH;
+    if (ma && mb) return;
+    if (mb) {
+        if (sa.type == SHAPE_SPHERE)
+            collide_sphere_vs_mesh(out, cs, sa, pA, sb, pB, qB, movement);
+        else
+            collide_convex_vs_mesh(out, cs, sa, pA, qA, sb, pB, qB, movement);
+        return;
+    }
+    if (ma) {
+        size_t first = out.size();
+        if (sb.type == SHAPE_SPHERE)
+            collide_sphere_vs_mesh(out, cs, sb, pB, sa, pA, qA, movement);
+        else
+            collide_convex_vs_mesh(out, cs, sb, pB, qB, sa, pA, qA, movement);
+        for (size_t i = first; i < out.size(); i++) {  // createInvertedCollector collide-shape-vs-shape.ts:227-270
+            Hit &h = out[i];
+            std::swap(h.pa, h.pb);
+            h.axis = neg(h.axis);
+            std::swap(h.subA, h.subB);
+            std::swap(h.faceA, h.faceB);
+        }
+        return;
+    }
+    Hit h;
+    if (collide_shapes(h, cs, sa, pA, qA, sb, pB, qB)) out.push_back(h);
 }
 
 }  // namespace orc

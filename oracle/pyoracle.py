@@ -48,6 +48,9 @@ def load():
         "orc_get_manifolds": ([vp, dp], i32),
         "orc_island_count": ([vp], i32),
         "orc_ccd_counts": ([vp, ip], None),
+        "orc_add_mesh": ([vp, i32, dp, i32, C.c_void_p, i32, dp], i32),
+        "orc_get_manifold_subs": ([vp, C.c_void_p], i32),
+        "orc_fix_normal": ([dp], i32),
         "orc_clip_poly_vs_plane": ([dp, i32, dp, dp, dp], i32),
         "orc_clip_poly_vs_poly": ([dp, i32, dp, i32, dp, dp], i32),
         "orc_manifold_between_faces": ([dp, dp, dp, C.c_double, dp, i32, dp, i32, dp, dp], i32),
@@ -135,9 +138,9 @@ def settings_array(ws) -> np.ndarray:
 class OracleWorld:
     """One oracle world built from the same bodies and settings as a GPU world."""
 
-    def __init__(self, ws, bodies: np.ndarray, hulls=()):
-        """hulls: convex hull records as GpuWorld.get_convex_hull returns them, in index order
-        (the bodies name them by index)."""
+    def __init__(self, ws, bodies: np.ndarray, hulls=(), meshes=()):
+        """hulls / meshes: convex hull and triangle mesh records as GpuWorld.get_convex_hull /
+        get_triangle_mesh return them, in index order (the bodies name them by index)."""
         lib = load()
         self.lib = lib
         L = ws.layers
@@ -160,9 +163,26 @@ class OracleWorld:
                                       bpp.ctypes.data)
         for h in hulls:
             self.add_hull(h)
+        for m in meshes:
+            self.add_mesh(m)
         rows = rows_from_bodies(bodies)
         assert lib.orc_add_bodies(self.h, dptr(rows), len(rows)) == 0
         self.n = len(rows)
+
+    def add_mesh(self, m) -> int:
+        v = np.ascontiguousarray(m["vertices"], dtype=np.float64)
+        t = np.ascontiguousarray(m["triangles"], dtype=np.int32)
+        nd = np.ascontiguousarray(m["nodes"], dtype=np.float64)
+        k = self.lib.orc_add_mesh(self.h, len(v), dptr(v), len(t), t.ctypes.data, len(nd), dptr(nd))
+        assert k >= 0
+        return k
+
+    def manifold_sub_shapes(self) -> np.ndarray:
+        """Sub-shape ids (A, B) of the manifolds, in manifolds() order."""
+        n = self.lib.orc_manifold_count(self.h)
+        o = np.zeros((max(n, 1), 2), dtype=np.uint32)
+        self.lib.orc_get_manifold_subs(self.h, o.ctypes.data)
+        return o[:n]
 
     def add_hull(self, h) -> int:
         pts = np.ascontiguousarray(h["points"], dtype=np.float64)
@@ -293,3 +313,13 @@ def gpu_rows_to_state(rows: np.ndarray) -> np.ndarray:
     o = np.zeros((len(rows), STATE), dtype=np.float64)
     o[:, :16] = rows
     return o
+
+
+def fix_normal(v0, v1, v2, triangle_normal, active_edges, point, normal, movement) -> int:
+    """fixNormal (active-edges.ts:74-153) in the oracle: 1 when it keeps the normal, 0 when it
+    returns the triangle normal."""
+    a = np.zeros(25, dtype=np.float64)
+    for k, v in enumerate((v0, v1, v2, triangle_normal, point, normal, movement)):
+        a[3 * k: 3 * k + 3] = v
+    a[24] = active_edges
+    return load().orc_fix_normal(dptr(a))
