@@ -74,6 +74,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--adjoint", type=int, default=1, help="measure the rollout adjoint (1) or skip it (0)")
     ap.add_argument("--ragdolls", type=int, default=1, help="measure the jointed-ragdoll workload (1) or skip it (0)")
+    ap.add_argument("--terrain", type=int, default=1, help="measure the mixed-shape terrain workload (1) or skip it (0)")
     ap.add_argument("--settle", type=int, default=360,
                     help="untimed steps before the warm-up so the timed steps are contact-rich")
     return ap.parse_args()
@@ -421,6 +422,53 @@ def ragdoll_measurement(cpu_seconds: float = 8.0):
                              "gpu_same_phase_value": sc.n / (gpu_first * 1e-3)}}
 
 
+def terrain_measurement(cpu_seconds: float = 8.0):
+    """The mixed-shape terrain workload: 20,000 bodies (spheres, boxes, capsules and convex hulls
+    of 16-32 points in the mixed pile's size ranges) dropped from 5-40 m over a 256 x 256-cell
+    heightfield mesh (1 m cells, 4 m of relief, 131,072 triangles); 20 % of them start at
+    20-60 m/s with LINEAR_CAST motion quality.  dt 1/60, 8/2 iterations, 300 steps from spawn on
+    the GPU, timed per phase; the FP64 oracle on the same scene for a bounded number of steps
+    from spawn on one host core."""
+    from crashcat_gb300 import _lib, scenes, world as W
+    from oracle import build as obuild, pyoracle
+    sc = scenes.mesh_drop(n=20000, n_cells=256, seed=2, amplitude=4.0, heights=(5.0, 40.0), fast_fraction=0.2)
+    ws = W.standard_settings(velocity_iterations=8, position_iterations=2)
+    g = W.GpuWorld(ws, sc.n + 16)
+    for p in sc.hull_points:
+        g.add_convex_hull(p)
+    g.add_triangle_mesh(*sc.mesh)
+    g.add_bodies(sc.bodies)
+    phases, total_ms, status = [], 0.0, 0
+    for first, count in ((0, 100), (100, 100), (200, 100)):
+        status |= g.step(sc.dt, count)
+        st = g.stats()
+        total_ms += st["last_call_ms"]
+        phases.append({"steps": [first, first + count], "ms_per_step": st["last_call_ms"] / count,
+                       "awake": st["num_awake"], "manifolds": st["num_manifolds"], "epa": st["num_epa"],
+                       "mesh_pairs": st["num_mesh_pairs"], "mesh_hits": st["num_mesh_hits"],
+                       "ccd": st["num_ccd"], "ccd_hits": st["num_ccd_hits"], "islands": st["num_islands"]})
+    rows, _ = g.get_state()
+    hulls = [g.get_convex_hull(i) for i in range(len(sc.hull_points))]
+    mesh = g.get_triangle_mesh(0)
+    del g
+    obuild.build()
+    o = pyoracle.OracleWorld(ws, sc.bodies, hulls, [mesh])
+    t0, k = time.perf_counter(), 0
+    while time.perf_counter() - t0 < cpu_seconds and k < 100:
+        o.step(sc.dt, 1)
+        k += 1
+    cpu_s = time.perf_counter() - t0
+    return {"workload": "terrain_mixed", "bodies": int(sc.n - 1), "triangles": int(len(mesh["triangles"])),
+            "hulls": int(len(hulls)), "linear_cast_bodies": int((sc.bodies["motion_quality"] == 1).sum()),
+            "steps": 300, "value": (sc.n - 1) * 300 / (total_ms * 1e-3), "unit": METRIC,
+            "ms_per_step": total_ms / 300, "phases": phases, "status": int(status),
+            "finite": bool(np.isfinite(rows).all()),
+            "below_terrain": int((rows[1:, 1] < -2.5).sum()),
+            "cpu_baseline": {"value": (sc.n - 1) * k / cpu_s, "unit": METRIC, "cores": 1, "kind": "port",
+                             "sample": f"first {k} steps from spawn (falling phase)",
+                             "gpu_same_phase_value": (sc.n - 1) / (phases[0]["ms_per_step"] * 1e-3)}}
+
+
 def single_world_comparison(scene, ws_batched, settled_rows, dt, steps: int, sample_worlds: int = 48):
     """Steps a spread sample of the workload's worlds through the plain single-world path:
     one handle per world, each stepped once per step with cc_world_step (which blocks until
@@ -547,6 +595,7 @@ def run_gpu(args, rank, world_size, local):
     single = single_world_comparison(scene, ws, settled_rows, dt, steps=max(3, min(args.steps, 10)))
     adjoint = adjoint_measurement() if args.adjoint else None
     ragdolls = ragdoll_measurement() if args.ragdolls and rank == 0 else None
+    terrain = terrain_measurement() if args.terrain and rank == 0 else None
     single["batched_over_single"] = value / world_size / single["value"]
 
     if rank == 0:
@@ -571,6 +620,7 @@ def run_gpu(args, rank, world_size, local):
             "vs_single_world": single,
             "adjoint": adjoint,
             "ragdolls": ragdolls,
+            "terrain": terrain,
             "clocks": clk.summary(),
             "gpu_launches": stats["gpu_launches_per_step"] * args.steps,
             "counters": {k: stats_w[k] for k in ("num_awake", "num_pairs", "num_manifolds", "num_contact_points",

@@ -38,6 +38,7 @@ struct cc_world {
     std::vector<DevSwing> swings;
     std::vector<cc_hull::Hull> hulls;  // convex hull shapes as built
     std::vector<cc_mesh::Mesh> meshes;  // triangle meshes as built
+    bool hulls_dirty = false, meshes_dirty = false;  // added since the last upload
     float *d_state_rows = nullptr;  // 16 floats per body staging for get/set state
     float *h_pinned_rows = nullptr;
     DevCounters *h_ctr = nullptr;   // pinned mirror of the device counters
@@ -785,8 +786,25 @@ static void enqueue_step(cc_world *W, float dt, float ratio, cudaEvent_t *ev = n
     cudaMemcpyAsync(W->h_ctr, w.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s);
 }
 
+// hulls and meshes added since the last launch go to the device in one upload each
+static int upload_hulls(cc_world *W);
+static int upload_meshes(cc_world *W);
+static int sync_shapes(cc_world *W) {
+    int r = CC_OK;
+    if (W->hulls_dirty) {
+        if ((r = upload_hulls(W)) != CC_OK) return r;
+        W->hulls_dirty = false;
+    }
+    if (W->meshes_dirty) {
+        if ((r = upload_meshes(W)) != CC_OK) return r;
+        W->meshes_dirty = false;
+    }
+    return r;
+}
+
 static int run_steps(cc_world *W, float dt, int n_steps) {
     if (W->w.n == 0) return CC_OK;
+    if (int r = sync_shapes(W)) return r;
     upload_settings(W->dev_settings, W->settings.speculative_contact_distance, W->stream);
     int status = CC_OK;
     if (!W->ev_begin) {
@@ -878,6 +896,7 @@ int cc_world_get_state(cc_world *W, float *rows, uint8_t *sleeping) {
     if (!W || !rows) return CC_ERR_INVALID;
     DevWorld &w = W->w;
     if (w.n == 0) return CC_OK;
+    if (int r = sync_shapes(W)) return r;
     k_pack_state<<<grid_for(w.n, 256), 256, 0, W->stream>>>(w, W->d_state_rows, nullptr);
     CC_TRY(cudaMemcpyAsync(rows, W->d_state_rows, sizeof(float) * 16 * w.n, cudaMemcpyDeviceToHost, W->stream));
     if (sleeping) {
@@ -894,6 +913,7 @@ int cc_world_set_state(cc_world *W, const float *rows) {
     if (!W || !rows) return CC_ERR_INVALID;
     DevWorld &w = W->w;
     if (w.n == 0) return CC_OK;
+    if (int r = sync_shapes(W)) return r;
     CC_TRY(cudaMemcpyAsync(W->d_state_rows, rows, sizeof(float) * 16 * w.n, cudaMemcpyHostToDevice, W->stream));
     k_unpack_state<<<grid_for(w.n, 256), 256, 0, W->stream>>>(w, W->d_state_rows);
     CC_TRY(cudaStreamSynchronize(W->stream));
@@ -1045,6 +1065,7 @@ int cc_world_debug_islands(cc_world *W, int32_t *island_of_body, int32_t *cons_r
 int cc_world_profile_steps(cc_world *W, float dt, int32_t n_steps, float *stage_ms, int32_t n_stages) {
     if (!W || !stage_ms || n_steps <= 0 || n_stages < CC_PROFILE_STAGES) return CC_ERR_INVALID;
     if (W->w.n == 0) return CC_OK;
+    if (int r = sync_shapes(W)) return r;
     upload_settings(W->dev_settings, W->settings.speculative_contact_distance, W->stream);
     cudaEvent_t ev[CC_PROFILE_STAGES + 1];
     for (int k = 0; k <= CC_PROFILE_STAGES; k++) CC_TRY(cudaEventCreate(&ev[k]));
@@ -1149,6 +1170,9 @@ int cc_world_get_stats(cc_world *W, cc_stats *o) {
     o->giant_colours = c.giant_colours;
     o->num_ccd = c.num_ccd;
     o->num_ccd_hits = c.num_ccd_hits;
+    o->num_mesh_pairs = c.num_mesh_pairs;
+    o->num_mesh_hits = c.num_mesh_hits;
+    o->mesh_reduced = c.mesh_reduced;
     return CC_OK;
 }
 
@@ -1240,6 +1264,7 @@ extern "C" int cc_world_rollout_grad(cc_world *W, float dt, int32_t n_steps, int
                                      const float *targets, float *loss, float *grad_linvel, float *grad_angvel,
                                      float *grad_friction) {
     if (!W || !targets || n_steps <= 0 || checkpoint_every <= 0 || !(dt > 0.f)) return CC_ERR_INVALID;
+    if (int r = sync_shapes(W)) return r;
     DevWorld &w = W->w;
     if (w.n == 0) return CC_ERR_INVALID;
     // the adjoint covers contacts and the discrete integration only
@@ -1920,10 +1945,8 @@ int cc_world_add_triangle_mesh(cc_world *W, const double *positions, int32_t nv,
     int r = build_mesh_from(positions, nv, indices, nt, degenerate_tolerance, active_edge_cos, m);
     if (r != CC_OK) return r;
     W->meshes.push_back(std::move(m));
-    if ((r = upload_meshes(W)) != CC_OK) {
-        W->meshes.pop_back();
-        return r;
-    }
+    W->meshes_dirty = true;  // uploaded with the next launch (sync_shapes)
+    drop_graph(W);
     if (out_mesh) *out_mesh = (int32_t)W->meshes.size() - 1;
     return CC_OK;
 }
@@ -1954,10 +1977,8 @@ int cc_world_add_convex_hull(cc_world *W, const float *points, int32_t n, float 
     int r = build_hull_from(points, n, convex_radius, h);
     if (r != CC_OK) return r;
     W->hulls.push_back(h);
-    if ((r = upload_hulls(W)) != CC_OK) {
-        W->hulls.pop_back();
-        return r;
-    }
+    W->hulls_dirty = true;  // uploaded with the next launch (sync_shapes)
+    drop_graph(W);
     if (out_hull) *out_hull = (int32_t)W->hulls.size() - 1;
     return CC_OK;
 }

@@ -164,6 +164,9 @@ typedef struct cc_stats {
     int32_t giant_colours;     /* colours of the largest of them */
     int32_t num_ccd;           /* LINEAR_CAST bodies cast along their motion in the last step */
     int32_t num_ccd_hits;      /* of them, those whose cast hit a body (findCCDContacts update.ts:1354) */
+    int32_t num_mesh_pairs;    /* broadphase pairs with a triangle mesh body */
+    int32_t num_mesh_hits;     /* triangle hits handed to those pairs' reduction */
+    int32_t mesh_reduced;      /* mesh pairs whose hits wanted more manifolds than a pair keeps (4) */
 } cc_stats;
 
 typedef struct cc_world cc_world;
