@@ -2393,9 +2393,9 @@ void launch_mesh_narrowphase(DevWorld &w, int pass, cudaStream_t s) {
 // false on a miss, else the time of impact, the closest points then and the unnormalised
 // separating axis (closest points found without the last point being required,
 // computeClosestPointToSimplex gjk.ts:524-596).
-template <typename S>
-__device__ bool gjk_cast(S &lambda_out, V<S> &pa, V<S> &pb, V<S> &axis_out, const Sup<S> &A, const Sup<S> &B,
-                         V<S> disp, S tol, S rA, S rB, S maxLambda) {
+template <typename S, class SA, class SB>
+__device__ bool gjk_cast(S &lambda_out, V<S> &pa, V<S> &pb, V<S> &axis_out, const SA &A, const SB &B, V<S> disp,
+                         S tol, S rA, S rB, S maxLambda) {
     S sqtol = tol * tol;
     const S sumR = rA + rB;
     Simplex<S> sx;
@@ -2521,6 +2521,240 @@ __device__ __forceinline__ float ray_box_entry(float3 o, float3 d, float len, fl
     return t0;
 }
 
+// rayDistanceToBox3 cast-utils.ts:14-49 (the entry fraction, +inf on a miss)
+__device__ __forceinline__ float ray_fraction_to_box(float3 o, float3 d, float len, float3 lo, float3 hi) {
+    float t = ray_box_entry(o, d, len, lo, hi);
+    return t < CUDART_INF_F ? t / len : CUDART_INF_F;
+}
+// rayCylinder / raySphereFromOrigin sphere-triangle.ts:17-83, 156-195
+__device__ float ray_cylinder(float3 dir, float3 ca, float3 cb, float r) {
+    float3 axis = cb - ca, st = -ca;
+    float sda = dot3(st, axis), dda = dot3(dir, axis), eda = sda + dda;
+    if (sda < 0.f && eda < 0.f) return CUDART_INF_F;
+    float al2 = lensq3(axis);
+    if (sda > al2 && eda > al2) return CUDART_INF_F;
+    float a = al2 * lensq3(dir) - dda * dda;
+    if (fabsf(a) < 1e-6f) return CUDART_INF_F;
+    float b = al2 * dot3(st, dir) - dda * sda;
+    float c = al2 * (lensq3(st) - r * r) - sda * sda;
+    float det = b * b - a * c;
+    if (det < 0.f) return CUDART_INF_F;
+    float t = -(b + sqrtf(det)) / a;
+    if (t < 0.f || t > 1.f) return CUDART_INF_F;
+    float hda = sda + t * dda;
+    if (hda < 0.f || hda > al2) return CUDART_INF_F;
+    return t;
+}
+__device__ float ray_sphere_from_origin(float3 dir, float3 c, float r) {
+    float a = lensq3(dir), b = -2.f * dot3(dir, c), cc = lensq3(c) - r * r;
+    float disc = b * b - 4.f * a * cc;
+    if (disc < 0.f || a < 1e-10f) return cc <= 0.f ? 0.f : CUDART_INF_F;
+    float sq = sqrtf(disc);
+    float t1 = (-b - sq) / (2.f * a), t2 = (-b + sq) / (2.f * a);
+    if (t1 > t2) {
+        float t = t1;
+        t1 = t2;
+        t2 = t;
+    }
+    if (t1 >= 0.f && t1 <= 1.f) return t1;
+    if (t2 >= 0.f && t2 <= 1.f) return 0.f;
+    if (t1 < 0.f && t2 > 1.f) return 0.f;
+    return CUDART_INF_F;
+}
+
+// castConvexVsTriangleMesh triangle-mesh.ts:638-1019 and castSphereVsTriangleMesh :1781-2236
+// for the continuous-collision visitor (default cast settings: tolerances 0.01, support mode
+// DEFAULT, back faces culled, no movement direction, no deepest point).  collect(fraction,
+// world point on A, world penetration axis) is the collector; fps its early-out fraction.
+template <class Collect>
+__device__ void ccd_cast_mesh(const DevWorld &w, uint32_t fa, float4 sa, float3 pA, float4 qA4, float3 disp, int b,
+                              const float &fps, Collect &&collect) {
+    const DevMesh &M = w.meshes[mesh_of(w.shape[b])];
+    if (M.num_tris == 0) return;
+    const float3 pB = xyz(w.pos[b]);
+    const float4 qB4 = w.quat[b];
+    const Q<float> qB{qB4.x, qB4.y, qB4.z, qB4.w}, iqB{-qB4.x, -qB4.y, -qB4.z, qB4.w};
+    auto toB = [&](float3 v) {
+        V<float> q = qrotS(iqB, V<float>{v.x, v.y, v.z});
+        return f3(q.x, q.y, q.z);
+    };
+    auto toW = [&](float3 v) {
+        V<float> q = qrotS(qB, V<float>{v.x, v.y, v.z});
+        return f3(q.x, q.y, q.z);
+    };
+    const float3 dInB = toB(disp);
+    const float4 *nodes = w.mesh_nodes + 2 * M.first_node;
+    int stack[MESH_STACK];
+    float sdist[MESH_STACK];
+    if (shape_of(fa) == SHAPE_SPHERE) {
+        const float r = sa.x;
+        const float3 start = toB(pA - pB), end = start + dInB;
+        const float3 lo = f3(fminf(start.x, end.x) - r, fminf(start.y, end.y) - r, fminf(start.z, end.z) - r);
+        const float3 hi = f3(fmaxf(start.x, end.x) + r, fmaxf(start.y, end.y) + r, fmaxf(start.z, end.z) + r);
+        const float3 qc = (lo + hi) * 0.5f;
+        // castSphereVsTriangleMeshAddHit :1781-1868: the penetration axis is the negated contact normal
+        auto emit = [&](float fraction, float3 cp, float3 cn) {
+            collect(fraction, toW(start + cp) + pB, -normalize3(toW(cn)));
+        };
+        int sp = 0;
+        stack[sp++] = 0;
+        while (sp > 0) {
+            const int node = stack[--sp];
+            const float4 nlo = nodes[2 * node], nhi = nodes[2 * node + 1];
+            if (!node_hits_box(nlo, nhi, lo, hi)) continue;
+            const int aux = __float_as_int(nlo.w), tag = __float_as_int(nhi.w);
+            if (tag >= 0) {
+                const int left = node + 1, right = aux;
+                float ld = lensq3(qc - (xyz(nodes[2 * left]) + xyz(nodes[2 * left + 1])) * 0.5f);
+                float rd = lensq3(qc - (xyz(nodes[2 * right]) + xyz(nodes[2 * right + 1])) * 0.5f);
+                if (sp + 2 > MESH_STACK) continue;
+                if (ld <= rd) {
+                    stack[sp++] = right;
+                    stack[sp++] = left;
+                } else {
+                    stack[sp++] = left;
+                    stack[sp++] = right;
+                }
+                continue;
+            }
+            for (int ti = aux; ti < aux + (-tag - 1); ti++) {
+                const int4 tr = w.mesh_tris[M.first_tri + ti];
+                const float3 v0 = xyz(w.mesh_verts[tr.x]) - start, v1 = xyz(w.mesh_verts[tr.y]) - start,
+                             v2 = xyz(w.mesh_verts[tr.z]) - start;
+                float3 tn = cross3(v1 - v0, v2 - v0);
+                const float tl = sqrtf(lensq3(tn));
+                if (tl == 0.f) continue;
+                tn = tn * (1.f / tl);
+                const float ndd = dot3(tn, dInB);
+                if (ndd > 0.f) continue;  // back face
+                if (fabsf(dot3(v0, tn)) <= r) {  // touching at the start
+                    float dsq;
+                    int feature;
+                    float3 q = closest_on_triangle(v0, v1, v2, dsq, feature);
+                    if (dsq <= r * r) {
+                        const float ql = sqrtf(dsq), pen = r - ql;
+                        if (-pen >= fps) continue;
+                        const float3 cn = ql > 0.f ? q * (1.f / ql) : f3(0.f, 1.f, 0.f);
+                        emit(0.f, q + cn * pen, cn);
+                        continue;
+                    }
+                }
+                if (fabsf(ndd) > 1e-6f) {  // the plane
+                    const float3 d = tn * ((ndd > 0.f ? 1.f : (ndd < 0.f ? -1.f : 0.f)) * r);
+                    const float pi = dot3(v0 - d, tn) / ndd;
+                    if (pi * fabsf(ndd) >= -r && pi < fps && pi >= 0.f) {
+                        const float3 p = d + dInB * pi;
+                        const float3 a0 = v0 - p, a1 = v1 - p, a2 = v2 - p;
+                        const float3 nn = cross3(a1, a2);
+                        const float nl = sqrtf(lensq3(nn));
+                        if (nl > 0.f) {
+                            const float area = dot3(nn, tn) / nl;
+                            if (area > 0.f) {
+                                const float u = dot3(cross3(a1, a2), tn) / (area * nl),
+                                            v = dot3(cross3(a2, a0), tn) / (area * nl),
+                                            ww = dot3(cross3(a0, a1), tn) / (area * nl);
+                                if (u >= 0.f && v >= 0.f && ww >= 0.f) {
+                                    emit(pi, p, -tn);
+                                    continue;
+                                }
+                            }
+                        }
+                    }
+                }
+                float f = CUDART_INF_F;  // edges and vertices
+                f = fminf(f, ray_cylinder(dInB, v0, v1, r));
+                f = fminf(f, ray_cylinder(dInB, v1, v2, r));
+                f = fminf(f, ray_cylinder(dInB, v2, v0, r));
+                f = fminf(f, ray_sphere_from_origin(dInB, v0, r));
+                f = fminf(f, ray_sphere_from_origin(dInB, v1, r));
+                f = fminf(f, ray_sphere_from_origin(dInB, v2, r));
+                if (f >= 0.f && f < fps) {
+                    const float3 p = dInB * f;
+                    float dsq;
+                    int feature;
+                    const float3 q = closest_on_triangle(v0 - p, v1 - p, v2 - p, dsq, feature);
+                    emit(f, p + q, normalize3(q));
+                }
+            }
+        }
+        return;
+    }
+    // the GJK cast of the convex shape: A placed in the mesh's frame
+    const Q<float> qAq{qA4.x, qA4.y, qA4.z, qA4.w};
+    const Q<float> qAInB = qmulS(iqB, qAq);
+    const float3 posAInB = toB(pA - pB);
+    float3 llo, lhi;
+    convex_local_bounds(w, fa, sa, llo, lhi);
+    float3 blo = f3(3.0e38f, 3.0e38f, 3.0e38f), bhi = f3(-3.0e38f, -3.0e38f, -3.0e38f);
+    for (int c = 0; c < 8; c++) {
+        V<float> p{(c & 1) ? lhi.x : llo.x, (c & 2) ? lhi.y : llo.y, (c & 4) ? lhi.z : llo.z};
+        V<float> q = qrotS(qAInB, p);
+        float3 qq = f3(q.x, q.y, q.z) + posAInB;
+        blo = f3(fminf(blo.x, qq.x), fminf(blo.y, qq.y), fminf(blo.z, qq.z));
+        bhi = f3(fmaxf(bhi.x, qq.x), fmaxf(bhi.y, qq.y), fmaxf(bhi.z, qq.z));
+    }
+    const HullView hv = hull_view(w);
+    // SupportFunctionMode.DEFAULT: the full box, the other shapes' core with their radius
+    Sup<float> supA = make_sup<float>(shape_of(fa), sa, shape_of(fa) != SHAPE_BOX, hv);
+    const float crA = supA.convex_radius;
+    set_transform(supA, qAInB, V<float>{posAInB.x, posAInB.y, posAInB.z});
+    const float3 origin = (blo + bhi) * 0.5f, half = (bhi - blo) * 0.5f;
+    const float rlen = sqrtf(lensq3(dInB));
+    const float3 rdir = rlen > 1e-10f ? dInB * (1.f / rlen) : f3(0.f, 0.f, 0.f);
+    const V<float> dv{dInB.x, dInB.y, dInB.z};
+    int sp = 0;
+    stack[sp] = 0;
+    sdist[sp++] = 0.f;
+    while (sp > 0) {
+        --sp;
+        const int node = stack[sp];
+        if (sdist[sp] >= fps) continue;
+        const float4 nlo = nodes[2 * node], nhi = nodes[2 * node + 1];
+        const int aux = __float_as_int(nlo.w), tag = __float_as_int(nhi.w);
+        if (tag >= 0) {
+            const int left = node + 1, right = aux;
+            float ld = ray_fraction_to_box(origin, rdir, rlen, xyz(nodes[2 * left]) - half,
+                                           xyz(nodes[2 * left + 1]) + half);
+            float rd = ray_fraction_to_box(origin, rdir, rlen, xyz(nodes[2 * right]) - half,
+                                           xyz(nodes[2 * right + 1]) + half);
+            if (sp + 2 > MESH_STACK) continue;
+            if (ld <= rd) {
+                if (rd < fps) stack[sp] = right, sdist[sp++] = rd;
+                if (ld < fps) stack[sp] = left, sdist[sp++] = ld;
+            } else {
+                if (ld < fps) stack[sp] = left, sdist[sp++] = ld;
+                if (rd < fps) stack[sp] = right, sdist[sp++] = rd;
+            }
+            continue;
+        }
+        for (int ti = aux; ti < aux + (-tag - 1); ti++) {
+            const int4 tr = w.mesh_tris[M.first_tri + ti];
+            const float3 a = xyz(w.mesh_verts[tr.x]), bb = xyz(w.mesh_verts[tr.y]), c = xyz(w.mesh_verts[tr.z]);
+            const float3 tlo = f3(fminf(a.x, fminf(bb.x, c.x)), fminf(a.y, fminf(bb.y, c.y)), fminf(a.z, fminf(bb.z, c.z)));
+            const float3 thi = f3(fmaxf(a.x, fmaxf(bb.x, c.x)), fmaxf(a.y, fmaxf(bb.y, c.y)), fmaxf(a.z, fmaxf(bb.z, c.z)));
+            if (!(ray_box_entry(origin, rdir, rlen, tlo - half, thi + half) < CUDART_INF_F)) continue;
+            if (fps <= 0.f) return;
+            const float3 n = cross3(bb - a, c - a);
+            if (dot3(n, dInB) > 0.f) continue;  // back face
+            Sup<float, true, true> supT = make_sup<float, true, true>(SHAPE_SPHERE, make_float4(0.f, 0.f, 0.f, 0.f), false, hv);
+            supT.kind = SUP_TRIANGLE;
+            supT.r0 = V<float>{a.x, a.y, a.z};
+            supT.r1 = V<float>{bb.x, bb.y, bb.z};
+            supT.r2 = V<float>{c.x, c.y, c.z};
+            supT.convex_radius = 0.f;
+            float lambda;
+            V<float> cpa, cpb, ax;
+            if (!gjk_cast(lambda, cpa, cpb, ax, supA, supT, dv, 0.01f, crA, 0.f, fps)) continue;
+            if (lsq(ax) < 0.01f * 0.01f) ax = dv;  // penetration.ts:693-698
+            const float depth = sqrtf(lsq(cpa - cpb));
+            if (lambda == 0.f && -depth >= fps) continue;
+            float3 axf = f3(ax.x, ax.y, ax.z);
+            if (tr.w != 0b111) axf = fix_normal(a, bb, c, n, tr.w, f3(cpb.x, cpb.y, cpb.z), axf, f3(0.f, 0.f, 0.f));
+            collect(lambda, toW(f3(cpa.x, cpa.y, cpa.z)) + pB, toW(axf));
+        }
+    }
+}
+
 // findCCDContacts update.ts:1354-1470: one thread per record.  The swept bounds are cast
 // through the refitted tree (dbvt.castAABB dbvt.ts:869-975: a ray from the swept centre along
 // the displacement against boxes grown by the swept half extents, nodes past the distance cull
@@ -2582,9 +2816,6 @@ __global__ void __launch_bounds__(128) k_ccd_find(DevWorld w, const int2 *node_w
             if (!((ga.x & gb.y) != 0u && (gb.x & ga.y) != 0u)) continue;
             // ccdBodyVisitor.visit update.ts:1153-1206
             if (b == a) continue;
-            // casts against triangle meshes (castConvexVsTriangleMesh triangle-mesh.ts:1784-2100)
-            // are not built: a mesh body is not a cast candidate
-            if (shape_of(fb) == SHAPE_MESH) continue;
             const int cb = w.ccd_index[b];
             if (cb >= 0 && a > b) continue;  // a pair of cast bodies is cast once, by the lower index
             if (fb & F_SENSOR) continue;
@@ -2593,6 +2824,29 @@ __global__ void __launch_bounds__(128) k_ccd_find(DevWorld w, const int2 *node_w
             if (lensq3(rel) < thr_sq) continue;
             const float3 blo = xyz(w.aabb_lo[b]) - half_a, bhi = xyz(w.aabb_hi[b]) + half_a;
             if (!(ray_box_entry(pA, rel, sqrtf(lensq3(rel)), blo, bhi) < CUDART_INF_F)) continue;
+            // ccdCastShapeCollector.addHit update.ts:1044-1109
+            auto collect = [&](float lambda, float3 paw, float3 axw) {
+                const float3 nrm = normalize3(axw);
+                const float den = dot3(nrm, delta);
+                if (den <= max_pen) return;
+                const float fps = lambda + max_pen / den;
+                if (!(fps < best_fps || (fps == best_fps && best >= 0 && b < best))) return;
+                best = b;
+                best_fps = fps;
+                best_frac = lambda;
+                best_n = nrm;
+                float3 pt = paw;
+                // calculateBodyMotion update.ts:984-994
+                if (motion_of(fb) != STATIC && (fb & F_LINEAR_CAST)) {
+                    float3 mb = xyz(w.linvel[b]) * dt;
+                    if (lensq3(mb) > 1e-12f) pt = pt + mb * lambda;
+                }
+                best_p = pt;
+            };
+            if (shape_of(fb) == SHAPE_MESH) {
+                ccd_cast_mesh(w, fa, w.shape[a], pA, qA, rel, b, best_fps, collect);
+                continue;
+            }
             // castConvexVsConvex: A in B's frame
             const float3 pB = xyz(w.pos[b]);
             const float4 qB = w.quat[b];
@@ -2611,26 +2865,10 @@ __global__ void __launch_bounds__(128) k_ccd_find(DevWorld w, const int2 *node_w
             // penetrationCastShape penetration.ts:693-698: a too short axis becomes the cast direction
             if (lsq(ax) < 1e-4f * 1e-4f) ax = dInB;
             if (lambda > 1.f || dot(ax, dInB) <= 0.f || lambda >= best_fps) continue;
-            // ccdCastShapeCollector.addHit update.ts:1044-1109
             const Q<float> qBq{qB.x, qB.y, qB.z, qB.w};
             const V<float> axw = qrotS(qBq, ax);
-            const float3 nrm = normalize3(f3(axw.x, axw.y, axw.z));
-            const float den = dot3(nrm, delta);
-            if (den <= max_pen) continue;
-            const float fps = lambda + max_pen / den;
-            if (!(fps < best_fps || (fps == best_fps && best >= 0 && b < best))) continue;
-            best = b;
-            best_fps = fps;
-            best_frac = lambda;
-            best_n = nrm;
             const V<float> paw = qrotS(qBq, cpa);
-            float3 pt = f3(paw.x + pB.x, paw.y + pB.y, paw.z + pB.z);
-            // calculateBodyMotion update.ts:984-994
-            if (motion_of(fb) != STATIC && (fb & F_LINEAR_CAST)) {
-                float3 mb = xyz(w.linvel[b]) * dt;
-                if (lensq3(mb) > 1e-12f) pt = pt + mb * lambda;
-            }
-            best_p = pt;
+            collect(lambda, f3(paw.x + pB.x, paw.y + pB.y, paw.z + pB.z), f3(axw.x, axw.y, axw.z));
         }
         if (best >= 0) {
             c.hit = best;

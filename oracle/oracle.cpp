@@ -1324,8 +1324,6 @@ static void find_ccd_contacts(World &w, double dt) {
             if (!(t < std::numeric_limits<double>::infinity()) || t / castLen > castLen) continue;
             // ccdBodyVisitor.visit update.ts:1153-1250
             if (B.index == A.index) continue;
-            // castConvexVsTriangleMesh (triangle-mesh.ts) is not restated: meshes are not cast against
-            if (B.shape.type == SHAPE_TRIANGLE_MESH) continue;
             const World::CCDRecord *cb = B.ccdIndex >= 0 ? &w.ccd[B.ccdIndex] : nullptr;
             if (cb && c.body > cb->body) continue;
             if (B.sensor) continue;
@@ -1335,26 +1333,41 @@ static void find_ccd_contacts(World &w, double dt) {
             if (!(ray_box_entry(A.position, rel, relLen, box_grow(B.aabb, halfA)) <
                   std::numeric_limits<double>::infinity()))
                 continue;
+            // ccdCastShapeCollector.addHit update.ts:1044-1109
+            auto collect = [&](double fraction, V3 pa, V3 axis) {
+                V3 n = normalize(axis);
+                double den = dot(n, c.delta);
+                if (den <= c.maxPenetration) return;
+                double fps = fraction + c.maxPenetration / den;
+                if (fps >= c.fps) return;
+                c.hit = B.index;
+                c.fraction = fraction;
+                c.fps = fps;
+                c.normal = n;
+                // calculateBodyMotion update.ts:984-994: a moving LINEAR_CAST body B counts its
+                // velocity step, whether or not it took the continuous path this step
+                V3 mB{0, 0, 0};
+                if (B.motion != STATIC && B.linearCast) mB = scale(B.linvel, dt);
+                c.point = lensq(mB) > 1e-12 ? add(pa, scale(mB, fraction)) : pa;
+                c.friction = combine(A.friction, B.friction, A.frictionCombine, B.frictionCombine);
+                c.restitution = combine(A.restitution, B.restitution, A.restitutionCombine, B.restitutionCombine);
+            };
+            if (B.shape.type == SHAPE_TRIANGLE_MESH) {
+                // castShapeVsShape dispatch (triangle-mesh.ts:223-237): the sphere's own cast
+                // for spheres, the GJK cast for the other shapes; the collector's early-out
+                // fraction tightens with each hit
+                auto onHit = [&](const CastMeshHit &h) { collect(h.fraction, h.pa, h.axis); };
+                auto earlyOut = [&]() { return c.fps; };
+                if (A.shape.type == SHAPE_SPHERE)
+                    cast_sphere_vs_mesh(A.shape, A.position, rel, B.shape, B.position, B.quat, onHit, earlyOut);
+                else
+                    cast_convex_vs_mesh(A.shape, A.position, A.quat, rel, B.shape, B.position, B.quat, onHit, earlyOut);
+                continue;
+            }
             CastHit h;
             if (!cast_convex_vs_convex(h, A.shape, A.position, A.quat, rel, B.shape, B.position, B.quat, c.fps, false))
                 continue;
-            // ccdCastShapeCollector.addHit update.ts:1044-1109
-            V3 n = normalize(h.axis);
-            double den = dot(n, c.delta);
-            if (den <= c.maxPenetration) continue;
-            double fps = h.fraction + c.maxPenetration / den;
-            if (fps >= c.fps) continue;
-            c.hit = B.index;
-            c.fraction = h.fraction;
-            c.fps = fps;
-            c.normal = n;
-            // calculateBodyMotion update.ts:984-994: a moving LINEAR_CAST body B counts its
-            // velocity step, whether or not it took the continuous path this step
-            V3 mB{0, 0, 0};
-            if (B.motion != STATIC && B.linearCast) mB = scale(B.linvel, dt);
-            c.point = lensq(mB) > 1e-12 ? add(h.pa, scale(mB, h.fraction)) : h.pa;
-            c.friction = combine(A.friction, B.friction, A.frictionCombine, B.frictionCombine);
-            c.restitution = combine(A.restitution, B.restitution, A.restitutionCombine, B.restitutionCombine);
+            collect(h.fraction, h.pa, h.axis);
         }
     }
 }

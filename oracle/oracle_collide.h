@@ -1987,6 +1987,245 @@ inline void collide_sphere_vs_mesh(std::vector<Hit> &out, const CollideSettings 
     });
 }
 
+// rayDistanceToBox3 cast-utils.ts:14-49: the entry fraction of the segment origin + t * dir
+// (t in [0, length]) into the box, +inf on a miss
+inline double ray_fraction_to_box(V3 o, V3 d, double length, const Box3 &b) {
+    double t0 = 0, t1 = length;
+    const double oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+    const double mn[3] = {b.mn.x, b.mn.y, b.mn.z}, mx[3] = {b.mx.x, b.mx.y, b.mx.z};
+    for (int i = 0; i < 3; i++) {
+        if (std::fabs(dd[i]) < 1e-10) {
+            if (oo[i] < mn[i] || oo[i] > mx[i]) return std::numeric_limits<double>::infinity();
+        } else {
+            double inv = 1.0 / dd[i];
+            double a = (mn[i] - oo[i]) * inv, c = (mx[i] - oo[i]) * inv;
+            t0 = std::max(t0, std::min(a, c));
+            t1 = std::min(t1, std::max(a, c));
+            if (t1 < t0) return std::numeric_limits<double>::infinity();
+        }
+    }
+    return t0 >= 0 ? t0 / length : std::numeric_limits<double>::infinity();
+}
+
+// A shape cast hit handed to a cast collector: fraction, world points, the unnormalised
+// penetration axis.  The collector returns nothing; earlyOut() is its current early-out fraction.
+struct CastMeshHit {
+    double fraction;
+    V3 pa, pb, axis;
+};
+
+// castConvexVsTriangleMesh triangle-mesh.ts:638-1019 with the default cast settings the
+// continuous-collision visitor uses (tolerances 0.01, SupportFunctionMode.DEFAULT, no deepest
+// point, back faces culled, no movement direction)
+template <class Add, class EarlyOut>
+inline void cast_convex_vs_mesh(const Shape &sa, V3 pA, Q4 qA, V3 disp, const Shape &sb, V3 pB, Q4 qB, Add &&onHit,
+                                EarlyOut &&earlyOut) {
+    const MeshData &M = *sb.mesh;
+    if (M.nodes.empty()) return;
+    Q4 iqB = qconj(qB);
+    V3 posAInB = rotate(iqB, sub(pA, pB));
+    Q4 qAInB = qmul(iqB, qA);
+    V3 dInB = rotate(iqB, disp);
+    Box3 base{{1e300, 1e300, 1e300}, {-1e300, -1e300, -1e300}};
+    for (int c = 0; c < 8; c++) {
+        V3 p{(c & 1) ? sa.aabb.mx.x : sa.aabb.mn.x, (c & 2) ? sa.aabb.mx.y : sa.aabb.mn.y,
+             (c & 4) ? sa.aabb.mx.z : sa.aabb.mn.z};
+        V3 q = add(rotate(qAInB, p), posAInB);
+        base.mn = {std::min(base.mn.x, q.x), std::min(base.mn.y, q.y), std::min(base.mn.z, q.z)};
+        base.mx = {std::max(base.mx.x, q.x), std::max(base.mx.y, q.y), std::max(base.mx.z, q.z)};
+    }
+    // SupportFunctionMode.DEFAULT: a box keeps its full extent (box.ts / support.ts:364), the
+    // other shapes their core with the convex radius (sphere.ts:258, capsule.ts:396, convex-hull.ts:978)
+    Support supA = make_support(sa, sa.type == SHAPE_BOX ? INCLUDE_CONVEX_RADIUS : EXCLUDE_CONVEX_RADIUS);
+    V3 origin = scale(add(base.mn, base.mx), 0.5);
+    double rlen = len(dInB);
+    V3 rdir = rlen > 1e-10 ? normalize(dInB) : V3{0, 0, 0};
+    V3 half = scale(sub(base.mx, base.mn), 0.5);
+    std::vector<std::pair<int, double>> stack{{0, 0.0}};
+    while (!stack.empty()) {
+        auto [node, dist] = stack.back();
+        stack.pop_back();
+        if (dist >= earlyOut()) continue;
+        const auto &nd = M.nodes[node];
+        if (nd[7] < 0) {
+            int start = (int)nd[6], count = (int)(-nd[7]) - 1;
+            for (int t = start; t < start + count; t++) {
+                const auto &tr = M.tris[t];
+                V3 a = M.verts[tr[0]], b = M.verts[tr[1]], c = M.verts[tr[2]];
+                Box3 tb{{std::min(a.x, std::min(b.x, c.x)) - half.x, std::min(a.y, std::min(b.y, c.y)) - half.y,
+                         std::min(a.z, std::min(b.z, c.z)) - half.z},
+                        {std::max(a.x, std::max(b.x, c.x)) + half.x, std::max(a.y, std::max(b.y, c.y)) + half.y,
+                         std::max(a.z, std::max(b.z, c.z)) + half.z}};
+                if (!(ray_fraction_to_box(origin, rdir, rlen, tb) < std::numeric_limits<double>::infinity())) continue;
+                if (earlyOut() <= 0) return;
+                V3 n = cross(sub(b, a), sub(c, a));
+                if (dot(n, dInB) > 0) continue;  // back face
+                Support tri;
+                tri.kind = SUP_TRIANGLE;
+                tri.ta = a;
+                tri.tb = b;
+                tri.tc = c;
+                Support A = supA;
+                A.transformed = true;
+                A.m = mat4_from_rt(qAInB, posAInB);
+                double lambda;
+                V3 pa, pb, ax;
+                const double tol = 0.01;
+                if (!gjk_cast_shape(lambda, pa, pb, ax, A, tri, dInB, tol, supA.convex_radius, 0.0, earlyOut()))
+                    continue;
+                if (lensq(ax) < tol * tol) ax = dInB;  // penetration.ts:693-698
+                double depth = len(sub(pa, pb));
+                if (lambda == 0 && -depth >= earlyOut()) continue;
+                if (tr[3] != 0b111)  // fixNormal with the triangle normal as given (back faces culled)
+                    ax = fix_normal(a, b, c, n, tr[3], pb, ax, V3{0, 0, 0});
+                onHit(CastMeshHit{lambda, add(rotate(qB, pa), pB), add(rotate(qB, pb), pB), rotate(qB, ax)});
+            }
+            continue;
+        }
+        int left = node + 1, right = (int)nd[6];
+        auto grown = [&](int k) {
+            const auto &c = M.nodes[k];
+            return Box3{{c[0] - half.x, c[1] - half.y, c[2] - half.z}, {c[3] + half.x, c[4] + half.y, c[5] + half.z}};
+        };
+        double ld = ray_fraction_to_box(origin, rdir, rlen, grown(left));
+        double rd = ray_fraction_to_box(origin, rdir, rlen, grown(right));
+        if (ld <= rd) {
+            if (rd < earlyOut()) stack.push_back({right, rd});
+            if (ld < earlyOut()) stack.push_back({left, ld});
+        } else {
+            if (ld < earlyOut()) stack.push_back({left, ld});
+            if (rd < earlyOut()) stack.push_back({right, rd});
+        }
+    }
+}
+
+// rayCylinder / raySphereFromOrigin sphere-triangle.ts:17-83, 156-195
+inline double ray_cylinder(V3 dir, V3 ca, V3 cb, double r) {
+    V3 axis = sub(cb, ca), start = neg(ca);
+    double sda = dot(start, axis), dda = dot(dir, axis), eda = sda + dda;
+    if (sda < 0 && eda < 0) return std::numeric_limits<double>::infinity();
+    double al2 = lensq(axis);
+    if (sda > al2 && eda > al2) return std::numeric_limits<double>::infinity();
+    double a = al2 * lensq(dir) - dda * dda;
+    if (std::fabs(a) < 1e-6) return std::numeric_limits<double>::infinity();
+    double b = al2 * dot(start, dir) - dda * sda;
+    double c = al2 * (lensq(start) - r * r) - sda * sda;
+    double det = b * b - a * c;
+    if (det < 0) return std::numeric_limits<double>::infinity();
+    double t = -(b + std::sqrt(det)) / a;
+    if (t < 0 || t > 1) return std::numeric_limits<double>::infinity();
+    double hda = sda + t * dda;
+    if (hda < 0 || hda > al2) return std::numeric_limits<double>::infinity();
+    return t;
+}
+inline double ray_sphere_from_origin(V3 dir, V3 c, double r) {
+    double a = lensq(dir), b = -2 * dot(dir, c), cc = lensq(c) - r * r;
+    double disc = b * b - 4 * a * cc;
+    if (disc < 0) return cc <= 0 ? 0 : std::numeric_limits<double>::infinity();
+    if (a < 1e-10) return cc <= 0 ? 0 : std::numeric_limits<double>::infinity();
+    double sq = std::sqrt(disc);
+    double t1 = (-b - sq) / (2 * a), t2 = (-b + sq) / (2 * a);
+    if (t1 > t2) std::swap(t1, t2);
+    if (t1 >= 0 && t1 <= 1) return t1;
+    if (t2 >= 0 && t2 <= 1) return 0;
+    if (t1 < 0 && t2 > 1) return 0;
+    return std::numeric_limits<double>::infinity();
+}
+
+// castSphereVsTriangleMesh triangle-mesh.ts:1870-2236 with castSphereVsTriangleMeshAddHit
+// :1781-1868 (default cast settings, no movement direction).  The hit's penetration axis is the
+// negated contact normal (:1847-1848).
+template <class Add, class EarlyOut>
+inline void cast_sphere_vs_mesh(const Shape &sa, V3 pA, V3 disp, const Shape &sb, V3 pB, Q4 qB, Add &&onHit,
+                                EarlyOut &&earlyOut) {
+    const MeshData &M = *sb.mesh;
+    if (M.nodes.empty()) return;
+    const double r = sa.radius;
+    Q4 iqB = qconj(qB);
+    V3 start = rotate(iqB, sub(pA, pB)), dir = rotate(iqB, disp);
+    V3 end = add(start, dir);
+    Box3 sw{{std::min(start.x, end.x) - r, std::min(start.y, end.y) - r, std::min(start.z, end.z) - r},
+            {std::max(start.x, end.x) + r, std::max(start.y, end.y) + r, std::max(start.z, end.z) + r}};
+    V3 qc = scale(add(sw.mn, sw.mx), 0.5);
+    auto emit = [&](bool back, V3 tn, int active, double fraction, V3 ca, V3 cbp, V3 cn) {
+        V3 fn = cn;
+        if (active != 0b111) {  // movement direction zero: the normal kept unless the check below flips it
+            V3 tnf = back ? tn : neg(tn);
+            V3 mv{0, 0, 0};
+            if (dot(mv, cn) * len(tnf) < dot(mv, tnf) * len(cn)) fn = tnf;
+        }
+        V3 pa = add(rotate(qB, add(start, ca)), pB), pb = add(rotate(qB, add(start, cbp)), pB);
+        V3 nw = normalize(rotate(qB, fn));
+        onHit(CastMeshHit{fraction, pa, pb, neg(nw)});
+    };
+    mesh_walk(M, sw, qc, [&](int t) {
+        const auto &tr = M.tris[t];
+        V3 rv0 = sub(M.verts[tr[0]], start), rv1 = sub(M.verts[tr[1]], start), rv2 = sub(M.verts[tr[2]], start);
+        V3 tn = cross(sub(rv1, rv0), sub(rv2, rv0));
+        double tl = len(tn);
+        if (tl == 0) return;
+        tn = scale(tn, 1.0 / tl);
+        double ndd = dot(tn, dir);
+        bool back = ndd > 0;
+        if (back) return;
+        int active = tr[3];
+        // already touching at the start
+        if (std::fabs(dot(rv0, tn)) <= r) {
+            double dsq;
+            int feature;
+            V3 q = closest_point_on_triangle(rv0, rv1, rv2, dsq, feature);
+            if (dsq <= r * r) {
+                double ql = std::sqrt(dsq);
+                double pen = r - ql;
+                if (-pen >= earlyOut()) return;
+                V3 cn = ql > 0 ? scale(q, 1 / ql) : V3{0, 1, 0};
+                emit(back, tn, active, 0.0, scale_add(q, cn, pen), q, cn);
+                return;
+            }
+        }
+        // the plane
+        double andd = std::fabs(ndd);
+        if (andd > 1e-6) {
+            V3 d = scale(tn, (ndd > 0 ? 1.0 : (ndd < 0 ? -1.0 : 0.0)) * r);
+            double pi = dot(sub(rv0, d), tn) / ndd;
+            if (pi * andd >= -r && pi < earlyOut() && pi >= 0) {
+                V3 p = scale_add(d, dir, pi);
+                V3 v0r = sub(rv0, p), v1r = sub(rv1, p), v2r = sub(rv2, p);
+                V3 nn = cross(v1r, v2r);
+                double nl = len(nn);
+                if (nl > 0) {
+                    double area = dot(nn, tn) / nl;
+                    if (area > 0) {
+                        double u = dot(cross(v1r, v2r), tn) / (area * nl), v = dot(cross(v2r, v0r), tn) / (area * nl),
+                               w = dot(cross(v0r, v1r), tn) / (area * nl);
+                        if (u >= 0 && v >= 0 && w >= 0) {
+                            emit(back, tn, 0b111, pi, p, p, back ? tn : neg(tn));
+                            return;
+                        }
+                    }
+                }
+            }
+        }
+        // edges and vertices
+        double f = std::numeric_limits<double>::infinity();
+        f = std::min(f, ray_cylinder(dir, rv0, rv1, r));
+        f = std::min(f, ray_cylinder(dir, rv1, rv2, r));
+        f = std::min(f, ray_cylinder(dir, rv2, rv0, r));
+        f = std::min(f, ray_sphere_from_origin(dir, rv0, r));
+        f = std::min(f, ray_sphere_from_origin(dir, rv1, r));
+        f = std::min(f, ray_sphere_from_origin(dir, rv2, r));
+        if (f >= 0 && f < earlyOut()) {
+            V3 p = scale(dir, f);
+            double dsq;
+            int feature;
+            V3 q = closest_point_on_triangle(sub(rv0, p), sub(rv1, p), sub(rv2, p), dsq, feature);
+            V3 cn = normalize(q);
+            V3 cp = add(p, q);
+            emit(back, tn, active, f, cp, cp, cn);
+        }
+    });
+}
+
 // the hits of a body pair in narrowphase order (collideShapeVsShape narrowphase.ts:172-238 with
 // the mesh registrations triangle-mesh.ts:223-237: a mesh as shape A runs the convex-vs-mesh
 // function reversed, collide-shape-vs-shape.ts:227-354)

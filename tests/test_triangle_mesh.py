@@ -245,3 +245,72 @@ def test_terrain_drop_settles(gpu_lib, oracle_lib):
     assert rows[1:, 1].min() > -1.5  # the terrain spans +-1 m: nothing fell through
     assert abs(rows[1:, 1].mean() - st[1:, 1].mean()) < 0.05
     assert g.stats()["overflow_flags"] == 0
+
+
+# ---------------------------------------------------------------------------
+# continuous collision against a mesh (castConvexVsTriangleMesh / castSphereVsTriangleMesh)
+# ---------------------------------------------------------------------------
+def ccd_mesh_scene(shape: str, amplitude: float):
+    """A LINEAR_CAST body at 80 m/s straight down onto an 8 x 8 terrain of the given relief."""
+    b = scenes.blank_bodies(2)
+    b["shape_type"][0] = _lib.SHAPE_TRIANGLE_MESH
+    b["motion_type"][0] = _lib.STATIC
+    b["object_layer"][0] = scenes.LAYER_NOT_MOVING
+    if shape == "box":
+        scenes.set_box(b, 1, (0.2, 0.2, 0.2))
+    else:
+        scenes.set_sphere(b, 1, 0.2)
+    b["position"][1] = (0.3, 3.0, 0.2)
+    b["linear_velocity"][1] = (0.0, -80.0, 0.0)
+    b["motion_quality"][1] = 1
+    b["gravity_factor"][1] = 0.0
+    return b
+
+
+CCD_MESH_CASES = [
+    # (shape, relief, active-edge cosine, caught by the cast)
+    ("box", 3.0, -2.0, True),     # sharp terrain: active edges, the hit registers
+    ("box", 0.0, -0.5, True),     # flat, every edge active: the hit registers
+    ("box", 0.0, -2.0, False),    # flat, inner edges inactive: fixNormal turns the axis to the
+                                  # triangle normal, which faces the body; the collector drops it
+    ("sphere", 0.0, -0.5, False), # the sphere cast reports the negated contact normal
+                                  # (triangle-mesh.ts:1847-1848): the collector drops it
+]
+
+
+@pytest.mark.parametrize("shape,relief,cos,caught", CCD_MESH_CASES)
+def test_oracle_ccd_against_mesh(gpu_lib, oracle_lib, shape, relief, cos, caught):
+    """The continuous-collision cast against a mesh as the reference wires it: the visitor casts
+    every LINEAR_CAST body against the mesh body (update.ts:1210-1240), and the collector keeps a
+    hit only when its penetration axis points along the motion (update.ts:1050-1054)."""
+    pos, idx = scenes.heightfield(8, 1.0, relief, seed=3)
+    m = _lib.build_triangle_mesh(pos, idx, -1.0, cos)
+    o = pyoracle.OracleWorld(world.standard_settings(), ccd_mesh_scene(shape, relief), (), [m])
+    hits = 0
+    for _ in range(4):
+        o.step(1 / 60, 1)
+        hits += o.ccd_counts()[1]
+    y = o.state()[1, 1]
+    if caught:
+        assert hits >= 1 and y > -relief / 2 - 0.3, y
+    else:
+        assert hits == 0 and y < -1.0, y
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape,relief,cos,caught", CCD_MESH_CASES)
+def test_ccd_against_mesh_parity(gpu_lib, oracle_lib, shape, relief, cos, caught):
+    pos, idx = scenes.heightfield(8, 1.0, relief, seed=3)
+    ws = world.standard_settings()
+    g = world.GpuWorld(ws, 8)
+    g.add_triangle_mesh(pos, idx, -1.0, cos)
+    b = ccd_mesh_scene(shape, relief)
+    g.add_bodies(b)
+    o = pyoracle.OracleWorld(ws, b, (), [g.get_triangle_mesh(0)])
+    for k in range(4):
+        g.step(1 / 60, 1)
+        o.step(1 / 60, 1)
+        s = g.stats()
+        assert (s["num_ccd"], s["num_ccd_hits"]) == o.ccd_counts(), k
+        rows, _ = g.get_state()
+        np.testing.assert_allclose(rows[1, 0:3], o.state()[1, 0:3], atol=5e-3, err_msg=f"step {k}")
