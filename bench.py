@@ -422,6 +422,57 @@ def ragdoll_measurement(cpu_seconds: float = 8.0):
                              "gpu_same_phase_value": sc.n / (gpu_first * 1e-3)}}
 
 
+def terrain_rays(n: int, half: float, seed: int = 3) -> np.ndarray:
+    """Rays from 20-50 m above the terrain, pointing down at random (y component at most -0.5 before
+    normalising), 100 m long: a cc_ray array."""
+    from crashcat_gb300 import _lib
+    rng = np.random.default_rng(seed)
+    r = np.zeros(n, _lib.RAY_DTYPE)
+    r["origin"] = np.stack([rng.uniform(-half, half, n), rng.uniform(20.0, 50.0, n), rng.uniform(-half, half, n)], 1)
+    d = rng.normal(size=(n, 3))
+    d[:, 1] = -np.abs(d[:, 1]) - 0.5
+    r["direction"] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    r["length"] = 100.0
+    return r
+
+
+def ray_query_measurement(g, rays, reps: int = 10):
+    """Closest-hit castRay of every ray against the world (cc_world_cast_rays_device on resident
+    buffers: the query tree of the current poses, then one thread per ray), and the same through
+    cc_world_cast_rays with host arrays (copies in and out inside the timed region)."""
+    import ctypes as C
+    import torch
+    from crashcat_gb300 import _lib
+    n = len(rays)
+    d_rays = torch.from_numpy(rays.view(np.uint8).copy()).cuda()
+    d_hits = torch.empty(n * _lib.RAY_HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    f = _lib.QueryFilter(0xFFFFFFFF, 0xFFFFFFFF, 0xFFFFFFFF, _lib.CAST_RAY_TREAT_CONVEX_AS_SOLID)
+
+    def call():
+        _lib.check(g._lib.cc_world_cast_rays_device(g.handle, d_rays.data_ptr(), n, C.byref(f), d_hits.data_ptr()),
+                   "cc_world_cast_rays_device")
+
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        call()
+    torch.cuda.synchronize()
+    dev_s = (time.perf_counter() - t0) / reps
+    hits = d_hits.cpu().numpy().view(_lib.RAY_HIT_DTYPE)
+    g.cast_rays(rays[:1024])
+    t0 = time.perf_counter()
+    for _ in range(3):
+        h2 = g.cast_rays(rays)
+    e2e_s = (time.perf_counter() - t0) / 3
+    return {"rays": n, "value": n / dev_s, "unit": "rays/s", "ms_per_batch": dev_s * 1e3,
+            "e2e": {"value": n / e2e_s, "unit": "rays/s", "h2d_bytes_per_step": int(rays.nbytes),
+                    "d2h_bytes_per_step": int(h2.nbytes)},
+            "hit_fraction": float((hits["body"] >= 0).mean()), "terrain_hits": float((hits["body"] == 0).mean()),
+            "device_equals_host_api": bool((h2["body"] == hits["body"]).all()), "_bodies": hits["body"].copy()}
+
+
 def terrain_measurement(cpu_seconds: float = 8.0):
     """The mixed-shape terrain workload: 20,000 bodies (spheres, boxes, capsules and convex hulls
     of 16-32 points in the mixed pile's size ranges) dropped from 5-40 m over a 256 x 256-cell
@@ -450,8 +501,22 @@ def terrain_measurement(cpu_seconds: float = 8.0):
     rows, _ = g.get_state()
     hulls = [g.get_convex_hull(i) for i in range(len(sc.hull_points))]
     mesh = g.get_triangle_mesh(0)
+    rays = terrain_rays(1 << 20, 0.4 * 256)
+    queries = ray_query_measurement(g, rays)
     del g
     obuild.build()
+    o = pyoracle.OracleWorld(ws, sc.bodies, hulls, [mesh])
+    # the oracle's closest-hit ray cast on a sample of the same rays, from the settled poses
+    st = o.state()
+    st[:, 0:13] = rows[:, 0:13]
+    o.set_state(st)
+    sample = np.stack([np.concatenate([r["origin"], r["direction"], [r["length"]]]) for r in rays[:2000]])
+    t0 = time.perf_counter()
+    ofr, obo, _ = o.cast_rays(sample)
+    ray_cpu_s = time.perf_counter() - t0
+    queries["cpu_baseline"] = {"value": len(sample) / ray_cpu_s, "unit": "rays/s", "cores": 1, "kind": "port",
+                               "sample": "first 2,000 of the rays, brute force over the bodies"}
+    queries["sample_same_body"] = float((queries.pop("_bodies")[:len(sample)] == obo).mean())
     o = pyoracle.OracleWorld(ws, sc.bodies, hulls, [mesh])
     t0, k = time.perf_counter(), 0
     while time.perf_counter() - t0 < cpu_seconds and k < 100:
@@ -464,6 +529,7 @@ def terrain_measurement(cpu_seconds: float = 8.0):
             "ms_per_step": total_ms / 300, "phases": phases, "status": int(status),
             "finite": bool(np.isfinite(rows).all()),
             "below_terrain": int((rows[1:, 1] < -2.5).sum()),
+            "ray_queries": queries,
             "cpu_baseline": {"value": (sc.n - 1) * k / cpu_s, "unit": METRIC, "cores": 1, "kind": "port",
                              "sample": f"first {k} steps from spawn (falling phase)",
                              "gpu_same_phase_value": (sc.n - 1) / (phases[0]["ms_per_step"] * 1e-3)}}

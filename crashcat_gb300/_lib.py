@@ -75,6 +75,21 @@ class HullInfo(C.Structure):
                 ("bounds_max", C.c_float * 3)]
 
 
+CAST_RAY_TREAT_CONVEX_AS_SOLID = 1
+CAST_RAY_COLLIDE_WITH_BACKFACES = 2
+
+# cc_ray: origin xyz, length, unit direction xyz, world; cc_ray_hit: body, fraction, sub-shape id
+RAY_DTYPE = np.dtype([("origin", np.float32, 3), ("length", np.float32), ("direction", np.float32, 3),
+                      ("world", np.int32)])
+RAY_HIT_DTYPE = np.dtype([("body", np.int32), ("fraction", np.float32), ("sub_shape_id", np.uint32),
+                          ("reserved", np.int32)])
+
+
+class QueryFilter(C.Structure):
+    _fields_ = [("object_layer_mask", C.c_uint32), ("collision_group", C.c_uint32),
+                ("collision_mask", C.c_uint32), ("flags", C.c_int32)]
+
+
 class MeshInfo(C.Structure):
     _fields_ = [("num_vertices", C.c_int32), ("num_triangles", C.c_int32), ("num_nodes", C.c_int32),
                 ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3)]
@@ -130,6 +145,8 @@ EXPORTS = {
     "cc_world_get_triangle_mesh": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_void_p], C.c_int),
     "cc_world_get_manifold_sub_shapes": ([C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
+    "cc_world_cast_rays": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
+    "cc_world_cast_rays_device": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
     "cc_world_add_convex_hull": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.POINTER(C.c_int32)], C.c_int),
     "cc_world_get_convex_hull": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),

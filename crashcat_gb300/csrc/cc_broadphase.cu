@@ -510,4 +510,18 @@ void launch_broadphase(DevWorld &w, cudaStream_t s) {
     k_find_pairs<<<grid_for(n, 128, 16), 128, 0, s>>>(w, w.node_world);
 }
 
+// the broadphase without its pair search: current boxes, Morton order and tree
+void launch_query_tree(DevWorld &w, cudaStream_t s) {
+    int n = w.n;
+    if (n == 0) return;
+    k_reset_scene<<<1, 32, 0, s>>>(w.scene);
+    k_update_bounds<<<grid_for(n, 256), 256, 0, s>>>(w, w.scene);
+    k_morton<<<grid_for(n, 256), 256, 0, s>>>(w, w.scene);
+    int wbits = 0;
+    while ((1 << wbits) < w.num_worlds) wbits++;
+    radix_sort_pairs_u64(w.morton, w.morton_alt, w.order, w.order_alt, n, 30 + wbits, w.scan_tmp, s);
+    if (n > 1) k_lbvh_build<<<grid_for(n - 1, 256), 256, 0, s>>>(w, w.node_world);
+    k_lbvh_refit<<<grid_for(n, 256), 256, 0, s>>>(w, w.node_world, nullptr);
+}
+
 }  // namespace cc

@@ -593,6 +593,30 @@ void launch_solver(DevWorld &w, float dt, float warm_ratio, cudaStream_t s, cuda
 void launch_ccd(DevWorld &w, float dt, cudaStream_t s);
 void launch_ccd_bounds(DevWorld &w, float dt, cudaStream_t s);
 void launch_ccd_find(DevWorld &w, float dt, cudaStream_t s);
+
+// world ray queries: a ray is origin, length, unit direction and the world it is cast in; its hit
+// is the body (-1 on a miss), the fraction of the length and the sub-shape id
+struct DevRay {
+    float origin[3];
+    float length;
+    float direction[3];
+    int world;
+};
+struct DevRayHit {
+    int body;
+    float fraction;
+    uint32_t sub_shape_id;
+    int pad;
+};
+enum : int { CC_RAY_SOLID = 1, CC_RAY_BACKFACES = 2 };  // treatConvexAsSolid, collideWithBackfaces
+struct DevRayFilter {
+    uint32_t layer_mask, groups, mask;
+    int flags;
+};
+// the boxes and the tree of the current poses, for queries between steps
+void launch_query_tree(DevWorld &w, cudaStream_t s);
+void launch_cast_rays(DevWorld &w, const DevRay *rays, int nr, const DevRayFilter &f, DevRayHit *hits,
+                      cudaStream_t s);
 int giant_blocks_for_device();
 void launch_update_bounds(DevWorld &w, cudaStream_t s);
 void upload_settings(const DevSettings &s, double spec64, cudaStream_t st);

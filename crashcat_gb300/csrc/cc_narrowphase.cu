@@ -2884,6 +2884,248 @@ void launch_ccd_find(DevWorld &w, float dt, cudaStream_t s) {
     k_ccd_find<<<grid_for(w.n, 128, 16), 128, 0, s>>>(w, w.node_world, dt);
 }
 
+// ---------------------------------------------------------------------------
+// world queries: castRay (query.ts:78-90) with the closest-hit collector
+// (ClosestCastRayCollector cast-ray-vs-shape.ts:180-205), one thread per ray
+// ---------------------------------------------------------------------------
+// gjkCastRay gjk.ts:622-790: origin + lambda * dir against a support in its own frame; false
+// when the ray misses before maxLambda
+template <typename S, class SA>
+__device__ bool gjk_cast_ray(S &lambda_out, V<S> origin, V<S> dir, S tol, const SA &A, S maxLambda) {
+    const S sqtol = tol * tol;
+    Simplex<S> sx;
+    sx.size = 0;
+    S lambda = S(0);
+    V<S> x = origin;
+    V<S> p = A.get(V<S>{S(0), S(0), S(0)});
+    V<S> v = x - p;
+    S vls = s_max_value<S>();
+    bool allow_restart = false;
+    for (int it = 0; it < 100; it++) {
+        p = A.get(v);
+        const V<S> wv = x - p;
+        const S vdw = dot(v, wv);
+        if (vdw > S(0)) {
+            const S vdr = dot(v, dir);
+            if (vdr >= S(-1.0e-18)) return false;
+            const S old = lambda;
+            lambda -= vdw / vdr;
+            if (old == lambda) break;
+            if (lambda >= maxLambda) return false;
+            x = origin + dir * lambda;
+            vls = s_max_value<S>();
+            allow_restart = true;
+        }
+        sx.pts[sx.size].p = p;
+        sx.size++;
+        for (int i = 0; i < sx.size; i++) sx.pts[i].y = x - sx.pts[i].p;
+        CP<S> cp;
+        switch (sx.size) {
+            case 1:
+                cp = {sx.pts[0].y, 1};
+                break;
+            case 2:
+                cp = closest_line(sx.pts[0].y, sx.pts[1].y, S(1e-10));
+                break;
+            case 3:
+                cp = closest_tri(sx.pts[0].y, sx.pts[1].y, sx.pts[2].y, false, S(1e-10));
+                break;
+            default:
+                cp = closest_tetra(sx.pts[0].y, sx.pts[1].y, sx.pts[2].y, sx.pts[3].y, false, S(1e-5));
+                break;
+        }
+        const S nd = lsq(cp.p);
+        if (nd < vls) {
+            vls = nd;
+            v = cp.p;
+        } else {
+            if (!allow_restart) break;
+            allow_restart = false;
+            sx.pts[0].p = p;
+            sx.size = 1;
+            v = x - p;
+            vls = s_max_value<S>();
+            continue;
+        }
+        if (cp.set == 0xf) break;
+        int ns = 0;
+        for (int i = 0; i < sx.size; i++)
+            if (cp.set & (1 << i)) {
+                if (ns != i) sx.pts[ns].p = sx.pts[i].p;
+                ns++;
+            }
+        sx.size = ns;
+        if (vls <= sqtol) break;
+    }
+    lambda_out = lambda;
+    return true;
+}
+
+// raycast3.intersectsTriangle of mathcat 0.0.10 (not vendored), taken as the Moller-Trumbore test
+// over t in [0, len] along the ray direction with back faces culled when asked; the hit's fraction
+// is t / len
+__device__ __forceinline__ bool ray_triangle(float3 o, float3 d, float len, float3 a, float3 b, float3 c,
+                                             bool cull_back, float &fraction) {
+    const float3 e1 = b - a, e2 = c - a;
+    const float3 pv = cross3(d, e2);
+    const float det = dot3(e1, pv);
+    if (cull_back ? det < 1e-10f : fabsf(det) < 1e-10f) return false;
+    const float inv = 1.f / det;
+    const float3 tv = o - a;
+    const float u = dot3(tv, pv) * inv;
+    if (u < 0.f || u > 1.f) return false;
+    const float3 qv = cross3(tv, e1);
+    const float v = dot3(d, qv) * inv;
+    if (v < 0.f || u + v > 1.f) return false;
+    const float t = dot3(e2, qv) * inv;
+    if (t < 0.f || t > len) return false;
+    fraction = t / len;
+    return true;
+}
+
+// castRayVsTriangleMesh triangle-mesh.ts:259-430: the closest triangle below max_f of the mesh of
+// body b, the ray in the mesh's frame; nearer child first, subtrees beyond the best hit skipped
+__device__ bool ray_vs_mesh(const DevWorld &w, int b, float3 o, float3 d, float len, bool cull_back, float max_f,
+                            float &fraction, uint32_t &sub) {
+    const DevMesh &M = w.meshes[mesh_of(w.shape[b])];
+    if (M.num_tris == 0) return false;
+    const float4 *nodes = w.mesh_nodes + 2 * M.first_node;
+    int stack[MESH_STACK];
+    float sdist[MESH_STACK];
+    int sp = 0;
+    stack[sp] = 0;
+    sdist[sp++] = -CUDART_INF_F;
+    float best = max_f;
+    bool found = false;
+    while (sp > 0) {
+        if (best <= 0.f) break;
+        --sp;
+        const int node = stack[sp];
+        if (sdist[sp] >= best) continue;
+        const float4 nlo = nodes[2 * node], nhi = nodes[2 * node + 1];
+        const int aux = __float_as_int(nlo.w), tag = __float_as_int(nhi.w);
+        if (tag < 0) {
+            for (int ti = aux; ti < aux + (-tag - 1); ti++) {
+                const int4 tr = w.mesh_tris[M.first_tri + ti];
+                float f;
+                if (ray_triangle(o, d, len, xyz(w.mesh_verts[tr.x]), xyz(w.mesh_verts[tr.y]), xyz(w.mesh_verts[tr.z]),
+                                 cull_back, f) &&
+                    f < best) {
+                    best = f;
+                    found = true;
+                    sub = M.sub_bits >= 32 ? (uint32_t)ti : ((0xffffffffu & ~((1u << M.sub_bits) - 1u)) | (uint32_t)ti);
+                }
+            }
+            continue;
+        }
+        const int left = node + 1, right = aux;
+        const float ld = ray_fraction_to_box(o, d, len, xyz(nodes[2 * left]), xyz(nodes[2 * left + 1]));
+        const float rd = ray_fraction_to_box(o, d, len, xyz(nodes[2 * right]), xyz(nodes[2 * right + 1]));
+        if (sp + 2 > MESH_STACK) {
+            atomicOr(&w.ctr->overflow, OVF_SLOTS);
+            continue;
+        }
+        if (ld <= rd) {
+            if (rd < best) { stack[sp] = right; sdist[sp++] = rd; }
+            if (ld < best) { stack[sp] = left; sdist[sp++] = ld; }
+        } else {
+            if (ld < best) { stack[sp] = left; sdist[sp++] = ld; }
+            if (rd < best) { stack[sp] = right; sdist[sp++] = rd; }
+        }
+    }
+    if (found) fraction = best;
+    return found;
+}
+
+// castRayVsShape for one body (castRayVsConvex convex.ts:54-126 with the INCLUDE_CONVEX_RADIUS
+// support and tolerance 1e-3, or the mesh walk): the hit below max_f and its sub-shape id
+__device__ bool ray_vs_body(const DevWorld &w, const HullView &hv, int b, float3 o, float3 d, float len,
+                            uint32_t flags, float max_f, float &fraction, uint32_t &sub) {
+    const uint32_t fb = w.flags[b];
+    const float3 pB = xyz(w.pos[b]);
+    const float4 qB = w.quat[b];
+    const float3 lo = qrot_inv(qB, o - pB), ld = qrot_inv(qB, d);
+    if (shape_of(fb) == SHAPE_MESH)
+        return ray_vs_mesh(w, b, lo, ld, len, !(flags & CC_RAY_BACKFACES), max_f, fraction, sub);
+    const Sup<float> sup = make_sup<float>(shape_of(fb), w.shape[b], false, hv);
+    float lambda;
+    if (!gjk_cast_ray(lambda, V<float>{lo.x, lo.y, lo.z}, V<float>{ld.x * len, ld.y * len, ld.z * len}, 1e-3f, sup,
+                      max_f))
+        return false;
+    if (!((flags & CC_RAY_SOLID) || lambda > 0.f)) return false;
+    fraction = fmaxf(0.f, lambda);
+    sub = 0xffffffffu;
+    return true;
+}
+
+// broadphase.castRay / dbvt.castRay (broadphase.ts:280-298, dbvt.ts:779-865) over the world's
+// subtree of the device tree: every body whose box the segment enters and that passes the filter
+// is cast; the least fraction wins, ties to the lower body index.
+__global__ void __launch_bounds__(128) k_cast_rays(DevWorld w, const int2 *node_world, const DevRay *rays, int nr,
+                                                   DevRayFilter flt, DevRayHit *hits) {
+    const int n = w.n;
+    const HullView hv = hull_view(w);
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nr; r += gridDim.x * blockDim.x) {
+        const DevRay ry = rays[r];
+        const float3 o = f3(ry.origin[0], ry.origin[1], ry.origin[2]);
+        const float3 d = f3(ry.direction[0], ry.direction[1], ry.direction[2]);
+        const float len = ry.length;
+        const int wr = ry.world;
+        float best = 1.f + 1e-4f;  // INITIAL_EARLY_OUT_FRACTION cast-utils.ts:3
+        int hit = -1;
+        uint32_t hsub = 0xffffffffu;
+        if (n > 0 && wr >= 0 && wr < w.num_worlds && len > 0.f) {
+            int stack[CCD_STACK];
+            int sp = 0;
+            stack[sp++] = 0;
+            while (sp > 0) {
+                const int node = stack[--sp];
+                const int2 nw = node_world[node];
+                if (wr < nw.x || wr > nw.y) continue;
+                if (!(ray_box_entry(o, d, len, xyz(w.node_lo[node]), xyz(w.node_hi[node])) < CUDART_INF_F)) continue;
+                if (node < n - 1) {
+                    const int2 ch = w.node_child[node];
+                    if (sp + 2 <= CCD_STACK) {
+                        stack[sp++] = ch.y;
+                        stack[sp++] = ch.x;
+                    } else {
+                        atomicOr(&w.ctr->overflow, OVF_SLOTS);
+                    }
+                    continue;
+                }
+                const int b = w.order[node - (n - 1)];
+                if (w.world[b] != wr) continue;
+                const uint32_t fb = w.flags[b];
+                if (!(flt.layer_mask & (1u << layer_of(fb)))) continue;
+                const uint2 gb = w.groups[b];
+                if (!((flt.groups & gb.y) != 0u && (gb.x & flt.mask) != 0u)) continue;
+                // a later-found body of lower index may still take an equal fraction
+                const float max_f = (hit >= 0 && b < hit) ? nextafterf(best, CUDART_INF_F) : best;
+                float f;
+                uint32_t sub;
+                if (!ray_vs_body(w, hv, b, o, d, len, flt.flags, max_f, f, sub)) continue;
+                if (f < best || (f == best && b < hit)) {
+                    best = f;
+                    hit = b;
+                    hsub = sub;
+                }
+            }
+        }
+        DevRayHit h;
+        h.body = hit;
+        h.fraction = hit >= 0 ? best : 1.f;
+        h.sub_shape_id = hsub;
+        h.pad = 0;
+        hits[r] = h;
+    }
+}
+
+void launch_cast_rays(DevWorld &w, const DevRay *rays, int nr, const DevRayFilter &f, DevRayHit *hits,
+                      cudaStream_t s) {
+    if (nr <= 0) return;
+    k_cast_rays<<<grid_for(nr, 128, 16), 128, 0, s>>>(w, w.node_world, rays, nr, f, hits);
+}
+
 void launch_mesh_narrowphase(DevWorld &w, int pass, cudaStream_t s);
 
 void launch_narrowphase(DevWorld &w, float, cudaStream_t s, cudaEvent_t mid) {

@@ -39,6 +39,9 @@ struct cc_world {
     std::vector<cc_hull::Hull> hulls;  // convex hull shapes as built
     std::vector<cc_mesh::Mesh> meshes;  // triangle meshes as built
     bool hulls_dirty = false, meshes_dirty = false;  // added since the last upload
+    DevRay *q_rays = nullptr;  // ray query staging (cc_world_cast_rays), grown on demand
+    DevRayHit *q_hits = nullptr;
+    int q_cap = 0;
     float *d_state_rows = nullptr;  // 16 floats per body staging for get/set state
     float *h_pinned_rows = nullptr;
     DevCounters *h_ctr = nullptr;   // pinned mirror of the device counters
@@ -516,6 +519,8 @@ int cc_world_destroy(cc_world *W) {
                     w.mesh_epa_count};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    if (W->q_rays) cudaFree(W->q_rays);
+    if (W->q_hits) cudaFree(W->q_hits);
     for (void *p : W->adj.allocs)
         if (p) cudaFree(p);
     if (W->h_ctr) cudaFreeHost(W->h_ctr);
@@ -967,6 +972,45 @@ int cc_world_get_manifold_sub_shapes(cc_world *W, uint32_t *out, int32_t capacit
         k++;
     }
     *count = k;
+    return CC_OK;
+}
+
+static_assert(sizeof(cc_ray) == sizeof(DevRay) && sizeof(cc_ray_hit) == sizeof(DevRayHit), "ray layouts");
+
+static int queue_cast_rays(cc_world *W, const DevRay *rays, int n, const cc_query_filter *f, DevRayHit *hits) {
+    if (int r = sync_shapes(W)) return r;
+    DevWorld &w = W->w;
+    DevRayFilter flt{f->object_layer_mask, f->collision_group, f->collision_mask, f->flags};
+    launch_query_tree(w, W->stream);
+    launch_cast_rays(w, rays, n, flt, hits, W->stream);
+    return cuda_ok(cudaGetLastError());
+}
+
+int cc_world_cast_rays_device(cc_world *W, const cc_ray *rays, int32_t count, const cc_query_filter *filter,
+                              cc_ray_hit *hits) {
+    if (!W || count < 0 || !filter || (count > 0 && (!rays || !hits))) return CC_ERR_INVALID;
+    if (count == 0) return CC_OK;
+    return queue_cast_rays(W, (const DevRay *)rays, count, filter, (DevRayHit *)hits);
+}
+
+int cc_world_cast_rays(cc_world *W, const cc_ray *rays, int32_t count, const cc_query_filter *filter,
+                       cc_ray_hit *hits) {
+    if (!W || count < 0 || !filter || (count > 0 && (!rays || !hits))) return CC_ERR_INVALID;
+    if (count == 0) return CC_OK;
+    if (count > W->q_cap) {
+        if (W->q_rays) cudaFree(W->q_rays);
+        if (W->q_hits) cudaFree(W->q_hits);
+        W->q_rays = nullptr;
+        W->q_hits = nullptr;
+        W->q_cap = 0;
+        CC_TRY(cudaMalloc(&W->q_rays, sizeof(DevRay) * (size_t)count));
+        CC_TRY(cudaMalloc(&W->q_hits, sizeof(DevRayHit) * (size_t)count));
+        W->q_cap = count;
+    }
+    CC_TRY(cudaMemcpyAsync(W->q_rays, rays, sizeof(DevRay) * (size_t)count, cudaMemcpyHostToDevice, W->stream));
+    if (int r = queue_cast_rays(W, W->q_rays, count, filter, W->q_hits)) return r;
+    CC_TRY(cudaMemcpyAsync(hits, W->q_hits, sizeof(DevRayHit) * (size_t)count, cudaMemcpyDeviceToHost, W->stream));
+    CC_TRY(cudaStreamSynchronize(W->stream));
     return CC_OK;
 }
 

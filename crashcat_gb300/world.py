@@ -388,6 +388,28 @@ class GpuWorld:
               "cc_world_get_manifold_sub_shapes")
         return out[:n.value]
 
+    # ---- world queries (query.ts) ----
+    def cast_rays(self, rays: np.ndarray, object_layer_mask: int = 0xFFFFFFFF, collision_group: int = 0xFFFFFFFF,
+                  collision_mask: int = 0xFFFFFFFF, treat_convex_as_solid: bool = True,
+                  collide_with_backfaces: bool = False) -> np.ndarray:
+        """cc_world_cast_rays: the closest hit of each ray (a _lib.RAY_DTYPE array, or rows of
+        origin xyz, unit direction xyz, length[, world]) as a _lib.RAY_HIT_DTYPE array."""
+        rays = np.asarray(rays)
+        if rays.dtype != _lib.RAY_DTYPE:
+            rows = np.asarray(rays, np.float64).reshape(len(rays), -1)
+            r = np.zeros(len(rows), _lib.RAY_DTYPE)
+            r["origin"], r["direction"], r["length"] = rows[:, 0:3], rows[:, 3:6], rows[:, 6]
+            r["world"] = rows[:, 7].astype(np.int32) if rows.shape[1] > 7 else 0
+            rays = r
+        rays = np.ascontiguousarray(rays)
+        hits = np.zeros(len(rays), _lib.RAY_HIT_DTYPE)
+        flags = (_lib.CAST_RAY_TREAT_CONVEX_AS_SOLID if treat_convex_as_solid else 0) | (
+            _lib.CAST_RAY_COLLIDE_WITH_BACKFACES if collide_with_backfaces else 0)
+        f = _lib.QueryFilter(object_layer_mask, collision_group, collision_mask, flags)
+        check(self._lib.cc_world_cast_rays(self.handle, rays.ctypes.data, len(rays), C.byref(f), hits.ctypes.data),
+              "cc_world_cast_rays")
+        return hits
+
     # ---- hinge joints (hinge-constraint.ts) ----
     def add_hinges(self, hinges: np.ndarray) -> np.ndarray:
         """cc_world_add_hinges: records of _lib.HINGE_DTYPE; returns the joint indices."""

@@ -421,6 +421,62 @@ int cc_world_rollout_grad(cc_world *world, float dt, int32_t n_steps, int32_t ch
                           float *grad_friction);
 
 /* ---------------------------------------------------------------------------
+ * World ray queries: castRay (src/query.ts:78-90) with the closest-hit
+ * collector (createClosestCastRayCollector, src/collision/cast-ray-vs-shape.ts:
+ * 180-205), a batch of rays per call.
+ *
+ * Each ray is cast against the bodies of its world at their current poses
+ * (the boxes and tree are rebuilt from the poses before the rays are cast).
+ * A body is a candidate when the segment origin + t * direction, t in
+ * [0, length], enters its bounding box (dbvt.castRay, src/broadphase/
+ * dbvt.ts:779-865), its object layer bit is set in object_layer_mask
+ * (filterObjectLayer) and the groups pass (shouldPairCollide with the filter's
+ * collision_group and collision_mask).  Convex shapes are cast with gjkCastRay
+ * (castRayVsConvex, src/shapes/convex.ts:54-126); triangle meshes walk their
+ * BVH (castRayVsTriangleMesh, src/shapes/triangle-mesh.ts:259-430).
+ *
+ * hit.body is the body index (-1 on a miss), hit.fraction the fraction of the
+ * length (1 on a miss), hit.sub_shape_id the triangle's sub-shape id for a
+ * mesh, else 0xffffffff.  Equal fractions go to the lower body index.
+ * direction must be unit length (the reference normalises it, query.ts).
+ * flags: CC_CAST_RAY_TREAT_CONVEX_AS_SOLID (a ray starting inside a convex
+ * shape hits at fraction 0; the reference default) and
+ * CC_CAST_RAY_COLLIDE_WITH_BACKFACES (mesh triangles seen from behind count).
+ *
+ *   cc_world_cast_rays: host arrays; returns when the hits are written.
+ *   cc_world_cast_rays_device: device arrays; queued on the world's stream.
+ * count < 0 or a NULL argument: CC_ERR_INVALID; count 0 does nothing.
+ * ------------------------------------------------------------------------- */
+#define CC_CAST_RAY_TREAT_CONVEX_AS_SOLID 1
+#define CC_CAST_RAY_COLLIDE_WITH_BACKFACES 2
+
+typedef struct cc_ray {
+    float origin[3];
+    float length;
+    float direction[3];  /* unit */
+    int32_t world;
+} cc_ray;
+
+typedef struct cc_ray_hit {
+    int32_t body;
+    float fraction;
+    uint32_t sub_shape_id;
+    int32_t reserved;
+} cc_ray_hit;
+
+typedef struct cc_query_filter {
+    uint32_t object_layer_mask;  /* bit per object layer */
+    uint32_t collision_group;
+    uint32_t collision_mask;
+    int32_t flags;               /* CC_CAST_RAY_* */
+} cc_query_filter;
+
+int cc_world_cast_rays(cc_world *world, const cc_ray *rays, int32_t count, const cc_query_filter *filter,
+                       cc_ray_hit *hits);
+int cc_world_cast_rays_device(cc_world *world, const cc_ray *rays, int32_t count, const cc_query_filter *filter,
+                              cc_ray_hit *hits);
+
+/* ---------------------------------------------------------------------------
  * Allocation-free penetration query.  No counterpart in the reference: it is
  * the narrowphase of one convex pair (collideConvexVsConvex,
  * src/shapes/convex.ts:257-346, with penetrationDepthStepGJK / EPA of

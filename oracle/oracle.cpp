@@ -2183,6 +2183,41 @@ void orc_ccd_counts(void *wp, int *out) {
     out[1] = ((World *)wp)->ccdHits;
 }
 
+// castRay query.ts:78-90 with the closest-hit collector (cast-ray-vs-shape.ts:180-205): each ray
+// (origin xyz, direction xyz unit, length) against every body whose current AABB the segment
+// enters (dbvt.castRay dbvt.ts:779-865) and that passes the filter (object layer bit in
+// layerMask, collision group/mask); hit = (body index, fraction, sub-shape id) or body -1.
+// Ties in fraction go to the lower body index.
+void orc_cast_rays(void *wp, const double *rays, int n, uint32_t layerMask, uint32_t groups, uint32_t mask,
+                   int treatConvexAsSolid, double *fractions, int *bodies, uint32_t *subs) {
+    World &W = *(World *)wp;
+    for (auto &b : W.bodies) update_aabb(b);
+    for (int r = 0; r < n; r++) {
+        const double *ry = rays + 7 * r;
+        V3 o{ry[0], ry[1], ry[2]}, d{ry[3], ry[4], ry[5]};
+        double len = ry[6];
+        double best = 1.0 + 1e-4;  // INITIAL_EARLY_OUT_FRACTION cast-utils.ts:3
+        int hit = -1;
+        uint32_t hsub = EMPTY_SUB_SHAPE_ID;
+        for (auto &b : W.bodies) {
+            if (!((groups & b.mask) != 0 && (b.groups & mask) != 0)) continue;
+            if (!(layerMask & (1u << b.objectLayer))) continue;
+            if (!(ray_fraction_to_box(o, d, len, b.aabb) < std::numeric_limits<double>::infinity())) continue;
+            double f;
+            uint32_t sub;
+            if (!cast_ray_vs_shape(b.shape, b.position, b.quat, o, d, len, treatConvexAsSolid != 0, best, f, sub)) continue;
+            if (f < best || (f == best && hit >= 0 && b.index < hit)) {
+                best = f;
+                hit = b.index;
+                hsub = sub;
+            }
+        }
+        fractions[r] = hit >= 0 ? best : 1.0;
+        bodies[r] = hit;
+        subs[r] = hsub;
+    }
+}
+
 // ---- unit-level entry points for the known-answer tests -------------------
 // Faces are passed as n vertices (xyz doubles).  Returns the output vertex count.
 int orc_clip_poly_vs_plane(const double *poly, int n, const double *origin, const double *normal, double *out) {

@@ -2226,6 +2226,145 @@ inline void cast_sphere_vs_mesh(const Shape &sa, V3 pA, V3 disp, const Shape &sb
     });
 }
 
+// ----------------------------------------------------------------------------
+// Ray casts (query.ts:78-90, convex.ts:54-126, gjk.ts:622-790, triangle-mesh.ts castRay)
+// ----------------------------------------------------------------------------
+// gjkCastRay gjk.ts:622-790: the ray origin + lambda * dir against a support in its own frame;
+// false when the ray misses before maxLambda
+inline bool gjk_cast_ray(double &lambdaOut, V3 origin, V3 dir, double tol, const Support &S, double maxLambda) {
+    const double sqtol = tol * tol;
+    Simplex sx;
+    double lambda = 0.0;
+    V3 x = origin;
+    V3 p = S.get({0, 0, 0});
+    V3 v = sub(x, p);
+    double vls = std::numeric_limits<double>::max();
+    bool allowRestart = false;
+    for (int it = 0; it < GJK_MAX_ITERATIONS; it++) {
+        p = S.get(v);
+        V3 w = sub(x, p);
+        double vdw = dot(v, w);
+        if (vdw > 0.0) {
+            double vdr = dot(v, dir);
+            if (vdr >= -1.0e-18) return false;
+            double old = lambda;
+            lambda -= vdw / vdr;
+            if (old == lambda) break;
+            if (lambda >= maxLambda) return false;
+            x = scale_add(origin, dir, lambda);
+            vls = std::numeric_limits<double>::max();
+            allowRestart = true;
+        }
+        sx.pts[sx.size].p = p;
+        sx.size++;
+        for (int i = 0; i < sx.size; i++) sx.pts[i].y = sub(x, sx.pts[i].p);
+        ClosestToSimplex c;
+        if (closest_to_simplex(c, vls, false, sx)) {
+            vls = c.sqdist;
+            v = c.point;
+        } else {
+            if (!allowRestart) break;
+            allowRestart = false;
+            sx.pts[0].p = p;
+            sx.size = 1;
+            v = sub(x, p);
+            vls = std::numeric_limits<double>::max();
+            continue;
+        }
+        if (c.set == 0xf) break;
+        int ns = 0;
+        for (int i = 0; i < sx.size; i++)
+            if (c.set & (1 << i)) {
+                if (ns != i) sx.pts[ns].p = sx.pts[i].p;
+                ns++;
+            }
+        sx.size = ns;
+        if (vls <= sqtol) break;
+    }
+    lambdaOut = lambda;
+    return true;
+}
+
+// raycast3.intersectsTriangle of mathcat 0.0.10 (not vendored), taken as the Moller-Trumbore
+// test over t in [0, length] along the ray's direction, back faces culled when asked; the hit's
+// fraction is t / length
+inline bool ray_triangle(V3 o, V3 d, double length, V3 a, V3 b, V3 c, bool cullBack, double &fraction) {
+    const double EPS = 1e-10;
+    V3 e1 = sub(b, a), e2 = sub(c, a);
+    V3 pv = cross(d, e2);
+    double det = dot(e1, pv);
+    if (cullBack ? det < EPS : std::fabs(det) < EPS) return false;
+    double inv = 1.0 / det;
+    V3 tv = sub(o, a);
+    double u = dot(tv, pv) * inv;
+    if (u < 0 || u > 1) return false;
+    V3 qv = cross(tv, e1);
+    double v = dot(d, qv) * inv;
+    if (v < 0 || u + v > 1) return false;
+    double t = dot(e2, qv) * inv;
+    if (t < 0 || t > length) return false;
+    fraction = t / length;
+    return true;
+}
+
+// castRayVsShape for one body (castRayVsConvex convex.ts:54-126, castRayVsTriangleMesh
+// triangle-mesh.ts): the closest hit below maxFraction, its sub-shape id
+inline bool cast_ray_vs_shape(const Shape &s, V3 pos, Q4 q, V3 origin, V3 dir, double length, bool solid,
+                              double maxFraction, double &fraction, uint32_t &subId) {
+    Q4 iq = qconj(q);
+    V3 lo = rotate(iq, sub(origin, pos)), ld = rotate(iq, dir);
+    if (s.type == SHAPE_TRIANGLE_MESH) {
+        const MeshData &M = *s.mesh;
+        if (M.nodes.empty()) return false;
+        bool found = false;
+        double best = maxFraction;
+        std::vector<std::pair<int, double>> stack{{0, -std::numeric_limits<double>::infinity()}};
+        while (!stack.empty()) {
+            if (best <= 0) break;
+            auto [node, dist] = stack.back();
+            stack.pop_back();
+            if (dist >= best) continue;
+            const auto &nd = M.nodes[node];
+            if (nd[7] < 0) {
+                int start = (int)nd[6], count = (int)(-nd[7]) - 1;
+                for (int t = start; t < start + count; t++) {
+                    const auto &tr = M.tris[t];
+                    double f;
+                    if (ray_triangle(lo, ld, length, M.verts[tr[0]], M.verts[tr[1]], M.verts[tr[2]], true, f) &&
+                        f < best) {
+                        best = f;
+                        found = true;
+                        subId = mesh_sub_shape_id(M, t);
+                    }
+                }
+                continue;
+            }
+            int left = node + 1, right = (int)nd[6];
+            auto box = [&](int k) {
+                const auto &c = M.nodes[k];
+                return Box3{{c[0], c[1], c[2]}, {c[3], c[4], c[5]}};
+            };
+            double ldist = ray_fraction_to_box(lo, ld, length, box(left)), rdist = ray_fraction_to_box(lo, ld, length, box(right));
+            if (ldist <= rdist) {
+                if (rdist < best) stack.push_back({right, rdist});
+                if (ldist < best) stack.push_back({left, ldist});
+            } else {
+                if (ldist < best) stack.push_back({left, ldist});
+                if (rdist < best) stack.push_back({right, rdist});
+            }
+        }
+        if (found) fraction = best;
+        return found;
+    }
+    Support S = make_support(s, INCLUDE_CONVEX_RADIUS);
+    double lambda;
+    if (!gjk_cast_ray(lambda, lo, scale(ld, length), 1e-3, S, maxFraction)) return false;
+    if (!(solid || lambda > 0.0)) return false;
+    fraction = std::max(0.0, lambda);
+    subId = EMPTY_SUB_SHAPE_ID;
+    return true;
+}
+
 // the hits of a body pair in narrowphase order (collideShapeVsShape narrowphase.ts:172-238 with
 // the mesh registrations triangle-mesh.ts:223-237: a mesh as shape A runs the convex-vs-mesh
 // function reversed, collide-shape-vs-shape.ts:227-354)

@@ -48,6 +48,7 @@ def load():
         "orc_get_manifolds": ([vp, dp], i32),
         "orc_island_count": ([vp], i32),
         "orc_ccd_counts": ([vp, ip], None),
+        "orc_cast_rays": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, i32, dp, ip, vp], None),
         "orc_add_mesh": ([vp, i32, dp, i32, C.c_void_p, i32, dp], i32),
         "orc_get_manifold_subs": ([vp, C.c_void_p], i32),
         "orc_fix_normal": ([dp], i32),
@@ -231,6 +232,19 @@ class OracleWorld:
         o = np.zeros(2, dtype=np.int32)
         self.lib.orc_ccd_counts(self.h, iptr(o))
         return int(o[0]), int(o[1])
+
+    def cast_rays(self, rays: np.ndarray, layer_mask: int = 0xFFFFFFFF, groups: int = 0xFFFFFFFF,
+                  mask: int = 0xFFFFFFFF, treat_convex_as_solid: bool = True):
+        """Closest hit of each ray (origin xyz, unit direction xyz, length) over the world's
+        bodies: (fraction float64, body int32 (-1 on a miss), sub-shape id uint32)."""
+        rays = np.ascontiguousarray(rays, dtype=np.float64).reshape(-1, 7)
+        n = rays.shape[0]
+        fr = np.zeros(max(n, 1), dtype=np.float64)
+        bo = np.zeros(max(n, 1), dtype=np.int32)
+        su = np.zeros(max(n, 1), dtype=np.uint32)
+        self.lib.orc_cast_rays(self.h, dptr(rays), n, layer_mask, groups, mask, int(treat_convex_as_solid),
+                               dptr(fr), iptr(bo), su.ctypes.data)
+        return fr[:n], bo[:n], su[:n]
 
     def aabbs(self) -> np.ndarray:
         o = np.zeros((self.n, 6), dtype=np.float64)

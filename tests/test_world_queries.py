@@ -1,0 +1,272 @@
+"""World ray queries: castRay (src/query.ts:78-90) with the closest-hit collector
+(createClosestCastRayCollector, src/collision/cast-ray-vs-shape.ts:180-205).
+
+Known answers (CPU, the oracle): the cases of tst/query.test.ts (a unit box hit from -5 along +x
+at fraction 0.4 of 10, missed from 5 above), tst/collision/cast-ray-vs-shape.test.ts (a unit
+sphere 5 along +x hit at 4 of 1000; the ray offset by 0.1 still hits; single triangles hit from
+the front, missed from behind and when parallel; of two stacked triangles the nearer is kept) and
+tst/collision/cast-ray-treat-convex-as-solid.test.ts (a ray starting inside a sphere, box or
+capsule hits at fraction 0 when convex shapes are solid and not at all otherwise; from 3 m outside
+a unit sphere it hits at (3 - 1) / 10 = 0.2).  The reference asserts most of these as ranges; the
+exact values follow from the geometry and are asserted to the GJK tolerance (1e-3 m along the ray).
+
+mathcat's raycast3.intersectsTriangle is not vendored with the reference; both sides take it as
+the Moller-Trumbore test over [0, length] with back faces culled unless asked, so the triangle
+cases pin the mesh walk and the culling rule, not the library's own arithmetic.
+
+GPU tolerances (FP32 device, FP64 oracle, the same poses):
+  * the known answers: the same hit or miss, fraction within 2e-6 of length 1000 (1e-4 of 10);
+  * 4,096 random rays through a terrain with a mixed pile: the same body for at least 99 % of
+    rays (grazing rays and near-ties may go either way in FP32), fraction within 1e-4 where the
+    bodies agree, the same triangle sub-shape id for at least 99 % of mesh hits;
+  * filters and worlds: bit-exact selection (a layer or group that excludes a body never hits
+    it; a ray of world k only hits bodies of world k).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from crashcat_gb300 import _lib, scenes, world
+from oracle import pyoracle
+
+
+def ray(o, d, length):
+    d = np.asarray(d, np.float64)
+    d = d / np.linalg.norm(d)
+    return [*o, *d, length]
+
+
+def one_body(kind, pos=(0.0, 0.0, 0.0), **kw):
+    b = scenes.blank_bodies(1)
+    if kind == "sphere":
+        scenes.set_sphere(b, 0, kw.get("radius", 1.0))
+    elif kind == "box":
+        scenes.set_box(b, 0, kw.get("half", (1.0, 1.0, 1.0)))
+    elif kind == "capsule":
+        scenes.set_capsule(b, 0, kw.get("radius", 0.5), kw.get("half_height", 1.0))
+    b["position"][0] = pos
+    b["motion_type"][0] = _lib.STATIC
+    b["object_layer"][0] = scenes.LAYER_NOT_MOVING
+    return b
+
+
+def mesh_body():
+    b = scenes.blank_bodies(1)
+    b["shape_type"][0] = _lib.SHAPE_TRIANGLE_MESH
+    b["shape_params"][0] = 0.0
+    b["motion_type"][0] = _lib.STATIC
+    b["object_layer"][0] = scenes.LAYER_NOT_MOVING
+    return b
+
+
+# (name, body kind, body position, ray, solid, expected fraction or None for a miss)
+CONVEX_CASES = [
+    ("query_box_hit", "box", (0, 0, 0), ray((-5, 0, 0), (1, 0, 0), 10), True, 0.4),
+    ("query_box_miss_above", "box", (0, 0, 0), ray((-5, 5, 0), (1, 0, 0), 10), True, None),
+    ("sphere_from_outside", "sphere", (5, 0, 0), ray((0, 0, 0), (1, 0, 0), 1000), True, 0.004),
+    ("sphere_offset_ray", "sphere", (5, 0, 0), ray((0, -0.1, 0), (1, 0, 0), 1000), True,
+     (5 - math.sqrt(1 - 0.01)) / 1000),
+    ("sphere_example_case", "sphere", (2, 0.044676984915871, 0), ray((-3, 0, 0), (1, 0, 0), 10), True,
+     (5 - math.sqrt(1 - 0.044676984915871 ** 2)) / 10),
+    ("sphere_miss_side", "sphere", (5, 0, 0), ray((0, 2, 0), (1, 0, 0), 1000), True, None),
+    ("box_pointing_away", "box", (5, 0, 0), ray((0, 0, 0), (-1, 0, 0), 1000), True, None),
+    ("solid_sphere_inside", "sphere", (0, 0, 0), ray((0, 0, 0), (1, 0, 0), 10), True, 0.0),
+    ("hollow_sphere_inside", "sphere", (0, 0, 0), ray((0, 0, 0), (1, 0, 0), 10), False, None),
+    ("solid_sphere_outside", "sphere", (0, 0, 0), ray((-3, 0, 0), (1, 0, 0), 10), True, 0.2),
+    ("hollow_sphere_outside", "sphere", (0, 0, 0), ray((-3, 0, 0), (1, 0, 0), 10), False, 0.2),
+    ("solid_box_inside", "box", (0, 0, 0), ray((0, 0, 0), (1, 0, 0), 10), True, 0.0),
+    ("hollow_box_inside", "box", (0, 0, 0), ray((0, 0, 0), (1, 0, 0), 10), False, None),
+    ("solid_capsule_inside", "capsule", (0, 0, 0), ray((0, 0, 0), (1, 0, 0), 10), True, 0.0),
+    ("hollow_capsule_inside", "capsule", (0, 0, 0), ray((0, 0, 0), (1, 0, 0), 10), False, None),
+]
+
+TRI = [0, 0, 0, 1, 0, 0, 0, 1, 0]
+# (name, positions, indices, ray, expected fraction or None, the hit triangle's z)
+MESH_CASES = [
+    ("triangle_front", TRI, [0, 2, 1], ray((0.2, 0.2, -1), (0, 0, 1), 1000), 0.001, 0.0),
+    ("triangle_behind", TRI, [0, 1, 2], ray((0.2, 0.2, 1), (0, 0, 1), 1000), None, None),
+    ("triangle_parallel", TRI, [0, 1, 2], ray((0.2, 0.2, 1), (1, 0, 0), 1000), None, None),
+    ("two_triangles_nearest", TRI + [0, 0, 1, 1, 0, 1, 0, 1, 1], [0, 2, 1, 3, 5, 4],
+     ray((0.2, 0.2, -1), (0, 0, 1), 1000), 0.001, 0.0),
+    ("two_triangles_from_above", TRI + [0, 0, 1, 1, 0, 1, 0, 1, 1], [0, 1, 2, 3, 4, 5],
+     ray((0.2, 0.2, 3), (0, 0, -1), 1000), 0.002, 1.0),
+]
+
+
+def oracle_single(bodies, mesh=None):
+    return pyoracle.OracleWorld(world.standard_settings(), bodies, (), [mesh] if mesh is not None else ())
+
+
+@pytest.mark.parametrize("case", CONVEX_CASES, ids=[c[0] for c in CONVEX_CASES])
+def test_oracle_convex_known_answers(oracle_lib, case):
+    _, kind, pos, r, solid, want = case
+    o = oracle_single(one_body(kind, pos))
+    fr, bo, su = o.cast_rays(np.array([r]), treat_convex_as_solid=solid)
+    if want is None:
+        assert bo[0] == -1
+    else:
+        assert bo[0] == 0
+        assert abs(fr[0] - want) <= 1e-3 / r[6] + 1e-12, (fr[0], want)
+        assert su[0] == 0xFFFFFFFF
+
+
+def mesh_triangle_z(m, sub):
+    """z of the first vertex of the triangle a sub-shape id names (subShape.pushIndex
+    sub-shape.ts:60-64: the index in the low bits(triangle count - 1) bits, ones above)."""
+    bits = max(len(m["triangles"]) - 1, 0).bit_length()
+    tri = int(sub) & ((1 << bits) - 1)
+    assert (int(sub) | ((1 << bits) - 1)) == 0xFFFFFFFF
+    return float(m["vertices"][m["triangles"][tri, 0], 2])
+
+
+@pytest.mark.parametrize("case", MESH_CASES, ids=[c[0] for c in MESH_CASES])
+def test_oracle_mesh_known_answers(gpu_lib, oracle_lib, case):
+    _, p, idx, r, want, z = case
+    m = _lib.build_triangle_mesh(np.array(p, np.float64).reshape(-1, 3), np.array(idx, np.int64).reshape(-1, 3))
+    o = oracle_single(mesh_body(), m)
+    fr, bo, su = o.cast_rays(np.array([r]))
+    if want is None:
+        assert bo[0] == -1
+        return
+    assert bo[0] == 0
+    assert abs(fr[0] - want) < 1e-12
+    assert mesh_triangle_z(m, su[0]) == z
+
+
+def test_oracle_backfaces_culled(gpu_lib, oracle_lib):
+    """Back faces are culled by default (createDefaultCastRaySettings collideWithBackfaces false;
+    the mesh walk passes !collideWithBackfaces to intersectsTriangle, triangle-mesh.ts:366-373)."""
+    m = _lib.build_triangle_mesh(np.array(TRI, np.float64).reshape(-1, 3), np.array([[0, 1, 2]]))
+    o = oracle_single(mesh_body(), m)
+    r = np.array([ray((0.2, 0.2, 1), (0, 0, -1), 10)])
+    assert o.cast_rays(r)[1][0] == 0  # front face from +z: (1,0,0) x (0,1,0) points to +z
+    r = np.array([ray((0.2, 0.2, -1), (0, 0, 1), 10)])
+    assert o.cast_rays(r)[1][0] == -1
+
+
+def test_oracle_closest_body_and_filters(oracle_lib):
+    """Closest of several bodies along the ray; a body outside the filter is passed over."""
+    b = scenes.blank_bodies(3)
+    for i, x in enumerate((9.0, 3.0, 6.0)):
+        scenes.set_sphere(b, i, 0.5)
+        b["position"][i] = (x, 0, 0)
+        b["motion_type"][i] = _lib.STATIC
+        b["object_layer"][i] = scenes.LAYER_NOT_MOVING
+    b["collision_groups"][1] = 2
+    o = oracle_single(b)
+    r = np.array([ray((0, 0, 0), (1, 0, 0), 20)])
+    fr, bo, _ = o.cast_rays(r)
+    assert bo[0] == 1 and abs(fr[0] - 2.5 / 20) < 1e-4
+    fr, bo, _ = o.cast_rays(r, mask=~2 & 0xFFFFFFFF)
+    assert bo[0] == 2 and abs(fr[0] - 5.5 / 20) < 1e-4
+    fr, bo, _ = o.cast_rays(r, layer_mask=0)
+    assert bo[0] == -1
+
+
+# ---------------------------------------------------------------------------
+# GPU against the oracle
+# ---------------------------------------------------------------------------
+@pytest.mark.gpu
+def test_gpu_known_answers(gpu_lib, oracle_lib):
+    for _, kind, pos, r, solid, want in CONVEX_CASES:
+        g = world.GpuWorld(world.standard_settings(), 4)
+        g.add_bodies(one_body(kind, pos))
+        h = g.cast_rays(np.array([r]), treat_convex_as_solid=solid)
+        if want is None:
+            assert h["body"][0] == -1, (kind, r)
+        else:
+            assert h["body"][0] == 0, (kind, r)
+            assert abs(float(h["fraction"][0]) - want) <= 2e-3 / r[6] + 2e-6, (kind, r, h["fraction"][0], want)
+    for _, p, idx, r, want, z in MESH_CASES:
+        pos = np.array(p, np.float64).reshape(-1, 3)
+        ind = np.array(idx, np.int64).reshape(-1, 3)
+        g = world.GpuWorld(world.standard_settings(), 4)
+        g.add_triangle_mesh(pos, ind)
+        g.add_bodies(mesh_body())
+        h = g.cast_rays(np.array([r]))
+        if want is None:
+            assert h["body"][0] == -1
+            continue
+        assert h["body"][0] == 0
+        assert abs(float(h["fraction"][0]) - want) < 1e-6
+        assert mesh_triangle_z(g.get_triangle_mesh(0), h["sub_shape_id"][0]) == z
+    # collideWithBackfaces: the triangle seen from behind counts when asked
+    g = world.GpuWorld(world.standard_settings(), 4)
+    g.add_triangle_mesh(np.array(TRI, np.float64).reshape(-1, 3), np.array([[0, 1, 2]]))
+    g.add_bodies(mesh_body())
+    r = np.array([ray((0.2, 0.2, -1), (0, 0, 1), 10)])
+    assert g.cast_rays(r)["body"][0] == -1
+    h = g.cast_rays(r, collide_with_backfaces=True)
+    assert h["body"][0] == 0 and abs(float(h["fraction"][0]) - 0.1) < 1e-6
+
+
+def random_rays(rng, n, half, top):
+    o = np.stack([rng.uniform(-half, half, n), rng.uniform(top * 0.5, top, n), rng.uniform(-half, half, n)], 1)
+    d = rng.normal(size=(n, 3))
+    d[:, 1] = -np.abs(d[:, 1]) - 0.3
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return np.concatenate([o, d, rng.uniform(5.0, 30.0, (n, 1))], 1)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", [5, 6])
+def test_gpu_rays_through_terrain_pile(gpu_lib, oracle_lib, seed):
+    sc = scenes.mesh_drop(n=120, n_cells=16, seed=seed, heights=(0.0, 3.0))
+    ws = world.standard_settings()
+    g = world.GpuWorld(ws, sc.n + 16)
+    for p in sc.hull_points or ():
+        g.add_convex_hull(p)
+    g.add_triangle_mesh(*sc.mesh)
+    g.add_bodies(sc.bodies)
+    hulls = [g.get_convex_hull(i) for i in range(len(sc.hull_points or ()))]
+    o = pyoracle.OracleWorld(ws, sc.bodies, hulls, [g.get_triangle_mesh(0)])
+    g.step(sc.dt, 30)
+    rows, _ = g.get_state()
+    st = o.state()
+    st[:, 0:13] = rows[:, 0:13]
+    o.set_state(st)
+    rng = np.random.default_rng(seed)
+    rays = random_rays(rng, 4096, 7.0, 8.0)
+    h = g.cast_rays(rays)
+    fr, bo, su = o.cast_rays(rays)
+    same = h["body"] == bo
+    assert same.mean() >= 0.99, same.mean()
+    assert (bo >= 0).sum() > 2000  # most rays reach something
+    hit = same & (bo >= 0)
+    assert np.abs(h["fraction"][hit] - fr[hit]).max() < 1e-4
+    mesh = hit & (bo == 0)
+    assert mesh.sum() > 500
+    assert (h["sub_shape_id"][mesh] == su[mesh]).mean() >= 0.99
+    # a filter that leaves out the static layer never hits the terrain
+    h2 = g.cast_rays(rays, object_layer_mask=~(1 << scenes.LAYER_NOT_MOVING) & 0xFFFFFFFF)
+    assert not (h2["body"] == 0).any()
+    fr2, bo2, _ = o.cast_rays(rays, layer_mask=~(1 << scenes.LAYER_NOT_MOVING) & 0xFFFFFFFF)
+    assert (h2["body"] == bo2).mean() >= 0.99
+
+
+@pytest.mark.gpu
+def test_gpu_rays_stay_in_their_world(gpu_lib, oracle_lib):
+    """Worlds share the device tree; a ray only meets bodies of its own world.  Every world holds
+    the same spheres shifted by the world index along z, so a ray of world k hits body k * 4 + j."""
+    nw, per = 64, 4
+    b = scenes.blank_bodies(nw * per)
+    for k in range(nw):
+        for j in range(per):
+            i = k * per + j
+            scenes.set_sphere(b, i, 0.4)
+            b["position"][i] = (2.0 * j + 2.0, 0.0, 0.0)
+            b["motion_type"][i] = _lib.STATIC
+            b["object_layer"][i] = scenes.LAYER_NOT_MOVING
+            b["world"][i] = k
+    ws = world.standard_settings()
+    ws.num_worlds = nw
+    g = world.GpuWorld(ws, nw * per)
+    g.add_bodies(b)
+    rays = np.zeros((nw, 8))
+    rays[:, 3] = 1.0
+    rays[:, 6] = 20.0
+    rays[:, 7] = np.arange(nw)
+    h = g.cast_rays(rays)
+    np.testing.assert_array_equal(h["body"], np.arange(nw) * per)
+    np.testing.assert_allclose(h["fraction"], 1.6 / 20.0, atol=1e-4)
