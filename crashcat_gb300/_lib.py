@@ -84,6 +84,11 @@ RAY_DTYPE = np.dtype([("origin", np.float32, 3), ("length", np.float32), ("direc
 RAY_HIT_DTYPE = np.dtype([("body", np.int32), ("fraction", np.float32), ("sub_shape_id", np.uint32),
                           ("reserved", np.int32)])
 
+# cc_point: position xyz, world; cc_point_hit: count, lowest body hit, its sub-shape id
+POINT_DTYPE = np.dtype([("position", np.float32, 3), ("world", np.int32)])
+POINT_HIT_DTYPE = np.dtype([("count", np.int32), ("body", np.int32), ("sub_shape_id", np.uint32),
+                            ("reserved", np.int32)])
+
 
 class QueryFilter(C.Structure):
     _fields_ = [("object_layer_mask", C.c_uint32), ("collision_group", C.c_uint32),
@@ -145,6 +150,9 @@ EXPORTS = {
     "cc_world_get_triangle_mesh": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_void_p], C.c_int),
     "cc_world_get_manifold_sub_shapes": ([C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
+    "cc_world_collide_points": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_float, C.c_void_p], C.c_int),
+    "cc_world_collide_points_device": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_float, C.c_void_p],
+                                       C.c_int),
     "cc_world_cast_rays": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
     "cc_world_cast_rays_device": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
     "cc_world_add_convex_hull": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.POINTER(C.c_int32)], C.c_int),

@@ -617,6 +617,9 @@ struct DevRayFilter {
 void launch_query_tree(DevWorld &w, cudaStream_t s);
 void launch_cast_rays(DevWorld &w, const DevRay *rays, int nr, const DevRayFilter &f, DevRayHit *hits,
                       cudaStream_t s);
+// points: xyz and the world (int bits in w); out: hit count, lowest body hit (-1), its sub-shape id
+void launch_collide_points(DevWorld &w, const float4 *pts, int np, const DevRayFilter &f, float tol, int4 *out,
+                           cudaStream_t s);
 int giant_blocks_for_device();
 void launch_update_bounds(DevWorld &w, cudaStream_t s);
 void upload_settings(const DevSettings &s, double spec64, cudaStream_t st);

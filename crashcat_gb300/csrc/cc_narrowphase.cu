@@ -3120,6 +3120,160 @@ __global__ void __launch_bounds__(128) k_cast_rays(DevWorld w, const int2 *node_
     }
 }
 
+// ---------------------------------------------------------------------------
+// world queries: collidePoint (query.ts:470-490) with every hit collected
+// ---------------------------------------------------------------------------
+// the odd-even count of collidePointVsTriangleMesh triangle-mesh.ts:482-570: a +Y ray from the
+// point, 1.1 x the mesh height long, back faces counted, every hit kept (hitCountCollector
+// :441-467 never lowers its early-out fraction); last = the last hit's sub-shape id in walk order
+__device__ int mesh_ray_hit_count(const DevWorld &w, const DevMesh &M, float3 o, float len, uint32_t &last) {
+    const float early = 1.f + 1e-4f;
+    const float3 d = f3(0.f, 1.f, 0.f);
+    const float4 *nodes = w.mesh_nodes + 2 * M.first_node;
+    int stack[MESH_STACK];
+    float sdist[MESH_STACK];
+    int sp = 0, count = 0;
+    stack[sp] = 0;
+    sdist[sp++] = -CUDART_INF_F;
+    while (sp > 0) {
+        --sp;
+        const int node = stack[sp];
+        if (sdist[sp] >= early) continue;
+        const float4 nlo = nodes[2 * node], nhi = nodes[2 * node + 1];
+        const int aux = __float_as_int(nlo.w), tag = __float_as_int(nhi.w);
+        if (tag < 0) {
+            for (int ti = aux; ti < aux + (-tag - 1); ti++) {
+                const int4 tr = w.mesh_tris[M.first_tri + ti];
+                float f;
+                if (ray_triangle(o, d, len, xyz(w.mesh_verts[tr.x]), xyz(w.mesh_verts[tr.y]), xyz(w.mesh_verts[tr.z]),
+                                 false, f) &&
+                    f < early) {
+                    count++;
+                    last = M.sub_bits >= 32 ? (uint32_t)ti : ((0xffffffffu & ~((1u << M.sub_bits) - 1u)) | (uint32_t)ti);
+                }
+            }
+            continue;
+        }
+        const int left = node + 1, right = aux;
+        const float ld = ray_fraction_to_box(o, d, len, xyz(nodes[2 * left]), xyz(nodes[2 * left + 1]));
+        const float rd = ray_fraction_to_box(o, d, len, xyz(nodes[2 * right]), xyz(nodes[2 * right + 1]));
+        if (sp + 2 > MESH_STACK) {
+            atomicOr(&w.ctr->overflow, OVF_SLOTS);
+            continue;
+        }
+        if (ld <= rd) {
+            if (rd < early) { stack[sp] = right; sdist[sp++] = rd; }
+            if (ld < early) { stack[sp] = left; sdist[sp++] = ld; }
+        } else {
+            if (ld < early) { stack[sp] = left; sdist[sp++] = ld; }
+            if (rd < early) { stack[sp] = right; sdist[sp++] = rd; }
+        }
+    }
+    return count;
+}
+
+// collidePointVsShape for one body: sphere.ts:272-301 (distance), box.ts:370-410 (half extents),
+// convex.ts:142-216 (local bounds, then GJK of the INCLUDE_CONVEX_RADIUS support against the point
+// with the query's collision tolerance), triangle-mesh.ts:482-570 (local bounds, odd-even count)
+__device__ bool point_in_body(const DevWorld &w, const HullView &hv, int b, float3 p, float tol, uint32_t &sub) {
+    sub = 0xffffffffu;
+    const uint32_t fb = w.flags[b];
+    const float4 sp = w.shape[b];
+    const float3 l = p - xyz(w.pos[b]);
+    const int shape = shape_of(fb);
+    if (shape == SHAPE_SPHERE) return lensq3(l) <= sp.x * sp.x;
+    const float3 lp = qrot_inv(w.quat[b], l);
+    if (shape == SHAPE_BOX) return fabsf(lp.x) <= sp.x && fabsf(lp.y) <= sp.y && fabsf(lp.z) <= sp.z;
+    if (shape == SHAPE_MESH) {
+        const DevMesh &M = w.meshes[mesh_of(sp)];
+        if (M.num_tris == 0) return false;
+        if (lp.x < M.lo.x || lp.x > M.hi.x || lp.y < M.lo.y || lp.y > M.hi.y || lp.z < M.lo.z || lp.z > M.hi.z)
+            return false;
+        uint32_t last = 0xffffffffu;
+        if ((mesh_ray_hit_count(w, M, lp, (M.hi.y - M.lo.y) * 1.1f, last) & 1) == 0) return false;
+        sub = last;
+        return true;
+    }
+    float3 lo, hi;  // the shape's local bounds: capsule.ts computeCapsuleAABB, the hull's points
+    if (shape == SHAPE_HULL) {
+        const DevHull &h = hv.hulls[hull_of(sp)];
+        lo = xyz(h.lo);
+        hi = xyz(h.hi);
+    } else {
+        const float th = sp.y + sp.x;
+        lo = f3(-sp.x, -th, -sp.x);
+        hi = f3(sp.x, th, sp.x);
+    }
+    if (lp.x < lo.x || lp.x > hi.x || lp.y < lo.y || lp.y > hi.y || lp.z < lo.z || lp.z > hi.z) return false;
+    const Sup<float> A = make_sup<float>(shape, sp, false, hv);
+    Sup<float> P = make_sup<float>(SHAPE_SPHERE, make_float4(0.f, 0.f, 0.f, 0.f), true, hv);
+    set_transform(P, Q<float>{0.f, 0.f, 0.f, 1.f}, V<float>{lp.x, lp.y, lp.z});
+    V<float> dir{lp.x, lp.y, lp.z};
+    if (lsq(dir) < 1e-10f) dir = V<float>{0.f, 1.f, 0.f};
+    Simplex<float> sx;
+    sx.size = 0;
+    const GjkOut<float> g = gjk(A, P, tol, dir, 0.f, sx);
+    return g.sqdist <= tol * tol;
+}
+
+// broadphase.intersectPoint / dbvt.intersectPoint (broadphase.ts:314-324, dbvt.ts:683-740) over the
+// world's subtree: every body whose box holds the point and that passes the filter is tested;
+// the hit count, and the lowest body index among the hits with its sub-shape id
+__global__ void __launch_bounds__(128) k_collide_points(DevWorld w, const int2 *node_world, const float4 *pts, int np,
+                                                        DevRayFilter flt, float tol, int4 *out) {
+    const int n = w.n;
+    const HullView hv = hull_view(w);
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < np; r += gridDim.x * blockDim.x) {
+        const float4 q = pts[r];
+        const float3 p = xyz(q);
+        const int wr = __float_as_int(q.w);
+        int count = 0, first = -1;
+        uint32_t fsub = 0xffffffffu;
+        if (n > 0 && wr >= 0 && wr < w.num_worlds) {
+            int stack[CCD_STACK];
+            int sp = 0;
+            stack[sp++] = 0;
+            while (sp > 0) {
+                const int node = stack[--sp];
+                const int2 nw = node_world[node];
+                if (wr < nw.x || wr > nw.y) continue;
+                const float4 lo = w.node_lo[node], hi = w.node_hi[node];
+                if (p.x < lo.x || p.x > hi.x || p.y < lo.y || p.y > hi.y || p.z < lo.z || p.z > hi.z) continue;
+                if (node < n - 1) {
+                    const int2 ch = w.node_child[node];
+                    if (sp + 2 <= CCD_STACK) {
+                        stack[sp++] = ch.y;
+                        stack[sp++] = ch.x;
+                    } else {
+                        atomicOr(&w.ctr->overflow, OVF_SLOTS);
+                    }
+                    continue;
+                }
+                const int b = w.order[node - (n - 1)];
+                if (w.world[b] != wr) continue;
+                const uint32_t fb = w.flags[b];
+                if (!(flt.layer_mask & (1u << layer_of(fb)))) continue;
+                const uint2 gb = w.groups[b];
+                if (!((flt.groups & gb.y) != 0u && (gb.x & flt.mask) != 0u)) continue;
+                uint32_t sub;
+                if (!point_in_body(w, hv, b, p, tol, sub)) continue;
+                count++;
+                if (first < 0 || b < first) {
+                    first = b;
+                    fsub = sub;
+                }
+            }
+        }
+        out[r] = make_int4(count, first, (int)fsub, 0);
+    }
+}
+
+void launch_collide_points(DevWorld &w, const float4 *pts, int np, const DevRayFilter &f, float tol, int4 *out,
+                           cudaStream_t s) {
+    if (np <= 0) return;
+    k_collide_points<<<grid_for(np, 128, 16), 128, 0, s>>>(w, w.node_world, pts, np, f, tol, out);
+}
+
 void launch_cast_rays(DevWorld &w, const DevRay *rays, int nr, const DevRayFilter &f, DevRayHit *hits,
                       cudaStream_t s) {
     if (nr <= 0) return;

@@ -986,6 +986,41 @@ static int queue_cast_rays(cc_world *W, const DevRay *rays, int n, const cc_quer
     return cuda_ok(cudaGetLastError());
 }
 
+int cc_world_collide_points_device(cc_world *W, const cc_point *points, int32_t count, const cc_query_filter *filter,
+                                   float collision_tolerance, cc_point_hit *hits) {
+    if (!W || count < 0 || !filter || (count > 0 && (!points || !hits))) return CC_ERR_INVALID;
+    if (count == 0) return CC_OK;
+    if (int r = sync_shapes(W)) return r;
+    DevRayFilter flt{filter->object_layer_mask, filter->collision_group, filter->collision_mask, filter->flags};
+    launch_query_tree(W->w, W->stream);
+    launch_collide_points(W->w, (const float4 *)points, count, flt, collision_tolerance, (int4 *)hits, W->stream);
+    return cuda_ok(cudaGetLastError());
+}
+
+int cc_world_collide_points(cc_world *W, const cc_point *points, int32_t count, const cc_query_filter *filter,
+                            float collision_tolerance, cc_point_hit *hits) {
+    if (!W || count < 0 || !filter || (count > 0 && (!points || !hits))) return CC_ERR_INVALID;
+    if (count == 0) return CC_OK;
+    static_assert(sizeof(cc_point) == sizeof(DevRayHit) && sizeof(cc_point_hit) == sizeof(DevRayHit), "16 bytes");
+    if (count > W->q_cap) {
+        if (W->q_rays) cudaFree(W->q_rays);
+        if (W->q_hits) cudaFree(W->q_hits);
+        W->q_rays = nullptr;
+        W->q_hits = nullptr;
+        W->q_cap = 0;
+        CC_TRY(cudaMalloc(&W->q_rays, sizeof(DevRay) * (size_t)count));
+        CC_TRY(cudaMalloc(&W->q_hits, sizeof(DevRayHit) * (size_t)count));
+        W->q_cap = count;
+    }
+    CC_TRY(cudaMemcpyAsync(W->q_rays, points, sizeof(cc_point) * (size_t)count, cudaMemcpyHostToDevice, W->stream));
+    if (int r = cc_world_collide_points_device(W, (const cc_point *)W->q_rays, count, filter, collision_tolerance,
+                                               (cc_point_hit *)W->q_hits))
+        return r;
+    CC_TRY(cudaMemcpyAsync(hits, W->q_hits, sizeof(cc_point_hit) * (size_t)count, cudaMemcpyDeviceToHost, W->stream));
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    return CC_OK;
+}
+
 int cc_world_cast_rays_device(cc_world *W, const cc_ray *rays, int32_t count, const cc_query_filter *filter,
                               cc_ray_hit *hits) {
     if (!W || count < 0 || !filter || (count > 0 && (!rays || !hits))) return CC_ERR_INVALID;

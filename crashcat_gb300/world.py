@@ -410,6 +410,26 @@ class GpuWorld:
               "cc_world_cast_rays")
         return hits
 
+    def collide_points(self, points: np.ndarray, object_layer_mask: int = 0xFFFFFFFF,
+                       collision_group: int = 0xFFFFFFFF, collision_mask: int = 0xFFFFFFFF,
+                       collision_tolerance: float = 1e-4) -> np.ndarray:
+        """cc_world_collide_points: per point (a _lib.POINT_DTYPE array, or rows of xyz[, world])
+        the number of bodies holding it, the lowest of them and its sub-shape id, as a
+        _lib.POINT_HIT_DTYPE array."""
+        points = np.asarray(points)
+        if points.dtype != _lib.POINT_DTYPE:
+            rows = np.asarray(points, np.float64).reshape(len(points), -1)
+            p = np.zeros(len(rows), _lib.POINT_DTYPE)
+            p["position"] = rows[:, 0:3]
+            p["world"] = rows[:, 3].astype(np.int32) if rows.shape[1] > 3 else 0
+            points = p
+        points = np.ascontiguousarray(points)
+        hits = np.zeros(len(points), _lib.POINT_HIT_DTYPE)
+        f = _lib.QueryFilter(object_layer_mask, collision_group, collision_mask, 0)
+        check(self._lib.cc_world_collide_points(self.handle, points.ctypes.data, len(points), C.byref(f),
+                                                collision_tolerance, hits.ctypes.data), "cc_world_collide_points")
+        return hits
+
     # ---- hinge joints (hinge-constraint.ts) ----
     def add_hinges(self, hinges: np.ndarray) -> np.ndarray:
         """cc_world_add_hinges: records of _lib.HINGE_DTYPE; returns the joint indices."""

@@ -477,6 +477,43 @@ int cc_world_cast_rays_device(cc_world *world, const cc_ray *rays, int32_t count
                               cc_ray_hit *hits);
 
 /* ---------------------------------------------------------------------------
+ * World point queries: collidePoint (src/query.ts:470-490) with every hit
+ * collected (createAllCollidePointCollector), a batch of points per call.
+ *
+ * Bodies of the point's world whose bounding box holds the point
+ * (dbvt.intersectPoint, src/broadphase/dbvt.ts:683-740) and that pass the
+ * filter (flags unused) are tested with collidePointVsShape:
+ *   - sphere: distance (src/shapes/sphere.ts:272-301);
+ *   - box: half extents (src/shapes/box.ts:370-410);
+ *   - capsule and convex hull: local bounds, then GJK against the point with
+ *     collision_tolerance (src/shapes/convex.ts:142-216; the reference's
+ *     default is 1e-4);
+ *   - triangle mesh: local bounds, then the odd-even count of a +Y ray
+ *     (src/shapes/triangle-mesh.ts:482-570).
+ * hit.count is the number of bodies holding the point.  hit.body is the
+ * lowest such body index (-1: none) and hit.sub_shape_id its sub-shape id:
+ * the last triangle the mesh's ray met, else 0xffffffff.
+ *   cc_world_collide_points: host arrays; returns when the hits are written.
+ *   cc_world_collide_points_device: device arrays; queued on the world's stream.
+ * ------------------------------------------------------------------------- */
+typedef struct cc_point {
+    float position[3];
+    int32_t world;
+} cc_point;
+
+typedef struct cc_point_hit {
+    int32_t count;
+    int32_t body;
+    uint32_t sub_shape_id;
+    int32_t reserved;
+} cc_point_hit;
+
+int cc_world_collide_points(cc_world *world, const cc_point *points, int32_t count, const cc_query_filter *filter,
+                            float collision_tolerance, cc_point_hit *hits);
+int cc_world_collide_points_device(cc_world *world, const cc_point *points, int32_t count,
+                                   const cc_query_filter *filter, float collision_tolerance, cc_point_hit *hits);
+
+/* ---------------------------------------------------------------------------
  * Allocation-free penetration query.  No counterpart in the reference: it is
  * the narrowphase of one convex pair (collideConvexVsConvex,
  * src/shapes/convex.ts:257-346, with penetrationDepthStepGJK / EPA of

@@ -2218,6 +2218,35 @@ void orc_cast_rays(void *wp, const double *rays, int n, uint32_t layerMask, uint
     }
 }
 
+// collidePoint query.ts:470-490 with every hit collected (createAllCollidePointCollector): per
+// point (xyz) the number of bodies that contain it, the lowest such body index (-1 if none) and
+// that body's sub-shape id; bodies whose current AABB contains the point and that pass the filter
+// (dbvt.intersectPoint dbvt.ts:683-740)
+void orc_collide_points(void *wp, const double *pts, int n, uint32_t layerMask, uint32_t groups, uint32_t mask,
+                        double tol, int *counts, int *bodies, uint32_t *subs) {
+    World &W = *(World *)wp;
+    for (auto &b : W.bodies) update_aabb(b);
+    for (int r = 0; r < n; r++) {
+        V3 p{pts[3 * r], pts[3 * r + 1], pts[3 * r + 2]};
+        int c = 0, first = -1;
+        uint32_t fsub = EMPTY_SUB_SHAPE_ID;
+        for (auto &b : W.bodies) {
+            if (!((groups & b.mask) != 0 && (b.groups & mask) != 0)) continue;
+            if (!(layerMask & (1u << b.objectLayer))) continue;
+            if (!box_contains(b.aabb, p)) continue;
+            uint32_t sub;
+            if (!point_in_shape(b.shape, b.position, b.quat, p, tol, sub)) continue;
+            if (c++ == 0) {
+                first = b.index;
+                fsub = sub;
+            }
+        }
+        counts[r] = c;
+        bodies[r] = first;
+        subs[r] = fsub;
+    }
+}
+
 // ---- unit-level entry points for the known-answer tests -------------------
 // Faces are passed as n vertices (xyz doubles).  Returns the output vertex count.
 int orc_clip_poly_vs_plane(const double *poly, int n, const double *origin, const double *normal, double *out) {

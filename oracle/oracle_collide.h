@@ -2365,6 +2365,85 @@ inline bool cast_ray_vs_shape(const Shape &s, V3 pos, Q4 q, V3 origin, V3 dir, d
     return true;
 }
 
+// the hit count of a ray through a mesh with every hit kept (hitCountCollector
+// triangle-mesh.ts:441-467: its early-out fraction stays INITIAL_EARLY_OUT_FRACTION, so every
+// node the ray enters is walked) and the sub-shape id of the last hit in walk order
+inline int mesh_ray_hit_count(const MeshData &M, V3 o, V3 d, double length, uint32_t &lastSub) {
+    const double early = 1.0 + 1e-4;
+    int count = 0;
+    if (M.nodes.empty()) return 0;
+    std::vector<std::pair<int, double>> stack{{0, -std::numeric_limits<double>::infinity()}};
+    while (!stack.empty()) {
+        auto [node, dist] = stack.back();
+        stack.pop_back();
+        if (dist >= early) continue;
+        const auto &nd = M.nodes[node];
+        if (nd[7] < 0) {
+            int start = (int)nd[6], n = (int)(-nd[7]) - 1;
+            for (int t = start; t < start + n; t++) {
+                const auto &tr = M.tris[t];
+                double f;
+                if (ray_triangle(o, d, length, M.verts[tr[0]], M.verts[tr[1]], M.verts[tr[2]], false, f) && f < early) {
+                    count++;
+                    lastSub = mesh_sub_shape_id(M, t);
+                }
+            }
+            continue;
+        }
+        int left = node + 1, right = (int)nd[6];
+        auto box = [&](int k) {
+            const auto &c = M.nodes[k];
+            return Box3{{c[0], c[1], c[2]}, {c[3], c[4], c[5]}};
+        };
+        double ldist = ray_fraction_to_box(o, d, length, box(left)), rdist = ray_fraction_to_box(o, d, length, box(right));
+        if (ldist <= rdist) {
+            if (rdist < early) stack.push_back({right, rdist});
+            if (ldist < early) stack.push_back({left, ldist});
+        } else {
+            if (ldist < early) stack.push_back({left, ldist});
+            if (rdist < early) stack.push_back({right, rdist});
+        }
+    }
+    return count;
+}
+
+inline bool box_contains(const Box3 &b, V3 p) {  // box3.containsPoint
+    return p.x >= b.mn.x && p.x <= b.mx.x && p.y >= b.mn.y && p.y <= b.mx.y && p.z >= b.mn.z && p.z <= b.mx.z;
+}
+
+// collidePointVsShape for one body: collidePointVsSphere sphere.ts:272-301, collidePointVsBox
+// box.ts:370-410, collidePointVsConvex convex.ts:142-216 (GJK of the INCLUDE_CONVEX_RADIUS support
+// against the point, collisionTolerance 1e-4 by default), collidePointVsTriangleMesh
+// triangle-mesh.ts:482-570 (odd-even count of a +Y ray 1.1 x the mesh height long, back faces
+// counted).  True when the point is inside; subId is the mesh's last-hit triangle.
+inline bool point_in_shape(const Shape &s, V3 pos, Q4 q, V3 point, double tol, uint32_t &subId) {
+    subId = EMPTY_SUB_SHAPE_ID;
+    V3 l = sub(point, pos);
+    if (s.type == SHAPE_SPHERE) return dot(l, l) <= s.radius * s.radius;
+    V3 lp = rotate(qconj(q), l);
+    if (s.type == SHAPE_BOX)
+        return std::fabs(lp.x) <= s.half_extents.x && std::fabs(lp.y) <= s.half_extents.y &&
+               std::fabs(lp.z) <= s.half_extents.z;
+    if (!box_contains(s.aabb, lp)) return false;
+    if (s.type == SHAPE_TRIANGLE_MESH) {
+        double h = s.aabb.mx.y - s.aabb.mn.y;
+        uint32_t last = EMPTY_SUB_SHAPE_ID;
+        int n = mesh_ray_hit_count(*s.mesh, lp, {0, 1, 0}, h * 1.1, last);
+        if ((n & 1) == 0) return false;
+        subId = last;
+        return true;
+    }
+    Support S = make_support(s, INCLUDE_CONVEX_RADIUS);
+    Support P;
+    P.kind = SUP_SPHERE_POINT;
+    P.transformed = true;
+    P.m = mat4_from_rt({0, 0, 0, 1}, lp);
+    V3 dir = lp;
+    if (dot(dir, dir) < 1e-10) dir = {0, 1, 0};
+    GjkResult g = gjk_closest_points(S, P, tol, dir, 0.0);
+    return g.sqdist <= tol * tol;
+}
+
 // the hits of a body pair in narrowphase order (collideShapeVsShape narrowphase.ts:172-238 with
 // the mesh registrations triangle-mesh.ts:223-237: a mesh as shape A runs the convex-vs-mesh
 // function reversed, collide-shape-vs-shape.ts:227-354)

@@ -48,6 +48,7 @@ def load():
         "orc_get_manifolds": ([vp, dp], i32),
         "orc_island_count": ([vp], i32),
         "orc_ccd_counts": ([vp, ip], None),
+        "orc_collide_points": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double, ip, ip, vp], None),
         "orc_cast_rays": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, i32, dp, ip, vp], None),
         "orc_add_mesh": ([vp, i32, dp, i32, C.c_void_p, i32, dp], i32),
         "orc_get_manifold_subs": ([vp, C.c_void_p], i32),
@@ -245,6 +246,19 @@ class OracleWorld:
         self.lib.orc_cast_rays(self.h, dptr(rays), n, layer_mask, groups, mask, int(treat_convex_as_solid),
                                dptr(fr), iptr(bo), su.ctypes.data)
         return fr[:n], bo[:n], su[:n]
+
+    def collide_points(self, points: np.ndarray, layer_mask: int = 0xFFFFFFFF, groups: int = 0xFFFFFFFF,
+                       mask: int = 0xFFFFFFFF, tolerance: float = 1e-4):
+        """Per point: (number of bodies containing it, the lowest such body (-1: none), its
+        sub-shape id)."""
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        n = pts.shape[0]
+        co = np.zeros(max(n, 1), dtype=np.int32)
+        bo = np.zeros(max(n, 1), dtype=np.int32)
+        su = np.zeros(max(n, 1), dtype=np.uint32)
+        self.lib.orc_collide_points(self.h, dptr(pts), n, layer_mask, groups, mask, tolerance, iptr(co), iptr(bo),
+                                    su.ctypes.data)
+        return co[:n], bo[:n], su[:n]
 
     def aabbs(self) -> np.ndarray:
         o = np.zeros((self.n, 6), dtype=np.float64)

@@ -270,3 +270,132 @@ def test_gpu_rays_stay_in_their_world(gpu_lib, oracle_lib):
     h = g.cast_rays(rays)
     np.testing.assert_array_equal(h["body"], np.arange(nw) * per)
     np.testing.assert_allclose(h["fraction"], 1.6 / 20.0, atol=1e-4)
+
+
+# ---------------------------------------------------------------------------
+# collidePoint (query.ts:470-490): the reference's known answers
+# (tst/query.test.ts collidePoint, tst/collision/collide-point-vs-shape.test.ts)
+# ---------------------------------------------------------------------------
+Q45Y = (0.0, math.sin(math.pi / 8), 0.0, math.cos(math.pi / 8))  # 45 degrees about +Y
+# (name, body kind, kwargs, body position, quaternion, point, inside)
+POINT_CASES = [
+    ("query_box_inside", "box", {}, (0, 0, 0), None, (0.5, 0.5, 0.5), True),
+    ("query_box_outside", "box", {}, (0, 0, 0), None, (5, 5, 5), False),
+    ("sphere_centre", "sphere", {}, (0, 0, 0), None, (0, 0, 0), True),
+    ("sphere_translated", "sphere", {}, (5, 3, -2), None, (5, 3, -2), True),
+    ("sphere_surface", "sphere", {}, (0, 0, 0), None, (1, 0, 0), True),
+    ("sphere_outside", "sphere", {}, (0, 0, 0), None, (2, 0, 0), False),
+    ("sphere_outside_unscaled", "sphere", {}, (0, 0, 0), None, (1.5, 0, 0), False),
+    ("box_centre", "box", {}, (0, 0, 0), None, (0, 0, 0), True),
+    ("box_off_centre", "box", {"half": (2, 2, 2)}, (0, 0, 0), None, (1, 1, 1), True),
+    ("box_face", "box", {}, (0, 0, 0), None, (1, 0, 0), True),
+    ("box_corner", "box", {}, (0, 0, 0), None, (1, 1, 1), True),
+    ("box_outside", "box", {}, (0, 0, 0), None, (2, 0, 0), False),
+    ("box_rotated_45", "box", {}, (0, 0, 0), Q45Y, (1.4, 0, 0), True),
+    ("box_rotated_inside", "box", {}, (0, 0, 0), Q45Y, (0.5, 0, 0), True),
+    ("box_translated", "box", {}, (5, 3, -2), None, (5, 3, -2), True),
+    ("box_translated_rotated", "box", {}, (10, 5, 3), Q45Y, (11, 5, 3), True),
+    ("capsule_cap_inside", "capsule", {}, (0, 0, 0), None, (0, 1.4, 0), True),
+    ("capsule_cap_outside", "capsule", {}, (0, 0, 0), None, (0, 1.6, 0), False),
+    ("capsule_side_inside", "capsule", {}, (0, 0, 0), None, (0.45, 0, 0), True),
+    ("capsule_side_outside", "capsule", {}, (0, 0, 0), None, (0.55, 0, 0), False),
+]
+
+CUBE_INDICES = [0, 1, 3, 0, 3, 2, 4, 7, 5, 4, 6, 7, 2, 3, 6, 3, 7, 6, 1, 0, 4, 1, 4, 5, 1, 7, 3, 1, 5, 7, 0, 2, 6,
+                0, 6, 4]
+
+
+def randomized_cube(seed=7):
+    """The test's cube with each corner scaled by 0.1-0.3 per axis (seeded here)."""
+    rng = np.random.default_rng(seed)
+    base = np.array([[x, y, z] for y in (-1.0, 1.0) for z in (-1.0, 1.0) for x in (-1.0, 1.0)])
+    return base * rng.uniform(0.1, 0.3, (8, 3))
+
+
+# (name, mesh body position, point, inside)
+MESH_POINT_CASES = [
+    ("cube_centre", (0, 0, 0), (0, 0, 0), True),
+    ("cube_far_outside", (0, 0, 0), (5, 0, 0), False),
+    ("cube_translated", (10, 5, 3), (10, 5, 3), True),
+]
+
+
+@pytest.mark.parametrize("case", POINT_CASES, ids=[c[0] for c in POINT_CASES])
+def test_oracle_point_known_answers(oracle_lib, case):
+    _, kind, kw, pos, q, p, inside = case
+    b = one_body(kind, pos, **kw)
+    if q is not None:
+        b["quaternion"][0] = q
+    co, bo, su = oracle_single(b).collide_points(np.array([p], np.float64))
+    assert (co[0] == 1) == inside and (bo[0] == 0) == inside
+    assert su[0] == 0xFFFFFFFF
+
+
+@pytest.mark.parametrize("case", MESH_POINT_CASES, ids=[c[0] for c in MESH_POINT_CASES])
+def test_oracle_mesh_point_known_answers(gpu_lib, oracle_lib, case):
+    _, pos, p, inside = case
+    m = _lib.build_triangle_mesh(randomized_cube(), np.array(CUBE_INDICES).reshape(-1, 3))
+    b = mesh_body()
+    b["position"][0] = pos
+    co, bo, su = oracle_single(b, m).collide_points(np.array([p], np.float64))
+    assert (co[0] == 1) == inside
+    if inside:
+        assert su[0] != 0xFFFFFFFF  # the last triangle the +Y ray met
+
+
+@pytest.mark.gpu
+def test_gpu_point_known_answers(gpu_lib, oracle_lib):
+    for _, kind, kw, pos, q, p, inside in POINT_CASES:
+        b = one_body(kind, pos, **kw)
+        if q is not None:
+            b["quaternion"][0] = q
+        g = world.GpuWorld(world.standard_settings(), 4)
+        g.add_bodies(b)
+        h = g.collide_points(np.array([p], np.float64))
+        assert (h["count"][0] == 1) == inside, (kind, p)
+        assert (h["body"][0] == 0) == inside
+    m_pos, m_idx = randomized_cube(), np.array(CUBE_INDICES).reshape(-1, 3)
+    for _, pos, p, inside in MESH_POINT_CASES:
+        g = world.GpuWorld(world.standard_settings(), 4)
+        g.add_triangle_mesh(m_pos, m_idx)
+        b = mesh_body()
+        b["position"][0] = pos
+        g.add_bodies(b)
+        o = oracle_single(b, g.get_triangle_mesh(0))
+        h = g.collide_points(np.array([p], np.float64))
+        co, bo, su = o.collide_points(np.array([p], np.float64))
+        assert (h["count"][0] == 1) == inside
+        assert h["sub_shape_id"][0] == su[0]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", [5, 6])
+def test_gpu_points_in_terrain_pile(gpu_lib, oracle_lib, seed):
+    """Points scattered through a terrain pile: under the terrain (odd-even count of the open
+    heightfield), in bodies, in several bodies, in none."""
+    sc = scenes.mesh_drop(n=120, n_cells=16, seed=seed, heights=(0.0, 3.0))
+    ws = world.standard_settings()
+    g = world.GpuWorld(ws, sc.n + 16)
+    for p in sc.hull_points or ():
+        g.add_convex_hull(p)
+    g.add_triangle_mesh(*sc.mesh)
+    g.add_bodies(sc.bodies)
+    hulls = [g.get_convex_hull(i) for i in range(len(sc.hull_points or ()))]
+    o = pyoracle.OracleWorld(ws, sc.bodies, hulls, [g.get_triangle_mesh(0)])
+    g.step(sc.dt, 30)
+    rows, _ = g.get_state()
+    st = o.state()
+    st[:, 0:13] = rows[:, 0:13]
+    o.set_state(st)
+    rng = np.random.default_rng(seed)
+    # half of the points near body centres (inside something), half anywhere in the pile's box
+    near = rows[rng.integers(1, sc.n, 4096), 0:3] + rng.normal(scale=0.3, size=(4096, 3))
+    anywhere = np.stack([rng.uniform(-7, 7, 4096), rng.uniform(-3, 6, 4096), rng.uniform(-7, 7, 4096)], 1)
+    pts = np.concatenate([near, anywhere])
+    h = g.collide_points(pts)
+    co, bo, su = o.collide_points(pts)
+    assert (h["count"] == co).mean() >= 0.995
+    assert (h["body"] == bo).mean() >= 0.995
+    assert (co > 0).mean() > 0.25 and (bo == 0).sum() > 300 and (co > 1).sum() > 0
+    mesh = (bo == 0) & (h["body"] == 0)
+    assert (h["sub_shape_id"][mesh] == su[mesh]).mean() >= 0.99
