@@ -473,6 +473,23 @@ def ray_query_measurement(g, rays, reps: int = 10):
             "device_equals_host_api": bool((h2["body"] == hits["body"]).all()), "_bodies": hits["body"].copy()}
 
 
+def ray_profile(steps: int = 60, rays: int = 1 << 20, reps: int = 3):
+    """The terrain workload's ray queries alone, for a profiler: the scene stepped `steps` times,
+    then `reps` batches of `rays` closest-hit rays on resident buffers.  Prints one JSON line."""
+    from crashcat_gb300 import scenes, world as W
+    sc = scenes.mesh_drop(n=20000, n_cells=256, seed=2, amplitude=4.0, heights=(5.0, 40.0), fast_fraction=0.2)
+    g = W.GpuWorld(W.standard_settings(velocity_iterations=8, position_iterations=2), sc.n + 16)
+    for p in sc.hull_points:
+        g.add_convex_hull(p)
+    g.add_triangle_mesh(*sc.mesh)
+    g.add_bodies(sc.bodies)
+    if steps > 0:
+        g.step(sc.dt, steps)
+    q = ray_query_measurement(g, terrain_rays(rays, 0.4 * 256), reps=reps)
+    q.pop("_bodies")
+    print(json.dumps(q))
+
+
 def terrain_measurement(cpu_seconds: float = 8.0):
     """The mixed-shape terrain workload: 20,000 bodies (spheres, boxes, capsules and convex hulls
     of 16-32 points in the mixed pile's size ranges) dropped from 5-40 m over a 256 x 256-cell

@@ -510,6 +510,35 @@ void launch_broadphase(DevWorld &w, cudaStream_t s) {
     k_find_pairs<<<grid_for(n, 128, 16), 128, 0, s>>>(w, w.node_world);
 }
 
+// ray sort keys: the ray's world above the Morton code of its origin in the bodies' centre bounds
+// (origins outside are clamped to the bounds' faces)
+__global__ void k_ray_keys(const DevRay *rays, int nr, const unsigned int *scene, unsigned long long *keys, int *idx) {
+    float3 smin = f3(ord2f(scene[0]), ord2f(scene[1]), ord2f(scene[2]));
+    float3 smax = f3(ord2f(scene[3]), ord2f(scene[4]), ord2f(scene[5]));
+    float3 ext = smax - smin;
+    float3 inv = f3(ext.x > 0.f ? 1023.f / ext.x : 0.f, ext.y > 0.f ? 1023.f / ext.y : 0.f,
+                    ext.z > 0.f ? 1023.f / ext.z : 0.f);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nr; i += gridDim.x * blockDim.x) {
+        const DevRay r = rays[i];
+        float3 t = f3(r.origin[0], r.origin[1], r.origin[2]) - smin;
+        unsigned int qx = (unsigned int)fminf(fmaxf(t.x * inv.x, 0.f), 1023.f);
+        unsigned int qy = (unsigned int)fminf(fmaxf(t.y * inv.y, 0.f), 1023.f);
+        unsigned int qz = (unsigned int)fminf(fmaxf(t.z * inv.z, 0.f), 1023.f);
+        unsigned int m = (expand_bits10(qx) << 2) | (expand_bits10(qy) << 1) | expand_bits10(qz);
+        const unsigned int wd = r.world < 0 ? 0u : (unsigned int)r.world;
+        keys[i] = ((unsigned long long)wd << 30) | m;
+        idx[i] = i;
+    }
+}
+
+void launch_ray_order(DevWorld &w, const DevRay *rays, int nr, unsigned long long *keys, int *idx, int *tmp,
+                      cudaStream_t s) {
+    k_ray_keys<<<grid_for(nr, 256), 256, 0, s>>>(rays, nr, w.scene, keys, idx);
+    int wbits = 0;
+    while ((1 << wbits) < w.num_worlds) wbits++;
+    radix_sort_pairs_u64(keys, keys + nr, idx, idx + nr, nr, 30 + wbits, tmp, s, nullptr);
+}
+
 // the broadphase without its pair search: current boxes, Morton order and tree
 void launch_query_tree(DevWorld &w, cudaStream_t s) {
     int n = w.n;

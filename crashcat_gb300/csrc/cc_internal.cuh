@@ -615,8 +615,12 @@ struct DevRayFilter {
 };
 // the boxes and the tree of the current poses, for queries between steps
 void launch_query_tree(DevWorld &w, cudaStream_t s);
-void launch_cast_rays(DevWorld &w, const DevRay *rays, int nr, const DevRayFilter &f, DevRayHit *hits,
+// order: the rays sorted by world and the Morton code of their origin (coherent warps), from
+// launch_ray_order; keys/keys_alt 2 x nr, idx/idx_alt 2 x nr, tmp radix_tmp_ints(nr)
+void launch_ray_order(DevWorld &w, const DevRay *rays, int nr, unsigned long long *keys, int *idx, int *tmp,
                       cudaStream_t s);
+void launch_cast_rays(DevWorld &w, const DevRay *rays, const int *order, int nr, const DevRayFilter &f,
+                      DevRayHit *hits, cudaStream_t s);
 // points: xyz and the world (int bits in w); out: hit count, lowest body hit (-1), its sub-shape id
 void launch_collide_points(DevWorld &w, const float4 *pts, int np, const DevRayFilter &f, float tol, int4 *out,
                            cudaStream_t s);
@@ -646,5 +650,6 @@ void exclusive_scan_int(const int *in, int *out, int n, int *total, int *tmp, cu
 void radix_sort_pairs_u64(unsigned long long *keys, unsigned long long *keys_alt, int *vals, int *vals_alt, int n,
                           int bits, int *tmp, cudaStream_t s, const int *n_dev = nullptr);
 size_t scan_tmp_ints(int n);
+size_t radix_tmp_ints(int n);
 
 }  // namespace cc

@@ -3061,11 +3061,12 @@ __device__ bool ray_vs_body(const DevWorld &w, const HullView &hv, int b, float3
 // broadphase.castRay / dbvt.castRay (broadphase.ts:280-298, dbvt.ts:779-865) over the world's
 // subtree of the device tree: every body whose box the segment enters and that passes the filter
 // is cast; the least fraction wins, ties to the lower body index.
-__global__ void __launch_bounds__(128) k_cast_rays(DevWorld w, const int2 *node_world, const DevRay *rays, int nr,
-                                                   DevRayFilter flt, DevRayHit *hits) {
+__global__ void __launch_bounds__(128) k_cast_rays(DevWorld w, const int2 *node_world, const DevRay *rays,
+                                                   const int *order, int nr, DevRayFilter flt, DevRayHit *hits) {
     const int n = w.n;
     const HullView hv = hull_view(w);
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nr; r += gridDim.x * blockDim.x) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nr; k += gridDim.x * blockDim.x) {
+        const int r = order ? order[k] : k;
         const DevRay ry = rays[r];
         const float3 o = f3(ry.origin[0], ry.origin[1], ry.origin[2]);
         const float3 d = f3(ry.direction[0], ry.direction[1], ry.direction[2]);
@@ -3075,21 +3076,41 @@ __global__ void __launch_bounds__(128) k_cast_rays(DevWorld w, const int2 *node_
         int hit = -1;
         uint32_t hsub = 0xffffffffu;
         if (n > 0 && wr >= 0 && wr < w.num_worlds && len > 0.f) {
+            // Nearer child first, and a subtree whose box the ray enters beyond the best hit (by more
+            // than twice the GJK tolerance, 1e-3 m) is skipped: a shape lies inside its box, so no hit
+            // in it can come first.  The reference casts every body whose box the segment enters; the
+            // least fraction is the same.
             int stack[CCD_STACK];
+            float sdist[CCD_STACK];
             int sp = 0;
-            stack[sp++] = 0;
+            const float t_root = ray_box_entry(o, d, len, xyz(w.node_lo[0]), xyz(w.node_hi[0]));
+            if (t_root < CUDART_INF_F) {
+                stack[sp] = 0;
+                sdist[sp++] = t_root;
+            }
             while (sp > 0) {
-                const int node = stack[--sp];
+                --sp;
+                const int node = stack[sp];
+                if (sdist[sp] > best * len + 2e-3f) continue;
                 const int2 nw = node_world[node];
                 if (wr < nw.x || wr > nw.y) continue;
-                if (!(ray_box_entry(o, d, len, xyz(w.node_lo[node]), xyz(w.node_hi[node])) < CUDART_INF_F)) continue;
                 if (node < n - 1) {
                     const int2 ch = w.node_child[node];
-                    if (sp + 2 <= CCD_STACK) {
-                        stack[sp++] = ch.y;
-                        stack[sp++] = ch.x;
-                    } else {
+                    const float tl = ray_box_entry(o, d, len, xyz(w.node_lo[ch.x]), xyz(w.node_hi[ch.x]));
+                    const float tr = ray_box_entry(o, d, len, xyz(w.node_lo[ch.y]), xyz(w.node_hi[ch.y]));
+                    if (sp + 2 > CCD_STACK) {
                         atomicOr(&w.ctr->overflow, OVF_SLOTS);
+                        continue;
+                    }
+                    const int far_n = tl <= tr ? ch.y : ch.x, near_n = tl <= tr ? ch.x : ch.y;
+                    const float far_t = fmaxf(tl, tr), near_t = fminf(tl, tr);
+                    if (far_t < CUDART_INF_F) {
+                        stack[sp] = far_n;
+                        sdist[sp++] = far_t;
+                    }
+                    if (near_t < CUDART_INF_F) {
+                        stack[sp] = near_n;
+                        sdist[sp++] = near_t;
                     }
                     continue;
                 }
@@ -3274,10 +3295,10 @@ void launch_collide_points(DevWorld &w, const float4 *pts, int np, const DevRayF
     k_collide_points<<<grid_for(np, 128, 16), 128, 0, s>>>(w, w.node_world, pts, np, f, tol, out);
 }
 
-void launch_cast_rays(DevWorld &w, const DevRay *rays, int nr, const DevRayFilter &f, DevRayHit *hits,
-                      cudaStream_t s) {
+void launch_cast_rays(DevWorld &w, const DevRay *rays, const int *order, int nr, const DevRayFilter &f,
+                      DevRayHit *hits, cudaStream_t s) {
     if (nr <= 0) return;
-    k_cast_rays<<<grid_for(nr, 128, 16), 128, 0, s>>>(w, w.node_world, rays, nr, f, hits);
+    k_cast_rays<<<grid_for(nr, 128, 16), 128, 0, s>>>(w, w.node_world, rays, order, nr, f, hits);
 }
 
 void launch_mesh_narrowphase(DevWorld &w, int pass, cudaStream_t s);

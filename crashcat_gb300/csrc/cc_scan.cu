@@ -168,6 +168,12 @@ __global__ void k_radix_scatter(const unsigned long long *keys, const int *vals,
 }
 
 // Sorts (keys, vals) by the low `bits` bits of the keys; result ends in keys/vals.
+// ints of scratch radix_sort_pairs_u64 needs for n keys
+size_t radix_tmp_ints(int n) {
+    size_t nblocks = (size_t)(n + RS_TILE - 1) / RS_TILE;
+    return nblocks * 256 + 32 + scan_tmp_ints((int)(nblocks * 256));
+}
+
 void radix_sort_pairs_u64(unsigned long long *keys, unsigned long long *keys_alt, int *vals, int *vals_alt, int n,
                           int bits, int *tmp, cudaStream_t s, const int *) {
     if (n <= 1) return;

@@ -42,6 +42,9 @@ struct cc_world {
     DevRay *q_rays = nullptr;  // ray query staging (cc_world_cast_rays), grown on demand
     DevRayHit *q_hits = nullptr;
     int q_cap = 0;
+    unsigned long long *q_keys = nullptr;  // ray sort: 2 x keys, 2 x indices, radix scratch
+    int *q_idx = nullptr, *q_tmp = nullptr;
+    int q_sort_cap = 0;
     float *d_state_rows = nullptr;  // 16 floats per body staging for get/set state
     float *h_pinned_rows = nullptr;
     DevCounters *h_ctr = nullptr;   // pinned mirror of the device counters
@@ -521,6 +524,9 @@ int cc_world_destroy(cc_world *W) {
         if (p) cudaFree(p);
     if (W->q_rays) cudaFree(W->q_rays);
     if (W->q_hits) cudaFree(W->q_hits);
+    if (W->q_keys) cudaFree(W->q_keys);
+    if (W->q_idx) cudaFree(W->q_idx);
+    if (W->q_tmp) cudaFree(W->q_tmp);
     for (void *p : W->adj.allocs)
         if (p) cudaFree(p);
     if (W->h_ctr) cudaFreeHost(W->h_ctr);
@@ -981,8 +987,21 @@ static int queue_cast_rays(cc_world *W, const DevRay *rays, int n, const cc_quer
     if (int r = sync_shapes(W)) return r;
     DevWorld &w = W->w;
     DevRayFilter flt{f->object_layer_mask, f->collision_group, f->collision_mask, f->flags};
+    if (n > W->q_sort_cap) {
+        if (W->q_keys) cudaFree(W->q_keys);
+        if (W->q_idx) cudaFree(W->q_idx);
+        if (W->q_tmp) cudaFree(W->q_tmp);
+        W->q_keys = nullptr;
+        W->q_idx = W->q_tmp = nullptr;
+        W->q_sort_cap = 0;
+        CC_TRY(cudaMalloc(&W->q_keys, sizeof(unsigned long long) * 2 * (size_t)n));
+        CC_TRY(cudaMalloc(&W->q_idx, sizeof(int) * 2 * (size_t)n));
+        CC_TRY(cudaMalloc(&W->q_tmp, sizeof(int) * radix_tmp_ints(n)));
+        W->q_sort_cap = n;
+    }
     launch_query_tree(w, W->stream);
-    launch_cast_rays(w, rays, n, flt, hits, W->stream);
+    launch_ray_order(w, rays, n, W->q_keys, W->q_idx, W->q_tmp, W->stream);
+    launch_cast_rays(w, rays, W->q_idx, n, flt, hits, W->stream);
     return cuda_ok(cudaGetLastError());
 }
 
