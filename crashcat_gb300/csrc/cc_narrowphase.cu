@@ -3038,15 +3038,16 @@ __device__ bool ray_vs_mesh(const DevWorld &w, int b, float3 o, float3 d, float 
 }
 
 // castRayVsShape for one body (castRayVsConvex convex.ts:54-126 with the INCLUDE_CONVEX_RADIUS
-// support and tolerance 1e-3, or the mesh walk): the hit below max_f and its sub-shape id
+// support and tolerance 1e-3, or the mesh walk): the hit below max_f and its sub-shape id.
+// MESH selects the triangle-mesh branch, so that each kernel instance holds only one of them.
+template <bool MESH>
 __device__ bool ray_vs_body(const DevWorld &w, const HullView &hv, int b, float3 o, float3 d, float len,
                             uint32_t flags, float max_f, float &fraction, uint32_t &sub) {
     const uint32_t fb = w.flags[b];
     const float3 pB = xyz(w.pos[b]);
     const float4 qB = w.quat[b];
     const float3 lo = qrot_inv(qB, o - pB), ld = qrot_inv(qB, d);
-    if (shape_of(fb) == SHAPE_MESH)
-        return ray_vs_mesh(w, b, lo, ld, len, !(flags & CC_RAY_BACKFACES), max_f, fraction, sub);
+    if (MESH) return ray_vs_mesh(w, b, lo, ld, len, !(flags & CC_RAY_BACKFACES), max_f, fraction, sub);
     const Sup<float> sup = make_sup<float>(shape_of(fb), w.shape[b], false, hv);
     float lambda;
     if (!gjk_cast_ray(lambda, V<float>{lo.x, lo.y, lo.z}, V<float>{ld.x * len, ld.y * len, ld.z * len}, 1e-3f, sup,
@@ -3061,6 +3062,10 @@ __device__ bool ray_vs_body(const DevWorld &w, const HullView &hv, int b, float3
 // broadphase.castRay / dbvt.castRay (broadphase.ts:280-298, dbvt.ts:779-865) over the world's
 // subtree of the device tree: every body whose box the segment enters and that passes the filter
 // is cast; the least fraction wins, ties to the lower body index.
+// PASS 0 casts every body; with meshes present, PASS 1 casts the meshes alone and PASS 2 the
+// convex bodies, starting from PASS 1's hits (so the ground's hit culls what lies beyond it, and
+// each instance carries one shape family's code).
+template <int PASS>
 __global__ void __launch_bounds__(128) k_cast_rays(DevWorld w, const int2 *node_world, const DevRay *rays,
                                                    const int *order, int nr, DevRayFilter flt, DevRayHit *hits) {
     const int n = w.n;
@@ -3075,6 +3080,14 @@ __global__ void __launch_bounds__(128) k_cast_rays(DevWorld w, const int2 *node_
         float best = 1.f + 1e-4f;  // INITIAL_EARLY_OUT_FRACTION cast-utils.ts:3
         int hit = -1;
         uint32_t hsub = 0xffffffffu;
+        if (PASS == 2) {
+            const DevRayHit h0 = hits[r];
+            if (h0.body >= 0) {
+                best = h0.fraction;
+                hit = h0.body;
+                hsub = h0.sub_shape_id;
+            }
+        }
         if (n > 0 && wr >= 0 && wr < w.num_worlds && len > 0.f) {
             // Nearer child first, and a subtree whose box the ray enters beyond the best hit (by more
             // than twice the GJK tolerance, 1e-3 m) is skipped: a shape lies inside its box, so no hit
@@ -3124,7 +3137,11 @@ __global__ void __launch_bounds__(128) k_cast_rays(DevWorld w, const int2 *node_
                 const float max_f = (hit >= 0 && b < hit) ? nextafterf(best, CUDART_INF_F) : best;
                 float f;
                 uint32_t sub;
-                if (!ray_vs_body(w, hv, b, o, d, len, flt.flags, max_f, f, sub)) continue;
+                const bool is_mesh = shape_of(fb) == SHAPE_MESH;
+                if (is_mesh ? PASS == 2 : PASS == 1) continue;
+                const bool ok = is_mesh ? ray_vs_body<true>(w, hv, b, o, d, len, flt.flags, max_f, f, sub)
+                                        : ray_vs_body<false>(w, hv, b, o, d, len, flt.flags, max_f, f, sub);
+                if (!ok) continue;
                 if (f < best || (f == best && b < hit)) {
                     best = f;
                     hit = b;
@@ -3298,7 +3315,12 @@ void launch_collide_points(DevWorld &w, const float4 *pts, int np, const DevRayF
 void launch_cast_rays(DevWorld &w, const DevRay *rays, const int *order, int nr, const DevRayFilter &f,
                       DevRayHit *hits, cudaStream_t s) {
     if (nr <= 0) return;
-    k_cast_rays<<<grid_for(nr, 128, 16), 128, 0, s>>>(w, w.node_world, rays, order, nr, f, hits);
+    if (w.num_mesh_bodies > 0) {
+        k_cast_rays<1><<<grid_for(nr, 128, 16), 128, 0, s>>>(w, w.node_world, rays, order, nr, f, hits);
+        k_cast_rays<2><<<grid_for(nr, 128, 16), 128, 0, s>>>(w, w.node_world, rays, order, nr, f, hits);
+    } else {
+        k_cast_rays<0><<<grid_for(nr, 128, 16), 128, 0, s>>>(w, w.node_world, rays, order, nr, f, hits);
+    }
 }
 
 void launch_mesh_narrowphase(DevWorld &w, int pass, cudaStream_t s);
