@@ -89,6 +89,12 @@ POINT_DTYPE = np.dtype([("position", np.float32, 3), ("world", np.int32)])
 POINT_HIT_DTYPE = np.dtype([("count", np.int32), ("body", np.int32), ("sub_shape_id", np.uint32),
                             ("reserved", np.int32)])
 
+# cc_shape_cast / cc_shape_cast_hit
+SHAPE_CAST_DTYPE = np.dtype([("shape_type", np.int32), ("shape_params", np.float32, 4), ("position", np.float32, 3),
+                             ("quaternion", np.float32, 4), ("displacement", np.float32, 3), ("world", np.int32)])
+SHAPE_CAST_HIT_DTYPE = np.dtype([("body", np.int32), ("fraction", np.float32), ("normal", np.float32, 3),
+                                 ("point", np.float32, 3)])
+
 
 class QueryFilter(C.Structure):
     _fields_ = [("object_layer_mask", C.c_uint32), ("collision_group", C.c_uint32),
@@ -153,6 +159,8 @@ EXPORTS = {
     "cc_world_collide_points": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_float, C.c_void_p], C.c_int),
     "cc_world_collide_points_device": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_float, C.c_void_p],
                                        C.c_int),
+    "cc_world_cast_shapes": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
+    "cc_world_cast_shapes_device": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
     "cc_world_cast_rays": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
     "cc_world_cast_rays_device": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
     "cc_world_add_convex_hull": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.POINTER(C.c_int32)], C.c_int),

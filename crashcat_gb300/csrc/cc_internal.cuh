@@ -621,6 +621,24 @@ void launch_ray_order(DevWorld &w, const DevRay *rays, int nr, unsigned long lon
                       cudaStream_t s);
 void launch_cast_rays(DevWorld &w, const DevRay *rays, const int *order, int nr, const DevRayFilter &f,
                       DevRayHit *hits, cudaStream_t s);
+// shape casts: a sphere, box or capsule (params as a body's shape record) at a pose, moved by a
+// displacement, in a world; the hit: body (-1), fraction, normal, contact point on the cast shape
+struct DevShapeCast {
+    int shape_type;
+    float params[4];
+    float position[3];
+    float quaternion[4];
+    float displacement[3];
+    int world;
+};
+struct DevShapeCastHit {
+    int body;
+    float fraction;
+    float normal[3];
+    float point[3];
+};
+void launch_cast_shapes(DevWorld &w, const DevShapeCast *qs, int nq, const DevRayFilter &f, DevShapeCastHit *hits,
+                        cudaStream_t s);
 // points: xyz and the world (int bits in w); out: hit count, lowest body hit (-1), its sub-shape id
 void launch_collide_points(DevWorld &w, const float4 *pts, int np, const DevRayFilter &f, float tol, int4 *out,
                            cudaStream_t s);

@@ -3312,6 +3312,137 @@ void launch_collide_points(DevWorld &w, const float4 *pts, int np, const DevRayF
     k_collide_points<<<grid_for(np, 128, 16), 128, 0, s>>>(w, w.node_world, pts, np, f, tol, out);
 }
 
+// ---------------------------------------------------------------------------
+// world queries: castShape (query.ts:196-214) with the closest-hit collector
+// (ClosestCastShapeCollector cast-shape-vs-shape.ts:199-217), default cast settings
+// ---------------------------------------------------------------------------
+// broadphase.castAABB (broadphase.ts:327-345) of the cast shape's start box along the
+// displacement over the world's subtree, nearer child first and subtrees beyond the best hit
+// skipped; castShapeVsShape per body: castConvexVsConvexLocal convex.ts:744-830 (EXCLUDE supports,
+// tolerance 1e-4, back faces dropped), or for a mesh the sphere's own cast or
+// castConvexVsTriangleMesh (ccd_cast_mesh, the same default settings).
+__global__ void __launch_bounds__(128) k_cast_shapes(DevWorld w, const int2 *node_world, const DevShapeCast *qs,
+                                                     int nq, DevRayFilter flt, DevShapeCastHit *hits) {
+    const int n = w.n;
+    const HullView hv = hull_view(w);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nq; k += gridDim.x * blockDim.x) {
+        const DevShapeCast q = qs[k];
+        const int shape = q.shape_type;
+        const float4 sa = make_float4(q.params[0], q.params[1], q.params[2], q.params[3]);
+        const uint32_t fa = (uint32_t)shape << F_SHAPE_SHIFT;
+        const float3 pA = f3(q.position[0], q.position[1], q.position[2]);
+        const float4 qA = make_float4(q.quaternion[0], q.quaternion[1], q.quaternion[2], q.quaternion[3]);
+        const float3 disp = f3(q.displacement[0], q.displacement[1], q.displacement[2]);
+        const int wr = q.world;
+        float best = 1.f + 1e-4f;  // INITIAL_EARLY_OUT_FRACTION cast-utils.ts:3
+        int hit = -1;
+        float3 hn = f3(0.f, 0.f, 0.f), hp = f3(0.f, 0.f, 0.f);
+        const bool valid = shape == SHAPE_SPHERE || shape == SHAPE_BOX || shape == SHAPE_CAPSULE;
+        if (valid && n > 0 && wr >= 0 && wr < w.num_worlds) {
+            // the start box: the local bounds (symmetric about the origin) through |R|
+            const float3 hl = shape == SHAPE_SPHERE ? f3(sa.x, sa.x, sa.x)
+                              : shape == SHAPE_BOX  ? f3(sa.x, sa.y, sa.z)
+                                                    : f3(sa.x, sa.y + sa.x, sa.x);
+            const float3 ex = qrot(qA, f3(1.f, 0.f, 0.f)), ey = qrot(qA, f3(0.f, 1.f, 0.f)),
+                         ez = qrot(qA, f3(0.f, 0.f, 1.f));
+            const float3 half = f3(fabsf(ex.x) * hl.x + fabsf(ey.x) * hl.y + fabsf(ez.x) * hl.z,
+                                   fabsf(ex.y) * hl.x + fabsf(ey.y) * hl.y + fabsf(ez.y) * hl.z,
+                                   fabsf(ex.z) * hl.x + fabsf(ey.z) * hl.y + fabsf(ez.z) * hl.z);
+            const float clen = sqrtf(lensq3(disp));
+            const float3 cdir = clen > 0.f ? disp * (1.f / clen) : f3(0.f, 0.f, 0.f);
+            const Sup<float> supA0 = make_sup<float>(shape, sa, true, hv);
+            auto entry = [&](int node) {
+                return ray_box_entry(pA, cdir, clen, xyz(w.node_lo[node]) - half, xyz(w.node_hi[node]) + half);
+            };
+            int stack[CCD_STACK];
+            float sdist[CCD_STACK];
+            int sp = 0;
+            const float t_root = entry(0);
+            if (t_root < CUDART_INF_F) {
+                stack[sp] = 0;
+                sdist[sp++] = t_root;
+            }
+            while (sp > 0) {
+                --sp;
+                const int node = stack[sp];
+                if (sdist[sp] > best * clen + 2e-2f) continue;  // beyond the best hit by twice the mesh tolerance
+                const int2 nw = node_world[node];
+                if (wr < nw.x || wr > nw.y) continue;
+                if (node < n - 1) {
+                    const int2 ch = w.node_child[node];
+                    const float tl = entry(ch.x), tr = entry(ch.y);
+                    if (sp + 2 > CCD_STACK) {
+                        atomicOr(&w.ctr->overflow, OVF_SLOTS);
+                        continue;
+                    }
+                    const int far_n = tl <= tr ? ch.y : ch.x, near_n = tl <= tr ? ch.x : ch.y;
+                    const float far_t = fmaxf(tl, tr), near_t = fminf(tl, tr);
+                    if (far_t < CUDART_INF_F) {
+                        stack[sp] = far_n;
+                        sdist[sp++] = far_t;
+                    }
+                    if (near_t < CUDART_INF_F) {
+                        stack[sp] = near_n;
+                        sdist[sp++] = near_t;
+                    }
+                    continue;
+                }
+                const int b = w.order[node - (n - 1)];
+                if (w.world[b] != wr) continue;
+                const uint32_t fb = w.flags[b];
+                if (!(flt.layer_mask & (1u << layer_of(fb)))) continue;
+                const uint2 gb = w.groups[b];
+                if (!((flt.groups & gb.y) != 0u && (gb.x & flt.mask) != 0u)) continue;
+                auto collect = [&](float lambda, float3 paw, float3 axw) {
+                    if (!(lambda < best || (lambda == best && hit >= 0 && b < hit))) return;
+                    best = lambda;
+                    hit = b;
+                    hn = -normalize3(axw);
+                    hp = paw;
+                };
+                if (shape_of(fb) == SHAPE_MESH) {
+                    ccd_cast_mesh(w, fa, sa, pA, qA, disp, b, best, collect);
+                    continue;
+                }
+                const float3 pB = xyz(w.pos[b]);
+                const float4 qB = w.quat[b];
+                const Q<float> iqB{-qB.x, -qB.y, -qB.z, qB.w};
+                const V<float> posAInB = qrotS(iqB, V<float>{pA.x - pB.x, pA.y - pB.y, pA.z - pB.z});
+                const Q<float> qAInB = qmulS(iqB, Q<float>{qA.x, qA.y, qA.z, qA.w});
+                const V<float> dInB = qrotS(iqB, V<float>{disp.x, disp.y, disp.z});
+                Sup<float> supA = supA0;
+                set_transform(supA, qAInB, posAInB);
+                const Sup<float> supB = make_sup<float>(shape_of(fb), w.shape[b], true, hv);
+                const float max_l = (hit >= 0 && b < hit) ? nextafterf(best, CUDART_INF_F) : best;
+                float lambda;
+                V<float> cpa, cpb, ax;
+                if (!gjk_cast(lambda, cpa, cpb, ax, supA, supB, dInB, 1e-4f, supA.convex_radius, supB.convex_radius,
+                              max_l))
+                    continue;
+                // penetrationCastShape penetration.ts:693-698: a too short axis becomes the cast direction
+                if (lsq(ax) < 1e-4f * 1e-4f) ax = dInB;
+                if (lambda > 1.f || dot(ax, dInB) <= 0.f || lambda >= max_l) continue;
+                const Q<float> qBq{qB.x, qB.y, qB.z, qB.w};
+                const V<float> axw = qrotS(qBq, ax);
+                const V<float> paw = qrotS(qBq, cpa);
+                collect(lambda, f3(paw.x + pB.x, paw.y + pB.y, paw.z + pB.z), f3(axw.x, axw.y, axw.z));
+            }
+        }
+        DevShapeCastHit h;
+        h.body = hit;
+        h.fraction = hit >= 0 ? best : 1.f;
+        h.normal[0] = hn.x, h.normal[1] = hn.y, h.normal[2] = hn.z;
+        h.point[0] = hp.x, h.point[1] = hp.y, h.point[2] = hp.z;
+        hits[k] = h;
+    }
+}
+
+void launch_cast_shapes(DevWorld &w, const DevShapeCast *qs, int nq, const DevRayFilter &f, DevShapeCastHit *hits,
+                        cudaStream_t s) {
+    if (nq <= 0) return;
+    k_cast_shapes<<<grid_for(nq, 128, 16), 128, 0, s>>>(w, w.node_world, qs, nq, f, hits);
+}
+
 void launch_cast_rays(DevWorld &w, const DevRay *rays, const int *order, int nr, const DevRayFilter &f,
                       DevRayHit *hits, cudaStream_t s) {
     if (nr <= 0) return;

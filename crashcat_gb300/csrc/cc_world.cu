@@ -1040,6 +1040,40 @@ int cc_world_collide_points(cc_world *W, const cc_point *points, int32_t count, 
     return CC_OK;
 }
 
+static_assert(sizeof(cc_shape_cast) == sizeof(DevShapeCast) && sizeof(cc_shape_cast_hit) == sizeof(DevShapeCastHit),
+              "shape cast layouts");
+
+int cc_world_cast_shapes_device(cc_world *W, const cc_shape_cast *casts, int32_t count, const cc_query_filter *filter,
+                                cc_shape_cast_hit *hits) {
+    if (!W || count < 0 || !filter || (count > 0 && (!casts || !hits))) return CC_ERR_INVALID;
+    if (count == 0) return CC_OK;
+    if (int r = sync_shapes(W)) return r;
+    DevRayFilter flt{filter->object_layer_mask, filter->collision_group, filter->collision_mask, filter->flags};
+    launch_query_tree(W->w, W->stream);
+    launch_cast_shapes(W->w, (const DevShapeCast *)casts, count, flt, (DevShapeCastHit *)hits, W->stream);
+    return cuda_ok(cudaGetLastError());
+}
+
+int cc_world_cast_shapes(cc_world *W, const cc_shape_cast *casts, int32_t count, const cc_query_filter *filter,
+                         cc_shape_cast_hit *hits) {
+    if (!W || count < 0 || !filter || (count > 0 && (!casts || !hits))) return CC_ERR_INVALID;
+    for (int i = 0; i < count; i++) {
+        const int t = casts[i].shape_type;
+        if (t != CC_SHAPE_SPHERE && t != CC_SHAPE_BOX && t != CC_SHAPE_CAPSULE) return CC_ERR_INVALID;
+    }
+    if (count == 0) return CC_OK;
+    void *d = nullptr;
+    const size_t in_b = sizeof(cc_shape_cast) * (size_t)count, out_b = sizeof(cc_shape_cast_hit) * (size_t)count;
+    CC_TRY(cudaMallocAsync(&d, in_b + out_b, W->stream));
+    int r = cuda_ok(cudaMemcpyAsync(d, casts, in_b, cudaMemcpyHostToDevice, W->stream));
+    cc_shape_cast_hit *dh = (cc_shape_cast_hit *)((char *)d + in_b);
+    if (r == CC_OK) r = cc_world_cast_shapes_device(W, (const cc_shape_cast *)d, count, filter, dh);
+    if (r == CC_OK) r = cuda_ok(cudaMemcpyAsync(hits, dh, out_b, cudaMemcpyDeviceToHost, W->stream));
+    cudaFreeAsync(d, W->stream);
+    if (r == CC_OK) r = cuda_ok(cudaStreamSynchronize(W->stream));
+    return r;
+}
+
 int cc_world_cast_rays_device(cc_world *W, const cc_ray *rays, int32_t count, const cc_query_filter *filter,
                               cc_ray_hit *hits) {
     if (!W || count < 0 || !filter || (count > 0 && (!rays || !hits))) return CC_ERR_INVALID;

@@ -410,6 +410,17 @@ class GpuWorld:
               "cc_world_cast_rays")
         return hits
 
+    def cast_shapes(self, casts: np.ndarray, object_layer_mask: int = 0xFFFFFFFF, collision_group: int = 0xFFFFFFFF,
+                    collision_mask: int = 0xFFFFFFFF) -> np.ndarray:
+        """cc_world_cast_shapes: the closest hit of each shape cast (a _lib.SHAPE_CAST_DTYPE array)
+        as a _lib.SHAPE_CAST_HIT_DTYPE array."""
+        casts = np.ascontiguousarray(casts, dtype=_lib.SHAPE_CAST_DTYPE)
+        hits = np.zeros(len(casts), _lib.SHAPE_CAST_HIT_DTYPE)
+        f = _lib.QueryFilter(object_layer_mask, collision_group, collision_mask, 0)
+        check(self._lib.cc_world_cast_shapes(self.handle, casts.ctypes.data, len(casts), C.byref(f), hits.ctypes.data),
+              "cc_world_cast_shapes")
+        return hits
+
     def collide_points(self, points: np.ndarray, object_layer_mask: int = 0xFFFFFFFF,
                        collision_group: int = 0xFFFFFFFF, collision_mask: int = 0xFFFFFFFF,
                        collision_tolerance: float = 1e-4) -> np.ndarray:

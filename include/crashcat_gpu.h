@@ -477,6 +477,46 @@ int cc_world_cast_rays_device(cc_world *world, const cc_ray *rays, int32_t count
                               cc_ray_hit *hits);
 
 /* ---------------------------------------------------------------------------
+ * World shape casts: castShape (src/query.ts:196-214) with the closest-hit
+ * collector (ClosestCastShapeCollector, src/collision/cast-shape-vs-shape.ts:
+ * 199-217) and createDefaultCastShapeSettings (:116-127), a batch per call.
+ *
+ * A sphere, box or capsule (shape_params as cc_body_desc) at position and
+ * quaternion moves by displacement in its world.  Every body that passes the
+ * filter (flags unused) and that the swept box reaches (broadphase.castAABB)
+ * is cast with castShapeVsShape:
+ *   - a convex body: castConvexVsConvex (src/shapes/convex.ts:744-830);
+ *   - a mesh: the sphere's own cast or castConvexVsTriangleMesh.
+ * hit.body is the body index (-1: miss), hit.fraction the fraction of the
+ * displacement (1 on a miss), hit.normal the reference's hit normal (the
+ * penetration axis negated and normalised), hit.point the contact point on
+ * the cast shape, world space.  Equal fractions go to the lower body index.
+ * Other cast shapes: CC_ERR_INVALID.
+ *   cc_world_cast_shapes: host arrays; returns when the hits are written.
+ *   cc_world_cast_shapes_device: device arrays; queued on the world's stream.
+ * ------------------------------------------------------------------------- */
+typedef struct cc_shape_cast {
+    int32_t shape_type;     /* CC_SHAPE_SPHERE, CC_SHAPE_BOX or CC_SHAPE_CAPSULE */
+    float shape_params[4];  /* as cc_body_desc.shape_params */
+    float position[3];
+    float quaternion[4];    /* x, y, z, w */
+    float displacement[3];
+    int32_t world;
+} cc_shape_cast;
+
+typedef struct cc_shape_cast_hit {
+    int32_t body;
+    float fraction;
+    float normal[3];
+    float point[3];
+} cc_shape_cast_hit;
+
+int cc_world_cast_shapes(cc_world *world, const cc_shape_cast *casts, int32_t count, const cc_query_filter *filter,
+                         cc_shape_cast_hit *hits);
+int cc_world_cast_shapes_device(cc_world *world, const cc_shape_cast *casts, int32_t count,
+                                const cc_query_filter *filter, cc_shape_cast_hit *hits);
+
+/* ---------------------------------------------------------------------------
  * World point queries: collidePoint (src/query.ts:470-490) with every hit
  * collected (createAllCollidePointCollector), a batch of points per call.
  *

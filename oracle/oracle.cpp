@@ -2247,6 +2247,64 @@ void orc_collide_points(void *wp, const double *pts, int n, uint32_t layerMask, 
     }
 }
 
+// castShape query.ts:196-214 with the closest-hit collector (ClosestCastShapeCollector
+// cast-shape-vs-shape.ts:199-217) and the default cast settings (createDefaultCastShapeSettings
+// :116-127): each query (shape type, 4 shape params, position xyz, quaternion xyzw, displacement
+// xyz; 15 doubles) is cast against every body that passes the filter (a body out of reach of the
+// swept box cannot be hit, so this is the set broadphase.castAABB visits, less the misses) by
+// castShapeVsShape: castConvexVsConvex convex.ts:744-830, or for a mesh the sphere's own cast or
+// castConvexVsTriangleMesh.  Out per query: fraction, normal (-penetration axis, normalised),
+// contact point on the cast shape (7 doubles); the body (-1 on a miss).  Ties go to the lower
+// body index.
+int orc_cast_shapes(void *wp, const double *qs, int n, uint32_t layerMask, uint32_t groups, uint32_t mask,
+                    double *out, int *bodies) {
+    World &W = *(World *)wp;
+    for (int r = 0; r < n; r++) {
+        const double *q = qs + 15 * r;
+        double row[F_COUNT] = {};
+        row[F_SHAPE] = q[0];
+        row[F_DENSITY] = 1000.0;
+        for (int k = 0; k < 4; k++) row[F_P0 + k] = q[1 + k];
+        Shape sa;
+        if (!shape_from_row(sa, row, nullptr) || sa.type == SHAPE_TRIANGLE_MESH) return -1;
+        V3 pA{q[5], q[6], q[7]}, disp{q[12], q[13], q[14]};
+        Q4 qA{q[8], q[9], q[10], q[11]};
+        double best = 1.0 + 1e-4;  // INITIAL_EARLY_OUT_FRACTION cast-utils.ts:3
+        int hit = -1;
+        V3 hn{0, 0, 0}, hp{0, 0, 0};
+        for (auto &B : W.bodies) {
+            if (!((groups & B.mask) != 0 && (B.groups & mask) != 0)) continue;
+            if (!(layerMask & (1u << B.objectLayer))) continue;
+            auto collect = [&](double fraction, V3 pa, V3 axis) {
+                if (!(fraction < best || (fraction == best && hit >= 0 && B.index < hit))) return;
+                best = fraction;
+                hit = B.index;
+                hn = neg(normalize(axis));
+                hp = pa;
+            };
+            if (B.shape.type == SHAPE_TRIANGLE_MESH) {
+                auto onHit = [&](const CastMeshHit &h) { collect(h.fraction, h.pa, h.axis); };
+                auto earlyOut = [&]() { return best; };
+                if (sa.type == SHAPE_SPHERE)
+                    cast_sphere_vs_mesh(sa, pA, disp, B.shape, B.position, B.quat, onHit, earlyOut);
+                else
+                    cast_convex_vs_mesh(sa, pA, qA, disp, B.shape, B.position, B.quat, onHit, earlyOut);
+                continue;
+            }
+            CastHit h;
+            const double maxL = (hit >= 0 && B.index < hit) ? std::nextafter(best, 2.0) : best;
+            if (!cast_convex_vs_convex(h, sa, pA, qA, disp, B.shape, B.position, B.quat, maxL, false)) continue;
+            collect(h.fraction, h.pa, h.axis);
+        }
+        double *o = out + 7 * r;
+        o[0] = hit >= 0 ? best : 1.0;
+        o[1] = hn.x, o[2] = hn.y, o[3] = hn.z;
+        o[4] = hp.x, o[5] = hp.y, o[6] = hp.z;
+        bodies[r] = hit;
+    }
+    return 0;
+}
+
 // ---- unit-level entry points for the known-answer tests -------------------
 // Faces are passed as n vertices (xyz doubles).  Returns the output vertex count.
 int orc_clip_poly_vs_plane(const double *poly, int n, const double *origin, const double *normal, double *out) {

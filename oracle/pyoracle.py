@@ -49,6 +49,7 @@ def load():
         "orc_island_count": ([vp], i32),
         "orc_ccd_counts": ([vp, ip], None),
         "orc_collide_points": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double, ip, ip, vp], None),
+        "orc_cast_shapes": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, dp, ip], i32),
         "orc_cast_rays": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, i32, dp, ip, vp], None),
         "orc_add_mesh": ([vp, i32, dp, i32, C.c_void_p, i32, dp], i32),
         "orc_get_manifold_subs": ([vp, C.c_void_p], i32),
@@ -259,6 +260,19 @@ class OracleWorld:
         self.lib.orc_collide_points(self.h, dptr(pts), n, layer_mask, groups, mask, tolerance, iptr(co), iptr(bo),
                                     su.ctypes.data)
         return co[:n], bo[:n], su[:n]
+
+    def cast_shapes(self, queries: np.ndarray, layer_mask: int = 0xFFFFFFFF, groups: int = 0xFFFFFFFF,
+                    mask: int = 0xFFFFFFFF):
+        """Closest hit of each shape cast (shape type, 4 params, position xyz, quaternion xyzw,
+        displacement xyz): (fraction, normal xyz, point on the cast shape xyz) rows and the
+        body hit (-1 on a miss)."""
+        q = np.ascontiguousarray(queries, dtype=np.float64).reshape(-1, 15)
+        n = q.shape[0]
+        out = np.zeros((max(n, 1), 7), dtype=np.float64)
+        bo = np.zeros(max(n, 1), dtype=np.int32)
+        if self.lib.orc_cast_shapes(self.h, dptr(q), n, layer_mask, groups, mask, dptr(out), iptr(bo)) != 0:
+            raise ValueError("orc_cast_shapes: a cast shape must be a sphere, box or capsule")
+        return out[:n], bo[:n]
 
     def aabbs(self) -> np.ndarray:
         o = np.zeros((self.n, 6), dtype=np.float64)

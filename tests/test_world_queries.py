@@ -399,3 +399,107 @@ def test_gpu_points_in_terrain_pile(gpu_lib, oracle_lib, seed):
     assert (co > 0).mean() > 0.25 and (bo == 0).sum() > 300 and (co > 1).sum() > 0
     mesh = (bo == 0) & (h["body"] == 0)
     assert (h["sub_shape_id"][mesh] == su[mesh]).mean() >= 0.99
+
+
+# ---------------------------------------------------------------------------
+# castShape (query.ts:196-214) with the closest-hit collector and the default cast settings
+# ---------------------------------------------------------------------------
+SHAPE_IDS = {"sphere": _lib.SHAPE_SPHERE, "box": _lib.SHAPE_BOX, "capsule": _lib.SHAPE_CAPSULE}
+
+
+def cast_row(kind, params, pos, disp, q=(0.0, 0.0, 0.0, 1.0)):
+    p = list(params) + [0.0] * (4 - len(params))
+    return [SHAPE_IDS[kind], *p, *pos, *q, *disp]
+
+
+def cast_array(rows, worlds=None):
+    rows = np.asarray(rows, np.float64).reshape(-1, 15)
+    c = np.zeros(len(rows), _lib.SHAPE_CAST_DTYPE)
+    c["shape_type"] = rows[:, 0].astype(np.int32)
+    c["shape_params"], c["position"] = rows[:, 1:5], rows[:, 5:8]
+    c["quaternion"], c["displacement"] = rows[:, 8:12], rows[:, 12:15]
+    c["world"] = 0 if worlds is None else worlds
+    return c
+
+
+# (name, cast kind, params, start, displacement, expected fraction or None): tst/query.test.ts's
+# sphere sweeps against a unit box at the origin, and a box and a capsule swept the same way
+SHAPE_CAST_CASES = [
+    ("query_sphere_hits_box", "sphere", (0.5,), (-3, 0, 0), (6, 0, 0), 1.5 / 6),
+    ("query_sphere_misses_box", "sphere", (0.5,), (-5, 5, 0), (10, 0, 0), None),
+    ("box_hits_box", "box", (0.5, 0.5, 0.5, 0.05), (-4, 0, 0), (8, 0, 0), 2.5 / 8),
+    ("capsule_hits_box_from_above", "capsule", (0.3, 0.5), (0, 5, 0), (0, -8, 0), 3.2 / 8),
+    ("sphere_moving_away", "sphere", (0.5,), (-3, 0, 0), (-6, 0, 0), None),
+]
+
+
+@pytest.mark.parametrize("case", SHAPE_CAST_CASES, ids=[c[0] for c in SHAPE_CAST_CASES])
+def test_oracle_shape_cast_known_answers(oracle_lib, case):
+    _, kind, params, start, disp, want = case
+    o = oracle_single(one_body("box"))
+    out, bo = o.cast_shapes(np.array([cast_row(kind, params, start, disp)]))
+    if want is None:
+        assert bo[0] == -1
+        return
+    assert bo[0] == 0
+    assert abs(out[0, 0] - want) < 2e-3 / np.linalg.norm(disp) + 1e-9, (out[0, 0], want)
+    d = np.asarray(disp, np.float64) / np.linalg.norm(disp)
+    np.testing.assert_allclose(out[0, 1:4], -d, atol=1e-3)  # the normal faces the cast back
+
+
+@pytest.mark.gpu
+def test_gpu_shape_cast_known_answers(gpu_lib, oracle_lib):
+    for _, kind, params, start, disp, want in SHAPE_CAST_CASES:
+        g = world.GpuWorld(world.standard_settings(), 4)
+        g.add_bodies(one_body("box"))
+        h = g.cast_shapes(cast_array([cast_row(kind, params, start, disp)]))
+        if want is None:
+            assert h["body"][0] == -1, kind
+            continue
+        assert h["body"][0] == 0, kind
+        assert abs(float(h["fraction"][0]) - want) < 3e-3 / np.linalg.norm(disp), (kind, h["fraction"][0], want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", [5, 6])
+def test_gpu_shape_casts_through_terrain_pile(gpu_lib, oracle_lib, seed):
+    """Spheres, boxes and capsules swept down through a terrain pile, against the oracle at the
+    same poses: the same body for at least 97 % of casts (FP32 and the casts' own tolerances,
+    1e-4 m convex and 1e-2 m mesh, decide near-ties); where the bodies agree, 99 % of the hit
+    distances within 2e-3 m and all within 0.1 m (a grazing cast can converge on another face in
+    FP32: one cast of 1,024 was 0.07 m off)."""
+    sc = scenes.mesh_drop(n=120, n_cells=16, seed=seed, heights=(0.0, 3.0))
+    ws = world.standard_settings()
+    g = world.GpuWorld(ws, sc.n + 16)
+    for p in sc.hull_points or ():
+        g.add_convex_hull(p)
+    g.add_triangle_mesh(*sc.mesh)
+    g.add_bodies(sc.bodies)
+    hulls = [g.get_convex_hull(i) for i in range(len(sc.hull_points or ()))]
+    o = pyoracle.OracleWorld(ws, sc.bodies, hulls, [g.get_triangle_mesh(0)])
+    g.step(sc.dt, 30)
+    rows, _ = g.get_state()
+    st = o.state()
+    st[:, 0:13] = rows[:, 0:13]
+    o.set_state(st)
+    rng = np.random.default_rng(seed)
+    n = 1024
+    kinds = rng.integers(0, 3, n)
+    params = np.zeros((n, 4))
+    params[kinds == 0, 0] = rng.uniform(0.1, 0.4, (kinds == 0).sum())
+    params[kinds == 1, 0:3] = rng.uniform(0.1, 0.4, ((kinds == 1).sum(), 3))
+    params[kinds == 1, 3] = 0.05
+    params[kinds == 2, 0:2] = rng.uniform(0.1, 0.3, ((kinds == 2).sum(), 2))
+    start = np.stack([rng.uniform(-6, 6, n), rng.uniform(7, 10, n), rng.uniform(-6, 6, n)], 1)
+    disp = np.stack([rng.uniform(-2, 2, n), rng.uniform(-14, -10, n), rng.uniform(-2, 2, n)], 1)
+    q = scenes.random_quaternions(rng, n)
+    rows_ = np.concatenate([kinds[:, None], params, start, q, disp], 1)
+    h = g.cast_shapes(cast_array(rows_))
+    out, bo = o.cast_shapes(rows_)
+    same = h["body"] == bo
+    assert same.mean() >= 0.97, same.mean()
+    assert (bo >= 0).mean() > 0.9 and (bo == 0).sum() > 100 and (bo > 0).sum() > 50
+    hit = same & (bo >= 0)
+    lens = np.linalg.norm(disp, axis=1)
+    err = np.abs((h["fraction"][hit] - out[hit, 0]) * lens[hit])
+    assert np.quantile(err, 0.99) < 2e-3 and err.max() < 0.1, (np.quantile(err, 0.99), err.max())
