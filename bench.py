@@ -490,6 +490,61 @@ def ray_profile(steps: int = 60, rays: int = 1 << 20, reps: int = 3):
     print(json.dumps(q))
 
 
+def terrain_casts(n: int, half: float, seed: int = 4) -> np.ndarray:
+    """Spheres, boxes and capsules (0.1-0.4 m) at random orientations, starting 20-50 m above the
+    terrain and swept 40-60 m down with up to 5 m of drift: a cc_shape_cast array."""
+    from crashcat_gb300 import _lib, scenes
+    rng = np.random.default_rng(seed)
+    c = np.zeros(n, _lib.SHAPE_CAST_DTYPE)
+    kinds = rng.integers(0, 3, n)
+    c["shape_type"] = kinds
+    p = np.zeros((n, 4), np.float32)
+    p[kinds == 0, 0] = rng.uniform(0.1, 0.4, (kinds == 0).sum())
+    p[kinds == 1, 0:3] = rng.uniform(0.1, 0.4, ((kinds == 1).sum(), 3))
+    p[kinds == 1, 3] = 0.05
+    p[kinds == 2, 0:2] = rng.uniform(0.1, 0.3, ((kinds == 2).sum(), 2))
+    c["shape_params"] = p
+    c["position"] = np.stack([rng.uniform(-half, half, n), rng.uniform(20.0, 50.0, n), rng.uniform(-half, half, n)], 1)
+    c["quaternion"] = scenes.random_quaternions(rng, n)
+    c["displacement"] = np.stack([rng.uniform(-5, 5, n), rng.uniform(-60, -40, n), rng.uniform(-5, 5, n)], 1)
+    return c
+
+
+def shape_cast_measurement(g, casts, reps: int = 10):
+    """Closest-hit castShape of every sweep (cc_world_cast_shapes_device on resident buffers,
+    the query tree rebuilt first), and through cc_world_cast_shapes with host arrays."""
+    import ctypes as C
+    import torch
+    from crashcat_gb300 import _lib
+    n = len(casts)
+    d_in = torch.from_numpy(casts.view(np.uint8).copy()).cuda()
+    d_out = torch.empty(n * _lib.SHAPE_CAST_HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    f = _lib.QueryFilter(0xFFFFFFFF, 0xFFFFFFFF, 0xFFFFFFFF, 0)
+
+    def call():
+        _lib.check(g._lib.cc_world_cast_shapes_device(g.handle, d_in.data_ptr(), n, C.byref(f), d_out.data_ptr()),
+                   "cc_world_cast_shapes_device")
+
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        call()
+    torch.cuda.synchronize()
+    dev_s = (time.perf_counter() - t0) / reps
+    hits = d_out.cpu().numpy().view(_lib.SHAPE_CAST_HIT_DTYPE)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        h2 = g.cast_shapes(casts)
+    e2e_s = (time.perf_counter() - t0) / 3
+    return {"casts": n, "value": n / dev_s, "unit": "casts/s", "ms_per_batch": dev_s * 1e3,
+            "e2e": {"value": n / e2e_s, "unit": "casts/s", "h2d_bytes_per_step": int(casts.nbytes),
+                    "d2h_bytes_per_step": int(h2.nbytes)},
+            "hit_fraction": float((hits["body"] >= 0).mean()), "terrain_hits": float((hits["body"] == 0).mean()),
+            "device_equals_host_api": bool((h2["body"] == hits["body"]).all()), "_bodies": hits["body"].copy()}
+
+
 def terrain_measurement(cpu_seconds: float = 8.0):
     """The mixed-shape terrain workload: 20,000 bodies (spheres, boxes, capsules and convex hulls
     of 16-32 points in the mixed pile's size ranges) dropped from 5-40 m over a 256 x 256-cell
@@ -520,6 +575,8 @@ def terrain_measurement(cpu_seconds: float = 8.0):
     mesh = g.get_triangle_mesh(0)
     rays = terrain_rays(1 << 20, 0.4 * 256)
     queries = ray_query_measurement(g, rays)
+    casts = terrain_casts(1 << 16, 0.4 * 256)
+    sweeps = shape_cast_measurement(g, casts)
     del g
     obuild.build()
     o = pyoracle.OracleWorld(ws, sc.bodies, hulls, [mesh])
@@ -534,6 +591,16 @@ def terrain_measurement(cpu_seconds: float = 8.0):
     queries["cpu_baseline"] = {"value": len(sample) / ray_cpu_s, "unit": "rays/s", "cores": 1, "kind": "port",
                                "sample": "first 2,000 of the rays, brute force over the bodies"}
     queries["sample_same_body"] = float((queries.pop("_bodies")[:len(sample)] == obo).mean())
+    # the oracle's castShape on a sample of the same sweeps
+    cs = casts[:100]
+    crow = np.concatenate([cs["shape_type"][:, None], cs["shape_params"], cs["position"], cs["quaternion"],
+                           cs["displacement"]], 1).astype(np.float64)
+    t0 = time.perf_counter()
+    _, cbo = o.cast_shapes(crow)
+    cast_cpu_s = time.perf_counter() - t0
+    sweeps["cpu_baseline"] = {"value": len(cs) / cast_cpu_s, "unit": "casts/s", "cores": 1, "kind": "port",
+                              "sample": "first 100 of the sweeps, every body cast"}
+    sweeps["sample_same_body"] = float((sweeps.pop("_bodies")[:len(cs)] == cbo).mean())
     o = pyoracle.OracleWorld(ws, sc.bodies, hulls, [mesh])
     t0, k = time.perf_counter(), 0
     while time.perf_counter() - t0 < cpu_seconds and k < 100:
@@ -547,6 +614,7 @@ def terrain_measurement(cpu_seconds: float = 8.0):
             "finite": bool(np.isfinite(rows).all()),
             "below_terrain": int((rows[1:, 1] < -2.5).sum()),
             "ray_queries": queries,
+            "shape_casts": sweeps,
             "cpu_baseline": {"value": (sc.n - 1) * k / cpu_s, "unit": METRIC, "cores": 1, "kind": "port",
                              "sample": f"first {k} steps from spawn (falling phase)",
                              "gpu_same_phase_value": (sc.n - 1) / (phases[0]["ms_per_step"] * 1e-3)}}
