@@ -474,8 +474,9 @@ def ray_query_measurement(g, rays, reps: int = 10):
 
 
 def ray_profile(steps: int = 60, rays: int = 1 << 20, reps: int = 3):
-    """The terrain workload's ray queries alone, for a profiler: the scene stepped `steps` times,
-    then `reps` batches of `rays` closest-hit rays on resident buffers.  Prints one JSON line."""
+    """The terrain workload's queries alone, for a profiler: the scene stepped `steps` times, then
+    `reps` batches of `rays` closest-hit rays and of 65,536 shape casts on resident buffers.
+    Prints one JSON line."""
     from crashcat_gb300 import scenes, world as W
     sc = scenes.mesh_drop(n=20000, n_cells=256, seed=2, amplitude=4.0, heights=(5.0, 40.0), fast_fraction=0.2)
     g = W.GpuWorld(W.standard_settings(velocity_iterations=8, position_iterations=2), sc.n + 16)
@@ -487,7 +488,9 @@ def ray_profile(steps: int = 60, rays: int = 1 << 20, reps: int = 3):
         g.step(sc.dt, steps)
     q = ray_query_measurement(g, terrain_rays(rays, 0.4 * 256), reps=reps)
     q.pop("_bodies")
-    print(json.dumps(q))
+    c = shape_cast_measurement(g, terrain_casts(1 << 16, 0.4 * 256), reps=reps)
+    c.pop("_bodies")
+    print(json.dumps({"ray_queries": q, "shape_casts": c}))
 
 
 def terrain_casts(n: int, half: float, seed: int = 4) -> np.ndarray:

@@ -3321,6 +3321,9 @@ void launch_collide_points(DevWorld &w, const float4 *pts, int np, const DevRayF
 // skipped; castShapeVsShape per body: castConvexVsConvexLocal convex.ts:744-830 (EXCLUDE supports,
 // tolerance 1e-4, back faces dropped), or for a mesh the sphere's own cast or
 // castConvexVsTriangleMesh (ccd_cast_mesh, the same default settings).
+// PASS 0 casts every body; with meshes present PASS 1 casts the meshes and PASS 2 the convex
+// bodies from PASS 1's hits, as the ray queries do.
+template <int PASS>
 __global__ void __launch_bounds__(128) k_cast_shapes(DevWorld w, const int2 *node_world, const DevShapeCast *qs,
                                                      int nq, DevRayFilter flt, DevShapeCastHit *hits) {
     const int n = w.n;
@@ -3337,6 +3340,15 @@ __global__ void __launch_bounds__(128) k_cast_shapes(DevWorld w, const int2 *nod
         float best = 1.f + 1e-4f;  // INITIAL_EARLY_OUT_FRACTION cast-utils.ts:3
         int hit = -1;
         float3 hn = f3(0.f, 0.f, 0.f), hp = f3(0.f, 0.f, 0.f);
+        if (PASS == 2) {
+            const DevShapeCastHit h0 = hits[k];
+            if (h0.body >= 0) {
+                hit = h0.body;
+                best = h0.fraction;
+                hn = f3(h0.normal[0], h0.normal[1], h0.normal[2]);
+                hp = f3(h0.point[0], h0.point[1], h0.point[2]);
+            }
+        }
         const bool valid = shape == SHAPE_SPHERE || shape == SHAPE_BOX || shape == SHAPE_CAPSULE;
         if (valid && n > 0 && wr >= 0 && wr < w.num_worlds) {
             // the start box: the local bounds (symmetric about the origin) through |R|
@@ -3401,9 +3413,10 @@ __global__ void __launch_bounds__(128) k_cast_shapes(DevWorld w, const int2 *nod
                     hp = paw;
                 };
                 if (shape_of(fb) == SHAPE_MESH) {
-                    ccd_cast_mesh(w, fa, sa, pA, qA, disp, b, best, collect);
+                    if (PASS != 2) ccd_cast_mesh(w, fa, sa, pA, qA, disp, b, best, collect);
                     continue;
                 }
+                if (PASS == 1) continue;
                 const float3 pB = xyz(w.pos[b]);
                 const float4 qB = w.quat[b];
                 const Q<float> iqB{-qB.x, -qB.y, -qB.z, qB.w};
@@ -3440,7 +3453,12 @@ __global__ void __launch_bounds__(128) k_cast_shapes(DevWorld w, const int2 *nod
 void launch_cast_shapes(DevWorld &w, const DevShapeCast *qs, int nq, const DevRayFilter &f, DevShapeCastHit *hits,
                         cudaStream_t s) {
     if (nq <= 0) return;
-    k_cast_shapes<<<grid_for(nq, 128, 16), 128, 0, s>>>(w, w.node_world, qs, nq, f, hits);
+    if (w.num_mesh_bodies > 0) {
+        k_cast_shapes<1><<<grid_for(nq, 128, 16), 128, 0, s>>>(w, w.node_world, qs, nq, f, hits);
+        k_cast_shapes<2><<<grid_for(nq, 128, 16), 128, 0, s>>>(w, w.node_world, qs, nq, f, hits);
+    } else {
+        k_cast_shapes<0><<<grid_for(nq, 128, 16), 128, 0, s>>>(w, w.node_world, qs, nq, f, hits);
+    }
 }
 
 void launch_cast_rays(DevWorld &w, const DevRay *rays, const int *order, int nr, const DevRayFilter &f,
