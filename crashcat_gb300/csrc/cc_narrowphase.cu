@@ -3324,7 +3324,7 @@ void launch_collide_points(DevWorld &w, const float4 *pts, int np, const DevRayF
 // PASS 0 casts every body; with meshes present PASS 1 casts the meshes and PASS 2 the convex
 // bodies from PASS 1's hits, as the ray queries do.
 template <int PASS>
-__global__ void __launch_bounds__(128) k_cast_shapes(DevWorld w, const int2 *node_world, const DevShapeCast *qs,
+__global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *node_world, const DevShapeCast *qs,
                                                      int nq, DevRayFilter flt, DevShapeCastHit *hits) {
     const int n = w.n;
     const HullView hv = hull_view(w);
