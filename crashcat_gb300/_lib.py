@@ -129,6 +129,22 @@ BODY_DTYPE = np.dtype([
 ])
 MOTION_DISCRETE, MOTION_LINEAR_CAST = 0, 1
 
+# cc_world_step_taped: the rows of one step's velocity solve (cc_tape_body / cc_tape_contact)
+TAPE_DYNAMIC, TAPE_MOVING = 1, 2
+TAPE_BODY_DTYPE = np.dtype([("linear_velocity", np.float32, 3), ("angular_velocity", np.float32, 3),
+                            ("inv_inertia", np.float32, 6), ("inv_mass", np.float32), ("flags", np.uint32)])
+TAPE_POINT_DTYPE = np.dtype([("r_a", np.float32, 3), ("r_b", np.float32, 3), ("eff_normal", np.float32),
+                             ("eff_tangent1", np.float32), ("eff_tangent2", np.float32), ("bias_normal", np.float32),
+                             ("lambda_normal", np.float32), ("lambda_tangent1", np.float32),
+                             ("lambda_tangent2", np.float32), ("final_normal", np.float32),
+                             ("final_tangent1", np.float32), ("final_tangent2", np.float32),
+                             ("prev_point", np.int32)])
+TAPE_CONTACT_DTYPE = np.dtype([("body_a", np.int32), ("body_b", np.int32), ("num_points", np.int32),
+                               ("island", np.int32), ("has_prev", np.int32), ("sort_key", np.uint32),
+                               ("normal", np.float32, 3), ("tangent1", np.float32, 3), ("tangent2", np.float32, 3),
+                               ("friction", np.float32), ("inv_mass_a", np.float32), ("inv_mass_b", np.float32),
+                               ("points", TAPE_POINT_DTYPE, 4)])
+
 EXPORTS = {
     "cc_world_settings_default": ([C.POINTER(Settings)], C.c_int),
     "cc_world_create": ([C.POINTER(Settings), C.POINTER(C.c_void_p)], C.c_int),
@@ -147,6 +163,8 @@ EXPORTS = {
     "cc_world_profile_steps": ([C.c_void_p, C.c_float, C.c_int32, C.c_void_p, C.c_int32], C.c_int),
     "cc_world_rollout_grad": ([C.c_void_p, C.c_float, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_void_p], C.c_int),
+    "cc_world_step_taped": ([C.c_void_p, C.c_float, C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32),
+                             C.POINTER(C.c_float)], C.c_int),
     "cc_penetration_static": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_float, C.c_float, C.c_void_p], C.c_int),
     "cc_world_add_hinges": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
     "cc_world_add_triangle_mesh": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_double, C.c_double,
@@ -250,6 +268,7 @@ def swing_twist_defaults(n: int) -> np.ndarray:
 # cc_penetration_static limits and record layouts (numpy mirrors of the C structs)
 STATIC_MAX_QUERIES = 32768
 STATIC_EPA_SLOTS = 304
+PENETRATION_UNSUPPORTED = -CC_ERR_UNSUPPORTED  # cc_penetration_result.hit of a shape type the query cannot take
 SHAPE_POSE_DTYPE = np.dtype([("shape_type", np.int32), ("shape_params", np.float32, 4),
                              ("position", np.float32, 3), ("quaternion", np.float32, 4)])
 PEN_QUERY_DTYPE = np.dtype([("a", SHAPE_POSE_DTYPE), ("b", SHAPE_POSE_DTYPE), ("max_separation", np.float32)])

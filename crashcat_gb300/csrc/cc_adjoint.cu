@@ -102,6 +102,96 @@ void launch_tape_record(DevWorld &w, TapeStep &t, cudaStream_t s) {
     k_tape_record<<<grid_for(nmax, 256), 256, 0, s>>>(w, t);
 }
 
+// The tape of a finished step in the layout of cc_tape_body / cc_tape_contact
+// (cc_world_step_taped): the rows as the velocity solve found them, and the final impulses
+// that the solve stored into this step's cache record (storeAppliedImpulses,
+// contact-constraints.ts:1061-1076).  A manifold without a constraint gets body_a = -1.
+__global__ void k_tape_export(DevWorld w, TapeStep t, cc_tape_body *bodies, cc_tape_contact *cons) {
+    const int nm = t.counts[0];
+    const CacheRecord *recs = w.cache_recs[*w.cache_parity];
+    int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    for (int i = tid; i < w.n; i += stride) {
+        uint32_t f = t.flags[i];
+        cc_tape_body b;
+        float4 v = t.v[i], a = t.w[i];
+        b.linear_velocity[0] = v.x;
+        b.linear_velocity[1] = v.y;
+        b.linear_velocity[2] = v.z;
+        b.angular_velocity[0] = a.x;
+        b.angular_velocity[1] = a.y;
+        b.angular_velocity[2] = a.z;
+        const bool dyn = motion_of(f) == DYNAMIC && !sleeping_of(f);
+        Sym3 I{0, 0, 0, 0, 0, 0};
+        if (dyn) I = world_inv_inertia(t.q[i], w.inertia_rot[i], xyz(w.inv_inertia[i]), dof_of(f));
+        b.inv_inertia[0] = I.xx;
+        b.inv_inertia[1] = I.xy;
+        b.inv_inertia[2] = I.xz;
+        b.inv_inertia[3] = I.yy;
+        b.inv_inertia[4] = I.yz;
+        b.inv_inertia[5] = I.zz;
+        b.inv_mass = w.inv_inertia[i].w;
+        b.flags = (dyn ? (uint32_t)CC_TAPE_DYNAMIC : 0u) | (motion_of(f) != STATIC ? (uint32_t)CC_TAPE_MOVING : 0u) |
+                  ((uint32_t)dof_of(f) << 8);
+        bodies[i] = b;
+    }
+    for (int i = tid; i < nm; i += stride) {
+        cc_tape_contact o;
+        int ci = t.valid[i];
+        if (ci < 0) {
+            o.body_a = o.body_b = -1;
+            o.num_points = 0;
+            cons[i] = o;
+            continue;
+        }
+        const ContactConstraint &c = t.cons[ci];
+        const CacheRecord &r = recs[c.cache_slot];
+        o.body_a = c.a;
+        o.body_b = c.b;
+        o.num_points = c.n;
+        o.island = c.island;
+        o.has_prev = c.pad0 >= 0 ? 1 : 0;
+        o.sort_key = c.sort_key;
+        const float3 ax[3] = {c.normal, c.t1, c.t2};
+        float *dst[3] = {o.normal, o.tangent1, o.tangent2};
+        for (int k = 0; k < 3; k++) {
+            dst[k][0] = ax[k].x;
+            dst[k][1] = ax[k].y;
+            dst[k][2] = ax[k].z;
+        }
+        o.friction = c.friction;
+        o.inv_mass_a = c.invMassA;
+        o.inv_mass_b = c.invMassB;
+        for (int q = 0; q < 4; q++) {
+            cc_tape_point &op = o.points[q];
+            const ContactPoint &p = c.p[q < c.n ? q : 0];
+            op.r_a[0] = p.rA.x;
+            op.r_a[1] = p.rA.y;
+            op.r_a[2] = p.rA.z;
+            op.r_b[0] = p.rB.x;
+            op.r_b[1] = p.rB.y;
+            op.r_b[2] = p.rB.z;
+            op.eff_normal = p.eff_n;
+            op.eff_tangent1 = p.eff_t1;
+            op.eff_tangent2 = p.eff_t2;
+            op.bias_normal = p.bias_n;
+            op.lambda_normal = p.lam_n;
+            op.lambda_tangent1 = p.lam_t1;
+            op.lambda_tangent2 = p.lam_t2;
+            const int k = q < c.n ? q : 0;
+            op.final_normal = r.ln[k];
+            op.final_tangent1 = r.lt1[k];
+            op.final_tangent2 = r.lt2[k];
+            op.prev_point = q < c.n ? __float_as_int(p.pad) : -1;
+        }
+        cons[i] = o;
+    }
+}
+
+void launch_tape_export(DevWorld &w, TapeStep &t, cc_tape_body *bodies, cc_tape_contact *cons, cudaStream_t s) {
+    int nmax = w.max_manifolds > w.n ? w.max_manifolds : w.n;
+    k_tape_export<<<grid_for(nmax, 256), 256, 0, s>>>(w, t, bodies, cons);
+}
+
 // ---------------------------------------------------------------------------
 // checkpoints: body state plus the cache table the next step reads (the current parity)
 // ---------------------------------------------------------------------------

@@ -569,11 +569,12 @@ __device__ inline Sym3 world_inv_inertia(float4 q, float4 inertia_rot, float3 d,
     return s;
 }
 
-// grid sizing: 152 SMs on GB300
-constexpr int NUM_SMS = 152;
+// grid sizing: multiples of the current device's SM count (152 on GB300), read once per
+// device with cudaDevAttrMultiProcessorCount
+int device_sm_count();
 inline int grid_for(int n, int block, int max_blocks_per_sm = 8) {
     int g = (n + block - 1) / block;
-    int cap = NUM_SMS * max_blocks_per_sm;
+    int cap = device_sm_count() * max_blocks_per_sm;
     if (g > cap) g = cap;
     if (g < 1) g = 1;
     return g;
@@ -649,6 +650,7 @@ void launch_cache_begin(DevWorld &w, cudaStream_t s);
 size_t epa_scratch_bytes();
 void upload_settings_adjoint(const DevSettings &s, cudaStream_t st);
 void launch_tape_record(DevWorld &w, TapeStep &t, cudaStream_t s);
+void launch_tape_export(DevWorld &w, TapeStep &t, cc_tape_body *bodies, cc_tape_contact *cons, cudaStream_t s);
 void checkpoint_save(const DevWorld &w, Checkpoint &c, cudaStream_t s);
 void checkpoint_restore(DevWorld &w, const Checkpoint &c, cudaStream_t s);
 void launch_rollout_loss(const DevWorld &w, const float *targets, float4 *sums, float *loss, AdjBuffers &a,
@@ -657,8 +659,8 @@ void launch_adjoint_step(DevWorld &w, TapeStep &t, AdjBuffers &a, float dt, floa
                          const AdjHandoff &out, cudaStream_t s);
 size_t epa_packed_block_bytes();
 size_t epa_item_bytes();
-constexpr int EPA_DEFAULT_MAX_THREADS = NUM_SMS * 4 * 64;  // one EPA polytope per resident EPA thread
-constexpr int EPA_MAX_THREADS = NUM_SMS * 8 * 64;          // upper bound of the launch-shape override
+inline int epa_default_max_threads() { return device_sm_count() * 4 * 64; }  // one polytope per resident EPA thread
+inline int epa_max_threads() { return device_sm_count() * 8 * 64; }          // upper bound of the launch-shape override
 constexpr int EPA_BIG_THREADS = 1024;  // threads of the fallback pass with the reference's polytope limits
 constexpr int JOINT_PARTNERS = 8;      // joined bodies remembered per body for the broadphase pair filter
 constexpr int GIANT_COLOURS = 1024;    // colours of the giant-island solve; the rest go to one thread in order

@@ -2381,9 +2381,9 @@ __global__ void __launch_bounds__(64) k_mesh_narrowphase(DevWorld w, EpaItem *ep
 void launch_mesh_narrowphase(DevWorld &w, int pass, cudaStream_t s) {
     EpaItem *items = (EpaItem *)w.epa_items;
     if (pass == 0)
-        k_mesh_narrowphase<0><<<NUM_SMS * 4, 64, 0, s>>>(w, items);
+        k_mesh_narrowphase<0><<<device_sm_count() * 4, 64, 0, s>>>(w, items);
     else
-        k_mesh_narrowphase<1><<<NUM_SMS * 4, 64, 0, s>>>(w, items);
+        k_mesh_narrowphase<1><<<device_sm_count() * 4, 64, 0, s>>>(w, items);
 }
 
 // ---------------------------------------------------------------------------
@@ -3476,8 +3476,8 @@ void launch_mesh_narrowphase(DevWorld &w, int pass, cudaStream_t s);
 
 void launch_narrowphase(DevWorld &w, float, cudaStream_t s, cudaEvent_t mid) {
     EpaItem *items = (EpaItem *)w.epa_items;
-    k_narrowphase<false><<<NUM_SMS * 8, 128, 0, s>>>(w, items);
-    if (w.num_hulls > 0) k_narrowphase<true><<<NUM_SMS * 8, 128, 0, s>>>(w, items);
+    k_narrowphase<false><<<device_sm_count() * 8, 128, 0, s>>>(w, items);
+    if (w.num_hulls > 0) k_narrowphase<true><<<device_sm_count() * 8, 128, 0, s>>>(w, items);
     if (w.num_mesh_bodies > 0) launch_mesh_narrowphase(w, 0, s);
     if (mid) cudaEventRecord(mid, s);
     if (w.num_hulls > 0) {
@@ -3491,8 +3491,8 @@ void launch_narrowphase(DevWorld &w, float, cudaStream_t s, cudaEvent_t mid) {
         k_epa_big<false><<<EPA_BIG_THREADS / EPA_BLOCK, EPA_BLOCK, 0, s>>>(w, items, (EpaScratch *)w.epa_scratch,
                                                                            w.epa_fallback);
     }
-    k_epa_emit<false><<<NUM_SMS * 8, 128, 0, s>>>(w, items);
-    if (w.num_hulls > 0) k_epa_emit<true><<<NUM_SMS * 8, 128, 0, s>>>(w, items);
+    k_epa_emit<false><<<device_sm_count() * 8, 128, 0, s>>>(w, items);
+    if (w.num_hulls > 0) k_epa_emit<true><<<device_sm_count() * 8, 128, 0, s>>>(w, items);
     if (w.num_mesh_bodies > 0) {
         k_epa_mesh<<<EPA_BIG_THREADS / EPA_BLOCK, EPA_BLOCK, 0, s>>>(w, items, (EpaScratch *)w.epa_scratch);
         launch_mesh_narrowphase(w, 1, s);
@@ -3556,7 +3556,9 @@ __global__ void __launch_bounds__(128) k_static_gjk(const cc_penetration_query *
     int sha = qy.a.shape_type, shb = qy.b.shape_type;
     float maxSep = qy.max_separation;
     if (sha < SHAPE_SPHERE || sha > SHAPE_CAPSULE || shb < SHAPE_SPHERE || shb > SHAPE_CAPSULE) {
-        res[i] = r;  // unknown shape type: reported as no hit
+        // hulls and meshes keep their data in a world, and other values name no shape
+        r.hit = CC_PENETRATION_UNSUPPORTED;
+        res[i] = r;
         return;
     }
     if (sha == SHAPE_SPHERE && shb == SHAPE_SPHERE) {

@@ -6,6 +6,20 @@
 
 namespace cc {
 
+// SM count of the current device, read once per device (a benign race: every writer stores the
+// same value); 152 when the attribute cannot be read
+int device_sm_count() {
+    constexpr int MAX_DEVICES = 64;
+    static int cached[MAX_DEVICES] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return 152;
+    int v = cached[dev];
+    if (v > 0) return v;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 152;
+    cached[dev] = v;
+    return v;
+}
+
 constexpr int SCAN_BLOCK = 1024;
 constexpr int SCAN_ITEMS = 4;
 constexpr int SCAN_TILE = SCAN_BLOCK * SCAN_ITEMS;

@@ -1936,13 +1936,13 @@ void launch_solver(DevWorld &w, float dt, float ratio, cudaStream_t s, cudaEvent
     // the per-CTA and per-warp classes hold disjoint islands: run them side by side
     cudaEventRecord(w.ev_fork, s);
     cudaStreamWaitEvent(w.aux_stream, w.ev_fork, 0);
-    k_solve_large<false><<<NUM_SMS * 2, LARGE_BLOCK, 0, w.aux_stream>>>(
+    k_solve_large<false><<<device_sm_count() * 2, LARGE_BLOCK, 0, w.aux_stream>>>(
         w, ct, w.large_list, w.scratch_order, w.scratch_colour, w.scratch_claim, dt, ratio, phase);
     if (joints)
-        k_solve_large<true><<<NUM_SMS * 2, LARGE_BLOCK, 0, w.aux_stream>>>(
+        k_solve_large<true><<<device_sm_count() * 2, LARGE_BLOCK, 0, w.aux_stream>>>(
             w, ct, w.large_joint_list, w.scratch_order, w.scratch_colour, w.scratch_claim, dt, ratio, phase);
     cudaEventRecord(w.ev_join, w.aux_stream);
-    k_solve_warp<<<NUM_SMS * w.warp_blocks_per_sm, WARP_BLOCK, warp_smem, s>>>(w, ct, dt, ratio, phase);
+    k_solve_warp<<<device_sm_count() * w.warp_blocks_per_sm, WARP_BLOCK, warp_smem, s>>>(w, ct, dt, ratio, phase);
     cudaStreamWaitEvent(s, w.ev_join, 0);
     // giant islands: a cooperative launch (all blocks co-resident), after the other tiers so that
     // it runs alone; it returns at once when the step has no giant island
@@ -2136,9 +2136,7 @@ void launch_ccd(DevWorld &w, float dt, cudaStream_t s) {
 // blocks of the giant-island launch: one per SM, fewer if the kernel cannot be resident at that
 // count (a cooperative launch needs every block resident at once)
 int giant_blocks_for_device() {
-    int dev = 0, sms = NUM_SMS, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int sms = device_sm_count(), per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_giant, GIANT_BLOCK, 0);
     if (per_sm < 1) return 0;
     return sms;

@@ -63,6 +63,10 @@ struct cc_world {
         float *d_targets = nullptr, *d_loss = nullptr;
         std::vector<void *> allocs;
     } adj;
+    // cc_world_step_taped: the step's rows in the C-ABI layout, grown on demand
+    cc_tape_body *x_bodies = nullptr;
+    cc_tape_contact *x_cons = nullptr;
+    int x_cap_bodies = 0, x_cap_cons = 0;
 };
 
 static int cuda_ok(cudaError_t e) {
@@ -403,12 +407,12 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
             return r;
         }
         w.epa_items = p;
-        // EPA threads scale with the world: about one per 8 bodies, 1,024 to EPA_DEFAULT_MAX_THREADS
+        // EPA threads scale with the world: about one per 8 bodies, 1,024 to epa_default_max_threads()
         int et = cap / 8;
-        et = et < 1024 ? 1024 : (et > EPA_DEFAULT_MAX_THREADS ? EPA_DEFAULT_MAX_THREADS : et);
+        et = et < 1024 ? 1024 : (et > epa_default_max_threads() ? epa_default_max_threads() : et);
         if (const char *e = getenv("CRASHCAT_EPA_THREADS")) {
             int v = atoi(e);
-            if (v >= 64 && v <= EPA_MAX_THREADS) et = v;
+            if (v >= 64 && v <= epa_max_threads()) et = v;
         }
         w.epa_threads = (et + 63) / 64 * 64;
         // launch-shape tunable: the packed polytope's point limit (4 to 32); items that need
@@ -529,6 +533,8 @@ int cc_world_destroy(cc_world *W) {
     if (W->q_tmp) cudaFree(W->q_tmp);
     for (void *p : W->adj.allocs)
         if (p) cudaFree(p);
+    if (W->x_bodies) cudaFree(W->x_bodies);
+    if (W->x_cons) cudaFree(W->x_cons);
     if (W->h_ctr) cudaFreeHost(W->h_ctr);
     if (W->ev_begin) cudaEventDestroy(W->ev_begin);
     if (W->ev_end) cudaEventDestroy(W->ev_end);
@@ -1469,6 +1475,69 @@ extern "C" int cc_world_rollout_grad(cc_world *W, float dt, int32_t n_steps, int
     cudaEventElapsedTime(&W->last_call_ms, W->ev_begin, W->ev_end);
     W->last_ctr = *W->h_ctr;
     return CC_OK;
+}
+
+// One step (the launch sequence cc_world_step runs) with the tape of its velocity solve read
+// back in the C-ABI layout.
+extern "C" int cc_world_step_taped(cc_world *W, float dt, cc_tape_body *bodies, cc_tape_contact *contacts,
+                                   int32_t capacity, int32_t *count, float *warm_ratio_out) {
+    if (!W || !count || capacity < 0 || !std::isfinite(dt)) return CC_ERR_INVALID;
+    if (int r = sync_shapes(W)) return r;
+    DevWorld &w = W->w;
+    *count = 0;
+    if (w.n == 0) return CC_OK;
+    int r = ensure_adjoint(W, 1, 1);
+    if (r != CC_OK) return r;
+    if (W->x_cap_bodies < w.cap) {
+        if (W->x_bodies) cudaFree(W->x_bodies);
+        W->x_bodies = nullptr;
+        W->x_cap_bodies = 0;
+        CC_TRY(cudaMalloc(&W->x_bodies, sizeof(cc_tape_body) * (size_t)w.cap));
+        W->x_cap_bodies = w.cap;
+    }
+    if (W->x_cap_cons < w.max_manifolds) {
+        if (W->x_cons) cudaFree(W->x_cons);
+        W->x_cons = nullptr;
+        W->x_cap_cons = 0;
+        CC_TRY(cudaMalloc(&W->x_cons, sizeof(cc_tape_contact) * (size_t)w.max_manifolds));
+        W->x_cap_cons = w.max_manifolds;
+    }
+    cudaStream_t s = W->stream;
+    upload_settings(W->dev_settings, W->settings.speculative_contact_distance, s);
+    if (!W->ev_begin) {
+        CC_TRY(cudaEventCreate(&W->ev_begin));
+        CC_TRY(cudaEventCreate(&W->ev_end));
+    }
+    float ratio = (W->settings.warm_starting && W->prev_dt > 0) ? (float)(dt / W->prev_dt) : 0.f;
+    if (dt <= 0.f) ratio = 0.f;
+    TapeStep &t = W->adj.tapes[0];
+    CC_TRY(cudaEventRecord(W->ev_begin, s));
+    enqueue_step(W, dt, ratio, nullptr, &t);
+    CC_TRY(cudaEventRecord(W->ev_end, s));
+    launch_tape_export(w, t, W->x_bodies, W->x_cons, s);
+    if (dt > 0.f) W->prev_dt = dt;
+    W->steps_done++;
+    CC_TRY(cudaStreamSynchronize(s));
+    CC_TRY(cudaGetLastError());
+    cudaEventElapsedTime(&W->last_call_ms, W->ev_begin, W->ev_end);
+    W->last_ctr = *W->h_ctr;
+    int status = CC_OK;
+    if (W->last_ctr.overflow) status = (W->last_ctr.overflow & OVF_TIMEOUT) ? CC_ERR_TIMEOUT : CC_ERR_CAPACITY;
+    W->last_status = status;
+    if (warm_ratio_out) *warm_ratio_out = ratio;
+    if (bodies) CC_TRY(cudaMemcpy(bodies, W->x_bodies, sizeof(cc_tape_body) * (size_t)w.n, cudaMemcpyDeviceToHost));
+    int nm = W->last_ctr.num_manifolds < w.max_manifolds ? W->last_ctr.num_manifolds : w.max_manifolds;
+    std::vector<cc_tape_contact> all((size_t)nm);
+    if (nm > 0) CC_TRY(cudaMemcpy(all.data(), W->x_cons, sizeof(cc_tape_contact) * (size_t)nm, cudaMemcpyDeviceToHost));
+    int k = 0;
+    for (int i = 0; i < nm; i++) k += all[i].body_a >= 0;
+    *count = k;
+    if (!contacts) return status;
+    if (k > capacity) return CC_ERR_CAPACITY;
+    k = 0;
+    for (int i = 0; i < nm; i++)
+        if (all[i].body_a >= 0) contacts[k++] = all[i];
+    return status;
 }
 
 // ---------------------------------------------------------------------------

@@ -11,8 +11,9 @@ The reference's user-facing calls (src/index.ts) map as follows:
 The device world is created lazily on the first ``update_world`` with every
 body added so far; later bodies are appended to it.  Body state lives on the
 device; ``RigidBody`` views read it back on demand.  Listener callbacks
-cannot run inside kernels: ``update_world`` accepts ``listener=None`` only and
-raises otherwise.
+cannot run inside kernels: ``update_world`` calls a listener's
+onContactAdded / onContactPersisted / onContactRemoved after the step from the
+library's event buffer, and rejects onBodyPairValidate / onContactValidate.
 """
 from __future__ import annotations
 
@@ -332,6 +333,22 @@ class GpuWorld:
                                                   _lib.ptr(targets), _lib.ptr(loss), _lib.ptr(gv), _lib.ptr(gw),
                                                   _lib.ptr(gm)), "cc_world_rollout_grad")
         return loss, gv, gw, gm
+
+    def step_taped(self, dt: float, capacity: int | None = None):
+        """One step with the rows of its velocity solve (cc_world_step_taped): returns
+        (bodies [n] TAPE_BODY_DTYPE, contacts TAPE_CONTACT_DTYPE, warm-start ratio, status)."""
+        bodies = np.zeros(self.n, dtype=_lib.TAPE_BODY_DTYPE)
+        cap = capacity if capacity is not None else max(self.n * 8, 1024)
+        cons = np.zeros(cap, dtype=_lib.TAPE_CONTACT_DTYPE)
+        cnt = C.c_int32(0)
+        ratio = C.c_float(0.0)
+        st = self._lib.cc_world_step_taped(self.handle, C.c_float(dt), _lib.ptr(bodies), _lib.ptr(cons), cap,
+                                           C.byref(cnt), C.byref(ratio))
+        if st not in (_lib.CC_OK, _lib.CC_ERR_CAPACITY):
+            check(st, "cc_world_step_taped")
+        if cnt.value > cap:
+            raise RuntimeError(f"cc_world_step_taped: {cnt.value} constraints exceed the capacity {cap}")
+        return bodies, cons[: cnt.value], float(ratio.value), st
 
     def contact_events(self) -> np.ndarray:
         """Contact events of the last step as rows (type 1 added / 2 persisted / 3 removed,

@@ -42,6 +42,8 @@
  *   cc_world_set_swing_twist_* <- swingTwistConstraint setters src/constraints/swing-twist-constraint.ts:319-416
  *   cc_world_set_skip_joint_pairs <- a Listener.onBodyPairValidate rejecting joined bodies
  *                                 src/broadphase/broadphase.ts:112-123
+ *   cc_world_step_taped        <- updateWorld, then reading world.contactConstraints
+ *                                 src/constraints/contact-constraints.ts:32-146
  *   cc_world_get_stats         <- (no counterpart: per-step counters)
  *   cc_status_string           <- assert() messages          src/utils/assert.ts:1-9
  */
@@ -421,6 +423,58 @@ int cc_world_rollout_grad(cc_world *world, float dt, int32_t n_steps, int32_t ch
                           float *grad_friction);
 
 /* ---------------------------------------------------------------------------
+ * One step with its solver rows read back: reading world.contactConstraints
+ * after updateWorld (src/constraints/contact-constraints.ts:32-146, the rows
+ * addContactConstraint builds at :437-857) together with the body velocities
+ * the velocity solve starts from.  These are exactly the constants over which
+ * cc_world_rollout_grad differentiates a step, so a host-side replay of the
+ * rows (a frozen-contact forward, or a dual-number pass) checks the adjoint.
+ *
+ *   bodies   : one cc_tape_body per body (num_bodies), written when not NULL;
+ *   contacts : the step's contact constraints in manifold order, up to capacity;
+ *              *count = the number of constraints (more than capacity: the call
+ *              returns CC_ERR_CAPACITY after the step, with nothing written);
+ *   warm_ratio: the warm-start ratio dt / previous dt the step used.
+ * The step itself is the one cc_world_step(world, dt, 1) takes.
+ * ------------------------------------------------------------------------- */
+enum { CC_TAPE_DYNAMIC = 1,  /* dynamic and awake: takes impulses in this step's solve */
+       CC_TAPE_MOVING = 2 }; /* not static: its velocity enters the rows */
+
+typedef struct cc_tape_body {
+    float linear_velocity[3];   /* after the force integration, before the warm start */
+    float angular_velocity[3];
+    float inv_inertia[6];       /* world-space inverse inertia at the step's orientation:
+                                   xx, xy, xz, yy, yz, zz (DOF mask applied) */
+    float inv_mass;
+    uint32_t flags;             /* CC_TAPE_* | DOF mask << 8 (cc_body_desc.allowed_dofs) */
+} cc_tape_body;
+
+typedef struct cc_tape_point {
+    float r_a[3], r_b[3];       /* moment arms from the centres of mass to the contact midpoint */
+    float eff_normal, eff_tangent1, eff_tangent2;  /* effective masses; 0: row inactive */
+    float bias_normal;          /* calculateNormalVelocityBias */
+    float lambda_normal, lambda_tangent1, lambda_tangent2;  /* warm-start impulses from the
+                                   contact cache, before the warm-start ratio */
+    float final_normal, final_tangent1, final_tangent2;     /* after the velocity iterations */
+    int32_t prev_point;         /* cached point of the previous step it matched (-1: none) */
+} cc_tape_point;
+
+typedef struct cc_tape_contact {
+    int32_t body_a, body_b;     /* body indices, ordered by id */
+    int32_t num_points;
+    int32_t island;
+    int32_t has_prev;           /* the pair had a contact in the previous step's cache */
+    uint32_t sort_key;          /* computeContactSortKey */
+    float normal[3], tangent1[3], tangent2[3];
+    float friction;             /* combined friction */
+    float inv_mass_a, inv_mass_b;
+    cc_tape_point points[4];
+} cc_tape_contact;
+
+int cc_world_step_taped(cc_world *world, float dt, cc_tape_body *bodies, cc_tape_contact *contacts,
+                        int32_t capacity, int32_t *count, float *warm_ratio);
+
+/* ---------------------------------------------------------------------------
  * World ray queries: castRay (src/query.ts:78-90) with the closest-hit
  * collector (createClosestCastRayCollector, src/collision/cast-ray-vs-shape.ts:
  * 180-205), a batch of rays per call.
@@ -554,11 +608,10 @@ int cc_world_collide_points_device(cc_world *world, const cc_point *points, int3
                                    const cc_query_filter *filter, float collision_tolerance, cc_point_hit *hits);
 
 /* ---------------------------------------------------------------------------
- * Allocation-free penetration query.  No counterpart in the reference: it is
- * the narrowphase of one convex pair (collideConvexVsConvex,
- * src/shapes/convex.ts:257-346, with penetrationDepthStepGJK / EPA of
- * src/collision/penetration.ts) offered as a batch query on caller-owned
- * device buffers.
+ * Allocation-free penetration query.  It has no counterpart in the reference:
+ * it is this library's narrowphase of one convex pair (FP32 GJK, then FP64 EPA
+ * when the shrunk shapes overlap) offered as a batch query on caller-owned
+ * device buffers, with no world handle.
  *
  * Why it exists: a world handle reserves its EPA polytopes (about 47 KB per
  * EPA thread) when it is created.  Some callers cannot allocate device memory
@@ -567,8 +620,9 @@ int cc_world_collide_points_device(cc_world *world, const cc_point *points, int3
  * stall the device (cudaMalloc and cudaFree synchronise it), or code that only
  * owns buffers handed to it by another allocator.  This entry point runs on
  * CC_STATIC_EPA_SLOTS polytopes and a queue of CC_STATIC_MAX_QUERIES items
- * held in file-scope device arrays of the library (about 20 MB per device),
- * and calls no cudaMalloc, cudaFree or other allocating routine.
+ * held in file-scope device arrays of the library (about 20 MB per device,
+ * held until the process exits), and calls no cudaMalloc, cudaFree or other
+ * allocating routine.
  *
  * Use:
  *   - queries and results are DEVICE pointers to count elements;
@@ -581,13 +635,18 @@ int cc_world_collide_points_device(cc_world *world, const cc_point *points, int3
  *   - count > CC_STATIC_MAX_QUERIES returns CC_ERR_CAPACITY and queues
  *     nothing; count < 0 or a NULL buffer returns CC_ERR_INVALID; count == 0
  *     queues nothing and returns CC_OK.
+ *   - shapes: sphere, box and capsule.  A query naming any other shape type
+ *     (a convex hull or a triangle mesh, whose data lives in a world, or a
+ *     value that names no shape) gets hit = CC_PENETRATION_UNSUPPORTED in its
+ *     result.  The check runs on the device, so it is reported per query and
+ *     not as the call's status, which would need a wait on the stream.
  *   - the EPA queue counter must start at zero: every call clears it on the
  *     stream before its first kernel.
  *   - the arrays are shared by every call on the device: two calls whose
  *     kernels overlap on the GPU (different streams, or different host
  *     threads) race on them.  Serialise calls on one stream.
- *   - A and B are taken in the given order (the world orders a pair by motion
- *     type and body id first, src/update.ts:74); max_separation is the
+ *   - A and B are taken in the given order (a world puts the body of lower
+ *     motion type, then of lower id, first); max_separation is the
  *     speculative contact distance of the world settings (0 for sensors).
  * ------------------------------------------------------------------------- */
 #define CC_STATIC_MAX_QUERIES 32768
@@ -606,8 +665,11 @@ typedef struct cc_penetration_query {
     float max_separation;
 } cc_penetration_query;
 
+#define CC_PENETRATION_UNSUPPORTED (-CC_ERR_UNSUPPORTED)
+
 typedef struct cc_penetration_result {
-    int32_t hit;        /* 1: the shapes are closer than max_separation */
+    int32_t hit;        /* 1: the shapes are closer than max_separation; 0: they are not;
+                           CC_PENETRATION_UNSUPPORTED: a shape type this query cannot take */
     float normal[3];    /* unit contact normal, A to B, world space */
     float depth;        /* penetration depth (negative: separation) */
     float point_a[3];   /* deepest point on A, world space */

@@ -13,7 +13,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 SRC = [os.path.join(HERE, f) for f in ("oracle.cpp", "oracle_collide.h", "oracle_math.h", "oracle_joints.h",
-                                              "oracle_joint_types.h")]
+                                              "oracle_joint_types.h", "oracle_frozen.h")]
 
 
 def build(force: bool = False) -> str:

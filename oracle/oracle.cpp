@@ -27,6 +27,7 @@
 #include <tuple>
 #include <vector>
 
+#include "oracle_frozen.h"
 #include "oracle_collide.h"
 
 namespace orc {
@@ -112,6 +113,7 @@ struct AxisPart {
 struct WorldContactPoint {
     V3 posA, posB, localA, localB;
     AxisPart n, t1, t2;
+    int prevPoint = -1;  // cached point whose impulses warm-started this one (-1: none)
 };
 struct ContactConstraint {
     int bodyA, bodyB;
@@ -125,6 +127,7 @@ struct ContactConstraint {
     double invIScaleA = 1, invIScaleB = 1;
     ContactKey contactKey;
     uint32_t sortKey;
+    bool hasPrev = false;  // the contact existed in the previous step
 };
 
 struct Island {
@@ -185,6 +188,11 @@ struct World {
     std::vector<CCDRecord> ccd;
     double ccdNormalLambda = 0, ccdFrictionLambda = 0;
     int ccdHits = 0;  // records whose cast hit a body, last step
+    // the rows of the last step's velocity solve, in the frozen-replay layout of oracle_frozen.h
+    // (recorded when recordTape is set)
+    bool recordTape = false;
+    std::vector<double> tapeBodies, tapeCons, tapeV2;
+    double tapeRatio = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -778,6 +786,7 @@ static bool add_contact_constraint(World &w, Body *A, Body *B, Manifold m, doubl
         cc.subB = m.subB;
         cc.contactKey = key;
         cc.sortKey = sort_key(A->index, B->index, m.subA, m.subB);
+        cc.hasPrev = existing;
         cc.normal = m.normal;
         double nx = cc.normal.x, ny = cc.normal.y, nz = cc.normal.z;
         if (std::fabs(nx) > std::fabs(ny)) {
@@ -819,6 +828,7 @@ static bool add_contact_constraint(World &w, Body *A, Body *B, Manifold m, doubl
                         cp.n.totalLambda = p.ln;
                         cp.t1.totalLambda = p.lt1;
                         cp.t2.totalLambda = p.lt2;
+                        cp.prevPoint = j;
                         set = true;
                         break;
                     }
@@ -1448,6 +1458,72 @@ static void resolve_ccd_contacts(World &w) {
     }
 }
 
+// The rows the velocity solve starts from (oracle_frozen.h layout): per body the velocities
+// after the force integration, the world inverse inertia, the inverse mass and flags; per
+// contact constraint the axes, friction, inverse masses and per point the moment arms to the
+// contact midpoint (as addContactConstraint computes them, contact-constraints.ts:700-720),
+// effective masses, bias, the cached (pre-ratio) impulses and the cached point they came from.
+static void record_tape_rows(World &w, double dt) {
+    using namespace orc_frozen;
+    const size_t n = w.bodies.size();
+    w.tapeBodies.assign(n * BODY_ROW, 0.0);
+    for (size_t i = 0; i < n; i++) {
+        const Body &b = w.bodies[i];
+        double *o = &w.tapeBodies[i * BODY_ROW];
+        o[0] = b.linvel.x, o[1] = b.linvel.y, o[2] = b.linvel.z;
+        o[3] = b.angvel.x, o[4] = b.angvel.y, o[5] = b.angvel.z;
+        const bool dyn = b.motion == DYNAMIC && !b.sleeping;
+        if (dyn) {
+            M4 I = inv_inertia_for_rotation(b, mat4_from_quat(b.quat));
+            const int idx[9] = {0, 1, 2, 4, 5, 6, 8, 9, 10};
+            for (int k = 0; k < 9; k++) o[6 + k] = I.m[idx[k]];
+        }
+        o[15] = b.invMass;
+        o[16] = (double)((dyn ? T_DYNAMIC : 0) | (b.motion != STATIC ? T_MOVING : 0) | (b.dof << 8));
+    }
+    w.tapeRatio = (w.s.warmStarting && w.prevDt > 0) ? dt / w.prevDt : 0.0;
+    w.tapeCons.assign(w.constraints.size() * CON_ROW, 0.0);
+    for (size_t k = 0; k < w.constraints.size(); k++) {
+        const ContactConstraint &c = w.constraints[k];
+        const Body &A = w.bodies[c.bodyA], &B = w.bodies[c.bodyB];
+        double *r = &w.tapeCons[k * CON_ROW];
+        r[0] = c.bodyA, r[1] = c.bodyB, r[2] = c.n, r[3] = A.islandIndex, r[4] = c.hasPrev ? 1 : 0;
+        r[5] = (double)c.sortKey;
+        const V3 ax[3] = {c.normal, c.t1, c.t2};
+        for (int x = 0; x < 3; x++) r[6 + 3 * x] = ax[x].x, r[7 + 3 * x] = ax[x].y, r[8 + 3 * x] = ax[x].z;
+        r[15] = c.friction, r[16] = c.invMassA, r[17] = c.invMassB;
+        for (int q = 0; q < c.n; q++) {
+            const WorldContactPoint &cp = c.pts[q];
+            double *pt = r + CON_HEAD + q * POINT_ROW;
+            V3 mid{(cp.posA.x + cp.posB.x) * 0.5, (cp.posA.y + cp.posB.y) * 0.5, (cp.posA.z + cp.posB.z) * 0.5};
+            V3 rA = sub(mid, A.com), rB = sub(mid, B.com);
+            pt[0] = rA.x, pt[1] = rA.y, pt[2] = rA.z, pt[3] = rB.x, pt[4] = rB.y, pt[5] = rB.z;
+            const AxisPart *parts[3] = {&cp.n, &cp.t1, &cp.t2};
+            for (int x = 0; x < 3; x++) pt[6 + x] = parts[x]->effMass, pt[10 + x] = parts[x]->totalLambda;
+            pt[9] = cp.n.bias;
+            pt[13] = cp.prevPoint;
+        }
+        for (int q = c.n; q < 4; q++) (r + CON_HEAD + q * POINT_ROW)[13] = -1;
+    }
+}
+// the final impulses of each constraint and the post-solve velocities of every body
+static void record_tape_finals(World &w) {
+    using namespace orc_frozen;
+    for (size_t k = 0; k < w.constraints.size(); k++) {
+        const ContactConstraint &c = w.constraints[k];
+        for (int q = 0; q < c.n; q++) {
+            double *pt = &w.tapeCons[k * CON_ROW + CON_HEAD + q * POINT_ROW];
+            pt[14] = c.pts[q].n.totalLambda, pt[15] = c.pts[q].t1.totalLambda, pt[16] = c.pts[q].t2.totalLambda;
+        }
+    }
+    w.tapeV2.assign(w.bodies.size() * 6, 0.0);
+    for (size_t i = 0; i < w.bodies.size(); i++) {
+        const Body &b = w.bodies[i];
+        double *o = &w.tapeV2[i * 6];
+        o[0] = b.linvel.x, o[1] = b.linvel.y, o[2] = b.linvel.z, o[3] = b.angvel.x, o[4] = b.angvel.y, o[5] = b.angvel.z;
+    }
+}
+
 static void step(World &w, double dt) {
     // ccd.clear ccd.ts:108-124
     w.ccd.clear();
@@ -1538,6 +1614,7 @@ static void step(World &w, double dt) {
                 hinge_setup(j, w.bodies[j.a], w.bodies[j.b], dt);
             }
         }
+        if (w.recordTape) record_tape_rows(w, dt);
         if (w.s.warmStarting) {
             double ratio = (w.s.warmStarting && w.prevDt > 0) ? dt / w.prevDt : 0.0;
             warm_start_all(w, ratio);
@@ -1615,6 +1692,7 @@ static void step(World &w, double dt) {
                 }
             }
         }
+        if (w.recordTape) record_tape_finals(w);
         // storeAppliedImpulses contact-constraints.ts:1061-1076
         w.manifoldLambda.assign(w.constraints.size(), 0.0);
         for (size_t k = 0; k < w.constraints.size(); k++)
@@ -2432,6 +2510,51 @@ void orc_inverse_inertia(const double *row, double *out9) {
     int k = 0;
     for (int c = 0; c < 3; c++)
         for (int r = 0; r < 3; r++) out9[k++] = I.m[c * 4 + r];
+}
+
+// Record (1) or stop recording (0) the rows of each step's velocity solve.
+void orc_set_record_tape(void *wp, int on) { ((World *)wp)->recordTape = on != 0; }
+// The last recorded step: body rows (n x BODY_ROW), contact rows (count x CON_ROW), post-solve
+// velocities (n x 6) and the warm-start ratio; returns the contact count (arrays may be NULL).
+int orc_get_solver_tape(void *wp, double *bodies, double *cons, double *v2, double *ratio) {
+    World &w = *(World *)wp;
+    if (bodies) std::copy(w.tapeBodies.begin(), w.tapeBodies.end(), bodies);
+    if (cons) std::copy(w.tapeCons.begin(), w.tapeCons.end(), cons);
+    if (v2) std::copy(w.tapeV2.begin(), w.tapeV2.end(), v2);
+    if (ratio) *ratio = w.tapeRatio;
+    return (int)(w.tapeCons.size() / orc_frozen::CON_ROW);
+}
+// Frozen-contact replay of a taped rollout (oracle_frozen.h).  mode 0: the real parts are the
+// tape's at every step and the dual parts carry the derivative along (dv, dw, dmu): out =
+// [loss at the tape, directional derivative].  mode 1: the replay's own trajectory from the
+// initial state moved by eps x (dv, dw, dmu): out = [loss(eps), its derivative along the
+// direction]; the loss is taken against a replay at eps = 0.  v2_out (steps x n x 6) and
+// lam_out (contacts x 12) receive the replay's post-solve velocities and final impulses.
+int orc_frozen_rollout(int n, int steps, int worlds, int iters, double dt, const double *consts,
+                       const double *bodies, const double *v0, const double *ratio, const int *con_off,
+                       const double *cons, const double *x_final, const double *targets, int mode, double eps,
+                       const double *dv, const double *dw, const double *dmu, double *out, double *v2_out,
+                       double *lam_out) {
+    using namespace orc_frozen;
+    if (n <= 0 || steps <= 0 || (mode != 0 && mode != 1)) return -1;
+    Tape T;
+    T.n = n, T.steps = steps, T.worlds = worlds, T.iters = iters, T.dt = dt;
+    T.consts = consts, T.bodies = bodies, T.v0 = v0, T.ratio = ratio, T.con_off = con_off, T.cons = cons;
+    T.x_final = x_final, T.targets = targets;
+    std::vector<V3s<double>> ref;
+    if (mode == 1) {
+        Replay<double> nominal(T, 1);
+        nominal.run(0.0, nullptr, nullptr, nullptr);
+        ref = nominal.vsum;
+    }
+    Replay<Dual> r(T, mode);
+    r.v2_out = v2_out;
+    r.lam_out = lam_out;
+    r.run(eps, dv, dw, dmu);
+    Dual L = r.loss(mode == 1 ? &ref : nullptr);
+    out[0] = L.v;
+    out[1] = L.d;
+    return 0;
 }
 
 }  // extern "C"

@@ -9,8 +9,8 @@
 // gl-matrix conventions (column-major Mat4, [x,y,z,w] quaternions); the
 // helpers below restate the published gl-matrix algorithms.  Choices that no
 // reference test pins (vec3.length as sqrt of the dot product rather than
-// Math.hypot, box overlap inclusive) are the oracle's own and are listed in
-// the design doc.
+// Math.hypot, box overlap inclusive) are the oracle's own: mathcat 0.0.10 is
+// not vendored with the reference, so no test pins them.
 #pragma once
 #include <cmath>
 #include <cstdint>

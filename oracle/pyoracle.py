@@ -66,6 +66,10 @@ def load():
         "orc_set_skip_joint_pairs": ([vp, i32], None),
         "orc_add_swing_twist": ([vp, dp], i32),
         "orc_add_hull": ([vp, i32, dp, dp, i32, C.c_void_p, i32, C.c_void_p, dp, dp], i32),
+        "orc_set_record_tape": ([vp, i32], None),
+        "orc_get_solver_tape": ([vp, vp, vp, vp, vp], i32),
+        "orc_frozen_rollout": ([i32, i32, i32, i32, C.c_double, dp, dp, dp, dp, ip, dp, dp, dp, i32, C.c_double,
+                                vp, vp, vp, dp, vp, vp], i32),
     }
     for k, (a, r) in sig.items():
         f = getattr(lib, k)
@@ -339,6 +343,20 @@ class OracleWorld:
             ev[names[t]].add((a, b))
         return ev
 
+    def step_taped(self, dt: float):
+        """One step with the rows of its velocity solve (orc_get_solver_tape): returns
+        (body rows [n, 17], contact rows [k, 86], post-solve velocities [n, 6], warm-start ratio)
+        in the layout of oracle_frozen.h."""
+        self.lib.orc_set_record_tape(self.h, 1)
+        self.lib.orc_step(self.h, dt, 1)
+        k = self.lib.orc_get_solver_tape(self.h, None, None, None, None)
+        bodies = np.zeros((self.n, BODY_ROW))
+        cons = np.zeros((max(k, 1), CON_ROW))
+        v2 = np.zeros((self.n, 6))
+        ratio = C.c_double(0.0)
+        self.lib.orc_get_solver_tape(self.h, bodies.ctypes.data, cons.ctypes.data, v2.ctypes.data, C.byref(ratio))
+        return bodies, cons[:k], v2, float(ratio.value)
+
     def manifolds(self) -> np.ndarray:
         n = self.lib.orc_manifold_count(self.h)
         o = np.zeros((max(n, 1), 32), dtype=np.float64)
@@ -365,3 +383,124 @@ def fix_normal(v0, v1, v2, triangle_normal, active_edges, point, normal, movemen
         a[3 * k: 3 * k + 3] = v
     a[24] = active_edges
     return load().orc_fix_normal(dptr(a))
+
+
+# ---------------------------------------------------------------------------
+# frozen-contact replay of a taped rollout (oracle_frozen.h)
+# ---------------------------------------------------------------------------
+BODY_ROW, CONST_ROW, CON_HEAD, POINT_ROW = 17, 6, 18, 17
+CON_ROW = CON_HEAD + 4 * POINT_ROW
+TAPE_DYNAMIC, TAPE_MOVING = 1, 2
+
+
+def tape_consts(bodies: np.ndarray, dt: float) -> np.ndarray:
+    """Per body (world, in the loss, friction, friction combine mode, linear and angular damping
+    factors max(0, 1 - c dt)) from a BODY_DTYPE array."""
+    c = np.zeros((len(bodies), CONST_ROW))
+    c[:, 0] = bodies["world"]
+    c[:, 1] = bodies["motion_type"] == 2
+    c[:, 2] = bodies["friction"].astype(np.float64)
+    c[:, 3] = bodies["friction_combine"]
+    c[:, 4] = np.maximum(0.0, 1.0 - bodies["linear_damping"].astype(np.float64) * dt)
+    c[:, 5] = np.maximum(0.0, 1.0 - bodies["angular_damping"].astype(np.float64) * dt)
+    return c
+
+
+def tape_rows_from_gpu(tb: np.ndarray, tc: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """cc_tape_body / cc_tape_contact records (crashcat_gb300._lib TAPE_*_DTYPE) -> the replay's
+    body rows [n, 17] and contact rows [k, 86]."""
+    b = np.zeros((len(tb), BODY_ROW))
+    b[:, 0:3] = tb["linear_velocity"]
+    b[:, 3:6] = tb["angular_velocity"]
+    s = tb["inv_inertia"].astype(np.float64)  # xx xy xz yy yz zz -> 3x3 column-major
+    b[:, 6:15] = s[:, [0, 1, 2, 1, 3, 4, 2, 4, 5]]
+    b[:, 15] = tb["inv_mass"]
+    b[:, 16] = tb["flags"]
+    c = np.zeros((len(tc), CON_ROW))
+    c[:, 0] = tc["body_a"]
+    c[:, 1] = tc["body_b"]
+    c[:, 2] = tc["num_points"]
+    c[:, 3] = tc["island"]
+    c[:, 4] = tc["has_prev"]
+    c[:, 5] = tc["sort_key"]
+    c[:, 6:9] = tc["normal"]
+    c[:, 9:12] = tc["tangent1"]
+    c[:, 12:15] = tc["tangent2"]
+    c[:, 15] = tc["friction"]
+    c[:, 16] = tc["inv_mass_a"]
+    c[:, 17] = tc["inv_mass_b"]
+    for q in range(4):
+        p = tc["points"][:, q]
+        o = CON_HEAD + q * POINT_ROW
+        c[:, o:o + 3] = p["r_a"]
+        c[:, o + 3:o + 6] = p["r_b"]
+        c[:, o + 6] = p["eff_normal"]
+        c[:, o + 7] = p["eff_tangent1"]
+        c[:, o + 8] = p["eff_tangent2"]
+        c[:, o + 9] = p["bias_normal"]
+        c[:, o + 10] = p["lambda_normal"]
+        c[:, o + 11] = p["lambda_tangent1"]
+        c[:, o + 12] = p["lambda_tangent2"]
+        c[:, o + 13] = np.where(q < tc["num_points"], p["prev_point"], -1)
+        c[:, o + 14] = p["final_normal"]
+        c[:, o + 15] = p["final_tangent1"]
+        c[:, o + 16] = p["final_tangent2"]
+    return b, c
+
+
+class FrozenTape:
+    """The rows of every step of a rollout, for orc_frozen_rollout: consts [n, 6], then per step
+    the body rows, the velocities at the step's start [n, 6], the warm-start ratio and the
+    contact rows; finish() takes the positions after the last step."""
+
+    def __init__(self, consts: np.ndarray, targets: np.ndarray, velocity_iterations: int, dt: float):
+        self.consts = np.ascontiguousarray(consts, dtype=np.float64)
+        self.targets = np.ascontiguousarray(targets, dtype=np.float64).reshape(-1, 3)
+        self.iters = int(velocity_iterations)
+        self.dt = float(dt)
+        self.bodies, self.v0, self.ratio, self.cons = [], [], [], []
+        self.x_final = None
+
+    def add_step(self, body_rows, v0, ratio, con_rows):
+        self.bodies.append(np.asarray(body_rows, dtype=np.float64))
+        self.v0.append(np.asarray(v0, dtype=np.float64))
+        self.ratio.append(float(ratio))
+        self.cons.append(np.asarray(con_rows, dtype=np.float64).reshape(-1, CON_ROW))
+
+    def finish(self, x_final):
+        self.x_final = np.ascontiguousarray(x_final, dtype=np.float64)
+
+    def replay(self, mode: int, eps: float = 0.0, dv=None, dw=None, dmu=None, want_v2: bool = False):
+        """mode 0: (loss at the tape, its derivative along (dv, dw, dmu)); mode 1: (loss of the
+        replay's own trajectory moved by eps along the direction, its derivative there).
+        With want_v2 also the post-solve velocities [steps, n, 6] and the final impulses
+        [contacts, 4, 3] of the replay."""
+        lib = load()
+        n, steps = len(self.consts), len(self.bodies)
+        bodies = np.ascontiguousarray(np.stack(self.bodies))
+        v0 = np.ascontiguousarray(np.stack(self.v0))
+        ratio = np.ascontiguousarray(self.ratio, dtype=np.float64)
+        off = np.zeros(steps + 1, dtype=np.int32)
+        off[1:] = np.cumsum([len(c) for c in self.cons])
+        cons = np.ascontiguousarray(np.concatenate(self.cons) if off[-1] else np.zeros((1, CON_ROW)))
+
+        def opt(a, shape):
+            if a is None:
+                return None, None
+            a = np.ascontiguousarray(a, dtype=np.float64).reshape(shape)
+            return a, a.ctypes.data
+
+        dv_a, dv_p = opt(dv, (n, 3))
+        dw_a, dw_p = opt(dw, (n, 3))
+        dm_a, dm_p = opt(dmu, (n,))
+        out = np.zeros(2)
+        v2 = np.zeros((steps, n, 6)) if want_v2 else None
+        lam = np.zeros((max(int(off[-1]), 1), 4, 3)) if want_v2 else None
+        st = lib.orc_frozen_rollout(n, steps, len(self.targets), self.iters, self.dt, dptr(self.consts), dptr(bodies),
+                                    dptr(v0), dptr(ratio), iptr(off), dptr(cons), dptr(self.x_final),
+                                    dptr(self.targets), mode, eps, dv_p, dw_p, dm_p, dptr(out),
+                                    v2.ctypes.data if want_v2 else None, lam.ctypes.data if want_v2 else None)
+        assert st == 0
+        if want_v2:
+            return float(out[0]), float(out[1]), v2, lam[: int(off[-1])]
+        return float(out[0]), float(out[1])

@@ -1,6 +1,8 @@
 """cc_penetration_static, the allocation-free penetration query, against the
 world step's narrowphase (cc_world_step with dt = 0, then
-cc_world_get_manifolds) on the same shape pairs.
+cc_world_get_manifolds) on the same shape pairs, and against the FP64 oracle's
+collideConvexVsConvex / collideSphereVsSphere of each pair (hit, normal, depth
+and both contact points).
 
 Both run the same FP32 GJK and FP64 EPA source, inlined into different
 kernels (so the compiler may contract multiply-adds differently).  The
@@ -18,6 +20,7 @@ import numpy as np
 import pytest
 
 from crashcat_gb300 import _lib, scenes, world
+from oracle import pyoracle
 
 pytestmark = pytest.mark.gpu
 
@@ -80,6 +83,72 @@ def check_against_world(lib, sc):
         bad += not ok
     assert bad <= 0.01 * len(mans)
     assert abs(int(res["hit"].sum()) - len(mans)) <= 0.01 * len(pairs)
+
+
+def oracle_hits(sc, rows, order, max_sep):
+    """The oracle's pair collide in FP64 on the same (FP32) poses: hit, pa, pb, axis, depth."""
+    lib = pyoracle.load()
+    b = sc.bodies.copy()
+    b["position"] = rows[:, 0:3]
+    b["quaternion"] = rows[:, 3:7]
+    orows = pyoracle.rows_from_bodies(b)
+    out = np.zeros((len(order), 13))
+    for k, (a, bb) in enumerate(order):
+        ra, rb = np.ascontiguousarray(orows[a]), np.ascontiguousarray(orows[bb])
+        o = np.zeros(13)
+        lib.orc_collide_pair(pyoracle.dptr(ra), pyoracle.dptr(rb), float(max_sep), pyoracle.dptr(o))
+        out[k] = o
+    return out
+
+
+def check_against_oracle(lib, sc):
+    """Every pair's hit flag, and for the pairs both hit: the unit normal, the depth and both
+    contact points.  GJK contacts within 1e-4 (normal) and 1e-3 m (depth, points); EPA contacts
+    within 1e-3 and 5e-3 m, since EPA seeded from an FP32 simplex may settle on another triangle of
+    a flat face; at most 2 % of the EPA contacts may put their points elsewhere on such a face."""
+    rows, pairs, _, max_sep = world_contacts(sc)
+    order = [ordered(sc, int(a), int(b)) for a, b in pairs.tolist()]
+    res = run_static(lib, queries_for(sc, rows, order, max_sep))
+    orc = oracle_hits(sc, rows, order, max_sep)
+    ohit = orc[:, 0] == 1
+    ghit = res["hit"] == 1
+    assert ohit.sum() > 20
+    assert int((ohit != ghit).sum()) <= max(1, int(0.01 * len(order)))
+    both = ohit & ghit
+    n_o = orc[both, 7:10] / np.linalg.norm(orc[both, 7:10], axis=1, keepdims=True)
+    epa = res["used_epa"][both] == 1
+    dn = np.abs(res["normal"][both] - n_o).max(1)
+    dd = np.abs(res["depth"][both] - orc[both, 10])
+    dpa = np.abs(res["point_a"][both] - orc[both, 1:4]).max(1)
+    dpb = np.abs(res["point_b"][both] - orc[both, 4:7]).max(1)
+    g = ~epa
+    assert (dn[g] < 1e-4).all() and (dd[g] < 1e-3).all()
+    assert (dpa[g] < 1e-3).all() and (dpb[g] < 1e-3).all()
+    assert epa.sum() > 0
+    assert (dn[epa] < 1e-3).mean() >= 0.98 and (dd[epa] < 1e-3 + 1e-3 * np.abs(orc[both, 10][epa])).mean() >= 0.98
+    assert ((dpa[epa] < 5e-3) & (dpb[epa] < 5e-3)).mean() >= 0.98
+
+
+def test_static_query_matches_oracle(gpu_lib):
+    check_against_oracle(gpu_lib, scenes.random_pairs_scene(n=300, seed=7, capsule_fraction=0.2))
+    check_against_oracle(gpu_lib, scenes.random_pairs_scene(n=300, seed=9))
+
+
+def test_static_query_marks_unsupported_shapes(gpu_lib):
+    """A hull, a mesh or a value that names no shape comes back as CC_PENETRATION_UNSUPPORTED;
+    the sphere-box query beside them is answered as usual."""
+    q = np.zeros(4, dtype=_lib.PEN_QUERY_DTYPE)
+    q["a"]["quaternion"] = (0, 0, 0, 1)
+    q["b"]["quaternion"] = (0, 0, 0, 1)
+    q["a"]["shape_type"] = _lib.SHAPE_SPHERE
+    q["a"]["shape_params"] = (0.5, 0, 0, 0)
+    q["b"]["shape_params"] = (0.5, 0.5, 0.5, 0.05)
+    q["b"]["position"] = (0.0, 0.8, 0.0)
+    q["b"]["shape_type"] = (_lib.SHAPE_BOX, _lib.SHAPE_CONVEX_HULL, _lib.SHAPE_TRIANGLE_MESH, 99)
+    q["max_separation"] = 0.02
+    res = run_static(gpu_lib, q)
+    assert res["hit"][0] == 1 and abs(float(res["depth"][0]) - 0.2) < 1e-4
+    assert (res["hit"][1:] == _lib.PENETRATION_UNSUPPORTED).all()
 
 
 def test_static_query_matches_world_twice(gpu_lib):
