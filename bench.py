@@ -25,8 +25,19 @@ adjoint: the differentiable-rollout workload (1,024 worlds x 64 boxes, 120 steps
 dt 1/60, checkpoint every 10 steps).  forward_ms_per_step = the plain rollout (graph-
 replayed steps, CUDA events); ms_per_step = cc_world_rollout_grad (forward with
 checkpoints, recomputation with tapes, reverse sweep, gradients to the host) / 120;
-fd_check = central finite differences (h = 1e-3) of the full step along seeded
-directions against the adjoint, on the first 8 worlds.
+fd_check: on the first 8 worlds, the adjoint's directional derivative along seeded
+directions against the oracle's FP64 dual-number replay of the GPU's per-step solver rows
+(the model the adjoint differentiates), against central differences (h = 1e-3 and 1e-5) of
+that frozen-contact replay, and against central differences of the full GPU step.
+
+error: the batched workload's first 16 worlds stepped through the settle phase on the GPU and
+on the FP64 oracle: penetration, mechanical energy and resting heights on each side, energy
+drift, and how far positions diverged.  cube_heap, ragdolls, terrain and adjoint carry the
+same report for their workloads.
+
+cube_heap: the plain single-world workload (1,000 boxes dropped on a floor, dt 1/60, 10/2
+iterations, 600 steps) through cc_world_step, with its stage roofline; its cpu_baseline is the
+oracle on the whole workload (600 steps, one core).
 
 ragdolls: the jointed-ragdoll workload (2,000 ragdolls x 11 capsules with 4 hinges and 6
 swing-twist joints each, 600 steps at dt 1/60, 12/4 iterations): GPU body-steps/s over the
@@ -75,6 +86,9 @@ def parse():
     ap.add_argument("--adjoint", type=int, default=1, help="measure the rollout adjoint (1) or skip it (0)")
     ap.add_argument("--ragdolls", type=int, default=1, help="measure the jointed-ragdoll workload (1) or skip it (0)")
     ap.add_argument("--terrain", type=int, default=1, help="measure the mixed-shape terrain workload (1) or skip it (0)")
+    ap.add_argument("--cube-heap", type=int, default=1, help="measure the plain cube-heap workload (1) or skip it (0)")
+    ap.add_argument("--errors", type=int, default=1,
+                    help="report the batched workload's error against the FP64 oracle (1) or skip it (0)")
     ap.add_argument("--settle", type=int, default=360,
                     help="untimed steps before the warm-up so the timed steps are contact-rich")
     return ap.parse_args()
@@ -184,6 +198,87 @@ def algorithmic_bytes(stage: str, st: dict, n_bodies: int) -> float:
         # both solver kernels together move these bytes; each is charged its share of them
         return 216.0 * na + (48 + 180 * P) * nm + 24 * P * nm
     raise ValueError(stage)
+
+
+# ---------------------------------------------------------------------------
+# error against the FP64 oracle, per workload (penetration, energy, resting heights)
+# ---------------------------------------------------------------------------
+def mass_properties(bodies, hulls=()):
+    """Mass and body-frame inertia tensor (about the centre of mass) of every body: solid boxes,
+    spheres and capsules (cylinder plus two hemispheres), convex hulls from their built volume and
+    unit-density inertia.  Used for the energy figures only."""
+    n = len(bodies)
+    m = np.zeros(n)
+    inertia = np.zeros((n, 3, 3))
+    rho = bodies["density"].astype(np.float64)
+    prm = bodies["shape_params"].astype(np.float64)
+    for i in range(n):
+        st = int(bodies["shape_type"][i])
+        if st == 1:  # box
+            hx, hy, hz = prm[i, 0:3]
+            m[i] = rho[i] * 8 * hx * hy * hz
+            inertia[i] = np.diag([hy * hy + hz * hz, hx * hx + hz * hz, hx * hx + hy * hy]) * m[i] / 3
+        elif st == 0:  # sphere
+            r = prm[i, 0]
+            m[i] = rho[i] * 4.0 / 3.0 * math.pi * r ** 3
+            inertia[i] = np.eye(3) * 0.4 * m[i] * r * r
+        elif st == 2:  # capsule along local Y
+            r, h = prm[i, 0], prm[i, 1]
+            mc, ms = rho[i] * math.pi * r * r * 2 * h, rho[i] * 4.0 / 3.0 * math.pi * r ** 3
+            iy = mc * r * r / 2 + ms * 0.4 * r * r
+            ix = mc * (r * r / 4 + (2 * h) ** 2 / 12) + ms * (0.4 * r * r + h * h + 0.75 * h * r)
+            m[i] = mc + ms
+            inertia[i] = np.diag([ix, iy, ix])
+        elif st == 3 and hulls:  # convex hull
+            hd = hulls[int(prm[i, 0])]
+            m[i] = rho[i] * float(hd["volume"])
+            inertia[i] = rho[i] * np.asarray(hd["inertia"], dtype=np.float64)
+    return m, inertia
+
+
+def _quat_matrices(q):
+    x, y, z, w = q[:, 0], q[:, 1], q[:, 2], q[:, 3]
+    return np.stack([np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)], -1),
+                     np.stack([2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)], -1),
+                     np.stack([2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], -1)], 1)
+
+
+def step_metrics(rows, bodies, depths, mass, inertia, g: float = 9.81) -> dict:
+    """Mechanical energy (kinetic + rotational + potential m g y of the centre of mass), contact
+    penetration (positive manifold depths of the last step) and centre-of-mass heights of the
+    dynamic bodies, from state rows (position, quaternion, linear / angular velocity, centre of mass:
+    the first 16 columns of both the GPU's and the oracle's rows)."""
+    r = np.asarray(rows, dtype=np.float64)
+    dyn = bodies["motion_type"] == 2
+    v, w, com = r[dyn, 7:10], r[dyn, 10:13], r[dyn, 13:16]
+    R = _quat_matrices(r[dyn, 3:7] / np.linalg.norm(r[dyn, 3:7], axis=1, keepdims=True))
+    Iw = R @ inertia[dyn] @ np.transpose(R, (0, 2, 1))
+    ke = 0.5 * float((mass[dyn] * (v * v).sum(1)).sum()) + 0.5 * float(np.einsum("ni,nij,nj->", w, Iw, w))
+    pe = float((mass[dyn] * g * com[:, 1]).sum())
+    pen = np.maximum(np.asarray(depths, dtype=np.float64), 0.0)
+    return {"energy_j": ke + pe, "kinetic_j": ke, "max_penetration_m": float(pen.max()) if len(pen) else 0.0,
+            "mean_penetration_m": float(pen.mean()) if len(pen) else 0.0, "contacts": int(len(pen)),
+            "mean_height_m": float(com[:, 1].mean()), "min_height_m": float(com[:, 1].min())}
+
+
+def error_report(bodies, rows0, gpu_rows, gpu_depths, orc_rows, orc_depths, mass, inertia, steps: int,
+                 note: str = "") -> dict:
+    """The GPU against the FP64 oracle after `steps` steps from the same start: both sides'
+    metrics, their energy drifts from the start, and how far the bodies' positions diverged."""
+    s0 = step_metrics(rows0, bodies, [], mass, inertia)
+    g = step_metrics(gpu_rows, bodies, gpu_depths, mass, inertia)
+    o = step_metrics(orc_rows, bodies, orc_depths, mass, inertia)
+    dyn = bodies["motion_type"] == 2
+    dp = np.linalg.norm(np.asarray(gpu_rows, np.float64)[dyn, 0:3] - np.asarray(orc_rows, np.float64)[dyn, 0:3], axis=1)
+    drift_o = o["energy_j"] - s0["energy_j"]
+    return {"steps": steps, "gpu": g, "oracle": o, "initial_energy_j": s0["energy_j"],
+            "energy_drift_gpu_j": g["energy_j"] - s0["energy_j"], "energy_drift_oracle_j": drift_o,
+            "energy_drift_rel_diff": abs(g["energy_j"] - o["energy_j"]) / max(abs(drift_o), 1e-9),
+            "max_penetration_diff_m": g["max_penetration_m"] - o["max_penetration_m"],
+            "mean_height_diff_m": g["mean_height_m"] - o["mean_height_m"],
+            "position_diff_m": {"median": float(np.median(dp)), "p95": float(np.percentile(dp, 95)),
+                                "max": float(dp.max())},
+            "note": note}
 
 
 # ---------------------------------------------------------------------------
@@ -351,7 +446,39 @@ def adjoint_measurement(num_worlds: int = 1024, steps: int = 120, checkpoint_eve
         return tot
 
     g8 = make(sub, nw)
-    _, gv8, gw8, gm8 = g8.rollout_grad(sc.dt, steps, tg, checkpoint_every=checkpoint_every)
+    loss8, gv8, gw8, gm8 = g8.rollout_grad(sc.dt, steps, tg, checkpoint_every=checkpoint_every)
+    # the rows of every step of the same rollout (cc_world_step_taped) for the oracle's frozen-contact
+    # replay: FP64 central differences through the replay and its FP64 dual-number derivative
+    from oracle import build as obuild, pyoracle
+    obuild.build()
+    gt = make(sub, nw)
+    tape = pyoracle.FrozenTape(pyoracle.tape_consts(sub, sc.dt), tg, sc.velocity_iterations, sc.dt)
+    rows, _ = gt.get_state()
+    for _ in range(steps):
+        tb, tc, ratio, _st = gt.step_taped(sc.dt)
+        b_rows, c_rows = pyoracle.tape_rows_from_gpu(tb, tc)
+        tape.add_step(b_rows, rows[:, 7:13], ratio, c_rows)
+        rows, _ = gt.get_state()
+    tape.finish(rows[:, 0:3])
+    rows_g, depth_g = rows.copy(), gt.get_manifolds()[:, 6]
+    del gt
+    tape_loss, _ = tape.replay(0)
+    # the forward rollout's error against the oracle, one oracle world per world
+    import copy as _copy
+    ws1 = W.standard_settings(velocity_iterations=sc.velocity_iterations,
+                              position_iterations=sc.position_iterations, allow_sleeping=False)
+    rows_o, depth_o = [], []
+    for k in range(nw):
+        bk = _copy.deepcopy(sub[sub["world"] == k])
+        bk["world"] = 0
+        o = pyoracle.OracleWorld(ws1, bk)
+        o.step(sc.dt, steps)
+        rows_o.append(o.state())
+        depth_o.append(o.manifolds()[:, 6])
+    rows_start, _ = make(sub, nw).get_state()
+    m8, i8 = mass_properties(sub)
+    fwd_err = error_report(sub, rows_start, rows_g, depth_g, np.concatenate(rows_o), np.concatenate(depth_o), m8, i8,
+                           steps, f"the first {nw} worlds, {steps} steps from the start")
     rng = np.random.default_rng(5)
     dyn = (sub["motion_type"] == 2)[:, None]
     checks, h = [], 1e-3
@@ -369,31 +496,177 @@ def adjoint_measurement(num_worlds: int = 1024, steps: int = 120, checkpoint_eve
 
         fd = (host_loss(pert(1)) - host_loss(pert(-1))) / (2 * h)
         ad = float((gv8 * dv).sum() + (gw8 * dw).sum() + (gm8 * dm).sum())
-        checks.append({"direction": ["v", "v+w", "v+w+friction"][k], "fd": fd, "adjoint": ad,
-                       "rel_err": abs(fd - ad) / max(abs(fd), 1e-12)})
+        _, dual = tape.replay(0, 0.0, dv, dw, dm)
+        lp, _ = tape.replay(1, h, dv, dw, dm)
+        lm, _ = tape.replay(1, -h, dv, dw, dm)
+        ffd = (lp - lm) / (2 * h)
+        lp5, _ = tape.replay(1, 1e-5, dv, dw, dm)
+        lm5, _ = tape.replay(1, -1e-5, dv, dw, dm)
+        ffd5 = (lp5 - lm5) / 2e-5
+        checks.append({"direction": ["v", "v+w", "v+w+friction"][k], "adjoint": ad,
+                       "fp64_dual": dual, "rel_err_vs_dual": abs(dual - ad) / max(abs(dual), 1e-12),
+                       "frozen_fd": ffd, "rel_err_vs_frozen_fd": abs(ffd - ad) / max(abs(ffd), 1e-12),
+                       "frozen_fd_h1e-5": ffd5, "rel_err_vs_frozen_fd_h1e-5": abs(ffd5 - ad) / max(abs(ffd5), 1e-12),
+                       "full_step_fd": fd, "rel_err_vs_full_step_fd": abs(fd - ad) / max(abs(fd), 1e-12)})
     return {"workload": "diff_rollout_worlds", "worlds": num_worlds, "bodies": int(sc.n), "steps": steps,
             "checkpoint_every": checkpoint_every, "ms_per_step": adj_ms, "forward_ms_per_step": fwd_ms,
             "adjoint_over_forward": adj_ms / fwd_ms, "loss": float(loss.sum()),
             "grad_norms": {"linvel": float(np.linalg.norm(gv)), "angvel": float(np.linalg.norm(gw)),
                            "friction": float(np.linalg.norm(gm))},
+            "error": fwd_err,
             "fd_check": {"worlds": nw, "h": h, "directions": checks,
-                         "model": "adjoint over each step's fixed contact set; FD through the full step"}}
+                         "tape_loss_fp64": tape_loss, "adjoint_loss": float(loss8.sum()),
+                         "model": "the adjoint differentiates each step's velocity solve and integration over its "
+                                  "fixed contact rows; fp64_dual = the oracle's FP64 dual-number replay of the GPU's "
+                                  "rows (cc_world_step_taped), frozen_fd = central differences of that replay "
+                                  "(FP64); full_step_fd = central differences of the full GPU step, whose contact "
+                                  "set and geometry move with the perturbation"}}
 
 
-def ragdoll_measurement(cpu_seconds: float = 8.0):
-    """The jointed-ragdoll workload (2,000 ragdolls of 11 capsules, 4 hinges and 6 swing-twist
-    joints each, in a 60 m arena of static walls; dt 1/60, 12/4 iterations): all 600 steps from
-    spawn on the GPU, timed per phase (falling, piling up, resting pile), and the FP64 oracle on
-    the same scene for a bounded number of steps from spawn on one host core."""
+def cube_heap_measurement(peak: float, peak_kind: str):
+    """The plain cube heap (1,000 boxes on a 10 x 10 x 10 grid dropped onto a static box floor,
+    dt 1/60, 10/2 iterations, 600 steps) on one single-world handle through cc_world_step:
+    body-steps/s over all 600 steps (1,001 bodies, the floor included as in the batched figure),
+    per phase, with the dominant stage's roofline on the settled heap; the FP64 oracle steps the
+    same 600 steps on one host core (the whole workload: it is CPU-runnable), and the error of
+    the GPU against it after the 600 steps."""
     from crashcat_gb300 import scenes, world as W
     from oracle import build as obuild, pyoracle
-    sc = scenes.ragdolls()
+    sc = scenes.cube_heap()
     ws = W.standard_settings(velocity_iterations=sc.velocity_iterations, position_iterations=sc.position_iterations)
+    g = W.GpuWorld(ws, sc.n + 8)
+    g.add_bodies(sc.bodies)
+    rows0, _ = g.get_state()
+    phases, total_ms, status = [], 0.0, 0
+    for first, count in ((0, 100), (100, 500)):
+        status |= g.step(sc.dt, count)
+        st = g.stats()
+        total_ms += st["last_call_ms"]
+        phases.append({"steps": [first, first + count], "ms_per_step": st["last_call_ms"] / count,
+                       "awake": st["num_awake"], "manifolds": st["num_manifolds"], "islands": st["num_islands"],
+                       "max_island_constraints": st["max_island_constraints"]})
+    rows_g, _ = g.get_state()
+    depth_g = g.get_manifolds()[:, 6]
+    prof = g.profile_steps(sc.dt, 10)
+    pst = g.stats()
+    dom = max(prof, key=prof.get)
+    bytes_dom = algorithmic_bytes(dom, pst, sc.n)
+    achieved = bytes_dom / (prof[dom] * 1e-3) / 1e9 if prof[dom] > 0 else 0.0
+    del g
+    obuild.build()
+    o = pyoracle.OracleWorld(ws, sc.bodies)
+    t0 = time.perf_counter()
+    o.step(sc.dt, 600)
+    cpu_s = time.perf_counter() - t0
+    rows_o = o.state()
+    depth_o = o.manifolds()[:, 6]
+    m, inertia = mass_properties(sc.bodies)
+    return {"workload": "cube_heap", "bodies": int(sc.n), "steps": 600, "api": "cc_world_step (one world)",
+            "value": sc.n * 600 / (total_ms * 1e-3), "unit": METRIC, "ms_per_step": total_ms / 600,
+            "phases": phases, "status": int(status),
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "algorithmic_bytes_per_launch": bytes_dom,
+                         "stage_ms": prof, "note": "one world of 1,001 bodies: launch and latency bound"},
+            "cpu_baseline": {"value": sc.n * 600 / cpu_s, "unit": METRIC, "cores": 1, "kind": "port",
+                             "sample": "the whole workload: all 600 steps from the same start, FP64 oracle"},
+            "error": error_report(sc.bodies, rows0, rows_g, depth_g, rows_o, depth_o, m, inertia, 600,
+                                  "after 600 steps from the same start; the stacks topple chaotically, so "
+                                  "per-body positions diverge while heights, energy and penetration agree")}
+
+
+def batched_error(scene, ws_batched, steps: int = 360, worlds: int = 16) -> dict:
+    """The batched workload's error against the oracle: its first `worlds` worlds stepped `steps`
+    steps (the settle phase) by a batched GPU handle holding just them and by the oracle, one
+    oracle world per world."""
+    import copy
+    from crashcat_gb300 import world as W
+    from oracle import build as obuild, pyoracle
+    obuild.build()
+    parts = split_worlds(scene)[:worlds]
+    bodies = np.concatenate(parts)
+    ws = copy.deepcopy(ws_batched)
+    ws.num_worlds = worlds
+    g = W.GpuWorld(ws, len(bodies) + 8)
+    g.add_bodies(bodies)
+    rows0, _ = g.get_state()
+    g.step(scene.dt, steps)
+    rows_g, _ = g.get_state()
+    depth_g = g.get_manifolds()[:, 6]
+    del g
+    ws1 = copy.deepcopy(ws_batched)
+    ws1.num_worlds = 1
+    rows_o, depth_o = [], []
+    t0 = time.perf_counter()
+    for b in parts:
+        b = b.copy()
+        b["world"] = 0
+        o = pyoracle.OracleWorld(ws1, b)
+        o.step(scene.dt, steps)
+        rows_o.append(o.state())
+        depth_o.append(o.manifolds()[:, 6])
+    cpu_s = time.perf_counter() - t0
+    m, inertia = mass_properties(bodies)
+    rep = error_report(bodies, rows0, rows_g, depth_g, np.concatenate(rows_o), np.concatenate(depth_o), m, inertia,
+                       steps, f"the first {worlds} of the {scene.num_worlds} worlds ({len(bodies)} bodies), the "
+                              f"{steps} settle steps from spawn")
+    rep["oracle_seconds"] = cpu_s
+    return rep
+
+
+def joint_gaps(sc, rows) -> np.ndarray:
+    """Distance between the two bodies' anchor points of every hinge and swing-twist joint at the
+    poses in rows (the anchors taken in each body's frame at creation): 0 for a joint that holds."""
+    def rot(q, v):
+        u = q[..., :3]
+        t = 2.0 * np.cross(u, v)
+        return v + q[..., 3:4] * t + np.cross(u, t)
+
+    out = []
+    b = sc.bodies
+    r = np.asarray(rows, dtype=np.float64)
+    for recs, fa, fb in ((sc.hinges, "point_a", "point_b"), (sc.swings, "position_a", "position_b")):
+        if recs is None or len(recs) == 0:
+            continue
+        ends = []
+        for body_f, f in (("body_a", fa), ("body_b", fb)):
+            i = recs[body_f]
+            q0 = b["quaternion"][i].astype(np.float64) * np.array([-1, -1, -1, 1.0])
+            local = rot(q0, recs[f].astype(np.float64) - b["position"][i].astype(np.float64))
+            ends.append(r[i, 0:3] + rot(r[i, 3:7], local))
+        out.append(np.linalg.norm(ends[0] - ends[1], axis=1))
+    return np.concatenate(out) if out else np.zeros(0)
+
+
+def _ragdoll_worlds(sc, ws):
+    from crashcat_gb300 import world as W
+    from oracle import pyoracle
     g = W.GpuWorld(ws, sc.n + 16)
     g.add_bodies(sc.bodies)
     g.add_hinges(sc.hinges)
     g.add_swing_twists(sc.swings)
     g.set_skip_joint_pairs(True)
+    o = pyoracle.OracleWorld(ws, sc.bodies)
+    for h in sc.hinges:
+        o.add_hinge_record(h)
+    for h in sc.swings:
+        o.add_swing_twist_record(h)
+    o.set_skip_joint_pairs(True)
+    return g, o
+
+
+def ragdoll_measurement(cpu_seconds: float = 8.0):
+    """The jointed-ragdoll workload (2,000 ragdolls of 11 capsules at seeded random joint poses,
+    4 hinges and 6 swing-twist joints each, in a 60 m arena of static walls; dt 1/60, 12/4
+    iterations): all 600 steps from spawn on the GPU, timed per phase (falling, piling up,
+    resting pile).  The FP64 oracle on one host core: the first steps from spawn (the falling
+    phase) and a few steps of the resting pile from the GPU's state after 600 steps.  The error:
+    27 ragdolls in a 16 m arena (the same generator), 300 steps on the GPU and on the oracle."""
+    from crashcat_gb300 import scenes, world as W
+    from oracle import build as obuild
+    obuild.build()
+    sc = scenes.ragdolls()
+    ws = W.standard_settings(velocity_iterations=sc.velocity_iterations, position_iterations=sc.position_iterations)
+    g, o = _ragdoll_worlds(sc, ws)
     phases, total_ms, status = [], 0.0, 0
     for first, count in ((0, 100), (100, 400), (500, 100)):
         status |= g.step(sc.dt, count)
@@ -404,27 +677,51 @@ def ragdoll_measurement(cpu_seconds: float = 8.0):
                        "giant_islands": st["num_giant_islands"], "giant_colours": st["giant_colours"],
                        "manifolds": st["num_manifolds"]})
     rows, _ = g.get_state()
+    gaps_g = joint_gaps(sc, rows)
     del g
-    obuild.build()
-    o = pyoracle.OracleWorld(ws, sc.bodies)
-    for h in sc.hinges:
-        o.add_hinge_record(h)
-    for h in sc.swings:
-        o.add_swing_twist_record(h)
-    o.set_skip_joint_pairs(True)
     t0, k = time.perf_counter(), 0
     while time.perf_counter() - t0 < cpu_seconds and k < 100:
         o.step(sc.dt, 1)
         k += 1
     cpu_s = time.perf_counter() - t0
+    # the resting pile: the oracle from the GPU's state after the 600 steps (positions, orientations
+    # and velocities; its contact cache and joint impulses start empty)
+    st = o.state()
+    st[:, 0:13] = rows[:, 0:13]
+    o.set_state(st)
+    t0, kp = time.perf_counter(), 0
+    while time.perf_counter() - t0 < cpu_seconds and kp < 20:
+        o.step(sc.dt, 1)
+        kp += 1
+    pile_s = time.perf_counter() - t0
+    del o
+    # error against the oracle on a small arena of the same generator
+    se = scenes.ragdolls(num=27, arena=16.0)
+    ge, oe = _ragdoll_worlds(se, ws)
+    rows0, _ = ge.get_state()
+    ge.step(se.dt, 300)
+    oe.step(se.dt, 300)
+    rg, _ = ge.get_state()
+    ro = oe.state()
+    m, inertia = mass_properties(se.bodies)
+    err = error_report(se.bodies, rows0, rg, ge.get_manifolds()[:, 6], ro, oe.manifolds()[:, 6], m, inertia, 300,
+                       "27 ragdolls in a 16 m arena, 300 steps from spawn")
+    jg, jo = joint_gaps(se, rg), joint_gaps(se, ro)
+    err["joint_gap_m"] = {"gpu_max": float(jg.max()), "gpu_mean": float(jg.mean()), "oracle_max": float(jo.max()),
+                          "oracle_mean": float(jo.mean())}
     gpu_first = phases[0]["ms_per_step"]
     return {"workload": "ragdolls", "ragdolls": 2000, "bodies": int(sc.n), "hinges": int(len(sc.hinges)),
             "swing_twists": int(len(sc.swings)), "steps": 600, "value": sc.n * 600 / (total_ms * 1e-3),
             "unit": METRIC, "ms_per_step": total_ms / 600, "phases": phases, "status": int(status),
-            "finite": bool(np.isfinite(rows).all()),
+            "finite": bool(np.isfinite(rows).all()), "spawn": "seeded random joint poses inside 60 % of the limits",
+            "joint_gap_after_600_m": {"max": float(gaps_g.max()), "mean": float(gaps_g.mean())},
             "cpu_baseline": {"value": sc.n * k / cpu_s, "unit": METRIC, "cores": 1, "kind": "port",
                              "sample": f"first {k} steps from spawn (falling phase)",
-                             "gpu_same_phase_value": sc.n / (gpu_first * 1e-3)}}
+                             "gpu_same_phase_value": sc.n / (gpu_first * 1e-3)},
+            "cpu_baseline_pile": {"value": sc.n * kp / pile_s, "unit": METRIC, "cores": 1, "kind": "port",
+                                  "sample": f"{kp} steps of the resting pile from the GPU's state after 600 steps",
+                                  "gpu_same_phase_value": sc.n / (phases[2]["ms_per_step"] * 1e-3)},
+            "error": err}
 
 
 def terrain_rays(n: int, half: float, seed: int = 3) -> np.ndarray:
@@ -615,6 +912,17 @@ def terrain_measurement(cpu_seconds: float = 8.0):
         o.step(sc.dt, 1)
         k += 1
     cpu_s = time.perf_counter() - t0
+    # the settled pile: the oracle from the GPU's state after the 300 steps
+    st = o.state()
+    st[:, 0:13] = rows[:, 0:13]
+    o.set_state(st)
+    t0, kp = time.perf_counter(), 0
+    while time.perf_counter() - t0 < cpu_seconds and kp < 100:
+        o.step(sc.dt, 1)
+        kp += 1
+    pile_s = time.perf_counter() - t0
+    del o
+    err = terrain_error(ws)
     return {"workload": "terrain_mixed", "bodies": int(sc.n - 1), "triangles": int(len(mesh["triangles"])),
             "hulls": int(len(hulls)), "linear_cast_bodies": int((sc.bodies["motion_quality"] == 1).sum()),
             "steps": 300, "value": (sc.n - 1) * 300 / (total_ms * 1e-3), "unit": METRIC,
@@ -625,7 +933,43 @@ def terrain_measurement(cpu_seconds: float = 8.0):
             "shape_casts": sweeps,
             "cpu_baseline": {"value": (sc.n - 1) * k / cpu_s, "unit": METRIC, "cores": 1, "kind": "port",
                              "sample": f"first {k} steps from spawn (falling phase)",
-                             "gpu_same_phase_value": (sc.n - 1) / (phases[0]["ms_per_step"] * 1e-3)}}
+                             "gpu_same_phase_value": (sc.n - 1) / (phases[0]["ms_per_step"] * 1e-3)},
+            "cpu_baseline_pile": {"value": (sc.n - 1) * kp / pile_s, "unit": METRIC, "cores": 1, "kind": "port",
+                                  "sample": f"{kp} steps of the settled pile from the GPU's state after 300 steps",
+                                  "gpu_same_phase_value": (sc.n - 1) / (phases[2]["ms_per_step"] * 1e-3)},
+            "error": err}
+
+
+def terrain_error(ws, n: int = 600, cells: int = 48, steps: int = 200) -> dict:
+    """The terrain workload's error against the oracle on a scaled copy of its generator (n bodies
+    of every shape over a cells x cells heightfield with the same relief, drop heights and 20 %
+    LINEAR_CAST bodies): `steps` steps from spawn on the GPU and on the oracle, with the count of
+    bodies that ended below the terrain on each side."""
+    from crashcat_gb300 import scenes, world as W
+    from oracle import pyoracle
+    sc = scenes.mesh_drop(n=n, n_cells=cells, seed=2, amplitude=4.0, heights=(5.0, 40.0), fast_fraction=0.2)
+    g = W.GpuWorld(ws, sc.n + 16)
+    for p in sc.hull_points:
+        g.add_convex_hull(p)
+    g.add_triangle_mesh(*sc.mesh)
+    g.add_bodies(sc.bodies)
+    hulls = [g.get_convex_hull(i) for i in range(len(sc.hull_points))]
+    mesh = g.get_triangle_mesh(0)
+    rows0, _ = g.get_state()
+    g.step(sc.dt, steps)
+    rg, _ = g.get_state()
+    dg = g.get_manifolds()[:, 6]
+    del g
+    o = pyoracle.OracleWorld(ws, sc.bodies, hulls, [mesh])
+    o.step(sc.dt, steps)
+    ro = o.state()
+    m, inertia = mass_properties(sc.bodies, hulls)
+    rep = error_report(sc.bodies, rows0, rg, dg, ro, o.manifolds()[:, 6], m, inertia, steps,
+                       f"{n} bodies over a {cells} x {cells}-cell heightfield (the terrain generator scaled "
+                       f"down), {steps} steps from spawn")
+    rep["below_terrain"] = {"gpu": int((rg[1:, 1] < -2.5).sum()), "oracle": int((ro[1:, 1] < -2.5).sum()),
+                            "bodies": n}
+    return rep
 
 
 def single_world_comparison(scene, ws_batched, settled_rows, dt, steps: int, sample_worlds: int = 48):
@@ -752,6 +1096,8 @@ def run_gpu(args, rank, world_size, local):
             traffic = None
 
     single = single_world_comparison(scene, ws, settled_rows, dt, steps=max(3, min(args.steps, 10)))
+    cube_heap = cube_heap_measurement(peak, peak_kind) if args.cube_heap and rank == 0 else None
+    error = batched_error(scene, ws, steps=args.settle or 360) if args.errors and rank == 0 else None
     adjoint = adjoint_measurement() if args.adjoint else None
     ragdolls = ragdoll_measurement() if args.ragdolls and rank == 0 else None
     terrain = terrain_measurement() if args.terrain and rank == 0 else None
@@ -776,7 +1122,9 @@ def run_gpu(args, rank, world_size, local):
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                          "algorithmic_bytes_per_launch": bytes_dom, "stage_ms": prof},
             "cpu_baseline": cpu,
+            "error": error,
             "vs_single_world": single,
+            "cube_heap": cube_heap,
             "adjoint": adjoint,
             "ragdolls": ragdolls,
             "terrain": terrain,

@@ -65,6 +65,8 @@ class Settings(C.Structure):
         ("ccd_linear_cast_threshold", C.c_double),
         ("ccd_linear_cast_max_penetration", C.c_double),
         ("ccd_min_velocity_for_restitution", C.c_double),
+        ("device_wait_polls", C.c_int32),
+        ("island_link_attempts", C.c_int32),
     ]
 
 
@@ -126,6 +128,7 @@ BODY_DTYPE = np.dtype([
     ("friction_combine", np.int32), ("restitution_combine", np.int32),
     ("collision_groups", np.uint32), ("collision_mask", np.uint32), ("allowed_dofs", np.int32),
     ("motion_quality", np.int32),
+    ("num_velocity_steps_override", np.int32), ("num_position_steps_override", np.int32),
 ])
 MOTION_DISCRETE, MOTION_LINEAR_CAST = 0, 1
 
@@ -159,6 +162,7 @@ EXPORTS = {
     "cc_world_get_manifolds": ([C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
     "cc_world_get_stats": ([C.c_void_p, C.POINTER(Stats)], C.c_int),
     "cc_world_get_contact_events": ([C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
+    "cc_world_get_island_iterations": ([C.c_void_p, C.c_void_p], C.c_int),
     "cc_world_debug_islands": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
     "cc_world_profile_steps": ([C.c_void_p, C.c_float, C.c_int32, C.c_void_p, C.c_int32], C.c_int),
     "cc_world_rollout_grad": ([C.c_void_p, C.c_float, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -214,6 +218,7 @@ HINGE_DTYPE = np.dtype([
     ("target_angular_velocity", np.float32), ("target_angle", np.float32), ("motor_spring", SPRING_DTYPE),
     ("min_torque_limit", np.float32), ("max_torque_limit", np.float32),
     ("priority", np.int32), ("enabled", np.int32),
+    ("num_velocity_steps_override", np.int32), ("num_position_steps_override", np.int32),
 ])
 
 
@@ -247,6 +252,7 @@ SWING_TWIST_DTYPE = np.dtype([
     ("swing_min_torque_limit", np.float32), ("swing_max_torque_limit", np.float32),
     ("twist_min_torque_limit", np.float32), ("twist_max_torque_limit", np.float32),
     ("priority", np.int32), ("enabled", np.int32),
+    ("num_velocity_steps_override", np.int32), ("num_position_steps_override", np.int32),
 ])
 
 

@@ -253,53 +253,65 @@ void checkpoint_restore(DevWorld &w, const Checkpoint &c, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // loss and its gradient with respect to the final positions
 // ---------------------------------------------------------------------------
-__global__ void k_world_sums(DevWorld w, float4 *sums) {
+// Per-world sums of the dynamic bodies' positions in 40.24 fixed point: integer additions
+// commute, so the sums (and the loss and its gradient) do not depend on the order in which
+// threads add them.  sums: 4 per world (x, y, z, count).
+constexpr float WS_SCALE = 16777216.f;  // 2^24: 6e-8 m resolution, +-5e11 m of summed range
+__global__ void k_world_sums(DevWorld w, unsigned long long *sums) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
         if (motion_of(w.flags[i]) != DYNAMIC) continue;
         float4 p = w.pos[i];
-        float4 *s = sums + w.world[i];
-        atomicAdd(&s->x, p.x);
-        atomicAdd(&s->y, p.y);
-        atomicAdd(&s->z, p.z);
-        atomicAdd(&s->w, 1.f);
+        unsigned long long *s = sums + 4 * (size_t)w.world[i];
+        atomicAdd(&s[0], (unsigned long long)__float2ll_rn(p.x * WS_SCALE));
+        atomicAdd(&s[1], (unsigned long long)__float2ll_rn(p.y * WS_SCALE));
+        atomicAdd(&s[2], (unsigned long long)__float2ll_rn(p.z * WS_SCALE));
+        atomicAdd(&s[3], 1ull);
     }
 }
-__global__ void k_loss(int nw, const float4 *sums, const float *targets, float *loss) {
+__device__ __forceinline__ float4 world_centroid(const unsigned long long *sums, int k) {
+    const unsigned long long *s = sums + 4 * (size_t)k;
+    float c = (float)(long long)s[3];
+    if (!(c > 0.f)) return make_float4(0.f, 0.f, 0.f, 0.f);
+    double inv = 1.0 / ((double)WS_SCALE * (double)c);
+    return make_float4((float)((double)(long long)s[0] * inv), (float)((double)(long long)s[1] * inv),
+                       (float)((double)(long long)s[2] * inv), c);
+}
+__global__ void k_loss(int nw, const unsigned long long *sums, const float *targets, float *loss) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += gridDim.x * blockDim.x) {
-        float4 s = sums[k];
+        float4 c = world_centroid(sums, k);
         float l = 0.f;
-        if (s.w > 0.f) {
-            float3 d = f3(s.x / s.w - targets[3 * k], s.y / s.w - targets[3 * k + 1], s.z / s.w - targets[3 * k + 2]);
+        if (c.w > 0.f) {
+            float3 d = f3(c.x - targets[3 * k], c.y - targets[3 * k + 1], c.z - targets[3 * k + 2]);
             l = dot3(d, d);
         }
         loss[k] = l;
     }
 }
-__global__ void k_xbar(DevWorld w, const float4 *sums, const float *targets, float4 *xbar) {
+__global__ void k_xbar(DevWorld w, const unsigned long long *sums, const float *targets, float4 *xbar) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
         float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
         if (motion_of(w.flags[i]) == DYNAMIC) {
             int k = w.world[i];
-            float4 s = sums[k];
-            if (s.w > 0.f) {
-                float sc = 2.f / s.w;
-                g = make_float4((s.x / s.w - targets[3 * k]) * sc, (s.y / s.w - targets[3 * k + 1]) * sc,
-                                (s.z / s.w - targets[3 * k + 2]) * sc, 0.f);
+            float4 c = world_centroid(sums, k);
+            if (c.w > 0.f) {
+                float sc = 2.f / c.w;
+                g = make_float4((c.x - targets[3 * k]) * sc, (c.y - targets[3 * k + 1]) * sc,
+                                (c.z - targets[3 * k + 2]) * sc, 0.f);
             }
         }
         xbar[i] = g;
     }
 }
 
-void launch_rollout_loss(const DevWorld &w, const float *targets, float4 *sums, float *loss, AdjBuffers &a,
-                         cudaStream_t s) {
-    cudaMemsetAsync(sums, 0, sizeof(float4) * (size_t)w.num_worlds, s);
+void launch_rollout_loss(const DevWorld &w, const float *targets, unsigned long long *sums, float *loss,
+                         AdjBuffers &a, cudaStream_t s) {
+    cudaMemsetAsync(sums, 0, sizeof(unsigned long long) * 4 * (size_t)w.num_worlds, s);
     k_world_sums<<<grid_for(w.n, 256), 256, 0, s>>>(w, sums);
     k_loss<<<grid_for(w.num_worlds, 256), 256, 0, s>>>(w.num_worlds, sums, targets, loss);
     k_xbar<<<grid_for(w.n, 256), 256, 0, s>>>(w, sums, targets, a.xbar);
     cudaMemsetAsync(a.vbar, 0, sizeof(float4) * (size_t)w.n, s);
     cudaMemsetAsync(a.wbar, 0, sizeof(float4) * (size_t)w.n, s);
-    cudaMemsetAsync(a.mu_body, 0, sizeof(float) * (size_t)w.n, s);
+    cudaMemsetAsync(a.mu_body, 0, sizeof(unsigned long long) * (size_t)w.n, s);
     cudaMemsetAsync(a.mu_con, 0, sizeof(float) * (size_t)w.max_manifolds, s);
 }
 
@@ -654,8 +666,9 @@ __global__ void k_adj_mu(DevWorld w, TapeStep t, AdjBuffers a) {
         float da, db;
         combine_grad_friction(w.material[c.a].x, w.material[c.b].x, (fa >> F_FCOMB_SHIFT) & 7,
                               (fb >> F_FCOMB_SHIFT) & 7, da, db);
-        atomicAdd(&a.mu_body[c.a], g * da);
-        atomicAdd(&a.mu_body[c.b], g * db);
+        // integer sums: the same result whatever order the constraints of a body arrive in
+        atomicAdd(&a.mu_body[c.a], (unsigned long long)__double2ll_rn((double)(g * da) * ADJ_MU_SCALE));
+        atomicAdd(&a.mu_body[c.b], (unsigned long long)__double2ll_rn((double)(g * db) * ADJ_MU_SCALE));
     }
 }
 

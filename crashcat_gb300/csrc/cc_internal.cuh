@@ -102,6 +102,8 @@ struct DevSettings {
     uint32_t cast_pairs[CC_MAX_LAYERS];
     int small_island_max_cons;  // islands up to this many contacts run on one thread
     int small_island_max_joints;  // islands with joints: up to this many joints run on one thread
+    unsigned wait_polls;        // polls of a bounded device wait (grid barrier) before it gives up
+    int link_attempts;          // attempts of one union-find link before it gives up (OVF_ISLAND)
 };
 
 // Manifold produced by the narrowphase for one body pair (<= 4 points),
@@ -174,6 +176,7 @@ struct Checkpoint {
     CacheRecord *recs;
     int *parity;
 };
+constexpr double ADJ_MU_SCALE = 1073741824.0;  // 2^30: fixed-point scale of AdjBuffers::mu_body
 struct AdjBuffers {
     float4 *vbar, *wbar;    // adjoints of the linear / angular velocity
     float4 *xbar;           // dL/dx of each body
@@ -182,7 +185,7 @@ struct AdjBuffers {
     float *u_tape;          // pre-projection value of every row update: iterations x manifolds x 12
     float *lam_bar;         // adjoint of every row's impulse: manifolds x 12
     float *mu_con;          // dL/d(combined friction) per constraint
-    float *mu_body;         // dL/d(friction) per body
+    unsigned long long *mu_body;  // dL/d(friction) per body in 34.30 fixed point (order-free sums)
     float dt;
 };
 
@@ -222,6 +225,7 @@ struct DevJointHead {
     int priority, index;  // constraintPriority and the per-type creation index (sort key)
     int flags;            // JF_*
     int island;           // island of this step (-1: in none)
+    int iter_ovr;         // velocity | position << 8 iteration overrides (0: the world's counts)
 };
 // PointConstraintPart (point-constraint-part.ts)
 struct DevPoint {
@@ -344,6 +348,8 @@ struct DevWorld {
     int *island_body_off, *island_cons_off;
     int *island_bodies, *island_cons;
     int *island_fill_b, *island_fill_c;
+    uint32_t *iter_ovr;  // per body: velocity | position << 8 iteration overrides (0: the world's counts)
+    int *island_iters;   // per island: max velocity override, max position override, defaults wanted (bits 0/1)
     int *island_order;
     float4 *inv_inertia_world;   // 2 per body: xx xy xz yy | yz zz 0 0
     // scan scratch
@@ -569,6 +575,18 @@ __device__ inline Sym3 world_inv_inertia(float4 q, float4 inertia_rot, float3 d,
     return s;
 }
 
+// An island's iteration counts (islands.ts:344-386): the largest override among its dynamic
+// bodies and joints, raised to the world's count when any of them asks for the default (0).
+__device__ __forceinline__ void island_iterations(const DevWorld &w, int isl, int def_vel, int def_pos, int &vel,
+                                                  int &pos) {
+    const int *s = w.island_iters + 3 * (size_t)isl;
+    const int f = s[2];
+    vel = s[0];
+    pos = s[1];
+    if (f & 1) vel = vel > def_vel ? vel : def_vel;
+    if (f & 2) pos = pos > def_pos ? pos : def_pos;
+}
+
 // grid sizing: multiples of the current device's SM count (152 on GB300), read once per
 // device with cudaDevAttrMultiProcessorCount
 int device_sm_count();
@@ -653,7 +671,7 @@ void launch_tape_record(DevWorld &w, TapeStep &t, cudaStream_t s);
 void launch_tape_export(DevWorld &w, TapeStep &t, cc_tape_body *bodies, cc_tape_contact *cons, cudaStream_t s);
 void checkpoint_save(const DevWorld &w, Checkpoint &c, cudaStream_t s);
 void checkpoint_restore(DevWorld &w, const Checkpoint &c, cudaStream_t s);
-void launch_rollout_loss(const DevWorld &w, const float *targets, float4 *sums, float *loss, AdjBuffers &a,
+void launch_rollout_loss(const DevWorld &w, const float *targets, unsigned long long *sums, float *loss, AdjBuffers &a,
                          cudaStream_t s);
 void launch_adjoint_step(DevWorld &w, TapeStep &t, AdjBuffers &a, float dt, float ratio, const AdjHandoff &in,
                          const AdjHandoff &out, cudaStream_t s);

@@ -390,6 +390,7 @@ __global__ void k_uf_init(DevWorld w) {
         w.island_cons_count[i] = 0;
         w.island_fill_b[i] = 0;
         w.island_fill_c[i] = 0;
+        w.island_iters[3 * i] = w.island_iters[3 * i + 1] = w.island_iters[3 * i + 2] = 0;
         if (w.island_joint_count) {
             w.island_joint_count[i] = 0;
             w.island_fill_j[i] = 0;
@@ -398,9 +399,16 @@ __global__ void k_uf_init(DevWorld w) {
     }
 }
 
+// A union-find link that gave up leaves islands that may share bodies; the solve tiers then
+// skip the step rather than let two islands' solvers touch one body (the host reports
+// CC_ERR_CAPACITY for the step).
+__device__ __forceinline__ bool islands_failed(const DevWorld &w) {
+    return (*(volatile int *)&w.ctr->overflow & OVF_ISLAND) != 0;
+}
+
 // union of the sets of two bodies (bounded retry; gives up with an overflow flag)
 __device__ void uf_union(DevWorld &w, int a, int b) {
-    for (int guard = 0; guard < 1 << 20; guard++) {
+    for (int guard = 0; guard < c_settings.link_attempts; guard++) {
         int ra = uf_find(w.uf_parent, a), rb = uf_find(w.uf_parent, b);
         if (ra == rb) return;
         int hi = max(ra, rb), lo = min(ra, rb);
@@ -436,12 +444,25 @@ __global__ void k_uf_roots(DevWorld w, int *root_flag) {
     }
 }
 
+// a body's or joint's iteration overrides joining its island's (islands.ts:350-375)
+__device__ __forceinline__ void add_iteration_overrides(DevWorld &w, int isl, uint32_t ovr) {
+    int v = (int)(ovr & 0xffu), p = (int)((ovr >> 8) & 0xffu);
+    int *s = w.island_iters + 3 * (size_t)isl;
+    if (v > 0) atomicMax(&s[0], v);
+    if (p > 0) atomicMax(&s[1], p);
+    int f = (v == 0 ? 1 : 0) | (p == 0 ? 2 : 0);
+    if (f) atomicOr(&s[2], f);
+}
+
 __global__ void k_island_count(DevWorld w, const int *island_id_of_root) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
         int r = w.uf_parent[i];
         int isl = r >= 0 ? island_id_of_root[r] : -1;
         w.island_of_body[i] = isl;
-        if (isl >= 0) atomicAdd(&w.island_body_count[isl], 1);
+        if (isl >= 0) {
+            atomicAdd(&w.island_body_count[isl], 1);
+            if (motion_of(w.flags[i]) == DYNAMIC) add_iteration_overrides(w, isl, w.iter_ovr[i]);
+        }
     }
     int nm = min(w.ctr->num_manifolds, w.max_manifolds);
     for (int ci = blockIdx.x * blockDim.x + threadIdx.x; ci < nm; ci += gridDim.x * blockDim.x) {
@@ -465,7 +486,10 @@ __global__ void k_island_count(DevWorld w, const int *island_id_of_root) {
             }
         }
         h.island = isl;
-        if (isl >= 0) atomicAdd(&w.island_joint_count[isl], 1);
+        if (isl >= 0) {
+            atomicAdd(&w.island_joint_count[isl], 1);
+            add_iteration_overrides(w, isl, (uint32_t)h.iter_ovr);
+        }
     }
 }
 
@@ -848,10 +872,13 @@ __global__ void k_joint_setup(DevWorld w, float dt) {
 template <bool JOINTS>
 __global__ void __launch_bounds__(128) k_solve_small(DevWorld w, CacheTables ct, const int *small_list, float dt,
                                                       float ratio, int phase) {
+    if (islands_failed(w)) return;
     int ns = JOINTS ? w.ctr->num_small_joint_islands : w.ctr->num_small_islands;
     CacheRecord *crecs = ct.recs[*ct.parity];
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
         int isl = small_list[s];
+        int vel_iters, pos_iters;  // the island's iteration counts (islands.ts:344-386)
+        island_iterations(w, isl, c_settings.vel_iters, c_settings.pos_iters, vel_iters, pos_iters);
         int nb = w.island_body_count[isl], nc = w.island_cons_count[isl];
         int nj = JOINTS ? w.island_joint_count[isl] : 0;
         const int *bl = w.island_bodies + w.island_body_off[isl];
@@ -906,7 +933,7 @@ __global__ void __launch_bounds__(128) k_solve_small(DevWorld w, CacheTables ct,
         }
         if (vel) {
             if (nc > 0 || nj > 0) {
-                for (int it = 0; it < c_settings.vel_iters; it++) {
+                for (int it = 0; it < vel_iters; it++) {
                     for (int k = 0; k < nc; k++) {
                         ContactConstraint &c = w.cons[order[k]];
                         BodyRef A = load_body(w, c.a), B = load_body(w, c.b);
@@ -922,7 +949,7 @@ __global__ void __launch_bounds__(128) k_solve_small(DevWorld w, CacheTables ct,
             if (phase == SOLVE_VELOCITY) continue;
         }
         if (nc > 0 || nj > 0) {
-            for (int it = 0; it < c_settings.pos_iters; it++) {
+            for (int it = 0; it < pos_iters; it++) {
                 bool any = false;
                 for (int k = 0; k < nc; k++) {
                     const ContactConstraint &c = w.cons[order[k]];
@@ -973,6 +1000,7 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
                                                               int *scratch_order, int *scratch_colour,
                                                               int *scratch_claim, float dt, float ratio,
                                                               int phase) {
+    if (islands_failed(w)) return;
     __shared__ int s_any;
     __shared__ int s_ncol;
     __shared__ int s_colour_start[257];
@@ -981,6 +1009,8 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
     CacheRecord *crecs = ct.recs[*ct.parity];
     for (int li = blockIdx.x; li < nl; li += gridDim.x) {
         int isl = large_list[li];
+        int vel_iters, pos_iters;
+        island_iterations(w, isl, c_settings.vel_iters, c_settings.pos_iters, vel_iters, pos_iters);
         int nb = w.island_body_count[isl], nc = w.island_cons_count[isl];
         const int *bl = w.island_bodies + w.island_body_off[isl];
         const int *cl = w.island_cons + w.island_cons_off[isl];
@@ -1190,7 +1220,7 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
                     __syncthreads();
                 }
             }
-            for (int it = 0; it < c_settings.vel_iters; it++) {
+            for (int it = 0; it < vel_iters; it++) {
                 sweep(1);
                 if (nj > 0) {
                     __syncthreads();
@@ -1202,7 +1232,7 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
             __syncthreads();
             if (phase == SOLVE_VELOCITY) continue;
         }
-        for (int it = 0; it < c_settings.pos_iters; it++) {
+        for (int it = 0; it < pos_iters; it++) {
             if (threadIdx.x == 0) s_any = 0;
             __syncthreads();
             for (int c = 0; c <= 256; c++) {
@@ -1312,6 +1342,7 @@ __device__ __forceinline__ void warp_store(WarpIsland &s, int local, const BodyR
 
 __global__ void __launch_bounds__(WARP_BLOCK) k_solve_warp(DevWorld w, CacheTables ct, float dt, float ratio,
                                                             int phase) {
+    if (islands_failed(w)) return;
     extern __shared__ WarpIsland s_isl[];  // WARPS_PER_BLOCK entries
     const int lane = threadIdx.x & 31;
     WarpIsland &S = s_isl[threadIdx.x >> 5];
@@ -1324,6 +1355,8 @@ __global__ void __launch_bounds__(WARP_BLOCK) k_solve_warp(DevWorld w, CacheTabl
         li = __shfl_sync(FULL, li, 0);
         if (li >= nmid) break;
         const int isl = w.mid_list[li];
+        int vel_iters, pos_iters;
+        island_iterations(w, isl, c_settings.vel_iters, c_settings.pos_iters, vel_iters, pos_iters);
         const int nb = w.island_body_count[isl], nc = w.island_cons_count[isl];
         const int *bl = w.island_bodies + w.island_body_off[isl];
         const int *cl = w.island_cons + w.island_cons_off[isl];
@@ -1449,7 +1482,7 @@ __global__ void __launch_bounds__(WARP_BLOCK) k_solve_warp(DevWorld w, CacheTabl
         __syncwarp();
         // warm start and velocity iterations, colour by colour
         const bool vel = phase != SOLVE_POSITION;
-        for (int pass = (c_settings.warm_starting ? -1 : 0); vel && pass < c_settings.vel_iters; pass++) {
+        for (int pass = (c_settings.warm_starting ? -1 : 0); vel && pass < vel_iters; pass++) {
             for (int c = 0; c < nsweep; c++) {
                 int s0 = S.cstart[c], s1 = S.cstart[c + 1];
                 bool serial = tail && c == ncol;
@@ -1486,7 +1519,7 @@ __global__ void __launch_bounds__(WARP_BLOCK) k_solve_warp(DevWorld w, CacheTabl
             if (phase == SOLVE_VELOCITY) continue;
         }
         // position iterations (contact-constraints.ts:1098-1216), early exit as update.ts:218-221
-        for (int it = 0; it < c_settings.pos_iters; it++) {
+        for (int it = 0; it < pos_iters; it++) {
             bool any = false;
             for (int c = 0; c < nsweep; c++) {
                 int s0 = S.cstart[c], s1 = S.cstart[c + 1];
@@ -1546,7 +1579,6 @@ __global__ void __launch_bounds__(WARP_BLOCK) k_solve_warp(DevWorld w, CacheTabl
 //                change the result.
 // ---------------------------------------------------------------------------
 constexpr int GIANT_BLOCK = 256;
-constexpr unsigned GIANT_SPIN_LIMIT = 1u << 21;  // polls (each ~100 ns or more) before a barrier gives up
 
 // Grid barrier over the co-resident blocks of the cooperative launch.  The wait is bounded:
 // a block that gives up raises bar_error and OVF_TIMEOUT, and every block then leaves.
@@ -1566,7 +1598,7 @@ __device__ bool grid_barrier(DevCounters *ctr, unsigned nblocks) {
         } else {
             unsigned spins = 0;
             while (*gen == g) {
-                if (*err || ++spins > GIANT_SPIN_LIMIT) {
+                if (*err || ++spins > c_settings.wait_polls) {
                     atomicExch(&ctr->bar_error, 1);
                     atomicOr(&ctr->overflow, OVF_TIMEOUT);
                     ok = 0;
@@ -1597,7 +1629,7 @@ __global__ void __launch_bounds__(GIANT_BLOCK) k_solve_giant(DevWorld w, CacheTa
                                                               int phase) {
     DevCounters *ctr = w.ctr;
     const int ng = ctr->num_giant_islands;
-    if (ng == 0) return;
+    if (ng == 0 || islands_failed(w)) return;
     const unsigned nblk = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
     CacheRecord *crecs = ct.recs[*ct.parity];
@@ -1608,6 +1640,8 @@ __global__ void __launch_bounds__(GIANT_BLOCK) k_solve_giant(DevWorld w, CacheTa
     const unsigned long long NONE = ~0ull;
     for (int g = 0; g < ng; g++) {
         int isl = w.giant_list[g];
+        int vel_iters, pos_iters;
+        island_iterations(w, isl, c_settings.vel_iters, c_settings.pos_iters, vel_iters, pos_iters);
         int nb = w.island_body_count[isl], nc = w.island_cons_count[isl];
         int nj = joint_total(w) > 0 ? w.island_joint_count[isl] : 0;
         const int *bl = w.island_bodies + w.island_body_off[isl];
@@ -1810,7 +1844,7 @@ __global__ void __launch_bounds__(GIANT_BLOCK) k_solve_giant(DevWorld w, CacheTa
             if (c_settings.warm_starting) {
                 if (!sweep(false, 0, dummy) || !sweep(true, 0, dummy)) return;
             }
-            for (int it = 0; it < c_settings.vel_iters; it++)
+            for (int it = 0; it < vel_iters; it++)
                 if (!sweep(false, 1, dummy) || !sweep(true, 1, dummy)) return;
             for (int k = tid; k < nc; k += nthr) store_impulses(w, crecs, w.cons[cl[k]]);
             for (int k = tid; k < nb; k += nthr) integrate_body(w, bl[k], dt, phase == SOLVE_VELOCITY);
@@ -1818,7 +1852,7 @@ __global__ void __launch_bounds__(GIANT_BLOCK) k_solve_giant(DevWorld w, CacheTa
             if (!grid_barrier(ctr, nblk)) return;
             if (phase == SOLVE_VELOCITY) continue;
         }
-        for (int it = 0; it < c_settings.pos_iters; it++) {
+        for (int it = 0; it < pos_iters; it++) {
             int p = it & 1, any = 0;
             if (!sweep(false, 2, any) || !sweep(true, 2, any)) return;
             any = __syncthreads_or(any);

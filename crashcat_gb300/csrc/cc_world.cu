@@ -32,6 +32,7 @@ struct cc_world {
     double prev_dt = 0.0;
     int steps_done = 0;
     int last_status = CC_OK;
+    bool any_iter_override = false;  // a body or joint overrides the iteration counts
     DevCounters last_ctr{};
     std::vector<uint64_t> ids;
     std::vector<DevHinge> hinges;  // host copy of each joint as created (bodies, flags, limits, motors)
@@ -59,7 +60,7 @@ struct cc_world {
         std::vector<double> ckpt_prev_dt;
         AdjBuffers buf{};
         AdjHandoff hand[2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-        float4 *sums = nullptr;
+        unsigned long long *sums = nullptr;  // per world: fixed-point x, y, z sums and the count
         float *d_targets = nullptr, *d_loss = nullptr;
         std::vector<void *> allocs;
     } adj;
@@ -295,6 +296,8 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
     d.allow_sleeping = s->allow_sleeping;
     d.time_before_sleep = (float)s->time_before_sleep;
     d.sleep_threshold = (float)s->point_velocity_sleep_threshold;
+    d.wait_polls = s->device_wait_polls > 0 ? (unsigned)s->device_wait_polls : (1u << 21);
+    d.link_attempts = s->island_link_attempts > 0 ? s->island_link_attempts : (1 << 20);
     d.ccd_threshold = (float)s->ccd_linear_cast_threshold;
     d.ccd_max_penetration = (float)s->ccd_linear_cast_max_penetration;
     d.ccd_min_vel_restitution = (float)s->ccd_min_velocity_for_restitution;
@@ -392,6 +395,8 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
     ALLOC(island_cons, w.max_manifolds);
     ALLOC(island_fill_b, cap);
     ALLOC(island_fill_c, cap);
+    ALLOC(iter_ovr, cap);
+    ALLOC(island_iters, 3 * cap);
     ALLOC(inv_inertia_world, 2 * (size_t)cap);
     {
         size_t tmp = scan_tmp_ints(cap > w.max_manifolds ? cap : w.max_manifolds);
@@ -512,7 +517,7 @@ int cc_world_destroy(cc_world *W) {
                     w.node_parent, w.node_child, w.node_lo, w.node_hi, w.node_flag, w.pairs, w.manifolds, w.cons,
                     w.cons_of_manifold, w.uf_parent, w.island_of_body, w.island_id_of_root, w.island_body_count,
                     w.island_cons_count, w.island_body_off, w.island_cons_off, w.island_bodies, w.island_cons,
-                    w.island_fill_b, w.island_fill_c, w.inv_inertia_world, w.scan_tmp, w.ctr, w.scene,
+                    w.island_fill_b, w.island_fill_c, w.iter_ovr, w.island_iters, w.inv_inertia_world, w.scan_tmp, w.ctr, w.scene,
                     w.node_world, w.epa_items, w.epa_packed, w.epa_scratch, w.epa_fallback, w.cache_keys[0], w.cache_keys[1], w.cache_recs[0],
                     w.cache_recs[1], w.cache_parity, w.root_flag, w.small_list, w.large_list, w.scratch_order,
                     w.scratch_colour, w.scratch_claim, w.mid_list, w.body_local, w.contact_event,
@@ -562,7 +567,7 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
     if (w.n + n > w.cap) return CC_ERR_CAPACITY;
     std::vector<float4> pos(n), quat(n), com(n), lin(n), ang(n), zero(n), ii(n), ir(n), sh(n), mat(n), damp(n),
         sph(3 * (size_t)n);
-    std::vector<uint32_t> flags(n);
+    std::vector<uint32_t> flags(n), ovr(n);
     std::vector<uint2> groups(n);
     std::vector<int> world(n);
     std::vector<float> timer(n, 0.f);
@@ -597,6 +602,11 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
         if (d.motion_quality != CC_MOTION_DISCRETE && d.motion_quality != CC_MOTION_LINEAR_CAST) return CC_ERR_INVALID;
         if (d.object_layer < 0 || d.object_layer >= W->settings.num_object_layers) return CC_ERR_INVALID;
         if (d.world < 0 || d.world >= w.num_worlds) return CC_ERR_INVALID;
+        if (d.num_velocity_steps_override < 0 || d.num_velocity_steps_override > 255 ||
+            d.num_position_steps_override < 0 || d.num_position_steps_override > 255)
+            return CC_ERR_INVALID;
+        ovr[i] = (uint32_t)d.num_velocity_steps_override | ((uint32_t)d.num_position_steps_override << 8);
+        if (ovr[i]) W->any_iter_override = true;
         double mass;
         double idiag[3];
         double irot[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};  // principal axes (columns)
@@ -736,6 +746,7 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
     CC_TRY(cudaMemcpyAsync(w.material + o, mat.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
     CC_TRY(cudaMemcpyAsync(w.damping + o, damp.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
     CC_TRY(cudaMemcpyAsync(w.flags + o, flags.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s));
+    CC_TRY(cudaMemcpyAsync(w.iter_ovr + o, ovr.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s));
     CC_TRY(cudaMemcpyAsync(w.groups + o, groups.data(), sizeof(uint2) * n, cudaMemcpyHostToDevice, s));
     CC_TRY(cudaMemcpyAsync(w.world + o, world.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
     CC_TRY(cudaMemcpyAsync(w.sleep_sph + 3 * o, sph.data(), sizeof(float4) * 3 * n, cudaMemcpyHostToDevice, s));
@@ -1196,6 +1207,29 @@ int cc_world_debug_islands(cc_world *W, int32_t *island_of_body, int32_t *cons_r
     return CC_OK;
 }
 
+int cc_world_get_island_iterations(cc_world *W, int32_t *out) {
+    if (!W || !out) return CC_ERR_INVALID;
+    DevWorld &w = W->w;
+    if (w.n == 0) return CC_OK;
+    int ni = W->last_ctr.num_islands;
+    std::vector<int> iob((size_t)w.n), it(3 * (size_t)(ni > 0 ? ni : 1));
+    CC_TRY(cudaMemcpy(iob.data(), w.island_of_body, sizeof(int) * w.n, cudaMemcpyDeviceToHost));
+    if (ni > 0) CC_TRY(cudaMemcpy(it.data(), w.island_iters, sizeof(int) * 3 * (size_t)ni, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < w.n; i++) {
+        int isl = iob[i];
+        if (isl < 0 || isl >= ni) {
+            out[2 * i] = out[2 * i + 1] = -1;
+            continue;
+        }
+        int v = it[3 * isl], p = it[3 * isl + 1], f = it[3 * isl + 2];
+        if (f & 1) v = v > W->settings.velocity_iterations ? v : W->settings.velocity_iterations;
+        if (f & 2) p = p > W->settings.position_iterations ? p : W->settings.position_iterations;
+        out[2 * i] = v;
+        out[2 * i + 1] = p;
+    }
+    return CC_OK;
+}
+
 // Stage profiler: runs n_steps with CUDA events between the stages and returns the
 // mean milliseconds of each stage: integrate forces, broadphase, narrowphase (GJK,
 // faces, clipping), EPA, contacts + islands, per-thread island solve, per-CTA island
@@ -1384,7 +1418,7 @@ static int ensure_adjoint(cc_world *W, int seg_len, int n_ckpt) {
         AA(A.hand[k].keys, cc);
         AA(A.hand[k].vals, cc * 12);
     }
-    AA(A.sums, (size_t)w.num_worlds);
+    AA(A.sums, 4 * (size_t)w.num_worlds);
     AA(A.d_targets, 3 * (size_t)w.num_worlds);
     AA(A.d_loss, (size_t)w.num_worlds);
 #undef AA
@@ -1406,7 +1440,7 @@ extern "C" int cc_world_rollout_grad(cc_world *W, float dt, int32_t n_steps, int
     DevWorld &w = W->w;
     if (w.n == 0) return CC_ERR_INVALID;
     // the adjoint covers contacts and the discrete integration only
-    if (w.num_hinges + w.num_swings > 0 || w.num_linear_cast > 0) return CC_ERR_UNSUPPORTED;
+    if (w.num_hinges + w.num_swings > 0 || w.num_linear_cast > 0 || W->any_iter_override) return CC_ERR_UNSUPPORTED;
     int K = checkpoint_every < n_steps ? checkpoint_every : n_steps;
     int nseg = (n_steps + K - 1) / K;
     int r = ensure_adjoint(W, K, nseg + 1);
@@ -1456,8 +1490,12 @@ extern "C" int cc_world_rollout_grad(cc_world *W, float dt, int32_t n_steps, int
     CC_TRY(cudaEventRecord(W->ev_end, s));
     std::vector<float4> tmp((size_t)w.n);
     if (loss) CC_TRY(cudaMemcpyAsync(loss, A.d_loss, sizeof(float) * w.num_worlds, cudaMemcpyDeviceToHost, s));
-    if (grad_friction)
-        CC_TRY(cudaMemcpyAsync(grad_friction, A.buf.mu_body, sizeof(float) * w.n, cudaMemcpyDeviceToHost, s));
+    std::vector<unsigned long long> mu_fx;
+    if (grad_friction) {
+        mu_fx.resize((size_t)w.n);
+        CC_TRY(cudaMemcpyAsync(mu_fx.data(), A.buf.mu_body, sizeof(unsigned long long) * w.n, cudaMemcpyDeviceToHost,
+                               s));
+    }
     for (int k = 0; k < 2; k++) {
         float *out = k == 0 ? grad_linvel : grad_angvel;
         if (!out) continue;
@@ -1472,6 +1510,8 @@ extern "C" int cc_world_rollout_grad(cc_world *W, float dt, int32_t n_steps, int
     }
     CC_TRY(cudaStreamSynchronize(s));
     CC_TRY(cudaGetLastError());
+    if (grad_friction)
+        for (int i = 0; i < w.n; i++) grad_friction[i] = (float)((double)(long long)mu_fx[i] / ADJ_MU_SCALE);
     cudaEventElapsedTime(&W->last_call_ms, W->ev_begin, W->ev_end);
     W->last_ctr = *W->h_ctr;
     return CC_OK;
@@ -1653,6 +1693,11 @@ int cc_world_add_hinges(cc_world *W, const cc_hinge_desc *d, int32_t n, int32_t 
         j.h.a = h.body_a;
         j.h.b = h.body_b;
         j.h.index = w.num_hinges + i;
+        if (h.num_velocity_steps_override < 0 || h.num_velocity_steps_override > 255 ||
+            h.num_position_steps_override < 0 || h.num_position_steps_override > 255)
+            return CC_ERR_INVALID;
+        j.h.iter_ovr = (int)((uint32_t)h.num_velocity_steps_override | ((uint32_t)h.num_position_steps_override << 8));
+        if (j.h.iter_ovr) W->any_iter_override = true;
         j.h.priority = h.priority;
         j.h.island = -1;
         DQ qa = dq(quat[j.h.a]), qb = dq(quat[j.h.b]);
@@ -1857,6 +1902,11 @@ int cc_world_add_swing_twists(cc_world *W, const cc_swing_twist_desc *d, int32_t
         j.h.a = h.body_a;
         j.h.b = h.body_b;
         j.h.index = w.num_swings + i;
+        if (h.num_velocity_steps_override < 0 || h.num_velocity_steps_override > 255 ||
+            h.num_position_steps_override < 0 || h.num_position_steps_override > 255)
+            return CC_ERR_INVALID;
+        j.h.iter_ovr = (int)((uint32_t)h.num_velocity_steps_override | ((uint32_t)h.num_position_steps_override << 8));
+        if (j.h.iter_ovr) W->any_iter_override = true;
         j.h.priority = h.priority;
         j.h.island = -1;
         j.h.flags = h.enabled ? JF_ENABLED : 0;

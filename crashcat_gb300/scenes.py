@@ -493,9 +493,11 @@ def _qmul(a, b):
 
 
 def _qrot(q, v):
-    u = np.asarray(q[:3], dtype=np.float64)
-    t = 2.0 * np.cross(u, v)
-    return np.asarray(v, dtype=np.float64) + q[3] * t + np.cross(u, t)
+    ux, uy, uz, w = float(q[0]), float(q[1]), float(q[2]), float(q[3])
+    vx, vy, vz = float(v[0]), float(v[1]), float(v[2])
+    tx, ty, tz = 2.0 * (uy * vz - uz * vy), 2.0 * (uz * vx - ux * vz), 2.0 * (ux * vy - uy * vx)
+    return np.array([vx + w * tx + (uy * tz - uz * ty), vy + w * ty + (uz * tx - ux * tz),
+                     vz + w * tz + (ux * ty - uy * tx)])
 
 
 def _tangent(axis):
@@ -552,15 +554,125 @@ def _ragdoll_parts(scale: float = 1.8):
     return parts, joints
 
 
+def _rot(axis, angle):
+    """Rotation matrix of `angle` about the unit `axis`."""
+    a = np.asarray(axis, dtype=np.float64)
+    a = a / np.linalg.norm(a)
+    K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    return np.eye(3) + math.sin(angle) * K + (1 - math.cos(angle)) * (K @ K)
+
+
+def _mat_to_quat(R):
+    """Unit quaternion (x, y, z, w) of a rotation matrix."""
+    tr = R[0, 0] + R[1, 1] + R[2, 2]
+    if tr > 0:
+        s = math.sqrt(tr + 1.0) * 2
+        q = [(R[2, 1] - R[1, 2]) / s, (R[0, 2] - R[2, 0]) / s, (R[1, 0] - R[0, 1]) / s, 0.25 * s]
+    elif R[0, 0] > R[1, 1] and R[0, 0] > R[2, 2]:
+        s = math.sqrt(1.0 + R[0, 0] - R[1, 1] - R[2, 2]) * 2
+        q = [0.25 * s, (R[0, 1] + R[1, 0]) / s, (R[0, 2] + R[2, 0]) / s, (R[2, 1] - R[1, 2]) / s]
+    elif R[1, 1] > R[2, 2]:
+        s = math.sqrt(1.0 + R[1, 1] - R[0, 0] - R[2, 2]) * 2
+        q = [(R[0, 1] + R[1, 0]) / s, 0.25 * s, (R[1, 2] + R[2, 1]) / s, (R[0, 2] - R[2, 0]) / s]
+    else:
+        s = math.sqrt(1.0 + R[2, 2] - R[0, 0] - R[1, 1]) * 2
+        q = [(R[0, 2] + R[2, 0]) / s, (R[1, 2] + R[2, 1]) / s, 0.25 * s, (R[1, 0] - R[0, 1]) / s]
+    q = np.array(q)
+    return q / np.linalg.norm(q)
+
+
+def _segment_distances(p0, p1, q0, q1):
+    """Distances between the segments p0[k]-p1[k] and q0[k]-q1[k] (clamped closest points)."""
+    d1, d2, r = p1 - p0, q1 - q0, p0 - q0
+    a, e, f = (d1 * d1).sum(1), (d2 * d2).sum(1), (d2 * r).sum(1)
+    c, b = (d1 * r).sum(1), (d1 * d2).sum(1)
+    den = a * e - b * b
+    s = np.where(den > 1e-12, np.clip((b * f - c * e) / np.where(den > 1e-12, den, 1.0), 0.0, 1.0), 0.0)
+    t = (b * s + f) / e
+    lo, hi = t < 0.0, t > 1.0
+    s = np.where(lo, np.clip(-c / a, 0.0, 1.0), np.where(hi, np.clip((b - c) / a, 0.0, 1.0), s))
+    t = np.clip(t, 0.0, 1.0)
+    return np.linalg.norm((p0 + d1 * s[:, None]) - (q0 + d2 * t[:, None]), axis=1)
+
+
+def _pose_overlaps(T, parts, joints, margin: float = 0.05) -> bool:
+    """Whether two parts that share no joint overlap (capsule segments closer than their radii)."""
+    names = list(parts)
+    joined = {frozenset((na, nb)) for _, na, nb, _, _ in joints}
+    ends0, ends1, rad = [], [], []
+    for name in names:
+        c, axis, length, thick = parts[name]
+        R, t = T[name]
+        hh = max(length / 2 - thick / 2, 0.05)
+        ax = R @ np.asarray(axis, dtype=np.float64) * hh
+        mid = R @ np.asarray(c, dtype=np.float64) + t
+        ends0.append(mid - ax)
+        ends1.append(mid + ax)
+        rad.append(thick / 2)
+    ii, jj = zip(*[(i, j) for i in range(len(names)) for j in range(i + 1, len(names))
+                   if frozenset((names[i], names[j])) not in joined])
+    ii, jj = np.array(ii), np.array(jj)
+    e0, e1, rad = np.array(ends0), np.array(ends1), np.array(rad)
+    d = _segment_distances(e0[ii], e1[ii], e0[jj], e1[jj])
+    return bool((d < rad[ii] + rad[jj] + margin).any())
+
+
+def _ragdoll_pose(rng, parts, joints, cones, twist, fill: float = 0.6, tries: int = 64):
+    """A seeded random pose: every joint turned by a random angle inside `fill` of its limits,
+    the parts placed by walking the joint tree out from the upper body; poses in which two parts
+    that share no joint overlap are drawn again.  Returns per part the rotation R and
+    translation t of the pose in the ragdoll frame (rest point x -> R x + t)."""
+    for _ in range(tries):
+        T = _ragdoll_pose_once(rng, parts, joints, cones, twist, fill)
+        if not _pose_overlaps(T, parts, joints):
+            return T
+    return {name: (np.eye(3), np.zeros(3)) for name in parts}
+
+
+def _ragdoll_pose_once(rng, parts, joints, cones, twist, fill):
+    T = {name: (np.eye(3), np.zeros(3)) for name in parts}
+    placed = {"upper_body"}
+    done = set()
+    while len(done) < len(joints):
+        for j, (kind, na, nbn, piv, axis) in enumerate(joints):
+            if j in done or (na in placed) == (nbn in placed):
+                continue
+            child, parent = (na, nbn) if nbn in placed else (nbn, na)
+            a = np.asarray(axis, dtype=np.float64)
+            if kind == "hinge":
+                lo, hi = (-2.0, 0.05) if axis[0] else (-0.05, 2.2)
+                theta = rng.uniform(lo, hi) * fill
+                # the hinge angle is B's rotation relative to A about the axis; the child is A
+                Rj = _rot(a, -theta if child == na else theta)
+            else:
+                u = _tangent(a)
+                v = np.cross(a, u)
+                phi = rng.uniform(0.0, 2 * math.pi)
+                s_axis = math.cos(phi) * u + math.sin(phi) * v
+                Rj = _rot(s_axis, rng.uniform(0.0, fill * cones[j])) @ _rot(a, rng.uniform(-fill, fill) * twist)
+            Rp, tp = T[parent]
+            P = Rp @ np.asarray(piv, dtype=np.float64) + tp
+            Rw = Rp @ Rj @ Rp.T
+            T[child] = (Rw @ Rp, Rw @ (tp - P) + P)
+            placed.add(child)
+            done.add(j)
+    return T
+
+
 def ragdolls(num: int = 2000, seed: int = 3, arena: float = 60.0, spacing: float = 4.4,
-             cone_deg=(30.0, 80.0), twist_deg: float = 45.0) -> Scene:
+             cone_deg=(30.0, 80.0), twist_deg: float = 45.0, random_poses: bool = True) -> Scene:
     """Jointed ragdolls: per ragdoll 11 capsule bodies (the ragdoll example's parts and
     sizes at scale 1.8) joined by 4 hinges (knees, elbows) and 6 swing-twist joints (neck,
     spine, hips, shoulders; cone half-angles drawn from U(30, 80) degrees per joint, twist
     limits +-45 degrees, motors off), each ragdoll at a seeded random orientation on a grid
-    inside an arena of 6 static walls (a 60 m box).  Joined bodies do not collide (the
-    ragdoll example's pair filter); dt 1/60, 12 velocity / 4 position iterations."""
+    inside an arena of 6 static walls (a 60 m box).  With random_poses every joint starts
+    turned by a seeded random angle inside 60 % of its limits (hinges along their axis, swing
+    about a random axis across the twist axis plus a twist); the joints are created in that
+    pose, each body's joint axes turned with it, so the pose is a bend of the joint and not its
+    zero.  Joined bodies do not collide (the ragdoll example's pair filter); dt 1/60, 12
+    velocity / 4 position iterations."""
     rng = np.random.Generator(np.random.PCG64(seed))
+    pose_rng = np.random.Generator(np.random.PCG64(seed + 1000))
     parts, joints = _ragdoll_parts()
     names = list(parts)
     nb_r = len(names)
@@ -589,6 +701,9 @@ def ragdolls(num: int = 2000, seed: int = 3, arena: float = 60.0, spacing: float
         origin = np.array([-half + 1.0 + spacing * (i + 0.5), 1.0 + spacing * (j + 0.5), -half + 1.0 + spacing * (k + 0.5)])
         q = rng.normal(size=4)
         q /= np.linalg.norm(q)
+        cones = [np.radians(rng.uniform(*cone_deg)) if kind == "swing" else 0.0 for kind, *_ in joints]
+        T = (_ragdoll_pose(pose_rng, parts, joints, cones, np.radians(twist_deg)) if random_poses
+             else {name: (np.eye(3), np.zeros(3)) for name in parts})
         base = walls + r * nb_r
         idx = {}
         for p, name in enumerate(names):
@@ -597,34 +712,38 @@ def ragdolls(num: int = 2000, seed: int = 3, arena: float = 60.0, spacing: float
             idx[name] = bi
             radius = thick / 2
             set_capsule(b, bi, radius, max(length / 2 - radius, 0.05))
-            b["position"][bi] = origin + _qrot(q, np.asarray(c) - centre)
+            R, t = T[name]
+            b["position"][bi] = origin + _qrot(q, R @ np.asarray(c, dtype=np.float64) + t - centre)
             # capsules lie along local Y: arms are turned onto X
             qp = np.array([0.0, 0.0, -math.sin(math.pi / 4), math.cos(math.pi / 4)]) if axis[0] else np.array([0, 0, 0, 1.0])
-            b["quaternion"][bi] = _qmul(q, qp)
+            b["quaternion"][bi] = _qmul(_qmul(q, _mat_to_quat(R)), qp)
             b["restitution"][bi] = 0.0
-        for kind, na, nbn, piv, axis in joints:
-            pw = origin + _qrot(q, np.asarray(piv, dtype=np.float64) - centre)
-            aw = _qrot(q, np.asarray(axis, dtype=np.float64))
+
+        def turned(name, v):  # a rest-frame direction carried by a part's pose, then the ragdoll's orientation
+            return _qrot(q, T[name][0] @ np.asarray(v, dtype=np.float64))
+
+        for jn, (kind, na, nbn, piv, axis) in enumerate(joints):
+            RB, tB = T[nbn]
+            pw = origin + _qrot(q, RB @ np.asarray(piv, dtype=np.float64) + tB - centre)
             if kind == "hinge":
                 h = h_all[hk]
                 hk += 1
                 h["body_a"], h["body_b"] = idx[na], idx[nbn]
                 h["point_a"] = h["point_b"] = pw
-                h["hinge_axis_a"] = h["hinge_axis_b"] = aw
-                limb = _qrot(q, np.array([1.0, 0, 0]) if axis[2] else np.array([0, 1.0, 0]))
-                h["normal_axis_a"] = h["normal_axis_b"] = limb
+                h["hinge_axis_a"], h["hinge_axis_b"] = turned(na, axis), turned(nbn, axis)
+                limb = np.array([1.0, 0, 0]) if axis[2] else np.array([0, 1.0, 0])
+                h["normal_axis_a"], h["normal_axis_b"] = turned(na, limb), turned(nbn, limb)
                 h["limits_min"], h["limits_max"] = (-2.0, 0.05) if axis[0] else (-0.05, 2.2)
             else:
                 sj = s_all[sk]
                 sk += 1
                 sj["body_a"], sj["body_b"] = idx[na], idx[nbn]
                 sj["position_a"] = sj["position_b"] = pw
-                pl = _qrot(q, _tangent(np.asarray(axis, dtype=np.float64)))
-                sj["twist_axis_a"] = sj["twist_axis_b"] = aw
-                sj["plane_axis_a"] = sj["plane_axis_b"] = pl
+                tg = _tangent(np.asarray(axis, dtype=np.float64))
+                sj["twist_axis_a"], sj["twist_axis_b"] = turned(na, axis), turned(nbn, axis)
+                sj["plane_axis_a"], sj["plane_axis_b"] = turned(na, tg), turned(nbn, tg)
                 sj["swing_type"] = SWING_CONE
-                cone = np.radians(rng.uniform(*cone_deg))
-                sj["normal_half_cone_angle"] = sj["plane_half_cone_angle"] = cone
+                sj["normal_half_cone_angle"] = sj["plane_half_cone_angle"] = cones[jn]
                 sj["twist_min_angle"], sj["twist_max_angle"] = -np.radians(twist_deg), np.radians(twist_deg)
     return Scene("ragdolls", b, dt=1.0 / 60.0, steps=600, velocity_iterations=12, position_iterations=4,
                  seed=seed, hinges=h_all, swings=s_all, skip_joint_pairs=True)

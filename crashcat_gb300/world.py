@@ -67,6 +67,9 @@ class WorldSettings:
     layers: Layers = dataclasses.field(default_factory=Layers)
     num_worlds: int = 1
     max_bodies: int = 0
+    # bounds of the device-side waits (0: the library's defaults); see cc_world_settings
+    device_wait_polls: int = 0
+    island_link_attempts: int = 0
 
     def to_c(self, max_bodies: int) -> _lib.Settings:
         s = _lib.Settings()
@@ -97,6 +100,8 @@ class WorldSettings:
             s.broadphase_pairs[i] = L.broadphase_pairs[i]
         s.max_bodies = max(1, max_bodies)
         s.num_worlds = self.num_worlds
+        s.device_wait_polls = self.device_wait_polls
+        s.island_link_attempts = self.island_link_attempts
         return s
 
 
@@ -199,6 +204,9 @@ class RigidBodySettings:
     collision_mask: int = 0xFFFFFFFF
     allowed_degrees_of_freedom: int = 0b111111
     world: int = 0
+    # motionProperties.numVelocityStepsOverride / numPositionStepsOverride (motion-properties.ts:59-61)
+    num_velocity_steps_override: int = 0
+    num_position_steps_override: int = 0
 
 
 def body_desc(s: RigidBodySettings) -> np.ndarray:
@@ -227,6 +235,8 @@ def body_desc(s: RigidBodySettings) -> np.ndarray:
               "collision_groups", "collision_mask"):
         d[f] = getattr(s, f)
     d["allowed_dofs"] = s.allowed_degrees_of_freedom
+    d["num_velocity_steps_override"] = s.num_velocity_steps_override
+    d["num_position_steps_override"] = s.num_position_steps_override
     return d
 
 
@@ -298,6 +308,13 @@ class GpuWorld:
         check(self._lib.cc_world_get_manifolds(self.handle, ptr(out), cnt.value, C.byref(cnt)),
               "cc_world_get_manifolds")
         return out[: cnt.value]
+
+    def island_iterations(self) -> np.ndarray:
+        """(velocity, position) iteration counts of the island each body was solved in during the
+        last step, [n, 2]; -1 for bodies in no island (cc_world_get_island_iterations)."""
+        out = np.zeros((max(self.n, 1), 2), dtype=np.int32)
+        check(self._lib.cc_world_get_island_iterations(self.handle, ptr(out)), "cc_world_get_island_iterations")
+        return out[: self.n]
 
     def debug_islands(self):
         cnt = C.c_int32()

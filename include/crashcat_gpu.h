@@ -116,6 +116,13 @@ typedef struct cc_world_settings {
     double ccd_linear_cast_threshold;
     double ccd_linear_cast_max_penetration;
     double ccd_min_velocity_for_restitution;
+    /* bounds of the device-side waits (no counterpart in the reference: the single-threaded step
+     * never waits).  device_wait_polls: polls of a grid barrier of the whole-grid island solve
+     * before it gives up, sets CC_ERR_TIMEOUT for the step and every block leaves (0: 2^21, about
+     * 0.2 s).  island_link_attempts: compare-and-swap attempts of one union-find link before it
+     * gives up; the step then skips its solve and returns CC_ERR_CAPACITY (0: 2^20). */
+    int32_t device_wait_polls;
+    int32_t island_link_attempts;
 } cc_world_settings;
 
 /* RigidBodySettings (src/body/rigid-body.ts:37-139) for the supported shapes.
@@ -147,6 +154,12 @@ typedef struct cc_body_desc {
     uint32_t collision_mask;
     int32_t allowed_dofs;
     int32_t motion_quality;  /* cc_motion_quality */
+    /* MotionProperties.numVelocityStepsOverride / numPositionStepsOverride
+     * (src/body/motion-properties.ts:59-61): 0 = the world's iteration counts.  An island
+     * runs the largest override of its dynamic bodies and joints, and at least the world's
+     * count when any of them is 0 (src/islands.ts:344-386).  At most 255. */
+    int32_t num_velocity_steps_override;
+    int32_t num_position_steps_override;
 } cc_body_desc;
 
 /* Per-step counters of the last completed step. */
@@ -319,6 +332,8 @@ typedef struct cc_hinge_desc {
     float min_torque_limit, max_torque_limit;  /* N m (reference default: -inf, +inf) */
     int32_t priority;                  /* constraintPriority: lower is solved first */
     int32_t enabled;
+    int32_t num_velocity_steps_override; /* hinge-constraint.ts:161-163, 0: the world's count */
+    int32_t num_position_steps_override;
 } cc_hinge_desc;
 
 /* hingeConstraint.create (hinge-constraint.ts:240-387) for n joints; out_index (may be NULL)
@@ -366,6 +381,8 @@ typedef struct cc_swing_twist_desc {
     float twist_min_torque_limit, twist_max_torque_limit;
     int32_t priority;
     int32_t enabled;
+    int32_t num_velocity_steps_override; /* swing-twist-constraint.ts settings, 0: the world's count */
+    int32_t num_position_steps_override;
 } cc_swing_twist_desc;
 
 /* swingTwistConstraint.create (swing-twist-constraint.ts:180-296) for n joints. */
@@ -395,6 +412,11 @@ int cc_world_set_skip_joint_pairs(cc_world *world, int32_t on);
  * clipping), EPA, contacts and islands, per-thread island solve, per-CTA
  * island solve] into stage_ms (n_stages >= 7). */
 int cc_world_profile_steps(cc_world *world, float dt, int32_t n_steps, float *stage_ms, int32_t n_stages);
+
+/* The velocity and position iteration counts of the island each body was solved in
+ * during the last step (Island.numVelocitySteps / numPositionSteps, src/islands.ts:344-386):
+ * 2 ints per body; -1, -1 for a body in no island (static or sleeping). */
+int cc_world_get_island_iterations(cc_world *world, int32_t *out);
 
 /* Diagnostic readout with no reference counterpart: island index per body of
  * the last step (-1 for static or sleeping bodies) and, per contact

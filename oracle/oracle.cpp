@@ -1229,6 +1229,21 @@ static void build_islands(World &w) {
             ps = std::max(ps, b.posOverride);
             dp = dp || b.posOverride == 0;
         }
+        // getConstraintIterationOverrides of the island's user constraints (hinge-constraint.ts:819-827)
+        for (int id : is.jointIndices) {
+            int jv, jp;
+            if (id >= JOINT_SWING) {
+                jv = w.swings[id - JOINT_SWING].velOverride;
+                jp = w.swings[id - JOINT_SWING].posOverride;
+            } else {
+                jv = w.joints[id].velOverride;
+                jp = w.joints[id].posOverride;
+            }
+            vs = std::max(vs, jv);
+            dv = dv || jv == 0;
+            ps = std::max(ps, jp);
+            dp = dp || jp == 0;
+        }
         if (dv) vs = std::max(vs, w.s.velocityIterations);
         if (dp) ps = std::max(ps, w.s.positionIterations);
         is.velSteps = vs;
@@ -1810,7 +1825,9 @@ enum {
     F_GROUPS = 28,
     F_MASK = 29,
     F_MOTION_QUALITY = 30,  // 0 discrete, 1 linear cast (MotionQuality motion-properties.ts:8-26)
-    F_COUNT = 31
+    F_VEL_OVERRIDE = 31,    // numVelocityStepsOverride / numPositionStepsOverride (motion-properties.ts:59-61)
+    F_POS_OVERRIDE = 32,
+    F_COUNT = 33
 };
 
 void *orc_world_create(const double *settings, int n_obj, const int *obj_to_bp, int n_bp, const uint8_t *obj_pairs,
@@ -1910,6 +1927,8 @@ int orc_add_bodies(void *wp, const double *rows, int n) {
         b.angDamp = r[F_ANG_DAMP];
         b.allowSleeping = r[F_ALLOW_SLEEP] != 0;
         b.linearCast = r[F_MOTION_QUALITY] == 1;
+        b.velOverride = (int)r[F_VEL_OVERRIDE];
+        b.posOverride = (int)r[F_POS_OVERRIDE];
         b.groups = (uint32_t)r[F_GROUPS];
         b.mask = (uint32_t)r[F_MASK];
         double mass;
@@ -1951,6 +1970,8 @@ int orc_add_hinge(void *wp, const double *d) {
     j.b = b;
     j.index = (int)w.joints.size();
     j.priority = (int)d[35];
+    j.velOverride = (int)d[36];
+    j.posOverride = (int)d[37];
     V3 pA{d[2], d[3], d[4]}, pB{d[5], d[6], d[7]};
     V3 h1 = normalize(V3{d[8], d[9], d[10]}), h2 = normalize(V3{d[11], d[12], d[13]});
     V3 n1 = normalize(V3{d[14], d[15], d[16]}), n2 = normalize(V3{d[17], d[18], d[19]});
@@ -2064,6 +2085,8 @@ int orc_add_swing_twist(void *wp, const double *d) {
     j.b = b;
     j.index = (int)w.swings.size();
     j.priority = (int)d[46];
+    j.velOverride = (int)d[47];
+    j.posOverride = (int)d[48];
     V3 t1 = normalize(V3{d[8], d[9], d[10]}), p1 = normalize(V3{d[11], d[12], d[13]});
     V3 t2 = normalize(V3{d[14], d[15], d[16]}), p2 = normalize(V3{d[17], d[18], d[19]});
     V3 n1 = cross(p1, t1), n2 = cross(p2, t2);
@@ -2236,6 +2259,18 @@ int orc_get_manifolds(void *wp, double *out) {
 
 // Island statistics of the last step: number of islands with contacts.
 int orc_island_count(void *wp) { return (int)((World *)wp)->islands.size(); }
+// Island.numVelocitySteps / numPositionSteps of the last step, per body (2 ints; -1 when the body
+// is in no island)
+void orc_get_island_iterations(void *wp, int *out) {
+    World &w = *(World *)wp;
+    for (size_t i = 0; i < w.bodies.size(); i++) out[2 * i] = out[2 * i + 1] = -1;
+    for (const Island &is : w.islands)
+        for (int64_t ai : is.bodyIndices) {
+            int bi = w.activeBodyIndices[ai];
+            out[2 * bi] = is.velSteps;
+            out[2 * bi + 1] = is.posSteps;
+        }
+}
 // sub-shape ids of the manifolds, in orc_get_manifolds order (2 per manifold, id order)
 int orc_get_manifold_subs(void *wp, uint32_t *out) {
     World &w = *(World *)wp;

@@ -47,6 +47,7 @@ enum MotorState { MOTOR_OFF = 0, MOTOR_VELOCITY = 1, MOTOR_POSITION = 2 };
 struct HingeJoint {
     int a = 0, b = 0;
     int priority = 0, index = 0;
+    int velOverride = 0, posOverride = 0;  // numVelocityStepsOverride / numPositionStepsOverride
     bool enabled = true;
     V3 lp1, lp2, lh1, lh2, ln1, ln2;
     Q4 invInitial{0, 0, 0, 1};
@@ -92,6 +93,7 @@ struct SwingTwistPart {
 struct SwingTwistJoint {
     int a = 0, b = 0;
     int priority = 0, index = 0;
+    int velOverride = 0, posOverride = 0;
     bool enabled = true;
     V3 lp1, lp2;
     Q4 c2b1{0, 0, 0, 1}, c2b2{0, 0, 0, 1};  // constraint space to body space

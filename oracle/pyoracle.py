@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 
-F_COUNT = 31  # doubles per body row, see oracle.cpp (enum F_*)
+F_COUNT = 33  # doubles per body row, see oracle.cpp (enum F_*)
 STATE = 17    # pos3 quat4 linvel3 angvel3 com3 sleeping
 
 _lib = None
@@ -67,6 +67,7 @@ def load():
         "orc_add_swing_twist": ([vp, dp], i32),
         "orc_add_hull": ([vp, i32, dp, dp, i32, C.c_void_p, i32, C.c_void_p, dp, dp], i32),
         "orc_set_record_tape": ([vp, i32], None),
+        "orc_get_island_iterations": ([vp, ip], None),
         "orc_get_solver_tape": ([vp, vp, vp, vp, vp], i32),
         "orc_frozen_rollout": ([i32, i32, i32, i32, C.c_double, dp, dp, dp, dp, ip, dp, dp, dp, i32, C.c_double,
                                 vp, vp, vp, dp, vp, vp], i32),
@@ -112,6 +113,8 @@ def rows_from_bodies(b: np.ndarray) -> np.ndarray:
     r[:, 28] = b["collision_groups"]
     r[:, 29] = b["collision_mask"]
     r[:, 30] = b["motion_quality"]
+    r[:, 31] = b["num_velocity_steps_override"]
+    r[:, 32] = b["num_position_steps_override"]
     return np.ascontiguousarray(r)
 
 
@@ -284,7 +287,7 @@ class OracleWorld:
         return o
 
     def add_hinge(self, desc: np.ndarray) -> int:
-        """Hinge joint from a 36-double descriptor (oracle.cpp orc_add_hinge layout)."""
+        """Hinge joint from a 38-double descriptor (oracle.cpp orc_add_hinge layout)."""
         d = np.ascontiguousarray(desc, dtype=np.float64)
         k = self.lib.orc_add_hinge(self.h, dptr(d))
         assert k >= 0
@@ -292,7 +295,7 @@ class OracleWorld:
 
     def add_hinge_record(self, h) -> int:
         """Hinge joint from a cc_hinge_desc record (fields by name)."""
-        d = np.zeros(36, dtype=np.float64)
+        d = np.zeros(38, dtype=np.float64)
         d[0], d[1] = h["body_a"], h["body_b"]
         for k, f in enumerate(("point_a", "point_b", "hinge_axis_a", "hinge_axis_b", "normal_axis_a", "normal_axis_b")):
             d[2 + 3 * k: 5 + 3 * k] = h[f]
@@ -305,11 +308,12 @@ class OracleWorld:
         d[30:33] = (h["motor_spring"]["mode"], h["motor_spring"]["frequency_or_stiffness"],
                     h["motor_spring"]["damping"])
         d[33], d[34], d[35] = h["min_torque_limit"], h["max_torque_limit"], h["priority"]
+        d[36], d[37] = h["num_velocity_steps_override"], h["num_position_steps_override"]
         return self.add_hinge(d)
 
     def add_swing_twist_record(self, h) -> int:
         """Swing-twist joint from a cc_swing_twist_desc record (fields by name)."""
-        d = np.zeros(47, dtype=np.float64)
+        d = np.zeros(49, dtype=np.float64)
         d[0], d[1] = h["body_a"], h["body_b"]
         for k, f in enumerate(("position_a", "position_b", "twist_axis_a", "plane_axis_a", "twist_axis_b",
                                "plane_axis_b")):
@@ -325,6 +329,7 @@ class OracleWorld:
         d[42], d[43] = h["swing_min_torque_limit"], h["swing_max_torque_limit"]
         d[44], d[45] = h["twist_min_torque_limit"], h["twist_max_torque_limit"]
         d[46] = h["priority"]
+        d[47], d[48] = h["num_velocity_steps_override"], h["num_position_steps_override"]
         k = self.lib.orc_add_swing_twist(self.h, dptr(d))
         assert k >= 0
         return k
@@ -342,6 +347,12 @@ class OracleWorld:
         for t, a, b in out[:n].tolist():
             ev[names[t]].add((a, b))
         return ev
+
+    def island_iterations(self) -> np.ndarray:
+        """(velocity, position) steps of each body's island in the last step, [n, 2] (-1: none)."""
+        o = np.zeros((self.n, 2), dtype=np.int32)
+        self.lib.orc_get_island_iterations(self.h, iptr(o))
+        return o
 
     def step_taped(self, dt: float):
         """One step with the rows of its velocity solve (orc_get_solver_tape): returns

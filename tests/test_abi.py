@@ -57,10 +57,35 @@ def test_invalid_arguments_are_rejected(lib):
     assert lib.cc_world_step(None, C.c_float(0.01), 1) == _lib.CC_ERR_INVALID
 
 
-def test_body_desc_layout_matches_c():
-    # 24 fields of 4 bytes each (shape_params 4, vec3/quat inline), motion_quality last
-    assert _lib.BODY_DTYPE.itemsize == 4 * (1 + 4 + 1 + 4 + 3 + 4 + 3 + 3 + 7 + 2 + 2 + 1 + 1)
-    assert _lib.BODY_DTYPE.names[-1] == "motion_quality"
+def test_record_layouts_match_c(tmp_path):
+    """The numpy mirrors of the C records have the C compiler's sizes and field offsets
+    (a probe compiled against include/crashcat_gpu.h prints them)."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    recs = {"cc_body_desc": _lib.BODY_DTYPE, "cc_hinge_desc": _lib.HINGE_DTYPE,
+            "cc_swing_twist_desc": _lib.SWING_TWIST_DTYPE, "cc_tape_body": _lib.TAPE_BODY_DTYPE,
+            "cc_tape_contact": _lib.TAPE_CONTACT_DTYPE, "cc_penetration_query": _lib.PEN_QUERY_DTYPE,
+            "cc_penetration_result": _lib.PEN_RESULT_DTYPE, "cc_ray": _lib.RAY_DTYPE,
+            "cc_shape_cast": _lib.SHAPE_CAST_DTYPE, "cc_shape_cast_hit": _lib.SHAPE_CAST_HIT_DTYPE}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{ROOT}/include/crashcat_gpu.h"',
+             'int main(void) {']
+    for name, dt in recs.items():
+        lines.append(f'printf("{name} size %zu\\n", sizeof({name}));')
+        for f in dt.names:
+            lines.append(f'printf("{name} {f} %zu\\n", offsetof({name}, {f}));')
+    lines += ['return 0;', '}']
+    src = tmp_path / "probe.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", "-std=c11", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for name, dt in recs.items():
+        assert got[(name, "size")] == dt.itemsize, name
+        for f in dt.names:
+            assert got[(name, f)] == dt.fields[f][1], (name, f)
 
 
 def test_layer_tables_follow_reference():

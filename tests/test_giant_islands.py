@@ -13,7 +13,7 @@ than constraint order); ragdolls over 20 steps 5e-3 m, as the ragdoll parity tes
 import numpy as np
 import pytest
 
-from crashcat_gb300 import scenes, world
+from crashcat_gb300 import _lib, scenes, world
 from oracle import pyoracle
 
 pytestmark = pytest.mark.gpu
@@ -102,3 +102,59 @@ def test_pile_of_ragdolls_runs_on_the_grid_tier(gpu_lib, monkeypatch):
     assert rows[6:, 1].min() > -0.2
     from test_swing_twist import joint_gaps
     assert joint_gaps(sc, rows.astype(np.float64)).max() < 0.05
+
+
+def test_grid_barrier_wait_runs_out_with_a_status(gpu_lib, monkeypatch):
+    """The grid barrier of the whole-grid solve polls a bounded number of times.  With the bound
+    set to one poll the first barrier gives up: every block leaves, the step returns
+    CC_ERR_TIMEOUT with OVF_TIMEOUT in the counters, and the device keeps answering (a world with
+    the default bound then steps normally)."""
+    monkeypatch.setenv("CRASHCAT_GIANT_MIN", "16")
+    sc = scenes.box_pyramid(base=8)
+    ws = world.standard_settings(device_wait_polls=1)
+    g = world.GpuWorld(ws, sc.n + 8)
+    g.add_bodies(sc.bodies)
+    st = g.step(sc.dt, 3)
+    assert st == _lib.CC_ERR_TIMEOUT
+    assert g.stats()["overflow_flags"] & 64
+    assert g.stats()["num_giant_islands"] >= 1
+    ok = world.GpuWorld(world.standard_settings(), sc.n + 8)
+    ok.add_bodies(sc.bodies)
+    assert ok.step(sc.dt, 3) == _lib.CC_OK
+    assert np.isfinite(ok.get_state()[0]).all()
+
+
+def slab_with_boxes(n_side=8):
+    """A dynamic slab resting on the floor, created last (the highest body index, so every link of
+    a box on it targets the slab's root), with n_side^2 small boxes resting on it."""
+    n = n_side * n_side
+    b = scenes.blank_bodies(n + 2)
+    scenes.static_floor(b, 0)
+    idx = np.arange(1, n + 1)
+    scenes.set_box(b, idx, (0.2, 0.2, 0.2))
+    g = np.arange(n)
+    b["position"][idx] = np.stack([(g % n_side - n_side / 2) * 0.6, np.full(n, 0.5 + 0.2 - 0.005),
+                                   (g // n_side - n_side / 2) * 0.6], 1)
+    scenes.set_box(b, n + 1, (3.0, 0.25, 3.0))
+    b["position"][n + 1] = (0.0, 0.25 - 0.005, 0.0)
+    return b
+
+
+def test_union_find_link_bound_skips_the_solve(gpu_lib):
+    """With one compare-and-swap attempt per union-find link, links that lose a race give up: many
+    boxes rest on one slab whose root every link targets, so the lanes of a warp race for it.  The
+    step reports CC_ERR_CAPACITY with OVF_ISLAND and skips its solve (no body moves), and the device
+    keeps answering."""
+    b = slab_with_boxes()
+    ws = world.standard_settings(island_link_attempts=1)
+    g = world.GpuWorld(ws, len(b) + 8)
+    g.add_bodies(b)
+    before, _ = g.get_state()
+    st = g.step(1 / 60, 1)
+    assert st == _lib.CC_ERR_CAPACITY
+    assert g.stats()["overflow_flags"] & 8
+    after, _ = g.get_state()
+    np.testing.assert_array_equal(after[:, 0:7], before[:, 0:7])
+    ok = world.GpuWorld(world.standard_settings(), len(b) + 8)
+    ok.add_bodies(b)
+    assert ok.step(1 / 60, 2) == _lib.CC_OK

@@ -221,3 +221,27 @@ def test_swing_twist_setters(gpu_lib):
     assert rows2[1, 1] < y0 + vy0 * t - 0.5 * 9.81 * t * t * 0.9 * damp
     with pytest.raises(_lib.CCError):
         g.set_swing_twist_limits(5, 0.1, 0.1, -0.1, 0.1)
+
+
+def test_random_ragdoll_poses_start_inside_their_limits(oracle_lib):
+    """Ragdolls spawned at seeded random joint poses (each joint turned inside its limits, the
+    joints created in that pose): with gravity off nothing moves over 10 steps, so no hinge or
+    swing-twist limit and no contact pushes at spawn, and the joints hold; the pose differs from
+    the rest pose."""
+    sc = scenes.ragdolls(num=8, arena=12.0, spacing=5.0)
+    ws = settings_of(sc)
+    ws.gravity_enabled = False
+    o = pyoracle.OracleWorld(ws, sc.bodies)
+    for h in sc.hinges:
+        o.add_hinge_record(h)
+    for h in sc.swings:
+        o.add_swing_twist_record(h)
+    o.set_skip_joint_pairs(True)
+    st0 = o.state()
+    o.step(sc.dt, 10)
+    st = o.state()
+    assert np.abs(st[:, 0:3] - st0[:, 0:3]).max() < 1e-5
+    assert joint_gaps(sc, st).max() < 1e-4
+    rest = scenes.ragdolls(num=8, arena=12.0, spacing=5.0, random_poses=False).bodies["position"]
+    moved = np.linalg.norm(rest[6:] - sc.bodies["position"][6:], axis=1)
+    assert (moved > 0.05).mean() > 0.5
