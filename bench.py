@@ -87,6 +87,7 @@ def parse():
     ap.add_argument("--ragdolls", type=int, default=1, help="measure the jointed-ragdoll workload (1) or skip it (0)")
     ap.add_argument("--terrain", type=int, default=1, help="measure the mixed-shape terrain workload (1) or skip it (0)")
     ap.add_argument("--cube-heap", type=int, default=1, help="measure the plain cube-heap workload (1) or skip it (0)")
+    ap.add_argument("--tune", type=int, default=1, help="autotune the launch shapes before the warm-up (1) or not (0)")
     ap.add_argument("--errors", type=int, default=1,
                     help="report the batched workload's error against the FP64 oracle (1) or skip it (0)")
     ap.add_argument("--settle", type=int, default=360,
@@ -1028,6 +1029,8 @@ def run_gpu(args, rank, world_size, local):
     dt = scene.dt
     if args.settle:
         g.step(dt, args.settle)
+    # launch shapes tuned on the settled state (the tuner leaves the state as it found it)
+    tune = g.autotune(dt, 3) if args.tune else None
     for _ in range(args.warmup):
         g.step(dt, 1)
     stats_w = g.stats()
@@ -1122,6 +1125,7 @@ def run_gpu(args, rank, world_size, local):
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                          "algorithmic_bytes_per_launch": bytes_dom, "stage_ms": prof},
             "cpu_baseline": cpu,
+            "autotune": tune,
             "error": error,
             "vs_single_world": single,
             "cube_heap": cube_heap,

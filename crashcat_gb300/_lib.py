@@ -70,6 +70,13 @@ class Settings(C.Structure):
     ]
 
 
+class TuneReport(C.Structure):
+    _fields_ = [("default_ms", C.c_float), ("tuned_ms", C.c_float), ("trials", C.c_int32),
+                ("epa_blocks_per_sm", C.c_int32), ("epa_lockstep", C.c_int32), ("warp_blocks_per_sm", C.c_int32),
+                ("small_island_max_contacts", C.c_int32), ("giant_min", C.c_int32),
+                ("graph_kernels_per_step", C.c_int32)]
+
+
 class HullInfo(C.Structure):
     _fields_ = [("num_points", C.c_int32), ("num_faces", C.c_int32), ("num_face_vertices", C.c_int32),
                 ("convex_radius", C.c_float), ("volume", C.c_float), ("inner_radius", C.c_float),
@@ -167,6 +174,7 @@ EXPORTS = {
     "cc_world_profile_steps": ([C.c_void_p, C.c_float, C.c_int32, C.c_void_p, C.c_int32], C.c_int),
     "cc_world_rollout_grad": ([C.c_void_p, C.c_float, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_void_p], C.c_int),
+    "cc_world_autotune": ([C.c_void_p, C.c_float, C.c_int32, C.POINTER(TuneReport)], C.c_int),
     "cc_world_step_taped": ([C.c_void_p, C.c_float, C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32),
                              C.POINTER(C.c_float)], C.c_int),
     "cc_penetration_static": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_float, C.c_float, C.c_void_p], C.c_int),

@@ -104,6 +104,7 @@ struct DevSettings {
     int small_island_max_joints;  // islands with joints: up to this many joints run on one thread
     unsigned wait_polls;        // polls of a bounded device wait (grid barrier) before it gives up
     int link_attempts;          // attempts of one union-find link before it gives up (OVF_ISLAND)
+    int test_withhold_block;    // test hook: block 0 of the whole-grid solve skips its barriers
 };
 
 // Manifold produced by the narrowphase for one body pair (<= 4 points),

@@ -1465,8 +1465,22 @@ struct Hull {
         }
         return best;
     }
-    // findEdge epa-convex-hull-builder.ts:476-540; returns the edge count or -1
-    __device__ int find_edge(int ft, V<R> vtx) {
+    // The facing test of every triangle slot below `upto` against p, as a bit mask.  The lanes of a
+    // warp run the loop together (upto is the same on every lane), so the FP64 tests issue with
+    // every lane whose polytope has that slot; find_edge then reads the bits (the geometry of a
+    // triangle does not change while its flags do).  Packed store only (at most 64 slots).
+    __device__ unsigned long long facing_mask(V<R> p, int upto) const {
+        unsigned long long m = 0ull;
+        for (int t = 0; t < upto; t++)
+            if (t < ntri && facing(t, p)) m |= 1ull << t;
+        return m;
+    }
+    __device__ bool facing_of(int t, V<R> vtx, const unsigned long long *mask) const {
+        return mask ? ((*mask >> t) & 1ull) != 0 : facing(t, vtx);
+    }
+    // findEdge epa-convex-hull-builder.ts:476-540; returns the edge count or -1.  mask: the facing
+    // bits of the triangle slots (facing_mask), or null to test them as they are met
+    __device__ int find_edge(int ft, V<R> vtx, const unsigned long long *mask = nullptr) {
         int ne = 0;
         add_flags(ft, TF_REMOVED);
         int sp = 0;
@@ -1486,7 +1500,7 @@ struct Hull {
                 int nen = st.ne(ct, ei);
                 int est = st.st(ct, ei);
                 if (n >= 0 && !(flags(n) & TF_REMOVED)) {
-                    if (facing(n, vtx)) {
+                    if (facing_of(n, vtx, mask)) {
                         add_flags(n, TF_REMOVED);
                         sp++;
                         if (sp >= S::ECAP) {
@@ -1511,8 +1525,8 @@ struct Hull {
         return ne >= 3 ? ne : -1;
     }
     // addPoint epa-convex-hull-builder.ts:541-600
-    __device__ int add_point(int ft, int idx, R closest) {
-        int ne = find_edge(ft, st.Y(idx));
+    __device__ int add_point(int ft, int idx, R closest, const unsigned long long *mask = nullptr) {
+        int ne = find_edge(ft, st.Y(idx), mask);
         if (ne < 0) return -1;
         for (int i = 0; i < ne; i++) {
             int in = (i + 1) % ne;
@@ -1553,11 +1567,15 @@ struct Hull {
     }
 };
 
-// penetrationDepthStepEPA penetration.ts:214-614; true and the result on success
+// penetrationDepthStepEPA penetration.ts:214-614, in three parts: the seed polytope
+// (epa_seed), the growth until the origin is inside and the expansion towards the closest face
+// (epa_loops, or the lock-step rounds of k_epa), and the result from the last face (epa_result).
+constexpr R EPA_MAXD = 1.7976931348623157e308;
+
+// the simplex filled to a tetrahedron, its first two triangles and the remaining simplex points
+// (penetration.ts:226-345); false when it cannot start
 template <class S, class SA, class SB>
-__device__ bool epa(Hull<S> &h, const SA &A, const SB &B, R tol, V<R> &outAxis,
-                    V<R> &outPa, V<R> &outPb) {
-    const R MAXD = 1.7976931348623157e308;
+__device__ bool epa_seed(Hull<S> &h, const SA &A, const SB &B) {
     if (h.npts == 1) {
         h.npts = 0;
         h.add_sup(A, B, {0.0, 1.0, 0.0});
@@ -1602,8 +1620,44 @@ __device__ bool epa(Hull<S> &h, const SA &A, const SB &B, R tol, V<R> &outAxis,
     h.push(t2);
     for (int i = 3; i < h.npts; i++) {
         int t = h.find_facing(h.st.Y(i));
-        if (t >= 0 && h.add_point(t, i, MAXD) < 0) return false;
+        if (t >= 0 && h.add_point(t, i, EPA_MAXD) < 0) return false;
     }
+    return true;
+}
+
+// the contact from the last face the expansion kept (penetration.ts:509-614)
+template <class S>
+__device__ bool epa_result(Hull<S> &h, int last, bool flip, V<R> &outAxis, V<R> &outPa, V<R> &outPb) {
+    if (h.overflow) return false;
+    if (last < 0) return false;
+    V<R> ln = h.st.normal(last);
+    R nls = lsq(ln);
+    V<R> pn = ln * (dot(h.st.centroid(last), ln) / nls);
+    if (lsq(pn) < R_MIN_NORMAL_SQ) return false;
+    if (flip) pn = -pn;
+    R l0, l1;
+    bool rel0;
+    h.lambdas(last, l0, l1, rel0);
+    int s0 = h.st.st(last, 0), s1 = h.st.st(last, 1), s2 = h.st.st(last, 2);
+    V<R> xp0 = h.st.P(s0), xp1 = h.st.P(s1), xp2 = h.st.P(s2);
+    V<R> xq0 = h.st.Q(s0), xq1 = h.st.Q(s1), xq2 = h.st.Q(s2);
+    if (rel0) {
+        outPa = xp0 + (xp1 - xp0) * l0 + (xp2 - xp0) * l1;
+        outPb = xq0 + (xq1 - xq0) * l0 + (xq2 - xq0) * l1;
+    } else {
+        outPa = xp1 + (xp0 - xp1) * l0 + (xp2 - xp1) * l1;
+        outPb = xq1 + (xq0 - xq1) * l0 + (xq2 - xq1) * l1;
+    }
+    outAxis = pn;
+    return true;
+}
+
+// The whole EPA of one pair, sequentially; true and the result on success
+template <class S, class SA, class SB>
+__device__ bool epa(Hull<S> &h, const SA &A, const SB &B, R tol, V<R> &outAxis,
+                    V<R> &outPa, V<R> &outPb) {
+    const R MAXD = EPA_MAXD;
+    if (!epa_seed(h, A, B)) return false;
     int guard = 0;
     while (guard++ < 4096) {
         if (h.nq == 0) return false;
@@ -1663,28 +1717,141 @@ __device__ bool epa(Hull<S> &h, const SA &A, const SB &B, R tol, V<R> &outAxis,
             break;
         }
     } while (h.nq > 0 && h.npts < 128 && guard++ < 4096);
-    if (h.overflow) return false;
-    if (last < 0) return false;
-    V<R> ln = h.st.normal(last);
-    R nls = lsq(ln);
-    V<R> pn = ln * (dot(h.st.centroid(last), ln) / nls);
-    if (lsq(pn) < R_MIN_NORMAL_SQ) return false;
-    if (flip) pn = -pn;
-    R l0, l1;
-    bool rel0;
-    h.lambdas(last, l0, l1, rel0);
-    int s0 = h.st.st(last, 0), s1 = h.st.st(last, 1), s2 = h.st.st(last, 2);
-    V<R> xp0 = h.st.P(s0), xp1 = h.st.P(s1), xp2 = h.st.P(s2);
-    V<R> xq0 = h.st.Q(s0), xq1 = h.st.Q(s1), xq2 = h.st.Q(s2);
-    if (rel0) {
-        outPa = xp0 + (xp1 - xp0) * l0 + (xp2 - xp0) * l1;
-        outPb = xq0 + (xq1 - xq0) * l0 + (xq2 - xq0) * l1;
-    } else {
-        outPa = xp1 + (xp0 - xp1) * l0 + (xp2 - xp1) * l1;
-        outPb = xq1 + (xq0 - xq1) * l0 + (xq2 - xq1) * l1;
+    return epa_result(h, last, flip, outAxis, outPa, outPb);
+}
+
+// The same EPA with the growth and expansion loops cut into rounds that every lane of a warp runs
+// together: select a face (pop), one support point, the checks, and the horizon walk with the new
+// faces.  Each lane's polytope sees exactly the operations of epa(), in the same order; only the
+// facing tests of the horizon walk are taken for every face slot up front (facing_mask), in a loop
+// the lanes share, so that the FP64 work issues with most lanes of the warp active (on GB300 an
+// FP64 warp instruction costs the same whatever the number of active lanes).  Every lane of the
+// warp calls this; `active` says whether the lane has a pair.
+enum : int { EPA_DONE = 0, EPA_GROW = 1, EPA_EXPAND = 2, EPA_FAIL = 3 };
+template <class S, class SA, class SB>
+__device__ bool epa_lockstep(bool active, Hull<S> &h, const SA &A, const SB &B, R tol, V<R> &outAxis,
+                             V<R> &outPa, V<R> &outPb) {
+    static_assert(S::TRI <= 64, "the facing mask holds one bit per face slot");
+    const R MAXD = EPA_MAXD;
+    int phase = active ? (epa_seed(h, A, B) ? EPA_GROW : EPA_FAIL) : EPA_DONE;
+    int gguard = 0, eguard = 0, last = -1;
+    R closest = MAXD;
+    bool flip = false;
+    while (__any_sync(0xffffffffu, phase == EPA_GROW || phase == EPA_EXPAND)) {
+        // select: the face to expand (the loop heads of epa())
+        bool work = false;
+        int t = -1;
+        if (phase == EPA_GROW) {
+            if (!(gguard++ < 4096)) {
+                phase = EPA_EXPAND;
+            } else if (h.nq == 0) {
+                phase = EPA_FAIL;
+            } else {
+                t = h.st.q(0);
+                if (h.flags(t) & TF_REMOVED) {
+                    h.pop();
+                    if (h.nq == 0)
+                        phase = EPA_FAIL;
+                    else
+                        h.free_tri(t);
+                } else if (h.cls(t) >= 0.0) {
+                    phase = EPA_EXPAND;
+                } else {
+                    h.pop();
+                    work = true;
+                }
+            }
+        } else if (phase == EPA_EXPAND) {
+            t = h.pop();
+            if (t < 0) {
+                phase = EPA_FAIL;
+            } else if (h.flags(t) & TF_REMOVED) {
+                h.free_tri(t);
+                if (!(h.nq > 0 && h.npts < 128 && eguard++ < 4096)) phase = EPA_DONE;
+            } else if (h.cls(t) >= closest) {
+                phase = EPA_DONE;
+            } else {
+                if (last >= 0) h.free_tri(last);
+                last = t;
+                work = true;
+            }
+        }
+        // one support point along the face normal
+        V<R> tn{0.0, 0.0, 0.0};
+        int ni = -1;
+        if (work) {
+            tn = h.st.normal(t);
+            ni = h.add_sup(A, B, tn);
+            if (ni < 0) {
+                phase = phase == EPA_GROW ? EPA_FAIL : EPA_DONE;
+                work = false;
+            }
+        }
+        // the checks of the new point
+        R d = 0.0;
+        if (work) {
+            V<R> wv = h.st.Y(ni);
+            if (phase == EPA_GROW) {
+                if (!h.facing(t, wv)) {
+                    phase = EPA_FAIL;
+                    work = false;
+                }
+            } else {
+                d = dot(tn, wv);
+                if (d < 0.0) {
+                    phase = EPA_FAIL;
+                    work = false;
+                } else {
+                    R dsq = (d * d) / lsq(tn);
+                    if (dsq - h.cls(t) < h.cls(t) * tol) {
+                        phase = EPA_DONE;
+                        work = false;
+                    } else {
+                        closest = closest < dsq ? closest : dsq;
+                        if (!h.facing(t, wv)) {
+                            phase = EPA_DONE;
+                            work = false;
+                        }
+                    }
+                }
+            }
+        }
+        // the horizon and the new faces
+        if (work) {
+            const int upto = __reduce_max_sync(__activemask(), h.ntri);
+            const unsigned long long mask = h.facing_mask(h.st.Y(ni), upto);
+            int ne = h.add_point(t, ni, phase == EPA_GROW ? MAXD : closest, &mask);
+            if (phase == EPA_GROW) {
+                if (ne < 0) {
+                    phase = EPA_FAIL;
+                } else {
+                    h.free_tri(t);
+                    if (h.nq == 0 || h.npts >= 32) phase = EPA_FAIL;
+                }
+            } else if (ne < 0) {
+                phase = EPA_DONE;
+            } else {
+                bool defect = false;
+                for (int k = 0; k < ne; k++) {
+                    int q = h.st.newt(k);
+                    if (dot(h.st.normal(q), h.st.centroid(q)) < 0.0) {
+                        defect = true;
+                        break;
+                    }
+                }
+                if (defect) {
+                    V<R> nn = -tn;
+                    V<R> w2 = A.get(nn) - B.get(tn);
+                    if (dot(nn, w2) < d) flip = true;
+                    phase = EPA_DONE;
+                } else if (!(h.nq > 0 && h.npts < 128 && eguard++ < 4096)) {
+                    phase = EPA_DONE;
+                }
+            }
+        }
     }
-    outAxis = pn;
-    return true;
+    if (!active || phase == EPA_FAIL) return false;
+    return epa_result(h, last, flip, outAxis, outPa, outPb);
 }
 
 // Supports of one queued pair in A's local frame (convex.ts:440-452): EPA runs on the full
@@ -1759,27 +1926,29 @@ __device__ void epa_finish(const DevWorld &w, EpaItem &it, bool ok, R maxSep, V<
     it.pad = __float_as_int((float)(penetration));
 }
 
-// Packed pass.  fetch_warp = 1: a warp takes 32 consecutive items at a time and its lanes
-// start them together, which keeps the lanes in the same phase of the algorithm (on GB300
-// an FP64 warp instruction costs the same whatever the number of active lanes);
-// fetch_warp = 0: each thread takes its next item as soon as it finishes one.  Items that
-// outgrow the packed limits go to the fallback list.
+// Packed pass.  fetch_warp = 1: a warp takes 32 consecutive items at a time and runs them in
+// lock-step rounds (epa_lockstep); fetch_warp = 0: each thread takes its next item as soon as it
+// finishes one and runs it alone (epa).  Items that outgrow the packed limits go to the fallback
+// list.
 template <bool H>
 __device__ __forceinline__ void epa_packed_item(DevWorld &w, EpaItem *items, int i, Hull<PackedStore> &h,
-                                                int *fallback, int pts_limit) {
-    EpaItem &it = items[i];
-    if (it.tri >= 0) return;  // mesh triangles: k_epa_mesh
+                                                int *fallback, int pts_limit, bool lockstep) {
+    const bool active = i >= 0 && items[i].tri < 0;  // mesh triangles: k_epa_mesh
     Sup<R, H> A, B;
-    R maxSep;
-    epa_setup(w, it, A, B, maxSep);
-    h.start(it, pts_limit);
-    V<R> axis, pa, pb;
-    bool ok = epa(h, A, B, R(c_settings.penetration_tol), axis, pa, pb);
+    R maxSep = 0.0;
+    if (active) {
+        epa_setup(w, items[i], A, B, maxSep);
+        h.start(items[i], pts_limit);
+    }
+    V<R> axis{0.0, 0.0, 0.0}, pa{0.0, 0.0, 0.0}, pb{0.0, 0.0, 0.0};
+    bool ok = lockstep ? epa_lockstep(active, h, A, B, R(c_settings.penetration_tol), axis, pa, pb)
+                       : (active && epa(h, A, B, R(c_settings.penetration_tol), axis, pa, pb));
+    if (!active) return;
     if (h.overflow) {
         fallback[atomicAdd(&w.ctr->epa_fallback, 1)] = i;
         return;
     }
-    epa_finish(w, it, ok, maxSep, axis, pa, pb);
+    epa_finish(w, items[i], ok, maxSep, axis, pa, pb);
 }
 
 // H: the world has convex hulls (without them the support code leaves the hull loop out)
@@ -1797,12 +1966,12 @@ __global__ void __launch_bounds__(EPA_BLOCK) k_epa(DevWorld w, EpaItem *items, P
             if (lane == 0) base = atomicAdd(&w.ctr->epa_cursor, 32);
             base = __shfl_sync(0xffffffffu, base, 0);
             if (base >= ne) break;
-            if (base + lane < ne) epa_packed_item<H>(w, items, base + lane, h, fallback, pts_limit);
+            epa_packed_item<H>(w, items, base + lane < ne ? base + lane : -1, h, fallback, pts_limit, true);
             __syncwarp();
         }
     } else {
         for (int i = atomicAdd(&w.ctr->epa_cursor, 1); i < ne; i = atomicAdd(&w.ctr->epa_cursor, 1))
-            epa_packed_item<H>(w, items, i, h, fallback, pts_limit);
+            epa_packed_item<H>(w, items, i, h, fallback, pts_limit, false);
     }
 }
 

@@ -1630,6 +1630,7 @@ __global__ void __launch_bounds__(GIANT_BLOCK) k_solve_giant(DevWorld w, CacheTa
     DevCounters *ctr = w.ctr;
     const int ng = ctr->num_giant_islands;
     if (ng == 0 || islands_failed(w)) return;
+    if (c_settings.test_withhold_block && blockIdx.x == 0) return;  // the others' barrier waits run out
     const unsigned nblk = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
     CacheRecord *crecs = ct.recs[*ct.parity];

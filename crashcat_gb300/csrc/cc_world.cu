@@ -64,6 +64,16 @@ struct cc_world {
         float *d_targets = nullptr, *d_loss = nullptr;
         std::vector<void *> allocs;
     } adj;
+    int epa_packed_blocks = 0;  // packed EPA polytope blocks allocated
+    // cc_world_autotune: a snapshot of the state the trials start from
+    struct TuneSnapshot {
+        bool ready = false;
+        Checkpoint c{};
+        char *joints = nullptr;  // hinges then swing-twists
+        size_t joint_bytes = 0;
+        float2 *ccd = nullptr;
+        std::vector<void *> allocs;
+    } tune;
     // cc_world_step_taped: the step's rows in the C-ABI layout, grown on demand
     cc_tape_body *x_bodies = nullptr;
     cc_tape_contact *x_cons = nullptr;
@@ -297,6 +307,9 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
     d.time_before_sleep = (float)s->time_before_sleep;
     d.sleep_threshold = (float)s->point_velocity_sleep_threshold;
     d.wait_polls = s->device_wait_polls > 0 ? (unsigned)s->device_wait_polls : (1u << 21);
+    // test hook: block 0 of the whole-grid island solve leaves before its first grid barrier, so
+    // the other blocks' bounded wait on that barrier runs out (a flag that nothing sets)
+    d.test_withhold_block = getenv("CRASHCAT_TEST_WITHHOLD_BARRIER") ? 1 : 0;
     d.link_attempts = s->island_link_attempts > 0 ? s->island_link_attempts : (1 << 20);
     d.ccd_threshold = (float)s->ccd_linear_cast_threshold;
     d.ccd_max_penetration = (float)s->ccd_linear_cast_max_penetration;
@@ -445,6 +458,7 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
             return r;
         }
         w.epa_packed = q;
+        W->epa_packed_blocks = w.epa_threads / 64;
         char *g = nullptr;
         if ((r = dalloc(&g, epa_scratch_bytes() * (size_t)EPA_BIG_THREADS)) != CC_OK) {
             cc_world_destroy(W);
@@ -477,7 +491,7 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
     w.giant_min = 8192;
     if (const char *e = getenv("CRASHCAT_GIANT_MIN")) {
         int v = atoi(e);
-        if (v >= 64) w.giant_min = v;
+        if (v >= 1) w.giant_min = v;
     }
     w.giant_blocks = giant_blocks_for_device();
     if (const char *e = getenv("CRASHCAT_GIANT_BLOCKS")) {  // launch-shape tunable, at most one per SM
@@ -537,6 +551,8 @@ int cc_world_destroy(cc_world *W) {
     if (W->q_idx) cudaFree(W->q_idx);
     if (W->q_tmp) cudaFree(W->q_tmp);
     for (void *p : W->adj.allocs)
+        if (p) cudaFree(p);
+    for (void *p : W->tune.allocs)
         if (p) cudaFree(p);
     if (W->x_bodies) cudaFree(W->x_bodies);
     if (W->x_cons) cudaFree(W->x_cons);
@@ -1514,6 +1530,172 @@ extern "C" int cc_world_rollout_grad(cc_world *W, float dt, int32_t n_steps, int
         for (int i = 0; i < w.n; i++) grad_friction[i] = (float)((double)(long long)mu_fx[i] / ADJ_MU_SCALE);
     cudaEventElapsedTime(&W->last_call_ms, W->ev_begin, W->ev_end);
     W->last_ctr = *W->h_ctr;
+    return CC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// launch-shape autotuner
+// ---------------------------------------------------------------------------
+struct TuneShape {
+    int epa_blocks_per_sm, epa_lockstep, warp_blocks_per_sm, small_max, giant_min;
+};
+static TuneShape tune_shape_of(const cc_world *W) {
+    const DevWorld &w = W->w;
+    return TuneShape{w.epa_threads / 64 / device_sm_count(), w.epa_fetch_warp, w.warp_blocks_per_sm,
+                     W->dev_settings.small_island_max_cons, w.giant_min};
+}
+static int tune_apply(cc_world *W, const TuneShape &t) {
+    DevWorld &w = W->w;
+    int blocks = t.epa_blocks_per_sm * device_sm_count();
+    if (blocks > W->epa_packed_blocks) {
+        if (w.epa_packed) cudaFree(w.epa_packed);
+        w.epa_packed = nullptr;
+        W->epa_packed_blocks = 0;
+        char *q = nullptr;
+        if (int r = dalloc(&q, epa_packed_block_bytes() * (size_t)blocks)) return r;
+        w.epa_packed = q;
+        W->epa_packed_blocks = blocks;
+    }
+    w.epa_threads = blocks * 64;
+    w.epa_fetch_warp = t.epa_lockstep;
+    w.warp_blocks_per_sm = t.warp_blocks_per_sm;
+    W->dev_settings.small_island_max_cons = t.small_max;
+    w.giant_min = t.giant_min;
+    drop_graph(W);
+    return CC_OK;
+}
+static int tune_snapshot(cc_world *W, bool save) {
+    DevWorld &w = W->w;
+    auto &T = W->tune;
+    cudaStream_t s = W->stream;
+    if (!T.ready) {
+        size_t cap = (size_t)w.cap, cc = (size_t)w.cache_cap;
+        int r;
+#define TA(ptr, count)                                                \
+    if ((r = dalloc(&(ptr), (count))) != CC_OK) return r;             \
+    T.allocs.push_back((void *)(ptr));
+        Checkpoint &c = T.c;
+        TA(c.pos, cap) TA(c.quat, cap) TA(c.com, cap) TA(c.linvel, cap) TA(c.angvel, cap) TA(c.force, cap)
+        TA(c.torque, cap) TA(c.sleep_sph, 3 * cap) TA(c.sleep_timer, cap) TA(c.flags, cap) TA(c.keys, cc)
+        TA(c.recs, cc) TA(c.parity, 1)
+        if (w.ccd_lambda) {
+            TA(T.ccd, (size_t)w.num_worlds)
+        }
+#undef TA
+        T.ready = true;
+    }
+    // joint records carry their accumulated impulses from step to step
+    size_t jb = sizeof(DevHinge) * (size_t)w.num_hinges + sizeof(DevSwing) * (size_t)w.num_swings;
+    if (save && jb > T.joint_bytes) {
+        if (T.joints) cudaFree(T.joints);
+        T.joints = nullptr;
+        T.joint_bytes = 0;
+        if (int r = dalloc(&T.joints, jb)) return r;
+        T.joint_bytes = jb;
+    }
+    if (save) {
+        checkpoint_save(w, T.c, s);
+    } else {
+        checkpoint_restore(w, T.c, s);
+    }
+    size_t hb = sizeof(DevHinge) * (size_t)w.num_hinges, sb = sizeof(DevSwing) * (size_t)w.num_swings;
+    if (hb) CC_TRY(cudaMemcpyAsync(save ? (void *)T.joints : (void *)w.hinges, save ? (void *)w.hinges : (void *)T.joints,
+                                   hb, cudaMemcpyDeviceToDevice, s));
+    if (sb)
+        CC_TRY(cudaMemcpyAsync(save ? (void *)(T.joints + hb) : (void *)w.swings,
+                               save ? (void *)w.swings : (void *)(T.joints + hb), sb, cudaMemcpyDeviceToDevice, s));
+    if (w.ccd_lambda && T.ccd)
+        CC_TRY(cudaMemcpyAsync(save ? (void *)T.ccd : (void *)w.ccd_lambda, save ? (void *)w.ccd_lambda : (void *)T.ccd,
+                               sizeof(float2) * (size_t)w.num_worlds, cudaMemcpyDeviceToDevice, s));
+    CC_TRY(cudaStreamSynchronize(s));
+    return CC_OK;
+}
+
+extern "C" int cc_world_autotune(cc_world *W, float dt, int32_t steps, cc_tune_report *rep) {
+    if (!W || !(dt > 0.f) || steps <= 0 || !rep) return CC_ERR_INVALID;
+    if (int r = sync_shapes(W)) return r;
+    DevWorld &w = W->w;
+    memset(rep, 0, sizeof(*rep));
+    if (w.n == 0) return CC_OK;
+    const double prev_dt = W->prev_dt;
+    const int steps_done = W->steps_done;
+    if (int r = tune_snapshot(W, true)) return r;
+    int trials = 0;
+    auto trial = [&](float &ms) -> int {
+        if (int r = tune_snapshot(W, false)) return r;
+        W->prev_dt = prev_dt;
+        int st = run_steps(W, dt, 1);
+        if (st == CC_ERR_CUDA) return st;
+        st = run_steps(W, dt, steps);
+        if (st == CC_ERR_CUDA) return st;
+        ms = W->last_call_ms / (float)steps;
+        trials++;
+        return CC_OK;
+    };
+    TuneShape cur = tune_shape_of(W);
+    float best = 0.f;
+    if (int r = trial(best)) return r;
+    rep->default_ms = best;
+    const bool piles = W->last_ctr.max_island_constraints > 2048;
+    const int sms = device_sm_count();
+    const int epa_cap = epa_max_threads() / 64 / sms;
+    for (int dim = 0; dim < 5; dim++) {
+        std::vector<int> cand;
+        if (dim == 0) cand = {2, 4, 6, 8};
+        if (dim == 1) cand = {1, 0};
+        if (dim == 2) cand = {1, 2, 3, 4};
+        if (dim == 3) cand = {4, 8, 16};
+        if (dim == 4 && piles) cand = {2048, 8192, 32768};
+        for (int v : cand) {
+            TuneShape t = cur;
+            int *field = dim == 0 ? &t.epa_blocks_per_sm
+                                  : dim == 1 ? &t.epa_lockstep
+                                  : dim == 2 ? &t.warp_blocks_per_sm : dim == 3 ? &t.small_max : &t.giant_min;
+            if (*field == v) continue;
+            if (dim == 0 && v > epa_cap) continue;
+            *field = v;
+            if (int r = tune_apply(W, t)) return r;
+            float ms = 0.f;
+            if (int r = trial(ms)) return r;
+            if (ms < 0.98f * best) {
+                best = ms;
+                cur = t;
+            }
+        }
+        if (int r = tune_apply(W, cur)) return r;
+    }
+    // keep the chosen shapes and leave the world where it was
+    if (int r = tune_apply(W, cur)) return r;
+    if (int r = tune_snapshot(W, false)) return r;
+    W->prev_dt = prev_dt;
+    W->steps_done = steps_done;
+    rep->tuned_ms = best;
+    rep->trials = trials;
+    rep->epa_blocks_per_sm = cur.epa_blocks_per_sm;
+    rep->epa_lockstep = cur.epa_lockstep;
+    rep->warp_blocks_per_sm = cur.warp_blocks_per_sm;
+    rep->small_island_max_contacts = cur.small_max;
+    rep->giant_min = cur.giant_min;
+    // kernel nodes of the step graph with the chosen shapes (captured by one more trial step)
+    float ms = 0.f;
+    if (int r = trial(ms)) return r;
+    if (W->graph) {
+        size_t nn = 0;
+        cudaGraphGetNodes(W->graph, nullptr, &nn);
+        std::vector<cudaGraphNode_t> nodes(nn);
+        cudaGraphGetNodes(W->graph, nodes.data(), &nn);
+        int k = 0;
+        for (size_t i = 0; i < nn; i++) {
+            cudaGraphNodeType ty;
+            cudaGraphNodeGetType(nodes[i], &ty);
+            k += ty == cudaGraphNodeTypeKernel;
+        }
+        rep->graph_kernels_per_step = k;
+    }
+    if (int r = tune_snapshot(W, false)) return r;
+    W->prev_dt = prev_dt;
+    W->steps_done = steps_done;
+    drop_graph(W);
     return CC_OK;
 }
 

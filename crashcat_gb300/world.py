@@ -351,6 +351,14 @@ class GpuWorld:
                                                   _lib.ptr(gm)), "cc_world_rollout_grad")
         return loss, gv, gw, gm
 
+    def autotune(self, dt: float, steps_per_trial: int = 3) -> dict:
+        """cc_world_autotune: times candidate launch shapes on the current state (which it leaves
+        as it found it) and keeps the fastest; returns the report as a dict."""
+        rep = _lib.TuneReport()
+        check(self._lib.cc_world_autotune(self.handle, C.c_float(dt), steps_per_trial, C.byref(rep)),
+              "cc_world_autotune")
+        return {f: getattr(rep, f) for f, _ in _lib.TuneReport._fields_}
+
     def step_taped(self, dt: float, capacity: int | None = None):
         """One step with the rows of its velocity solve (cc_world_step_taped): returns
         (bodies [n] TAPE_BODY_DTYPE, contacts TAPE_CONTACT_DTYPE, warm-start ratio, status)."""

@@ -44,6 +44,7 @@
  *                                 src/broadphase/broadphase.ts:112-123
  *   cc_world_step_taped        <- updateWorld, then reading world.contactConstraints
  *                                 src/constraints/contact-constraints.ts:32-146
+ *   cc_world_autotune          <- (no counterpart: launch shapes of this library)
  *   cc_world_get_stats         <- (no counterpart: per-step counters)
  *   cc_status_string           <- assert() messages          src/utils/assert.ts:1-9
  */
@@ -443,6 +444,34 @@ int cc_world_debug_islands(cc_world *world, int32_t *island_of_body, int32_t *co
 int cc_world_rollout_grad(cc_world *world, float dt, int32_t n_steps, int32_t checkpoint_every,
                           const float *targets, float *loss, float *grad_linvel, float *grad_angvel,
                           float *grad_friction);
+
+/* ---------------------------------------------------------------------------
+ * Launch-shape autotuner (no counterpart in the reference, which runs on one
+ * thread).  Times candidate launch shapes on the world's current state and keeps
+ * the fastest: coordinate descent over the EPA pass's resident blocks per SM and
+ * its lock-step rounds, the per-warp island tier's blocks per SM, the largest
+ * island solved by one thread, and (when the world has islands of thousands of
+ * constraints) the size from which the whole grid solves an island.  Every trial
+ * restores the state the call started from (bodies, contact cache, joint
+ * impulses), runs one untimed step and then steps_per_trial timed steps (CUDA
+ * events), so the call leaves the world where it found it.  A candidate must be
+ * 2 % faster to replace the current shape.  Each island's solve order and each
+ * EPA polytope are the same under every shape, so results change at most by the
+ * FP32 rounding of the kernel that solves an island.
+ * ------------------------------------------------------------------------- */
+typedef struct cc_tune_report {
+    float default_ms;            /* ms per step with the shapes the world had */
+    float tuned_ms;              /* ms per step with the shapes it keeps */
+    int32_t trials;
+    int32_t epa_blocks_per_sm;   /* 64-thread EPA blocks per SM */
+    int32_t epa_lockstep;        /* 1: a warp runs its 32 EPA items in lock-step rounds */
+    int32_t warp_blocks_per_sm;  /* blocks of the per-warp island tier per SM */
+    int32_t small_island_max_contacts;  /* islands up to this many contacts: one thread */
+    int32_t giant_min;           /* islands with more constraints: the whole grid */
+    int32_t graph_kernels_per_step;  /* kernel nodes of the captured step graph */
+} cc_tune_report;
+
+int cc_world_autotune(cc_world *world, float dt, int32_t steps_per_trial, cc_tune_report *report);
 
 /* ---------------------------------------------------------------------------
  * One step with its solver rows read back: reading world.contactConstraints

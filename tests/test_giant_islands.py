@@ -77,7 +77,7 @@ def test_ragdolls_on_other_tiers(gpu_lib, oracle_lib, tier, monkeypatch):
     if tier == "cta":
         monkeypatch.setenv("CRASHCAT_SMALL_JOINTS_MAX", "0")
     else:
-        monkeypatch.setenv("CRASHCAT_GIANT_MIN", "8")
+        monkeypatch.setenv("CRASHCAT_GIANT_MIN", "8")  # a lone ragdoll's 10 joints and its contacts
     sc = scenes.ragdolls(num=4, arena=12.0)
     g, o = make(sc), oracle(sc)
     g.step(sc.dt, 20)
@@ -105,19 +105,23 @@ def test_pile_of_ragdolls_runs_on_the_grid_tier(gpu_lib, monkeypatch):
 
 
 def test_grid_barrier_wait_runs_out_with_a_status(gpu_lib, monkeypatch):
-    """The grid barrier of the whole-grid solve polls a bounded number of times.  With the bound
-    set to one poll the first barrier gives up: every block leaves, the step returns
-    CC_ERR_TIMEOUT with OVF_TIMEOUT in the counters, and the device keeps answering (a world with
-    the default bound then steps normally)."""
-    monkeypatch.setenv("CRASHCAT_GIANT_MIN", "16")
-    sc = scenes.box_pyramid(base=8)
-    ws = world.standard_settings(device_wait_polls=1)
+    """The grid barrier of the whole-grid solve polls a bounded number of times.  With block 0
+    withheld from its barriers (CRASHCAT_TEST_WITHHOLD_BARRIER: a flag that nothing sets) the
+    other blocks' wait runs out after 20,000 polls: every block leaves, the step returns
+    CC_ERR_TIMEOUT with OVF_TIMEOUT in the counters, and the device keeps answering (a world
+    without the hook then steps normally)."""
+    monkeypatch.setenv("CRASHCAT_GIANT_MIN", "64")
+    monkeypatch.setenv("CRASHCAT_TEST_WITHHOLD_BARRIER", "1")
+    sc = scenes.box_pyramid(base=12)
+    ws = world.standard_settings(device_wait_polls=20000)
     g = world.GpuWorld(ws, sc.n + 8)
     g.add_bodies(sc.bodies)
-    st = g.step(sc.dt, 3)
-    assert st == _lib.CC_ERR_TIMEOUT
-    assert g.stats()["overflow_flags"] & 64
+    with pytest.raises(_lib.CCError) as e:
+        g.step(sc.dt, 3)
+    assert e.value.status == _lib.CC_ERR_TIMEOUT
     assert g.stats()["num_giant_islands"] >= 1
+    assert g.stats()["overflow_flags"] & 64
+    monkeypatch.delenv("CRASHCAT_TEST_WITHHOLD_BARRIER")
     ok = world.GpuWorld(world.standard_settings(), sc.n + 8)
     ok.add_bodies(sc.bodies)
     assert ok.step(sc.dt, 3) == _lib.CC_OK

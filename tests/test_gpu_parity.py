@@ -290,6 +290,33 @@ def test_epa_fallback_pass_matches_packed_pass(gpu_lib, monkeypatch):
         np.testing.assert_allclose(packed[k][8:], fallback[k][8:], atol=1e-4)
 
 
+def test_epa_lockstep_rounds_match_the_sequential_pass(gpu_lib, monkeypatch):
+    """The packed EPA pass runs a warp's 32 items in lock-step rounds; each lane's polytope sees
+    the same operations in the same order as the one-item-per-thread pass (CRASHCAT_EPA_FETCH_WARP
+    = 0), so the contacts of a settled batch of worlds, with thousands of EPA items, come out bit
+    for bit the same, and so does the state a few steps later."""
+    sc = scenes.batched_worlds(num_worlds=64, seed=4)
+    ws = world.standard_settings(velocity_iterations=sc.velocity_iterations,
+                                 position_iterations=sc.position_iterations)
+    ws.num_worlds = sc.num_worlds
+
+    def run():
+        g = world.GpuWorld(ws, sc.n + 16)
+        g.add_bodies(sc.bodies)
+        g.step(sc.dt, 200)
+        n_epa = g.stats()["num_epa"]
+        m = g.get_manifolds()
+        g.step(sc.dt, 5)
+        return n_epa, m, g.get_state()[0]
+
+    n_a, m_a, s_a = run()
+    monkeypatch.setenv("CRASHCAT_EPA_FETCH_WARP", "0")
+    n_b, m_b, s_b = run()
+    assert n_a > 500 and n_a == n_b
+    np.testing.assert_array_equal(m_a[np.lexsort(m_a[:, 1::-1].T)], m_b[np.lexsort(m_b[:, 1::-1].T)])
+    np.testing.assert_array_equal(s_a, s_b)
+
+
 # ---- capsules ------------------------------------------------------------------------
 @pytest.mark.parametrize("seed", [17, 18])
 def test_capsule_pairs_and_manifolds(gpu_lib, oracle_lib, seed):
