@@ -88,6 +88,8 @@ def parse():
     ap.add_argument("--terrain", type=int, default=1, help="measure the mixed-shape terrain workload (1) or skip it (0)")
     ap.add_argument("--cube-heap", type=int, default=1, help="measure the plain cube-heap workload (1) or skip it (0)")
     ap.add_argument("--tune", type=int, default=1, help="autotune the launch shapes before the warm-up (1) or not (0)")
+    ap.add_argument("--only", default="", choices=["", "cube_heap"],
+                    help="run one workload alone and print its report (for profiling)")
     ap.add_argument("--errors", type=int, default=1,
                     help="report the batched workload's error against the FP64 oracle (1) or skip it (0)")
     ap.add_argument("--settle", type=int, default=360,
@@ -524,7 +526,7 @@ def adjoint_measurement(num_worlds: int = 1024, steps: int = 120, checkpoint_eve
                                   "set and geometry move with the perturbation"}}
 
 
-def cube_heap_measurement(peak: float, peak_kind: str):
+def cube_heap_measurement(peak: float, peak_kind: str, oracle: bool = True):
     """The plain cube heap (1,000 boxes on a 10 x 10 x 10 grid dropped onto a static box floor,
     dt 1/60, 10/2 iterations, 600 steps) on one single-world handle through cc_world_step:
     body-steps/s over all 600 steps (1,001 bodies, the floor included as in the batched figure),
@@ -554,6 +556,9 @@ def cube_heap_measurement(peak: float, peak_kind: str):
     bytes_dom = algorithmic_bytes(dom, pst, sc.n)
     achieved = bytes_dom / (prof[dom] * 1e-3) / 1e9 if prof[dom] > 0 else 0.0
     del g
+    if not oracle:
+        return {"workload": "cube_heap", "value": sc.n * 600 / (total_ms * 1e-3), "unit": METRIC,
+                "ms_per_step": total_ms / 600, "phases": phases, "stage_ms": prof}
     obuild.build()
     o = pyoracle.OracleWorld(ws, sc.bodies)
     t0 = time.perf_counter()
@@ -1147,6 +1152,10 @@ def run_gpu(args, rank, world_size, local):
 def main():
     args = parse()
     rank, world_size, local = dist_env()
+    if args.only == "cube_heap":
+        peak, peak_kind = read_peaks()
+        print(json.dumps(cube_heap_measurement(peak, peak_kind, oracle=args.cpu_seconds > 0)), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world_size)
         return

@@ -1205,6 +1205,8 @@ struct PackedBlock {
     R nx[PK_TRI][EPA_BLOCK], ny[PK_TRI][EPA_BLOCK], nz[PK_TRI][EPA_BLOCK];
     R cx[PK_TRI][EPA_BLOCK], cy[PK_TRI][EPA_BLOCK], cz[PK_TRI][EPA_BLOCK];
     R cl[PK_TRI][EPA_BLOCK];
+    float fnx[PK_TRI][EPA_BLOCK], fny[PK_TRI][EPA_BLOCK], fnz[PK_TRI][EPA_BLOCK];  // FP32 copies of the
+    float fcx[PK_TRI][EPA_BLOCK], fcy[PK_TRI][EPA_BLOCK], fcz[PK_TRI][EPA_BLOCK];  // normal and centroid
     uint32_t vf[PK_TRI][EPA_BLOCK];   // st0 | st1 << 8 | st2 << 16 | flags << 24
     uint32_t nbt[PK_TRI][EPA_BLOCK];  // neighbour triangles, 8 bits each (0xff: none)
     uint32_t nbe[PK_TRI][EPA_BLOCK];  // neighbour edges, 8 bits each
@@ -1253,7 +1255,15 @@ struct PackedStore {
         b->cy[t][j] = c.y;
         b->cz[t][j] = c.z;
         b->cl[t][j] = cls;
+        b->fnx[t][j] = (float)n.x;
+        b->fny[t][j] = (float)n.y;
+        b->fnz[t][j] = (float)n.z;
+        b->fcx[t][j] = (float)c.x;
+        b->fcy[t][j] = (float)c.y;
+        b->fcz[t][j] = (float)c.z;
     }
+    __device__ float3 normal32(int t) const { return make_float3(b->fnx[t][j], b->fny[t][j], b->fnz[t][j]); }
+    __device__ float3 centroid32(int t) const { return make_float3(b->fcx[t][j], b->fcy[t][j], b->fcz[t][j]); }
     __device__ void set_flags(int t, int f) { b->vf[t][j] = (b->vf[t][j] & 0x00ffffffu) | ((uint32_t)f << 24); }
     __device__ void set_st(int t, int a, int c, int d) {
         b->vf[t][j] = (b->vf[t][j] & 0xff000000u) | (uint32_t)a | ((uint32_t)c << 8) | ((uint32_t)d << 16);
@@ -1288,6 +1298,15 @@ struct PackedStore {
     __device__ void set_newt(int i, int t) { b->nw[i][j] = (uint8_t)t; }
 };
 
+// An integer key with the order of the doubles it comes from (-0 and +0 equal, no NaNs here):
+// the heap and the face selection compare closest distances with integer instructions, which
+// keeps them off the FP64 pipe.
+__device__ __forceinline__ unsigned long long order_key(R x) {
+    long long b = __double_as_longlong(x);
+    if (b == (long long)0x8000000000000000ull) b = 0;
+    return b < 0 ? ~(unsigned long long)b : ((unsigned long long)b | 0x8000000000000000ull);
+}
+
 template <class S>
 struct Hull {
     S st;
@@ -1310,7 +1329,7 @@ struct Hull {
         while (cur > 0) {
             int par = (cur - 1) >> 1;
             int qp = st.q(par), qc = st.q(cur);
-            if (st.cls(qp) > st.cls(qc)) {
+            if (order_key(st.cls(qp)) > order_key(st.cls(qc))) {
                 st.set_q(par, qc);
                 st.set_q(cur, qp);
                 cur = par;
@@ -1330,9 +1349,9 @@ struct Hull {
             int child = (largest << 1) + 1;
             if (child >= count) break;
             int prevL = largest;
-            if (st.cls(st.q(largest)) > st.cls(st.q(child))) largest = child;
+            if (order_key(st.cls(st.q(largest))) > order_key(st.cls(st.q(child)))) largest = child;
             ++child;
-            if (child < count && st.cls(st.q(largest)) > st.cls(st.q(child))) largest = child;
+            if (child < count && order_key(st.cls(st.q(largest))) > order_key(st.cls(st.q(child)))) largest = child;
             if (prevL == largest) break;
             int t2 = st.q(prevL);
             st.set_q(prevL, st.q(largest));
@@ -1469,10 +1488,30 @@ struct Hull {
     // warp run the loop together (upto is the same on every lane), so the FP64 tests issue with
     // every lane whose polytope has that slot; find_edge then reads the bits (the geometry of a
     // triangle does not change while its flags do).  Packed store only (at most 64 slots).
+    //
+    // The test is taken in FP32 on the faces' FP32 copies first.  Rounding the inputs and the
+    // FP32 arithmetic move the dot product by at most about 6 x 2^-24 x S, S = sum |n_i|
+    // (|p_i| + |c_i|); when the FP32 value is further than 2^-19 x S from zero its sign is the
+    // exact sign, and so the sign the FP64 test gives.  Closer calls are taken in FP64.
     __device__ unsigned long long facing_mask(V<R> p, int upto) const {
+        const float px = (float)p.x, py = (float)p.y, pz = (float)p.z;
+        const float ax = fabsf(px), ay = fabsf(py), az = fabsf(pz);
         unsigned long long m = 0ull;
-        for (int t = 0; t < upto; t++)
-            if (t < ntri && facing(t, p)) m |= 1ull << t;
+        for (int t = 0; t < upto; t++) {
+            if (t >= ntri) continue;
+            const float3 n = st.normal32(t), c = st.centroid32(t);
+            const float r = n.x * (px - c.x) + n.y * (py - c.y) + n.z * (pz - c.z);
+            const float e = 1.9073486328125e-06f *  // 2^-19
+                            (fabsf(n.x) * (ax + fabsf(c.x)) + fabsf(n.y) * (ay + fabsf(c.y)) + fabsf(n.z) * (az + fabsf(c.z)));
+            bool f;
+            if (r > e)
+                f = true;
+            else if (r < -e)
+                f = false;
+            else
+                f = facing(t, p);
+            if (f) m |= 1ull << t;
+        }
         return m;
     }
     __device__ bool facing_of(int t, V<R> vtx, const unsigned long long *mask) const {
@@ -1720,138 +1759,148 @@ __device__ bool epa(Hull<S> &h, const SA &A, const SB &B, R tol, V<R> &outAxis,
     return epa_result(h, last, flip, outAxis, outPa, outPb);
 }
 
-// The same EPA with the growth and expansion loops cut into rounds that every lane of a warp runs
+// The same EPA with the growth and expansion loops cut into rounds that the lanes of a warp run
 // together: select a face (pop), one support point, the checks, and the horizon walk with the new
 // faces.  Each lane's polytope sees exactly the operations of epa(), in the same order; only the
 // facing tests of the horizon walk are taken for every face slot up front (facing_mask), in a loop
 // the lanes share, so that the FP64 work issues with most lanes of the warp active (on GB300 an
-// FP64 warp instruction costs the same whatever the number of active lanes).  Every lane of the
-// warp calls this; `active` says whether the lane has a pair.
+// FP64 warp instruction costs the same whatever the number of active lanes).
 enum : int { EPA_DONE = 0, EPA_GROW = 1, EPA_EXPAND = 2, EPA_FAIL = 3 };
+// one lane's EPA in progress: the locals of epa() between its loops
+struct EpaLane {
+    int phase, gguard, eguard, last;
+    R closest;
+    bool flip;
+    __device__ void begin(bool seeded) {
+        phase = seeded ? EPA_GROW : EPA_FAIL;
+        gguard = eguard = 0;
+        last = -1;
+        closest = EPA_MAXD;
+        flip = false;
+    }
+    __device__ bool running() const { return phase == EPA_GROW || phase == EPA_EXPAND; }
+};
+
+// one round of epa()'s growth / expansion loops for the lanes that are running
 template <class S, class SA, class SB>
-__device__ bool epa_lockstep(bool active, Hull<S> &h, const SA &A, const SB &B, R tol, V<R> &outAxis,
-                             V<R> &outPa, V<R> &outPb) {
+__device__ void epa_round(EpaLane &L, Hull<S> &h, const SA &A, const SB &B, R tol) {
     static_assert(S::TRI <= 64, "the facing mask holds one bit per face slot");
     const R MAXD = EPA_MAXD;
-    int phase = active ? (epa_seed(h, A, B) ? EPA_GROW : EPA_FAIL) : EPA_DONE;
-    int gguard = 0, eguard = 0, last = -1;
-    R closest = MAXD;
-    bool flip = false;
-    while (__any_sync(0xffffffffu, phase == EPA_GROW || phase == EPA_EXPAND)) {
-        // select: the face to expand (the loop heads of epa())
-        bool work = false;
-        int t = -1;
-        if (phase == EPA_GROW) {
-            if (!(gguard++ < 4096)) {
-                phase = EPA_EXPAND;
+    // select: the face to expand (the loop heads of epa()).  Faces removed by an earlier
+    // horizon are popped and dropped here, inside the same round, so that every lane with a
+    // polytope left reaches the support and the new faces together.
+    bool work = false;
+    int t = -1;
+    while (!work && (L.phase == EPA_GROW || L.phase == EPA_EXPAND)) {
+        if (L.phase == EPA_GROW) {
+            if (!(L.gguard++ < 4096)) {
+                L.phase = EPA_EXPAND;
             } else if (h.nq == 0) {
-                phase = EPA_FAIL;
+                L.phase = EPA_FAIL;
             } else {
                 t = h.st.q(0);
                 if (h.flags(t) & TF_REMOVED) {
                     h.pop();
                     if (h.nq == 0)
-                        phase = EPA_FAIL;
+                        L.phase = EPA_FAIL;
                     else
                         h.free_tri(t);
-                } else if (h.cls(t) >= 0.0) {
-                    phase = EPA_EXPAND;
+                } else if (order_key(h.cls(t)) >= order_key(0.0)) {
+                    L.phase = EPA_EXPAND;
                 } else {
                     h.pop();
                     work = true;
                 }
             }
-        } else if (phase == EPA_EXPAND) {
+        } else {
             t = h.pop();
             if (t < 0) {
-                phase = EPA_FAIL;
+                L.phase = EPA_FAIL;
             } else if (h.flags(t) & TF_REMOVED) {
                 h.free_tri(t);
-                if (!(h.nq > 0 && h.npts < 128 && eguard++ < 4096)) phase = EPA_DONE;
-            } else if (h.cls(t) >= closest) {
-                phase = EPA_DONE;
+                if (!(h.nq > 0 && h.npts < 128 && L.eguard++ < 4096)) L.phase = EPA_DONE;
+            } else if (order_key(h.cls(t)) >= order_key(L.closest)) {
+                L.phase = EPA_DONE;
             } else {
-                if (last >= 0) h.free_tri(last);
-                last = t;
+                if (L.last >= 0) h.free_tri(L.last);
+                L.last = t;
                 work = true;
             }
         }
-        // one support point along the face normal
-        V<R> tn{0.0, 0.0, 0.0};
-        int ni = -1;
-        if (work) {
-            tn = h.st.normal(t);
-            ni = h.add_sup(A, B, tn);
-            if (ni < 0) {
-                phase = phase == EPA_GROW ? EPA_FAIL : EPA_DONE;
+    }
+    // one support point along the face normal
+    V<R> tn{0.0, 0.0, 0.0};
+    int ni = -1;
+    if (work) {
+        tn = h.st.normal(t);
+        ni = h.add_sup(A, B, tn);
+        if (ni < 0) {
+            L.phase = L.phase == EPA_GROW ? EPA_FAIL : EPA_DONE;
+            work = false;
+        }
+    }
+    // the checks of the new point
+    R d = 0.0;
+    if (work) {
+        V<R> wv = h.st.Y(ni);
+        if (L.phase == EPA_GROW) {
+            if (!h.facing(t, wv)) {
+                L.phase = EPA_FAIL;
                 work = false;
             }
-        }
-        // the checks of the new point
-        R d = 0.0;
-        if (work) {
-            V<R> wv = h.st.Y(ni);
-            if (phase == EPA_GROW) {
-                if (!h.facing(t, wv)) {
-                    phase = EPA_FAIL;
-                    work = false;
-                }
+        } else {
+            d = dot(tn, wv);
+            if (d < 0.0) {
+                L.phase = EPA_FAIL;
+                work = false;
             } else {
-                d = dot(tn, wv);
-                if (d < 0.0) {
-                    phase = EPA_FAIL;
+                R dsq = (d * d) / lsq(tn);
+                if (dsq - h.cls(t) < h.cls(t) * tol) {
+                    L.phase = EPA_DONE;
                     work = false;
                 } else {
-                    R dsq = (d * d) / lsq(tn);
-                    if (dsq - h.cls(t) < h.cls(t) * tol) {
-                        phase = EPA_DONE;
+                    L.closest = L.closest < dsq ? L.closest : dsq;
+                    if (!h.facing(t, wv)) {
+                        L.phase = EPA_DONE;
                         work = false;
-                    } else {
-                        closest = closest < dsq ? closest : dsq;
-                        if (!h.facing(t, wv)) {
-                            phase = EPA_DONE;
-                            work = false;
-                        }
                     }
-                }
-            }
-        }
-        // the horizon and the new faces
-        if (work) {
-            const int upto = __reduce_max_sync(__activemask(), h.ntri);
-            const unsigned long long mask = h.facing_mask(h.st.Y(ni), upto);
-            int ne = h.add_point(t, ni, phase == EPA_GROW ? MAXD : closest, &mask);
-            if (phase == EPA_GROW) {
-                if (ne < 0) {
-                    phase = EPA_FAIL;
-                } else {
-                    h.free_tri(t);
-                    if (h.nq == 0 || h.npts >= 32) phase = EPA_FAIL;
-                }
-            } else if (ne < 0) {
-                phase = EPA_DONE;
-            } else {
-                bool defect = false;
-                for (int k = 0; k < ne; k++) {
-                    int q = h.st.newt(k);
-                    if (dot(h.st.normal(q), h.st.centroid(q)) < 0.0) {
-                        defect = true;
-                        break;
-                    }
-                }
-                if (defect) {
-                    V<R> nn = -tn;
-                    V<R> w2 = A.get(nn) - B.get(tn);
-                    if (dot(nn, w2) < d) flip = true;
-                    phase = EPA_DONE;
-                } else if (!(h.nq > 0 && h.npts < 128 && eguard++ < 4096)) {
-                    phase = EPA_DONE;
                 }
             }
         }
     }
-    if (!active || phase == EPA_FAIL) return false;
-    return epa_result(h, last, flip, outAxis, outPa, outPb);
+    // the horizon and the new faces
+    if (work) {
+        const int upto = __reduce_max_sync(__activemask(), h.ntri);
+        const unsigned long long mask = h.facing_mask(h.st.Y(ni), upto);
+        int ne = h.add_point(t, ni, L.phase == EPA_GROW ? MAXD : L.closest, &mask);
+        if (L.phase == EPA_GROW) {
+            if (ne < 0) {
+                L.phase = EPA_FAIL;
+            } else {
+                h.free_tri(t);
+                if (h.nq == 0 || h.npts >= 32) L.phase = EPA_FAIL;
+            }
+        } else if (ne < 0) {
+            L.phase = EPA_DONE;
+        } else {
+            bool defect = false;
+            for (int k = 0; k < ne; k++) {
+                int q = h.st.newt(k);
+                if (dot(h.st.normal(q), h.st.centroid(q)) < 0.0) {
+                    defect = true;
+                    break;
+                }
+            }
+            if (defect) {
+                V<R> nn = -tn;
+                V<R> w2 = A.get(nn) - B.get(tn);
+                if (dot(nn, w2) < d) L.flip = true;
+                L.phase = EPA_DONE;
+            } else if (!(h.nq > 0 && h.npts < 128 && L.eguard++ < 4096)) {
+                L.phase = EPA_DONE;
+            }
+        }
+    }
 }
 
 // Supports of one queued pair in A's local frame (convex.ts:440-452): EPA runs on the full
@@ -1926,29 +1975,27 @@ __device__ void epa_finish(const DevWorld &w, EpaItem &it, bool ok, R maxSep, V<
     it.pad = __float_as_int((float)(penetration));
 }
 
-// Packed pass.  fetch_warp = 1: a warp takes 32 consecutive items at a time and runs them in
-// lock-step rounds (epa_lockstep); fetch_warp = 0: each thread takes its next item as soon as it
-// finishes one and runs it alone (epa).  Items that outgrow the packed limits go to the fallback
-// list.
+// Packed pass.  fetch_warp = 1: the lanes of a warp run their items in lock-step rounds
+// (epa_round), and a lane whose polytope is done writes its result and takes the next item at
+// once, so the warp stays full until the queue runs dry; fetch_warp = 0: each thread takes its
+// next item as soon as it finishes one and runs it alone (epa).  Items that outgrow the packed
+// limits go to the fallback list.
 template <bool H>
 __device__ __forceinline__ void epa_packed_item(DevWorld &w, EpaItem *items, int i, Hull<PackedStore> &h,
-                                                int *fallback, int pts_limit, bool lockstep) {
-    const bool active = i >= 0 && items[i].tri < 0;  // mesh triangles: k_epa_mesh
+                                                int *fallback, int pts_limit) {
+    EpaItem &it = items[i];
+    if (it.tri >= 0) return;  // mesh triangles: k_epa_mesh
     Sup<R, H> A, B;
-    R maxSep = 0.0;
-    if (active) {
-        epa_setup(w, items[i], A, B, maxSep);
-        h.start(items[i], pts_limit);
-    }
-    V<R> axis{0.0, 0.0, 0.0}, pa{0.0, 0.0, 0.0}, pb{0.0, 0.0, 0.0};
-    bool ok = lockstep ? epa_lockstep(active, h, A, B, R(c_settings.penetration_tol), axis, pa, pb)
-                       : (active && epa(h, A, B, R(c_settings.penetration_tol), axis, pa, pb));
-    if (!active) return;
+    R maxSep;
+    epa_setup(w, it, A, B, maxSep);
+    h.start(it, pts_limit);
+    V<R> axis, pa, pb;
+    bool ok = epa(h, A, B, R(c_settings.penetration_tol), axis, pa, pb);
     if (h.overflow) {
         fallback[atomicAdd(&w.ctr->epa_fallback, 1)] = i;
         return;
     }
-    epa_finish(w, items[i], ok, maxSep, axis, pa, pb);
+    epa_finish(w, it, ok, maxSep, axis, pa, pb);
 }
 
 // H: the world has convex hulls (without them the support code leaves the hull loop out)
@@ -1959,19 +2006,54 @@ __global__ void __launch_bounds__(EPA_BLOCK) k_epa(DevWorld w, EpaItem *items, P
     Hull<PackedStore> h;
     h.st.b = blocks + blockIdx.x;
     h.st.j = threadIdx.x;
-    if (fetch_warp) {
-        const int lane = threadIdx.x & 31;
-        while (true) {
-            int base = 0;
-            if (lane == 0) base = atomicAdd(&w.ctr->epa_cursor, 32);
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (base >= ne) break;
-            epa_packed_item<H>(w, items, base + lane < ne ? base + lane : -1, h, fallback, pts_limit, true);
-            __syncwarp();
-        }
-    } else {
+    if (!fetch_warp) {
         for (int i = atomicAdd(&w.ctr->epa_cursor, 1); i < ne; i = atomicAdd(&w.ctr->epa_cursor, 1))
-            epa_packed_item<H>(w, items, i, h, fallback, pts_limit, false);
+            epa_packed_item<H>(w, items, i, h, fallback, pts_limit);
+        return;
+    }
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    const R tol = R(c_settings.penetration_tol);
+    int item = -1;           // the item this lane's polytope belongs to
+    bool exhausted = false;  // the queue has nothing left for this lane
+    EpaLane L;
+    L.phase = EPA_DONE;
+    Sup<R, H> A, B;
+    R maxSep = 0.0;
+    while (true) {
+        // a lane whose polytope is done writes the result and takes the next item
+        const bool idle = !L.running();
+        if (idle && item >= 0) {
+            V<R> axis{0.0, 0.0, 0.0}, pa{0.0, 0.0, 0.0}, pb{0.0, 0.0, 0.0};
+            bool ok = L.phase != EPA_FAIL && epa_result(h, L.last, L.flip, axis, pa, pb);
+            if (h.overflow)
+                fallback[atomicAdd(&w.ctr->epa_fallback, 1)] = item;
+            else
+                epa_finish(w, items[item], ok, maxSep, axis, pa, pb);
+            item = -1;
+        }
+        const bool need = idle && !exhausted;
+        const unsigned want = __ballot_sync(FULL, need);
+        if (want) {
+            const int leader = __ffs(want) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(&w.ctr->epa_cursor, __popc(want));
+            base = __shfl_sync(FULL, base, leader);
+            if (need) {
+                const int i = base + __popc(want & below);
+                if (i >= ne) {
+                    exhausted = true;
+                } else if (items[i].tri < 0) {  // mesh triangles: k_epa_mesh
+                    item = i;
+                    epa_setup(w, items[i], A, B, maxSep);
+                    h.start(items[i], pts_limit);
+                    L.begin(epa_seed(h, A, B));
+                }
+            }
+        }
+        if (!__any_sync(FULL, L.running() || item >= 0 || !exhausted)) break;
+        epa_round(L, h, A, B, tol);
     }
 }
 
