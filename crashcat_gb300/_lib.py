@@ -208,6 +208,19 @@ EXPORTS = {
     "cc_world_set_swing_twist_motor": ([C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                         C.c_float], C.c_int),
     "cc_world_set_swing_twist_enabled": ([C.c_void_p, C.c_int32, C.c_int32], C.c_int),
+    "cc_world_add_point_joints": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
+    "cc_world_add_distance_joints": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
+    "cc_world_add_fixed_joints": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
+    "cc_world_add_cone_joints": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
+    "cc_world_add_slider_joints": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
+    "cc_world_set_distance": ([C.c_void_p, C.c_int32, C.c_float, C.c_float], C.c_int),
+    "cc_world_set_cone_half_angle": ([C.c_void_p, C.c_int32, C.c_float], C.c_int),
+    "cc_world_set_slider_limits": ([C.c_void_p, C.c_int32, C.c_float, C.c_float], C.c_int),
+    "cc_world_set_slider_motor": ([C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_float], C.c_int),
+    "cc_world_get_slider_positions": ([C.c_void_p, C.c_void_p, C.c_int32], C.c_int),
+    "cc_world_set_joint_enabled": ([C.c_void_p, C.c_int32, C.c_int32, C.c_int32], C.c_int),
+    "cc_world_get_joint_lambdas": ([C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)],
+                                   C.c_int),
     "cc_status_string": ([C.c_int], C.c_char_p),
 }
 
@@ -276,6 +289,63 @@ def swing_twist_defaults(n: int) -> np.ndarray:
     h["swing_min_torque_limit"] = h["twist_min_torque_limit"] = -np.inf
     h["swing_max_torque_limit"] = h["twist_max_torque_limit"] = np.inf
     h["enabled"] = 1
+    return h
+
+
+# cc_joint_type (the reference's ConstraintType) and the point, distance, fixed, cone and
+# slider joint descriptions
+JOINT_POINT, JOINT_DISTANCE, JOINT_HINGE, JOINT_SLIDER, JOINT_FIXED, JOINT_CONE, JOINT_SWING_TWIST = range(7)
+_JOINT_TAIL = [("priority", np.int32), ("enabled", np.int32),
+               ("num_velocity_steps_override", np.int32), ("num_position_steps_override", np.int32)]
+POINT_JOINT_DTYPE = np.dtype([("body_a", np.int32), ("body_b", np.int32), ("space", np.int32),
+                        ("point_a", np.float32, 3), ("point_b", np.float32, 3)] + _JOINT_TAIL)
+DISTANCE_JOINT_DTYPE = np.dtype([("body_a", np.int32), ("body_b", np.int32), ("space", np.int32),
+                           ("point_a", np.float32, 3), ("point_b", np.float32, 3),
+                           ("min_distance", np.float32), ("max_distance", np.float32),
+                           ("spring", SPRING_DTYPE)] + _JOINT_TAIL)
+FIXED_JOINT_DTYPE = np.dtype([("body_a", np.int32), ("body_b", np.int32), ("space", np.int32),
+                        ("auto_detect_point", np.int32), ("point_a", np.float32, 3), ("point_b", np.float32, 3),
+                        ("axis_x_a", np.float32, 3), ("axis_y_a", np.float32, 3),
+                        ("axis_x_b", np.float32, 3), ("axis_y_b", np.float32, 3)] + _JOINT_TAIL)
+CONE_JOINT_DTYPE = np.dtype([("body_a", np.int32), ("body_b", np.int32), ("space", np.int32),
+                       ("point_a", np.float32, 3), ("point_b", np.float32, 3),
+                       ("twist_axis_a", np.float32, 3), ("twist_axis_b", np.float32, 3),
+                       ("half_cone_angle", np.float32)] + _JOINT_TAIL)
+SLIDER_JOINT_DTYPE = np.dtype([("body_a", np.int32), ("body_b", np.int32), ("space", np.int32),
+                         ("auto_detect_point", np.int32), ("point_a", np.float32, 3), ("point_b", np.float32, 3),
+                         ("slider_axis_a", np.float32, 3), ("slider_axis_b", np.float32, 3),
+                         ("normal_axis_a", np.float32, 3), ("normal_axis_b", np.float32, 3),
+                         ("limits_min", np.float32), ("limits_max", np.float32), ("limits_spring", SPRING_DTYPE),
+                         ("max_friction_force", np.float32), ("motor_spring", SPRING_DTYPE),
+                         ("min_force_limit", np.float32), ("max_force_limit", np.float32),
+                         ("motor_state", np.int32), ("target_velocity", np.float32),
+                         ("target_position", np.float32)] + _JOINT_TAIL)
+JOINT_DTYPES = {JOINT_POINT: POINT_JOINT_DTYPE, JOINT_DISTANCE: DISTANCE_JOINT_DTYPE,
+                JOINT_FIXED: FIXED_JOINT_DTYPE, JOINT_CONE: CONE_JOINT_DTYPE, JOINT_SLIDER: SLIDER_JOINT_DTYPE}
+JOINT_ADDERS = {JOINT_POINT: "cc_world_add_point_joints", JOINT_DISTANCE: "cc_world_add_distance_joints",
+                JOINT_FIXED: "cc_world_add_fixed_joints", JOINT_CONE: "cc_world_add_cone_joints",
+                JOINT_SLIDER: "cc_world_add_slider_joints"}
+
+
+def joint_defaults(joint_type: int, n: int) -> np.ndarray:
+    """n records of a point, distance, fixed, cone or slider joint with the reference's create
+    defaults: world space, enabled, priority 0; distance bounds unset (the current distance);
+    fixed axes X = (1,0,0), Y = (0,1,0); slider without limits, motor off, position-motor spring
+    2 Hz / damping 1 and unbounded force (slider-constraint.ts:380-404, motor-settings.ts:37-51)."""
+    h = np.zeros(n, JOINT_DTYPES[joint_type])
+    h["enabled"] = 1
+    if joint_type == JOINT_DISTANCE:
+        h["min_distance"] = h["max_distance"] = -1.0
+    elif joint_type == JOINT_FIXED:
+        h["axis_x_a"] = h["axis_x_b"] = (1.0, 0.0, 0.0)
+        h["axis_y_a"] = h["axis_y_b"] = (0.0, 1.0, 0.0)
+    elif joint_type == JOINT_SLIDER:
+        h["limits_min"] = -np.inf
+        h["limits_max"] = np.inf
+        h["motor_spring"]["frequency_or_stiffness"] = 2.0
+        h["motor_spring"]["damping"] = 1.0
+        h["min_force_limit"] = -np.inf
+        h["max_force_limit"] = np.inf
     return h
 
 

@@ -217,8 +217,11 @@ struct DevMesh {
 };
 constexpr int MESH_KEY_BITS = 21;  // body indices and triangle indices in a mesh contact's cache key
 
-// user joints of both types share one id space: hinges 0.., swing-twists JOINT_SWING | index
-constexpr int JOINT_SWING = 1 << 30;
+// user joints of every type share one id space, packed as the reference's ConstraintId
+// (constraint-id.ts:1-35): the ConstraintType above bit 24, the per-type index below
+enum : int { JT_POINT = 0, JT_DISTANCE = 1, JT_HINGE = 2, JT_SLIDER = 3, JT_FIXED = 4, JT_CONE = 5, JT_SWING = 6,
+             JT_TYPES = 7 };
+constexpr int JOINT_TYPE_SHIFT = 24, JOINT_INDEX_MASK = (1 << JOINT_TYPE_SHIFT) - 1;
 
 // fields every joint type starts with
 struct DevJointHead {
@@ -239,6 +242,60 @@ struct DevPoint {
 struct DevAngle {
     float3 i1, i2;  // I1^-1 axis, I2^-1 axis
     float eff, soft, bias, lambda;
+};
+
+// RotationEulerConstraintPart (rotation-euler-constraint-part.ts): 3 rotational rows
+struct DevEuler {
+    float invI1[6], invI2[6];  // symmetric xx xy xz yy yz zz
+    float eff[9];              // row-major
+    float3 lambda;
+};
+// AxisConstraintPart (axis-constraint-part.ts) of a joint: one row along a world axis
+struct DevAxis {
+    float3 r1xa, r2xa, i1, i2;  // (r1 + u) x axis, r2 x axis, and the inverse inertias times them
+    float eff, soft, bias, lambda;
+};
+// DualAxisConstraintPart (dual-axis-constraint-part.ts): 2 translational rows; eff as the
+// reference's column-major mat2 [m00, m10, m01, m11]
+struct DevDual {
+    float3 r1xn1, r1xn2, r2xn1, r2xn2, i1n1, i1n2, i2n1, i2n2;
+    float eff[4], lambda[2];
+};
+
+// Point, distance, fixed, cone and slider joints in one record (point-, distance-, fixed-,
+// cone-, slider-constraint.ts): the fields of the joint's type are used, the rest stay zero.
+struct DevJoint {
+    DevJointHead h;
+    int type;                     // JT_POINT .. JT_CONE
+    float3 lp1, lp2;              // attachment points from the centres of mass, body space
+    float4 inv_initial;           // fixed, slider: inverse initial relative orientation
+    // distance
+    float min_dist, max_dist;
+    int spring_mode;
+    float spring_freq, spring_damping;
+    // cone: twist axes (body space), cosine of the half cone angle
+    float3 lt1, lt2;
+    float cos_half_cone;
+    // slider: axis and normals (body A space), limits, friction and motor
+    float3 ls1, ln1, ln2;
+    int slider_flags;             // bit 0: limits
+    float limits_min, limits_max;
+    int limits_spring_mode;
+    float limits_freq, limits_damping, max_friction_force;
+    int motor_state, motor_spring_mode;
+    float motor_freq, motor_damping, min_force, max_force, target_velocity, target_position;
+    // per-step state
+    float3 wp1, wp2, wn;          // distance: world points and normal
+    float min_lambda, max_lambda;
+    float3 w_rot_axis;            // cone: rotation axis of the limit
+    float cos_theta;
+    float3 r1, r2, u, ws, n1, n2; // slider: arms, separation, world axis and normals
+    float d;                      // slider: position along the axis
+    DevPoint pt;
+    DevEuler rot;
+    DevAxis ax, motor;            // distance row, cone unused; slider limits (ax) and motor
+    DevAngle ang;                 // cone limit
+    DevDual dual;                 // slider position rows
 };
 
 struct DevHinge {
@@ -387,6 +444,11 @@ struct DevWorld {
     int num_hinges, max_hinges;
     DevSwing *swings;
     int num_swings, max_swings;
+    // point, distance, fixed, cone and slider joints, sorted by (type, per-type index)
+    DevJoint *others;
+    int num_others, max_others;
+    int type_count[JT_TYPES];  // joints of each type (hinges and swing-twists included)
+    int type_first[JT_TYPES];  // first record of each type in others
     int skip_joint_pairs;              // broadphase skips body pairs that share an enabled joint
     int *joint_partners;               // JOINT_PARTNERS per body: other bodies joined to it (-1: none)
     int *island_joint_count, *island_joint_off, *island_fill_j;
@@ -467,13 +529,27 @@ __device__ inline float shape_inner_radius(const DevWorld &w, uint32_t f, float4
 }
 
 // ---- user joints of every type under one id ---------------------------------------------
-__device__ __forceinline__ int joint_total(const DevWorld &w) { return w.num_hinges + w.num_swings; }
-// the k-th joint in type order (hinges, then swing-twists), each type in creation order
+__device__ __forceinline__ int joint_total(const DevWorld &w) { return w.num_hinges + w.num_swings + w.num_others; }
+__device__ __forceinline__ int joint_type_of(int id) { return id >> JOINT_TYPE_SHIFT; }
+__device__ __forceinline__ int joint_index_of(int id) { return id & JOINT_INDEX_MASK; }
+// the k-th joint in type order, each type in creation order (the order in which the reference
+// walks its constraint pools, constraints.ts:264-318)
 __device__ __forceinline__ int joint_id_at(const DevWorld &w, int k) {
-    return k < w.num_hinges ? k : (JOINT_SWING | (k - w.num_hinges));
+    for (int t = 0; t < JT_TYPES; t++) {
+        const int c = w.type_count[t];
+        if (k < c) return (t << JOINT_TYPE_SHIFT) | k;
+        k -= c;
+    }
+    return -1;
+}
+__device__ __forceinline__ DevJoint &other_joint(const DevWorld &w, int id) {
+    return w.others[w.type_first[joint_type_of(id)] + joint_index_of(id)];
 }
 __device__ __forceinline__ DevJointHead &joint_head(const DevWorld &w, int id) {
-    return id & JOINT_SWING ? w.swings[id & ~JOINT_SWING].h : w.hinges[id].h;
+    const int t = joint_type_of(id), i = joint_index_of(id);
+    if (t == JT_HINGE) return w.hinges[i].h;
+    if (t == JT_SWING) return w.swings[i].h;
+    return w.others[w.type_first[t] + i].h;
 }
 __device__ __forceinline__ bool joint_active(const DevWorld &w, const DevJointHead &h) {
     return (h.flags & JF_ENABLED) && !(sleeping_of(w.flags[h.a]) && sleeping_of(w.flags[h.b]));
@@ -484,7 +560,7 @@ __device__ __forceinline__ bool joint_before(const DevWorld &w, int x, int y) {
     const DevJointHead &a = joint_head(w, x), &b = joint_head(w, y);
     if (a.priority != b.priority) return a.priority < b.priority;
     if (a.index != b.index) return a.index < b.index;
-    return (x & JOINT_SWING) < (y & JOINT_SWING);
+    return joint_type_of(x) < joint_type_of(y);
 }
 
 

@@ -1,7 +1,7 @@
-// User joints on the device: setup, warm start, velocity and position solve of the hinge
-// (src/constraints/hinge-constraint.ts) and swing-twist (swing-twist-constraint.ts) joints and
-// the constraint parts they are built from (constraint-part/point-, hinge-rotation-, angle-,
-// swing-twist-, rotation-euler-constraint-part.ts, spring-part.ts).  FP32 like the contact
+// User joints on the device: setup, warm start, velocity and position solve of the point,
+// distance, hinge, slider, fixed, cone and swing-twist joints (src/constraints/*-constraint.ts)
+// and the constraint parts they are built from (constraint-part/point-, axis-, dual-axis-,
+// hinge-rotation-, angle-, swing-twist-, rotation-euler-constraint-part.ts, spring-part.ts).  FP32 like the contact
 // solver; the 3x3 and 2x2 effective-mass inversions and the swing ellipse projection run in
 // FP64.  Body state is read and written in global memory; the joints of an island are solved
 // in order by one thread of the per-CTA island solve.
@@ -682,24 +682,578 @@ __device__ bool swing_solve_position(DevWorld &w, DevSwing &j) {
     return imp;
 }
 
+// ---- velocity steps with the translation DOF lock (motion-properties.ts:702-720) ----------
+__device__ __forceinline__ void add_lin_locked(DevWorld &w, int i, float3 d) {
+    float4 v = w.linvel[i];
+    float3 n = f3(v.x + d.x, v.y + d.y, v.z + d.z);
+    const int dof = dof_of(w.flags[i]);
+    if (!(dof & 1)) n.x = 0.f;
+    if (!(dof & 2)) n.y = 0.f;
+    if (!(dof & 4)) n.z = 0.f;
+    w.linvel[i] = make_float4(n.x, n.y, n.z, v.w);
+}
+// AngleConstraintPart.solvePositionConstraint (angle-constraint-part.ts)
+__device__ bool angle_solve_position(DevWorld &w, const DevAngle &p, const JBody &A, const JBody &B, float C,
+                                     float beta) {
+    if (C == 0.f || p.eff == 0.f || p.soft != 0.f) return false;
+    const float l = -p.eff * beta * C;
+    if (A.motion == DYNAMIC) add_rotation(w, A.i, -(p.i1 * l));
+    if (B.motion == DYNAMIC) add_rotation(w, B.i, p.i2 * l);
+    return true;
+}
+
+// ---- rotation-euler part (rotation-euler-constraint-part.ts) -------------------------
+__device__ __forceinline__ void euler_deactivate(DevEuler &p) {
+    for (int k = 0; k < 9; k++) p.eff[k] = 0.f;
+    p.lambda = f3(0.f, 0.f, 0.f);
+}
+// calculateConstraintProperties :127-156: K = (I1^-1 + I2^-1)^-1, inverted in FP64
+__device__ void euler_calc(DevEuler &p, const JBody &A, const JBody &B) {
+    sym_store(p.invI1, A.I);
+    sym_store(p.invI2, B.I);
+    Sym3 sum{A.I.xx + B.I.xx, A.I.xy + B.I.xy, A.I.xz + B.I.xz, A.I.yy + B.I.yy, A.I.yz + B.I.yz, A.I.zz + B.I.zz};
+    float m[9];
+    jm_from_sym(m, sum);
+    if (!jm_invert(p.eff, m)) euler_deactivate(p);
+}
+__device__ bool euler_apply(DevWorld &w, const DevEuler &p, const JBody &A, const JBody &B, float3 l) {
+    if (lensq3(l) == 0.f) return false;
+    if (A.motion == DYNAMIC) add_ang(w, A.i, -symmul(sym_load(p.invI1), l));
+    if (B.motion == DYNAMIC) add_ang(w, B.i, symmul(sym_load(p.invI2), l));
+    return true;
+}
+__device__ void euler_warm(DevWorld &w, DevEuler &p, const JBody &A, const JBody &B, float ratio) {
+    p.lambda = p.lambda * ratio;
+    euler_apply(w, p, A, B, p.lambda);
+}
+__device__ bool euler_solve_velocity(DevWorld &w, DevEuler &p, const JBody &A, const JBody &B) {
+    float3 w1 = A.motion != STATIC ? xyz(w.angvel[A.i]) : f3(0.f, 0.f, 0.f);
+    float3 w2 = B.motion != STATIC ? xyz(w.angvel[B.i]) : f3(0.f, 0.f, 0.f);
+    float3 l = jm_mv(p.eff, w1 - w2);
+    p.lambda = p.lambda + l;
+    return euler_apply(w, p, A, B, l);
+}
+// solvePositionConstraint :256-311: error 2 xyz of q2 invInitial q1^-1 with w made positive
+__device__ bool euler_solve_position(DevWorld &w, const DevEuler &p, const JBody &A, const JBody &B, float4 inv_initial,
+                                     float beta) {
+    float4 diff = qmul(qmul(w.quat[B.i], inv_initial), qconj4(w.quat[A.i]));
+    if (diff.w < 0.f) diff = make_float4(-diff.x, -diff.y, -diff.z, -diff.w);
+    float3 err = f3(2.f * diff.x, 2.f * diff.y, 2.f * diff.z);
+    if (lensq3(err) < 1e-12f) return false;
+    float3 l = jm_mv(p.eff, err) * (-beta);
+    if (A.motion == DYNAMIC) add_rotation(w, A.i, -symmul(sym_load(p.invI1), l));
+    if (B.motion == DYNAMIC) add_rotation(w, B.i, symmul(sym_load(p.invI2), l));
+    return true;
+}
+
+// ---- axis part of a joint (axis-constraint-part.ts) ----------------------------------
+__device__ float axis_iem(DevAxis &p, const JBody &A, const JBody &B, float3 r1, float3 r2, float3 ax) {
+    float iem = 0.f;
+    p.r1xa = p.r2xa = p.i1 = p.i2 = f3(0.f, 0.f, 0.f);
+    if (A.motion == DYNAMIC) {
+        p.r1xa = cross3(r1, ax);
+        p.i1 = symmul(A.I, p.r1xa);
+        iem += A.im + dot3(p.i1, p.r1xa);
+    }
+    if (B.motion == DYNAMIC) {
+        p.r2xa = cross3(r2, ax);
+        p.i2 = symmul(B.I, p.r2xa);
+        iem += B.im + dot3(p.i2, p.r2xa);
+    }
+    return iem;
+}
+__device__ __forceinline__ void axis_deactivate(DevAxis &p) {
+    p.eff = 0.f;
+    p.lambda = 0.f;
+}
+__device__ void axis_calc(DevAxis &p, const JBody &A, const JBody &B, float3 r1, float3 r2, float3 ax, float bias) {
+    float iem = axis_iem(p, A, B, r1, r2, ax);
+    if (iem == 0.f) {
+        axis_deactivate(p);
+    } else {
+        p.eff = 1.f / iem;
+        p.soft = 0.f;
+        p.bias = bias;
+    }
+}
+__device__ void axis_calc_settings(DevAxis &p, float dt, const JBody &A, const JBody &B, float3 r1, float3 r2,
+                                   float3 ax, float bias, float C, int mode, float fs, float damping) {
+    float iem = axis_iem(p, A, B, r1, r2, ax);
+    if (iem == 0.f)
+        axis_deactivate(p);
+    else
+        p.eff = spring_settings(p.soft, p.bias, dt, iem, bias, C, mode, fs, damping);
+}
+__device__ void axis_push(DevWorld &w, const DevAxis &p, const JBody &A, const JBody &B, float3 ax, float l) {
+    if (A.motion == DYNAMIC) {
+        add_lin_locked(w, A.i, ax * (-l * A.im));
+        add_ang(w, A.i, -(p.i1 * l));
+    }
+    if (B.motion == DYNAMIC) {
+        add_lin_locked(w, B.i, ax * (l * B.im));
+        add_ang(w, B.i, p.i2 * l);
+    }
+}
+__device__ void axis_warm(DevWorld &w, DevAxis &p, const JBody &A, const JBody &B, float3 ax, float ratio) {
+    p.lambda *= ratio;
+    if (p.lambda == 0.f) return;
+    axis_push(w, p, A, B, ax, p.lambda);
+}
+// solveVelocityConstraint: getTotalLambda :578-625, clamp, applyLambda :640-707
+__device__ bool axis_solve_velocity(DevWorld &w, DevAxis &p, const JBody &A, const JBody &B, float3 ax, float mn,
+                                    float mx) {
+    const bool mA = A.motion != STATIC, mB = B.motion != STATIC;
+    float jv = 0.f;
+    if (mA && mB)
+        jv = dot3(ax, xyz(w.linvel[A.i]) - xyz(w.linvel[B.i]));
+    else if (mA)
+        jv = dot3(ax, xyz(w.linvel[A.i]));
+    else if (mB)
+        jv = -dot3(ax, xyz(w.linvel[B.i]));
+    if (mA) jv += dot3(p.r1xa, xyz(w.angvel[A.i]));
+    if (mB) jv -= dot3(p.r2xa, xyz(w.angvel[B.i]));
+    float tl = p.lambda + p.eff * (jv - (p.soft * p.lambda + p.bias));
+    tl = fmaxf(mn, fminf(mx, tl));
+    const float dl = tl - p.lambda;
+    p.lambda = tl;
+    if (dl == 0.f) return false;
+    axis_push(w, p, A, B, ax, dl);
+    return true;
+}
+// solvePositionConstraintWithMassOverride :790-847
+__device__ bool axis_solve_position(DevWorld &w, const DevAxis &p, const JBody &A, const JBody &B, float3 ax, float C,
+                                    float beta) {
+    if (C == 0.f || p.eff == 0.f || p.soft != 0.f) return false;
+    const float l = -p.eff * beta * C;
+    if (A.motion == DYNAMIC) {
+        add_position_step(w, A.i, ax * (-l * A.im));
+        add_rotation(w, A.i, -(p.i1 * l));
+    }
+    if (B.motion == DYNAMIC) {
+        add_position_step(w, B.i, ax * (l * B.im));
+        add_rotation(w, B.i, p.i2 * l);
+    }
+    return true;
+}
+
+// ---- dual-axis part (dual-axis-constraint-part.ts) -----------------------------------
+__device__ __forceinline__ void dual_deactivate(DevDual &p) {
+    p.lambda[0] = p.lambda[1] = 0.f;
+    p.eff[0] = p.eff[1] = p.eff[2] = p.eff[3] = 0.f;
+}
+__device__ __forceinline__ bool dual_active(const DevDual &p) {
+    return p.eff[0] != 0.f || p.eff[1] != 0.f || p.eff[2] != 0.f || p.eff[3] != 0.f;
+}
+// calculateConstraintProperties :78-140; the 2x2 inversion (mat2.invert) in FP64
+__device__ void dual_calc(DevDual &p, const JBody &A, float3 r1u, const JBody &B, float3 r2, float3 n1, float3 n2) {
+    double iem[4] = {0.0, 0.0, 0.0, 0.0};
+    p.r1xn1 = p.r1xn2 = p.r2xn1 = p.r2xn2 = p.i1n1 = p.i1n2 = p.i2n1 = p.i2n2 = f3(0.f, 0.f, 0.f);
+    if (A.motion == DYNAMIC) {
+        p.r1xn1 = cross3(r1u, n1);
+        p.r1xn2 = cross3(r1u, n2);
+        p.i1n1 = symmul(A.I, p.r1xn1);
+        p.i1n2 = symmul(A.I, p.r1xn2);
+        iem[0] += A.im + dot3(p.r1xn1, p.i1n1);
+        iem[1] += dot3(p.r1xn2, p.i1n1);
+        iem[2] += dot3(p.r1xn1, p.i1n2);
+        iem[3] += A.im + dot3(p.r1xn2, p.i1n2);
+    }
+    if (B.motion == DYNAMIC) {
+        p.r2xn1 = cross3(r2, n1);
+        p.r2xn2 = cross3(r2, n2);
+        p.i2n1 = symmul(B.I, p.r2xn1);
+        p.i2n2 = symmul(B.I, p.r2xn2);
+        iem[0] += B.im + dot3(p.r2xn1, p.i2n1);
+        iem[1] += dot3(p.r2xn2, p.i2n1);
+        iem[2] += dot3(p.r2xn1, p.i2n2);
+        iem[3] += B.im + dot3(p.r2xn2, p.i2n2);
+    }
+    double det = iem[0] * iem[3] - iem[2] * iem[1];
+    if (det == 0.0) {
+        dual_deactivate(p);
+        return;
+    }
+    det = 1.0 / det;
+    p.eff[0] = (float)(iem[3] * det);
+    p.eff[1] = (float)(-iem[1] * det);
+    p.eff[2] = (float)(-iem[2] * det);
+    p.eff[3] = (float)(iem[0] * det);
+}
+__device__ void dual_push(DevWorld &w, const DevDual &p, const JBody &A, const JBody &B, float3 n1, float3 n2, float l0,
+                          float l1) {
+    const float3 imp = n1 * l0 + n2 * l1;
+    if (A.motion == DYNAMIC) {
+        add_lin_locked(w, A.i, imp * (-A.im));
+        add_ang(w, A.i, -(p.i1n1 * l0 + p.i1n2 * l1));
+    }
+    if (B.motion == DYNAMIC) {
+        add_lin_locked(w, B.i, imp * B.im);
+        add_ang(w, B.i, p.i2n1 * l0 + p.i2n2 * l1);
+    }
+}
+__device__ void dual_warm(DevWorld &w, DevDual &p, const JBody &A, const JBody &B, float3 n1, float3 n2, float ratio) {
+    if (!dual_active(p)) return;
+    p.lambda[0] *= ratio;
+    p.lambda[1] *= ratio;
+    if (p.lambda[0] == 0.f && p.lambda[1] == 0.f) return;
+    dual_push(w, p, A, B, n1, n2, p.lambda[0], p.lambda[1]);
+}
+__device__ bool dual_solve_velocity(DevWorld &w, DevDual &p, const JBody &A, const JBody &B, float3 n1, float3 n2) {
+    if (!dual_active(p)) return false;
+    const bool mA = A.motion != STATIC, mB = B.motion != STATIC;
+    float j0 = 0.f, j1 = 0.f;
+    if (mA) {
+        const float3 v = xyz(w.linvel[A.i]), av = xyz(w.angvel[A.i]);
+        j0 += dot3(n1, v) + dot3(p.r1xn1, av);
+        j1 += dot3(n2, v) + dot3(p.r1xn2, av);
+    }
+    if (mB) {
+        const float3 v = xyz(w.linvel[B.i]), av = xyz(w.angvel[B.i]);
+        j0 -= dot3(n1, v) + dot3(p.r2xn1, av);
+        j1 -= dot3(n2, v) + dot3(p.r2xn2, av);
+    }
+    const float l0 = p.eff[0] * j0 + p.eff[2] * j1, l1 = p.eff[1] * j0 + p.eff[3] * j1;
+    p.lambda[0] += l0;
+    p.lambda[1] += l1;
+    if (l0 == 0.f && l1 == 0.f) return false;
+    dual_push(w, p, A, B, n1, n2, l0, l1);
+    return true;
+}
+__device__ bool dual_solve_position(DevWorld &w, const DevDual &p, const JBody &A, const JBody &B, float3 u, float3 n1,
+                                    float3 n2, float beta) {
+    if (!dual_active(p)) return false;
+    const float c0 = dot3(u, n1), c1 = dot3(u, n2);
+    if (c0 == 0.f && c1 == 0.f) return false;
+    const float l0 = -beta * (p.eff[0] * c0 + p.eff[2] * c1), l1 = -beta * (p.eff[1] * c0 + p.eff[3] * c1);
+    if (l0 == 0.f && l1 == 0.f) return false;
+    const float3 imp = n1 * l0 + n2 * l1;
+    if (A.motion == DYNAMIC) {
+        add_position_step(w, A.i, imp * (-A.im));
+        add_rotation(w, A.i, -(p.i1n1 * l0 + p.i1n2 * l1));
+    }
+    if (B.motion == DYNAMIC) {
+        add_position_step(w, B.i, imp * B.im);
+        add_rotation(w, B.i, p.i2n1 * l0 + p.i2n2 * l1);
+    }
+    return true;
+}
+
+// ---- point joint (point-constraint.ts:186-244) ---------------------------------------
+__device__ void pointj_setup(DevWorld &w, DevJoint &j) {
+    JBody A = jbody(w, j.h.a), B = jbody(w, j.h.b);
+    point_calc(j.pt, A, B, w.quat[j.h.a], w.quat[j.h.b], j.lp1, j.lp2);
+}
+__device__ bool pointj_solve_position(DevWorld &w, DevJoint &j) {
+    JBody A = jbody(w, j.h.a), B = jbody(w, j.h.b);
+    point_calc(j.pt, A, B, w.quat[j.h.a], w.quat[j.h.b], j.lp1, j.lp2);
+    return point_solve_position(w, j.pt, A, B, c_settings.baumgarte);
+}
+
+// ---- fixed joint (fixed-constraint.ts:299-395) ---------------------------------------
+__device__ void fixed_setup(DevWorld &w, DevJoint &j) {
+    JBody A = jbody(w, j.h.a), B = jbody(w, j.h.b);
+    euler_calc(j.rot, A, B);
+    point_calc(j.pt, A, B, w.quat[j.h.a], w.quat[j.h.b], j.lp1, j.lp2);
+}
+__device__ bool fixed_solve_position(DevWorld &w, DevJoint &j) {
+    const float beta = c_settings.baumgarte;
+    JBody A = jbody(w, j.h.a), B = jbody(w, j.h.b);
+    euler_calc(j.rot, A, B);
+    bool rot = euler_solve_position(w, j.rot, A, B, j.inv_initial, beta);
+    A = jbody(w, j.h.a);
+    B = jbody(w, j.h.b);
+    point_calc(j.pt, A, B, w.quat[j.h.a], w.quat[j.h.b], j.lp1, j.lp2);
+    bool pos = point_solve_position(w, j.pt, A, B, beta);
+    return rot || pos;
+}
+
+// ---- distance joint (distance-constraint.ts:270-465) ---------------------------------
+__device__ void distance_calc(DevWorld &w, DevJoint &j, const JBody &A, const JBody &B, float dt) {
+    const float3 ca = xyz(w.com[j.h.a]), cb = xyz(w.com[j.h.b]);
+    j.wp1 = qrot(w.quat[j.h.a], j.lp1) + ca;
+    j.wp2 = qrot(w.quat[j.h.b], j.lp2) + cb;
+    const float3 delta = j.wp2 - j.wp1;
+    const float dl = sqrtf(lensq3(delta));
+    if (dl > 0.f) j.wn = delta * (1.f / dl);
+    const float3 r1u = j.wp2 - ca, r2 = j.wp2 - cb;
+    const float INF = __int_as_float(0x7f800000);
+    float C;
+    if (j.min_dist == j.max_dist) {  // a rod: both directions
+        C = dl - j.min_dist;
+        j.min_lambda = -INF;
+        j.max_lambda = INF;
+    } else if (dl <= j.min_dist) {  // too close: push apart only
+        C = dl - j.min_dist;
+        j.min_lambda = 0.f;
+        j.max_lambda = INF;
+    } else if (dl >= j.max_dist) {  // too far: pull together only
+        C = dl - j.max_dist;
+        j.min_lambda = -INF;
+        j.max_lambda = 0.f;
+    } else {
+        axis_deactivate(j.ax);
+        return;
+    }
+    axis_calc_settings(j.ax, dt, A, B, r1u, r2, j.wn, 0.f, C, j.spring_mode, j.spring_freq, j.spring_damping);
+}
+__device__ bool distance_solve_position(DevWorld &w, DevJoint &j, float dt) {
+    if (j.spring_freq > 0.f) return false;
+    // the error on the world points of the last property calculation (setup, or the previous
+    // position iteration), then the properties are refreshed (solvePosition :420-458)
+    const float d = dot3(j.wp2 - j.wp1, j.wn);
+    float err = 0.f;
+    if (d < j.min_dist)
+        err = d - j.min_dist;
+    else if (d > j.max_dist)
+        err = d - j.max_dist;
+    if (err == 0.f) return false;
+    JBody A = jbody(w, j.h.a), B = jbody(w, j.h.b);
+    distance_calc(w, j, A, B, dt);
+    return axis_solve_position(w, j.ax, A, B, j.wn, err, c_settings.baumgarte);
+}
+
+// ---- cone joint (cone-constraint.ts:321-448) -----------------------------------------
+__device__ void cone_rot_calc(DevWorld &w, DevJoint &j, const JBody &A, const JBody &B) {
+    const float3 t1 = qrot(w.quat[j.h.a], j.lt1), t2 = qrot(w.quat[j.h.b], j.lt2);
+    j.cos_theta = dot3(t1, t2);
+    if (j.cos_theta < j.cos_half_cone) {
+        const float3 ra = cross3(t2, t1);
+        const float l = sqrtf(lensq3(ra));
+        if (l > 1e-6f) j.w_rot_axis = ra * (1.f / l);
+        angle_calc(j.ang, A, B, j.w_rot_axis, 0.f);
+    } else {
+        angle_deactivate(j.ang);
+    }
+}
+__device__ void cone_setup(DevWorld &w, DevJoint &j) {
+    JBody A = jbody(w, j.h.a), B = jbody(w, j.h.b);
+    point_calc(j.pt, A, B, w.quat[j.h.a], w.quat[j.h.b], j.lp1, j.lp2);
+    cone_rot_calc(w, j, A, B);
+}
+__device__ bool cone_solve_position(DevWorld &w, DevJoint &j) {
+    const float beta = c_settings.baumgarte;
+    JBody A = jbody(w, j.h.a), B = jbody(w, j.h.b);
+    point_calc(j.pt, A, B, w.quat[j.h.a], w.quat[j.h.b], j.lp1, j.lp2);
+    bool pos = point_solve_position(w, j.pt, A, B, beta);
+    A = jbody(w, j.h.a);
+    B = jbody(w, j.h.b);
+    cone_rot_calc(w, j, A, B);
+    bool rot = false;
+    if (j.ang.eff != 0.f) rot = angle_solve_position(w, j.ang, A, B, j.cos_theta - j.cos_half_cone, beta);
+    return pos || rot;
+}
+
+// ---- slider joint (slider-constraint.ts:546-1038) ------------------------------------
+enum : int { SL_LIMITS = 1 };
+__device__ void slider_r1r2u(DevWorld &w, DevJoint &j) {  // calculateR1R2U :546-562
+    j.r1 = qrot(w.quat[j.h.a], j.lp1);
+    j.r2 = qrot(w.quat[j.h.b], j.lp2);
+    j.u = xyz(w.com[j.h.b]) - xyz(w.com[j.h.a]) + j.r2 - j.r1;
+}
+__device__ void slider_axis_pos(DevWorld &w, DevJoint &j) {  // calculateSlidingAxisAndPosition :564-577
+    if ((j.slider_flags & SL_LIMITS) || j.motor_state != 0 || j.max_friction_force > 0.f) {
+        j.ws = qrot(w.quat[j.h.a], j.ls1);
+        j.d = dot3(j.u, j.ws);
+    }
+}
+__device__ void slider_pos_calc(DevWorld &w, DevJoint &j, const JBody &A, const JBody &B) {  // :579-609
+    const float4 qa = w.quat[j.h.a];
+    j.n1 = qrot(qa, j.ln1);
+    j.n2 = qrot(qa, j.ln2);
+    dual_calc(j.dual, A, j.r1 + j.u, B, j.r2, j.n1, j.n2);
+}
+__device__ void slider_limits_calc(DevJoint &j, const JBody &A, const JBody &B, float dt) {  // :611-696
+    if (!(j.slider_flags & SL_LIMITS)) {
+        axis_deactivate(j.ax);
+        return;
+    }
+    const bool below = j.d <= j.limits_min, above = j.d >= j.limits_max;
+    if (below || above) {
+        const float err = below ? j.d - j.limits_min : j.d - j.limits_max;
+        if (j.limits_freq > 0.f)
+            axis_calc_settings(j.ax, dt, A, B, j.r1 + j.u, j.r2, j.ws, 0.f, err, j.limits_spring_mode, j.limits_freq,
+                               j.limits_damping);
+        else
+            axis_calc(j.ax, A, B, j.r1 + j.u, j.r2, j.ws, 0.f);
+    } else {
+        axis_deactivate(j.ax);
+    }
+}
+__device__ void slider_motor_calc(DevJoint &j, const JBody &A, const JBody &B, float dt) {  // :698-785
+    const float3 r1u = j.r1 + j.u;
+    if (j.motor_state == 0) {
+        if (j.max_friction_force > 0.f)
+            axis_calc(j.motor, A, B, r1u, j.r2, j.ws, 0.f);
+        else
+            axis_deactivate(j.motor);
+    } else if (j.motor_state == 1) {
+        axis_calc(j.motor, A, B, r1u, j.r2, j.ws, -j.target_velocity);
+    } else if (j.motor_freq > 0.f) {
+        axis_calc_settings(j.motor, dt, A, B, r1u, j.r2, j.ws, 0.f, j.d - j.target_position, j.motor_spring_mode,
+                           j.motor_freq, j.motor_damping);
+    } else {
+        axis_deactivate(j.motor);
+    }
+}
+__device__ void slider_setup(DevWorld &w, DevJoint &j, float dt) {  // setupVelocity :787-827
+    JBody A = jbody(w, j.h.a), B = jbody(w, j.h.b);
+    slider_r1r2u(w, j);
+    slider_pos_calc(w, j, A, B);
+    euler_calc(j.rot, A, B);
+    slider_axis_pos(w, j);
+    slider_limits_calc(j, A, B, dt);
+    slider_motor_calc(j, A, B, dt);
+}
+__device__ void slider_warm(DevWorld &w, DevJoint &j, const JBody &A, const JBody &B, float ratio) {  // :829-877
+    if (j.motor.eff != 0.f) axis_warm(w, j.motor, A, B, j.ws, ratio);
+    dual_warm(w, j.dual, A, B, j.n1, j.n2, ratio);
+    euler_warm(w, j.rot, A, B, ratio);
+    if (j.ax.eff != 0.f) axis_warm(w, j.ax, A, B, j.ws, ratio);
+}
+__device__ bool slider_solve_velocity(DevWorld &w, DevJoint &j, const JBody &A, const JBody &B, float dt) {  // :879-958
+    const float INF = __int_as_float(0x7f800000);
+    bool motor = false, limit = false;
+    if (j.motor.eff != 0.f) {
+        if (j.motor_state == 0) {
+            const float ml = j.max_friction_force * dt;
+            motor = axis_solve_velocity(w, j.motor, A, B, j.ws, -ml, ml);
+        } else {
+            motor = axis_solve_velocity(w, j.motor, A, B, j.ws, dt * j.min_force, dt * j.max_force);
+        }
+    }
+    bool pos = dual_solve_velocity(w, j.dual, A, B, j.n1, j.n2);
+    bool rot = euler_solve_velocity(w, j.rot, A, B);
+    if (j.ax.eff != 0.f) {
+        float mn, mx;
+        if (j.limits_min == j.limits_max) {
+            mn = -INF;
+            mx = INF;
+        } else if (j.d <= j.limits_min) {
+            mn = 0.f;
+            mx = INF;
+        } else {
+            mn = -INF;
+            mx = 0.f;
+        }
+        limit = axis_solve_velocity(w, j.ax, A, B, j.ws, mn, mx);
+    }
+    return motor || pos || rot || limit;
+}
+__device__ bool slider_solve_position(DevWorld &w, DevJoint &j, float dt) {  // :960-1038
+    const float beta = c_settings.baumgarte;
+    JBody A = jbody(w, j.h.a), B = jbody(w, j.h.b);
+    slider_r1r2u(w, j);
+    slider_pos_calc(w, j, A, B);
+    bool pos = dual_solve_position(w, j.dual, A, B, j.u, j.n1, j.n2, beta);
+    A = jbody(w, j.h.a);
+    B = jbody(w, j.h.b);
+    euler_calc(j.rot, A, B);
+    bool rot = euler_solve_position(w, j.rot, A, B, j.inv_initial, beta);
+    bool limit = false;
+    if ((j.slider_flags & SL_LIMITS) && !(j.limits_freq > 0.f)) {
+        A = jbody(w, j.h.a);
+        B = jbody(w, j.h.b);
+        slider_r1r2u(w, j);
+        slider_axis_pos(w, j);
+        slider_limits_calc(j, A, B, dt);
+        if (j.ax.eff != 0.f) {
+            const float err = j.d <= j.limits_min ? j.d - j.limits_min : j.d - j.limits_max;
+            limit = axis_solve_position(w, j.ax, A, B, j.ws, err, beta);
+        }
+    }
+    return pos || rot || limit;
+}
+
+// ---- the joints of one record (point, distance, fixed, cone, slider) -----------------
+__device__ void other_setup(DevWorld &w, DevJoint &j, float dt) {
+    switch (j.type) {
+    case JT_POINT: pointj_setup(w, j); break;
+    case JT_DISTANCE: {
+        JBody A = jbody(w, j.h.a), B = jbody(w, j.h.b);
+        distance_calc(w, j, A, B, dt);
+        break;
+    }
+    case JT_FIXED: fixed_setup(w, j); break;
+    case JT_CONE: cone_setup(w, j); break;
+    case JT_SLIDER: slider_setup(w, j, dt); break;
+    }
+}
+__device__ void other_warm(DevWorld &w, DevJoint &j, float ratio) {
+    JBody A = jbody(w, j.h.a, false), B = jbody(w, j.h.b, false);
+    switch (j.type) {
+    case JT_POINT: point_warm(w, j.pt, A, B, ratio); break;
+    case JT_DISTANCE: axis_warm(w, j.ax, A, B, j.wn, ratio); break;
+    case JT_FIXED:
+        euler_warm(w, j.rot, A, B, ratio);
+        point_warm(w, j.pt, A, B, ratio);
+        break;
+    case JT_CONE:
+        point_warm(w, j.pt, A, B, ratio);
+        if (j.ang.eff != 0.f) angle_warm(w, j.ang, A, B, ratio);
+        break;
+    case JT_SLIDER: slider_warm(w, j, A, B, ratio); break;
+    }
+}
+__device__ bool other_solve_velocity(DevWorld &w, DevJoint &j, float dt) {
+    JBody A = jbody(w, j.h.a, false), B = jbody(w, j.h.b, false);
+    switch (j.type) {
+    case JT_POINT: return point_solve_velocity(w, j.pt, A, B);
+    case JT_DISTANCE:
+        return j.ax.eff != 0.f && axis_solve_velocity(w, j.ax, A, B, j.wn, j.min_lambda, j.max_lambda);
+    case JT_FIXED: {
+        bool rot = euler_solve_velocity(w, j.rot, A, B);
+        bool pos = point_solve_velocity(w, j.pt, A, B);
+        return rot || pos;
+    }
+    case JT_CONE: {
+        const float INF = __int_as_float(0x7f800000);
+        bool pos = point_solve_velocity(w, j.pt, A, B);
+        bool rot = j.ang.eff != 0.f && angle_solve_velocity(w, j.ang, A, B, j.w_rot_axis, 0.f, INF);
+        return pos || rot;
+    }
+    case JT_SLIDER: return slider_solve_velocity(w, j, A, B, dt);
+    }
+    return false;
+}
+__device__ bool other_solve_position(DevWorld &w, DevJoint &j, float dt) {
+    switch (j.type) {
+    case JT_POINT: return pointj_solve_position(w, j);
+    case JT_DISTANCE: return distance_solve_position(w, j, dt);
+    case JT_FIXED: return fixed_solve_position(w, j);
+    case JT_CONE: return cone_solve_position(w, j);
+    case JT_SLIDER: return slider_solve_position(w, j, dt);
+    }
+    return false;
+}
+
 // ---- dispatch on the joint id (the id helpers are in cc_internal.cuh) ------------------
 __device__ void joint_setup(DevWorld &w, int id, float dt) {
-    if (id & JOINT_SWING)
-        swing_setup(w, w.swings[id & ~JOINT_SWING], dt);
+    const int t = joint_type_of(id), i = joint_index_of(id);
+    if (t == JT_SWING)
+        swing_setup(w, w.swings[i], dt);
+    else if (t == JT_HINGE)
+        hinge_setup(w, w.hinges[i], dt);
     else
-        hinge_setup(w, w.hinges[id], dt);
+        other_setup(w, other_joint(w, id), dt);
 }
 __device__ void joint_warm(DevWorld &w, int id, float ratio) {
-    if (id & JOINT_SWING)
-        swing_warm(w, w.swings[id & ~JOINT_SWING], ratio);
+    const int t = joint_type_of(id), i = joint_index_of(id);
+    if (t == JT_SWING)
+        swing_warm(w, w.swings[i], ratio);
+    else if (t == JT_HINGE)
+        hinge_warm(w, w.hinges[i], ratio);
     else
-        hinge_warm(w, w.hinges[id], ratio);
+        other_warm(w, other_joint(w, id), ratio);
 }
 __device__ bool joint_solve_velocity(DevWorld &w, int id, float dt) {
-    return id & JOINT_SWING ? swing_solve_velocity(w, w.swings[id & ~JOINT_SWING], dt)
-                            : hinge_solve_velocity(w, w.hinges[id], dt);
+    const int t = joint_type_of(id), i = joint_index_of(id);
+    if (t == JT_SWING) return swing_solve_velocity(w, w.swings[i], dt);
+    if (t == JT_HINGE) return hinge_solve_velocity(w, w.hinges[i], dt);
+    return other_solve_velocity(w, other_joint(w, id), dt);
 }
 __device__ bool joint_solve_position(DevWorld &w, int id, float dt) {
-    return id & JOINT_SWING ? swing_solve_position(w, w.swings[id & ~JOINT_SWING])
-                            : hinge_solve_position(w, w.hinges[id], dt);
+    const int t = joint_type_of(id), i = joint_index_of(id);
+    if (t == JT_SWING) return swing_solve_position(w, w.swings[i]);
+    if (t == JT_HINGE) return hinge_solve_position(w, w.hinges[i], dt);
+    return other_solve_position(w, other_joint(w, id), dt);
 }

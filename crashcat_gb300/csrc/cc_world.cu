@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
 #include <new>
 #include <vector>
 
@@ -37,6 +38,7 @@ struct cc_world {
     std::vector<uint64_t> ids;
     std::vector<DevHinge> hinges;  // host copy of each joint as created (bodies, flags, limits, motors)
     std::vector<DevSwing> swings;
+    std::vector<DevJoint> others;  // point, distance, fixed, cone, slider joints by (type, index)
     std::vector<cc_hull::Hull> hulls;  // convex hull shapes as built
     std::vector<cc_mesh::Mesh> meshes;  // triangle meshes as built
     bool hulls_dirty = false, meshes_dirty = false;  // added since the last upload
@@ -69,7 +71,7 @@ struct cc_world {
     struct TuneSnapshot {
         bool ready = false;
         Checkpoint c{};
-        char *joints = nullptr;  // hinges then swing-twists
+        char *joints = nullptr;  // hinges, swing-twists, then the other joint records
         size_t joint_bytes = 0;
         float2 *ccd = nullptr;
         std::vector<void *> allocs;
@@ -536,7 +538,7 @@ int cc_world_destroy(cc_world *W) {
                     w.cache_recs[1], w.cache_parity, w.root_flag, w.small_list, w.large_list, w.scratch_order,
                     w.scratch_colour, w.scratch_claim, w.mid_list, w.body_local, w.contact_event,
                     w.removed_keys, W->d_state_rows, w.hinges, w.island_joints, w.island_joint_count,
-                    w.island_joint_off, w.island_fill_j, w.joint_wake, w.joint_partners, w.swings,
+                    w.island_joint_off, w.island_fill_j, w.joint_wake, w.joint_partners, w.swings, w.others,
                     w.giant_list, w.giant_claim, w.giant_count, w.small_joint_list, w.large_joint_list,
                     w.hulls, w.hull_points, w.hull_shrunk,
                     w.hull_planes, w.hull_faces, w.hull_vidx, w.ccd_flag, w.ccd_slot, w.ccd_index, w.ccd,
@@ -1456,7 +1458,8 @@ extern "C" int cc_world_rollout_grad(cc_world *W, float dt, int32_t n_steps, int
     DevWorld &w = W->w;
     if (w.n == 0) return CC_ERR_INVALID;
     // the adjoint covers contacts and the discrete integration only
-    if (w.num_hinges + w.num_swings > 0 || w.num_linear_cast > 0 || W->any_iter_override) return CC_ERR_UNSUPPORTED;
+    if (w.num_hinges + w.num_swings + w.num_others > 0 || w.num_linear_cast > 0 || W->any_iter_override)
+        return CC_ERR_UNSUPPORTED;
     int K = checkpoint_every < n_steps ? checkpoint_every : n_steps;
     int nseg = (n_steps + K - 1) / K;
     int r = ensure_adjoint(W, K, nseg + 1);
@@ -1585,7 +1588,8 @@ static int tune_snapshot(cc_world *W, bool save) {
         T.ready = true;
     }
     // joint records carry their accumulated impulses from step to step
-    size_t jb = sizeof(DevHinge) * (size_t)w.num_hinges + sizeof(DevSwing) * (size_t)w.num_swings;
+    size_t jb = sizeof(DevHinge) * (size_t)w.num_hinges + sizeof(DevSwing) * (size_t)w.num_swings +
+                sizeof(DevJoint) * (size_t)w.num_others;
     if (save && jb > T.joint_bytes) {
         if (T.joints) cudaFree(T.joints);
         T.joints = nullptr;
@@ -1604,6 +1608,10 @@ static int tune_snapshot(cc_world *W, bool save) {
     if (sb)
         CC_TRY(cudaMemcpyAsync(save ? (void *)(T.joints + hb) : (void *)w.swings,
                                save ? (void *)w.swings : (void *)(T.joints + hb), sb, cudaMemcpyDeviceToDevice, s));
+    size_t ob = sizeof(DevJoint) * (size_t)w.num_others;
+    if (ob)
+        CC_TRY(cudaMemcpyAsync(save ? (void *)(T.joints + hb + sb) : (void *)w.others,
+                               save ? (void *)w.others : (void *)(T.joints + hb + sb), ob, cudaMemcpyDeviceToDevice, s));
     if (w.ccd_lambda && T.ccd)
         CC_TRY(cudaMemcpyAsync(save ? (void *)T.ccd : (void *)w.ccd_lambda, save ? (void *)w.ccd_lambda : (void *)T.ccd,
                                sizeof(float2) * (size_t)w.num_worlds, cudaMemcpyDeviceToDevice, s));
@@ -1782,7 +1790,7 @@ static int grow_joints(cc_world *W, T *&arr, int count, int &cap_io, int need) {
     cap_io = cap;
     return CC_OK;
 }
-static int ensure_joint_capacity(cc_world *W, int need_hinges, int need_swings) {
+static int ensure_joint_capacity(cc_world *W, int need_hinges, int need_swings, int need_others = -1) {
     DevWorld &w = W->w;
     int r;
     if (!w.island_joint_count) {
@@ -1795,7 +1803,8 @@ static int ensure_joint_capacity(cc_world *W, int need_hinges, int need_swings) 
     }
     if ((r = grow_joints(W, w.hinges, w.num_hinges, w.max_hinges, need_hinges)) != CC_OK) return r;
     if ((r = grow_joints(W, w.swings, w.num_swings, w.max_swings, need_swings)) != CC_OK) return r;
-    int need_lists = w.max_hinges + w.max_swings;
+    if (need_others >= 0 && (r = grow_joints(W, w.others, w.num_others, w.max_others, need_others)) != CC_OK) return r;
+    int need_lists = w.max_hinges + w.max_swings + w.max_others;
     if (need_lists > w.max_joints) {
         int *nl = nullptr;
         if ((r = dalloc(&nl, 5 * (size_t)need_lists)) != CC_OK) return r;
@@ -1832,6 +1841,7 @@ static int upload_partners(cc_world *W) {
     };
     for (const DevHinge &j : W->hinges) add_joint(j.h);
     for (const DevSwing &j : W->swings) add_joint(j.h);
+    for (const DevJoint &j : W->others) add_joint(j.h);
     CC_TRY(cudaStreamSynchronize(W->stream));
     CC_TRY(cudaMemcpy(w.joint_partners, part.data(), sizeof(int) * part.size(), cudaMemcpyHostToDevice));
     return over && w.skip_joint_pairs ? CC_ERR_CAPACITY : CC_OK;
@@ -1931,6 +1941,7 @@ int cc_world_add_hinges(cc_world *W, const cc_hinge_desc *d, int32_t n, int32_t 
         if (out_index) out_index[i] = w.num_hinges + i;
     }
     w.num_hinges += n;
+    w.type_count[JT_HINGE] = w.num_hinges;
     drop_graph(W);
     return upload_partners(W);
 }
@@ -2139,6 +2150,7 @@ int cc_world_add_swing_twists(cc_world *W, const cc_swing_twist_desc *d, int32_t
         if (out_index) out_index[i] = w.num_swings + i;
     }
     w.num_swings += n;
+    w.type_count[JT_SWING] = w.num_swings;
     drop_graph(W);
     return upload_partners(W);
 }
@@ -2502,3 +2514,436 @@ static int export_hull(const cc_hull::Hull &h, cc_hull_info *info, float *points
         for (size_t k = 0; k < h.vidx.size(); k++) face_vertices[k] = h.vidx[k];
     return CC_OK;
 }
+
+// ---------------------------------------------------------------------------
+// point, distance, fixed, cone and slider joints: created in FP64 from the bodies' current
+// poses (the create functions of point-, distance-, fixed-, cone- and slider-constraint.ts)
+// into one record type, DevJoint, kept sorted by (type, per-type index)
+// ---------------------------------------------------------------------------
+namespace {
+struct BodyPoses {
+    std::vector<float4> quat, com, inv;  // inv.w: inverse mass
+    std::vector<int> world;
+};
+int read_poses(cc_world *W, BodyPoses &p) {
+    DevWorld &w = W->w;
+    p.quat.resize((size_t)w.n);
+    p.com.resize((size_t)w.n);
+    p.inv.resize((size_t)w.n);
+    p.world.resize((size_t)w.n);
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    CC_TRY(cudaMemcpy(p.quat.data(), w.quat, sizeof(float4) * w.n, cudaMemcpyDeviceToHost));
+    CC_TRY(cudaMemcpy(p.com.data(), w.com, sizeof(float4) * w.n, cudaMemcpyDeviceToHost));
+    CC_TRY(cudaMemcpy(p.inv.data(), w.inv_inertia, sizeof(float4) * w.n, cudaMemcpyDeviceToHost));
+    CC_TRY(cudaMemcpy(p.world.data(), w.world, sizeof(int) * w.n, cudaMemcpyDeviceToHost));
+    return CC_OK;
+}
+// the fields every joint description carries
+template <typename D>
+bool common_ok(const DevWorld &w, const D &d) {
+    return d.body_a >= 0 && d.body_b >= 0 && d.body_a < w.n && d.body_b < w.n &&
+           (d.space == CC_SPACE_WORLD || d.space == CC_SPACE_LOCAL) && d.num_velocity_steps_override >= 0 &&
+           d.num_velocity_steps_override <= 255 && d.num_position_steps_override >= 0 &&
+           d.num_position_steps_override <= 255 && finite3(d.point_a) && finite3(d.point_b);
+}
+template <typename D>
+DevJoint joint_record(cc_world *W, const D &d, int type, int index) {
+    DevJoint j;
+    memset(&j, 0, sizeof(j));
+    j.type = type;
+    j.h.a = d.body_a;
+    j.h.b = d.body_b;
+    j.h.index = index;
+    j.h.priority = d.priority;
+    j.h.island = -1;
+    j.h.flags = d.enabled ? JF_ENABLED : 0;
+    j.h.iter_ovr = (int)((uint32_t)d.num_velocity_steps_override | ((uint32_t)d.num_position_steps_override << 8));
+    if (j.h.iter_ovr) W->any_iter_override = true;
+    j.inv_initial = make_float4(0.f, 0.f, 0.f, 1.f);
+    j.wn = make_float3(0.f, 1.f, 0.f);
+    return j;
+}
+// attachment points from the centres of mass in body space (world-space input taken against
+// the current poses), or the inverse-mass-weighted anchor of autoDetectPoint
+void attach(DevJoint &j, const BodyPoses &p, const float *pa, const float *pb, int space, bool auto_detect) {
+    const int a = j.h.a, b = j.h.b;
+    if (space == CC_SPACE_WORLD) {
+        DQ iqa = dconj(dq(p.quat[a])), iqb = dconj(dq(p.quat[b]));
+        D3 ca = d3(p.com[a]), cb = d3(p.com[b]);
+        D3 wa = d3(pa), wb = d3(pb);
+        if (auto_detect) {
+            double ima = p.inv[a].w, imb = p.inv[b].w, im = ima + imb;
+            D3 anchor = ca;
+            if (im > 0) anchor = {ca.x * (ima / im) + cb.x * (imb / im), ca.y * (ima / im) + cb.y * (imb / im),
+                                  ca.z * (ima / im) + cb.z * (imb / im)};
+            wa = wb = anchor;
+        }
+        j.lp1 = f3d(drot(iqa, dsub(wa, ca)));
+        j.lp2 = f3d(drot(iqb, dsub(wb, cb)));
+    } else {
+        j.lp1 = f3d(d3(pa));
+        j.lp2 = f3d(d3(pb));
+    }
+}
+// mathcat's (gl-matrix's) approximate vec3.equals: |a - b| <= 1e-6 max(1, |a|, |b|) per component
+bool dequals(D3 a, D3 b) {
+    auto eq = [](double x, double y) {
+        return std::fabs(x - y) <= 1e-6 * std::max(1.0, std::max(std::fabs(x), std::fabs(y)));
+    };
+    return eq(a.x, b.x) && eq(a.y, b.y) && eq(a.z, b.z);
+}
+float4 f4q(DQ q) { return make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w); }
+}  // namespace
+
+// insert new records of one type after the existing ones of that type, keeping the device
+// records' accumulated impulses
+static int add_other_joints(cc_world *W, int type, const std::vector<DevJoint> &made, int32_t *out_index) {
+    DevWorld &w = W->w;
+    const int n = (int)made.size();
+    int r = ensure_joint_capacity(W, w.num_hinges, w.num_swings, w.num_others + n);
+    if (r != CC_OK) return r;
+    if (w.num_others > 0) {
+        CC_TRY(cudaStreamSynchronize(W->stream));
+        CC_TRY(cudaMemcpy(W->others.data(), w.others, sizeof(DevJoint) * w.num_others, cudaMemcpyDeviceToHost));
+    }
+    auto pos = std::upper_bound(W->others.begin(), W->others.end(), type,
+                                [](int t, const DevJoint &j) { return t < j.type; });
+    W->others.insert(pos, made.begin(), made.end());
+    for (int i = 0; i < n; i++)
+        if (out_index) out_index[i] = made[i].h.index;
+    w.num_others += n;
+    for (int t = 0; t < JT_TYPES; t++) {
+        if (t == JT_HINGE || t == JT_SWING) continue;
+        w.type_count[t] = 0;
+        w.type_first[t] = 0;
+    }
+    for (int k = w.num_others - 1; k >= 0; k--) {
+        w.type_first[W->others[k].type] = k;
+        w.type_count[W->others[k].type]++;
+    }
+    CC_TRY(cudaMemcpy(w.others, W->others.data(), sizeof(DevJoint) * w.num_others, cudaMemcpyHostToDevice));
+    drop_graph(W);
+    return upload_partners(W);
+}
+template <typename F>
+static int edit_other(cc_world *W, int type, int32_t index, F f) {
+    DevWorld &w = W->w;
+    if (type < 0 || type >= JT_TYPES || type == JT_HINGE || type == JT_SWING) return CC_ERR_INVALID;
+    if (index < 0 || index >= w.type_count[type]) return CC_ERR_INVALID;
+    return edit_joint(W, w.others, W->others, w.num_others, w.type_first[type] + index, f);
+}
+
+extern "C" {
+
+int cc_world_add_point_joints(cc_world *W, const cc_point_desc *d, int32_t n, int32_t *out_index) {
+    if (!W || (!d && n > 0) || n < 0) return CC_ERR_INVALID;
+    if (n == 0) return CC_OK;
+    DevWorld &w = W->w;
+    for (int i = 0; i < n; i++)
+        if (!common_ok(w, d[i])) return CC_ERR_INVALID;
+    BodyPoses p;
+    if (int r = read_poses(W, p)) return r;
+    std::vector<DevJoint> made;
+    for (int i = 0; i < n; i++) {
+        if (p.world[d[i].body_a] != p.world[d[i].body_b]) return CC_ERR_INVALID;
+        DevJoint j = joint_record(W, d[i], JT_POINT, w.type_count[JT_POINT] + i);
+        attach(j, p, d[i].point_a, d[i].point_b, d[i].space, false);
+        made.push_back(j);
+    }
+    return add_other_joints(W, JT_POINT, made, out_index);
+}
+
+int cc_world_add_distance_joints(cc_world *W, const cc_distance_desc *d, int32_t n, int32_t *out_index) {
+    if (!W || (!d && n > 0) || n < 0) return CC_ERR_INVALID;
+    if (n == 0) return CC_OK;
+    DevWorld &w = W->w;
+    for (int i = 0; i < n; i++)
+        if (!common_ok(w, d[i]) || !spring_ok(d[i].spring) || std::isnan(d[i].min_distance) ||
+            std::isnan(d[i].max_distance))
+            return CC_ERR_INVALID;
+    BodyPoses p;
+    if (int r = read_poses(W, p)) return r;
+    std::vector<DevJoint> made;
+    for (int i = 0; i < n; i++) {
+        const cc_distance_desc &h = d[i];
+        if (p.world[h.body_a] != p.world[h.body_b]) return CC_ERR_INVALID;
+        DevJoint j = joint_record(W, h, JT_DISTANCE, w.type_count[JT_DISTANCE] + i);
+        attach(j, p, h.point_a, h.point_b, h.space, false);
+        // the current distance of the attachment points (distance-constraint.ts:166-181)
+        D3 wp1, wp2;
+        if (h.space == CC_SPACE_WORLD) {
+            wp1 = d3(h.point_a);
+            wp2 = d3(h.point_b);
+        } else {
+            D3 r1 = drot(dq(p.quat[h.body_a]), d3(h.point_a)), r2 = drot(dq(p.quat[h.body_b]), d3(h.point_b));
+            D3 ca = d3(p.com[h.body_a]), cb = d3(p.com[h.body_b]);
+            wp1 = {r1.x + ca.x, r1.y + ca.y, r1.z + ca.z};
+            wp2 = {r2.x + cb.x, r2.y + cb.y, r2.z + cb.z};
+        }
+        D3 dd = dsub(wp2, wp1);
+        double dist = std::sqrt(dd.x * dd.x + dd.y * dd.y + dd.z * dd.z);
+        double mn = h.min_distance, mx = h.max_distance;
+        if (mn < 0 && mx < 0) {
+            mn = mx = dist;
+        } else {
+            double m0 = mn < 0 ? std::min(dist, mx) : mn, m1 = mx < 0 ? std::max(dist, mn) : mx;
+            mn = m0;
+            mx = m1;
+        }
+        j.min_dist = (float)mn;
+        j.max_dist = (float)mx;
+        j.spring_mode = h.spring.mode;
+        j.spring_freq = h.spring.frequency_or_stiffness;
+        j.spring_damping = h.spring.damping;
+        j.wp1 = f3d(wp1);
+        j.wp2 = f3d(wp2);
+        made.push_back(j);
+    }
+    return add_other_joints(W, JT_DISTANCE, made, out_index);
+}
+
+int cc_world_set_distance(cc_world *W, int32_t index, float min_distance, float max_distance) {
+    if (!W || std::isnan(min_distance) || std::isnan(max_distance)) return CC_ERR_INVALID;
+    return edit_other(W, JT_DISTANCE, index, [&](DevJoint &j) {  // setDistance :484-493
+        if (min_distance >= 0) j.min_dist = min_distance;
+        if (max_distance >= 0) j.max_dist = max_distance;
+        if (j.min_dist > j.max_dist) j.min_dist = j.max_dist = (j.min_dist + j.max_dist) / 2;
+    });
+}
+
+int cc_world_add_fixed_joints(cc_world *W, const cc_fixed_desc *d, int32_t n, int32_t *out_index) {
+    if (!W || (!d && n > 0) || n < 0) return CC_ERR_INVALID;
+    if (n == 0) return CC_OK;
+    DevWorld &w = W->w;
+    for (int i = 0; i < n; i++)
+        if (!common_ok(w, d[i]) || !finite3(d[i].axis_x_a) || !finite3(d[i].axis_y_a) || !finite3(d[i].axis_x_b) ||
+            !finite3(d[i].axis_y_b))
+            return CC_ERR_INVALID;
+    BodyPoses p;
+    if (int r = read_poses(W, p)) return r;
+    std::vector<DevJoint> made;
+    for (int i = 0; i < n; i++) {
+        const cc_fixed_desc &h = d[i];
+        if (p.world[h.body_a] != p.world[h.body_b]) return CC_ERR_INVALID;
+        DevJoint j = joint_record(W, h, JT_FIXED, w.type_count[JT_FIXED] + i);
+        attach(j, p, h.point_a, h.point_b, h.space, h.auto_detect_point != 0);
+        // getInvInitialOrientationXY (rotation-euler-constraint-part.ts:71-111)
+        D3 x1 = dnormalize(d3(h.axis_x_a)), y1 = dnormalize(d3(h.axis_y_a));
+        D3 x2 = dnormalize(d3(h.axis_x_b)), y2 = dnormalize(d3(h.axis_y_b));
+        DQ r0{0, 0, 0, 1};
+        if (!(dequals(x1, x2) && dequals(y1, y2)))
+            r0 = dqmul(quat_from_columns(x2, y2, dcross(x2, y2)), dconj(quat_from_columns(x1, y1, dcross(x1, y1))));
+        if (h.space == CC_SPACE_WORLD)
+            j.inv_initial = f4q(dqmul(dqmul(dconj(dq(p.quat[h.body_b])), r0), dq(p.quat[h.body_a])));
+        else
+            j.inv_initial = f4q(r0);
+        made.push_back(j);
+    }
+    return add_other_joints(W, JT_FIXED, made, out_index);
+}
+
+int cc_world_add_cone_joints(cc_world *W, const cc_cone_desc *d, int32_t n, int32_t *out_index) {
+    if (!W || (!d && n > 0) || n < 0) return CC_ERR_INVALID;
+    if (n == 0) return CC_OK;
+    DevWorld &w = W->w;
+    for (int i = 0; i < n; i++)
+        if (!common_ok(w, d[i]) || !finite3(d[i].twist_axis_a) || !finite3(d[i].twist_axis_b) ||
+            !std::isfinite(d[i].half_cone_angle))
+            return CC_ERR_INVALID;
+    BodyPoses p;
+    if (int r = read_poses(W, p)) return r;
+    std::vector<DevJoint> made;
+    for (int i = 0; i < n; i++) {
+        const cc_cone_desc &h = d[i];
+        if (p.world[h.body_a] != p.world[h.body_b]) return CC_ERR_INVALID;
+        DevJoint j = joint_record(W, h, JT_CONE, w.type_count[JT_CONE] + i);
+        attach(j, p, h.point_a, h.point_b, h.space, false);
+        D3 t1 = dnormalize(d3(h.twist_axis_a)), t2 = dnormalize(d3(h.twist_axis_b));
+        j.cos_half_cone = (float)std::cos((double)h.half_cone_angle);
+        // getNormalizedPerpendicular (cone-constraint.ts:118-136): the fallback limit axis
+        double ax = std::fabs(t1.x), ay = std::fabs(t1.y), az = std::fabs(t1.z);
+        D3 perp = (ax <= ay && ax <= az) ? D3{0, -t1.z, t1.y} : (ay <= az ? D3{t1.z, 0, -t1.x} : D3{-t1.y, t1.x, 0});
+        perp = dnormalize(perp);
+        if (h.space == CC_SPACE_WORLD) {
+            j.lt1 = f3d(drot(dconj(dq(p.quat[h.body_a])), t1));
+            j.lt2 = f3d(drot(dconj(dq(p.quat[h.body_b])), t2));
+            j.w_rot_axis = f3d(perp);
+        } else {
+            j.lt1 = f3d(t1);
+            j.lt2 = f3d(t2);
+            j.w_rot_axis = f3d(drot(dq(p.quat[h.body_a]), perp));
+        }
+        j.cos_theta = 1.f;
+        made.push_back(j);
+    }
+    return add_other_joints(W, JT_CONE, made, out_index);
+}
+
+int cc_world_set_cone_half_angle(cc_world *W, int32_t index, float half_cone_angle) {
+    if (!W || std::isnan(half_cone_angle)) return CC_ERR_INVALID;
+    const double PI = 3.14159265358979323846;
+    return edit_other(W, JT_CONE, index, [&](DevJoint &j) {  // setHalfConeAngle :262-264
+        j.cos_half_cone = (float)std::cos(std::max(0.0, std::min(PI, (double)half_cone_angle)));
+    });
+}
+
+int cc_world_add_slider_joints(cc_world *W, const cc_slider_desc *d, int32_t n, int32_t *out_index) {
+    if (!W || (!d && n > 0) || n < 0) return CC_ERR_INVALID;
+    if (n == 0) return CC_OK;
+    DevWorld &w = W->w;
+    for (int i = 0; i < n; i++) {
+        const cc_slider_desc &h = d[i];
+        if (!common_ok(w, h) || !finite3(h.slider_axis_a) || !finite3(h.slider_axis_b) || !finite3(h.normal_axis_a) ||
+            !finite3(h.normal_axis_b) || !spring_ok(h.limits_spring) || !spring_ok(h.motor_spring) ||
+            std::isnan(h.limits_min) || std::isnan(h.limits_max) || std::isnan(h.max_friction_force) ||
+            std::isnan(h.min_force_limit) || std::isnan(h.max_force_limit) || h.motor_state < 0 || h.motor_state > 2 ||
+            !std::isfinite(h.target_velocity) || !std::isfinite(h.target_position))
+            return CC_ERR_INVALID;
+    }
+    BodyPoses p;
+    if (int r = read_poses(W, p)) return r;
+    std::vector<DevJoint> made;
+    for (int i = 0; i < n; i++) {
+        const cc_slider_desc &h = d[i];
+        if (p.world[h.body_a] != p.world[h.body_b]) return CC_ERR_INVALID;
+        DevJoint j = joint_record(W, h, JT_SLIDER, w.type_count[JT_SLIDER] + i);
+        attach(j, p, h.point_a, h.point_b, h.space, h.auto_detect_point != 0);
+        D3 s1 = dnormalize(d3(h.slider_axis_a)), s2 = dnormalize(d3(h.slider_axis_b));
+        D3 n1 = dnormalize(d3(h.normal_axis_a)), n2 = dnormalize(d3(h.normal_axis_b));
+        // getInvInitialOrientationXY (slider-constraint.ts:203-259)
+        const double eps = 1e-6;
+        DQ r0{0, 0, 0, 1};
+        if (!(std::fabs(s1.x - s2.x) < eps && std::fabs(s1.y - s2.y) < eps && std::fabs(s1.z - s2.z) < eps &&
+              std::fabs(n1.x - n2.x) < eps && std::fabs(n1.y - n2.y) < eps && std::fabs(n1.z - n2.z) < eps))
+            r0 = dqmul(quat_from_columns(s2, n2, dcross(s2, n2)), dconj(quat_from_columns(s1, n1, dcross(s1, n1))));
+        D3 ls1, ln1;
+        if (h.space == CC_SPACE_WORLD) {
+            DQ iqa = dconj(dq(p.quat[h.body_a]));
+            ls1 = dnormalize(drot(iqa, s1));
+            ln1 = dnormalize(drot(iqa, n1));
+            j.inv_initial = f4q(dqmul(dqmul(dconj(dq(p.quat[h.body_b])), r0), dq(p.quat[h.body_a])));
+        } else {
+            ls1 = s1;
+            ln1 = n1;
+            j.inv_initial = f4q(r0);
+        }
+        j.ls1 = f3d(ls1);
+        j.ln1 = f3d(ln1);
+        j.ln2 = f3d(dcross(ls1, ln1));
+        // limits :384-388 (min raised to <= 0, max to >= 0) and the setters :495-520
+        const float INF = std::numeric_limits<float>::infinity();
+        j.limits_min = std::min(h.limits_min, 0.f);
+        j.limits_max = std::max(h.limits_max, 0.f);
+        j.slider_flags = (j.limits_min != -INF || j.limits_max != INF) ? 1 : 0;
+        j.limits_spring_mode = h.limits_spring.mode;
+        j.limits_freq = h.limits_spring.frequency_or_stiffness;
+        j.limits_damping = h.limits_spring.damping;
+        j.max_friction_force = h.max_friction_force;
+        j.motor_spring_mode = h.motor_spring.mode;
+        j.motor_freq = h.motor_spring.frequency_or_stiffness;
+        j.motor_damping = h.motor_spring.damping;
+        j.min_force = h.min_force_limit;
+        j.max_force = h.max_force_limit;
+        j.motor_state = h.motor_state;
+        j.target_velocity = h.target_velocity;
+        j.target_position =
+            j.slider_flags ? std::max(j.limits_min, std::min(j.limits_max, h.target_position)) : h.target_position;
+        made.push_back(j);
+    }
+    return add_other_joints(W, JT_SLIDER, made, out_index);
+}
+
+int cc_world_set_slider_limits(cc_world *W, int32_t index, float limits_min, float limits_max) {
+    if (!W || std::isnan(limits_min) || std::isnan(limits_max)) return CC_ERR_INVALID;
+    return edit_other(W, JT_SLIDER, index, [&](DevJoint &j) {  // setLimits :488-493
+        const float INF = std::numeric_limits<float>::infinity();
+        j.limits_min = std::min(limits_min, 0.f);
+        j.limits_max = std::max(limits_max, 0.f);
+        j.slider_flags = (j.limits_min != -INF || j.limits_max != INF) ? 1 : 0;
+    });
+}
+
+int cc_world_set_slider_motor(cc_world *W, int32_t index, int32_t motor_state, float target_velocity,
+                              float target_position) {
+    if (!W || motor_state < 0 || motor_state > 2 || !std::isfinite(target_velocity) || !std::isfinite(target_position))
+        return CC_ERR_INVALID;
+    return edit_other(W, JT_SLIDER, index, [&](DevJoint &j) {  // setMotorState / setTargetVelocity / setTargetPosition
+        j.motor_state = motor_state;
+        j.target_velocity = target_velocity;
+        j.target_position = j.slider_flags ? std::max(j.limits_min, std::min(j.limits_max, target_position))
+                                           : target_position;
+    });
+}
+
+int cc_world_get_slider_positions(cc_world *W, float *out, int32_t capacity) {
+    if (!W || capacity < 0 || (capacity > 0 && !out)) return CC_ERR_INVALID;
+    DevWorld &w = W->w;
+    const int ns = w.type_count[JT_SLIDER];
+    const int n = std::min(capacity, ns);
+    if (n > 0) {
+        BodyPoses p;
+        if (int r = read_poses(W, p)) return r;
+        for (int k = 0; k < n; k++) {  // getCurrentPosition :460-476
+            const DevJoint &j = W->others[w.type_first[JT_SLIDER] + k];
+            DQ qa = dq(p.quat[j.h.a]), qb = dq(p.quat[j.h.b]);
+            D3 r1 = drot(qa, {j.lp1.x, j.lp1.y, j.lp1.z}), r2 = drot(qb, {j.lp2.x, j.lp2.y, j.lp2.z});
+            D3 ca = d3(p.com[j.h.a]), cb = d3(p.com[j.h.b]);
+            D3 u{cb.x - ca.x + r2.x - r1.x, cb.y - ca.y + r2.y - r1.y, cb.z - ca.z + r2.z - r1.z};
+            D3 ax = drot(qa, {j.ls1.x, j.ls1.y, j.ls1.z});
+            out[k] = (float)(u.x * ax.x + u.y * ax.y + u.z * ax.z);
+        }
+    }
+    return capacity < ns ? CC_ERR_CAPACITY : CC_OK;
+}
+
+int cc_world_set_joint_enabled(cc_world *W, int32_t type, int32_t index, int32_t enabled) {
+    if (!W) return CC_ERR_INVALID;
+    if (type == JT_HINGE) return cc_world_set_hinge_enabled(W, index, enabled);
+    if (type == JT_SWING) return cc_world_set_swing_twist_enabled(W, index, enabled);
+    int r = edit_other(W, type, index,
+                       [&](DevJoint &j) { j.h.flags = enabled ? (j.h.flags | JF_ENABLED) : (j.h.flags & ~JF_ENABLED); });
+    if (r != CC_OK) return r;
+    return upload_partners(W);
+}
+
+int cc_world_get_joint_lambdas(cc_world *W, int32_t type, int32_t index, float *out, int32_t capacity,
+                               int32_t *count) {
+    if (!W || capacity < 0 || (capacity > 0 && !out)) return CC_ERR_INVALID;
+    DevWorld &w = W->w;
+    if (type < 0 || type >= JT_TYPES || type == JT_HINGE || type == JT_SWING) return CC_ERR_INVALID;
+    if (index < 0 || index >= w.type_count[type]) return CC_ERR_INVALID;
+    DevJoint j;
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    CC_TRY(cudaMemcpy(&j, w.others + w.type_first[type] + index, sizeof(DevJoint), cudaMemcpyDeviceToHost));
+    float v[7];
+    int m = 0;
+    auto put3 = [&](float3 a) {
+        v[m++] = a.x;
+        v[m++] = a.y;
+        v[m++] = a.z;
+    };
+    switch (type) {
+        case JT_POINT: put3(j.pt.lambda); break;
+        case JT_DISTANCE: v[m++] = j.ax.lambda; break;
+        case JT_FIXED:
+            put3(j.pt.lambda);
+            put3(j.rot.lambda);
+            break;
+        case JT_CONE:
+            put3(j.pt.lambda);
+            v[m++] = j.ang.lambda;
+            break;
+        case JT_SLIDER:
+            v[m++] = j.dual.lambda[0];
+            v[m++] = j.dual.lambda[1];
+            put3(j.rot.lambda);
+            v[m++] = j.ax.lambda;
+            v[m++] = j.motor.lambda;
+            break;
+    }
+    for (int k = 0; k < std::min(m, capacity); k++) out[k] = v[k];
+    if (count) *count = m;
+    return capacity < m ? CC_ERR_CAPACITY : CC_OK;
+}
+
+}  // extern "C"

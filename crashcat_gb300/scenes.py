@@ -16,8 +16,8 @@ from typing import Optional
 
 from ._lib import (BODY_DTYPE, COMBINE_GEOMETRIC_MEAN, COMBINE_MAX, DYNAMIC, MOTOR_OFF, MOTOR_POSITION,
                    MOTOR_VELOCITY, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_CONVEX_HULL, SHAPE_SPHERE, SHAPE_TRIANGLE_MESH, STATIC,
-                   SWING_CONE, SWING_PYRAMID,
-                   hinge_defaults, swing_twist_defaults)
+                   SWING_CONE, SWING_PYRAMID, JOINT_CONE, JOINT_DISTANCE, JOINT_FIXED, JOINT_POINT, JOINT_SLIDER,
+                   SPRING_STIFFNESS_AND_DAMPING, hinge_defaults, joint_defaults, swing_twist_defaults)
 
 # object layers of the reference's test helper (tst/helpers.ts:5-26)
 LAYER_MOVING = 0
@@ -45,6 +45,7 @@ class Scene:
     seed: int = 0
     hinges: Optional[np.ndarray] = None  # cc_hinge_desc records (_lib.HINGE_DTYPE)
     swings: Optional[np.ndarray] = None  # cc_swing_twist_desc records (_lib.SWING_TWIST_DTYPE)
+    joints: Optional[dict] = None  # {joint type: records of _lib.JOINT_DTYPES[type]} of the other joint types
     hull_points: Optional[list] = None  # point sets of the convex hulls, in hull index order
     skip_joint_pairs: bool = False
     gravity: tuple = (0.0, -9.81, 0.0)
@@ -1002,3 +1003,140 @@ def mesh_drop(n: int = 64, n_cells: int = 24, seed: int = 5, amplitude: float = 
     sc = Scene("mesh_drop", b, dt=1.0 / 60.0, steps=120, seed=seed, hull_points=hulls)
     sc.mesh = (pos, idx)
     return sc
+
+
+def joint_zoo(seed: int = 91) -> Scene:
+    """One world of every point, distance, fixed, cone and slider joint configuration, each
+    group hung from (or slid along) its own static post, 4 m apart in Z so no group touches
+    another; joined bodies do not collide (the ragdoll example's pair filter).  Released under
+    gravity with small seeded sideways velocities:
+
+    * point: two chains of 4 boxes (0.4 x 0.1 x 0.1 m) joined end to end by ball joints and
+      released horizontally, the second with 0.5 m/s sideways;
+    * distance: a rigid 1.5 m rod to a sphere released horizontally; a slack rope (0.5..2 m)
+      to a sphere 1 m below its post; a stiff spring (2000 N/m, 1 m rest length) to a sphere
+      hung 0.3 m below its rest length;
+    * fixed: a cantilever of two boxes welded end to end to a post; a free pair of welded
+      boxes thrown spinning as one rigid body;
+    * cone: two pendulum capsules with 30 degree cones about the hanging direction, started
+      20 degrees out and swinging outwards;
+    * slider: a box on a 30 degree incline rail with limits -1..1 m; a velocity motor (2 m/s)
+      and a position motor (0.5 m) on horizontal rails; a horizontal slide held back by 20 N of
+      friction; a slider between two free boxes."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    rows = []   # (shape, params, position, quaternion, static, linear velocity, angular velocity)
+
+    def body(shape, params, pos, static=False, q=(0.0, 0.0, 0.0, 1.0), v=(0.0, 0.0, 0.0), w=(0.0, 0.0, 0.0)):
+        rows.append((shape, params, pos, q, static, v, w))
+        return len(rows) - 1
+
+    def post(pos):
+        return body("box", (0.1, 0.1, 0.1), pos, static=True)
+
+    J = {t: [] for t in (JOINT_POINT, JOINT_DISTANCE, JOINT_FIXED, JOINT_CONE, JOINT_SLIDER)}
+
+    def joint(t, a, b, **f):
+        r = joint_defaults(t, 1)[0]
+        r["body_a"], r["body_b"] = a, b
+        for k, v in f.items():
+            if isinstance(v, dict):
+                for kk, vv in v.items():
+                    r[k][kk] = vv
+            else:
+                r[k] = v
+        J[t].append(r)
+
+    jitter = lambda: (0.0, 0.0, float(rng.uniform(-0.05, 0.05)))
+    # point: ball-joint chains
+    for c in range(2):
+        z = 4.0 * c
+        prev, x = post((0.0, 8.0, z)), 0.0
+        for i in range(4):
+            v = (0.0, 0.0, 0.5) if c == 1 else jitter()
+            j = body("box", (0.4, 0.1, 0.1), (x + 0.5, 8.0, z), v=v)
+            joint(JOINT_POINT, prev, j, point_a=(x, 8.0, z), point_b=(x, 8.0, z))
+            prev, x = j, x + 1.0
+    # distance: rod, slack rope, spring
+    z = 8.0
+    a = post((0.0, 8.0, z))
+    s1 = body("sphere", (0.2,), (1.5, 8.0, z), v=jitter())
+    joint(JOINT_DISTANCE, a, s1, point_a=(0.0, 8.0, z), point_b=(1.5, 8.0, z))
+    a = post((3.0, 8.0, z))
+    s2 = body("sphere", (0.2,), (3.0, 7.0, z), v=(0.3, 0.0, 0.0))
+    joint(JOINT_DISTANCE, a, s2, point_a=(3.0, 8.0, z), point_b=(3.0, 7.0, z), min_distance=0.5, max_distance=2.0)
+    a = post((6.0, 8.0, z))
+    s3 = body("sphere", (0.2,), (6.0, 6.7, z))
+    joint(JOINT_DISTANCE, a, s3, point_a=(6.0, 8.0, z), point_b=(6.0, 6.7, z), min_distance=1.0, max_distance=1.0,
+          spring={"mode": SPRING_STIFFNESS_AND_DAMPING, "frequency_or_stiffness": 2000.0, "damping": 0.0})
+    # fixed: cantilever and a free welded pair
+    z = 12.0
+    a = post((0.0, 8.0, z))
+    f1 = body("box", (0.4, 0.1, 0.1), (0.5, 8.0, z))
+    f2 = body("box", (0.4, 0.1, 0.1), (1.5, 8.0, z))
+    joint(JOINT_FIXED, a, f1, point_a=(0.0, 8.0, z), point_b=(0.0, 8.0, z))
+    joint(JOINT_FIXED, f1, f2, point_a=(1.0, 8.0, z), point_b=(1.0, 8.0, z))
+    spin = np.array([0.5, 1.0, 2.0])
+    g1 = body("box", (0.3, 0.2, 0.1), (4.0, 8.0, z), v=(1.0, 2.0, 0.0), w=tuple(spin))
+    # the second box moves with the first as one rigid body: v2 = v1 + w x (p2 - p1)
+    v2 = np.array([1.0, 2.0, 0.0]) + np.cross(spin, np.array([0.5, 0.4, 0.0]))
+    g2 = body("box", (0.2, 0.3, 0.1), (4.5, 8.4, z), v=tuple(v2), w=tuple(spin))
+    joint(JOINT_FIXED, g1, g2, auto_detect_point=1)
+    # cone: pendulums 20 degrees out, swinging outwards
+    z = 16.0
+    for c in range(2):
+        x = 4.0 * c
+        a = post((x, 8.0, z))
+        ang = math.radians(20.0)
+        d = (math.sin(ang), -math.cos(ang), 0.0) if c == 0 else (0.0, -math.cos(ang), math.sin(ang))
+        q = (0.0, 0.0, math.sin(ang / 2), math.cos(ang / 2)) if c == 0 else (-math.sin(ang / 2), 0.0, 0.0, math.cos(ang / 2))
+        centre = (x + 0.8 * d[0], 8.0 + 0.8 * d[1], z + 0.8 * d[2])
+        sp = 3.0
+        v = (sp * math.cos(ang), sp * math.sin(ang), 0.0) if c == 0 else (0.0, sp * math.sin(ang), sp * math.cos(ang))
+        k = body("capsule", (0.1, 0.6), centre, q=q, v=v)
+        joint(JOINT_CONE, a, k, point_a=(x, 8.0, z), point_b=(x, 8.0, z), twist_axis_a=(0.0, -1.0, 0.0),
+              twist_axis_b=d, half_cone_angle=math.radians(30.0))
+    # slider: incline with limits, velocity and position motors, friction, free pair
+    z = 20.0
+    a = post((0.0, 8.0, z))
+    ax = (math.cos(math.radians(30.0)), -math.sin(math.radians(30.0)), 0.0)
+    n_ax = (math.sin(math.radians(30.0)), math.cos(math.radians(30.0)), 0.0)
+    b1 = body("box", (0.2, 0.2, 0.2), (0.0, 8.0, z))
+    joint(JOINT_SLIDER, a, b1, point_a=(0.0, 8.0, z), point_b=(0.0, 8.0, z), slider_axis_a=ax, slider_axis_b=ax,
+          normal_axis_a=n_ax, normal_axis_b=n_ax, limits_min=-1.0, limits_max=1.0)
+    for i, (state, tv, tp) in enumerate(((1, 2.0, 0.0), (2, 0.0, 0.5))):
+        a = post((6.0 + 6.0 * i, 8.0, z))
+        bm = body("box", (0.2, 0.2, 0.2), (6.0 + 6.0 * i, 8.0, z))
+        joint(JOINT_SLIDER, a, bm, point_a=(6.0 + 6.0 * i, 8.0, z), point_b=(6.0 + 6.0 * i, 8.0, z),
+              slider_axis_a=(1.0, 0.0, 0.0), slider_axis_b=(1.0, 0.0, 0.0),
+              normal_axis_a=(0.0, 1.0, 0.0), normal_axis_b=(0.0, 1.0, 0.0), motor_state=state, target_velocity=tv,
+              target_position=tp)
+    a = post((18.0, 8.0, z))
+    bf = body("box", (0.2, 0.2, 0.2), (18.0, 8.0, z), v=(3.0, 0.0, 0.0))
+    joint(JOINT_SLIDER, a, bf, point_a=(18.0, 8.0, z), point_b=(18.0, 8.0, z), slider_axis_a=(1.0, 0.0, 0.0),
+          slider_axis_b=(1.0, 0.0, 0.0),
+          normal_axis_a=(0.0, 1.0, 0.0), normal_axis_b=(0.0, 1.0, 0.0), max_friction_force=20.0)
+    p1 = body("box", (0.3, 0.2, 0.2), (28.0, 8.0, z), v=(0.0, 1.0, 0.0), w=(0.0, 0.0, 1.0))
+    p2 = body("box", (0.2, 0.2, 0.2), (29.0, 8.0, z), v=(2.0, 1.0, 0.0), w=(0.0, 0.0, 1.0))
+    joint(JOINT_SLIDER, p1, p2, slider_axis_a=(1.0, 0.0, 0.0), slider_axis_b=(1.0, 0.0, 0.0),
+          normal_axis_a=(0.0, 1.0, 0.0), normal_axis_b=(0.0, 1.0, 0.0), auto_detect_point=1)
+
+    b = blank_bodies(len(rows))
+    for i, (shape, params, pos, q, static, v, w) in enumerate(rows):
+        if shape == "box":
+            set_box(b, i, params)
+        elif shape == "sphere":
+            set_sphere(b, i, params[0])
+        else:
+            set_capsule(b, i, params[0], params[1])
+        b["position"][i] = pos
+        b["quaternion"][i] = q
+        b["linear_velocity"][i] = v
+        b["angular_velocity"][i] = w
+        if static:
+            b["motion_type"][i] = STATIC
+            b["object_layer"][i] = LAYER_NOT_MOVING
+    b["linear_damping"] = 0.0
+    b["angular_damping"] = 0.0
+    b["allow_sleeping"][:] = 0
+    joints = {t: np.array(r, dtype=joint_defaults(t, 0).dtype) for t, r in J.items()}
+    return Scene("joint_zoo", b, dt=1.0 / 60.0, steps=120, seed=seed, joints=joints, skip_joint_pairs=True)

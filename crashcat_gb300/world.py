@@ -538,6 +538,49 @@ class GpuWorld:
     def set_skip_joint_pairs(self, on: bool) -> None:
         check(self._lib.cc_world_set_skip_joint_pairs(self.handle, int(bool(on))), "cc_world_set_skip_joint_pairs")
 
+    def add_joints(self, joint_type: int, joints: np.ndarray) -> np.ndarray:
+        """cc_world_add_{point,distance,fixed,cone,slider}_joints: records of
+        _lib.JOINT_DTYPES[joint_type]; returns the joints' per-type indices."""
+        fn = _lib.JOINT_ADDERS[joint_type]
+        joints = np.ascontiguousarray(joints, dtype=_lib.JOINT_DTYPES[joint_type])
+        out = np.zeros(len(joints), dtype=np.int32)
+        check(getattr(self._lib, fn)(self.handle, ptr(joints), len(joints), ptr(out)), fn)
+        return out
+
+    def set_joint_enabled(self, joint_type: int, index: int, enabled: bool) -> None:
+        check(self._lib.cc_world_set_joint_enabled(self.handle, joint_type, index, int(bool(enabled))),
+              "cc_world_set_joint_enabled")
+
+    def joint_lambdas(self, joint_type: int, index: int) -> np.ndarray:
+        """cc_world_get_joint_lambdas: the accumulated impulses of one joint after the last step."""
+        out = np.zeros(8, dtype=np.float32)
+        n = C.c_int32(0)
+        check(self._lib.cc_world_get_joint_lambdas(self.handle, joint_type, index, ptr(out), 8, C.byref(n)),
+              "cc_world_get_joint_lambdas")
+        return out[:n.value]
+
+    def set_distance(self, index: int, min_distance: float, max_distance: float) -> None:
+        check(self._lib.cc_world_set_distance(self.handle, index, C.c_float(min_distance), C.c_float(max_distance)),
+              "cc_world_set_distance")
+
+    def set_cone_half_angle(self, index: int, half_cone_angle: float) -> None:
+        check(self._lib.cc_world_set_cone_half_angle(self.handle, index, C.c_float(half_cone_angle)),
+              "cc_world_set_cone_half_angle")
+
+    def set_slider_limits(self, index: int, lo: float, hi: float) -> None:
+        check(self._lib.cc_world_set_slider_limits(self.handle, index, C.c_float(lo), C.c_float(hi)),
+              "cc_world_set_slider_limits")
+
+    def set_slider_motor(self, index: int, state: int, target_velocity: float = 0.0,
+                         target_position: float = 0.0) -> None:
+        check(self._lib.cc_world_set_slider_motor(self.handle, index, state, C.c_float(target_velocity),
+                                                  C.c_float(target_position)), "cc_world_set_slider_motor")
+
+    def slider_positions(self, n: int) -> np.ndarray:
+        out = np.zeros(max(n, 1), dtype=np.float32)
+        check(self._lib.cc_world_get_slider_positions(self.handle, ptr(out), n), "cc_world_get_slider_positions")
+        return out[:n]
+
     def stats(self) -> dict:
         s = _lib.Stats()
         check(self._lib.cc_world_get_stats(self.handle, C.byref(s)), "cc_world_get_stats")

@@ -401,6 +401,119 @@ int cc_world_set_swing_twist_motor(cc_world *world, int32_t index, int32_t swing
                                    const float *target_orientation, float max_friction_torque);
 int cc_world_set_swing_twist_enabled(cc_world *world, int32_t index, int32_t enabled);
 
+/* ---------------------------------------------------------------------------
+ * Point, distance, fixed, cone and slider joints (src/constraints/point-, distance-,
+ * fixed-, cone- and slider-constraint.ts).  Every joint type keeps its own index space, as
+ * the reference's per-type constraint pools do; the *_index arguments below are those
+ * per-type indices.  Joints are solved after an island's contacts in (priority, index,
+ * type) order (constraints.ts:248-261); the types are numbered as the reference's
+ * ConstraintType (constraint-id.ts:24-36).
+ * ------------------------------------------------------------------------- */
+enum cc_joint_type {
+    CC_JOINT_POINT = 0, CC_JOINT_DISTANCE = 1, CC_JOINT_HINGE = 2, CC_JOINT_SLIDER = 3,
+    CC_JOINT_FIXED = 4, CC_JOINT_CONE = 5, CC_JOINT_SWING_TWIST = 6
+};
+
+/* PointConstraintSettings (point-constraint.ts:44-63): removes the 3 translational DOF. */
+typedef struct cc_point_desc {
+    int32_t body_a, body_b;
+    int32_t space;                     /* cc_constraint_space of the points */
+    float point_a[3], point_b[3];
+    int32_t priority, enabled;
+    int32_t num_velocity_steps_override, num_position_steps_override;
+} cc_point_desc;
+/* pointConstraint.create (point-constraint.ts:66-139) for n joints. */
+int cc_world_add_point_joints(cc_world *world, const cc_point_desc *joints, int32_t n, int32_t *out_index);
+
+/* DistanceConstraintSettings (distance-constraint.ts:58-82): keeps the attachment points
+ * between min_distance and max_distance (a negative value is unset: both unset = the current
+ * distance; one unset = the current distance clamped by the other), with an optional spring. */
+typedef struct cc_distance_desc {
+    int32_t body_a, body_b;
+    int32_t space;
+    float point_a[3], point_b[3];
+    float min_distance, max_distance;
+    cc_spring_settings spring;         /* frequency 0 = rigid */
+    int32_t priority, enabled;
+    int32_t num_velocity_steps_override, num_position_steps_override;
+} cc_distance_desc;
+/* distanceConstraint.create (distance-constraint.ts:96-204) for n joints. */
+int cc_world_add_distance_joints(cc_world *world, const cc_distance_desc *joints, int32_t n, int32_t *out_index);
+/* setDistance (distance-constraint.ts:484-493): a negative value keeps the current bound;
+ * min > max makes both their mean. */
+int cc_world_set_distance(cc_world *world, int32_t index, float min_distance, float max_distance);
+
+/* FixedConstraintSettings (fixed-constraint.ts:63-101): welds two bodies.  The pivot is
+ * point_a / point_b (the reference's omitted point is the body's centre of mass), or, with
+ * auto_detect_point, the inverse-mass-weighted mean of the two centres of mass (world space
+ * only).  The axes give the relative orientation to hold (defaults: X = (1,0,0), Y = (0,1,0)). */
+typedef struct cc_fixed_desc {
+    int32_t body_a, body_b;
+    int32_t space;
+    int32_t auto_detect_point;
+    float point_a[3], point_b[3];
+    float axis_x_a[3], axis_y_a[3], axis_x_b[3], axis_y_b[3];
+    int32_t priority, enabled;
+    int32_t num_velocity_steps_override, num_position_steps_override;
+} cc_fixed_desc;
+/* fixedConstraint.create (fixed-constraint.ts:103-250) for n joints. */
+int cc_world_add_fixed_joints(cc_world *world, const cc_fixed_desc *joints, int32_t n, int32_t *out_index);
+
+/* ConeConstraintSettings (cone-constraint.ts:94-116): a point constraint plus a cone limit
+ * on the angle between the two twist axes. */
+typedef struct cc_cone_desc {
+    int32_t body_a, body_b;
+    int32_t space;
+    float point_a[3], point_b[3];
+    float twist_axis_a[3], twist_axis_b[3];  /* normalised on creation */
+    float half_cone_angle;                   /* radians (0: the axes stay aligned) */
+    int32_t priority, enabled;
+    int32_t num_velocity_steps_override, num_position_steps_override;
+} cc_cone_desc;
+/* coneConstraint.create (cone-constraint.ts:150-230) for n joints. */
+int cc_world_add_cone_joints(cc_world *world, const cc_cone_desc *joints, int32_t n, int32_t *out_index);
+/* setHalfConeAngle (cone-constraint.ts:262-264): clamped to [0, pi]. */
+int cc_world_set_cone_half_angle(cc_world *world, int32_t index, float half_cone_angle);
+
+/* SliderConstraintSettings (slider-constraint.ts:152-179): one translational DOF along the
+ * slider axis, with limits (soft with a spring), friction while the motor is off, and a
+ * velocity or position motor.  motor_state / target_velocity / target_position are applied
+ * after creation as setMotorState / setTargetVelocity / setTargetPosition do. */
+typedef struct cc_slider_desc {
+    int32_t body_a, body_b;
+    int32_t space;
+    int32_t auto_detect_point;
+    float point_a[3], point_b[3];
+    float slider_axis_a[3], slider_axis_b[3];
+    float normal_axis_a[3], normal_axis_b[3];
+    float limits_min, limits_max;      /* metres; -inf / +inf = no limit; min is raised to <= 0, max to >= 0 */
+    cc_spring_settings limits_spring;
+    float max_friction_force;          /* N while the motor is off */
+    cc_spring_settings motor_spring;   /* position motor (reference default: frequency 2 Hz, damping 1) */
+    float min_force_limit, max_force_limit;  /* N (reference default: -inf, +inf) */
+    int32_t motor_state;               /* cc_motor_state */
+    float target_velocity;             /* m/s */
+    float target_position;             /* m, clamped to the limits */
+    int32_t priority, enabled;
+    int32_t num_velocity_steps_override, num_position_steps_override;
+} cc_slider_desc;
+/* sliderConstraint.create (slider-constraint.ts:261-412) for n joints. */
+int cc_world_add_slider_joints(cc_world *world, const cc_slider_desc *joints, int32_t n, int32_t *out_index);
+/* setLimits / setMotorState + setTargetVelocity + setTargetPosition (slider-constraint.ts:488-520). */
+int cc_world_set_slider_limits(cc_world *world, int32_t index, float limits_min, float limits_max);
+int cc_world_set_slider_motor(cc_world *world, int32_t index, int32_t motor_state, float target_velocity,
+                              float target_position);
+/* getCurrentPosition (slider-constraint.ts:460-476) of every slider, n floats. */
+int cc_world_get_slider_positions(cc_world *world, float *out, int32_t capacity);
+
+/* ConstraintBase.enabled of one joint of any type (cc_joint_type). */
+int cc_world_set_joint_enabled(cc_world *world, int32_t type, int32_t index, int32_t enabled);
+/* The accumulated impulses of one joint after the last step (getTotalLambda* of each type):
+ * point 3 (point part); distance 1; fixed 6 (point, rotation); cone 4 (point, cone angle);
+ * slider 7 (2 position, 3 rotation, limits, motor).  *count receives the number written. */
+int cc_world_get_joint_lambdas(cc_world *world, int32_t type, int32_t index, float *out, int32_t capacity,
+                               int32_t *count);
+
 /* on != 0: the broadphase skips body pairs that share an enabled joint, the declarative form
  * of a Listener.onBodyPairValidate that rejects them (src/broadphase/broadphase.ts:112-123; the
  * ragdoll example's filter).  Each body may then share joints with at most 8 other bodies

@@ -158,6 +158,11 @@ struct World {
     std::vector<std::array<int64_t, 3>> events;
     std::vector<HingeJoint> joints;
     std::vector<SwingTwistJoint> swings;
+    std::vector<PointJoint> points;
+    std::vector<DistanceJoint> distances;
+    std::vector<FixedJoint> fixeds;
+    std::vector<ConeJoint> cones;
+    std::vector<SliderJoint> sliders;
     std::vector<std::unique_ptr<HullData>> hulls;  // convex hull shapes the bodies refer to
     std::vector<std::unique_ptr<MeshData>> meshes;  // triangle meshes the bodies refer to
     // skip broadphase pairs of bodies that share an enabled joint: the declarative form of the
@@ -528,27 +533,52 @@ static void bvh_build(const std::vector<Body> &bodies, std::vector<int> &idx, st
     nodes[ni].right = r;
 }
 
-// User joints of every type under one id: hinges are 0.., swing-twists JOINT_SWING + index.
+// User joints of every type under one id, as the reference's ConstraintId packs them
+// (constraint-id.ts:1-35): the ConstraintType above bit 24, the per-type index below.
 // joint_ids lists them type by type, each in creation order, the order in which the
 // reference walks its constraint pools (constraints.ts:264-318, islands.ts:210-225).
-constexpr int JOINT_SWING = 1 << 24;
+enum JointType { JT_POINT = 0, JT_DISTANCE = 1, JT_HINGE = 2, JT_SLIDER = 3, JT_FIXED = 4, JT_CONE = 5, JT_SWING = 6 };
+constexpr int JOINT_TYPE_SHIFT = 24, JOINT_INDEX_MASK = (1 << JOINT_TYPE_SHIFT) - 1;
+inline int joint_type(int id) { return id >> JOINT_TYPE_SHIFT; }
+inline int joint_index(int id) { return id & JOINT_INDEX_MASK; }
 struct JointInfo {
     int a, b, priority, index, type;
     bool enabled;
+    int velOverride, posOverride;
 };
+static const JointBase &joint_base(const World &w, int id) {
+    int i = joint_index(id);
+    switch (joint_type(id)) {
+    case JT_POINT: return w.points[i];
+    case JT_DISTANCE: return w.distances[i];
+    case JT_SLIDER: return w.sliders[i];
+    case JT_FIXED: return w.fixeds[i];
+    case JT_CONE: return w.cones[i];
+    default: break;
+    }
+    static const JointBase none;
+    return none;
+}
 static std::vector<int> joint_ids(const World &w) {
     std::vector<int> ids;
-    for (size_t i = 0; i < w.joints.size(); i++) ids.push_back((int)i);
-    for (size_t i = 0; i < w.swings.size(); i++) ids.push_back(JOINT_SWING + (int)i);
+    size_t count[7] = {w.points.size(), w.distances.size(), w.joints.size(), w.sliders.size(),
+                       w.fixeds.size(),  w.cones.size(),     w.swings.size()};
+    for (int t = 0; t < 7; t++)
+        for (size_t i = 0; i < count[t]; i++) ids.push_back((t << JOINT_TYPE_SHIFT) | (int)i);
     return ids;
 }
 static JointInfo joint_info(const World &w, int id) {
-    if (id >= JOINT_SWING) {
-        const SwingTwistJoint &j = w.swings[id - JOINT_SWING];
-        return {j.a, j.b, j.priority, j.index, 6, j.enabled};  // ConstraintType.SWING_TWIST
+    int t = joint_type(id), i = joint_index(id);
+    if (t == JT_SWING) {
+        const SwingTwistJoint &j = w.swings[i];
+        return {j.a, j.b, j.priority, j.index, t, j.enabled, j.velOverride, j.posOverride};
     }
-    const HingeJoint &j = w.joints[id];
-    return {j.a, j.b, j.priority, j.index, 2, j.enabled};  // ConstraintType.HINGE
+    if (t == JT_HINGE) {
+        const HingeJoint &j = w.joints[i];
+        return {j.a, j.b, j.priority, j.index, t, j.enabled, j.velOverride, j.posOverride};
+    }
+    const JointBase &j = joint_base(w, id);
+    return {j.a, j.b, j.priority, j.index, t, j.enabled, j.velOverride, j.posOverride};
 }
 
 static void find_colliding_pairs(World &w) {
@@ -1092,6 +1122,62 @@ static void apply_dof_pos(Body &b) {
 
 #include "oracle_joints.h"
 
+// ConstraintDef dispatch of every joint type (constraints.ts:264-342)
+static void joint_setup(World &w, int id, double dt) {
+    int i = joint_index(id);
+    switch (joint_type(id)) {
+    case JT_POINT: { PointJoint &j = w.points[i]; pointj_setup(j, w.bodies[j.a], w.bodies[j.b]); break; }
+    case JT_DISTANCE: { DistanceJoint &j = w.distances[i]; distance_calc(j, w.bodies[j.a], w.bodies[j.b], dt); break; }
+    case JT_HINGE: { HingeJoint &j = w.joints[i]; hinge_setup(j, w.bodies[j.a], w.bodies[j.b], dt); break; }
+    case JT_SLIDER: { SliderJoint &j = w.sliders[i]; slider_setup(j, w.bodies[j.a], w.bodies[j.b], dt); break; }
+    case JT_FIXED: { FixedJoint &j = w.fixeds[i]; fixed_setup(j, w.bodies[j.a], w.bodies[j.b]); break; }
+    case JT_CONE: { ConeJoint &j = w.cones[i]; cone_setup(j, w.bodies[j.a], w.bodies[j.b]); break; }
+    case JT_SWING: { SwingTwistJoint &j = w.swings[i]; swing_setup(j, w.bodies[j.a], w.bodies[j.b], dt); break; }
+    }
+}
+static void joint_warm(World &w, int id, double ratio) {
+    int i = joint_index(id);
+    switch (joint_type(id)) {
+    case JT_POINT: { PointJoint &j = w.points[i]; pointj_warm(j, w.bodies[j.a], w.bodies[j.b], ratio); break; }
+    case JT_DISTANCE: { DistanceJoint &j = w.distances[i]; distance_warm(j, w.bodies[j.a], w.bodies[j.b], ratio); break; }
+    case JT_HINGE: { HingeJoint &j = w.joints[i]; hinge_warm(j, w.bodies[j.a], w.bodies[j.b], ratio); break; }
+    case JT_SLIDER: { SliderJoint &j = w.sliders[i]; slider_warm(j, w.bodies[j.a], w.bodies[j.b], ratio); break; }
+    case JT_FIXED: { FixedJoint &j = w.fixeds[i]; fixed_warm(j, w.bodies[j.a], w.bodies[j.b], ratio); break; }
+    case JT_CONE: { ConeJoint &j = w.cones[i]; cone_warm(j, w.bodies[j.a], w.bodies[j.b], ratio); break; }
+    case JT_SWING: { SwingTwistJoint &j = w.swings[i]; swing_warm(j, w.bodies[j.a], w.bodies[j.b], ratio); break; }
+    }
+}
+static bool joint_solve_velocity(World &w, int id, double dt) {
+    int i = joint_index(id);
+    switch (joint_type(id)) {
+    case JT_POINT: { PointJoint &j = w.points[i]; return pointj_solve_velocity(j, w.bodies[j.a], w.bodies[j.b]); }
+    case JT_DISTANCE: { DistanceJoint &j = w.distances[i]; return distance_solve_velocity(j, w.bodies[j.a], w.bodies[j.b]); }
+    case JT_HINGE: { HingeJoint &j = w.joints[i]; return hinge_solve_velocity(j, w.bodies[j.a], w.bodies[j.b], dt); }
+    case JT_SLIDER: { SliderJoint &j = w.sliders[i]; return slider_solve_velocity(j, w.bodies[j.a], w.bodies[j.b], dt); }
+    case JT_FIXED: { FixedJoint &j = w.fixeds[i]; return fixed_solve_velocity(j, w.bodies[j.a], w.bodies[j.b]); }
+    case JT_CONE: { ConeJoint &j = w.cones[i]; return cone_solve_velocity(j, w.bodies[j.a], w.bodies[j.b]); }
+    case JT_SWING: { SwingTwistJoint &j = w.swings[i]; return swing_solve_velocity(j, w.bodies[j.a], w.bodies[j.b], dt); }
+    }
+    return false;
+}
+static bool joint_solve_position(World &w, int id, double dt) {
+    int i = joint_index(id);
+    double beta = w.s.baumgarteFactor;
+    switch (joint_type(id)) {
+    case JT_POINT: { PointJoint &j = w.points[i]; return pointj_solve_position(j, w.bodies[j.a], w.bodies[j.b], beta); }
+    case JT_DISTANCE: {
+        DistanceJoint &j = w.distances[i];
+        return distance_solve_position(j, w.bodies[j.a], w.bodies[j.b], dt, beta);
+    }
+    case JT_HINGE: { HingeJoint &j = w.joints[i]; return hinge_solve_position(j, w.bodies[j.a], w.bodies[j.b], dt, beta); }
+    case JT_SLIDER: { SliderJoint &j = w.sliders[i]; return slider_solve_position(j, w.bodies[j.a], w.bodies[j.b], dt, beta); }
+    case JT_FIXED: { FixedJoint &j = w.fixeds[i]; return fixed_solve_position(j, w.bodies[j.a], w.bodies[j.b], beta); }
+    case JT_CONE: { ConeJoint &j = w.cones[i]; return cone_solve_position(j, w.bodies[j.a], w.bodies[j.b], beta); }
+    case JT_SWING: { SwingTwistJoint &j = w.swings[i]; return swing_solve_position(j, w.bodies[j.a], w.bodies[j.b], beta); }
+    }
+    return false;
+}
+
 // solvePositionConstraintsForIsland contact-constraints.ts:1098-1216
 static bool solve_position(World &w, const std::vector<int> &ids) {
     bool any = false;
@@ -1231,14 +1317,8 @@ static void build_islands(World &w) {
         }
         // getConstraintIterationOverrides of the island's user constraints (hinge-constraint.ts:819-827)
         for (int id : is.jointIndices) {
-            int jv, jp;
-            if (id >= JOINT_SWING) {
-                jv = w.swings[id - JOINT_SWING].velOverride;
-                jp = w.swings[id - JOINT_SWING].posOverride;
-            } else {
-                jv = w.joints[id].velOverride;
-                jp = w.joints[id].posOverride;
-            }
+            JointInfo ji = joint_info(w, id);
+            int jv = ji.velOverride, jp = ji.posOverride;
             vs = std::max(vs, jv);
             dv = dv || jv == 0;
             ps = std::max(ps, jp);
@@ -1621,13 +1701,7 @@ static void step(World &w, double dt) {
         };
         for (int id : joint_ids(w)) {
             if (!joint_active(id)) continue;
-            if (id >= JOINT_SWING) {
-                SwingTwistJoint &j = w.swings[id - JOINT_SWING];
-                swing_setup(j, w.bodies[j.a], w.bodies[j.b], dt);
-            } else {
-                HingeJoint &j = w.joints[id];
-                hinge_setup(j, w.bodies[j.a], w.bodies[j.b], dt);
-            }
+            joint_setup(w, id, dt);
         }
         if (w.recordTape) record_tape_rows(w, dt);
         if (w.s.warmStarting) {
@@ -1635,13 +1709,7 @@ static void step(World &w, double dt) {
             warm_start_all(w, ratio);
             for (int id : joint_ids(w)) {
                 if (!joint_active(id)) continue;
-                if (id >= JOINT_SWING) {
-                    SwingTwistJoint &j = w.swings[id - JOINT_SWING];
-                    swing_warm(j, w.bodies[j.a], w.bodies[j.b], ratio);
-                } else {
-                    HingeJoint &j = w.joints[id];
-                    hinge_warm(j, w.bodies[j.a], w.bodies[j.b], ratio);
-                }
+                joint_warm(w, id, ratio);
             }
         }
         w.prevDt = dt;
@@ -1696,15 +1764,7 @@ static void step(World &w, double dt) {
             }
             for (int i = 0; i < is.velSteps; i++) {
                 if (!is.contactIndices.empty()) solve_velocity(w, is.contactIndices);
-                for (int ji : is.jointIndices) {
-                    if (ji >= JOINT_SWING) {
-                        SwingTwistJoint &j = w.swings[ji - JOINT_SWING];
-                        swing_solve_velocity(j, w.bodies[j.a], w.bodies[j.b], dt);
-                    } else {
-                        HingeJoint &j = w.joints[ji];
-                        hinge_solve_velocity(j, w.bodies[j.a], w.bodies[j.b], dt);
-                    }
-                }
+                for (int ji : is.jointIndices) joint_solve_velocity(w, ji, dt);
             }
         }
         if (w.recordTape) record_tape_finals(w);
@@ -1766,16 +1826,7 @@ static void step(World &w, double dt) {
             for (int i = 0; i < is.posSteps; i++) {
                 bool applied = false;
                 if (!is.contactIndices.empty()) applied = solve_position(w, is.contactIndices);
-                for (int ji : is.jointIndices) {
-                    if (ji >= JOINT_SWING) {
-                        SwingTwistJoint &j = w.swings[ji - JOINT_SWING];
-                        applied = swing_solve_position(j, w.bodies[j.a], w.bodies[j.b], w.s.baumgarteFactor) || applied;
-                    } else {
-                        HingeJoint &j = w.joints[ji];
-                        applied =
-                            hinge_solve_position(j, w.bodies[j.a], w.bodies[j.b], dt, w.s.baumgarteFactor) || applied;
-                    }
-                }
+                for (int ji : is.jointIndices) applied = joint_solve_position(w, ji, dt) || applied;
                 if (!applied) break;
             }
         }
@@ -2137,6 +2188,231 @@ int orc_add_swing_twist(void *wp, const double *d) {
     w.swings.push_back(j);
     return j.index;
 }
+// Point, distance, fixed, cone and slider joints (the create functions of point-, distance-,
+// fixed-, cone- and slider-constraint.ts) from a flat record of doubles:
+//   0 bodyA, 1 bodyB, 2 space (0 world, 1 local), 3 priority, 4 velocity override,
+//   5 position override, 6 enabled, then per type:
+//   point     7-9 pointA, 10-12 pointB
+//   distance  7-9 pointA, 10-12 pointB, 13 minDistance, 14 maxDistance (< 0: unset),
+//             15-17 spring (mode, frequency or stiffness, damping)
+//   fixed     7 autoDetectPoint, 8-10 point1, 11-13 point2, 14-16 axisX1, 17-19 axisY1,
+//             20-22 axisX2, 23-25 axisY2
+//   cone      7-9 pointA, 10-12 pointB, 13-15 twistAxisA, 16-18 twistAxisB, 19 halfConeAngle
+//   slider    7 autoDetectPoint, 8-10 pointA, 11-13 pointB, 14-16 sliderAxisA, 17-19 sliderAxisB,
+//             20-22 normalAxisA, 23-25 normalAxisB, 26 limitsMin, 27 limitsMax,
+//             28-30 limits spring, 31 maxFrictionForce, 32-34 motor spring, 35 min force,
+//             36 max force, 37 motor state, 38 target velocity, 39 target position
+//             (37-39 through setMotorState / setTargetVelocity / setTargetPosition)
+// Returns the joint's per-type index, or -1.
+int orc_add_joint(void *wp, int type, const double *d) {
+    World &w = *(World *)wp;
+    int a = (int)d[0], b = (int)d[1];
+    if (a < 0 || b < 0 || a >= (int)w.bodies.size() || b >= (int)w.bodies.size()) return -1;
+    const Body &A = w.bodies[a], &B = w.bodies[b];
+    const bool world_space = (int)d[2] == 0;
+    const Q4 iqA = qconj(A.quat), iqB = qconj(B.quat);
+    auto base = [&](JointBase &j, int index) {
+        j.a = a;
+        j.b = b;
+        j.index = index;
+        j.priority = (int)d[3];
+        j.velOverride = (int)d[4];
+        j.posOverride = (int)d[5];
+        j.enabled = d[6] != 0;
+    };
+    auto v = [&](int k) { return V3{d[k], d[k + 1], d[k + 2]}; };
+    // the anchor of autoDetectPoint: the inverse-mass-weighted mean of the centres of mass
+    auto anchor = [&]() {
+        double im = A.invMass + B.invMass;
+        if (im == 0) return A.com;
+        return add(scale(A.com, A.invMass / im), scale(B.com, B.invMass / im));
+    };
+    switch (type) {
+    case JT_POINT: {
+        PointJoint j;
+        base(j, (int)w.points.size());
+        if (world_space) {
+            j.lp1 = rotate(iqA, sub(v(7), A.com));
+            j.lp2 = rotate(iqB, sub(v(10), B.com));
+        } else {
+            j.lp1 = v(7);
+            j.lp2 = v(10);
+        }
+        w.points.push_back(j);
+        return j.index;
+    }
+    case JT_DISTANCE: {  // distance-constraint.ts create :121-214
+        DistanceJoint j;
+        base(j, (int)w.distances.size());
+        if (world_space) {
+            j.lp1 = rotate(iqA, sub(v(7), A.com));
+            j.lp2 = rotate(iqB, sub(v(10), B.com));
+            j.wp1 = v(7);
+            j.wp2 = v(10);
+        } else {
+            j.lp1 = v(7);
+            j.lp2 = v(10);
+            j.wp1 = add(rotate(A.quat, j.lp1), A.com);
+            j.wp2 = add(rotate(B.quat, j.lp2), B.com);
+        }
+        double dist = len(sub(j.wp2, j.wp1));
+        double mn = d[13], mx = d[14];
+        if (mn < 0 && mx < 0) {
+            j.minDistance = j.maxDistance = dist;
+        } else {
+            j.minDistance = mn < 0 ? std::min(dist, mx) : mn;
+            j.maxDistance = mx < 0 ? std::max(dist, mn) : mx;
+        }
+        j.spring = {(int)d[15], d[16], d[17]};
+        w.distances.push_back(j);
+        return j.index;
+    }
+    case JT_FIXED: {  // fixed-constraint.ts create :131-262
+        FixedJoint j;
+        base(j, (int)w.fixeds.size());
+        Q4 r0 = inv_initial_orientation_xy(normalize(v(14)), normalize(v(17)), normalize(v(20)), normalize(v(23)));
+        if (world_space) {
+            if (d[7] != 0) {
+                V3 p = anchor();
+                j.lp1 = rotate(iqA, sub(p, A.com));
+                j.lp2 = rotate(iqB, sub(p, B.com));
+            } else {
+                j.lp1 = rotate(iqA, sub(v(8), A.com));
+                j.lp2 = rotate(iqB, sub(v(11), B.com));
+            }
+            j.invInitial = qmul(qmul(iqB, r0), A.quat);
+        } else {
+            j.lp1 = v(8);
+            j.lp2 = v(11);
+            j.invInitial = r0;
+        }
+        w.fixeds.push_back(j);
+        return j.index;
+    }
+    case JT_CONE: {  // cone-constraint.ts create :150-230
+        ConeJoint j;
+        base(j, (int)w.cones.size());
+        V3 t1 = normalize(v(13)), t2 = normalize(v(16));
+        j.cosHalfCone = std::cos(d[19]);
+        // getNormalizedPerpendicular :118-136
+        double ax = std::fabs(t1.x), ay = std::fabs(t1.y), az = std::fabs(t1.z);
+        V3 perp = (ax <= ay && ax <= az) ? V3{0, -t1.z, t1.y} : (ay <= az ? V3{t1.z, 0, -t1.x} : V3{-t1.y, t1.x, 0});
+        j.wRotAxis = normalize(perp);
+        if (world_space) {
+            j.lp1 = rotate(iqA, sub(v(7), A.com));
+            j.lp2 = rotate(iqB, sub(v(10), B.com));
+            j.lt1 = rotate(iqA, t1);
+            j.lt2 = rotate(iqB, t2);
+        } else {
+            j.lp1 = v(7);
+            j.lp2 = v(10);
+            j.lt1 = t1;
+            j.lt2 = t2;
+            j.wRotAxis = rotate(A.quat, j.wRotAxis);
+        }
+        w.cones.push_back(j);
+        return j.index;
+    }
+    case JT_SLIDER: {  // slider-constraint.ts create :261-412 and the setters :488-525
+        SliderJoint j;
+        base(j, (int)w.sliders.size());
+        V3 s1 = normalize(v(14)), s2 = normalize(v(17)), n1 = normalize(v(20)), n2 = normalize(v(23));
+        // getInvInitialOrientationXY :203-259 (exact component test with eps 1e-6)
+        const double eps = 1e-6;
+        Q4 r0{0, 0, 0, 1};
+        if (!(std::fabs(s1.x - s2.x) < eps && std::fabs(s1.y - s2.y) < eps && std::fabs(s1.z - s2.z) < eps &&
+              std::fabs(n1.x - n2.x) < eps && std::fabs(n1.y - n2.y) < eps && std::fabs(n1.z - n2.z) < eps))
+            r0 = qmul(axes_to_quat(s2, n2), qconj(axes_to_quat(s1, n1)));
+        if (world_space) {
+            if (d[7] != 0) {
+                V3 p = anchor();
+                j.lp1 = rotate(iqA, sub(p, A.com));
+                j.lp2 = rotate(iqB, sub(p, B.com));
+            } else {
+                j.lp1 = rotate(iqA, sub(v(8), A.com));
+                j.lp2 = rotate(iqB, sub(v(11), B.com));
+            }
+            j.lSlider1 = normalize(rotate(iqA, s1));
+            j.lNormal1 = normalize(rotate(iqA, n1));
+            j.lNormal2 = cross(j.lSlider1, j.lNormal1);
+            j.invInitial = qmul(qmul(iqB, r0), A.quat);
+        } else {
+            j.lp1 = v(8);
+            j.lp2 = v(11);
+            j.lSlider1 = s1;
+            j.lNormal1 = n1;
+            j.lNormal2 = cross(j.lSlider1, j.lNormal1);
+            j.invInitial = r0;
+        }
+        j.limitsMin = std::min(d[26], 0.0);
+        j.limitsMax = std::max(d[27], 0.0);
+        j.hasLimits = j.limitsMin != -1.0 / 0.0 || j.limitsMax != 1.0 / 0.0;
+        j.limitsSpring = {(int)d[28], d[29], d[30]};
+        j.maxFrictionForce = d[31];
+        j.motorSpring = {(int)d[32], d[33], d[34]};
+        j.minForceLimit = d[35];
+        j.maxForceLimit = d[36];
+        j.motorState = (int)d[37];
+        j.targetVelocity = d[38];
+        j.targetPosition = j.hasLimits ? std::max(j.limitsMin, std::min(j.limitsMax, d[39])) : d[39];
+        w.sliders.push_back(j);
+        return j.index;
+    }
+    default: return -1;
+    }
+}
+// Total impulses of one joint (getTotalLambda* of each type): point 3 (point part),
+// distance 1, fixed 6 (point, rotation), cone 4 (point, angle), slider 2 + 3 + 1 + 1
+// (position, rotation, limits, motor).  Returns the count written, or -1.
+int orc_get_joint_lambdas(void *wp, int type, int index, double *out) {
+    World &w = *(World *)wp;
+    auto put3 = [&](int k, V3 a) {
+        out[k] = a.x;
+        out[k + 1] = a.y;
+        out[k + 2] = a.z;
+    };
+    switch (type) {
+    case JT_POINT:
+        if (index < 0 || index >= (int)w.points.size()) return -1;
+        put3(0, w.points[index].point.totalLambda);
+        return 3;
+    case JT_DISTANCE:
+        if (index < 0 || index >= (int)w.distances.size()) return -1;
+        out[0] = w.distances[index].axis.totalLambda;
+        return 1;
+    case JT_FIXED:
+        if (index < 0 || index >= (int)w.fixeds.size()) return -1;
+        put3(0, w.fixeds[index].point.totalLambda);
+        put3(3, w.fixeds[index].rot.totalLambda);
+        return 6;
+    case JT_CONE:
+        if (index < 0 || index >= (int)w.cones.size()) return -1;
+        put3(0, w.cones[index].point.totalLambda);
+        out[3] = w.cones[index].angle.totalLambda;
+        return 4;
+    case JT_SLIDER: {
+        if (index < 0 || index >= (int)w.sliders.size()) return -1;
+        const SliderJoint &j = w.sliders[index];
+        out[0] = j.pos.totalLambda[0];
+        out[1] = j.pos.totalLambda[1];
+        put3(2, j.rot.totalLambda);
+        out[5] = j.limits.totalLambda;
+        out[6] = j.motor.totalLambda;
+        return 7;
+    }
+    default: return -1;
+    }
+}
+// getCurrentPosition slider-constraint.ts:460-476 of one slider, or NaN
+double orc_slider_position(void *wp, int index) {
+    World &w = *(World *)wp;
+    if (index < 0 || index >= (int)w.sliders.size()) return 0.0 / 0.0;
+    const SliderJoint &j = w.sliders[index];
+    const Body &A = w.bodies[j.a], &B = w.bodies[j.b];
+    V3 u = sub(add(sub(B.com, A.com), rotate(B.quat, j.lp2)), rotate(A.quat, j.lp1));
+    return dot(u, rotate(A.quat, j.lSlider1));
+}
+
 // Contact events of the last step, 3 int64 per event (type, body index A, body index B); returns the count.
 int orc_get_events(void *wp, int64_t *out, int cap) {
     const World &w = *(World *)wp;

@@ -1,6 +1,7 @@
-// Data of crashcat's hinge joint and its constraint parts (TEST INFRASTRUCTURE: the parity
-// oracle): src/constraints/hinge-constraint.ts, constraint-part/{point,hinge-rotation,angle,
-// spring}-*.ts.  Included by oracle.cpp inside namespace orc, before the World; the functions
+// Data of crashcat's user joints and their constraint parts (TEST INFRASTRUCTURE: the parity
+// oracle): src/constraints/{point,distance,hinge,slider,fixed,cone,swing-twist}-constraint.ts,
+// constraint-part/{point,hinge-rotation,angle,rotation-euler,dual-axis,swing-twist,spring}-*.ts.
+// Included by oracle.cpp inside namespace orc, before the World; the functions
 // are in oracle_joints.h.
 #pragma once
 
@@ -108,4 +109,79 @@ struct SwingTwistJoint {
     PointPart point;
     SwingTwistPart st;
     AnglePart motor[3];  // twist, swing Y, swing Z
+};
+
+// RotationEulerConstraintPart rotation-euler-constraint-part.ts (3 rotational rows)
+struct EulerPart {
+    M3 invI1, invI2, effMass;
+    V3 totalLambda{0, 0, 0};
+};
+
+// DualAxisConstraintPart dual-axis-constraint-part.ts (2 translational rows); effMass as
+// mathcat's column-major mat2: [m00, m10, m01, m11]
+struct DualAxisPart {
+    V3 r1xn1{0, 0, 0}, r1xn2{0, 0, 0}, r2xn1{0, 0, 0}, r2xn2{0, 0, 0};
+    V3 i1n1{0, 0, 0}, i1n2{0, 0, 0}, i2n1{0, 0, 0}, i2n2{0, 0, 0};
+    double eff[4] = {0, 0, 0, 0};
+    double totalLambda[2] = {0, 0};
+};
+
+// fields every joint type carries (constraints.ts makeConstraintBase)
+struct JointBase {
+    int a = 0, b = 0;
+    int priority = 0, index = 0;
+    int velOverride = 0, posOverride = 0;
+    bool enabled = true;
+};
+
+// PointConstraint point-constraint.ts:21-26
+struct PointJoint : JointBase {
+    V3 lp1, lp2;
+    PointPart point;
+};
+
+// FixedConstraint fixed-constraint.ts:28-46
+struct FixedJoint : JointBase {
+    V3 lp1, lp2;
+    Q4 invInitial{0, 0, 0, 1};
+    PointPart point;
+    EulerPart rot;
+};
+
+// DistanceConstraint distance-constraint.ts:24-49
+struct DistanceJoint : JointBase {
+    V3 lp1, lp2;
+    double minDistance = 0, maxDistance = 0;
+    SpringSettings spring;
+    V3 wp1{0, 0, 0}, wp2{0, 0, 0}, wn{0, 1, 0};
+    double minLambda = 0, maxLambda = 0;
+    AxisPart axis;
+};
+
+// ConeConstraint cone-constraint.ts:24-46
+struct ConeJoint : JointBase {
+    V3 lp1, lp2, lt1{1, 0, 0}, lt2{1, 0, 0};
+    double cosHalfCone = 1;
+    V3 wRotAxis{0, 1, 0};
+    double cosTheta = 1;
+    PointPart point;
+    AnglePart angle;
+};
+
+// SliderConstraint slider-constraint.ts:56-101 (motor settings: motor-settings.ts:37-51)
+struct SliderJoint : JointBase {
+    V3 lp1, lp2, lSlider1, lNormal1, lNormal2;
+    Q4 invInitial{0, 0, 0, 1};
+    V3 r1{0, 0, 0}, r2{0, 0, 0}, u{0, 0, 0}, wSlider{0, 0, 0}, n1{0, 0, 0}, n2{0, 0, 0};
+    double d = 0;
+    bool hasLimits = false;
+    double limitsMin = -1.0 / 0.0, limitsMax = 1.0 / 0.0;
+    SpringSettings limitsSpring;
+    int motorState = MOTOR_OFF;
+    double targetVelocity = 0, targetPosition = 0, maxFrictionForce = 0;
+    SpringSettings motorSpring{FREQUENCY_AND_DAMPING, 2.0, 1.0};
+    double minForceLimit = -1.0 / 0.0, maxForceLimit = 1.0 / 0.0;
+    DualAxisPart pos;
+    EulerPart rot;
+    AxisPart limits, motor;
 };

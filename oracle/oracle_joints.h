@@ -880,3 +880,449 @@ inline bool swing_solve_position(SwingTwistJoint &j, Body &A, Body &B, double ba
     imp = point_solve_position(j.point, A, B, baumgarte) || imp;
     return imp;
 }
+
+// ---- RotationEulerConstraintPart (rotation-euler-constraint-part.ts) -----------------
+inline void euler_deactivate(EulerPart &p) {  // deactivate :49-52
+    p.effMass = m3_zero();
+    p.totalLambda = {0, 0, 0};
+}
+// getInvInitialOrientationXY :71-111; vec3.equals is mathcat's (gl-matrix's) approximate
+// comparison, |a - b| <= 1e-6 max(1, |a|, |b|) per component
+inline bool vec3_equals(V3 a, V3 b) {
+    auto eq = [](double x, double y) {
+        return std::fabs(x - y) <= 1e-6 * std::max(1.0, std::max(std::fabs(x), std::fabs(y)));
+    };
+    return eq(a.x, b.x) && eq(a.y, b.y) && eq(a.z, b.z);
+}
+inline Q4 axes_to_quat(V3 x, V3 y) {  // quat.fromMat3 of the columns (x, y, x cross y)
+    V3 z = cross(x, y);
+    M3 m;
+    V3 c[3] = {x, y, z};
+    for (int k = 0; k < 3; k++) {
+        m.m[k][0] = c[k].x;
+        m.m[k][1] = c[k].y;
+        m.m[k][2] = c[k].z;
+    }
+    return quat_from_m3(m);
+}
+inline Q4 inv_initial_orientation_xy(V3 x1, V3 y1, V3 x2, V3 y2) {
+    if (vec3_equals(x1, x2) && vec3_equals(y1, y2)) return {0, 0, 0, 1};
+    return qmul(axes_to_quat(x2, y2), qconj(axes_to_quat(x1, y1)));
+}
+// calculateConstraintProperties :127-156
+inline void euler_calc(EulerPart &p, const Body &A, const Body &B) {
+    p.invI1 = world_inv_inertia(A);
+    p.invI2 = world_inv_inertia(B);
+    if (!m3_invert(p.effMass, m3_add(p.invI1, p.invI2))) euler_deactivate(p);
+}
+// applyVelocityStep :226-247
+inline bool euler_apply(EulerPart &p, Body &A, Body &B, V3 l) {
+    if (lensq(l) == 0) return false;
+    if (A.motion == DYNAMIC) A.angvel = sub(A.angvel, m3_mul(p.invI1, l));
+    if (B.motion == DYNAMIC) B.angvel = add(B.angvel, m3_mul(p.invI2, l));
+    return true;
+}
+inline void euler_warm(EulerPart &p, Body &A, Body &B, double ratio) {  // warmStart :158-169
+    p.totalLambda = scale(p.totalLambda, ratio);
+    euler_apply(p, A, B, p.totalLambda);
+}
+inline bool euler_solve_velocity(EulerPart &p, Body &A, Body &B) {  // solveVelocityConstraint :176-213
+    V3 w1 = A.motion != STATIC ? A.angvel : V3{0, 0, 0};
+    V3 w2 = B.motion != STATIC ? B.angvel : V3{0, 0, 0};
+    V3 l = m3_mul(p.effMass, sub(w1, w2));
+    p.totalLambda = add(p.totalLambda, l);
+    return euler_apply(p, A, B, l);
+}
+// solvePositionConstraint :256-311: error = 2 xyz of q2 invInitial q1^-1 (w made positive)
+inline bool euler_solve_position(EulerPart &p, Body &A, Body &B, Q4 invInitial, double baumgarte) {
+    Q4 diff = qmul(qmul(B.quat, invInitial), qconj(A.quat));
+    if (diff.w < 0) diff = {-diff.x, -diff.y, -diff.z, -diff.w};
+    V3 err{2 * diff.x, 2 * diff.y, 2 * diff.z};
+    if (lensq(err) < 1e-12) return false;
+    V3 l = scale(m3_mul(p.effMass, err), -baumgarte);
+    if (A.motion == DYNAMIC) sub_rotation_step(A, m3_mul(p.invI1, l));
+    if (B.motion == DYNAMIC) add_rotation_step(B, m3_mul(p.invI2, l));
+    return true;
+}
+
+// ---- AxisConstraintPart with a spring, and its position solve ------------------------
+inline M4 world_inv_inertia4(const Body &b) {
+    M4 r{};
+    if (b.motion == DYNAMIC) r = inv_inertia_for_rotation(b, mat4_from_quat(b.quat));
+    return r;
+}
+inline double dyn_inv_mass(const Body &b) { return b.motion == DYNAMIC ? b.invMass : 0.0; }
+// calculateConstraintPropertiesWithSettings axis-constraint-part.ts:400-440
+inline void axis_calc_settings(AxisPart &p, double dt, const Body &A, const Body &B, V3 r1, V3 r2, V3 ax, double bias,
+                               double C, const SpringSettings &s) {
+    double iem = inv_eff_mass(p, A, B, dyn_inv_mass(A), dyn_inv_mass(B), world_inv_inertia4(A),
+                              world_inv_inertia4(B), r1, r2, ax);
+    if (iem == 0) {
+        p.effMass = 0;
+        p.totalLambda = 0;
+        return;
+    }
+    SpringPart sp;
+    p.effMass = spring_with_settings(sp, dt, iem, bias, C, s);
+    p.softness = sp.softness;
+    p.bias = sp.bias;
+}
+inline void axis_calc(AxisPart &p, const Body &A, const Body &B, V3 r1, V3 r2, V3 ax, double bias) {
+    calc_props(p, A, B, dyn_inv_mass(A), dyn_inv_mass(B), world_inv_inertia4(A), world_inv_inertia4(B), r1, r2, ax,
+               bias);
+}
+inline void axis_deactivate(AxisPart &p) {
+    p.effMass = 0;
+    p.totalLambda = 0;
+}
+// solveVelocityConstraint :557-570 (getTotalLambda, clamp, applyLambda)
+inline bool axis_solve_velocity(AxisPart &p, Body &A, Body &B, V3 ax, double mn, double mx) {
+    double tl = total_lambda(p, A, B, ax);
+    return apply_lambda(p, A, B, dyn_inv_mass(A), dyn_inv_mass(B), ax, std::max(mn, std::min(mx, tl)));
+}
+// solvePositionConstraintWithMassOverride :790-847
+inline bool axis_solve_position(AxisPart &p, Body &A, Body &B, V3 ax, double C, double baumgarte) {
+    if (C == 0 || p.effMass == 0 || p.softness != 0) return false;
+    double l = -p.effMass * baumgarte * C;
+    if (A.motion == DYNAMIC) {
+        A.com = sub(A.com, scale(ax, l * A.invMass));
+        apply_dof_pos(A);
+        sub_rotation_step(A, scale(p.invI1, l));
+    }
+    if (B.motion == DYNAMIC) {
+        B.com = add(B.com, scale(ax, l * B.invMass));
+        apply_dof_pos(B);
+        add_rotation_step(B, scale(p.invI2, l));
+    }
+    return true;
+}
+
+// ---- DualAxisConstraintPart (dual-axis-constraint-part.ts) ---------------------------
+inline void dual_deactivate(DualAxisPart &p) {
+    p.totalLambda[0] = p.totalLambda[1] = 0;
+    for (double &e : p.eff) e = 0;
+}
+inline bool dual_active(const DualAxisPart &p) { return p.eff[0] != 0 || p.eff[1] != 0 || p.eff[2] != 0 || p.eff[3] != 0; }
+// calculateConstraintProperties :78-140 (mat2.invert: null when the determinant is 0)
+inline void dual_calc(DualAxisPart &p, const Body &A, V3 r1u, const Body &B, V3 r2, V3 n1, V3 n2) {
+    double iem[4] = {0, 0, 0, 0};
+    auto side = [&](const Body &b, V3 r, V3 &c1, V3 &c2, V3 &i1, V3 &i2) {
+        c1 = cross(r, n1);
+        c2 = cross(r, n2);
+        M3 I = world_inv_inertia(b);
+        i1 = m3_mul(I, c1);
+        i2 = m3_mul(I, c2);
+        iem[0] += b.invMass + dot(c1, i1);
+        iem[1] += dot(c2, i1);
+        iem[2] += dot(c1, i2);
+        iem[3] += b.invMass + dot(c2, i2);
+    };
+    if (A.motion == DYNAMIC) side(A, r1u, p.r1xn1, p.r1xn2, p.i1n1, p.i1n2);
+    if (B.motion == DYNAMIC) side(B, r2, p.r2xn1, p.r2xn2, p.i2n1, p.i2n2);
+    double det = iem[0] * iem[3] - iem[2] * iem[1];
+    if (det == 0) {
+        dual_deactivate(p);
+        return;
+    }
+    det = 1.0 / det;
+    p.eff[0] = iem[3] * det;
+    p.eff[1] = -iem[1] * det;
+    p.eff[2] = -iem[2] * det;
+    p.eff[3] = iem[0] * det;
+}
+inline void dual_apply(DualAxisPart &p, Body &A, Body &B, V3 n1, V3 n2, double l0, double l1) {
+    V3 imp = scale_add(scale(n1, l0), n2, l1);
+    if (A.motion == DYNAMIC) {
+        A.linvel = sub(A.linvel, scale(imp, A.invMass));
+        apply_dof_lin(A);
+        A.angvel = sub(A.angvel, scale_add(scale(p.i1n1, l0), p.i1n2, l1));
+    }
+    if (B.motion == DYNAMIC) {
+        B.linvel = add(B.linvel, scale(imp, B.invMass));
+        apply_dof_lin(B);
+        B.angvel = add(B.angvel, scale_add(scale(p.i2n1, l0), p.i2n2, l1));
+    }
+}
+inline void dual_warm(DualAxisPart &p, Body &A, Body &B, V3 n1, V3 n2, double ratio) {  // warmStart :148-186
+    if (!dual_active(p)) return;
+    p.totalLambda[0] *= ratio;
+    p.totalLambda[1] *= ratio;
+    if (p.totalLambda[0] == 0 && p.totalLambda[1] == 0) return;
+    dual_apply(p, A, B, n1, n2, p.totalLambda[0], p.totalLambda[1]);
+}
+// solveVelocityConstraint :194-267
+inline bool dual_solve_velocity(DualAxisPart &p, Body &A, Body &B, V3 n1, V3 n2) {
+    if (!dual_active(p)) return false;
+    bool mA = A.motion != STATIC, mB = B.motion != STATIC;
+    double j0 = 0, j1 = 0;
+    if (mA && mB) {
+        j0 = dot(n1, A.linvel) - dot(n1, B.linvel);
+        j1 = dot(n2, A.linvel) - dot(n2, B.linvel);
+    } else if (mA) {
+        j0 = dot(n1, A.linvel);
+        j1 = dot(n2, A.linvel);
+    } else if (mB) {
+        j0 = -dot(n1, B.linvel);
+        j1 = -dot(n2, B.linvel);
+    }
+    if (mA) {
+        j0 += dot(p.r1xn1, A.angvel);
+        j1 += dot(p.r1xn2, A.angvel);
+    }
+    if (mB) {
+        j0 -= dot(p.r2xn1, B.angvel);
+        j1 -= dot(p.r2xn2, B.angvel);
+    }
+    double l0 = p.eff[0] * j0 + p.eff[2] * j1, l1 = p.eff[1] * j0 + p.eff[3] * j1;  // vec2.transformMat2
+    p.totalLambda[0] += l0;
+    p.totalLambda[1] += l1;
+    if (l0 == 0 && l1 == 0) return false;
+    dual_apply(p, A, B, n1, n2, l0, l1);
+    return true;
+}
+// solvePositionConstraint :275-330
+inline bool dual_solve_position(DualAxisPart &p, Body &A, Body &B, V3 u, V3 n1, V3 n2, double baumgarte) {
+    if (!dual_active(p)) return false;
+    double c0 = dot(u, n1), c1 = dot(u, n2);
+    if (c0 == 0 && c1 == 0) return false;
+    double l0 = -baumgarte * (p.eff[0] * c0 + p.eff[2] * c1), l1 = -baumgarte * (p.eff[1] * c0 + p.eff[3] * c1);
+    if (l0 == 0 && l1 == 0) return false;
+    V3 imp = scale_add(scale(n1, l0), n2, l1);
+    if (A.motion == DYNAMIC) {
+        A.com = sub(A.com, scale(imp, A.invMass));
+        apply_dof_pos(A);
+        sub_rotation_step(A, scale_add(scale(p.i1n1, l0), p.i1n2, l1));
+    }
+    if (B.motion == DYNAMIC) {
+        B.com = add(B.com, scale(imp, B.invMass));
+        apply_dof_pos(B);
+        add_rotation_step(B, scale_add(scale(p.i2n1, l0), p.i2n2, l1));
+    }
+    return true;
+}
+
+// ---- PointConstraint (point-constraint.ts:186-244) -----------------------------------
+inline void pointj_setup(PointJoint &j, const Body &A, const Body &B) { point_calc(j.point, A, j.lp1, B, j.lp2); }
+inline void pointj_warm(PointJoint &j, Body &A, Body &B, double ratio) { point_warm(j.point, A, B, ratio); }
+inline bool pointj_solve_velocity(PointJoint &j, Body &A, Body &B) { return point_solve_velocity(j.point, A, B); }
+inline bool pointj_solve_position(PointJoint &j, Body &A, Body &B, double baumgarte) {
+    point_calc(j.point, A, j.lp1, B, j.lp2);
+    return point_solve_position(j.point, A, B, baumgarte);
+}
+
+// ---- FixedConstraint (fixed-constraint.ts:299-395) -----------------------------------
+inline void fixed_setup(FixedJoint &j, const Body &A, const Body &B) {
+    euler_calc(j.rot, A, B);
+    point_calc(j.point, A, j.lp1, B, j.lp2);
+}
+inline void fixed_warm(FixedJoint &j, Body &A, Body &B, double ratio) {
+    euler_warm(j.rot, A, B, ratio);
+    point_warm(j.point, A, B, ratio);
+}
+inline bool fixed_solve_velocity(FixedJoint &j, Body &A, Body &B) {
+    bool rot = euler_solve_velocity(j.rot, A, B);
+    bool pos = point_solve_velocity(j.point, A, B);
+    return rot || pos;
+}
+inline bool fixed_solve_position(FixedJoint &j, Body &A, Body &B, double baumgarte) {
+    euler_calc(j.rot, A, B);
+    bool rot = euler_solve_position(j.rot, A, B, j.invInitial, baumgarte);
+    point_calc(j.point, A, j.lp1, B, j.lp2);
+    bool pos = point_solve_position(j.point, A, B, baumgarte);
+    return rot || pos;
+}
+
+// ---- DistanceConstraint (distance-constraint.ts:270-465) -----------------------------
+// calculateDistanceConstraintProperties :270-373
+inline void distance_calc(DistanceJoint &j, const Body &A, const Body &B, double dt) {
+    j.wp1 = add(rotate(A.quat, j.lp1), A.com);
+    j.wp2 = add(rotate(B.quat, j.lp2), B.com);
+    V3 delta = sub(j.wp2, j.wp1);
+    double dl = len(delta);
+    if (dl > 0) j.wn = scale(delta, 1 / dl);
+    V3 r1u = sub(j.wp2, A.com), r2 = sub(j.wp2, B.com);
+    if (j.minDistance == j.maxDistance) {
+        axis_calc_settings(j.axis, dt, A, B, r1u, r2, j.wn, 0, dl - j.minDistance, j.spring);
+        j.minLambda = -1.0 / 0.0;
+        j.maxLambda = 1.0 / 0.0;
+    } else if (dl <= j.minDistance) {
+        axis_calc_settings(j.axis, dt, A, B, r1u, r2, j.wn, 0, dl - j.minDistance, j.spring);
+        j.minLambda = 0;
+        j.maxLambda = 1.0 / 0.0;
+    } else if (dl >= j.maxDistance) {
+        axis_calc_settings(j.axis, dt, A, B, r1u, r2, j.wn, 0, dl - j.maxDistance, j.spring);
+        j.minLambda = -1.0 / 0.0;
+        j.maxLambda = 0;
+    } else {
+        axis_deactivate(j.axis);
+    }
+}
+inline void distance_warm(DistanceJoint &j, Body &A, Body &B, double ratio) {
+    warm_start(j.axis, A, B, dyn_inv_mass(A), dyn_inv_mass(B), j.wn, ratio);
+}
+inline bool distance_solve_velocity(DistanceJoint &j, Body &A, Body &B) {
+    if (j.axis.effMass == 0) return false;
+    return axis_solve_velocity(j.axis, A, B, j.wn, j.minLambda, j.maxLambda);
+}
+// solvePosition :420-458: the error is measured on the world points of the last property
+// calculation (setup, or the previous position iteration), then the properties are refreshed
+inline bool distance_solve_position(DistanceJoint &j, Body &A, Body &B, double dt, double baumgarte) {
+    if (j.spring.frequencyOrStiffness > 0) return false;
+    double d = dot(sub(j.wp2, j.wp1), j.wn);
+    double err = 0;
+    if (d < j.minDistance)
+        err = d - j.minDistance;
+    else if (d > j.maxDistance)
+        err = d - j.maxDistance;
+    if (err == 0) return false;
+    distance_calc(j, A, B, dt);
+    return axis_solve_position(j.axis, A, B, j.wn, err, baumgarte);
+}
+
+// ---- ConeConstraint (cone-constraint.ts:321-448) -------------------------------------
+// calculateRotationConstraintProperties :321-347
+inline void cone_rot_calc(ConeJoint &j, const Body &A, const Body &B) {
+    V3 t1 = rotate(A.quat, j.lt1), t2 = rotate(B.quat, j.lt2);
+    j.cosTheta = dot(t1, t2);
+    if (j.cosTheta < j.cosHalfCone) {
+        V3 ra = cross(t2, t1);
+        double l = len(ra);
+        if (l > 1e-6) j.wRotAxis = scale(ra, 1 / l);
+        angle_calc(j.angle, A, B, j.wRotAxis, 0);
+    } else {
+        angle_deactivate(j.angle);
+    }
+}
+inline void cone_setup(ConeJoint &j, const Body &A, const Body &B) {
+    point_calc(j.point, A, j.lp1, B, j.lp2);
+    cone_rot_calc(j, A, B);
+}
+inline void cone_warm(ConeJoint &j, Body &A, Body &B, double ratio) {
+    point_warm(j.point, A, B, ratio);
+    if (angle_active(j.angle)) angle_warm(j.angle, A, B, ratio);
+}
+inline bool cone_solve_velocity(ConeJoint &j, Body &A, Body &B) {
+    bool pos = point_solve_velocity(j.point, A, B);
+    bool rot = false;
+    if (angle_active(j.angle)) rot = angle_solve_velocity(j.angle, A, B, j.wRotAxis, 0, 1.0 / 0.0);
+    return pos || rot;
+}
+inline bool cone_solve_position(ConeJoint &j, Body &A, Body &B, double baumgarte) {
+    point_calc(j.point, A, j.lp1, B, j.lp2);
+    bool pos = point_solve_position(j.point, A, B, baumgarte);
+    cone_rot_calc(j, A, B);
+    bool rot = false;
+    if (angle_active(j.angle)) rot = angle_solve_position(j.angle, A, B, j.cosTheta - j.cosHalfCone, baumgarte);
+    return pos || rot;
+}
+
+// ---- SliderConstraint (slider-constraint.ts:546-1038) --------------------------------
+inline void slider_r1r2u(SliderJoint &j, const Body &A, const Body &B) {  // calculateR1R2U :546-562
+    j.r1 = m3mul(mat4_from_quat(A.quat), j.lp1);
+    j.r2 = m3mul(mat4_from_quat(B.quat), j.lp2);
+    j.u = sub(add(sub(B.com, A.com), j.r2), j.r1);
+}
+inline void slider_axis_pos(SliderJoint &j, const Body &A) {  // calculateSlidingAxisAndPosition :564-577
+    if (j.hasLimits || j.motorState != MOTOR_OFF || j.maxFrictionForce > 0) {
+        j.wSlider = m3mul(mat4_from_quat(A.quat), j.lSlider1);
+        j.d = dot(j.u, j.wSlider);
+    }
+}
+inline void slider_pos_calc(SliderJoint &j, const Body &A, const Body &B) {  // :579-609
+    M4 RA = mat4_from_quat(A.quat);
+    j.n1 = m3mul(RA, j.lNormal1);
+    j.n2 = m3mul(RA, j.lNormal2);
+    dual_calc(j.pos, A, add(j.r1, j.u), B, j.r2, j.n1, j.n2);
+}
+inline void slider_limits_calc(SliderJoint &j, const Body &A, const Body &B, double dt) {  // :611-696
+    if (!j.hasLimits) {
+        axis_deactivate(j.limits);
+        return;
+    }
+    bool below = j.d <= j.limitsMin, above = j.d >= j.limitsMax;
+    if (below || above) {
+        double err = below ? j.d - j.limitsMin : j.d - j.limitsMax;
+        V3 r1u = add(j.r1, j.u);
+        if (j.limitsSpring.frequencyOrStiffness > 0)
+            axis_calc_settings(j.limits, dt, A, B, r1u, j.r2, j.wSlider, 0, err, j.limitsSpring);
+        else
+            axis_calc(j.limits, A, B, r1u, j.r2, j.wSlider, 0);
+    } else {
+        axis_deactivate(j.limits);
+    }
+}
+inline void slider_motor_calc(SliderJoint &j, const Body &A, const Body &B, double dt) {  // :698-785
+    V3 r1u = add(j.r1, j.u);
+    if (j.motorState == MOTOR_OFF) {
+        if (j.maxFrictionForce > 0)
+            axis_calc(j.motor, A, B, r1u, j.r2, j.wSlider, 0);
+        else
+            axis_deactivate(j.motor);
+    } else if (j.motorState == MOTOR_VELOCITY) {
+        axis_calc(j.motor, A, B, r1u, j.r2, j.wSlider, -j.targetVelocity);
+    } else if (j.motorSpring.frequencyOrStiffness > 0) {
+        axis_calc_settings(j.motor, dt, A, B, r1u, j.r2, j.wSlider, 0, j.d - j.targetPosition, j.motorSpring);
+    } else {
+        axis_deactivate(j.motor);
+    }
+}
+inline void slider_setup(SliderJoint &j, const Body &A, const Body &B, double dt) {  // setupVelocity :787-827
+    slider_r1r2u(j, A, B);
+    slider_pos_calc(j, A, B);
+    euler_calc(j.rot, A, B);
+    slider_axis_pos(j, A);
+    slider_limits_calc(j, A, B, dt);
+    slider_motor_calc(j, A, B, dt);
+}
+inline void slider_warm(SliderJoint &j, Body &A, Body &B, double ratio) {  // warmStartVelocity :829-877
+    if (j.motor.effMass != 0) warm_start(j.motor, A, B, dyn_inv_mass(A), dyn_inv_mass(B), j.wSlider, ratio);
+    dual_warm(j.pos, A, B, j.n1, j.n2, ratio);
+    euler_warm(j.rot, A, B, ratio);
+    if (j.limits.effMass != 0) warm_start(j.limits, A, B, dyn_inv_mass(A), dyn_inv_mass(B), j.wSlider, ratio);
+}
+inline bool slider_solve_velocity(SliderJoint &j, Body &A, Body &B, double dt) {  // solveVelocity :879-958
+    bool motor = false, limit = false;
+    if (j.motor.effMass != 0) {
+        if (j.motorState == MOTOR_OFF) {
+            double ml = j.maxFrictionForce * dt;
+            motor = axis_solve_velocity(j.motor, A, B, j.wSlider, -ml, ml);
+        } else {
+            motor = axis_solve_velocity(j.motor, A, B, j.wSlider, dt * j.minForceLimit, dt * j.maxForceLimit);
+        }
+    }
+    bool pos = dual_solve_velocity(j.pos, A, B, j.n1, j.n2);
+    bool rot = euler_solve_velocity(j.rot, A, B);
+    if (j.limits.effMass != 0) {
+        double mn, mx;
+        if (j.limitsMin == j.limitsMax) {
+            mn = -1.0 / 0.0;
+            mx = 1.0 / 0.0;
+        } else if (j.d <= j.limitsMin) {
+            mn = 0;
+            mx = 1.0 / 0.0;
+        } else {
+            mn = -1.0 / 0.0;
+            mx = 0;
+        }
+        limit = axis_solve_velocity(j.limits, A, B, j.wSlider, mn, mx);
+    }
+    return motor || pos || rot || limit;
+}
+inline bool slider_solve_position(SliderJoint &j, Body &A, Body &B, double dt, double baumgarte) {  // :960-1038
+    slider_r1r2u(j, A, B);
+    slider_pos_calc(j, A, B);
+    bool pos = dual_solve_position(j.pos, A, B, j.u, j.n1, j.n2, baumgarte);
+    euler_calc(j.rot, A, B);
+    bool rot = euler_solve_position(j.rot, A, B, j.invInitial, baumgarte);
+    bool limit = false;
+    if (j.hasLimits && !(j.limitsSpring.frequencyOrStiffness > 0)) {
+        slider_r1r2u(j, A, B);
+        slider_axis_pos(j, A);
+        slider_limits_calc(j, A, B, dt);
+        if (j.limits.effMass != 0) {
+            double err = j.d <= j.limitsMin ? j.d - j.limitsMin : j.d - j.limitsMax;
+            limit = axis_solve_position(j.limits, A, B, j.wSlider, err, baumgarte);
+        }
+    }
+    return pos || rot || limit;
+}

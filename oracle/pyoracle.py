@@ -65,6 +65,9 @@ def load():
         "orc_add_hinge": ([vp, dp], i32),
         "orc_set_skip_joint_pairs": ([vp, i32], None),
         "orc_add_swing_twist": ([vp, dp], i32),
+        "orc_add_joint": ([vp, i32, dp], i32),
+        "orc_get_joint_lambdas": ([vp, i32, i32, dp], i32),
+        "orc_slider_position": ([vp, i32], C.c_double),
         "orc_add_hull": ([vp, i32, dp, dp, i32, C.c_void_p, i32, C.c_void_p, dp, dp], i32),
         "orc_set_record_tape": ([vp, i32], None),
         "orc_get_island_iterations": ([vp, ip], None),
@@ -333,6 +336,59 @@ class OracleWorld:
         k = self.lib.orc_add_swing_twist(self.h, dptr(d))
         assert k >= 0
         return k
+
+    def add_joint_record(self, joint_type: int, h) -> int:
+        """Point, distance, fixed, cone or slider joint from a record of the C description
+        (crashcat_gb300._lib.JOINT_DTYPES; fields by name) in the orc_add_joint layout."""
+        d = np.zeros(40, dtype=np.float64)
+        d[0], d[1], d[2] = h["body_a"], h["body_b"], h["space"]
+        d[3], d[4], d[5], d[6] = (h["priority"], h["num_velocity_steps_override"], h["num_position_steps_override"],
+                                  h["enabled"])
+
+        def put(k, fields):
+            for f in fields:
+                d[k:k + 3] = h[f]
+                k += 3
+            return k
+
+        def spring(k, f):
+            d[k:k + 3] = (h[f]["mode"], h[f]["frequency_or_stiffness"], h[f]["damping"])
+
+        if joint_type == 0:  # point
+            put(7, ("point_a", "point_b"))
+        elif joint_type == 1:  # distance
+            put(7, ("point_a", "point_b"))
+            d[13], d[14] = h["min_distance"], h["max_distance"]
+            spring(15, "spring")
+        elif joint_type == 4:  # fixed
+            d[7] = h["auto_detect_point"]
+            put(8, ("point_a", "point_b", "axis_x_a", "axis_y_a", "axis_x_b", "axis_y_b"))
+        elif joint_type == 5:  # cone
+            put(7, ("point_a", "point_b", "twist_axis_a", "twist_axis_b"))
+            d[19] = h["half_cone_angle"]
+        elif joint_type == 3:  # slider
+            d[7] = h["auto_detect_point"]
+            put(8, ("point_a", "point_b", "slider_axis_a", "slider_axis_b", "normal_axis_a", "normal_axis_b"))
+            d[26], d[27] = h["limits_min"], h["limits_max"]
+            spring(28, "limits_spring")
+            d[31] = h["max_friction_force"]
+            spring(32, "motor_spring")
+            d[35], d[36] = h["min_force_limit"], h["max_force_limit"]
+            d[37], d[38], d[39] = h["motor_state"], h["target_velocity"], h["target_position"]
+        else:
+            raise ValueError(f"joint type {joint_type}")
+        k = self.lib.orc_add_joint(self.h, int(joint_type), dptr(d))
+        assert k >= 0
+        return k
+
+    def joint_lambdas(self, joint_type: int, index: int) -> np.ndarray:
+        out = np.zeros(8, dtype=np.float64)
+        n = self.lib.orc_get_joint_lambdas(self.h, int(joint_type), int(index), dptr(out))
+        assert n >= 0
+        return out[:n]
+
+    def slider_position(self, index: int) -> float:
+        return float(self.lib.orc_slider_position(self.h, int(index)))
 
     def set_skip_joint_pairs(self, on: bool) -> None:
         self.lib.orc_set_skip_joint_pairs(self.h, 1 if on else 0)
