@@ -26,6 +26,9 @@ SHAPE_BOX = 1
 SHAPE_CAPSULE = 2
 SHAPE_CONVEX_HULL = 3
 SHAPE_TRIANGLE_MESH = 4
+SHAPE_CYLINDER = 5
+SHAPE_PLANE = 6
+SHAPE_EMPTY = 7
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 COMBINE_AVERAGE, COMBINE_MULTIPLY, COMBINE_MIN, COMBINE_MAX, COMBINE_GEOMETRIC_MEAN = 0, 1, 2, 3, 4
 MAX_LAYERS = 32
@@ -136,7 +139,11 @@ BODY_DTYPE = np.dtype([
     ("collision_groups", np.uint32), ("collision_mask", np.uint32), ("allowed_dofs", np.int32),
     ("motion_quality", np.int32),
     ("num_velocity_steps_override", np.int32), ("num_position_steps_override", np.int32),
+    ("shape_scale", np.float32, 3), ("shape_position", np.float32, 3), ("shape_quaternion", np.float32, 4),
+    ("com_offset", np.float32, 3),
+    ("mass_properties_mode", np.int32), ("mass", np.float32), ("inertia", np.float32, 6),
 ])
+MASS_FROM_SHAPE, MASS_GIVEN, MASS_AND_INERTIA_GIVEN = 0, 1, 2
 MOTION_DISCRETE, MOTION_LINEAR_CAST = 0, 1
 
 # cc_world_step_taped: the rows of one step's velocity solve (cc_tape_body / cc_tape_contact)

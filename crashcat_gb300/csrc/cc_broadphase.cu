@@ -123,7 +123,16 @@ __device__ void exact_aabb(float4 p4, float4 q4, const double lo[3], const doubl
 }
 
 // local bounds of the shape in FP64 (box.ts:77-84, sphere.ts, capsule.ts:84-94)
-__device__ __forceinline__ void shape_bounds(const DevWorld &w, uint32_t f, float4 sp, double lo[3], double hi[3]) {
+__device__ __forceinline__ void shape_bounds(const DevWorld &w, int i, uint32_t f, float4 sp, double lo[3],
+                                             double hi[3]) {
+    if (f & F_DECORATED) {  // the decorated shape's bounds (computeTransformedLocalBounds transformed.ts)
+        const DevFrame &d = w.frames[i];
+        for (int k = 0; k < 3; k++) {
+            lo[k] = d.lo[k];
+            hi[k] = d.hi[k];
+        }
+        return;
+    }
     int s = shape_of(f);
     if (s == SHAPE_MESH) {  // the mesh's root node bounds (triangle-mesh.ts:124-130)
         const DevMesh &m = w.meshes[mesh_of(sp)];
@@ -153,6 +162,9 @@ __device__ __forceinline__ void shape_bounds(const DevWorld &w, uint32_t f, floa
     } else if (s == SHAPE_CAPSULE) {
         ex = ez = sp.x;
         ey = da((double)sp.y, (double)sp.x);  // half height + radius
+    } else if (s == SHAPE_CYLINDER) {  // cylinder.ts calculateAABB
+        ex = ez = sp.y;
+        ey = sp.x;
     } else {
         ex = ey = ez = sp.x;
     }
@@ -180,7 +192,7 @@ __global__ void k_update_bounds(DevWorld w, unsigned int *scene) {
         uint32_t f = w.flags[i];
         if (motion_of(f) != STATIC && !sleeping_of(f)) awake++;
         double lo[3], hi[3];
-        shape_bounds(w, f, w.shape[i], lo, hi);
+        shape_bounds(w, i, f, w.shape[i], lo, hi);
         double b[6];
         exact_aabb(w.pos[i], w.quat[i], lo, hi, b);
         double *o = w.aabb64 + (size_t)i * 6;
@@ -460,11 +472,11 @@ __global__ void k_ccd_prepare(DevWorld w, float dt) {
         const bool cast = w.ccd_flag[i] != 0;
         const float4 sp = w.shape[i];
         if (motion_of(f) != STATIC && !sleeping_of(f) && !cast) {
-            float3 p = xyz(w.com[i]) - qrot(w.quat[i], shape_com(w, f, sp));
+            float3 p = xyz(w.com[i]) - qrot(w.quat[i], shape_com(w, i, f, sp));
             w.pos[i] = make_float4(p.x, p.y, p.z, 0.f);
         }
         double lo[3], hi[3], b[6];
-        shape_bounds(w, f, sp, lo, hi);
+        shape_bounds(w, i, f, sp, lo, hi);
         exact_aabb(w.pos[i], w.quat[i], lo, hi, b);
         double *o = w.aabb64 + (size_t)i * 6;
         for (int k = 0; k < 6; k++) o[k] = b[k];
@@ -472,7 +484,7 @@ __global__ void k_ccd_prepare(DevWorld w, float dt) {
         w.aabb_hi[i] = make_float4(__double2float_ru(b[3]), __double2float_ru(b[4]), __double2float_ru(b[5]), 0.f);
         w.ccd_index[i] = cast ? w.ccd_slot[i] : -1;
         if (!cast) continue;
-        const float inner = shape_inner_radius(w, f, sp);
+        const float inner = shape_inner_radius(w, i, f, sp);
         const float thr = c_settings.ccd_threshold * inner;
         const float3 d = xyz(w.linvel[i]) * dt;
         CcdRec r;

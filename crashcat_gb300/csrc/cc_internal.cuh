@@ -28,6 +28,7 @@ enum : uint32_t {
     F_RCOMB_SHIFT = 18,          // bits 18-20 restitution combine mode
     F_LAYER_SHIFT = 21,          // bits 21-25 object layer
     F_LINEAR_CAST = 1u << 26,    // MotionQuality.LINEAR_CAST
+    F_DECORATED = 1u << 27,      // the shape has decorators (DevWorld::frames)
 };
 __host__ __device__ inline int motion_of(uint32_t f) { return (int)(f & F_MOTION_MASK); }
 __host__ __device__ inline int shape_of(uint32_t f) { return (int)((f >> F_SHAPE_SHIFT) & 7u); }
@@ -36,7 +37,8 @@ __host__ __device__ inline int layer_of(uint32_t f) { return (int)((f >> F_LAYER
 __host__ __device__ inline bool sleeping_of(uint32_t f) { return (f & F_SLEEPING) != 0; }
 
 constexpr int STATIC = 0, KINEMATIC = 1, DYNAMIC = 2;
-constexpr int SHAPE_SPHERE = 0, SHAPE_BOX = 1, SHAPE_CAPSULE = 2, SHAPE_HULL = 3, SHAPE_MESH = 4;
+constexpr int SHAPE_SPHERE = 0, SHAPE_BOX = 1, SHAPE_CAPSULE = 2, SHAPE_HULL = 3, SHAPE_MESH = 4, SHAPE_CYLINDER = 5,
+              SHAPE_PLANE = 6, SHAPE_EMPTY = 7;  // an empty shape (empty-shape.ts) collides with nothing
 
 // Per-step overflow flags (status bits in DevCounters::overflow)
 enum : int { OVF_PAIRS = 1, OVF_MANIFOLDS = 2, OVF_EPA = 4, OVF_ISLAND = 8, OVF_CACHE = 16, OVF_SLOTS = 32,
@@ -202,6 +204,17 @@ struct DevHull {
     float convex_radius, inner_radius, pad0, pad1;
     float4 com;     // centre of mass in the input frame (xyz)
     float4 lo, hi;  // bounds of the points (xyz)
+};
+
+// Shape decorators of one body (src/shapes/scaled.ts, transformed.ts, offset-center-of-mass.ts),
+// nested as OffsetCenterOfMass(Transformed(Scaled(leaf))): the scale is baked into the leaf's
+// shape record; the collision geometry is the leaf at (t_pos, t_rot) in the body frame; com,
+// the inner radius and the local bounds are the decorated shape's.
+struct DevFrame {
+    float4 t_pos;         // TransformedShape.position (xyz) | getInnerRadius of the decorated shape (w)
+    float4 t_rot;         // TransformedShape.quaternion
+    float4 com;           // centre of mass of the decorated shape in the body frame (xyz)
+    double lo[3], hi[3];  // local bounds of the decorated shape
 };
 
 // Triangle mesh shape (src/shapes/triangle-mesh.ts, utils/triangle-mesh-data.ts and
@@ -439,6 +452,7 @@ struct DevWorld {
     int *contact_event;               // per manifold: 1 added, 2 persisted (listener.ts:58-79)
     unsigned long long *removed_keys;  // pairs in contact last step but not this step
     int *mid_list;    // islands solved by one warp each
+    DevFrame *frames;  // per body: shape decorators (allocated with the first decorated body)
     // hinge joints and their island lists
     DevHinge *hinges;
     int num_hinges, max_hinges;
@@ -513,18 +527,24 @@ __host__ __device__ inline int hull_of(float4 sp) {
     return v;
 #endif
 }
-// the shape's centre of mass in the body frame (zero for every shape but the hull)
-__device__ inline float3 shape_com(const DevWorld &w, uint32_t f, float4 sp) {
+// body i's shape's centre of mass in the body frame (zero for the undecorated shapes but the hull)
+__device__ inline float3 shape_com(const DevWorld &w, int i, uint32_t f, float4 sp) {
+    if (f & F_DECORATED) {
+        const float4 c = w.frames[i].com;
+        return make_float3(c.x, c.y, c.z);
+    }
     if (shape_of(f) != SHAPE_HULL) return make_float3(0.f, 0.f, 0.f);
     float4 c = w.hulls[hull_of(sp)].com;
     return make_float3(c.x, c.y, c.z);
 }
 
-// getInnerRadius box.ts:333-335, sphere.ts:147-149, capsule.ts:254-256, convex-hull.ts:549-558
-__device__ inline float shape_inner_radius(const DevWorld &w, uint32_t f, float4 sp) {
+// getInnerRadius box.ts:333-335, sphere.ts:147-149, capsule.ts:254-256, convex-hull.ts:549-558, cylinder.ts
+__device__ inline float shape_inner_radius(const DevWorld &w, int i, uint32_t f, float4 sp) {
+    if (f & F_DECORATED) return w.frames[i].t_pos.w;  // scaled.ts getInnerRadius: min|s| x the leaf's
     int s = shape_of(f);
     if (s == SHAPE_BOX) return fminf(sp.x, fminf(sp.y, sp.z));
     if (s == SHAPE_HULL) return w.hulls[hull_of(sp)].inner_radius;
+    if (s == SHAPE_CYLINDER) return fminf(sp.x, sp.y);  // cylinder.ts getInnerRadius
     return sp.x;  // sphere and capsule radius
 }
 
@@ -593,6 +613,17 @@ __host__ __device__ inline float3 qrot_inv(float4 q, float3 v) { return qrot(mak
 __host__ __device__ inline float4 qmul(float4 a, float4 b) {
     return make_float4(a.x * b.w + a.w * b.x + a.y * b.z - a.z * b.y, a.y * b.w + a.w * b.y + a.z * b.x - a.x * b.z,
                        a.z * b.w + a.w * b.z + a.x * b.y - a.y * b.x, a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z);
+}
+// the pose of body i's collision geometry: the body's, composed with TransformedShape's
+// (collideTransformedVsShape transformed.ts passes the inner shape pos + q t, q r)
+__device__ __forceinline__ void geom_pose(const DevWorld &w, int i, uint32_t f, float3 &p, float4 &q) {
+    p = make_float3(w.pos[i].x, w.pos[i].y, w.pos[i].z);
+    q = w.quat[i];
+    if (f & F_DECORATED) {
+        const DevFrame &d = w.frames[i];
+        p = p + qrot(q, make_float3(d.t_pos.x, d.t_pos.y, d.t_pos.z));
+        q = qmul(q, d.t_rot);
+    }
 }
 __device__ inline float4 qnormalize(float4 q) {
     float l = q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w;

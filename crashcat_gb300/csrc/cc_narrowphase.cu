@@ -110,7 +110,7 @@ __device__ __forceinline__ Q<S> qmulS(Q<S> a, Q<S> b) {
 // support functions
 // ---------------------------------------------------------------------------
 enum { SUP_BOX = 0, SUP_POINT = 1, SUP_SPHERE = 2, SUP_CAPSULE_SEGMENT = 3, SUP_CAPSULE_SURFACE = 4, SUP_HULL = 5,
-       SUP_TRIANGLE = 6 };
+       SUP_TRIANGLE = 6, SUP_CYLINDER = 7 };
 // the world's convex hull arrays, as the support functions read them
 struct HullView {
     const DevHull *hulls;
@@ -155,6 +155,16 @@ struct Sup {
             return d2 > d3 ? r1 : r2;
         }
         if (kind == SUP_POINT) return {S(0), S(0), S(0)};
+        if (kind == SUP_CYLINDER) {  // cylinder{No,With}ConvexGetSupport cylinder.ts
+            const S hl = sq_root(d.x * d.x + d.z * d.z);
+            V<S> o{S(0), d.y >= S(0) ? he.y : -he.y, S(0)};
+            if (hl > S(0)) {
+                const S sc = radius / hl;
+                o.x = d.x * sc;
+                o.z = d.z * sc;
+            }
+            return o;
+        }
         // capsule: segment +-h on Y (capsuleNoConvexGetSupport capsule.ts:268-275)
         if (kind == SUP_CAPSULE_SEGMENT) return {S(0), d.y > S(0) ? he.y : -he.y, S(0)};
         S l = lsq(d);
@@ -217,6 +227,18 @@ __device__ Sup<S, H, T> make_sup(int shape, float4 sp, bool exclude, const HullV
             o.convex_radius = cr;
         } else {
             o.he = {S(sp.x), S(sp.y), S(sp.z)};
+            o.convex_radius = S(0);
+        }
+    } else if (shape == SHAPE_CYLINDER) {
+        // getCylinderSupportFunction cylinder.ts (half height sp.x, radius sp.y, convex radius sp.z)
+        o.kind = SUP_CYLINDER;
+        if (exclude) {
+            o.he = {S(0), S(sp.x) - S(sp.z), S(0)};
+            o.radius = S(sp.y) - S(sp.z);
+            o.convex_radius = S(sp.z);
+        } else {
+            o.he = {S(0), S(sp.x), S(0)};
+            o.radius = S(sp.y);
             o.convex_radius = S(0);
         }
     } else if (shape == SHAPE_CAPSULE) {
@@ -687,6 +709,34 @@ __device__ void box_face(FaceN<N> &f, float3 dir, float4 he4, float4 q, float3 t
 // capsule getSupportingFace capsule.ts:192-251: the segment on the side opposite to dir
 // (body space) when both caps project within the capsule projection slop, else no face;
 // rotated by q and moved by t
+// cylinder getSupportingFace cylinder.ts (half height sp.x, radius sp.y): the side edge facing
+// away from d, or the cap octagon (CYLINDER_CAP_OCTAGON) turned towards d's horizontal part
+template <int N>
+__device__ void cylinder_face(FaceN<N> &f, float3 d, float4 sp, float4 q, float3 t) {
+    const float OCTX[8] = {0.0f, 0.707106769f, 1.0f, 0.707106769f, 0.0f, -0.707106769f, -1.0f, -0.707106769f};
+    const float OCTZ[8] = {1.0f, 0.707106769f, 0.0f, -0.707106769f, -1.0f, -0.707106769f, 0.0f, 0.707106769f};
+    const float h = sp.x, r = sp.y;
+    const float xz = d.x * d.x + d.z * d.z, yy = d.y * d.y;
+    if (xz > yy) {
+        const float fct = -r / sqrtf(xz);
+        f.n = 2;
+        f.v[0] = qrot(q, f3(d.x * fct, h, d.z * fct)) + t;
+        f.v[1] = qrot(q, f3(d.x * fct, -h, d.z * fct)) + t;
+        return;
+    }
+    const float sx = d.y < 0.f ? r : -r, sy = d.y < 0.f ? h : -h, sz = r;
+    float c = 1.f, sn = 0.f;
+    if (xz > 0.00765427f * yy) {
+        const float hl = sqrtf(xz);
+        c = d.x / hl;
+        sn = d.z / hl;
+    }
+    f.n = 8;
+    for (int i = 0; i < 8; i++) {
+        const float x = sx * OCTX[i], z = sz * OCTZ[i];
+        f.v[i] = qrot(q, f3(x * c - z * sn, sy, x * sn + z * c)) + t;
+    }
+}
 template <int N>
 __device__ void capsule_face(FaceN<N> &f, float3 d, float4 sp, float4 q, float3 t) {
     float r = sp.x, h = sp.y;
@@ -706,6 +756,39 @@ __device__ void capsule_face(FaceN<N> &f, float3 d, float4 sp, float4 q, float3 
 
 // convex hull getSupportingFace convex-hull.ts:479-541 (unit scale): the face whose plane
 // normal is most opposed to dir, at most 16 of its vertices, rotated by q and moved by t
+// ---- plane shape (src/shapes/plane.ts): shape record (unit normal xyz, constant) --------
+// getOrthogonalBasis plane.ts:210-233
+__device__ void plane_basis(float3 n, float3 &p1, float3 &p2) {
+    p1 = cross3(n, f3(0.f, 1.f, 0.f));
+    const float l = lensq3(p1);
+    p1 = l < 1e-6f ? f3(1.f, 0.f, 0.f) : p1 * (1.f / sqrtf(l));
+    p2 = normalize3(cross3(p1, n));
+    p1 = normalize3(cross3(n, p2));
+}
+// the plane of a body at (p, q): transformPlane plane.ts:196-208
+__device__ __forceinline__ void plane_world(float4 sp, float3 p, float4 q, float3 &n, float &c) {
+    n = qrot(q, xyz(sp));
+    c = sp.w - dot3(p, n);
+}
+// getAdaptivePlaneSupportingFace plane.ts:655-706: a square on the world plane (nw, cw) centred
+// under cpos with half side |size| (the convex leaf's bounds diagonal), minus t
+template <int N>
+__device__ void plane_face(FaceN<N> &f, float3 nw, float cw, float3 cpos, float size, float3 t) {
+    const float3 center = cpos - nw * (dot3(nw, cpos) + cw);
+    float3 p1, p2;
+    plane_basis(nw, p1, p2);
+    p1 = p1 * size;
+    p2 = p2 * size;
+    f.n = 4;
+    f.v[0] = center + (p1 + p2) - t;
+    f.v[1] = center + (p1 - p2) - t;
+    f.v[2] = center - (p1 + p2) - t;
+    f.v[3] = center + (p2 - p1) - t;
+}
+__device__ float convex_bounds_size(const DevWorld &w, uint32_t f, float4 sp);
+// SupportFunctionMode.DEFAULT: box and cylinder include their convex radius, the rest exclude it
+__device__ __forceinline__ bool default_excludes(int shape) { return shape != SHAPE_BOX && shape != SHAPE_CYLINDER; }
+
 template <int N>
 __device__ void hull_face(FaceN<N> &f, float3 dir, const DevWorld &w, float4 sp, float4 q, float3 t) {
     const DevHull &h = w.hulls[hull_of(sp)];
@@ -933,9 +1016,11 @@ __device__ void manifold_faces(PtsN<N> &out, float3 cp1, float3 cp2, float3 axis
 template <int N>
 __device__ void emit_manifold(DevWorld &w, int a, int b, float3 pa, float3 pb, float3 axis, float penetration,
                               bool faces) {
-    float4 qa = w.quat[a], qb = w.quat[b];
-    float3 posA = xyz(w.pos[a]), posB = xyz(w.pos[b]);
     uint32_t fa = w.flags[a], fb = w.flags[b];
+    float3 posA, posB;
+    float4 qa, qb;
+    geom_pose(w, a, fa, posA, qa);
+    geom_pose(w, b, fb, posB, qb);
     PtsN<N> pts;
     float maxd = c_settings.spec_dist + c_settings.manifold_tol;
     float3 nrm = normalize3(axis);
@@ -953,6 +1038,22 @@ __device__ void emit_manifold(DevWorld &w, int a, int b, float3 pa, float3 pb, f
         if (shape_of(fb) == SHAPE_HULL) hull_face(fB, axB, w, w.shape[b], qb, posB - posA);
         if (shape_of(fb) == SHAPE_BOX) box_face(fB, axB, w.shape[b], qb, posB - posA);
         if (shape_of(fb) == SHAPE_CAPSULE) capsule_face(fB, axB, w.shape[b], qb, posB - posA);
+        if (shape_of(fa) == SHAPE_CYLINDER) cylinder_face(fA, -axA, w.shape[a], qa, f3(0.f, 0.f, 0.f));
+        if (shape_of(fb) == SHAPE_CYLINDER) cylinder_face(fB, axB, w.shape[b], qb, posB - posA);
+        // a plane's face is the square under the convex body, made when the convex face has
+        // vertices (collideConvexVsPlane plane.ts:588-606)
+        if (shape_of(fa) == SHAPE_PLANE && fB.n > 0) {
+            float3 nw;
+            float cw;
+            plane_world(w.shape[a], posA, qa, nw, cw);
+            plane_face(fA, nw, cw, posB, convex_bounds_size(w, fb, w.shape[b]), posA);
+        }
+        if (shape_of(fb) == SHAPE_PLANE && fA.n > 0) {
+            float3 nw;
+            float cw;
+            plane_world(w.shape[b], posB, qb, nw, cw);
+            plane_face(fB, nw, cw, posA, convex_bounds_size(w, fa, w.shape[a]), posA);
+        }
         haveFaces = fA.n >= 2 && fB.n >= 3;
     }
     if (haveFaces) {
@@ -1013,11 +1114,16 @@ __global__ void __launch_bounds__(128) k_narrowphase(DevWorld w, EpaItem *epa_it
             fb = tf;
         }
         float maxSep = ((fa | fb) & F_SENSOR) ? 0.f : c_settings.spec_dist;
-        float4 pa4 = w.pos[a], pb4 = w.pos[b];
-        float4 qa = w.quat[a], qb = w.quat[b];
+        float3 pa3, pb3;
+        float4 qa, qb;
+        geom_pose(w, a, fa, pa3, qa);
+        geom_pose(w, b, fb, pb3, qb);
+        const float4 pa4 = make_float4(pa3.x, pa3.y, pa3.z, 0.f), pb4 = make_float4(pb3.x, pb3.y, pb3.z, 0.f);
         float4 sa = w.shape[a], sb = w.shape[b];
         int sha = shape_of(fa), shb = shape_of(fb);
+        if (sha == SHAPE_EMPTY || shb == SHAPE_EMPTY) continue;  // empty-shape.ts registers no collide function
         if (sha == SHAPE_MESH || shb == SHAPE_MESH) {  // the mesh passes take these pairs
+            if (sha == SHAPE_PLANE || shb == SHAPE_PLANE) continue;  // no mesh-vs-plane function
             if (!HULLS) {
                 int k = atomicAdd(&w.ctr->num_mesh_pairs, 1);
                 if (k < w.max_pairs) w.mesh_pairs[k] = pi;
@@ -1025,6 +1131,33 @@ __global__ void __launch_bounds__(128) k_narrowphase(DevWorld w, EpaItem *epa_it
             continue;
         }
         if ((sha == SHAPE_HULL || shb == SHAPE_HULL) != HULLS) continue;
+        if (sha == SHAPE_PLANE || shb == SHAPE_PLANE) {
+            // collideConvexVsPlane plane.ts:474-629, reversed when the plane is A (the usual case:
+            // the plane is static); a plane against a plane has no collide function
+            if (sha == SHAPE_PLANE && shb == SHAPE_PLANE) continue;
+            const bool planeA = sha == SHAPE_PLANE;
+            const float3 pC = planeA ? pb3 : pa3, pP = planeA ? pa3 : pb3;
+            const float4 qC = planeA ? qb : qa, qP = planeA ? qa : qb;
+            const float4 sC = planeA ? sb : sa, sP = planeA ? sa : sb;
+            const int shC = planeA ? shb : sha;
+            // the plane in the convex body's frame
+            const float3 nl = qrot_inv(qC, qrot(qP, xyz(sP)));
+            const float cl = sP.w - dot3(qrot_inv(qC, pP - pC), nl);
+            const Sup<float, HULLS> S = make_sup<float, HULLS>(shC, sC, default_excludes(shC), hull_view(w));
+            const V<float> spv = S.get(V<float>{-nl.x, -nl.y, -nl.z});
+            const float3 sp3 = f3(spv.x, spv.y, spv.z);
+            const float sd = dot3(nl, sp3) + cl, cr = S.convex_radius;
+            const float pen = -sd + cr;
+            if (!(pen > -maxSep)) continue;
+            const float3 p1 = pC + qrot(qC, sp3 - nl * cr), p2 = pC + qrot(qC, sp3 - nl * sd);
+            const float3 ax = qrot(qC, -nl);  // from the convex body into the plane
+            // points relative to A's position; the axis from A to B
+            if (planeA)
+                emit_manifold<HULLS ? 32 : 16>(w, a, b, p2 - pa3, p1 - pa3, -ax, pen, true);
+            else
+                emit_manifold<HULLS ? 32 : 16>(w, a, b, p1 - pa3, p2 - pa3, ax, pen, true);
+            continue;
+        }
         if (sha == SHAPE_SPHERE && shb == SHAPE_SPHERE) {
             // collideSphereVsSphere sphere.ts:319-410 (no speculative distance)
             float3 d = xyz(pb4) - xyz(pa4);
@@ -1911,7 +2044,10 @@ __device__ void epa_setup(const DevWorld &w, const EpaItem &it, Sup<R, H> &A, Su
     uint32_t fa = w.flags[a], fb = w.flags[b];
     float maxSepF = ((fa | fb) & F_SENSOR) ? 0.f : c_settings.spec_dist;
     maxSep = R(maxSepF < 1.f ? maxSepF : 1.f);
-    float4 pa4 = w.pos[a], pb4 = w.pos[b], qa = w.quat[a], qb = w.quat[b];
+    float3 pa4, pb4;
+    float4 qa, qb;
+    geom_pose(w, a, fa, pa4, qa);
+    geom_pose(w, b, fb, pb4, qb);
     Q<R> iA{R(-qa.x), R(-qa.y), R(-qa.z), R(qa.w)};
     Q<R> qB{R(qb.x), R(qb.y), R(qb.z), R(qb.w)};
     Q<R> rel = qmulS(iA, qB);
@@ -1930,7 +2066,10 @@ __device__ void epa_setup_mesh(const DevWorld &w, const EpaItem &it, Sup<R> &A, 
     uint32_t fa = w.flags[a], fb = w.flags[b];
     float maxSepF = ((fa | fb) & F_SENSOR) ? 0.f : c_settings.spec_dist;
     maxSep = R(maxSepF < 1.f ? maxSepF : 1.f);
-    float4 pa4 = w.pos[a], pb4 = w.pos[b], qa = w.quat[a], qb = w.quat[b];
+    float3 pa4, pb4;
+    float4 qa, qb;
+    geom_pose(w, a, fa, pa4, qa);
+    geom_pose(w, b, fb, pb4, qb);
     Q<R> iA{R(-qa.x), R(-qa.y), R(-qa.z), R(qa.w)};
     Q<R> rel = qmulS(iA, Q<R>{R(qb.x), R(qb.y), R(qb.z), R(qb.w)});
     V<R> posBInA = qrotS(iA, V<R>{R(pb4.x) - R(pa4.x), R(pb4.y) - R(pa4.y), R(pb4.z) - R(pa4.z)});
@@ -1960,7 +2099,9 @@ __device__ void epa_finish(const DevWorld &w, EpaItem &it, bool ok, R maxSep, V<
         it.size = 0;
         return;
     }
-    float4 qa = w.quat[it.a];
+    float3 pa_unused;
+    float4 qa;
+    geom_pose(w, it.a, w.flags[it.a], pa_unused, qa);
     // mesh items keep the convex body's frame: the mesh pass fixes the normal there
     Q<R> qA = it.tri >= 0 ? Q<R>{R(0), R(0), R(0), R(1)} : Q<R>{R(qa.x), R(qa.y), R(qa.z), R(qa.w)};
     V<R> dd = pa - pb;
@@ -2331,10 +2472,19 @@ __device__ void convex_local_bounds(const DevWorld &w, uint32_t f, float4 sp, fl
     } else if (s == SHAPE_CAPSULE) {
         lo = f3(-sp.x, -(sp.y + sp.x), -sp.x);
         hi = f3(sp.x, sp.y + sp.x, sp.x);
+    } else if (s == SHAPE_CYLINDER) {
+        lo = f3(-sp.y, -sp.x, -sp.y);
+        hi = f3(sp.y, sp.x, sp.y);
     } else {
         lo = f3(-sp.x, -sp.x, -sp.x);
         hi = f3(sp.x, sp.x, sp.x);
     }
+}
+// |size| of a convex leaf's local bounds (box3.size + vec3.length, plane.ts:680-681)
+__device__ float convex_bounds_size(const DevWorld &w, uint32_t f, float4 sp) {
+    float3 lo, hi;
+    convex_local_bounds(w, f, sp, lo, hi);
+    return sqrtf(lensq3(hi - lo));
 }
 
 // One mesh pair.  PASS 0: pairs with no triangle in need of EPA are reduced and emitted; a
@@ -2365,10 +2515,12 @@ __global__ void __launch_bounds__(64) k_mesh_narrowphase(DevWorld w, EpaItem *ep
         const bool inverted = meshA;
         const int cv = inverted ? b : a, mh = inverted ? a : b;
         const uint32_t fc = inverted ? fb : fa;
-        const float3 base = xyz(w.pos[a]);
+        float3 base, pc, pm;
+        float4 qbase, qc4, qm4;
+        geom_pose(w, a, fa, base, qbase);
         const float maxSepIn = ((fa | fb) & F_SENSOR) ? 0.f : c_settings.spec_dist;
-        const float4 qc4 = w.quat[cv], qm4 = w.quat[mh];
-        const float3 pc = xyz(w.pos[cv]), pm = xyz(w.pos[mh]);
+        geom_pose(w, cv, w.flags[cv], pc, qc4);
+        geom_pose(w, mh, w.flags[mh], pm, qm4);
         const float3 cvRel = pc - base;  // the convex body's position relative to the base
         const Q<float> qC{qc4.x, qc4.y, qc4.z, qc4.w}, iqC{-qc4.x, -qc4.y, -qc4.z, qc4.w};
         const Q<float> qM{qm4.x, qm4.y, qm4.z, qm4.w}, iqM{-qm4.x, -qm4.y, -qm4.z, qm4.w};
@@ -2611,6 +2763,7 @@ __global__ void __launch_bounds__(64) k_mesh_narrowphase(DevWorld w, EpaItem *ep
                         if (s == SHAPE_BOX) box_face(fConvex, -axl, sc, qc4, cvRel);
                         if (s == SHAPE_CAPSULE) capsule_face(fConvex, -axl, sc, qc4, cvRel);
                         if (s == SHAPE_HULL) hull_face(fConvex, -axl, w, sc, qc4, cvRel);
+                        if (s == SHAPE_CYLINDER) cylinder_face(fConvex, -axl, sc, qc4, cvRel);
                         fTri.n = 3;
                         fTri.v[0] = to_base(V<float>{t0.x, t0.y, t0.z});
                         fTri.v[1] = to_base(V<float>{t1.x, t1.y, t1.z});
@@ -2813,6 +2966,35 @@ __device__ float ray_sphere_from_origin(float3 dir, float3 c, float r) {
     return CUDART_INF_F;
 }
 
+// castConvexVsPlane plane.ts:727-918 for a convex support S of the moving shape at (pA, qA)
+// (SupportFunctionMode.DEFAULT) against a plane body at (pP, qP): the plane's own equation
+// against the world support point, the hit carried by the plane body's transform, as the
+// reference computes them; back faces culled
+__device__ bool cast_vs_plane(const Sup<float> &S, float3 pA, float4 qA, float3 disp, float4 spP, float3 pP,
+                              float4 qP, float early, float &frac, float3 &paw, float3 &axw) {
+    const float3 n = xyz(spP);
+    const float3 nA = -qrot_inv(qA, n);
+    const V<float> s = S.get(V<float>{nA.x, nA.y, nA.z});
+    const float3 spw = pA + qrot(qA, f3(s.x, s.y, s.z));
+    const float sd = dot3(n, spw) + spP.w, cr = S.convex_radius, pen = -sd + cr;
+    const float dn = dot3(disp, n);
+    float3 ht = pP;
+    if (pen > 0.f) {
+        if (dn > 0.f || pen <= -early) return false;
+        frac = 0.f;
+        paw = pP + qrot(qP, spw - n * cr);
+    } else if (dn < 0.f) {
+        frac = pen / dn;
+        if (frac >= early) return false;
+        ht = pP + qrot(qP, disp * frac);
+        paw = ht + qrot(qP, spw - n * cr);
+    } else {
+        return false;
+    }
+    axw = ht + qrot(qP, -n);  // vec3.transformMat4 of -n: a point transform
+    return true;
+}
+
 // castConvexVsTriangleMesh triangle-mesh.ts:638-1019 and castSphereVsTriangleMesh :1781-2236
 // for the continuous-collision visitor (default cast settings: tolerances 0.01, support mode
 // DEFAULT, back faces culled, no movement direction, no deepest point).  collect(fraction,
@@ -2822,8 +3004,9 @@ __device__ void ccd_cast_mesh(const DevWorld &w, uint32_t fa, float4 sa, float3 
                               const float &fps, Collect &&collect) {
     const DevMesh &M = w.meshes[mesh_of(w.shape[b])];
     if (M.num_tris == 0) return;
-    const float3 pB = xyz(w.pos[b]);
-    const float4 qB4 = w.quat[b];
+    float3 pB;
+    float4 qB4;
+    geom_pose(w, b, w.flags[b], pB, qB4);
     const Q<float> qB{qB4.x, qB4.y, qB4.z, qB4.w}, iqB{-qB4.x, -qB4.y, -qB4.z, qB4.w};
     auto toB = [&](float3 v) {
         V<float> q = qrotS(iqB, V<float>{v.x, v.y, v.z});
@@ -3034,8 +3217,9 @@ __global__ void __launch_bounds__(128) k_ccd_find(DevWorld w, const int2 *node_w
         const int wa = w.world[a];
         const uint32_t allowed = c_settings.cast_pairs[layer_of(fa)];
         const uint2 ga = w.groups[a];
-        const float3 pA = xyz(w.pos[a]);
-        const float4 qA = w.quat[a];
+        float3 pA;
+        float4 qA;
+        geom_pose(w, a, fa, pA, qA);
         const Sup<float> supA0 = make_sup<float>(shape_of(fa), w.shape[a], true, hv);
         float best_fps = c.fps, best_frac = c.point.w;
         int best = -1;
@@ -3074,7 +3258,7 @@ __global__ void __launch_bounds__(128) k_ccd_find(DevWorld w, const int2 *node_w
             if (cb >= 0) rel = rel - xyz(w.ccd[cb].delta);
             if (lensq3(rel) < thr_sq) continue;
             const float3 blo = xyz(w.aabb_lo[b]) - half_a, bhi = xyz(w.aabb_hi[b]) + half_a;
-            if (!(ray_box_entry(pA, rel, sqrtf(lensq3(rel)), blo, bhi) < CUDART_INF_F)) continue;
+            if (!(ray_box_entry(xyz(w.pos[a]), rel, sqrtf(lensq3(rel)), blo, bhi) < CUDART_INF_F)) continue;
             // ccdCastShapeCollector.addHit update.ts:1044-1109
             auto collect = [&](float lambda, float3 paw, float3 axw) {
                 const float3 nrm = normalize3(axw);
@@ -3094,13 +3278,24 @@ __global__ void __launch_bounds__(128) k_ccd_find(DevWorld w, const int2 *node_w
                 }
                 best_p = pt;
             };
+            if (shape_of(fb) == SHAPE_EMPTY || shape_of(fa) == SHAPE_EMPTY) continue;
             if (shape_of(fb) == SHAPE_MESH) {
                 ccd_cast_mesh(w, fa, w.shape[a], pA, qA, rel, b, best_fps, collect);
                 continue;
             }
+            if (shape_of(fb) == SHAPE_PLANE) {
+                float3 pB, paw, axw;
+                float4 qB;
+                float frac;
+                geom_pose(w, b, fb, pB, qB);
+                const Sup<float> S = make_sup<float>(shape_of(fa), w.shape[a], default_excludes(shape_of(fa)), hv);
+                if (cast_vs_plane(S, pA, qA, rel, w.shape[b], pB, qB, best_fps, frac, paw, axw)) collect(frac, paw, axw);
+                continue;
+            }
             // castConvexVsConvex: A in B's frame
-            const float3 pB = xyz(w.pos[b]);
-            const float4 qB = w.quat[b];
+            float3 pB;
+            float4 qB;
+            geom_pose(w, b, fb, pB, qB);
             const Q<float> iqB{-qB.x, -qB.y, -qB.z, qB.w};
             const V<float> posAInB = qrotS(iqB, V<float>{pA.x - pB.x, pA.y - pB.y, pA.z - pB.z});
             const Q<float> qAInB = qmulS(iqB, Q<float>{qA.x, qA.y, qA.z, qA.w});
@@ -3295,10 +3490,30 @@ template <bool MESH>
 __device__ bool ray_vs_body(const DevWorld &w, const HullView &hv, int b, float3 o, float3 d, float len,
                             uint32_t flags, float max_f, float &fraction, uint32_t &sub) {
     const uint32_t fb = w.flags[b];
-    const float3 pB = xyz(w.pos[b]);
-    const float4 qB = w.quat[b];
+    float3 pB;
+    float4 qB;
+    geom_pose(w, b, fb, pB, qB);
     const float3 lo = qrot_inv(qB, o - pB), ld = qrot_inv(qB, d);
     if (MESH) return ray_vs_mesh(w, b, lo, ld, len, !(flags & CC_RAY_BACKFACES), max_f, fraction, sub);
+    if (shape_of(fb) == SHAPE_EMPTY) return false;
+    if (shape_of(fb) == SHAPE_PLANE) {  // castRayVsPlane plane.ts:320-398
+        float3 n;
+        float c;
+        plane_world(w.shape[b], pB, qB, n, c);
+        const float dist = dot3(n, o) + c;
+        sub = 0xffffffffu;
+        if ((flags & CC_RAY_SOLID) && dist <= 0.f && max_f > 0.f) {
+            fraction = 0.f;
+            return true;
+        }
+        const float dn = dot3(d, n);
+        if (fabsf(dn) < 1e-10f) return false;
+        if (!(flags & CC_RAY_BACKFACES) && dn > 0.f) return false;
+        const float f = -dist / dn / len;
+        if (!(f >= 0.f && f < max_f)) return false;
+        fraction = f;
+        return true;
+    }
     const Sup<float> sup = make_sup<float>(shape_of(fb), w.shape[b], false, hv);
     float lambda;
     if (!gjk_cast_ray(lambda, V<float>{lo.x, lo.y, lo.z}, V<float>{ld.x * len, ld.y * len, ld.z * len}, 1e-3f, sup,
@@ -3468,10 +3683,20 @@ __device__ bool point_in_body(const DevWorld &w, const HullView &hv, int b, floa
     sub = 0xffffffffu;
     const uint32_t fb = w.flags[b];
     const float4 sp = w.shape[b];
-    const float3 l = p - xyz(w.pos[b]);
+    float3 pB;
+    float4 qB;
+    geom_pose(w, b, fb, pB, qB);
+    const float3 l = p - pB;
     const int shape = shape_of(fb);
+    if (shape == SHAPE_EMPTY) return false;
+    if (shape == SHAPE_PLANE) {  // collidePointVsPlane plane.ts:404-460
+        float3 n;
+        float c;
+        plane_world(sp, pB, qB, n, c);
+        return dot3(n, p) + c < 0.f;
+    }
     if (shape == SHAPE_SPHERE) return lensq3(l) <= sp.x * sp.x;
-    const float3 lp = qrot_inv(w.quat[b], l);
+    const float3 lp = qrot_inv(qB, l);
     if (shape == SHAPE_BOX) return fabsf(lp.x) <= sp.x && fabsf(lp.y) <= sp.y && fabsf(lp.z) <= sp.z;
     if (shape == SHAPE_MESH) {
         const DevMesh &M = w.meshes[mesh_of(sp)];
@@ -3488,6 +3713,9 @@ __device__ bool point_in_body(const DevWorld &w, const HullView &hv, int b, floa
         const DevHull &h = hv.hulls[hull_of(sp)];
         lo = xyz(h.lo);
         hi = xyz(h.hi);
+    } else if (shape == SHAPE_CYLINDER) {  // cylinder.ts calculateAABB
+        lo = f3(-sp.y, -sp.x, -sp.y);
+        hi = f3(sp.y, sp.x, sp.y);
     } else {
         const float th = sp.y + sp.x;
         lo = f3(-sp.x, -th, -sp.x);
@@ -3663,13 +3891,25 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
                     hn = -normalize3(axw);
                     hp = paw;
                 };
+                if (shape_of(fb) == SHAPE_EMPTY) continue;
                 if (shape_of(fb) == SHAPE_MESH) {
                     if (PASS != 2) ccd_cast_mesh(w, fa, sa, pA, qA, disp, b, best, collect);
                     continue;
                 }
+                if (shape_of(fb) == SHAPE_PLANE) {
+                    if (PASS == 1) continue;
+                    float3 pB, paw, axw;
+                    float4 qB;
+                    float frac;
+                    geom_pose(w, b, fb, pB, qB);
+                    const Sup<float> S = make_sup<float>(shape, sa, default_excludes(shape), hv);
+                    if (cast_vs_plane(S, pA, qA, disp, w.shape[b], pB, qB, best, frac, paw, axw)) collect(frac, paw, axw);
+                    continue;
+                }
                 if (PASS == 1) continue;
-                const float3 pB = xyz(w.pos[b]);
-                const float4 qB = w.quat[b];
+                float3 pB;
+                float4 qB;
+                geom_pose(w, b, fb, pB, qB);
                 const Q<float> iqB{-qB.x, -qB.y, -qB.z, qB.w};
                 const V<float> posAInB = qrotS(iqB, V<float>{pA.x - pB.x, pA.y - pB.y, pA.z - pB.z});
                 const Q<float> qAInB = qmulS(iqB, Q<float>{qA.x, qA.y, qA.z, qA.w});

@@ -325,13 +325,18 @@ __global__ void k_contact_setup(DevWorld w, CacheTables ct, float dt) {
 }
 
 // sleep test points (getSleepTestPoints sleep.ts:22-74)
-__device__ void sleep_points(const DevWorld &w, uint32_t f, float4 sp, float4 q, float3 com, float3 out[3]) {
+__device__ void sleep_points(const DevWorld &w, int i, uint32_t f, float4 sp, float4 q, float3 com, float3 out[3]) {
     int sh = shape_of(f);
     float3 e = sh == SHAPE_BOX ? f3(sp.x, sp.y, sp.z)
                                : (sh == SHAPE_CAPSULE ? f3(sp.x, sp.y + sp.x, sp.x) : f3(sp.x, sp.x, sp.x));
+    if (sh == SHAPE_CYLINDER) e = f3(sp.y, sp.x, sp.y);
     if (sh == SHAPE_HULL) {  // half extents of the hull's bounds
         const DevHull &h = w.hulls[hull_of(sp)];
         e = f3(0.5f * (h.hi.x - h.lo.x), 0.5f * (h.hi.y - h.lo.y), 0.5f * (h.hi.z - h.lo.z));
+    }
+    if (f & F_DECORATED) {  // half extents of the decorated shape's bounds
+        const DevFrame &d = w.frames[i];
+        e = f3((float)(0.5 * (d.hi[0] - d.lo[0])), (float)(0.5 * (d.hi[1] - d.lo[1])), (float)(0.5 * (d.hi[2] - d.lo[2])));
     }
     out[0] = com;
     int lowest = (e.x <= e.y && e.x <= e.z) ? 0 : (e.y <= e.z ? 1 : 2);
@@ -349,7 +354,7 @@ __device__ void sleep_points(const DevWorld &w, uint32_t f, float4 sp, float4 q,
 }
 __device__ void reset_sleep(DevWorld &w, int i) {
     float3 p[3];
-    sleep_points(w, w.flags[i], w.shape[i], w.quat[i], xyz(w.com[i]), p);
+    sleep_points(w, i, w.flags[i], w.shape[i], w.quat[i], xyz(w.com[i]), p);
     for (int k = 0; k < 3; k++) w.sleep_sph[3 * i + k] = make_float4(p[k].x, p[k].y, p[k].z, 0.f);
     w.sleep_timer[i] = 0.f;
 }
@@ -747,10 +752,10 @@ __device__ void integrate_body(DevWorld &w, int i, float dt, bool ccd) {
     float4 q = rotation_step(w.quat[i], av * dt);
     w.quat[i] = q;
     if (ccd && (f & F_LINEAR_CAST) && m == DYNAMIC && !(f & F_SENSOR)) {
-        float thr = c_settings.ccd_threshold * shape_inner_radius(w, f, w.shape[i]);
+        float thr = c_settings.ccd_threshold * shape_inner_radius(w, i, f, w.shape[i]);
         if (lensq3(v * dt) > thr * thr) {
             // setQuaternion rigid-body.ts:737-752: the centre of mass follows the rotation
-            float3 c = xyz(w.pos[i]) + qrot(q, shape_com(w, f, w.shape[i]));
+            float3 c = xyz(w.pos[i]) + qrot(q, shape_com(w, i, f, w.shape[i]));
             w.com[i] = make_float4(c.x, c.y, c.z, 0.f);
             w.ccd_flag[i] = 1;
             return;
@@ -765,7 +770,7 @@ __device__ void finish_body(DevWorld &w, int i) {
     uint32_t f = w.flags[i];
     if (motion_of(f) == STATIC || sleeping_of(f)) return;
     // updatePositionFromCenterOfMass rigid-body.ts:545-553: position = com - rotation x shape com
-    float3 com = xyz(w.com[i]) - qrot(w.quat[i], shape_com(w, f, w.shape[i]));
+    float3 com = xyz(w.com[i]) - qrot(w.quat[i], shape_com(w, i, f, w.shape[i]));
     w.pos[i] = make_float4(com.x, com.y, com.z, 0.f);
     w.force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     w.torque[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -776,7 +781,7 @@ __device__ bool sleep_update(DevWorld &w, int i, float dt) {
     uint32_t f = w.flags[i];
     if (!(f & F_ALLOW_SLEEP) || (f & F_SENSOR)) return false;
     float3 p[3];
-    sleep_points(w, f, w.shape[i], w.quat[i], xyz(w.com[i]), p);
+    sleep_points(w, i, f, w.shape[i], w.quat[i], xyz(w.com[i]), p);
     float maxMove = c_settings.sleep_threshold * c_settings.time_before_sleep;
     for (int k = 0; k < 3; k++) {
         float4 s = w.sleep_sph[3 * i + k];
@@ -2147,7 +2152,7 @@ __global__ void k_ccd_resolve(DevWorld w) {
             }
             const uint32_t fa = w.flags[a];
             const float3 p = xyz(w.pos[a]) + xyz(c.delta) * move;
-            const float3 cm = p + qrot(w.quat[a], shape_com(w, fa, w.shape[a]));
+            const float3 cm = p + qrot(w.quat[a], shape_com(w, a, fa, w.shape[a]));
             w.pos[a] = make_float4(p.x, p.y, p.z, 0.f);
             w.com[a] = make_float4(cm.x, cm.y, cm.z, 0.f);
         }

@@ -538,7 +538,7 @@ int cc_world_destroy(cc_world *W) {
                     w.cache_recs[1], w.cache_parity, w.root_flag, w.small_list, w.large_list, w.scratch_order,
                     w.scratch_colour, w.scratch_claim, w.mid_list, w.body_local, w.contact_event,
                     w.removed_keys, W->d_state_rows, w.hinges, w.island_joints, w.island_joint_count,
-                    w.island_joint_off, w.island_fill_j, w.joint_wake, w.joint_partners, w.swings, w.others,
+                    w.island_joint_off, w.island_fill_j, w.joint_wake, w.joint_partners, w.swings, w.others, w.frames,
                     w.giant_list, w.giant_claim, w.giant_count, w.small_joint_list, w.large_joint_list,
                     w.hulls, w.hull_points, w.hull_shrunk,
                     w.hull_planes, w.hull_faces, w.hull_vidx, w.ccd_flag, w.ccd_slot, w.ccd_index, w.ccd,
@@ -589,11 +589,28 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
     std::vector<uint2> groups(n);
     std::vector<int> world(n);
     std::vector<float> timer(n, 0.f);
+    std::vector<DevFrame> frames(n);
+    bool any_decorated = false;
     for (int i = 0; i < n; i++) {
         const cc_body_desc &d = b[i];
         if (d.shape_type != CC_SHAPE_BOX && d.shape_type != CC_SHAPE_SPHERE && d.shape_type != CC_SHAPE_CAPSULE &&
-            d.shape_type != CC_SHAPE_CONVEX_HULL && d.shape_type != CC_SHAPE_TRIANGLE_MESH)
+            d.shape_type != CC_SHAPE_CONVEX_HULL && d.shape_type != CC_SHAPE_TRIANGLE_MESH &&
+            d.shape_type != CC_SHAPE_CYLINDER && d.shape_type != CC_SHAPE_PLANE && d.shape_type != CC_SHAPE_EMPTY)
             return CC_ERR_UNSUPPORTED;
+        if (d.mass_properties_mode < 0 || d.mass_properties_mode > 2 || !std::isfinite(d.mass)) return CC_ERR_INVALID;
+        for (int k = 0; k < 6; k++)
+            if (!std::isfinite(d.inertia[k])) return CC_ERR_INVALID;
+        const bool plane = d.shape_type == CC_SHAPE_PLANE;
+        D3 pn{0, 1, 0};
+        if (plane) {  // plane.ts create :77-98; no mass (:120-122): static or kinematic only
+            pn = dnormalize(d3(d.shape_params));
+            if (!(pn.x * pn.x + pn.y * pn.y + pn.z * pn.z > 0) || !std::isfinite(d.shape_params[3]) ||
+                d.motion_type == CC_DYNAMIC)
+                return CC_ERR_INVALID;
+        }
+        if (d.shape_type == CC_SHAPE_CYLINDER &&  // cylinder.ts update: 0 <= convex radius <= half height, radius
+            !(d.shape_params[2] >= 0.f && d.shape_params[0] >= d.shape_params[2] && d.shape_params[1] >= d.shape_params[2]))
+            return CC_ERR_INVALID;
         const cc_mesh::Mesh *mesh = nullptr;
         int mesh_index = -1;
         if (d.shape_type == CC_SHAPE_TRIANGLE_MESH) {
@@ -625,11 +642,29 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
             return CC_ERR_INVALID;
         ovr[i] = (uint32_t)d.num_velocity_steps_override | ((uint32_t)d.num_position_steps_override << 8);
         if (ovr[i]) W->any_iter_override = true;
+        // shape decorators, OffsetCenterOfMass(Transformed(Scaled(leaf))) (scaled.ts, transformed.ts,
+        // offset-center-of-mass.ts)
+        if (!finite3(d.shape_scale) || !finite3(d.shape_position) || !finite3(d.com_offset) ||
+            !std::isfinite(d.shape_quaternion[0]) || !std::isfinite(d.shape_quaternion[1]) ||
+            !std::isfinite(d.shape_quaternion[2]) || !std::isfinite(d.shape_quaternion[3]))
+            return CC_ERR_INVALID;
+        double sc[3] = {d.shape_scale[0], d.shape_scale[1], d.shape_scale[2]};
+        for (int k = 0; k < 3; k++)
+            if (sc[k] == 0) sc[k] = 1;
+        DQ tq{d.shape_quaternion[0], d.shape_quaternion[1], d.shape_quaternion[2], d.shape_quaternion[3]};
+        if (tq.x == 0 && tq.y == 0 && tq.z == 0 && tq.w == 0) tq = {0, 0, 0, 1};
+        const D3 tp = d3(d.shape_position), off = d3(d.com_offset);
+        const bool scaled = sc[0] != 1 || sc[1] != 1 || sc[2] != 1;
+        const bool transformed = tp.x != 0 || tp.y != 0 || tp.z != 0 || tq.x != 0 || tq.y != 0 || tq.z != 0 || tq.w != 1;
+        const bool offset = off.x != 0 || off.y != 0 || off.z != 0;
+        // a plane keeps its local bounds (computePlaneLocalBounds plane.ts:273-295) in a frame
+        const bool decorated = scaled || transformed || offset || plane;
+        if (scaled && (hull || mesh || plane)) return CC_ERR_UNSUPPORTED;
         double mass;
         double idiag[3];
         double irot[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};  // principal axes (columns)
-        if (mesh) {
-            mass = 0.0;  // computeMassProperties triangle-mesh.ts:153-158
+        if (mesh || plane) {
+            mass = 0.0;  // computeMassProperties triangle-mesh.ts:153-158, plane.ts:120-122
             idiag[0] = idiag[1] = idiag[2] = 0.0;
         } else if (hull) {
             // computeMassProperties convex-hull.ts:453-459, principal axes of the inertia
@@ -643,6 +678,13 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
             idiag[0] = (fy * fy + fz * fz) * (mass / 12.0);
             idiag[1] = (fx * fx + fz * fz) * (mass / 12.0);
             idiag[2] = (fx * fx + fy * fy) * (mass / 12.0);
+        } else if (d.shape_type == CC_SHAPE_CYLINDER) {
+            // computeMassProperties cylinder.ts
+            double h = d.shape_params[0], r = d.shape_params[1];
+            mass = M_PI * r * r * 2 * h * d.density;
+            double iyy = 0.5 * mass * r * r;
+            idiag[1] = iyy;
+            idiag[0] = idiag[2] = 0.5 * iyy + (mass * 4 * h * h) / 12;
         } else if (d.shape_type == CC_SHAPE_CAPSULE) {
             // computeMassProperties capsule.ts:119-157: cylinder plus two hemispheres along Y
             double r = d.shape_params[0], h = d.shape_params[1];
@@ -662,10 +704,147 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
             double in = 0.4 * mass * r * r;
             idiag[0] = idiag[1] = idiag[2] = in;
         }
+        bool given_tensor = false;
+        DevFrame fr;
+        memset(&fr, 0, sizeof(fr));
+        if (decorated && !mesh && !plane) {
+            // computeMassProperties: massProperties.scale (mass-properties.ts:59-112), rotate
+            // (:121-160), translate (:168-205) of the leaf's, then the principal axes
+            double t[9] = {idiag[0], 0, 0, 0, idiag[1], 0, 0, 0, idiag[2]};
+            if (hull)
+                for (int k = 0; k < 9; k++) t[k] = hull->inertia[k] * d.density;
+            if (scaled) {
+                double half = 0.5 * (t[0] + t[4] + t[8]);
+                double q0 = sc[0] * sc[0] * (half - t[0]), q1 = sc[1] * sc[1] * (half - t[4]),
+                       q2 = sc[2] * sc[2] * (half - t[8]);
+                double ms = std::fabs(sc[0] * sc[1] * sc[2]);
+                double nt[9] = {q1 + q2,           sc[0] * sc[1] * t[1], sc[0] * sc[2] * t[2],
+                                sc[0] * sc[1] * t[3], q0 + q2,           sc[1] * sc[2] * t[5],
+                                sc[0] * sc[2] * t[6], sc[1] * sc[2] * t[7], q0 + q1};
+                for (int k = 0; k < 9; k++) t[k] = nt[k] * ms;
+                mass *= ms;
+            }
+            if (transformed) {
+                D3 cols[3] = {drot(tq, D3{1, 0, 0}), drot(tq, D3{0, 1, 0}), drot(tq, D3{0, 0, 1})};
+                double R[9] = {cols[0].x, cols[1].x, cols[2].x, cols[0].y, cols[1].y, cols[2].y,
+                               cols[0].z, cols[1].z, cols[2].z};  // row-major
+                double rt[9], o[9];
+                for (int a = 0; a < 3; a++)
+                    for (int c = 0; c < 3; c++) {
+                        rt[3 * a + c] = 0;
+                        for (int k = 0; k < 3; k++) rt[3 * a + c] += R[3 * a + k] * t[3 * k + c];
+                    }
+                for (int a = 0; a < 3; a++)
+                    for (int c = 0; c < 3; c++) {
+                        o[3 * a + c] = 0;
+                        for (int k = 0; k < 3; k++) o[3 * a + c] += rt[3 * a + k] * R[3 * c + k];
+                    }
+                for (int k = 0; k < 9; k++) t[k] = o[k];
+            }
+            if (offset) {
+                double dd = off.x * off.x + off.y * off.y + off.z * off.z, v[3] = {off.x, off.y, off.z};
+                for (int a = 0; a < 3; a++)
+                    for (int c = 0; c < 3; c++) t[3 * a + c] += mass * ((a == c ? dd : 0.0) - v[a] * v[c]);
+            }
+            cc_hull::principal_axes(t, idiag, irot);
+        }
+        // MassPropertiesOverride (rigid-body.ts:309-326, 676-700): a given mass scales the shape's
+        // inertia (scaleToMass mass-properties.ts:220-240); a given mass and inertia replace them
+        if (d.mass_properties_mode == CC_MASS_GIVEN) {
+            if (mass > 0)
+                for (int k = 0; k < 3; k++) idiag[k] *= d.mass / mass;
+            mass = d.mass;
+        } else if (d.mass_properties_mode == CC_MASS_AND_INERTIA_GIVEN) {
+            const float *t = d.inertia;
+            double g[9] = {t[0], t[1], t[2], t[1], t[3], t[4], t[2], t[4], t[5]};
+            cc_hull::principal_axes(g, idiag, irot);
+            mass = d.mass;
+            given_tensor = true;
+        }
+        if (decorated) {
+            // the leaf's local bounds, times |s| per axis (computeScaledLocalBounds), then the corners
+            // moved by the transform (computeTransformedLocalBounds); the offset moves none of them
+            double lo[3], hi[3];
+            if (plane) {
+                // getOrthogonalBasis :210-233, getPlaneVertices :235-271: the face's corners and
+                // the corners one half extent behind it
+                const double he = 1000.0, c = d.shape_params[3];
+                D3 p1 = dcross(pn, D3{0, 1, 0});
+                double l = p1.x * p1.x + p1.y * p1.y + p1.z * p1.z;
+                p1 = l < 1e-6 ? D3{1, 0, 0} : D3{p1.x / std::sqrt(l), p1.y / std::sqrt(l), p1.z / std::sqrt(l)};
+                D3 p2 = dnormalize(dcross(p1, pn));
+                p1 = dnormalize(dcross(pn, p2));
+                D3 pt{-c * pn.x, -c * pn.y, -c * pn.z};
+                for (int k = 0; k < 3; k++) lo[k] = 1e300, hi[k] = -1e300;
+                for (int v = 0; v < 4; v++) {
+                    const double s1 = (v == 0 || v == 1) ? he : -he, s2 = (v == 0 || v == 3) ? he : -he;
+                    D3 q{pt.x + s1 * p1.x + s2 * p2.x, pt.y + s1 * p1.y + s2 * p2.y, pt.z + s1 * p1.z + s2 * p2.z};
+                    for (int back = 0; back < 2; back++) {
+                        double e[3] = {q.x - back * he * pn.x, q.y - back * he * pn.y, q.z - back * he * pn.z};
+                        for (int k = 0; k < 3; k++) lo[k] = std::min(lo[k], e[k]), hi[k] = std::max(hi[k], e[k]);
+                    }
+                }
+            } else if (mesh) {
+                for (int k = 0; k < 3; k++) {
+                    lo[k] = mesh->lo[k];
+                    hi[k] = mesh->hi[k];
+                }
+            } else if (hull) {
+                lo[0] = hull->lo.x, lo[1] = hull->lo.y, lo[2] = hull->lo.z;
+                hi[0] = hull->hi.x, hi[1] = hull->hi.y, hi[2] = hull->hi.z;
+            } else {
+                const float *q = d.shape_params;
+                double e[3] = {q[0], q[0], q[0]};
+                if (d.shape_type == CC_SHAPE_BOX) e[0] = q[0], e[1] = q[1], e[2] = q[2];
+                if (d.shape_type == CC_SHAPE_CAPSULE) e[1] = (double)q[1] + (double)q[0];
+                if (d.shape_type == CC_SHAPE_CYLINDER) e[0] = e[2] = q[1], e[1] = q[0];
+                for (int k = 0; k < 3; k++) lo[k] = -e[k], hi[k] = e[k];
+            }
+            for (int k = 0; k < 3; k++) {
+                lo[k] *= std::fabs(sc[k]);
+                hi[k] *= std::fabs(sc[k]);
+            }
+            if (transformed) {
+                double nlo[3] = {1e300, 1e300, 1e300}, nhi[3] = {-1e300, -1e300, -1e300};
+                for (int c = 0; c < 8; c++) {
+                    D3 k = drot(tq, D3{(c & 1) ? hi[0] : lo[0], (c & 2) ? hi[1] : lo[1], (c & 4) ? hi[2] : lo[2]});
+                    double v[3] = {k.x + tp.x, k.y + tp.y, k.z + tp.z};
+                    for (int a = 0; a < 3; a++) {
+                        nlo[a] = std::min(nlo[a], v[a]);
+                        nhi[a] = std::max(nhi[a], v[a]);
+                    }
+                }
+                for (int a = 0; a < 3; a++) lo[a] = nlo[a], hi[a] = nhi[a];
+            }
+            for (int k = 0; k < 3; k++) fr.lo[k] = lo[k], fr.hi[k] = hi[k];
+            // centre of mass: computeTransformedCenterOfMass + the offset (a scaled shape's is zero)
+            D3 c{0, 0, 0};
+            if (hull && !scaled) c = D3{hull->com.x, hull->com.y, hull->com.z};
+            if (transformed) {
+                D3 r = drot(tq, c);
+                c = {r.x + tp.x, r.y + tp.y, r.z + tp.z};
+            }
+            c = {c.x + off.x, c.y + off.y, c.z + off.z};
+            fr.com = make_float4((float)c.x, (float)c.y, (float)c.z, 0.f);
+            // getInnerRadius: min|s| x the leaf's
+            double inner = hull ? hull->inner_radius
+                                : (d.shape_type == CC_SHAPE_BOX
+                                       ? std::min((double)d.shape_params[0],
+                                                  std::min((double)d.shape_params[1], (double)d.shape_params[2]))
+                                       : (double)d.shape_params[0]);
+            if (d.shape_type == CC_SHAPE_CYLINDER)
+                inner = std::min((double)d.shape_params[0], (double)d.shape_params[1]);
+            if (mesh || plane) inner = 0;
+            double minScale = std::min(std::fabs(sc[0]), std::min(std::fabs(sc[1]), std::fabs(sc[2])));
+            fr.t_pos = make_float4((float)tp.x, (float)tp.y, (float)tp.z, (float)(minScale * inner));
+            fr.t_rot = make_float4((float)tq.x, (float)tq.y, (float)tq.z, (float)tq.w);
+            any_decorated = true;
+        }
+        frames[i] = fr;
         int dof = d.allowed_dofs & 63;
         float inv_mass = 0.f;
         float3 inv_i = f3(0.f, 0.f, 0.f);
-        if (d.motion_type != CC_STATIC && !mesh) {
+        if (d.motion_type != CC_STATIC && !mesh && !plane) {
             if ((dof & 7) != 0) {
                 if (!(mass > 0)) return CC_ERR_INVALID;
                 inv_mass = (float)(1.0 / mass);
@@ -682,7 +861,11 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
         pos[i] = make_float4(d.position[0], d.position[1], d.position[2], 0.f);
         quat[i] = make_float4(d.quaternion[0], d.quaternion[1], d.quaternion[2], d.quaternion[3]);
         com[i] = pos[i];  // the shape's centre of mass is its origin, hulls aside
-        if (hull) {  // updateCenterOfMassPosition rigid-body.ts:527-536: position + rotation x com
+        if (decorated) {  // updateCenterOfMassPosition rigid-body.ts:527-536: position + rotation x com
+            D3 c = drot(dq(quat[i]), D3{fr.com.x, fr.com.y, fr.com.z});
+            com[i] = make_float4((float)(d.position[0] + c.x), (float)(d.position[1] + c.y), (float)(d.position[2] + c.z),
+                                 0.f);
+        } else if (hull) {  // updateCenterOfMassPosition rigid-body.ts:527-536: position + rotation x com
             DQ q = dq(quat[i]);
             D3 c = drot(q, D3{hull->com.x, hull->com.y, hull->com.z});
             com[i] = make_float4((float)(d.position[0] + c.x), (float)(d.position[1] + c.y), (float)(d.position[2] + c.z),
@@ -694,10 +877,26 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
         ii[i] = make_float4(inv_i.x, inv_i.y, inv_i.z, inv_mass);
         ir[i] = make_float4(0.f, 0.f, 0.f, 1.f);
         sh[i] = make_float4(d.shape_params[0], d.shape_params[1], d.shape_params[2], d.shape_params[3]);
-        if (hull) {
+        if (plane) sh[i] = make_float4((float)pn.x, (float)pn.y, (float)pn.z, d.shape_params[3]);
+        if (scaled) {  // the scale baked into the leaf (setBoxSupport support.ts:343-372, sphere.ts:195-197,
+                       // capsule.ts:308-318)
+            const double ax = std::fabs(sc[0]), ay = std::fabs(sc[1]), az = std::fabs(sc[2]);
+            if (d.shape_type == CC_SHAPE_BOX)
+                sh[i] = make_float4((float)(ax * d.shape_params[0]), (float)(ay * d.shape_params[1]),
+                                    (float)(az * d.shape_params[2]),
+                                    (float)std::min(d.shape_params[3] * std::min(ax, std::min(ay, az)), 0.05));
+            else if (d.shape_type == CC_SHAPE_CYLINDER)  // setCylinder*Support cylinder.ts: |s.x| throughout
+                sh[i] = make_float4((float)(ax * d.shape_params[0]), (float)(ax * d.shape_params[1]),
+                                    (float)(ax * d.shape_params[2]), 0.f);
+            else
+                sh[i] = make_float4((float)(ax * d.shape_params[0]), (float)(ax * d.shape_params[1]), 0.f, 0.f);
+        }
+        if (hull || (decorated && !mesh && !plane) || given_tensor) {  // principal axes of a full inertia tensor
             DQ r = quat_from_columns(D3{irot[0], irot[3], irot[6]}, D3{irot[1], irot[4], irot[7]},
                                      D3{irot[2], irot[5], irot[8]});
             ir[i] = make_float4((float)r.x, (float)r.y, (float)r.z, (float)r.w);
+        }
+        if (hull) {
             float hi_bits;
             memcpy(&hi_bits, &hull_index, sizeof(float));
             sh[i] = make_float4(hi_bits, (float)hull->convex_radius, 0.f, 0.f);
@@ -717,6 +916,7 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
         f |= (uint32_t)(d.restitution_combine & 7) << F_RCOMB_SHIFT;
         f |= (uint32_t)(d.object_layer & 31) << F_LAYER_SHIFT;
         if (d.motion_quality == CC_MOTION_LINEAR_CAST) f |= F_LINEAR_CAST;
+        if (decorated) f |= F_DECORATED;
         flags[i] = f;
         groups[i] = make_uint2(d.collision_groups, d.collision_mask);
         world[i] = d.world;
@@ -729,7 +929,12 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
                        ? f3(d.shape_params[0], d.shape_params[1], d.shape_params[2])
                        : (d.shape_type == CC_SHAPE_CAPSULE
                               ? f3(d.shape_params[0], d.shape_params[1] + d.shape_params[0], d.shape_params[0])
-                              : f3(d.shape_params[0], d.shape_params[0], d.shape_params[0]));
+                              : (d.shape_type == CC_SHAPE_CYLINDER
+                                     ? f3(d.shape_params[1], d.shape_params[0], d.shape_params[1])
+                                     : f3(d.shape_params[0], d.shape_params[0], d.shape_params[0])));
+        if (decorated)  // half extents of the decorated shape's bounds
+            e = f3((float)(0.5 * (fr.hi[0] - fr.lo[0])), (float)(0.5 * (fr.hi[1] - fr.lo[1])),
+                   (float)(0.5 * (fr.hi[2] - fr.lo[2])));
         float3 c = xyz(com[i]);
         float3 p[3];
         p[0] = c;
@@ -751,6 +956,13 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
     }
     size_t o = w.n;
     cudaStream_t s = W->stream;
+    if (any_decorated && !w.frames) {  // the decorator records, allocated with the first decorated body
+        int r = dalloc(&w.frames, w.cap);
+        if (r != CC_OK) return r;
+        CC_TRY(cudaMemset(w.frames, 0, sizeof(DevFrame) * (size_t)w.cap));
+        drop_graph(W);
+    }
+    if (w.frames) CC_TRY(cudaMemcpyAsync(w.frames + o, frames.data(), sizeof(DevFrame) * n, cudaMemcpyHostToDevice, s));
     CC_TRY(cudaMemcpyAsync(w.pos + o, pos.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
     CC_TRY(cudaMemcpyAsync(w.quat + o, quat.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
     CC_TRY(cudaMemcpyAsync(w.com + o, com.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
@@ -926,7 +1138,7 @@ __global__ void k_unpack_state(DevWorld w, const float *rows) {
         w.quat[i] = make_float4(o[3], o[4], o[5], o[6]);
         w.linvel[i] = make_float4(o[7], o[8], o[9], 0.f);
         w.angvel[i] = make_float4(o[10], o[11], o[12], 0.f);
-        float3 c = qrot(w.quat[i], shape_com(w, w.flags[i], w.shape[i]));
+        float3 c = qrot(w.quat[i], shape_com(w, i, w.flags[i], w.shape[i]));
         w.com[i] = make_float4(o[0] + c.x, o[1] + c.y, o[2] + c.z, 0.f);
     }
 }

@@ -15,7 +15,8 @@ import numpy as np
 from typing import Optional
 
 from ._lib import (BODY_DTYPE, COMBINE_GEOMETRIC_MEAN, COMBINE_MAX, DYNAMIC, MOTOR_OFF, MOTOR_POSITION,
-                   MOTOR_VELOCITY, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_CONVEX_HULL, SHAPE_SPHERE, SHAPE_TRIANGLE_MESH, STATIC,
+                   MOTOR_VELOCITY, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_CONVEX_HULL, SHAPE_CYLINDER, SHAPE_EMPTY,
+                   SHAPE_PLANE, SHAPE_SPHERE, SHAPE_TRIANGLE_MESH, STATIC,
                    SWING_CONE, SWING_PYRAMID, JOINT_CONE, JOINT_DISTANCE, JOINT_FIXED, JOINT_POINT, JOINT_SLIDER,
                    SPRING_STIFFNESS_AND_DAMPING, hinge_defaults, joint_defaults, swing_twist_defaults)
 
@@ -97,6 +98,29 @@ def set_capsule(b: np.ndarray, idx, radius, half_height) -> None:
     b["shape_params"][idx, 0] = radius
     b["shape_params"][idx, 1] = half_height
     b["shape_params"][idx, 2:] = 0.0
+
+
+def set_cylinder(b: np.ndarray, idx, half_height, radius, convex_radius: float = DEFAULT_CONVEX_RADIUS) -> None:
+    """Cylinder along local Y (src/shapes/cylinder.ts): half height, radius, convex radius."""
+    b["shape_type"][idx] = SHAPE_CYLINDER
+    b["shape_params"][idx, 0] = half_height
+    b["shape_params"][idx, 1] = radius
+    b["shape_params"][idx, 2] = convex_radius
+    b["shape_params"][idx, 3] = 0.0
+
+
+def set_plane(b: np.ndarray, idx, normal, constant: float = 0.0) -> None:
+    """Plane (src/shapes/plane.ts): n . x + c = 0 in the body frame, solid below; static or
+    kinematic bodies only."""
+    b["shape_type"][idx] = SHAPE_PLANE
+    b["shape_params"][idx, 0:3] = normal
+    b["shape_params"][idx, 3] = constant
+
+
+def set_empty(b: np.ndarray, idx) -> None:
+    """Empty shape (src/shapes/empty-shape.ts): no collision and no mass."""
+    b["shape_type"][idx] = SHAPE_EMPTY
+    b["shape_params"][idx] = 0.0
 
 
 def set_hull(b: np.ndarray, idx, hull_index: int) -> None:
@@ -1140,3 +1164,99 @@ def joint_zoo(seed: int = 91) -> Scene:
     b["allow_sleeping"][:] = 0
     joints = {t: np.array(r, dtype=joint_defaults(t, 0).dtype) for t, r in J.items()}
     return Scene("joint_zoo", b, dt=1.0 / 60.0, steps=120, seed=seed, joints=joints, skip_joint_pairs=True)
+
+
+def decorated_pile(n: int = 120, seed: int = 6, extent: float = 4.0, heights=(0.5, 4.0), grid: float = 0.0) -> Scene:
+    """n decorated convex bodies (src/shapes/transformed.ts, scaled.ts, offset-center-of-mass.ts)
+    dropped on a static box floor, a seeded mix of: a box rotated and shifted in its body frame
+    (TransformedShape); a non-uniformly scaled box (ScaledShape); a uniformly scaled sphere; a
+    capsule laid along X by its transform; a box with its centre of mass moved off its middle
+    (OffsetCenterOfMassShape); a scaled box that is also transformed and offset; a cylinder
+    (src/shapes/cylinder.ts); and a uniformly scaled cylinder laid on its side.  Random
+    orientations, drop heights in ``heights``, positions within +-``extent`` in X and Z, or with
+    ``grid`` > 0 on a square grid of that spacing (bodies that never touch one another)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = blank_bodies(n + 1)
+    set_box(b, 0, (50.0, 0.5, 50.0))
+    b["motion_type"][0] = STATIC
+    b["object_layer"][0] = LAYER_NOT_MOVING
+    b["position"][0] = (0.0, -0.5, 0.0)
+
+    def rand_quat():
+        q = rng.normal(size=4)
+        return q / np.linalg.norm(q)
+
+    for i in range(1, n + 1):
+        kind = int(rng.integers(0, 8))
+        if kind in (6, 7):  # cylinders: plain, and laid on their side by the transform, scaled
+            set_cylinder(b, i, float(rng.uniform(0.15, 0.35)), float(rng.uniform(0.15, 0.3)))
+            if kind == 7:
+                b["shape_quaternion"][i] = (math.sin(math.pi / 4), 0.0, 0.0, math.cos(math.pi / 4))
+                b["shape_scale"][i] = float(rng.uniform(0.8, 1.3))
+        elif kind in (0, 4, 5):
+            set_box(b, i, tuple(rng.uniform(0.15, 0.4, 3)))
+        elif kind == 1:
+            set_box(b, i, (0.25, 0.25, 0.25))
+        elif kind == 2:
+            set_sphere(b, i, float(rng.uniform(0.15, 0.3)))
+        else:
+            set_capsule(b, i, float(rng.uniform(0.1, 0.2)), float(rng.uniform(0.2, 0.4)))
+        if kind in (0, 5):
+            b["shape_position"][i] = rng.uniform(-0.2, 0.2, 3)
+            b["shape_quaternion"][i] = rand_quat()
+        if kind == 1:
+            b["shape_scale"][i] = rng.uniform(0.6, 1.8, 3)
+        if kind == 2:
+            b["shape_scale"][i] = float(rng.uniform(0.7, 1.5))
+        if kind == 3:
+            b["shape_quaternion"][i] = (0.0, 0.0, math.sin(math.pi / 4), math.cos(math.pi / 4))
+        if kind in (4, 5):
+            b["com_offset"][i] = rng.uniform(-0.1, 0.1, 3)
+        if kind == 5:
+            b["shape_scale"][i] = rng.uniform(0.7, 1.3, 3)
+        b["position"][i] = (rng.uniform(-extent, extent), rng.uniform(*heights), rng.uniform(-extent, extent))
+        if grid > 0:
+            side = int(math.ceil(math.sqrt(n)))
+            b["position"][i, 0] = grid * ((i - 1) % side)
+            b["position"][i, 2] = grid * ((i - 1) // side)
+        b["quaternion"][i] = rand_quat()
+    return Scene("decorated_pile", b, dt=1.0 / 60.0, steps=120, seed=seed)
+
+
+def plane_drop(n: int = 40, seed: int = 9, grid: float = 0.0) -> Scene:
+    """n convex bodies (boxes, spheres, capsules, cylinders; a third of them with a given mass,
+    src/body/rigid-body.ts:309-326) dropped onto a static plane shape (src/shapes/plane.ts)
+    tilted 10 degrees about Z, with a static empty-shape body (empty-shape.ts) among them that
+    nothing collides with.  Positions within +-3 m in X and Z (or on a ``grid``-spaced square),
+    heights 0.5 to 2.5 m above the plane."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = blank_bodies(n + 2)
+    tilt = math.radians(10.0)
+    set_plane(b, 0, (-math.sin(tilt), math.cos(tilt), 0.0), 0.0)
+    b["motion_type"][0] = STATIC
+    b["object_layer"][0] = LAYER_NOT_MOVING
+    set_empty(b, 1)
+    b["motion_type"][1] = STATIC
+    b["object_layer"][1] = LAYER_NOT_MOVING
+    b["position"][1] = (0.0, 1.0, 0.0)
+    side = int(math.ceil(math.sqrt(n)))
+    for i in range(2, n + 2):
+        kind = int(rng.integers(0, 4))
+        if kind == 0:
+            set_box(b, i, tuple(rng.uniform(0.15, 0.35, 3)))
+        elif kind == 1:
+            set_sphere(b, i, float(rng.uniform(0.15, 0.3)))
+        elif kind == 2:
+            set_capsule(b, i, float(rng.uniform(0.1, 0.2)), float(rng.uniform(0.2, 0.4)))
+        else:
+            set_cylinder(b, i, float(rng.uniform(0.15, 0.3)), float(rng.uniform(0.15, 0.3)))
+        if i % 3 == 0:
+            b["mass_properties_mode"][i] = 1
+            b["mass"][i] = float(rng.uniform(5.0, 50.0))
+        x, z = rng.uniform(-3.0, 3.0), rng.uniform(-3.0, 3.0)
+        if grid > 0:
+            x, z = grid * ((i - 2) % side) - grid * side / 2, grid * ((i - 2) // side) - grid * side / 2
+        b["position"][i] = (x, x * math.tan(tilt) + rng.uniform(0.5, 2.5), z)
+        q = rng.normal(size=4)
+        b["quaternion"][i] = q / np.linalg.norm(q)
+    return Scene("plane_drop", b, dt=1.0 / 60.0, steps=120, seed=seed)

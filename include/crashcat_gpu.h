@@ -67,9 +67,17 @@ enum cc_status {
     CC_ERR_UNSUPPORTED = 6
 };
 
+/* cc_body_desc.shape_params per type: sphere (radius); box (half extents x y z, convex radius);
+ * capsule (radius, half height of the segment on Y); convex hull (hull index); triangle mesh
+ * (mesh index); cylinder (half height on Y, radius, convex radius, with 0 <= convex radius <=
+ * both; src/shapes/cylinder.ts); plane (normal x y z, normalised on creation, and the constant
+ * of n . x + c = 0, solid below; src/shapes/plane.ts, half extent 1000, static or kinematic
+ * bodies only: a plane has no mass); empty (no parameters, no collision, no mass;
+ * src/shapes/empty-shape.ts). */
 enum cc_shape_type { CC_SHAPE_SPHERE = 0, CC_SHAPE_BOX = 1, CC_SHAPE_CAPSULE = 2, CC_SHAPE_CONVEX_HULL = 3,
-                     CC_SHAPE_TRIANGLE_MESH = 4 };
+                     CC_SHAPE_TRIANGLE_MESH = 4, CC_SHAPE_CYLINDER = 5, CC_SHAPE_PLANE = 6, CC_SHAPE_EMPTY = 7 };
 enum cc_motion_type { CC_STATIC = 0, CC_KINEMATIC = 1, CC_DYNAMIC = 2 };
+enum cc_mass_mode { CC_MASS_FROM_SHAPE = 0, CC_MASS_GIVEN = 1, CC_MASS_AND_INERTIA_GIVEN = 2 };
 enum cc_motion_quality { CC_MOTION_DISCRETE = 0, CC_MOTION_LINEAR_CAST = 1 };  /* MotionQuality motion-properties.ts:8-26 */
 enum cc_combine_mode { CC_COMBINE_AVERAGE = 0, CC_COMBINE_MULTIPLY = 1, CC_COMBINE_MIN = 2, CC_COMBINE_MAX = 3,
                        CC_COMBINE_GEOMETRIC_MEAN = 4 };
@@ -161,6 +169,31 @@ typedef struct cc_body_desc {
      * count when any of them is 0 (src/islands.ts:344-386).  At most 255. */
     int32_t num_velocity_steps_override;
     int32_t num_position_steps_override;
+    /* Shape decorators around the shape above (src/shapes/scaled.ts, transformed.ts,
+     * offset-center-of-mass.ts), nested as OffsetCenterOfMassShape(TransformedShape(
+     * ScaledShape(shape))); all zero = no decorator.
+     *  - shape_scale: ScaledShape.scale, a zero component reads as 1.  The scale is baked into
+     *    the shape: box half extents |s| per axis with the convex radius min(r min|s|, 0.05)
+     *    (setBoxSupport support.ts:343-372); sphere and capsule |s.x| (sphere.ts:195-197,
+     *    capsule.ts:308-318).  A scaled convex hull or triangle mesh is CC_ERR_UNSUPPORTED.
+     *    Mass properties follow massProperties.scale (mass-properties.ts:59-112).
+     *  - shape_position / shape_quaternion: TransformedShape, the shape's pose in the body
+     *    frame (all-zero quaternion = identity); collisions, casts and queries see the shape
+     *    there (collideTransformedVsShape, transformed.ts).
+     *  - com_offset: OffsetCenterOfMassShape.offset, moves the centre of mass (and the
+     *    inertia by the parallel-axis term) but not the collision geometry. */
+    float shape_scale[3];
+    float shape_position[3];
+    float shape_quaternion[4];
+    float com_offset[3];
+    /* Mass properties (RigidBodySettings.mass / massPropertiesOverride, rigid-body.ts:309-326,
+     * 676-700): cc_mass_mode; with CC_MASS_GIVEN the shape's inertia is scaled to `mass`
+     * (scaleToMass mass-properties.ts:220-240); with CC_MASS_AND_INERTIA_GIVEN `mass` and
+     * `inertia` (xx xy xz yy yz zz, about the centre of mass, body frame) are used as given.
+     * A dynamic body whose shape has no mass (empty) needs one of them. */
+    int32_t mass_properties_mode;
+    float mass;
+    float inertia[6];
 } cc_body_desc;
 
 /* Per-step counters of the last completed step. */

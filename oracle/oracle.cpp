@@ -215,6 +215,12 @@ static void shape_mass(const Shape &s, double &mass, V3 &inertiaDiag) {
         mass = (4.0 / 3.0) * M_PI * s.radius * r2 * s.density;
         double in = (2.0 / 5.0) * mass * r2;
         inertiaDiag = {in, in, in};
+    } else if (s.type == SHAPE_CYLINDER) {
+        // computeMassProperties cylinder.ts
+        mass = M_PI * s.radius * s.radius * 2 * s.half_height * s.density;
+        double iyy = 0.5 * mass * s.radius * s.radius;
+        double ixx = 0.5 * iyy + (mass * 4 * s.half_height * s.half_height) / 12;
+        inertiaDiag = {ixx, iyy, ixx};
     } else if (s.type == SHAPE_CONVEX_HULL) {
         // computeMassProperties convex-hull.ts:453-459: the inertia tensor goes through
         // set_mass_properties_tensor
@@ -915,7 +921,11 @@ static bool narrowphase(World &w, Body *A, Body *B, double dt) {
     // activeEdgeMovementDirection update.ts:729-733
     V3 movement = sub(A->linvel, B->linvel);
     std::vector<Hit> hits;
-    collide_hits(hits, cs, A->shape, A->position, A->quat, B->shape, B->position, B->quat, movement);
+    V3 gpA, gpB;
+    Q4 gqA, gqB;
+    geometry_pose(A->shape, A->position, A->quat, gpA, gqA);
+    geometry_pose(B->shape, B->position, B->quat, gpB, gqB);
+    collide_hits(hits, cs, A->shape, gpA, gqA, B->shape, gpB, gqB, movement);
     // narrowphaseWithReductionCollector.addHit update.ts:385-519: hits whose normal is within
     // normalCosMaxDeltaRotation of a manifold's accumulated normal join it, at most 32 manifolds
     const double maxContactDistance = w.s.speculativeContactDistance + w.s.manifoldTolerance;
@@ -1360,9 +1370,12 @@ static void check_island_sleep(World &w, Island &is, double dt) {
 // ---------------------------------------------------------------------------
 // getInnerRadius box.ts:333-335, sphere.ts:147-149, capsule.ts:254-256, convex-hull.ts:549-558
 static double inner_radius(const Shape &s) {
+    if (s.decorated && s.innerRadius >= 0) return s.innerRadius;
     switch (s.type) {
         case SHAPE_BOX:
             return std::min(s.half_extents.x, std::min(s.half_extents.y, s.half_extents.z));
+        case SHAPE_CYLINDER:  // cylinder.ts getInnerRadius
+            return std::min(s.half_height, s.radius);
         case SHAPE_CONVEX_HULL: {
             double r = std::numeric_limits<double>::max();
             for (double c : s.hull->plane_c) r = std::min(r, -c);
@@ -1438,6 +1451,10 @@ static void find_ccd_contacts(World &w, double dt) {
             if (!(ray_box_entry(A.position, rel, relLen, box_grow(B.aabb, halfA)) <
                   std::numeric_limits<double>::infinity()))
                 continue;
+            V3 gpA, gpB;
+            Q4 gqA, gqB;
+            geometry_pose(A.shape, A.position, A.quat, gpA, gqA);
+            geometry_pose(B.shape, B.position, B.quat, gpB, gqB);
             // ccdCastShapeCollector.addHit update.ts:1044-1109
             auto collect = [&](double fraction, V3 pa, V3 axis) {
                 V3 n = normalize(axis);
@@ -1457,6 +1474,13 @@ static void find_ccd_contacts(World &w, double dt) {
                 c.friction = combine(A.friction, B.friction, A.frictionCombine, B.frictionCombine);
                 c.restitution = combine(A.restitution, B.restitution, A.restitutionCombine, B.restitutionCombine);
             };
+            if (B.shape.type == SHAPE_EMPTY || A.shape.type == SHAPE_EMPTY) continue;
+            if (B.shape.type == SHAPE_PLANE) {  // castConvexVsPlane plane.ts:727-918
+                CastHit h;
+                if (cast_convex_vs_plane(h, A.shape, gpA, gqA, rel, B.shape, gpB, gqB, c.fps, false))
+                    collect(h.fraction, h.pa, h.axis);
+                continue;
+            }
             if (B.shape.type == SHAPE_TRIANGLE_MESH) {
                 // castShapeVsShape dispatch (triangle-mesh.ts:223-237): the sphere's own cast
                 // for spheres, the GJK cast for the other shapes; the collector's early-out
@@ -1464,14 +1488,13 @@ static void find_ccd_contacts(World &w, double dt) {
                 auto onHit = [&](const CastMeshHit &h) { collect(h.fraction, h.pa, h.axis); };
                 auto earlyOut = [&]() { return c.fps; };
                 if (A.shape.type == SHAPE_SPHERE)
-                    cast_sphere_vs_mesh(A.shape, A.position, rel, B.shape, B.position, B.quat, onHit, earlyOut);
+                    cast_sphere_vs_mesh(A.shape, gpA, rel, B.shape, gpB, gqB, onHit, earlyOut);
                 else
-                    cast_convex_vs_mesh(A.shape, A.position, A.quat, rel, B.shape, B.position, B.quat, onHit, earlyOut);
+                    cast_convex_vs_mesh(A.shape, gpA, gqA, rel, B.shape, gpB, gqB, onHit, earlyOut);
                 continue;
             }
             CastHit h;
-            if (!cast_convex_vs_convex(h, A.shape, A.position, A.quat, rel, B.shape, B.position, B.quat, c.fps, false))
-                continue;
+            if (!cast_convex_vs_convex(h, A.shape, gpA, gqA, rel, B.shape, gpB, gqB, c.fps, false)) continue;
             collect(h.fraction, h.pa, h.axis);
         }
     }
@@ -1878,7 +1901,14 @@ enum {
     F_MOTION_QUALITY = 30,  // 0 discrete, 1 linear cast (MotionQuality motion-properties.ts:8-26)
     F_VEL_OVERRIDE = 31,    // numVelocityStepsOverride / numPositionStepsOverride (motion-properties.ts:59-61)
     F_POS_OVERRIDE = 32,
-    F_COUNT = 33
+    F_SCALE = 33,           // ScaledShape.scale (0 components read as 1)
+    F_TPOS = 36,            // TransformedShape.position
+    F_TROT = 39,            // TransformedShape.quaternion (all zero: identity)
+    F_COM_OFFSET = 43,      // OffsetCenterOfMassShape.offset
+    F_MASS_MODE = 46,       // MassPropertiesOverride: 0 from the shape, 1 mass given, 2 mass and inertia given
+    F_MASS = 47,            // RigidBodySettings.mass / massPropertiesOverride.mass
+    F_INERTIA = 48,         // massPropertiesOverride inertia xx xy xz yy yz zz
+    F_COUNT = 54
 };
 
 void *orc_world_create(const double *settings, int n_obj, const int *obj_to_bp, int n_bp, const uint8_t *obj_pairs,
@@ -1919,6 +1949,70 @@ void orc_world_destroy(void *wp) { delete (World *)wp; }
 
 // rigidBody.create rigid-body.ts:390-434 for each row
 // Shape fields of a body row (F_SHAPE, F_DENSITY, F_P0..F_P0 + 3); false for an unknown type.
+// The decorators of a body row around its leaf shape, nested as
+// OffsetCenterOfMass(Transformed(Scaled(leaf))): the scale baked into the leaf (box half
+// extents |s| per axis with the convex radius min(r min|s|, 0.05) of setBoxSupport
+// support.ts:343-372; sphere and capsule |s.x|, sphere.ts:195-197, capsule.ts:308-318), the
+// local bounds of computeScaledLocalBounds / computeTransformedLocalBounds (scaled.ts,
+// transformed.ts), the centre of mass of computeTransformedCenterOfMass +
+// computeOffsetCenterOfMassCenterOfMass and the inner radius min|s| x the leaf's (scaled.ts
+// getInnerRadius).  A scaled convex hull or mesh is refused.
+static bool decorate(Shape &s, const double *r) {
+    V3 sc{r[F_SCALE], r[F_SCALE + 1], r[F_SCALE + 2]};
+    if (sc.x == 0) sc.x = 1;
+    if (sc.y == 0) sc.y = 1;
+    if (sc.z == 0) sc.z = 1;
+    V3 tp{r[F_TPOS], r[F_TPOS + 1], r[F_TPOS + 2]};
+    Q4 tq{r[F_TROT], r[F_TROT + 1], r[F_TROT + 2], r[F_TROT + 3]};
+    if (tq.x == 0 && tq.y == 0 && tq.z == 0 && tq.w == 0) tq = {0, 0, 0, 1};
+    V3 off{r[F_COM_OFFSET], r[F_COM_OFFSET + 1], r[F_COM_OFFSET + 2]};
+    const bool scaled = sc.x != 1 || sc.y != 1 || sc.z != 1;
+    const bool transformed = tp.x != 0 || tp.y != 0 || tp.z != 0 || tq.x != 0 || tq.y != 0 || tq.z != 0 || tq.w != 1;
+    const bool offset = off.x != 0 || off.y != 0 || off.z != 0;
+    if (!scaled && !transformed && !offset) return true;
+    const V3 as{std::fabs(sc.x), std::fabs(sc.y), std::fabs(sc.z)};
+    const double minScale = std::min(as.x, std::min(as.y, as.z));
+    const double leafInner = inner_radius(s);
+    if (scaled) {
+        if (s.type == SHAPE_CONVEX_HULL || s.type == SHAPE_TRIANGLE_MESH) return false;
+        if (s.type == SHAPE_BOX) {
+            s.half_extents = {s.half_extents.x * as.x, s.half_extents.y * as.y, s.half_extents.z * as.z};
+            s.convex_radius = std::min(s.convex_radius * minScale, 0.05);
+        } else if (s.type == SHAPE_CYLINDER) {  // setCylinder*Support cylinder.ts: |s.x| throughout
+            s.radius *= as.x;
+            s.half_height *= as.x;
+            s.convex_radius *= as.x;
+        } else {
+            s.radius *= as.x;
+            s.half_height *= as.x;
+        }
+        // computeScaledLocalBounds: the leaf's bounds times |s| per axis
+        s.aabb = {{s.aabb.mn.x * as.x, s.aabb.mn.y * as.y, s.aabb.mn.z * as.z},
+                  {s.aabb.mx.x * as.x, s.aabb.mx.y * as.y, s.aabb.mx.z * as.z}};
+        // computeScaledCenterOfMass reads the scaled shape's own (zero) centre of mass
+        s.com = {0, 0, 0};
+    }
+    s.leafAabb = s.aabb;
+    if (transformed) {
+        Box3 b{{1e300, 1e300, 1e300}, {-1e300, -1e300, -1e300}};
+        for (int c = 0; c < 8; c++) {
+            V3 k{(c & 1) ? s.aabb.mx.x : s.aabb.mn.x, (c & 2) ? s.aabb.mx.y : s.aabb.mn.y,
+                 (c & 4) ? s.aabb.mx.z : s.aabb.mn.z};
+            V3 t = add(rotate(tq, k), tp);
+            b.mn = {std::min(b.mn.x, t.x), std::min(b.mn.y, t.y), std::min(b.mn.z, t.z)};
+            b.mx = {std::max(b.mx.x, t.x), std::max(b.mx.y, t.y), std::max(b.mx.z, t.z)};
+        }
+        s.aabb = b;
+        s.com = add(rotate(tq, s.com), tp);
+    }
+    s.com = add(s.com, off);
+    s.decorated = true;
+    s.tPos = tp;
+    s.tRot = tq;
+    s.innerRadius = (scaled ? minScale : 1.0) * leafInner;
+    return true;
+}
+
 static bool shape_from_row(Shape &s, const double *r, const World *w = nullptr) {
     s.type = (int)r[F_SHAPE];
     s.density = r[F_DENSITY];
@@ -1942,6 +2036,21 @@ static bool shape_from_row(Shape &s, const double *r, const World *w = nullptr) 
     } else if (s.type == SHAPE_SPHERE) {
         s.radius = r[F_P0];
         s.aabb = {{-s.radius, -s.radius, -s.radius}, {s.radius, s.radius, s.radius}};
+    } else if (s.type == SHAPE_EMPTY) {  // empty-shape.ts: a point of bounds, no mass
+        s.aabb = {{0, 0, 0}, {0, 0, 0}};
+    } else if (s.type == SHAPE_PLANE) {
+        // plane.ts create :77-98: the normal normalised, the constant as given
+        s.pn = normalize(V3{r[F_P0], r[F_P0 + 1], r[F_P0 + 2]});
+        s.pc = r[F_P0 + 3];
+        if (!(lensq(s.pn) > 0)) return false;
+        s.aabb = plane_local_bounds(s.pn, s.pc, s.halfExtent);
+    } else if (s.type == SHAPE_CYLINDER) {
+        // cylinder.ts: half height along Y, radius, convex radius (update: 0 <= cr <= h, r)
+        s.half_height = r[F_P0];
+        s.radius = r[F_P0 + 1];
+        s.convex_radius = r[F_P0 + 2];
+        if (!(s.convex_radius >= 0 && s.half_height >= s.convex_radius && s.radius >= s.convex_radius)) return false;
+        s.aabb = {{-s.radius, -s.half_height, -s.radius}, {s.radius, s.half_height, s.radius}};
     } else if (s.type == SHAPE_CAPSULE) {
         // capsule.ts:84-94: segment +-halfHeight on Y with radius r
         s.radius = r[F_P0];
@@ -1951,7 +2060,111 @@ static bool shape_from_row(Shape &s, const double *r, const World *w = nullptr) 
     } else {
         return false;
     }
-    return true;
+    return decorate(s, r);
+}
+
+// computeMassProperties of OffsetCenterOfMass(Transformed(Scaled(leaf))): the leaf's mass
+// and inertia, massProperties.scale (mass-properties.ts:59-112), rotate (:121-160) and
+// translate (:168-205); I is row-major
+static void decorated_mass(const double *r, const World *w, double &mass, double I[9]) {
+    double row[F_COUNT];
+    for (int k = 0; k < F_COUNT; k++) row[k] = r[k];
+    for (int k = F_SCALE; k < F_COUNT; k++) row[k] = 0;  // the leaf alone
+    Shape leaf;
+    shape_from_row(leaf, row, w);
+    V3 d;
+    shape_mass(leaf, mass, d);
+    double t[9] = {d.x, 0, 0, 0, d.y, 0, 0, 0, d.z};
+    if (leaf.type == SHAPE_CONVEX_HULL)
+        for (int k = 0; k < 9; k++) t[k] = leaf.hull->inertia[k] * leaf.density;
+    V3 sc{r[F_SCALE], r[F_SCALE + 1], r[F_SCALE + 2]};
+    if (sc.x == 0) sc.x = 1;
+    if (sc.y == 0) sc.y = 1;
+    if (sc.z == 0) sc.z = 1;
+    if (sc.x != 1 || sc.y != 1 || sc.z != 1) {
+        double half = 0.5 * (t[0] + t[4] + t[8]);
+        double q0 = sc.x * sc.x * (half - t[0]), q1 = sc.y * sc.y * (half - t[4]), q2 = sc.z * sc.z * (half - t[8]);
+        double ms = std::fabs(sc.x * sc.y * sc.z);
+        double n[9] = {q1 + q2, sc.x * sc.y * t[1], sc.x * sc.z * t[2], sc.x * sc.y * t[3], q0 + q2, sc.y * sc.z * t[5],
+                       sc.x * sc.z * t[6], sc.y * sc.z * t[7], q0 + q1};
+        for (int k = 0; k < 9; k++) t[k] = n[k] * ms;
+        mass *= ms;
+    }
+    Q4 tq{r[F_TROT], r[F_TROT + 1], r[F_TROT + 2], r[F_TROT + 3]};
+    if (!(tq.x == 0 && tq.y == 0 && tq.z == 0 && tq.w == 0) && !(tq.x == 0 && tq.y == 0 && tq.z == 0 && tq.w == 1)) {
+        M4 R4 = mat4_from_quat(tq);  // column-major: element (i, j) at m[4 j + i]
+        double rt[9], o[9];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double acc = 0;
+                for (int k = 0; k < 3; k++) acc += R4.m[4 * k + i] * t[3 * k + j];
+                rt[3 * i + j] = acc;
+            }
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double acc = 0;
+                for (int k = 0; k < 3; k++) acc += rt[3 * i + k] * R4.m[4 * k + j];
+                o[3 * i + j] = acc;
+            }
+        for (int k = 0; k < 9; k++) t[k] = o[k];
+    }
+    V3 off{r[F_COM_OFFSET], r[F_COM_OFFSET + 1], r[F_COM_OFFSET + 2]};
+    if (off.x != 0 || off.y != 0 || off.z != 0) {
+        double dd = dot(off, off), v[3] = {off.x, off.y, off.z};
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) t[3 * i + j] += mass * ((i == j ? dd : 0.0) - v[i] * v[j]);
+    }
+    for (int k = 0; k < 9; k++) I[k] = t[k];
+}
+
+// Mass properties of a body row (rigid-body.ts setRigidBody :309-326, updateShape :676-700,
+// MotionProperties.setMassProperties motion-properties.ts:419-491); -1 when the row asks for a
+// mass the shape cannot give
+static int setup_mass(Body &b, const Shape &s, const double *r, const World *w) {
+    double mass;
+    V3 idiag;
+    shape_mass(s, mass, idiag);
+    // meshes and planes have no mass (triangle-mesh.ts:153-158, plane.ts:120-122)
+    if ((s.type == SHAPE_TRIANGLE_MESH || s.type == SHAPE_PLANE) && b.motion == DYNAMIC) return -1;
+    const int massMode = (int)r[F_MASS_MODE];
+    if (massMode != 0 && b.motion != STATIC && s.type != SHAPE_TRIANGLE_MESH && s.type != SHAPE_PLANE) {
+        // rigid-body.ts setRigidBody :309-326 and updateShape :676-700: a given mass scales the
+        // shape's inertia (scaleToMass mass-properties.ts:220-240), or mass and inertia given
+        double I[9];
+        if (s.decorated) {
+            decorated_mass(r, w, mass, I);
+        } else if (s.type == SHAPE_CONVEX_HULL) {
+            for (int k = 0; k < 9; k++) I[k] = s.hull->inertia[k] * s.density;
+        } else {
+            double t[9] = {idiag.x, 0, 0, 0, idiag.y, 0, 0, 0, idiag.z};
+            for (int k = 0; k < 9; k++) I[k] = t[k];
+        }
+        if (massMode == 1) {
+            double m = r[F_MASS];
+            if (mass > 0)
+                for (int k = 0; k < 9; k++) I[k] *= m / mass;
+            mass = m;
+        } else {
+            const double *t = r + F_INERTIA;
+            double g[9] = {t[0], t[1], t[2], t[1], t[3], t[4], t[2], t[4], t[5]};
+            for (int k = 0; k < 9; k++) I[k] = g[k];
+            mass = r[F_MASS];
+        }
+        if ((b.dof & 7) != 0 && !(mass > 0)) return -1;  // setMassProperties asserts a mass
+        set_mass_properties_tensor(b, mass, I, 1.0);
+    } else if (b.motion != STATIC && s.type != SHAPE_TRIANGLE_MESH && s.type != SHAPE_PLANE) {
+        if ((b.dof & 7) != 0 && !(mass > 0)) return -1;  // an empty shape needs a given mass
+        if (s.decorated) {
+            double I[9];
+            decorated_mass(r, w, mass, I);
+            set_mass_properties_tensor(b, mass, I, 1.0);
+        } else if (s.type == SHAPE_CONVEX_HULL) {
+            set_mass_properties_tensor(b, mass, s.hull->inertia, s.density);
+        } else {
+            set_mass_properties(b, mass, idiag);
+        }
+    }
+    return 0;
 }
 
 int orc_add_bodies(void *wp, const double *rows, int n) {
@@ -1982,16 +2195,7 @@ int orc_add_bodies(void *wp, const double *rows, int n) {
         b.posOverride = (int)r[F_POS_OVERRIDE];
         b.groups = (uint32_t)r[F_GROUPS];
         b.mask = (uint32_t)r[F_MASK];
-        double mass;
-        V3 idiag;
-        shape_mass(s, mass, idiag);
-        if (s.type == SHAPE_TRIANGLE_MESH && b.motion == DYNAMIC) return -1;  // meshes have no mass
-        if (b.motion != STATIC && s.type != SHAPE_TRIANGLE_MESH) {
-            if (s.type == SHAPE_CONVEX_HULL)
-                set_mass_properties_tensor(b, mass, s.hull->inertia, s.density);
-            else
-                set_mass_properties(b, mass, idiag);
-        }
+        if (setup_mass(b, s, r, &w) != 0) return -1;
         update_com(b);
         update_aabb(b);
         w.bodies.push_back(b);
@@ -2594,7 +2798,10 @@ void orc_cast_rays(void *wp, const double *rays, int n, uint32_t layerMask, uint
             if (!(ray_fraction_to_box(o, d, len, b.aabb) < std::numeric_limits<double>::infinity())) continue;
             double f;
             uint32_t sub;
-            if (!cast_ray_vs_shape(b.shape, b.position, b.quat, o, d, len, treatConvexAsSolid != 0, best, f, sub)) continue;
+            V3 gp;
+            Q4 gq;
+            geometry_pose(b.shape, b.position, b.quat, gp, gq);
+            if (!cast_ray_vs_shape(b.shape, gp, gq, o, d, len, treatConvexAsSolid != 0, best, f, sub)) continue;
             if (f < best || (f == best && hit >= 0 && b.index < hit)) {
                 best = f;
                 hit = b.index;
@@ -2624,7 +2831,10 @@ void orc_collide_points(void *wp, const double *pts, int n, uint32_t layerMask, 
             if (!(layerMask & (1u << b.objectLayer))) continue;
             if (!box_contains(b.aabb, p)) continue;
             uint32_t sub;
-            if (!point_in_shape(b.shape, b.position, b.quat, p, tol, sub)) continue;
+            V3 gp;
+            Q4 gq;
+            geometry_pose(b.shape, b.position, b.quat, gp, gq);
+            if (!point_in_shape(b.shape, gp, gq, p, tol, sub)) continue;
             if (c++ == 0) {
                 first = b.index;
                 fsub = sub;
@@ -2664,6 +2874,9 @@ int orc_cast_shapes(void *wp, const double *qs, int n, uint32_t layerMask, uint3
         for (auto &B : W.bodies) {
             if (!((groups & B.mask) != 0 && (B.groups & mask) != 0)) continue;
             if (!(layerMask & (1u << B.objectLayer))) continue;
+            V3 gpB;
+            Q4 gqB;
+            geometry_pose(B.shape, B.position, B.quat, gpB, gqB);
             auto collect = [&](double fraction, V3 pa, V3 axis) {
                 if (!(fraction < best || (fraction == best && hit >= 0 && B.index < hit))) return;
                 best = fraction;
@@ -2671,18 +2884,25 @@ int orc_cast_shapes(void *wp, const double *qs, int n, uint32_t layerMask, uint3
                 hn = neg(normalize(axis));
                 hp = pa;
             };
+            if (B.shape.type == SHAPE_EMPTY) continue;
+            if (B.shape.type == SHAPE_PLANE) {
+                CastHit h;
+                if (cast_convex_vs_plane(h, sa, pA, qA, disp, B.shape, gpB, gqB, best, false))
+                    collect(h.fraction, h.pa, h.axis);
+                continue;
+            }
             if (B.shape.type == SHAPE_TRIANGLE_MESH) {
                 auto onHit = [&](const CastMeshHit &h) { collect(h.fraction, h.pa, h.axis); };
                 auto earlyOut = [&]() { return best; };
                 if (sa.type == SHAPE_SPHERE)
-                    cast_sphere_vs_mesh(sa, pA, disp, B.shape, B.position, B.quat, onHit, earlyOut);
+                    cast_sphere_vs_mesh(sa, pA, disp, B.shape, gpB, gqB, onHit, earlyOut);
                 else
-                    cast_convex_vs_mesh(sa, pA, qA, disp, B.shape, B.position, B.quat, onHit, earlyOut);
+                    cast_convex_vs_mesh(sa, pA, qA, disp, B.shape, gpB, gqB, onHit, earlyOut);
                 continue;
             }
             CastHit h;
             const double maxL = (hit >= 0 && B.index < hit) ? std::nextafter(best, 2.0) : best;
-            if (!cast_convex_vs_convex(h, sa, pA, qA, disp, B.shape, B.position, B.quat, maxL, false)) continue;
+            if (!cast_convex_vs_convex(h, sa, pA, qA, disp, B.shape, gpB, gqB, maxL, false)) continue;
             collect(h.fraction, h.pa, h.axis);
         }
         double *o = out + 7 * r;
@@ -2791,7 +3011,10 @@ int orc_collide_pair(const double *rowA, const double *rowB, double maxSep, doub
     CollideSettings cs;
     cs.maxSeparation = maxSep;
     Hit h;
-    bool f = collide_shapes(h, cs, s[0], p[0], q[0], s[1], p[1], q[1]);
+    V3 gp[2];
+    Q4 gq[2];
+    for (int k = 0; k < 2; k++) geometry_pose(s[k], p[k], q[k], gp[k], gq[k]);
+    bool f = collide_shapes(h, cs, s[0], gp[0], gq[0], s[1], gp[1], gq[1]);
     out[0] = f ? 1 : 0;
     out[1] = h.pa.x;
     out[2] = h.pa.y;
@@ -2812,10 +3035,8 @@ void orc_inverse_inertia(const double *row, double *out9) {
     Body b;
     Shape &s = b.shape;
     shape_from_row(s, row);
-    double mass;
-    V3 d;
-    shape_mass(s, mass, d);
-    set_mass_properties(b, mass, d);
+    b.motion = DYNAMIC;
+    setup_mass(b, s, row, nullptr);
     b.quat = {row[F_QUAT], row[F_QUAT + 1], row[F_QUAT + 2], row[F_QUAT + 3]};
     M4 I = inv_inertia_for_rotation(b, mat4_from_quat(b.quat));
     int k = 0;

@@ -19,7 +19,8 @@ namespace orc {
 constexpr double DEFAULT_CONVEX_RADIUS = 0.05;  // src/collision/support.ts:5
 constexpr uint32_t EMPTY_SUB_SHAPE_ID = 0xffffffffu;  // src/body/sub-shape.ts:4
 
-enum ShapeType : int { SHAPE_SPHERE = 0, SHAPE_BOX = 1, SHAPE_CAPSULE = 2, SHAPE_CONVEX_HULL = 3, SHAPE_TRIANGLE_MESH = 4 };
+enum ShapeType : int { SHAPE_SPHERE = 0, SHAPE_BOX = 1, SHAPE_CAPSULE = 2, SHAPE_CONVEX_HULL = 3, SHAPE_TRIANGLE_MESH = 4,
+                       SHAPE_CYLINDER = 5, SHAPE_PLANE = 6, SHAPE_EMPTY = 7 };
 
 // Triangle mesh as built (src/shapes/utils/triangle-mesh-data.ts, triangle-mesh-bvh.ts): welded
 // vertices, triangles (vertex indices, active-edge bits AB 1 / BC 2 / CA 4) in the order the BVH
@@ -54,19 +55,41 @@ struct Shape {
     int type = SHAPE_BOX;
     V3 half_extents;          // box
     double convex_radius = 0;  // box
-    double radius = 0;         // sphere / capsule
-    double half_height = 0;    // capsule (segment along Y)
+    double radius = 0;         // sphere / capsule / cylinder
+    double half_height = 0;    // capsule (segment along Y) / cylinder (along Y)
     double density = 1000;
+    V3 pn{0, 1, 0};            // plane: unit normal and constant (n . x + c = 0, solid below)
+    double pc = 0, halfExtent = 1000;  // plane: DEFAULT_PLANE_HALF_EXTENT plane.ts:36
     V3 com;                    // shape-local centre of mass
     Box3 aabb;                 // shape-local bounds
+    // decorators (scaled.ts, transformed.ts, offset-center-of-mass.ts) as
+    // OffsetCenterOfMass(Transformed(Scaled(leaf))): the scale is baked into the leaf's
+    // dimensions above; the collision geometry is the leaf at (tPos, tRot) in the body frame
+    // (collideTransformedVsShape transformed.ts); com, aabb and innerRadius are the decorated
+    // shape's
+    bool decorated = false;
+    Box3 leafAabb;             // the (scaled) leaf's bounds in its own frame, which its collisions use
+    V3 tPos{0, 0, 0};
+    Q4 tRot{0, 0, 0, 1};
+    double innerRadius = -1;   // getInnerRadius of the decorated shape (< 0: the leaf's)
 };
+// the pose of a shape's collision geometry for a body at (p, q)
+inline void geometry_pose(const Shape &s, V3 p, Q4 q, V3 &gp, Q4 &gq) {
+    if (!s.decorated) {
+        gp = p;
+        gq = q;
+        return;
+    }
+    gp = add(p, rotate(q, s.tPos));
+    gq = qmul(q, s.tRot);
+}
 
 // ----------------------------------------------------------------------------
 // Support functions (src/collision/support.ts, src/shapes/sphere.ts:173-266)
 // ----------------------------------------------------------------------------
 enum SupportMode { INCLUDE_CONVEX_RADIUS = 0, EXCLUDE_CONVEX_RADIUS = 1 };
 enum SupportKind { SUP_BOX, SUP_SPHERE_POINT, SUP_SPHERE_SURFACE, SUP_CAPSULE_SEGMENT, SUP_CAPSULE_SURFACE, SUP_HULL,
-                   SUP_TRIANGLE };
+                   SUP_TRIANGLE, SUP_CYLINDER };
 
 struct Support {
     int kind = SUP_BOX;
@@ -114,6 +137,16 @@ struct Support {
             }
             case SUP_CAPSULE_SEGMENT:  // capsule.ts: segment +-h on Y
                 return {0, d.y > 0 ? half_height : -half_height, 0};
+            case SUP_CYLINDER: {  // cylinder{No,With}ConvexGetSupport cylinder.ts
+                double hl = std::sqrt(d.x * d.x + d.z * d.z);
+                V3 o{0, d.y >= 0 ? half_height : -half_height, 0};
+                if (hl > 0) {
+                    double s = radius / hl;
+                    o.x = d.x * s;
+                    o.z = d.z * s;
+                }
+                return o;
+            }
             case SUP_CAPSULE_SURFACE: {  // capsuleWithConvexGetSupport capsule.ts:321-338
                 double l = d.x * d.x + d.y * d.y + d.z * d.z;
                 if (!(l > 0)) return {0, half_height, 0};
@@ -175,6 +208,19 @@ inline Support make_support(const Shape &s, SupportMode mode) {
             o.he = s.half_extents;
             o.convex_radius = 0;
         }
+    } else if (s.type == SHAPE_CYLINDER) {
+        // getCylinderSupportFunction cylinder.ts: the full cylinder, or the one shrunk by the
+        // convex radius with that radius reported
+        o.kind = SUP_CYLINDER;
+        if (mode == INCLUDE_CONVEX_RADIUS) {
+            o.half_height = s.half_height;
+            o.radius = s.radius;
+            o.convex_radius = 0;
+        } else {
+            o.half_height = s.half_height - s.convex_radius;
+            o.radius = s.radius - s.convex_radius;
+            o.convex_radius = s.convex_radius;
+        }
     } else if (s.type == SHAPE_SPHERE) {
         if (mode == INCLUDE_CONVEX_RADIUS) {
             o.kind = SUP_SPHERE_SURFACE;
@@ -196,6 +242,14 @@ inline Support make_support(const Shape &s, SupportMode mode) {
         }
     }
     return o;
+}
+
+// SupportFunctionMode.DEFAULT: the box and the cylinder include their convex radius
+// (support.ts:351, cylinder.ts:412), the other shapes exclude it (sphere.ts:258,
+// capsule.ts:396, convex-hull.ts:978)
+inline Support make_support_default(const Shape &s) {
+    return make_support(s, (s.type == SHAPE_BOX || s.type == SHAPE_CYLINDER) ? INCLUDE_CONVEX_RADIUS
+                                                                            : EXCLUDE_CONVEX_RADIUS);
 }
 
 // ----------------------------------------------------------------------------
@@ -1159,6 +1213,35 @@ inline void transform_face(Face &f, V3 p, Q4 q) {
     }
 }
 
+// cylinder getSupportingFace cylinder.ts: the side edge facing away from dir, or the cap
+// octagon (CYLINDER_CAP_OCTAGON) turned towards dir's horizontal part
+inline void cylinder_supporting_face(Face &f, V3 d, double h, double r) {
+    static const double OCT[8][3] = {{0.0, 1.0, 1.0},          {0.707106769, 1.0, 0.707106769},
+                                     {1.0, 1.0, 0.0},          {0.707106769, 1.0, -0.707106769},
+                                     {0.0, 1.0, -1.0},         {-0.707106769, 1.0, -0.707106769},
+                                     {-1.0, 1.0, 0.0},         {-0.707106769, 1.0, 0.707106769}};
+    double xz = d.x * d.x + d.z * d.z, yy = d.y * d.y;
+    if (xz > yy) {
+        double fct = -r / std::sqrt(xz);
+        f.n = 2;
+        f.v[0] = {d.x * fct, h, d.z * fct};
+        f.v[1] = {d.x * fct, -h, d.z * fct};
+        return;
+    }
+    double sx = d.y < 0 ? r : -r, sy = d.y < 0 ? h : -h, sz = r;
+    double c = 1, sn = 0;
+    if (xz > 0.00765427 * yy) {
+        double hl = std::sqrt(xz);
+        c = d.x / hl;
+        sn = d.z / hl;
+    }
+    f.n = 8;
+    for (int i = 0; i < 8; i++) {
+        double x = sx * OCT[i][0], y = sy * OCT[i][1], z = sz * OCT[i][2];
+        f.v[i] = {x * c - z * sn, y, x * sn + z * c};
+    }
+}
+
 // box getSupportingFace box.ts:129-332 (scale not inside out)
 inline void box_supporting_face(Face &f, V3 dir, V3 he) {
     double hx = he.x, hy = he.y, hz = he.z;
@@ -1257,6 +1340,9 @@ inline void shape_supporting_face(Face &f, const Shape &s, V3 dir, V3 p, Q4 q) {
     } else if (s.type == SHAPE_CAPSULE) {
         capsule_supporting_face(f, dir, s.half_height, s.radius);
         if (f.n > 0) transform_face(f, p, q);
+    } else if (s.type == SHAPE_CYLINDER) {
+        cylinder_supporting_face(f, dir, s.half_height, s.radius);
+        transform_face(f, p, q);
     } else {
         f.n = 0;
     }
@@ -1612,6 +1698,162 @@ struct CastHit {
     V3 pa, pb, axis;  // world-space points and the unnormalised penetration axis
 };
 
+// ---- plane shape (src/shapes/plane.ts) ------------------------------------------------
+// getOrthogonalBasis :210-233
+inline void plane_basis(V3 n, V3 &p1, V3 &p2) {
+    p1 = cross(n, V3{0, 1, 0});
+    double l = lensq(p1);
+    p1 = l < 1e-6 ? V3{1, 0, 0} : scale(p1, 1 / std::sqrt(l));
+    p2 = normalize(cross(p1, n));
+    p1 = normalize(cross(n, p2));
+}
+// getPlaneVertices :235-271
+inline void plane_vertices(V3 out[4], V3 n, double c, double he) {
+    V3 p1, p2;
+    plane_basis(n, p1, p2);
+    p1 = scale(p1, he);
+    p2 = scale(p2, he);
+    V3 pt = scale(n, -c);
+    out[0] = add(pt, add(p1, p2));
+    out[1] = add(pt, sub(p1, p2));
+    out[2] = sub(pt, add(p1, p2));
+    out[3] = add(pt, add(neg(p1), p2));
+}
+// computePlaneLocalBounds :273-295: the face's corners and the corners one half extent behind
+inline Box3 plane_local_bounds(V3 n, double c, double he) {
+    V3 v[4];
+    plane_vertices(v, n, c, he);
+    Box3 b{{1e300, 1e300, 1e300}, {-1e300, -1e300, -1e300}};
+    auto grow = [&](V3 p) {
+        b.mn = {std::min(b.mn.x, p.x), std::min(b.mn.y, p.y), std::min(b.mn.z, p.z)};
+        b.mx = {std::max(b.mx.x, p.x), std::max(b.mx.y, p.y), std::max(b.mx.z, p.z)};
+    };
+    for (V3 p : v) {
+        grow(p);
+        grow(sub(p, scale(n, he)));
+    }
+    return b;
+}
+// transformPlane :196-208 for a rotation and translation
+inline void transform_plane(V3 &n, double &c, V3 n0, double c0, Q4 q, V3 t) {
+    n = rotate(q, n0);
+    c = c0 - dot(t, n);
+}
+// getAdaptivePlaneSupportingFace :655-706: a square on the world plane centred under the convex
+// shape's position, |size of its bounds| from the centre to each side
+inline void plane_adaptive_face(Face &f, const Shape &convex, V3 convexPos, V3 nw, double cw) {
+    V3 center = sub(convexPos, scale(nw, dot(nw, convexPos) + cw));
+    V3 p1, p2;
+    plane_basis(nw, p1, p2);
+    const Box3 &a = convex.decorated ? convex.leafAabb : convex.aabb;
+    double size = len(sub(a.mx, a.mn));
+    p1 = scale(p1, size);
+    p2 = scale(p2, size);
+    f.n = 4;
+    f.v[0] = add(center, add(p1, p2));
+    f.v[1] = add(center, sub(p1, p2));
+    f.v[2] = sub(center, add(p1, p2));
+    f.v[3] = add(center, add(neg(p1), p2));
+}
+// collideConvexVsPlane :474-629: A convex at (pA, qA), B the plane shape at (pB, qB)
+inline bool collide_convex_vs_plane(Hit &hit, const CollideSettings &cs, const Shape &sa, V3 pA, Q4 qA,
+                                    const Shape &sb, V3 pB, Q4 qB) {
+    // the plane in A's frame: inverse(A) x B
+    Q4 iqA = qconj(qA);
+    V3 nl;
+    double cl;
+    transform_plane(nl, cl, sb.pn, sb.pc, qmul(iqA, qB), rotate(iqA, sub(pB, pA)));
+    Support S = make_support_default(sa);
+    V3 sp = S.get(neg(nl));
+    double sd = dot(nl, sp) + cl;
+    double cr = S.convex_radius;
+    double pen = -sd + cr;
+    if (!(pen > -cs.maxSeparation)) return false;
+    V3 p1 = sub(sp, scale(nl, cr)), p2 = sub(sp, scale(nl, sd));
+    hit.pa = add(pA, rotate(qA, p1));
+    hit.pb = add(pA, rotate(qA, p2));
+    hit.axis = rotate(qA, neg(nl));
+    hit.penetration = pen;
+    hit.faceA.n = hit.faceB.n = 0;
+    if (cs.collectFaces) {
+        shape_supporting_face(hit.faceA, sa, nl, pA, qA);
+        if (hit.faceA.n > 0) {
+            V3 nw;
+            double cw;
+            transform_plane(nw, cw, sb.pn, sb.pc, qB, pB);
+            plane_adaptive_face(hit.faceB, sa, pA, nw, cw);
+        }
+    }
+    return true;
+}
+// castRayVsPlane :320-398 (treatConvexAsSolid, back faces culled unless asked)
+inline bool cast_ray_vs_plane(const Shape &s, V3 pos, Q4 q, V3 origin, V3 dir, double length, bool solid,
+                              bool backfaces, double maxFraction, double &fraction) {
+    V3 n;
+    double c;
+    transform_plane(n, c, s.pn, s.pc, q, pos);
+    double d = dot(n, origin) + c;
+    if (solid && d <= 0.0 && maxFraction > 0.0) {
+        fraction = 0;
+        return true;
+    }
+    double dn = dot(dir, n);
+    if (std::fabs(dn) < 1e-10) return false;
+    if (!backfaces && dn > 0.0) return false;
+    double f = -d / dn / length;
+    if (f >= 0.0 && f < maxFraction) {
+        fraction = f;
+        return true;
+    }
+    return false;
+}
+// collidePointVsPlane :404-460
+inline bool point_in_plane(const Shape &s, V3 pos, Q4 q, V3 point) {
+    V3 n;
+    double c;
+    transform_plane(n, c, s.pn, s.pc, q, pos);
+    return dot(n, point) + c < 0.0;
+}
+// castConvexVsPlane :727-918: the plane's own (unposed) equation against the world support point,
+// the hit's points carried by the plane body's transform, as the reference computes them
+inline bool cast_convex_vs_plane(CastHit &hit, const Shape &sa, V3 pA, Q4 qA, V3 disp, const Shape &sb, V3 pB, Q4 qB,
+                                 double earlyOut, bool backfaces) {
+    const V3 n = sb.pn;
+    Support S = make_support_default(sa);
+    V3 nInA = neg(rotate(qconj(qA), n));
+    V3 spw = add(pA, rotate(qA, S.get(nInA)));
+    double sd = dot(n, spw) + sb.pc;
+    double cr = S.convex_radius;
+    double pen = -sd + cr;
+    double dn = dot(disp, n);
+    double fraction;
+    V3 p1, p2;
+    Q4 hq = qB;
+    V3 ht = pB;
+    if (pen > 0.0) {
+        if (!backfaces && dn > 0.0) return false;
+        if (pen <= -earlyOut) return false;
+        fraction = 0;
+        p1 = add(pB, rotate(qB, sub(spw, scale(n, cr))));
+        p2 = add(pB, rotate(qB, sub(spw, scale(n, sd))));
+    } else if (dn < 0.0) {
+        fraction = pen / dn;
+        if (fraction >= earlyOut) return false;
+        // mat4.translate(planeToWorld, disp x fraction): the translation goes through the rotation
+        ht = add(pB, rotate(qB, scale(disp, fraction)));
+        p1 = add(ht, rotate(qB, sub(spw, scale(n, cr))));
+        p2 = p1;
+    } else {
+        return false;
+    }
+    hit.fraction = fraction;
+    hit.pa = p1;
+    hit.pb = p2;
+    // vec3.transformMat4 of -n by comHit (a point transform: the translation is added)
+    hit.axis = add(ht, rotate(hq, neg(n)));
+    return true;
+}
+
 // gjkCastShape gjk.ts:853-1259.  A (already placed in B's space) moves by disp, B is fixed;
 // returns false on a miss, else the time of impact and the closest points at that time.
 inline bool gjk_cast_shape(double &lambdaOut, V3 &pa, V3 &pb, V3 &axisOut, const Support &A, const Support &B,
@@ -1876,11 +2118,12 @@ inline void collide_convex_vs_mesh(std::vector<Hit> &out, const CollideSettings 
     Q4 cInMQ = qmul(iqB, qA);
     V3 cInMP = rotate(iqB, sub(pA, pB));
     const double ms = cs.maxSeparation;
-    Box3 b1{sub(sa.aabb.mn, V3{ms, ms, ms}), add(sa.aabb.mx, V3{ms, ms, ms})};
+    const Box3 &la = sa.decorated ? sa.leafAabb : sa.aabb;
+    Box3 b1{sub(la.mn, V3{ms, ms, ms}), add(la.mx, V3{ms, ms, ms})};
     Box3 b12{{1e300, 1e300, 1e300}, {-1e300, -1e300, -1e300}};
     for (int c = 0; c < 8; c++) {
-        V3 p{(c & 1) ? sa.aabb.mx.x : sa.aabb.mn.x, (c & 2) ? sa.aabb.mx.y : sa.aabb.mn.y,
-             (c & 4) ? sa.aabb.mx.z : sa.aabb.mn.z};
+        const Box3 &lb = sa.decorated ? sa.leafAabb : sa.aabb;
+        V3 p{(c & 1) ? lb.mx.x : lb.mn.x, (c & 2) ? lb.mx.y : lb.mn.y, (c & 4) ? lb.mx.z : lb.mn.z};
         V3 q = add(rotate(cInMQ, p), cInMP);
         b12.mn = {std::min(b12.mn.x, q.x), std::min(b12.mn.y, q.y), std::min(b12.mn.z, q.z)};
         b12.mx = {std::max(b12.mx.x, q.x), std::max(b12.mx.y, q.y), std::max(b12.mx.z, q.z)};
@@ -2028,8 +2271,8 @@ inline void cast_convex_vs_mesh(const Shape &sa, V3 pA, Q4 qA, V3 disp, const Sh
     V3 dInB = rotate(iqB, disp);
     Box3 base{{1e300, 1e300, 1e300}, {-1e300, -1e300, -1e300}};
     for (int c = 0; c < 8; c++) {
-        V3 p{(c & 1) ? sa.aabb.mx.x : sa.aabb.mn.x, (c & 2) ? sa.aabb.mx.y : sa.aabb.mn.y,
-             (c & 4) ? sa.aabb.mx.z : sa.aabb.mn.z};
+        const Box3 &lb = sa.decorated ? sa.leafAabb : sa.aabb;
+        V3 p{(c & 1) ? lb.mx.x : lb.mn.x, (c & 2) ? lb.mx.y : lb.mn.y, (c & 4) ? lb.mx.z : lb.mn.z};
         V3 q = add(rotate(qAInB, p), posAInB);
         base.mn = {std::min(base.mn.x, q.x), std::min(base.mn.y, q.y), std::min(base.mn.z, q.z)};
         base.mx = {std::max(base.mx.x, q.x), std::max(base.mx.y, q.y), std::max(base.mx.z, q.z)};
@@ -2356,6 +2599,11 @@ inline bool cast_ray_vs_shape(const Shape &s, V3 pos, Q4 q, V3 origin, V3 dir, d
         if (found) fraction = best;
         return found;
     }
+    if (s.type == SHAPE_EMPTY) return false;
+    if (s.type == SHAPE_PLANE) {
+        subId = EMPTY_SUB_SHAPE_ID;
+        return cast_ray_vs_plane(s, pos, q, origin, dir, length, solid, false, maxFraction, fraction);
+    }
     Support S = make_support(s, INCLUDE_CONVEX_RADIUS);
     double lambda;
     if (!gjk_cast_ray(lambda, lo, scale(ld, length), 1e-3, S, maxFraction)) return false;
@@ -2418,15 +2666,18 @@ inline bool box_contains(const Box3 &b, V3 p) {  // box3.containsPoint
 // counted).  True when the point is inside; subId is the mesh's last-hit triangle.
 inline bool point_in_shape(const Shape &s, V3 pos, Q4 q, V3 point, double tol, uint32_t &subId) {
     subId = EMPTY_SUB_SHAPE_ID;
+    if (s.type == SHAPE_EMPTY) return false;
+    if (s.type == SHAPE_PLANE) return point_in_plane(s, pos, q, point);
     V3 l = sub(point, pos);
     if (s.type == SHAPE_SPHERE) return dot(l, l) <= s.radius * s.radius;
     V3 lp = rotate(qconj(q), l);
     if (s.type == SHAPE_BOX)
         return std::fabs(lp.x) <= s.half_extents.x && std::fabs(lp.y) <= s.half_extents.y &&
                std::fabs(lp.z) <= s.half_extents.z;
-    if (!box_contains(s.aabb, lp)) return false;
+    const Box3 &la = s.decorated ? s.leafAabb : s.aabb;
+    if (!box_contains(la, lp)) return false;
     if (s.type == SHAPE_TRIANGLE_MESH) {
-        double h = s.aabb.mx.y - s.aabb.mn.y;
+        double h = la.mx.y - la.mn.y;
         uint32_t last = EMPTY_SUB_SHAPE_ID;
         int n = mesh_ray_hit_count(*s.mesh, lp, {0, 1, 0}, h * 1.1, last);
         if ((n & 1) == 0) return false;
@@ -2453,6 +2704,16 @@ inline void collide_hits(std::vector<Hit> &out, const CollideSettings &cs, const
 // collideShapeVsShape narrowphase.ts:172-238 (dispatch for the supported convex shapes)
 inline bool collide_shapes(Hit &hit, const CollideSettings &cs, const Shape &sa, V3 pA, Q4 qA, const Shape &sb,
                            V3 pB, Q4 qB) {
+    if (sa.type == SHAPE_EMPTY || sb.type == SHAPE_EMPTY) return false;
+    if (sa.type == SHAPE_PLANE && sb.type == SHAPE_PLANE) return false;
+    if (sb.type == SHAPE_PLANE) return collide_convex_vs_plane(hit, cs, sa, pA, qA, sb, pB, qB);
+    if (sa.type == SHAPE_PLANE) {  // reversedCollideShapeVsShape collide-shape-vs-shape.ts:227-354
+        if (!collide_convex_vs_plane(hit, cs, sb, pB, qB, sa, pA, qA)) return false;
+        std::swap(hit.pa, hit.pb);
+        hit.axis = neg(hit.axis);
+        std::swap(hit.faceA, hit.faceB);
+        return true;
+    }
     if (sa.type == SHAPE_SPHERE && sb.type == SHAPE_SPHERE) return collide_sphere_vs_sphere(hit, sa, pA, sb, pB);
     return collide_convex_vs_convex(hit, cs, sa, pA, qA, sb, pB, qB);
 }
@@ -2461,6 +2722,9 @@ inline void collide_hits(std::vector<Hit> &out, const CollideSettings &cs, const
                          const Shape &sb, V3 pB, Q4 qB, V3 movement) {
     const bool ma = sa.type == SHAPE_TRIANGLE_MESH, mb = sb.type == SHAPE_TRIANGLE_MESH;
     if (ma && mb) return;
+    if (sa.type == SHAPE_EMPTY || sb.type == SHAPE_EMPTY) return;  // empty-shape.ts: registers nothing
+    // a plane collides with convex shapes only (plane.ts register :297-308)
+    if ((ma && sb.type == SHAPE_PLANE) || (mb && sa.type == SHAPE_PLANE)) return;
     if (mb) {
         if (sa.type == SHAPE_SPHERE)
             collide_sphere_vs_mesh(out, cs, sa, pA, sb, pB, qB, movement);

@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 
-F_COUNT = 33  # doubles per body row, see oracle.cpp (enum F_*)
+F_COUNT = 54  # doubles per body row, see oracle.cpp (enum F_*)
 STATE = 17    # pos3 quat4 linvel3 angvel3 com3 sleeping
 
 _lib = None
@@ -118,6 +118,13 @@ def rows_from_bodies(b: np.ndarray) -> np.ndarray:
     r[:, 30] = b["motion_quality"]
     r[:, 31] = b["num_velocity_steps_override"]
     r[:, 32] = b["num_position_steps_override"]
+    r[:, 33:36] = b["shape_scale"]
+    r[:, 36:39] = b["shape_position"]
+    r[:, 39:43] = b["shape_quaternion"]
+    r[:, 43:46] = b["com_offset"]
+    r[:, 46] = b["mass_properties_mode"]
+    r[:, 47] = b["mass"]
+    r[:, 48:54] = b["inertia"]
     return np.ascontiguousarray(r)
 
 
