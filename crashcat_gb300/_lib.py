@@ -228,6 +228,10 @@ EXPORTS = {
     "cc_world_set_joint_enabled": ([C.c_void_p, C.c_int32, C.c_int32, C.c_int32], C.c_int),
     "cc_world_get_joint_lambdas": ([C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)],
                                    C.c_int),
+    "cc_world_add_six_dof_joints": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
+    "cc_world_set_six_dof_limits": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
+    "cc_world_set_six_dof_motor": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.c_void_p], C.c_int),
     "cc_status_string": ([C.c_int], C.c_char_p),
 }
 
@@ -301,7 +305,7 @@ def swing_twist_defaults(n: int) -> np.ndarray:
 
 # cc_joint_type (the reference's ConstraintType) and the point, distance, fixed, cone and
 # slider joint descriptions
-JOINT_POINT, JOINT_DISTANCE, JOINT_HINGE, JOINT_SLIDER, JOINT_FIXED, JOINT_CONE, JOINT_SWING_TWIST = range(7)
+JOINT_POINT, JOINT_DISTANCE, JOINT_HINGE, JOINT_SLIDER, JOINT_FIXED, JOINT_CONE, JOINT_SWING_TWIST, JOINT_SIX_DOF = range(8)
 _JOINT_TAIL = [("priority", np.int32), ("enabled", np.int32),
                ("num_velocity_steps_override", np.int32), ("num_position_steps_override", np.int32)]
 POINT_JOINT_DTYPE = np.dtype([("body_a", np.int32), ("body_b", np.int32), ("space", np.int32),
@@ -327,11 +331,23 @@ SLIDER_JOINT_DTYPE = np.dtype([("body_a", np.int32), ("body_b", np.int32), ("spa
                          ("min_force_limit", np.float32), ("max_force_limit", np.float32),
                          ("motor_state", np.int32), ("target_velocity", np.float32),
                          ("target_position", np.float32)] + _JOINT_TAIL)
+SIX_DOF_JOINT_DTYPE = np.dtype([("body_a", np.int32), ("body_b", np.int32), ("space", np.int32),
+                                ("swing_type", np.int32), ("position_a", np.float32, 3), ("position_b", np.float32, 3),
+                                ("axis_x_a", np.float32, 3), ("axis_y_a", np.float32, 3),
+                                ("axis_x_b", np.float32, 3), ("axis_y_b", np.float32, 3),
+                                ("limit_min", np.float32, 6), ("limit_max", np.float32, 6),
+                                ("max_friction", np.float32, 6), ("limits_spring", SPRING_DTYPE, 3),
+                                ("motor_spring", SPRING_DTYPE, 6), ("motor_min_force", np.float32, 6),
+                                ("motor_max_force", np.float32, 6), ("motor_state", np.int32, 6),
+                                ("target_velocity", np.float32, 3), ("target_angular_velocity", np.float32, 3),
+                                ("target_position", np.float32, 3), ("target_orientation", np.float32, 4)]
+                               + _JOINT_TAIL)
 JOINT_DTYPES = {JOINT_POINT: POINT_JOINT_DTYPE, JOINT_DISTANCE: DISTANCE_JOINT_DTYPE,
-                JOINT_FIXED: FIXED_JOINT_DTYPE, JOINT_CONE: CONE_JOINT_DTYPE, JOINT_SLIDER: SLIDER_JOINT_DTYPE}
+                JOINT_FIXED: FIXED_JOINT_DTYPE, JOINT_CONE: CONE_JOINT_DTYPE, JOINT_SLIDER: SLIDER_JOINT_DTYPE,
+                JOINT_SIX_DOF: SIX_DOF_JOINT_DTYPE}
 JOINT_ADDERS = {JOINT_POINT: "cc_world_add_point_joints", JOINT_DISTANCE: "cc_world_add_distance_joints",
                 JOINT_FIXED: "cc_world_add_fixed_joints", JOINT_CONE: "cc_world_add_cone_joints",
-                JOINT_SLIDER: "cc_world_add_slider_joints"}
+                JOINT_SLIDER: "cc_world_add_slider_joints", JOINT_SIX_DOF: "cc_world_add_six_dof_joints"}
 
 
 def joint_defaults(joint_type: int, n: int) -> np.ndarray:
@@ -346,6 +362,16 @@ def joint_defaults(joint_type: int, n: int) -> np.ndarray:
     elif joint_type == JOINT_FIXED:
         h["axis_x_a"] = h["axis_x_b"] = (1.0, 0.0, 0.0)
         h["axis_y_a"] = h["axis_y_b"] = (0.0, 1.0, 0.0)
+    elif joint_type == JOINT_SIX_DOF:  # six-dof-constraint.ts:119-163, 405-430
+        h["axis_x_a"] = h["axis_x_b"] = (1.0, 0.0, 0.0)
+        h["axis_y_a"] = h["axis_y_b"] = (0.0, 1.0, 0.0)
+        h["limit_min"] = (-np.inf, -np.inf, -np.inf, -np.pi, -np.pi, -np.pi)
+        h["limit_max"] = (np.inf, np.inf, np.inf, np.pi, np.pi, np.pi)
+        h["motor_spring"]["frequency_or_stiffness"] = (10.0, 10.0, 10.0, 2.0, 2.0, 2.0)
+        h["motor_spring"]["damping"] = 1.0
+        h["motor_min_force"] = -np.inf
+        h["motor_max_force"] = np.inf
+        h["target_orientation"] = (0.0, 0.0, 0.0, 1.0)
     elif joint_type == JOINT_SLIDER:
         h["limits_min"] = -np.inf
         h["limits_max"] = np.inf

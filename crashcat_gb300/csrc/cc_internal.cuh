@@ -233,7 +233,7 @@ constexpr int MESH_KEY_BITS = 21;  // body indices and triangle indices in a mes
 // user joints of every type share one id space, packed as the reference's ConstraintId
 // (constraint-id.ts:1-35): the ConstraintType above bit 24, the per-type index below
 enum : int { JT_POINT = 0, JT_DISTANCE = 1, JT_HINGE = 2, JT_SLIDER = 3, JT_FIXED = 4, JT_CONE = 5, JT_SWING = 6,
-             JT_TYPES = 7 };
+             JT_SIX_DOF = 7, JT_TYPES = 8 };
 constexpr int JOINT_TYPE_SHIFT = 24, JOINT_INDEX_MASK = (1 << JOINT_TYPE_SHIFT) - 1;
 
 // fields every joint type starts with
@@ -354,6 +354,38 @@ struct DevSwing {
     DevAngle sy, sz, tw, motor[3];  // limits (swing Y, swing Z, twist), motors (twist, swing Y, swing Z)
 };
 
+// SixDOFConstraint (six-dof-constraint.ts:66-117): per-axis limits, friction and motors over
+// translation X Y Z and rotation X Y Z of the constraint frame; the rotation limits through the
+// swing-twist part (the same fields as DevSwing's, read by the same templates)
+enum : int { SD_TRANS_MOTOR = 1, SD_ROT_MOTOR = 2, SD_SPRING_LIMITS = 4 };
+struct DevSixDof {
+    DevJointHead h;
+    int swing_type, rotation_flags;
+    int free_axis, fixed_axis, flags, rot_pos_motor;  // axis bits; SD_*; rotation position motors (bits 0-2)
+    float3 lp1, lp2;
+    float4 c2b1, c2b2;  // constraint space to body space
+    float limit_min[6], limit_max[6], max_friction[6];
+    int limits_spring_mode[3];
+    float limits_freq[3], limits_damping[3];
+    int motor_state[6], motor_spring_mode[6];
+    float motor_freq[6], motor_damping[6], motor_min_force[6], motor_max_force[6];
+    float3 target_v, target_w, target_p;
+    float4 target_q;
+    // swing-twist part limits (sines and cosines of half angles)
+    float sin_twist_min, sin_twist_max, cos_twist_min, cos_twist_max;
+    float y_half_min, y_half_max, sin_y_min, sin_y_max, cos_y_min, cos_y_max;
+    float z_half_min, z_half_max, sin_z_min, sin_z_max, cos_z_min, cos_z_max;
+    // per-step state
+    float3 t_axis[3], r_axis[3];
+    float disp[3];
+    float3 ws_y, ws_z, ws_twist;
+    DevAngle sy, sz, tw;
+    DevAxis trans[3], motor_t[3];
+    DevAngle motor_r[3];
+    DevPoint pt;
+    DevEuler rot;
+};
+
 // impulse adjoints handed from one step's reverse to the previous step's, keyed by body pair
 struct AdjHandoff {
     unsigned long long *keys;  // cache_cap entries, EMPTY_KEY when free
@@ -461,6 +493,8 @@ struct DevWorld {
     // point, distance, fixed, cone and slider joints, sorted by (type, per-type index)
     DevJoint *others;
     int num_others, max_others;
+    DevSixDof *sixdofs;
+    int num_sixdofs, max_sixdofs;
     int type_count[JT_TYPES];  // joints of each type (hinges and swing-twists included)
     int type_first[JT_TYPES];  // first record of each type in others
     int skip_joint_pairs;              // broadphase skips body pairs that share an enabled joint
@@ -549,7 +583,9 @@ __device__ inline float shape_inner_radius(const DevWorld &w, int i, uint32_t f,
 }
 
 // ---- user joints of every type under one id ---------------------------------------------
-__device__ __forceinline__ int joint_total(const DevWorld &w) { return w.num_hinges + w.num_swings + w.num_others; }
+__device__ __forceinline__ int joint_total(const DevWorld &w) {
+    return w.num_hinges + w.num_swings + w.num_others + w.num_sixdofs;
+}
 __device__ __forceinline__ int joint_type_of(int id) { return id >> JOINT_TYPE_SHIFT; }
 __device__ __forceinline__ int joint_index_of(int id) { return id & JOINT_INDEX_MASK; }
 // the k-th joint in type order, each type in creation order (the order in which the reference
@@ -569,6 +605,7 @@ __device__ __forceinline__ DevJointHead &joint_head(const DevWorld &w, int id) {
     const int t = joint_type_of(id), i = joint_index_of(id);
     if (t == JT_HINGE) return w.hinges[i].h;
     if (t == JT_SWING) return w.swings[i].h;
+    if (t == JT_SIX_DOF) return w.sixdofs[i].h;
     return w.others[w.type_first[t] + i].h;
 }
 __device__ __forceinline__ bool joint_active(const DevWorld &w, const DevJointHead &h) {

@@ -479,7 +479,8 @@ __device__ bool hinge_solve_position(DevWorld &w, DevHinge &j, float dt) {
 
 // ---- swing-twist limits (swing-twist-constraint-part.ts) -------------------------------
 // calculateConstraintProperties :481-652 (limit axes and their angle parts)
-__device__ void st_calc(DevSwing &p, const JBody &A, const JBody &B, float4 q, float4 c2w) {
+template <class P>
+__device__ void st_calc(P &p, const JBody &A, const JBody &B, float4 q, float4 c2w) {
     float4 sw, tw;
     get_swing_twist(q, sw, tw);
     float4 csw = sw, ctw = tw;
@@ -545,7 +546,8 @@ __device__ void st_calc(DevSwing &p, const JBody &A, const JBody &B, float4 q, f
 }
 // solvePositionConstraint :743-776 through a RotationEulerConstraintPart
 // (rotation-euler-constraint-part.ts calculateConstraintProperties, solvePositionConstraint)
-__device__ bool st_solve_position(DevWorld &w, DevSwing &p, const JBody &A, const JBody &B, float4 q, float beta) {
+template <class P>
+__device__ bool st_solve_position(DevWorld &w, P &p, const JBody &A, const JBody &B, float4 q, float beta) {
     float4 sw, tw;
     get_swing_twist(q, sw, tw);
     if (clamp_swing_twist(p, sw, tw) == 0) return false;
@@ -565,6 +567,27 @@ __device__ bool st_solve_position(DevWorld &w, DevSwing &p, const JBody &A, cons
     if (A.motion == DYNAMIC) add_rotation(w, A.i, -jm_mv(I1, l));
     if (B.motion == DYNAMIC) add_rotation(w, B.i, jm_mv(I2, l));
     return true;
+}
+// warm start and velocity solve of the three limit parts (swing-twist-constraint-part.ts
+// warmStart, solveVelocityConstraint): swing Y, swing Z, twist
+template <class P>
+__device__ void st_warm(DevWorld &w, P &p, const JBody &A, const JBody &B, float ratio) {
+    angle_warm(w, p.sy, A, B, ratio);
+    angle_warm(w, p.sz, A, B, ratio);
+    angle_warm(w, p.tw, A, B, ratio);
+}
+template <class P>
+__device__ bool st_solve_velocity(DevWorld &w, P &p, const JBody &A, const JBody &B) {
+    const float INF = __int_as_float(0x7f800000);
+    bool imp = false;
+    if (p.sy.eff != 0.f)
+        imp = angle_solve_velocity(w, p.sy, A, B, p.ws_y, -INF, p.sin_y_min == p.sin_y_max ? INF : 0.f) || imp;
+    if (p.sz.eff != 0.f)
+        imp = angle_solve_velocity(w, p.sz, A, B, p.ws_z, -INF, p.sin_z_min == p.sin_z_max ? INF : 0.f) || imp;
+    if (p.tw.eff != 0.f)
+        imp = angle_solve_velocity(w, p.tw, A, B, p.ws_twist, -INF, p.sin_twist_min == p.sin_twist_max ? INF : 0.f) ||
+              imp;
+    return imp;
 }
 
 // ---- swing-twist (swing-twist-constraint.ts) ------------------------------------------
@@ -1226,10 +1249,265 @@ __device__ bool other_solve_position(DevWorld &w, DevJoint &j, float dt) {
     return false;
 }
 
+// ---- six-DOF joint (six-dof-constraint.ts) -------------------------------------------
+__device__ __forceinline__ bool sd_fixed(const DevSixDof &j, int a) { return (j.fixed_axis >> a) & 1; }
+__device__ __forceinline__ bool sd_free(const DevSixDof &j, int a) { return (j.free_axis >> a) & 1; }
+__device__ __forceinline__ bool sd_trans_constrained(const DevSixDof &j) { return (j.free_axis & 7) != 7; }
+__device__ __forceinline__ bool sd_trans_fully(const DevSixDof &j) {
+    return (j.fixed_axis & 7) == 7 && !(j.flags & SD_SPRING_LIMITS);
+}
+__device__ __forceinline__ bool sd_rot_constrained(const DevSixDof &j) { return (j.free_axis & 56) != 56; }
+__device__ __forceinline__ bool sd_rot_fully(const DevSixDof &j) { return (j.fixed_axis & 56) == 56; }
+__device__ __forceinline__ bool sd_friction(const DevSixDof &j, int a) {
+    return !sd_fixed(j, a) && j.max_friction[a] > 0.f;
+}
+// getTwistAroundAxis :37-49
+__device__ float4 twist_around(float4 q, float3 axis) {
+    const float d = q.x * axis.x + q.y * axis.y + q.z * axis.z;
+    const float l = d * d + q.w * q.w;
+    if (!(l > 1e-10f)) return make_float4(0.f, 0.f, 0.f, 1.f);
+    const float il = 1.f / sqrtf(l);
+    return make_float4(d * axis.x * il, d * axis.y * il, d * axis.z * il, q.w * il);
+}
+// getPositionConstraintProperties :535-566
+__device__ void sd_position_props(const DevWorld &w, const DevSixDof &j, float3 &r1u, float3 &r2, float3 &u) {
+    const float3 ca = xyz(w.com[j.h.a]), cb = xyz(w.com[j.h.b]);
+    const float3 p1 = qrot(w.quat[j.h.a], j.lp1) + ca, p2 = qrot(w.quat[j.h.b], j.lp2) + cb;
+    r1u = p2 - ca;
+    r2 = p2 - cb;
+    u = p2 - p1;
+}
+__device__ __forceinline__ float f3_at(float3 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
+// setupVelocity :568-881
+__device__ void sixdof_setup(DevWorld &w, DevSixDof &j, float dt) {
+    JBody A = jbody(w, j.h.a), B = jbody(w, j.h.b);
+    const float4 qa = w.quat[j.h.a], qb = w.quat[j.h.b];
+    const float4 c1w = qmul(qa, j.c2b1);
+    const float3 E[3] = {f3(1.f, 0.f, 0.f), f3(0.f, 1.f, 0.f), f3(0.f, 0.f, 1.f)};
+    for (int i = 0; i < 3; i++) j.t_axis[i] = qrot(c1w, E[i]);
+    if (sd_trans_fully(j)) {
+        point_calc(j.pt, A, B, qa, qb, j.lp1, j.lp2);
+    } else if (sd_trans_constrained(j) || (j.flags & SD_TRANS_MOTOR)) {
+        float3 r1u, r2, u;
+        sd_position_props(w, j, r1u, r2, u);
+        for (int i = 0; i < 3; i++) {
+            const float3 ta = j.t_axis[i];
+            const float d = dot3(ta, u);
+            j.disp[i] = d;
+            bool on = false;
+            float C = 0.f;
+            if (sd_fixed(j, i)) {
+                C = d - j.limit_min[i];
+                on = true;
+            } else if (!sd_free(j, i)) {
+                if (d <= j.limit_min[i]) {
+                    C = d - j.limit_min[i];
+                    on = true;
+                } else if (d >= j.limit_max[i]) {
+                    C = d - j.limit_max[i];
+                    on = true;
+                }
+            }
+            if (on) {
+                if (j.limits_freq[i] > 0.f)
+                    axis_calc_settings(j.trans[i], dt, A, B, r1u, r2, ta, 0.f, C, j.limits_spring_mode[i],
+                                       j.limits_freq[i], j.limits_damping[i]);
+                else
+                    axis_calc(j.trans[i], A, B, r1u, r2, ta, 0.f);
+            } else {
+                axis_deactivate(j.trans[i]);
+            }
+            if (j.motor_state[i] == 0) {
+                if (sd_friction(j, i))
+                    axis_calc(j.motor_t[i], A, B, r1u, r2, ta, 0.f);
+                else
+                    axis_deactivate(j.motor_t[i]);
+            } else if (j.motor_state[i] == 1) {
+                axis_calc(j.motor_t[i], A, B, r1u, r2, ta, -f3_at(j.target_v, i));
+            } else if (j.motor_freq[i] > 0.f) {
+                axis_calc_settings(j.motor_t[i], dt, A, B, r1u, r2, ta, 0.f, dot3(ta, u) - f3_at(j.target_p, i),
+                                   j.motor_spring_mode[i], j.motor_freq[i], j.motor_damping[i]);
+            } else {
+                axis_deactivate(j.motor_t[i]);
+            }
+        }
+    }
+    const float4 c2w = qmul(qb, j.c2b2);
+    const float4 q = qmul(qconj4(c1w), c2w);
+    if (sd_rot_fully(j)) {
+        euler_calc(j.rot, A, B);
+    } else if (sd_rot_constrained(j) || (j.flags & SD_ROT_MOTOR)) {
+        if (sd_rot_constrained(j)) {
+            st_calc(j, A, B, q, c1w);
+        } else {
+            angle_deactivate(j.sy);
+            angle_deactivate(j.sz);
+            angle_deactivate(j.tw);
+        }
+        if (j.flags & SD_ROT_MOTOR) {
+            for (int i = 0; i < 3; i++) j.r_axis[i] = qrot(c2w, E[i]);
+            float4 t = j.target_q;
+            if (q.x * t.x + q.y * t.y + q.z * t.z + q.w * t.w < 0.f) t = qscale4(t, -1.f);
+            const float4 diff = qmul(qconj4(q), t);
+            float4 pd;
+            switch (j.rot_pos_motor) {
+                case 1: pd = twist_around(diff, E[0]); break;
+                case 2: pd = twist_around(diff, E[1]); break;
+                case 4: pd = twist_around(diff, E[2]); break;
+                case 3: pd = qmul(diff, qconj4(twist_around(diff, E[2]))); break;
+                case 5: pd = qmul(diff, qconj4(twist_around(diff, E[1]))); break;
+                case 6: pd = qmul(diff, qconj4(twist_around(diff, E[0]))); break;
+                default: pd = diff; break;
+            }
+            const float err[3] = {-2.f * pd.x, -2.f * pd.y, -2.f * pd.z};
+            for (int i = 0; i < 3; i++) {
+                const int a = 3 + i;
+                if (j.motor_state[a] == 0) {
+                    if (sd_friction(j, a))
+                        angle_calc(j.motor_r[i], A, B, j.r_axis[i], 0.f);
+                    else
+                        angle_deactivate(j.motor_r[i]);
+                } else if (j.motor_state[a] == 1) {
+                    angle_calc(j.motor_r[i], A, B, j.r_axis[i], -f3_at(j.target_w, i));
+                } else if (j.motor_freq[a] > 0.f) {
+                    angle_calc_settings(j.motor_r[i], dt, A, B, j.r_axis[i], 0.f, err[i], j.motor_spring_mode[a],
+                                        j.motor_freq[a], j.motor_damping[a]);
+                } else {
+                    angle_deactivate(j.motor_r[i]);
+                }
+            }
+        }
+    }
+}
+// warmStartVelocity :883-942
+__device__ void sixdof_warm(DevWorld &w, DevSixDof &j, float ratio) {
+    JBody A = jbody(w, j.h.a, false), B = jbody(w, j.h.b, false);
+    if (j.flags & SD_TRANS_MOTOR)
+        for (int i = 0; i < 3; i++)
+            if (j.motor_t[i].eff != 0.f) axis_warm(w, j.motor_t[i], A, B, j.t_axis[i], ratio);
+    if (j.flags & SD_ROT_MOTOR)
+        for (int i = 0; i < 3; i++)
+            if (j.motor_r[i].eff != 0.f) angle_warm(w, j.motor_r[i], A, B, ratio);
+    if (sd_rot_fully(j))
+        euler_warm(w, j.rot, A, B, ratio);
+    else if (sd_rot_constrained(j))
+        st_warm(w, j, A, B, ratio);
+    if (sd_trans_fully(j)) {
+        point_warm(w, j.pt, A, B, ratio);
+    } else if (sd_trans_constrained(j)) {
+        for (int i = 0; i < 3; i++)
+            if (j.trans[i].eff != 0.f) axis_warm(w, j.trans[i], A, B, j.t_axis[i], ratio);
+    }
+}
+// solveVelocity :966-1082 (returns false, as the reference does)
+__device__ bool sixdof_solve_velocity(DevWorld &w, DevSixDof &j, float dt) {
+    JBody A = jbody(w, j.h.a, false), B = jbody(w, j.h.b, false);
+    const float INF = __int_as_float(0x7f800000);
+    if (j.flags & SD_TRANS_MOTOR)
+        for (int i = 0; i < 3; i++) {
+            if (j.motor_t[i].eff == 0.f) continue;
+            if (j.motor_state[i] == 0) {
+                const float ml = j.max_friction[i] * dt;
+                axis_solve_velocity(w, j.motor_t[i], A, B, j.t_axis[i], -ml, ml);
+            } else {
+                axis_solve_velocity(w, j.motor_t[i], A, B, j.t_axis[i], dt * j.motor_min_force[i],
+                                    dt * j.motor_max_force[i]);
+            }
+        }
+    if (j.flags & SD_ROT_MOTOR)
+        for (int i = 0; i < 3; i++) {
+            const int a = 3 + i;
+            if (j.motor_r[i].eff == 0.f) continue;
+            if (j.motor_state[a] == 0) {
+                const float ml = j.max_friction[a] * dt;
+                angle_solve_velocity(w, j.motor_r[i], A, B, j.r_axis[i], -ml, ml);
+            } else {
+                angle_solve_velocity(w, j.motor_r[i], A, B, j.r_axis[i], dt * j.motor_min_force[a],
+                                     dt * j.motor_max_force[a]);
+            }
+        }
+    if (sd_rot_fully(j))
+        euler_solve_velocity(w, j.rot, A, B);
+    else if (sd_rot_constrained(j))
+        st_solve_velocity(w, j, A, B);
+    if (sd_trans_fully(j)) {
+        point_solve_velocity(w, j.pt, A, B);
+    } else if (sd_trans_constrained(j)) {
+        for (int i = 0; i < 3; i++) {
+            if (j.trans[i].eff == 0.f) continue;
+            float mn = -INF, mx = INF;
+            if (!sd_fixed(j, i)) {
+                if (j.disp[i] <= j.limit_min[i])
+                    mn = 0.f;
+                else if (j.disp[i] >= j.limit_max[i])
+                    mx = 0.f;
+            }
+            axis_solve_velocity(w, j.trans[i], A, B, j.t_axis[i], mn, mx);
+        }
+    }
+    return false;
+}
+// quat.fromEuler for an 'xyz' euler (mathcat): q = qx qy qz
+__device__ float4 quat_from_euler_xyz(float x, float y, float z) {
+    const float c1 = cosf(0.5f * x), s1 = sinf(0.5f * x), c2 = cosf(0.5f * y), s2 = sinf(0.5f * y),
+                c3 = cosf(0.5f * z), s3 = sinf(0.5f * z);
+    return make_float4(s1 * c2 * c3 + c1 * s2 * s3, c1 * s2 * c3 - s1 * c2 * s3, c1 * c2 * s3 + s1 * s2 * c3,
+                       c1 * c2 * c3 - s1 * s2 * s3);
+}
+// solvePosition :1084-1236
+__device__ bool sixdof_solve_position(DevWorld &w, DevSixDof &j) {
+    const float beta = c_settings.baumgarte;
+    bool imp = false;
+    JBody A = jbody(w, j.h.a), B = jbody(w, j.h.b);
+    if (sd_rot_fully(j)) {
+        const float4 off = qmul(j.c2b1, quat_from_euler_xyz(j.limit_min[3], j.limit_min[4], j.limit_min[5]));
+        const float4 inv_initial = qmul(j.c2b2, qconj4(off));
+        euler_calc(j.rot, A, B);
+        imp = euler_solve_position(w, j.rot, A, B, inv_initial, beta) || imp;
+    } else if (sd_rot_constrained(j)) {
+        const float4 c1w = qmul(w.quat[j.h.a], j.c2b1), c2w = qmul(w.quat[j.h.b], j.c2b2);
+        imp = st_solve_position(w, j, A, B, qmul(qconj4(c1w), c2w), beta) || imp;
+    }
+    A = jbody(w, j.h.a);
+    B = jbody(w, j.h.b);
+    if (sd_trans_fully(j)) {
+        const float3 lp1 = j.lp1 + qrot(j.c2b1, f3(j.limit_min[0], j.limit_min[1], j.limit_min[2]));
+        point_calc(j.pt, A, B, w.quat[j.h.a], w.quat[j.h.b], lp1, j.lp2);
+        imp = point_solve_position(w, j.pt, A, B, beta) || imp;
+    } else if (sd_trans_constrained(j)) {
+        const float3 E[3] = {f3(1.f, 0.f, 0.f), f3(0.f, 1.f, 0.f), f3(0.f, 0.f, 1.f)};
+        for (int i = 0; i < 3; i++) {
+            if (j.limits_freq[i] > 0.f) continue;
+            float3 r1u, r2, u;
+            sd_position_props(w, j, r1u, r2, u);
+            const float3 ta = qrot(qmul(w.quat[j.h.a], j.c2b1), E[i]);
+            float err = 0.f;
+            if (sd_fixed(j, i)) {
+                err = dot3(u, ta) - j.limit_min[i];
+            } else if (!sd_free(j, i)) {
+                const float d = dot3(u, ta);
+                if (d <= j.limit_min[i])
+                    err = d - j.limit_min[i];
+                else if (d >= j.limit_max[i])
+                    err = d - j.limit_max[i];
+            }
+            if (err != 0.f) {
+                A = jbody(w, j.h.a);
+                B = jbody(w, j.h.b);
+                axis_calc(j.trans[i], A, B, r1u, r2, ta, 0.f);
+                imp = axis_solve_position(w, j.trans[i], A, B, ta, err, beta) || imp;
+            }
+        }
+    }
+    return imp;
+}
+
 // ---- dispatch on the joint id (the id helpers are in cc_internal.cuh) ------------------
 __device__ void joint_setup(DevWorld &w, int id, float dt) {
     const int t = joint_type_of(id), i = joint_index_of(id);
-    if (t == JT_SWING)
+    if (t == JT_SIX_DOF)
+        sixdof_setup(w, w.sixdofs[i], dt);
+    else if (t == JT_SWING)
         swing_setup(w, w.swings[i], dt);
     else if (t == JT_HINGE)
         hinge_setup(w, w.hinges[i], dt);
@@ -1238,7 +1516,9 @@ __device__ void joint_setup(DevWorld &w, int id, float dt) {
 }
 __device__ void joint_warm(DevWorld &w, int id, float ratio) {
     const int t = joint_type_of(id), i = joint_index_of(id);
-    if (t == JT_SWING)
+    if (t == JT_SIX_DOF)
+        sixdof_warm(w, w.sixdofs[i], ratio);
+    else if (t == JT_SWING)
         swing_warm(w, w.swings[i], ratio);
     else if (t == JT_HINGE)
         hinge_warm(w, w.hinges[i], ratio);
@@ -1247,12 +1527,14 @@ __device__ void joint_warm(DevWorld &w, int id, float ratio) {
 }
 __device__ bool joint_solve_velocity(DevWorld &w, int id, float dt) {
     const int t = joint_type_of(id), i = joint_index_of(id);
+    if (t == JT_SIX_DOF) return sixdof_solve_velocity(w, w.sixdofs[i], dt);
     if (t == JT_SWING) return swing_solve_velocity(w, w.swings[i], dt);
     if (t == JT_HINGE) return hinge_solve_velocity(w, w.hinges[i], dt);
     return other_solve_velocity(w, other_joint(w, id), dt);
 }
 __device__ bool joint_solve_position(DevWorld &w, int id, float dt) {
     const int t = joint_type_of(id), i = joint_index_of(id);
+    if (t == JT_SIX_DOF) return sixdof_solve_position(w, w.sixdofs[i]);
     if (t == JT_SWING) return swing_solve_position(w, w.swings[i]);
     if (t == JT_HINGE) return hinge_solve_position(w, w.hinges[i], dt);
     return other_solve_position(w, other_joint(w, id), dt);

@@ -1938,7 +1938,7 @@ void launch_contacts_and_islands(DevWorld &w, float dt, float, cudaStream_t s) {
     k_contact_setup<<<grid_for(w.max_manifolds, 128, 16), 128, 0, s>>>(w, ct, dt);
     k_removed_contacts<<<grid_for(w.cache_cap, 256), 256, 0, s>>>(w, ct);
     k_apply_wake<<<grid_for(w.n, 256), 256, 0, s>>>(w);
-    const int nj = w.num_hinges + w.num_swings + w.num_others;
+    const int nj = w.num_hinges + w.num_swings + w.num_others + w.num_sixdofs;
     if (nj > 0 && dt > 0.f) {
         k_joint_wake_scan<<<grid_for(nj, 256), 256, 0, s>>>(w);
         k_joint_wake_serial<<<1, 1, 0, s>>>(w);
@@ -1958,7 +1958,7 @@ void launch_contacts_and_islands(DevWorld &w, float dt, float, cudaStream_t s) {
 
 void launch_solver(DevWorld &w, float dt, float ratio, cudaStream_t s, cudaEvent_t mid, int phase) {
     CacheTables ct = tables_of(w);
-    const bool joints = w.num_hinges + w.num_swings + w.num_others > 0;
+    const bool joints = w.num_hinges + w.num_swings + w.num_others + w.num_sixdofs > 0;
     // the per-warp tier takes its islands from a cursor: rewind it for the second pass
     if (phase == SOLVE_POSITION) cudaMemsetAsync(&w.ctr->mid_cursor, 0, sizeof(int), s);
     k_solve_small<false><<<grid_for(w.n, 128, 16), 128, 0, s>>>(w, ct, w.small_list, dt, ratio, phase);

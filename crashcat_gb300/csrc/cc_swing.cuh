@@ -47,7 +47,9 @@ __host__ __device__ inline void ellipse_closest(double px, double py, double a, 
     oy = bSq * py / (t + bSq);
 }
 // clampSwingTwist :278-402
-__host__ __device__ inline int clamp_swing_twist(const DevSwing &p, float4 &swing, float4 &twist) {
+// (P: a record holding the swing-twist limits, the swing-twist joint's or the six-DOF joint's)
+template <class P>
+__host__ __device__ inline int clamp_swing_twist(const P &p, float4 &swing, float4 &twist) {
     int cl = 0;
     bool neg_s = swing.w < 0.f, neg_t = twist.w < 0.f;
     if (neg_s) swing = qscale4(swing, -1.f);

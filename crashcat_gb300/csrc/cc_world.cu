@@ -39,6 +39,7 @@ struct cc_world {
     std::vector<DevHinge> hinges;  // host copy of each joint as created (bodies, flags, limits, motors)
     std::vector<DevSwing> swings;
     std::vector<DevJoint> others;  // point, distance, fixed, cone, slider joints by (type, index)
+    std::vector<DevSixDof> sixdofs;
     std::vector<cc_hull::Hull> hulls;  // convex hull shapes as built
     std::vector<cc_mesh::Mesh> meshes;  // triangle meshes as built
     bool hulls_dirty = false, meshes_dirty = false;  // added since the last upload
@@ -538,7 +539,7 @@ int cc_world_destroy(cc_world *W) {
                     w.cache_recs[1], w.cache_parity, w.root_flag, w.small_list, w.large_list, w.scratch_order,
                     w.scratch_colour, w.scratch_claim, w.mid_list, w.body_local, w.contact_event,
                     w.removed_keys, W->d_state_rows, w.hinges, w.island_joints, w.island_joint_count,
-                    w.island_joint_off, w.island_fill_j, w.joint_wake, w.joint_partners, w.swings, w.others, w.frames,
+                    w.island_joint_off, w.island_fill_j, w.joint_wake, w.joint_partners, w.swings, w.others, w.sixdofs, w.frames,
                     w.giant_list, w.giant_claim, w.giant_count, w.small_joint_list, w.large_joint_list,
                     w.hulls, w.hull_points, w.hull_shrunk,
                     w.hull_planes, w.hull_faces, w.hull_vidx, w.ccd_flag, w.ccd_slot, w.ccd_index, w.ccd,
@@ -1670,7 +1671,7 @@ extern "C" int cc_world_rollout_grad(cc_world *W, float dt, int32_t n_steps, int
     DevWorld &w = W->w;
     if (w.n == 0) return CC_ERR_INVALID;
     // the adjoint covers contacts and the discrete integration only
-    if (w.num_hinges + w.num_swings + w.num_others > 0 || w.num_linear_cast > 0 || W->any_iter_override)
+    if (w.num_hinges + w.num_swings + w.num_others + w.num_sixdofs > 0 || w.num_linear_cast > 0 || W->any_iter_override)
         return CC_ERR_UNSUPPORTED;
     int K = checkpoint_every < n_steps ? checkpoint_every : n_steps;
     int nseg = (n_steps + K - 1) / K;
@@ -1801,7 +1802,7 @@ static int tune_snapshot(cc_world *W, bool save) {
     }
     // joint records carry their accumulated impulses from step to step
     size_t jb = sizeof(DevHinge) * (size_t)w.num_hinges + sizeof(DevSwing) * (size_t)w.num_swings +
-                sizeof(DevJoint) * (size_t)w.num_others;
+                sizeof(DevJoint) * (size_t)w.num_others + sizeof(DevSixDof) * (size_t)w.num_sixdofs;
     if (save && jb > T.joint_bytes) {
         if (T.joints) cudaFree(T.joints);
         T.joints = nullptr;
@@ -1824,6 +1825,11 @@ static int tune_snapshot(cc_world *W, bool save) {
     if (ob)
         CC_TRY(cudaMemcpyAsync(save ? (void *)(T.joints + hb + sb) : (void *)w.others,
                                save ? (void *)w.others : (void *)(T.joints + hb + sb), ob, cudaMemcpyDeviceToDevice, s));
+    size_t xb = sizeof(DevSixDof) * (size_t)w.num_sixdofs;
+    if (xb)
+        CC_TRY(cudaMemcpyAsync(save ? (void *)(T.joints + hb + sb + ob) : (void *)w.sixdofs,
+                               save ? (void *)w.sixdofs : (void *)(T.joints + hb + sb + ob), xb,
+                               cudaMemcpyDeviceToDevice, s));
     if (w.ccd_lambda && T.ccd)
         CC_TRY(cudaMemcpyAsync(save ? (void *)T.ccd : (void *)w.ccd_lambda, save ? (void *)w.ccd_lambda : (void *)T.ccd,
                                sizeof(float2) * (size_t)w.num_worlds, cudaMemcpyDeviceToDevice, s));
@@ -2002,7 +2008,8 @@ static int grow_joints(cc_world *W, T *&arr, int count, int &cap_io, int need) {
     cap_io = cap;
     return CC_OK;
 }
-static int ensure_joint_capacity(cc_world *W, int need_hinges, int need_swings, int need_others = -1) {
+static int ensure_joint_capacity(cc_world *W, int need_hinges, int need_swings, int need_others = -1,
+                                 int need_sixdofs = -1) {
     DevWorld &w = W->w;
     int r;
     if (!w.island_joint_count) {
@@ -2016,7 +2023,10 @@ static int ensure_joint_capacity(cc_world *W, int need_hinges, int need_swings, 
     if ((r = grow_joints(W, w.hinges, w.num_hinges, w.max_hinges, need_hinges)) != CC_OK) return r;
     if ((r = grow_joints(W, w.swings, w.num_swings, w.max_swings, need_swings)) != CC_OK) return r;
     if (need_others >= 0 && (r = grow_joints(W, w.others, w.num_others, w.max_others, need_others)) != CC_OK) return r;
-    int need_lists = w.max_hinges + w.max_swings + w.max_others;
+    if (need_sixdofs >= 0 &&
+        (r = grow_joints(W, w.sixdofs, w.num_sixdofs, w.max_sixdofs, need_sixdofs)) != CC_OK)
+        return r;
+    int need_lists = w.max_hinges + w.max_swings + w.max_others + w.max_sixdofs;
     if (need_lists > w.max_joints) {
         int *nl = nullptr;
         if ((r = dalloc(&nl, 5 * (size_t)need_lists)) != CC_OK) return r;
@@ -2054,6 +2064,7 @@ static int upload_partners(cc_world *W) {
     for (const DevHinge &j : W->hinges) add_joint(j.h);
     for (const DevSwing &j : W->swings) add_joint(j.h);
     for (const DevJoint &j : W->others) add_joint(j.h);
+    for (const DevSixDof &j : W->sixdofs) add_joint(j.h);
     CC_TRY(cudaStreamSynchronize(W->stream));
     CC_TRY(cudaMemcpy(w.joint_partners, part.data(), sizeof(int) * part.size(), cudaMemcpyHostToDevice));
     return over && w.skip_joint_pairs ? CC_ERR_CAPACITY : CC_OK;
@@ -2183,10 +2194,11 @@ static int edit_swing(cc_world *W, int32_t index, F f) {
 
 // SwingTwistConstraintPart.setLimits (swing-twist-constraint-part.ts:140-236) in FP64: a limit
 // inside +-0.5 degrees locks its axis, one beyond +-179.5 degrees frees it
-static void swing_set_limits(DevSwing &p) {
+template <class P>
+static void st_set_limits(P &p, double twist_min, double twist_max, double ymin, double ymax, double zmin,
+                          double zmax) {
     const double PI = 3.14159265358979323846;
     const double locked = 0.5 * PI / 180.0, free_a = 179.5 * PI / 180.0;
-    double ymin = -p.plane_half_cone, ymax = p.plane_half_cone, zmin = -p.normal_half_cone, zmax = p.normal_half_cone;
     p.y_half_min = (float)(0.5 * ymin);
     p.y_half_max = (float)(0.5 * ymax);
     p.z_half_min = (float)(0.5 * zmin);
@@ -2210,10 +2222,15 @@ static void swing_set_limits(DevSwing &p) {
             cmax = (float)std::cos(0.5 * mx);
         }
     };
-    axis(p.twist_min, p.twist_max, ST_TWIST_LOCKED, ST_TWIST_FREE, p.sin_twist_min, p.sin_twist_max, p.cos_twist_min,
+    axis(twist_min, twist_max, ST_TWIST_LOCKED, ST_TWIST_FREE, p.sin_twist_min, p.sin_twist_max, p.cos_twist_min,
          p.cos_twist_max);
     axis(ymin, ymax, ST_SWING_Y_LOCKED, ST_SWING_Y_FREE, p.sin_y_min, p.sin_y_max, p.cos_y_min, p.cos_y_max);
     axis(zmin, zmax, ST_SWING_Z_LOCKED, ST_SWING_Z_FREE, p.sin_z_min, p.sin_z_max, p.cos_z_min, p.cos_z_max);
+}
+// the swing-twist constraint's limits: twist [min, max], swing Y +-plane, swing Z +-normal half cone
+static void swing_set_limits(DevSwing &p) {
+    st_set_limits(p, p.twist_min, p.twist_max, -(double)p.plane_half_cone, (double)p.plane_half_cone,
+                  -(double)p.normal_half_cone, (double)p.normal_half_cone);
 }
 // setTargetOrientationCS (swing-twist-constraint.ts:405-416): the target clamped into the limits
 static void swing_set_target(DevSwing &p, const float *q) {
@@ -2825,7 +2842,7 @@ static int add_other_joints(cc_world *W, int type, const std::vector<DevJoint> &
         if (out_index) out_index[i] = made[i].h.index;
     w.num_others += n;
     for (int t = 0; t < JT_TYPES; t++) {
-        if (t == JT_HINGE || t == JT_SWING) continue;
+        if (t == JT_HINGE || t == JT_SWING || t == JT_SIX_DOF) continue;
         w.type_count[t] = 0;
         w.type_first[t] = 0;
     }
@@ -2838,9 +2855,14 @@ static int add_other_joints(cc_world *W, int type, const std::vector<DevJoint> &
     return upload_partners(W);
 }
 template <typename F>
+static int edit_sixdof(cc_world *W, int32_t index, F f) {
+    return edit_joint(W, W->w.sixdofs, W->sixdofs, W->w.num_sixdofs, index, f);
+}
+template <typename F>
 static int edit_other(cc_world *W, int type, int32_t index, F f) {
     DevWorld &w = W->w;
-    if (type < 0 || type >= JT_TYPES || type == JT_HINGE || type == JT_SWING) return CC_ERR_INVALID;
+    if (type < 0 || type >= JT_TYPES || type == JT_HINGE || type == JT_SWING || type == JT_SIX_DOF)
+        return CC_ERR_INVALID;
     if (index < 0 || index >= w.type_count[type]) return CC_ERR_INVALID;
     return edit_joint(W, w.others, W->others, w.num_others, w.type_first[type] + index, f);
 }
@@ -3112,10 +3134,226 @@ int cc_world_set_joint_enabled(cc_world *W, int32_t type, int32_t index, int32_t
     if (!W) return CC_ERR_INVALID;
     if (type == JT_HINGE) return cc_world_set_hinge_enabled(W, index, enabled);
     if (type == JT_SWING) return cc_world_set_swing_twist_enabled(W, index, enabled);
+    if (type == JT_SIX_DOF) {
+        int r = edit_sixdof(
+            W, index, [&](DevSixDof &j) { j.h.flags = enabled ? (j.h.flags | JF_ENABLED) : (j.h.flags & ~JF_ENABLED); });
+        if (r != CC_OK) return r;
+        return upload_partners(W);
+    }
     int r = edit_other(W, type, index,
                        [&](DevJoint &j) { j.h.flags = enabled ? (j.h.flags | JF_ENABLED) : (j.h.flags & ~JF_ENABLED); });
     if (r != CC_OK) return r;
     return upload_partners(W);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// six-DOF joints (six-dof-constraint.ts)
+// ---------------------------------------------------------------------------
+namespace {
+// updateTranslationLimits + updateRotationLimits + updateFixedFreeAxis (:240-285) in FP64 over
+// the requested limits; the swing-twist part takes the rotation limits (setLimits)
+void sixdof_set_limits(DevSixDof &j, const double in_min[6], const double in_max[6]) {
+    const double PI = 3.14159265358979323846;
+    double mn[6], mx[6];
+    for (int i = 0; i < 6; i++) {
+        mn[i] = in_min[i];
+        mx[i] = in_max[i];
+    }
+    for (int i = 0; i < 3; i++)
+        if (mn[i] > mx[i]) mn[i] = mx[i] = 0.0;
+    if (j.swing_type == CC_SWING_CONE) {
+        mx[4] = std::max(0.0, mx[4]);
+        mx[5] = std::max(0.0, mx[5]);
+        mn[4] = -mx[4];
+        mn[5] = -mx[5];
+    }
+    for (int i = 3; i < 6; i++) {
+        mn[i] = std::max(-PI, std::min(PI, mn[i]));
+        mx[i] = std::max(-PI, std::min(PI, mx[i]));
+        if (mn[i] > mx[i]) mn[i] = mx[i] = 0.0;
+    }
+    st_set_limits(j, mn[3], mx[3], mn[4], mx[4], mn[5], mx[5]);
+    j.free_axis = j.fixed_axis = 0;
+    for (int a = 0; a < 6; a++) {
+        const double lim = a >= 3 ? PI : INFINITY;
+        if (mn[a] >= mx[a])
+            j.fixed_axis |= 1 << a;
+        else if (mn[a] <= -lim && mx[a] >= lim)
+            j.free_axis |= 1 << a;
+        j.limit_min[a] = (float)mn[a];
+        j.limit_max[a] = (float)mx[a];
+    }
+}
+// cacheTranslationMotorActive / cacheRotationMotorActive / cacheRotationPositionMotorActive /
+// cacheHasSpringLimits (:287-323)
+void sixdof_cache_motors(DevSixDof &j) {
+    auto friction = [&](int a) { return !((j.fixed_axis >> a) & 1) && j.max_friction[a] > 0.f; };
+    j.flags &= SD_SPRING_LIMITS;
+    j.rot_pos_motor = 0;
+    for (int i = 0; i < 3; i++) {
+        if (j.motor_state[i] != 0 || friction(i)) j.flags |= SD_TRANS_MOTOR;
+        if (j.motor_state[3 + i] != 0 || friction(3 + i)) j.flags |= SD_ROT_MOTOR;
+        if (j.motor_state[3 + i] == 2) j.rot_pos_motor |= 1 << i;
+    }
+}
+// setTargetOrientationCS (:1293-1299): the target clamped into the rotation limits
+void sixdof_set_target(DevSixDof &j, const float *q) {
+    float4 o = make_float4(q[0], q[1], q[2], q[3]), sw, tw;
+    get_swing_twist(o, sw, tw);
+    clamp_swing_twist(j, sw, tw);
+    j.target_q = qmul(sw, tw);
+}
+bool limits_ok(const float *mn, const float *mx) {
+    for (int k = 0; k < 6; k++)
+        if (std::isnan(mn[k]) || std::isnan(mx[k])) return false;
+    return true;
+}
+}  // namespace
+
+extern "C" {
+
+int cc_world_add_six_dof_joints(cc_world *W, const cc_six_dof_desc *d, int32_t n, int32_t *out_index) {
+    if (!W || (!d && n > 0) || n < 0) return CC_ERR_INVALID;
+    if (n == 0) return CC_OK;
+    DevWorld &w = W->w;
+    for (int i = 0; i < n; i++) {
+        const cc_six_dof_desc &h = d[i];
+        if (h.body_a < 0 || h.body_b < 0 || h.body_a >= w.n || h.body_b >= w.n) return CC_ERR_INVALID;
+        if (h.space != CC_SPACE_WORLD && h.space != CC_SPACE_LOCAL) return CC_ERR_INVALID;
+        if (h.swing_type != CC_SWING_CONE && h.swing_type != CC_SWING_PYRAMID) return CC_ERR_INVALID;
+        if (h.num_velocity_steps_override < 0 || h.num_velocity_steps_override > 255 ||
+            h.num_position_steps_override < 0 || h.num_position_steps_override > 255)
+            return CC_ERR_INVALID;
+        if (!finite3(h.position_a) || !finite3(h.position_b) || !finite3(h.axis_x_a) || !finite3(h.axis_y_a) ||
+            !finite3(h.axis_x_b) || !finite3(h.axis_y_b) || !finite3(h.target_velocity) ||
+            !finite3(h.target_angular_velocity) || !finite3(h.target_position) || !limits_ok(h.limit_min, h.limit_max))
+            return CC_ERR_INVALID;
+        for (int k = 0; k < 4; k++)
+            if (!std::isfinite(h.target_orientation[k])) return CC_ERR_INVALID;
+        for (int k = 0; k < 3; k++)
+            if (!spring_ok(h.limits_spring[k])) return CC_ERR_INVALID;
+        for (int k = 0; k < 6; k++)
+            if (!spring_ok(h.motor_spring[k]) || h.motor_state[k] < 0 || h.motor_state[k] > 2 ||
+                std::isnan(h.max_friction[k]) || std::isnan(h.motor_min_force[k]) || std::isnan(h.motor_max_force[k]))
+                return CC_ERR_INVALID;
+    }
+    BodyPoses p;
+    if (int r = read_poses(W, p)) return r;
+    std::vector<DevSixDof> made((size_t)n);
+    for (int i = 0; i < n; i++) {
+        const cc_six_dof_desc &h = d[i];
+        if (p.world[h.body_a] != p.world[h.body_b]) return CC_ERR_INVALID;
+        DevSixDof &j = made[i];
+        memset(&j, 0, sizeof(j));
+        j.h.a = h.body_a;
+        j.h.b = h.body_b;
+        j.h.index = w.num_sixdofs + i;
+        j.h.iter_ovr = (int)((uint32_t)h.num_velocity_steps_override | ((uint32_t)h.num_position_steps_override << 8));
+        if (j.h.iter_ovr) W->any_iter_override = true;
+        j.h.priority = h.priority;
+        j.h.island = -1;
+        j.h.flags = h.enabled ? JF_ENABLED : 0;
+        // constraint space from the columns (X, Y, X x Y) of each body (create :376-412)
+        D3 x1 = dnormalize(d3(h.axis_x_a)), y1 = dnormalize(d3(h.axis_y_a));
+        D3 x2 = dnormalize(d3(h.axis_x_b)), y2 = dnormalize(d3(h.axis_y_b));
+        DQ c1 = quat_from_columns(x1, y1, dcross(x1, y1)), c2 = quat_from_columns(x2, y2, dcross(x2, y2));
+        if (h.space == CC_SPACE_WORLD) {
+            DQ iqa = dconj(dq(p.quat[h.body_a])), iqb = dconj(dq(p.quat[h.body_b]));
+            j.lp1 = f3d(drot(iqa, dsub(d3(h.position_a), d3(p.com[h.body_a]))));
+            j.lp2 = f3d(drot(iqb, dsub(d3(h.position_b), d3(p.com[h.body_b]))));
+            c1 = dqmul(iqa, c1);
+            c2 = dqmul(iqb, c2);
+        } else {
+            j.lp1 = f3d(d3(h.position_a));
+            j.lp2 = f3d(d3(h.position_b));
+        }
+        j.c2b1 = f4q(c1);
+        j.c2b2 = f4q(c2);
+        j.swing_type = h.swing_type;
+        double mn[6], mx[6];
+        for (int k = 0; k < 6; k++) {
+            mn[k] = h.limit_min[k];
+            mx[k] = h.limit_max[k];
+            j.max_friction[k] = h.max_friction[k];
+            j.motor_state[k] = h.motor_state[k];
+            j.motor_spring_mode[k] = h.motor_spring[k].mode;
+            j.motor_freq[k] = h.motor_spring[k].frequency_or_stiffness;
+            j.motor_damping[k] = h.motor_spring[k].damping;
+            j.motor_min_force[k] = h.motor_min_force[k];
+            j.motor_max_force[k] = h.motor_max_force[k];
+        }
+        for (int k = 0; k < 3; k++) {
+            j.limits_spring_mode[k] = h.limits_spring[k].mode;
+            j.limits_freq[k] = h.limits_spring[k].frequency_or_stiffness;
+            j.limits_damping[k] = h.limits_spring[k].damping;
+            if (j.limits_freq[k] > 0.f) j.flags |= SD_SPRING_LIMITS;
+        }
+        sixdof_set_limits(j, mn, mx);
+        sixdof_cache_motors(j);
+        j.target_v = make_float3(h.target_velocity[0], h.target_velocity[1], h.target_velocity[2]);
+        j.target_w = make_float3(h.target_angular_velocity[0], h.target_angular_velocity[1],
+                                 h.target_angular_velocity[2]);
+        j.target_p = make_float3(h.target_position[0], h.target_position[1], h.target_position[2]);
+        sixdof_set_target(j, h.target_orientation);
+    }
+    int r = ensure_joint_capacity(W, w.num_hinges, w.num_swings, -1, w.num_sixdofs + n);
+    if (r != CC_OK) return r;
+    CC_TRY(cudaMemcpy(w.sixdofs + w.num_sixdofs, made.data(), sizeof(DevSixDof) * n, cudaMemcpyHostToDevice));
+    for (int i = 0; i < n; i++) {
+        W->sixdofs.push_back(made[i]);
+        if (out_index) out_index[i] = w.num_sixdofs + i;
+    }
+    w.num_sixdofs += n;
+    w.type_count[JT_SIX_DOF] = w.num_sixdofs;
+    drop_graph(W);
+    return upload_partners(W);
+}
+
+int cc_world_set_six_dof_limits(cc_world *W, int32_t index, const float *limit_min, const float *limit_max) {
+    if (!W || !limit_min || !limit_max || !limits_ok(limit_min, limit_max)) return CC_ERR_INVALID;
+    return edit_sixdof(W, index, [&](DevSixDof &j) {  // setTranslationLimits + setRotationLimits :1238-1260
+        double mn[6], mx[6];
+        for (int k = 0; k < 6; k++) {
+            mn[k] = limit_min[k];
+            mx[k] = limit_max[k];
+        }
+        sixdof_set_limits(j, mn, mx);
+    });
+}
+
+int cc_world_set_six_dof_motor(cc_world *W, int32_t index, const int32_t *motor_state, const float *target_velocity,
+                               const float *target_angular_velocity, const float *target_position,
+                               const float *target_orientation, const float *max_friction) {
+    if (!W || !motor_state || !target_velocity || !target_angular_velocity || !target_position ||
+        !target_orientation || !max_friction || !finite3(target_velocity) || !finite3(target_angular_velocity) ||
+        !finite3(target_position))
+        return CC_ERR_INVALID;
+    for (int k = 0; k < 6; k++)
+        if (motor_state[k] < 0 || motor_state[k] > 2 || std::isnan(max_friction[k])) return CC_ERR_INVALID;
+    for (int k = 0; k < 4; k++)
+        if (!std::isfinite(target_orientation[k])) return CC_ERR_INVALID;
+    return edit_sixdof(W, index, [&](DevSixDof &j) {  // setMaxFriction, setMotorState, setTarget*CS :1262-1306
+        for (int k = 0; k < 6; k++) {
+            j.max_friction[k] = max_friction[k];
+            if (j.motor_state[k] != motor_state[k]) {  // a changed state deactivates that motor part
+                j.motor_state[k] = motor_state[k];
+                if (k < 3) {
+                    j.motor_t[k].eff = 0.f;
+                    j.motor_t[k].lambda = 0.f;
+                } else {
+                    j.motor_r[k - 3].eff = 0.f;
+                    j.motor_r[k - 3].lambda = 0.f;
+                }
+            }
+        }
+        sixdof_cache_motors(j);
+        j.target_v = make_float3(target_velocity[0], target_velocity[1], target_velocity[2]);
+        j.target_w = make_float3(target_angular_velocity[0], target_angular_velocity[1], target_angular_velocity[2]);
+        j.target_p = make_float3(target_position[0], target_position[1], target_position[2]);
+        sixdof_set_target(j, target_orientation);
+    });
 }
 
 int cc_world_get_joint_lambdas(cc_world *W, int32_t type, int32_t index, float *out, int32_t capacity,
@@ -3124,6 +3362,18 @@ int cc_world_get_joint_lambdas(cc_world *W, int32_t type, int32_t index, float *
     DevWorld &w = W->w;
     if (type < 0 || type >= JT_TYPES || type == JT_HINGE || type == JT_SWING) return CC_ERR_INVALID;
     if (index < 0 || index >= w.type_count[type]) return CC_ERR_INVALID;
+    if (type == JT_SIX_DOF) {  // translation rows, point, rotation, swing Y, swing Z, twist, motors
+        DevSixDof x;
+        CC_TRY(cudaStreamSynchronize(W->stream));
+        CC_TRY(cudaMemcpy(&x, w.sixdofs + index, sizeof(DevSixDof), cudaMemcpyDeviceToHost));
+        const float v[18] = {x.trans[0].lambda, x.trans[1].lambda, x.trans[2].lambda, x.pt.lambda.x, x.pt.lambda.y,
+                             x.pt.lambda.z, x.rot.lambda.x, x.rot.lambda.y, x.rot.lambda.z, x.sy.lambda, x.sz.lambda,
+                             x.tw.lambda, x.motor_t[0].lambda, x.motor_t[1].lambda, x.motor_t[2].lambda,
+                             x.motor_r[0].lambda, x.motor_r[1].lambda, x.motor_r[2].lambda};
+        for (int k = 0; k < std::min(18, capacity); k++) out[k] = v[k];
+        if (count) *count = 18;
+        return capacity < 18 ? CC_ERR_CAPACITY : CC_OK;
+    }
     DevJoint j;
     CC_TRY(cudaStreamSynchronize(W->stream));
     CC_TRY(cudaMemcpy(&j, w.others + w.type_first[type] + index, sizeof(DevJoint), cudaMemcpyDeviceToHost));

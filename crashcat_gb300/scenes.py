@@ -17,8 +17,9 @@ from typing import Optional
 from ._lib import (BODY_DTYPE, COMBINE_GEOMETRIC_MEAN, COMBINE_MAX, DYNAMIC, MOTOR_OFF, MOTOR_POSITION,
                    MOTOR_VELOCITY, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_CONVEX_HULL, SHAPE_CYLINDER, SHAPE_EMPTY,
                    SHAPE_PLANE, SHAPE_SPHERE, SHAPE_TRIANGLE_MESH, STATIC,
-                   SWING_CONE, SWING_PYRAMID, JOINT_CONE, JOINT_DISTANCE, JOINT_FIXED, JOINT_POINT, JOINT_SLIDER,
-                   SPRING_STIFFNESS_AND_DAMPING, hinge_defaults, joint_defaults, swing_twist_defaults)
+                   SWING_CONE, SWING_PYRAMID, JOINT_CONE, JOINT_DISTANCE, JOINT_FIXED, JOINT_POINT, JOINT_SIX_DOF,
+                   JOINT_SLIDER, SPRING_DTYPE, SPRING_FREQUENCY_AND_DAMPING, SPRING_STIFFNESS_AND_DAMPING,
+                   hinge_defaults, joint_defaults, swing_twist_defaults)
 
 # object layers of the reference's test helper (tst/helpers.ts:5-26)
 LAYER_MOVING = 0
@@ -1164,6 +1165,141 @@ def joint_zoo(seed: int = 91) -> Scene:
     b["allow_sleeping"][:] = 0
     joints = {t: np.array(r, dtype=joint_defaults(t, 0).dtype) for t, r in J.items()}
     return Scene("joint_zoo", b, dt=1.0 / 60.0, steps=120, seed=seed, joints=joints, skip_joint_pairs=True)
+
+
+def six_dof_zoo(seed: int = 93) -> Scene:
+    """One world of six-DOF joint configurations (src/constraints/six-dof-constraint.ts), each
+    on its own static post, 4 m apart in Z; joined bodies do not collide.  Constraint frames
+    are given in world space with the bodies unrotated, so every joint starts at its rest pose:
+
+    * locked: all six axes fixed, a 1 m cantilever box (a weld);
+    * ball: translations fixed, rotations free, a capsule pendulum pushed at 3 m/s;
+    * cone: translations fixed, twist free, swing cone of 30 degrees, the same push;
+    * pyramid: translations fixed, twist +-10 degrees, swing Y +-20 and Z +-40 degrees, two
+      pendulums pushed across each swing axis (X twist points down, Y along world X, Z along
+      world Z: a push along world X swings about Z, one along world Z about Y);
+    * prismatic: X limited to [-1, 1] m along a 30 degree incline, everything else fixed;
+    * translation motors along free X: velocity 2 m/s, position 0.5 m;
+    * rotation motors about free X (Y, Z rotation and translations fixed, pivot at the centre of
+      mass): velocity 3 rad/s, position 45 degrees of twist;
+    * friction: free X with 20 N of friction, box launched at 3 m/s;
+    * soft limit: Y limited to [-0.1, 0.1] m with a 2 Hz / 0.5 damping limit spring, hanging;
+    * a free pair of boxes welded by all six axes, thrown spinning."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    rows = []
+
+    def body(shape, params, pos, static=False, v=(0.0, 0.0, 0.0), w=(0.0, 0.0, 0.0)):
+        rows.append((shape, params, pos, static, v, w))
+        return len(rows) - 1
+
+    def post(pos):
+        return body("box", (0.1, 0.1, 0.1), pos, static=True)
+
+    recs = []
+    INF, PI = float("inf"), math.pi
+    FREE_MIN, FREE_MAX = (-INF, -INF, -INF, -PI, -PI, -PI), (INF, INF, INF, PI, PI, PI)
+
+    def joint(a, b, pos_a, pos_b=None, lmin=FREE_MIN, lmax=FREE_MAX, **f):
+        r = joint_defaults(JOINT_SIX_DOF, 1)[0]
+        r["body_a"], r["body_b"] = a, b
+        r["position_a"] = pos_a
+        r["position_b"] = pos_a if pos_b is None else pos_b
+        r["limit_min"], r["limit_max"] = lmin, lmax
+        for k, v in f.items():
+            if isinstance(v, dict):
+                for kk, vv in v.items():
+                    r[k][kk] = vv
+            else:
+                r[k] = v
+        recs.append(r)
+
+    zero6 = (0.0,) * 6
+    down = dict(axis_x_a=(0.0, -1.0, 0.0), axis_y_a=(1.0, 0.0, 0.0), axis_x_b=(0.0, -1.0, 0.0),
+                axis_y_b=(1.0, 0.0, 0.0))
+    jit = lambda: float(rng.uniform(-0.05, 0.05))
+    # locked cantilever
+    a = post((0.0, 8.0, 0.0))
+    c = body("box", (0.4, 0.1, 0.1), (0.5, 8.0, 0.0))
+    joint(a, c, (0.0, 8.0, 0.0), lmin=zero6, lmax=zero6)
+    # ball, cone, pyramid pendulums: capsule centres 0.8 m below their pivots
+    specs = [(4.0, (0.0, 0.0, 0.0, -PI, -PI, -PI), (0.0, 0.0, 0.0, PI, PI, PI), 0, (3.0, 0.0, jit())),
+             (8.0, (0.0, 0.0, 0.0, -PI, -math.radians(30), -math.radians(30)),
+              (0.0, 0.0, 0.0, PI, math.radians(30), math.radians(30)), 0, (3.0, 0.0, jit())),
+             (12.0, (0.0, 0.0, 0.0, -math.radians(10), -math.radians(20), -math.radians(40)),
+              (0.0, 0.0, 0.0, math.radians(10), math.radians(20), math.radians(40)), 1, (3.0, 0.0, 0.0)),
+             (12.0, (0.0, 0.0, 0.0, -math.radians(10), -math.radians(20), -math.radians(40)),
+              (0.0, 0.0, 0.0, math.radians(10), math.radians(20), math.radians(40)), 1, (0.0, 0.0, 3.0))]
+    for k, (z, lmin, lmax, swing, v) in enumerate(specs):
+        x = 4.0 * k
+        a = post((x, 8.0, z))
+        p = body("capsule", (0.1, 0.6), (x, 7.2, z), v=v)
+        joint(a, p, (x, 8.0, z), lmin=lmin, lmax=lmax, swing_type=swing, **down)
+    # prismatic incline: X along the incline (downhill), Y its normal
+    z = 16.0
+    ax = (math.cos(math.radians(30.0)), -math.sin(math.radians(30.0)), 0.0)
+    n_ax = (math.sin(math.radians(30.0)), math.cos(math.radians(30.0)), 0.0)
+    a = post((0.0, 8.0, z))
+    b1 = body("box", (0.2, 0.2, 0.2), (0.0, 8.0, z))
+    joint(a, b1, (0.0, 8.0, z), lmin=(-1.0,) + zero6[1:], lmax=(1.0,) + zero6[1:], axis_x_a=ax, axis_y_a=n_ax,
+          axis_x_b=ax, axis_y_b=n_ax)
+    # translation motors along free X
+    z = 20.0
+    for i, (state, tv, tp) in enumerate(((1, 2.0, 0.0), (2, 0.0, 0.5))):
+        x = 6.0 * i
+        a = post((x, 8.0, z))
+        bm = body("box", (0.2, 0.2, 0.2), (x, 8.0, z))
+        ms = [0] * 6
+        ms[0] = state
+        joint(a, bm, (x, 8.0, z), lmin=(-INF,) + zero6[1:], lmax=(INF,) + zero6[1:], motor_state=ms,
+              target_velocity=(tv, 0.0, 0.0), target_position=(tp, 0.0, 0.0))
+    # rotation motors about free X
+    for i, state in enumerate((1, 2)):
+        x = 12.0 + 6.0 * i
+        a = post((x, 8.0, z))
+        bm = body("box", (0.3, 0.2, 0.1), (x, 8.0, z))
+        ms = [0] * 6
+        ms[3] = state
+        h = math.radians(45.0) / 2
+        joint(a, bm, (x, 8.0, z), lmin=zero6[:3] + (-PI, 0.0, 0.0), lmax=zero6[:3] + (PI, 0.0, 0.0), motor_state=ms,
+              target_angular_velocity=(3.0, 0.0, 0.0), target_orientation=(math.sin(h), 0.0, 0.0, math.cos(h)))
+    # friction along free X
+    z = 24.0
+    a = post((0.0, 8.0, z))
+    bf = body("box", (0.2, 0.2, 0.2), (0.0, 8.0, z), v=(3.0, 0.0, 0.0))
+    joint(a, bf, (0.0, 8.0, z), lmin=(-INF,) + zero6[1:], lmax=(INF,) + zero6[1:],
+          max_friction=(20.0, 0.0, 0.0, 0.0, 0.0, 0.0))
+    # soft limit on Y (up)
+    a = post((6.0, 8.0, z))
+    bs = body("box", (0.2, 0.2, 0.2), (6.0, 8.0, z))
+    sp = np.zeros(3, dtype=SPRING_DTYPE)
+    sp[1] = (SPRING_FREQUENCY_AND_DAMPING, 2.0, 0.5)
+    joint(a, bs, (6.0, 8.0, z), lmin=(0.0, -0.1, 0.0, 0.0, 0.0, 0.0), lmax=(0.0, 0.1, 0.0, 0.0, 0.0, 0.0),
+          limits_spring=sp)
+    # free welded pair
+    z = 28.0
+    spin = np.array([0.5, 1.0, 2.0])
+    g1 = body("box", (0.3, 0.2, 0.1), (4.0, 8.0, z), v=(1.0, 2.0, 0.0), w=tuple(spin))
+    v2 = np.array([1.0, 2.0, 0.0]) + np.cross(spin, np.array([0.5, 0.4, 0.0]))
+    g2 = body("box", (0.2, 0.3, 0.1), (4.5, 8.4, z), v=tuple(v2), w=tuple(spin))
+    joint(g1, g2, (4.25, 8.2, z), lmin=zero6, lmax=zero6)
+
+    b = blank_bodies(len(rows))
+    for i, (shape, params, pos, static, v, w) in enumerate(rows):
+        if shape == "box":
+            set_box(b, i, params)
+        else:
+            set_capsule(b, i, params[0], params[1])
+        b["position"][i] = pos
+        b["linear_velocity"][i] = v
+        b["angular_velocity"][i] = w
+        if static:
+            b["motion_type"][i] = STATIC
+            b["object_layer"][i] = LAYER_NOT_MOVING
+    b["linear_damping"] = 0.0
+    b["angular_damping"] = 0.0
+    b["allow_sleeping"][:] = 0
+    joints = {JOINT_SIX_DOF: np.array(recs, dtype=joint_defaults(JOINT_SIX_DOF, 0).dtype)}
+    return Scene("six_dof_zoo", b, dt=1.0 / 60.0, steps=120, seed=seed, joints=joints, skip_joint_pairs=True)
 
 
 def decorated_pile(n: int = 120, seed: int = 6, extent: float = 4.0, heights=(0.5, 4.0), grid: float = 0.0) -> Scene:

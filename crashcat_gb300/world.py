@@ -539,7 +539,7 @@ class GpuWorld:
         check(self._lib.cc_world_set_skip_joint_pairs(self.handle, int(bool(on))), "cc_world_set_skip_joint_pairs")
 
     def add_joints(self, joint_type: int, joints: np.ndarray) -> np.ndarray:
-        """cc_world_add_{point,distance,fixed,cone,slider}_joints: records of
+        """cc_world_add_{point,distance,fixed,cone,slider,six_dof}_joints: records of
         _lib.JOINT_DTYPES[joint_type]; returns the joints' per-type indices."""
         fn = _lib.JOINT_ADDERS[joint_type]
         joints = np.ascontiguousarray(joints, dtype=_lib.JOINT_DTYPES[joint_type])
@@ -553,9 +553,9 @@ class GpuWorld:
 
     def joint_lambdas(self, joint_type: int, index: int) -> np.ndarray:
         """cc_world_get_joint_lambdas: the accumulated impulses of one joint after the last step."""
-        out = np.zeros(8, dtype=np.float32)
+        out = np.zeros(18, dtype=np.float32)
         n = C.c_int32(0)
-        check(self._lib.cc_world_get_joint_lambdas(self.handle, joint_type, index, ptr(out), 8, C.byref(n)),
+        check(self._lib.cc_world_get_joint_lambdas(self.handle, joint_type, index, ptr(out), 18, C.byref(n)),
               "cc_world_get_joint_lambdas")
         return out[:n.value]
 
@@ -575,6 +575,25 @@ class GpuWorld:
                          target_position: float = 0.0) -> None:
         check(self._lib.cc_world_set_slider_motor(self.handle, index, state, C.c_float(target_velocity),
                                                   C.c_float(target_position)), "cc_world_set_slider_motor")
+
+    def set_six_dof_limits(self, index: int, limit_min, limit_max) -> None:
+        """setTranslationLimits + setRotationLimits of six-DOF joint ``index`` (6 + 6 values)."""
+        mn = np.ascontiguousarray(limit_min, dtype=np.float32).reshape(6)
+        mx = np.ascontiguousarray(limit_max, dtype=np.float32).reshape(6)
+        check(self._lib.cc_world_set_six_dof_limits(self.handle, index, ptr(mn), ptr(mx)),
+              "cc_world_set_six_dof_limits")
+
+    def set_six_dof_motor(self, index: int, motor_state, target_velocity=(0.0, 0.0, 0.0),
+                          target_angular_velocity=(0.0, 0.0, 0.0), target_position=(0.0, 0.0, 0.0),
+                          target_orientation=(0.0, 0.0, 0.0, 1.0), max_friction=(0.0,) * 6) -> None:
+        """setMaxFriction + setMotorState per axis and the constraint-space targets of six-DOF
+        joint ``index``."""
+        ms = np.ascontiguousarray(motor_state, dtype=np.int32).reshape(6)
+        arrs = [np.ascontiguousarray(v, dtype=np.float32).reshape(k) for v, k in
+                ((target_velocity, 3), (target_angular_velocity, 3), (target_position, 3),
+                 (target_orientation, 4), (max_friction, 6))]
+        check(self._lib.cc_world_set_six_dof_motor(self.handle, index, ptr(ms), *[ptr(x) for x in arrs]),
+              "cc_world_set_six_dof_motor")
 
     def slider_positions(self, n: int) -> np.ndarray:
         out = np.zeros(max(n, 1), dtype=np.float32)

@@ -539,11 +539,53 @@ int cc_world_set_slider_motor(cc_world *world, int32_t index, int32_t motor_stat
 /* getCurrentPosition (slider-constraint.ts:460-476) of every slider, n floats. */
 int cc_world_get_slider_positions(cc_world *world, float *out, int32_t capacity);
 
+/* SixDOFConstraintSettings (src/constraints/six-dof-constraint.ts:60-117).  Axes 0-2 are the
+ * translations along the constraint frame's X, Y, Z, axes 3-5 the rotations about them (3 twist,
+ * 4 swing Y, 5 swing Z).  An axis with limit_min >= limit_max is fixed (at limit_min); one with
+ * [-inf, +inf] (translation) or [-pi, pi] (rotation) is free; anything else is limited.  The
+ * constraint frame of body A (B) has columns axis_x_a, axis_y_a and their cross product.
+ * motor_state / target_* are applied after creation as setMotorState / setTarget*CS do; the
+ * target orientation is clamped into the rotation limits.  Reference defaults: limits free,
+ * no friction, motor springs 10 Hz (translation) and 2 Hz (rotation) with damping 1, motor
+ * forces unbounded, target orientation identity. */
+typedef struct cc_six_dof_desc {
+    int32_t body_a, body_b;
+    int32_t space;
+    int32_t swing_type;                /* cc_swing_type of the rotation limits */
+    float position_a[3], position_b[3];
+    float axis_x_a[3], axis_y_a[3];
+    float axis_x_b[3], axis_y_b[3];
+    float limit_min[6], limit_max[6];  /* metres (0-2) and radians (3-5) */
+    float max_friction[6];             /* N or N m while an axis' motor is off */
+    cc_spring_settings limits_spring[3];  /* soft translation limits when frequency_or_stiffness > 0 */
+    cc_spring_settings motor_spring[6];   /* position motors */
+    float motor_min_force[6], motor_max_force[6];
+    int32_t motor_state[6];            /* cc_motor_state per axis */
+    float target_velocity[3];          /* m/s along the constraint axes */
+    float target_angular_velocity[3];  /* rad/s about the constraint axes */
+    float target_position[3];          /* m, constraint space */
+    float target_orientation[4];       /* x y z w, body B's constraint frame relative to A's */
+    int32_t priority, enabled;
+    int32_t num_velocity_steps_override, num_position_steps_override;
+} cc_six_dof_desc;
+/* sixDOFConstraint.create (six-dof-constraint.ts:335-480) for n joints. */
+int cc_world_add_six_dof_joints(cc_world *world, const cc_six_dof_desc *joints, int32_t n, int32_t *out_index);
+/* setTranslationLimits then setRotationLimits (six-dof-constraint.ts:1238-1260): 6 + 6 floats. */
+int cc_world_set_six_dof_limits(cc_world *world, int32_t index, const float *limit_min, const float *limit_max);
+/* setMaxFriction and setMotorState per axis, setTargetVelocityCS, setTargetAngularVelocityCS,
+ * setTargetPositionCS, setTargetOrientationCS (six-dof-constraint.ts:1262-1306). */
+int cc_world_set_six_dof_motor(cc_world *world, int32_t index, const int32_t *motor_state,
+                               const float *target_velocity, const float *target_angular_velocity,
+                               const float *target_position, const float *target_orientation,
+                               const float *max_friction);
+
 /* ConstraintBase.enabled of one joint of any type (cc_joint_type). */
 int cc_world_set_joint_enabled(cc_world *world, int32_t type, int32_t index, int32_t enabled);
 /* The accumulated impulses of one joint after the last step (getTotalLambda* of each type):
  * point 3 (point part); distance 1; fixed 6 (point, rotation); cone 4 (point, cone angle);
- * slider 7 (2 position, 3 rotation, limits, motor).  *count receives the number written. */
+ * slider 7 (2 position, 3 rotation, limits, motor); six-DOF 18 (3 translation limits, point 3,
+ * rotation 3, swing Y, swing Z, twist, 3 translation motors, 3 rotation motors).  *count
+ * receives the number written. */
 int cc_world_get_joint_lambdas(cc_world *world, int32_t type, int32_t index, float *out, int32_t capacity,
                                int32_t *count);
 

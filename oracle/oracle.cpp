@@ -163,6 +163,7 @@ struct World {
     std::vector<FixedJoint> fixeds;
     std::vector<ConeJoint> cones;
     std::vector<SliderJoint> sliders;
+    std::vector<SixDofJoint> sixdofs;
     std::vector<std::unique_ptr<HullData>> hulls;  // convex hull shapes the bodies refer to
     std::vector<std::unique_ptr<MeshData>> meshes;  // triangle meshes the bodies refer to
     // skip broadphase pairs of bodies that share an enabled joint: the declarative form of the
@@ -543,7 +544,9 @@ static void bvh_build(const std::vector<Body> &bodies, std::vector<int> &idx, st
 // (constraint-id.ts:1-35): the ConstraintType above bit 24, the per-type index below.
 // joint_ids lists them type by type, each in creation order, the order in which the
 // reference walks its constraint pools (constraints.ts:264-318, islands.ts:210-225).
-enum JointType { JT_POINT = 0, JT_DISTANCE = 1, JT_HINGE = 2, JT_SLIDER = 3, JT_FIXED = 4, JT_CONE = 5, JT_SWING = 6 };
+enum JointType {
+    JT_POINT = 0, JT_DISTANCE = 1, JT_HINGE = 2, JT_SLIDER = 3, JT_FIXED = 4, JT_CONE = 5, JT_SWING = 6, JT_SIX_DOF = 7
+};
 constexpr int JOINT_TYPE_SHIFT = 24, JOINT_INDEX_MASK = (1 << JOINT_TYPE_SHIFT) - 1;
 inline int joint_type(int id) { return id >> JOINT_TYPE_SHIFT; }
 inline int joint_index(int id) { return id & JOINT_INDEX_MASK; }
@@ -560,6 +563,7 @@ static const JointBase &joint_base(const World &w, int id) {
     case JT_SLIDER: return w.sliders[i];
     case JT_FIXED: return w.fixeds[i];
     case JT_CONE: return w.cones[i];
+    case JT_SIX_DOF: return w.sixdofs[i];
     default: break;
     }
     static const JointBase none;
@@ -567,9 +571,9 @@ static const JointBase &joint_base(const World &w, int id) {
 }
 static std::vector<int> joint_ids(const World &w) {
     std::vector<int> ids;
-    size_t count[7] = {w.points.size(), w.distances.size(), w.joints.size(), w.sliders.size(),
-                       w.fixeds.size(),  w.cones.size(),     w.swings.size()};
-    for (int t = 0; t < 7; t++)
+    size_t count[8] = {w.points.size(), w.distances.size(), w.joints.size(), w.sliders.size(),
+                       w.fixeds.size(),  w.cones.size(),     w.swings.size(), w.sixdofs.size()};
+    for (int t = 0; t < 8; t++)
         for (size_t i = 0; i < count[t]; i++) ids.push_back((t << JOINT_TYPE_SHIFT) | (int)i);
     return ids;
 }
@@ -1143,6 +1147,7 @@ static void joint_setup(World &w, int id, double dt) {
     case JT_FIXED: { FixedJoint &j = w.fixeds[i]; fixed_setup(j, w.bodies[j.a], w.bodies[j.b]); break; }
     case JT_CONE: { ConeJoint &j = w.cones[i]; cone_setup(j, w.bodies[j.a], w.bodies[j.b]); break; }
     case JT_SWING: { SwingTwistJoint &j = w.swings[i]; swing_setup(j, w.bodies[j.a], w.bodies[j.b], dt); break; }
+    case JT_SIX_DOF: { SixDofJoint &j = w.sixdofs[i]; sixdof_setup(j, w.bodies[j.a], w.bodies[j.b], dt); break; }
     }
 }
 static void joint_warm(World &w, int id, double ratio) {
@@ -1155,6 +1160,7 @@ static void joint_warm(World &w, int id, double ratio) {
     case JT_FIXED: { FixedJoint &j = w.fixeds[i]; fixed_warm(j, w.bodies[j.a], w.bodies[j.b], ratio); break; }
     case JT_CONE: { ConeJoint &j = w.cones[i]; cone_warm(j, w.bodies[j.a], w.bodies[j.b], ratio); break; }
     case JT_SWING: { SwingTwistJoint &j = w.swings[i]; swing_warm(j, w.bodies[j.a], w.bodies[j.b], ratio); break; }
+    case JT_SIX_DOF: { SixDofJoint &j = w.sixdofs[i]; sixdof_warm(j, w.bodies[j.a], w.bodies[j.b], ratio); break; }
     }
 }
 static bool joint_solve_velocity(World &w, int id, double dt) {
@@ -1167,6 +1173,7 @@ static bool joint_solve_velocity(World &w, int id, double dt) {
     case JT_FIXED: { FixedJoint &j = w.fixeds[i]; return fixed_solve_velocity(j, w.bodies[j.a], w.bodies[j.b]); }
     case JT_CONE: { ConeJoint &j = w.cones[i]; return cone_solve_velocity(j, w.bodies[j.a], w.bodies[j.b]); }
     case JT_SWING: { SwingTwistJoint &j = w.swings[i]; return swing_solve_velocity(j, w.bodies[j.a], w.bodies[j.b], dt); }
+    case JT_SIX_DOF: { SixDofJoint &j = w.sixdofs[i]; return sixdof_solve_velocity(j, w.bodies[j.a], w.bodies[j.b], dt); }
     }
     return false;
 }
@@ -1184,6 +1191,7 @@ static bool joint_solve_position(World &w, int id, double dt) {
     case JT_FIXED: { FixedJoint &j = w.fixeds[i]; return fixed_solve_position(j, w.bodies[j.a], w.bodies[j.b], beta); }
     case JT_CONE: { ConeJoint &j = w.cones[i]; return cone_solve_position(j, w.bodies[j.a], w.bodies[j.b], beta); }
     case JT_SWING: { SwingTwistJoint &j = w.swings[i]; return swing_solve_position(j, w.bodies[j.a], w.bodies[j.b], beta); }
+    case JT_SIX_DOF: { SixDofJoint &j = w.sixdofs[i]; return sixdof_solve_position(j, w.bodies[j.a], w.bodies[j.b], beta); }
     }
     return false;
 }
@@ -2407,6 +2415,12 @@ int orc_add_swing_twist(void *wp, const double *d) {
 //             28-30 limits spring, 31 maxFrictionForce, 32-34 motor spring, 35 min force,
 //             36 max force, 37 motor state, 38 target velocity, 39 target position
 //             (37-39 through setMotorState / setTargetVelocity / setTargetPosition)
+//   six-DOF   7-9 position1, 10-12 position2, 13-15 axisX1, 16-18 axisY1, 19-21 axisX2, 22-24 axisY2,
+//             25 swingType, 26-31 limitMin, 32-37 limitMax, 38-43 maxFriction, 44-52 limits
+//             springs (3 x mode, frequency or stiffness, damping), 53-70 motor springs (6 x 3),
+//             71-76 motor min force, 77-82 motor max force, 83-88 motor states, 89-91 target
+//             velocity, 92-94 target angular velocity, 95-97 target position, 98-101 target
+//             orientation (83-101 through setMotorState and the setTarget*CS setters)
 // Returns the joint's per-type index, or -1.
 int orc_add_joint(void *wp, int type, const double *d) {
     World &w = *(World *)wp;
@@ -2562,12 +2576,50 @@ int orc_add_joint(void *wp, int type, const double *d) {
         w.sliders.push_back(j);
         return j.index;
     }
+    case JT_SIX_DOF: {  // six-dof-constraint.ts create :335-480 and the setters :1262-1299
+        SixDofJoint j;
+        base(j, (int)w.sixdofs.size());
+        auto frame = [&](V3 x, V3 y) { return axes_to_quat(normalize(x), normalize(y)); };
+        j.c2b1 = frame(v(13), v(16));
+        j.c2b2 = frame(v(19), v(22));
+        if (world_space) {
+            j.lp1 = rotate(iqA, sub(v(7), A.com));
+            j.lp2 = rotate(iqB, sub(v(10), B.com));
+            j.c2b1 = qmul(iqA, j.c2b1);
+            j.c2b2 = qmul(iqB, j.c2b2);
+        } else {
+            j.lp1 = v(7);
+            j.lp2 = v(10);
+        }
+        j.swingType = (int)d[25];
+        for (int k = 0; k < 6; k++) {
+            j.limitMin[k] = d[26 + k];
+            j.limitMax[k] = d[32 + k];
+            j.maxFriction[k] = d[38 + k];
+            j.motorSpring[k] = {(int)d[53 + 3 * k], d[54 + 3 * k], d[55 + 3 * k]};
+            j.motorMinForce[k] = d[71 + k];
+            j.motorMaxForce[k] = d[77 + k];
+            j.motorState[k] = (int)d[83 + k];
+        }
+        for (int k = 0; k < 3; k++) j.limitsSpring[k] = {(int)d[44 + 3 * k], d[45 + 3 * k], d[46 + 3 * k]};
+        sd_update(j);
+        j.targetVelocity = v(89);
+        j.targetAngularVelocity = v(92);
+        j.targetPosition = v(95);
+        Q4 to{d[98], d[99], d[100], d[101]}, sw, tw;  // setTargetOrientationCS: clamped into the limits
+        get_swing_twist(to, sw, tw);
+        clamp_swing_twist(j.st, sw, tw);
+        j.targetOrientation = qmul(sw, tw);
+        w.sixdofs.push_back(j);
+        return j.index;
+    }
     default: return -1;
     }
 }
 // Total impulses of one joint (getTotalLambda* of each type): point 3 (point part),
 // distance 1, fixed 6 (point, rotation), cone 4 (point, angle), slider 2 + 3 + 1 + 1
-// (position, rotation, limits, motor).  Returns the count written, or -1.
+// (position, rotation, limits, motor), six-DOF 18 (3 translation rows, point, rotation, swing Y,
+// swing Z, twist, 3 translation motors, 3 rotation motors).  Returns the count written, or -1.
 int orc_get_joint_lambdas(void *wp, int type, int index, double *out) {
     World &w = *(World *)wp;
     auto put3 = [&](int k, V3 a) {
@@ -2603,6 +2655,19 @@ int orc_get_joint_lambdas(void *wp, int type, int index, double *out) {
         out[5] = j.limits.totalLambda;
         out[6] = j.motor.totalLambda;
         return 7;
+    }
+    case JT_SIX_DOF: {
+        if (index < 0 || index >= (int)w.sixdofs.size()) return -1;
+        const SixDofJoint &j = w.sixdofs[index];
+        for (int k = 0; k < 3; k++) out[k] = j.translation[k].totalLambda;
+        put3(3, j.point.totalLambda);
+        put3(6, j.rot.totalLambda);
+        out[9] = j.st.swingY.totalLambda;
+        out[10] = j.st.swingZ.totalLambda;
+        out[11] = j.st.twist.totalLambda;
+        for (int k = 0; k < 3; k++) out[12 + k] = j.motorTranslation[k].totalLambda;
+        for (int k = 0; k < 3; k++) out[15 + k] = j.motorRotation[k].totalLambda;
+        return 18;
     }
     default: return -1;
     }

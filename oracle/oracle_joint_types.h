@@ -185,3 +185,30 @@ struct SliderJoint : JointBase {
     EulerPart rot;
     AxisPart limits, motor;
 };
+
+// SixDOFConstraint six-dof-constraint.ts:66-117 (defaults makeSixDOFConstraint :119-163)
+struct SixDofJoint : JointBase {
+    V3 lp1, lp2;
+    Q4 c2b1{0, 0, 0, 1}, c2b2{0, 0, 0, 1};  // constraintToBody1 / 2
+    double limitMin[6] = {-1.0 / 0.0, -1.0 / 0.0, -1.0 / 0.0, -M_PI, -M_PI, -M_PI};
+    double limitMax[6] = {1.0 / 0.0, 1.0 / 0.0, 1.0 / 0.0, M_PI, M_PI, M_PI};
+    SpringSettings limitsSpring[3];
+    double maxFriction[6] = {0, 0, 0, 0, 0, 0};
+    int motorState[6] = {MOTOR_OFF, MOTOR_OFF, MOTOR_OFF, MOTOR_OFF, MOTOR_OFF, MOTOR_OFF};
+    SpringSettings motorSpring[6];
+    double motorMinForce[6] = {-1.0 / 0.0, -1.0 / 0.0, -1.0 / 0.0, -1.0 / 0.0, -1.0 / 0.0, -1.0 / 0.0};
+    double motorMaxForce[6] = {1.0 / 0.0, 1.0 / 0.0, 1.0 / 0.0, 1.0 / 0.0, 1.0 / 0.0, 1.0 / 0.0};
+    V3 targetVelocity{0, 0, 0}, targetAngularVelocity{0, 0, 0}, targetPosition{0, 0, 0};
+    Q4 targetOrientation{0, 0, 0, 1};
+    int swingType = SWING_CONE;
+    V3 translationAxis[3], rotationAxis[3];
+    double displacement[3] = {0, 0, 0};
+    int freeAxis = 0, fixedAxis = 0;
+    bool translationMotorActive = false, rotationMotorActive = false, hasSpringLimits = false;
+    int rotationPositionMotorActive = 0;
+    AxisPart translation[3], motorTranslation[3];
+    PointPart point;
+    SwingTwistPart st;
+    EulerPart rot;
+    AnglePart motorRotation[3];
+};

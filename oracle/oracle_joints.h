@@ -1326,3 +1326,284 @@ inline bool slider_solve_position(SliderJoint &j, Body &A, Body &B, double dt, d
     }
     return pos || rot || limit;
 }
+
+// swingTwistConstraintPart.deactivate: the three limit parts
+inline void st_deactivate(SwingTwistPart &p) {
+    angle_deactivate(p.swingY);
+    angle_deactivate(p.swingZ);
+    angle_deactivate(p.twist);
+}
+
+// ---- SixDOFConstraint (six-dof-constraint.ts) -----------------------------------------
+inline bool sd_fixed(const SixDofJoint &j, int a) { return (j.fixedAxis & (1 << a)) != 0; }
+inline bool sd_free(const SixDofJoint &j, int a) { return (j.freeAxis & (1 << a)) != 0; }
+inline bool sd_trans_constrained(const SixDofJoint &j) { return (j.freeAxis & 7) != 7; }
+inline bool sd_trans_fully(const SixDofJoint &j) { return (j.fixedAxis & 7) == 7 && !j.hasSpringLimits; }
+inline bool sd_rot_constrained(const SixDofJoint &j) { return (j.freeAxis & 56) != 56; }
+inline bool sd_rot_fully(const SixDofJoint &j) { return (j.fixedAxis & 56) == 56; }
+inline bool sd_friction(const SixDofJoint &j, int a) { return !sd_fixed(j, a) && j.maxFriction[a] > 0; }
+// updateTranslationLimits / updateRotationLimits / updateFixedFreeAxis and the cached motor
+// flags (:240-333), applied after creation and after every setter
+inline void sd_update(SixDofJoint &j) {
+    for (int i = 0; i < 3; i++)
+        if (j.limitMin[i] > j.limitMax[i]) j.limitMin[i] = j.limitMax[i] = 0;
+    if (j.swingType == SWING_CONE) {
+        j.limitMax[4] = std::max(0.0, j.limitMax[4]);
+        j.limitMax[5] = std::max(0.0, j.limitMax[5]);
+        j.limitMin[4] = -j.limitMax[4];
+        j.limitMin[5] = -j.limitMax[5];
+    }
+    for (int i = 3; i < 6; i++) {
+        j.limitMin[i] = std::max(-M_PI, std::min(M_PI, j.limitMin[i]));
+        j.limitMax[i] = std::max(-M_PI, std::min(M_PI, j.limitMax[i]));
+        if (j.limitMin[i] > j.limitMax[i]) j.limitMin[i] = j.limitMax[i] = 0;
+    }
+    j.st.swingType = j.swingType;
+    st_set_limits(j.st, j.limitMin[3], j.limitMax[3], j.limitMin[4], j.limitMax[4], j.limitMin[5], j.limitMax[5]);
+    j.freeAxis = j.fixedAxis = 0;
+    for (int a = 0; a < 6; a++) {
+        double lim = a >= 3 ? M_PI : 1.0 / 0.0;
+        if (j.limitMin[a] >= j.limitMax[a])
+            j.fixedAxis |= 1 << a;
+        else if (j.limitMin[a] <= -lim && j.limitMax[a] >= lim)
+            j.freeAxis |= 1 << a;
+    }
+    j.hasSpringLimits = j.limitsSpring[0].frequencyOrStiffness > 0 || j.limitsSpring[1].frequencyOrStiffness > 0 ||
+                        j.limitsSpring[2].frequencyOrStiffness > 0;
+    j.translationMotorActive = j.rotationMotorActive = false;
+    for (int i = 0; i < 3; i++) {
+        j.translationMotorActive = j.translationMotorActive || j.motorState[i] != MOTOR_OFF || sd_friction(j, i);
+        j.rotationMotorActive = j.rotationMotorActive || j.motorState[3 + i] != MOTOR_OFF || sd_friction(j, 3 + i);
+    }
+    j.rotationPositionMotorActive = 0;
+    for (int i = 0; i < 3; i++)
+        if (j.motorState[3 + i] == MOTOR_POSITION) j.rotationPositionMotorActive |= 1 << i;
+}
+// getTwistAroundAxis :37-49
+inline Q4 twist_around(Q4 q, V3 axis) {
+    double d = q.x * axis.x + q.y * axis.y + q.z * axis.z;
+    double l = d * d + q.w * q.w;
+    if (!(l > 1e-10)) return {0, 0, 0, 1};
+    double il = 1 / std::sqrt(l);
+    return {d * axis.x * il, d * axis.y * il, d * axis.z * il, q.w * il};
+}
+// getPositionConstraintProperties :535-566
+inline void sd_position_props(const SixDofJoint &j, const Body &A, const Body &B, V3 &r1u, V3 &r2, V3 &u) {
+    V3 p1 = add(rotate(A.quat, j.lp1), A.com), p2 = add(rotate(B.quat, j.lp2), B.com);
+    r1u = sub(p2, A.com);
+    r2 = sub(p2, B.com);
+    u = sub(p2, p1);
+}
+inline V3 m4_column(const M4 &m, int i) { return {m.m[4 * i], m.m[4 * i + 1], m.m[4 * i + 2]}; }
+// setupVelocity :568-881
+inline void sixdof_setup(SixDofJoint &j, const Body &A, const Body &B, double dt) {
+    Q4 c1w = qmul(A.quat, j.c2b1);
+    M4 ax = mat4_from_quat(c1w);
+    for (int i = 0; i < 3; i++) j.translationAxis[i] = m4_column(ax, i);
+    if (sd_trans_fully(j)) {
+        point_calc(j.point, A, j.lp1, B, j.lp2);
+    } else if (sd_trans_constrained(j) || j.translationMotorActive) {
+        V3 r1u, r2, u;
+        sd_position_props(j, A, B, r1u, r2, u);
+        for (int i = 0; i < 3; i++) {
+            const V3 ta = j.translationAxis[i];
+            double d = dot(ta, u);
+            j.displacement[i] = d;
+            bool on = false;
+            double C = 0;
+            if (sd_fixed(j, i)) {
+                C = d - j.limitMin[i];
+                on = true;
+            } else if (!sd_free(j, i)) {
+                if (d <= j.limitMin[i]) {
+                    C = d - j.limitMin[i];
+                    on = true;
+                } else if (d >= j.limitMax[i]) {
+                    C = d - j.limitMax[i];
+                    on = true;
+                }
+            }
+            if (on) {
+                if (j.limitsSpring[i].frequencyOrStiffness > 0)
+                    axis_calc_settings(j.translation[i], dt, A, B, r1u, r2, ta, 0, C, j.limitsSpring[i]);
+                else
+                    axis_calc(j.translation[i], A, B, r1u, r2, ta, 0);
+            } else {
+                axis_deactivate(j.translation[i]);
+            }
+            if (j.motorState[i] == MOTOR_OFF) {
+                if (sd_friction(j, i))
+                    axis_calc(j.motorTranslation[i], A, B, r1u, r2, ta, 0);
+                else
+                    axis_deactivate(j.motorTranslation[i]);
+            } else if (j.motorState[i] == MOTOR_VELOCITY) {
+                axis_calc(j.motorTranslation[i], A, B, r1u, r2, ta, -(&j.targetVelocity.x)[i]);
+            } else if (j.motorSpring[i].frequencyOrStiffness > 0) {
+                axis_calc_settings(j.motorTranslation[i], dt, A, B, r1u, r2, ta, 0,
+                                   dot(ta, u) - (&j.targetPosition.x)[i], j.motorSpring[i]);
+            } else {
+                axis_deactivate(j.motorTranslation[i]);
+            }
+        }
+    }
+    Q4 c2w = qmul(B.quat, j.c2b2);
+    Q4 q = qmul(qconj(c1w), c2w);
+    if (sd_rot_fully(j)) {
+        euler_calc(j.rot, A, B);
+    } else if (sd_rot_constrained(j) || j.rotationMotorActive) {
+        if (sd_rot_constrained(j))
+            st_calc(j.st, A, B, q, c1w);
+        else
+            st_deactivate(j.st);
+        if (j.rotationMotorActive) {
+            M4 rm = mat4_from_quat(c2w);
+            for (int i = 0; i < 3; i++) j.rotationAxis[i] = m4_column(rm, i);
+            Q4 t = j.targetOrientation;
+            if (q.x * t.x + q.y * t.y + q.z * t.z + q.w * t.w < 0) t = qscale(t, -1);
+            Q4 diff = qmul(qconj(q), t), pd;
+            const V3 X{1, 0, 0}, Y{0, 1, 0}, Z{0, 0, 1};
+            switch (j.rotationPositionMotorActive) {
+                case 1: pd = twist_around(diff, X); break;
+                case 2: pd = twist_around(diff, Y); break;
+                case 4: pd = twist_around(diff, Z); break;
+                case 3: pd = qmul(diff, qconj(twist_around(diff, Z))); break;
+                case 5: pd = qmul(diff, qconj(twist_around(diff, Y))); break;
+                case 6: pd = qmul(diff, qconj(twist_around(diff, X))); break;
+                default: pd = diff; break;
+            }
+            double err[3] = {-2 * pd.x, -2 * pd.y, -2 * pd.z};
+            for (int i = 0; i < 3; i++) {
+                const int a = 3 + i;
+                if (j.motorState[a] == MOTOR_OFF) {
+                    if (sd_friction(j, a))
+                        angle_calc(j.motorRotation[i], A, B, j.rotationAxis[i], 0);
+                    else
+                        angle_deactivate(j.motorRotation[i]);
+                } else if (j.motorState[a] == MOTOR_VELOCITY) {
+                    angle_calc(j.motorRotation[i], A, B, j.rotationAxis[i], -(&j.targetAngularVelocity.x)[i]);
+                } else if (j.motorSpring[a].frequencyOrStiffness > 0) {
+                    angle_calc_settings(j.motorRotation[i], dt, A, B, j.rotationAxis[i], 0, err[i], j.motorSpring[a]);
+                } else {
+                    angle_deactivate(j.motorRotation[i]);
+                }
+            }
+        }
+    }
+}
+// warmStartVelocity :883-942
+inline void sixdof_warm(SixDofJoint &j, Body &A, Body &B, double ratio) {
+    double imA = dyn_inv_mass(A), imB = dyn_inv_mass(B);
+    if (j.translationMotorActive)
+        for (int i = 0; i < 3; i++)
+            if (j.motorTranslation[i].effMass != 0)
+                warm_start(j.motorTranslation[i], A, B, imA, imB, j.translationAxis[i], ratio);
+    if (j.rotationMotorActive)
+        for (int i = 0; i < 3; i++)
+            if (angle_active(j.motorRotation[i])) angle_warm(j.motorRotation[i], A, B, ratio);
+    if (sd_rot_fully(j))
+        euler_warm(j.rot, A, B, ratio);
+    else if (sd_rot_constrained(j))
+        st_warm(j.st, A, B, ratio);
+    if (sd_trans_fully(j)) {
+        point_warm(j.point, A, B, ratio);
+    } else if (sd_trans_constrained(j)) {
+        for (int i = 0; i < 3; i++)
+            if (j.translation[i].effMass != 0) warm_start(j.translation[i], A, B, imA, imB, j.translationAxis[i], ratio);
+    }
+}
+// solveVelocity :966-1082 (returns false, as the reference does)
+inline bool sixdof_solve_velocity(SixDofJoint &j, Body &A, Body &B, double dt) {
+    if (j.translationMotorActive)
+        for (int i = 0; i < 3; i++) {
+            if (j.motorTranslation[i].effMass == 0) continue;
+            if (j.motorState[i] == MOTOR_OFF) {
+                double ml = j.maxFriction[i] * dt;
+                axis_solve_velocity(j.motorTranslation[i], A, B, j.translationAxis[i], -ml, ml);
+            } else {
+                axis_solve_velocity(j.motorTranslation[i], A, B, j.translationAxis[i], dt * j.motorMinForce[i],
+                                    dt * j.motorMaxForce[i]);
+            }
+        }
+    if (j.rotationMotorActive)
+        for (int i = 0; i < 3; i++) {
+            const int a = 3 + i;
+            if (!angle_active(j.motorRotation[i])) continue;
+            if (j.motorState[a] == MOTOR_OFF) {
+                double ml = j.maxFriction[a] * dt;
+                angle_solve_velocity(j.motorRotation[i], A, B, j.rotationAxis[i], -ml, ml);
+            } else {
+                angle_solve_velocity(j.motorRotation[i], A, B, j.rotationAxis[i], dt * j.motorMinForce[a],
+                                     dt * j.motorMaxForce[a]);
+            }
+        }
+    if (sd_rot_fully(j))
+        euler_solve_velocity(j.rot, A, B);
+    else if (sd_rot_constrained(j))
+        st_solve_velocity(j.st, A, B);
+    if (sd_trans_fully(j)) {
+        point_solve_velocity(j.point, A, B);
+    } else if (sd_trans_constrained(j)) {
+        for (int i = 0; i < 3; i++) {
+            if (j.translation[i].effMass == 0) continue;
+            double mn = -1.0 / 0.0, mx = 1.0 / 0.0;
+            if (!sd_fixed(j, i)) {
+                if (j.displacement[i] <= j.limitMin[i])
+                    mn = 0;
+                else if (j.displacement[i] >= j.limitMax[i])
+                    mx = 0;
+            }
+            axis_solve_velocity(j.translation[i], A, B, j.translationAxis[i], mn, mx);
+        }
+    }
+    return false;
+}
+// quat.fromEuler for an 'xyz' euler (mathcat, unpinned): the rotation X then Y then Z applied
+// to the frame, q = qx qy qz
+inline Q4 quat_from_euler_xyz(double x, double y, double z) {
+    double c1 = std::cos(x / 2), s1 = std::sin(x / 2), c2 = std::cos(y / 2), s2 = std::sin(y / 2), c3 = std::cos(z / 2),
+           s3 = std::sin(z / 2);
+    return {s1 * c2 * c3 + c1 * s2 * s3, c1 * s2 * c3 - s1 * c2 * s3, c1 * c2 * s3 + s1 * s2 * c3,
+            c1 * c2 * c3 - s1 * s2 * s3};
+}
+// solvePosition :1084-1236
+inline bool sixdof_solve_position(SixDofJoint &j, Body &A, Body &B, double baumgarte) {
+    bool imp = false;
+    if (sd_rot_fully(j)) {
+        Q4 off = qmul(j.c2b1, quat_from_euler_xyz(j.limitMin[3], j.limitMin[4], j.limitMin[5]));
+        Q4 invInitial = qmul(j.c2b2, qconj(off));
+        euler_calc(j.rot, A, B);
+        imp = euler_solve_position(j.rot, A, B, invInitial, baumgarte) || imp;
+    } else if (sd_rot_constrained(j)) {
+        Q4 c1w = qmul(A.quat, j.c2b1), c2w = qmul(B.quat, j.c2b2);
+        Q4 q = qmul(qconj(c1w), c2w);
+        imp = st_solve_position(j.st, A, B, q, j.c2b1, j.c2b2, baumgarte) || imp;
+    }
+    if (sd_trans_fully(j)) {
+        V3 lp1 = add(j.lp1, rotate(j.c2b1, V3{j.limitMin[0], j.limitMin[1], j.limitMin[2]}));
+        point_calc(j.point, A, lp1, B, j.lp2);
+        imp = point_solve_position(j.point, A, B, baumgarte) || imp;
+    } else if (sd_trans_constrained(j)) {
+        for (int i = 0; i < 3; i++) {
+            if (j.limitsSpring[i].frequencyOrStiffness > 0) continue;
+            V3 r1u, r2, u;
+            sd_position_props(j, A, B, r1u, r2, u);
+            V3 e{i == 0 ? 1.0 : 0.0, i == 1 ? 1.0 : 0.0, i == 2 ? 1.0 : 0.0};
+            V3 ta = rotate(qmul(A.quat, j.c2b1), e);
+            double err = 0;
+            if (sd_fixed(j, i)) {
+                err = dot(u, ta) - j.limitMin[i];
+            } else if (!sd_free(j, i)) {
+                double d = dot(u, ta);
+                if (d <= j.limitMin[i])
+                    err = d - j.limitMin[i];
+                else if (d >= j.limitMax[i])
+                    err = d - j.limitMax[i];
+            }
+            if (err != 0) {
+                axis_calc(j.translation[i], A, B, r1u, r2, ta, 0);
+                imp = axis_solve_position(j.translation[i], A, B, ta, err, baumgarte) || imp;
+            }
+        }
+    }
+    return imp;
+}

@@ -347,7 +347,7 @@ class OracleWorld:
     def add_joint_record(self, joint_type: int, h) -> int:
         """Point, distance, fixed, cone or slider joint from a record of the C description
         (crashcat_gb300._lib.JOINT_DTYPES; fields by name) in the orc_add_joint layout."""
-        d = np.zeros(40, dtype=np.float64)
+        d = np.zeros(102, dtype=np.float64)
         d[0], d[1], d[2] = h["body_a"], h["body_b"], h["space"]
         d[3], d[4], d[5], d[6] = (h["priority"], h["num_velocity_steps_override"], h["num_position_steps_override"],
                                   h["enabled"])
@@ -382,6 +382,19 @@ class OracleWorld:
             spring(32, "motor_spring")
             d[35], d[36] = h["min_force_limit"], h["max_force_limit"]
             d[37], d[38], d[39] = h["motor_state"], h["target_velocity"], h["target_position"]
+        elif joint_type == 7:  # six-DOF
+            put(7, ("position_a", "position_b", "axis_x_a", "axis_y_a", "axis_x_b", "axis_y_b"))
+            d[25] = h["swing_type"]
+            d[26:32], d[32:38], d[38:44] = h["limit_min"], h["limit_max"], h["max_friction"]
+            for k in range(3):
+                sp = h["limits_spring"][k]
+                d[44 + 3 * k:47 + 3 * k] = (sp["mode"], sp["frequency_or_stiffness"], sp["damping"])
+            for k in range(6):
+                sp = h["motor_spring"][k]
+                d[53 + 3 * k:56 + 3 * k] = (sp["mode"], sp["frequency_or_stiffness"], sp["damping"])
+            d[71:77], d[77:83], d[83:89] = h["motor_min_force"], h["motor_max_force"], h["motor_state"]
+            d[89:92], d[92:95], d[95:98] = h["target_velocity"], h["target_angular_velocity"], h["target_position"]
+            d[98:102] = h["target_orientation"]
         else:
             raise ValueError(f"joint type {joint_type}")
         k = self.lib.orc_add_joint(self.h, int(joint_type), dptr(d))
@@ -389,7 +402,7 @@ class OracleWorld:
         return k
 
     def joint_lambdas(self, joint_type: int, index: int) -> np.ndarray:
-        out = np.zeros(8, dtype=np.float64)
+        out = np.zeros(18, dtype=np.float64)
         n = self.lib.orc_get_joint_lambdas(self.h, int(joint_type), int(index), dptr(out))
         assert n >= 0
         return out[:n]
