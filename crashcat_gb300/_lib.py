@@ -106,6 +106,18 @@ SHAPE_CAST_DTYPE = np.dtype([("shape_type", np.int32), ("shape_params", np.float
                              ("quaternion", np.float32, 4), ("displacement", np.float32, 3), ("world", np.int32)])
 SHAPE_CAST_HIT_DTYPE = np.dtype([("body", np.int32), ("fraction", np.float32), ("normal", np.float32, 3),
                                  ("point", np.float32, 3)])
+# query collectors (cc_collector) and the collide query's records
+COLLECT_CLOSEST, COLLECT_ANY, COLLECT_ALL = 0, 1, 2
+COLLIDE_SHAPE_DTYPE = np.dtype([("shape_type", np.int32), ("shape_params", np.float32, 4),
+                                ("position", np.float32, 3), ("quaternion", np.float32, 4), ("world", np.int32)])
+COLLIDE_SHAPE_HIT_DTYPE = np.dtype([("body", np.int32), ("sub_shape_id", np.uint32), ("penetration", np.float32),
+                                    ("point_a", np.float32, 3), ("point_b", np.float32, 3),
+                                    ("axis", np.float32, 3)])
+
+
+class CollideShapeSettings(C.Structure):
+    _fields_ = [("max_separation_distance", C.c_float), ("collision_tolerance", C.c_float),
+                ("penetration_tolerance", C.c_float), ("collide_with_backfaces", C.c_int32)]
 
 
 class QueryFilter(C.Structure):
@@ -199,6 +211,12 @@ EXPORTS = {
     "cc_world_cast_shapes": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
     "cc_world_cast_shapes_device": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
     "cc_world_cast_rays": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
+    "cc_world_cast_rays_collect": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32,
+                                    C.c_void_p, C.c_void_p], C.c_int),
+    "cc_world_cast_shapes_collect": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32,
+                                      C.c_void_p, C.c_void_p], C.c_int),
+    "cc_world_collide_shapes": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
+                                 C.c_void_p, C.c_void_p], C.c_int),
     "cc_world_cast_rays_device": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
     "cc_world_add_convex_hull": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.POINTER(C.c_int32)], C.c_int),
     "cc_world_get_convex_hull": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -783,8 +783,14 @@ void launch_query_tree(DevWorld &w, cudaStream_t s);
 // launch_ray_order; keys/keys_alt 2 x nr, idx/idx_alt 2 x nr, tmp radix_tmp_ints(nr)
 void launch_ray_order(DevWorld &w, const DevRay *rays, int nr, unsigned long long *keys, int *idx, int *tmp,
                       cudaStream_t s);
+// the hit collectors of the queries: closest, any (the first found) and all (cast-ray-vs-shape.ts
+// :66-205, cast-shape-vs-shape.ts:165-226, collide-shape-vs-shape.ts:82-176)
+enum : int { COLLECT_CLOSEST = 0, COLLECT_ANY = 1, COLLECT_ALL = 2 };
+// hits: nr x (mode ALL ? cap : 1) records; counts (modes ANY and ALL): hits found per ray.  Mode ALL
+// leaves each ray's first min(count, cap) hits sorted by fraction, body, sub-shape id.
 void launch_cast_rays(DevWorld &w, const DevRay *rays, const int *order, int nr, const DevRayFilter &f,
-                      DevRayHit *hits, cudaStream_t s);
+                      DevRayHit *hits, cudaStream_t s, int mode = COLLECT_CLOSEST, int cap = 1,
+                      int *counts = nullptr);
 // shape casts: a sphere, box or capsule (params as a body's shape record) at a pose, moved by a
 // displacement, in a world; the hit: body (-1), fraction, normal, contact point on the cast shape
 struct DevShapeCast {
@@ -802,7 +808,32 @@ struct DevShapeCastHit {
     float point[3];
 };
 void launch_cast_shapes(DevWorld &w, const DevShapeCast *qs, int nq, const DevRayFilter &f, DevShapeCastHit *hits,
-                        cudaStream_t s);
+                        cudaStream_t s, int mode = COLLECT_CLOSEST, int cap = 1, int *counts = nullptr);
+// collide queries: a sphere, box or capsule at a pose in a world; the hit: body, sub-shape id of
+// the body (a mesh triangle), penetration, contact points on the query shape and on the body, the
+// unit penetration axis (world space)
+struct DevCollideShape {
+    int shape_type;
+    float params[4];
+    float position[3];
+    float quaternion[4];
+    int world;
+};
+struct DevCollideHit {
+    int body;
+    uint32_t sub_shape_id;
+    float penetration;
+    float point_a[3], point_b[3], axis[3];
+};
+struct DevCollideSettings {
+    float max_separation, collision_tol, penetration_tol;
+    int backfaces;
+};
+// hits: nq x (mode ALL ? cap : 1); counts: hits found per query (every mode).  Mode ALL leaves each
+// query's first min(count, cap) hits sorted by body, then sub-shape id.
+void launch_collide_shapes(DevWorld &w, const DevCollideShape *qs, int nq, const DevRayFilter &f,
+                           const DevCollideSettings &cs, int mode, int cap, DevCollideHit *hits, int *counts,
+                           cudaStream_t s);
 // points: xyz and the world (int bits in w); out: hit count, lowest body hit (-1), its sub-shape id
 void launch_collide_points(DevWorld &w, const float4 *pts, int np, const DevRayFilter &f, float tol, int4 *out,
                            cudaStream_t s);

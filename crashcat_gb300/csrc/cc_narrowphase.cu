@@ -3431,18 +3431,21 @@ __device__ __forceinline__ bool ray_triangle(float3 o, float3 d, float len, floa
 
 // castRayVsTriangleMesh triangle-mesh.ts:259-430: the closest triangle below max_f of the mesh of
 // body b, the ray in the mesh's frame; nearer child first, subtrees beyond the best hit skipped
-__device__ bool ray_vs_mesh(const DevWorld &w, int b, float3 o, float3 d, float len, bool cull_back, float max_f,
-                            float &fraction, uint32_t &sub) {
+// castRayVsTriangleMesh triangle-mesh.ts:259-432 in the mesh's frame: every triangle hit below
+// the collector's early-out fraction `early` (read live: on_hit(fraction, sub-shape id) may lower
+// it) in the walk's nearer-child-first order; the walk ends once early <= 0
+template <class OnHit>
+__device__ void ray_mesh_walk(const DevWorld &w, int b, float3 o, float3 d, float len, bool cull_back,
+                              const float &early, OnHit &&on_hit) {
     const DevMesh &M = w.meshes[mesh_of(w.shape[b])];
-    if (M.num_tris == 0) return false;
+    if (M.num_tris == 0) return;
     const float4 *nodes = w.mesh_nodes + 2 * M.first_node;
     int stack[MESH_STACK];
     float sdist[MESH_STACK];
     int sp = 0;
     stack[sp] = 0;
     sdist[sp++] = -CUDART_INF_F;
-    float best = max_f;
-    bool found = false;
+    const float &best = early;
     while (sp > 0) {
         if (best <= 0.f) break;
         --sp;
@@ -3456,11 +3459,9 @@ __device__ bool ray_vs_mesh(const DevWorld &w, int b, float3 o, float3 d, float 
                 float f;
                 if (ray_triangle(o, d, len, xyz(w.mesh_verts[tr.x]), xyz(w.mesh_verts[tr.y]), xyz(w.mesh_verts[tr.z]),
                                  cull_back, f) &&
-                    f < best) {
-                    best = f;
-                    found = true;
-                    sub = M.sub_bits >= 32 ? (uint32_t)ti : ((0xffffffffu & ~((1u << M.sub_bits) - 1u)) | (uint32_t)ti);
-                }
+                    f < best)
+                    on_hit(f, M.sub_bits >= 32 ? (uint32_t)ti
+                                               : ((0xffffffffu & ~((1u << M.sub_bits) - 1u)) | (uint32_t)ti));
             }
             continue;
         }
@@ -3479,6 +3480,17 @@ __device__ bool ray_vs_mesh(const DevWorld &w, int b, float3 o, float3 d, float 
             if (rd < best) { stack[sp] = right; sdist[sp++] = rd; }
         }
     }
+}
+// the closest hit of the walk (ClosestCastRayCollector: each hit lowers the early-out fraction)
+__device__ bool ray_vs_mesh(const DevWorld &w, int b, float3 o, float3 d, float len, bool cull_back, float max_f,
+                            float &fraction, uint32_t &sub) {
+    float best = max_f;
+    bool found = false;
+    ray_mesh_walk(w, b, o, d, len, cull_back, best, [&](float f, uint32_t s) {
+        best = f;
+        found = true;
+        sub = s;
+    });
     if (found) fraction = best;
     return found;
 }
@@ -3527,15 +3539,21 @@ __device__ bool ray_vs_body(const DevWorld &w, const HullView &hv, int b, float3
 
 // broadphase.castRay / dbvt.castRay (broadphase.ts:280-298, dbvt.ts:779-865) over the world's
 // subtree of the device tree: every body whose box the segment enters and that passes the filter
-// is cast; the least fraction wins, ties to the lower body index.
+// is cast, into one of the collectors of cast-ray-vs-shape.ts:66-205:
+//   COLLECT_CLOSEST: the least fraction wins, ties to the lower body index (hits[r]);
+//   COLLECT_ANY: the first hit of the walk ends it (hits[r], counts[r] = 0 or 1);
+//   COLLECT_ALL: every hit below the initial early-out fraction, one per convex body and one per
+//     triangle of a mesh, appended to hits[r * cap ...] while room is left; counts[r] the total.
 // PASS 0 casts every body; with meshes present, PASS 1 casts the meshes alone and PASS 2 the
 // convex bodies, starting from PASS 1's hits (so the ground's hit culls what lies beyond it, and
 // each instance carries one shape family's code).
-template <int PASS>
+template <int PASS, int MODE>
 __global__ void __launch_bounds__(128) k_cast_rays(DevWorld w, const int2 *node_world, const DevRay *rays,
-                                                   const int *order, int nr, DevRayFilter flt, DevRayHit *hits) {
+                                                   const int *order, int nr, DevRayFilter flt, DevRayHit *hits,
+                                                   int cap, int *counts) {
     const int n = w.n;
     const HullView hv = hull_view(w);
+    const float INITIAL = 1.f + 1e-4f;  // INITIAL_EARLY_OUT_FRACTION cast-utils.ts:3
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nr; k += gridDim.x * blockDim.x) {
         const int r = order ? order[k] : k;
         const DevRay ry = rays[r];
@@ -3543,22 +3561,46 @@ __global__ void __launch_bounds__(128) k_cast_rays(DevWorld w, const int2 *node_
         const float3 d = f3(ry.direction[0], ry.direction[1], ry.direction[2]);
         const float len = ry.length;
         const int wr = ry.world;
-        float best = 1.f + 1e-4f;  // INITIAL_EARLY_OUT_FRACTION cast-utils.ts:3
+        float best = INITIAL;
         int hit = -1;
         uint32_t hsub = 0xffffffffu;
+        int cnt = 0;
+        DevRayHit *out = hits + (size_t)r * (MODE == COLLECT_ALL ? cap : 1);
         if (PASS == 2) {
-            const DevRayHit h0 = hits[r];
-            if (h0.body >= 0) {
-                best = h0.fraction;
-                hit = h0.body;
-                hsub = h0.sub_shape_id;
+            if (MODE == COLLECT_CLOSEST) {
+                const DevRayHit h0 = hits[r];
+                if (h0.body >= 0) {
+                    best = h0.fraction;
+                    hit = h0.body;
+                    hsub = h0.sub_shape_id;
+                }
+            } else {
+                cnt = counts[r];
+                if (MODE == COLLECT_ANY && cnt > 0) continue;  // PASS 1 found one
             }
         }
+        // ANY: the hit ends the walk (SHOULD_EARLY_OUT_FRACTION); ALL: appended while room is left
+        auto add = [&](int b, float f, uint32_t sub) {
+            if (MODE == COLLECT_ALL && cnt < cap) {
+                DevRayHit h;
+                h.body = b;
+                h.fraction = f;
+                h.sub_shape_id = sub;
+                h.pad = 0;
+                out[cnt] = h;
+            }
+            if (MODE == COLLECT_ANY) {
+                hit = b;
+                best = f;
+                hsub = sub;
+            }
+            cnt++;
+        };
         if (n > 0 && wr >= 0 && wr < w.num_worlds && len > 0.f) {
             // Nearer child first, and a subtree whose box the ray enters beyond the best hit (by more
             // than twice the GJK tolerance, 1e-3 m) is skipped: a shape lies inside its box, so no hit
             // in it can come first.  The reference casts every body whose box the segment enters; the
-            // least fraction is the same.
+            // least fraction is the same.  ANY and ALL keep the initial early-out fraction.
             int stack[CCD_STACK];
             float sdist[CCD_STACK];
             int sp = 0;
@@ -3568,6 +3610,7 @@ __global__ void __launch_bounds__(128) k_cast_rays(DevWorld w, const int2 *node_
                 sdist[sp++] = t_root;
             }
             while (sp > 0) {
+                if (MODE == COLLECT_ANY && cnt > 0) break;
                 --sp;
                 const int node = stack[sp];
                 if (sdist[sp] > best * len + 2e-3f) continue;
@@ -3599,12 +3642,28 @@ __global__ void __launch_bounds__(128) k_cast_rays(DevWorld w, const int2 *node_
                 if (!(flt.layer_mask & (1u << layer_of(fb)))) continue;
                 const uint2 gb = w.groups[b];
                 if (!((flt.groups & gb.y) != 0u && (gb.x & flt.mask) != 0u)) continue;
-                // a later-found body of lower index may still take an equal fraction
-                const float max_f = (hit >= 0 && b < hit) ? nextafterf(best, CUDART_INF_F) : best;
-                float f;
-                uint32_t sub;
                 const bool is_mesh = shape_of(fb) == SHAPE_MESH;
                 if (is_mesh ? PASS == 2 : PASS == 1) continue;
+                float f;
+                uint32_t sub;
+                if (MODE != COLLECT_CLOSEST) {
+                    if (is_mesh) {  // every triangle hit (AnyCastRayCollector / AllCastRayCollector)
+                        float3 pB;
+                        float4 qB;
+                        geom_pose(w, b, fb, pB, qB);
+                        float early = INITIAL;
+                        ray_mesh_walk(w, b, qrot_inv(qB, o - pB), qrot_inv(qB, d), len,
+                                      !(flt.flags & CC_RAY_BACKFACES), early, [&](float fh, uint32_t sh) {
+                                          add(b, fh, sh);
+                                          if (MODE == COLLECT_ANY) early = 0.f;
+                                      });
+                    } else if (ray_vs_body<false>(w, hv, b, o, d, len, flt.flags, INITIAL, f, sub)) {
+                        add(b, f, sub);
+                    }
+                    continue;
+                }
+                // a later-found body of lower index may still take an equal fraction
+                const float max_f = (hit >= 0 && b < hit) ? nextafterf(best, CUDART_INF_F) : best;
                 const bool ok = is_mesh ? ray_vs_body<true>(w, hv, b, o, d, len, flt.flags, max_f, f, sub)
                                         : ray_vs_body<false>(w, hv, b, o, d, len, flt.flags, max_f, f, sub);
                 if (!ok) continue;
@@ -3615,12 +3674,14 @@ __global__ void __launch_bounds__(128) k_cast_rays(DevWorld w, const int2 *node_
                 }
             }
         }
+        if (MODE != COLLECT_CLOSEST) counts[r] = cnt;
+        if (MODE == COLLECT_ALL) continue;
         DevRayHit h;
         h.body = hit;
         h.fraction = hit >= 0 ? best : 1.f;
         h.sub_shape_id = hsub;
         h.pad = 0;
-        hits[r] = h;
+        out[0] = h;
     }
 }
 
@@ -3801,10 +3862,13 @@ void launch_collide_points(DevWorld &w, const float4 *pts, int np, const DevRayF
 // tolerance 1e-4, back faces dropped), or for a mesh the sphere's own cast or
 // castConvexVsTriangleMesh (ccd_cast_mesh, the same default settings).
 // PASS 0 casts every body; with meshes present PASS 1 casts the meshes and PASS 2 the convex
-// bodies from PASS 1's hits, as the ray queries do.
-template <int PASS>
+// bodies from PASS 1's hits, as the ray queries do.  MODE picks the collector of
+// cast-shape-vs-shape.ts:165-226 as for the rays: the closest hit, the first hit found, or every
+// hit (one per convex body, one per mesh triangle) appended to hits[k * cap ...].
+template <int PASS, int MODE>
 __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *node_world, const DevShapeCast *qs,
-                                                     int nq, DevRayFilter flt, DevShapeCastHit *hits) {
+                                                     int nq, DevRayFilter flt, DevShapeCastHit *hits, int cap,
+                                                     int *counts) {
     const int n = w.n;
     const HullView hv = hull_view(w);
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nq; k += gridDim.x * blockDim.x) {
@@ -3817,17 +3881,27 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
         const float3 disp = f3(q.displacement[0], q.displacement[1], q.displacement[2]);
         const int wr = q.world;
         float best = 1.f + 1e-4f;  // INITIAL_EARLY_OUT_FRACTION cast-utils.ts:3
+        const float INITIAL = best;
         int hit = -1;
         float3 hn = f3(0.f, 0.f, 0.f), hp = f3(0.f, 0.f, 0.f);
+        int cnt = 0;
+        DevShapeCastHit *out = hits + (size_t)k * (MODE == COLLECT_ALL ? cap : 1);
         if (PASS == 2) {
-            const DevShapeCastHit h0 = hits[k];
-            if (h0.body >= 0) {
-                hit = h0.body;
-                best = h0.fraction;
-                hn = f3(h0.normal[0], h0.normal[1], h0.normal[2]);
-                hp = f3(h0.point[0], h0.point[1], h0.point[2]);
+            if (MODE == COLLECT_CLOSEST) {
+                const DevShapeCastHit h0 = hits[k];
+                if (h0.body >= 0) {
+                    hit = h0.body;
+                    best = h0.fraction;
+                    hn = f3(h0.normal[0], h0.normal[1], h0.normal[2]);
+                    hp = f3(h0.point[0], h0.point[1], h0.point[2]);
+                }
+            } else {
+                cnt = counts[k];
+                if (MODE == COLLECT_ANY && cnt > 0) continue;  // PASS 1 found one
             }
         }
+        // the early-out fraction of the ANY and ALL collectors: the initial one, 0 after ANY's hit
+        float early = INITIAL;
         const bool valid = shape == SHAPE_SPHERE || shape == SHAPE_BOX || shape == SHAPE_CAPSULE;
         if (valid && n > 0 && wr >= 0 && wr < w.num_worlds) {
             // the start box: the local bounds (symmetric about the origin) through |R|
@@ -3854,6 +3928,7 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
                 sdist[sp++] = t_root;
             }
             while (sp > 0) {
+                if (MODE == COLLECT_ANY && cnt > 0) break;
                 --sp;
                 const int node = stack[sp];
                 if (sdist[sp] > best * clen + 2e-2f) continue;  // beyond the best hit by twice the mesh tolerance
@@ -3885,15 +3960,33 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
                 const uint2 gb = w.groups[b];
                 if (!((flt.groups & gb.y) != 0u && (gb.x & flt.mask) != 0u)) continue;
                 auto collect = [&](float lambda, float3 paw, float3 axw) {
+                    if (MODE != COLLECT_CLOSEST) {
+                        if (!(lambda < early)) return;
+                        if (MODE == COLLECT_ANY) early = 0.f;  // SHOULD_EARLY_OUT_FRACTION
+                        if (MODE == COLLECT_ALL && cnt >= cap) {
+                            cnt++;
+                            return;
+                        }
+                        DevShapeCastHit h;
+                        h.body = b;
+                        h.fraction = lambda;
+                        const float3 nn = -normalize3(axw);
+                        h.normal[0] = nn.x, h.normal[1] = nn.y, h.normal[2] = nn.z;
+                        h.point[0] = paw.x, h.point[1] = paw.y, h.point[2] = paw.z;
+                        out[MODE == COLLECT_ALL ? cnt : 0] = h;
+                        cnt++;
+                        return;
+                    }
                     if (!(lambda < best || (lambda == best && hit >= 0 && b < hit))) return;
                     best = lambda;
                     hit = b;
                     hn = -normalize3(axw);
                     hp = paw;
                 };
+                const float &limit = MODE == COLLECT_CLOSEST ? best : early;
                 if (shape_of(fb) == SHAPE_EMPTY) continue;
                 if (shape_of(fb) == SHAPE_MESH) {
-                    if (PASS != 2) ccd_cast_mesh(w, fa, sa, pA, qA, disp, b, best, collect);
+                    if (PASS != 2) ccd_cast_mesh(w, fa, sa, pA, qA, disp, b, limit, collect);
                     continue;
                 }
                 if (shape_of(fb) == SHAPE_PLANE) {
@@ -3903,7 +3996,7 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
                     float frac;
                     geom_pose(w, b, fb, pB, qB);
                     const Sup<float> S = make_sup<float>(shape, sa, default_excludes(shape), hv);
-                    if (cast_vs_plane(S, pA, qA, disp, w.shape[b], pB, qB, best, frac, paw, axw)) collect(frac, paw, axw);
+                    if (cast_vs_plane(S, pA, qA, disp, w.shape[b], pB, qB, limit, frac, paw, axw)) collect(frac, paw, axw);
                     continue;
                 }
                 if (PASS == 1) continue;
@@ -3917,7 +4010,9 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
                 Sup<float> supA = supA0;
                 set_transform(supA, qAInB, posAInB);
                 const Sup<float> supB = make_sup<float>(shape_of(fb), w.shape[b], true, hv);
-                const float max_l = (hit >= 0 && b < hit) ? nextafterf(best, CUDART_INF_F) : best;
+                const float max_l = MODE != COLLECT_CLOSEST ? early
+                                    : (hit >= 0 && b < hit) ? nextafterf(best, CUDART_INF_F)
+                                                            : best;
                 float lambda;
                 V<float> cpa, cpb, ax;
                 if (!gjk_cast(lambda, cpa, cpb, ax, supA, supB, dInB, 1e-4f, supA.convex_radius, supB.convex_radius,
@@ -3932,34 +4027,501 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
                 collect(lambda, f3(paw.x + pB.x, paw.y + pB.y, paw.z + pB.z), f3(axw.x, axw.y, axw.z));
             }
         }
+        if (MODE != COLLECT_CLOSEST) counts[k] = cnt;
+        if (MODE == COLLECT_ALL || (MODE == COLLECT_ANY && cnt > 0)) continue;
         DevShapeCastHit h;
         h.body = hit;
         h.fraction = hit >= 0 ? best : 1.f;
         h.normal[0] = hn.x, h.normal[1] = hn.y, h.normal[2] = hn.z;
         h.point[0] = hp.x, h.point[1] = hp.y, h.point[2] = hp.z;
-        hits[k] = h;
+        out[0] = h;
     }
 }
 
-void launch_cast_shapes(DevWorld &w, const DevShapeCast *qs, int nq, const DevRayFilter &f, DevShapeCastHit *hits,
-                        cudaStream_t s) {
+// ---------------------------------------------------------------------------
+// world queries: collideShape (query.ts:286-311) with the closest, any and all-hit collectors
+// (ClosestCollideShapeCollector, AnyCollideShapeCollector, AllCollideShapeCollector,
+// collide-shape-vs-shape.ts:82-176)
+// ---------------------------------------------------------------------------
+// penetrationDepthStepEPA (penetration.ts:214-614) from a GJK simplex on one thread's polytope
+template <class SB>
+__device__ bool query_epa(EpaScratch *slot, const Simplex<float> &sx, const Sup<R> &A, const SB &B, R tol,
+                          V<R> &axis, V<R> &pa, V<R> &pb) {
+    EpaItem it;
+    it.a = it.b = 0;
+    it.size = sx.size;
+    it.pad = 0;
+    it.tri = -1;
+    for (int k = 0; k < 4; k++) {
+        SP<float> sp = sx.pts[k < sx.size ? k : 0];
+        it.y[k] = f3(sp.y.x, sp.y.y, sp.y.z);
+        it.p[k] = f3(sp.p.x, sp.p.y, sp.p.z);
+        it.q[k] = f3(sp.q.x, sp.q.y, sp.q.z);
+    }
+    Hull<BigStore> h;
+    h.st.s = slot;
+    h.start(it);
+    return epa(h, A, B, tol, axis, pa, pb);
+}
+
+// the local bounds of a query shape (box.ts:77-84, sphere, capsule.ts:84-94)
+__device__ __forceinline__ float3 query_half(int shape, float4 sa) {
+    return shape == SHAPE_SPHERE ? f3(sa.x, sa.x, sa.x)
+           : shape == SHAPE_BOX  ? f3(sa.x, sa.y, sa.z)
+                                 : f3(sa.x, sa.y + sa.x, sa.x);
+}
+
+// collideConvexVsTriangleMesh triangle-mesh.ts:1140-1386 / collideSphereVsTriangleMesh
+// :1418-1712 of the query shape A at (pA, qA) against mesh body b at (pB, qB), no movement
+// direction (active edges take the triangle normal): every triangle hit through add
+template <class Add>
+__device__ bool collide_query_mesh(const DevWorld &w, const HullView &hv, EpaScratch *slot, int shA, float4 sa,
+                                   float3 pA, float4 qA4, int b, float3 pB, float4 qB4, const DevCollideSettings &cs,
+                                   Add &&add) {
+    const DevMesh &M = w.meshes[mesh_of(w.shape[b])];
+    if (M.num_tris == 0) return true;
+    const float ms = cs.max_separation;
+    const Q<float> qA{qA4.x, qA4.y, qA4.z, qA4.w}, iqA{-qA4.x, -qA4.y, -qA4.z, qA4.w};
+    const Q<float> qM{qB4.x, qB4.y, qB4.z, qB4.w}, iqM{-qB4.x, -qB4.y, -qB4.z, qB4.w};
+    const Q<float> m2c = qmulS(iqA, qM);
+    const V<float> m2cPos = qrotS(iqA, V<float>{pB.x - pA.x, pB.y - pA.y, pB.z - pA.z});
+    const Q<float> cInM = qmulS(iqM, qA);
+    const V<float> cInMPos = qrotS(iqM, V<float>{pA.x - pB.x, pA.y - pB.y, pA.z - pB.z});
+    const bool sphere = shA == SHAPE_SPHERE;
+    float3 qlo, qhi, qcenter, blo1 = f3(0.f, 0.f, 0.f), bhi1 = f3(0.f, 0.f, 0.f);
+    if (sphere) {
+        const float er = sa.x + ms;
+        qcenter = f3(cInMPos.x, cInMPos.y, cInMPos.z);
+        qlo = qcenter - f3(er, er, er);
+        qhi = qcenter + f3(er, er, er);
+    } else {
+        const float3 hl = query_half(shA, sa);
+        blo1 = -hl - f3(ms, ms, ms);
+        bhi1 = hl + f3(ms, ms, ms);
+        qlo = f3(3.0e38f, 3.0e38f, 3.0e38f);
+        qhi = f3(-3.0e38f, -3.0e38f, -3.0e38f);
+        for (int c = 0; c < 8; c++) {
+            V<float> p{(c & 1) ? hl.x : -hl.x, (c & 2) ? hl.y : -hl.y, (c & 4) ? hl.z : -hl.z};
+            V<float> q = qrotS(cInM, p) + cInMPos;
+            qlo = f3(fminf(qlo.x, q.x), fminf(qlo.y, q.y), fminf(qlo.z, q.z));
+            qhi = f3(fmaxf(qhi.x, q.x), fmaxf(qhi.y, q.y), fmaxf(qhi.z, q.z));
+        }
+        qlo = qlo - f3(ms, ms, ms);
+        qhi = qhi + f3(ms, ms, ms);
+        qcenter = (qlo + qhi) * 0.5f;
+    }
+    Sup<float> supA;
+    if (!sphere) supA = make_sup<float>(shA, sa, true, hv);
+    int stack[MESH_STACK];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+        const int node = stack[--sp];
+        const float4 nlo = w.mesh_nodes[2 * (M.first_node + node)], nhi = w.mesh_nodes[2 * (M.first_node + node) + 1];
+        if (!node_hits_box(nlo, nhi, qlo, qhi)) continue;
+        const int aux = __float_as_int(nlo.w), tag = __float_as_int(nhi.w);
+        if (tag >= 0) {  // internal: the nearer child (centre to centre) first
+            const int left = node + 1, right = aux;
+            const float4 l0 = w.mesh_nodes[2 * (M.first_node + left)], l1 = w.mesh_nodes[2 * (M.first_node + left) + 1];
+            const float4 r0 = w.mesh_nodes[2 * (M.first_node + right)],
+                         r1 = w.mesh_nodes[2 * (M.first_node + right) + 1];
+            const float ld = lensq3(qcenter - (xyz(l0) + xyz(l1)) * 0.5f);
+            const float rd = lensq3(qcenter - (xyz(r0) + xyz(r1)) * 0.5f);
+            if (sp + 2 > MESH_STACK) {
+                atomicOr(&w.ctr->overflow, OVF_SLOTS);
+                continue;
+            }
+            stack[sp++] = ld <= rd ? right : left;
+            stack[sp++] = ld <= rd ? left : right;
+            continue;
+        }
+        for (int ti = aux; ti < aux + (-tag - 1); ti++) {
+            const int4 tr = w.mesh_tris[M.first_tri + ti];
+            const float3 m0 = xyz(w.mesh_verts[tr.x]), m1 = xyz(w.mesh_verts[tr.y]), m2 = xyz(w.mesh_verts[tr.z]);
+            const uint32_t tsub =
+                M.sub_bits >= 32 ? (uint32_t)ti : ((0xffffffffu & ~((1u << M.sub_bits) - 1u)) | (uint32_t)ti);
+            if (sphere) {  // in the mesh frame
+                const float r = sa.x;
+                const float3 c = qcenter;
+                const float3 v0 = m0 - c, v1 = m1 - c, v2 = m2 - c;
+                const float3 tn = cross3(v1 - v0, v2 - v0);
+                const bool back = dot3(tn, v0) > 0.f;
+                if (back && !cs.backfaces) continue;
+                float dsq;
+                int feature;
+                const float3 p2 = closest_on_triangle(v0, v1, v2, dsq, feature);
+                if (dsq > (r + ms) * (r + ms)) continue;
+                const float pen = r - sqrtf(dsq);
+                float3 ax = dsq > 0.f ? normalize3(p2) : f3(0.f, 1.f, 0.f);
+                const float3 p1 = ax * r;
+                const int feat_edges[8] = {0b000, 0b101, 0b011, 0b001, 0b110, 0b100, 0b010, 0b000};
+                // an inactive edge or vertex: with no movement direction the triangle normal wins
+                if (feature != 0b111 && tr.w != 0b111 && (tr.w & feat_edges[feature]) == 0) ax = back ? tn : -tn;
+                auto to_w = [&](float3 v) {
+                    V<float> q = qrotS(qM, V<float>{v.x, v.y, v.z});
+                    return f3(q.x, q.y, q.z) + pB;
+                };
+                V<float> aw = qrotS(qM, V<float>{ax.x, ax.y, ax.z});
+                if (!add(b, tsub, pen, to_w(c + p1), to_w(c + p2), normalize3(f3(aw.x, aw.y, aw.z)))) return false;
+                continue;
+            }
+            // in the query shape's frame
+            auto to_c = [&](float3 v) {
+                V<float> q = qrotS(m2c, V<float>{v.x, v.y, v.z}) + m2cPos;
+                return f3(q.x, q.y, q.z);
+            };
+            const float3 t0 = to_c(m0), t1 = to_c(m1), t2 = to_c(m2);
+            const float3 tlo = f3(fminf(t0.x, fminf(t1.x, t2.x)), fminf(t0.y, fminf(t1.y, t2.y)),
+                                  fminf(t0.z, fminf(t1.z, t2.z)));
+            const float3 thi = f3(fmaxf(t0.x, fmaxf(t1.x, t2.x)), fmaxf(t0.y, fmaxf(t1.y, t2.y)),
+                                  fmaxf(t0.z, fmaxf(t1.z, t2.z)));
+            if (!(tlo.x <= bhi1.x && thi.x >= blo1.x && tlo.y <= bhi1.y && thi.y >= blo1.y && tlo.z <= bhi1.z &&
+                  thi.z >= blo1.z))
+                continue;
+            const float3 tn = cross3(t1 - t0, t2 - t0);
+            const bool back = dot3(tn, t0) > 0.f;
+            if (back && !cs.backfaces) continue;
+            Sup<float, true, true> supT =
+                make_sup<float, true, true>(SHAPE_SPHERE, make_float4(0.f, 0.f, 0.f, 0.f), false, hv);
+            supT.kind = SUP_TRIANGLE;
+            supT.r0 = V<float>{t0.x, t0.y, t0.z};
+            supT.r1 = V<float>{t1.x, t1.y, t1.z};
+            supT.r2 = V<float>{t2.x, t2.y, t2.z};
+            supT.convex_radius = 0.f;
+            V<float> axis{-tn.x, -tn.y, -tn.z};
+            axis = lsq(axis) < 1e-10f ? V<float>{1.f, 0.f, 0.f} : axis * (1.f / sq_root(lsq(axis)));
+            const float rA = supA.convex_radius + ms;
+            Simplex<float> sx;
+            GjkOut<float> g = gjk(supA, supT, cs.collision_tol, axis, rA * rA, sx);
+            if (g.sqdist > rA * rA) continue;  // NOT_COLLIDING
+            V<float> pa, pb, pax;
+            float pen;
+            if (!(g.sqdist > 0.f)) {  // INDETERMINATE: EPA in FP64
+                const R msE = R(fminf(ms, 1.f));
+                Sup<R> A = make_sup<R>(shA, sa, false, hv);
+                A.add_r = msE;
+                Sup<R, true, true> T = make_sup<R, true, true>(SHAPE_SPHERE, make_float4(0.f, 0.f, 0.f, 0.f), false, hv);
+                T.kind = SUP_TRIANGLE;
+                T.r0 = V<R>{R(t0.x), R(t0.y), R(t0.z)};
+                T.r1 = V<R>{R(t1.x), R(t1.y), R(t1.z)};
+                T.r2 = V<R>{R(t2.x), R(t2.y), R(t2.z)};
+                T.convex_radius = R(0);
+                V<R> eax, ea, eb;
+                if (!query_epa(slot, sx, A, T, R(cs.penetration_tol), eax, ea, eb)) continue;
+                const V<R> dd = ea - eb;
+                const R al = sq_root(lsq(eax));
+                pen = (float)(sq_root(lsq(dd)) - msE);
+                if (al > R(0)) ea = ea + eax * (-(msE / al));
+                pa = V<float>{(float)ea.x, (float)ea.y, (float)ea.z};
+                pb = V<float>{(float)eb.x, (float)eb.y, (float)eb.z};
+                pax = V<float>{(float)eax.x, (float)eax.y, (float)eax.z};
+            } else {  // COLLIDING: penetrationDepthStepGJK penetration.ts:84-106
+                const float vl = sqrtf(g.sqdist);
+                pa = g.pa + g.axis * (rA / vl);
+                pb = g.pb;
+                pax = g.axis;
+                const V<float> dd = pa - pb;
+                pen = sqrtf(lsq(dd)) - ms;
+                const float al = sqrtf(lsq(pax));
+                if (al > 0.f) pa = pa + pax * (-(ms / al));
+            }
+            if (tr.w != 0b111) {  // active edges: fixNormal with no movement direction
+                const float3 fixed = fix_normal(t0, t1, t2, back ? tn : -tn, tr.w, f3(pb.x, pb.y, pb.z),
+                                                f3(pax.x, pax.y, pax.z), f3(0.f, 0.f, 0.f));
+                pax = V<float>{fixed.x, fixed.y, fixed.z};
+            }
+            const V<float> paw = qrotS(qA, pa), pbw = qrotS(qA, pb), axw = qrotS(qA, pax);
+            if (!add(b, tsub, pen, f3(paw.x, paw.y, paw.z) + pA, f3(pbw.x, pbw.y, pbw.z) + pA,
+                     normalize3(f3(axw.x, axw.y, axw.z))))
+                return false;
+        }
+    }
+    return true;
+}
+
+// collideShapeVsShape (narrowphase.ts:172-238) of the query shape A against body b: the hit(s)
+// through add(body, sub-shape id, penetration, point on A, point on B, unit axis), all world
+// space; false once add asks the walk to stop
+template <class Add>
+__device__ bool collide_query_body(const DevWorld &w, const HullView &hv, EpaScratch *slot, int shA, float4 sa,
+                                   float3 pA, float4 qA, int b, const DevCollideSettings &cs, Add &&add) {
+    const uint32_t fb = w.flags[b];
+    const int shB = shape_of(fb);
+    if (shB == SHAPE_EMPTY) return true;  // empty-shape.ts registers no collide function
+    const float ms = cs.max_separation;
+    const float4 sb = w.shape[b];
+    float3 pB;
+    float4 qB;
+    geom_pose(w, b, fb, pB, qB);
+    if (shB == SHAPE_MESH) return collide_query_mesh(w, hv, slot, shA, sa, pA, qA, b, pB, qB, cs, add);
+    if (shB == SHAPE_PLANE) {  // collideConvexVsPlane plane.ts:474-629, the plane in A's frame
+        const float3 nl = qrot_inv(qA, qrot(qB, xyz(sb)));
+        const float cl = sb.w - dot3(qrot_inv(qA, pB - pA), nl);
+        const Sup<float> S = make_sup<float>(shA, sa, default_excludes(shA), hv);
+        const V<float> spv = S.get(V<float>{-nl.x, -nl.y, -nl.z});
+        const float3 sp3 = f3(spv.x, spv.y, spv.z);
+        const float sd = dot3(nl, sp3) + cl, cr = S.convex_radius;
+        const float pen = -sd + cr;
+        if (!(pen > -ms)) return true;
+        return add(b, 0xffffffffu, pen, pA + qrot(qA, sp3 - nl * cr), pA + qrot(qA, sp3 - nl * sd), qrot(qA, -nl));
+    }
+    if (shA == SHAPE_SPHERE && shB == SHAPE_SPHERE) {  // collideSphereVsSphere sphere.ts:319-410
+        const float3 d = pB - pA;
+        const float dsq = lensq3(d), rs = sa.x + sb.x;
+        if (dsq >= rs * rs) return true;
+        const float dist = sqrtf(dsq);
+        const float3 nn = dist > 0.f ? d * (1.f / dist) : f3(0.f, 1.f, 0.f);
+        return add(b, 0xffffffffu, rs - dist, pA + nn * sa.x, pB - nn * sb.x, nn);
+    }
+    // collideConvexVsConvex convex.ts:257-346: B in A's local frame
+    const Q<float> qAq{qA.x, qA.y, qA.z, qA.w}, iA{-qA.x, -qA.y, -qA.z, qA.w};
+    const Q<float> rel = qmulS(iA, Q<float>{qB.x, qB.y, qB.z, qB.w});
+    const V<float> posBInA = qrotS(iA, V<float>{pB.x - pA.x, pB.y - pA.y, pB.z - pA.z});
+    const Sup<float> supA = make_sup<float>(shA, sa, true, hv);
+    Sup<float> supB = make_sup<float>(shB, sb, true, hv);
+    set_transform(supB, rel, posBInA);
+    V<float> axis = posBInA;
+    if (lsq(axis) <= 1e-12f) axis = {1.f, 0.f, 0.f};
+    const float rA = supA.convex_radius + ms, rB = supB.convex_radius, cr = rA + rB;
+    Simplex<float> sx;
+    const GjkOut<float> g = gjk(supA, supB, cs.collision_tol, axis, cr * cr, sx);
+    if (g.sqdist > cr * cr) return true;  // NOT_COLLIDING
+    V<float> pa, pb, ax;
+    float pen;
+    if (!(g.sqdist > 0.f)) {  // INDETERMINATE: EPA in FP64 with the separation clamped to 1 (convex.ts:448)
+        const R msE = R(fminf(ms, 1.f));
+        const Q<R> iAr{R(-qA.x), R(-qA.y), R(-qA.z), R(qA.w)};
+        Sup<R> A = make_sup<R>(shA, sa, false, hv);
+        A.add_r = msE;
+        Sup<R> B = make_sup<R>(shB, sb, false, hv);
+        set_transform(B, qmulS(iAr, Q<R>{R(qB.x), R(qB.y), R(qB.z), R(qB.w)}),
+                      qrotS(iAr, V<R>{R(pB.x) - R(pA.x), R(pB.y) - R(pA.y), R(pB.z) - R(pA.z)}));
+        V<R> eax, ea, eb;
+        if (!query_epa(slot, sx, A, B, R(cs.penetration_tol), eax, ea, eb)) return true;  // convex.ts:331
+        const V<R> dd = ea - eb;
+        const R al = sq_root(lsq(eax));
+        pen = (float)(sq_root(lsq(dd)) - msE);
+        if (al > R(0)) ea = ea + eax * (-(msE / al));
+        pa = V<float>{(float)ea.x, (float)ea.y, (float)ea.z};
+        pb = V<float>{(float)eb.x, (float)eb.y, (float)eb.z};
+        ax = V<float>{(float)eax.x, (float)eax.y, (float)eax.z};
+    } else {  // COLLIDING: penetrationDepthStepGJK penetration.ts:84-106
+        const float vl = sqrtf(g.sqdist);
+        pa = g.pa + g.axis * (rA / vl);
+        pb = g.pb + g.axis * (-(rB / vl));
+        const V<float> dd = pa - pb;
+        pen = sqrtf(lsq(dd)) - ms;
+        const float al = sqrtf(lsq(g.axis));
+        if (al > 0.f) pa = pa + g.axis * (-(ms / al));
+        ax = g.axis;
+    }
+    const V<float> paw = qrotS(qAq, pa), pbw = qrotS(qAq, pb), axw = qrotS(qAq, ax);
+    return add(b, 0xffffffffu, pen, f3(paw.x, paw.y, paw.z) + pA, f3(pbw.x, pbw.y, pbw.z) + pA,
+               normalize3(f3(axw.x, axw.y, axw.z)));
+}
+
+// broadphase.intersectAABB (broadphase.ts:300-312) of the query's box, grown by the separation
+// distance, over the world's subtree; every body that passes the filter is collided with
+// collideShapeVsShape into the collector:
+//   COLLECT_CLOSEST: the deepest penetration (ties to the lower body index, then sub-shape id);
+//   COLLECT_ANY: the first hit of the walk ends it;
+//   COLLECT_ALL: every hit appended to hits[k * cap ...] while room is left.
+// One EPA polytope per thread (the world's reference-limit EPA slots), so the grid is the slot count.
+template <int MODE>
+__global__ void __launch_bounds__(64) k_collide_shapes(DevWorld w, const int2 *node_world, const DevCollideShape *qs,
+                                                       int nq, DevRayFilter flt, DevCollideSettings cs, int cap,
+                                                       DevCollideHit *hits, int *counts) {
+    const int n = w.n;
+    const HullView hv = hull_view(w);
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    EpaScratch *slot = (EpaScratch *)w.epa_scratch + tid;
+    for (int k = tid; k < nq; k += gridDim.x * blockDim.x) {
+        const DevCollideShape q = qs[k];
+        const int shA = q.shape_type;
+        const float4 sa = make_float4(q.params[0], q.params[1], q.params[2], q.params[3]);
+        const float3 pA = f3(q.position[0], q.position[1], q.position[2]);
+        const float4 qA = make_float4(q.quaternion[0], q.quaternion[1], q.quaternion[2], q.quaternion[3]);
+        const int wr = q.world;
+        DevCollideHit best;
+        best.body = -1;
+        best.sub_shape_id = 0xffffffffu;
+        best.penetration = 0.f;
+        for (int c = 0; c < 3; c++) best.point_a[c] = best.point_b[c] = best.axis[c] = 0.f;
+        int cnt = 0;
+        DevCollideHit *out = hits + (size_t)k * (MODE == COLLECT_ALL ? cap : 1);
+        auto add = [&](int b, uint32_t sub, float pen, float3 pa, float3 pb, float3 ax) -> bool {
+            const bool take = MODE != COLLECT_CLOSEST || cnt == 0 || pen > best.penetration ||
+                              (pen == best.penetration &&
+                               (b < best.body || (b == best.body && sub < best.sub_shape_id)));
+            if (take && !(MODE == COLLECT_ALL && cnt >= cap)) {
+                DevCollideHit h;
+                h.body = b;
+                h.sub_shape_id = sub;
+                h.penetration = pen;
+                h.point_a[0] = pa.x, h.point_a[1] = pa.y, h.point_a[2] = pa.z;
+                h.point_b[0] = pb.x, h.point_b[1] = pb.y, h.point_b[2] = pb.z;
+                h.axis[0] = ax.x, h.axis[1] = ax.y, h.axis[2] = ax.z;
+                if (MODE == COLLECT_ALL)
+                    out[cnt] = h;
+                else
+                    best = h;
+            }
+            if (MODE == COLLECT_CLOSEST) {
+                cnt = 1;
+                return true;
+            }
+            cnt++;
+            return MODE == COLLECT_ALL;
+        };
+        const bool valid = shA == SHAPE_SPHERE || shA == SHAPE_BOX || shA == SHAPE_CAPSULE;
+        if (valid && n > 0 && wr >= 0 && wr < w.num_worlds) {
+            // box3.transformMat4 of the local bounds, grown by the separation (query.ts:294-298)
+            const float3 hl = query_half(shA, sa);
+            const float3 ex = qrot(qA, f3(1.f, 0.f, 0.f)), ey = qrot(qA, f3(0.f, 1.f, 0.f)),
+                         ez = qrot(qA, f3(0.f, 0.f, 1.f));
+            const float m = cs.max_separation;
+            const float3 half = f3(fabsf(ex.x) * hl.x + fabsf(ey.x) * hl.y + fabsf(ez.x) * hl.z + m,
+                                   fabsf(ex.y) * hl.x + fabsf(ey.y) * hl.y + fabsf(ez.y) * hl.z + m,
+                                   fabsf(ex.z) * hl.x + fabsf(ey.z) * hl.y + fabsf(ez.z) * hl.z + m);
+            const float3 lo = pA - half, hi = pA + half;
+            auto overlaps = [&](int node) {
+                const float4 a = w.node_lo[node], c = w.node_hi[node];
+                return a.x <= hi.x && c.x >= lo.x && a.y <= hi.y && c.y >= lo.y && a.z <= hi.z && c.z >= lo.z;
+            };
+            int stack[CCD_STACK];
+            int sp = 0;
+            if (overlaps(0)) stack[sp++] = 0;
+            bool go = true;
+            while (sp > 0 && go) {
+                const int node = stack[--sp];
+                const int2 nw = node_world[node];
+                if (wr < nw.x || wr > nw.y) continue;
+                if (node < n - 1) {
+                    const int2 ch = w.node_child[node];
+                    if (sp + 2 > CCD_STACK) {
+                        atomicOr(&w.ctr->overflow, OVF_SLOTS);
+                        continue;
+                    }
+                    if (overlaps(ch.y)) stack[sp++] = ch.y;
+                    if (overlaps(ch.x)) stack[sp++] = ch.x;
+                    continue;
+                }
+                const int b = w.order[node - (n - 1)];
+                if (w.world[b] != wr) continue;
+                const uint32_t fb = w.flags[b];
+                if (!(flt.layer_mask & (1u << layer_of(fb)))) continue;
+                const uint2 gb = w.groups[b];
+                if (!((flt.groups & gb.y) != 0u && (gb.x & flt.mask) != 0u)) continue;
+                go = collide_query_body(w, hv, slot, shA, sa, pA, qA, b, cs, add);
+            }
+        }
+        counts[k] = cnt;
+        if (MODE != COLLECT_ALL) out[0] = best;
+    }
+}
+
+// the first min(count, cap) hits of each query of an ALL collector in a fixed order (insertion sort)
+template <class H, class Less>
+__device__ void sort_hits(H *a, int m, Less less) {
+    for (int i = 1; i < m; i++) {
+        const H x = a[i];
+        int j = i - 1;
+        while (j >= 0 && less(x, a[j])) {
+            a[j + 1] = a[j];
+            j--;
+        }
+        a[j + 1] = x;
+    }
+}
+__global__ void k_sort_ray_hits(DevRayHit *hits, const int *counts, int nq, int cap) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nq) return;
+    sort_hits(hits + (size_t)k * cap, min(counts[k], cap), [](const DevRayHit &x, const DevRayHit &y) {
+        if (x.fraction != y.fraction) return x.fraction < y.fraction;
+        if (x.body != y.body) return x.body < y.body;
+        return x.sub_shape_id < y.sub_shape_id;
+    });
+}
+__global__ void k_sort_cast_hits(DevShapeCastHit *hits, const int *counts, int nq, int cap) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nq) return;
+    sort_hits(hits + (size_t)k * cap, min(counts[k], cap), [](const DevShapeCastHit &x, const DevShapeCastHit &y) {
+        if (x.fraction != y.fraction) return x.fraction < y.fraction;
+        if (x.body != y.body) return x.body < y.body;
+        if (x.point[0] != y.point[0]) return x.point[0] < y.point[0];
+        if (x.point[1] != y.point[1]) return x.point[1] < y.point[1];
+        return x.point[2] < y.point[2];
+    });
+}
+__global__ void k_sort_collide_hits(DevCollideHit *hits, const int *counts, int nq, int cap) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nq) return;
+    sort_hits(hits + (size_t)k * cap, min(counts[k], cap), [](const DevCollideHit &x, const DevCollideHit &y) {
+        if (x.body != y.body) return x.body < y.body;
+        return x.sub_shape_id < y.sub_shape_id;
+    });
+}
+
+void launch_collide_shapes(DevWorld &w, const DevCollideShape *qs, int nq, const DevRayFilter &f,
+                           const DevCollideSettings &cs, int mode, int cap, DevCollideHit *hits, int *counts,
+                           cudaStream_t s) {
     if (nq <= 0) return;
+    const int blocks = std::min(EPA_BIG_THREADS, (nq + 63) / 64 * 64) / 64;  // one EPA slot per thread
+    if (mode == COLLECT_ANY)
+        k_collide_shapes<COLLECT_ANY><<<blocks, 64, 0, s>>>(w, w.node_world, qs, nq, f, cs, 1, hits, counts);
+    else if (mode == COLLECT_ALL)
+        k_collide_shapes<COLLECT_ALL><<<blocks, 64, 0, s>>>(w, w.node_world, qs, nq, f, cs, cap, hits, counts);
+    else
+        k_collide_shapes<COLLECT_CLOSEST><<<blocks, 64, 0, s>>>(w, w.node_world, qs, nq, f, cs, 1, hits, counts);
+    if (mode == COLLECT_ALL) k_sort_collide_hits<<<(nq + 127) / 128, 128, 0, s>>>(hits, counts, nq, cap);
+}
+
+template <int MODE>
+static void cast_shapes_mode(DevWorld &w, const DevShapeCast *qs, int nq, const DevRayFilter &f, DevShapeCastHit *hits,
+                             int cap, int *counts, cudaStream_t s) {
     if (w.num_mesh_bodies > 0) {
-        k_cast_shapes<1><<<grid_for(nq, 128, 16), 128, 0, s>>>(w, w.node_world, qs, nq, f, hits);
-        k_cast_shapes<2><<<grid_for(nq, 128, 16), 128, 0, s>>>(w, w.node_world, qs, nq, f, hits);
+        k_cast_shapes<1, MODE><<<grid_for(nq, 128, 16), 128, 0, s>>>(w, w.node_world, qs, nq, f, hits, cap, counts);
+        k_cast_shapes<2, MODE><<<grid_for(nq, 128, 16), 128, 0, s>>>(w, w.node_world, qs, nq, f, hits, cap, counts);
     } else {
-        k_cast_shapes<0><<<grid_for(nq, 128, 16), 128, 0, s>>>(w, w.node_world, qs, nq, f, hits);
+        k_cast_shapes<0, MODE><<<grid_for(nq, 128, 16), 128, 0, s>>>(w, w.node_world, qs, nq, f, hits, cap, counts);
+    }
+}
+void launch_cast_shapes(DevWorld &w, const DevShapeCast *qs, int nq, const DevRayFilter &f, DevShapeCastHit *hits,
+                        cudaStream_t s, int mode, int cap, int *counts) {
+    if (nq <= 0) return;
+    if (mode == COLLECT_ANY) {
+        cast_shapes_mode<COLLECT_ANY>(w, qs, nq, f, hits, 1, counts, s);
+    } else if (mode == COLLECT_ALL) {
+        cast_shapes_mode<COLLECT_ALL>(w, qs, nq, f, hits, cap, counts, s);
+        k_sort_cast_hits<<<(nq + 127) / 128, 128, 0, s>>>(hits, counts, nq, cap);
+    } else {
+        cast_shapes_mode<COLLECT_CLOSEST>(w, qs, nq, f, hits, 1, nullptr, s);
     }
 }
 
-void launch_cast_rays(DevWorld &w, const DevRay *rays, const int *order, int nr, const DevRayFilter &f,
-                      DevRayHit *hits, cudaStream_t s) {
-    if (nr <= 0) return;
+template <int MODE>
+static void cast_rays_mode(DevWorld &w, const DevRay *rays, const int *order, int nr, const DevRayFilter &f,
+                           DevRayHit *hits, int cap, int *counts, cudaStream_t s) {
     if (w.num_mesh_bodies > 0) {
-        k_cast_rays<1><<<grid_for(nr, 128, 16), 128, 0, s>>>(w, w.node_world, rays, order, nr, f, hits);
-        k_cast_rays<2><<<grid_for(nr, 128, 16), 128, 0, s>>>(w, w.node_world, rays, order, nr, f, hits);
+        k_cast_rays<1, MODE><<<grid_for(nr, 128, 16), 128, 0, s>>>(w, w.node_world, rays, order, nr, f, hits, cap,
+                                                                  counts);
+        k_cast_rays<2, MODE><<<grid_for(nr, 128, 16), 128, 0, s>>>(w, w.node_world, rays, order, nr, f, hits, cap,
+                                                                  counts);
     } else {
-        k_cast_rays<0><<<grid_for(nr, 128, 16), 128, 0, s>>>(w, w.node_world, rays, order, nr, f, hits);
+        k_cast_rays<0, MODE><<<grid_for(nr, 128, 16), 128, 0, s>>>(w, w.node_world, rays, order, nr, f, hits, cap,
+                                                                  counts);
+    }
+}
+void launch_cast_rays(DevWorld &w, const DevRay *rays, const int *order, int nr, const DevRayFilter &f,
+                      DevRayHit *hits, cudaStream_t s, int mode, int cap, int *counts) {
+    if (nr <= 0) return;
+    if (mode == COLLECT_ANY) {
+        cast_rays_mode<COLLECT_ANY>(w, rays, order, nr, f, hits, 1, counts, s);
+    } else if (mode == COLLECT_ALL) {
+        cast_rays_mode<COLLECT_ALL>(w, rays, order, nr, f, hits, cap, counts, s);
+        k_sort_ray_hits<<<(nr + 127) / 128, 128, 0, s>>>(hits, counts, nr, cap);
+    } else {
+        cast_rays_mode<COLLECT_CLOSEST>(w, rays, order, nr, f, hits, 1, nullptr, s);
     }
 }
 

@@ -1231,7 +1231,8 @@ int cc_world_get_manifold_sub_shapes(cc_world *W, uint32_t *out, int32_t capacit
 
 static_assert(sizeof(cc_ray) == sizeof(DevRay) && sizeof(cc_ray_hit) == sizeof(DevRayHit), "ray layouts");
 
-static int queue_cast_rays(cc_world *W, const DevRay *rays, int n, const cc_query_filter *f, DevRayHit *hits) {
+static int queue_cast_rays(cc_world *W, const DevRay *rays, int n, const cc_query_filter *f, DevRayHit *hits,
+                           int mode = COLLECT_CLOSEST, int cap = 1, int *counts = nullptr) {
     if (int r = sync_shapes(W)) return r;
     DevWorld &w = W->w;
     DevRayFilter flt{f->object_layer_mask, f->collision_group, f->collision_mask, f->flags};
@@ -1249,7 +1250,7 @@ static int queue_cast_rays(cc_world *W, const DevRay *rays, int n, const cc_quer
     }
     launch_query_tree(w, W->stream);
     launch_ray_order(w, rays, n, W->q_keys, W->q_idx, W->q_tmp, W->stream);
-    launch_cast_rays(w, rays, W->q_idx, n, flt, hits, W->stream);
+    launch_cast_rays(w, rays, W->q_idx, n, flt, hits, W->stream, mode, cap, counts);
     return cuda_ok(cudaGetLastError());
 }
 
@@ -1347,6 +1348,140 @@ int cc_world_cast_rays(cc_world *W, const cc_ray *rays, int32_t count, const cc_
     if (int r = queue_cast_rays(W, W->q_rays, count, filter, W->q_hits)) return r;
     CC_TRY(cudaMemcpyAsync(hits, W->q_hits, sizeof(DevRayHit) * (size_t)count, cudaMemcpyDeviceToHost, W->stream));
     CC_TRY(cudaStreamSynchronize(W->stream));
+    return CC_OK;
+}
+
+// ---- the collectors of the batched queries ---------------------------------------
+static_assert(sizeof(cc_collide_shape) == sizeof(DevCollideShape) && sizeof(cc_collide_shape_hit) == sizeof(DevCollideHit),
+              "collide shape layouts");
+static_assert(CC_COLLECT_CLOSEST == COLLECT_CLOSEST && CC_COLLECT_ANY == COLLECT_ANY && CC_COLLECT_ALL == COLLECT_ALL,
+              "collector ids");
+
+}  // extern "C"
+
+// One query batch through the device: the inputs copied in, the kernels queued by run(d_in,
+// d_hits, d_counts, cap), the hits copied out into count x max_hits records (closest and any: the
+// first record of each query) and the counts (the closest collector's from its hit).  Mode ALL
+// returns CC_ERR_CAPACITY when a query found more than max_hits hits.
+template <typename In, typename Hit, typename Run>
+static int run_collect(cc_world *W, const In *in, int count, int mode, int max_hits, Hit *hits, int32_t *counts,
+                       Run &&run) {
+    const int cap = mode == COLLECT_ALL ? max_hits : 1;
+    const size_t in_b = sizeof(In) * (size_t)count, hit_b = sizeof(Hit) * (size_t)count * (size_t)cap,
+                 cnt_b = sizeof(int) * (size_t)count;
+    const size_t off_h = (in_b + 255) / 256 * 256, off_c = off_h + (hit_b + 255) / 256 * 256;
+    char *d = nullptr;
+    CC_TRY(cudaMallocAsync((void **)&d, off_c + cnt_b, W->stream));
+    int r = cuda_ok(cudaMemcpyAsync(d, in, in_b, cudaMemcpyHostToDevice, W->stream));
+    Hit *dh = (Hit *)(d + off_h);
+    int *dc = (int *)(d + off_c);
+    if (r == CC_OK) r = run((const In *)d, dh, mode == COLLECT_CLOSEST ? nullptr : dc, cap);
+    if (r == CC_OK) {
+        if (cap == max_hits)
+            r = cuda_ok(cudaMemcpyAsync(hits, dh, hit_b, cudaMemcpyDeviceToHost, W->stream));
+        else
+            r = cuda_ok(cudaMemcpy2DAsync(hits, sizeof(Hit) * (size_t)max_hits, dh, sizeof(Hit), sizeof(Hit), count,
+                                          cudaMemcpyDeviceToHost, W->stream));
+    }
+    if (r == CC_OK && mode != COLLECT_CLOSEST && counts)
+        r = cuda_ok(cudaMemcpyAsync(counts, dc, cnt_b, cudaMemcpyDeviceToHost, W->stream));
+    cudaFreeAsync(d, W->stream);
+    if (r == CC_OK) r = cuda_ok(cudaStreamSynchronize(W->stream));
+    if (r != CC_OK) return r;
+    if (mode == COLLECT_CLOSEST && counts)
+        for (int i = 0; i < count; i++) counts[i] = hits[(size_t)i * max_hits].body >= 0 ? 1 : 0;
+    if (mode == COLLECT_ALL)
+        for (int i = 0; i < count; i++)
+            if (counts[i] > max_hits) return CC_ERR_CAPACITY;
+    return CC_OK;
+}
+
+static bool collect_args_ok(const void *in, int32_t count, const cc_query_filter *filter, int32_t collector,
+                            int32_t max_hits, const void *hits, const int32_t *counts) {
+    if (count < 0 || !filter || collector < CC_COLLECT_CLOSEST || collector > CC_COLLECT_ALL || max_hits < 1)
+        return false;
+    if (count > 0 && (!in || !hits)) return false;
+    return !(collector == CC_COLLECT_ALL && count > 0 && !counts);
+}
+
+extern "C" {
+
+int cc_world_cast_rays_collect(cc_world *W, const cc_ray *rays, int32_t count, const cc_query_filter *filter,
+                               int32_t collector, int32_t max_hits, cc_ray_hit *hits, int32_t *counts) {
+    if (!W || !collect_args_ok(rays, count, filter, collector, max_hits, hits, counts)) return CC_ERR_INVALID;
+    if (count == 0) return CC_OK;
+    return run_collect(W, (const DevRay *)rays, count, collector, max_hits, (DevRayHit *)hits, counts,
+                       [&](const DevRay *d, DevRayHit *h, int *c, int cap) {
+                           return queue_cast_rays(W, d, count, filter, h, collector, cap, c);
+                       });
+}
+
+int cc_world_cast_shapes_collect(cc_world *W, const cc_shape_cast *casts, int32_t count, const cc_query_filter *filter,
+                                 int32_t collector, int32_t max_hits, cc_shape_cast_hit *hits, int32_t *counts) {
+    if (!W || !collect_args_ok(casts, count, filter, collector, max_hits, hits, counts)) return CC_ERR_INVALID;
+    for (int i = 0; i < count; i++) {
+        const int t = casts[i].shape_type;
+        if (t != CC_SHAPE_SPHERE && t != CC_SHAPE_BOX && t != CC_SHAPE_CAPSULE) return CC_ERR_INVALID;
+    }
+    if (count == 0) return CC_OK;
+    if (int r = sync_shapes(W)) return r;
+    DevRayFilter flt{filter->object_layer_mask, filter->collision_group, filter->collision_mask, filter->flags};
+    return run_collect(W, (const DevShapeCast *)casts, count, collector, max_hits, (DevShapeCastHit *)hits, counts,
+                       [&](const DevShapeCast *d, DevShapeCastHit *h, int *c, int cap) {
+                           launch_query_tree(W->w, W->stream);
+                           launch_cast_shapes(W->w, d, count, flt, h, W->stream, collector, cap, c);
+                           return cuda_ok(cudaGetLastError());
+                       });
+}
+
+int cc_world_collide_shapes(cc_world *W, const cc_collide_shape *shapes, int32_t count, const cc_query_filter *filter,
+                            const cc_collide_shape_settings *settings, int32_t collector, int32_t max_hits,
+                            cc_collide_shape_hit *hits, int32_t *counts) {
+    if (!W || !settings || !collect_args_ok(shapes, count, filter, collector, max_hits, hits, counts))
+        return CC_ERR_INVALID;
+    if (!(settings->max_separation_distance >= 0.f) || !(settings->collision_tolerance > 0.f) ||
+        !(settings->penetration_tolerance > 0.f))
+        return CC_ERR_INVALID;
+    for (int i = 0; i < count; i++) {
+        const int t = shapes[i].shape_type;
+        if (t != CC_SHAPE_SPHERE && t != CC_SHAPE_BOX && t != CC_SHAPE_CAPSULE) return CC_ERR_INVALID;
+    }
+    if (count == 0) return CC_OK;
+    if (!W->w.epa_scratch) return CC_ERR_UNSUPPORTED;
+    if (int r = sync_shapes(W)) return r;
+    DevRayFilter flt{filter->object_layer_mask, filter->collision_group, filter->collision_mask, filter->flags};
+    DevCollideSettings cs{settings->max_separation_distance, settings->collision_tolerance,
+                          settings->penetration_tolerance, settings->collide_with_backfaces != 0};
+    // every query reports its count, the closest collector's too
+    const int mode = collector;
+    const int cap = mode == COLLECT_ALL ? max_hits : 1;
+    const size_t in_b = sizeof(DevCollideShape) * (size_t)count,
+                 hit_b = sizeof(DevCollideHit) * (size_t)count * (size_t)cap, cnt_b = sizeof(int) * (size_t)count;
+    const size_t off_h = (in_b + 255) / 256 * 256, off_c = off_h + (hit_b + 255) / 256 * 256;
+    char *d = nullptr;
+    CC_TRY(cudaMallocAsync((void **)&d, off_c + cnt_b, W->stream));
+    DevCollideHit *dh = (DevCollideHit *)(d + off_h);
+    int *dc = (int *)(d + off_c);
+    int r = cuda_ok(cudaMemcpyAsync(d, shapes, in_b, cudaMemcpyHostToDevice, W->stream));
+    if (r == CC_OK) {
+        launch_query_tree(W->w, W->stream);
+        launch_collide_shapes(W->w, (const DevCollideShape *)d, count, flt, cs, mode, cap, dh, dc, W->stream);
+        r = cuda_ok(cudaGetLastError());
+    }
+    if (r == CC_OK) {
+        if (cap == max_hits)
+            r = cuda_ok(cudaMemcpyAsync(hits, dh, hit_b, cudaMemcpyDeviceToHost, W->stream));
+        else
+            r = cuda_ok(cudaMemcpy2DAsync(hits, sizeof(DevCollideHit) * (size_t)max_hits, dh, sizeof(DevCollideHit),
+                                          sizeof(DevCollideHit), count, cudaMemcpyDeviceToHost, W->stream));
+    }
+    if (r == CC_OK && counts) r = cuda_ok(cudaMemcpyAsync(counts, dc, cnt_b, cudaMemcpyDeviceToHost, W->stream));
+    cudaFreeAsync(d, W->stream);
+    if (r == CC_OK) r = cuda_ok(cudaStreamSynchronize(W->stream));
+    if (r != CC_OK) return r;
+    if (mode == COLLECT_ALL)
+        for (int i = 0; i < count; i++)
+            if (counts[i] > max_hits) return CC_ERR_CAPACITY;
     return CC_OK;
 }
 

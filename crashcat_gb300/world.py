@@ -463,6 +463,54 @@ class GpuWorld:
               "cc_world_cast_shapes")
         return hits
 
+    def cast_rays_collect(self, rays: np.ndarray, collector: int, max_hits: int = 1,
+                          object_layer_mask: int = 0xFFFFFFFF, collision_group: int = 0xFFFFFFFF,
+                          collision_mask: int = 0xFFFFFFFF, treat_convex_as_solid: bool = True,
+                          collide_with_backfaces: bool = False):
+        """cc_world_cast_rays_collect: (hits as a (n, max_hits) _lib.RAY_HIT_DTYPE array, counts)."""
+        rays = np.ascontiguousarray(rays, dtype=_lib.RAY_DTYPE)
+        hits = np.zeros((len(rays), max_hits), _lib.RAY_HIT_DTYPE)
+        counts = np.zeros(len(rays), np.int32)
+        flags = (_lib.CAST_RAY_TREAT_CONVEX_AS_SOLID if treat_convex_as_solid else 0) | (
+            _lib.CAST_RAY_COLLIDE_WITH_BACKFACES if collide_with_backfaces else 0)
+        f = _lib.QueryFilter(object_layer_mask, collision_group, collision_mask, flags)
+        check(self._lib.cc_world_cast_rays_collect(self.handle, rays.ctypes.data, len(rays), C.byref(f), collector,
+                                                   max_hits, hits.ctypes.data, counts.ctypes.data),
+              "cc_world_cast_rays_collect")
+        return hits, counts
+
+    def cast_shapes_collect(self, casts: np.ndarray, collector: int, max_hits: int = 1,
+                            object_layer_mask: int = 0xFFFFFFFF, collision_group: int = 0xFFFFFFFF,
+                            collision_mask: int = 0xFFFFFFFF):
+        """cc_world_cast_shapes_collect: (hits as a (n, max_hits) _lib.SHAPE_CAST_HIT_DTYPE array,
+        counts)."""
+        casts = np.ascontiguousarray(casts, dtype=_lib.SHAPE_CAST_DTYPE)
+        hits = np.zeros((len(casts), max_hits), _lib.SHAPE_CAST_HIT_DTYPE)
+        counts = np.zeros(len(casts), np.int32)
+        f = _lib.QueryFilter(object_layer_mask, collision_group, collision_mask, 0)
+        check(self._lib.cc_world_cast_shapes_collect(self.handle, casts.ctypes.data, len(casts), C.byref(f),
+                                                     collector, max_hits, hits.ctypes.data, counts.ctypes.data),
+              "cc_world_cast_shapes_collect")
+        return hits, counts
+
+    def collide_shapes(self, shapes: np.ndarray, collector: int = _lib.COLLECT_CLOSEST, max_hits: int = 1,
+                       max_separation_distance: float = 0.0, collision_tolerance: float = 1e-4,
+                       penetration_tolerance: float = 1e-4, collide_with_backfaces: bool = True,
+                       object_layer_mask: int = 0xFFFFFFFF, collision_group: int = 0xFFFFFFFF,
+                       collision_mask: int = 0xFFFFFFFF):
+        """cc_world_collide_shapes (collideShape with createDefaultCollideShapeSettings' defaults):
+        (hits as a (n, max_hits) _lib.COLLIDE_SHAPE_HIT_DTYPE array, counts)."""
+        shapes = np.ascontiguousarray(shapes, dtype=_lib.COLLIDE_SHAPE_DTYPE)
+        hits = np.zeros((len(shapes), max_hits), _lib.COLLIDE_SHAPE_HIT_DTYPE)
+        counts = np.zeros(len(shapes), np.int32)
+        f = _lib.QueryFilter(object_layer_mask, collision_group, collision_mask, 0)
+        cs = _lib.CollideShapeSettings(max_separation_distance, collision_tolerance, penetration_tolerance,
+                                       int(collide_with_backfaces))
+        check(self._lib.cc_world_collide_shapes(self.handle, shapes.ctypes.data, len(shapes), C.byref(f),
+                                                C.byref(cs), collector, max_hits, hits.ctypes.data,
+                                                counts.ctypes.data), "cc_world_collide_shapes")
+        return hits, counts
+
     def collide_points(self, points: np.ndarray, object_layer_mask: int = 0xFFFFFFFF,
                        collision_group: int = 0xFFFFFFFF, collision_mask: int = 0xFFFFFFFF,
                        collision_tolerance: float = 1e-4) -> np.ndarray:

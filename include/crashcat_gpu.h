@@ -847,6 +847,90 @@ int cc_world_collide_points_device(cc_world *world, const cc_point *points, int3
                                    const cc_query_filter *filter, float collision_tolerance, cc_point_hit *hits);
 
 /* ---------------------------------------------------------------------------
+ * Hit collectors of the batched queries: the closest hit, any hit, or all hits
+ * (ClosestCastRayCollector / AnyCastRayCollector / AllCastRayCollector,
+ * src/collision/cast-ray-vs-shape.ts:66-205; the cast-shape collectors,
+ * cast-shape-vs-shape.ts:165-226; the collide-shape collectors,
+ * collide-shape-vs-shape.ts:82-176).
+ *
+ * hits holds count x max_hits records, query i's at hits[i * max_hits]:
+ *   CC_COLLECT_CLOSEST: one record per query, as cc_world_cast_rays /
+ *     cc_world_cast_shapes write it (collide: the deepest penetration, ties to
+ *     the lower body index, then sub-shape id); counts[i] 0 or 1 (counts may be
+ *     NULL).
+ *   CC_COLLECT_ANY: one record, the first hit the device tree walk meets (the
+ *     walk and a mesh's triangle walk stop there); counts[i] 0 or 1.  Which hit
+ *     is "first" follows the device tree, not the reference's dbvt.
+ *   CC_COLLECT_ALL: every hit below the initial early-out fraction (casts) or
+ *     within the separation distance (collide): one per convex body, one per
+ *     mesh triangle.  counts[i] = the number found (required); the first
+ *     min(counts[i], max_hits) records are sorted by fraction, body index,
+ *     sub-shape id (rays), fraction, body, contact point (shape casts), or
+ *     body, sub-shape id (collide).  A query with more hits than max_hits makes
+ *     the call return CC_ERR_CAPACITY; which of its hits were kept is then
+ *     unspecified (call again with the largest count).
+ * The reference's All collectors keep hits in traversal order; these sort them.
+ * ------------------------------------------------------------------------- */
+enum cc_collector { CC_COLLECT_CLOSEST = 0, CC_COLLECT_ANY = 1, CC_COLLECT_ALL = 2 };
+
+int cc_world_cast_rays_collect(cc_world *world, const cc_ray *rays, int32_t count, const cc_query_filter *filter,
+                               int32_t collector, int32_t max_hits, cc_ray_hit *hits, int32_t *counts);
+int cc_world_cast_shapes_collect(cc_world *world, const cc_shape_cast *casts, int32_t count,
+                                 const cc_query_filter *filter, int32_t collector, int32_t max_hits,
+                                 cc_shape_cast_hit *hits, int32_t *counts);
+
+/* ---------------------------------------------------------------------------
+ * World collide queries: collideShape (src/query.ts:286-311) with a collector
+ * above.  A sphere, box or capsule (shape_params as cc_body_desc) at position
+ * and quaternion, in its world.  Every body that passes the filter (flags
+ * unused) and whose box meets the query's box (the local bounds through the
+ * rotation, grown by max_separation_distance: broadphase.intersectAABB) is
+ * collided with collideShapeVsShape (narrowphase.ts:172-238):
+ *   - a convex body: collideConvexVsConvex (src/shapes/convex.ts:257-641;
+ *     GJK, then EPA in FP64 when the cores overlap) or sphere-vs-sphere;
+ *   - a plane: collideConvexVsPlane (src/shapes/plane.ts:474-629);
+ *   - a mesh: collideConvexVsTriangleMesh / collideSphereVsTriangleMesh
+ *     (src/shapes/triangle-mesh.ts), one hit per triangle, active edges
+ *     honoured with no movement direction;
+ *   - an empty shape: nothing.
+ * The hit (CollideShapeHit collide-shape-vs-shape.ts:8-31, without faces):
+ * body index, the body's sub-shape id (a mesh triangle, else 0xffffffff),
+ * penetration (negative down to -max_separation_distance for a separated
+ * pair), the contact points on the query shape and on the body, and the unit
+ * penetration axis (the direction to move the body out), all world space.
+ * Settings as createDefaultCollideShapeSettings (:202-212) names them; its
+ * defaults: 0, 1e-4, 1e-4, back faces on.  Other query shapes or a negative
+ * separation: CC_ERR_INVALID.
+ * ------------------------------------------------------------------------- */
+typedef struct cc_collide_shape {
+    int32_t shape_type;     /* CC_SHAPE_SPHERE, CC_SHAPE_BOX or CC_SHAPE_CAPSULE */
+    float shape_params[4];
+    float position[3];
+    float quaternion[4];    /* x, y, z, w */
+    int32_t world;
+} cc_collide_shape;
+
+typedef struct cc_collide_shape_hit {
+    int32_t body;
+    uint32_t sub_shape_id;
+    float penetration;
+    float point_a[3];       /* on the query shape */
+    float point_b[3];       /* on the body */
+    float axis[3];          /* unit penetration axis */
+} cc_collide_shape_hit;
+
+typedef struct cc_collide_shape_settings {
+    float max_separation_distance;
+    float collision_tolerance;
+    float penetration_tolerance;
+    int32_t collide_with_backfaces;
+} cc_collide_shape_settings;
+
+int cc_world_collide_shapes(cc_world *world, const cc_collide_shape *shapes, int32_t count,
+                            const cc_query_filter *filter, const cc_collide_shape_settings *settings,
+                            int32_t collector, int32_t max_hits, cc_collide_shape_hit *hits, int32_t *counts);
+
+/* ---------------------------------------------------------------------------
  * Allocation-free penetration query.  It has no counterpart in the reference:
  * it is this library's narrowphase of one convex pair (FP32 GJK, then FP64 EPA
  * when the shrunk shapes overlap) offered as a batch query on caller-owned

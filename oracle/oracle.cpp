@@ -2979,6 +2979,199 @@ int orc_cast_shapes(void *wp, const double *qs, int n, uint32_t layerMask, uint3
     return 0;
 }
 
+// castRay query.ts:78-90 with the AllCastRayCollector (cast-ray-vs-shape.ts:66-94): per ray
+// (7 doubles as orc_cast_rays) every hit of every body whose AABB the segment enters and that
+// passes the filter: a convex body's one hit below INITIAL_EARLY_OUT_FRACTION, each triangle hit
+// of a mesh (back faces culled).  Sorted by fraction, body index, sub-shape id; the first cap
+// written to fractions / bodies / subs[r * cap ...], counts[r] = the number found.
+void orc_cast_rays_all(void *wp, const double *rays, int n, uint32_t layerMask, uint32_t groups, uint32_t mask,
+                       int treatConvexAsSolid, int cap, double *fractions, int *bodies, uint32_t *subs, int *counts) {
+    World &W = *(World *)wp;
+    for (auto &b : W.bodies) update_aabb(b);
+    const double initial = 1.0 + 1e-4;
+    for (int r = 0; r < n; r++) {
+        const double *ry = rays + 7 * r;
+        V3 o{ry[0], ry[1], ry[2]}, d{ry[3], ry[4], ry[5]};
+        double len = ry[6];
+        struct H {
+            double f;
+            int b;
+            uint32_t sub;
+        };
+        std::vector<H> hs;
+        for (auto &b : W.bodies) {
+            if (!((groups & b.mask) != 0 && (b.groups & mask) != 0)) continue;
+            if (!(layerMask & (1u << b.objectLayer))) continue;
+            if (!(ray_fraction_to_box(o, d, len, b.aabb) < std::numeric_limits<double>::infinity())) continue;
+            V3 gp;
+            Q4 gq;
+            geometry_pose(b.shape, b.position, b.quat, gp, gq);
+            if (b.shape.type == SHAPE_TRIANGLE_MESH) {
+                Q4 iq = qconj(gq);
+                std::vector<std::pair<double, uint32_t>> th;
+                mesh_ray_all_hits(*b.shape.mesh, rotate(iq, sub(o, gp)), rotate(iq, d), len, th);
+                for (auto &t : th) hs.push_back({t.first, b.index, t.second});
+                continue;
+            }
+            double f;
+            uint32_t sb;
+            if (cast_ray_vs_shape(b.shape, gp, gq, o, d, len, treatConvexAsSolid != 0, initial, f, sb))
+                hs.push_back({f, b.index, sb});
+        }
+        std::sort(hs.begin(), hs.end(), [](const H &x, const H &y) {
+            if (x.f != y.f) return x.f < y.f;
+            if (x.b != y.b) return x.b < y.b;
+            return x.sub < y.sub;
+        });
+        counts[r] = (int)hs.size();
+        for (int k = 0; k < (int)hs.size() && k < cap; k++) {
+            fractions[r * cap + k] = hs[k].f;
+            bodies[r * cap + k] = hs[k].b;
+            subs[r * cap + k] = hs[k].sub;
+        }
+    }
+}
+
+// castShape query.ts:196-214 with the AllCastShapeCollector (cast-shape-vs-shape.ts:165-197):
+// per query (15 doubles as orc_cast_shapes) every hit below INITIAL_EARLY_OUT_FRACTION: a convex
+// body's or a plane's one hit, each triangle hit of a mesh.  Sorted by fraction, body, contact
+// point; the first cap written as 7 doubles (fraction, normal, point) to out[(r * cap + k) * 7]
+// and bodies[r * cap + k]; counts[r] = the number found.
+int orc_cast_shapes_all(void *wp, const double *qs, int n, uint32_t layerMask, uint32_t groups, uint32_t mask,
+                        int cap, double *out, int *bodies, int *counts) {
+    World &W = *(World *)wp;
+    const double initial = 1.0 + 1e-4;
+    for (int r = 0; r < n; r++) {
+        const double *q = qs + 15 * r;
+        double row[F_COUNT] = {};
+        row[F_SHAPE] = q[0];
+        row[F_DENSITY] = 1000.0;
+        for (int k = 0; k < 4; k++) row[F_P0 + k] = q[1 + k];
+        Shape sa;
+        if (!shape_from_row(sa, row, nullptr) || sa.type == SHAPE_TRIANGLE_MESH) return -1;
+        V3 pA{q[5], q[6], q[7]}, disp{q[12], q[13], q[14]};
+        Q4 qA{q[8], q[9], q[10], q[11]};
+        struct H {
+            double f;
+            int b;
+            V3 n, p;
+        };
+        std::vector<H> hs;
+        for (auto &B : W.bodies) {
+            if (!((groups & B.mask) != 0 && (B.groups & mask) != 0)) continue;
+            if (!(layerMask & (1u << B.objectLayer))) continue;
+            V3 gpB;
+            Q4 gqB;
+            geometry_pose(B.shape, B.position, B.quat, gpB, gqB);
+            auto collect = [&](double fraction, V3 pa, V3 axis) {
+                if (fraction < initial) hs.push_back({fraction, B.index, neg(normalize(axis)), pa});
+            };
+            if (B.shape.type == SHAPE_EMPTY) continue;
+            if (B.shape.type == SHAPE_PLANE) {
+                CastHit h;
+                if (cast_convex_vs_plane(h, sa, pA, qA, disp, B.shape, gpB, gqB, initial, false))
+                    collect(h.fraction, h.pa, h.axis);
+                continue;
+            }
+            if (B.shape.type == SHAPE_TRIANGLE_MESH) {
+                auto onHit = [&](const CastMeshHit &h) { collect(h.fraction, h.pa, h.axis); };
+                auto earlyOut = [&]() { return initial; };
+                if (sa.type == SHAPE_SPHERE)
+                    cast_sphere_vs_mesh(sa, pA, disp, B.shape, gpB, gqB, onHit, earlyOut);
+                else
+                    cast_convex_vs_mesh(sa, pA, qA, disp, B.shape, gpB, gqB, onHit, earlyOut);
+                continue;
+            }
+            CastHit h;
+            if (cast_convex_vs_convex(h, sa, pA, qA, disp, B.shape, gpB, gqB, initial, false))
+                collect(h.fraction, h.pa, h.axis);
+        }
+        std::sort(hs.begin(), hs.end(), [](const H &x, const H &y) {
+            if (x.f != y.f) return x.f < y.f;
+            if (x.b != y.b) return x.b < y.b;
+            if (x.p.x != y.p.x) return x.p.x < y.p.x;
+            if (x.p.y != y.p.y) return x.p.y < y.p.y;
+            return x.p.z < y.p.z;
+        });
+        counts[r] = (int)hs.size();
+        for (int k = 0; k < (int)hs.size() && k < cap; k++) {
+            double *o = out + (size_t)(r * cap + k) * 7;
+            o[0] = hs[k].f;
+            o[1] = hs[k].n.x, o[2] = hs[k].n.y, o[3] = hs[k].n.z;
+            o[4] = hs[k].p.x, o[5] = hs[k].p.y, o[6] = hs[k].p.z;
+            bodies[r * cap + k] = hs[k].b;
+        }
+    }
+    return 0;
+}
+
+// collideShape query.ts:286-311 with the AllCollideShapeCollector (collide-shape-vs-shape.ts
+// :82-113): per query (shape type, 4 shape params, position xyz, quaternion xyzw; 12 doubles)
+// every hit of collideShapeVsShape (collide_hits, no movement direction) against every body whose
+// current AABB meets the query's box (the shape's local bounds through its pose, grown by the
+// separation: broadphase.intersectAABB) and that passes the filter.  settings: maxSeparation,
+// collisionTolerance, penetrationTolerance, collideWithBackfaces.  Sorted by body, sub-shape id;
+// the first cap written as 10 doubles (penetration, point on the query shape, point on the body,
+// unit axis) to out[(r * cap + k) * 10], bodies / subs[r * cap + k]; counts[r] = the number found.
+int orc_collide_shapes_all(void *wp, const double *qs, int n, uint32_t layerMask, uint32_t groups, uint32_t mask,
+                           const double *settings, int cap, double *out, int *bodies, uint32_t *subs, int *counts) {
+    World &W = *(World *)wp;
+    for (auto &b : W.bodies) update_aabb(b);
+    CollideSettings cs;
+    cs.maxSeparation = settings[0];
+    cs.collisionTolerance = settings[1];
+    cs.penetrationTolerance = settings[2];
+    cs.collideWithBackfaces = settings[3] != 0;
+    cs.collectFaces = false;
+    for (int r = 0; r < n; r++) {
+        const double *q = qs + 12 * r;
+        double row[F_COUNT] = {};
+        row[F_SHAPE] = q[0];
+        row[F_DENSITY] = 1000.0;
+        for (int k = 0; k < 4; k++) row[F_P0 + k] = q[1 + k];
+        Body qb;
+        if (!shape_from_row(qb.shape, row, nullptr) || qb.shape.type == SHAPE_TRIANGLE_MESH) return -1;
+        qb.position = {q[5], q[6], q[7]};
+        qb.quat = {q[8], q[9], q[10], q[11]};
+        update_aabb(qb);
+        const double m = cs.maxSeparation;
+        Box3 E{sub(qb.aabb.mn, V3{m, m, m}), add(qb.aabb.mx, V3{m, m, m})};
+        struct H {
+            int b;
+            Hit h;
+        };
+        std::vector<H> hs;
+        for (auto &B : W.bodies) {
+            if (!((groups & B.mask) != 0 && (B.groups & mask) != 0)) continue;
+            if (!(layerMask & (1u << B.objectLayer))) continue;
+            if (!box_overlap(B.aabb, E)) continue;
+            V3 gp;
+            Q4 gq;
+            geometry_pose(B.shape, B.position, B.quat, gp, gq);
+            std::vector<Hit> out1;
+            collide_hits(out1, cs, qb.shape, qb.position, qb.quat, B.shape, gp, gq, V3{0, 0, 0});
+            for (auto &h : out1) hs.push_back({B.index, h});
+        }
+        std::stable_sort(hs.begin(), hs.end(), [](const H &x, const H &y) {
+            if (x.b != y.b) return x.b < y.b;
+            return x.h.subB < y.h.subB;
+        });
+        counts[r] = (int)hs.size();
+        for (int k = 0; k < (int)hs.size() && k < cap; k++) {
+            const Hit &h = hs[k].h;
+            V3 ax = normalize(h.axis);
+            double *o = out + (size_t)(r * cap + k) * 10;
+            o[0] = h.penetration;
+            o[1] = h.pa.x, o[2] = h.pa.y, o[3] = h.pa.z;
+            o[4] = h.pb.x, o[5] = h.pb.y, o[6] = h.pb.z;
+            o[7] = ax.x, o[8] = ax.y, o[9] = ax.z;
+            bodies[r * cap + k] = hs[k].b;
+            subs[r * cap + k] = h.subB;
+        }
+    }
+    return 0;
+}
+
 // ---- unit-level entry points for the known-answer tests -------------------
 // Faces are passed as n vertices (xyz doubles).  Returns the output vertex count.
 int orc_clip_poly_vs_plane(const double *poly, int n, const double *origin, const double *normal, double *out) {

@@ -1580,6 +1580,7 @@ struct CollideSettings {
     double collisionTolerance = 1e-4;
     double penetrationTolerance = 1e-4;
     bool collectFaces = true;
+    bool collideWithBackfaces = false;  // the narrowphase's; collideShape queries default to true
 };
 
 // collideConvexVsConvex convex.ts:257-346 + collideConvexVsConvexLocal convex.ts:359-641
@@ -2140,7 +2141,7 @@ inline void collide_convex_vs_mesh(std::vector<Hit> &out, const CollideSettings 
         if (!box_overlap_incl(tb, b1)) return;
         V3 n = cross(sub(b, a), sub(c, a));
         bool backFacing = dot(n, a) > 0.0;
-        if (backFacing) return;  // collideWithBackfaces false
+        if (backFacing && !cs.collideWithBackfaces) return;
         Support tri;
         tri.kind = SUP_TRIANGLE;
         tri.ta = a;
@@ -2201,7 +2202,7 @@ inline void collide_sphere_vs_mesh(std::vector<Hit> &out, const CollideSettings 
         V3 v0 = sub(sv0, c), v1 = sub(sv1, c), v2 = sub(sv2, c);
         V3 tn = cross(sub(v1, v0), sub(v2, v0));
         bool back = dot(tn, v0) > 0;
-        if (back) return;
+        if (back && !cs.collideWithBackfaces) return;
         double dsq;
         int feature;
         V3 p2 = closest_point_on_triangle(v0, v1, v2, dsq, feature);
@@ -2611,6 +2612,40 @@ inline bool cast_ray_vs_shape(const Shape &s, V3 pos, Q4 q, V3 origin, V3 dir, d
     fraction = std::max(0.0, lambda);
     subId = EMPTY_SUB_SHAPE_ID;
     return true;
+}
+
+// castRayVsTriangleMesh triangle-mesh.ts:259-432 with the AllCastRayCollector (cast-ray-vs-shape.ts
+// :66-94): its early-out fraction stays INITIAL_EARLY_OUT_FRACTION, so every triangle hit below it
+// is added, in walk order, as (fraction, sub-shape id); back faces culled
+inline void mesh_ray_all_hits(const MeshData &M, V3 o, V3 d, double length,
+                              std::vector<std::pair<double, uint32_t>> &hits) {
+    const double early = 1.0 + 1e-4;
+    if (M.nodes.empty()) return;
+    std::vector<std::pair<int, double>> stack{{0, -std::numeric_limits<double>::infinity()}};
+    while (!stack.empty()) {
+        auto [node, dist] = stack.back();
+        stack.pop_back();
+        if (dist >= early) continue;
+        const auto &nd = M.nodes[node];
+        if (nd[7] < 0) {
+            int start = (int)nd[6], count = (int)(-nd[7]) - 1;
+            for (int t = start; t < start + count; t++) {
+                const auto &tr = M.tris[t];
+                double f;
+                if (ray_triangle(o, d, length, M.verts[tr[0]], M.verts[tr[1]], M.verts[tr[2]], true, f) && f < early)
+                    hits.push_back({f, mesh_sub_shape_id(M, t)});
+            }
+            continue;
+        }
+        int left = node + 1, right = (int)nd[6];
+        auto box = [&](int k) {
+            const auto &c = M.nodes[k];
+            return Box3{{c[0], c[1], c[2]}, {c[3], c[4], c[5]}};
+        };
+        double ldist = ray_fraction_to_box(o, d, length, box(left)), rdist = ray_fraction_to_box(o, d, length, box(right));
+        if (rdist < early) stack.push_back({right, rdist});
+        if (ldist < early) stack.push_back({left, ldist});
+    }
 }
 
 // the hit count of a ray through a mesh with every hit kept (hitCountCollector

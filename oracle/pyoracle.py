@@ -51,6 +51,10 @@ def load():
         "orc_collide_points": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double, ip, ip, vp], None),
         "orc_cast_shapes": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, dp, ip], i32),
         "orc_cast_rays": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, i32, dp, ip, vp], None),
+        "orc_cast_rays_all": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, i32, i32, dp, ip, vp, ip], None),
+        "orc_cast_shapes_all": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, i32, dp, ip, ip], i32),
+        "orc_collide_shapes_all": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, dp, i32, dp, ip, vp, ip],
+                                   i32),
         "orc_add_mesh": ([vp, i32, dp, i32, C.c_void_p, i32, dp], i32),
         "orc_get_manifold_subs": ([vp, C.c_void_p], i32),
         "orc_fix_normal": ([dp], i32),
@@ -290,6 +294,54 @@ class OracleWorld:
         if self.lib.orc_cast_shapes(self.h, dptr(q), n, layer_mask, groups, mask, dptr(out), iptr(bo)) != 0:
             raise ValueError("orc_cast_shapes: a cast shape must be a sphere, box or capsule")
         return out[:n], bo[:n]
+
+    def cast_rays_all(self, rays: np.ndarray, cap: int, layer_mask: int = 0xFFFFFFFF, groups: int = 0xFFFFFFFF,
+                      mask: int = 0xFFFFFFFF, treat_convex_as_solid: bool = True):
+        """Every hit of each ray (AllCastRayCollector), sorted by fraction, body, sub-shape id:
+        (fractions (n, cap), bodies (n, cap), sub-shape ids (n, cap), counts (n))."""
+        rays = np.ascontiguousarray(rays, dtype=np.float64).reshape(-1, 7)
+        n = rays.shape[0]
+        fr = np.zeros((max(n, 1), cap), dtype=np.float64)
+        bo = np.full((max(n, 1), cap), -1, dtype=np.int32)
+        su = np.zeros((max(n, 1), cap), dtype=np.uint32)
+        co = np.zeros(max(n, 1), dtype=np.int32)
+        self.lib.orc_cast_rays_all(self.h, dptr(rays), n, layer_mask, groups, mask, int(treat_convex_as_solid), cap,
+                                   dptr(fr), iptr(bo), su.ctypes.data, iptr(co))
+        return fr[:n], bo[:n], su[:n], co[:n]
+
+    def cast_shapes_all(self, queries: np.ndarray, cap: int, layer_mask: int = 0xFFFFFFFF,
+                        groups: int = 0xFFFFFFFF, mask: int = 0xFFFFFFFF):
+        """Every hit of each shape cast (AllCastShapeCollector), sorted by fraction, body, point:
+        ((n, cap, 7) rows of fraction, normal, point; bodies (n, cap); counts (n))."""
+        q = np.ascontiguousarray(queries, dtype=np.float64).reshape(-1, 15)
+        n = q.shape[0]
+        out = np.zeros((max(n, 1), cap, 7), dtype=np.float64)
+        bo = np.full((max(n, 1), cap), -1, dtype=np.int32)
+        co = np.zeros(max(n, 1), dtype=np.int32)
+        if self.lib.orc_cast_shapes_all(self.h, dptr(q), n, layer_mask, groups, mask, cap, dptr(out), iptr(bo),
+                                        iptr(co)) != 0:
+            raise ValueError("orc_cast_shapes_all: a cast shape must be a sphere, box or capsule")
+        return out[:n], bo[:n], co[:n]
+
+    def collide_shapes_all(self, queries: np.ndarray, cap: int, max_separation: float = 0.0,
+                           collision_tolerance: float = 1e-4, penetration_tolerance: float = 1e-4,
+                           backfaces: bool = True, layer_mask: int = 0xFFFFFFFF, groups: int = 0xFFFFFFFF,
+                           mask: int = 0xFFFFFFFF):
+        """Every hit of each collide query (shape type, 4 params, position xyz, quaternion xyzw)
+        (AllCollideShapeCollector), sorted by body, sub-shape id: ((n, cap, 10) rows of
+        penetration, point on the query shape, point on the body, unit axis; bodies (n, cap);
+        sub-shape ids (n, cap); counts (n))."""
+        q = np.ascontiguousarray(queries, dtype=np.float64).reshape(-1, 12)
+        n = q.shape[0]
+        st = np.array([max_separation, collision_tolerance, penetration_tolerance, float(backfaces)])
+        out = np.zeros((max(n, 1), cap, 10), dtype=np.float64)
+        bo = np.full((max(n, 1), cap), -1, dtype=np.int32)
+        su = np.zeros((max(n, 1), cap), dtype=np.uint32)
+        co = np.zeros(max(n, 1), dtype=np.int32)
+        if self.lib.orc_collide_shapes_all(self.h, dptr(q), n, layer_mask, groups, mask, dptr(st), cap, dptr(out),
+                                           iptr(bo), su.ctypes.data, iptr(co)) != 0:
+            raise ValueError("orc_collide_shapes_all: a query shape must be a sphere, box or capsule")
+        return out[:n], bo[:n], su[:n], co[:n]
 
     def aabbs(self) -> np.ndarray:
         o = np.zeros((self.n, 6), dtype=np.float64)
