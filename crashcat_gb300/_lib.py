@@ -105,7 +105,7 @@ POINT_HIT_DTYPE = np.dtype([("count", np.int32), ("body", np.int32), ("sub_shape
 SHAPE_CAST_DTYPE = np.dtype([("shape_type", np.int32), ("shape_params", np.float32, 4), ("position", np.float32, 3),
                              ("quaternion", np.float32, 4), ("displacement", np.float32, 3), ("world", np.int32)])
 SHAPE_CAST_HIT_DTYPE = np.dtype([("body", np.int32), ("fraction", np.float32), ("normal", np.float32, 3),
-                                 ("point", np.float32, 3)])
+                                 ("point", np.float32, 3), ("sub_shape_id", np.uint32), ("reserved", np.int32)])
 # query collectors (cc_collector) and the collide query's records
 COLLECT_CLOSEST, COLLECT_ANY, COLLECT_ALL = 0, 1, 2
 COLLIDE_SHAPE_DTYPE = np.dtype([("shape_type", np.int32), ("shape_params", np.float32, 4),

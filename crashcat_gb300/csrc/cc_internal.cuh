@@ -806,6 +806,8 @@ struct DevShapeCastHit {
     float fraction;
     float normal[3];
     float point[3];
+    uint32_t sub_shape_id;  // the mesh triangle's, else 0xffffffff
+    int pad;
 };
 void launch_cast_shapes(DevWorld &w, const DevShapeCast *qs, int nq, const DevRayFilter &f, DevShapeCastHit *hits,
                         cudaStream_t s, int mode = COLLECT_CLOSEST, int cap = 1, int *counts = nullptr);

@@ -1725,6 +1725,14 @@ struct Hull {
         st.set_point(i, p - q, p, q);
         return i;
     }
+    // an FP64 GJK simplex the polytope starts from
+    __device__ void start(const Simplex<R> &sx) {
+        pts_limit = S::PTS;
+        npts = sx.size;
+        nq = ntri = nfree = 0;
+        overflow = false;
+        for (int k = 0; k < sx.size; k++) st.set_point(k, sx.pts[k].y, sx.pts[k].p, sx.pts[k].q);
+    }
     // the GJK simplex the polytope starts from
     __device__ void start(const EpaItem &it, int limit = S::PTS) {
         pts_limit = limit < S::PTS ? limit : S::PTS;
@@ -2995,10 +3003,24 @@ __device__ bool cast_vs_plane(const Sup<float> &S, float3 pA, float4 qA, float3 
     return true;
 }
 
+// a triangle's sub-shape id (subShape.pushIndex sub-shape.ts:60-64: the index in the low bits,
+// ones above)
+__device__ __forceinline__ uint32_t tri_sub_id(const DevMesh &M, int ti) {
+    return M.sub_bits >= 32 ? (uint32_t)ti : ((0xffffffffu & ~((1u << M.sub_bits) - 1u)) | (uint32_t)ti);
+}
+
+// the convex shapes a cast or collide query may be: sphere, box, capsule, cylinder, or a convex
+// hull of the world (its index as int bits, as bodies keep it)
+__device__ __forceinline__ bool query_shape_ok(const DevWorld &w, int shape, float4 sp) {
+    if (shape == SHAPE_HULL) return (unsigned)hull_of(sp) < (unsigned)w.num_hulls;
+    return shape == SHAPE_SPHERE || shape == SHAPE_BOX || shape == SHAPE_CAPSULE || shape == SHAPE_CYLINDER;
+}
+
 // castConvexVsTriangleMesh triangle-mesh.ts:638-1019 and castSphereVsTriangleMesh :1781-2236
 // for the continuous-collision visitor (default cast settings: tolerances 0.01, support mode
 // DEFAULT, back faces culled, no movement direction, no deepest point).  collect(fraction,
-// world point on A, world penetration axis) is the collector; fps its early-out fraction.
+// world point on A, world penetration axis, the triangle's sub-shape id) is the collector; fps its
+// early-out fraction.
 template <class Collect>
 __device__ void ccd_cast_mesh(const DevWorld &w, uint32_t fa, float4 sa, float3 pA, float4 qA4, float3 disp, int b,
                               const float &fps, Collect &&collect) {
@@ -3027,8 +3049,9 @@ __device__ void ccd_cast_mesh(const DevWorld &w, uint32_t fa, float4 sa, float3 
         const float3 hi = f3(fmaxf(start.x, end.x) + r, fmaxf(start.y, end.y) + r, fmaxf(start.z, end.z) + r);
         const float3 qc = (lo + hi) * 0.5f;
         // castSphereVsTriangleMeshAddHit :1781-1868: the penetration axis is the negated contact normal
+        uint32_t tsub = 0xffffffffu;
         auto emit = [&](float fraction, float3 cp, float3 cn) {
-            collect(fraction, toW(start + cp) + pB, -normalize3(toW(cn)));
+            collect(fraction, toW(start + cp) + pB, -normalize3(toW(cn)), tsub);
         };
         int sp = 0;
         stack[sp++] = 0;
@@ -3053,6 +3076,7 @@ __device__ void ccd_cast_mesh(const DevWorld &w, uint32_t fa, float4 sa, float3 
             }
             for (int ti = aux; ti < aux + (-tag - 1); ti++) {
                 const int4 tr = w.mesh_tris[M.first_tri + ti];
+                tsub = tri_sub_id(M, ti);
                 const float3 v0 = xyz(w.mesh_verts[tr.x]) - start, v1 = xyz(w.mesh_verts[tr.y]) - start,
                              v2 = xyz(w.mesh_verts[tr.z]) - start;
                 float3 tn = cross3(v1 - v0, v2 - v0);
@@ -3184,7 +3208,7 @@ __device__ void ccd_cast_mesh(const DevWorld &w, uint32_t fa, float4 sa, float3 
             if (lambda == 0.f && -depth >= fps) continue;
             float3 axf = f3(ax.x, ax.y, ax.z);
             if (tr.w != 0b111) axf = fix_normal(a, bb, c, n, tr.w, f3(cpb.x, cpb.y, cpb.z), axf, f3(0.f, 0.f, 0.f));
-            collect(lambda, toW(f3(cpa.x, cpa.y, cpa.z)) + pB, toW(axf));
+            collect(lambda, toW(f3(cpa.x, cpa.y, cpa.z)) + pB, toW(axf), tri_sub_id(M, ti));
         }
     }
 }
@@ -3260,7 +3284,7 @@ __global__ void __launch_bounds__(128) k_ccd_find(DevWorld w, const int2 *node_w
             const float3 blo = xyz(w.aabb_lo[b]) - half_a, bhi = xyz(w.aabb_hi[b]) + half_a;
             if (!(ray_box_entry(xyz(w.pos[a]), rel, sqrtf(lensq3(rel)), blo, bhi) < CUDART_INF_F)) continue;
             // ccdCastShapeCollector.addHit update.ts:1044-1109
-            auto collect = [&](float lambda, float3 paw, float3 axw) {
+            auto collect = [&](float lambda, float3 paw, float3 axw, uint32_t = 0xffffffffu) {
                 const float3 nrm = normalize3(axw);
                 const float den = dot3(nrm, delta);
                 if (den <= max_pen) return;
@@ -3883,6 +3907,7 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
         float best = 1.f + 1e-4f;  // INITIAL_EARLY_OUT_FRACTION cast-utils.ts:3
         const float INITIAL = best;
         int hit = -1;
+        uint32_t hsub = 0xffffffffu;
         float3 hn = f3(0.f, 0.f, 0.f), hp = f3(0.f, 0.f, 0.f);
         int cnt = 0;
         DevShapeCastHit *out = hits + (size_t)k * (MODE == COLLECT_ALL ? cap : 1);
@@ -3894,6 +3919,7 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
                     best = h0.fraction;
                     hn = f3(h0.normal[0], h0.normal[1], h0.normal[2]);
                     hp = f3(h0.point[0], h0.point[1], h0.point[2]);
+                    hsub = h0.sub_shape_id;
                 }
             } else {
                 cnt = counts[k];
@@ -3902,12 +3928,12 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
         }
         // the early-out fraction of the ANY and ALL collectors: the initial one, 0 after ANY's hit
         float early = INITIAL;
-        const bool valid = shape == SHAPE_SPHERE || shape == SHAPE_BOX || shape == SHAPE_CAPSULE;
+        const bool valid = query_shape_ok(w, shape, sa);
         if (valid && n > 0 && wr >= 0 && wr < w.num_worlds) {
-            // the start box: the local bounds (symmetric about the origin) through |R|
-            const float3 hl = shape == SHAPE_SPHERE ? f3(sa.x, sa.x, sa.x)
-                              : shape == SHAPE_BOX  ? f3(sa.x, sa.y, sa.z)
-                                                    : f3(sa.x, sa.y + sa.x, sa.x);
+            // the start box: the local bounds through the pose (box3.transformMat4 query.ts:206-208)
+            float3 llo, lhi;
+            convex_local_bounds(w, fa, sa, llo, lhi);
+            const float3 hl = (lhi - llo) * 0.5f, centre = pA + qrot(qA, (lhi + llo) * 0.5f);
             const float3 ex = qrot(qA, f3(1.f, 0.f, 0.f)), ey = qrot(qA, f3(0.f, 1.f, 0.f)),
                          ez = qrot(qA, f3(0.f, 0.f, 1.f));
             const float3 half = f3(fabsf(ex.x) * hl.x + fabsf(ey.x) * hl.y + fabsf(ez.x) * hl.z,
@@ -3917,7 +3943,7 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
             const float3 cdir = clen > 0.f ? disp * (1.f / clen) : f3(0.f, 0.f, 0.f);
             const Sup<float> supA0 = make_sup<float>(shape, sa, true, hv);
             auto entry = [&](int node) {
-                return ray_box_entry(pA, cdir, clen, xyz(w.node_lo[node]) - half, xyz(w.node_hi[node]) + half);
+                return ray_box_entry(centre, cdir, clen, xyz(w.node_lo[node]) - half, xyz(w.node_hi[node]) + half);
             };
             int stack[CCD_STACK];
             float sdist[CCD_STACK];
@@ -3959,7 +3985,7 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
                 if (!(flt.layer_mask & (1u << layer_of(fb)))) continue;
                 const uint2 gb = w.groups[b];
                 if (!((flt.groups & gb.y) != 0u && (gb.x & flt.mask) != 0u)) continue;
-                auto collect = [&](float lambda, float3 paw, float3 axw) {
+                auto collect = [&](float lambda, float3 paw, float3 axw, uint32_t sub = 0xffffffffu) {
                     if (MODE != COLLECT_CLOSEST) {
                         if (!(lambda < early)) return;
                         if (MODE == COLLECT_ANY) early = 0.f;  // SHOULD_EARLY_OUT_FRACTION
@@ -3973,6 +3999,8 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
                         const float3 nn = -normalize3(axw);
                         h.normal[0] = nn.x, h.normal[1] = nn.y, h.normal[2] = nn.z;
                         h.point[0] = paw.x, h.point[1] = paw.y, h.point[2] = paw.z;
+                        h.sub_shape_id = sub;
+                        h.pad = 0;
                         out[MODE == COLLECT_ALL ? cnt : 0] = h;
                         cnt++;
                         return;
@@ -3980,6 +4008,7 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
                     if (!(lambda < best || (lambda == best && hit >= 0 && b < hit))) return;
                     best = lambda;
                     hit = b;
+                    hsub = sub;
                     hn = -normalize3(axw);
                     hp = paw;
                 };
@@ -4034,6 +4063,8 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
         h.fraction = hit >= 0 ? best : 1.f;
         h.normal[0] = hn.x, h.normal[1] = hn.y, h.normal[2] = hn.z;
         h.point[0] = hp.x, h.point[1] = hp.y, h.point[2] = hp.z;
+        h.sub_shape_id = hit >= 0 ? hsub : 0xffffffffu;
+        h.pad = 0;
         out[0] = h;
     }
 }
@@ -4043,33 +4074,19 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
 // (ClosestCollideShapeCollector, AnyCollideShapeCollector, AllCollideShapeCollector,
 // collide-shape-vs-shape.ts:82-176)
 // ---------------------------------------------------------------------------
-// penetrationDepthStepEPA (penetration.ts:214-614) from a GJK simplex on one thread's polytope
+// penetrationDepthStepEPA (penetration.ts:214-614) from an FP64 GJK simplex on one thread's
+// polytope.  A collide query runs GJK in FP64 as well (the query is no hot path), so EPA starts
+// from the simplex the FP64 restatement reaches: on a flat Minkowski difference (a box through a
+// triangle) EPA can stop on a different face when started elsewhere.
 template <class SB>
-__device__ bool query_epa(EpaScratch *slot, const Simplex<float> &sx, const Sup<R> &A, const SB &B, R tol,
+__device__ bool query_epa(EpaScratch *slot, const Simplex<R> &sx, const Sup<R> &A, const SB &B, R tol,
                           V<R> &axis, V<R> &pa, V<R> &pb) {
-    EpaItem it;
-    it.a = it.b = 0;
-    it.size = sx.size;
-    it.pad = 0;
-    it.tri = -1;
-    for (int k = 0; k < 4; k++) {
-        SP<float> sp = sx.pts[k < sx.size ? k : 0];
-        it.y[k] = f3(sp.y.x, sp.y.y, sp.y.z);
-        it.p[k] = f3(sp.p.x, sp.p.y, sp.p.z);
-        it.q[k] = f3(sp.q.x, sp.q.y, sp.q.z);
-    }
     Hull<BigStore> h;
     h.st.s = slot;
-    h.start(it);
+    h.start(sx);
     return epa(h, A, B, tol, axis, pa, pb);
 }
 
-// the local bounds of a query shape (box.ts:77-84, sphere, capsule.ts:84-94)
-__device__ __forceinline__ float3 query_half(int shape, float4 sa) {
-    return shape == SHAPE_SPHERE ? f3(sa.x, sa.x, sa.x)
-           : shape == SHAPE_BOX  ? f3(sa.x, sa.y, sa.z)
-                                 : f3(sa.x, sa.y + sa.x, sa.x);
-}
 
 // collideConvexVsTriangleMesh triangle-mesh.ts:1140-1386 / collideSphereVsTriangleMesh
 // :1418-1712 of the query shape A at (pA, qA) against mesh body b at (pB, qB), no movement
@@ -4083,8 +4100,6 @@ __device__ bool collide_query_mesh(const DevWorld &w, const HullView &hv, EpaScr
     const float ms = cs.max_separation;
     const Q<float> qA{qA4.x, qA4.y, qA4.z, qA4.w}, iqA{-qA4.x, -qA4.y, -qA4.z, qA4.w};
     const Q<float> qM{qB4.x, qB4.y, qB4.z, qB4.w}, iqM{-qB4.x, -qB4.y, -qB4.z, qB4.w};
-    const Q<float> m2c = qmulS(iqA, qM);
-    const V<float> m2cPos = qrotS(iqA, V<float>{pB.x - pA.x, pB.y - pA.y, pB.z - pA.z});
     const Q<float> cInM = qmulS(iqM, qA);
     const V<float> cInMPos = qrotS(iqM, V<float>{pA.x - pB.x, pA.y - pB.y, pA.z - pB.z});
     const bool sphere = shA == SHAPE_SPHERE;
@@ -4095,13 +4110,14 @@ __device__ bool collide_query_mesh(const DevWorld &w, const HullView &hv, EpaScr
         qlo = qcenter - f3(er, er, er);
         qhi = qcenter + f3(er, er, er);
     } else {
-        const float3 hl = query_half(shA, sa);
-        blo1 = -hl - f3(ms, ms, ms);
-        bhi1 = hl + f3(ms, ms, ms);
+        float3 llo, lhi;
+        convex_local_bounds(w, (uint32_t)shA << F_SHAPE_SHIFT, sa, llo, lhi);
+        blo1 = llo - f3(ms, ms, ms);
+        bhi1 = lhi + f3(ms, ms, ms);
         qlo = f3(3.0e38f, 3.0e38f, 3.0e38f);
         qhi = f3(-3.0e38f, -3.0e38f, -3.0e38f);
         for (int c = 0; c < 8; c++) {
-            V<float> p{(c & 1) ? hl.x : -hl.x, (c & 2) ? hl.y : -hl.y, (c & 4) ? hl.z : -hl.z};
+            V<float> p{(c & 1) ? lhi.x : llo.x, (c & 2) ? lhi.y : llo.y, (c & 4) ? lhi.z : llo.z};
             V<float> q = qrotS(cInM, p) + cInMPos;
             qlo = f3(fminf(qlo.x, q.x), fminf(qlo.y, q.y), fminf(qlo.z, q.z));
             qhi = f3(fmaxf(qhi.x, q.x), fmaxf(qhi.y, q.y), fmaxf(qhi.z, q.z));
@@ -4110,8 +4126,11 @@ __device__ bool collide_query_mesh(const DevWorld &w, const HullView &hv, EpaScr
         qhi = qhi + f3(ms, ms, ms);
         qcenter = (qlo + qhi) * 0.5f;
     }
-    Sup<float> supA;
-    if (!sphere) supA = make_sup<float>(shA, sa, true, hv);
+    Sup<R> supA;
+    if (!sphere) supA = make_sup<R>(shA, sa, true, hv);
+    const Q<R> m2cR = qmulS(Q<R>{R(-qA4.x), R(-qA4.y), R(-qA4.z), R(qA4.w)}, Q<R>{R(qB4.x), R(qB4.y), R(qB4.z), R(qB4.w)});
+    const V<R> m2cPosR = qrotS(Q<R>{R(-qA4.x), R(-qA4.y), R(-qA4.z), R(qA4.w)},
+                               V<R>{R(pB.x) - R(pA.x), R(pB.y) - R(pA.y), R(pB.z) - R(pA.z)});
     int stack[MESH_STACK];
     int sp = 0;
     stack[sp++] = 0;
@@ -4165,74 +4184,62 @@ __device__ bool collide_query_mesh(const DevWorld &w, const HullView &hv, EpaScr
                 if (!add(b, tsub, pen, to_w(c + p1), to_w(c + p2), normalize3(f3(aw.x, aw.y, aw.z)))) return false;
                 continue;
             }
-            // in the query shape's frame
-            auto to_c = [&](float3 v) {
-                V<float> q = qrotS(m2c, V<float>{v.x, v.y, v.z}) + m2cPos;
-                return f3(q.x, q.y, q.z);
-            };
-            const float3 t0 = to_c(m0), t1 = to_c(m1), t2 = to_c(m2);
-            const float3 tlo = f3(fminf(t0.x, fminf(t1.x, t2.x)), fminf(t0.y, fminf(t1.y, t2.y)),
-                                  fminf(t0.z, fminf(t1.z, t2.z)));
-            const float3 thi = f3(fmaxf(t0.x, fmaxf(t1.x, t2.x)), fmaxf(t0.y, fmaxf(t1.y, t2.y)),
-                                  fmaxf(t0.z, fmaxf(t1.z, t2.z)));
-            if (!(tlo.x <= bhi1.x && thi.x >= blo1.x && tlo.y <= bhi1.y && thi.y >= blo1.y && tlo.z <= bhi1.z &&
-                  thi.z >= blo1.z))
+            // in the query shape's frame, FP64
+            auto to_c = [&](float3 v) { return qrotS(m2cR, V<R>{R(v.x), R(v.y), R(v.z)}) + m2cPosR; };
+            const V<R> T0 = to_c(m0), T1 = to_c(m1), T2 = to_c(m2);
+            const V<R> tlo{fmin(T0.x, fmin(T1.x, T2.x)), fmin(T0.y, fmin(T1.y, T2.y)), fmin(T0.z, fmin(T1.z, T2.z))};
+            const V<R> thi{fmax(T0.x, fmax(T1.x, T2.x)), fmax(T0.y, fmax(T1.y, T2.y)), fmax(T0.z, fmax(T1.z, T2.z))};
+            if (!(tlo.x <= R(bhi1.x) && thi.x >= R(blo1.x) && tlo.y <= R(bhi1.y) && thi.y >= R(blo1.y) &&
+                  tlo.z <= R(bhi1.z) && thi.z >= R(blo1.z)))
                 continue;
-            const float3 tn = cross3(t1 - t0, t2 - t0);
-            const bool back = dot3(tn, t0) > 0.f;
+            const V<R> tn = crs(T1 - T0, T2 - T0);
+            const bool back = dot(tn, T0) > R(0);
             if (back && !cs.backfaces) continue;
-            Sup<float, true, true> supT =
-                make_sup<float, true, true>(SHAPE_SPHERE, make_float4(0.f, 0.f, 0.f, 0.f), false, hv);
+            Sup<R, true, true> supT = make_sup<R, true, true>(SHAPE_SPHERE, make_float4(0.f, 0.f, 0.f, 0.f), false, hv);
             supT.kind = SUP_TRIANGLE;
-            supT.r0 = V<float>{t0.x, t0.y, t0.z};
-            supT.r1 = V<float>{t1.x, t1.y, t1.z};
-            supT.r2 = V<float>{t2.x, t2.y, t2.z};
-            supT.convex_radius = 0.f;
-            V<float> axis{-tn.x, -tn.y, -tn.z};
-            axis = lsq(axis) < 1e-10f ? V<float>{1.f, 0.f, 0.f} : axis * (1.f / sq_root(lsq(axis)));
-            const float rA = supA.convex_radius + ms;
-            Simplex<float> sx;
-            GjkOut<float> g = gjk(supA, supT, cs.collision_tol, axis, rA * rA, sx);
+            supT.r0 = T0;
+            supT.r1 = T1;
+            supT.r2 = T2;
+            supT.convex_radius = R(0);
+            V<R> axis{-tn.x, -tn.y, -tn.z};
+            axis = lsq(axis) < R(1e-10) ? V<R>{R(1), R(0), R(0)} : axis * (R(1) / sq_root(lsq(axis)));
+            const R rA = supA.convex_radius + R(ms);
+            Simplex<R> sx;
+            GjkOut<R> g = gjk(supA, supT, R(cs.collision_tol), axis, rA * rA, sx);
             if (g.sqdist > rA * rA) continue;  // NOT_COLLIDING
-            V<float> pa, pb, pax;
-            float pen;
-            if (!(g.sqdist > 0.f)) {  // INDETERMINATE: EPA in FP64
+            V<R> pa, pb, pax;
+            R pen;
+            if (!(g.sqdist > R(0))) {  // INDETERMINATE: EPA
                 const R msE = R(fminf(ms, 1.f));
                 Sup<R> A = make_sup<R>(shA, sa, false, hv);
                 A.add_r = msE;
-                Sup<R, true, true> T = make_sup<R, true, true>(SHAPE_SPHERE, make_float4(0.f, 0.f, 0.f, 0.f), false, hv);
-                T.kind = SUP_TRIANGLE;
-                T.r0 = V<R>{R(t0.x), R(t0.y), R(t0.z)};
-                T.r1 = V<R>{R(t1.x), R(t1.y), R(t1.z)};
-                T.r2 = V<R>{R(t2.x), R(t2.y), R(t2.z)};
-                T.convex_radius = R(0);
-                V<R> eax, ea, eb;
-                if (!query_epa(slot, sx, A, T, R(cs.penetration_tol), eax, ea, eb)) continue;
-                const V<R> dd = ea - eb;
-                const R al = sq_root(lsq(eax));
-                pen = (float)(sq_root(lsq(dd)) - msE);
-                if (al > R(0)) ea = ea + eax * (-(msE / al));
-                pa = V<float>{(float)ea.x, (float)ea.y, (float)ea.z};
-                pb = V<float>{(float)eb.x, (float)eb.y, (float)eb.z};
-                pax = V<float>{(float)eax.x, (float)eax.y, (float)eax.z};
+                if (!query_epa(slot, sx, A, supT, R(cs.penetration_tol), pax, pa, pb)) continue;
+                const V<R> dd = pa - pb;
+                const R al = sq_root(lsq(pax));
+                pen = sq_root(lsq(dd)) - msE;
+                if (al > R(0)) pa = pa + pax * (-(msE / al));
             } else {  // COLLIDING: penetrationDepthStepGJK penetration.ts:84-106
-                const float vl = sqrtf(g.sqdist);
+                const R vl = sq_root(g.sqdist);
                 pa = g.pa + g.axis * (rA / vl);
                 pb = g.pb;
                 pax = g.axis;
-                const V<float> dd = pa - pb;
-                pen = sqrtf(lsq(dd)) - ms;
-                const float al = sqrtf(lsq(pax));
-                if (al > 0.f) pa = pa + pax * (-(ms / al));
+                const V<R> dd = pa - pb;
+                pen = sq_root(lsq(dd)) - R(ms);
+                const R al = sq_root(lsq(pax));
+                if (al > R(0)) pa = pa + pax * (-(R(ms) / al));
             }
             if (tr.w != 0b111) {  // active edges: fixNormal with no movement direction
-                const float3 fixed = fix_normal(t0, t1, t2, back ? tn : -tn, tr.w, f3(pb.x, pb.y, pb.z),
-                                                f3(pax.x, pax.y, pax.z), f3(0.f, 0.f, 0.f));
-                pax = V<float>{fixed.x, fixed.y, fixed.z};
+                auto f3r = [](V<R> v) { return f3((float)v.x, (float)v.y, (float)v.z); };
+                const float3 tnf = f3r(tn);
+                const float3 fixed = fix_normal(f3r(T0), f3r(T1), f3r(T2), back ? tnf : -tnf, tr.w, f3r(pb), f3r(pax),
+                                                f3(0.f, 0.f, 0.f));
+                pax = V<R>{R(fixed.x), R(fixed.y), R(fixed.z)};
             }
-            const V<float> paw = qrotS(qA, pa), pbw = qrotS(qA, pb), axw = qrotS(qA, pax);
-            if (!add(b, tsub, pen, f3(paw.x, paw.y, paw.z) + pA, f3(pbw.x, pbw.y, pbw.z) + pA,
-                     normalize3(f3(axw.x, axw.y, axw.z))))
+            const Q<R> qAr{R(qA4.x), R(qA4.y), R(qA4.z), R(qA4.w)};
+            const V<R> paw = qrotS(qAr, pa), pbw = qrotS(qAr, pb), axw = qrotS(qAr, pax);
+            if (!add(b, tsub, (float)pen, f3((float)paw.x, (float)paw.y, (float)paw.z) + pA,
+                     f3((float)pbw.x, (float)pbw.y, (float)pbw.z) + pA,
+                     normalize3(f3((float)axw.x, (float)axw.y, (float)axw.z))))
                 return false;
         }
     }
@@ -4273,51 +4280,46 @@ __device__ bool collide_query_body(const DevWorld &w, const HullView &hv, EpaScr
         const float3 nn = dist > 0.f ? d * (1.f / dist) : f3(0.f, 1.f, 0.f);
         return add(b, 0xffffffffu, rs - dist, pA + nn * sa.x, pB - nn * sb.x, nn);
     }
-    // collideConvexVsConvex convex.ts:257-346: B in A's local frame
-    const Q<float> qAq{qA.x, qA.y, qA.z, qA.w}, iA{-qA.x, -qA.y, -qA.z, qA.w};
-    const Q<float> rel = qmulS(iA, Q<float>{qB.x, qB.y, qB.z, qB.w});
-    const V<float> posBInA = qrotS(iA, V<float>{pB.x - pA.x, pB.y - pA.y, pB.z - pA.z});
-    const Sup<float> supA = make_sup<float>(shA, sa, true, hv);
-    Sup<float> supB = make_sup<float>(shB, sb, true, hv);
+    // collideConvexVsConvex convex.ts:257-346: B in A's local frame, GJK and EPA in FP64
+    const Q<R> qAr{R(qA.x), R(qA.y), R(qA.z), R(qA.w)}, iA{R(-qA.x), R(-qA.y), R(-qA.z), R(qA.w)};
+    const Q<R> rel = qmulS(iA, Q<R>{R(qB.x), R(qB.y), R(qB.z), R(qB.w)});
+    const V<R> posBInA = qrotS(iA, V<R>{R(pB.x) - R(pA.x), R(pB.y) - R(pA.y), R(pB.z) - R(pA.z)});
+    const Sup<R> supA = make_sup<R>(shA, sa, true, hv);
+    Sup<R> supB = make_sup<R>(shB, sb, true, hv);
     set_transform(supB, rel, posBInA);
-    V<float> axis = posBInA;
-    if (lsq(axis) <= 1e-12f) axis = {1.f, 0.f, 0.f};
-    const float rA = supA.convex_radius + ms, rB = supB.convex_radius, cr = rA + rB;
-    Simplex<float> sx;
-    const GjkOut<float> g = gjk(supA, supB, cs.collision_tol, axis, cr * cr, sx);
+    V<R> axis = posBInA;
+    if (lsq(axis) <= R(1e-12)) axis = {R(1), R(0), R(0)};
+    const R rA = supA.convex_radius + R(ms), rB = supB.convex_radius, cr = rA + rB;
+    Simplex<R> sx;
+    const GjkOut<R> g = gjk(supA, supB, R(cs.collision_tol), axis, cr * cr, sx);
     if (g.sqdist > cr * cr) return true;  // NOT_COLLIDING
-    V<float> pa, pb, ax;
-    float pen;
-    if (!(g.sqdist > 0.f)) {  // INDETERMINATE: EPA in FP64 with the separation clamped to 1 (convex.ts:448)
+    V<R> pa, pb, ax;
+    R pen;
+    if (!(g.sqdist > R(0))) {  // INDETERMINATE: EPA with the separation clamped to 1 (convex.ts:448)
         const R msE = R(fminf(ms, 1.f));
-        const Q<R> iAr{R(-qA.x), R(-qA.y), R(-qA.z), R(qA.w)};
         Sup<R> A = make_sup<R>(shA, sa, false, hv);
         A.add_r = msE;
         Sup<R> B = make_sup<R>(shB, sb, false, hv);
-        set_transform(B, qmulS(iAr, Q<R>{R(qB.x), R(qB.y), R(qB.z), R(qB.w)}),
-                      qrotS(iAr, V<R>{R(pB.x) - R(pA.x), R(pB.y) - R(pA.y), R(pB.z) - R(pA.z)}));
-        V<R> eax, ea, eb;
-        if (!query_epa(slot, sx, A, B, R(cs.penetration_tol), eax, ea, eb)) return true;  // convex.ts:331
-        const V<R> dd = ea - eb;
-        const R al = sq_root(lsq(eax));
-        pen = (float)(sq_root(lsq(dd)) - msE);
-        if (al > R(0)) ea = ea + eax * (-(msE / al));
-        pa = V<float>{(float)ea.x, (float)ea.y, (float)ea.z};
-        pb = V<float>{(float)eb.x, (float)eb.y, (float)eb.z};
-        ax = V<float>{(float)eax.x, (float)eax.y, (float)eax.z};
+        set_transform(B, rel, posBInA);
+        if (!query_epa(slot, sx, A, B, R(cs.penetration_tol), ax, pa, pb)) return true;  // convex.ts:331
+        const V<R> dd = pa - pb;
+        const R al = sq_root(lsq(ax));
+        pen = sq_root(lsq(dd)) - msE;
+        if (al > R(0)) pa = pa + ax * (-(msE / al));
     } else {  // COLLIDING: penetrationDepthStepGJK penetration.ts:84-106
-        const float vl = sqrtf(g.sqdist);
+        const R vl = sq_root(g.sqdist);
         pa = g.pa + g.axis * (rA / vl);
         pb = g.pb + g.axis * (-(rB / vl));
-        const V<float> dd = pa - pb;
-        pen = sqrtf(lsq(dd)) - ms;
-        const float al = sqrtf(lsq(g.axis));
-        if (al > 0.f) pa = pa + g.axis * (-(ms / al));
+        const V<R> dd = pa - pb;
+        pen = sq_root(lsq(dd)) - R(ms);
+        const R al = sq_root(lsq(g.axis));
+        if (al > R(0)) pa = pa + g.axis * (-(R(ms) / al));
         ax = g.axis;
     }
-    const V<float> paw = qrotS(qAq, pa), pbw = qrotS(qAq, pb), axw = qrotS(qAq, ax);
-    return add(b, 0xffffffffu, pen, f3(paw.x, paw.y, paw.z) + pA, f3(pbw.x, pbw.y, pbw.z) + pA,
-               normalize3(f3(axw.x, axw.y, axw.z)));
+    const V<R> paw = qrotS(qAr, pa), pbw = qrotS(qAr, pb), axw = qrotS(qAr, ax);
+    return add(b, 0xffffffffu, (float)pen, f3((float)paw.x, (float)paw.y, (float)paw.z) + pA,
+               f3((float)pbw.x, (float)pbw.y, (float)pbw.z) + pA,
+               normalize3(f3((float)axw.x, (float)axw.y, (float)axw.z)));
 }
 
 // broadphase.intersectAABB (broadphase.ts:300-312) of the query's box, grown by the separation
@@ -4373,17 +4375,19 @@ __global__ void __launch_bounds__(64) k_collide_shapes(DevWorld w, const int2 *n
             cnt++;
             return MODE == COLLECT_ALL;
         };
-        const bool valid = shA == SHAPE_SPHERE || shA == SHAPE_BOX || shA == SHAPE_CAPSULE;
+        const bool valid = query_shape_ok(w, shA, sa);
         if (valid && n > 0 && wr >= 0 && wr < w.num_worlds) {
             // box3.transformMat4 of the local bounds, grown by the separation (query.ts:294-298)
-            const float3 hl = query_half(shA, sa);
+            float3 llo, lhi;
+            convex_local_bounds(w, (uint32_t)shA << F_SHAPE_SHIFT, sa, llo, lhi);
+            const float3 hl = (lhi - llo) * 0.5f, centre = pA + qrot(qA, (lhi + llo) * 0.5f);
             const float3 ex = qrot(qA, f3(1.f, 0.f, 0.f)), ey = qrot(qA, f3(0.f, 1.f, 0.f)),
                          ez = qrot(qA, f3(0.f, 0.f, 1.f));
             const float m = cs.max_separation;
             const float3 half = f3(fabsf(ex.x) * hl.x + fabsf(ey.x) * hl.y + fabsf(ez.x) * hl.z + m,
                                    fabsf(ex.y) * hl.x + fabsf(ey.y) * hl.y + fabsf(ez.y) * hl.z + m,
                                    fabsf(ex.z) * hl.x + fabsf(ey.z) * hl.y + fabsf(ez.z) * hl.z + m);
-            const float3 lo = pA - half, hi = pA + half;
+            const float3 lo = centre - half, hi = centre + half;
             auto overlaps = [&](int node) {
                 const float4 a = w.node_lo[node], c = w.node_hi[node];
                 return a.x <= hi.x && c.x >= lo.x && a.y <= hi.y && c.y >= lo.y && a.z <= hi.z && c.z >= lo.z;
@@ -4448,9 +4452,7 @@ __global__ void k_sort_cast_hits(DevShapeCastHit *hits, const int *counts, int n
     sort_hits(hits + (size_t)k * cap, min(counts[k], cap), [](const DevShapeCastHit &x, const DevShapeCastHit &y) {
         if (x.fraction != y.fraction) return x.fraction < y.fraction;
         if (x.body != y.body) return x.body < y.body;
-        if (x.point[0] != y.point[0]) return x.point[0] < y.point[0];
-        if (x.point[1] != y.point[1]) return x.point[1] < y.point[1];
-        return x.point[2] < y.point[2];
+        return x.sub_shape_id < y.sub_shape_id;
     });
 }
 __global__ void k_sort_collide_hits(DevCollideHit *hits, const int *counts, int nq, int cap) {

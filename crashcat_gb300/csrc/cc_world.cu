@@ -1292,6 +1292,31 @@ int cc_world_collide_points(cc_world *W, const cc_point *points, int32_t count, 
 static_assert(sizeof(cc_shape_cast) == sizeof(DevShapeCast) && sizeof(cc_shape_cast_hit) == sizeof(DevShapeCastHit),
               "shape cast layouts");
 
+// A cast or collide query's shape: a sphere, box or capsule, a cylinder within cylinder.ts's
+// limits, or a convex hull of this world named by its index in shape_params[0].
+static bool query_shape_valid(const cc_world *W, int t, const float *p) {
+    if (t == CC_SHAPE_SPHERE || t == CC_SHAPE_BOX || t == CC_SHAPE_CAPSULE) return true;
+    if (t == CC_SHAPE_CYLINDER) return p[2] >= 0.f && p[0] >= p[2] && p[1] >= p[2];
+    if (t == CC_SHAPE_CONVEX_HULL) {
+        const int h = (int)p[0];
+        return p[0] == (float)h && h >= 0 && h < (int)W->hulls.size();
+    }
+    return false;
+}
+}  // extern "C"
+// the queries as the device reads them: a hull index as int bits, as the bodies' shape records keep it
+template <class Q>
+static std::vector<Q> device_queries(const Q *q, int n) {
+    std::vector<Q> out(q, q + n);
+    for (Q &x : out)
+        if (x.shape_type == CC_SHAPE_CONVEX_HULL) {
+            const int h = (int)x.shape_params[0];
+            memcpy(&x.shape_params[0], &h, sizeof(int));
+        }
+    return out;
+}
+extern "C" {
+
 int cc_world_cast_shapes_device(cc_world *W, const cc_shape_cast *casts, int32_t count, const cc_query_filter *filter,
                                 cc_shape_cast_hit *hits) {
     if (!W || count < 0 || !filter || (count > 0 && (!casts || !hits))) return CC_ERR_INVALID;
@@ -1306,15 +1331,14 @@ int cc_world_cast_shapes_device(cc_world *W, const cc_shape_cast *casts, int32_t
 int cc_world_cast_shapes(cc_world *W, const cc_shape_cast *casts, int32_t count, const cc_query_filter *filter,
                          cc_shape_cast_hit *hits) {
     if (!W || count < 0 || !filter || (count > 0 && (!casts || !hits))) return CC_ERR_INVALID;
-    for (int i = 0; i < count; i++) {
-        const int t = casts[i].shape_type;
-        if (t != CC_SHAPE_SPHERE && t != CC_SHAPE_BOX && t != CC_SHAPE_CAPSULE) return CC_ERR_INVALID;
-    }
+    for (int i = 0; i < count; i++)
+        if (!query_shape_valid(W, casts[i].shape_type, casts[i].shape_params)) return CC_ERR_INVALID;
     if (count == 0) return CC_OK;
+    const std::vector<cc_shape_cast> dq = device_queries(casts, count);
     void *d = nullptr;
     const size_t in_b = sizeof(cc_shape_cast) * (size_t)count, out_b = sizeof(cc_shape_cast_hit) * (size_t)count;
     CC_TRY(cudaMallocAsync(&d, in_b + out_b, W->stream));
-    int r = cuda_ok(cudaMemcpyAsync(d, casts, in_b, cudaMemcpyHostToDevice, W->stream));
+    int r = cuda_ok(cudaMemcpyAsync(d, dq.data(), in_b, cudaMemcpyHostToDevice, W->stream));
     cc_shape_cast_hit *dh = (cc_shape_cast_hit *)((char *)d + in_b);
     if (r == CC_OK) r = cc_world_cast_shapes_device(W, (const cc_shape_cast *)d, count, filter, dh);
     if (r == CC_OK) r = cuda_ok(cudaMemcpyAsync(hits, dh, out_b, cudaMemcpyDeviceToHost, W->stream));
@@ -1419,14 +1443,13 @@ int cc_world_cast_rays_collect(cc_world *W, const cc_ray *rays, int32_t count, c
 int cc_world_cast_shapes_collect(cc_world *W, const cc_shape_cast *casts, int32_t count, const cc_query_filter *filter,
                                  int32_t collector, int32_t max_hits, cc_shape_cast_hit *hits, int32_t *counts) {
     if (!W || !collect_args_ok(casts, count, filter, collector, max_hits, hits, counts)) return CC_ERR_INVALID;
-    for (int i = 0; i < count; i++) {
-        const int t = casts[i].shape_type;
-        if (t != CC_SHAPE_SPHERE && t != CC_SHAPE_BOX && t != CC_SHAPE_CAPSULE) return CC_ERR_INVALID;
-    }
+    for (int i = 0; i < count; i++)
+        if (!query_shape_valid(W, casts[i].shape_type, casts[i].shape_params)) return CC_ERR_INVALID;
     if (count == 0) return CC_OK;
     if (int r = sync_shapes(W)) return r;
     DevRayFilter flt{filter->object_layer_mask, filter->collision_group, filter->collision_mask, filter->flags};
-    return run_collect(W, (const DevShapeCast *)casts, count, collector, max_hits, (DevShapeCastHit *)hits, counts,
+    const std::vector<cc_shape_cast> dq = device_queries(casts, count);
+    return run_collect(W, (const DevShapeCast *)dq.data(), count, collector, max_hits, (DevShapeCastHit *)hits, counts,
                        [&](const DevShapeCast *d, DevShapeCastHit *h, int *c, int cap) {
                            launch_query_tree(W->w, W->stream);
                            launch_cast_shapes(W->w, d, count, flt, h, W->stream, collector, cap, c);
@@ -1442,12 +1465,11 @@ int cc_world_collide_shapes(cc_world *W, const cc_collide_shape *shapes, int32_t
     if (!(settings->max_separation_distance >= 0.f) || !(settings->collision_tolerance > 0.f) ||
         !(settings->penetration_tolerance > 0.f))
         return CC_ERR_INVALID;
-    for (int i = 0; i < count; i++) {
-        const int t = shapes[i].shape_type;
-        if (t != CC_SHAPE_SPHERE && t != CC_SHAPE_BOX && t != CC_SHAPE_CAPSULE) return CC_ERR_INVALID;
-    }
+    for (int i = 0; i < count; i++)
+        if (!query_shape_valid(W, shapes[i].shape_type, shapes[i].shape_params)) return CC_ERR_INVALID;
     if (count == 0) return CC_OK;
     if (!W->w.epa_scratch) return CC_ERR_UNSUPPORTED;
+    const std::vector<cc_collide_shape> dq = device_queries(shapes, count);
     if (int r = sync_shapes(W)) return r;
     DevRayFilter flt{filter->object_layer_mask, filter->collision_group, filter->collision_mask, filter->flags};
     DevCollideSettings cs{settings->max_separation_distance, settings->collision_tolerance,
@@ -1462,7 +1484,7 @@ int cc_world_collide_shapes(cc_world *W, const cc_collide_shape *shapes, int32_t
     CC_TRY(cudaMallocAsync((void **)&d, off_c + cnt_b, W->stream));
     DevCollideHit *dh = (DevCollideHit *)(d + off_h);
     int *dc = (int *)(d + off_c);
-    int r = cuda_ok(cudaMemcpyAsync(d, shapes, in_b, cudaMemcpyHostToDevice, W->stream));
+    int r = cuda_ok(cudaMemcpyAsync(d, dq.data(), in_b, cudaMemcpyHostToDevice, W->stream));
     if (r == CC_OK) {
         launch_query_tree(W->w, W->stream);
         launch_collide_shapes(W->w, (const DevCollideShape *)d, count, flt, cs, mode, cap, dh, dc, W->stream);

@@ -783,7 +783,8 @@ int cc_world_cast_rays_device(cc_world *world, const cc_ray *rays, int32_t count
  * hit.body is the body index (-1: miss), hit.fraction the fraction of the
  * displacement (1 on a miss), hit.normal the reference's hit normal (the
  * penetration axis negated and normalised), hit.point the contact point on
- * the cast shape, world space.  Equal fractions go to the lower body index.
+ * the cast shape, world space, hit.sub_shape_id the mesh triangle's sub-shape
+ * id (0xffffffff for other shapes).  Equal fractions go to the lower body index.
  * Other cast shapes: CC_ERR_INVALID.
  *   cc_world_cast_shapes: host arrays; returns when the hits are written.
  *   cc_world_cast_shapes_device: device arrays; queued on the world's stream.
@@ -802,6 +803,8 @@ typedef struct cc_shape_cast_hit {
     float fraction;
     float normal[3];
     float point[3];
+    uint32_t sub_shape_id;  /* the mesh triangle hit, else 0xffffffff */
+    int32_t reserved;
 } cc_shape_cast_hit;
 
 int cc_world_cast_shapes(cc_world *world, const cc_shape_cast *casts, int32_t count, const cc_query_filter *filter,
@@ -865,8 +868,7 @@ int cc_world_collide_points_device(cc_world *world, const cc_point *points, int3
  *     within the separation distance (collide): one per convex body, one per
  *     mesh triangle.  counts[i] = the number found (required); the first
  *     min(counts[i], max_hits) records are sorted by fraction, body index,
- *     sub-shape id (rays), fraction, body, contact point (shape casts), or
- *     body, sub-shape id (collide).  A query with more hits than max_hits makes
+ *     sub-shape id (rays and shape casts), or body, sub-shape id (collide).  A query with more hits than max_hits makes
  *     the call return CC_ERR_CAPACITY; which of its hits were kept is then
  *     unspecified (call again with the largest count).
  * The reference's All collectors keep hits in traversal order; these sort them.

@@ -2841,6 +2841,11 @@ void orc_ccd_counts(void *wp, int *out) {
     out[1] = ((World *)wp)->ccdHits;
 }
 
+// the convex shapes a cast or collide query may be (a hull names one of the world's hulls)
+static bool query_shape(int t) {
+    return t == SHAPE_SPHERE || t == SHAPE_BOX || t == SHAPE_CAPSULE || t == SHAPE_CYLINDER || t == SHAPE_CONVEX_HULL;
+}
+
 // castRay query.ts:78-90 with the closest-hit collector (cast-ray-vs-shape.ts:180-205): each ray
 // (origin xyz, direction xyz unit, length) against every body whose current AABB the segment
 // enters (dbvt.castRay dbvt.ts:779-865) and that passes the filter (object layer bit in
@@ -2918,10 +2923,11 @@ void orc_collide_points(void *wp, const double *pts, int n, uint32_t layerMask, 
 // swept box cannot be hit, so this is the set broadphase.castAABB visits, less the misses) by
 // castShapeVsShape: castConvexVsConvex convex.ts:744-830, or for a mesh the sphere's own cast or
 // castConvexVsTriangleMesh.  Out per query: fraction, normal (-penetration axis, normalised),
-// contact point on the cast shape (7 doubles); the body (-1 on a miss).  Ties go to the lower
+// contact point on the cast shape (7 doubles); the body (-1 on a miss) and its sub-shape id (a mesh
+// triangle's, else 0xffffffff; subs may be NULL).  Ties go to the lower
 // body index.
 int orc_cast_shapes(void *wp, const double *qs, int n, uint32_t layerMask, uint32_t groups, uint32_t mask,
-                    double *out, int *bodies) {
+                    double *out, int *bodies, uint32_t *subs) {
     World &W = *(World *)wp;
     for (int r = 0; r < n; r++) {
         const double *q = qs + 15 * r;
@@ -2930,11 +2936,12 @@ int orc_cast_shapes(void *wp, const double *qs, int n, uint32_t layerMask, uint3
         row[F_DENSITY] = 1000.0;
         for (int k = 0; k < 4; k++) row[F_P0 + k] = q[1 + k];
         Shape sa;
-        if (!shape_from_row(sa, row, nullptr) || sa.type == SHAPE_TRIANGLE_MESH) return -1;
+        if (!shape_from_row(sa, row, &W) || !query_shape(sa.type)) return -1;
         V3 pA{q[5], q[6], q[7]}, disp{q[12], q[13], q[14]};
         Q4 qA{q[8], q[9], q[10], q[11]};
         double best = 1.0 + 1e-4;  // INITIAL_EARLY_OUT_FRACTION cast-utils.ts:3
         int hit = -1;
+        uint32_t hsub = EMPTY_SUB_SHAPE_ID;
         V3 hn{0, 0, 0}, hp{0, 0, 0};
         for (auto &B : W.bodies) {
             if (!((groups & B.mask) != 0 && (B.groups & mask) != 0)) continue;
@@ -2942,10 +2949,11 @@ int orc_cast_shapes(void *wp, const double *qs, int n, uint32_t layerMask, uint3
             V3 gpB;
             Q4 gqB;
             geometry_pose(B.shape, B.position, B.quat, gpB, gqB);
-            auto collect = [&](double fraction, V3 pa, V3 axis) {
+            auto collect = [&](double fraction, V3 pa, V3 axis, uint32_t sub = EMPTY_SUB_SHAPE_ID) {
                 if (!(fraction < best || (fraction == best && hit >= 0 && B.index < hit))) return;
                 best = fraction;
                 hit = B.index;
+                hsub = sub;
                 hn = neg(normalize(axis));
                 hp = pa;
             };
@@ -2957,7 +2965,7 @@ int orc_cast_shapes(void *wp, const double *qs, int n, uint32_t layerMask, uint3
                 continue;
             }
             if (B.shape.type == SHAPE_TRIANGLE_MESH) {
-                auto onHit = [&](const CastMeshHit &h) { collect(h.fraction, h.pa, h.axis); };
+                auto onHit = [&](const CastMeshHit &h) { collect(h.fraction, h.pa, h.axis, h.sub); };
                 auto earlyOut = [&]() { return best; };
                 if (sa.type == SHAPE_SPHERE)
                     cast_sphere_vs_mesh(sa, pA, disp, B.shape, gpB, gqB, onHit, earlyOut);
@@ -2975,6 +2983,7 @@ int orc_cast_shapes(void *wp, const double *qs, int n, uint32_t layerMask, uint3
         o[1] = hn.x, o[2] = hn.y, o[3] = hn.z;
         o[4] = hp.x, o[5] = hp.y, o[6] = hp.z;
         bodies[r] = hit;
+        if (subs) subs[r] = hsub;
     }
     return 0;
 }
@@ -3034,11 +3043,11 @@ void orc_cast_rays_all(void *wp, const double *rays, int n, uint32_t layerMask, 
 
 // castShape query.ts:196-214 with the AllCastShapeCollector (cast-shape-vs-shape.ts:165-197):
 // per query (15 doubles as orc_cast_shapes) every hit below INITIAL_EARLY_OUT_FRACTION: a convex
-// body's or a plane's one hit, each triangle hit of a mesh.  Sorted by fraction, body, contact
-// point; the first cap written as 7 doubles (fraction, normal, point) to out[(r * cap + k) * 7]
-// and bodies[r * cap + k]; counts[r] = the number found.
+// body's or a plane's one hit, each triangle hit of a mesh.  Sorted by fraction, body, sub-shape
+// id; the first cap written as 7 doubles (fraction, normal, point) to out[(r * cap + k) * 7],
+// bodies and subs[r * cap + k]; counts[r] = the number found.
 int orc_cast_shapes_all(void *wp, const double *qs, int n, uint32_t layerMask, uint32_t groups, uint32_t mask,
-                        int cap, double *out, int *bodies, int *counts) {
+                        int cap, double *out, int *bodies, uint32_t *subs, int *counts) {
     World &W = *(World *)wp;
     const double initial = 1.0 + 1e-4;
     for (int r = 0; r < n; r++) {
@@ -3048,12 +3057,13 @@ int orc_cast_shapes_all(void *wp, const double *qs, int n, uint32_t layerMask, u
         row[F_DENSITY] = 1000.0;
         for (int k = 0; k < 4; k++) row[F_P0 + k] = q[1 + k];
         Shape sa;
-        if (!shape_from_row(sa, row, nullptr) || sa.type == SHAPE_TRIANGLE_MESH) return -1;
+        if (!shape_from_row(sa, row, &W) || !query_shape(sa.type)) return -1;
         V3 pA{q[5], q[6], q[7]}, disp{q[12], q[13], q[14]};
         Q4 qA{q[8], q[9], q[10], q[11]};
         struct H {
             double f;
             int b;
+            uint32_t sub;
             V3 n, p;
         };
         std::vector<H> hs;
@@ -3063,8 +3073,8 @@ int orc_cast_shapes_all(void *wp, const double *qs, int n, uint32_t layerMask, u
             V3 gpB;
             Q4 gqB;
             geometry_pose(B.shape, B.position, B.quat, gpB, gqB);
-            auto collect = [&](double fraction, V3 pa, V3 axis) {
-                if (fraction < initial) hs.push_back({fraction, B.index, neg(normalize(axis)), pa});
+            auto collect = [&](double fraction, V3 pa, V3 axis, uint32_t sub = EMPTY_SUB_SHAPE_ID) {
+                if (fraction < initial) hs.push_back({fraction, B.index, sub, neg(normalize(axis)), pa});
             };
             if (B.shape.type == SHAPE_EMPTY) continue;
             if (B.shape.type == SHAPE_PLANE) {
@@ -3074,7 +3084,7 @@ int orc_cast_shapes_all(void *wp, const double *qs, int n, uint32_t layerMask, u
                 continue;
             }
             if (B.shape.type == SHAPE_TRIANGLE_MESH) {
-                auto onHit = [&](const CastMeshHit &h) { collect(h.fraction, h.pa, h.axis); };
+                auto onHit = [&](const CastMeshHit &h) { collect(h.fraction, h.pa, h.axis, h.sub); };
                 auto earlyOut = [&]() { return initial; };
                 if (sa.type == SHAPE_SPHERE)
                     cast_sphere_vs_mesh(sa, pA, disp, B.shape, gpB, gqB, onHit, earlyOut);
@@ -3089,9 +3099,7 @@ int orc_cast_shapes_all(void *wp, const double *qs, int n, uint32_t layerMask, u
         std::sort(hs.begin(), hs.end(), [](const H &x, const H &y) {
             if (x.f != y.f) return x.f < y.f;
             if (x.b != y.b) return x.b < y.b;
-            if (x.p.x != y.p.x) return x.p.x < y.p.x;
-            if (x.p.y != y.p.y) return x.p.y < y.p.y;
-            return x.p.z < y.p.z;
+            return x.sub < y.sub;
         });
         counts[r] = (int)hs.size();
         for (int k = 0; k < (int)hs.size() && k < cap; k++) {
@@ -3100,6 +3108,7 @@ int orc_cast_shapes_all(void *wp, const double *qs, int n, uint32_t layerMask, u
             o[1] = hs[k].n.x, o[2] = hs[k].n.y, o[3] = hs[k].n.z;
             o[4] = hs[k].p.x, o[5] = hs[k].p.y, o[6] = hs[k].p.z;
             bodies[r * cap + k] = hs[k].b;
+            subs[r * cap + k] = hs[k].sub;
         }
     }
     return 0;
@@ -3130,7 +3139,7 @@ int orc_collide_shapes_all(void *wp, const double *qs, int n, uint32_t layerMask
         row[F_DENSITY] = 1000.0;
         for (int k = 0; k < 4; k++) row[F_P0 + k] = q[1 + k];
         Body qb;
-        if (!shape_from_row(qb.shape, row, nullptr) || qb.shape.type == SHAPE_TRIANGLE_MESH) return -1;
+        if (!shape_from_row(qb.shape, row, &W) || !query_shape(qb.shape.type)) return -1;
         qb.position = {q[5], q[6], q[7]};
         qb.quat = {q[8], q[9], q[10], q[11]};
         update_aabb(qb);

@@ -2256,6 +2256,7 @@ inline double ray_fraction_to_box(V3 o, V3 d, double length, const Box3 &b) {
 struct CastMeshHit {
     double fraction;
     V3 pa, pb, axis;
+    uint32_t sub = EMPTY_SUB_SHAPE_ID;  // the triangle's sub-shape id
 };
 
 // castConvexVsTriangleMesh triangle-mesh.ts:638-1019 with the default cast settings the
@@ -2322,7 +2323,8 @@ inline void cast_convex_vs_mesh(const Shape &sa, V3 pA, Q4 qA, V3 disp, const Sh
                 if (lambda == 0 && -depth >= earlyOut()) continue;
                 if (tr[3] != 0b111)  // fixNormal with the triangle normal as given (back faces culled)
                     ax = fix_normal(a, b, c, n, tr[3], pb, ax, V3{0, 0, 0});
-                onHit(CastMeshHit{lambda, add(rotate(qB, pa), pB), add(rotate(qB, pb), pB), rotate(qB, ax)});
+                onHit(CastMeshHit{lambda, add(rotate(qB, pa), pB), add(rotate(qB, pb), pB), rotate(qB, ax),
+                                  mesh_sub_shape_id(M, t)});
             }
             continue;
         }
@@ -2391,6 +2393,7 @@ inline void cast_sphere_vs_mesh(const Shape &sa, V3 pA, V3 disp, const Shape &sb
     Box3 sw{{std::min(start.x, end.x) - r, std::min(start.y, end.y) - r, std::min(start.z, end.z) - r},
             {std::max(start.x, end.x) + r, std::max(start.y, end.y) + r, std::max(start.z, end.z) + r}};
     V3 qc = scale(add(sw.mn, sw.mx), 0.5);
+    uint32_t cur_sub = EMPTY_SUB_SHAPE_ID;
     auto emit = [&](bool back, V3 tn, int active, double fraction, V3 ca, V3 cbp, V3 cn) {
         V3 fn = cn;
         if (active != 0b111) {  // movement direction zero: the normal kept unless the check below flips it
@@ -2400,9 +2403,10 @@ inline void cast_sphere_vs_mesh(const Shape &sa, V3 pA, V3 disp, const Shape &sb
         }
         V3 pa = add(rotate(qB, add(start, ca)), pB), pb = add(rotate(qB, add(start, cbp)), pB);
         V3 nw = normalize(rotate(qB, fn));
-        onHit(CastMeshHit{fraction, pa, pb, neg(nw)});
+        onHit(CastMeshHit{fraction, pa, pb, neg(nw), cur_sub});
     };
     mesh_walk(M, sw, qc, [&](int t) {
+        cur_sub = mesh_sub_shape_id(M, t);
         const auto &tr = M.tris[t];
         V3 rv0 = sub(M.verts[tr[0]], start), rv1 = sub(M.verts[tr[1]], start), rv2 = sub(M.verts[tr[2]], start);
         V3 tn = cross(sub(rv1, rv0), sub(rv2, rv0));

@@ -49,10 +49,10 @@ def load():
         "orc_island_count": ([vp], i32),
         "orc_ccd_counts": ([vp, ip], None),
         "orc_collide_points": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double, ip, ip, vp], None),
-        "orc_cast_shapes": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, dp, ip], i32),
+        "orc_cast_shapes": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, dp, ip, vp], i32),
         "orc_cast_rays": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, i32, dp, ip, vp], None),
         "orc_cast_rays_all": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, i32, i32, dp, ip, vp, ip], None),
-        "orc_cast_shapes_all": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, i32, dp, ip, ip], i32),
+        "orc_cast_shapes_all": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, i32, dp, ip, vp, ip], i32),
         "orc_collide_shapes_all": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, dp, i32, dp, ip, vp, ip],
                                    i32),
         "orc_add_mesh": ([vp, i32, dp, i32, C.c_void_p, i32, dp], i32),
@@ -283,17 +283,19 @@ class OracleWorld:
         return co[:n], bo[:n], su[:n]
 
     def cast_shapes(self, queries: np.ndarray, layer_mask: int = 0xFFFFFFFF, groups: int = 0xFFFFFFFF,
-                    mask: int = 0xFFFFFFFF):
+                    mask: int = 0xFFFFFFFF, with_subs: bool = False):
         """Closest hit of each shape cast (shape type, 4 params, position xyz, quaternion xyzw,
-        displacement xyz): (fraction, normal xyz, point on the cast shape xyz) rows and the
-        body hit (-1 on a miss)."""
+        displacement xyz): (fraction, normal xyz, point on the cast shape xyz) rows, the body hit
+        (-1 on a miss) and, with_subs, its sub-shape id."""
         q = np.ascontiguousarray(queries, dtype=np.float64).reshape(-1, 15)
         n = q.shape[0]
         out = np.zeros((max(n, 1), 7), dtype=np.float64)
         bo = np.zeros(max(n, 1), dtype=np.int32)
-        if self.lib.orc_cast_shapes(self.h, dptr(q), n, layer_mask, groups, mask, dptr(out), iptr(bo)) != 0:
-            raise ValueError("orc_cast_shapes: a cast shape must be a sphere, box or capsule")
-        return out[:n], bo[:n]
+        su = np.zeros(max(n, 1), dtype=np.uint32)
+        if self.lib.orc_cast_shapes(self.h, dptr(q), n, layer_mask, groups, mask, dptr(out), iptr(bo),
+                                    su.ctypes.data) != 0:
+            raise ValueError("orc_cast_shapes: a cast shape must be a sphere, box, capsule, cylinder or one of the world's hulls")
+        return (out[:n], bo[:n], su[:n]) if with_subs else (out[:n], bo[:n])
 
     def cast_rays_all(self, rays: np.ndarray, cap: int, layer_mask: int = 0xFFFFFFFF, groups: int = 0xFFFFFFFF,
                       mask: int = 0xFFFFFFFF, treat_convex_as_solid: bool = True):
@@ -311,17 +313,19 @@ class OracleWorld:
 
     def cast_shapes_all(self, queries: np.ndarray, cap: int, layer_mask: int = 0xFFFFFFFF,
                         groups: int = 0xFFFFFFFF, mask: int = 0xFFFFFFFF):
-        """Every hit of each shape cast (AllCastShapeCollector), sorted by fraction, body, point:
-        ((n, cap, 7) rows of fraction, normal, point; bodies (n, cap); counts (n))."""
+        """Every hit of each shape cast (AllCastShapeCollector), sorted by fraction, body, sub-shape
+        id: ((n, cap, 7) rows of fraction, normal, point; bodies (n, cap); sub-shape ids (n, cap);
+        counts (n))."""
         q = np.ascontiguousarray(queries, dtype=np.float64).reshape(-1, 15)
         n = q.shape[0]
         out = np.zeros((max(n, 1), cap, 7), dtype=np.float64)
         bo = np.full((max(n, 1), cap), -1, dtype=np.int32)
+        su = np.zeros((max(n, 1), cap), dtype=np.uint32)
         co = np.zeros(max(n, 1), dtype=np.int32)
         if self.lib.orc_cast_shapes_all(self.h, dptr(q), n, layer_mask, groups, mask, cap, dptr(out), iptr(bo),
-                                        iptr(co)) != 0:
-            raise ValueError("orc_cast_shapes_all: a cast shape must be a sphere, box or capsule")
-        return out[:n], bo[:n], co[:n]
+                                        su.ctypes.data, iptr(co)) != 0:
+            raise ValueError("orc_cast_shapes_all: a cast shape must be a sphere, box, capsule, cylinder or one of the world's hulls")
+        return out[:n], bo[:n], su[:n], co[:n]
 
     def collide_shapes_all(self, queries: np.ndarray, cap: int, max_separation: float = 0.0,
                            collision_tolerance: float = 1e-4, penetration_tolerance: float = 1e-4,
@@ -340,7 +344,7 @@ class OracleWorld:
         co = np.zeros(max(n, 1), dtype=np.int32)
         if self.lib.orc_collide_shapes_all(self.h, dptr(q), n, layer_mask, groups, mask, dptr(st), cap, dptr(out),
                                            iptr(bo), su.ctypes.data, iptr(co)) != 0:
-            raise ValueError("orc_collide_shapes_all: a query shape must be a sphere, box or capsule")
+            raise ValueError("orc_collide_shapes_all: a query shape must be a sphere, box, capsule, cylinder or one of the world's hulls")
         return out[:n], bo[:n], su[:n], co[:n]
 
     def aabbs(self) -> np.ndarray:

@@ -137,6 +137,27 @@ def test_oracle_collide_triangle(gpu_lib, oracle_lib, backfaces):
         assert co[0] == 1 and abs(out[0, 0, 0] - 0.05) < 1e-3, out[0, 0, 0]
 
 
+CUBE = np.array([[x, y, z] for x in (-0.5, 0.5) for y in (-0.5, 0.5) for z in (-0.5, 0.5)], np.float64)
+
+
+def test_oracle_cylinder_and_hull_queries(gpu_lib, oracle_lib):
+    """An upright cylinder (half height 0.5, radius 0.3) whose base is 0.1 m into a unit box's
+    top face, and a hull of a 1 m cube 0.2 m into it: collide 0.1 m and 0.2 m along -y.  Raised
+    by 1 m and cast 3 m straight down, they touch the face after 0.9 m and 0.8 m."""
+    hull = _lib.build_convex_hull(CUBE, 0.0)
+    o = pyoracle.OracleWorld(world.standard_settings(), static_bodies(UNIT_BOX), [hull], ())
+    rows = np.array([qrow(_lib.SHAPE_CYLINDER, (0.5, 0.3, 0.05), (0, 1.4, 0)),
+                     qrow(_lib.SHAPE_CONVEX_HULL, (0.0,), (0.3, 1.3, 0.0))])
+    out, bo, su, co = o.collide_shapes_all(rows, 4)
+    assert (co == 1).all() and (bo[:, 0] == 0).all()
+    np.testing.assert_allclose(out[:, 0, 0], [0.1, 0.2], atol=1e-3)
+    np.testing.assert_allclose(out[:, 0, 7:10], [[0, -1, 0], [0, -1, 0]], atol=1e-3)
+    casts = np.concatenate([rows + np.array([0] * 6 + [1.0] + [0] * 5), np.tile([0, -3.0, 0], (2, 1))], 1)
+    out, bo = o.cast_shapes(casts)
+    # from 0.1 m / 0.2 m into the box, raised 1 m: 0.9 m / 0.8 m of the 3 m displacement
+    np.testing.assert_allclose(out[:, 0], [0.9 / 3, 0.8 / 3], atol=2e-3)
+
+
 def line_of_spheres():
     return static_bodies([("sphere", (0.5,), (9.0, 0.0, 0.0)), ("sphere", (0.5,), (3.0, 0.0, 0.0)),
                           ("sphere", (0.5,), (6.0, 0.0, 0.0))])
@@ -157,8 +178,8 @@ def test_oracle_all_ray_hits(oracle_lib):
 def test_oracle_all_shape_cast_hits(oracle_lib):
     o = oracle_of(line_of_spheres())
     q = np.array([[SPH, 0.25, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 20, 0, 0]], np.float64)
-    out, bo, co = o.cast_shapes_all(q, 8)
-    assert co[0] == 3 and list(bo[0, :3]) == [1, 2, 0]
+    out, bo, su, co = o.cast_shapes_all(q, 8)
+    assert co[0] == 3 and list(bo[0, :3]) == [1, 2, 0] and (su[0, :3] == 0xFFFFFFFF).all()
     np.testing.assert_allclose(out[0, :3, 0], [2.25 / 20, 5.25 / 20, 8.25 / 20], atol=1e-3)
 
 
@@ -222,6 +243,20 @@ def random_shapes(rng, n, y_range):
     params[kinds == 1, 0:3] = rng.uniform(0.2, 0.6, ((kinds == 1).sum(), 3))
     params[kinds == 1, 3] = 0.05
     params[kinds == 2, 0:2] = rng.uniform(0.2, 0.4, ((kinds == 2).sum(), 2))
+    pos = np.stack([rng.uniform(-6, 6, n), rng.uniform(*y_range, n), rng.uniform(-6, 6, n)], 1)
+    q = scenes.random_quaternions(rng, n)
+    return np.concatenate([kinds[:, None], params, pos, q], 1)
+
+
+def random_cyl_hull(rng, n, y_range, n_hulls):
+    """Cylinders and the pile's own hulls as query shapes."""
+    kinds = np.where(rng.random(n) < 0.5, _lib.SHAPE_CYLINDER, _lib.SHAPE_CONVEX_HULL)
+    params = np.zeros((n, 4))
+    cyl = kinds == _lib.SHAPE_CYLINDER
+    params[cyl, 0] = rng.uniform(0.2, 0.5, cyl.sum())
+    params[cyl, 1] = rng.uniform(0.2, 0.5, cyl.sum())
+    params[cyl, 2] = 0.05
+    params[~cyl, 0] = rng.integers(0, n_hulls, (~cyl).sum())
     pos = np.stack([rng.uniform(-6, 6, n), rng.uniform(*y_range, n), rng.uniform(-6, 6, n)], 1)
     q = scenes.random_quaternions(rng, n)
     return np.concatenate([kinds[:, None], params, pos, q], 1)
@@ -314,20 +349,66 @@ def test_gpu_shape_cast_collectors_in_terrain_pile(gpu_lib, oracle_lib, seed):
     casts["shape_params"], casts["position"], casts["quaternion"] = rows[:, 1:5], rows[:, 5:8], rows[:, 8:12]
     casts["displacement"] = disp
     cap = 256
-    out, bo, co = o.cast_shapes_all(q15, cap)
+    out, bo, su, co = o.cast_shapes_all(q15, cap)
     h, c = g.cast_shapes_collect(casts, _lib.COLLECT_ALL, cap)
     assert (co <= cap).all() and (co > 1).sum() > 100
-    # a swept shape meets many terrain triangles; compare the hit bodies and the nearest hit
-    bodies_same = np.array([sorted(set(h["body"][k, :c[k]])) == sorted(set(bo[k, :co[k]])) for k in range(n)])
+    # a swept shape meets many terrain triangles; compare the (body, triangle) sets and the nearest hit
+    keys_g = [set(hit_keys(h["body"][k], h["sub_shape_id"][k], c[k])) for k in range(n)]
+    keys_o = [set(hit_keys(bo[k], su[k], co[k])) for k in range(n)]
+    bodies_same = np.array([{b for b, _ in keys_g[k]} == {b for b, _ in keys_o[k]} for k in range(n)])
     assert bodies_same.mean() >= 0.95, bodies_same.mean()
+    overlap = np.array([len(keys_g[k] & keys_o[k]) / max(1, len(keys_g[k] | keys_o[k])) for k in range(n)])
+    assert np.quantile(overlap, 0.05) >= 0.9, np.quantile(overlap, 0.05)
     counts_close = np.abs(c - co) <= np.maximum(2, 0.05 * co)
     assert counts_close.mean() >= 0.95, counts_close.mean()
     both = (c > 0) & (co > 0)
     lens = np.linalg.norm(disp, axis=1)
     err = np.abs(h["fraction"][both, 0] - out[both, 0, 0]) * lens[both]
     assert np.quantile(err, 0.99) < 2e-3 and err.max() < 0.1, (np.quantile(err, 0.99), err.max())
+    # the closest collector names the same triangle as the oracle's closest cast
+    hc = g.cast_shapes(casts)
+    oc, ob, osub = o.cast_shapes(q15, with_subs=True)
+    mesh = (hc["body"] == ob) & (ob == 0)
+    assert mesh.sum() > 100 and (hc["sub_shape_id"][mesh] == osub[mesh]).mean() >= 0.95
+    assert (hc["sub_shape_id"][(hc["body"] > 0)] == 0xFFFFFFFF).all()
     ha, ca = g.cast_shapes_collect(casts, _lib.COLLECT_ANY, 1)
     assert ((ca == 1) == (co > 0)).mean() >= 0.99
     hb = ha["body"][:, 0]
     inside = [hb[k] in set(bo[k, :co[k]]) for k in np.flatnonzero((ca == 1) & (co > 0))]
     assert np.mean(inside) >= 0.99
+
+
+@pytest.mark.gpu
+def test_gpu_cylinder_and_hull_queries_in_terrain_pile(gpu_lib, oracle_lib):
+    """Cylinders and convex hulls as collide and cast query shapes in a terrain pile: the all-hit
+    collide lists and the closest casts against the oracle's, with the bounds of the other tests."""
+    sc, g, o = terrain_pile(5)
+    rng = np.random.default_rng(400)
+    rows = random_cyl_hull(rng, 512, (-1.0, 3.0), len(sc.hull_points))
+    cap = 64
+    out, bo, su, co = o.collide_shapes_all(rows, cap)
+    h, c = g.collide_shapes(qarray(rows), _lib.COLLECT_ALL, cap)
+    assert co.sum() > 300
+    same = np.array([hit_keys(h["body"][k], h["sub_shape_id"][k], c[k]) == hit_keys(bo[k], su[k], co[k])
+                     for k in range(len(rows))])
+    assert same.mean() >= 0.97, same.mean()
+    up = random_cyl_hull(rng, 512, (7.0, 10.0), len(sc.hull_points))
+    disp = np.stack([rng.uniform(-2, 2, 512), rng.uniform(-14, -10, 512), rng.uniform(-2, 2, 512)], 1)
+    casts = np.zeros(512, _lib.SHAPE_CAST_DTYPE)
+    casts["shape_type"] = up[:, 0].astype(np.int32)
+    casts["shape_params"], casts["position"], casts["quaternion"] = up[:, 1:5], up[:, 5:8], up[:, 8:12]
+    casts["displacement"] = disp
+    hc = g.cast_shapes(casts)
+    oc, ob = o.cast_shapes(np.concatenate([up, disp], 1))
+    agree = hc["body"] == ob
+    assert agree.mean() >= 0.95 and (ob >= 0).mean() > 0.9, agree.mean()
+    lens = np.linalg.norm(disp, axis=1)
+    hit = agree & (ob >= 0)
+    err = np.abs(hc["fraction"][hit] - oc[hit, 0]) * lens[hit]
+    assert np.quantile(err, 0.99) < 2e-3, np.quantile(err, 0.99)
+    # a hull index the world does not have is refused
+    bad = casts[:1].copy()
+    bad["shape_type"] = _lib.SHAPE_CONVEX_HULL
+    bad["shape_params"][0, 0] = 99.0
+    with pytest.raises(_lib.CCError):
+        g.cast_shapes(bad)
