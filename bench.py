@@ -880,6 +880,7 @@ def terrain_measurement(cpu_seconds: float = 8.0):
         phases.append({"steps": [first, first + count], "ms_per_step": st["last_call_ms"] / count,
                        "awake": st["num_awake"], "manifolds": st["num_manifolds"], "epa": st["num_epa"],
                        "mesh_pairs": st["num_mesh_pairs"], "mesh_hits": st["num_mesh_hits"],
+                       "mesh_big": st["mesh_big"], "mesh_reduced": st["mesh_reduced"],
                        "ccd": st["num_ccd"], "ccd_hits": st["num_ccd_hits"], "islands": st["num_islands"]})
     rows, _ = g.get_state()
     hulls = [g.get_convex_hull(i) for i in range(len(sc.hull_points))]

@@ -136,7 +136,7 @@ class Stats(C.Structure):
         "num_islands", "max_island_constraints", "overflow_flags", "gpu_launches_per_step")] + [
         ("last_call_ms", C.c_float), ("num_giant_islands", C.c_int32), ("giant_colours", C.c_int32),
         ("num_ccd", C.c_int32), ("num_ccd_hits", C.c_int32), ("num_mesh_pairs", C.c_int32),
-        ("num_mesh_hits", C.c_int32), ("mesh_reduced", C.c_int32)]
+        ("num_mesh_hits", C.c_int32), ("mesh_reduced", C.c_int32), ("mesh_big", C.c_int32)]
 
 
 # numpy mirror of cc_body_desc (natural C alignment, 4-byte fields only)

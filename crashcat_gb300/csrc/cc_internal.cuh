@@ -73,8 +73,8 @@ struct DevCounters {
     int num_ccd_hits;  // of them, those whose cast hit a body
     int num_mesh_pairs;   // broadphase pairs with a triangle mesh body
     int num_mesh_hits;    // triangle hits reported to the mesh pairs' reduction
-    int mesh_reduced;     // mesh pairs whose hits needed more manifolds than a pair keeps
-    int pad[1];
+    int mesh_reduced;     // mesh pairs whose hits needed more manifolds than the reference's pool of 32
+    int num_mesh_big;     // mesh pairs run again with the 32-manifold pool (their hits overflowed 4)
 };
 
 // Settings copied into constant memory once per world.
@@ -529,6 +529,8 @@ struct DevWorld {
     int *mesh_pairs;      // pairs with a mesh body this step (index into pairs)
     int *mesh_epa_base;   // per mesh pair: its first EPA item, -1 when it needs none
     int *mesh_epa_count;  // per mesh pair: its EPA items
+    int *mesh_big;        // mesh pairs handed to the 32-manifold pass this step
+    void *mesh_big_red;   // MESH_BIG_THREADS reduction slots of 32 manifolds
     // continuous collision (LINEAR_CAST bodies, update.ts:896-1670)
     int num_linear_cast;  // bodies with LINEAR_CAST motion quality (0: the single-pass solve)
     int *ccd_flag;        // per body: deferred its translation this step
@@ -844,6 +846,8 @@ void launch_update_bounds(DevWorld &w, cudaStream_t s);
 void upload_settings(const DevSettings &s, double spec64, cudaStream_t st);
 void launch_cache_begin(DevWorld &w, cudaStream_t s);
 size_t epa_scratch_bytes();
+size_t mesh_big_slot_bytes();
+constexpr int MESH_BIG_THREADS = 256;  // threads (and 32-manifold slots) of the mesh pairs' big-pool pass
 void upload_settings_adjoint(const DevSettings &s, cudaStream_t st);
 void launch_tape_record(DevWorld &w, TapeStep &t, cudaStream_t s);
 void launch_tape_export(DevWorld &w, TapeStep &t, cc_tape_body *bodies, cc_tape_contact *cons, cudaStream_t s);

@@ -2267,22 +2267,26 @@ size_t epa_item_bytes() { return sizeof(EpaItem); }
 // collideSphereVsTriangleMesh :1418-1712 into narrowphaseWithReductionCollector
 // (update.ts:385-558), one mesh pair per thread
 // ---------------------------------------------------------------------------
-constexpr int MESH_MAXM = 4;   // manifolds a mesh pair keeps (the reference's pool holds 32)
-constexpr int MESH_MAXP = 56;  // points of one manifold before its prune (at most 32 + one hit's)
+constexpr int MESH_MAXM = 4;     // manifolds a mesh pair keeps in the first passes
+constexpr int MESH_BIG_M = 32;   // the reference's pool (update.ts:358-361), for the pairs that need more
+constexpr int MESH_MAXP = 56;    // points of one manifold before its prune (at most 32 + one hit's)
 constexpr int MESH_STACK = 64;
 
-struct MeshReduce {
+template <int M>
+struct MeshReduceT {
     int nm;
-    float3 normal[MESH_MAXM];  // accumulated (unnormalised) normals
-    float depth[MESH_MAXM];
-    uint32_t sub_a[MESH_MAXM], sub_b[MESH_MAXM];
-    PtsN<MESH_MAXP> pts[MESH_MAXM];
+    float3 normal[M];  // accumulated (unnormalised) normals
+    float depth[M];
+    uint32_t sub_a[M], sub_b[M];
+    PtsN<MESH_MAXP> pts[M];
     bool dropped;  // a new normal group arrived with every slot taken
 };
+using MeshReduce = MeshReduceT<MESH_MAXM>;
+size_t mesh_big_slot_bytes() { return sizeof(MeshReduceT<MESH_BIG_M>); }
 
 // addHit update.ts:385-519 (points relative to the base, the narrowphase's body A)
-template <int N>
-__device__ void mesh_add_hit(MeshReduce &r, float3 pa, float3 pb, float3 axis, float penetration, uint32_t sa,
+template <int N, int M>
+__device__ void mesh_add_hit(MeshReduceT<M> &r, float3 pa, float3 pb, float3 axis, float penetration, uint32_t sa,
                              uint32_t sb, const FaceN<N> &fA, const FaceN<N> &fB) {
     const float3 n = normalize3(axis);
     int m = -1;
@@ -2292,7 +2296,7 @@ __device__ void mesh_add_hit(MeshReduce &r, float3 pa, float3 pb, float3 axis, f
             break;
         }
     if (m < 0) {
-        if (r.nm >= MESH_MAXM) {
+        if (r.nm >= M) {
             // pool full: the shallowest manifold makes way for a deeper hit
             int sh = 0;
             for (int i = 1; i < r.nm; i++)
@@ -2331,7 +2335,8 @@ __device__ void mesh_add_hit(MeshReduce &r, float3 pa, float3 pb, float3 axis, f
 }
 
 // finalizeAndCreateConstraints update.ts:525-558: the manifolds into the contact pipeline
-__device__ void mesh_emit(DevWorld &w, MeshReduce &r, int a, int b, float3 base) {
+template <int M>
+__device__ void mesh_emit(DevWorld &w, MeshReduceT<M> &r, int a, int b, float3 base) {
     for (int i = 0; i < r.nm; i++) {
         PtsN<MESH_MAXP> &P = r.pts[i];
         float3 nrm = normalize3(r.normal[i]);
@@ -2495,14 +2500,16 @@ __device__ float convex_bounds_size(const DevWorld &w, uint32_t f, float4 sp) {
     return sqrtf(lensq3(hi - lo));
 }
 
-// One mesh pair.  PASS 0: pairs with no triangle in need of EPA are reduced and emitted; a
+// One mesh pair k.  PASS 0: pairs with no triangle in need of EPA are reduced and emitted; a
 // pair with some reserves one EPA item per such triangle, in traversal order, and waits.
 // PASS 1 (after the EPA passes): those pairs again, each such triangle taking its item.
-template <int PASS>
-__global__ void __launch_bounds__(64) k_mesh_narrowphase(DevWorld w, EpaItem *epa_items) {
-    const int npairs = min(w.ctr->num_mesh_pairs, w.max_pairs);
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < npairs; k += gridDim.x * blockDim.x) {
-        if (PASS == 1 && w.mesh_epa_base[k] < 0) continue;
+// PASS 2: a pair whose hits wanted more than the 4 manifolds of the first passes' pool, again
+// with the reference's pool of 32 (red in global memory) and its EPA items, if it has some.
+// A pair of the first passes that overflows its pool is handed to PASS 2 instead of emitted.
+template <int PASS, int M>
+__device__ void mesh_pair(DevWorld &w, EpaItem *epa_items, int k, MeshReduceT<M> &red) {
+    {
+        if (PASS == 1 && w.mesh_epa_base[k] < 0) return;
         int2 pr = w.pairs[w.mesh_pairs[k]];
         int a = pr.x, b = pr.y;
         uint32_t fa = w.flags[a], fb = w.flags[b];
@@ -2517,7 +2524,7 @@ __global__ void __launch_bounds__(64) k_mesh_narrowphase(DevWorld w, EpaItem *ep
         }
         if (PASS == 0) w.mesh_epa_base[k] = -1;
         const bool meshA = shape_of(fa) == SHAPE_MESH, meshB = shape_of(fb) == SHAPE_MESH;
-        if (meshA == meshB) continue;  // mesh against mesh: no collide function (triangle-mesh.ts:223-237)
+        if (meshA == meshB) return;  // mesh against mesh: no collide function (triangle-mesh.ts:223-237)
         // collideTriangleMeshVsConvex = the convex-vs-mesh function with the hit reversed
         // (reversedCollideShapeVsShape collide-shape-vs-shape.ts:227-354)
         const bool inverted = meshA;
@@ -2572,14 +2579,13 @@ __global__ void __launch_bounds__(64) k_mesh_narrowphase(DevWorld w, EpaItem *ep
         const HullView hv = hull_view(w);
         Sup<float> supA;
         if (!sphere) supA = make_sup<float>(shape_of(fc), sc, true, hv);
-        MeshReduce red;
         red.nm = 0;
         red.dropped = false;
         int epa_needed = 0, epa_next = 0;
-        const int epa_base = PASS == 1 ? w.mesh_epa_base[k] : -1;
-        const int epa_count = PASS == 1 ? w.mesh_epa_count[k] : 0;
+        const int epa_base = PASS >= 1 ? w.mesh_epa_base[k] : -1;
+        const int epa_count = PASS >= 1 ? w.mesh_epa_count[k] : 0;
         for (int round = 0; round < 2; round++) {  // PASS 0 runs a second round to fill the EPA items
-            if (round == 1 && (PASS == 1 || epa_needed == 0)) break;
+            if (round == 1 && (PASS >= 1 || epa_needed == 0)) break;
             int reserve = -1;
             if (round == 1) {
                 // the whole block or nothing: the EPA passes read every item below min(num_epa, max_epa)
@@ -2777,7 +2783,7 @@ __global__ void __launch_bounds__(64) k_mesh_narrowphase(DevWorld w, EpaItem *ep
                         fTri.v[1] = to_base(V<float>{t1.x, t1.y, t1.z});
                         fTri.v[2] = to_base(V<float>{t2.x, t2.y, t2.z});
                     }
-                    atomicAdd(&w.ctr->num_mesh_hits, 1);
+                    if (PASS != 2) atomicAdd(&w.ctr->num_mesh_hits, 1);
                     if (inverted)  // the inverted collector: points, axis, sub-shape ids and faces swapped
                         mesh_add_hit(red, hpb, hpa, -hax, hpen, tsub, 0xffffffffu, fTri, fConvex);
                     else
@@ -2785,17 +2791,44 @@ __global__ void __launch_bounds__(64) k_mesh_narrowphase(DevWorld w, EpaItem *ep
                 }
             }
         }
-        if (PASS == 0 && epa_needed > 0) continue;  // finished by the second pass
+        if (PASS == 0 && epa_needed > 0) return;  // finished by the second pass
+        if (PASS != 2 && red.dropped && w.mesh_big) {  // the pool overflowed: the 32-manifold pass takes it
+            const int o = atomicAdd(&w.ctr->num_mesh_big, 1);
+            if (o < w.max_pairs) {
+                w.mesh_big[o] = k;
+                return;
+            }
+        }
         mesh_emit(w, red, a, b, base);
     }
 }
 
+template <int PASS>
+__global__ void __launch_bounds__(64) k_mesh_narrowphase(DevWorld w, EpaItem *epa_items) {
+    const int npairs = min(w.ctr->num_mesh_pairs, w.max_pairs);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < npairs; k += gridDim.x * blockDim.x) {
+        MeshReduce red;
+        mesh_pair<PASS, MESH_MAXM>(w, epa_items, k, red);
+    }
+}
+// the pairs whose hits overflowed the 4-manifold pool, with the reference's 32 (one global slot
+// per thread)
+__global__ void __launch_bounds__(64) k_mesh_big(DevWorld w, EpaItem *epa_items) {
+    const int nbig = min(w.ctr->num_mesh_big, w.max_pairs);
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    MeshReduceT<MESH_BIG_M> &red = ((MeshReduceT<MESH_BIG_M> *)w.mesh_big_red)[tid];
+    for (int j = tid; j < nbig; j += gridDim.x * blockDim.x) mesh_pair<2, MESH_BIG_M>(w, epa_items, w.mesh_big[j], red);
+}
+
+
 void launch_mesh_narrowphase(DevWorld &w, int pass, cudaStream_t s) {
     EpaItem *items = (EpaItem *)w.epa_items;
-    if (pass == 0)
+    if (pass == 0) {
         k_mesh_narrowphase<0><<<device_sm_count() * 4, 64, 0, s>>>(w, items);
-    else
+    } else {
         k_mesh_narrowphase<1><<<device_sm_count() * 4, 64, 0, s>>>(w, items);
+        if (w.mesh_big) k_mesh_big<<<MESH_BIG_THREADS / 64, 64, 0, s>>>(w, items);
+    }
 }
 
 // ---------------------------------------------------------------------------

@@ -545,7 +545,7 @@ int cc_world_destroy(cc_world *W) {
                     w.hull_planes, w.hull_faces, w.hull_vidx, w.ccd_flag, w.ccd_slot, w.ccd_index, w.ccd,
                     w.ccd_world_off, w.ccd_world_fill, w.ccd_seg, w.ccd_lambda, w.ccd_scan_tmp,
                     w.meshes, w.mesh_verts, w.mesh_tris, w.mesh_nodes, w.mesh_pairs, w.mesh_epa_base,
-                    w.mesh_epa_count};
+                    w.mesh_epa_count, w.mesh_big, w.mesh_big_red};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (W->q_rays) cudaFree(W->q_rays);
@@ -990,10 +990,14 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
     }
     if (mc > 0 && !w.mesh_pairs) {
         int r;
+        char *big = nullptr;
         if ((r = dalloc(&w.mesh_pairs, (size_t)w.max_pairs)) != CC_OK ||
             (r = dalloc(&w.mesh_epa_base, (size_t)w.max_pairs)) != CC_OK ||
-            (r = dalloc(&w.mesh_epa_count, (size_t)w.max_pairs)) != CC_OK)
+            (r = dalloc(&w.mesh_epa_count, (size_t)w.max_pairs)) != CC_OK ||
+            (r = dalloc(&w.mesh_big, (size_t)w.max_pairs)) != CC_OK ||
+            (r = dalloc(&big, mesh_big_slot_bytes() * (size_t)MESH_BIG_THREADS)) != CC_OK)
             return r;
+        w.mesh_big_red = big;
     }
     w.num_mesh_bodies += mc;
     if (lc > 0) {
@@ -1733,6 +1737,7 @@ int cc_world_get_stats(cc_world *W, cc_stats *o) {
     o->num_mesh_pairs = c.num_mesh_pairs;
     o->num_mesh_hits = c.num_mesh_hits;
     o->mesh_reduced = c.mesh_reduced;
+    o->mesh_big = c.num_mesh_big;
     return CC_OK;
 }
 

@@ -215,7 +215,8 @@ typedef struct cc_stats {
     int32_t num_ccd_hits;      /* of them, those whose cast hit a body (findCCDContacts update.ts:1354) */
     int32_t num_mesh_pairs;    /* broadphase pairs with a triangle mesh body */
     int32_t num_mesh_hits;     /* triangle hits handed to those pairs' reduction */
-    int32_t mesh_reduced;      /* mesh pairs whose hits wanted more manifolds than a pair keeps (4) */
+    int32_t mesh_reduced;      /* mesh pairs whose hits wanted more manifolds than the reference's pool of 32 */
+    int32_t mesh_big;          /* mesh pairs whose hits needed more than 4 manifolds (run again with 32) */
 } cc_stats;
 
 typedef struct cc_world cc_world;

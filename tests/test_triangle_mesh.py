@@ -314,3 +314,58 @@ def test_ccd_against_mesh_parity(gpu_lib, oracle_lib, shape, relief, cos, caught
         assert (s["num_ccd"], s["num_ccd_hits"]) == o.ccd_counts(), k
         rows, _ = g.get_state()
         np.testing.assert_allclose(rows[1, 0:3], o.state()[1, 0:3], atol=5e-3, err_msg=f"step {k}")
+
+
+# ---------------------------------------------------------------------------
+# the reduction collector's pool of 32 manifolds (update.ts:358-361)
+# ---------------------------------------------------------------------------
+def cone_bowl(sectors: int = 12, radius: float = 3.0, slope_deg: float = 30.0):
+    """An inverted cone of `sectors` facets sloping `slope_deg` up from the apex at the origin:
+    adjacent facet normals differ by cos = 0.75 + 0.25 cos(360 / sectors), below the manifold
+    merge threshold cos 5 degrees, so a body sitting in the apex touches one normal group per
+    facet."""
+    h = radius * math.tan(math.radians(slope_deg))
+    ang = 2.0 * math.pi * np.arange(sectors) / sectors
+    pos = np.concatenate([[[0.0, 0.0, 0.0]], np.stack([radius * np.cos(ang), np.full(sectors, h),
+                                                        radius * np.sin(ang)], 1)])
+    idx = np.array([[0, (i + 1) % sectors + 1, i + 1] for i in range(sectors)])  # facing up
+    return pos, idx
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", ["sphere", "box"])
+def test_bowl_uses_the_32_manifold_pool(gpu_lib, oracle_lib, shape):
+    """A sphere (or box) settled in the apex of a 12-facet bowl touches every facet with its own
+    normal: 12 manifolds for the one pair, as the reference's pool of 32 keeps them.  The pair
+    overflows the 4-manifold pool of the first passes and is run again with 32 (stats mesh_big);
+    no pair outgrows 32 (mesh_reduced 0).  The manifolds match the oracle's at the same poses."""
+    b = scenes.blank_bodies(2)
+    b["shape_type"][0] = _lib.SHAPE_TRIANGLE_MESH
+    b["motion_type"][0] = _lib.STATIC
+    b["object_layer"][0] = scenes.LAYER_NOT_MOVING
+    if shape == "sphere":
+        scenes.set_sphere(b, 1, 1.0)
+    else:
+        scenes.set_box(b, 1, (0.8, 0.8, 0.8))
+    b["position"][1] = (0.0, 2.5, 0.0)
+    sc = scenes.Scene("bowl", b, dt=1 / 60, steps=60)
+    sc.mesh = cone_bowl()
+    g, o = gpu_and_oracle_mesh(sc)
+    g.step(sc.dt, 60)
+    rows, _ = g.get_state()
+    st = o.state()
+    st[:, 0:13] = rows[:, 0:13]
+    o.set_state(st)
+    g.step(0.0, 1)
+    o.step(0.0, 1)
+    stats = g.stats()
+    assert stats["mesh_big"] == 1 and stats["mesh_reduced"] == 0, stats
+    gm, gs = g.get_manifolds(), g.get_manifold_sub_shapes()
+    om, os_ = o.manifolds(), o.manifold_sub_shapes()
+    assert len(om) > 4 and len(gm) == len(om), (len(gm), len(om))
+    gk = {(int(s[0]), int(s[1])): r for r, s in zip(gm, gs)}
+    ok = {(int(s[0]), int(s[1])): r for r, s in zip(om, os_)}
+    assert set(gk) == set(ok)
+    for k in ok:
+        np.testing.assert_allclose(gk[k][3:6], ok[k][3:6], atol=1e-3)
+        assert abs(gk[k][6] - ok[k][6]) < 2e-3
