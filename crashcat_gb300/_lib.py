@@ -29,6 +29,7 @@ SHAPE_TRIANGLE_MESH = 4
 SHAPE_CYLINDER = 5
 SHAPE_PLANE = 6
 SHAPE_EMPTY = 7
+SHAPE_COMPOUND = 8
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 COMBINE_AVERAGE, COMBINE_MULTIPLY, COMBINE_MIN, COMBINE_MAX, COMBINE_GEOMETRIC_MEAN = 0, 1, 2, 3, 4
 MAX_LAYERS = 32
@@ -106,6 +107,11 @@ SHAPE_CAST_DTYPE = np.dtype([("shape_type", np.int32), ("shape_params", np.float
                              ("quaternion", np.float32, 4), ("displacement", np.float32, 3), ("world", np.int32)])
 SHAPE_CAST_HIT_DTYPE = np.dtype([("body", np.int32), ("fraction", np.float32), ("normal", np.float32, 3),
                                  ("point", np.float32, 3), ("sub_shape_id", np.uint32), ("reserved", np.int32)])
+# a compound shape's child (cc_compound_child)
+COMPOUND_CHILD_DTYPE = np.dtype([("shape_type", np.int32), ("shape_params", np.float32, 4),
+                                 ("position", np.float32, 3), ("quaternion", np.float32, 4),
+                                 ("density", np.float32)])
+
 # query collectors (cc_collector) and the collide query's records
 COLLECT_CLOSEST, COLLECT_ANY, COLLECT_ALL = 0, 1, 2
 COLLIDE_SHAPE_DTYPE = np.dtype([("shape_type", np.int32), ("shape_params", np.float32, 4),

@@ -14,8 +14,9 @@ import numpy as np
 
 from typing import Optional
 
-from ._lib import (BODY_DTYPE, COMBINE_GEOMETRIC_MEAN, COMBINE_MAX, DYNAMIC, MOTOR_OFF, MOTOR_POSITION,
-                   MOTOR_VELOCITY, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_CONVEX_HULL, SHAPE_CYLINDER, SHAPE_EMPTY,
+from ._lib import (BODY_DTYPE, COMBINE_GEOMETRIC_MEAN, COMBINE_MAX, COMPOUND_CHILD_DTYPE, DYNAMIC, MOTOR_OFF,
+                   MOTOR_POSITION, MOTOR_VELOCITY, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_COMPOUND, SHAPE_CONVEX_HULL,
+                   SHAPE_CYLINDER, SHAPE_EMPTY,
                    SHAPE_PLANE, SHAPE_SPHERE, SHAPE_TRIANGLE_MESH, STATIC,
                    SWING_CONE, SWING_PYRAMID, JOINT_CONE, JOINT_DISTANCE, JOINT_FIXED, JOINT_POINT, JOINT_SIX_DOF,
                    JOINT_SLIDER, SPRING_DTYPE, SPRING_FREQUENCY_AND_DAMPING, SPRING_STIFFNESS_AND_DAMPING,
@@ -122,6 +123,36 @@ def set_empty(b: np.ndarray, idx) -> None:
     """Empty shape (src/shapes/empty-shape.ts): no collision and no mass."""
     b["shape_type"][idx] = SHAPE_EMPTY
     b["shape_params"][idx] = 0.0
+
+
+def set_compound(b: np.ndarray, idx, compound_index: int) -> None:
+    """A compound body (src/shapes/compound.ts): the index from GpuWorld.add_compound in
+    shape_params[0]; mass and inertia come from the children's densities."""
+    b["shape_type"][idx] = SHAPE_COMPOUND
+    b["shape_params"][idx] = 0.0
+    b["shape_params"][idx, 0] = float(compound_index)
+
+
+def compound_children(specs) -> np.ndarray:
+    """Child records from (kind, params, position[, quaternion[, density]]) tuples, kind one of
+    sphere, box, capsule, cylinder, hull (params: the hull index)."""
+    kinds = {"sphere": SHAPE_SPHERE, "box": SHAPE_BOX, "capsule": SHAPE_CAPSULE, "cylinder": SHAPE_CYLINDER,
+             "hull": SHAPE_CONVEX_HULL}
+    c = np.zeros(len(specs), COMPOUND_CHILD_DTYPE)
+    for i, sp in enumerate(specs):
+        kind, params, pos = sp[0], sp[1], sp[2]
+        q = sp[3] if len(sp) > 3 else (0.0, 0.0, 0.0, 1.0)
+        c["shape_type"][i] = kinds[kind]
+        p = list(params)
+        if kind == "box" and len(p) == 3:
+            p.append(DEFAULT_CONVEX_RADIUS)
+        if kind == "cylinder" and len(p) == 2:
+            p.append(DEFAULT_CONVEX_RADIUS)
+        c["shape_params"][i, :len(p)] = p
+        c["position"][i] = pos
+        c["quaternion"][i] = q
+        c["density"][i] = sp[4] if len(sp) > 4 else 1000.0
+    return c
 
 
 def set_hull(b: np.ndarray, idx, hull_index: int) -> None:

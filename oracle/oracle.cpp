@@ -166,6 +166,7 @@ struct World {
     std::vector<SixDofJoint> sixdofs;
     std::vector<std::unique_ptr<HullData>> hulls;  // convex hull shapes the bodies refer to
     std::vector<std::unique_ptr<MeshData>> meshes;  // triangle meshes the bodies refer to
+    std::vector<std::unique_ptr<CompoundData>> compounds;  // compound shapes the bodies refer to
     // skip broadphase pairs of bodies that share an enabled joint: the declarative form of the
     // ragdoll example's onBodyPairValidate (examples/src/example-ragdoll.ts:487-489)
     bool skipJointPairs = false;
@@ -206,6 +207,11 @@ struct World {
 // ---------------------------------------------------------------------------
 // setMassAndInertiaOfSolidBox mass-properties.ts:36-52 / sphere.ts:97-123
 static void shape_mass(const Shape &s, double &mass, V3 &inertiaDiag) {
+    if (s.type == SHAPE_COMPOUND) {  // the tensor goes through set_mass_properties_tensor
+        mass = s.compound->mass;
+        inertiaDiag = {0, 0, 0};
+        return;
+    }
     if (s.type == SHAPE_BOX) {
         V3 full = scale(s.half_extents, 2);
         mass = full.x * full.y * full.z * s.density;
@@ -1379,6 +1385,7 @@ static void check_island_sleep(World &w, Island &is, double dt) {
 // getInnerRadius box.ts:333-335, sphere.ts:147-149, capsule.ts:254-256, convex-hull.ts:549-558
 static double inner_radius(const Shape &s) {
     if (s.decorated && s.innerRadius >= 0) return s.innerRadius;
+    if (s.type == SHAPE_COMPOUND) return s.compound->innerRadius;
     switch (s.type) {
         case SHAPE_BOX:
             return std::min(s.half_extents.x, std::min(s.half_extents.y, s.half_extents.z));
@@ -1483,6 +1490,18 @@ static void find_ccd_contacts(World &w, double dt) {
                 c.restitution = combine(A.restitution, B.restitution, A.restitutionCombine, B.restitutionCombine);
             };
             if (B.shape.type == SHAPE_EMPTY || A.shape.type == SHAPE_EMPTY) continue;
+            if (B.shape.type == SHAPE_COMPOUND) {  // castShapeVsCompound compound.ts:776-866: each child
+                const CompoundData &C = *B.shape.compound;
+                for (int i = 0; i < (int)C.shapes.size(); i++) {
+                    V3 cp;
+                    Q4 cq;
+                    compound_child_pose(C, i, gpB, gqB, cp, cq);
+                    CastHit h;
+                    if (cast_convex_vs_convex(h, A.shape, gpA, gqA, rel, C.shapes[i], cp, cq, c.fps, false))
+                        collect(h.fraction, h.pa, h.axis);
+                }
+                continue;
+            }
             if (B.shape.type == SHAPE_PLANE) {  // castConvexVsPlane plane.ts:727-918
                 CastHit h;
                 if (cast_convex_vs_plane(h, A.shape, gpA, gqA, rel, B.shape, gpB, gqB, c.fps, false))
@@ -2021,6 +2040,22 @@ static bool decorate(Shape &s, const double *r) {
     return true;
 }
 
+// computeCompoundLocalBounds compound.ts:70-108: the children's bounds' corners through their poses
+static Box3 compound_bounds(const CompoundData &c) {
+    Box3 b{{1e300, 1e300, 1e300}, {-1e300, -1e300, -1e300}};
+    for (size_t i = 0; i < c.shapes.size(); i++) {
+        const Box3 &a = c.shapes[i].aabb;
+        for (int k = 0; k < 8; k++) {
+            V3 p{(k & 1) ? a.mx.x : a.mn.x, (k & 2) ? a.mx.y : a.mn.y, (k & 4) ? a.mx.z : a.mn.z};
+            V3 q = add(rotate(c.rot[i], p), c.pos[i]);
+            b.mn = {std::min(b.mn.x, q.x), std::min(b.mn.y, q.y), std::min(b.mn.z, q.z)};
+            b.mx = {std::max(b.mx.x, q.x), std::max(b.mx.y, q.y), std::max(b.mx.z, q.z)};
+        }
+    }
+    return b;
+}
+static V3 compound_com(const CompoundData &c);
+
 static bool shape_from_row(Shape &s, const double *r, const World *w = nullptr) {
     s.type = (int)r[F_SHAPE];
     s.density = r[F_DENSITY];
@@ -2032,6 +2067,14 @@ static bool shape_from_row(Shape &s, const double *r, const World *w = nullptr) 
         s.com = s.hull->com;
         s.aabb = s.hull->bounds;
         s.convex_radius = s.hull->convex_radius;
+    } else if (s.type == SHAPE_COMPOUND) {  // F_P0: the compound index; no decorators on it
+        int c = (int)r[F_P0];
+        if (!w || c < 0 || c >= (int)w->compounds.size()) return false;
+        s.compound = w->compounds[c].get();
+        s.aabb = compound_bounds(*s.compound);
+        s.com = compound_com(*s.compound);
+        if (!decorate(s, r)) return false;
+        return !s.decorated;
     } else if (s.type == SHAPE_TRIANGLE_MESH) {  // F_P0: the mesh index
         int m = (int)r[F_P0];
         if (!w || m < 0 || m >= (int)w->meshes.size()) return false;
@@ -2143,6 +2186,8 @@ static int setup_mass(Body &b, const Shape &s, const double *r, const World *w) 
             decorated_mass(r, w, mass, I);
         } else if (s.type == SHAPE_CONVEX_HULL) {
             for (int k = 0; k < 9; k++) I[k] = s.hull->inertia[k] * s.density;
+        } else if (s.type == SHAPE_COMPOUND) {
+            for (int k = 0; k < 9; k++) I[k] = s.compound->inertia[k];
         } else {
             double t[9] = {idiag.x, 0, 0, 0, idiag.y, 0, 0, 0, idiag.z};
             for (int k = 0; k < 9; k++) I[k] = t[k];
@@ -2168,6 +2213,8 @@ static int setup_mass(Body &b, const Shape &s, const double *r, const World *w) 
             set_mass_properties_tensor(b, mass, I, 1.0);
         } else if (s.type == SHAPE_CONVEX_HULL) {
             set_mass_properties_tensor(b, mass, s.hull->inertia, s.density);
+        } else if (s.type == SHAPE_COMPOUND) {
+            set_mass_properties_tensor(b, mass, s.compound->inertia, 1.0);
         } else {
             set_mass_properties(b, mass, idiag);
         }
@@ -2199,6 +2246,7 @@ int orc_add_bodies(void *wp, const double *rows, int n) {
         b.angDamp = r[F_ANG_DAMP];
         b.allowSleeping = r[F_ALLOW_SLEEP] != 0;
         b.linearCast = r[F_MOTION_QUALITY] == 1;
+        if (b.linearCast && s.type == SHAPE_COMPOUND) return -1;  // a cast compound is not restated
         b.velOverride = (int)r[F_VEL_OVERRIDE];
         b.posOverride = (int)r[F_POS_OVERRIDE];
         b.groups = (uint32_t)r[F_GROUPS];
@@ -2336,6 +2384,84 @@ int orc_add_mesh(void *wp, int nv, const double *verts, int nt, const int *tris,
     if (nn > 0) m->bounds = {{nodes[0], nodes[1], nodes[2]}, {nodes[3], nodes[4], nodes[5]}};
     w.meshes.push_back(std::move(m));
     return (int)w.meshes.size() - 1;
+}
+
+// compound.ts create / update (:43-57, :143-147) and computeMassProperties (:177-230): children
+// given as 13 doubles (shape type, 4 shape params, position xyz, quaternion xyzw, density);
+// convex children only (sphere, box, capsule, cylinder, a hull of this world).  Returns the
+// compound index, or -1.
+static V3 compound_com(const CompoundData &c) {
+    // computeCompoundCenterOfMass :110-141: the children's centres of mass weighted by mass
+    V3 acc{0, 0, 0};
+    double total = 0;
+    for (size_t i = 0; i < c.shapes.size(); i++) {
+        double m;
+        V3 d;
+        shape_mass(c.shapes[i], m, d);
+        acc = add(acc, scale(add(c.pos[i], rotate(c.rot[i], c.shapes[i].com)), m));
+        total += m;
+    }
+    return total > 0 ? scale(acc, 1.0 / total) : V3{0, 0, 0};
+}
+int orc_add_compound(void *wp, const double *rows, int n) {
+    World &w = *(World *)wp;
+    if (n <= 0) return -1;
+    auto c = std::make_unique<CompoundData>();
+    for (int i = 0; i < n; i++) {
+        const double *q = rows + 13 * i;
+        double row[F_COUNT] = {};
+        row[F_SHAPE] = q[0];
+        for (int k = 0; k < 4; k++) row[F_P0 + k] = q[1 + k];
+        row[F_DENSITY] = q[12];
+        Shape ch;
+        if (!shape_from_row(ch, row, &w)) return -1;
+        if (ch.type != SHAPE_SPHERE && ch.type != SHAPE_BOX && ch.type != SHAPE_CAPSULE && ch.type != SHAPE_CYLINDER &&
+            ch.type != SHAPE_CONVEX_HULL)
+            return -1;
+        c->shapes.push_back(ch);
+        c->pos.push_back({q[5], q[6], q[7]});
+        c->rot.push_back(Q4{q[8], q[9], q[10], q[11]});
+    }
+    unsigned maxi = (unsigned)(n - 1);
+    c->subBits = maxi == 0 ? 0 : 32 - __builtin_clz(maxi);
+    c->innerRadius = std::numeric_limits<double>::max();
+    for (const Shape &ch : c->shapes) c->innerRadius = std::min(c->innerRadius, inner_radius(ch));
+    const V3 com = compound_com(*c);
+    double I[9] = {};
+    c->mass = 0;
+    for (int i = 0; i < n; i++) {
+        const Shape &ch = c->shapes[i];
+        double m;
+        V3 d;
+        shape_mass(ch, m, d);
+        double t[9] = {d.x, 0, 0, 0, d.y, 0, 0, 0, d.z};
+        if (ch.type == SHAPE_CONVEX_HULL)
+            for (int k = 0; k < 9; k++) t[k] = ch.hull->inertia[k] * ch.density;
+        // massProperties.rotate (mass-properties.ts:121-160): R I R^T
+        M4 R4 = mat4_from_quat(c->rot[i]);  // column-major: element (i, j) at m[4 j + i]
+        double rt[9], o[9];
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) {
+                double acc = 0;
+                for (int k = 0; k < 3; k++) acc += R4.m[4 * k + a] * t[3 * k + b];
+                rt[3 * a + b] = acc;
+            }
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) {
+                double acc = 0;
+                for (int k = 0; k < 3; k++) acc += rt[3 * a + k] * R4.m[4 * k + b];
+                o[3 * a + b] = acc;
+            }
+        // massProperties.translate (:168-205) by the child's centre of mass from the compound's
+        V3 off = sub(add(c->pos[i], rotate(c->rot[i], ch.com)), com);
+        double dd = dot(off, off), v[3] = {off.x, off.y, off.z};
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) I[3 * a + b] += o[3 * a + b] + m * ((a == b ? dd : 0.0) - v[a] * v[b]);
+        c->mass += m;
+    }
+    for (int k = 0; k < 9; k++) c->inertia[k] = I[k];
+    w.compounds.push_back(std::move(c));
+    return (int)w.compounds.size() - 1;
 }
 
 int orc_add_swing_twist(void *wp, const double *d) {
@@ -2958,6 +3084,19 @@ int orc_cast_shapes(void *wp, const double *qs, int n, uint32_t layerMask, uint3
                 hp = pa;
             };
             if (B.shape.type == SHAPE_EMPTY) continue;
+            if (B.shape.type == SHAPE_COMPOUND) {  // castShapeVsCompound compound.ts:776-866
+                const CompoundData &C = *B.shape.compound;
+                for (int i = 0; i < (int)C.shapes.size(); i++) {
+                    V3 cp;
+                    Q4 cq;
+                    compound_child_pose(C, i, gpB, gqB, cp, cq);
+                    CastHit h;
+                    const double maxL = (hit >= 0 && B.index < hit) ? std::nextafter(best, 2.0) : best;
+                    if (cast_convex_vs_convex(h, sa, pA, qA, disp, C.shapes[i], cp, cq, maxL, false))
+                        collect(h.fraction, h.pa, h.axis, compound_sub_id(C, i));
+                }
+                continue;
+            }
             if (B.shape.type == SHAPE_PLANE) {
                 CastHit h;
                 if (cast_convex_vs_plane(h, sa, pA, qA, disp, B.shape, gpB, gqB, best, false))
@@ -3015,6 +3154,19 @@ void orc_cast_rays_all(void *wp, const double *rays, int n, uint32_t layerMask, 
             V3 gp;
             Q4 gq;
             geometry_pose(b.shape, b.position, b.quat, gp, gq);
+            if (b.shape.type == SHAPE_COMPOUND) {  // castRayVsCompound: each child's hit
+                const CompoundData &C = *b.shape.compound;
+                for (int i = 0; i < (int)C.shapes.size(); i++) {
+                    V3 cp;
+                    Q4 cq;
+                    compound_child_pose(C, i, gp, gq, cp, cq);
+                    double f;
+                    uint32_t sb;
+                    if (cast_ray_vs_shape(C.shapes[i], cp, cq, o, d, len, treatConvexAsSolid != 0, initial, f, sb))
+                        hs.push_back({f, b.index, compound_sub_id(C, i)});
+                }
+                continue;
+            }
             if (b.shape.type == SHAPE_TRIANGLE_MESH) {
                 Q4 iq = qconj(gq);
                 std::vector<std::pair<double, uint32_t>> th;
@@ -3077,6 +3229,18 @@ int orc_cast_shapes_all(void *wp, const double *qs, int n, uint32_t layerMask, u
                 if (fraction < initial) hs.push_back({fraction, B.index, sub, neg(normalize(axis)), pa});
             };
             if (B.shape.type == SHAPE_EMPTY) continue;
+            if (B.shape.type == SHAPE_COMPOUND) {
+                const CompoundData &C = *B.shape.compound;
+                for (int i = 0; i < (int)C.shapes.size(); i++) {
+                    V3 cp;
+                    Q4 cq;
+                    compound_child_pose(C, i, gpB, gqB, cp, cq);
+                    CastHit h;
+                    if (cast_convex_vs_convex(h, sa, pA, qA, disp, C.shapes[i], cp, cq, initial, false))
+                        collect(h.fraction, h.pa, h.axis, compound_sub_id(C, i));
+                }
+                continue;
+            }
             if (B.shape.type == SHAPE_PLANE) {
                 CastHit h;
                 if (cast_convex_vs_plane(h, sa, pA, qA, disp, B.shape, gpB, gqB, initial, false))

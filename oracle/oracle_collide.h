@@ -20,7 +20,7 @@ constexpr double DEFAULT_CONVEX_RADIUS = 0.05;  // src/collision/support.ts:5
 constexpr uint32_t EMPTY_SUB_SHAPE_ID = 0xffffffffu;  // src/body/sub-shape.ts:4
 
 enum ShapeType : int { SHAPE_SPHERE = 0, SHAPE_BOX = 1, SHAPE_CAPSULE = 2, SHAPE_CONVEX_HULL = 3, SHAPE_TRIANGLE_MESH = 4,
-                       SHAPE_CYLINDER = 5, SHAPE_PLANE = 6, SHAPE_EMPTY = 7 };
+                       SHAPE_CYLINDER = 5, SHAPE_PLANE = 6, SHAPE_EMPTY = 7, SHAPE_COMPOUND = 8 };
 
 // Triangle mesh as built (src/shapes/utils/triangle-mesh-data.ts, triangle-mesh-bvh.ts): welded
 // vertices, triangles (vertex indices, active-edge bits AB 1 / BC 2 / CA 4) in the order the BVH
@@ -49,9 +49,11 @@ struct HullData {
 };
 
 // Shape data (src/shapes/box.ts:38-70, src/shapes/sphere.ts, src/shapes/capsule.ts, convex-hull.ts)
+struct CompoundData;
 struct Shape {
     const HullData *hull = nullptr;  // convex hull
     const MeshData *mesh = nullptr;  // triangle mesh
+    const CompoundData *compound = nullptr;  // compound shape
     int type = SHAPE_BOX;
     V3 half_extents;          // box
     double convex_radius = 0;  // box
@@ -73,6 +75,30 @@ struct Shape {
     Q4 tRot{0, 0, 0, 1};
     double innerRadius = -1;   // getInnerRadius of the decorated shape (< 0: the leaf's)
 };
+// CompoundShape (compound.ts): convex children at poses in the compound's frame; the compound's
+// com, aabb and mass come from them (computeCompoundCenterOfMass :110-141, computeCompound-
+// LocalBounds :70-108, computeMassProperties :177-230)
+struct CompoundData {
+    std::vector<Shape> shapes;
+    std::vector<V3> pos;
+    std::vector<Q4> rot;
+    int subBits = 0;      // the bits subShape.pushIndex gives a child index of shapes.size()
+    double innerRadius = 0;  // getInnerRadius :283-289: the least of the children's
+    double mass = 0, inertia[9] = {};  // about the compound's centre of mass, row-major
+};
+// subShape.pushIndex (sub-shape.ts:60-64) of child i onto an empty id: the index in the low
+// subBits bits, ones above
+inline uint32_t compound_sub_id(const CompoundData &c, int i) {
+    if (c.subBits >= 32) return (uint32_t)i;
+    return (0xffffffffu & ~((1u << c.subBits) - 1u)) | (uint32_t)i;
+}
+// child i of a compound at (p, q): the child's world pose (the accumulated transform of
+// collideCompoundVsShape :520-526)
+inline void compound_child_pose(const CompoundData &c, int i, V3 p, Q4 q, V3 &cp, Q4 &cq) {
+    cp = add(p, rotate(q, c.pos[i]));
+    cq = qmul(q, c.rot[i]);
+}
+
 // the pose of a shape's collision geometry for a body at (p, q)
 inline void geometry_pose(const Shape &s, V3 p, Q4 q, V3 &gp, Q4 &gq) {
     if (!s.decorated) {
@@ -2559,6 +2585,26 @@ inline bool ray_triangle(V3 o, V3 d, double length, V3 a, V3 b, V3 c, bool cullB
 // triangle-mesh.ts): the closest hit below maxFraction, its sub-shape id
 inline bool cast_ray_vs_shape(const Shape &s, V3 pos, Q4 q, V3 origin, V3 dir, double length, bool solid,
                               double maxFraction, double &fraction, uint32_t &subId) {
+    if (s.type == SHAPE_COMPOUND) {  // castRayVsCompound compound.ts:350-421: each child, the closest
+        const CompoundData &C = *s.compound;
+        double best = maxFraction;
+        bool found = false;
+        for (int i = 0; i < (int)C.shapes.size(); i++) {
+            if (best <= 0) break;
+            V3 cp;
+            Q4 cq;
+            compound_child_pose(C, i, pos, q, cp, cq);
+            double f;
+            uint32_t sub;
+            if (cast_ray_vs_shape(C.shapes[i], cp, cq, origin, dir, length, solid, best, f, sub) && f < best) {
+                best = f;
+                found = true;
+                subId = compound_sub_id(C, i);
+            }
+        }
+        if (found) fraction = best;
+        return found;
+    }
     Q4 iq = qconj(q);
     V3 lo = rotate(iq, sub(origin, pos)), ld = rotate(iq, dir);
     if (s.type == SHAPE_TRIANGLE_MESH) {
@@ -2706,6 +2752,20 @@ inline bool box_contains(const Box3 &b, V3 p) {  // box3.containsPoint
 inline bool point_in_shape(const Shape &s, V3 pos, Q4 q, V3 point, double tol, uint32_t &subId) {
     subId = EMPTY_SUB_SHAPE_ID;
     if (s.type == SHAPE_EMPTY) return false;
+    if (s.type == SHAPE_COMPOUND) {  // collidePointVsCompound compound.ts:423-492: the first child
+        const CompoundData &C = *s.compound;
+        for (int i = 0; i < (int)C.shapes.size(); i++) {
+            V3 cp;
+            Q4 cq;
+            compound_child_pose(C, i, pos, q, cp, cq);
+            uint32_t sub;
+            if (point_in_shape(C.shapes[i], cp, cq, point, tol, sub)) {
+                subId = compound_sub_id(C, i);
+                return true;
+            }
+        }
+        return false;
+    }
     if (s.type == SHAPE_PLANE) return point_in_plane(s, pos, q, point);
     V3 l = sub(point, pos);
     if (s.type == SHAPE_SPHERE) return dot(l, l) <= s.radius * s.radius;
@@ -2759,6 +2819,25 @@ inline bool collide_shapes(Hit &hit, const CollideSettings &cs, const Shape &sa,
 
 inline void collide_hits(std::vector<Hit> &out, const CollideSettings &cs, const Shape &sa, V3 pA, Q4 qA,
                          const Shape &sb, V3 pB, Q4 qB, V3 movement) {
+    if (sa.type == SHAPE_COMPOUND || sb.type == SHAPE_COMPOUND) {
+        // collideCompoundVsShape / collideShapeVsCompound compound.ts:494-678: each child in turn
+        // (A's first when both are compounds), its sub-shape id pushed onto the hits
+        const bool onA = sa.type == SHAPE_COMPOUND;
+        const CompoundData &C = *(onA ? sa : sb).compound;
+        for (int i = 0; i < (int)C.shapes.size(); i++) {
+            V3 cp;
+            Q4 cq;
+            compound_child_pose(C, i, onA ? pA : pB, onA ? qA : qB, cp, cq);
+            const size_t first = out.size();
+            if (onA)
+                collide_hits(out, cs, C.shapes[i], cp, cq, sb, pB, qB, movement);
+            else
+                collide_hits(out, cs, sa, pA, qA, C.shapes[i], cp, cq, movement);
+            const uint32_t id = compound_sub_id(C, i);
+            for (size_t k = first; k < out.size(); k++) (onA ? out[k].subA : out[k].subB) = id;
+        }
+        return;
+    }
     const bool ma = sa.type == SHAPE_TRIANGLE_MESH, mb = sb.type == SHAPE_TRIANGLE_MESH;
     if (ma && mb) return;
     if (sa.type == SHAPE_EMPTY || sb.type == SHAPE_EMPTY) return;  // empty-shape.ts: registers nothing

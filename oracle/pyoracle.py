@@ -51,6 +51,7 @@ def load():
         "orc_collide_points": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double, ip, ip, vp], None),
         "orc_cast_shapes": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, dp, ip, vp], i32),
         "orc_cast_rays": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, i32, dp, ip, vp], None),
+        "orc_add_compound": ([vp, dp, i32], i32),
         "orc_cast_rays_all": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, i32, i32, dp, ip, vp, ip], None),
         "orc_cast_shapes_all": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, i32, dp, ip, vp, ip], i32),
         "orc_collide_shapes_all": ([vp, dp, i32, C.c_uint32, C.c_uint32, C.c_uint32, dp, i32, dp, ip, vp, ip],
@@ -162,9 +163,10 @@ def settings_array(ws) -> np.ndarray:
 class OracleWorld:
     """One oracle world built from the same bodies and settings as a GPU world."""
 
-    def __init__(self, ws, bodies: np.ndarray, hulls=(), meshes=()):
+    def __init__(self, ws, bodies: np.ndarray, hulls=(), meshes=(), compounds=()):
         """hulls / meshes: convex hull and triangle mesh records as GpuWorld.get_convex_hull /
-        get_triangle_mesh return them, in index order (the bodies name them by index)."""
+        get_triangle_mesh return them, in index order (the bodies name them by index);
+        compounds: arrays of _lib.COMPOUND_CHILD_DTYPE records, in index order."""
         lib = load()
         self.lib = lib
         L = ws.layers
@@ -189,9 +191,24 @@ class OracleWorld:
             self.add_hull(h)
         for m in meshes:
             self.add_mesh(m)
+        for c in compounds:
+            self.add_compound(c)
         rows = rows_from_bodies(bodies)
         assert lib.orc_add_bodies(self.h, dptr(rows), len(rows)) == 0
         self.n = len(rows)
+
+    def add_compound(self, children) -> int:
+        """A compound shape from child records (shape_type, shape_params, position, quaternion,
+        density); returns its index."""
+        rows = np.zeros((len(children), 13), dtype=np.float64)
+        rows[:, 0] = children["shape_type"]
+        rows[:, 1:5] = children["shape_params"]
+        rows[:, 5:8] = children["position"]
+        rows[:, 8:12] = children["quaternion"]
+        rows[:, 12] = children["density"]
+        k = self.lib.orc_add_compound(self.h, dptr(rows), len(rows))
+        assert k >= 0, "orc_add_compound: children must be convex shapes of this world"
+        return k
 
     def add_mesh(self, m) -> int:
         v = np.ascontiguousarray(m["vertices"], dtype=np.float64)
