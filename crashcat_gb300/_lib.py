@@ -217,6 +217,7 @@ EXPORTS = {
     "cc_world_cast_shapes": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
     "cc_world_cast_shapes_device": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
     "cc_world_cast_rays": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
+    "cc_world_add_compound": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
     "cc_world_cast_rays_collect": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32,
                                     C.c_void_p, C.c_void_p], C.c_int),
     "cc_world_cast_shapes_collect": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32,

@@ -29,16 +29,22 @@ enum : uint32_t {
     F_LAYER_SHIFT = 21,          // bits 21-25 object layer
     F_LINEAR_CAST = 1u << 26,    // MotionQuality.LINEAR_CAST
     F_DECORATED = 1u << 27,      // the shape has decorators (DevWorld::frames)
+    F_SHAPE_HI = 1u << 28,       // the shape type's fourth bit
 };
 __host__ __device__ inline int motion_of(uint32_t f) { return (int)(f & F_MOTION_MASK); }
-__host__ __device__ inline int shape_of(uint32_t f) { return (int)((f >> F_SHAPE_SHIFT) & 7u); }
+__host__ __device__ inline int shape_of(uint32_t f) { return (int)(((f >> F_SHAPE_SHIFT) & 7u) | ((f >> 25) & 8u)); }
+// the flag bits of a shape type (bits 6-8 and 28)
+__host__ __device__ inline uint32_t shape_bits(int shape) {
+    return ((uint32_t)(shape & 7) << F_SHAPE_SHIFT) | ((uint32_t)(shape & 8) << 25);
+}
 __host__ __device__ inline int dof_of(uint32_t f) { return (int)((f >> F_DOF_SHIFT) & 63u); }
 __host__ __device__ inline int layer_of(uint32_t f) { return (int)((f >> F_LAYER_SHIFT) & 31u); }
 __host__ __device__ inline bool sleeping_of(uint32_t f) { return (f & F_SLEEPING) != 0; }
 
 constexpr int STATIC = 0, KINEMATIC = 1, DYNAMIC = 2;
 constexpr int SHAPE_SPHERE = 0, SHAPE_BOX = 1, SHAPE_CAPSULE = 2, SHAPE_HULL = 3, SHAPE_MESH = 4, SHAPE_CYLINDER = 5,
-              SHAPE_PLANE = 6, SHAPE_EMPTY = 7;  // an empty shape (empty-shape.ts) collides with nothing
+              SHAPE_PLANE = 6, SHAPE_EMPTY = 7,  // an empty shape (empty-shape.ts) collides with nothing
+              SHAPE_COMPOUND = 8;
 
 // Per-step overflow flags (status bits in DevCounters::overflow)
 enum : int { OVF_PAIRS = 1, OVF_MANIFOLDS = 2, OVF_EPA = 4, OVF_ISLAND = 8, OVF_CACHE = 16, OVF_SLOTS = 32,
@@ -75,6 +81,8 @@ struct DevCounters {
     int num_mesh_hits;    // triangle hits reported to the mesh pairs' reduction
     int mesh_reduced;     // mesh pairs whose hits needed more manifolds than the reference's pool of 32
     int num_mesh_big;     // mesh pairs run again with the 32-manifold pool (their hits overflowed 4)
+    int num_compound_pairs;  // broadphase pairs with a compound body and no mesh
+    int pad2[3];
 };
 
 // Settings copied into constant memory once per world.
@@ -404,6 +412,16 @@ struct CcdRec {
     int pad[2];
 };
 
+// a compound shape: its children's range and the bits of a child index in a sub-shape id
+struct DevCompound {
+    int first, count, sub_bits, pad;
+};
+// one child: its shape record (as a body's; a hull's index as int bits), its pose in the
+// compound's frame, its shape type (int bits in pos.w)
+struct DevChild {
+    float4 params, pos, quat;
+};
+
 struct DevWorld {
     int n;          // bodies in use
     int cap;        // body capacity
@@ -530,6 +548,12 @@ struct DevWorld {
     int *mesh_epa_base;   // per mesh pair: its first EPA item, -1 when it needs none
     int *mesh_epa_count;  // per mesh pair: its EPA items
     int *mesh_big;        // mesh pairs handed to the 32-manifold pass this step
+    // compound shapes (compound.ts): per compound its children's range, per child its shape
+    struct DevCompound *compounds;
+    struct DevChild *children;
+    int num_compounds;
+    int num_compound_bodies;
+    int *compound_pairs;  // pairs with a compound body and no mesh this step (index into pairs)
     void *mesh_big_red;   // MESH_BIG_THREADS reduction slots of 32 manifolds
     // continuous collision (LINEAR_CAST bodies, update.ts:896-1670)
     int num_linear_cast;  // bodies with LINEAR_CAST motion quality (0: the single-pass solve)
@@ -546,6 +570,16 @@ struct DevWorld {
 
 // the mesh index of a mesh body's shape record (same int-bits encoding as hull_of)
 __host__ __device__ inline int mesh_of(float4 sp) {
+#ifdef __CUDA_ARCH__
+    return __float_as_int(sp.x);
+#else
+    int v;
+    memcpy(&v, &sp.x, sizeof(int));
+    return v;
+#endif
+}
+// the compound index of a compound body's shape record (the same int-bits encoding)
+__host__ __device__ inline int compound_of(float4 sp) {
 #ifdef __CUDA_ARCH__
     return __float_as_int(sp.x);
 #else

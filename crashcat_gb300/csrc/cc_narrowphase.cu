@@ -1130,6 +1130,13 @@ __global__ void __launch_bounds__(128) k_narrowphase(DevWorld w, EpaItem *epa_it
             }
             continue;
         }
+        if (sha == SHAPE_COMPOUND || shb == SHAPE_COMPOUND) {  // the compound pass takes these pairs
+            if (!HULLS) {
+                const int k = atomicAdd(&w.ctr->num_compound_pairs, 1);
+                if (k < w.max_pairs) w.compound_pairs[k] = pi;
+            }
+            continue;
+        }
         if ((sha == SHAPE_HULL || shb == SHAPE_HULL) != HULLS) continue;
         if (sha == SHAPE_PLANE || shb == SHAPE_PLANE) {
             // collideConvexVsPlane plane.ts:474-629, reversed when the plane is A (the usual case:
@@ -2067,6 +2074,35 @@ __device__ void epa_setup(const DevWorld &w, const EpaItem &it, Sup<R, H> &A, Su
     set_transform(B, rel, posBInA);
 }
 
+// a body's convex sub-shapes: a compound's children at their composed poses, or its own shape
+struct SubShape {
+    int shape;
+    float4 sp;
+    float3 pos;
+    float4 quat;
+    uint32_t sub;  // subShape.pushIndex of the child index, 0xffffffff for a body's own shape
+};
+__device__ __forceinline__ int sub_count(const DevWorld &w, int b, uint32_t f) {
+    return shape_of(f) == SHAPE_COMPOUND ? w.compounds[compound_of(w.shape[b])].count : 1;
+}
+__device__ SubShape sub_shape(const DevWorld &w, int b, uint32_t f, int i) {
+    SubShape s;
+    geom_pose(w, b, f, s.pos, s.quat);
+    if (shape_of(f) != SHAPE_COMPOUND) {
+        s.shape = shape_of(f);
+        s.sp = w.shape[b];
+        s.sub = 0xffffffffu;
+        return s;
+    }
+    const DevCompound &C = w.compounds[compound_of(w.shape[b])];
+    const DevChild ch = w.children[C.first + i];
+    s.shape = __float_as_int(ch.pos.w);
+    s.sp = ch.params;
+    s.pos = s.pos + qrot(s.quat, xyz(ch.pos));  // the accumulated transform :520-526
+    s.quat = qmul(s.quat, ch.quat);
+    s.sub = C.sub_bits >= 32 ? (uint32_t)i : ((0xffffffffu & ~((1u << C.sub_bits) - 1u)) | (uint32_t)i);
+    return s;
+}
 // a mesh triangle's EPA (collideConvexVsTriangleMesh triangle-mesh.ts:1226-1247): A the convex
 // body with its radius and the separation, B the triangle's vertices in A's frame
 __device__ void epa_setup_mesh(const DevWorld &w, const EpaItem &it, Sup<R> &A, Sup<R, true, true> &B, R &maxSep) {
@@ -2074,16 +2110,20 @@ __device__ void epa_setup_mesh(const DevWorld &w, const EpaItem &it, Sup<R> &A, 
     uint32_t fa = w.flags[a], fb = w.flags[b];
     float maxSepF = ((fa | fb) & F_SENSOR) ? 0.f : c_settings.spec_dist;
     maxSep = R(maxSepF < 1.f ? maxSepF : 1.f);
-    float3 pa4, pb4;
-    float4 qa, qb;
-    geom_pose(w, a, fa, pa4, qa);
+    // the convex side: the body's shape, or a compound's child (its index above bit 24)
+    const int ti = it.tri & 0xffffff, ci = (it.tri >> 24) - 1;
+    const SubShape cs = sub_shape(w, a, fa, ci >= 0 ? ci : 0);
+    float3 pb4;
+    float4 qb;
+    const float3 pa4 = cs.pos;
+    const float4 qa = cs.quat;
     geom_pose(w, b, fb, pb4, qb);
     Q<R> iA{R(-qa.x), R(-qa.y), R(-qa.z), R(qa.w)};
     Q<R> rel = qmulS(iA, Q<R>{R(qb.x), R(qb.y), R(qb.z), R(qb.w)});
     V<R> posBInA = qrotS(iA, V<R>{R(pb4.x) - R(pa4.x), R(pb4.y) - R(pa4.y), R(pb4.z) - R(pa4.z)});
-    A = make_sup<R>(shape_of(fa), w.shape[a], false, hull_view(w));
+    A = make_sup<R>(cs.shape, cs.sp, false, hull_view(w));
     A.add_r = maxSep;
-    const int4 t = w.mesh_tris[w.meshes[mesh_of(w.shape[b])].first_tri + it.tri];
+    const int4 t = w.mesh_tris[w.meshes[mesh_of(w.shape[b])].first_tri + ti];
     const int vi[3] = {t.x, t.y, t.z};
     V<R> v[3];
     for (int k = 0; k < 3; k++) {
@@ -2529,56 +2569,19 @@ __device__ void mesh_pair(DevWorld &w, EpaItem *epa_items, int k, MeshReduceT<M>
         // (reversedCollideShapeVsShape collide-shape-vs-shape.ts:227-354)
         const bool inverted = meshA;
         const int cv = inverted ? b : a, mh = inverted ? a : b;
-        const uint32_t fc = inverted ? fb : fa;
-        float3 base, pc, pm;
-        float4 qbase, qc4, qm4;
+        const uint32_t fcb = inverted ? fb : fa;  // the convex body's flags
+        float3 base, pm;
+        float4 qbase, qm4;
         geom_pose(w, a, fa, base, qbase);
         const float maxSepIn = ((fa | fb) & F_SENSOR) ? 0.f : c_settings.spec_dist;
-        geom_pose(w, cv, w.flags[cv], pc, qc4);
         geom_pose(w, mh, w.flags[mh], pm, qm4);
-        const float3 cvRel = pc - base;  // the convex body's position relative to the base
-        const Q<float> qC{qc4.x, qc4.y, qc4.z, qc4.w}, iqC{-qc4.x, -qc4.y, -qc4.z, qc4.w};
         const Q<float> qM{qm4.x, qm4.y, qm4.z, qm4.w}, iqM{-qm4.x, -qm4.y, -qm4.z, qm4.w};
-        // mesh into the convex body's frame, and the convex body into the mesh's frame
-        const Q<float> m2c = qmulS(iqC, qM);
-        const V<float> m2cPos = qrotS(iqC, V<float>{pm.x - pc.x, pm.y - pc.y, pm.z - pc.z});
-        const Q<float> cInM = qmulS(iqM, qC);
-        const V<float> cInMPos = qrotS(iqM, V<float>{pc.x - pm.x, pc.y - pm.y, pc.z - pm.z});
         const DevMesh &M = w.meshes[mesh_of(w.shape[mh])];
-        const float4 sc = w.shape[cv];
-        const bool sphere = shape_of(fc) == SHAPE_SPHERE;
         // activeEdgeMovementDirection: A's velocity minus B's in the narrowphase order (update.ts:729-733)
         const float3 moveW = xyz(w.linvel[a]) - xyz(w.linvel[b]);
-        // query bounds in the mesh frame and the traversal's reference point
-        float3 qlo, qhi, qcenter, blo1, bhi1;
-        V<float> sphereC{0.f, 0.f, 0.f};
-        if (sphere) {
-            sphereC = cInMPos;
-            const float er = sc.x + maxSepIn;
-            qlo = f3(sphereC.x - er, sphereC.y - er, sphereC.z - er);
-            qhi = f3(sphereC.x + er, sphereC.y + er, sphereC.z + er);
-            qcenter = f3(sphereC.x, sphereC.y, sphereC.z);
-        } else {
-            float3 llo, lhi;
-            convex_local_bounds(w, fc, sc, llo, lhi);
-            blo1 = llo - f3(maxSepIn, maxSepIn, maxSepIn);
-            bhi1 = lhi + f3(maxSepIn, maxSepIn, maxSepIn);
-            // box3.transformMat4 of the local bounds (8 corners), grown by the separation
-            qlo = f3(3.0e38f, 3.0e38f, 3.0e38f);
-            qhi = f3(-3.0e38f, -3.0e38f, -3.0e38f);
-            for (int c = 0; c < 8; c++) {
-                V<float> p{(c & 1) ? lhi.x : llo.x, (c & 2) ? lhi.y : llo.y, (c & 4) ? lhi.z : llo.z};
-                V<float> q = qrotS(cInM, p) + cInMPos;
-                qlo = f3(fminf(qlo.x, q.x), fminf(qlo.y, q.y), fminf(qlo.z, q.z));
-                qhi = f3(fmaxf(qhi.x, q.x), fmaxf(qhi.y, q.y), fmaxf(qhi.z, q.z));
-            }
-            qlo = qlo - f3(maxSepIn, maxSepIn, maxSepIn);
-            qhi = qhi + f3(maxSepIn, maxSepIn, maxSepIn);
-            qcenter = (qlo + qhi) * 0.5f;
-        }
-        const HullView hv = hull_view(w);
-        Sup<float> supA;
-        if (!sphere) supA = make_sup<float>(shape_of(fc), sc, true, hv);
+        // a compound collides child by child (collideCompoundVsShape compound.ts:494-578)
+        const bool compound = shape_of(fcb) == SHAPE_COMPOUND;
+        const int ncv = sub_count(w, cv, fcb);
         red.nm = 0;
         red.dropped = false;
         int epa_needed = 0, epa_next = 0;
@@ -2607,6 +2610,50 @@ __device__ void mesh_pair(DevWorld &w, EpaItem *epa_items, int k, MeshReduceT<M>
                 w.mesh_epa_count[k] = epa_needed;
                 epa_next = 0;
             }
+            for (int ci = 0; ci < ncv; ci++) {
+            const SubShape csub = sub_shape(w, cv, fcb, ci);
+            const uint32_t fc = shape_bits(csub.shape);
+            const float3 pc = csub.pos;
+            const float4 qc4 = csub.quat;
+            const float3 cvRel = pc - base;  // the convex shape's position relative to the base
+            const Q<float> qC{qc4.x, qc4.y, qc4.z, qc4.w}, iqC{-qc4.x, -qc4.y, -qc4.z, qc4.w};
+            // mesh into the convex shape's frame, and the convex shape into the mesh's frame
+            const Q<float> m2c = qmulS(iqC, qM);
+            const V<float> m2cPos = qrotS(iqC, V<float>{pm.x - pc.x, pm.y - pc.y, pm.z - pc.z});
+            const Q<float> cInM = qmulS(iqM, qC);
+            const V<float> cInMPos = qrotS(iqM, V<float>{pc.x - pm.x, pc.y - pm.y, pc.z - pm.z});
+            const float4 sc = csub.sp;
+            const bool sphere = csub.shape == SHAPE_SPHERE;
+            // query bounds in the mesh frame and the traversal's reference point
+            float3 qlo, qhi, qcenter, blo1, bhi1;
+            V<float> sphereC{0.f, 0.f, 0.f};
+            if (sphere) {
+                sphereC = cInMPos;
+                const float er = sc.x + maxSepIn;
+                qlo = f3(sphereC.x - er, sphereC.y - er, sphereC.z - er);
+                qhi = f3(sphereC.x + er, sphereC.y + er, sphereC.z + er);
+                qcenter = f3(sphereC.x, sphereC.y, sphereC.z);
+            } else {
+                float3 llo, lhi;
+                convex_local_bounds(w, fc, sc, llo, lhi);
+                blo1 = llo - f3(maxSepIn, maxSepIn, maxSepIn);
+                bhi1 = lhi + f3(maxSepIn, maxSepIn, maxSepIn);
+                // box3.transformMat4 of the local bounds (8 corners), grown by the separation
+                qlo = f3(3.0e38f, 3.0e38f, 3.0e38f);
+                qhi = f3(-3.0e38f, -3.0e38f, -3.0e38f);
+                for (int c = 0; c < 8; c++) {
+                    V<float> p{(c & 1) ? lhi.x : llo.x, (c & 2) ? lhi.y : llo.y, (c & 4) ? lhi.z : llo.z};
+                    V<float> q = qrotS(cInM, p) + cInMPos;
+                    qlo = f3(fminf(qlo.x, q.x), fminf(qlo.y, q.y), fminf(qlo.z, q.z));
+                    qhi = f3(fmaxf(qhi.x, q.x), fmaxf(qhi.y, q.y), fmaxf(qhi.z, q.z));
+                }
+                qlo = qlo - f3(maxSepIn, maxSepIn, maxSepIn);
+                qhi = qhi + f3(maxSepIn, maxSepIn, maxSepIn);
+                qcenter = (qlo + qhi) * 0.5f;
+            }
+            const HullView hv = hull_view(w);
+            Sup<float> supA;
+            if (!sphere) supA = make_sup<float>(shape_of(fc), sc, true, hv);
             int stack[MESH_STACK];
             int sp = 0;
             stack[sp++] = 0;
@@ -2725,7 +2772,7 @@ __device__ void mesh_pair(DevWorld &w, EpaItem *epa_items, int k, MeshReduceT<M>
                                 EpaItem it;
                                 it.a = cv;
                                 it.b = mh;
-                                it.tri = ti;
+                                it.tri = compound ? (ti | ((ci + 1) << 24)) : ti;  // a child's: its index above bit 24
                                 it.size = sx.size;
                                 it.pad = 0;
                                 for (int q = 0; q < 4; q++) {
@@ -2785,11 +2832,12 @@ __device__ void mesh_pair(DevWorld &w, EpaItem *epa_items, int k, MeshReduceT<M>
                     }
                     if (PASS != 2) atomicAdd(&w.ctr->num_mesh_hits, 1);
                     if (inverted)  // the inverted collector: points, axis, sub-shape ids and faces swapped
-                        mesh_add_hit(red, hpb, hpa, -hax, hpen, tsub, 0xffffffffu, fTri, fConvex);
+                        mesh_add_hit(red, hpb, hpa, -hax, hpen, tsub, csub.sub, fTri, fConvex);
                     else
-                        mesh_add_hit(red, hpa, hpb, hax, hpen, 0xffffffffu, tsub, fConvex, fTri);
+                        mesh_add_hit(red, hpa, hpb, hax, hpen, csub.sub, tsub, fConvex, fTri);
                 }
             }
+            }  // children
         }
         if (PASS == 0 && epa_needed > 0) return;  // finished by the second pass
         if (PASS != 2 && red.dropped && w.mesh_big) {  // the pool overflowed: the 32-manifold pass takes it
@@ -2820,6 +2868,173 @@ __global__ void __launch_bounds__(64) k_mesh_big(DevWorld w, EpaItem *epa_items)
     for (int j = tid; j < nbig; j += gridDim.x * blockDim.x) mesh_pair<2, MESH_BIG_M>(w, epa_items, w.mesh_big[j], red);
 }
 
+
+// ---------------------------------------------------------------------------
+// compound pairs (compound.ts collideCompoundVsShape / collideShapeVsCompound :494-678): the
+// sub-shapes of each body (a compound's children at their composed poses, or the body's own
+// convex shape) collided pairwise, A's first, every hit into the reduction pool
+// ---------------------------------------------------------------------------
+// the supporting face of a convex sub-shape along a world direction, relative to the base
+template <int N>
+__device__ void sub_face(FaceN<N> &f, const DevWorld &w, const SubShape &s, float3 dir, float3 base) {
+    const float3 d = qrot_inv(s.quat, dir), t = s.pos - base;
+    if (s.shape == SHAPE_BOX) box_face(f, d, s.sp, s.quat, t);
+    if (s.shape == SHAPE_CAPSULE) capsule_face(f, d, s.sp, s.quat, t);
+    if (s.shape == SHAPE_HULL) hull_face(f, d, w, s.sp, s.quat, t);
+    if (s.shape == SHAPE_CYLINDER) cylinder_face(f, d, s.sp, s.quat, t);
+}
+// collideShapeVsShape (narrowphase.ts:172-238) of two sub-shapes, one of them possibly a plane:
+// the hit, relative to the base, with both supporting faces into the pool (EPA in FP64 on the
+// thread's polytope, from the FP32 GJK simplex as the narrowphase's EPA starts)
+template <int M>
+__device__ void collide_sub(const DevWorld &w, const HullView &hv, EpaScratch *slot, const SubShape &A,
+                            const SubShape &B, float maxSep, float3 base, MeshReduceT<M> &red) {
+    if (A.shape == SHAPE_EMPTY || B.shape == SHAPE_EMPTY) return;
+    if (A.shape == SHAPE_PLANE && B.shape == SHAPE_PLANE) return;
+    FaceN<32> fA, fB;
+    fA.n = fB.n = 0;
+    float3 pa, pb, ax;
+    float pen;
+    if (A.shape == SHAPE_PLANE || B.shape == SHAPE_PLANE) {  // collideConvexVsPlane plane.ts:474-629
+        const bool planeA = A.shape == SHAPE_PLANE;
+        const SubShape &Cv = planeA ? B : A, &P = planeA ? A : B;
+        const float3 nl = qrot_inv(Cv.quat, qrot(P.quat, xyz(P.sp)));
+        const float cl = P.sp.w - dot3(qrot_inv(Cv.quat, P.pos - Cv.pos), nl);
+        const Sup<float> S = make_sup<float>(Cv.shape, Cv.sp, default_excludes(Cv.shape), hv);
+        const V<float> spv = S.get(V<float>{-nl.x, -nl.y, -nl.z});
+        const float3 sp3 = f3(spv.x, spv.y, spv.z);
+        const float sd = dot3(nl, sp3) + cl, cr = S.convex_radius;
+        pen = -sd + cr;
+        if (!(pen > -maxSep)) return;
+        const float3 p1 = Cv.pos + qrot(Cv.quat, sp3 - nl * cr), p2 = Cv.pos + qrot(Cv.quat, sp3 - nl * sd);
+        const float3 axc = qrot(Cv.quat, -nl);  // from the convex shape into the plane
+        pa = planeA ? p2 : p1;
+        pb = planeA ? p1 : p2;
+        ax = planeA ? -axc : axc;
+        // the convex face, then the plane's square under it (plane.ts:588-606)
+        float3 llo, lhi;
+        convex_local_bounds(w, shape_bits(Cv.shape), Cv.sp, llo, lhi);
+        const float size = sqrtf(lensq3(lhi - llo));
+        float3 nw;
+        float cw;
+        plane_world(P.sp, P.pos, P.quat, nw, cw);
+        if (planeA) {
+            sub_face(fB, w, B, ax, base);
+            if (fB.n > 0) plane_face(fA, nw, cw, B.pos, size, base);
+        } else {
+            sub_face(fA, w, A, -ax, base);
+            if (fA.n > 0) plane_face(fB, nw, cw, A.pos, size, base);
+        }
+    } else if (A.shape == SHAPE_SPHERE && B.shape == SHAPE_SPHERE) {  // collideSphereVsSphere sphere.ts:319-410
+        const float3 d = B.pos - A.pos;
+        const float dsq = lensq3(d), rs = A.sp.x + B.sp.x;
+        if (dsq >= rs * rs) return;
+        const float dist = sqrtf(dsq);
+        const float3 nn = dist > 0.f ? d * (1.f / dist) : f3(0.f, 1.f, 0.f);
+        pa = A.pos + nn * A.sp.x;
+        pb = B.pos - nn * B.sp.x;
+        ax = nn;
+        pen = rs - dist;
+    } else {  // collideConvexVsConvex convex.ts:257-641: B in A's frame
+        const Q<float> qA{A.quat.x, A.quat.y, A.quat.z, A.quat.w}, iA{-A.quat.x, -A.quat.y, -A.quat.z, A.quat.w};
+        const Q<float> rel = qmulS(iA, Q<float>{B.quat.x, B.quat.y, B.quat.z, B.quat.w});
+        const V<float> posBInA = qrotS(iA, V<float>{B.pos.x - A.pos.x, B.pos.y - A.pos.y, B.pos.z - A.pos.z});
+        const Sup<float> supA = make_sup<float>(A.shape, A.sp, true, hv);
+        Sup<float> supB = make_sup<float>(B.shape, B.sp, true, hv);
+        set_transform(supB, rel, posBInA);
+        V<float> axis = posBInA;
+        if (lsq(axis) <= 1e-12f) axis = {1.f, 0.f, 0.f};
+        const float rA = supA.convex_radius + maxSep, rB = supB.convex_radius, cr = rA + rB;
+        Simplex<float> sx;
+        const GjkOut<float> g = gjk(supA, supB, c_settings.collision_tol, axis, cr * cr, sx);
+        if (g.sqdist > cr * cr) return;  // NOT_COLLIDING
+        V<float> lpa, lpb, lax;
+        if (!(g.sqdist > 0.f)) {  // INDETERMINATE: EPA in FP64 with the separation clamped to 1
+            const R msE = R(fminf(maxSep, 1.f));
+            const Q<R> iAr{R(iA.x), R(iA.y), R(iA.z), R(iA.w)};
+            Sup<R> EA = make_sup<R>(A.shape, A.sp, false, hv);
+            EA.add_r = msE;
+            Sup<R> EB = make_sup<R>(B.shape, B.sp, false, hv);
+            set_transform(EB, qmulS(iAr, Q<R>{R(B.quat.x), R(B.quat.y), R(B.quat.z), R(B.quat.w)}),
+                          qrotS(iAr, V<R>{R(B.pos.x) - R(A.pos.x), R(B.pos.y) - R(A.pos.y), R(B.pos.z) - R(A.pos.z)}));
+            EpaItem it;
+            it.a = it.b = 0;
+            it.size = sx.size;
+            it.pad = 0;
+            it.tri = -1;
+            for (int k = 0; k < 4; k++) {
+                SP<float> sp = sx.pts[k < sx.size ? k : 0];
+                it.y[k] = f3(sp.y.x, sp.y.y, sp.y.z);
+                it.p[k] = f3(sp.p.x, sp.p.y, sp.p.z);
+                it.q[k] = f3(sp.q.x, sp.q.y, sp.q.z);
+            }
+            Hull<BigStore> h;
+            h.st.s = slot;
+            h.start(it);
+            V<R> eax, ea, eb;
+            if (!epa(h, EA, EB, R(c_settings.penetration_tol), eax, ea, eb)) return;  // convex.ts:331
+            const V<R> dd = ea - eb;
+            const R al = sq_root(lsq(eax));
+            pen = (float)(sq_root(lsq(dd)) - msE);
+            if (al > R(0)) ea = ea + eax * (-(msE / al));
+            lpa = V<float>{(float)ea.x, (float)ea.y, (float)ea.z};
+            lpb = V<float>{(float)eb.x, (float)eb.y, (float)eb.z};
+            lax = V<float>{(float)eax.x, (float)eax.y, (float)eax.z};
+        } else {  // COLLIDING: penetrationDepthStepGJK penetration.ts:84-106
+            const float vl = sqrtf(g.sqdist);
+            lpa = g.pa + g.axis * (rA / vl);
+            lpb = g.pb + g.axis * (-(rB / vl));
+            const V<float> dd = lpa - lpb;
+            pen = sqrtf(lsq(dd)) - maxSep;
+            const float al = sqrtf(lsq(g.axis));
+            if (al > 0.f) lpa = lpa + g.axis * (-(maxSep / al));
+            lax = g.axis;
+        }
+        const V<float> paw = qrotS(qA, lpa), pbw = qrotS(qA, lpb), axw = qrotS(qA, lax);
+        pa = A.pos + f3(paw.x, paw.y, paw.z);
+        pb = A.pos + f3(pbw.x, pbw.y, pbw.z);
+        ax = f3(axw.x, axw.y, axw.z);
+        sub_face(fA, w, A, -ax, base);
+        sub_face(fB, w, B, ax, base);
+    }
+    mesh_add_hit(red, pa - base, pb - base, ax, pen, A.sub, B.sub, fA, fB);
+}
+
+// one compound pair per thread, the reduction pool of 32 manifolds and an EPA polytope in global
+// memory (the mesh passes' slots, used at another time of the step)
+__global__ void __launch_bounds__(64) k_compound_pairs(DevWorld w) {
+    const int np = min(w.ctr->num_compound_pairs, w.max_pairs);
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    MeshReduceT<MESH_BIG_M> &red = ((MeshReduceT<MESH_BIG_M> *)w.mesh_big_red)[tid];
+    EpaScratch *slot = (EpaScratch *)w.epa_scratch + tid;
+    const HullView hv = hull_view(w);
+    for (int k = tid; k < np; k += gridDim.x * blockDim.x) {
+        int2 pr = w.pairs[w.compound_pairs[k]];
+        int a = pr.x, b = pr.y;
+        uint32_t fa = w.flags[a], fb = w.flags[b];
+        const int ma = motion_of(fa), mb = motion_of(fb);
+        if (ma > mb || (ma == mb && b < a)) {  // narrowphase order (update.ts:74)
+            const int t = a;
+            a = b;
+            b = t;
+            const uint32_t tf = fa;
+            fa = fb;
+            fb = tf;
+        }
+        const float maxSep = ((fa | fb) & F_SENSOR) ? 0.f : c_settings.spec_dist;
+        float3 base;
+        float4 qbase;
+        geom_pose(w, a, fa, base, qbase);
+        red.nm = 0;
+        red.dropped = false;
+        const int na = sub_count(w, a, fa), nb = sub_count(w, b, fb);
+        for (int i = 0; i < na; i++) {
+            const SubShape A = sub_shape(w, a, fa, i);
+            for (int j = 0; j < nb; j++) collide_sub(w, hv, slot, A, sub_shape(w, b, fb, j), maxSep, base, red);
+        }
+        mesh_emit(w, red, a, b, base);
+    }
+}
 
 void launch_mesh_narrowphase(DevWorld &w, int pass, cudaStream_t s) {
     EpaItem *items = (EpaItem *)w.epa_items;
@@ -3349,29 +3564,33 @@ __global__ void __launch_bounds__(128) k_ccd_find(DevWorld w, const int2 *node_w
                 if (cast_vs_plane(S, pA, qA, rel, w.shape[b], pB, qB, best_fps, frac, paw, axw)) collect(frac, paw, axw);
                 continue;
             }
-            // castConvexVsConvex: A in B's frame
-            float3 pB;
-            float4 qB;
-            geom_pose(w, b, fb, pB, qB);
-            const Q<float> iqB{-qB.x, -qB.y, -qB.z, qB.w};
-            const V<float> posAInB = qrotS(iqB, V<float>{pA.x - pB.x, pA.y - pB.y, pA.z - pB.z});
-            const Q<float> qAInB = qmulS(iqB, Q<float>{qA.x, qA.y, qA.z, qA.w});
-            const V<float> dInB = qrotS(iqB, V<float>{rel.x, rel.y, rel.z});
-            Sup<float> supA = supA0;
-            set_transform(supA, qAInB, posAInB);
-            const Sup<float> supB = make_sup<float>(shape_of(fb), w.shape[b], true, hv);
-            float lambda;
-            V<float> cpa, cpb, ax;
-            if (!gjk_cast(lambda, cpa, cpb, ax, supA, supB, dInB, 1e-4f, supA.convex_radius, supB.convex_radius,
-                          best_fps))
-                continue;
-            // penetrationCastShape penetration.ts:693-698: a too short axis becomes the cast direction
-            if (lsq(ax) < 1e-4f * 1e-4f) ax = dInB;
-            if (lambda > 1.f || dot(ax, dInB) <= 0.f || lambda >= best_fps) continue;
-            const Q<float> qBq{qB.x, qB.y, qB.z, qB.w};
-            const V<float> axw = qrotS(qBq, ax);
-            const V<float> paw = qrotS(qBq, cpa);
-            collect(lambda, f3(paw.x + pB.x, paw.y + pB.y, paw.z + pB.z), f3(axw.x, axw.y, axw.z));
+            // castConvexVsConvex: A in B's frame; a compound target child by child
+            // (castShapeVsCompound compound.ts:776-866)
+            const int nsub = sub_count(w, b, fb);
+            for (int ci = 0; ci < nsub; ci++) {
+                const SubShape cs = sub_shape(w, b, fb, ci);
+                const float3 pB = cs.pos;
+                const float4 qB = cs.quat;
+                const Q<float> iqB{-qB.x, -qB.y, -qB.z, qB.w};
+                const V<float> posAInB = qrotS(iqB, V<float>{pA.x - pB.x, pA.y - pB.y, pA.z - pB.z});
+                const Q<float> qAInB = qmulS(iqB, Q<float>{qA.x, qA.y, qA.z, qA.w});
+                const V<float> dInB = qrotS(iqB, V<float>{rel.x, rel.y, rel.z});
+                Sup<float> supA = supA0;
+                set_transform(supA, qAInB, posAInB);
+                const Sup<float> supB = make_sup<float>(cs.shape, cs.sp, true, hv);
+                float lambda;
+                V<float> cpa, cpb, ax;
+                if (!gjk_cast(lambda, cpa, cpb, ax, supA, supB, dInB, 1e-4f, supA.convex_radius, supB.convex_radius,
+                              best_fps))
+                    continue;
+                // penetrationCastShape penetration.ts:693-698: a too short axis becomes the cast direction
+                if (lsq(ax) < 1e-4f * 1e-4f) ax = dInB;
+                if (lambda > 1.f || dot(ax, dInB) <= 0.f || lambda >= best_fps) continue;
+                const Q<float> qBq{qB.x, qB.y, qB.z, qB.w};
+                const V<float> axw = qrotS(qBq, ax);
+                const V<float> paw = qrotS(qBq, cpa);
+                collect(lambda, f3(paw.x + pB.x, paw.y + pB.y, paw.z + pB.z), f3(axw.x, axw.y, axw.z));
+            }
         }
         if (best >= 0) {
             c.hit = best;
@@ -3552,6 +3771,21 @@ __device__ bool ray_vs_mesh(const DevWorld &w, int b, float3 o, float3 d, float 
     return found;
 }
 
+// castRayVsConvex convex.ts:54-126 (the INCLUDE_CONVEX_RADIUS support, tolerance 1e-3) of one
+// convex shape at (pB, qB)
+__device__ bool ray_vs_convex(const HullView &hv, int shape, float4 sp, float3 pB, float4 qB, float3 o, float3 d,
+                              float len, uint32_t flags, float max_f, float &fraction) {
+    const float3 lo = qrot_inv(qB, o - pB), ld = qrot_inv(qB, d);
+    const Sup<float> sup = make_sup<float>(shape, sp, false, hv);
+    float lambda;
+    if (!gjk_cast_ray(lambda, V<float>{lo.x, lo.y, lo.z}, V<float>{ld.x * len, ld.y * len, ld.z * len}, 1e-3f, sup,
+                      max_f))
+        return false;
+    if (!((flags & CC_RAY_SOLID) || lambda > 0.f)) return false;
+    fraction = fmaxf(0.f, lambda);
+    return true;
+}
+
 // castRayVsShape for one body (castRayVsConvex convex.ts:54-126 with the INCLUDE_CONVEX_RADIUS
 // support and tolerance 1e-3, or the mesh walk): the hit below max_f and its sub-shape id.
 // MESH selects the triangle-mesh branch, so that each kernel instance holds only one of them.
@@ -3583,15 +3817,24 @@ __device__ bool ray_vs_body(const DevWorld &w, const HullView &hv, int b, float3
         fraction = f;
         return true;
     }
-    const Sup<float> sup = make_sup<float>(shape_of(fb), w.shape[b], false, hv);
-    float lambda;
-    if (!gjk_cast_ray(lambda, V<float>{lo.x, lo.y, lo.z}, V<float>{ld.x * len, ld.y * len, ld.z * len}, 1e-3f, sup,
-                      max_f))
-        return false;
-    if (!((flags & CC_RAY_SOLID) || lambda > 0.f)) return false;
-    fraction = fmaxf(0.f, lambda);
+    if (shape_of(fb) == SHAPE_COMPOUND) {  // castRayVsCompound compound.ts:350-421: the children's closest
+        bool found = false;
+        float best = max_f;
+        const int nc = sub_count(w, b, fb);
+        for (int i = 0; i < nc && best > 0.f; i++) {
+            const SubShape cs = sub_shape(w, b, fb, i);
+            float f;
+            if (ray_vs_convex(hv, cs.shape, cs.sp, cs.pos, cs.quat, o, d, len, flags, best, f) && f < best) {
+                best = f;
+                found = true;
+                sub = cs.sub;
+            }
+        }
+        if (found) fraction = best;
+        return found;
+    }
     sub = 0xffffffffu;
-    return true;
+    return ray_vs_convex(hv, shape_of(fb), w.shape[b], pB, qB, o, d, len, flags, max_f, fraction);
 }
 
 // broadphase.castRay / dbvt.castRay (broadphase.ts:280-298, dbvt.ts:779-865) over the world's
@@ -3714,6 +3957,14 @@ __global__ void __launch_bounds__(128) k_cast_rays(DevWorld w, const int2 *node_
                                           add(b, fh, sh);
                                           if (MODE == COLLECT_ANY) early = 0.f;
                                       });
+                    } else if (shape_of(fb) == SHAPE_COMPOUND) {  // one hit per child (castRayVsCompound)
+                        const int nc = sub_count(w, b, fb);
+                        for (int i = 0; i < nc; i++) {
+                            if (MODE == COLLECT_ANY && cnt > 0) break;
+                            const SubShape cs = sub_shape(w, b, fb, i);
+                            if (ray_vs_convex(hv, cs.shape, cs.sp, cs.pos, cs.quat, o, d, len, flt.flags, INITIAL, f))
+                                add(b, f, cs.sub);
+                        }
                     } else if (ray_vs_body<false>(w, hv, b, o, d, len, flt.flags, INITIAL, f, sub)) {
                         add(b, f, sub);
                     }
@@ -3794,38 +4045,14 @@ __device__ int mesh_ray_hit_count(const DevWorld &w, const DevMesh &M, float3 o,
     return count;
 }
 
-// collidePointVsShape for one body: sphere.ts:272-301 (distance), box.ts:370-410 (half extents),
-// convex.ts:142-216 (local bounds, then GJK of the INCLUDE_CONVEX_RADIUS support against the point
-// with the query's collision tolerance), triangle-mesh.ts:482-570 (local bounds, odd-even count)
-__device__ bool point_in_body(const DevWorld &w, const HullView &hv, int b, float3 p, float tol, uint32_t &sub) {
-    sub = 0xffffffffu;
-    const uint32_t fb = w.flags[b];
-    const float4 sp = w.shape[b];
-    float3 pB;
-    float4 qB;
-    geom_pose(w, b, fb, pB, qB);
+// collidePointVsShape of one convex shape at (pB, qB): sphere.ts:272-301 (distance), box.ts:370-410
+// (half extents), convex.ts:142-216 (local bounds, then GJK of the INCLUDE_CONVEX_RADIUS support
+// against the point with the query's collision tolerance)
+__device__ bool point_in_convex(const HullView &hv, int shape, float4 sp, float3 pB, float4 qB, float3 p, float tol) {
     const float3 l = p - pB;
-    const int shape = shape_of(fb);
-    if (shape == SHAPE_EMPTY) return false;
-    if (shape == SHAPE_PLANE) {  // collidePointVsPlane plane.ts:404-460
-        float3 n;
-        float c;
-        plane_world(sp, pB, qB, n, c);
-        return dot3(n, p) + c < 0.f;
-    }
     if (shape == SHAPE_SPHERE) return lensq3(l) <= sp.x * sp.x;
     const float3 lp = qrot_inv(qB, l);
     if (shape == SHAPE_BOX) return fabsf(lp.x) <= sp.x && fabsf(lp.y) <= sp.y && fabsf(lp.z) <= sp.z;
-    if (shape == SHAPE_MESH) {
-        const DevMesh &M = w.meshes[mesh_of(sp)];
-        if (M.num_tris == 0) return false;
-        if (lp.x < M.lo.x || lp.x > M.hi.x || lp.y < M.lo.y || lp.y > M.hi.y || lp.z < M.lo.z || lp.z > M.hi.z)
-            return false;
-        uint32_t last = 0xffffffffu;
-        if ((mesh_ray_hit_count(w, M, lp, (M.hi.y - M.lo.y) * 1.1f, last) & 1) == 0) return false;
-        sub = last;
-        return true;
-    }
     float3 lo, hi;  // the shape's local bounds: capsule.ts computeCapsuleAABB, the hull's points
     if (shape == SHAPE_HULL) {
         const DevHull &h = hv.hulls[hull_of(sp)];
@@ -3849,6 +4076,49 @@ __device__ bool point_in_body(const DevWorld &w, const HullView &hv, int b, floa
     sx.size = 0;
     const GjkOut<float> g = gjk(A, P, tol, dir, 0.f, sx);
     return g.sqdist <= tol * tol;
+}
+
+// collidePointVsShape for one body: the convex shapes above, the plane (plane.ts:404-460), a
+// compound's first child holding the point (compound.ts:423-492), triangle-mesh.ts:482-570 (local
+// bounds, odd-even count)
+__device__ bool point_in_body(const DevWorld &w, const HullView &hv, int b, float3 p, float tol, uint32_t &sub) {
+    sub = 0xffffffffu;
+    const uint32_t fb = w.flags[b];
+    const float4 sp = w.shape[b];
+    float3 pB;
+    float4 qB;
+    geom_pose(w, b, fb, pB, qB);
+    const int shape = shape_of(fb);
+    if (shape == SHAPE_EMPTY) return false;
+    if (shape == SHAPE_PLANE) {  // collidePointVsPlane plane.ts:404-460
+        float3 n;
+        float c;
+        plane_world(sp, pB, qB, n, c);
+        return dot3(n, p) + c < 0.f;
+    }
+    if (shape == SHAPE_COMPOUND) {
+        const int nc = sub_count(w, b, fb);
+        for (int i = 0; i < nc; i++) {
+            const SubShape cs = sub_shape(w, b, fb, i);
+            if (point_in_convex(hv, cs.shape, cs.sp, cs.pos, cs.quat, p, tol)) {
+                sub = cs.sub;
+                return true;
+            }
+        }
+        return false;
+    }
+    if (shape == SHAPE_MESH) {
+        const float3 lp = qrot_inv(qB, p - pB);
+        const DevMesh &M = w.meshes[mesh_of(sp)];
+        if (M.num_tris == 0) return false;
+        if (lp.x < M.lo.x || lp.x > M.hi.x || lp.y < M.lo.y || lp.y > M.hi.y || lp.z < M.lo.z || lp.z > M.hi.z)
+            return false;
+        uint32_t last = 0xffffffffu;
+        if ((mesh_ray_hit_count(w, M, lp, (M.hi.y - M.lo.y) * 1.1f, last) & 1) == 0) return false;
+        sub = last;
+        return true;
+    }
+    return point_in_convex(hv, shape, sp, pB, qB, p, tol);
 }
 
 // broadphase.intersectPoint / dbvt.intersectPoint (broadphase.ts:314-324, dbvt.ts:683-740) over the
@@ -3932,7 +4202,7 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
         const DevShapeCast q = qs[k];
         const int shape = q.shape_type;
         const float4 sa = make_float4(q.params[0], q.params[1], q.params[2], q.params[3]);
-        const uint32_t fa = (uint32_t)shape << F_SHAPE_SHIFT;
+        const uint32_t fa = shape_bits(shape);
         const float3 pA = f3(q.position[0], q.position[1], q.position[2]);
         const float4 qA = make_float4(q.quaternion[0], q.quaternion[1], q.quaternion[2], q.quaternion[3]);
         const float3 disp = f3(q.displacement[0], q.displacement[1], q.displacement[2]);
@@ -4062,31 +4332,36 @@ __global__ void __launch_bounds__(128, 4) k_cast_shapes(DevWorld w, const int2 *
                     continue;
                 }
                 if (PASS == 1) continue;
-                float3 pB;
-                float4 qB;
-                geom_pose(w, b, fb, pB, qB);
-                const Q<float> iqB{-qB.x, -qB.y, -qB.z, qB.w};
-                const V<float> posAInB = qrotS(iqB, V<float>{pA.x - pB.x, pA.y - pB.y, pA.z - pB.z});
-                const Q<float> qAInB = qmulS(iqB, Q<float>{qA.x, qA.y, qA.z, qA.w});
-                const V<float> dInB = qrotS(iqB, V<float>{disp.x, disp.y, disp.z});
-                Sup<float> supA = supA0;
-                set_transform(supA, qAInB, posAInB);
-                const Sup<float> supB = make_sup<float>(shape_of(fb), w.shape[b], true, hv);
-                const float max_l = MODE != COLLECT_CLOSEST ? early
-                                    : (hit >= 0 && b < hit) ? nextafterf(best, CUDART_INF_F)
-                                                            : best;
-                float lambda;
-                V<float> cpa, cpb, ax;
-                if (!gjk_cast(lambda, cpa, cpb, ax, supA, supB, dInB, 1e-4f, supA.convex_radius, supB.convex_radius,
-                              max_l))
-                    continue;
-                // penetrationCastShape penetration.ts:693-698: a too short axis becomes the cast direction
-                if (lsq(ax) < 1e-4f * 1e-4f) ax = dInB;
-                if (lambda > 1.f || dot(ax, dInB) <= 0.f || lambda >= max_l) continue;
-                const Q<float> qBq{qB.x, qB.y, qB.z, qB.w};
-                const V<float> axw = qrotS(qBq, ax);
-                const V<float> paw = qrotS(qBq, cpa);
-                collect(lambda, f3(paw.x + pB.x, paw.y + pB.y, paw.z + pB.z), f3(axw.x, axw.y, axw.z));
+                // a convex body, or a compound child by child (castShapeVsCompound compound.ts:776-866)
+                const int nsub = sub_count(w, b, fb);
+                for (int ci = 0; ci < nsub; ci++) {
+                    if (MODE == COLLECT_ANY && cnt > 0) break;
+                    const SubShape cs = sub_shape(w, b, fb, ci);
+                    const float3 pB = cs.pos;
+                    const float4 qB = cs.quat;
+                    const Q<float> iqB{-qB.x, -qB.y, -qB.z, qB.w};
+                    const V<float> posAInB = qrotS(iqB, V<float>{pA.x - pB.x, pA.y - pB.y, pA.z - pB.z});
+                    const Q<float> qAInB = qmulS(iqB, Q<float>{qA.x, qA.y, qA.z, qA.w});
+                    const V<float> dInB = qrotS(iqB, V<float>{disp.x, disp.y, disp.z});
+                    Sup<float> supA = supA0;
+                    set_transform(supA, qAInB, posAInB);
+                    const Sup<float> supB = make_sup<float>(cs.shape, cs.sp, true, hv);
+                    const float max_l = MODE != COLLECT_CLOSEST ? early
+                                        : (hit >= 0 && b < hit) ? nextafterf(best, CUDART_INF_F)
+                                                                : best;
+                    float lambda;
+                    V<float> cpa, cpb, ax;
+                    if (!gjk_cast(lambda, cpa, cpb, ax, supA, supB, dInB, 1e-4f, supA.convex_radius,
+                                  supB.convex_radius, max_l))
+                        continue;
+                    // penetrationCastShape penetration.ts:693-698: a too short axis becomes the cast direction
+                    if (lsq(ax) < 1e-4f * 1e-4f) ax = dInB;
+                    if (lambda > 1.f || dot(ax, dInB) <= 0.f || lambda >= max_l) continue;
+                    const Q<float> qBq{qB.x, qB.y, qB.z, qB.w};
+                    const V<float> axw = qrotS(qBq, ax);
+                    const V<float> paw = qrotS(qBq, cpa);
+                    collect(lambda, f3(paw.x + pB.x, paw.y + pB.y, paw.z + pB.z), f3(axw.x, axw.y, axw.z), cs.sub);
+                }
             }
         }
         if (MODE != COLLECT_CLOSEST) counts[k] = cnt;
@@ -4144,7 +4419,7 @@ __device__ bool collide_query_mesh(const DevWorld &w, const HullView &hv, EpaScr
         qhi = qcenter + f3(er, er, er);
     } else {
         float3 llo, lhi;
-        convex_local_bounds(w, (uint32_t)shA << F_SHAPE_SHIFT, sa, llo, lhi);
+        convex_local_bounds(w, shape_bits(shA), sa, llo, lhi);
         blo1 = llo - f3(ms, ms, ms);
         bhi1 = lhi + f3(ms, ms, ms);
         qlo = f3(3.0e38f, 3.0e38f, 3.0e38f);
@@ -4279,20 +4554,16 @@ __device__ bool collide_query_mesh(const DevWorld &w, const HullView &hv, EpaScr
     return true;
 }
 
-// collideShapeVsShape (narrowphase.ts:172-238) of the query shape A against body b: the hit(s)
-// through add(body, sub-shape id, penetration, point on A, point on B, unit axis), all world
-// space; false once add asks the walk to stop
+// collideShapeVsShape (narrowphase.ts:172-238) of the query shape A against one shape of body b
+// (shB, sb at pB, qB; subB its sub-shape id): the hit(s) through add(body, sub-shape id,
+// penetration, point on A, point on B, unit axis), all world space; false once add asks the walk
+// to stop
 template <class Add>
-__device__ bool collide_query_body(const DevWorld &w, const HullView &hv, EpaScratch *slot, int shA, float4 sa,
-                                   float3 pA, float4 qA, int b, const DevCollideSettings &cs, Add &&add) {
-    const uint32_t fb = w.flags[b];
-    const int shB = shape_of(fb);
+__device__ bool collide_query_shape(const DevWorld &w, const HullView &hv, EpaScratch *slot, int shA, float4 sa,
+                                    float3 pA, float4 qA, int b, int shB, float4 sb, float3 pB, float4 qB,
+                                    uint32_t subB, const DevCollideSettings &cs, Add &&add) {
     if (shB == SHAPE_EMPTY) return true;  // empty-shape.ts registers no collide function
     const float ms = cs.max_separation;
-    const float4 sb = w.shape[b];
-    float3 pB;
-    float4 qB;
-    geom_pose(w, b, fb, pB, qB);
     if (shB == SHAPE_MESH) return collide_query_mesh(w, hv, slot, shA, sa, pA, qA, b, pB, qB, cs, add);
     if (shB == SHAPE_PLANE) {  // collideConvexVsPlane plane.ts:474-629, the plane in A's frame
         const float3 nl = qrot_inv(qA, qrot(qB, xyz(sb)));
@@ -4303,7 +4574,7 @@ __device__ bool collide_query_body(const DevWorld &w, const HullView &hv, EpaScr
         const float sd = dot3(nl, sp3) + cl, cr = S.convex_radius;
         const float pen = -sd + cr;
         if (!(pen > -ms)) return true;
-        return add(b, 0xffffffffu, pen, pA + qrot(qA, sp3 - nl * cr), pA + qrot(qA, sp3 - nl * sd), qrot(qA, -nl));
+        return add(b, subB, pen, pA + qrot(qA, sp3 - nl * cr), pA + qrot(qA, sp3 - nl * sd), qrot(qA, -nl));
     }
     if (shA == SHAPE_SPHERE && shB == SHAPE_SPHERE) {  // collideSphereVsSphere sphere.ts:319-410
         const float3 d = pB - pA;
@@ -4311,7 +4582,7 @@ __device__ bool collide_query_body(const DevWorld &w, const HullView &hv, EpaScr
         if (dsq >= rs * rs) return true;
         const float dist = sqrtf(dsq);
         const float3 nn = dist > 0.f ? d * (1.f / dist) : f3(0.f, 1.f, 0.f);
-        return add(b, 0xffffffffu, rs - dist, pA + nn * sa.x, pB - nn * sb.x, nn);
+        return add(b, subB, rs - dist, pA + nn * sa.x, pB - nn * sb.x, nn);
     }
     // collideConvexVsConvex convex.ts:257-346: B in A's local frame, GJK and EPA in FP64
     const Q<R> qAr{R(qA.x), R(qA.y), R(qA.z), R(qA.w)}, iA{R(-qA.x), R(-qA.y), R(-qA.z), R(qA.w)};
@@ -4350,9 +4621,24 @@ __device__ bool collide_query_body(const DevWorld &w, const HullView &hv, EpaScr
         ax = g.axis;
     }
     const V<R> paw = qrotS(qAr, pa), pbw = qrotS(qAr, pb), axw = qrotS(qAr, ax);
-    return add(b, 0xffffffffu, (float)pen, f3((float)paw.x, (float)paw.y, (float)paw.z) + pA,
+    return add(b, subB, (float)pen, f3((float)paw.x, (float)paw.y, (float)paw.z) + pA,
                f3((float)pbw.x, (float)pbw.y, (float)pbw.z) + pA,
                normalize3(f3((float)axw.x, (float)axw.y, (float)axw.z)));
+}
+
+// the query shape A against body b: each of a compound's children (collideShapeVsCompound
+// compound.ts:580-678), else the body's own shape
+template <class Add>
+__device__ bool collide_query_body(const DevWorld &w, const HullView &hv, EpaScratch *slot, int shA, float4 sa,
+                                   float3 pA, float4 qA, int b, const DevCollideSettings &cs, Add &&add) {
+    const uint32_t fb = w.flags[b];
+    const int nsub = sub_count(w, b, fb);
+    for (int i = 0; i < nsub; i++) {
+        const SubShape s = sub_shape(w, b, fb, i);
+        if (!collide_query_shape(w, hv, slot, shA, sa, pA, qA, b, s.shape, s.sp, s.pos, s.quat, s.sub, cs, add))
+            return false;
+    }
+    return true;
 }
 
 // broadphase.intersectAABB (broadphase.ts:300-312) of the query's box, grown by the separation
@@ -4412,7 +4698,7 @@ __global__ void __launch_bounds__(64) k_collide_shapes(DevWorld w, const int2 *n
         if (valid && n > 0 && wr >= 0 && wr < w.num_worlds) {
             // box3.transformMat4 of the local bounds, grown by the separation (query.ts:294-298)
             float3 llo, lhi;
-            convex_local_bounds(w, (uint32_t)shA << F_SHAPE_SHIFT, sa, llo, lhi);
+            convex_local_bounds(w, shape_bits(shA), sa, llo, lhi);
             const float3 hl = (lhi - llo) * 0.5f, centre = pA + qrot(qA, (lhi + llo) * 0.5f);
             const float3 ex = qrot(qA, f3(1.f, 0.f, 0.f)), ey = qrot(qA, f3(0.f, 1.f, 0.f)),
                          ez = qrot(qA, f3(0.f, 0.f, 1.f));
@@ -4585,6 +4871,7 @@ void launch_narrowphase(DevWorld &w, float, cudaStream_t s, cudaEvent_t mid) {
         k_epa_mesh<<<EPA_BIG_THREADS / EPA_BLOCK, EPA_BLOCK, 0, s>>>(w, items, (EpaScratch *)w.epa_scratch);
         launch_mesh_narrowphase(w, 1, s);
     }
+    if (w.num_compound_bodies > 0) k_compound_pairs<<<MESH_BIG_THREADS / 64, 64, 0, s>>>(w);
 }
 
 // ---------------------------------------------------------------------------

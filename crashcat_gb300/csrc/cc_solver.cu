@@ -126,19 +126,31 @@ __device__ __forceinline__ float inv_eff_mass(bool dynA, bool dynB, float imA, f
 
 // ---------------------------------------------------------------------------
 // Contact cache key (the contact's (idA, idB, subShapeIdA, subShapeIdB), contacts.ts:481-513):
-// (A << 32) | B for convex pairs; with a mesh triangle, bit 63 set and A, B and the triangle
-// index in 21 bits each (the triangle index is the low bits of the mesh's sub-shape id)
+// (A << 32) | B for convex pairs; with a sub-shape (a mesh triangle, a compound child), bit 63
+// set and A, B and the sub-shape indices in 21 bits each.  The indices are the low bits of the
+// sub-shape ids (the triangle's, the child's), packed side by side while they fit in 21 bits
+// (a mesh of up to 2^21 triangles, or a compound of 2^k children against a mesh of up to
+// 2^(21-k)); past that they are folded into 21 bits by a multiplicative hash.
+__device__ __forceinline__ int sub_index_bits(const DevWorld &w, int body) {
+    const int s = shape_of(w.flags[body]);
+    if (s == SHAPE_MESH) return w.meshes[mesh_of(w.shape[body])].sub_bits;
+    if (s == SHAPE_COMPOUND) return w.compounds[compound_of(w.shape[body])].sub_bits;
+    return 0;
+}
 __device__ __forceinline__ unsigned long long contact_key(const DevWorld &w, int A, int B, uint32_t subA,
                                                           uint32_t subB) {
     if (subA == 0xffffffffu && subB == 0xffffffffu)
         return ((unsigned long long)(unsigned)A << 32) | (unsigned)B;
-    const uint32_t sub = subA != 0xffffffffu ? subA : subB;
-    const int mb = subA != 0xffffffffu ? A : B;
-    const int bits = w.meshes[mesh_of(w.shape[mb])].sub_bits;
-    const uint32_t tri = bits >= 32 ? sub : (sub & ((1u << bits) - 1u));
+    const int ba = subA != 0xffffffffu ? sub_index_bits(w, A) : 0;
+    const int bb = subB != 0xffffffffu ? sub_index_bits(w, B) : 0;
+    auto low = [](uint32_t sub, int bits) { return bits >= 32 ? sub : (sub & ((1u << bits) - 1u)); };
     const unsigned long long M = (1ull << MESH_KEY_BITS) - 1ull;
-    return (1ull << 63) | (((unsigned long long)A & M) << 42) | (((unsigned long long)B & M) << 21) |
-           ((unsigned long long)tri & M);
+    unsigned long long idx;
+    if (ba + bb <= MESH_KEY_BITS)
+        idx = ((unsigned long long)low(subA, ba) << bb) | low(subB, bb);
+    else
+        idx = ((unsigned long long)(subA * 0x9E3779B1u ^ subB * 0x85EBCA77u)) >> (32 - MESH_KEY_BITS);
+    return (1ull << 63) | (((unsigned long long)A & M) << 42) | (((unsigned long long)B & M) << 21) | (idx & M);
 }
 
 // contact setup: one manifold per thread

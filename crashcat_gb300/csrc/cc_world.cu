@@ -42,7 +42,14 @@ struct cc_world {
     std::vector<DevSixDof> sixdofs;
     std::vector<cc_hull::Hull> hulls;  // convex hull shapes as built
     std::vector<cc_mesh::Mesh> meshes;  // triangle meshes as built
-    bool hulls_dirty = false, meshes_dirty = false;  // added since the last upload
+    // compound shapes as registered: the children and the FP64 mass properties of compound.ts
+    struct Compound {
+        std::vector<cc_compound_child> children;
+        double mass = 0, inertia[9] = {}, com[3] = {}, lo[3] = {}, hi[3] = {}, inner = 0;
+        int sub_bits = 0;
+    };
+    std::vector<Compound> compounds;
+    bool hulls_dirty = false, meshes_dirty = false, compounds_dirty = false;  // added since the last upload
     DevRay *q_rays = nullptr;  // ray query staging (cc_world_cast_rays), grown on demand
     DevRayHit *q_hits = nullptr;
     int q_cap = 0;
@@ -545,7 +552,7 @@ int cc_world_destroy(cc_world *W) {
                     w.hull_planes, w.hull_faces, w.hull_vidx, w.ccd_flag, w.ccd_slot, w.ccd_index, w.ccd,
                     w.ccd_world_off, w.ccd_world_fill, w.ccd_seg, w.ccd_lambda, w.ccd_scan_tmp,
                     w.meshes, w.mesh_verts, w.mesh_tris, w.mesh_nodes, w.mesh_pairs, w.mesh_epa_base,
-                    w.mesh_epa_count, w.mesh_big, w.mesh_big_red};
+                    w.mesh_epa_count, w.mesh_big, w.mesh_big_red, w.compounds, w.children, w.compound_pairs};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (W->q_rays) cudaFree(W->q_rays);
@@ -596,7 +603,8 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
         const cc_body_desc &d = b[i];
         if (d.shape_type != CC_SHAPE_BOX && d.shape_type != CC_SHAPE_SPHERE && d.shape_type != CC_SHAPE_CAPSULE &&
             d.shape_type != CC_SHAPE_CONVEX_HULL && d.shape_type != CC_SHAPE_TRIANGLE_MESH &&
-            d.shape_type != CC_SHAPE_CYLINDER && d.shape_type != CC_SHAPE_PLANE && d.shape_type != CC_SHAPE_EMPTY)
+            d.shape_type != CC_SHAPE_CYLINDER && d.shape_type != CC_SHAPE_PLANE && d.shape_type != CC_SHAPE_EMPTY &&
+            d.shape_type != CC_SHAPE_COMPOUND)
             return CC_ERR_UNSUPPORTED;
         if (d.mass_properties_mode < 0 || d.mass_properties_mode > 2 || !std::isfinite(d.mass)) return CC_ERR_INVALID;
         for (int k = 0; k < 6; k++)
@@ -632,6 +640,16 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
                 return CC_ERR_INVALID;
             hull = &W->hulls[hull_index];
         }
+        const cc_world::Compound *cmp = nullptr;
+        int cmp_index = -1;
+        if (d.shape_type == CC_SHAPE_COMPOUND) {
+            cmp_index = (int)d.shape_params[0];
+            if (!(d.shape_params[0] == (float)cmp_index) || cmp_index < 0 || cmp_index >= (int)W->compounds.size())
+                return CC_ERR_INVALID;
+            if (d.motion_quality == CC_MOTION_LINEAR_CAST) return CC_ERR_UNSUPPORTED;  // no compound cast
+            if (w.cap >= (1 << MESH_KEY_BITS)) return CC_ERR_UNSUPPORTED;  // the contact key's 21-bit indices
+            cmp = &W->compounds[cmp_index];
+        }
         if (d.shape_type == CC_SHAPE_CAPSULE && !(d.shape_params[0] > 0.f && d.shape_params[1] > 0.f))
             return CC_ERR_INVALID;  // capsule.ts:55-61
         if (d.motion_type < 0 || d.motion_type > 2) return CC_ERR_INVALID;
@@ -658,8 +676,10 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
         const bool scaled = sc[0] != 1 || sc[1] != 1 || sc[2] != 1;
         const bool transformed = tp.x != 0 || tp.y != 0 || tp.z != 0 || tq.x != 0 || tq.y != 0 || tq.z != 0 || tq.w != 1;
         const bool offset = off.x != 0 || off.y != 0 || off.z != 0;
-        // a plane keeps its local bounds (computePlaneLocalBounds plane.ts:273-295) in a frame
-        const bool decorated = scaled || transformed || offset || plane;
+        // a plane keeps its local bounds (computePlaneLocalBounds plane.ts:273-295) in a frame, and
+        // a compound its bounds, centre of mass and inner radius (an identity transform)
+        if (cmp && (scaled || transformed || offset)) return CC_ERR_UNSUPPORTED;
+        const bool decorated = scaled || transformed || offset || plane || cmp;
         if (scaled && (hull || mesh || plane)) return CC_ERR_UNSUPPORTED;
         double mass;
         double idiag[3];
@@ -667,6 +687,13 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
         if (mesh || plane) {
             mass = 0.0;  // computeMassProperties triangle-mesh.ts:153-158, plane.ts:120-122
             idiag[0] = idiag[1] = idiag[2] = 0.0;
+        } else if (cmp) {
+            // the compound's mass and inertia (compound.ts:177-230, the children's densities),
+            // principal axes
+            mass = cmp->mass;
+            double I[9];
+            for (int k = 0; k < 9; k++) I[k] = cmp->inertia[k];
+            cc_hull::principal_axes(I, idiag, irot);
         } else if (hull) {
             // computeMassProperties convex-hull.ts:453-459, principal axes of the inertia
             mass = hull->volume * d.density;
@@ -708,7 +735,7 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
         bool given_tensor = false;
         DevFrame fr;
         memset(&fr, 0, sizeof(fr));
-        if (decorated && !mesh && !plane) {
+        if (decorated && !mesh && !plane && !cmp) {
             // computeMassProperties: massProperties.scale (mass-properties.ts:59-112), rotate
             // (:121-160), translate (:168-205) of the leaf's, then the principal axes
             double t[9] = {idiag[0], 0, 0, 0, idiag[1], 0, 0, 0, idiag[2]};
@@ -790,6 +817,11 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
                     lo[k] = mesh->lo[k];
                     hi[k] = mesh->hi[k];
                 }
+            } else if (cmp) {
+                for (int k = 0; k < 3; k++) {
+                    lo[k] = cmp->lo[k];
+                    hi[k] = cmp->hi[k];
+                }
             } else if (hull) {
                 lo[0] = hull->lo.x, lo[1] = hull->lo.y, lo[2] = hull->lo.z;
                 hi[0] = hull->hi.x, hi[1] = hull->hi.y, hi[2] = hull->hi.z;
@@ -821,6 +853,7 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
             // centre of mass: computeTransformedCenterOfMass + the offset (a scaled shape's is zero)
             D3 c{0, 0, 0};
             if (hull && !scaled) c = D3{hull->com.x, hull->com.y, hull->com.z};
+            if (cmp) c = D3{cmp->com[0], cmp->com[1], cmp->com[2]};
             if (transformed) {
                 D3 r = drot(tq, c);
                 c = {r.x + tp.x, r.y + tp.y, r.z + tp.z};
@@ -836,6 +869,7 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
             if (d.shape_type == CC_SHAPE_CYLINDER)
                 inner = std::min((double)d.shape_params[0], (double)d.shape_params[1]);
             if (mesh || plane) inner = 0;
+            if (cmp) inner = cmp->inner;
             double minScale = std::min(std::fabs(sc[0]), std::min(std::fabs(sc[1]), std::fabs(sc[2])));
             fr.t_pos = make_float4((float)tp.x, (float)tp.y, (float)tp.z, (float)(minScale * inner));
             fr.t_rot = make_float4((float)tq.x, (float)tq.y, (float)tq.z, (float)tq.w);
@@ -907,11 +941,16 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
             memcpy(&mi_bits, &mesh_index, sizeof(float));
             sh[i] = make_float4(mi_bits, 0.f, 0.f, 0.f);
         }
+        if (cmp) {
+            float ci_bits;
+            memcpy(&ci_bits, &cmp_index, sizeof(float));
+            sh[i] = make_float4(ci_bits, 0.f, 0.f, 0.f);
+        }
         mat[i] = make_float4(d.friction, d.restitution, d.gravity_factor, 0.f);
         damp[i] = make_float4(d.linear_damping, d.angular_damping, d.max_linear_velocity, d.max_angular_velocity);
         uint32_t f = (uint32_t)d.motion_type;
         if (d.allow_sleeping) f |= F_ALLOW_SLEEP;
-        f |= (uint32_t)d.shape_type << F_SHAPE_SHIFT;
+        f |= shape_bits(d.shape_type);
         f |= (uint32_t)dof << F_DOF_SHIFT;
         f |= (uint32_t)(d.friction_combine & 7) << F_FCOMB_SHIFT;
         f |= (uint32_t)(d.restitution_combine & 7) << F_RCOMB_SHIFT;
@@ -983,21 +1022,34 @@ int cc_world_add_bodies(cc_world *W, const cc_body_desc *b, int32_t n, int32_t *
     CC_TRY(cudaMemcpyAsync(w.sleep_sph + 3 * o, sph.data(), sizeof(float4) * 3 * n, cudaMemcpyHostToDevice, s));
     CC_TRY(cudaMemcpyAsync(w.sleep_timer + o, timer.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
     CC_TRY(cudaStreamSynchronize(s));
-    int lc = 0, mc = 0;
+    int lc = 0, mc = 0, cc = 0;
     for (int i = 0; i < n; i++) {
         lc += (flags[i] & F_LINEAR_CAST) != 0;
         mc += shape_of(flags[i]) == SHAPE_MESH;
+        cc += shape_of(flags[i]) == SHAPE_COMPOUND;
     }
+    if (cc > 0 && !w.compound_pairs) {  // the compound pairs' list and their 32-manifold slots
+        int r;
+        if ((r = dalloc(&w.compound_pairs, (size_t)w.max_pairs)) != CC_OK) return r;
+        if (!w.mesh_big_red) {
+            char *big = nullptr;
+            if ((r = dalloc(&big, mesh_big_slot_bytes() * (size_t)MESH_BIG_THREADS)) != CC_OK) return r;
+            w.mesh_big_red = big;
+        }
+    }
+    w.num_compound_bodies += cc;
     if (mc > 0 && !w.mesh_pairs) {
         int r;
-        char *big = nullptr;
         if ((r = dalloc(&w.mesh_pairs, (size_t)w.max_pairs)) != CC_OK ||
             (r = dalloc(&w.mesh_epa_base, (size_t)w.max_pairs)) != CC_OK ||
             (r = dalloc(&w.mesh_epa_count, (size_t)w.max_pairs)) != CC_OK ||
-            (r = dalloc(&w.mesh_big, (size_t)w.max_pairs)) != CC_OK ||
-            (r = dalloc(&big, mesh_big_slot_bytes() * (size_t)MESH_BIG_THREADS)) != CC_OK)
+            (r = dalloc(&w.mesh_big, (size_t)w.max_pairs)) != CC_OK)
             return r;
-        w.mesh_big_red = big;
+        if (!w.mesh_big_red) {
+            char *big = nullptr;
+            if ((r = dalloc(&big, mesh_big_slot_bytes() * (size_t)MESH_BIG_THREADS)) != CC_OK) return r;
+            w.mesh_big_red = big;
+        }
     }
     w.num_mesh_bodies += mc;
     if (lc > 0) {
@@ -1052,8 +1104,13 @@ static void enqueue_step(cc_world *W, float dt, float ratio, cudaEvent_t *ev = n
 // hulls and meshes added since the last launch go to the device in one upload each
 static int upload_hulls(cc_world *W);
 static int upload_meshes(cc_world *W);
+static int upload_compounds(cc_world *W);
 static int sync_shapes(cc_world *W) {
     int r = CC_OK;
+    if (W->compounds_dirty) {
+        if ((r = upload_compounds(W)) != CC_OK) return r;
+        W->compounds_dirty = false;
+    }
     if (W->hulls_dirty) {
         if ((r = upload_hulls(W)) != CC_OK) return r;
         W->hulls_dirty = false;
@@ -2805,6 +2862,193 @@ int cc_world_get_triangle_mesh(cc_world *W, int32_t mesh, cc_mesh_info *info, fl
 }  // extern "C"
 
 static int build_hull_from(const float *points, int32_t n, float convex_radius, cc_hull::Hull &h);
+
+// ---------------------------------------------------------------------------
+// compound shapes (compound.ts)
+// ---------------------------------------------------------------------------
+// one convex child's mass (its own density), inertia about its centre of mass (row-major, in the
+// child's frame), centre of mass and local bounds in the child's frame, and inner radius
+static bool child_leaf(const cc_world *W, const cc_compound_child &c, double &m, double I[9], double com[3],
+                       double lo[3], double hi[3], double &inner) {
+    const float *p = c.shape_params;
+    const double rho = c.density;
+    for (int k = 0; k < 9; k++) I[k] = 0;
+    for (int k = 0; k < 3; k++) com[k] = 0;
+    switch (c.shape_type) {
+        case CC_SHAPE_BOX: {  // setMassAndInertiaOfSolidBox mass-properties.ts:36-52
+            double f[3] = {2.0 * p[0], 2.0 * p[1], 2.0 * p[2]};
+            m = f[0] * f[1] * f[2] * rho;
+            I[0] = (f[1] * f[1] + f[2] * f[2]) * (m / 12.0);
+            I[4] = (f[0] * f[0] + f[2] * f[2]) * (m / 12.0);
+            I[8] = (f[0] * f[0] + f[1] * f[1]) * (m / 12.0);
+            for (int k = 0; k < 3; k++) lo[k] = -p[k], hi[k] = p[k];
+            inner = std::min((double)p[0], std::min((double)p[1], (double)p[2]));
+            return p[0] > 0 && p[1] > 0 && p[2] > 0 && p[3] >= 0;
+        }
+        case CC_SHAPE_SPHERE: {  // sphere.ts:97-123
+            double r = p[0];
+            m = (4.0 / 3.0) * M_PI * r * r * r * rho;
+            I[0] = I[4] = I[8] = 0.4 * m * r * r;
+            for (int k = 0; k < 3; k++) lo[k] = -r, hi[k] = r;
+            inner = r;
+            return r > 0;
+        }
+        case CC_SHAPE_CAPSULE: {  // capsule.ts:119-157
+            double r = p[0], h = p[1];
+            double volume = M_PI * r * r * (2 * h) + (4.0 / 3.0) * M_PI * r * r * r;
+            m = volume * rho;
+            double r2 = r * r, height = 2.0 * h;
+            double cyl = M_PI * height * r2 * rho, hemi = ((2.0 * M_PI) / 3.0) * r2 * r * rho;
+            I[4] = r2 * cyl * 0.5 + hemi * (2.0 / 5.0) * r2;
+            I[0] = I[8] = cyl * ((1.0 / 12.0) * height * height + (1.0 / 4.0) * r2) +
+                          hemi * ((2.0 / 5.0) * r2 + h * h + (3.0 / 8.0) * h * r);
+            lo[0] = lo[2] = -r, hi[0] = hi[2] = r;
+            lo[1] = -(h + r), hi[1] = h + r;
+            inner = r;
+            return r > 0 && h > 0;
+        }
+        case CC_SHAPE_CYLINDER: {  // cylinder.ts computeMassProperties, getInnerRadius
+            double h = p[0], r = p[1];
+            m = M_PI * r * r * 2 * h * rho;
+            I[4] = 0.5 * m * r * r;
+            I[0] = I[8] = 0.5 * I[4] + (m * 4 * h * h) / 12;
+            lo[0] = lo[2] = -r, hi[0] = hi[2] = r;
+            lo[1] = -h, hi[1] = h;
+            inner = std::min(h, r);
+            return p[2] >= 0.f && p[0] >= p[2] && p[1] >= p[2];
+        }
+        case CC_SHAPE_CONVEX_HULL: {  // convex-hull.ts:453-459, 549-558
+            const int hi_ = (int)p[0];
+            if (!(p[0] == (float)hi_) || hi_ < 0 || hi_ >= (int)W->hulls.size()) return false;
+            const cc_hull::Hull &H = W->hulls[hi_];
+            m = H.volume * rho;
+            for (int k = 0; k < 9; k++) I[k] = H.inertia[k] * rho;
+            com[0] = H.com.x, com[1] = H.com.y, com[2] = H.com.z;
+            lo[0] = H.lo.x, lo[1] = H.lo.y, lo[2] = H.lo.z;
+            hi[0] = H.hi.x, hi[1] = H.hi.y, hi[2] = H.hi.z;
+            inner = H.inner_radius;
+            return true;
+        }
+        default:
+            return false;
+    }
+}
+
+// every compound's children, uploaded whenever a compound is added
+static int upload_compounds(cc_world *W) {
+    DevWorld &w = W->w;
+    std::vector<DevCompound> hdr;
+    std::vector<DevChild> ch;
+    for (const cc_world::Compound &c : W->compounds) {
+        DevCompound d;
+        d.first = (int)ch.size();
+        d.count = (int)c.children.size();
+        d.sub_bits = c.sub_bits;
+        d.pad = 0;
+        for (const cc_compound_child &k : c.children) {
+            DevChild x;
+            x.params = make_float4(k.shape_params[0], k.shape_params[1], k.shape_params[2], k.shape_params[3]);
+            if (k.shape_type == CC_SHAPE_CONVEX_HULL) {  // the body record's form: the index as int bits
+                const int h = (int)k.shape_params[0];
+                float bits;
+                memcpy(&bits, &h, sizeof(float));
+                x.params = make_float4(bits, (float)W->hulls[h].convex_radius, 0.f, 0.f);
+            }
+            float tbits;
+            const int t = k.shape_type;
+            memcpy(&tbits, &t, sizeof(float));
+            x.pos = make_float4(k.position[0], k.position[1], k.position[2], tbits);
+            x.quat = make_float4(k.quaternion[0], k.quaternion[1], k.quaternion[2], k.quaternion[3]);
+            ch.push_back(x);
+        }
+        hdr.push_back(d);
+    }
+    CC_TRY(cudaStreamSynchronize(W->stream));
+    if (w.compounds) cudaFree(w.compounds);
+    if (w.children) cudaFree(w.children);
+    w.compounds = nullptr;
+    w.children = nullptr;
+    int r;
+    if ((r = dalloc(&w.compounds, hdr.size())) != CC_OK || (r = dalloc(&w.children, ch.size())) != CC_OK) return r;
+    CC_TRY(cudaMemcpy(w.compounds, hdr.data(), sizeof(DevCompound) * hdr.size(), cudaMemcpyHostToDevice));
+    CC_TRY(cudaMemcpy(w.children, ch.data(), sizeof(DevChild) * ch.size(), cudaMemcpyHostToDevice));
+    w.num_compounds = (int)hdr.size();
+    return CC_OK;
+}
+
+extern "C" {
+
+int cc_world_add_compound(cc_world *W, const cc_compound_child *children, int32_t n, int32_t *out_index) {
+    if (!W || !children || n < 1 || n > 4096) return CC_ERR_INVALID;
+    cc_world::Compound c;
+    c.children.assign(children, children + n);
+    std::vector<double> mass((size_t)n), inertia(9 * (size_t)n), ccom(3 * (size_t)n);
+    double total = 0, acc[3] = {0, 0, 0};
+    for (int i = 0; i < n; i++) {
+        const cc_compound_child &k = children[i];
+        if (!finite3(k.position) || !std::isfinite(k.density) || !(k.density > 0.f)) return CC_ERR_INVALID;
+        for (int j = 0; j < 4; j++)
+            if (!std::isfinite(k.shape_params[j]) || !std::isfinite(k.quaternion[j])) return CC_ERR_INVALID;
+        double m, I[9], com[3], lo[3], hi[3], inner;
+        if (!child_leaf(W, k, m, I, com, lo, hi, inner)) return CC_ERR_INVALID;
+        const DQ q{k.quaternion[0], k.quaternion[1], k.quaternion[2], k.quaternion[3]};
+        // computeCompoundLocalBounds :70-108: the child's bounds' corners through its pose
+        for (int cnr = 0; cnr < 8; cnr++) {
+            D3 v = drot(q, D3{(cnr & 1) ? hi[0] : lo[0], (cnr & 2) ? hi[1] : lo[1], (cnr & 4) ? hi[2] : lo[2]});
+            double e[3] = {v.x + k.position[0], v.y + k.position[1], v.z + k.position[2]};
+            for (int a = 0; a < 3; a++) {
+                c.lo[a] = (i == 0 && cnr == 0) ? e[a] : std::min(c.lo[a], e[a]);
+                c.hi[a] = (i == 0 && cnr == 0) ? e[a] : std::max(c.hi[a], e[a]);
+            }
+        }
+        c.inner = i == 0 ? inner : std::min(c.inner, inner);  // getInnerRadius :283-289
+        // the child's centre of mass in the compound's frame (computeCompoundCenterOfMass :110-141)
+        const D3 cw = drot(q, D3{com[0], com[1], com[2]});
+        ccom[3 * i] = cw.x + k.position[0];
+        ccom[3 * i + 1] = cw.y + k.position[1];
+        ccom[3 * i + 2] = cw.z + k.position[2];
+        for (int a = 0; a < 3; a++) acc[a] += ccom[3 * i + a] * m;
+        total += m;
+        mass[i] = m;
+        for (int j = 0; j < 9; j++) inertia[9 * i + j] = I[j];
+    }
+    for (int a = 0; a < 3; a++) c.com[a] = total > 0 ? acc[a] / total : 0.0;
+    // computeMassProperties :177-230: each child's inertia rotated by its quaternion and moved
+    // to the compound's centre of mass (massProperties.rotate / translate)
+    for (int i = 0; i < n; i++) {
+        const cc_compound_child &k = children[i];
+        const DQ q{k.quaternion[0], k.quaternion[1], k.quaternion[2], k.quaternion[3]};
+        const D3 cols[3] = {drot(q, D3{1, 0, 0}), drot(q, D3{0, 1, 0}), drot(q, D3{0, 0, 1})};
+        const double R[9] = {cols[0].x, cols[1].x, cols[2].x, cols[0].y, cols[1].y, cols[2].y,
+                             cols[0].z, cols[1].z, cols[2].z};  // row-major
+        const double *t = &inertia[9 * i];
+        double rt[9];
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) {
+                rt[3 * a + b] = 0;
+                for (int j = 0; j < 3; j++) rt[3 * a + b] += R[3 * a + j] * t[3 * j + b];
+            }
+        const double d[3] = {ccom[3 * i] - c.com[0], ccom[3 * i + 1] - c.com[1], ccom[3 * i + 2] - c.com[2]};
+        const double dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) {
+                double o = 0;
+                for (int j = 0; j < 3; j++) o += rt[3 * a + j] * R[3 * b + j];
+                c.inertia[3 * a + b] += o + mass[i] * ((a == b ? dd : 0.0) - d[a] * d[b]);
+            }
+    }
+    c.mass = total;
+    const unsigned maxi = (unsigned)(n - 1);
+    c.sub_bits = maxi == 0 ? 0 : 32 - __builtin_clz(maxi);
+    W->compounds.push_back(std::move(c));
+    W->compounds_dirty = true;  // uploaded with the next launch (sync_shapes)
+    drop_graph(W);
+    if (out_index) *out_index = (int32_t)W->compounds.size() - 1;
+    return CC_OK;
+}
+
+}  // extern "C"
+
 extern "C" {
 
 int cc_world_add_convex_hull(cc_world *W, const float *points, int32_t n, float convex_radius, int32_t *out_hull) {

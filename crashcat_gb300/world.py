@@ -414,6 +414,15 @@ class GpuWorld:
                                                    C.byref(out)), "cc_world_add_triangle_mesh")
         return out.value
 
+    def add_compound(self, children: np.ndarray) -> int:
+        """cc_world_add_compound: a compound shape from _lib.COMPOUND_CHILD_DTYPE records; the index
+        compound bodies name in shape_params[0]."""
+        children = np.ascontiguousarray(children, dtype=_lib.COMPOUND_CHILD_DTYPE)
+        out = C.c_int32(-1)
+        check(self._lib.cc_world_add_compound(self.handle, children.ctypes.data, len(children), C.byref(out)),
+              "cc_world_add_compound")
+        return out.value
+
     def get_triangle_mesh(self, index: int) -> dict:
         """cc_world_get_triangle_mesh: the built mesh's arrays (the oracle takes them as its shape data)."""
         return _lib._mesh_arrays(

@@ -75,7 +75,8 @@ enum cc_status {
  * bodies only: a plane has no mass); empty (no parameters, no collision, no mass;
  * src/shapes/empty-shape.ts). */
 enum cc_shape_type { CC_SHAPE_SPHERE = 0, CC_SHAPE_BOX = 1, CC_SHAPE_CAPSULE = 2, CC_SHAPE_CONVEX_HULL = 3,
-                     CC_SHAPE_TRIANGLE_MESH = 4, CC_SHAPE_CYLINDER = 5, CC_SHAPE_PLANE = 6, CC_SHAPE_EMPTY = 7 };
+                     CC_SHAPE_TRIANGLE_MESH = 4, CC_SHAPE_CYLINDER = 5, CC_SHAPE_PLANE = 6, CC_SHAPE_EMPTY = 7,
+                     CC_SHAPE_COMPOUND = 8 };
 enum cc_motion_type { CC_STATIC = 0, CC_KINEMATIC = 1, CC_DYNAMIC = 2 };
 enum cc_mass_mode { CC_MASS_FROM_SHAPE = 0, CC_MASS_GIVEN = 1, CC_MASS_AND_INERTIA_GIVEN = 2 };
 enum cc_motion_quality { CC_MOTION_DISCRETE = 0, CC_MOTION_LINEAR_CAST = 1 };  /* MotionQuality motion-properties.ts:8-26 */
@@ -221,10 +222,27 @@ typedef struct cc_stats {
 
 typedef struct cc_world cc_world;
 
+/* One child of a compound shape (src/shapes/compound.ts CompoundShapeChild): a convex shape
+ * (sphere, box, capsule, cylinder, or a convex hull of the world, shape_params as a body's),
+ * its pose in the compound's frame and its density (the compound's mass, centre of mass and
+ * inertia sum the children's, compound.ts:110-230). */
+typedef struct cc_compound_child {
+    int32_t shape_type;
+    float shape_params[4];
+    float position[3];
+    float quaternion[4];  /* x, y, z, w */
+    float density;
+} cc_compound_child;
+
 int cc_world_settings_default(cc_world_settings *out);
 int cc_world_create(const cc_world_settings *settings, cc_world **out);
 int cc_world_destroy(cc_world *world);
 int cc_world_add_bodies(cc_world *world, const cc_body_desc *bodies, int32_t n, int32_t *out_index);
+/* compound.create (compound.ts:43-57) from n >= 1 convex children; *out_index is the index a
+ * body names in shape_params[0] with shape_type CC_SHAPE_COMPOUND.  A compound body takes no
+ * decorators and no LINEAR_CAST motion quality (CC_ERR_UNSUPPORTED); its density field is
+ * unused (the children carry theirs). */
+int cc_world_add_compound(cc_world *world, const cc_compound_child *children, int32_t n, int32_t *out_index);
 int cc_world_num_bodies(const cc_world *world, int32_t *out);
 
 /* Advance every world held by the handle by n_steps steps of dt seconds; the

@@ -71,7 +71,9 @@ def test_record_layouts_match_c(tmp_path):
             "cc_shape_cast": _lib.SHAPE_CAST_DTYPE, "cc_shape_cast_hit": _lib.SHAPE_CAST_HIT_DTYPE,
             "cc_point_desc": _lib.POINT_JOINT_DTYPE, "cc_distance_desc": _lib.DISTANCE_JOINT_DTYPE,
             "cc_fixed_desc": _lib.FIXED_JOINT_DTYPE, "cc_cone_desc": _lib.CONE_JOINT_DTYPE,
-            "cc_slider_desc": _lib.SLIDER_JOINT_DTYPE, "cc_six_dof_desc": _lib.SIX_DOF_JOINT_DTYPE}
+            "cc_slider_desc": _lib.SLIDER_JOINT_DTYPE, "cc_six_dof_desc": _lib.SIX_DOF_JOINT_DTYPE,
+            "cc_compound_child": _lib.COMPOUND_CHILD_DTYPE, "cc_collide_shape": _lib.COLLIDE_SHAPE_DTYPE,
+            "cc_collide_shape_hit": _lib.COLLIDE_SHAPE_HIT_DTYPE}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{ROOT}/include/crashcat_gpu.h"',
              'int main(void) {']
     for name, dt in recs.items():

@@ -146,3 +146,154 @@ def test_oracle_refuses_a_cast_compound(oracle_lib):
     b["motion_quality"][0] = 1
     with pytest.raises(AssertionError):
         oracle_with(b, [TWO_BOXES])
+
+
+# ---------------------------------------------------------------------------
+# the GPU path against the oracle
+# ---------------------------------------------------------------------------
+@pytest.mark.gpu
+def test_gpu_compound_flies_like_the_oracle(gpu_lib, oracle_lib):
+    b, i0 = pair_scene()
+    g, o = gpu_with(b, [TWO_BOXES]), oracle_with(b, [TWO_BOXES])
+    g.step(1.0 / 60.0, 120)
+    o.step(1.0 / 60.0, 120)
+    rows, _ = g.get_state()
+    np.testing.assert_allclose(rows[:, 0:13], o.state()[:, 0:13], atol=2e-4)
+
+
+def compound_pile(n=24, seed=3):
+    """Tables, dumbbells (two spheres on a capsule) and L-shapes (two boxes and a cylinder) dropped
+    on a floor, on a 3 m grid so that each lands alone."""
+    rng = np.random.default_rng(seed)
+    b = floor_and(n)
+    shapes = [TABLE,
+              [("sphere", (0.25,), (-0.6, 0.0, 0.0)), ("sphere", (0.25,), (0.6, 0.0, 0.0)),
+               ("capsule", (0.08, 0.5), (0.0, 0.0, 0.0), (0.0, 0.0, math.sin(math.pi / 4), math.cos(math.pi / 4)))],
+              [("box", (0.5, 0.1, 0.1), (0.4, 0.0, 0.0)), ("box", (0.1, 0.4, 0.1), (0.0, 0.3, 0.0)),
+               ("cylinder", (0.1, 0.2), (0.0, 0.0, 0.3))]]
+    for i in range(1, n + 1):
+        scenes.set_compound(b, i, int(rng.integers(0, 3)))
+        b["position"][i] = (3.0 * ((i - 1) % 5), float(rng.uniform(0.8, 2.0)), 3.0 * ((i - 1) // 5))
+        q = rng.normal(size=4)
+        b["quaternion"][i] = q / np.linalg.norm(q)
+    return b, shapes
+
+
+@pytest.mark.gpu
+def test_gpu_compound_pile_tracks_oracle(gpu_lib, oracle_lib):
+    """Compounds of boxes, spheres, capsules and cylinders landing one by one: every body within
+    2e-3 m of the oracle through the fall and the first contacts; after settling, 90 % within
+    2e-3 m and all within 3 cm (a body landing on an edge tips on the last bits of FP32 against
+    FP64), and every manifold's sub-shape ids as the oracle's for the pairs both find."""
+    b, shapes = compound_pile()
+    g, o = gpu_with(b, shapes), oracle_with(b, shapes)
+    g.step(1.0 / 60.0, 20)
+    o.step(1.0 / 60.0, 20)
+    rows, _ = g.get_state()
+    np.testing.assert_allclose(rows[:, 0:3], o.state()[:, 0:3], atol=2e-3)
+    gs = {tuple(int(x) for x in s) for s in g.get_manifold_sub_shapes()}
+    os_ = {tuple(int(x) for x in s) for s in o.manifold_sub_shapes()}
+    assert len(os_) > 3 and gs == os_, (gs ^ os_)
+    for _ in range(2):
+        g.step(1.0 / 60.0, 50)
+        o.step(1.0 / 60.0, 50)
+        rows, _ = g.get_state()
+        err = np.abs(rows[:, 0:3] - o.state()[:, 0:3]).max(axis=1)
+        assert np.quantile(err, 0.9) < 2e-3 and err.max() < 3e-2, np.sort(err)[-5:]
+
+
+@pytest.mark.gpu
+def test_gpu_table_settles_on_its_legs(gpu_lib):
+    g = gpu_with(table_scene(), [TABLE])
+    g.step(1.0 / 60.0, 120)
+    rows, _ = g.get_state()
+    assert abs(abs(rows[1, 6]) - 1.0) < 1e-3 and -0.025 < rows[1, 1] < 0.005
+    subs = [tuple(int(x) for x in s) for s in g.get_manifold_sub_shapes()]
+    assert subs == [(0xFFFFFFFF, 0xFFFFFFF9)], subs
+
+
+@pytest.mark.gpu
+def test_gpu_compound_on_terrain(gpu_lib, oracle_lib):
+    """Compounds dropped on a terrain mesh: the mesh pass collides them child by child (its EPA
+    items carry the child); the first contacts' sub-shape ids (child, triangle) as the oracle's."""
+    sc = scenes.mesh_drop(n=4, n_cells=12, seed=5, heights=(0.0, 1.0))
+    b, shapes = compound_pile(n=12, seed=4)
+    b = b[1:]  # no box floor: the terrain
+    b["position"][:, 0] -= 6.0
+    b["position"][:, 2] -= 4.0
+    bodies = np.concatenate([sc.bodies[:1], b])
+    g = world.GpuWorld(world.standard_settings(), len(bodies) + 8)
+    g.add_triangle_mesh(*sc.mesh)
+    for c in shapes:
+        g.add_compound(scenes.compound_children(c))
+    g.add_bodies(bodies)
+    o = pyoracle.OracleWorld(world.standard_settings(), bodies, (), [g.get_triangle_mesh(0)],
+                             [scenes.compound_children(c) for c in shapes])
+    g.step(1.0 / 60.0, 40)
+    rows, _ = g.get_state()
+    st = o.state()
+    st[:, 0:13] = rows[:, 0:13]
+    o.set_state(st)
+    g.step(0.0, 1)
+    o.step(0.0, 1)
+    gs = {tuple(int(x) for x in s) for s in g.get_manifold_sub_shapes()}
+    os_ = {tuple(int(x) for x in s) for s in o.manifold_sub_shapes()}
+    assert len(os_) > 5
+    assert len(gs & os_) >= 0.9 * len(gs | os_), (len(gs & os_), len(gs | os_))
+    g.step(1.0 / 60.0, 60)
+    rows, _ = g.get_state()
+    assert np.isfinite(rows).all() and rows[1:, 1].min() > -1.5  # nothing fell through
+
+
+@pytest.mark.gpu
+def test_gpu_compound_queries(gpu_lib, oracle_lib):
+    b = scenes.blank_bodies(1)
+    scenes.set_compound(b, 0, 0)
+    b["motion_type"][0] = _lib.STATIC
+    b["object_layer"][0] = scenes.LAYER_NOT_MOVING
+    g = gpu_with(b, [TWO_BOXES])
+    one_bit = 0xFFFFFFFE
+    rays = np.zeros(2, _lib.RAY_DTYPE)
+    rays["origin"] = [(0.5, 3.0, 0.0), (-0.5, 3.0, 0.0)]
+    rays["direction"] = (0.0, -1.0, 0.0)
+    rays["length"] = 10.0
+    h = g.cast_rays(rays)
+    assert list(h["body"]) == [0, 0] and list(h["sub_shape_id"]) == [one_bit | 1, one_bit | 0]
+    np.testing.assert_allclose(h["fraction"], [0.25, 0.25], atol=2e-4)
+    ha, c = g.cast_rays_collect(rays[:1], _lib.COLLECT_ALL, 4)
+    assert c[0] == 1  # straight down the right box: one child
+    p = g.collide_points([[0.7, 0.2, 0.1], [-0.7, 0.2, 0.1], [0.0, 0.7, 0.0]])
+    assert list(p["count"]) == [1, 1, 0] and list(p["sub_shape_id"][:2]) == [one_bit | 1, one_bit | 0]
+    q = np.zeros(1, _lib.COLLIDE_SHAPE_DTYPE)
+    q["shape_type"] = _lib.SHAPE_BOX
+    q["shape_params"] = (0.3, 0.3, 0.3, 0.05)
+    q["position"] = (0.0, 0.7, 0.0)
+    q["quaternion"] = (0.0, 0.0, 0.0, 1.0)
+    hc, c = g.collide_shapes(q, _lib.COLLECT_ALL, 4)
+    assert c[0] == 2 and sorted(hc["sub_shape_id"][0, :2]) == [one_bit | 0, one_bit | 1]
+    np.testing.assert_allclose(hc["penetration"][0, :2], [0.1, 0.1], atol=1e-3)
+    cs = np.zeros(1, _lib.SHAPE_CAST_DTYPE)
+    cs["shape_type"] = _lib.SHAPE_SPHERE
+    cs["shape_params"] = (0.25, 0, 0, 0)
+    cs["position"] = (0.6, 3.0, 0.0)
+    cs["quaternion"] = (0.0, 0.0, 0.0, 1.0)
+    cs["displacement"] = (0.0, -4.0, 0.0)
+    hs = g.cast_shapes(cs)
+    assert hs["body"][0] == 0 and hs["sub_shape_id"][0] == one_bit | 1 and abs(hs["fraction"][0] - 2.25 / 4) < 1e-3
+
+
+@pytest.mark.gpu
+def test_gpu_compound_refusals(gpu_lib):
+    g = world.GpuWorld(world.standard_settings(), 8)
+    with pytest.raises(_lib.CCError):
+        g.add_compound(scenes.compound_children([("box", (0.5, 0.5, -0.5), (0.0, 0.0, 0.0))]))
+    idx = g.add_compound(scenes.compound_children(TWO_BOXES))
+    b = scenes.blank_bodies(1)
+    scenes.set_compound(b, 0, idx)
+    b["motion_quality"][0] = 1  # LINEAR_CAST
+    with pytest.raises(_lib.CCError):
+        g.add_bodies(b)
+    b["motion_quality"][0] = 0
+    b["shape_scale"][0] = (2.0, 1.0, 1.0)
+    with pytest.raises(_lib.CCError):
+        g.add_bodies(b)

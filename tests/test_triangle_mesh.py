@@ -333,10 +333,11 @@ def cone_bowl(sectors: int = 12, radius: float = 3.0, slope_deg: float = 30.0):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("shape", ["sphere", "box"])
+@pytest.mark.parametrize("shape", ["sphere", "cylinder"])
 def test_bowl_uses_the_32_manifold_pool(gpu_lib, oracle_lib, shape):
-    """A sphere (or box) settled in the apex of a 12-facet bowl touches every facet with its own
-    normal: 12 manifolds for the one pair, as the reference's pool of 32 keeps them.  The pair
+    """A sphere (or an upright cylinder, on its rim) settled in the apex of a 12-facet bowl
+    touches every facet with its own normal: 12 manifolds for the one pair, as the reference's
+    pool of 32 keeps them.  The pair
     overflows the 4-manifold pool of the first passes and is run again with 32 (stats mesh_big);
     no pair outgrows 32 (mesh_reduced 0).  The manifolds match the oracle's at the same poses."""
     b = scenes.blank_bodies(2)
@@ -346,7 +347,7 @@ def test_bowl_uses_the_32_manifold_pool(gpu_lib, oracle_lib, shape):
     if shape == "sphere":
         scenes.set_sphere(b, 1, 1.0)
     else:
-        scenes.set_box(b, 1, (0.8, 0.8, 0.8))
+        scenes.set_cylinder(b, 1, 0.3, 1.0)
     b["position"][1] = (0.0, 2.5, 0.0)
     sc = scenes.Scene("bowl", b, dt=1 / 60, steps=60)
     sc.mesh = cone_bowl()
