@@ -1438,6 +1438,59 @@ struct PackedStore {
     __device__ void set_newt(int i, int t) { b->nw[i][j] = (uint8_t)t; }
 };
 
+// The geometry half of createTriangle (epa-convex-hull-builder.ts:179-345) for slot idx of the
+// polytope in store s: centroid, normal, closest distance and the interior flags.  Returns whether
+// the face's normal and centroid have dot(n, c) < 0, the defect test penetration.ts:485-486
+// takes on every new face.
+template <class S>
+__device__ bool tri_geom(S &s, int idx, int i1, int i2, int i3) {
+    int fl = 0;
+    R cls = 1.0 / 0.0;
+    V<R> y0 = s.Y(i1), y1 = s.Y(i2), y2 = s.Y(i3);
+    // centroid (:219-225): the division by 3 is a multiplication by 1/3 here
+    V<R> c{(y0.x + y1.x + y2.x) * R_THIRD, (y0.y + y1.y + y2.y) * R_THIRD, (y0.z + y1.z + y2.z) * R_THIRD};
+    V<R> y10 = y1 - y0, y20 = y2 - y0, y21 = y2 - y1;
+    R y20d = lsq(y20), y21d = lsq(y21);
+    // the interior test l0 > -1e-3, l1 > -1e-3, l0 + l1 < 1 + 1e-3 is taken on the numerators
+    // (det > 0); the lambdas of the triangle the result uses are divided out in epa()
+    V<R> n;
+    if (y20d < y21d) {
+        n = crs(y10, y20);
+        R nl = lsq(n);
+        if (nl > R_MIN_NORMAL_SQ) {
+            R cdn = dot(c, n);
+            cls = (s_abs(cdn) * cdn) / nl;
+            R y10d = lsq(y10), y1020 = dot(y10, y20);
+            R det = y10d * y20d - y1020 * y1020;
+            if (det > 0.0) {
+                R a = dot(y0, y10), b = dot(y0, y20);
+                R l0n = y1020 * b - y20d * a, l1n = y1020 * a - y10d * b;
+                fl |= TF_REL0;
+                if (l0n > -R_EPS_INTERIOR * det && l1n > -R_EPS_INTERIOR * det && l0n + l1n < R_ONE_PLUS_EPS * det)
+                    fl |= TF_INTERIOR;
+            }
+        }
+    } else {
+        n = crs(y10, y21);
+        R nl = lsq(n);
+        if (nl > R_MIN_NORMAL_SQ) {
+            R cdn = dot(c, n);
+            cls = (s_abs(cdn) * cdn) / nl;
+            R y10d = lsq(y10), y1021 = dot(y10, y21);
+            R det = y10d * y21d - y1021 * y1021;
+            if (det > 0.0) {
+                R a = dot(y1, y10), b = dot(y1, y21);
+                R l0n = y21d * a - y1021 * b, l1n = y1021 * a - y10d * b;
+                if (l0n > -R_EPS_INTERIOR * det && l1n > -R_EPS_INTERIOR * det && l0n + l1n < R_ONE_PLUS_EPS * det)
+                    fl |= TF_INTERIOR;
+            }
+        }
+    }
+    s.set_geom(idx, n, c, cls);
+    s.set_flags(idx, fl);
+    return dot(n, c) < 0.0;
+}
+
 // An integer key with the order of the doubles it comes from (-0 and +0 equal, no NaNs here):
 // the heap and the face selection compare closest distances with integer instructions, which
 // keeps them off the FP64 pipe.
@@ -1504,8 +1557,8 @@ struct Hull {
         st.set_nb(t1, e1, t2, e2);
         st.set_nb(t2, e2, t1, e1);
     }
-    // createTriangle epa-convex-hull-builder.ts:179-345
-    __device__ int create(int i1, int i2, int i3) {
+    // createTriangle epa-convex-hull-builder.ts:179-345: a slot (alloc) and its geometry (tri_geom)
+    __device__ int alloc(int i1, int i2, int i3) {
         int idx;
         if (nfree > 0) {
             idx = st.fr(--nfree);
@@ -1516,52 +1569,13 @@ struct Hull {
             }
             idx = ntri++;
         }
-        int fl = 0;
-        R cls = 1.0 / 0.0;
         st.set_st(idx, i1, i2, i3);
         for (int k = 0; k < 3; k++) st.set_nb(idx, k, -1, 0);
-        V<R> y0 = st.Y(i1), y1 = st.Y(i2), y2 = st.Y(i3);
-        // centroid (:219-225): the division by 3 is a multiplication by 1/3 here
-        V<R> c{(y0.x + y1.x + y2.x) * R_THIRD, (y0.y + y1.y + y2.y) * R_THIRD, (y0.z + y1.z + y2.z) * R_THIRD};
-        V<R> y10 = y1 - y0, y20 = y2 - y0, y21 = y2 - y1;
-        R y20d = lsq(y20), y21d = lsq(y21);
-        // the interior test l0 > -1e-3, l1 > -1e-3, l0 + l1 < 1 + 1e-3 is taken on the numerators
-        // (det > 0); the lambdas of the triangle the result uses are divided out in epa()
-        V<R> n;
-        if (y20d < y21d) {
-            n = crs(y10, y20);
-            R nl = lsq(n);
-            if (nl > R_MIN_NORMAL_SQ) {
-                R cdn = dot(c, n);
-                cls = (s_abs(cdn) * cdn) / nl;
-                R y10d = lsq(y10), y1020 = dot(y10, y20);
-                R det = y10d * y20d - y1020 * y1020;
-                if (det > 0.0) {
-                    R a = dot(y0, y10), b = dot(y0, y20);
-                    R l0n = y1020 * b - y20d * a, l1n = y1020 * a - y10d * b;
-                    fl |= TF_REL0;
-                    if (l0n > -R_EPS_INTERIOR * det && l1n > -R_EPS_INTERIOR * det && l0n + l1n < R_ONE_PLUS_EPS * det)
-                        fl |= TF_INTERIOR;
-                }
-            }
-        } else {
-            n = crs(y10, y21);
-            R nl = lsq(n);
-            if (nl > R_MIN_NORMAL_SQ) {
-                R cdn = dot(c, n);
-                cls = (s_abs(cdn) * cdn) / nl;
-                R y10d = lsq(y10), y1021 = dot(y10, y21);
-                R det = y10d * y21d - y1021 * y1021;
-                if (det > 0.0) {
-                    R a = dot(y1, y10), b = dot(y1, y21);
-                    R l0n = y21d * a - y1021 * b, l1n = y1021 * a - y10d * b;
-                    if (l0n > -R_EPS_INTERIOR * det && l1n > -R_EPS_INTERIOR * det && l0n + l1n < R_ONE_PLUS_EPS * det)
-                        fl |= TF_INTERIOR;
-                }
-            }
-        }
-        st.set_geom(idx, n, c, cls);
-        st.set_flags(idx, fl);
+        return idx;
+    }
+    __device__ int create(int i1, int i2, int i3) {
+        int idx = alloc(i1, i2, i3);
+        if (idx >= 0) tri_geom(st, idx, i1, i2, i3);
         return idx;
     }
     // barycentric lambdas of triangle t (the second half of createTriangle)
@@ -1720,6 +1734,30 @@ struct Hull {
             link(st.newt(i), 1, st.newt(in), 2);
         }
         return ne;
+    }
+    // addPoint in two halves around the new faces' geometry, which the lock-step pass spreads
+    // over the warp (warp_tri_geom): the horizon and the new faces' slots in addPoint's order,
+    // then, once their geometry is written, the queue and the links
+    __device__ int add_point_slots(int ft, int idx, const unsigned long long *mask) {
+        int ne = find_edge(ft, st.Y(idx), mask);
+        if (ne < 0) return -1;
+        for (int i = 0; i < ne; i++) {
+            int nt = alloc(st.edge_st(i), st.edge_st((i + 1) % ne), idx);
+            if (nt < 0) return -1;
+            st.set_newt(i, nt);
+        }
+        return ne;
+    }
+    __device__ void add_point_links(int ne, R closest) {
+        for (int i = 0; i < ne; i++) {
+            int nt = st.newt(i);
+            if (((flags(nt) & TF_INTERIOR) && cls(nt) < closest) || cls(nt) < 0.0) push(nt);
+        }
+        for (int i = 0; i < ne; i++) {
+            int in = (i + 1) % ne;
+            link(st.newt(i), 0, st.edge_nt(i), st.edge_ne(i));
+            link(st.newt(i), 1, st.newt(in), 2);
+        }
     }
     template <class SA, class SB>
     __device__ int add_sup(const SA &A, const SB &B, V<R> d) {
@@ -1929,6 +1967,56 @@ struct EpaLane {
     __device__ bool running() const { return phase == EPA_GROW || phase == EPA_EXPAND; }
 };
 
+// The geometry of the new faces of every lane of the warp, spread over the lanes.  Lane l of
+// the warp owns ne_l new faces (0 when it has none) whose slots and corners add_point_slots has
+// written; the warp's faces are numbered in lane order and lane k computes faces k, k + 32, ...,
+// reading the owner's points and writing the owner's face slots in the block's packed store.
+// Each face is computed exactly as Hull::create computes it, so the polytopes are bit-identical
+// to the one-lane-at-a-time construction.  Returns whether one of the calling lane's own new faces
+// failed the defect test.  Every lane of the warp calls it together.
+__device__ bool warp_tri_geom(const PackedStore &st, int ne, int ni) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    int incl = ne;
+    for (int o = 1; o < 32; o <<= 1) {
+        int v = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(FULL, incl, 31);
+    const int excl = incl - ne;
+    bool defect = false;
+    __syncwarp();  // the owners' corners and slots are visible to the lanes that build the faces
+    for (int r = 0; r < total; r += 32) {
+        const int f = r + lane;
+        // the owner of face f: the first lane whose inclusive count is above f
+        int owner = 0;
+        for (int step = 16; step > 0; step >>= 1) {
+            int v = __shfl_sync(FULL, incl, owner + step - 1);
+            if (v <= f) owner += step;
+        }
+        const int o_ne = __shfl_sync(FULL, ne, owner & 31);
+        const int o_ex = __shfl_sync(FULL, excl, owner & 31);
+        const int o_ni = __shfl_sync(FULL, ni, owner & 31);
+        bool d = false;
+        if (f < total) {
+            PackedStore so = st;
+            so.j = (threadIdx.x & ~31) + owner;
+            const int i = f - o_ex;
+            const int nxt = i + 1 < o_ne ? i + 1 : 0;
+            d = tri_geom(so, so.newt(i), so.edge_st(i), so.edge_st(nxt), o_ni);
+        }
+        const unsigned m = __ballot_sync(FULL, d);
+        // this lane's faces among the round's 32
+        const int lo = max(excl - r, 0), hi = min(excl + ne - r, 32);
+        if (lo < hi) {
+            const unsigned bits = (hi - lo == 32 ? FULL : ((1u << (hi - lo)) - 1u)) << lo;
+            if (m & bits) defect = true;
+        }
+    }
+    __syncwarp();  // the faces' geometry is visible to their owners
+    return defect;
+}
+
 // one round of epa()'s growth / expansion loops for the lanes that are running
 template <class S, class SA, class SB>
 __device__ void epa_round(EpaLane &L, Hull<S> &h, const SA &A, const SB &B, R tol) {
@@ -2016,11 +2104,17 @@ __device__ void epa_round(EpaLane &L, Hull<S> &h, const SA &A, const SB &B, R to
             }
         }
     }
-    // the horizon and the new faces
+    // the horizon and the new faces: the slots per lane, the faces' geometry over the warp, then
+    // the queue and the links per lane
+    int ne = -1;
     if (work) {
         const int upto = __reduce_max_sync(__activemask(), h.ntri);
         const unsigned long long mask = h.facing_mask(h.st.Y(ni), upto);
-        int ne = h.add_point(t, ni, L.phase == EPA_GROW ? MAXD : L.closest, &mask);
+        ne = h.add_point_slots(t, ni, &mask);
+    }
+    const bool defect = warp_tri_geom(h.st, ne > 0 ? ne : 0, ni);
+    if (work) {
+        if (ne >= 0) h.add_point_links(ne, L.phase == EPA_GROW ? MAXD : L.closest);
         if (L.phase == EPA_GROW) {
             if (ne < 0) {
                 L.phase = EPA_FAIL;
@@ -2031,14 +2125,6 @@ __device__ void epa_round(EpaLane &L, Hull<S> &h, const SA &A, const SB &B, R to
         } else if (ne < 0) {
             L.phase = EPA_DONE;
         } else {
-            bool defect = false;
-            for (int k = 0; k < ne; k++) {
-                int q = h.st.newt(k);
-                if (dot(h.st.normal(q), h.st.centroid(q)) < 0.0) {
-                    defect = true;
-                    break;
-                }
-            }
             if (defect) {
                 V<R> nn = -tn;
                 V<R> w2 = A.get(nn) - B.get(tn);

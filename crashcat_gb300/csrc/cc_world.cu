@@ -435,8 +435,12 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
             return r;
         }
         w.epa_items = p;
-        // EPA threads scale with the world: about one per 8 bodies, 1,024 to epa_default_max_threads()
+        // EPA threads scale with the world: about one per 8 bodies, 1,024 to epa_default_max_threads(),
+        // and two blocks per SM (the tuner's smallest shape) once the world has that many bodies, so
+        // that every SM's FP64 pipe takes part
         int et = cap / 8;
+        const int two_per_sm = device_sm_count() * 2 * 64;
+        if (et < two_per_sm) et = cap < two_per_sm ? cap : two_per_sm;
         et = et < 1024 ? 1024 : (et > epa_default_max_threads() ? epa_default_max_threads() : et);
         if (const char *e = getenv("CRASHCAT_EPA_THREADS")) {
             int v = atoi(e);
