@@ -51,6 +51,12 @@ enum : int { OVF_PAIRS = 1, OVF_MANIFOLDS = 2, OVF_EPA = 4, OVF_ISLAND = 8, OVF_
              OVF_TIMEOUT = 64 };
 
 // Device-resident counters of one step (one 128-byte line).
+// Islands of the per-thread and per-warp solve tiers are listed by size, most constraints first:
+// the per-thread tier by its contact count (0 to 15, and 16 or more), the per-warp tier by the
+// power of two above its contact count less one (9-16, 17-32, 33-64, 65-128, 129-256).  Each
+// bucket is a list of the body capacity.
+constexpr int SMALL_BUCKETS = 17, MID_BUCKETS = 5;
+
 struct DevCounters {
     int num_pairs;
     int num_manifolds;
@@ -82,7 +88,10 @@ struct DevCounters {
     int mesh_reduced;     // mesh pairs whose hits needed more manifolds than the reference's pool of 32
     int num_mesh_big;     // mesh pairs run again with the 32-manifold pool (their hits overflowed 4)
     int num_compound_pairs;  // broadphase pairs with a compound body and no mesh
-    int pad2[3];
+    int small_bucket[SMALL_BUCKETS];  // per-thread tier islands by contact count
+    int mid_bucket[MID_BUCKETS];      // per-warp tier islands by size class
+    int mid_cursor_s;                 // cursor of the per-warp tier's small instance
+    int pad2[1];
 };
 
 // Settings copied into constant memory once per world.
@@ -487,8 +496,10 @@ struct DevWorld {
     int epa_threads;       // threads of the packed EPA pass
     int epa_packed_points; // support points a packed polytope may hold before its item falls back
     int epa_fetch_warp;    // EPA items taken 32 at a time per warp (1) or one at a time per thread (0)
-    cudaStream_t aux_stream;  // second stream: the per-CTA island solve runs beside the per-warp one
-    cudaEvent_t ev_fork, ev_join;
+    cudaStream_t aux_stream;   // second stream: the per-CTA island solve runs beside the per-warp one
+    cudaStream_t aux2_stream;  // third stream: the per-thread island solve beside both
+    cudaStream_t aux3_stream;  // fourth stream: the per-warp solve of the islands past 32 contacts
+    cudaEvent_t ev_fork, ev_join, ev_join2, ev_join3;
     int warp_blocks_per_sm;  // launch shape of the per-warp island solve
     int warp_carveout;       // shared-memory carveout (percent) of the per-warp island solve
     // persistent contact cache (double buffered by parity)

@@ -37,6 +37,9 @@ constexpr int SMALL_ISLAND_MAX_JOINTS = 16;  // bound of the per-thread class's 
 // islands above the per-thread class and within these limits run on one warp
 constexpr int WARP_MAX_CONS = 256;
 constexpr int WARP_MAX_BODIES = 128;
+// The per-warp tier in two instances: islands of at most 32 contacts and 48 bodies (nearly all of
+// them) with a small shared-memory footprint, so that more warps fit on an SM, and the rest.
+constexpr int WARP_S_CONS = 32, WARP_S_BODIES = 48;
 constexpr int WARP_MAX_COLOURS = 64;  // colours past this one are swept by one lane in order
 
 struct CacheTables {
@@ -535,6 +538,20 @@ __global__ void k_island_scatter(DevWorld w) {
 }
 
 // split islands into the per-thread and per-CTA classes
+// the per-warp tier's size class of an island of nc contacts: 9-16 -> 0, 17-32 -> 1, ... 129-256 -> 4
+__device__ __forceinline__ int mid_size_class(int nc) { return 31 - __clz(max(nc - 1, 1)) - 3; }
+
+// Entry k of a bucketed island list, the buckets taken from the last (largest islands) down;
+// -1 past the end.
+__device__ __forceinline__ int bucketed_island(const int *list, size_t cap, const int *counts, int nbuckets, int k) {
+    for (int b = nbuckets - 1; b >= 0; b--) {
+        const int c = counts[b];
+        if (k < c) return list[(size_t)b * cap + k];
+        k -= c;
+    }
+    return -1;
+}
+
 __global__ void k_island_classify(DevWorld w, int *small_list, int *large_list) {
     int ni = w.ctr->num_islands;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x) {
@@ -556,11 +573,17 @@ __global__ void k_island_classify(DevWorld w, int *small_list, int *large_list) 
                 w.large_joint_list[k] = i;
             }
         } else if (nc <= c_settings.small_island_max_cons && nb <= SMALL_ISLAND_MAX_BODIES) {
-            int k = atomicAdd(&w.ctr->num_small_islands, 1);
-            small_list[k] = i;
+            atomicAdd(&w.ctr->num_small_islands, 1);
+            const int b = min(nc, SMALL_BUCKETS - 1);
+            int k = atomicAdd(&w.ctr->small_bucket[b], 1);
+            small_list[(size_t)b * w.cap + k] = i;
         } else if (nc <= WARP_MAX_CONS && nb <= WARP_MAX_BODIES) {
-            int k = atomicAdd(&w.ctr->num_mid_islands, 1);
-            w.mid_list[k] = i;
+            atomicAdd(&w.ctr->num_mid_islands, 1);
+            // classes 0 and 1 (at most 32 contacts) go to the small instance when their bodies fit
+            int b = min(max(mid_size_class(nc), 0), MID_BUCKETS - 1);
+            if (b < 2 && nb > WARP_S_BODIES) b = 2;
+            int k = atomicAdd(&w.ctr->mid_bucket[b], 1);
+            w.mid_list[(size_t)b * w.cap + k] = i;
         } else {
             int k = atomicAdd(&w.ctr->num_large_islands, 1);
             large_list[k] = i;
@@ -892,8 +915,15 @@ __global__ void __launch_bounds__(128) k_solve_small(DevWorld w, CacheTables ct,
     if (islands_failed(w)) return;
     int ns = JOINTS ? w.ctr->num_small_joint_islands : w.ctr->num_small_islands;
     CacheRecord *crecs = ct.recs[*ct.parity];
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
-        int isl = small_list[s];
+    // Islands without joints come by size, most contacts first, in chunks of 32: a warp's lanes
+    // solve islands of one size.  Chunk c goes to block c mod gridDim.x, so the chunks of the
+    // largest islands are spread over the blocks (and the SMs) rather than packed into the first.
+    const int wpb = blockDim.x >> 5, lane = threadIdx.x & 31;
+    for (int r = 0;; r++) {
+        const int s = JOINTS ? (r * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x
+                             : ((r * wpb + (threadIdx.x >> 5)) * gridDim.x + blockIdx.x) * 32 + lane;
+        if (s >= ns) break;
+        int isl = JOINTS ? small_list[s] : bucketed_island(small_list, w.cap, w.ctr->small_bucket, SMALL_BUCKETS, s);
         int vel_iters, pos_iters;  // the island's iteration counts (islands.ts:344-386)
         island_iterations(w, isl, c_settings.vel_iters, c_settings.pos_iters, vel_iters, pos_iters);
         int nb = w.island_body_count[isl], nc = w.island_cons_count[isl];
@@ -1315,28 +1345,34 @@ __global__ void __launch_bounds__(LARGE_BLOCK) k_solve_large(DevWorld w, CacheTa
 constexpr int WARP_BLOCK = 128;
 constexpr int WARPS_PER_BLOCK = WARP_BLOCK / 32;
 
-struct WarpIsland {
-    uint32_t key[WARP_MAX_CONS];  // sort key, then colour
-    int ia[WARP_MAX_CONS];        // body A id, then local index of A (-1: not in the island)
-    int ib[WARP_MAX_CONS];
-    int idx[WARP_MAX_CONS];       // constraint index in rank order
-    int sorted[WARP_MAX_CONS];    // ranks grouped by colour, rank order inside a colour
+// one warp's island in shared memory, for islands of at most MC contacts and MB bodies
+template <int MC, int MB>
+struct WarpIslandT {
+    uint32_t key[MC];  // sort key, then colour
+    int ia[MC];        // body A id, then local index of A (-1: not in the island)
+    int ib[MC];
+    int idx[MC];       // constraint index in rank order
+    int sorted[MC];    // ranks grouped by colour, rank order inside a colour
     int cstart[WARP_MAX_COLOURS + 2];
-    float4 v[WARP_MAX_BODIES];    // linear velocity | inverse mass
-    float4 av[WARP_MAX_BODIES];   // angular velocity | flags (bit pattern)
-    float4 I0[WARP_MAX_BODIES];   // world inverse inertia xx xy xz yy
-    float2 I1[WARP_MAX_BODIES];   // yz zz
-    int body[WARP_MAX_BODIES];
-    int claim[WARP_MAX_BODIES];
+    float4 v[MB];    // linear velocity | inverse mass
+    float4 av[MB];   // angular velocity | flags (bit pattern)
+    float4 I0[MB];   // world inverse inertia xx xy xz yy
+    float2 I1[MB];   // yz zz
+    int body[MB];
+    int claim[MB];
 };
+using WarpIsland = WarpIslandT<WARP_MAX_CONS, WARP_MAX_BODIES>;
+using WarpIslandS = WarpIslandT<WARP_S_CONS, WARP_S_BODIES>;
 
-__device__ __forceinline__ bool rank_less(const WarpIsland &s, int x, int y) {
+template <class WI>
+__device__ __forceinline__ bool rank_less(const WI &s, int x, int y) {
     if (s.key[x] != s.key[y]) return s.key[x] < s.key[y];
     if (s.ia[x] != s.ia[y]) return s.ia[x] < s.ia[y];
     return s.ib[x] < s.ib[y];
 }
 
-__device__ __forceinline__ BodyRef warp_body(const DevWorld &w, const WarpIsland &s, int local, int global) {
+template <class WI>
+__device__ __forceinline__ BodyRef warp_body(const DevWorld &w, const WI &s, int local, int global) {
     if (local < 0) return load_body(w, global);
     BodyRef b;
     float4 v = s.v[local], av = s.av[local];
@@ -1351,27 +1387,42 @@ __device__ __forceinline__ BodyRef warp_body(const DevWorld &w, const WarpIsland
     b.I = Sym3{i0.x, i0.y, i0.z, i0.w, i1.x, i1.y};
     return b;
 }
-__device__ __forceinline__ void warp_store(WarpIsland &s, int local, const BodyRef &b) {
+template <class WI>
+__device__ __forceinline__ void warp_store(WI &s, int local, const BodyRef &b) {
     if (local < 0 || b.motion != DYNAMIC) return;
     s.v[local] = make_float4(b.v.x, b.v.y, b.v.z, s.v[local].w);
     s.av[local] = make_float4(b.w.x, b.w.y, b.w.z, s.av[local].w);
 }
 
+// WI: the shared-memory island (its capacity); the islands of size classes [b0, b1) of the
+// per-warp list, taken from *cursor after the first round
+template <class WI>
 __global__ void __launch_bounds__(WARP_BLOCK) k_solve_warp(DevWorld w, CacheTables ct, float dt, float ratio,
-                                                            int phase) {
+                                                            int phase, int b0, int b1, int *cursor) {
     if (islands_failed(w)) return;
-    extern __shared__ WarpIsland s_isl[];  // WARPS_PER_BLOCK entries
+    extern __shared__ __align__(16) unsigned char warp_smem_raw[];  // WARPS_PER_BLOCK islands
     const int lane = threadIdx.x & 31;
-    WarpIsland &S = s_isl[threadIdx.x >> 5];
+    WI &S = reinterpret_cast<WI *>(warp_smem_raw)[threadIdx.x >> 5];
     const unsigned FULL = 0xffffffffu;
-    const int nmid = w.ctr->num_mid_islands;
+    int nmid = 0;
+    for (int b = b0; b < b1; b++) nmid += w.ctr->mid_bucket[b];
     CacheRecord *crecs = ct.recs[*ct.parity];
+    // The first island of warp k of every block is island k x gridDim.x + blockIdx.x of the list
+    // (largest first), so the largest islands start together on different SMs; the rest come
+    // from the cursor, after the first round's.
+    const int nwarps = gridDim.x * WARPS_PER_BLOCK;
+    bool first = true;
     while (true) {
         int li = 0;
-        if (lane == 0) li = atomicAdd(&w.ctr->mid_cursor, 1);
+        if (first)
+            li = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+        else if (lane == 0)
+            li = nwarps + atomicAdd(cursor, 1);
         li = __shfl_sync(FULL, li, 0);
+        first = false;
         if (li >= nmid) break;
-        const int isl = w.mid_list[li];
+        // the largest islands are taken first, so the last ones to finish are small
+        const int isl = bucketed_island(w.mid_list + (size_t)b0 * w.cap, w.cap, w.ctr->mid_bucket + b0, b1 - b0, li);
         int vel_iters, pos_iters;
         island_iterations(w, isl, c_settings.vel_iters, c_settings.pos_iters, vel_iters, pos_iters);
         const int nb = w.island_body_count[isl], nc = w.island_cons_count[isl];
@@ -1972,19 +2023,55 @@ void launch_solver(DevWorld &w, float dt, float ratio, cudaStream_t s, cudaEvent
     CacheTables ct = tables_of(w);
     const bool joints = w.num_hinges + w.num_swings + w.num_others + w.num_sixdofs > 0;
     // the per-warp tier takes its islands from a cursor: rewind it for the second pass
-    if (phase == SOLVE_POSITION) cudaMemsetAsync(&w.ctr->mid_cursor, 0, sizeof(int), s);
-    k_solve_small<false><<<grid_for(w.n, 128, 16), 128, 0, s>>>(w, ct, w.small_list, dt, ratio, phase);
-    if (joints)
-        k_solve_small<true><<<grid_for(w.n, 128, 16), 128, 0, s>>>(w, ct, w.small_joint_list, dt, ratio, phase);
-    if (mid) cudaEventRecord(mid, s);
-    static bool warp_smem_set = false;  // set on the first (eager) step, before any graph capture
-    const size_t warp_smem = sizeof(WarpIsland) * WARPS_PER_BLOCK;
-    if (!warp_smem_set) {
-        cudaFuncSetAttribute(k_solve_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)warp_smem);
-        warp_smem_set = true;
+    if (phase == SOLVE_POSITION) {
+        cudaMemsetAsync(&w.ctr->mid_cursor, 0, sizeof(int), s);
+        cudaMemsetAsync(&w.ctr->mid_cursor_s, 0, sizeof(int), s);
     }
-    if (w.warp_carveout >= 0)
-        cudaFuncSetAttribute(k_solve_warp, cudaFuncAttributePreferredSharedMemoryCarveout, w.warp_carveout);
+    // The three tiers hold disjoint islands and run side by side on three streams: the per-thread
+    // tier on the third, the per-CTA tier on the second, the per-warp tier on the step's stream.
+    // The stage profiler (mid set) runs the per-thread tier first, alone, to time it apart.
+    const bool split = mid != nullptr;
+    cudaStream_t s_small = s;
+    if (!split) {
+        cudaEventRecord(w.ev_fork, s);
+        cudaStreamWaitEvent(w.aux2_stream, w.ev_fork, 0);
+        s_small = w.aux2_stream;
+    }
+    k_solve_small<false><<<grid_for(w.n, 128, 16), 128, 0, s_small>>>(w, ct, w.small_list, dt, ratio, phase);
+    if (joints)
+        k_solve_small<true><<<grid_for(w.n, 128, 16), 128, 0, s_small>>>(w, ct, w.small_joint_list, dt, ratio,
+                                                                        phase);
+    if (split)
+        cudaEventRecord(mid, s);
+    else
+        cudaEventRecord(w.ev_join2, w.aux2_stream);
+    // the per-warp tier's two instances: their shared memory, and for the small one the blocks
+    // that are resident at once (its first round assigns islands to every warp up front)
+    static bool warp_attr_set = false;  // set on the first (eager) step, before any graph capture
+    static int warp_s_blocks_per_sm = 1;
+    static bool warp_s_sized = false;  // sized after the carveout is first set
+    const size_t warp_smem = sizeof(WarpIsland) * WARPS_PER_BLOCK;
+    const size_t warp_s_smem = sizeof(WarpIslandS) * WARPS_PER_BLOCK;
+    if (!warp_attr_set) {
+        cudaFuncSetAttribute(k_solve_warp<WarpIsland>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)warp_smem);
+        cudaFuncSetAttribute(k_solve_warp<WarpIslandS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)warp_s_smem);
+        warp_attr_set = true;
+    }
+    if (w.warp_carveout >= 0) {
+        cudaFuncSetAttribute(k_solve_warp<WarpIsland>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             w.warp_carveout);
+        cudaFuncSetAttribute(k_solve_warp<WarpIslandS>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             w.warp_carveout);
+    }
+    if (!warp_s_sized) {
+        int nbk = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbk, k_solve_warp<WarpIslandS>, WARP_BLOCK, warp_s_smem) ==
+                cudaSuccess &&
+            nbk > 0)
+            warp_s_blocks_per_sm = nbk;
+        warp_s_sized = true;
+    }
     // the per-CTA and per-warp classes hold disjoint islands: run them side by side
     cudaEventRecord(w.ev_fork, s);
     cudaStreamWaitEvent(w.aux_stream, w.ev_fork, 0);
@@ -1994,8 +2081,16 @@ void launch_solver(DevWorld &w, float dt, float ratio, cudaStream_t s, cudaEvent
         k_solve_large<true><<<device_sm_count() * 2, LARGE_BLOCK, 0, w.aux_stream>>>(
             w, ct, w.large_joint_list, w.scratch_order, w.scratch_colour, w.scratch_claim, dt, ratio, phase);
     cudaEventRecord(w.ev_join, w.aux_stream);
-    k_solve_warp<<<device_sm_count() * w.warp_blocks_per_sm, WARP_BLOCK, warp_smem, s>>>(w, ct, dt, ratio, phase);
+    // the per-warp tier's large instance on a fourth stream, its small instance on the step's
+    cudaStreamWaitEvent(w.aux3_stream, w.ev_fork, 0);
+    k_solve_warp<WarpIsland><<<device_sm_count() * w.warp_blocks_per_sm, WARP_BLOCK, warp_smem, w.aux3_stream>>>(
+        w, ct, dt, ratio, phase, 2, MID_BUCKETS, &w.ctr->mid_cursor);
+    cudaEventRecord(w.ev_join3, w.aux3_stream);
+    k_solve_warp<WarpIslandS><<<device_sm_count() * warp_s_blocks_per_sm, WARP_BLOCK, warp_s_smem, s>>>(
+        w, ct, dt, ratio, phase, 0, 2, &w.ctr->mid_cursor_s);
     cudaStreamWaitEvent(s, w.ev_join, 0);
+    cudaStreamWaitEvent(s, w.ev_join3, 0);
+    if (!split) cudaStreamWaitEvent(s, w.ev_join2, 0);
     // giant islands: a cooperative launch (all blocks co-resident), after the other tiers so that
     // it runs alone; it returns at once when the step has no giant island
     cudaLaunchConfig_t cfg = {};

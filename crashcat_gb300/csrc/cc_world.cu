@@ -488,12 +488,12 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
     }
     ALLOC(cache_parity, 1);
     ALLOC(root_flag, cap);
-    ALLOC(small_list, cap);
+    ALLOC(small_list, (size_t)cap * SMALL_BUCKETS);
     ALLOC(large_list, cap);
     ALLOC(scratch_order, w.max_manifolds);
     ALLOC(scratch_colour, w.max_manifolds);
     ALLOC(scratch_claim, (size_t)cap + (size_t)w.max_manifolds + 16);
-    ALLOC(mid_list, cap);
+    ALLOC(mid_list, (size_t)cap * MID_BUCKETS);
     ALLOC(contact_event, w.max_manifolds);
     ALLOC(removed_keys, w.max_manifolds);
     ALLOC(body_local, cap);
@@ -515,8 +515,12 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
     if (w.giant_blocks <= 0) w.giant_min = 0x7fffffff;
     if ((r = cuda_ok(cudaStreamCreateWithFlags(&W->stream, cudaStreamNonBlocking))) != CC_OK ||
         (r = cuda_ok(cudaStreamCreateWithFlags(&w.aux_stream, cudaStreamNonBlocking))) != CC_OK ||
+        (r = cuda_ok(cudaStreamCreateWithFlags(&w.aux2_stream, cudaStreamNonBlocking))) != CC_OK ||
+        (r = cuda_ok(cudaStreamCreateWithFlags(&w.aux3_stream, cudaStreamNonBlocking))) != CC_OK ||
+        (r = cuda_ok(cudaEventCreateWithFlags(&w.ev_join3, cudaEventDisableTiming))) != CC_OK ||
         (r = cuda_ok(cudaEventCreateWithFlags(&w.ev_fork, cudaEventDisableTiming))) != CC_OK ||
-        (r = cuda_ok(cudaEventCreateWithFlags(&w.ev_join, cudaEventDisableTiming))) != CC_OK) {
+        (r = cuda_ok(cudaEventCreateWithFlags(&w.ev_join, cudaEventDisableTiming))) != CC_OK ||
+        (r = cuda_ok(cudaEventCreateWithFlags(&w.ev_join2, cudaEventDisableTiming))) != CC_OK) {
         cc_world_destroy(W);
         return r;
     }
@@ -575,8 +579,12 @@ int cc_world_destroy(cc_world *W) {
     if (W->ev_end) cudaEventDestroy(W->ev_end);
     if (W->stream) cudaStreamDestroy(W->stream);
     if (w.aux_stream) cudaStreamDestroy(w.aux_stream);
+    if (w.aux2_stream) cudaStreamDestroy(w.aux2_stream);
+    if (w.aux3_stream) cudaStreamDestroy(w.aux3_stream);
+    if (w.ev_join3) cudaEventDestroy(w.ev_join3);
     if (w.ev_fork) cudaEventDestroy(w.ev_fork);
     if (w.ev_join) cudaEventDestroy(w.ev_join);
+    if (w.ev_join2) cudaEventDestroy(w.ev_join2);
     delete W;
     return CC_OK;
 }
