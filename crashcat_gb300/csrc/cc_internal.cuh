@@ -56,6 +56,9 @@ enum : int { OVF_PAIRS = 1, OVF_MANIFOLDS = 2, OVF_EPA = 4, OVF_ISLAND = 8, OVF_
 // power of two above its contact count less one (9-16, 17-32, 33-64, 65-128, 129-256).  Each
 // bucket is a list of the body capacity.
 constexpr int SMALL_BUCKETS = 17, MID_BUCKETS = 5;
+// The narrowphase takes the broadphase pairs grouped by the shapes' collide routine
+// (pair_class), so that the lanes of a warp run one routine.
+constexpr int PAIR_CLASSES = 8;
 
 struct DevCounters {
     int num_pairs;
@@ -91,6 +94,8 @@ struct DevCounters {
     int small_bucket[SMALL_BUCKETS];  // per-thread tier islands by contact count
     int mid_bucket[MID_BUCKETS];      // per-warp tier islands by size class
     int mid_cursor_s;                 // cursor of the per-warp tier's small instance
+    int pair_class[PAIR_CLASSES];     // broadphase pairs per collide class
+    int pair_class_fill[PAIR_CLASSES];
     int pad2[1];
 };
 
@@ -462,6 +467,7 @@ struct DevWorld {
     int *pair_offset;
     int2 *pair_slots;     // per body fixed slots
     int2 *pairs;
+    int *pair_order;  // the pairs' indices grouped by collide class (k_pair_order)
     // narrowphase
     Manifold *manifolds;
     int *manifold_valid;

@@ -1094,13 +1094,60 @@ struct EpaItem {
     int tri;  // -1: a convex pair; else a = the convex body, b = the mesh body, this triangle
 };
 
+// The collide class of a pair, by the shapes' collide routine: the pairs the mesh and compound
+// passes take, plane pairs, sphere pairs, then the GJK pairs by their most expensive shape.
+__device__ __forceinline__ int pair_class(uint32_t fa, uint32_t fb) {
+    const int sa = shape_of(fa), sb = shape_of(fb);
+    const int lo = min(sa, sb), hi = max(sa, sb);
+    if (lo == SHAPE_EMPTY || hi == SHAPE_EMPTY || sa == SHAPE_MESH || sb == SHAPE_MESH || sa == SHAPE_COMPOUND ||
+        sb == SHAPE_COMPOUND)
+        return 0;
+    if (sa == SHAPE_PLANE || sb == SHAPE_PLANE) return 1;
+    if (sa == SHAPE_HULL || sb == SHAPE_HULL) return 2;
+    if (lo == SHAPE_SPHERE && hi == SHAPE_SPHERE) return 3;
+    if (sa == SHAPE_CYLINDER || sb == SHAPE_CYLINDER) return 4;
+    if (sa == SHAPE_CAPSULE || sb == SHAPE_CAPSULE) return 5;
+    if (sa == SHAPE_SPHERE || sb == SHAPE_SPHERE) return 6;  // a sphere against a box
+    return 7;                                                // box against box
+}
+
+// k_pair_order: the pairs' indices grouped by collide class into w.pair_order (classes in order,
+// any order inside a class).  Pass 0 counts the classes, pass 1 places the indices; one atomic
+// per class present in a warp.
+template <int PASS>
+__global__ void k_pair_order(DevWorld w) {
+    const int np = min(w.ctr->num_pairs, w.max_pairs);
+    const int lane = threadIdx.x & 31;
+    for (int base = blockIdx.x * blockDim.x; base < np; base += gridDim.x * blockDim.x) {
+        const int pi = base + threadIdx.x;  // the warp's lanes stay together through the loop
+        const bool live = pi < np;
+        int c = -1;
+        if (live) {
+            const int2 pr = w.pairs[pi];
+            c = pair_class(w.flags[pr.x], w.flags[pr.y]);
+        }
+        const unsigned same = __match_any_sync(0xffffffffu, c);
+        const int leader = __ffs(same) - 1;
+        int slot = 0;
+        if (live && lane == leader)
+            slot = atomicAdd(PASS == 0 ? &w.ctr->pair_class[c] : &w.ctr->pair_class_fill[c], __popc(same));
+        slot = __shfl_sync(same, slot, leader);
+        if (PASS == 1 && live) {
+            int off = 0;
+            for (int k = 0; k < c; k++) off += w.ctr->pair_class[k];
+            w.pair_order[off + slot + __popc(same & ((1u << lane) - 1u))] = pi;
+        }
+    }
+}
+
 // narrowphase for one pair: order A/B (update.ts:74), dispatch, GJK
 // HULLS: the pairs with a convex hull (launched only when the world has hulls); the other
 // instance takes every other pair, without the hull code
 template <bool HULLS>
 __global__ void __launch_bounds__(128) k_narrowphase(DevWorld w, EpaItem *epa_items) {
     int np = min(w.ctr->num_pairs, w.max_pairs);
-    for (int pi = blockIdx.x * blockDim.x + threadIdx.x; pi < np; pi += gridDim.x * blockDim.x) {
+    for (int pk = blockIdx.x * blockDim.x + threadIdx.x; pk < np; pk += gridDim.x * blockDim.x) {
+        const int pi = w.pair_order[pk];  // grouped by collide class
         int2 pr = w.pairs[pi];
         int a = pr.x, b = pr.y;
         uint32_t fa = w.flags[a], fb = w.flags[b];
@@ -4936,6 +4983,8 @@ void launch_mesh_narrowphase(DevWorld &w, int pass, cudaStream_t s);
 
 void launch_narrowphase(DevWorld &w, float, cudaStream_t s, cudaEvent_t mid) {
     EpaItem *items = (EpaItem *)w.epa_items;
+    k_pair_order<0><<<grid_for(w.max_pairs, 256), 256, 0, s>>>(w);
+    k_pair_order<1><<<grid_for(w.max_pairs, 256), 256, 0, s>>>(w);
     k_narrowphase<false><<<device_sm_count() * 8, 128, 0, s>>>(w, items);
     if (w.num_hulls > 0) k_narrowphase<true><<<device_sm_count() * 8, 128, 0, s>>>(w, items);
     if (w.num_mesh_bodies > 0) launch_mesh_narrowphase(w, 0, s);

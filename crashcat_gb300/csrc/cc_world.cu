@@ -404,6 +404,7 @@ int cc_world_create(const cc_world_settings *s, cc_world **out) {
     ALLOC(node_hi, 2 * (size_t)cap);
     ALLOC(node_flag, cap);
     ALLOC(pairs, w.max_pairs);
+    ALLOC(pair_order, w.max_pairs);
     ALLOC(manifolds, w.max_manifolds);
     ALLOC(cons, w.max_manifolds);
     ALLOC(cons_of_manifold, w.max_manifolds);
@@ -546,7 +547,7 @@ int cc_world_destroy(cc_world *W) {
     void *ptrs[] = {w.pos, w.quat, w.com, w.linvel, w.angvel, w.force, w.torque, w.inv_inertia, w.inertia_rot,
                     w.shape, w.material, w.damping, w.flags, w.groups, w.world, w.sleep_sph, w.sleep_timer,
                     w.aabb64, w.aabb_lo, w.aabb_hi, w.wake, w.morton, w.morton_alt, w.order, w.order_alt,
-                    w.node_parent, w.node_child, w.node_lo, w.node_hi, w.node_flag, w.pairs, w.manifolds, w.cons,
+                    w.node_parent, w.node_child, w.node_lo, w.node_hi, w.node_flag, w.pairs, w.pair_order, w.manifolds, w.cons,
                     w.cons_of_manifold, w.uf_parent, w.island_of_body, w.island_id_of_root, w.island_body_count,
                     w.island_cons_count, w.island_body_off, w.island_cons_off, w.island_bodies, w.island_cons,
                     w.island_fill_b, w.island_fill_c, w.iter_ovr, w.island_iters, w.inv_inertia_world, w.scan_tmp, w.ctr, w.scene,
