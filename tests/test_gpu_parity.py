@@ -229,10 +229,11 @@ def test_batched_worlds_are_independent(gpu_lib):
     assert ((p[:, 0] < sc.n) == (p[:, 1] < sc.n)).all()
 
 
-@pytest.mark.parametrize("base", [5, 9, 14])
+@pytest.mark.parametrize("base", [5, 9, 14, 20])
 def test_pyramid_island_first_step(gpu_lib, oracle_lib, base):
-    """One island per pyramid: base 5 (35 contacts) and 9 (117) run on one warp
-    (sort, colouring and shared-memory sweep), base 14 (287 contacts) on one CTA.
+    """One island per pyramid: base 5 (35 contacts) runs on the per-warp tier's small
+    instance, 9 (117) on its large one (sort, colouring and shared-memory sweep), base 14
+    (287 contacts) and 20 (590) on one CTA.
     The colouring keeps the reference's order, so the first step matches the
     oracle's velocities.  (Later steps meet prune ties between the pyramid's
     aligned faces, which FP32 and FP64 break differently.)"""
