@@ -552,42 +552,75 @@ __device__ __forceinline__ int bucketed_island(const int *list, size_t cap, cons
     return -1;
 }
 
+// Island classes of k_island_classify: a per-thread or per-warp size bucket, or one of these.
+enum : int { CL_NONE = -1, CL_MID0 = 100, CL_GIANT = 1000, CL_SMALL_JOINT, CL_LARGE_JOINT, CL_LARGE };
+
 __global__ void k_island_classify(DevWorld w, int *small_list, int *large_list) {
-    int ni = w.ctr->num_islands;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x) {
-        int nc = w.island_cons_count[i], nb = w.island_body_count[i];
-        int nj = joint_total(w) > 0 ? w.island_joint_count[i] : 0;
-        atomicMax(&w.ctr->max_island_constraints, nc + nj);
-        if (nc + nj > w.giant_min) {  // a pile: the whole grid solves it
-            int k = atomicAdd(&w.ctr->num_giant_islands, 1);
-            w.giant_list[k] = i;
-        } else if (nj > 0) {
-            // islands with joints: one thread in the reference's exact order when small (a lone
-            // ragdoll), else the per-CTA solve
-            if (nj <= c_settings.small_island_max_joints && nc <= SMALL_ISLAND_MAX_CONS &&
-                nb <= SMALL_ISLAND_MAX_BODIES) {
-                int k = atomicAdd(&w.ctr->num_small_joint_islands, 1);
-                w.small_joint_list[k] = i;
+    const int ni = w.ctr->num_islands;
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    // the lanes of a warp stay together through the loop: the list slots are taken with one
+    // atomic per class present in the warp
+    for (int base = blockIdx.x * blockDim.x; base < ni; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        int cls = CL_NONE, tot = 0;
+        if (i < ni) {
+            const int nc = w.island_cons_count[i], nb = w.island_body_count[i];
+            const int nj = joint_total(w) > 0 ? w.island_joint_count[i] : 0;
+            tot = nc + nj;
+            if (nc + nj > w.giant_min) {  // a pile: the whole grid solves it
+                cls = CL_GIANT;
+            } else if (nj > 0) {
+                // islands with joints: one thread in the reference's exact order when small (a lone
+                // ragdoll), else the per-CTA solve
+                cls = (nj <= c_settings.small_island_max_joints && nc <= SMALL_ISLAND_MAX_CONS &&
+                       nb <= SMALL_ISLAND_MAX_BODIES)
+                          ? CL_SMALL_JOINT
+                          : CL_LARGE_JOINT;
+            } else if (nc <= c_settings.small_island_max_cons && nb <= SMALL_ISLAND_MAX_BODIES) {
+                cls = min(nc, SMALL_BUCKETS - 1);
+            } else if (nc <= WARP_MAX_CONS && nb <= WARP_MAX_BODIES) {
+                // classes 0 and 1 (at most 32 contacts) go to the small instance when their bodies fit
+                int b = min(max(mid_size_class(nc), 0), MID_BUCKETS - 1);
+                if (b < 2 && nb > WARP_S_BODIES) b = 2;
+                cls = CL_MID0 + b;
             } else {
-                int k = atomicAdd(&w.ctr->num_large_joint_islands, 1);
-                w.large_joint_list[k] = i;
+                cls = CL_LARGE;
             }
-        } else if (nc <= c_settings.small_island_max_cons && nb <= SMALL_ISLAND_MAX_BODIES) {
-            atomicAdd(&w.ctr->num_small_islands, 1);
-            const int b = min(nc, SMALL_BUCKETS - 1);
-            int k = atomicAdd(&w.ctr->small_bucket[b], 1);
-            small_list[(size_t)b * w.cap + k] = i;
-        } else if (nc <= WARP_MAX_CONS && nb <= WARP_MAX_BODIES) {
-            atomicAdd(&w.ctr->num_mid_islands, 1);
-            // classes 0 and 1 (at most 32 contacts) go to the small instance when their bodies fit
-            int b = min(max(mid_size_class(nc), 0), MID_BUCKETS - 1);
-            if (b < 2 && nb > WARP_S_BODIES) b = 2;
-            int k = atomicAdd(&w.ctr->mid_bucket[b], 1);
-            w.mid_list[(size_t)b * w.cap + k] = i;
-        } else {
-            int k = atomicAdd(&w.ctr->num_large_islands, 1);
-            large_list[k] = i;
         }
+        const int mx = __reduce_max_sync(FULL, tot);
+        if (lane == 0 && mx > 0) atomicMax(&w.ctr->max_island_constraints, mx);
+        const unsigned same = __match_any_sync(FULL, cls);
+        const int leader = __ffs(same) - 1, cnt = __popc(same);
+        int *ctr = nullptr, *list = nullptr, *total = nullptr;
+        if (cls == CL_GIANT) {
+            ctr = &w.ctr->num_giant_islands;
+            list = w.giant_list;
+        } else if (cls == CL_SMALL_JOINT) {
+            ctr = &w.ctr->num_small_joint_islands;
+            list = w.small_joint_list;
+        } else if (cls == CL_LARGE_JOINT) {
+            ctr = &w.ctr->num_large_joint_islands;
+            list = w.large_joint_list;
+        } else if (cls == CL_LARGE) {
+            ctr = &w.ctr->num_large_islands;
+            list = large_list;
+        } else if (cls >= CL_MID0) {
+            ctr = &w.ctr->mid_bucket[cls - CL_MID0];
+            list = w.mid_list + (size_t)(cls - CL_MID0) * w.cap;
+            total = &w.ctr->num_mid_islands;
+        } else if (cls >= 0) {
+            ctr = &w.ctr->small_bucket[cls];
+            list = small_list + (size_t)cls * w.cap;
+            total = &w.ctr->num_small_islands;
+        }
+        int slot = 0;
+        if (ctr && lane == leader) {
+            slot = atomicAdd(ctr, cnt);
+            if (total) atomicAdd(total, cnt);
+        }
+        slot = __shfl_sync(same, slot, leader);
+        if (ctr) list[slot + __popc(same & ((1u << lane) - 1u))] = i;
     }
 }
 
