@@ -51,6 +51,7 @@ struct cc_world {
     std::vector<Compound> compounds;
     bool hulls_dirty = false, meshes_dirty = false, compounds_dirty = false;  // added since the last upload
     DevRay *q_rays = nullptr;  // ray query staging (cc_world_cast_rays), grown on demand
+    int h_query_ovf = 0;       // the device overflow word after a shape-cast query
     DevRayHit *q_hits = nullptr;
     int q_cap = 0;
     unsigned long long *q_keys = nullptr;  // ray sort: 2 x keys, 2 x indices, radix scratch
@@ -1416,8 +1417,15 @@ int cc_world_cast_shapes(cc_world *W, const cc_shape_cast *casts, int32_t count,
     cc_shape_cast_hit *dh = (cc_shape_cast_hit *)((char *)d + in_b);
     if (r == CC_OK) r = cc_world_cast_shapes_device(W, (const cc_shape_cast *)d, count, filter, dh);
     if (r == CC_OK) r = cuda_ok(cudaMemcpyAsync(hits, dh, out_b, cudaMemcpyDeviceToHost, W->stream));
+    int ovf = 0;
+    if (r == CC_OK)
+        r = cuda_ok(cudaMemcpyAsync(&W->h_query_ovf, &W->w.ctr->overflow, sizeof(int), cudaMemcpyDeviceToHost,
+                                    W->stream));
     cudaFreeAsync(d, W->stream);
     if (r == CC_OK) r = cuda_ok(cudaStreamSynchronize(W->stream));
+    ovf = W->h_query_ovf;
+    // a tree walk of these casts outgrew its stack (the step's own flags are in last_ctr)
+    if (r == CC_OK && (ovf & OVF_SLOTS) && !(W->last_ctr.overflow & OVF_SLOTS)) r = CC_ERR_CAPACITY;
     return r;
 }
 

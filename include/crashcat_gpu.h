@@ -793,7 +793,9 @@ int cc_world_cast_rays_device(cc_world *world, const cc_ray *rays, int32_t count
  * collector (ClosestCastShapeCollector, src/collision/cast-shape-vs-shape.ts:
  * 199-217) and createDefaultCastShapeSettings (:116-127), a batch per call.
  *
- * A sphere, box or capsule (shape_params as cc_body_desc) at position and
+ * A sphere, box, capsule, cylinder or convex hull (shape_params as
+ * cc_body_desc: a cylinder's convex radius at most its half height and
+ * radius, a hull's index among the world's hulls) at position and
  * quaternion moves by displacement in its world.  Every body that passes the
  * filter (flags unused) and that the swept box reaches (broadphase.castAABB)
  * is cast with castShapeVsShape:
@@ -804,12 +806,17 @@ int cc_world_cast_rays_device(cc_world *world, const cc_ray *rays, int32_t count
  * penetration axis negated and normalised), hit.point the contact point on
  * the cast shape, world space, hit.sub_shape_id the mesh triangle's sub-shape
  * id (0xffffffff for other shapes).  Equal fractions go to the lower body index.
- * Other cast shapes: CC_ERR_INVALID.
+ * Other cast shapes: CC_ERR_INVALID from cc_world_cast_shapes.
  *   cc_world_cast_shapes: host arrays; returns when the hits are written.
  *   cc_world_cast_shapes_device: device arrays; queued on the world's stream.
+ *     The host does not read the device array, so the kernel checks each cast:
+ *     one with another shape comes back as a miss (body -1, fraction 1).
+ * A tree walk that outgrows its stack (64 nodes) drops the subtree it could
+ * not push, so a hit may be missed: cc_world_cast_shapes then returns
+ * CC_ERR_CAPACITY (the hits are still written).
  * ------------------------------------------------------------------------- */
 typedef struct cc_shape_cast {
-    int32_t shape_type;     /* CC_SHAPE_SPHERE, CC_SHAPE_BOX or CC_SHAPE_CAPSULE */
+    int32_t shape_type;     /* CC_SHAPE_SPHERE, _BOX, _CAPSULE, _CYLINDER or _CONVEX_HULL */
     float shape_params[4];  /* as cc_body_desc.shape_params */
     float position[3];
     float quaternion[4];    /* x, y, z, w */

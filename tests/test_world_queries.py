@@ -272,6 +272,49 @@ def test_gpu_rays_stay_in_their_world(gpu_lib, oracle_lib):
     np.testing.assert_allclose(h["fraction"], 1.6 / 20.0, atol=1e-4)
 
 
+@pytest.mark.gpu
+def test_gpu_shape_casts_stay_in_their_world(gpu_lib):
+    """Worlds share the device tree; a shape cast only meets bodies of its own world.  Every world
+    of 64 holds the same spheres, so the sphere cast of world k hits body k * 4; a terrain mesh in
+    world 0 is hit by a cast down from world 0 and missed by the same cast from a world without
+    bodies, as are the spheres.  No tree walk outgrows its stack (the call would return
+    CC_ERR_CAPACITY)."""
+    nw, per = 64, 4
+    sc = scenes.mesh_drop(n=1, n_cells=12, seed=5, heights=(0.0, 1.0))
+    b = scenes.blank_bodies(nw * per)
+    for k in range(nw):
+        for j in range(per):
+            i = k * per + j
+            scenes.set_sphere(b, i, 0.4)
+            b["position"][i] = (2.0 * j + 2.0, 5.0, 0.0)
+            b["motion_type"][i] = _lib.STATIC
+            b["object_layer"][i] = scenes.LAYER_NOT_MOVING
+            b["world"][i] = k
+    terrain = sc.bodies[:1].copy()
+    terrain["world"][0] = 0
+    bodies = np.concatenate([b, terrain])
+    ws = world.standard_settings()
+    ws.num_worlds = nw + 1  # the last world has no bodies
+    g = world.GpuWorld(ws, len(bodies))
+    g.add_triangle_mesh(*sc.mesh)
+    g.add_bodies(bodies)
+    casts = np.zeros(nw + 3, _lib.SHAPE_CAST_DTYPE)
+    casts["shape_type"] = _lib.SHAPE_SPHERE
+    casts["shape_params"][:, 0] = 0.2
+    casts["quaternion"][:, 3] = 1.0
+    casts["position"][:nw] = (0.0, 5.0, 0.0)
+    casts["displacement"][:nw] = (20.0, 0.0, 0.0)
+    casts["world"][:nw] = np.arange(nw)
+    casts["position"][nw:] = [(0.0, 5.0, 0.0), (0.5, 4.0, 0.5), (0.5, 4.0, 0.5)]
+    casts["displacement"][nw:] = [(20.0, 0.0, 0.0), (0.0, -8.0, 0.0), (0.0, -8.0, 0.0)]
+    casts["world"][nw:] = [nw, 0, nw]
+    h = g.cast_shapes(casts)
+    np.testing.assert_array_equal(h["body"][:nw], np.arange(nw) * per)
+    np.testing.assert_allclose(h["fraction"][:nw], 1.4 / 20.0, atol=1e-4)
+    assert h["body"][nw] == -1 and h["body"][nw + 2] == -1
+    assert h["body"][nw + 1] == nw * per and 0.0 < h["fraction"][nw + 1] < 1.0
+
+
 # ---------------------------------------------------------------------------
 # collidePoint (query.ts:470-490): the reference's known answers
 # (tst/query.test.ts collidePoint, tst/collision/collide-point-vs-shape.test.ts)
