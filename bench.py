@@ -1094,6 +1094,15 @@ def run_gpu(args, rank, world_size, local):
     achieved = bytes_dom / (prof[dom] * 1e-3) / 1e9 if prof[dom] > 0 else 0.0
     # DRAM bytes per launch of the dominant stage: the per-unit traffic of the committed ncu
     # capture (profiles/traffic_per_unit.json) times this step's units
+    # the dominant stage's issue counters from the committed ncu capture: the stages are latency
+    # and issue bound, which the HBM fraction alone does not show
+    issue = None
+    ipath = os.path.join(ROOT, "profiles", "issue_counters.json")
+    if os.path.exists(ipath):
+        try:
+            issue = json.load(open(ipath)).get(dom)
+        except Exception:
+            issue = None
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic_per_unit.json")
     if os.path.exists(tpath):
@@ -1129,7 +1138,7 @@ def run_gpu(args, rank, world_size, local):
                     "api": "cc_world_step_host (pinned host rows in and out every step)"},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                         "algorithmic_bytes_per_launch": bytes_dom, "stage_ms": prof},
+                         "algorithmic_bytes_per_launch": bytes_dom, "stage_ms": prof, "issue": issue},
             "cpu_baseline": cpu,
             "autotune": tune,
             "error": error,
