@@ -353,7 +353,10 @@ __global__ void __launch_bounds__(128) k_find_pairs(DevWorld w, const int2 *node
     int nthreads = gridDim.x * blockDim.x;
     int iters = (n + nthreads - 1) / nthreads;
     for (int it = 0; it < iters; it++) {
-        int i = it * nthreads + blockIdx.x * blockDim.x + threadIdx.x;
+        // query bodies in the tree's leaf (Morton) order: the lanes of a warp walk neighbouring
+        // subtrees.  Pairs are appended, so the order changes no result.
+        const int q = it * nthreads + blockIdx.x * blockDim.x + threadIdx.x;
+        const int i = q < n ? w.order[q] : n;
         int2 buf[PAIR_BUF];
         int cnt = 0;
         uint32_t fa = i < n ? w.flags[i] : 0u;
